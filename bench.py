@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark: batched BVH navigation steps/s on one GB300 (replicas for N>1).
+
+Workload (BASELINE configs[1]): world box of half-length 1 m holding 4096
+rotated boxes (half-lengths U[5,30] mm, jittered 16^3 grid), 2^22 tracks
+uniform in the world outside all boxes, isotropic directions, step limit
+1 m; one step = ComputeStepAndNextVolume (step + propagated/relocated
+NavStateIndex) plus ComputeSafety for every track, in one launch of the
+all-FP64 kernel.  Synthetic data with the stated seeds.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  --impl reference times the CPU
+implementation of the same path (the oracle restatement: the reference
+itself cannot be built here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_TRACKS = 1 << 22
+METRIC = "nav steps/s on 1 GB300: mixed vs FP64 plain (exact next-vol); p50/p99 latency"
+UNIT = "steps/s"
+# algorithmic bytes per track and step: read p 24 + d 24 + slimit 8 + state 12,
+# write step 8 + state 12 + safety 8
+BYTES_PER_STEP = 24 + 24 + 8 + 12 + 8 + 12 + 8
+WORKLOAD = ("box-grid: 4096 rotated boxes in a 1 m world, 2^22 tracks, "
+            "ComputeStepAndNextVolume + ComputeSafety, all-FP64 kernel")
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self._t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload():
+    from vecgeom_gb300 import workloads as W
+
+    grid = W.box_grid_geometry(seed=3)
+    t = W.box_grid_tracks(grid, n=N_TRACKS, seed_points=4, seed_dirs=5, step_limit=1000.0)
+    return grid, t
+
+
+def cpu_sample_rate(grid, t, min_seconds: float, threads: int = 0):
+    """Oracle (CPU restatement of the reference) steps/s on host cores, over repeated passes
+    of a 2^20-track sample until `min_seconds` of work is done."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    og = pyoracle.OracleGeometry(grid.desc)
+    sample = t.head(1 << 20)
+    og.step(sample.head(1 << 14), calcsafety=True, nthreads=threads)  # warm caches
+    done, passes, t0 = 0, 0, pyoracle.now()
+    while True:
+        og.step(sample, calcsafety=True, nthreads=threads)
+        done += sample.n
+        passes += 1
+        el = pyoracle.now() - t0
+        if el >= min_seconds:
+            break
+    cores = threads if threads > 0 else pyoracle.ncores()
+    return done / el, cores, f"{passes} passes x 2^20 tracks of the same workload ({el:.1f} s)"
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    grid, t = make_workload()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pyoracle
+
+    og = pyoracle.OracleGeometry(grid.desc)
+    sample = t.head(1 << 20)
+    for _ in range(args.warmup):
+        og.step(sample.head(1 << 16), calcsafety=True)
+    times = []
+    for _ in range(args.steps):
+        t0 = pyoracle.now()
+        og.step(sample, calcsafety=True)
+        times.append(pyoracle.now() - t0)
+    total = sum(times)
+    value = sample.n * args.steps / total
+    cores = pyoracle.ncores()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "tracks_per_step": sample.n, "daughters": 4096},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"2^20 tracks of the 2^22-track workload per step, {args.steps} steps; "
+                                   "CPU restatement of VecGeom's BVHNavigator (reference not buildable here)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    import vecgeom_gb300 as V
+    from vecgeom_gb300 import build as B
+
+    B.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    grid, t = make_workload()
+    geo = V.Geometry(grid.desc, device=local)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pts = V.SOA3D(dev(t.x), dev(t.y), dev(t.z))
+    dirs = V.SOA3D(dev(t.dx), dev(t.dy), dev(t.dz))
+    sl = dev(t.step_limit)
+    st = np.zeros((t.n, 3), np.int32)
+    st[:, 0] = 1
+    inp = V.NavStatePool(dev(st))
+    out = V.NavStatePool.empty_like(inp)
+    steps = torch.empty(t.n, dtype=torch.float64, device="cuda")
+    saf = torch.empty(t.n, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def one():
+        geo.step(pts, dirs, sl, inp, out, steps, saf, stream=stream)
+
+    for _ in range(max(args.warmup, 3)):
+        one()
+    geo.synchronize(stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local) as clocks:
+        for a, b in evs:
+            a.record(stream)
+            one()
+            b.record(stream)
+        barrier()
+    geo.synchronize(stream)
+    per = [a.elapsed_time(b) for a, b in evs]
+    total_ms = evs[0][0].elapsed_time(evs[-1][1])
+    if dist is not None:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    value = ws * t.n * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    hx, hy, hz, hdx, hdy, hdz, hsl = (pin(a) for a in (t.x, t.y, t.z, t.dx, t.dy, t.dz, t.step_limit))
+    hst = torch.from_numpy(t.states.view(np.uint8)).pin_memory().numpy().view(t.states.dtype)
+    hout = torch.empty(t.n * 12, dtype=torch.uint8, pin_memory=True).numpy().view(t.states.dtype)
+    hstep = torch.empty(t.n, dtype=torch.float64, pin_memory=True).numpy()
+    hsaf = torch.empty(t.n, dtype=torch.float64, pin_memory=True).numpy()
+    hp, hd = V.SOA3D(hx, hy, hz), V.SOA3D(hdx, hdy, hdz)
+
+    def one_host():
+        geo.step(hp, hd, hsl, V.NavStatePool(hst), V.NavStatePool(hout), hstep, hsaf)
+
+    e2e_steps = max(3, min(args.steps, 10))
+    one_host()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        one_host()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        tt = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = ws * t.n * e2e_steps / e2e_s
+    h2d = t.n * (7 * 8 + 12)
+    d2h = t.n * (12 + 8 + 8)
+
+    if rank == 0:
+        hbm_peak, src = peaks()
+        avg_ms = statistics.mean(per)
+        achieved = t.n * BYTES_PER_STEP / (avg_ms * 1e-3) / 1e9
+        cpu = None
+        if ws == 1 and not args.no_cpu_baseline:
+            rate, cores, sample = cpu_sample_rate(grid, t, min_seconds=args.cpu_seconds)
+            cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        traffic = None
+        tp = ROOT / "profiles" / "traffic_step_fp64.json"
+        if tp.exists():
+            traffic = json.loads(tp.read_text()).get("bytes_per_launch_full_size")
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "tracks_per_step_per_gpu": t.n, "daughters": 4096,
+                       "step_limit_mm": 1000.0, "precision": "fp64-plain", "parallelism": f"replicas x{ws}",
+                       "l2": "inputs+outputs 400 MB per step > 129 MB L2: no flush needed"},
+            "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
+                           "batch_tracks": t.n},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps, "path": "vgn_compute_step_batch with pinned host buffers"},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
+                         "algorithmic_bytes_per_step": BYTES_PER_STEP,
+                         "kernel": "step_kernel_fp64", "kernel_avg_ms": avg_ms},
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

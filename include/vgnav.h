@@ -1,0 +1,164 @@
+/*
+ * vgnav.h -- C ABI of the GB300-native batched navigation library (libvgnav).
+ *
+ * The library replaces the batched navigation hot path of VecGeom 1.2.0:
+ * BVH traversal in BVHNavigator / BVHSafetyEstimator / BVHLevelLocator
+ * feeding the per-shape DistanceToIn/DistanceToOut/SafetyToIn/SafetyToOut
+ * kernels and the Transformation3D global-to-local transforms, over
+ * SOA3D<double> point/direction batches and NavStateIndex states.
+ *
+ * All entry points are plain C: pointers, sizes and an int status.
+ * Array arguments may be device pointers (cudaMalloc / torch CUDA tensors),
+ * in which case the call only enqueues work on `stream`, or host pointers,
+ * in which case the library stages the data through its own device
+ * workspace and the call returns once the results are back in host memory.
+ * A NULL stream is the legacy default stream.
+ */
+#ifndef VGNAV_H
+#define VGNAV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define VGN_OK 0
+#define VGN_ERR_ARG 1         /* invalid argument (null pointer, bad size, bad id) */
+#define VGN_ERR_UNSUPPORTED 2 /* shape or parameter set not supported */
+#define VGN_ERR_CUDA 3        /* CUDA runtime error (message in vgn_last_error) */
+#define VGN_ERR_NOMEM 4       /* device or host allocation failed */
+#define VGN_ERR_STACK 5       /* BVH traversal stack overflow on the device */
+#define VGN_ERR_RELOCATE 6    /* relocation exceeded the geometry depth bound */
+#define VGN_ERR_STATE 7       /* an input navigation state index is outside the table */
+
+/* ---- shape types (numbering of vgn_geometry_desc.lv_shape) ---------------- */
+enum vgn_shape_type {
+  VGN_BOX       = 0, /* params: dx, dy, dz                        (UnplacedBox.h)       */
+  VGN_TUBE      = 1, /* params: rmin, rmax, dz, sphi, dphi        (UnplacedTube.h:29)   */
+  VGN_CONE      = 2, /* params: rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi (UnplacedCone.h) */
+  VGN_TRD       = 3, /* params: x1, x2, y1, y2, z                 (UnplacedTrd.h)       */
+  VGN_TRAPEZOID = 4, /* params: dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2 (UnplacedTrapezoid.h) */
+  VGN_SPHERE    = 5, /* params: rmin, rmax, sphi, dphi, stheta, dtheta (UnplacedSphere.h) */
+  VGN_POLYCONE  = 6  /* params: sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] (UnplacedPolycone.h:79) */
+};
+
+/* ---- shape operations for vgn_shape_batch ------------------------------- */
+enum vgn_shape_op {
+  VGN_OP_DISTANCE_TO_IN  = 0, /* VUnplacedVolume::DistanceToIn  */
+  VGN_OP_DISTANCE_TO_OUT = 1, /* VUnplacedVolume::DistanceToOut */
+  VGN_OP_SAFETY_TO_IN    = 2, /* VUnplacedVolume::SafetyToIn    */
+  VGN_OP_SAFETY_TO_OUT   = 3, /* VUnplacedVolume::SafetyToOut   */
+  VGN_OP_CONTAINS        = 4, /* VUnplacedVolume::Contains, output 0.0 / 1.0 */
+  VGN_OP_INSIDE          = 5  /* VUnplacedVolume::Inside, output 1 kInside, 2 kSurface, 3 kOutside */
+};
+
+/* ---- flags --------------------------------------------------------------- */
+#define VGN_PRECISION_FP64 0x0  /* all-FP64 kernels, bit-exact with the CPU navigator   */
+#define VGN_PRECISION_MIXED 0x1 /* FP32 conservative traversal + FP64 refinement         */
+#define VGN_NO_RELOCATE 0x10    /* ComputeStep semantics: out state not relocated        */
+
+/* Navigation state, layout-identical to vecgeom::NavStateIndex
+ * (VecGeom/navigation/NavStateIndex.h:39-41): 12 bytes. */
+typedef struct vgn_state {
+  uint32_t nav_ind;     /* index into the navigation table (0 = outside the world) */
+  uint32_t last_exited; /* navigation index of the last exited state              */
+  uint8_t on_boundary;  /* 1 if the point sits on the boundary of Top()           */
+  uint8_t pad[3];
+} vgn_state;
+
+/* Flat geometry description.  Placed-volume ids are array indices, in
+ * creation order (VPlacedVolume::id(), source/PlacedVolume.cpp:32); the
+ * daughters of a logical volume are its placements in id order
+ * (LogicalVolume::PlaceDaughter, source/LogicalVolume.cpp:142-148). */
+typedef struct vgn_geometry_desc {
+  int32_t n_logical;
+  const int32_t *lv_shape;        /* [n_logical] vgn_shape_type                      */
+  const int32_t *lv_param_offset; /* [n_logical] offset of the shape's params        */
+  const double *params;           /* [n_params]                                      */
+  int32_t n_params;
+  int32_t n_placed;
+  const int32_t *pv_logical;   /* [n_placed] logical volume placed                     */
+  const int32_t *pv_mother;    /* [n_placed] mother logical volume, -1 for the world   */
+  const double *pv_transform;  /* [12*n_placed] tx,ty,tz,r0..r8 (Transformation3D ctor,
+                                  source/Transformation3D.cpp:52-61)                    */
+  int32_t world_placed;        /* id of the world placement                            */
+} vgn_geometry_desc;
+
+typedef struct vgn_geometry vgn_geometry;
+
+/* Close the geometry and make it resident on `device`: daughter bounding
+ * boxes (ABBoxManager::InitABBoxesForCompleteGeometry, source/ABBoxManager.cpp:109-142),
+ * one BVH per logical volume with daughters (BVHManager::Init,
+ * source/BVHManager.cpp:24-30), the navigation index table
+ * (GeoManager::MakeNavIndexTable, source/GeoManager.cpp:381-395) and their
+ * upload (replaces CudaManager::Synchronize + BVHManager::DeviceInit,
+ * source/CudaManager.cpp:101-222, source/BVHManager.cpp:33-45). */
+#define VGN_HOST_ONLY (-1) /* `device` value: close on the host only (tables can be inspected, no kernels) */
+int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry **out);
+int vgn_geometry_free(vgn_geometry *geom);
+
+/* Host copy of the navigation index table (NavIndexTable::GetTable,
+ * VecGeom/management/NavIndexTable.h:74-76). */
+int vgn_geometry_navindex(const vgn_geometry *geom, const uint32_t **table, size_t *n_words);
+/* Host copies of one logical volume's BVH (BVH.h:364-370); any out pointer may be NULL. */
+int vgn_geometry_bvh_info(const vgn_geometry *geom, int32_t lv, int32_t *depth, int32_t *n_nodes, int32_t *n_prims);
+int vgn_geometry_bvh_arrays(const vgn_geometry *geom, int32_t lv, int32_t *prim_id, int32_t *offset, int32_t *nchild,
+                            double *nodes_minmax, double *prims_minmax);
+/* Bytes of device memory held by the geometry tables. */
+int vgn_geometry_device_bytes(const vgn_geometry *geom, size_t *bytes);
+
+/* Batched navigation step with propagated state.
+ * Replaces VNavigatorHelper<BVHNavigator<false>>::ComputeStepsAndSafetiesAndPropagatedStates
+ * (VecGeom/navigation/VNavigator.h:913-941) and, per track,
+ * ComputeStepAndSafetyAndPropagatedState / ComputeStepAndPropagatedState
+ * (VNavigator.h:1014-1064, 436-492); with VGN_NO_RELOCATE, ComputeStep
+ * (VNavigator.h:494-540).  Unlike the reference batch call, tracks may sit in
+ * different volumes.  `safety` may be NULL (no safety computed); otherwise it
+ * receives ComputeSafetyForLocalPoint (BVHSafetyEstimator.h:38-46).
+ * out->nav_ind after the call is the next volume ("ComputeStepAndNextVolume"). */
+int vgn_compute_step_batch(const vgn_geometry *geom, int64_t n, const double *px, const double *py, const double *pz,
+                           const double *dx, const double *dy, const double *dz, const double *step_limit,
+                           const vgn_state *in, vgn_state *out, double *step, double *safety, int flags,
+                           void *stream);
+
+/* Alias with the name the spec API uses for the same operation. */
+int vgn_step_and_next_volume(const vgn_geometry *geom, int64_t n, const double *px, const double *py,
+                             const double *pz, const double *dx, const double *dy, const double *dz,
+                             const double *step_limit, const vgn_state *in, vgn_state *out, double *step,
+                             double *safety, int flags, void *stream);
+
+/* Batched isotropic safety: VSafetyEstimatorHelper<BVHSafetyEstimator>::ComputeSafety
+ * (VecGeom/navigation/VSafetyEstimator.h:98-107). */
+int vgn_compute_safety_batch(const vgn_geometry *geom, int64_t n, const double *px, const double *py,
+                             const double *pz, const vgn_state *in, double *safety, int flags, void *stream);
+
+/* Batched point location from the world: GlobalLocator::LocateGlobalPoint(world, p, state, true)
+ * (VecGeom/navigation/GlobalLocator.h:35-82) with BVHLevelLocator (BVH.h:234-244). */
+int vgn_locate_batch(const vgn_geometry *geom, int64_t n, const double *px, const double *py, const double *pz,
+                     vgn_state *out, int flags, void *stream);
+
+/* Batched unplaced-shape query on logical volume `lv`: the per-shape
+ * *Implementation kernels behind VUnplacedVolume (e.g.
+ * VecGeom/volumes/kernel/TubeImplementation.h:475-960).  dx/dy/dz and
+ * step_max are only read for the distance ops (step_max may be NULL). */
+int vgn_shape_batch(const vgn_geometry *geom, int32_t lv, int32_t op, int64_t n, const double *px, const double *py,
+                    const double *pz, const double *dx, const double *dy, const double *dz, const double *step_max,
+                    double *out, int flags, void *stream);
+
+/* Wait for the work of the previous calls on `stream`; returns the first
+ * device-side error status recorded by a kernel since the last call. */
+int vgn_synchronize(const vgn_geometry *geom, void *stream);
+
+/* Message of the last error raised on the calling thread. */
+const char *vgn_last_error(void);
+
+/* Library version string. */
+const char *vgn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VGNAV_H */

@@ -1,0 +1,140 @@
+/*
+ * or_internal.h -- internal types of the CPU oracle (test infrastructure only).
+ * Restates the scalar semantics of VecGeom 1.2.0 base types:
+ *   Vector3D      VecGeom/base/Vector3D.h
+ *   Transformation3D VecGeom/base/Transformation3D.h:59-63, 561-1000
+ *   AABB          VecGeom/base/AABB.h:26-228
+ *   constants     VecGeom/base/Math.h:26-53, VecGeom/base/Global.h:142-178
+ * The VecCore scalar calls the reference uses are restated as:
+ *   Min(a,b) = a < b ? a : b,  Max(a,b) = a > b ? a : b,  Sign(x) = copysign(1,x),
+ *   MaskedAssign(d,m,v) = if (m) d = v,  Blend(m,a,b) = m ? a : b.
+ */
+#ifndef OR_INTERNAL_H
+#define OR_INTERNAL_H
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "vgoracle.h"
+
+/* Math.h:27-53 (double precision branch) */
+#define kTolerance 1e-9
+#define kHalfTolerance (0.5 * kTolerance)
+#define kPushTolerance 1e-6
+#define kConeTolerance 1e-7
+#define kInfLength DBL_MAX
+#define kEpsilon DBL_EPSILON
+#define kTiny 1e-30
+#define kPi 3.14159265358979323846
+#define kTwoPi (2. * kPi)
+#define kHalfPi (0.5 * kPi)
+#define kAngTolerance 1e-9
+
+typedef struct { double x, y, z; } v3;
+
+static inline v3 v3_make(double x, double y, double z) { v3 r = {x, y, z}; return r; }
+static inline v3 v3_add(v3 a, v3 b) { return v3_make(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 v3_sub(v3 a, v3 b) { return v3_make(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 v3_mul(v3 a, v3 b) { return v3_make(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 v3_scale(double s, v3 a) { return v3_make(s * a.x, s * a.y, s * a.z); }
+static inline v3 v3_abs(v3 a) { return v3_make(fabs(a.x), fabs(a.y), fabs(a.z)); }
+static inline double or_min(double a, double b) { return a < b ? a : b; }
+static inline double or_max(double a, double b) { return a > b ? a : b; }
+/* vecCore::math::Min/Max of three, as used by Vector3D::Min/Max (Vector3D.h:276-280) */
+static inline double v3_minc(v3 a) { return or_min(or_min(a.x, a.y), a.z); }
+static inline double v3_maxc(v3 a) { return or_max(or_max(a.x, a.y), a.z); }
+static inline double v3_dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline double v3_mag2(v3 a) { return v3_dot(a, a); }
+static inline double v3_perp2(v3 a) { return a.x * a.x + a.y * a.y; }
+static inline double or_sign(double x) { return copysign(1.0, x); }
+/* Global.h:166-178 */
+static inline double NonZeroAbs(double x) { return fabs(x) + 1.0e-30; }
+static inline double NonZero(double x) { return x + copysign(1.0e-30, x); }
+
+/* Transformation3D members (Transformation3D.h:59-63) */
+typedef struct {
+  double t[3];
+  double r[9];
+  int identity, has_rot, has_trans;
+} or_xf;
+
+void xf_identity(or_xf *m);
+void xf_from12(or_xf *m, const double *a12);           /* 12-parameter constructor + SetProperties */
+v3 xf_transform(const or_xf *m, v3 p);                   /* Transform<kGeneric,kGeneric> */
+v3 xf_transform_dir(const or_xf *m, v3 d);               /* TransformDirection<kGeneric> */
+v3 xf_inverse_transform(const or_xf *m, v3 p);           /* InverseTransform */
+void xf_multiply_from_right(or_xf *m, const or_xf *rhs); /* MultiplyFromRight */
+
+/* AABB (AABB.h) */
+typedef struct { v3 mn, mx; } or_aabb;
+void aabb_intersect_invdir(const or_aabb *b, v3 p, v3 invdir, double *tmin, double *tmax);
+static inline double aabb_safety(const or_aabb *b, v3 p)
+{
+  /* AABB.h:81: ((point - Center()).Abs() - 0.5 * Size()).Max() */
+  v3 c = v3_scale(0.5, v3_add(b->mx, b->mn));
+  v3 s = v3_sub(b->mx, b->mn);
+  return v3_maxc(v3_sub(v3_abs(v3_sub(p, c)), v3_scale(0.5, s)));
+}
+static inline int aabb_contains(const or_aabb *b, v3 p)
+{
+  return p.x >= b->mn.x && p.x <= b->mx.x && p.y >= b->mn.y && p.y <= b->mx.y && p.z >= b->mn.z && p.z <= b->mx.z;
+}
+
+/* ---- shape parameter structs (cached members as the reference's *Struct) ---- */
+typedef struct { double d[3]; } or_box; /* BoxStruct.h fDimensions */
+
+typedef struct { /* TubeStruct.h:15-41 (no phi wedge: full-phi tubes) */
+  double rmin, rmax, z, sphi, dphi;
+  double rmin2, rmax2, alongphi1x, alongphi1y, alongphi2x, alongphi2y;
+  double tolIrmin2, tolOrmin2, tolIrmax2, tolOrmax2, tolIz, tolOz, tolIrmin, tolOrmin, tolIrmax, tolOrmax, maxval;
+} or_tube;
+
+typedef struct {
+  int type;
+  int param_off;
+  int nd;           /* number of daughters */
+  int *daughters;   /* placed-volume ids, in placement order */
+  /* shape */
+  union {
+    or_box box;
+    or_tube tube;
+  } s;
+  /* BVH (BVH.h:364-370), present when nd > 0 */
+  int bvh_depth, bvh_nodes;
+  int *prim_id, *offset, *nchild;
+  or_aabb *nodes, *aabbs;
+} or_lv;
+
+typedef struct {
+  int lv;
+  int mother_lv;
+  int child_id;
+  or_xf xf;
+} or_pv;
+
+struct or_geom {
+  int n_lv, n_pv, world_pv;
+  or_lv *lv;
+  or_pv *pv;
+  uint32_t *navind;
+  size_t navind_words;
+  int max_depth;
+};
+
+/* shapes (or_shapes.c) */
+int shape_init(or_lv *lv, const double *p, int n_params_avail, char *err, int errlen);
+void shape_extent(const or_lv *lv, v3 *mn, v3 *mx);
+double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c);
+double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c);
+double shape_safe_in(const or_lv *lv, v3 p, or_counters *c);
+double shape_safe_out(const or_lv *lv, v3 p, or_counters *c);
+int shape_contains(const or_lv *lv, v3 p, or_counters *c);
+int shape_inside(const or_lv *lv, v3 p, or_counters *c); /* EInside: kInside=1, kSurface=2, kOutside=3 */
+
+/* BVH build (or_bvh.c) */
+int bvh_build(or_geom *g, int lv);
+
+#endif

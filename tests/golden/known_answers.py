@@ -1,0 +1,248 @@
+"""Known-answer cases transcribed from the reference's own unit tests.
+
+Each case is one assert of test/unit_tests/Test<Shape>.cpp (VecGeom 1.2.0),
+cited by file:line, restated as data: shape and constructor parameters, the
+query, the point and direction, and the expected value with the comparison
+the reference applies (ApproxEqual, test/unit_tests/ApproxEqual.h:33-49:
+exact, or |diff| < 1e-6 when one side is 0, or relative 1e-6, with values
+above 1e100 treated as infinity of the same sign).
+
+Comparisons:
+  "approx"  ApproxEqual(value, expect)
+  "le0"     value <= 0
+  "lt0"     value < 0
+  "inf"     value >= kInfLength (DBL_MAX)
+  "eq"      value == expect (Inside enum: 1 kInside, 2 kSurface, 3 kOutside)
+
+These pin the CPU oracle (and, in the GPU tests, the CUDA kernels) to the
+reference's published expectations.
+"""
+import math
+
+BOX, TUBE = 0, 1
+KPI = 3.14159265358979323846
+S2 = 1.0 / math.sqrt(2.0)
+INF = 1.7976931348623157e308
+HALF_TOL = 0.5e-9
+
+pzero = (0.0, 0.0, 0.0)
+vx, vy, vz = (1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0)
+vmx, vmy, vmz = (-1.0, 0.0, 0.0), (0.0, -1.0, 0.0), (0.0, 0.0, -1.0)
+vxy = (S2, S2, 0.0)
+vmxy = (-S2, S2, 0.0)
+vmxmy = (-S2, -S2, 0.0)
+vxmy = (S2, -S2, 0.0)
+vxmz = (S2, 0.0, -S2)
+
+
+def _unit(v):
+    """Vector3D::Unit (VecGeom/base/Vector3D.h:284-290): divide by Sqrt(mag2 + kMinimum)."""
+    m = math.sqrt((v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) + 2.2250738585072014e-308)
+    return (v[0] / m, v[1] / m, v[2] / m)
+
+
+def _normalize(v):
+    """Vector3D::Normalize (VecGeom/base/Vector3D.h:198): multiply by 1/Length()."""
+    r = 1.0 / math.sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    return (v[0] * r, v[1] * r, v[2] * r)
+
+
+def _case(ref, shape, params, op, p, d, expect, cmp="approx"):
+    return dict(ref=ref, shape=shape, params=tuple(params), op=op, p=tuple(p), d=tuple(d) if d else None,
+                expect=expect, cmp=cmp)
+
+
+B1 = (20.0, 30.0, 40.0)   # TestBox.cpp:46 b1
+B2 = (10.0, 10.0, 10.0)   # TestBox.cpp:47 b2
+B4 = (5.0, 5.0, 5.0)      # TestBox.cpp:399 b4
+BOX3 = (0.14999999999999999, 24.707000000000001, 22.699999999999999)  # TestBox.cpp:48
+BX = (1.0, 200.0, 200.0)  # TestBox.cpp:439
+
+TB = "test/unit_tests/TestBox.cpp"
+BOX_CASES = [
+    _case(f"{TB}:171", BOX, B1, "dist_out", pzero, vx, 20.0),
+    _case(f"{TB}:175", BOX, B1, "dist_out", pzero, vmx, 20.0),
+    _case(f"{TB}:179", BOX, B1, "dist_out", pzero, vy, 30.0),
+    _case(f"{TB}:183", BOX, B1, "dist_out", pzero, vmy, 30.0),
+    _case(f"{TB}:187", BOX, B1, "dist_out", pzero, vz, 40.0),
+    _case(f"{TB}:191", BOX, B1, "dist_out", pzero, vmz, 40.0),
+    _case(f"{TB}:195", BOX, B1, "dist_out", pzero, vxy, math.sqrt(800.0)),
+    # signed-zero directions: pin Sign(x) = copysign(1, x) (BoxImplementation.h:115)
+    _case(f"{TB}:201", BOX, B1, "dist_out", pzero, (-0.0, -0.0, -1.0), 40.0),
+    _case(f"{TB}:203", BOX, B1, "dist_out", pzero, (0.0, -0.0, 1.0), 40.0),
+    _case(f"{TB}:205", BOX, B1, "dist_out", pzero, (0.0, 0.0, -1.0), 40.0),
+    _case(f"{TB}:207", BOX, B1, "dist_out", pzero, (0.0, 1.0, 0.0), 30.0),
+    _case(f"{TB}:209", BOX, B1, "dist_out", pzero, (0.0, 1.0, -0.0), 30.0),
+    _case(f"{TB}:211", BOX, B1, "dist_out", pzero, (-0.0, 1.0, 0.0), 30.0),
+    _case(f"{TB}:213", BOX, B1, "dist_out", pzero, (1.0, -0.0, 0.0), 20.0),
+    _case(f"{TB}:215", BOX, B1, "dist_out", pzero, (-1.0, 0.0, -0.0), 20.0),
+    _case(f"{TB}:217", BOX, B1, "dist_out", pzero, (-1.0, -0.0, -0.0), 20.0),
+    _case(f"{TB}:220", BOX, B1, "dist_out", (20.0, 0.0, 0.0), vx, 0.0),
+    _case(f"{TB}:224", BOX, B1, "dist_out", (20.0, 0.0, 0.0), vmx, 40.0),
+    _case(f"{TB}:228", BOX, B1, "dist_out", (-20.0, 0.0, 0.0), vmx, 0.0),
+    _case(f"{TB}:232", BOX, B1, "dist_out", (0.0, 30.0, 0.0), vy, 0.0),
+    _case(f"{TB}:236", BOX, B1, "dist_out", (0.0, -30.0, 0.0), vmy, 0.0),
+    _case(f"{TB}:240", BOX, B1, "dist_out", (0.0, 0.0, 40.0), vz, 0.0),
+    _case(f"{TB}:244", BOX, B1, "dist_out", (0.0, 0.0, -40.0), vmz, 0.0),
+    _case(f"{TB}:249", BOX, B1, "inside", pzero, None, 1, "eq"),
+    _case(f"{TB}:250", BOX, B1, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{TB}:251", BOX, B1, "inside", (20.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TB}:252", BOX, B1, "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TB}:253", BOX, B1, "inside", (0.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{TB}:255", BOX, B2, "inside", pzero, None, 1, "eq"),
+    _case(f"{TB}:256", BOX, B2, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{TB}:257", BOX, B2, "inside", (20.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TB}:258", BOX, B2, "inside", (0.0, 30.0, 0.0), None, 3, "eq"),
+    _case(f"{TB}:259", BOX, B2, "inside", (0.0, 0.0, 40.0), None, 3, "eq"),
+    _case(f"{TB}:260", BOX, B2, "inside", (10.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TB}:261", BOX, B2, "inside", (0.0, 10.0, 0.0), None, 2, "eq"),
+    _case(f"{TB}:262", BOX, B2, "inside", (0.0, 0.0, 10.0), None, 2, "eq"),
+    _case(f"{TB}:263", BOX, B2, "inside", (20.0, 20.0, 10.0), None, 3, "eq"),
+    _case(f"{TB}:264", BOX, B2, "inside", (100.0, 10.0, 30.0), None, 3, "eq"),
+    _case(f"{TB}:265", BOX, B2, "inside", (10.0, 20.0, 20.0), None, 3, "eq"),
+    _case(f"{TB}:268", BOX, B1, "safe_out", pzero, None, 20.0),
+    _case(f"{TB}:270", BOX, B1, "safe_out", vx, None, 19.0),
+    _case(f"{TB}:272", BOX, B1, "safe_out", vy, None, 20.0),
+    _case(f"{TB}:274", BOX, B1, "safe_out", vz, None, 20.0),
+    _case(f"{TB}:309", BOX, B1, "safe_in", (100.0, 0.0, 0.0), None, 80.0),
+    _case(f"{TB}:311", BOX, B1, "safe_in", (-100.0, 0.0, 0.0), None, 80.0),
+    _case(f"{TB}:313", BOX, B1, "safe_in", (0.0, 100.0, 0.0), None, 70.0),
+    _case(f"{TB}:315", BOX, B1, "safe_in", (0.0, -100.0, 0.0), None, 70.0),
+    _case(f"{TB}:317", BOX, B1, "safe_in", (0.0, 0.0, 100.0), None, 60.0),
+    _case(f"{TB}:319", BOX, B1, "safe_in", (0.0, 0.0, -100.0), None, 60.0),
+    _case(f"{TB}:323", BOX, B1, "dist_in", (100.0, 0.0, 0.0), vmx, 80.0),
+    _case(f"{TB}:325", BOX, B1, "dist_in", (-100.0, 0.0, 0.0), vx, 80.0),
+    _case(f"{TB}:327", BOX, B1, "dist_in", (0.0, 100.0, 0.0), vmy, 70.0),
+    _case(f"{TB}:329", BOX, B1, "dist_in", (0.0, -100.0, 0.0), vy, 70.0),
+    _case(f"{TB}:331", BOX, B1, "dist_in", (0.0, 0.0, 100.0), vmz, 60.0),
+    _case(f"{TB}:333", BOX, B1, "dist_in", (0.0, 0.0, -100.0), vz, 60.0),
+    _case(f"{TB}:338", BOX, B1, "dist_in", (0.0, 0.0, -50.0), (-0.0, -0.0, 1.0), 10.0),
+    _case(f"{TB}:340", BOX, B1, "dist_in", (0.0, 0.0, -50.0), (0.0, -0.0, 1.0), 10.0),
+    _case(f"{TB}:342", BOX, B1, "dist_in", (0.0, 0.0, 50.0), (0.0, 0.0, -1.0), 10.0),
+    _case(f"{TB}:344", BOX, B1, "dist_in", (0.0, -40.0, 0.0), (0.0, 1.0, 0.0), 10.0),
+    _case(f"{TB}:346", BOX, B1, "dist_in", (0.0, -40.0, 0.0), (0.0, 1.0, -0.0), 10.0),
+    _case(f"{TB}:348", BOX, B1, "dist_in", (0.0, -40.0, 0.0), (-0.0, 1.0, 0.0), 10.0),
+    _case(f"{TB}:350", BOX, B1, "dist_in", (-30.0, 0.0, -0.0), (1.0, -0.0, 0.0), 10.0),
+    _case(f"{TB}:352", BOX, B1, "dist_in", (30.0, 0.0, 0.0), (-1.0, 0.0, -0.0), 10.0),
+    _case(f"{TB}:354", BOX, B1, "dist_in", (-30.0, 0.0, 0.0), (1.0, -0.0, -0.0), 10.0),
+    _case(f"{TB}:357", BOX, B1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{TB}:360", BOX, B1, "dist_in", (-100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{TB}:365", BOX, B2, "dist_in", (9.0, 0.0, 12.0), vxmz, INF, "inf"),
+    _case(f"{TB}:370", BOX, B2, "dist_in", (12.0, 9.0, 0.0), vmxy, INF, "inf"),
+    _case(f"{TB}:374", BOX, B2, "dist_in", (12.0, 9.0, 0.0), vmx, 2.0),
+    _case(f"{TB}:378", BOX, B2, "dist_in", (32.0, -11.0, 0.0), vmxy, INF, "inf"),
+    _case(f"{TB}:382", BOX, B1, "dist_in", (-25.0, -35.0, 0.0), vx, INF, "inf"),
+    _case(f"{TB}:386", BOX, B1, "dist_in", (-25.0, -35.0, 0.0), vy, INF, "inf"),
+    _case(f"{TB}:394", BOX, BOX3, "dist_in", (0.15000000000000185, -22.048743592955137, 2.4268539333219472),
+          _unit((-0.76165597579890043, 0.64364445891356026, -0.074515708658524193)), 0.0),
+    _case(f"{TB}:402", BOX, B4, "dist_in", (-3.0087437277453119577, -4.9999999999999928946, 4.8935648380409944025),
+          _unit((0.76315134679548990437, 0.53698876104646497964, -0.35950395323836459305)), 0.0, "le0"),
+    _case(f"{TB}:407", BOX, B2, "dist_in", (10.0, 0.0, 0.0), (1.0, 0.0, 0.0), INF, "inf"),
+    _case(f"{TB}:415", BOX, B2, "dist_in", (10.0 - 0.9 * HALF_TOL, 0.0, 0.0), (1.0, 0.0, 0.0), INF, "inf"),
+    _case(f"{TB}:416", BOX, B2, "inside", (10.0 - 0.9 * HALF_TOL, 0.0, 0.0), None, 2, "eq"),
+]
+
+
+def _vecgeom431():
+    """Test_VECGEOM_431 (TestBox.cpp:432-590): points 6e-15 outside a face, entering or exiting."""
+    out = []
+    norm = _normalize
+    testp = (1.0 + 6.0e-15, 0.0, 0.0)
+    testv = norm((0.0 - 4.0e-06, 1.0, 1.0))
+    out.append(_case(f"{TB}:444", BOX, BX, "dist_in", testp, testv, 0.0))
+    out.append(_case(f"{TB}:446", BOX, BX, "dist_out", testp, testv, 200.0 * math.sqrt(2.0)))
+    out.append(_case(f"{TB}:456", BOX, BX, "dist_out", testp, vx, 0.0))
+    testp = (-1.0 - 6.0e-15, 0.0, 0.0)
+    testv = norm((0.0 + 4.0e-06, 1.0, 1.0))
+    out.append(_case(f"{TB}:467", BOX, BX, "dist_in", testp, testv, 0.0))
+    out.append(_case(f"{TB}:469", BOX, BX, "dist_out", testp, testv, 200.0 * math.sqrt(2.0)))
+    out.append(_case(f"{TB}:479", BOX, BX, "dist_out", testp, vmx, 0.0))
+    return out
+
+
+BOX_CASES += _vecgeom431()
+
+T = "test/unit_tests/TestTube.cpp"
+TWO_PI = 2 * KPI
+T1 = (0.0, 50.0, 50.0, 0.0, TWO_PI)      # TestTube.cpp:52
+T2 = (45.0, 50.0, 50.0, 0.0, TWO_PI)     # TestTube.cpp:54
+T2A = (5.0, 50.0, 50.0, 0.0, TWO_PI)     # TestTube.cpp:55
+TUBE8 = (2550.0, 2580.0, 2000.0, 0.0, TWO_PI)   # TestTube.cpp:66
+TUBE9 = (1150.0, 1180.0, 2000.0, 0.0, TWO_PI)   # TestTube.cpp:67
+TUBE10 = (400.0, 405.0, 400.0, 0.0, TWO_PI)     # TestTube.cpp:68
+
+TUBE_CASES = [
+    _case(f"{T}:120", TUBE, T1, "dist_out", (44.991, 21.816, 4.677), _unit((0.16636, 0.64765, -0.74356)), 0.0, "lt0"),
+    _case(f"{T}:152", TUBE, T1, "inside", pzero, None, 1, "eq"),
+    _case(f"{T}:153", TUBE, T1, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:154", TUBE, T1, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:155", TUBE, T1, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:156", TUBE, T1, "inside", (0.0, 0.0, 50.0), None, 2, "eq"),
+    _case(f"{T}:164", TUBE, T2, "inside", pzero, None, 3, "eq"),
+    _case(f"{T}:165", TUBE, T2, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:166", TUBE, T2, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:167", TUBE, T2, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:168", TUBE, T2, "inside", (0.0, 0.0, 50.0), None, 3, "eq"),
+    _case(f"{T}:170", TUBE, T2A, "inside", pzero, None, 3, "eq"),
+    _case(f"{T}:171", TUBE, T2A, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:172", TUBE, T2A, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:173", TUBE, T2A, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:174", TUBE, T2A, "inside", (0.0, 0.0, 50.0), None, 3, "eq"),
+    _case(f"{T}:179", TUBE, T1, "safe_out", pzero, None, 50.0),
+    _case(f"{T}:183", TUBE, T1, "dist_out", pzero, vx, 50.0),
+    _case(f"{T}:187", TUBE, T1, "dist_out", pzero, vmx, 50.0),
+    _case(f"{T}:191", TUBE, T1, "dist_out", pzero, vy, 50.0),
+    _case(f"{T}:195", TUBE, T1, "dist_out", pzero, vmy, 50.0),
+    _case(f"{T}:199", TUBE, T1, "dist_out", pzero, vz, 50.0),
+    _case(f"{T}:203", TUBE, T1, "dist_out", pzero, vmz, 50.0),
+    _case(f"{T}:207", TUBE, T1, "dist_out", pzero, vxy, 50.0),
+    _case(f"{T}:266", TUBE, T1, "safe_in", (100.0, 0.0, 0.0), None, 50.0),
+    _case(f"{T}:268", TUBE, T1, "safe_in", (-100.0, 0.0, 0.0), None, 50.0),
+    _case(f"{T}:270", TUBE, T1, "safe_in", (0.0, 100.0, 0.0), None, 50.0),
+    _case(f"{T}:272", TUBE, T1, "safe_in", (0.0, -100.0, 0.0), None, 50.0),
+    _case(f"{T}:274", TUBE, T1, "safe_in", (0.0, 0.0, 100.0), None, 50.0),
+    _case(f"{T}:276", TUBE, T1, "safe_in", (0.0, 0.0, -100.0), None, 50.0),
+    _case(f"{T}:281", TUBE, T1, "dist_in", (100.0, 0.0, 0.0), vmx, 50.0),
+    _case(f"{T}:283", TUBE, T1, "dist_in", (-100.0, 0.0, 0.0), vx, 50.0),
+    _case(f"{T}:285", TUBE, T1, "dist_in", (0.0, 100.0, 0.0), vmy, 50.0),
+    _case(f"{T}:287", TUBE, T1, "dist_in", (0.0, -100.0, 0.0), vy, 50.0),
+    _case(f"{T}:289", TUBE, T1, "dist_in", (0.0, 0.0, 100.0), vmz, 50.0),
+    _case(f"{T}:291", TUBE, T1, "dist_in", (0.0, 0.0, -100.0), vz, 50.0),
+    _case(f"{T}:293", TUBE, T1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{T}:396", TUBE, T1, "inside", pzero, None, 1, "eq"),
+    _case(f"{T}:397", TUBE, T1, "inside", (100.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{T}:399", TUBE, TUBE10, "inside", (-114.8213313833317, 382.7843220719649, -32.20788536438663), None, 3,
+          "eq"),
+    _case(f"{T}:414", TUBE, TUBE8, "dist_out", (6.71645645882942, 2579.415860329989, -1.519530725281157),
+          (-0.6305220496340839, -0.07780451841562354, 0.7722618738739774), 1022.64931421),
+    _case(f"{T}:418", TUBE, TUBE9, "dist_out", (2.267347771505638, 1170.164934028592, 4.820317321984064),
+          (-0.1443054266272111, -0.01508874701037938, 0.9894181489944458), 2016.51817758),
+]
+
+ALL_CASES = BOX_CASES + TUBE_CASES
+
+
+def approx_equal(x: float, y: float) -> bool:
+    """ApproxEqual<double> (test/unit_tests/ApproxEqual.h:33-49)."""
+    if x == y:
+        return True
+    if x * y == 0.0:
+        return abs(x - y) < 1e-6
+    if abs(x) > 1.0e100 or abs(y) > 1.0e100:
+        return (x * y > 0) and abs(x) > 1.0e100 and abs(y) > 1.0e100
+    return abs(x - y) / (abs(x) + abs(y)) < 1e-6
+
+
+def check(case, value) -> bool:
+    c = case["cmp"]
+    if c == "approx":
+        return approx_equal(value, case["expect"])
+    if c == "le0":
+        return value <= 0.0
+    if c == "lt0":
+        return value < 0.0
+    if c == "inf":
+        return value >= INF
+    if c == "eq":
+        return value == case["expect"]
+    raise ValueError(c)

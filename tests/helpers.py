@@ -1,0 +1,65 @@
+"""Helpers shared by the test modules: host-only product tables, GPU walks."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+
+from vecgeom_gb300 import _native as N
+from vecgeom_gb300 import workloads as W
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+class HostTables:
+    """libvgnav geometry closed on the host only (VGN_HOST_ONLY): tables, no kernels."""
+
+    def __init__(self, desc):
+        L = N.lib()
+        self._keep = [np.ascontiguousarray(desc.lv_shape, np.int32), np.ascontiguousarray(desc.lv_param_offset, np.int32),
+                      np.ascontiguousarray(desc.params, np.float64), np.ascontiguousarray(desc.pv_logical, np.int32),
+                      np.ascontiguousarray(desc.pv_mother, np.int32),
+                      np.ascontiguousarray(desc.pv_transform, np.float64).reshape(-1)]
+        k = self._keep
+        d = N.GeometryDesc(desc.n_logical, k[0].ctypes.data, k[1].ctypes.data, k[2].ctypes.data, k[2].shape[0],
+                           desc.n_placed, k[3].ctypes.data, k[4].ctypes.data, k[5].ctypes.data, desc.world_placed)
+        self.h = C.c_void_p()
+        N.check(L.vgn_geometry_create(C.byref(d), -1, C.byref(self.h)))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            N.lib().vgn_geometry_free(self.h)
+
+    def navindex(self):
+        p = C.POINTER(C.c_uint32)()
+        n = C.c_size_t()
+        N.check(N.lib().vgn_geometry_navindex(self.h, C.byref(p), C.byref(n)))
+        return np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+
+    def bvh(self, lv):
+        L = N.lib()
+        depth, nn, npr = C.c_int32(), C.c_int32(), C.c_int32()
+        N.check(L.vgn_geometry_bvh_info(self.h, lv, C.byref(depth), C.byref(nn), C.byref(npr)))
+        prim = np.zeros(npr.value, np.int32)
+        off = np.zeros(nn.value, np.int32)
+        nch = np.zeros(nn.value, np.int32)
+        nodes = np.zeros((nn.value, 6))
+        prims = np.zeros((npr.value, 6))
+        N.check(L.vgn_geometry_bvh_arrays(self.h, lv, prim.ctypes.data, off.ctypes.data, nch.ctypes.data,
+                                          nodes.ctypes.data, prims.ctypes.data))
+        return dict(depth=depth.value, prim_id=prim, offset=off, nchild=nch, nodes=nodes, prims=prims)
+
+
+def header_symbols():
+    text = (ROOT / "include" / "vgnav.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(vgn_\w+)\s*\(", text, re.M)))
+
+
+def advance(t: W.TrackBatch, step: np.ndarray, out_states: np.ndarray) -> W.TrackBatch:
+    """The transport loop's move: p += step * d, state = propagated state."""
+    return W.TrackBatch(t.x + step * t.dx, t.y + step * t.dy, t.z + step * t.dz, t.dx, t.dy, t.dz, t.step_limit,
+                        out_states)
+
+
+def keep(t: W.TrackBatch, mask: np.ndarray) -> W.TrackBatch:
+    return W.TrackBatch(*(a[mask] for a in (t.x, t.y, t.z, t.dx, t.dy, t.dz, t.step_limit, t.states)))

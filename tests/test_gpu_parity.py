@@ -1,0 +1,210 @@
+"""GPU parity: the libvgnav FP64 kernels against the CPU oracle, through the C ABI.
+
+Bar: bit-exact (np.array_equal on the float64 values, identical 12-byte
+states) for steps, safeties, next volumes, located states and shape queries,
+both through device pointers (torch CUDA tensors) and through host pointers
+(the library's own staging path)."""
+import numpy as np
+import pytest
+
+from golden import known_answers as KA
+from helpers import advance, keep
+from vecgeom_gb300 import workloads as W
+from vecgeom_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+OPS = {"dist_in": 0, "dist_out": 1, "safe_in": 2, "safe_out": 3, "contains": 4, "inside": 5}
+
+
+def to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def states_to_dev(torch, st):
+    a = np.zeros((st.shape[0], 3), np.int32)
+    a[:, 0] = st["nav_ind"].view(np.int32)
+    a[:, 1] = st["last_exited"].view(np.int32)
+    a[:, 2] = st["on_boundary"]
+    return torch.from_numpy(a).cuda()
+
+
+def gpu_step(torch, geo, t, safety=True, relocate=True):
+    from vecgeom_gb300.navigator import SOA3D, NavStatePool
+
+    pts = SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+    dirs = SOA3D(to_dev(torch, t.dx), to_dev(torch, t.dy), to_dev(torch, t.dz))
+    sl = to_dev(torch, t.step_limit)
+    inp = NavStatePool(states_to_dev(torch, t.states))
+    out = NavStatePool.empty_like(inp)
+    steps = torch.empty(t.n, dtype=torch.float64, device="cuda")
+    saf = torch.empty(t.n, dtype=torch.float64, device="cuda") if safety else None
+    geo.step(pts, dirs, sl, inp, out, steps, saf, relocate=relocate)
+    geo.synchronize()
+    return dict(step=steps.cpu().numpy(), out=out.to_numpy(), safety=None if saf is None else saf.cpu().numpy())
+
+
+def single_shape(shape, params):
+    b = W.GeometryBuilder()
+    lv = b.logical(shape, params)
+    b.place_world(lv)
+    return b.build()
+
+
+@pytest.mark.parametrize("case", KA.ALL_CASES, ids=lambda c: f"{c['ref'].split('/')[-1]}-{c['op']}")
+def test_kernel_known_answer(vgnav, cuda, case):
+    geo = vgnav.Geometry(single_shape(case["shape"], case["params"]))
+    p = [np.array([v]) for v in case["p"]]
+    d = [np.array([v]) for v in (case["d"] or (0.0, 0.0, 0.0))]
+    out = np.zeros(1)
+    geo.shape(0, OPS[case["op"]], vgnav.SOA3D(*p), vgnav.SOA3D(*d), out)
+    assert KA.check(case, float(out[0])), (case["ref"], float(out[0]))
+
+
+def test_tube_points_bit_exact(oracle, vgnav, cuda):
+    """Tube(10,50,100) with 2^20 points inside: DistanceToOut and SafetyToOut, plus the other queries."""
+    torch = cuda
+    t = W.tube_points()
+    desc = W.tube_geometry()
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    pts = vgnav.SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+    dirs = vgnav.SOA3D(to_dev(torch, t.dx), to_dev(torch, t.dy), to_dev(torch, t.dz))
+    out = torch.empty(t.n, dtype=torch.float64, device="cuda")
+    for op in range(6):
+        geo.shape(0, op, pts, dirs, out)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        ref = og.shape(0, op, t.x, t.y, t.z, t.dx, t.dy, t.dz)
+        assert np.array_equal(got, ref), (op, int(np.sum(got != ref)))
+    # points outside and on the surface band too
+    rng = np.random.Generator(np.random.PCG64(7))
+    x, y, z = (rng.uniform(-120, 120, 200000) for _ in range(3))
+    dx, dy, dz = W.isotropic(rng, 200000)
+    for op in range(6):
+        got = np.zeros_like(x)
+        geo.shape(0, op, vgnav.SOA3D(x, y, z), vgnav.SOA3D(dx, dy, dz), got)
+        assert np.array_equal(got, og.shape(0, op, x, y, z, dx, dy, dz)), op
+
+
+def test_box_grid_step_bit_exact(oracle, vgnav, cuda):
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid, n=1 << 16, seed_points=41, seed_dirs=42)
+    ref = og.step(t, calcsafety=True)
+    got = gpu_step(cuda, geo, t)
+    assert np.array_equal(got["step"], ref["step"])
+    assert np.array_equal(got["safety"], ref["safety"])
+    assert np.array_equal(got["out"], ref["out"])
+    # ComputeStep (no relocation)
+    ref_n = og.step(t, relocate=False)
+    got_n = gpu_step(cuda, geo, t, safety=False, relocate=False)
+    assert np.array_equal(got_n["step"], ref_n["step"])
+    assert np.array_equal(got_n["out"], ref_n["out"])
+
+
+def test_box_grid_host_pointer_path(oracle, vgnav, cuda):
+    """Same call with host numpy arrays: the library stages through the device."""
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid, n=50000, seed_points=43, seed_dirs=44)
+    ref = og.step(t)
+    out = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    steps = np.zeros(t.n)
+    saf = np.zeros(t.n)
+    geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit, vgnav.NavStatePool(t.states),
+             vgnav.NavStatePool(out), steps, saf)
+    assert np.array_equal(steps, ref["step"]) and np.array_equal(saf, ref["safety"])
+    assert np.array_equal(out, ref["out"])
+    # the alias entry point gives the same answer
+    out2 = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    steps2 = np.zeros(t.n)
+    geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit, vgnav.NavStatePool(t.states),
+             vgnav.NavStatePool(out2), steps2, None, api="alias")
+    assert np.array_equal(steps2, ref["step"]) and np.array_equal(out2, ref["out"])
+
+
+@pytest.mark.parametrize("which", ["box_grid", "nested"])
+def test_walk_to_world_exit(oracle, vgnav, cuda, which):
+    """Every step of every track, stepped until it leaves the world, equals the oracle."""
+    if which == "box_grid":
+        grid = W.box_grid_geometry()
+        desc = grid.desc
+        t = W.box_grid_tracks(grid, n=8192, seed_points=51, seed_dirs=52)
+    else:
+        desc = W.nested_geometry()
+        t = W.uniform_tracks(8192, 480.0, 53, 54)
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    if which == "nested":
+        st = np.zeros(t.n, dtype=W.STATE_DTYPE)
+        geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st))
+        assert np.array_equal(st, og.locate(t.x, t.y, t.z))
+        t.states = st
+    for it in range(400):
+        ref = og.step(t)
+        got = gpu_step(cuda, geo, t)
+        assert np.array_equal(got["step"], ref["step"]), it
+        assert np.array_equal(got["safety"], ref["safety"]), it
+        assert np.array_equal(got["out"], ref["out"]), it
+        t = advance(t, ref["step"], ref["out"])
+        t = keep(t, t.states["nav_ind"] != 0)
+        if t.n == 0:
+            break
+    assert t.n == 0
+
+
+def test_safety_and_locate_kernels(oracle, vgnav, cuda):
+    desc = W.nested_geometry()
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    t = W.uniform_tracks(100000, 490.0, 61, 62)
+    st = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st))
+    assert np.array_equal(st, og.locate(t.x, t.y, t.z))
+    inside = st["nav_ind"] != 0
+    x, y, z, s = t.x[inside], t.y[inside], t.z[inside], st[inside]
+    saf = np.zeros(x.shape[0])
+    geo.safety(vgnav.SOA3D(x, y, z), vgnav.NavStatePool(s), saf)
+    assert np.array_equal(saf, og.safety(x, y, z, s))
+
+
+def test_full_size_box_grid(oracle, vgnav, cuda):
+    """2^22 tracks of the 4096-box geometry: every result equals the oracle's."""
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid)
+    ref = og.step(t)
+    got = gpu_step(cuda, geo, t)
+    assert np.array_equal(got["step"], ref["step"])
+    assert np.array_equal(got["safety"], ref["safety"])
+    assert np.array_equal(got["out"], ref["out"])
+    # size-independent properties
+    assert np.all(got["safety"] <= got["step"] + 1e-9)
+    assert np.all((got["out"]["on_boundary"] == 1) | (got["step"] == t.step_limit))
+
+
+def test_edge_cases(oracle, vgnav, cuda):
+    grid = W.box_grid_geometry(seed=7, n=5)
+    geo = vgnav.Geometry(grid.desc)
+    # empty batch
+    z = np.zeros(0)
+    geo.step(vgnav.SOA3D(z, z, z), vgnav.SOA3D(z, z, z), z, vgnav.NavStatePool(np.zeros(0, W.STATE_DTYPE)),
+             vgnav.NavStatePool(np.zeros(0, W.STATE_DTYPE)), z)
+    # a navigation index that does not start a state record is refused, not dereferenced
+    t = W.uniform_tracks(64, 100.0, 71, 72)
+    t.states["nav_ind"] = 1
+    t.states["nav_ind"][5] = 2
+    t.states["nav_ind"][9] = 0xFFFFFFFE
+    out = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    with pytest.raises(N.VgnError) as e:
+        geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit,
+                 vgnav.NavStatePool(t.states), vgnav.NavStatePool(out), np.zeros(t.n))
+    assert e.value.code == N.VGN_ERR_STATE
+    # the context is still usable afterwards
+    t.states["nav_ind"] = 1
+    geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit, vgnav.NavStatePool(t.states),
+             vgnav.NavStatePool(out), np.zeros(t.n))

@@ -1,0 +1,59 @@
+"""The product's host geometry closing (C++) against the oracle's (C): the
+navigation index table and every BVH array must be identical word for word,
+since NavStateIndex values are offsets into the table and leaf order decides
+ties.  No GPU needed (geometry closed with VGN_HOST_ONLY)."""
+import numpy as np
+import pytest
+
+from helpers import HostTables
+from vecgeom_gb300 import workloads as W
+
+
+def geometries():
+    return {
+        "box_grid_4096": W.box_grid_geometry().desc,
+        "nested_3_levels": W.nested_geometry(),
+        "single_tube": W.tube_geometry(),
+        "box_grid_small": W.box_grid_geometry(seed=7, n=5).desc,
+    }
+
+
+@pytest.mark.parametrize("name", list(geometries()))
+def test_navindex_and_bvh_identical(oracle, vgnav, name):
+    desc = geometries()[name]
+    og = oracle.OracleGeometry(desc)
+    ht = HostTables(desc)
+    assert np.array_equal(og.navindex(), ht.navindex())
+    for lv in range(desc.n_logical):
+        if not np.any(desc.pv_mother == lv):
+            continue
+        a, b = og.bvh(lv), ht.bvh(lv)
+        assert a["depth"] == b["depth"]
+        for k in ("prim_id", "offset", "nchild", "nodes", "prims"):
+            assert np.array_equal(a[k], b[k]), (name, lv, k)
+
+
+def test_bvh_depth_rule(oracle):
+    """BVH depth = min(log2(n/2), 32) (source/BVH.cpp:71-73); internal nodes marked -1 only above 8 prims."""
+    desc = W.box_grid_geometry().desc
+    b = oracle.OracleGeometry(desc).bvh(0)
+    assert b["depth"] == 11 and len(b["nchild"]) == 4095
+    assert np.all(b["nchild"][b["nchild"] >= 0] <= 8) or np.any(b["nchild"] > 8)
+    internal = np.nonzero(b["nchild"] < 0)[0]
+    assert len(internal) > 0 and internal.max() < 4095 // 2
+
+
+def test_invalid_descriptions_rejected(vgnav):
+    from vecgeom_gb300 import _native as N
+
+    b = W.GeometryBuilder()
+    lv = b.logical(W.TUBE, (10.0, 50.0, 100.0, 0.0, 1.0))  # phi section: not supported
+    b.place_world(lv)
+    with pytest.raises(N.VgnError) as e:
+        HostTables(b.build())
+    assert e.value.code == N.VGN_ERR_UNSUPPORTED
+    b = W.GeometryBuilder()
+    lv = b.logical(99, (1.0,))
+    b.place_world(lv)
+    with pytest.raises(N.VgnError):
+        HostTables(b.build())

@@ -1,0 +1,25 @@
+"""Pin the CPU oracle against the reference's own unit-test known answers
+(test/unit_tests/TestBox.cpp, TestTube.cpp; see tests/golden/known_answers.py)."""
+import numpy as np
+import pytest
+
+from golden import known_answers as KA
+from vecgeom_gb300.workloads import GeometryBuilder
+
+OPS = {"dist_in": 0, "dist_out": 1, "safe_in": 2, "safe_out": 3, "contains": 4, "inside": 5}
+
+
+def single_shape(shape, params):
+    b = GeometryBuilder()
+    lv = b.logical(shape, params)
+    b.place_world(lv)
+    return b.build()
+
+
+@pytest.mark.parametrize("case", KA.ALL_CASES, ids=lambda c: f"{c['ref'].split('/')[-1]}-{c['op']}")
+def test_oracle_known_answer(oracle, case):
+    g = oracle.OracleGeometry(single_shape(case["shape"], case["params"]))
+    p = [np.array([v]) for v in case["p"]]
+    d = [np.array([v]) for v in (case["d"] or (0.0, 0.0, 0.0))]
+    val = float(g.shape(0, OPS[case["op"]], *p, *d)[0])
+    assert KA.check(case, val), f"{case['ref']}: {case['op']} -> {val!r}, expected {case['cmp']} {case['expect']!r}"

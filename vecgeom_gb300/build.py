@@ -1,0 +1,78 @@
+"""In-tree build of libvgnav.so for sm_103a (nvcc + g++, no cmake).
+
+Every translation unit is compiled in parallel into ``vecgeom_gb300/_build``
+and linked into ``vecgeom_gb300/lib/libvgnav.so``.  The FP64 kernel set is
+compiled with ``-fmad=false`` so that no multiply-add is contracted: its
+results are bit-identical to the reference's scalar CPU navigator.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIBDIR = PKG / "lib"
+LIB = LIBDIR / "libvgnav.so"
+INCLUDE = PKG.parent / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+# (source, extra nvcc flags)
+UNITS = [
+    ("kernels_fp64.cu", ["-fmad=false"]),
+    ("host_geometry.cpp", []),
+    ("host_shapes.cpp", []),
+    ("vgnav_api.cpp", []),
+]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libvgnav")
+
+
+def _compile(nvcc: str, src: str, extra: list[str]) -> Path:
+    out = BUILD / (src.replace(".", "_") + ".o")
+    srcp = CSRC / src
+    deps = [srcp] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "vgnav.h"]
+    if out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return out
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
+    if src.endswith(".cu"):
+        cmd = [nvcc, *ARCH, "-lineinfo", "-Xptxas", "-v", *common, *extra, "-c", str(srcp), "-o", str(out)]
+    else:
+        cmd = [nvcc, "-x", "c++", *common, "-Xcompiler", "-ffp-contract=off", *extra, "-c", str(srcp), "-o", str(out)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    (BUILD / (src + ".ptxas.txt")).write_text(res.stderr)
+    return out
+
+
+def build(verbose: bool = False) -> Path:
+    """Compile (incrementally) and link libvgnav.so; returns its path."""
+    nvcc = _nvcc()
+    BUILD.mkdir(exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(lambda u: _compile(nvcc, u[0], u[1]), UNITS))
+    if not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
+        cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-cudart", "static", "-lpthread"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    if verbose:
+        print(f"built {LIB}", file=sys.stderr)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)

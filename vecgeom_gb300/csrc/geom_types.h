@@ -1,0 +1,118 @@
+// geom_types.h -- device-resident geometry layout shared by the host builder
+// and the CUDA kernels.
+//
+// Everything the navigation kernels read lives in a handful of flat,
+// read-only arrays that stay resident in HBM (and, being a few MiB at most,
+// in the 129 MB L2):
+//   navind    the navigation index table, byte-for-byte the reference layout
+//             (source/NavIndexTable.cpp:9-99) so NavStateIndex values match
+//   pv        one 128-byte record per placed volume (transform + ids)
+//   lv        one 32-byte record per logical volume
+//   nodes     BVH nodes, 64-byte records, complete binary tree per volume
+//   prims     leaf primitives (daughter AABB + placed-volume id) stored in BVH
+//             leaf order, so a leaf's candidates are one contiguous run
+//   fnodes/fprims  the same boxes rounded outward to FP32 (mixed precision)
+//   shape     per-volume shape parameter rows (doubles, cached members)
+#pragma once
+
+#include <cstdint>
+
+namespace vgn {
+
+constexpr int kStackSize = 32;  // BVH::BVH_MAX_DEPTH (BVH.h:33)
+constexpr int kMaxLevels = 30;  // bound on geometry depth (relocation loops)
+
+enum ShapeType : int32_t { kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kNumShapes = 7 };
+
+// device error bits (OR-ed into the status word)
+enum DevError : uint32_t { kErrStack = 1u, kErrRelocate = 2u, kErrState = 4u };
+
+struct alignas(16) XForm {
+  double t[3];  // Transformation3D::fTranslation
+  double r[9];  // Transformation3D::fRotation (row-major as in the reference)
+};
+
+struct alignas(128) PVRec {
+  XForm xf;           // placement transformation (mother frame -> this volume's frame)
+  int32_t lv;         // logical volume placed
+  int32_t child_id;   // position in the mother's daughter list
+  int32_t shape;      // shape type of lv (cached)
+  int32_t shape_row;  // offset of lv's shape row in GeomView::shape (cached)
+  int32_t pad[4];
+};
+static_assert(sizeof(PVRec) == 128, "PVRec must be 128 bytes");
+
+struct alignas(32) LVRec {
+  int32_t shape;
+  int32_t shape_row;
+  int32_t nd;            // number of daughters
+  int32_t daughters_off; // into GeomView::daughters
+  int32_t nodes_off;     // first BVH node (into nodes / fnodes)
+  int32_t n_nodes;       // (2 << depth) - 1, 0 if no daughters
+  int32_t prims_off;     // first leaf primitive (into prims / fprims)
+  int32_t depth;
+};
+static_assert(sizeof(LVRec) == 32, "LVRec must be 32 bytes");
+
+struct alignas(64) NodeRec {
+  double mn[3], mx[3];
+  int32_t nchild;  // -1 internal, >= 0 leaf (BVH.cpp:85-86)
+  int32_t offset;  // first primitive position of this node
+  int32_t pad[2];
+};
+static_assert(sizeof(NodeRec) == 64, "NodeRec must be 64 bytes");
+
+struct alignas(64) PrimRec {
+  double mn[3], mx[3];  // daughter AABB with the 1e-3 margin (ABBoxManager.cpp:141-142)
+  int32_t pv;           // placed volume id
+  int32_t prim;         // daughter index in the mother
+  int32_t pad[2];
+};
+static_assert(sizeof(PrimRec) == 64, "PrimRec must be 64 bytes");
+
+// FP32 boxes rounded outward (min toward -inf, max toward +inf): a superset of
+// the FP64 box, so a conservative FP32 slab test never drops a candidate.
+struct alignas(32) FNodeRec {
+  float mn[3], mx[3];
+  int32_t nchild;
+  int32_t offset;
+};
+static_assert(sizeof(FNodeRec) == 32, "FNodeRec must be 32 bytes");
+
+struct alignas(32) FPrimRec {
+  float mn[3], mx[3];
+  int32_t pv;
+  int32_t prim;
+};
+static_assert(sizeof(FPrimRec) == 32, "FPrimRec must be 32 bytes");
+
+// Row layouts (doubles) of GeomView::shape per shape type.
+namespace row {
+// Box: BoxStruct::fDimensions
+constexpr int kBoxSize = 4;
+// Tube (full phi): TubeStruct cached members
+enum { TubeRmin = 0, TubeRmax, TubeZ, TubeRmin2, TubeRmax2, TubeTolIrmin2, TubeTolOrmin2, TubeTolIrmax2,
+       TubeTolOrmax2, TubeMaxVal, kTubeSize };
+}  // namespace row
+
+// Plain-pointer view of the device tables, passed to kernels by value.
+struct GeomView {
+  const uint32_t *navind;
+  const uint32_t *node_start;  // bitset: navigation indices that start a state record
+  const PVRec *pv;
+  const LVRec *lv;
+  const int32_t *daughters;
+  const NodeRec *nodes;
+  const PrimRec *prims;
+  const FNodeRec *fnodes;
+  const FPrimRec *fprims;
+  const double *shape;
+  uint32_t navind_words;
+  int32_t n_pv;
+  int32_t n_lv;
+  int32_t world_pv;
+  int32_t max_depth;
+  uint32_t *status;  // device error word (DevError bits)
+};
+
+}  // namespace vgn

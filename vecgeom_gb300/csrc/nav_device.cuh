@@ -1,0 +1,443 @@
+// nav_device.cuh -- device-side navigation: navigation-index decoding,
+// transforms, BVH traversal (FP64), relocation, safety and point location.
+//
+// One thread owns one track for the whole step: global->local transform,
+// mother DistanceToOut, BVH traversal with leaf DistanceToIn through a
+// switch on the shape type (no virtual calls), PrepareOutState, and the
+// relocation after the boundary.  Every loop is bounded; overflow of the
+// traversal stack or of the geometry depth sets a bit in the status word and
+// ends the track's work instead of trapping.
+#pragma once
+
+#include "shapes_fp64.cuh"
+
+namespace vgn {
+namespace dev {
+
+struct State {
+  uint32_t nav_ind, last_exited;
+  uint32_t on_boundary;
+};
+
+__device__ __forceinline__ void raise_error(const GeomView &g, uint32_t bit) { atomicOr(g.status, bit); }
+
+// ---- NavStateIndex decoding (NavStateIndex.h:136-265) ----
+__device__ __forceinline__ uint32_t ni_word(const GeomView &g, uint32_t i) { return __ldg(g.navind + i); }
+__device__ __forceinline__ int ni_top(const GeomView &g, uint32_t ni) { return ni > 0 ? (int)ni_word(g, ni + 1) : -1; }
+__device__ __forceinline__ uint32_t ni_pop(const GeomView &g, uint32_t ni) { return ni > 0 ? ni_word(g, ni) : 0u; }
+__device__ __forceinline__ uint32_t ni_push(const GeomView &g, uint32_t ni, int pv)
+{
+  return ni > 0 ? ni_word(g, ni + 3 + (uint32_t)__ldg(&g.pv[pv].child_id)) : 1u;
+}
+// a navigation index supplied by the caller must start a state record of the table
+__device__ __forceinline__ bool ni_valid(const GeomView &g, uint32_t ni)
+{
+  return ni > 0 && ni < g.navind_words && ((__ldg(g.node_start + (ni >> 5)) >> (ni & 31)) & 1u);
+}
+
+struct Xf {
+  double t[3];
+  double r[9];
+};
+
+// TopMatrixImpl with a cached global matrix at every level (NavStateIndex.h:232-265):
+// identity if the matrix flags are clear, else the stored translation/rotation.
+__device__ __forceinline__ void top_matrix(const GeomView &g, uint32_t ni, Xf &m)
+{
+  m.t[0] = m.t[1] = m.t[2] = 0.;
+  m.r[0] = 1.; m.r[1] = 0.; m.r[2] = 0.;
+  m.r[3] = 0.; m.r[4] = 1.; m.r[5] = 0.;
+  m.r[6] = 0.; m.r[7] = 0.; m.r[8] = 1.;
+  if (ni == 0) return;
+  const uint32_t w      = ni_word(g, ni + 2);
+  const uint32_t hasm   = (w >> 8) & 0xffu;
+  const uint32_t nd     = w >> 16;
+  if ((hasm & 0x03u) == 0) return;
+  uint32_t idx = ni + 3 + nd + ((nd + 1) & 1);
+  if ((idx * 4) % 8 != 0) idx += 1;
+  const double *a = reinterpret_cast<const double *>(g.navind + idx);
+  if (hasm & 0x02u) {
+    m.t[0] = __ldg(a + 0);
+    m.t[1] = __ldg(a + 1);
+    m.t[2] = __ldg(a + 2);
+  }
+  if (hasm & 0x01u) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) m.r[i] = __ldg(a + 3 + i);
+  }
+}
+
+// Transform<kGeneric,kGeneric> (Transformation3D.h:663-673, 729-735, 746-770)
+__device__ __forceinline__ D3 xf_point(const double *t, const double *r, D3 p)
+{
+  const double t0 = p.x - t[0], t1 = p.y - t[1], t2 = p.z - t[2];
+  double l0 = t0 * r[0], l1 = t0 * r[1], l2 = t0 * r[2];
+  l0 += t1 * r[3];
+  l1 += t1 * r[4];
+  l2 += t1 * r[5];
+  l0 += t2 * r[6];
+  l1 += t2 * r[7];
+  l2 += t2 * r[8];
+  return d3(l0, l1, l2);
+}
+
+// TransformDirection<kGeneric>
+__device__ __forceinline__ D3 xf_dir(const double *r, D3 d)
+{
+  double l0 = d.x * r[0], l1 = d.x * r[1], l2 = d.x * r[2];
+  l0 += d.y * r[3];
+  l1 += d.y * r[4];
+  l2 += d.y * r[5];
+  l0 += d.z * r[6];
+  l1 += d.z * r[7];
+  l2 += d.z * r[8];
+  return d3(l0, l1, l2);
+}
+
+// InverseTransform (Transformation3D.h:793-827)
+__device__ __forceinline__ D3 xf_inverse(const double *t, const double *r, D3 l)
+{
+  double a = t[0], b = t[1], c = t[2];
+  a += l.x * r[0];
+  a += l.y * r[1];
+  a += l.z * r[2];
+  b += l.x * r[3];
+  b += l.y * r[4];
+  b += l.z * r[5];
+  c += l.x * r[6];
+  c += l.y * r[7];
+  c += l.z * r[8];
+  return d3(a, b, c);
+}
+
+// placement transform of placed volume pv, read through the read-only cache
+struct PvXf {
+  double t[3];
+  double r[9];
+};
+__device__ __forceinline__ void load_pv_xf(const GeomView &g, int pv, PvXf &x)
+{
+  const double *src = &g.pv[pv].xf.t[0];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) x.t[i] = __ldg(src + i);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) x.r[i] = __ldg(src + 3 + i);
+}
+
+__device__ __forceinline__ const double *pv_row(const GeomView &g, int pv, int &type)
+{
+  type = __ldg(&g.pv[pv].shape);
+  return g.shape + __ldg(&g.pv[pv].shape_row);
+}
+
+// placed DistanceToIn / SafetyToIn / Contains (SpecializedPlacedVolImplHelper.h:118-175)
+__device__ __forceinline__ double pv_dist_in(const GeomView &g, int pv, D3 p, D3 d)
+{
+  PvXf x;
+  load_pv_xf(g, pv, x);
+  int type;
+  const double *row = pv_row(g, pv, type);
+  return shape_dist_in(type, row, xf_point(x.t, x.r, p), xf_dir(x.r, d));
+}
+
+__device__ __forceinline__ double pv_safe_in(const GeomView &g, int pv, D3 p)
+{
+  PvXf x;
+  load_pv_xf(g, pv, x);
+  int type;
+  const double *row = pv_row(g, pv, type);
+  return shape_safe_in(type, row, xf_point(x.t, x.r, p));
+}
+
+__device__ __forceinline__ bool pv_contains(const GeomView &g, int pv, D3 p, D3 &lp)
+{
+  PvXf x;
+  load_pv_xf(g, pv, x);
+  int type;
+  const double *row = pv_row(g, pv, type);
+  lp                = xf_point(x.t, x.r, p);
+  return shape_contains(type, row, lp);
+}
+
+__device__ __forceinline__ bool pv_unplaced_contains(const GeomView &g, int pv, D3 p)
+{
+  int type;
+  const double *row = pv_row(g, pv, type);
+  return shape_contains(type, row, p);
+}
+
+// AABB::ComputeIntersectionInvDir (AABB.h:136-154)
+__device__ __forceinline__ void slab(const double *mn, const double *mx, D3 p, D3 inv, double &tmin, double &tmax)
+{
+  double a0 = (__ldg(mn + 0) - p.x) * inv.x, b0 = (__ldg(mx + 0) - p.x) * inv.x;
+  double a1 = (__ldg(mn + 1) - p.y) * inv.y, b1 = (__ldg(mx + 1) - p.y) * inv.y;
+  double a2 = (__ldg(mn + 2) - p.z) * inv.z, b2 = (__ldg(mx + 2) - p.z) * inv.z;
+  double s;
+  if (a0 > b0) { s = a0; a0 = b0; b0 = s; }
+  if (a1 > b1) { s = a1; a1 = b1; b1 = s; }
+  if (a2 > b2) { s = a2; a2 = b2; b2 = s; }
+  tmin = max3(a0, a1, a2);
+  tmax = min3(b0, b1, b2) * (1. + 2 * kEpsilon);
+}
+
+// AABB::Safety (AABB.h:81)
+__device__ __forceinline__ double box_safety(const double *mn, const double *mx, D3 p)
+{
+  const double mn0 = __ldg(mn + 0), mn1 = __ldg(mn + 1), mn2 = __ldg(mn + 2);
+  const double mx0 = __ldg(mx + 0), mx1 = __ldg(mx + 1), mx2 = __ldg(mx + 2);
+  const double c0 = 0.5 * (mx0 + mn0), c1 = 0.5 * (mx1 + mn1), c2 = 0.5 * (mx2 + mn2);
+  const double s0 = mx0 - mn0, s1 = mx1 - mn1, s2 = mx2 - mn2;
+  return max3(fabs(p.x - c0) - 0.5 * s0, fabs(p.y - c1) - 0.5 * s1, fabs(p.z - c2) - 0.5 * s2);
+}
+
+__device__ __forceinline__ bool box_contains_pt(const double *mn, const double *mx, D3 p)
+{
+  return p.x >= __ldg(mn + 0) && p.x <= __ldg(mx + 0) && p.y >= __ldg(mn + 1) && p.y <= __ldg(mx + 1) &&
+         p.z >= __ldg(mn + 2) && p.z <= __ldg(mx + 2);
+}
+
+// BVH::CheckDaughterIntersections (BVH.h:96-146), FP64
+__device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVRec &lv, D3 lp, D3 ld, double &step,
+                                                    int last, int &hit)
+{
+  unsigned stack[kStackSize];
+  int sp        = 1;
+  stack[0]      = 0;
+  const D3 inv  = d3(1.0 / nonzero(ld.x), 1.0 / nonzero(ld.y), 1.0 / nonzero(ld.z));
+  const NodeRec *nodes = g.nodes + lv.nodes_off;
+  const PrimRec *prims = g.prims + lv.prims_off;
+  do {
+    const unsigned id = stack[--sp];
+    const int nchild  = __ldg(&nodes[id].nchild);
+    if (nchild >= 0) {
+      const int off = __ldg(&nodes[id].offset);
+      for (int i = 0; i < nchild; ++i) {
+        const PrimRec &q = prims[off + i];
+        double tmin, tmax;
+        slab(q.mn, q.mx, lp, inv, tmin, tmax);
+        if (tmin <= tmax && tmax >= 0.0 && tmin < step) {
+          const int vol     = __ldg(&q.pv);
+          const double dist = pv_dist_in(g, vol, lp, ld);
+          if (dist < step && !(dist <= 0.0 && vol == last)) step = dist, hit = vol;
+        }
+      }
+    } else {
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      double tminL, tmaxL, tminR, tmaxR;
+      slab(nodes[L].mn, nodes[L].mx, lp, inv, tminL, tmaxL);
+      slab(nodes[R].mn, nodes[R].mx, lp, inv, tminR, tmaxR);
+      const bool trL = tminL <= tmaxL && tmaxL >= 0.0 && tminL < step;
+      const bool trR = tminR <= tmaxR && tmaxR >= 0.0 && tminR < step;
+      if (sp + 2 > kStackSize) {
+        raise_error(g, kErrStack);
+        return false;
+      }
+      if (tminR < tminL) {
+        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
+      } else {
+        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = R;
+      }
+    }
+  } while (sp > 0);
+  return true;
+}
+
+// BVH::ComputeSafety (BVH.h:172-209), FP64
+__device__ __forceinline__ double bvh_safety(const GeomView &g, const LVRec &lv, D3 lp, double safety)
+{
+  unsigned stack[kStackSize];
+  int sp   = 1;
+  stack[0] = 0;
+  const NodeRec *nodes = g.nodes + lv.nodes_off;
+  const PrimRec *prims = g.prims + lv.prims_off;
+  do {
+    const unsigned id = stack[--sp];
+    const int nchild  = __ldg(&nodes[id].nchild);
+    if (nchild >= 0) {
+      const int off = __ldg(&nodes[id].offset);
+      for (int i = 0; i < nchild; ++i) {
+        const PrimRec &q = prims[off + i];
+        if (box_safety(q.mn, q.mx, lp) < safety) {
+          const double dist = pv_safe_in(g, __ldg(&q.pv), lp);
+          if (dist < safety) safety = dist;
+        }
+      }
+    } else {
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      const double sL = box_safety(nodes[L].mn, nodes[L].mx, lp);
+      const double sR = box_safety(nodes[R].mn, nodes[R].mx, lp);
+      const bool trL = sL < safety, trR = sR < safety;
+      if (sp + 2 > kStackSize) {
+        raise_error(g, kErrStack);
+        return safety;
+      }
+      if (sR < sL) {
+        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
+      } else {
+        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = R;
+      }
+    }
+  } while (sp > 0);
+  return safety;
+}
+
+// BVH::LevelLocate(exclvol, localpoint, pvol, daughterlocalpoint) (BVH.h:255-285)
+__device__ __forceinline__ bool bvh_level_locate(const GeomView &g, const LVRec &lv, int excl, D3 lp, int &pvol,
+                                                 D3 &dlp)
+{
+  unsigned stack[kStackSize];
+  int sp   = 1;
+  stack[0] = 0;
+  const NodeRec *nodes = g.nodes + lv.nodes_off;
+  const PrimRec *prims = g.prims + lv.prims_off;
+  do {
+    const unsigned id = stack[--sp];
+    const int nchild  = __ldg(&nodes[id].nchild);
+    if (nchild >= 0) {
+      const int off = __ldg(&nodes[id].offset);
+      for (int i = 0; i < nchild; ++i) {
+        const PrimRec &q = prims[off + i];
+        if (box_contains_pt(q.mn, q.mx, lp)) {
+          const int vol = __ldg(&q.pv);
+          if (vol != excl && pv_contains(g, vol, lp, dlp)) {
+            pvol = vol;
+            return true;
+          }
+        }
+      }
+    } else {
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      if (sp + 2 > kStackSize) {
+        raise_error(g, kErrStack);
+        return false;
+      }
+      if (box_contains_pt(nodes[L].mn, nodes[L].mx, lp)) stack[sp++] = L;
+      if (box_contains_pt(nodes[R].mn, nodes[R].mx, lp)) stack[sp++] = R;
+    }
+  } while (sp > 0);
+  return false;
+}
+
+__device__ __forceinline__ LVRec load_lv(const GeomView &g, int lvi)
+{
+  LVRec r;
+  const int4 *src = reinterpret_cast<const int4 *>(g.lv + lvi);
+  int4 a = __ldg(src), b = __ldg(src + 1);
+  r.shape = a.x; r.shape_row = a.y; r.nd = a.z; r.daughters_off = a.w;
+  r.nodes_off = b.x; r.n_nodes = b.y; r.prims_off = b.z; r.depth = b.w;
+  return r;
+}
+
+__device__ __forceinline__ int pv_lv(const GeomView &g, int pv) { return __ldg(&g.pv[pv].lv); }
+
+// GlobalLocator::LocateGlobalPoint (GlobalLocator.h:35-82), BVHLevelLocator attached
+__device__ __forceinline__ int locate_global_point(const GeomView &g, int vol, D3 point, uint32_t &path, bool top)
+{
+  int cand = vol;
+  D3 cur   = point;
+  if (top) cand = pv_unplaced_contains(g, vol, point) ? vol : -1;
+  if (cand >= 0) {
+    path     = ni_push(g, path, cand);
+    LVRec lv = load_lv(g, pv_lv(g, cand));
+    bool godeeper = true;
+    int guard     = 0;
+    while (lv.nd > 0 && godeeper) {
+      if (++guard > kMaxLevels) {
+        raise_error(g, kErrRelocate);
+        break;
+      }
+      int pv;
+      D3 tp;
+      godeeper = bvh_level_locate(g, lv, -1, cur, pv, tp);
+      if (godeeper) {
+        path = ni_push(g, path, pv);
+        cand = pv;
+        lv   = load_lv(g, pv_lv(g, cand));
+        cur  = tp;
+      }
+    }
+  }
+  return cand >= 0 ? ni_top(g, path) : -1;
+}
+
+// GlobalLocator::LocateGlobalPointExclVolume (GlobalLocator.h:88-135)
+__device__ __forceinline__ void locate_global_point_excl(const GeomView &g, int vol, int excl, D3 point, uint32_t &path)
+{
+  int cand = vol;
+  D3 cur   = point;
+  path     = ni_push(g, path, cand);
+  LVRec lv = load_lv(g, pv_lv(g, cand));
+  bool godeeper = true;
+  int guard     = 0;
+  while (lv.nd > 0 && godeeper) {
+    if (++guard > kMaxLevels) {
+      raise_error(g, kErrRelocate);
+      break;
+    }
+    D3 tp;
+    godeeper = bvh_level_locate(g, lv, excl, cur, cand, tp);
+    if (godeeper) {
+      lv   = load_lv(g, pv_lv(g, cand));
+      cur  = tp;
+      path = ni_push(g, path, cand);
+    }
+  }
+}
+
+// GlobalLocator::RelocatePointFromPathForceDifferent (GlobalLocator.h:171-200)
+__device__ __forceinline__ void relocate_force_different(const GeomView &g, D3 lp, uint32_t &path)
+{
+  int cm = ni_top(g, path);
+  const int entry = cm;
+  if (cm < 0) return;
+  D3 tmp    = lp;
+  int guard = 0;
+  while (cm >= 0) {
+    if (++guard > kMaxLevels + 1) {
+      raise_error(g, kErrRelocate);
+      return;
+    }
+    if (cm == entry || !pv_unplaced_contains(g, cm, tmp)) {
+      path = ni_pop(g, path);
+      PvXf x;
+      load_pv_xf(g, cm, x);
+      tmp = xf_inverse(x.t, x.r, tmp);
+      cm  = ni_top(g, path);
+    } else
+      break;
+  }
+  if (cm >= 0) {
+    path = ni_pop(g, path);
+    locate_global_point_excl(g, cm, entry, tmp, path);
+  }
+}
+
+// VNavigatorHelper::Relocate (VNavigator.h:1070-1091)
+__device__ __forceinline__ void relocate(const GeomView &g, D3 pab, const State &in, State &out)
+{
+  if (ni_top(g, out.nav_ind) == ni_top(g, in.nav_ind)) {
+    relocate_force_different(g, pab, out.nav_ind);
+  } else {
+    const int nextvol = ni_top(g, out.nav_ind);
+    out.nav_ind       = ni_pop(g, out.nav_ind);
+    PvXf x;
+    load_pv_xf(g, nextvol, x);
+    locate_global_point(g, nextvol, xf_point(x.t, x.r, pab), out.nav_ind, false);
+  }
+}
+
+// BVHSafetyEstimator::ComputeSafetyForLocalPoint (BVHSafetyEstimator.h:38-46)
+__device__ __forceinline__ double safety_local(const GeomView &g, D3 lp, int pv)
+{
+  const LVRec lv = load_lv(g, pv_lv(g, pv));
+  double safety  = shape_safe_out(lv.shape, g.shape + lv.shape_row, lp);
+  if (safety > 0.0 && lv.nd > 0) safety = bvh_safety(g, lv, lp, safety);
+  return safety;
+}
+
+}  // namespace dev
+}  // namespace vgn

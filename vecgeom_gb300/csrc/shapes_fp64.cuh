@@ -1,0 +1,344 @@
+// shapes_fp64.cuh -- FP64 device kernels of the unplaced shapes.
+//
+// These must give bit-identical doubles to the reference's scalar CPU path,
+// so each keeps the reference kernel's operation order and is compiled with
+// -fmad=false (no contraction into FMA).  IEEE-rounded '/' and sqrt are the
+// CUDA defaults (-prec-div / -prec-sqrt).
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "geom_types.h"
+
+namespace vgn {
+namespace dev {
+
+constexpr double kTolerance     = 1e-9;
+constexpr double kHalfTolerance = 0.5 * kTolerance;
+constexpr double kInfLength     = DBL_MAX;
+constexpr double kEpsilon       = DBL_EPSILON;
+
+enum : int { kInsideE = 1, kSurfaceE = 2, kOutsideE = 3 };
+
+struct D3 {
+  double x, y, z;
+};
+
+__device__ __forceinline__ D3 d3(double x, double y, double z) { return D3{x, y, z}; }
+__device__ __forceinline__ double vmin(double a, double b) { return a < b ? a : b; }
+__device__ __forceinline__ double vmax(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double min3(double a, double b, double c) { return vmin(vmin(a, b), c); }
+__device__ __forceinline__ double max3(double a, double b, double c) { return vmax(vmax(a, b), c); }
+// Global.h:166-178
+__device__ __forceinline__ double nonzero_abs(double x) { return fabs(x) + 1.0e-30; }
+__device__ __forceinline__ double nonzero(double x) { return x + copysign(1.0e-30, x); }
+__device__ __forceinline__ double sgn(double x) { return copysign(1.0, x); }
+
+// ---------------------------------------------------------------- Box
+// kernel/BoxImplementation.h:73-167; row = fDimensions
+__device__ __forceinline__ bool box_contains(const double *h, D3 p)
+{
+  return max3(fabs(p.x) - h[0], fabs(p.y) - h[1], fabs(p.z) - h[2]) < 0.0;
+}
+
+__device__ __forceinline__ int box_inside(const double *h, D3 p)
+{
+  const double dist = max3(fabs(p.x) - h[0], fabs(p.y) - h[1], fabs(p.z) - h[2]);
+  int r             = dist < 0.0 ? kInsideE : kOutsideE;
+  if (fabs(dist) < kHalfTolerance) r = kSurfaceE;
+  return r;
+}
+
+__device__ __forceinline__ double box_dist_in(const double *h, D3 p, D3 d)
+{
+  const double ix = 1.0 / nonzero(d.x), iy = 1.0 / nonzero(d.y), iz = 1.0 / nonzero(d.z);
+  const double sx = sgn(d.x), sy = sgn(d.y), sz = sgn(d.z);
+  const double inx = -sx * h[0] - p.x, iny = -sy * h[1] - p.y, inz = -sz * h[2] - p.z;
+  const double ox = sx * h[0] - p.x, oy = sy * h[1] - p.y, oz = sz * h[2] - p.z;
+  const double absOrthogOut = fabs(min3(sx * ox, sy * oy, sz * oz));
+  const double distOut      = min3(ox * ix, oy * iy, oz * iz);
+  double distance           = max3(inx * ix, iny * iy, inz * iz);
+  if (distance >= distOut || distOut <= kHalfTolerance || absOrthogOut <= kHalfTolerance) distance = kInfLength;
+  return distance;
+}
+
+__device__ __forceinline__ double box_dist_out(const double *h, D3 p, D3 d)
+{
+  const double ix = 1.0 / nonzero(d.x), iy = 1.0 / nonzero(d.y), iz = 1.0 / nonzero(d.z);
+  const double sx = sgn(d.x), sy = sgn(d.y), sz = sgn(d.z);
+  const double safetyIn = max3(fabs(p.x) - h[0], fabs(p.y) - h[1], fabs(p.z) - h[2]);
+  double distance       = min3((sx * h[0] - p.x) * ix, (sy * h[1] - p.y) * iy, (sz * h[2] - p.z) * iz);
+  if (safetyIn > kHalfTolerance) distance = -1.0;
+  return distance;
+}
+
+__device__ __forceinline__ double box_safe_in(const double *h, D3 p)
+{
+  return max3(fabs(p.x) - h[0], fabs(p.y) - h[1], fabs(p.z) - h[2]);
+}
+
+__device__ __forceinline__ double box_safe_out(const double *h, D3 p)
+{
+  return min3(h[0] - fabs(p.x), h[1] - fabs(p.y), h[2] - fabs(p.z));
+}
+
+// ---------------------------------------------------------------- Tube (full phi)
+// kernel/TubeImplementation.h; row layout vgn::row::Tube*
+namespace tb = row;
+
+// CircleTrajectoryIntersection (TubeImplementation.h:103-160), no phi
+__device__ __forceinline__ void tube_circle(double b, double c, double fz, D3 pos, D3 dir, bool largest, bool insector,
+                                            double &dist, bool &ok)
+{
+  double delta = b * b - c;
+  ok           = delta > 0.;
+  if (largest) ok |= delta == 0.;
+  if (!ok) delta = 0.;
+  delta = sqrt(delta);
+  if (!largest) delta = -delta;
+  dist = -b + delta;
+  ok &= dist >= -2 * kTolerance;
+  if (!ok) return;
+  if (insector) {
+    const double hitz = pos.z + dist * dir.z;
+    ok &= (fabs(hitz) <= fz);
+  }
+}
+
+// DistanceToInKernel (TubeImplementation.h:504-681)
+__device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 d)
+{
+  const bool hasrmin = t[tb::TubeRmin] > 0;
+  bool done          = false;
+  double distance    = kInfLength;
+  double distz       = fabs(p.z) - t[tb::TubeZ];
+  done |= distz > kHalfTolerance && p.z * d.z >= 0;
+  const double rsq   = p.x * p.x + p.y * p.y;
+  const double rdotn = p.x * d.x + p.y * d.y;
+  done |= rsq > t[tb::TubeTolIrmax2] && rdotn >= 0;
+  if (done) return distance;
+
+  distance    = -1.0;
+  bool inside = distz < -kHalfTolerance;
+  inside &= rsq < t[tb::TubeTolIrmax2];
+  if (hasrmin) inside &= rsq > t[tb::TubeTolIrmin2];
+  done |= inside;
+  if (done) return distance;
+
+  distance = kInfLength;
+  distz /= nonzero_abs(d.z);
+  const double hitx = p.x + distz * d.x;
+  const double hity = p.y + distz * d.y;
+  const double r2   = hitx * hitx + hity * hity;
+  bool okz          = distz > -kHalfTolerance && (p.z * d.z < 0);
+  okz &= (r2 <= t[tb::TubeRmax2]);
+  if (hasrmin) okz &= (t[tb::TubeRmin2] <= r2);
+  if (!done && okz) distance = distz;
+  done |= okz;
+
+  const double rho = p.x * p.x + p.y * p.y;
+  bool onsurf = (rho >= t[tb::TubeTolIrmax2]) && (rho <= t[tb::TubeTolOrmax2]) &&
+                (fabs(p.z) < (t[tb::TubeZ] + kTolerance)) && (d.x * p.x + d.y * p.y + d.z * 0. <= 0.);
+  if (hasrmin)
+    onsurf |= (rho >= t[tb::TubeTolOrmin2]) && (rho <= t[tb::TubeTolIrmin2]) &&
+              (fabs(p.z) < (t[tb::TubeZ] + kTolerance)) && (d.x * -p.x + d.y * -p.y + d.z * 0. <= 0.);
+  if (!done && onsurf) distance = 0.;
+  done |= onsurf;
+  if (done) return distance;
+
+  const double invnsq = 1. / nonzero(1. - d.z * d.z);
+  const double b      = invnsq * rdotn;
+  const double crmax  = invnsq * (rsq - t[tb::TubeRmax2]);
+  double dist_rmax;
+  bool ok_rmax;
+  tube_circle(b, crmax, t[tb::TubeZ], p, d, false, true, dist_rmax, ok_rmax);
+  ok_rmax &= dist_rmax < distance;
+  if (!done && ok_rmax) distance = dist_rmax;
+  done |= ok_rmax;
+  if (done) return distance;
+  if (hasrmin) {
+    const double crmin = invnsq * (rsq - t[tb::TubeRmin2]);
+    double dist_rmin;
+    bool ok_rmin;
+    tube_circle(b, crmin, t[tb::TubeZ], p, d, true, true, dist_rmin, ok_rmin);
+    ok_rmin &= dist_rmin < distance;
+    if (!done && ok_rmin) distance = dist_rmin;
+  }
+  return distance;
+}
+
+// DistanceToIn with the far-point pre-move (TubeImplementation.h:475-502)
+__device__ __forceinline__ double tube_dist_in(const double *t, D3 pt, D3 d)
+{
+  D3 p                = pt;
+  const double ptDist = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+  double distToMove   = 0.;
+  const double order  = 100.;
+  if (ptDist > order * t[tb::TubeMaxVal]) {
+    distToMove = ptDist - order * t[tb::TubeMaxVal];
+    p          = d3(p.x + distToMove * d.x, p.y + distToMove * d.y, p.z + distToMove * d.z);
+  }
+  double distance = tube_dist_in_kernel(t, p, d);
+  distance += distToMove;
+  return distance;
+}
+
+// DistanceToOut (TubeImplementation.h:683-823)
+__device__ __forceinline__ double tube_dist_out(const double *t, D3 p, D3 d)
+{
+  const bool hasrmin = t[tb::TubeRmin] > 0;
+  const double fz    = t[tb::TubeZ];
+  double distz       = fz - fabs(p.z);
+  if (distz < -kHalfTolerance) return -1.;
+  const double rsq   = p.x * p.x + p.y * p.y;
+  const double rdotn = d.x * p.x + d.y * p.y;
+  double crmax       = rsq - t[tb::TubeRmax2];
+  double crmin       = rsq;
+  if (crmax > 2.0 * kTolerance * t[tb::TubeRmax]) return -1.;
+  if (hasrmin) {
+    crmin -= t[tb::TubeRmin2];
+    if (crmin < -2.0 * kTolerance * t[tb::TubeRmin]) return -1.;
+  }
+  double distance      = kInfLength;
+  const double invdirz = 1. / nonzero(d.z);
+  distz                = (fz - p.z) * invdirz;
+  if (d.z < 0) distz = (-fz - p.z) * invdirz;
+  if (d.z != 0. && distz < distance) distance = distz;
+  const double invnsq = 1. / nonzero(1. - d.z * d.z);
+  const double b      = invnsq * rdotn;
+  if (hasrmin) {
+    double dist_rmin;
+    bool ok_rmin;
+    crmin *= invnsq;
+    tube_circle(b, crmin, fz, p, d, false, false, dist_rmin, ok_rmin);
+    if (ok_rmin && dist_rmin < distance) distance = dist_rmin;
+  }
+  double dist_rmax;
+  bool ok_rmax;
+  crmax *= invnsq;
+  tube_circle(b, crmax, fz, p, d, true, false, dist_rmax, ok_rmax);
+  if (ok_rmax && dist_rmax < distance) distance = dist_rmax;
+  return distance;
+}
+
+// SafetyToInOld (TubeImplementation.h:912-938)
+__device__ __forceinline__ double tube_safe_in(const double *t, D3 p)
+{
+  double safety         = fabs(p.z) - t[tb::TubeZ];
+  const double r        = sqrt(p.x * p.x + p.y * p.y);
+  const double safermax = r - t[tb::TubeRmax];
+  if (safermax > safety) safety = safermax;
+  if (t[tb::TubeRmin] > 0) {
+    const double safermin = t[tb::TubeRmin] - r;
+    if (safermin > safety) safety = safermin;
+  }
+  return safety;
+}
+
+// SafetyToOutOld (TubeImplementation.h:940-960)
+__device__ __forceinline__ double tube_safe_out(const double *t, D3 p)
+{
+  double safety         = t[tb::TubeZ] - fabs(p.z);
+  const double r        = sqrt(p.x * p.x + p.y * p.y);
+  const double safermax = t[tb::TubeRmax] - r;
+  if (safermax < safety) safety = safermax;
+  if (t[tb::TubeRmin] > 0) {
+    const double safermin = r - t[tb::TubeRmin];
+    if (safermin < safety) safety = safermin;
+  }
+  return safety;
+}
+
+// GenericKernelForContainsAndInside (TubeImplementation.h:392-450)
+__device__ __forceinline__ void tube_generic_ci(const double *t, D3 p, bool forinside, bool &cin, bool &cout)
+{
+  const double fz = t[tb::TubeZ], rmax = t[tb::TubeRmax], rmin = t[tb::TubeRmin];
+  const double absz = fabs(p.z);
+  cout = absz > (forinside ? fz + kHalfTolerance : fz);
+  if (forinside) cin = absz < fz - kHalfTolerance;
+  if (cout) return;
+  const double r2 = p.x * p.x + p.y * p.y;
+  cout |= r2 > (forinside ? rmax * (rmax + 2.0 * kTolerance) : rmax * rmax);
+  if (forinside) cin &= r2 < fabs(rmax * (rmax - 2.0 * kTolerance));
+  if (cout) return;
+  if (rmin > 0) {
+    cout |= r2 <= (forinside ? fabs(rmin * (rmin - 2.0 * kTolerance)) : rmin * rmin);
+    if (forinside) cin &= r2 > rmin * (rmin + 2.0 * kTolerance);
+  }
+}
+
+__device__ __forceinline__ bool tube_contains(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  tube_generic_ci(t, p, false, cin, cout);
+  return !cout;
+}
+
+__device__ __forceinline__ int tube_inside(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  tube_generic_ci(t, p, true, cin, cout);
+  int r = kSurfaceE;
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+// ---------------------------------------------------------------- dispatch
+__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
+{
+  switch (type) {
+  case kBox: return box_dist_in(r, p, d);
+  case kTube: return tube_dist_in(r, p, d);
+  }
+  return kInfLength;
+}
+
+__device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p, D3 d)
+{
+  switch (type) {
+  case kBox: return box_dist_out(r, p, d);
+  case kTube: return tube_dist_out(r, p, d);
+  }
+  return -1.;
+}
+
+__device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
+{
+  switch (type) {
+  case kBox: return box_safe_in(r, p);
+  case kTube: return tube_safe_in(r, p);
+  }
+  return kInfLength;
+}
+
+__device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p)
+{
+  switch (type) {
+  case kBox: return box_safe_out(r, p);
+  case kTube: return tube_safe_out(r, p);
+  }
+  return 0.;
+}
+
+__device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
+{
+  switch (type) {
+  case kBox: return box_contains(r, p);
+  case kTube: return tube_contains(r, p);
+  }
+  return false;
+}
+
+__device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
+{
+  switch (type) {
+  case kBox: return box_inside(r, p);
+  case kTube: return tube_inside(r, p);
+  }
+  return kOutsideE;
+}
+
+}  // namespace dev
+}  // namespace vgn

@@ -1,0 +1,467 @@
+// vgnav_api.cpp -- implementation of the C ABI declared in include/vgnav.h.
+//
+// Owns the device copy of a closed geometry (one flat upload per table,
+// instead of the reference's per-object deep copy), validates arguments,
+// stages host buffers through a device workspace when the caller passes host
+// memory, and maps device-side error bits to status codes.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/vgnav.h"
+#include "host_geometry.h"
+#include "launch.h"
+
+struct vgn_geometry {
+  int device = 0;
+  int num_sms = 0;
+  vgn::HostGeometry host;
+  std::vector<void *> allocations;
+  size_t device_bytes = 0;
+  uint32_t *d_status  = nullptr;
+  vgn::GeomView view{};
+  // staging workspace for calls made with host pointers
+  std::mutex ws_mutex;
+  void *d_ws      = nullptr;
+  size_t ws_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+  return fail(VGN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+class DeviceGuard {
+public:
+  explicit DeviceGuard(int dev)
+  {
+    if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+    if (prev_ != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard()
+  {
+    if (prev_ >= 0) cudaSetDevice(prev_);
+  }
+
+private:
+  int prev_ = -1;
+};
+
+template <typename T>
+int upload(vgn_geometry *g, const std::vector<T> &v, const T **dst)
+{
+  if (v.empty()) {
+    *dst = nullptr;
+    return VGN_OK;
+  }
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, v.size() * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(geometry table)");
+  g->allocations.push_back(p);
+  g->device_bytes += v.size() * sizeof(T);
+  e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(geometry table)");
+  *dst = static_cast<const T *>(p);
+  return VGN_OK;
+}
+
+// true when every non-null pointer is device-accessible, false when all are host
+// memory; -1 on a mix.
+int classify(std::initializer_list<const void *> ptrs)
+{
+  int kind = -2;
+  for (const void *p : ptrs) {
+    if (!p) continue;
+    cudaPointerAttributes attr;
+    int k = 0;
+    if (cudaPointerGetAttributes(&attr, p) == cudaSuccess)
+      k = (attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged) ? 1 : 0;
+    else
+      cudaGetLastError();
+    if (kind == -2)
+      kind = k;
+    else if (kind != k)
+      return -1;
+  }
+  return kind < 0 ? 0 : kind;
+}
+
+int check_status(const vgn_geometry *g, cudaStream_t s)
+{
+  uint32_t st = 0;
+  cudaError_t e = cudaMemcpyAsync(&st, g->d_status, sizeof(st), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "status readback");
+  if (st) {
+    cudaMemsetAsync(g->d_status, 0, sizeof(uint32_t), s);
+    cudaStreamSynchronize(s);
+    if (st & vgn::kErrStack) return fail(VGN_ERR_STACK, "BVH traversal stack overflow on the device");
+    if (st & vgn::kErrRelocate) return fail(VGN_ERR_RELOCATE, "relocation exceeded the geometry depth bound");
+    if (st & vgn::kErrState) return fail(VGN_ERR_STATE, "input navigation state outside the navigation table");
+  }
+  return VGN_OK;
+}
+
+void *workspace(vgn_geometry *g, size_t bytes)
+{
+  if (bytes <= g->ws_bytes) return g->d_ws;
+  if (g->d_ws) cudaFree(g->d_ws);
+  g->d_ws     = nullptr;
+  g->ws_bytes = 0;
+  if (cudaMalloc(&g->d_ws, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    g->d_ws = nullptr;
+    return nullptr;
+  }
+  g->ws_bytes = bytes;
+  return g->d_ws;
+}
+
+int max_blocks(const vgn_geometry *g) { return g->num_sms > 0 ? g->num_sms * 32 : 4096; }
+
+// bump allocator over the staging workspace (256-byte aligned sub-buffers)
+struct Carve {
+  char *base;
+  size_t off = 0;
+  template <typename T>
+  T *take(size_t count)
+  {
+    T *p = reinterpret_cast<T *>(base + off);
+    off += (count * sizeof(T) + 255) & ~size_t(255);
+    return p;
+  }
+};
+
+size_t carve_bytes(std::initializer_list<size_t> sizes)
+{
+  size_t b = 0;
+  for (size_t s : sizes) b += (s + 255) & ~size_t(255);
+  return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *vgn_last_error(void) { return g_last_error.c_str(); }
+
+const char *vgn_version(void) { return "vgnav-gb300 0.1 (sm_103a)"; }
+
+int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry **out)
+{
+  if (!desc || !out) return fail(VGN_ERR_ARG, "null argument");
+  *out = nullptr;
+  vgn_geometry *g = new (std::nothrow) vgn_geometry();
+  if (!g) return fail(VGN_ERR_NOMEM, "host allocation failed");
+  std::string err;
+  int rc = vgn::build_host_geometry(*desc, g->host, err);
+  if (rc) {
+    delete g;
+    return fail(rc, err);
+  }
+  g->device = device;
+  if (device == VGN_HOST_ONLY) {  // closed on the host, nothing uploaded
+    *out = g;
+    return VGN_OK;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess) {
+    delete g;
+    return cuda_fail(e, "cudaGetDeviceCount");
+  }
+  if (device < 0 || device >= ndev) {
+    delete g;
+    return fail(VGN_ERR_ARG, "device index out of range");
+  }
+  DeviceGuard guard(device);
+  cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+  vgn::GeomView &v = g->view;
+  const vgn::HostGeometry &h = g->host;
+  if ((rc = upload(g, h.navind, &v.navind)) || (rc = upload(g, h.node_start, &v.node_start)) || (rc = upload(g, h.pv_rec, &v.pv)) || (rc = upload(g, h.lv_rec, &v.lv)) ||
+      (rc = upload(g, h.daughters, &v.daughters)) || (rc = upload(g, h.nodes, &v.nodes)) ||
+      (rc = upload(g, h.prims, &v.prims)) || (rc = upload(g, h.fnodes, &v.fnodes)) ||
+      (rc = upload(g, h.fprims, &v.fprims)) || (rc = upload(g, h.shape, &v.shape))) {
+    vgn_geometry_free(g);
+    return rc;
+  }
+  e = cudaMalloc(&g->d_status, sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    vgn_geometry_free(g);
+    return cuda_fail(e, "cudaMalloc(status)");
+  }
+  cudaMemset(g->d_status, 0, sizeof(uint32_t));
+  v.status       = g->d_status;
+  v.navind_words = (uint32_t)h.navind.size();
+  v.n_pv         = (int32_t)h.pv.size();
+  v.n_lv         = (int32_t)h.lv.size();
+  v.world_pv     = h.world_pv;
+  v.max_depth    = h.max_depth;
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    vgn_geometry_free(g);
+    return cuda_fail(e, "geometry upload");
+  }
+  *out = g;
+  return VGN_OK;
+}
+
+int vgn_geometry_free(vgn_geometry *g)
+{
+  if (!g) return VGN_OK;
+  if (g->device != VGN_HOST_ONLY) {
+    DeviceGuard guard(g->device);
+    for (void *p : g->allocations) cudaFree(p);
+    if (g->d_status) cudaFree(g->d_status);
+    if (g->d_ws) cudaFree(g->d_ws);
+  }
+  delete g;
+  return VGN_OK;
+}
+
+int vgn_geometry_navindex(const vgn_geometry *g, const uint32_t **table, size_t *n_words)
+{
+  if (!g || !table || !n_words) return fail(VGN_ERR_ARG, "null argument");
+  *table   = g->host.navind.data();
+  *n_words = g->host.navind.size();
+  return VGN_OK;
+}
+
+int vgn_geometry_bvh_info(const vgn_geometry *g, int32_t lv, int32_t *depth, int32_t *n_nodes, int32_t *n_prims)
+{
+  if (!g || lv < 0 || lv >= (int32_t)g->host.lv.size()) return fail(VGN_ERR_ARG, "bad logical volume");
+  const vgn::HostLV &l = g->host.lv[lv];
+  if (l.daughters.empty()) return fail(VGN_ERR_ARG, "logical volume has no daughters");
+  if (depth) *depth = l.bvh.depth;
+  if (n_nodes) *n_nodes = (int32_t)l.bvh.nodes.size();
+  if (n_prims) *n_prims = (int32_t)l.daughters.size();
+  return VGN_OK;
+}
+
+int vgn_geometry_bvh_arrays(const vgn_geometry *g, int32_t lv, int32_t *prim_id, int32_t *offset, int32_t *nchild,
+                            double *nodes_minmax, double *prims_minmax)
+{
+  if (!g || lv < 0 || lv >= (int32_t)g->host.lv.size()) return fail(VGN_ERR_ARG, "bad logical volume");
+  const vgn::HostLV &l = g->host.lv[lv];
+  if (l.daughters.empty()) return fail(VGN_ERR_ARG, "logical volume has no daughters");
+  if (prim_id) std::memcpy(prim_id, l.bvh.prim_id.data(), l.bvh.prim_id.size() * sizeof(int32_t));
+  if (offset) std::memcpy(offset, l.bvh.offset.data(), l.bvh.offset.size() * sizeof(int32_t));
+  if (nchild) std::memcpy(nchild, l.bvh.nchild.data(), l.bvh.nchild.size() * sizeof(int32_t));
+  if (nodes_minmax)
+    for (size_t i = 0; i < l.bvh.nodes.size(); ++i) std::memcpy(nodes_minmax + 6 * i, &l.bvh.nodes[i], 6 * sizeof(double));
+  if (prims_minmax)
+    for (size_t i = 0; i < l.aabbs.size(); ++i) std::memcpy(prims_minmax + 6 * i, &l.aabbs[i], 6 * sizeof(double));
+  return VGN_OK;
+}
+
+int vgn_geometry_device_bytes(const vgn_geometry *g, size_t *bytes)
+{
+  if (!g || !bytes) return fail(VGN_ERR_ARG, "null argument");
+  *bytes = g->device_bytes;
+  return VGN_OK;
+}
+
+int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, const double *py, const double *pz,
+                           const double *dx, const double *dy, const double *dz, const double *step_limit,
+                           const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream)
+{
+  vgn_geometry *g = const_cast<vgn_geometry *>(gc);
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
+  if (n == 0) return VGN_OK;
+  if (!px || !py || !pz || !dx || !dy || !dz || !step_limit || !in || !out || !step)
+    return fail(VGN_ERR_ARG, "null array argument");
+  if ((flags & VGN_PRECISION_MIXED) != 0) return fail(VGN_ERR_UNSUPPORTED, "mixed precision kernels not built yet");
+  DeviceGuard guard(g->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int kind = classify({px, py, pz, dx, dy, dz, step_limit, in, out, step, safety});
+  if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
+  vgn::StepArgs a{};
+  a.n          = n;
+  a.reloc      = (flags & VGN_NO_RELOCATE) ? 0 : 1;
+  a.max_blocks = max_blocks(g);
+  if (kind == 1) {
+    a.px = px; a.py = py; a.pz = pz; a.dx = dx; a.dy = dy; a.dz = dz; a.slimit = step_limit;
+    a.in = in; a.out = out; a.step = step; a.safety = safety;
+    cudaError_t e = vgn::launch_step_fp64(g->view, a, s);
+    return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
+  }
+  // host buffers: stage through the device workspace
+  std::lock_guard<std::mutex> lock(g->ws_mutex);
+  const size_t nd = (size_t)n * sizeof(double), ns = (size_t)n * sizeof(vgn_state);
+  const size_t bytes = carve_bytes({nd, nd, nd, nd, nd, nd, nd, ns, ns, nd, nd});
+  void *ws = workspace(g, bytes);
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  Carve c{static_cast<char *>(ws)};
+  double *b[7];
+  for (int k = 0; k < 7; ++k) b[k] = c.take<double>(n);
+  vgn_state *din = c.take<vgn_state>(n), *dout = c.take<vgn_state>(n);
+  double *dstep = c.take<double>(n), *dsaf = c.take<double>(n);
+  const double *src[7] = {px, py, pz, dx, dy, dz, step_limit};
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  a.px = b[0]; a.py = b[1]; a.pz = b[2]; a.dx = b[3]; a.dy = b[4]; a.dz = b[5]; a.slimit = b[6];
+  a.in = din; a.out = dout; a.step = dstep; a.safety = safety ? dsaf : nullptr;
+  e = vgn::launch_step_fp64(g->view, a, s);
+  if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+  e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(step, dstep, nd, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && safety) e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
+int vgn_step_and_next_volume(const vgn_geometry *g, int64_t n, const double *px, const double *py, const double *pz,
+                             const double *dx, const double *dy, const double *dz, const double *step_limit,
+                             const vgn_state *in, vgn_state *out, double *step, double *safety, int flags,
+                             void *stream)
+{
+  return vgn_compute_step_batch(g, n, px, py, pz, dx, dy, dz, step_limit, in, out, step, safety, flags, stream);
+}
+
+int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px, const double *py, const double *pz,
+                             const vgn_state *in, double *safety, int flags, void *stream)
+{
+  vgn_geometry *g = const_cast<vgn_geometry *>(gc);
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
+  if (n == 0) return VGN_OK;
+  if (!px || !py || !pz || !in || !safety) return fail(VGN_ERR_ARG, "null array argument");
+  if ((flags & VGN_PRECISION_MIXED) != 0) return fail(VGN_ERR_UNSUPPORTED, "mixed precision kernels not built yet");
+  DeviceGuard guard(g->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int kind = classify({px, py, pz, in, safety});
+  if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
+  if (kind == 1) {
+    cudaError_t e = vgn::launch_safety_fp64(g->view, n, px, py, pz, in, safety, max_blocks(g), s);
+    return e == cudaSuccess ? VGN_OK : cuda_fail(e, "safety kernel launch");
+  }
+  std::lock_guard<std::mutex> lock(g->ws_mutex);
+  const size_t nd = (size_t)n * sizeof(double), ns = (size_t)n * sizeof(vgn_state);
+  void *ws = workspace(g, carve_bytes({nd, nd, nd, ns, nd}));
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  Carve c{static_cast<char *>(ws)};
+  double *bx = c.take<double>(n), *by = c.take<double>(n), *bz = c.take<double>(n);
+  vgn_state *din = c.take<vgn_state>(n);
+  double *dsaf   = c.take<double>(n);
+  cudaError_t e  = cudaMemcpyAsync(bx, px, nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(by, py, nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  e = vgn::launch_safety_fp64(g->view, n, bx, by, bz, din, dsaf, max_blocks(g), s);
+  if (e != cudaSuccess) return cuda_fail(e, "safety kernel launch");
+  e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
+int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const double *py, const double *pz,
+                     vgn_state *out, int flags, void *stream)
+{
+  (void)flags;
+  vgn_geometry *g = const_cast<vgn_geometry *>(gc);
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
+  if (n == 0) return VGN_OK;
+  if (!px || !py || !pz || !out) return fail(VGN_ERR_ARG, "null array argument");
+  DeviceGuard guard(g->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int kind = classify({px, py, pz, out});
+  if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
+  if (kind == 1) {
+    cudaError_t e = vgn::launch_locate_fp64(g->view, n, px, py, pz, out, max_blocks(g), s);
+    return e == cudaSuccess ? VGN_OK : cuda_fail(e, "locate kernel launch");
+  }
+  std::lock_guard<std::mutex> lock(g->ws_mutex);
+  const size_t nd = (size_t)n * sizeof(double), ns = (size_t)n * sizeof(vgn_state);
+  void *ws = workspace(g, carve_bytes({nd, nd, nd, ns}));
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  Carve c{static_cast<char *>(ws)};
+  double *bx = c.take<double>(n), *by = c.take<double>(n), *bz = c.take<double>(n);
+  vgn_state *dout = c.take<vgn_state>(n);
+  cudaError_t e   = cudaMemcpyAsync(bx, px, nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(by, py, nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  e = vgn::launch_locate_fp64(g->view, n, bx, by, bz, dout, max_blocks(g), s);
+  if (e != cudaSuccess) return cuda_fail(e, "locate kernel launch");
+  e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
+int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, const double *px, const double *py,
+                    const double *pz, const double *dx, const double *dy, const double *dz, const double *step_max,
+                    double *out, int flags, void *stream)
+{
+  (void)step_max;
+  vgn_geometry *g = const_cast<vgn_geometry *>(gc);
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (lv < 0 || lv >= (int32_t)g->host.lv.size()) return fail(VGN_ERR_ARG, "bad logical volume");
+  if (op < VGN_OP_DISTANCE_TO_IN || op > VGN_OP_INSIDE) return fail(VGN_ERR_ARG, "bad shape operation");
+  if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
+  if (n == 0) return VGN_OK;
+  const bool needdir = op <= VGN_OP_DISTANCE_TO_OUT;
+  if (!px || !py || !pz || !out || (needdir && (!dx || !dy || !dz))) return fail(VGN_ERR_ARG, "null array argument");
+  if ((flags & VGN_PRECISION_MIXED) != 0) return fail(VGN_ERR_UNSUPPORTED, "shape queries are FP64 only");
+  DeviceGuard guard(g->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int type   = g->host.lv[lv].shape;
+  const double *row = g->view.shape + g->host.lv[lv].shape_row;
+  const int kind = needdir ? classify({px, py, pz, dx, dy, dz, out}) : classify({px, py, pz, out});
+  if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
+  if (kind == 1) {
+    cudaError_t e = vgn::launch_shape_fp64(op, type, row, n, px, py, pz, dx, dy, dz, out, max_blocks(g), s);
+    return e == cudaSuccess ? VGN_OK : cuda_fail(e, "shape kernel launch");
+  }
+  std::lock_guard<std::mutex> lock(g->ws_mutex);
+  const size_t nd = (size_t)n * sizeof(double);
+  void *ws = workspace(g, carve_bytes({nd, nd, nd, nd, nd, nd, nd}));
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  Carve c{static_cast<char *>(ws)};
+  double *b[6];
+  for (int k = 0; k < 6; ++k) b[k] = c.take<double>(n);
+  double *dout = c.take<double>(n);
+  const double *src[6] = {px, py, pz, dx, dy, dz};
+  const int ncopy      = needdir ? 6 : 3;
+  cudaError_t e        = cudaSuccess;
+  for (int k = 0; k < ncopy && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  e = vgn::launch_shape_fp64(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5], dout, max_blocks(g), s);
+  if (e != cudaSuccess) return cuda_fail(e, "shape kernel launch");
+  e = cudaMemcpyAsync(out, dout, nd, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
+int vgn_synchronize(const vgn_geometry *g, void *stream)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  DeviceGuard guard(g->device);
+  return check_status(g, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

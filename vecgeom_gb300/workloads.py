@@ -1,0 +1,307 @@
+"""Geometry descriptions and seeded synthetic track workloads.
+
+A geometry is described the way VecGeom users build one: logical volumes
+(an unplaced shape each) and placements (logical volume, mother, transform),
+with placed-volume ids in creation order.  ``GeometryBuilder`` produces the
+flat arrays of ``vgn_geometry_desc``.
+
+Workloads (sizes as named):
+  * ``tube_points``   single Tube(rmin=10, rmax=50, dz=100, full phi),
+                      points uniform inside it, isotropic directions.
+  * ``box_grid``      world box of half-length 1000 mm holding 4096 boxes with
+                      half-lengths U[5,30] mm on a jittered 16^3 grid of pitch
+                      125 mm (jitter +-10 mm), each rotated about z by U[0,360)
+                      degrees; tracks uniform in the world outside all boxes,
+                      isotropic directions, step limit 1000 mm.
+All draws use numpy's PCG64 generators with fixed seeds.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE = range(7)
+SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone"]
+
+K_PI = 3.14159265358979323846
+K_TWO_PI = 2.0 * K_PI
+K_DEG_TO_RAD = K_PI / 180.0
+
+STATE_DTYPE = np.dtype([("nav_ind", "<u4"), ("last_exited", "<u4"), ("on_boundary", "u1"), ("pad", "u1", (3,))])
+assert STATE_DTYPE.itemsize == 12
+
+
+def transform_euler(tx: float, ty: float, tz: float, phi: float = 0.0, theta: float = 0.0, psi: float = 0.0):
+    """12 doubles of Transformation3D(tx,ty,tz,phi,theta,psi) (angles in degrees),
+    rotation from Transformation3D::SetRotation (source/Transformation3D.cpp:129-148)."""
+    sinphi, cosphi = math.sin(K_DEG_TO_RAD * phi), math.cos(K_DEG_TO_RAD * phi)
+    sinthe, costhe = math.sin(K_DEG_TO_RAD * theta), math.cos(K_DEG_TO_RAD * theta)
+    sinpsi, cospsi = math.sin(K_DEG_TO_RAD * psi), math.cos(K_DEG_TO_RAD * psi)
+    r = [
+        cospsi * cosphi - costhe * sinphi * sinpsi,
+        -sinpsi * cosphi - costhe * sinphi * cospsi,
+        sinthe * sinphi,
+        cospsi * sinphi + costhe * cosphi * sinpsi,
+        -sinpsi * sinphi + costhe * cosphi * cospsi,
+        -sinthe * cosphi,
+        sinpsi * sinthe,
+        cospsi * sinthe,
+        costhe,
+    ]
+    return [float(tx), float(ty), float(tz)] + r
+
+
+def transform_matrix(t, rot):
+    """12 doubles of Transformation3D(tx,ty,tz,r0..r8) from a translation and a row-major 3x3 matrix."""
+    return [float(v) for v in t] + [float(v) for v in np.asarray(rot, dtype=np.float64).reshape(9)]
+
+
+IDENTITY = transform_euler(0.0, 0.0, 0.0)
+IDENTITY[3:] = [1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0]
+
+
+@dataclass
+class GeometryDescription:
+    lv_shape: np.ndarray
+    lv_param_offset: np.ndarray
+    params: np.ndarray
+    pv_logical: np.ndarray
+    pv_mother: np.ndarray
+    pv_transform: np.ndarray  # (n_placed, 12)
+    world_placed: int
+    labels: list = field(default_factory=list)
+
+    @property
+    def n_logical(self) -> int:
+        return int(self.lv_shape.shape[0])
+
+    @property
+    def n_placed(self) -> int:
+        return int(self.pv_logical.shape[0])
+
+    def daughters_of(self, lv: int) -> np.ndarray:
+        return np.nonzero(self.pv_mother == lv)[0]
+
+
+class GeometryBuilder:
+    """Collects logical volumes and placements (VecGeom's LogicalVolume::PlaceDaughter order)."""
+
+    def __init__(self):
+        self._shapes: list[int] = []
+        self._offsets: list[int] = []
+        self._params: list[float] = []
+        self._pv_lv: list[int] = []
+        self._pv_mother: list[int] = []
+        self._pv_tr: list[list[float]] = []
+        self._world = -1
+
+    def logical(self, shape: int, params) -> int:
+        self._shapes.append(int(shape))
+        self._offsets.append(len(self._params))
+        self._params.extend(float(p) for p in params)
+        return len(self._shapes) - 1
+
+    def place(self, lv: int, mother: int, transform=None) -> int:
+        self._pv_lv.append(int(lv))
+        self._pv_mother.append(int(mother))
+        self._pv_tr.append(list(transform) if transform is not None else list(IDENTITY))
+        return len(self._pv_lv) - 1
+
+    def place_world(self, lv: int) -> int:
+        self._world = self.place(lv, -1, IDENTITY)
+        return self._world
+
+    def build(self) -> GeometryDescription:
+        if self._world < 0:
+            raise ValueError("no world placement")
+        return GeometryDescription(
+            lv_shape=np.asarray(self._shapes, dtype=np.int32),
+            lv_param_offset=np.asarray(self._offsets, dtype=np.int32),
+            params=np.asarray(self._params, dtype=np.float64),
+            pv_logical=np.asarray(self._pv_lv, dtype=np.int32),
+            pv_mother=np.asarray(self._pv_mother, dtype=np.int32),
+            pv_transform=np.asarray(self._pv_tr, dtype=np.float64).reshape(-1, 12),
+            world_placed=self._world,
+        )
+
+
+def isotropic(rng: np.random.Generator, n: int):
+    """Isotropic unit directions: z = U[-1,1], phi = U[0,2pi)."""
+    z = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    s = np.sqrt(1.0 - z * z)
+    return s * np.cos(phi), s * np.sin(phi), z
+
+
+def world_states(n: int) -> np.ndarray:
+    """States located in the world volume (navigation index 1)."""
+    st = np.zeros(n, dtype=STATE_DTYPE)
+    st["nav_ind"] = 1
+    return st
+
+
+@dataclass
+class TrackBatch:
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    dx: np.ndarray
+    dy: np.ndarray
+    dz: np.ndarray
+    step_limit: np.ndarray
+    states: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.x.shape[0])
+
+    def head(self, m: int) -> "TrackBatch":
+        return TrackBatch(*(a[:m].copy() for a in (self.x, self.y, self.z, self.dx, self.dy, self.dz,
+                                                    self.step_limit, self.states)))
+
+
+# ---------------------------------------------------------------- tube points
+TUBE_PARAMS = (10.0, 50.0, 100.0, 0.0, K_TWO_PI)
+
+
+def tube_geometry() -> GeometryDescription:
+    b = GeometryBuilder()
+    lv = b.logical(TUBE, TUBE_PARAMS)
+    b.place_world(lv)
+    return b.build()
+
+
+def tube_points(n: int = 1 << 20, seed_points: int = 1, seed_dirs: int = 2) -> TrackBatch:
+    """Points uniform inside Tube(10, 50, 100, full phi) by rejection in its bounding box."""
+    rmin, rmax, dz = TUBE_PARAMS[:3]
+    rng = np.random.Generator(np.random.PCG64(seed_points))
+    xs, ys, zs, have = [], [], [], 0
+    while have < n:
+        m = int((n - have) * 1.4) + 1024
+        x = rng.uniform(-rmax, rmax, m)
+        y = rng.uniform(-rmax, rmax, m)
+        z = rng.uniform(-dz, dz, m)
+        r2 = x * x + y * y
+        ok = (r2 > rmin * rmin) & (r2 < rmax * rmax)
+        xs.append(x[ok]); ys.append(y[ok]); zs.append(z[ok])
+        have += int(ok.sum())
+    x = np.concatenate(xs)[:n]; y = np.concatenate(ys)[:n]; z = np.concatenate(zs)[:n]
+    dx, dy, dzz = isotropic(np.random.Generator(np.random.PCG64(seed_dirs)), n)
+    return TrackBatch(x, y, z, dx, dy, dzz, np.full(n, 1e300), world_states(n))
+
+
+# ---------------------------------------------------------------- box grid
+BOXGRID_WORLD = 1000.0
+BOXGRID_N = 16
+BOXGRID_PITCH = 125.0
+
+
+@dataclass
+class BoxGrid:
+    desc: GeometryDescription
+    half: np.ndarray     # (4096, 3) half-lengths
+    centre: np.ndarray   # (4096, 3)
+    rot: np.ndarray      # (4096, 9) row-major rotation entries
+
+
+def box_grid_geometry(seed: int = 3, n: int = BOXGRID_N, pitch: float = BOXGRID_PITCH,
+                      world: float = BOXGRID_WORLD) -> BoxGrid:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    count = n * n * n
+    half = rng.uniform(5.0, 30.0, (count, 3))
+    jitter = rng.uniform(-10.0, 10.0, (count, 3))
+    phi = rng.uniform(0.0, 360.0, count)
+    idx = np.array([(i, j, k) for i in range(n) for j in range(n) for k in range(n)], dtype=np.float64)
+    centre = -world + 0.5 * pitch + pitch * idx + jitter
+    b = GeometryBuilder()
+    world_lv = b.logical(BOX, (world, world, world))
+    rot = np.zeros((count, 9))
+    for k in range(count):
+        lv = b.logical(BOX, half[k])
+        tr = transform_euler(centre[k, 0], centre[k, 1], centre[k, 2], phi[k], 0.0, 0.0)
+        rot[k] = tr[3:]
+        b.place(lv, world_lv, tr)
+    b.place_world(world_lv)
+    # non-overlap: the rotated box's AABB stays inside its own grid cell
+    ext_xy = np.abs(rot[:, 0:1]) * half[:, 0:1] + np.abs(rot[:, 1:2]) * half[:, 1:2]
+    ext_yx = np.abs(rot[:, 3:4]) * half[:, 0:1] + np.abs(rot[:, 4:5]) * half[:, 1:2]
+    reach = np.maximum(np.maximum(ext_xy, ext_yx)[:, 0], half[:, 2]) + 10.0
+    if not np.all(reach < 0.5 * pitch):
+        raise RuntimeError("box grid daughters would overlap")
+    return BoxGrid(b.build(), half, centre, rot)
+
+
+def _local(points: np.ndarray, centre: np.ndarray, rot: np.ndarray) -> np.ndarray:
+    """Transform<kGeneric,kGeneric>: l_i = sum_j (p_j - t_j) * R[3j+i]."""
+    t = points - centre
+    r = rot.reshape(-1, 3, 3)
+    return np.einsum("nj,nji->ni", t, r)
+
+
+def box_grid_tracks(grid: BoxGrid, n: int = 1 << 22, seed_points: int = 4, seed_dirs: int = 5,
+                    step_limit: float = 1000.0, margin: float = 1e-6) -> TrackBatch:
+    """Tracks uniform in the world, rejected when inside (or within `margin` of) a daughter box."""
+    rng = np.random.Generator(np.random.PCG64(seed_points))
+    w = BOXGRID_WORLD
+    out, have = [], 0
+    while have < n:
+        m = int((n - have) * 1.05) + 4096
+        p = rng.uniform(-w, w, (m, 3))
+        cell = np.clip(np.floor((p + w) / BOXGRID_PITCH).astype(np.int64), 0, BOXGRID_N - 1)
+        k = cell[:, 0] * BOXGRID_N * BOXGRID_N + cell[:, 1] * BOXGRID_N + cell[:, 2]
+        loc = _local(p, grid.centre[k], grid.rot[k])
+        inside = np.max(np.abs(loc) - grid.half[k], axis=1) < margin
+        p = p[~inside]
+        out.append(p)
+        have += p.shape[0]
+    p = np.concatenate(out)[:n]
+    dx, dy, dz = isotropic(np.random.Generator(np.random.PCG64(seed_dirs)), n)
+    return TrackBatch(p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), dx, dy, dz,
+                      np.full(n, step_limit), world_states(n))
+
+
+# ---------------------------------------------------------------- nested (multi-level)
+def nested_geometry(seed: int = 11) -> GeometryDescription:
+    """Three-level geometry for relocation tests: a world box (half 500 mm)
+    holding 27 rotated mother boxes (half 100 mm, 3x3x3 grid, pitch 300 mm),
+    each holding 8 rotated daughters alternating Box and Tube, every daughter
+    box holding one small box; placements follow VecGeom's usual bottom-up
+    construction (inner volumes placed first)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = GeometryBuilder()
+    world = b.logical(BOX, (500.0, 500.0, 500.0))
+    mothers = []
+    for i in range(27):
+        mothers.append(b.logical(BOX, (100.0, 100.0, 100.0)))
+    for m in mothers:
+        for k in range(8):
+            ix, iy, iz = (k >> 2) & 1, (k >> 1) & 1, k & 1
+            c = np.array([-50.0 + 100.0 * ix, -50.0 + 100.0 * iy, -50.0 + 100.0 * iz]) + rng.uniform(-5, 5, 3)
+            if k % 2 == 0:
+                h = rng.uniform(15.0, 25.0, 3)
+                lv = b.logical(BOX, h)
+                inner = b.logical(BOX, h * 0.4)
+                b.place(inner, lv, transform_euler(*(rng.uniform(-2, 2, 3)), rng.uniform(0, 360), 0.0, 0.0))
+            else:
+                rmin = rng.uniform(3.0, 8.0)
+                lv = b.logical(TUBE, (rmin, rng.uniform(18.0, 25.0), rng.uniform(15.0, 25.0), 0.0, K_TWO_PI))
+            b.place(lv, m, transform_euler(c[0], c[1], c[2], rng.uniform(0, 360), rng.uniform(0, 180),
+                                           rng.uniform(0, 360)))
+    for i, m in enumerate(mothers):
+        ix, iy, iz = i // 9, (i // 3) % 3, i % 3
+        c = np.array([-300.0 + 300.0 * ix, -300.0 + 300.0 * iy, -300.0 + 300.0 * iz]) + rng.uniform(-20, 20, 3)
+        b.place(m, world, transform_euler(c[0], c[1], c[2], rng.uniform(0, 360), rng.uniform(0, 180),
+                                          rng.uniform(0, 360)))
+    b.place_world(world)
+    return b.build()
+
+
+def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_limit: float = 1e4) -> TrackBatch:
+    """Points uniform in a cube of half-length `half`, isotropic directions, unlocated states."""
+    rng = np.random.Generator(np.random.PCG64(seed_points))
+    p = rng.uniform(-half, half, (n, 3))
+    dx, dy, dz = isotropic(np.random.Generator(np.random.PCG64(seed_dirs)), n)
+    return TrackBatch(p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), dx, dy, dz, np.full(n, step_limit),
+                      np.zeros(n, dtype=STATE_DTYPE))
