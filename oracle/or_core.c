@@ -258,6 +258,7 @@ static int shape_nparams(int type, const double *p, int avail)
   switch (type) {
   case OR_BOX: return 3;
   case OR_TUBE: return 5;
+  case OR_CONE: return 7;
   default: (void)p; (void)avail; return -1;
   }
 }

@@ -92,6 +92,16 @@ typedef struct { /* TubeStruct.h:15-41 (no phi wedge: full-phi tubes) */
   double tolIrmin2, tolOrmin2, tolIrmax2, tolOrmax2, tolIz, tolOz, tolIrmin, tolOrmin, tolIrmax, tolOrmax, maxval;
 } or_tube;
 
+typedef struct { /* ConeStruct.h:23-77 cached members, full phi */
+  double rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi;
+  double o_rmin1, o_rmin2, o_rmax1, o_rmax2; /* _frmin1.. (constructor arguments) */
+  double innerSlope, outerSlope, innerOffset, outerOffset, innerTolerance, outerTolerance;
+  double sqRmin1, sqRmin2, sqRmax1, sqRmax2, tolIz, tolOz;
+  double innerConeApex, tanInnerApexAngle, outerConeApex, tanOuterApexAngle;
+  double secRMin, secRMax, invSecRMin, invSecRMax, tanRMin, tanRMax, zNormInner, zNormOuter;
+  double originalRmax1, originalRmax2;
+} or_cone;
+
 typedef struct {
   int type;
   int param_off;
@@ -101,6 +111,7 @@ typedef struct {
   union {
     or_box box;
     or_tube tube;
+    or_cone cone;
   } s;
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;

@@ -321,6 +321,400 @@ static void tube_extent(const or_tube *t, v3 *mn, v3 *mx)
 }
 
 /* ================================================================== */
+/* Cone (full phi): kernel/ConeImplementation.h, ConeUtilities.h      */
+/* ================================================================== */
+
+/* ConeStruct constructor + CalculateCached (ConeStruct.h:79-157, 414-426) */
+static int cone_init(or_cone *c, const double *a, char *err, int errlen)
+{
+  double dphi = a[6];
+  c->rmin1 = a[0] < 0.0 ? 0.0 : a[0];
+  c->rmax1 = a[1];
+  c->rmin2 = a[2] < 0.0 ? 0.0 : a[2];
+  c->rmax2 = a[3];
+  c->dz    = a[4];
+  c->sphi  = a[5];
+  c->o_rmin1 = a[0];
+  c->o_rmax1 = a[1];
+  c->o_rmin2 = a[2];
+  c->o_rmax2 = a[3];
+  if (dphi >= kTwoPi - 0.5 * kAngTolerance) {
+    c->dphi = kTwoPi;
+    c->sphi = 0;
+  } else {
+    set_err(err, errlen, "cone: phi sections are not supported");
+    return -1;
+  }
+  c->originalRmax1 = c->rmax1;
+  c->originalRmax2 = c->rmax2;
+  if (c->rmin1 == c->rmax1) c->rmax1 += kConeTolerance;
+  if (c->rmin2 == c->rmax2) c->rmax2 += kConeTolerance;
+  c->sqRmin1    = c->rmin1 * c->rmin1;
+  c->sqRmax1    = c->rmax1 * c->rmax1;
+  c->sqRmin2    = c->rmin2 * c->rmin2;
+  c->sqRmax2    = c->rmax2 * c->rmax2;
+  c->tanRMin    = (c->rmin2 - c->rmin1) * 0.5 / c->dz;
+  c->secRMin    = sqrt(1.0 + c->tanRMin * c->tanRMin);
+  c->invSecRMin = 1. / NonZero(c->secRMin);
+  c->tanRMax    = (c->rmax2 - c->rmax1) * 0.5 / c->dz;
+  c->secRMax    = sqrt(1.0 + c->tanRMax * c->tanRMax);
+  c->invSecRMax = 1. / NonZero(c->secRMax);
+  c->innerSlope     = -(c->rmin1 - c->rmin2) / (2. * c->dz);
+  c->outerSlope     = -(c->rmax1 - c->rmax2) / (2. * c->dz);
+  c->innerOffset    = c->rmin2 - c->innerSlope * c->dz;
+  c->outerOffset    = c->rmax2 - c->outerSlope * c->dz;
+  c->innerTolerance = kConeTolerance * c->secRMin;
+  c->outerTolerance = kConeTolerance * c->secRMax;
+  if (c->rmin2 > c->rmin1) {
+    c->innerConeApex     = 2 * c->dz * c->rmin1 / (c->rmin2 - c->rmin1);
+    c->tanInnerApexAngle = c->rmin2 / (2 * c->dz + c->innerConeApex);
+  } else {
+    c->innerConeApex     = 2 * c->dz * c->rmin2 / NonZero(c->rmin1 - c->rmin2);
+    c->tanInnerApexAngle = c->rmin1 / (2 * c->dz + c->innerConeApex);
+  }
+  if (c->rmin1 == 0. || c->rmin2 == 0.) c->innerConeApex = 0.;
+  if (c->rmin1 == 0.) c->tanInnerApexAngle = c->rmin2 / (2 * c->dz);
+  if (c->rmin2 == 0.) c->tanInnerApexAngle = c->rmin1 / (2 * c->dz);
+  if (c->rmax2 > c->rmax1) {
+    c->outerConeApex     = 2 * c->dz * c->rmax1 / (c->rmax2 - c->rmax1);
+    c->tanOuterApexAngle = c->rmax2 / (2 * c->dz + c->outerConeApex);
+  } else {
+    c->outerConeApex     = 2 * c->dz * c->rmax2 / NonZero(c->rmax1 - c->rmax2);
+    c->tanOuterApexAngle = c->rmax1 / (2 * c->dz + c->outerConeApex);
+  }
+  if (c->rmax1 == 0. || c->rmax2 == 0.) c->outerConeApex = 0.;
+  if (c->rmax1 == 0.) c->tanOuterApexAngle = c->rmax2 / (2 * c->dz);
+  if (c->rmax2 == 0.) c->tanOuterApexAngle = c->rmax1 / (2 * c->dz);
+  c->zNormInner = c->tanRMin / NonZero(c->secRMin);
+  c->zNormOuter = -c->tanRMax / NonZero(c->secRMax);
+  c->tolIz      = c->dz - kHalfTolerance;
+  c->tolOz      = c->dz + kHalfTolerance;
+  return 0;
+}
+
+static inline int cone_has_rmin(const or_cone *c) { return c->rmin1 > 0 || c->rmin2 > 0; }
+
+/* MakePlus/MinusTolerantSquare<true> (kernel/GenericKernels.h:65-82) */
+static inline double plus_tol_sq(double x, double tol) { return x * (x + 2.0 * tol); }
+static inline double minus_tol_sq(double x, double tol) { return fabs(x * (x - 2.0 * tol)); }
+
+/* ConeUtilities::GetRadiusOfConeAtPoint (ConeUtilities.h:116-137) */
+static inline double cone_radius(const or_cone *c, double z, int inner)
+{
+  if (inner) return c->rmin1 == c->rmin2 ? c->rmin1 : c->innerSlope * z + c->innerOffset;
+  return c->originalRmax1 == c->originalRmax2 ? c->originalRmax1 : c->outerSlope * z + c->outerOffset;
+}
+
+/* ConeUtilities::GetNormal (ConeUtilities.h:206-238) */
+static inline v3 cone_normal(const or_cone *c, v3 p, int inner)
+{
+  double rho = sqrt(v3_perp2(p));
+  if (inner) {
+    if ((c->rmin1 == c->rmin2) && (c->rmin1 != 0.)) return v3_make(-p.x, -p.y, 0.);
+    return v3_make(-p.x, -p.y, c->zNormInner * (rho * c->secRMin));
+  }
+  if ((c->rmax1 == c->rmax2) && (c->rmax1 != 0.)) return v3_make(p.x, p.y, 0.);
+  return v3_make(p.x, p.y, c->zNormOuter * (rho * c->secRMax));
+}
+
+/* ConeUtilities::IsOnConicalSurface (ConeUtilities.h:240-255) */
+static inline int cone_on_surface(const or_cone *c, v3 p, int inner)
+{
+  const double rho      = v3_perp2(p);
+  const double coneRad  = cone_radius(c, p.z, inner);
+  const double coneRad2 = coneRad * coneRad;
+  const double tol      = inner ? c->innerTolerance : c->outerTolerance;
+  return (rho >= (coneRad2 - tol * coneRad)) && (rho <= (coneRad2 + tol * coneRad)) &&
+         (fabs(p.z) < (c->dz + kConeTolerance));
+}
+
+/* ConeHelpers<double>::DetectIntersectionAndCalculateDistanceToConicalSurface (ConeUtilities.h:591-762) */
+static int cone_conical(const or_cone *c, v3 p, v3 d, int fordistin, int inner, double *distance)
+{
+  int onsurf, ok = 0;
+  v3 n;
+  double pDotV2D, a, b, cc, b2, ac, d2, delta, newZ;
+  *distance = kInfLength;
+  onsurf    = cone_on_surface(c, p, inner);
+  n         = cone_normal(c, p, inner);
+  if (onsurf && fabs(v3_dot(d, n)) == 0.) return 0;
+  if (onsurf) {
+    if (fordistin) {
+      if (v3_dot(d, n) <= 0.) { *distance = 0.; return 1; }
+    } else {
+      if (v3_dot(d, n) >= 0.) { *distance = 0.; return 1; }
+    }
+  }
+  pDotV2D = p.x * d.x + p.y * d.y;
+  if (inner) {
+    if (c->rmin1 == c->rmin2) {
+      b  = pDotV2D;
+      a  = v3_perp2(d);
+      cc = v3_perp2(p) - c->rmin2 * c->rmin2;
+    } else {
+      double newPz, dirT;
+      if (c->rmin2 > c->rmin1)
+        newPz = (p.z + c->dz + c->innerConeApex) * c->tanInnerApexAngle;
+      else
+        newPz = (p.z - c->dz - c->innerConeApex) * c->tanInnerApexAngle;
+      dirT = d.z * c->tanInnerApexAngle;
+      a    = (d.x * d.x) + (d.y * d.y) - dirT * dirT;
+      b    = pDotV2D - (newPz * dirT);
+      cc   = v3_perp2(p) - (newPz * newPz);
+    }
+    b2 = b * b;
+    ac = a * cc;
+    if (b2 < ac) return 0;
+    d2    = b2 - ac;
+    delta = sqrt(d2);
+    if (fordistin) {
+      if (b >= 0.)
+        *distance = (cc / NonZero(-b - delta));
+      else
+        *distance = (-b + delta) / NonZero(a);
+    } else {
+      if (b == 0. && delta == 0.) return 0;
+      if (b >= 0.)
+        *distance = (-b - delta) / NonZero(a);
+      else
+        *distance = (cc / NonZero(-b + delta));
+    }
+    if (*distance < 0.) return 0;
+    newZ = p.z + (d.z * *distance);
+    ok   = (fabs(newZ) < c->dz);
+  } else {
+    if (c->originalRmax1 == c->originalRmax2) {
+      a  = v3_perp2(d);
+      b  = pDotV2D;
+      cc = (v3_perp2(p) - c->originalRmax2 * c->originalRmax2);
+    } else {
+      double newPz, dirT;
+      if (c->originalRmax2 > c->originalRmax1)
+        newPz = (p.z + c->dz + c->outerConeApex) * c->tanOuterApexAngle;
+      else
+        newPz = (p.z - c->dz - c->outerConeApex) * c->tanOuterApexAngle;
+      dirT = d.z * c->tanOuterApexAngle;
+      a    = d.x * d.x + d.y * d.y - dirT * dirT;
+      b    = (pDotV2D - (newPz * dirT));
+      cc   = (v3_perp2(p) - (newPz * newPz));
+    }
+    b2 = b * b;
+    ac = a * cc;
+    d2 = b2 - ac;
+    if (d2 < 0) return 0;
+    delta = sqrt(d2);
+    if (fordistin) {
+      if (b == 0. && delta == 0.) return 0;
+      if (b > 0.)
+        *distance = (-b - delta) / NonZero(a);
+      else
+        *distance = (cc / NonZero(-b + delta));
+      newZ = p.z + (d.z * *distance);
+      ok   = (fabs(newZ) < c->dz + kHalfTolerance);
+    } else {
+      if (b < 0.)
+        *distance = (-b + delta) / NonZero(a);
+      else
+        *distance = (cc / NonZero(-b - delta));
+      ok = *distance > 0.;
+    }
+    if (*distance < 0.) return 0;
+  }
+  return ok;
+}
+
+/* DistanceToIn (ConeImplementation.h:117-255), full phi */
+static double cone_dist_in(const or_cone *c, v3 p, v3 d)
+{
+  int done = 0, inside, okz, top, bot, ok;
+  double distance = kInfLength, distz, outerRad, rsq, hitx, hity, r2, dr;
+  const int hasrmin = cone_has_rmin(c);
+  distz = fabs(p.z) - c->dz;
+  done |= (distz > kConeTolerance && (p.z * d.z) >= 0.) || (fabs(distz) < kConeTolerance && (p.z * d.z) > 0.);
+  if (done) return distance;
+  outerRad = cone_radius(c, p.z, 0);
+  rsq      = v3_perp2(p);
+  done |= (rsq > minus_tol_sq(outerRad, c->outerTolerance)) && (v3_dot(d, cone_normal(c, p, 0)) >= 0.);
+  if (done) return distance;
+  distance = -1.0;
+  inside   = distz < -kConeTolerance;
+  inside &= rsq < minus_tol_sq(outerRad, c->outerTolerance);
+  if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, 1), c->innerTolerance);
+  done |= inside;
+  if (done) return distance;
+  distance = kInfLength;
+  distz /= NonZero(fabs(d.z));
+  hitx = p.x + distz * d.x;
+  hity = p.y + distz * d.y;
+  r2   = (hitx * hitx) + (hity * hity);
+  top  = (p.z >= c->tolIz) && (r2 <= c->sqRmax2 + kTolerance);
+  bot  = (p.z <= -c->tolIz) && (r2 <= c->sqRmax1 + kTolerance);
+  okz  = top || bot;
+  if (hasrmin) {
+    top &= (r2 >= c->sqRmin2 - kTolerance);
+    bot &= (r2 >= c->sqRmin1 - kTolerance);
+    okz &= (top || bot);
+  }
+  if (!done && okz) distance = distz;
+  done |= okz;
+  if (done) return distance;
+  ok = cone_conical(c, p, d, 1, 0, &dr);
+  ok &= dr < distance;
+  if (!done && ok) distance = dr;
+  done |= ok;
+  if (done) return distance;
+  if (hasrmin) {
+    ok = cone_conical(c, p, d, 1, 1, &dr);
+    ok &= dr < distance;
+    if (!done && ok) distance = dr;
+  }
+  return distance;
+}
+
+/* DistanceToOut (ConeImplementation.h:257-366), full phi */
+static double cone_dist_out(const or_cone *c, v3 p, v3 d)
+{
+  int done = 0, outside, up, down, onz, ok;
+  double distance = kInfLength, distz, rsq, outerRad, dirZInv, dr;
+  const int hasrmin = cone_has_rmin(c);
+  distz    = fabs(p.z) - c->dz;
+  distance = -1.0;
+  outside  = distz > kConeTolerance;
+  rsq      = v3_perp2(p);
+  outerRad = cone_radius(c, p.z, 0);
+  outside |= rsq > plus_tol_sq(outerRad, c->outerTolerance);
+  done |= outside;
+  if (done) return distance;
+  if (hasrmin && !outside) {
+    outside |= rsq < minus_tol_sq(cone_radius(c, p.z, 1), c->innerTolerance);
+    done |= outside;
+    if (done) return distance;
+  }
+  done |= outside;
+  if (done) return distance;
+  up   = d.z > 0.;
+  down = d.z < 0.;
+  onz  = !outside && ((up && p.z > 0. && fabs(distz) < kConeTolerance) ||
+                     (down && p.z < 0. && fabs(distz) < kConeTolerance));
+  if (!done && onz) distance = distz;
+  done |= onz;
+  if (done) return distance;
+  distance = kInfLength;
+  dirZInv  = 1. / NonZero(d.z);
+  if (up) distance = (c->dz - p.z) * dirZInv;
+  if (down) distance = (-c->dz - p.z) * dirZInv;
+  ok = cone_conical(c, p, d, 0, 0, &dr);
+  if (!done && ok && dr < distance) distance = dr;
+  if (hasrmin) {
+    ok = cone_conical(c, p, d, 0, 1, &dr);
+    if (!done && ok && dr < distance) distance = dr;
+  }
+  if (distance < 0. && fabs(distance) < kTolerance) distance = 0.;
+  return distance;
+}
+
+/* SafeDistanceToConicalSurface (ConeImplementation.h:502-516) */
+static inline double cone_safe_surface(const or_cone *c, v3 p, int inner)
+{
+  double rho = sqrt(v3_perp2(p));
+  if (inner) {
+    double pRMin = c->tanRMin * p.z + (c->rmin1 + c->rmin2) * 0.5;
+    return (rho - pRMin) * c->invSecRMin;
+  }
+  {
+    double pRMax = c->tanRMax * p.z + (c->rmax1 + c->rmax2) * 0.5;
+    return (pRMax - rho) * c->invSecRMax;
+  }
+}
+
+/* SafetyToIn (ConeImplementation.h:368-432), full phi */
+static double cone_safe_in(const or_cone *c, v3 p)
+{
+  int inside;
+  double safety, distz, outerRad, rsq, safeZ, so, si = -kInfLength;
+  const int hasrmin = cone_has_rmin(c);
+  distz    = fabs(p.z) - c->dz;
+  safety   = -1.0;
+  inside   = distz < -kConeTolerance;
+  outerRad = cone_radius(c, p.z, 0);
+  rsq      = v3_perp2(p);
+  inside &= rsq < minus_tol_sq(outerRad, c->outerTolerance);
+  if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, 1), c->innerTolerance);
+  if (inside) return safety;
+  safeZ = fabs(p.z) - c->dz;
+  so    = -cone_safe_surface(c, p, 0);
+  if (hasrmin) si = -cone_safe_surface(c, p, 1);
+  safety = or_max(safeZ, or_max(so, si));
+  if (fabs(safety) < kTolerance) safety = 0.;
+  return safety;
+}
+
+/* SafetyToOut (ConeImplementation.h:434-499), full phi */
+static double cone_safe_out(const or_cone *c, v3 p)
+{
+  int outside;
+  double safety, distz, rsq, outerRad, safeZ, so, si = kInfLength;
+  const int hasrmin = cone_has_rmin(c);
+  distz    = fabs(p.z) - c->dz;
+  rsq      = v3_perp2(p);
+  safety   = -1.0;
+  outside  = distz > kConeTolerance;
+  outerRad = cone_radius(c, p.z, 0);
+  outside |= rsq > plus_tol_sq(outerRad, c->outerTolerance);
+  if (hasrmin) outside |= rsq < minus_tol_sq(cone_radius(c, p.z, 1), c->innerTolerance);
+  if (outside) return safety;
+  safeZ = c->dz - fabs(p.z);
+  so    = cone_safe_surface(c, p, 0);
+  if (hasrmin) si = cone_safe_surface(c, p, 1);
+  safety = or_min(safeZ, or_min(so, si));
+  if (fabs(safety) < kTolerance) safety = 0.;
+  return safety;
+}
+
+/* ConeHelpers<double>::GenericKernelForContainsAndInside (ConeUtilities.h:764-813) */
+static void cone_generic_ci(const or_cone *c, v3 p, int forinside, int *cin, int *cout)
+{
+  double absz = fabs(p.z), r2, rmax;
+  *cout = absz > (forinside ? c->dz + kConeTolerance : c->dz);
+  if (forinside) *cin = absz < c->dz - kConeTolerance;
+  if (*cout) return;
+  r2   = p.x * p.x + p.y * p.y;
+  rmax = (c->originalRmax1 == c->originalRmax2) ? c->originalRmax1 : c->outerSlope * p.z + c->outerOffset;
+  *cout |= r2 > (forinside ? plus_tol_sq(rmax, c->outerTolerance) : rmax * rmax);
+  if (forinside) *cin &= r2 < minus_tol_sq(rmax, c->outerTolerance);
+  if (*cout) return;
+  if (cone_has_rmin(c)) {
+    double rmin = c->innerSlope * p.z + c->innerOffset;
+    *cout |= r2 <= (forinside ? minus_tol_sq(rmin, c->innerTolerance) : rmin * rmin);
+    if (forinside) *cin &= r2 > plus_tol_sq(rmin, c->innerTolerance);
+  }
+}
+
+static int cone_contains(const or_cone *c, v3 p)
+{
+  int cin = 0, cout = 0;
+  cone_generic_ci(c, p, 0, &cin, &cout);
+  return !cout;
+}
+
+static int cone_inside(const or_cone *c, v3 p)
+{
+  int cin = 0, cout = 0, r = kSurfaceE;
+  cone_generic_ci(c, p, 1, &cin, &cout);
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+/* UnplacedCone::Extent, full phi (source/UnplacedCone.cpp:149-165) */
+static void cone_extent(const or_cone *c, v3 *mn, v3 *mx)
+{
+  double m = c->o_rmax1 > c->o_rmax2 ? c->o_rmax1 : c->o_rmax2;
+  *mn      = v3_make(-m, -m, -c->dz);
+  *mx      = v3_make(m, m, c->dz);
+}
+
+/* ================================================================== */
 /* dispatch                                                           */
 /* ================================================================== */
 
@@ -334,6 +728,7 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
     lv->s.box.d[2] = p[2];
     return 0;
   case OR_TUBE: return tube_init(&lv->s.tube, p, err, errlen);
+  case OR_CONE: return cone_init(&lv->s.cone, p, err, errlen);
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -346,6 +741,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
     *mx = v3_make(lv->s.box.d[0], lv->s.box.d[1], lv->s.box.d[2]);
     return;
   case OR_TUBE: tube_extent(&lv->s.tube, mn, mx); return;
+  case OR_CONE: cone_extent(&lv->s.cone, mn, mx); return;
   }
 }
 
@@ -359,6 +755,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   switch (lv->type) {
   case OR_BOX: return box_dist_in(&lv->s.box, p, d);
   case OR_TUBE: return tube_dist_in(&lv->s.tube, p, d);
+  case OR_CONE: return cone_dist_in(&lv->s.cone, p, d);
   }
   return kInfLength;
 }
@@ -370,6 +767,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   switch (lv->type) {
   case OR_BOX: return box_dist_out(&lv->s.box, p, d);
   case OR_TUBE: return tube_dist_out(&lv->s.tube, p, d);
+  case OR_CONE: return cone_dist_out(&lv->s.cone, p, d);
   }
   return -1.;
 }
@@ -380,6 +778,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   switch (lv->type) {
   case OR_BOX: return box_safe_in(&lv->s.box, p);
   case OR_TUBE: return tube_safe_in(&lv->s.tube, p);
+  case OR_CONE: return cone_safe_in(&lv->s.cone, p);
   }
   return kInfLength;
 }
@@ -390,6 +789,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   switch (lv->type) {
   case OR_BOX: return box_safe_out(&lv->s.box, p);
   case OR_TUBE: return tube_safe_out(&lv->s.tube, p);
+  case OR_CONE: return cone_safe_out(&lv->s.cone, p);
   }
   return 0.;
 }
@@ -400,6 +800,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   switch (lv->type) {
   case OR_BOX: return box_contains(&lv->s.box, p);
   case OR_TUBE: return tube_contains(&lv->s.tube, p);
+  case OR_CONE: return cone_contains(&lv->s.cone, p);
   }
   return 0;
 }
@@ -410,6 +811,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   switch (lv->type) {
   case OR_BOX: return box_inside(&lv->s.box, p);
   case OR_TUBE: return tube_inside(&lv->s.tube, p);
+  case OR_CONE: return cone_inside(&lv->s.cone, p);
   }
   return kOutsideE;
 }

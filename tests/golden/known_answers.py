@@ -219,7 +219,129 @@ TUBE_CASES = [
           (-0.1443054266272111, -0.01508874701037938, 0.9894181489944458), 2016.51817758),
 ]
 
-ALL_CASES = BOX_CASES + TUBE_CASES
+CONE = 2
+C = "test/unit_tests/TestCons.cpp"
+# cones of TestCons.cpp:84-100 with full phi (rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi)
+C1 = (50.0, 100.0, 50.0, 100.0, 50.0, 0.0, TWO_PI)
+C2 = (50.0, 100.0, 50.0, 200.0, 50.0, -1.0, TWO_PI)
+C6 = (0.0, 150.0, 0.0, 150.0, 50.0, 0.0, TWO_PI)
+C7 = (95.0, 100.0, 95.0, 100.0, 50.0, 0.0, TWO_PI)
+C8A = (0.0, 100.0, 0.0, 150.0, 50.0, 0.0, TWO_PI)
+C8B = (50.0, 100.0, 100.0, 150.0, 50.0, 0.0, TWO_PI)
+C8C = (100.0, 150.0, 50.0, 100.0, 50.0, 0.0, TWO_PI)
+C9 = (50.0, 60.0, 0.0, 10.0, 50.0, 0.0, TWO_PI)
+CMS = (0.0, 70.0, 0.0, 157.8, 2949.0, 0.0, 6.283185307179586)
+CT1 = (0.0, 50.0, 0.0, 50.0, 50.0, 0.0, TWO_PI)   # TestCons.cpp:1006
+R1 = math.sqrt(50 * 50 / 2.0)
+R2 = math.sqrt(100 * 100 / 2.0)
+ponphi1 = (60 * math.cos(KPI / 6), -60 * math.sin(KPI / 6), 0.0)
+ponr1, ponr2 = (R1, R1, 0.0), (R2, R2, 0.0)
+pplx, pply, pplz, pmiz = (120.0, 0.0, 0.0), (0.0, 120.0, 0.0), (0.0, 0.0, 120.0), (0.0, 0.0, -120.0)
+ponmiz, ponplz = (0.0, 75.0, -50.0), (0.0, 75.0, 50.0)
+pparr1, pparr2, pparr3 = (0.0, 25.0, -150.0), (0.0, 75.0, -50.0), (0.0, 125.0, 50.0)
+vparr = (0.0, 1.0 / math.sqrt(5.0), 2.0 / math.sqrt(5.0))
+mvparr = (-0.0, -vparr[1], -vparr[2])
+vx2mz = (1.0 / math.sqrt(5.0), 0.0, -2.0 / math.sqrt(5.0))
+SQ5H = 100.0 * math.sqrt(5.0) / 2.0
+CMSP = (0.28628920024909, -0.43438111004815, -2949.0)
+CMSD = (6.0886686196674e-05, -9.2382200635766e-05, 0.99999999387917)
+# OutRange (TestCons.cpp:28-35): |value - expect| <= 1e-4 ("range")
+CONE_CASES = [
+    _case(f"{C}:373", CONE, C1, "safe_out", ponphi1, None, 10.0, "range"),
+    _case(f"{C}:377", CONE, C1, "safe_out", (45.0, 45.0, 45.0), None, 5.0, "range"),
+    _case(f"{C}:381", CONE, C1, "safe_out", (45.0, 45.0, -45.0), None, 5.0, "range"),
+    _case(f"{C}:385", CONE, C1, "safe_out", ponr1, None, 0.0, "range"),
+    _case(f"{C}:388", CONE, C1, "safe_out", ponr2, None, 0.0, "range"),
+    _case(f"{C}:392", CONE, C6, "safe_out", pzero, None, 50.0, "range"),
+    _case(f"{C}:407", CONE, C2, "dist_out", pplx, vx, 30.0, "range"),
+    _case(f"{C}:417", CONE, C2, "dist_out", pplx, vmx, 70.0, "range"),
+    _case(f"{C}:442", CONE, C6, "dist_out", ponplz, vmz, 100.0, "range"),
+    _case(f"{C}:446", CONE, C6, "dist_out", ponplz, vz, 0.0, "range"),
+    _case(f"{C}:451", CONE, C6, "dist_out", ponmiz, vz, 100.0, "range"),
+    _case(f"{C}:456", CONE, C6, "dist_out", ponmiz, vmz, 0.0, "range"),
+    _case(f"{C}:462", CONE, C7, "dist_out", ponr2, vmx, 100.0 / math.sqrt(2.0) - math.sqrt(95.0 * 95.0 - 100.0 * 100.0 / 2.0),
+          "range"),
+    _case(f"{C}:469", CONE, C8A, "dist_out", pparr2, vparr, SQ5H, "range"),
+    _case(f"{C}:474", CONE, C8A, "dist_out", pparr2, mvparr, 0.0, "range"),
+    _case(f"{C}:479", CONE, C8A, "dist_out", pparr2, vz, 100.0, "range"),
+    _case(f"{C}:484", CONE, C8A, "dist_out", pparr2, vmz, 0.0, "range"),
+    _case(f"{C}:489", CONE, C8A, "dist_out", pparr3, vparr, 0.0, "range"),
+    _case(f"{C}:494", CONE, C8A, "dist_out", pparr3, mvparr, SQ5H, "range"),
+    _case(f"{C}:499", CONE, C8A, "dist_out", pparr3, vz, 0.0, "range"),
+    _case(f"{C}:504", CONE, C8A, "dist_out", pparr3, vmz, 50.0, "range"),
+    _case(f"{C}:509", CONE, C8B, "dist_out", pparr2, vparr, SQ5H, "range"),
+    _case(f"{C}:514", CONE, C8B, "dist_out", pparr2, mvparr, 0.0, "range"),
+    _case(f"{C}:519", CONE, C8B, "dist_out", pparr2, vz, 50.0, "range"),
+    _case(f"{C}:524", CONE, C8B, "dist_out", pparr2, vmz, 0.0, "range"),
+    _case(f"{C}:529", CONE, C8B, "dist_out", pparr3, vparr, 0.0, "range"),
+    _case(f"{C}:534", CONE, C8B, "dist_out", pparr3, mvparr, SQ5H, "range"),
+    _case(f"{C}:539", CONE, C8B, "dist_out", pparr3, vz, 0.0, "range"),
+    _case(f"{C}:544", CONE, C8B, "dist_out", pparr3, vmz, 50.0, "range"),
+    _case(f"{C}:549", CONE, C9, "dist_out", (1e3 * 1e-9 * 1000, 0.0, 50.0), vx2mz, 111.8033988, "range"),
+    _case(f"{C}:559", CONE, C9, "dist_out", (5.0, 0.0, 50.0), vx2mz, 111.8033988, "range"),
+    _case(f"{C}:564", CONE, C9, "dist_out", (10.0, 0.0, 50.0), vx2mz, 111.8033988, "range"),
+    _case(f"{C}:577", CONE, CMS, "dist_out", CMSP, CMSD, 5898.0, "range"),
+    _case(f"{C}:626", CONE, C1, "safe_in", pzero, None, 50.0, "range"),
+    _case(f"{C}:630", CONE, C1, "safe_in", pplx, None, 20.0, "range"),
+    _case(f"{C}:634", CONE, C1, "safe_in", pply, None, 20.0, "range"),
+    _case(f"{C}:646", CONE, C1, "safe_in", pplz, None, 70.0, "range"),
+    _case(f"{C}:659", CONE, C1, "dist_in", pplz, vmz, INF, "inf"),
+    _case(f"{C}:663", CONE, C2, "dist_in", pplz, vmz, INF, "inf"),
+    _case(f"{C}:679", CONE, C6, "dist_in", pplz, vmz, 70.0, "range"),
+    _case(f"{C}:683", CONE, C7, "dist_in", pplz, vmz, INF, "inf"),
+    _case(f"{C}:687", CONE, C8A, "dist_in", pplz, vmz, 70.0, "range"),
+    _case(f"{C}:691", CONE, C8B, "dist_in", pplz, vmz, INF, "inf"),
+    _case(f"{C}:695", CONE, C8C, "dist_in", pplz, vmz, INF, "inf"),
+    _case(f"{C}:700", CONE, C9, "dist_in", pplz, vmz, 70.0, "range"),
+    _case(f"{C}:704", CONE, C9, "dist_in", (0.0, 0.0, 50.0), vmz, 0.0, "range"),
+    _case(f"{C}:710", CONE, C1, "dist_in", pmiz, vz, INF, "inf"),
+    _case(f"{C}:714", CONE, C2, "dist_in", pmiz, vz, INF, "inf"),
+    _case(f"{C}:730", CONE, C6, "dist_in", pmiz, vz, 70.0, "range"),
+    _case(f"{C}:734", CONE, C7, "dist_in", pmiz, vz, INF, "inf"),
+    _case(f"{C}:738", CONE, C8A, "dist_in", pmiz, vz, 70.0, "range"),
+    _case(f"{C}:742", CONE, C8B, "dist_in", pmiz, vz, INF, "inf"),
+    _case(f"{C}:746", CONE, C8C, "dist_in", pmiz, vz, INF, "inf"),
+    _case(f"{C}:750", CONE, C9, "dist_in", pmiz, vz, INF, "inf"),
+    _case(f"{C}:756", CONE, C1, "dist_in", pplx, vmx, 20.0, "range"),
+    _case(f"{C}:759", CONE, C1, "dist_in", pplz, vx, INF, "inf"),
+    _case(f"{C}:766", CONE, C1, "dist_in", (60.0, 150.0, 0.0), vmy, 70.0, "range"),
+    _case(f"{C}:776", CONE, C1, "dist_in", pplx, vx, INF, "inf"),
+    _case(f"{C}:788", CONE, C1, "dist_in", ponr2, vx, INF, "inf"),
+    _case(f"{C}:791", CONE, C1, "dist_in", ponr2, vmx, 0.0, "range"),
+    _case(f"{C}:795", CONE, C1, "dist_in", ponr1, vx, 0.0, "range"),
+    _case(f"{C}:798", CONE, C1, "dist_in", ponr1, vmx, 2.0 * math.sqrt(50 * 50 / 2.0), "range"),
+    _case(f"{C}:802", CONE, C1, "dist_in", ponr2, vmxmy, 0.0, "range"),
+    _case(f"{C}:807", CONE, C8B, "dist_in", pparr1, vparr, SQ5H, "range"),
+    _case(f"{C}:810", CONE, C8B, "dist_in", pparr2, mvparr, INF, "inf"),
+    _case(f"{C}:813", CONE, C8B, "dist_in", pparr3, vparr, INF, "inf"),
+    _case(f"{C}:816", CONE, C8B, "dist_in", pparr3, mvparr, 0.0, "range"),
+    _case(f"{C}:820", CONE, C8A, "dist_in", (0.0, 125.0, -1000.0), vz, 1000.0, "range"),
+    _case(f"{C}:1013", CONE, CT1, "inside", pzero, None, 1, "eq"),
+    _case(f"{C}:1014", CONE, CT1, "inside", (100.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{C}:1022", CONE, CT1, "safe_out", pzero, None, 50.0, "approx"),
+    _case(f"{C}:1026", CONE, CT1, "dist_out", pzero, vx, 50.0, "approx"),
+    _case(f"{C}:1029", CONE, CT1, "dist_out", pzero, vmx, 50.0, "approx"),
+    _case(f"{C}:1032", CONE, CT1, "dist_out", pzero, vy, 50.0, "approx"),
+    _case(f"{C}:1035", CONE, CT1, "dist_out", pzero, vmy, 50.0, "approx"),
+    _case(f"{C}:1038", CONE, CT1, "dist_out", pzero, vz, 50.0, "approx"),
+    _case(f"{C}:1041", CONE, CT1, "dist_out", pzero, vmz, 50.0, "approx"),
+    _case(f"{C}:1044", CONE, CT1, "dist_out", pzero, vxy, 50.0, "approx"),
+    _case(f"{C}:1049", CONE, CT1, "safe_in", (100.0, 0.0, 0.0), None, 50.0, "approx"),
+    _case(f"{C}:1051", CONE, CT1, "safe_in", (-100.0, 0.0, 0.0), None, 50.0, "approx"),
+    _case(f"{C}:1053", CONE, CT1, "safe_in", (0.0, 100.0, 0.0), None, 50.0, "approx"),
+    _case(f"{C}:1055", CONE, CT1, "safe_in", (0.0, -100.0, 0.0), None, 50.0, "approx"),
+    _case(f"{C}:1057", CONE, CT1, "safe_in", (0.0, 0.0, 100.0), None, 50.0, "approx"),
+    _case(f"{C}:1059", CONE, CT1, "safe_in", (0.0, 0.0, -100.0), None, 50.0, "approx"),
+    _case(f"{C}:1063", CONE, CT1, "dist_in", (100.0, 0.0, 0.0), vmx, 50.0, "approx"),
+    _case(f"{C}:1065", CONE, CT1, "dist_in", (-100.0, 0.0, 0.0), vx, 50.0, "approx"),
+    _case(f"{C}:1067", CONE, CT1, "dist_in", (0.0, 100.0, 0.0), vmy, 50.0, "approx"),
+    _case(f"{C}:1069", CONE, CT1, "dist_in", (0.0, -100.0, 0.0), vy, 50.0, "approx"),
+    _case(f"{C}:1071", CONE, CT1, "dist_in", (0.0, 0.0, 100.0), vmz, 50.0, "approx"),
+    _case(f"{C}:1073", CONE, CT1, "dist_in", (0.0, 0.0, -100.0), vz, 50.0, "approx"),
+    _case(f"{C}:1075", CONE, CT1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
+]
+
+ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:
@@ -245,4 +367,6 @@ def check(case, value) -> bool:
         return value >= INF
     if c == "eq":
         return value == case["expect"]
+    if c == "range":
+        return case["expect"] - 1e-4 <= value <= case["expect"] + 1e-4
     raise ValueError(c)

@@ -93,6 +93,12 @@ constexpr int kBoxSize = 4;
 // Tube (full phi): TubeStruct cached members
 enum { TubeRmin = 0, TubeRmax, TubeZ, TubeRmin2, TubeRmax2, TubeTolIrmin2, TubeTolOrmin2, TubeTolIrmax2,
        TubeTolOrmax2, TubeMaxVal, kTubeSize };
+// Cone (full phi): ConeStruct cached members
+enum { ConeRmin1 = 0, ConeRmax1, ConeRmin2, ConeRmax2, ConeDz, ConeOrigRmax1, ConeOrigRmax2, ConeInnerSlope,
+       ConeOuterSlope, ConeInnerOffset, ConeOuterOffset, ConeInnerTol, ConeOuterTol, ConeSqRmin1, ConeSqRmin2,
+       ConeSqRmax1, ConeSqRmax2, ConeTolIz, ConeInnerApex, ConeTanInnerApex, ConeOuterApex, ConeTanOuterApex,
+       ConeSecRMin, ConeSecRMax, ConeInvSecRMin, ConeInvSecRMax, ConeTanRMin, ConeTanRMax, ConeZNormInner,
+       ConeZNormOuter, ConeArgRmax1, ConeArgRmax2, kConeSize };
 }  // namespace row
 
 // Plain-pointer view of the device tables, passed to kernels by value.

@@ -285,12 +285,295 @@ __device__ __forceinline__ int tube_inside(const double *t, D3 p)
   return r;
 }
 
+// ---------------------------------------------------------------- Cone (full phi)
+// kernel/ConeImplementation.h:117-516, ConeUtilities.h:116-813; row layout vgn::row::Cone*
+constexpr double kConeTolerance = 1e-7;
+
+// MakePlus/MinusTolerantSquare<true> (kernel/GenericKernels.h:65-82)
+__device__ __forceinline__ double plus_tol_sq(double x, double tol) { return x * (x + 2.0 * tol); }
+__device__ __forceinline__ double minus_tol_sq(double x, double tol) { return fabs(x * (x - 2.0 * tol)); }
+
+__device__ __forceinline__ bool cone_has_rmin(const double *c) { return c[row::ConeRmin1] > 0 || c[row::ConeRmin2] > 0; }
+
+// GetRadiusOfConeAtPoint (ConeUtilities.h:116-137)
+__device__ __forceinline__ double cone_radius(const double *c, double z, bool inner)
+{
+  if (inner)
+    return c[row::ConeRmin1] == c[row::ConeRmin2] ? c[row::ConeRmin1]
+                                                    : c[row::ConeInnerSlope] * z + c[row::ConeInnerOffset];
+  return c[row::ConeOrigRmax1] == c[row::ConeOrigRmax2] ? c[row::ConeOrigRmax1]
+                                                          : c[row::ConeOuterSlope] * z + c[row::ConeOuterOffset];
+}
+
+// GetNormal (ConeUtilities.h:206-238)
+__device__ __forceinline__ D3 cone_normal(const double *c, D3 p, bool inner)
+{
+  const double rho = sqrt(p.x * p.x + p.y * p.y);
+  if (inner) {
+    if ((c[row::ConeRmin1] == c[row::ConeRmin2]) && (c[row::ConeRmin1] != 0.)) return d3(-p.x, -p.y, 0.);
+    return d3(-p.x, -p.y, c[row::ConeZNormInner] * (rho * c[row::ConeSecRMin]));
+  }
+  if ((c[row::ConeRmax1] == c[row::ConeRmax2]) && (c[row::ConeRmax1] != 0.)) return d3(p.x, p.y, 0.);
+  return d3(p.x, p.y, c[row::ConeZNormOuter] * (rho * c[row::ConeSecRMax]));
+}
+
+__device__ __forceinline__ double dot3(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// IsOnConicalSurface (ConeUtilities.h:240-255)
+__device__ __forceinline__ bool cone_on_surface(const double *c, D3 p, bool inner)
+{
+  const double rho      = p.x * p.x + p.y * p.y;
+  const double coneRad  = cone_radius(c, p.z, inner);
+  const double coneRad2 = coneRad * coneRad;
+  const double tol      = inner ? c[row::ConeInnerTol] : c[row::ConeOuterTol];
+  return (rho >= (coneRad2 - tol * coneRad)) && (rho <= (coneRad2 + tol * coneRad)) &&
+         (fabs(p.z) < (c[row::ConeDz] + kConeTolerance));
+}
+
+// ConeHelpers<double>::DetectIntersectionAndCalculateDistanceToConicalSurface (ConeUtilities.h:591-762)
+__device__ __forceinline__ bool cone_conical(const double *c, D3 p, D3 d, bool fordistin, bool inner, double &distance)
+{
+  distance          = kInfLength;
+  const bool onsurf = cone_on_surface(c, p, inner);
+  const D3 n        = cone_normal(c, p, inner);
+  const double dn   = dot3(d, n);
+  if (onsurf && fabs(dn) == 0.) return false;
+  if (onsurf) {
+    if (fordistin ? (dn <= 0.) : (dn >= 0.)) {
+      distance = 0.;
+      return true;
+    }
+  }
+  const double pDotV2D = p.x * d.x + p.y * d.y;
+  const double dz      = c[row::ConeDz];
+  double a, b, cc;
+  bool ok = false;
+  if (inner) {
+    if (c[row::ConeRmin1] == c[row::ConeRmin2]) {
+      b  = pDotV2D;
+      a  = d.x * d.x + d.y * d.y;
+      cc = (p.x * p.x + p.y * p.y) - c[row::ConeRmin2] * c[row::ConeRmin2];
+    } else {
+      const double tanA  = c[row::ConeTanInnerApex];
+      const double newPz = (c[row::ConeRmin2] > c[row::ConeRmin1]) ? (p.z + dz + c[row::ConeInnerApex]) * tanA
+                                                                     : (p.z - dz - c[row::ConeInnerApex]) * tanA;
+      const double dirT  = d.z * tanA;
+      a  = (d.x * d.x) + (d.y * d.y) - dirT * dirT;
+      b  = pDotV2D - (newPz * dirT);
+      cc = (p.x * p.x + p.y * p.y) - (newPz * newPz);
+    }
+    const double b2 = b * b, ac = a * cc;
+    if (b2 < ac) return false;
+    const double delta = sqrt(b2 - ac);
+    if (fordistin) {
+      distance = (b >= 0.) ? (cc / nonzero(-b - delta)) : (-b + delta) / nonzero(a);
+    } else {
+      if (b == 0. && delta == 0.) return false;
+      distance = (b >= 0.) ? (-b - delta) / nonzero(a) : (cc / nonzero(-b + delta));
+    }
+    if (distance < 0.) return false;
+    const double newZ = p.z + (d.z * distance);
+    ok                = (fabs(newZ) < dz);
+  } else {
+    if (c[row::ConeOrigRmax1] == c[row::ConeOrigRmax2]) {
+      a  = d.x * d.x + d.y * d.y;
+      b  = pDotV2D;
+      cc = ((p.x * p.x + p.y * p.y) - c[row::ConeOrigRmax2] * c[row::ConeOrigRmax2]);
+    } else {
+      const double tanA  = c[row::ConeTanOuterApex];
+      const double newPz = (c[row::ConeOrigRmax2] > c[row::ConeOrigRmax1])
+                               ? (p.z + dz + c[row::ConeOuterApex]) * tanA
+                               : (p.z - dz - c[row::ConeOuterApex]) * tanA;
+      const double dirT  = d.z * tanA;
+      a  = d.x * d.x + d.y * d.y - dirT * dirT;
+      b  = (pDotV2D - (newPz * dirT));
+      cc = ((p.x * p.x + p.y * p.y) - (newPz * newPz));
+    }
+    const double b2 = b * b, ac = a * cc, d2 = b2 - ac;
+    if (d2 < 0) return false;
+    const double delta = sqrt(d2);
+    if (fordistin) {
+      if (b == 0. && delta == 0.) return false;
+      distance = (b > 0.) ? (-b - delta) / nonzero(a) : (cc / nonzero(-b + delta));
+      const double newZ = p.z + (d.z * distance);
+      ok                = (fabs(newZ) < dz + kHalfTolerance);
+    } else {
+      distance = (b < 0.) ? (-b + delta) / nonzero(a) : (cc / nonzero(-b - delta));
+      ok       = distance > 0.;
+    }
+    if (distance < 0.) return false;
+  }
+  return ok;
+}
+
+// DistanceToIn (ConeImplementation.h:117-255)
+__device__ __forceinline__ double cone_dist_in(const double *c, D3 p, D3 d)
+{
+  const bool hasrmin = cone_has_rmin(c);
+  const double dz    = c[row::ConeDz];
+  double distance    = kInfLength;
+  double distz       = fabs(p.z) - dz;
+  if ((distz > kConeTolerance && (p.z * d.z) >= 0.) || (fabs(distz) < kConeTolerance && (p.z * d.z) > 0.))
+    return distance;
+  const double outerRad = cone_radius(c, p.z, false);
+  const double rsq      = p.x * p.x + p.y * p.y;
+  if ((rsq > minus_tol_sq(outerRad, c[row::ConeOuterTol])) && (dot3(d, cone_normal(c, p, false)) >= 0.))
+    return distance;
+  bool inside = distz < -kConeTolerance;
+  inside &= rsq < minus_tol_sq(outerRad, c[row::ConeOuterTol]);
+  if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, true), c[row::ConeInnerTol]);
+  if (inside) return -1.0;
+  distance = kInfLength;
+  distz /= nonzero(fabs(d.z));
+  const double hitx = p.x + distz * d.x;
+  const double hity = p.y + distz * d.y;
+  const double r2   = (hitx * hitx) + (hity * hity);
+  bool top = (p.z >= c[row::ConeTolIz]) && (r2 <= c[row::ConeSqRmax2] + kTolerance);
+  bool bot = (p.z <= -c[row::ConeTolIz]) && (r2 <= c[row::ConeSqRmax1] + kTolerance);
+  bool okz = top || bot;
+  if (hasrmin) {
+    top &= (r2 >= c[row::ConeSqRmin2] - kTolerance);
+    bot &= (r2 >= c[row::ConeSqRmin1] - kTolerance);
+    okz &= (top || bot);
+  }
+  if (okz) return distz;
+  double dr;
+  bool ok = cone_conical(c, p, d, true, false, dr);
+  ok &= dr < distance;
+  if (ok) return dr;
+  if (hasrmin) {
+    ok = cone_conical(c, p, d, true, true, dr);
+    ok &= dr < distance;
+    if (ok) distance = dr;
+  }
+  return distance;
+}
+
+// DistanceToOut (ConeImplementation.h:257-366)
+__device__ __forceinline__ double cone_dist_out(const double *c, D3 p, D3 d)
+{
+  const bool hasrmin = cone_has_rmin(c);
+  const double dz    = c[row::ConeDz];
+  const double distz = fabs(p.z) - dz;
+  bool outside       = distz > kConeTolerance;
+  const double rsq   = p.x * p.x + p.y * p.y;
+  outside |= rsq > plus_tol_sq(cone_radius(c, p.z, false), c[row::ConeOuterTol]);
+  if (outside) return -1.0;
+  if (hasrmin) {
+    outside |= rsq < minus_tol_sq(cone_radius(c, p.z, true), c[row::ConeInnerTol]);
+    if (outside) return -1.0;
+  }
+  const bool up = d.z > 0., down = d.z < 0.;
+  if ((up && p.z > 0. && fabs(distz) < kConeTolerance) || (down && p.z < 0. && fabs(distz) < kConeTolerance))
+    return distz;
+  double distance      = kInfLength;
+  const double dirZInv = 1. / nonzero(d.z);
+  if (up) distance = (dz - p.z) * dirZInv;
+  if (down) distance = (-dz - p.z) * dirZInv;
+  double dr;
+  bool ok = cone_conical(c, p, d, false, false, dr);
+  if (ok && dr < distance) distance = dr;
+  if (hasrmin) {
+    ok = cone_conical(c, p, d, false, true, dr);
+    if (ok && dr < distance) distance = dr;
+  }
+  if (distance < 0. && fabs(distance) < kTolerance) distance = 0.;
+  return distance;
+}
+
+// SafeDistanceToConicalSurface (ConeImplementation.h:502-516)
+__device__ __forceinline__ double cone_safe_surface(const double *c, D3 p, bool inner)
+{
+  const double rho = sqrt(p.x * p.x + p.y * p.y);
+  if (inner) {
+    const double pRMin = c[row::ConeTanRMin] * p.z + (c[row::ConeRmin1] + c[row::ConeRmin2]) * 0.5;
+    return (rho - pRMin) * c[row::ConeInvSecRMin];
+  }
+  const double pRMax = c[row::ConeTanRMax] * p.z + (c[row::ConeRmax1] + c[row::ConeRmax2]) * 0.5;
+  return (pRMax - rho) * c[row::ConeInvSecRMax];
+}
+
+// SafetyToIn (ConeImplementation.h:368-432)
+__device__ __forceinline__ double cone_safe_in(const double *c, D3 p)
+{
+  const bool hasrmin = cone_has_rmin(c);
+  const double distz = fabs(p.z) - c[row::ConeDz];
+  const double rsq   = p.x * p.x + p.y * p.y;
+  bool inside        = distz < -kConeTolerance;
+  inside &= rsq < minus_tol_sq(cone_radius(c, p.z, false), c[row::ConeOuterTol]);
+  if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, true), c[row::ConeInnerTol]);
+  if (inside) return -1.0;
+  const double safeZ = fabs(p.z) - c[row::ConeDz];
+  const double so    = -cone_safe_surface(c, p, false);
+  const double si    = hasrmin ? -cone_safe_surface(c, p, true) : -kInfLength;
+  double safety      = vmax(safeZ, vmax(so, si));
+  if (fabs(safety) < kTolerance) safety = 0.;
+  return safety;
+}
+
+// SafetyToOut (ConeImplementation.h:434-499)
+__device__ __forceinline__ double cone_safe_out(const double *c, D3 p)
+{
+  const bool hasrmin = cone_has_rmin(c);
+  const double distz = fabs(p.z) - c[row::ConeDz];
+  const double rsq   = p.x * p.x + p.y * p.y;
+  bool outside       = distz > kConeTolerance;
+  outside |= rsq > plus_tol_sq(cone_radius(c, p.z, false), c[row::ConeOuterTol]);
+  if (hasrmin) outside |= rsq < minus_tol_sq(cone_radius(c, p.z, true), c[row::ConeInnerTol]);
+  if (outside) return -1.0;
+  const double safeZ = c[row::ConeDz] - fabs(p.z);
+  const double so    = cone_safe_surface(c, p, false);
+  const double si    = hasrmin ? cone_safe_surface(c, p, true) : kInfLength;
+  double safety      = vmin(safeZ, vmin(so, si));
+  if (fabs(safety) < kTolerance) safety = 0.;
+  return safety;
+}
+
+// ConeHelpers<double>::GenericKernelForContainsAndInside (ConeUtilities.h:764-813)
+__device__ __forceinline__ void cone_generic_ci(const double *c, D3 p, bool forinside, bool &cin, bool &cout)
+{
+  const double dz = c[row::ConeDz], absz = fabs(p.z);
+  cout = absz > (forinside ? dz + kConeTolerance : dz);
+  if (forinside) cin = absz < dz - kConeTolerance;
+  if (cout) return;
+  const double r2   = p.x * p.x + p.y * p.y;
+  const double rmax = (c[row::ConeOrigRmax1] == c[row::ConeOrigRmax2])
+                          ? c[row::ConeOrigRmax1]
+                          : c[row::ConeOuterSlope] * p.z + c[row::ConeOuterOffset];
+  cout |= r2 > (forinside ? plus_tol_sq(rmax, c[row::ConeOuterTol]) : rmax * rmax);
+  if (forinside) cin &= r2 < minus_tol_sq(rmax, c[row::ConeOuterTol]);
+  if (cout) return;
+  if (cone_has_rmin(c)) {
+    const double rmin = c[row::ConeInnerSlope] * p.z + c[row::ConeInnerOffset];
+    cout |= r2 <= (forinside ? minus_tol_sq(rmin, c[row::ConeInnerTol]) : rmin * rmin);
+    if (forinside) cin &= r2 > plus_tol_sq(rmin, c[row::ConeInnerTol]);
+  }
+}
+
+__device__ __forceinline__ bool cone_contains(const double *c, D3 p)
+{
+  bool cin = false, cout = false;
+  cone_generic_ci(c, p, false, cin, cout);
+  return !cout;
+}
+
+__device__ __forceinline__ int cone_inside(const double *c, D3 p)
+{
+  bool cin = false, cout = false;
+  cone_generic_ci(c, p, true, cin, cout);
+  int r = kSurfaceE;
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
 // ---------------------------------------------------------------- dispatch
 __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
   switch (type) {
   case kBox: return box_dist_in(r, p, d);
   case kTube: return tube_dist_in(r, p, d);
+  case kCone: return cone_dist_in(r, p, d);
   }
   return kInfLength;
 }
@@ -300,6 +583,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   switch (type) {
   case kBox: return box_dist_out(r, p, d);
   case kTube: return tube_dist_out(r, p, d);
+  case kCone: return cone_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -309,6 +593,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   switch (type) {
   case kBox: return box_safe_in(r, p);
   case kTube: return tube_safe_in(r, p);
+  case kCone: return cone_safe_in(r, p);
   }
   return kInfLength;
 }
@@ -318,6 +603,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   switch (type) {
   case kBox: return box_safe_out(r, p);
   case kTube: return tube_safe_out(r, p);
+  case kCone: return cone_safe_out(r, p);
   }
   return 0.;
 }
@@ -327,6 +613,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   switch (type) {
   case kBox: return box_contains(r, p);
   case kTube: return tube_contains(r, p);
+  case kCone: return cone_contains(r, p);
   }
   return false;
 }
@@ -336,6 +623,7 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   switch (type) {
   case kBox: return box_inside(r, p);
   case kTube: return tube_inside(r, p);
+  case kCone: return cone_inside(r, p);
   }
   return kOutsideE;
 }
