@@ -38,7 +38,7 @@ UNIT = "steps/s"
 # write step 8 + state 12 + safety 8
 BYTES_PER_STEP = 24 + 24 + 8 + 12 + 8 + 12 + 8
 WORKLOAD = ("box-grid: 4096 rotated boxes in a 1 m world, 2^22 tracks, "
-            "ComputeStepAndNextVolume + ComputeSafety, all-FP64 kernel")
+            "ComputeStepAndNextVolume + ComputeSafety")
 
 
 def peaks():
@@ -111,11 +111,11 @@ def dist_setup():
     return ws, rank, local
 
 
-def make_workload():
+def make_workload(n_tracks: int = N_TRACKS):
     from vecgeom_gb300 import workloads as W
 
     grid = W.box_grid_geometry(seed=3)
-    t = W.box_grid_tracks(grid, n=N_TRACKS, seed_points=4, seed_dirs=5, step_limit=1000.0)
+    t = W.box_grid_tracks(grid, n=n_tracks, seed_points=4, seed_dirs=5, step_limit=1000.0)
     return grid, t
 
 
@@ -187,7 +187,7 @@ def run_ours(args, ws, rank, local):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    grid, t = make_workload()
+    grid, t = make_workload(args.tracks)
     geo = V.Geometry(grid.desc, device=local)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     pts = V.SOA3D(dev(t.x), dev(t.y), dev(t.z))
@@ -201,34 +201,46 @@ def run_ours(args, ws, rank, local):
     saf = torch.empty(t.n, dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def one():
-        geo.step(pts, dirs, sl, inp, out, steps, saf, stream=stream)
-
-    for _ in range(max(args.warmup, 3)):
-        one()
-    geo.synchronize(stream)
-
     def barrier():
         torch.cuda.synchronize()
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier()
-    with ClockSampler(local) as clocks:
+    def timed(mixed: bool, clocks=None):
+        def one():
+            geo.step(pts, dirs, sl, inp, out, steps, saf, mixed=mixed, stream=stream)
+
+        for _ in range(max(args.warmup, 3)):
+            one()
+        geo.synchronize(stream)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        barrier()
+        sampler = ClockSampler(local) if clocks is not None else None
+        if sampler:
+            sampler.__enter__()
         for a, b in evs:
             a.record(stream)
             one()
             b.record(stream)
         barrier()
-    geo.synchronize(stream)
-    per = [a.elapsed_time(b) for a, b in evs]
-    total_ms = evs[0][0].elapsed_time(evs[-1][1])
-    if dist is not None:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+        if sampler:
+            sampler.__exit__(None, None, None)
+            clocks.append(sampler.summary())
+        geo.synchronize(stream)
+        per = [a.elapsed_time(b) for a, b in evs]
+        total = evs[0][0].elapsed_time(evs[-1][1])
+        if dist is not None:
+            tt = torch.tensor([total], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            total = float(tt.item())
+        return per, total
+
+    plain_per, plain_ms = timed(False)
+    clock_log = []
+    per, total_ms = timed(True, clock_log)
+    plain_value = ws * t.n * args.steps / (plain_ms * 1e-3)
     value = ws * t.n * args.steps / (total_ms * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers ----
@@ -241,7 +253,7 @@ def run_ours(args, ws, rank, local):
     hp, hd = V.SOA3D(hx, hy, hz), V.SOA3D(hdx, hdy, hdz)
 
     def one_host():
-        geo.step(hp, hd, hsl, V.NavStatePool(hst), V.NavStatePool(hout), hstep, hsaf)
+        geo.step(hp, hd, hsl, V.NavStatePool(hst), V.NavStatePool(hout), hstep, hsaf, mixed=True)
 
     e2e_steps = max(3, min(args.steps, 10))
     one_host()
@@ -276,19 +288,24 @@ def run_ours(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "tracks_per_step_per_gpu": t.n, "daughters": 4096,
-                       "step_limit_mm": 1000.0, "precision": "fp64-plain", "parallelism": f"replicas x{ws}",
+                       "step_limit_mm": 1000.0, "parallelism": f"replicas x{ws}",
+                       "precision": "mixed: FP32-interval box decisions, FP64 transforms/shapes (bit-exact)",
                        "l2": "inputs+outputs 400 MB per step > 129 MB L2: no flush needed"},
             "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                            "batch_tracks": t.n},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps, "path": "vgn_compute_step_batch with pinned host buffers"},
+            "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms / args.steps,
+                           "p50_ms": float(np.percentile(plain_per, 50)),
+                           "p99_ms": float(np.percentile(plain_per, 99))},
+            "mixed_over_plain": value / plain_value,
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
                          "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
                          "algorithmic_bytes_per_step": BYTES_PER_STEP,
-                         "kernel": "step_kernel_fp64", "kernel_avg_ms": avg_ms},
-            "clocks": clocks.summary(),
+                         "kernel": "step_kernel<mixed>", "kernel_avg_ms": avg_ms},
+            "clocks": clock_log[0] if clock_log else None,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
@@ -305,6 +322,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tracks", type=int, default=N_TRACKS, help="tracks per step (smaller only for profiling)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

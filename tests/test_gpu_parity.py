@@ -29,7 +29,7 @@ def states_to_dev(torch, st):
     return torch.from_numpy(a).cuda()
 
 
-def gpu_step(torch, geo, t, safety=True, relocate=True):
+def gpu_step(torch, geo, t, safety=True, relocate=True, mixed=False):
     from vecgeom_gb300.navigator import SOA3D, NavStatePool
 
     pts = SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
@@ -39,7 +39,7 @@ def gpu_step(torch, geo, t, safety=True, relocate=True):
     out = NavStatePool.empty_like(inp)
     steps = torch.empty(t.n, dtype=torch.float64, device="cuda")
     saf = torch.empty(t.n, dtype=torch.float64, device="cuda") if safety else None
-    geo.step(pts, dirs, sl, inp, out, steps, saf, relocate=relocate)
+    geo.step(pts, dirs, sl, inp, out, steps, saf, relocate=relocate, mixed=mixed)
     geo.synchronize()
     return dict(step=steps.cpu().numpy(), out=out.to_numpy(), safety=None if saf is None else saf.cpu().numpy())
 
@@ -87,24 +87,26 @@ def test_tube_points_bit_exact(oracle, vgnav, cuda):
         assert np.array_equal(got, og.shape(0, op, x, y, z, dx, dy, dz)), op
 
 
-def test_box_grid_step_bit_exact(oracle, vgnav, cuda):
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_box_grid_step_bit_exact(oracle, vgnav, cuda, mixed):
     grid = W.box_grid_geometry()
     og = oracle.OracleGeometry(grid.desc)
     geo = vgnav.Geometry(grid.desc)
     t = W.box_grid_tracks(grid, n=1 << 16, seed_points=41, seed_dirs=42)
     ref = og.step(t, calcsafety=True)
-    got = gpu_step(cuda, geo, t)
+    got = gpu_step(cuda, geo, t, mixed=mixed)
     assert np.array_equal(got["step"], ref["step"])
     assert np.array_equal(got["safety"], ref["safety"])
     assert np.array_equal(got["out"], ref["out"])
     # ComputeStep (no relocation)
     ref_n = og.step(t, relocate=False)
-    got_n = gpu_step(cuda, geo, t, safety=False, relocate=False)
+    got_n = gpu_step(cuda, geo, t, safety=False, relocate=False, mixed=mixed)
     assert np.array_equal(got_n["step"], ref_n["step"])
     assert np.array_equal(got_n["out"], ref_n["out"])
 
 
-def test_box_grid_host_pointer_path(oracle, vgnav, cuda):
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_box_grid_host_pointer_path(oracle, vgnav, cuda, mixed):
     """Same call with host numpy arrays: the library stages through the device."""
     grid = W.box_grid_geometry()
     og = oracle.OracleGeometry(grid.desc)
@@ -115,19 +117,20 @@ def test_box_grid_host_pointer_path(oracle, vgnav, cuda):
     steps = np.zeros(t.n)
     saf = np.zeros(t.n)
     geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit, vgnav.NavStatePool(t.states),
-             vgnav.NavStatePool(out), steps, saf)
+             vgnav.NavStatePool(out), steps, saf, mixed=mixed)
     assert np.array_equal(steps, ref["step"]) and np.array_equal(saf, ref["safety"])
     assert np.array_equal(out, ref["out"])
     # the alias entry point gives the same answer
     out2 = np.zeros(t.n, dtype=W.STATE_DTYPE)
     steps2 = np.zeros(t.n)
     geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit, vgnav.NavStatePool(t.states),
-             vgnav.NavStatePool(out2), steps2, None, api="alias")
+             vgnav.NavStatePool(out2), steps2, None, api="alias", mixed=mixed)
     assert np.array_equal(steps2, ref["step"]) and np.array_equal(out2, ref["out"])
 
 
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["box_grid", "nested"])
-def test_walk_to_world_exit(oracle, vgnav, cuda, which):
+def test_walk_to_world_exit(oracle, vgnav, cuda, which, mixed):
     """Every step of every track, stepped until it leaves the world, equals the oracle."""
     if which == "box_grid":
         grid = W.box_grid_geometry()
@@ -140,12 +143,12 @@ def test_walk_to_world_exit(oracle, vgnav, cuda, which):
     geo = vgnav.Geometry(desc)
     if which == "nested":
         st = np.zeros(t.n, dtype=W.STATE_DTYPE)
-        geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st))
+        geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st), mixed=mixed)
         assert np.array_equal(st, og.locate(t.x, t.y, t.z))
         t.states = st
     for it in range(400):
         ref = og.step(t)
-        got = gpu_step(cuda, geo, t)
+        got = gpu_step(cuda, geo, t, mixed=mixed)
         assert np.array_equal(got["step"], ref["step"]), it
         assert np.array_equal(got["safety"], ref["safety"]), it
         assert np.array_equal(got["out"], ref["out"]), it
@@ -156,29 +159,31 @@ def test_walk_to_world_exit(oracle, vgnav, cuda, which):
     assert t.n == 0
 
 
-def test_safety_and_locate_kernels(oracle, vgnav, cuda):
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_safety_and_locate_kernels(oracle, vgnav, cuda, mixed):
     desc = W.nested_geometry()
     og = oracle.OracleGeometry(desc)
     geo = vgnav.Geometry(desc)
     t = W.uniform_tracks(100000, 490.0, 61, 62)
     st = np.zeros(t.n, dtype=W.STATE_DTYPE)
-    geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st))
+    geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st), mixed=mixed)
     assert np.array_equal(st, og.locate(t.x, t.y, t.z))
     inside = st["nav_ind"] != 0
     x, y, z, s = t.x[inside], t.y[inside], t.z[inside], st[inside]
     saf = np.zeros(x.shape[0])
-    geo.safety(vgnav.SOA3D(x, y, z), vgnav.NavStatePool(s), saf)
+    geo.safety(vgnav.SOA3D(x, y, z), vgnav.NavStatePool(s), saf, mixed=mixed)
     assert np.array_equal(saf, og.safety(x, y, z, s))
 
 
-def test_full_size_box_grid(oracle, vgnav, cuda):
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_full_size_box_grid(oracle, vgnav, cuda, mixed):
     """2^22 tracks of the 4096-box geometry: every result equals the oracle's."""
     grid = W.box_grid_geometry()
     og = oracle.OracleGeometry(grid.desc)
     geo = vgnav.Geometry(grid.desc)
     t = W.box_grid_tracks(grid)
     ref = og.step(t)
-    got = gpu_step(cuda, geo, t)
+    got = gpu_step(cuda, geo, t, mixed=mixed)
     assert np.array_equal(got["step"], ref["step"])
     assert np.array_equal(got["safety"], ref["safety"])
     assert np.array_equal(got["out"], ref["out"])

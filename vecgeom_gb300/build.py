@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra nvcc flags)
 UNITS = [
-    ("kernels_fp64.cu", ["-fmad=false"]),
+    ("kernels_nav.cu", ["-fmad=false"]),
     ("host_geometry.cpp", []),
     ("host_shapes.cpp", []),
     ("vgnav_api.cpp", []),

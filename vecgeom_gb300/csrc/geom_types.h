@@ -86,6 +86,42 @@ struct alignas(32) FPrimRec {
 };
 static_assert(sizeof(FPrimRec) == 32, "FPrimRec must be 32 bytes");
 
+// ---- FP32 interval images for the mixed-precision kernels ----
+// Every float pair [lo, hi] brackets a double of the FP64 tables (lo rounded
+// toward -inf, hi toward +inf), so FP32 interval arithmetic with directed
+// rounding bounds the value the FP64 code would compute; a decision is taken
+// in FP32 only when the whole interval falls on one side.
+struct alignas(64) INodeSlab {  // BVH node box, for slab tests
+  float mn_lo[3], mn_hi[3], mx_lo[3], mx_hi[3];
+  int32_t nchild;
+  int32_t offset;
+  int32_t pad[2];
+};
+static_assert(sizeof(INodeSlab) == 64, "INodeSlab must be 64 bytes");
+
+struct alignas(64) ISafe {  // box centre 0.5*(mx+mn) and half size 0.5*(mx-mn) (AABB::Safety)
+  float c_lo[3], c_hi[3], hs_lo[3], hs_hi[3];
+  int32_t pad[4];
+};
+static_assert(sizeof(ISafe) == 64, "ISafe must be 64 bytes");
+
+struct alignas(64) IPrimSlab {  // leaf primitive box in BVH leaf order
+  float mn_lo[3], mn_hi[3], mx_lo[3], mx_hi[3];
+  int32_t pv;
+  int32_t prim;
+  int32_t pad[2];
+};
+static_assert(sizeof(IPrimSlab) == 64, "IPrimSlab must be 64 bytes");
+
+struct alignas(128) IXForm {  // placement transform as intervals + box half-lengths (shape box only)
+  float t_lo[3], t_hi[3];
+  float r_lo[9], r_hi[9];
+  float h_lo[3], h_hi[3];  // box half-lengths; zero for other shapes
+  int32_t shape;
+  int32_t pad[1];
+};
+static_assert(sizeof(IXForm) == 128, "IXForm must be 128 bytes");
+
 // Row layouts (doubles) of GeomView::shape per shape type.
 namespace row {
 // Box: BoxStruct::fDimensions
@@ -112,6 +148,11 @@ struct GeomView {
   const PrimRec *prims;
   const FNodeRec *fnodes;
   const FPrimRec *fprims;
+  const INodeSlab *inodes;   // interval images (mixed precision), indexed like nodes
+  const ISafe *inode_safe;
+  const IPrimSlab *iprims;   // indexed like prims
+  const ISafe *iprim_safe;
+  const IXForm *ixf;         // per placed volume
   const double *shape;
   uint32_t navind_words;
   int32_t n_pv;

@@ -326,6 +326,8 @@ inline float round_up(double v)
 
 }  // namespace
 
+void build_interval_images(HostGeometry &g);
+
 int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string &err)
 {
   if (d.n_logical <= 0 || d.n_placed <= 0 || !d.lv_shape || !d.lv_param_offset || !d.params || !d.pv_logical ||
@@ -476,7 +478,66 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
       g.fprims.push_back(f);
     }
   }
+  build_interval_images(g);
   return VGN_OK;
+}
+
+void set_interval(float *lo, float *hi, double v)
+{
+  *lo = round_down(v);
+  *hi = round_up(v);
+}
+
+// Interval (FP32) images of the FP64 tables, for the mixed-precision kernels.
+void build_interval_images(HostGeometry &g)
+{
+  auto slab = [](const double *mn, const double *mx, float *mn_lo, float *mn_hi, float *mx_lo, float *mx_hi) {
+    for (int c = 0; c < 3; ++c) {
+      set_interval(&mn_lo[c], &mn_hi[c], mn[c]);
+      set_interval(&mx_lo[c], &mx_hi[c], mx[c]);
+    }
+  };
+  // AABB::Safety (AABB.h:81) uses Center() = 0.5*(max+min) and 0.5*Size() = 0.5*(max-min)
+  auto safe = [](const double *mn, const double *mx, ISafe &s) {
+    std::memset(&s, 0, sizeof(s));
+    for (int c = 0; c < 3; ++c) {
+      const double centre = 0.5 * (mx[c] + mn[c]);
+      const double half   = 0.5 * (mx[c] - mn[c]);
+      set_interval(&s.c_lo[c], &s.c_hi[c], centre);
+      set_interval(&s.hs_lo[c], &s.hs_hi[c], half);
+    }
+  };
+  g.inodes.assign(g.nodes.size(), INodeSlab());
+  g.inode_safe.assign(g.nodes.size(), ISafe());
+  for (size_t i = 0; i < g.nodes.size(); ++i) {
+    INodeSlab &n = g.inodes[i];
+    std::memset(&n, 0, sizeof(n));
+    slab(g.nodes[i].mn, g.nodes[i].mx, n.mn_lo, n.mn_hi, n.mx_lo, n.mx_hi);
+    n.nchild = g.nodes[i].nchild;
+    n.offset = g.nodes[i].offset;
+    safe(g.nodes[i].mn, g.nodes[i].mx, g.inode_safe[i]);
+  }
+  g.iprims.assign(g.prims.size(), IPrimSlab());
+  g.iprim_safe.assign(g.prims.size(), ISafe());
+  for (size_t i = 0; i < g.prims.size(); ++i) {
+    IPrimSlab &p = g.iprims[i];
+    std::memset(&p, 0, sizeof(p));
+    slab(g.prims[i].mn, g.prims[i].mx, p.mn_lo, p.mn_hi, p.mx_lo, p.mx_hi);
+    p.pv   = g.prims[i].pv;
+    p.prim = g.prims[i].prim;
+    safe(g.prims[i].mn, g.prims[i].mx, g.iprim_safe[i]);
+  }
+  g.ixf.assign(g.pv.size(), IXForm());
+  for (size_t i = 0; i < g.pv.size(); ++i) {
+    IXForm &x = g.ixf[i];
+    std::memset(&x, 0, sizeof(x));
+    for (int c = 0; c < 3; ++c) set_interval(&x.t_lo[c], &x.t_hi[c], g.pv[i].xf.t[c]);
+    for (int c = 0; c < 9; ++c) set_interval(&x.r_lo[c], &x.r_hi[c], g.pv[i].xf.r[c]);
+    const HostLV &lv = g.lv[g.pv[i].lv];
+    x.shape          = lv.shape;
+    if (lv.shape == kBox)
+      for (int c = 0; c < 3; ++c) set_interval(&x.h_lo[c], &x.h_hi[c], g.shape[lv.shape_row + c]);
+  }
 }
 
 }  // namespace vgn

@@ -67,6 +67,11 @@ struct HostGeometry {
   std::vector<PrimRec> prims;
   std::vector<FNodeRec> fnodes;
   std::vector<FPrimRec> fprims;
+  std::vector<INodeSlab> inodes;
+  std::vector<ISafe> inode_safe;
+  std::vector<IPrimSlab> iprims;
+  std::vector<ISafe> iprim_safe;
+  std::vector<IXForm> ixf;
 };
 
 // Returns 0 on success, a VGN_ERR_* code otherwise (message in err).

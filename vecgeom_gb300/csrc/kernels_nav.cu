@@ -1,0 +1,196 @@
+// kernels_nav.cu -- navigation kernels: step, safety, locate and shape queries,
+// each in an all-FP64 form and (step, safety, locate) a mixed-precision form.
+//
+// Compiled with -fmad=false: every FP64 expression keeps the reference's
+// operation order (no contraction into FMA), so results are bit-identical to
+// the reference's scalar CPU navigator.  The FP32 interval code of the mixed
+// form uses explicitly rounded intrinsics, which are never contracted.
+#include <cuda_runtime.h>
+
+#include "../../include/vgnav.h"
+#include "launch.h"
+#include "nav_step.cuh"
+
+namespace vgn {
+namespace dev {
+
+__device__ __forceinline__ State load_state(const vgn_state *s, int64_t i)
+{
+  const uint32_t *w = reinterpret_cast<const uint32_t *>(s + i);
+  State r;
+  r.nav_ind     = __ldg(w);
+  r.last_exited = __ldg(w + 1);
+  r.on_boundary = __ldg(w + 2) & 0xffu;
+  return r;
+}
+
+__device__ __forceinline__ void store_state(vgn_state *s, int64_t i, const State &st)
+{
+  uint32_t *w = reinterpret_cast<uint32_t *>(s + i);
+  w[0]        = st.nav_ind;
+  w[1]        = st.last_exited;
+  w[2]        = st.on_boundary & 0xffu;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) step_kernel(GeomView g, int64_t n, const double *__restrict__ px,
+                                                   const double *__restrict__ py, const double *__restrict__ pz,
+                                                   const double *__restrict__ dx, const double *__restrict__ dy,
+                                                   const double *__restrict__ dz, const double *__restrict__ slimit,
+                                                   const vgn_state *__restrict__ in, vgn_state *__restrict__ out,
+                                                   double *__restrict__ step, double *__restrict__ safety, int reloc)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const State s = load_state(in, i);
+    State o       = s;
+    double sf = 0., st;
+    if (!ni_valid(g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(g, s.last_exited))) {
+      raise_error(g, kErrState);
+      st = 0.;
+    } else {
+      st = nav_step<MIXED>(g, d3(px[i], py[i], pz[i]), d3(dx[i], dy[i], dz[i]), slimit[i], s, o,
+                           safety != nullptr, sf, reloc != 0);
+    }
+    step[i] = st;
+    if (safety) safety[i] = sf;
+    store_state(out, i, o);
+  }
+}
+
+// VSafetyEstimatorHelper::ComputeSafety (VSafetyEstimator.h:98-107)
+template <bool MIXED>
+__global__ void __launch_bounds__(256) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
+                                                     const double *__restrict__ py, const double *__restrict__ pz,
+                                                     const vgn_state *__restrict__ in, double *__restrict__ safety)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const State s = load_state(in, i);
+    if (!ni_valid(g, s.nav_ind)) {
+      raise_error(g, kErrState);
+      safety[i] = 0.;
+      continue;
+    }
+    Xf m;
+    top_matrix(g, s.nav_ind, m);
+    const LVRec lv = load_lv(g, pv_lv(g, ni_top(g, s.nav_ind)));
+    safety[i]      = safety_local<MIXED>(g, lv, xf_point(m.t, m.r, d3(px[i], py[i], pz[i])), d3(1., 0., 0.));
+  }
+}
+
+// GlobalLocator::LocateGlobalPoint(world, p, state, true)
+template <bool MIXED>
+__global__ void __launch_bounds__(256) locate_kernel(GeomView g, int64_t n, const double *__restrict__ px,
+                                                     const double *__restrict__ py, const double *__restrict__ pz,
+                                                     vgn_state *__restrict__ out)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    State s{0u, 0u, 0u};
+    locate_global_point<MIXED>(g, g.world_pv, d3(px[i], py[i], pz[i]), s.nav_ind, true);
+    store_state(out, i, s);
+  }
+}
+
+// unplaced shape queries on one logical volume
+template <int OP>
+__global__ void __launch_bounds__(256) shape_kernel_fp64(int type, const double *__restrict__ row, int64_t n,
+                                                         const double *__restrict__ px, const double *__restrict__ py,
+                                                         const double *__restrict__ pz, const double *__restrict__ dx,
+                                                         const double *__restrict__ dy, const double *__restrict__ dz,
+                                                         double *__restrict__ out)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const D3 p = d3(px[i], py[i], pz[i]);
+    double r;
+    if (OP == VGN_OP_DISTANCE_TO_IN)
+      r = shape_dist_in(type, row, p, d3(dx[i], dy[i], dz[i]));
+    else if (OP == VGN_OP_DISTANCE_TO_OUT)
+      r = shape_dist_out(type, row, p, d3(dx[i], dy[i], dz[i]));
+    else if (OP == VGN_OP_SAFETY_TO_IN)
+      r = shape_safe_in(type, row, p);
+    else if (OP == VGN_OP_SAFETY_TO_OUT)
+      r = shape_safe_out(type, row, p);
+    else if (OP == VGN_OP_CONTAINS)
+      r = shape_contains(type, row, p) ? 1. : 0.;
+    else
+      r = (double)shape_inside(type, row, p);
+    out[i] = r;
+  }
+}
+
+}  // namespace dev
+
+static inline unsigned grid_for(int64_t n, int block, int max_blocks)
+{
+  int64_t b = (n + block - 1) / block;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (unsigned)b;
+}
+
+cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(a.n, block, a.max_blocks);
+  if (mixed)
+    dev::step_kernel<true><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit, a.in, a.out,
+                                                  a.step, a.safety, a.reloc);
+  else
+    dev::step_kernel<false><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit, a.in,
+                                                   a.out, a.step, a.safety, a.reloc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
+                          const vgn_state *in, double *safety, bool mixed, int max_blocks, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(n, block, max_blocks);
+  if (mixed)
+    dev::safety_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety);
+  else
+    dev::safety_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
+                          vgn_state *out, bool mixed, int max_blocks, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(n, block, max_blocks);
+  if (mixed)
+    dev::locate_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, out);
+  else
+    dev::locate_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shape_fp64(int op, int type, const double *row, int64_t n, const double *px, const double *py,
+                              const double *pz, const double *dx, const double *dy, const double *dz, double *out,
+                              int max_blocks, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(n, block, max_blocks);
+  switch (op) {
+  case VGN_OP_DISTANCE_TO_IN:
+    dev::shape_kernel_fp64<VGN_OP_DISTANCE_TO_IN><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    break;
+  case VGN_OP_DISTANCE_TO_OUT:
+    dev::shape_kernel_fp64<VGN_OP_DISTANCE_TO_OUT><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    break;
+  case VGN_OP_SAFETY_TO_IN:
+    dev::shape_kernel_fp64<VGN_OP_SAFETY_TO_IN><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    break;
+  case VGN_OP_SAFETY_TO_OUT:
+    dev::shape_kernel_fp64<VGN_OP_SAFETY_TO_OUT><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    break;
+  case VGN_OP_CONTAINS:
+    dev::shape_kernel_fp64<VGN_OP_CONTAINS><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    break;
+  default:
+    dev::shape_kernel_fp64<VGN_OP_INSIDE><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    break;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace vgn

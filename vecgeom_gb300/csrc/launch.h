@@ -20,12 +20,12 @@ struct StepArgs {
   int max_blocks;
 };
 
-// all-FP64 kernels (kernels_fp64.cu)
-cudaError_t launch_step_fp64(const GeomView &g, const StepArgs &a, cudaStream_t s);
-cudaError_t launch_safety_fp64(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
-                               const vgn_state *in, double *safety, int max_blocks, cudaStream_t s);
-cudaError_t launch_locate_fp64(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
-                               vgn_state *out, int max_blocks, cudaStream_t s);
+// navigation kernels (kernels_nav.cu); mixed = FP32-interval box decisions
+cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s);
+cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
+                          const vgn_state *in, double *safety, bool mixed, int max_blocks, cudaStream_t s);
+cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
+                          vgn_state *out, bool mixed, int max_blocks, cudaStream_t s);
 cudaError_t launch_shape_fp64(int op, int type, const double *row, int64_t n, const double *px, const double *py,
                               const double *pz, const double *dx, const double *dy, const double *dz, double *out,
                               int max_blocks, cudaStream_t s);

@@ -334,110 +334,5 @@ __device__ __forceinline__ LVRec load_lv(const GeomView &g, int lvi)
 
 __device__ __forceinline__ int pv_lv(const GeomView &g, int pv) { return __ldg(&g.pv[pv].lv); }
 
-// GlobalLocator::LocateGlobalPoint (GlobalLocator.h:35-82), BVHLevelLocator attached
-__device__ __forceinline__ int locate_global_point(const GeomView &g, int vol, D3 point, uint32_t &path, bool top)
-{
-  int cand = vol;
-  D3 cur   = point;
-  if (top) cand = pv_unplaced_contains(g, vol, point) ? vol : -1;
-  if (cand >= 0) {
-    path     = ni_push(g, path, cand);
-    LVRec lv = load_lv(g, pv_lv(g, cand));
-    bool godeeper = true;
-    int guard     = 0;
-    while (lv.nd > 0 && godeeper) {
-      if (++guard > kMaxLevels) {
-        raise_error(g, kErrRelocate);
-        break;
-      }
-      int pv;
-      D3 tp;
-      godeeper = bvh_level_locate(g, lv, -1, cur, pv, tp);
-      if (godeeper) {
-        path = ni_push(g, path, pv);
-        cand = pv;
-        lv   = load_lv(g, pv_lv(g, cand));
-        cur  = tp;
-      }
-    }
-  }
-  return cand >= 0 ? ni_top(g, path) : -1;
-}
-
-// GlobalLocator::LocateGlobalPointExclVolume (GlobalLocator.h:88-135)
-__device__ __forceinline__ void locate_global_point_excl(const GeomView &g, int vol, int excl, D3 point, uint32_t &path)
-{
-  int cand = vol;
-  D3 cur   = point;
-  path     = ni_push(g, path, cand);
-  LVRec lv = load_lv(g, pv_lv(g, cand));
-  bool godeeper = true;
-  int guard     = 0;
-  while (lv.nd > 0 && godeeper) {
-    if (++guard > kMaxLevels) {
-      raise_error(g, kErrRelocate);
-      break;
-    }
-    D3 tp;
-    godeeper = bvh_level_locate(g, lv, excl, cur, cand, tp);
-    if (godeeper) {
-      lv   = load_lv(g, pv_lv(g, cand));
-      cur  = tp;
-      path = ni_push(g, path, cand);
-    }
-  }
-}
-
-// GlobalLocator::RelocatePointFromPathForceDifferent (GlobalLocator.h:171-200)
-__device__ __forceinline__ void relocate_force_different(const GeomView &g, D3 lp, uint32_t &path)
-{
-  int cm = ni_top(g, path);
-  const int entry = cm;
-  if (cm < 0) return;
-  D3 tmp    = lp;
-  int guard = 0;
-  while (cm >= 0) {
-    if (++guard > kMaxLevels + 1) {
-      raise_error(g, kErrRelocate);
-      return;
-    }
-    if (cm == entry || !pv_unplaced_contains(g, cm, tmp)) {
-      path = ni_pop(g, path);
-      PvXf x;
-      load_pv_xf(g, cm, x);
-      tmp = xf_inverse(x.t, x.r, tmp);
-      cm  = ni_top(g, path);
-    } else
-      break;
-  }
-  if (cm >= 0) {
-    path = ni_pop(g, path);
-    locate_global_point_excl(g, cm, entry, tmp, path);
-  }
-}
-
-// VNavigatorHelper::Relocate (VNavigator.h:1070-1091)
-__device__ __forceinline__ void relocate(const GeomView &g, D3 pab, const State &in, State &out)
-{
-  if (ni_top(g, out.nav_ind) == ni_top(g, in.nav_ind)) {
-    relocate_force_different(g, pab, out.nav_ind);
-  } else {
-    const int nextvol = ni_top(g, out.nav_ind);
-    out.nav_ind       = ni_pop(g, out.nav_ind);
-    PvXf x;
-    load_pv_xf(g, nextvol, x);
-    locate_global_point(g, nextvol, xf_point(x.t, x.r, pab), out.nav_ind, false);
-  }
-}
-
-// BVHSafetyEstimator::ComputeSafetyForLocalPoint (BVHSafetyEstimator.h:38-46)
-__device__ __forceinline__ double safety_local(const GeomView &g, D3 lp, int pv)
-{
-  const LVRec lv = load_lv(g, pv_lv(g, pv));
-  double safety  = shape_safe_out(lv.shape, g.shape + lv.shape_row, lp);
-  if (safety > 0.0 && lv.nd > 0) safety = bvh_safety(g, lv, lp, safety);
-  return safety;
-}
-
 }  // namespace dev
 }  // namespace vgn

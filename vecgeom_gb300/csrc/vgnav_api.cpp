@@ -196,7 +196,10 @@ int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry 
   if ((rc = upload(g, h.navind, &v.navind)) || (rc = upload(g, h.node_start, &v.node_start)) || (rc = upload(g, h.pv_rec, &v.pv)) || (rc = upload(g, h.lv_rec, &v.lv)) ||
       (rc = upload(g, h.daughters, &v.daughters)) || (rc = upload(g, h.nodes, &v.nodes)) ||
       (rc = upload(g, h.prims, &v.prims)) || (rc = upload(g, h.fnodes, &v.fnodes)) ||
-      (rc = upload(g, h.fprims, &v.fprims)) || (rc = upload(g, h.shape, &v.shape))) {
+      (rc = upload(g, h.fprims, &v.fprims)) || (rc = upload(g, h.shape, &v.shape)) ||
+      (rc = upload(g, h.inodes, &v.inodes)) || (rc = upload(g, h.inode_safe, &v.inode_safe)) ||
+      (rc = upload(g, h.iprims, &v.iprims)) || (rc = upload(g, h.iprim_safe, &v.iprim_safe)) ||
+      (rc = upload(g, h.ixf, &v.ixf))) {
     vgn_geometry_free(g);
     return rc;
   }
@@ -287,7 +290,7 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
   if (n == 0) return VGN_OK;
   if (!px || !py || !pz || !dx || !dy || !dz || !step_limit || !in || !out || !step)
     return fail(VGN_ERR_ARG, "null array argument");
-  if ((flags & VGN_PRECISION_MIXED) != 0) return fail(VGN_ERR_UNSUPPORTED, "mixed precision kernels not built yet");
+  const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
   DeviceGuard guard(g->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int kind = classify({px, py, pz, dx, dy, dz, step_limit, in, out, step, safety});
@@ -299,7 +302,7 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
   if (kind == 1) {
     a.px = px; a.py = py; a.pz = pz; a.dx = dx; a.dy = dy; a.dz = dz; a.slimit = step_limit;
     a.in = in; a.out = out; a.step = step; a.safety = safety;
-    cudaError_t e = vgn::launch_step_fp64(g->view, a, s);
+    cudaError_t e = vgn::launch_step(g->view, a, mixed, s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
   }
   // host buffers: stage through the device workspace
@@ -320,7 +323,7 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   a.px = b[0]; a.py = b[1]; a.pz = b[2]; a.dx = b[3]; a.dy = b[4]; a.dz = b[5]; a.slimit = b[6];
   a.in = din; a.out = dout; a.step = dstep; a.safety = safety ? dsaf : nullptr;
-  e = vgn::launch_step_fp64(g->view, a, s);
+  e = vgn::launch_step(g->view, a, mixed, s);
   if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(step, dstep, nd, cudaMemcpyDeviceToHost, s);
@@ -346,13 +349,13 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
   if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
   if (n == 0) return VGN_OK;
   if (!px || !py || !pz || !in || !safety) return fail(VGN_ERR_ARG, "null array argument");
-  if ((flags & VGN_PRECISION_MIXED) != 0) return fail(VGN_ERR_UNSUPPORTED, "mixed precision kernels not built yet");
+  const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
   DeviceGuard guard(g->device);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int kind = classify({px, py, pz, in, safety});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = vgn::launch_safety_fp64(g->view, n, px, py, pz, in, safety, max_blocks(g), s);
+    cudaError_t e = vgn::launch_safety(g->view, n, px, py, pz, in, safety, mixed, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "safety kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -368,7 +371,7 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
   if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = vgn::launch_safety_fp64(g->view, n, bx, by, bz, din, dsaf, max_blocks(g), s);
+  e = vgn::launch_safety(g->view, n, bx, by, bz, din, dsaf, mixed, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "safety kernel launch");
   e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
@@ -378,7 +381,7 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
 int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const double *py, const double *pz,
                      vgn_state *out, int flags, void *stream)
 {
-  (void)flags;
+  const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
   vgn_geometry *g = const_cast<vgn_geometry *>(gc);
   if (!g) return fail(VGN_ERR_ARG, "null geometry");
   if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
@@ -390,7 +393,7 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   const int kind = classify({px, py, pz, out});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = vgn::launch_locate_fp64(g->view, n, px, py, pz, out, max_blocks(g), s);
+    cudaError_t e = vgn::launch_locate(g->view, n, px, py, pz, out, mixed, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "locate kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -404,7 +407,7 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   if (e == cudaSuccess) e = cudaMemcpyAsync(by, py, nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = vgn::launch_locate_fp64(g->view, n, bx, by, bz, dout, max_blocks(g), s);
+  e = vgn::launch_locate(g->view, n, bx, by, bz, dout, mixed, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "locate kernel launch");
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");

@@ -161,9 +161,10 @@ class Geometry:
                                                  _ptr(states.data), _ptr(safeties),
                                                  N.VGN_PRECISION_MIXED if mixed else 0, _stream_ptr(stream)))
 
-    def locate(self, pts: SOA3D, out_states: NavStatePool, stream=None):
+    def locate(self, pts: SOA3D, out_states: NavStatePool, mixed: bool = False, stream=None):
         N.check(N.lib().vgn_locate_batch(self.handle, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z),
-                                         _ptr(out_states.data), 0, _stream_ptr(stream)))
+                                         _ptr(out_states.data), N.VGN_PRECISION_MIXED if mixed else 0,
+                                         _stream_ptr(stream)))
 
     def shape(self, lv: int, op: int, pts: SOA3D, dirs: SOA3D | None, out, stream=None):
         dx = dy = dz = None
@@ -203,4 +204,4 @@ class BVHNavigator:
         self.geometry.safety(globalpoints, states, out_safeties, mixed=self.mixed, stream=stream)
 
     def LocatePoints(self, globalpoints: SOA3D, out_states: NavStatePool, stream=None):
-        self.geometry.locate(globalpoints, out_states, stream=stream)
+        self.geometry.locate(globalpoints, out_states, mixed=self.mixed, stream=stream)
