@@ -27,3 +27,63 @@ def test_version_and_errors(vgnav):
     assert b"sm_103a" in L.vgn_version()
     assert L.vgn_compute_step_batch(None, 1, *([None] * 11), 0, None) == N.VGN_ERR_ARG
     assert b"null geometry" in L.vgn_last_error()
+
+
+CPP_PROGRAM = r"""
+#include <cstdio>
+#include "vgnav.hpp"
+int main() {
+  // world box (lv 0) holding one box daughter (lv 1); placement 0 = daughter, 1 = world
+  const int32_t lv_shape[2] = {VGN_BOX, VGN_BOX}, lv_off[2] = {0, 3};
+  const double params[6] = {100, 100, 100, 10, 20, 30};
+  const int32_t pv_lv[2] = {1, 0}, pv_mother[2] = {0, -1};
+  const double tr[24] = {5, 6, 7, 1, 0, 0, 0, 1, 0, 0, 0, 1,  0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+  vgn_geometry_desc d{2, lv_shape, lv_off, params, 6, 2, pv_lv, pv_mother, tr, 1};
+  vgnav::Geometry g(d, VGN_HOST_ONLY);
+  const uint32_t *tab = nullptr; size_t n = 0;
+  vgnav::check(vgn_geometry_navindex(g.get(), &tab, &n));
+  std::printf("%zu %u %u %zu %s\n", n, tab[2], tab[3], g.device_bytes(), vgn_version());
+  try {
+    vgnav::BVHNavigator nav(g);
+    double x = 0; vgn_state s{}; vgnav::SOA3D p{&x, &x, &x, 1}; vgnav::NavStatePool pool{&s, 1};
+    nav.LocatePoints(p, pool);
+  } catch (const vgnav::Error &e) { std::printf("error %d\n", e.code()); }
+  return 0;
+}
+"""
+
+
+def test_cpp_header_builds_and_links(vgnav, tmp_path):
+    """include/vgnav.hpp (the C++ host interface) compiles, links against libvgnav and runs on
+    a host-only geometry; the navigation table of world + one daughter has the reference layout."""
+    import subprocess
+
+    from helpers import ROOT
+
+    src = tmp_path / "t.cpp"
+    src.write_text(CPP_PROGRAM)
+    exe = tmp_path / "t"
+    libdir = ROOT / "vecgeom_gb300" / "lib"
+    subprocess.run(["g++", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-L", str(libdir), "-lvgnav",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    n, pv_world, word3, dev_bytes, ver = out[0].split(" ", 4)
+    assert "sm_103a" in ver
+    assert int(pv_world) == 1  # record of the world placement (id 1)
+    # world: 3 + 1 daughter + pad 0 = 4 words, pad to 8-byte boundary: (1 + 4) odd -> 1 pad word, 24 matrix words;
+    # daughter: 3 words + 1 pad + ... -> table of 1 + 29 + 28 = 58 words + 1 allocation word
+    assert int(n) == 59
+    assert int(word3) == (1 << 16) | (0x04 << 8) | 0  # world: level 0, matrix cached (identity), 1 daughter
+    assert int(dev_bytes) == 0
+    assert out[1] == f"error {1}"  # kernels refused on a host-only geometry (VGN_ERR_ARG)
+
+
+def test_c_header_is_plain_c(tmp_path):
+    import subprocess
+
+    from helpers import ROOT
+
+    src = tmp_path / "t.c"
+    src.write_text('#include "vgnav.h"\nint main(void) { vgn_state s; (void)s; return 0; }\n')
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
+                   check=True)

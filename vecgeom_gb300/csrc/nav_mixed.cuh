@@ -1,16 +1,33 @@
-// nav_mixed.cuh -- exact-decision mixed-precision BVH traversal.
+// nav_mixed.cuh -- mixed-precision BVH traversal with results bit-identical
+// to the all-FP64 traversal.
 //
-// GB300 executes FP64 at a small fraction of its FP32 rate.  The reference's
-// traversal spends most of its FP64 work on box tests whose only outcome is a
-// yes/no decision (visit a node, test a candidate, which child first).  Here
-// every such decision is first taken in FP32 interval arithmetic with directed
-// rounding (__fsub_rd, __fmul_ru, ...): the interval provably contains the
-// value the FP64 code would compute, so when it lies entirely on one side of
-// the threshold the FP64 decision is known.  Only when the interval straddles
-// the threshold is the quantity recomputed in FP64.  Distances that reach the
-// output (DistanceToIn/Out, SafetyToIn/Out, transforms) are always FP64.  The
-// result is therefore bit-identical to the all-FP64 traversal: same visit
-// order, same candidates, same tie-breaking.
+// GB300 executes FP64 at a small fraction of its FP32 rate, and a BVH
+// traversal in one thread per track leaves only a few lanes of each warp
+// active at a time.  Two measures keep the FP64 work small and coherent:
+//
+//  1. Every box test whose only outcome is a decision (visit a node, keep a
+//     candidate, which child first) runs in FP32 interval arithmetic with
+//     directed rounding (__fsub_rd, __fmul_ru, ...).  The interval provably
+//     contains the value the FP64 code would compute, so a decision is known
+//     whenever the interval lies on one side of the threshold; otherwise the
+//     quantity is recomputed in FP64.
+//  2. FP64 shape evaluations are taken out of the divergent traversal loop
+//     and run afterwards, where all lanes of a warp execute them together:
+//       step   -- the traversal collects the leaf candidates in visit order
+//                 (culling may be conservative: a candidate the FP64 code
+//                 would have culled lies beyond the step its box test used,
+//                 so it can never be accepted); the candidates are then
+//                 evaluated in that order with the reference's acceptance
+//                 rule.  The child order is always decided exactly, so the
+//                 candidate order -- and hence tie-breaking -- is the
+//                 reference's.
+//       safety -- the reference prunes with the running minimum, so the
+//                 pruning decisions must be exact.  Box daughters enter as
+//                 FP32-interval contenders; the running minimum is known as
+//                 an interval, resolved exactly (FP64) only when a decision
+//                 needs it and once at the end.
+// Distances that reach the output are always FP64 values computed by the
+// same code as the plain kernels.
 #pragma once
 
 #include "nav_device.cuh"
@@ -25,7 +42,24 @@ struct FI {
 // tri-state decisions
 enum : int { kNo = 0, kYes = 1, kMaybe = 2 };
 
-__device__ __forceinline__ FI fi(double x) { return FI{__double2float_rd(x), __double2float_ru(x)}; }
+// double -> float rounded toward -inf (up = false) or +inf (up = true), with
+// integer operations in the normal float range (the FP64 pipe stays free).
+__device__ __forceinline__ float d2f_dir(double x, bool up)
+{
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  if ((b << 1) == 0ull) return (float)x;  // +-0
+  const unsigned sign            = (unsigned)(b >> 63);
+  const int e                    = (int)((b >> 52) & 0x7ffull);
+  const int fe                   = e - 1023 + 127;
+  if (e == 0x7ff || fe <= 0 || fe >= 255) return up ? __double2float_ru(x) : __double2float_rd(x);
+  const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  unsigned bits                 = (sign << 31) | ((unsigned)fe << 23) | (unsigned)(mant >> 29);
+  const bool inexact            = (mant & 0x1FFFFFFFull) != 0ull;
+  if (inexact && (up ? sign == 0u : sign != 0u)) bits += 1u;  // away from zero in the rounding direction
+  return __uint_as_float(bits);
+}
+
+__device__ __forceinline__ FI fi(double x) { return FI{d2f_dir(x, false), d2f_dir(x, true)}; }
 __device__ __forceinline__ int fi_lt(FI a, FI b) { return a.hi < b.lo ? kYes : (a.lo >= b.hi ? kNo : kMaybe); }
 __device__ __forceinline__ int fi_le(FI a, FI b) { return a.hi <= b.lo ? kYes : (a.lo > b.hi ? kNo : kMaybe); }
 __device__ __forceinline__ int fi_ge0(FI a) { return a.lo >= 0.f ? kYes : (a.hi < 0.f ? kNo : kMaybe); }
@@ -72,15 +106,15 @@ struct MixedRay {
 
 __device__ __forceinline__ void make_ray(MixedRay &r, D3 lp, D3 ld)
 {
-  r.lp = lp;
-  r.ld = ld;
+  r.lp   = lp;
+  r.ld   = ld;
   r.p[0] = fi(lp.x);
   r.p[1] = fi(lp.y);
   r.p[2] = fi(lp.z);
   const double d[3] = {nonzero(ld.x), nonzero(ld.y), nonzero(ld.z)};  // Global.h:174-178
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const FI di = fi(d[k]);  // same sign at both ends: |d| >= 1e-30
+    const FI di = fi(d[k]);                                  // same sign at both ends: |d| >= 1e-30
     r.inv[k]    = FI{__frcp_rd(di.hi), __frcp_ru(di.lo)};  // 1/x decreases on each half line
     r.neg[k]    = di.hi < 0.f;
   }
@@ -96,9 +130,10 @@ __device__ __forceinline__ D3 ray_inv64(MixedRay &r)
   return r.inv64;
 }
 
-// Interval of AABB::ComputeIntersectionInvDir's (tmin, tmax).  The FP64 code's
-// swap leaves t(min side) <= t(max side) per axis; which side is "near" only
-// depends on the sign of the inverse direction, by monotonicity of rounding.
+// Interval of AABB::ComputeIntersectionInvDir's (tmin, tmax) (AABB.h:136-154).
+// The FP64 code's swap leaves t(min side) <= t(max side) per axis; which box
+// side is "near" only depends on the sign of the inverse direction, by
+// monotonicity of rounding.
 __device__ __forceinline__ void islab(const float *mn_lo, const float *mn_hi, const float *mx_lo, const float *mx_hi,
                                       const MixedRay &r, FI &tmin, FI &tmax)
 {
@@ -139,13 +174,14 @@ __device__ __forceinline__ FI isafety(const ISafe &s, const MixedRay &r)
   return m;
 }
 
-// Interval of a box daughter's SafetyToIn: placement transform then
-// BoxImplementation::SafetyToIn (BoxImplementation.h:153-158).
-__device__ __forceinline__ FI ibox_safety_in(const IXForm &x, const MixedRay &r)
+// Interval of max_k(|l_k| - h_k) for a box daughter, l = placement transform
+// of the point: BoxImplementation::SafetyToIn (BoxImplementation.h:153-158)
+// and the quantity BoxImplementation::Contains compares with 0.
+__device__ __forceinline__ FI ibox_safety_in(const IXForm &x, const FI *p)
 {
   FI t[3];
 #pragma unroll
-  for (int k = 0; k < 3; ++k) t[k] = fi_sub(r.p[k], FI{__ldg(&x.t_lo[k]), __ldg(&x.t_hi[k])});
+  for (int k = 0; k < 3; ++k) t[k] = fi_sub(p[k], FI{__ldg(&x.t_lo[k]), __ldg(&x.t_hi[k])});
   FI m;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -158,7 +194,31 @@ __device__ __forceinline__ FI ibox_safety_in(const IXForm &x, const MixedRay &r)
   return m;
 }
 
-// BVH::CheckDaughterIntersections (BVH.h:96-146) with interval decisions
+// ------------------------------------------------------------------ step
+constexpr int kMaxStepCand = 16;
+
+struct StepCands {
+  int n, head;
+  int pv[kMaxStepCand];
+  float tmin_lo[kMaxStepCand];
+};
+
+// Acceptance of one candidate, as in BVH.h:113-118; a candidate whose box is
+// entered at or beyond the current step cannot pass dist < step.
+__device__ __forceinline__ void eval_step_candidate(const GeomView &g, const MixedRay &r, int pv, float tmin_lo,
+                                                    double &step, FI &stepI, int last, int &hit)
+{
+  if (tmin_lo >= stepI.hi) return;
+  const double dist = pv_dist_in(g, pv, r.lp, r.ld);
+  if (dist < step && !(dist <= 0.0 && pv == last)) {
+    step  = dist;
+    hit   = pv;
+    stepI = fi(step);
+  }
+}
+
+// BVH::CheckDaughterIntersections (BVH.h:96-146): FP32 traversal collecting
+// candidates in visit order, then FP64 evaluation in that order.
 __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, const LVRec &lv, MixedRay &r,
                                                           double &step, int last, int &hit)
 {
@@ -166,10 +226,14 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
   int sp   = 1;
   stack[0] = 0;
   FI stepI = fi(step);
+  // Culling uses the step after the candidates evaluated so far: never below
+  // the step the FP64 traversal would hold at the same point.
+  StepCands c;
+  c.n = c.head = 0;
   const INodeSlab *inodes = g.inodes + lv.nodes_off;
   const IPrimSlab *iprims = g.iprims + lv.prims_off;
   const NodeRec *nodes    = g.nodes + lv.nodes_off;
-  const PrimRec *prims    = g.prims + lv.prims_off;
+  bool ok = true;
   do {
     const unsigned id = stack[--sp];
     const int nchild  = __ldg(&inodes[id].nchild);
@@ -179,65 +243,120 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
         const IPrimSlab &q = iprims[off + i];
         FI tmin, tmax;
         islab(q.mn_lo, q.mn_hi, q.mx_lo, q.mx_hi, r, tmin, tmax);
-        int dec = slab_decision(tmin, tmax, stepI);
-        if (dec == kMaybe) {
-          double a, b;
-          slab(prims[off + i].mn, prims[off + i].mx, r.lp, ray_inv64(r), a, b);
-          dec = (a <= b && b >= 0.0 && a < step) ? kYes : kNo;
+        if (slab_decision(tmin, tmax, stepI) == kNo) continue;
+        if (c.n == kMaxStepCand) {  // full: evaluate the oldest now (keeps the order)
+          eval_step_candidate(g, r, c.pv[c.head], c.tmin_lo[c.head], step, stepI, last, hit);
+          c.head = (c.head + 1) % kMaxStepCand;
+          --c.n;
         }
-        if (dec == kYes) {
-          const int vol     = __ldg(&q.pv);
-          const double dist = pv_dist_in(g, vol, r.lp, r.ld);
-          if (dist < step && !(dist <= 0.0 && vol == last)) {
-            step  = dist;
-            hit   = vol;
-            stepI = fi(step);
-          }
-        }
+        const int slot   = (c.head + c.n) % kMaxStepCand;
+        c.pv[slot]       = __ldg(&q.pv);
+        c.tmin_lo[slot]  = tmin.lo;
+        ++c.n;
       }
     } else {
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
       FI tminL, tmaxL, tminR, tmaxR;
       islab(inodes[L].mn_lo, inodes[L].mn_hi, inodes[L].mx_lo, inodes[L].mx_hi, r, tminL, tmaxL);
       islab(inodes[R].mn_lo, inodes[R].mn_hi, inodes[R].mx_lo, inodes[R].mx_hi, r, tminR, tmaxR);
-      int trL = slab_decision(tminL, tmaxL, stepI);
-      int trR = slab_decision(tminR, tmaxR, stepI);
-      int rfirst = fi_lt(tminR, tminL);
-      if (trL == kMaybe || trR == kMaybe || rfirst == kMaybe) {
-        const D3 inv = ray_inv64(r);
-        double a, b, c, d;
-        slab(nodes[L].mn, nodes[L].mx, r.lp, inv, a, b);
-        slab(nodes[R].mn, nodes[R].mx, r.lp, inv, c, d);
-        trL    = (a <= b && b >= 0.0 && a < step) ? kYes : kNo;
-        trR    = (c <= d && d >= 0.0 && c < step) ? kYes : kNo;
-        rfirst = c < a ? kYes : kNo;
+      const bool trL = slab_decision(tminL, tmaxL, stepI) != kNo;
+      const bool trR = slab_decision(tminR, tmaxR, stepI) != kNo;
+      int rfirst     = kNo;
+      if (trL && trR) {
+        rfirst = fi_lt(tminR, tminL);
+        if (rfirst == kMaybe) {  // the visit order must be the reference's: decide in FP64
+          const D3 inv = ray_inv64(r);
+          double a, b, cc, d;
+          slab(nodes[L].mn, nodes[L].mx, r.lp, inv, a, b);
+          slab(nodes[R].mn, nodes[R].mx, r.lp, inv, cc, d);
+          rfirst = cc < a ? kYes : kNo;
+        }
       }
       if (sp + 2 > kStackSize) {
         raise_error(g, kErrStack);
-        return false;
+        ok = false;
+        break;
       }
       if (rfirst == kYes) {
-        if (trR == kYes) stack[sp++] = R;
-        if (trL == kYes) stack[sp++] = L;
+        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
       } else {
-        if (trL == kYes) stack[sp++] = L;
-        if (trR == kYes) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = R;
       }
     }
   } while (sp > 0);
-  return true;
+  // FP64 phase: the lanes of a warp evaluate their candidates together
+  for (int k = 0; k < c.n; ++k) {
+    const int slot = (c.head + k) % kMaxStepCand;
+    eval_step_candidate(g, r, c.pv[slot], c.tmin_lo[slot], step, stepI, last, hit);
+  }
+  return ok;
 }
 
-// BVH::ComputeSafety (BVH.h:172-209) with interval decisions; a box daughter
-// whose SafetyToIn interval cannot go below the current safety is skipped
-// without any FP64 work (it would not change the result either way).
+// ------------------------------------------------------------------ safety
+constexpr int kMaxSafeCand = 8;
+
+// Running minimum of BVH::ComputeSafety known as: an exact part `known`
+// (mother safety and daughters evaluated in FP64) and pending box daughters
+// whose SafetyToIn is known as an FP32 interval.
+struct SafeRun {
+  double known;
+  FI knownI;
+  int n;
+  int pv[kMaxSafeCand];
+  float lo[kMaxSafeCand], hi[kMaxSafeCand];
+  FI cur;  // interval of the current running minimum
+};
+
+__device__ __forceinline__ void saferun_update(SafeRun &s)
+{
+  FI c = s.knownI;
+  for (int k = 0; k < s.n; ++k) c = FI{fminf(c.lo, s.lo[k]), fminf(c.hi, s.hi[k])};
+  s.cur = c;
+}
+
+// evaluate all pending daughters in FP64: the running minimum becomes exact
+__device__ __forceinline__ void saferun_resolve(const GeomView &g, const MixedRay &r, SafeRun &s)
+{
+  for (int k = 0; k < s.n; ++k) {
+    if (s.lo[k] >= s.cur.hi) continue;  // cannot be the minimum
+    const double d = pv_safe_in(g, s.pv[k], r.lp);
+    if (d < s.known) s.known = d;
+  }
+  s.n      = 0;
+  s.knownI = fi(s.known);
+  s.cur    = s.knownI;
+}
+
+// decision x < (running minimum), resolving the minimum when the intervals overlap;
+// `exact` is the FP64 value of x (computed only if still needed)
+template <typename ExactFn>
+__device__ __forceinline__ bool saferun_less(const GeomView &g, const MixedRay &r, SafeRun &s, FI x, ExactFn exact)
+{
+  int dec = fi_lt(x, s.cur);
+  if (dec != kMaybe) return dec == kYes;
+  if (s.n > 0) {
+    saferun_resolve(g, r, s);
+    dec = fi_lt(x, s.cur);
+    if (dec != kMaybe) return dec == kYes;
+  }
+  return exact() < s.known;
+}
+
+// BVH::ComputeSafety (BVH.h:172-209) with exact pruning decisions and
+// deferred FP64 evaluation of box daughters.
 __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRec &lv, const MixedRay &r,
                                                    double safety)
 {
   unsigned stack[kStackSize];
   int sp   = 1;
   stack[0] = 0;
-  FI safI  = fi(safety);
+  SafeRun s;
+  s.known  = safety;
+  s.knownI = fi(safety);
+  s.n      = 0;
+  s.cur    = s.knownI;
   const INodeSlab *inodes = g.inodes + lv.nodes_off;
   const ISafe *isafe_n    = g.inode_safe + lv.nodes_off;
   const ISafe *isafe_p    = g.iprim_safe + lv.prims_off;
@@ -250,47 +369,63 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
     if (nchild >= 0) {
       const int off = __ldg(&inodes[id].offset);
       for (int i = 0; i < nchild; ++i) {
-        const int vol = __ldg(&iprims[off + i].pv);
+        const int vol   = __ldg(&iprims[off + i].pv);
         const IXForm &x = g.ixf[vol];
-        if (__ldg(&x.shape) == kBox && fi_lt(ibox_safety_in(x, r), safI) == kNo) continue;
-        int dec = fi_lt(isafety(isafe_p[off + i], r), safI);
-        if (dec == kMaybe) dec = box_safety(prims[off + i].mn, prims[off + i].mx, r.lp) < safety ? kYes : kNo;
-        if (dec == kYes) {
+        const bool box  = __ldg(&x.shape) == kBox;
+        FI d{0.f, 0.f};
+        if (box) {
+          d = ibox_safety_in(x, r.p);
+          if (d.lo >= s.cur.hi) continue;  // SafetyToIn >= running minimum: no update either way
+        }
+        const PrimRec &pr = prims[off + i];
+        if (!saferun_less(g, r, s, isafety(isafe_p[off + i], r), [&] { return box_safety(pr.mn, pr.mx, r.lp); }))
+          continue;
+        if (box) {
+          if (s.n == kMaxSafeCand) saferun_resolve(g, r, s);
+          s.pv[s.n] = vol;
+          s.lo[s.n] = d.lo;
+          s.hi[s.n] = d.hi;
+          ++s.n;
+          saferun_update(s);
+        } else {
           const double dist = pv_safe_in(g, vol, r.lp);
-          if (dist < safety) {
-            safety = dist;
-            safI   = fi(safety);
+          if (dist < s.known) {
+            s.known  = dist;
+            s.knownI = fi(dist);
           }
+          saferun_update(s);
         }
       }
     } else {
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
       const FI sL = isafety(isafe_n[L], r);
       const FI sR = isafety(isafe_n[R], r);
-      int trL = fi_lt(sL, safI), trR = fi_lt(sR, safI), rfirst = fi_lt(sR, sL);
-      if (trL == kMaybe || trR == kMaybe || rfirst == kMaybe) {
-        const double a = box_safety(nodes[L].mn, nodes[L].mx, r.lp);
-        const double b = box_safety(nodes[R].mn, nodes[R].mx, r.lp);
-        trL    = a < safety ? kYes : kNo;
-        trR    = b < safety ? kYes : kNo;
-        rfirst = b < a ? kYes : kNo;
+      const bool trL = saferun_less(g, r, s, sL, [&] { return box_safety(nodes[L].mn, nodes[L].mx, r.lp); });
+      const bool trR = saferun_less(g, r, s, sR, [&] { return box_safety(nodes[R].mn, nodes[R].mx, r.lp); });
+      bool rfirst    = false;
+      if (trL && trR) {
+        const int o = fi_lt(sR, sL);
+        rfirst = o == kMaybe ? box_safety(nodes[R].mn, nodes[R].mx, r.lp) < box_safety(nodes[L].mn, nodes[L].mx, r.lp)
+                             : o == kYes;
       }
       if (sp + 2 > kStackSize) {
         raise_error(g, kErrStack);
-        return safety;
+        break;
       }
-      if (rfirst == kYes) {
-        if (trR == kYes) stack[sp++] = R;
-        if (trL == kYes) stack[sp++] = L;
+      if (rfirst) {
+        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
       } else {
-        if (trL == kYes) stack[sp++] = L;
-        if (trR == kYes) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = R;
       }
     }
   } while (sp > 0);
-  return safety;
+  if (s.n > 0) saferun_resolve(g, r, s);  // FP64 phase, coherent across the warp
+  return s.known;
 }
 
+// ------------------------------------------------------------------ locate
 // p >= mn && p <= mx per axis (AABB::Contains, AABB.h:69-72) as a tri-state
 __device__ __forceinline__ int icontains(const float *mn_lo, const float *mn_hi, const float *mx_lo,
                                          const float *mx_hi, const FI *p)
@@ -328,12 +463,15 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
         const IPrimSlab &q = iprims[off + i];
         int dec = icontains(q.mn_lo, q.mn_hi, q.mx_lo, q.mx_hi, p);
         if (dec == kMaybe) dec = box_contains_pt(prims[off + i].mn, prims[off + i].mx, lp) ? kYes : kNo;
-        if (dec == kYes) {
-          const int vol = __ldg(&q.pv);
-          if (vol != excl && pv_contains(g, vol, lp, dlp)) {
-            pvol = vol;
-            return true;
-          }
+        if (dec != kYes) continue;
+        const int vol = __ldg(&q.pv);
+        if (vol == excl) continue;
+        const IXForm &x = g.ixf[vol];
+        // a box daughter surely not containing the point needs no FP64 test
+        if (__ldg(&x.shape) == kBox && fi_ge0(ibox_safety_in(x, p)) == kYes) continue;
+        if (pv_contains(g, vol, lp, dlp)) {
+          pvol = vol;
+          return true;
         }
       }
     } else {
