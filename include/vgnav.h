@@ -148,6 +148,24 @@ int vgn_shape_batch(const vgn_geometry *geom, int32_t lv, int32_t op, int64_t n,
                     const double *pz, const double *dx, const double *dy, const double *dz, const double *step_max,
                     double *out, int flags, void *stream);
 
+/* Launch configuration of the step kernel for one precision form (flags &
+ * VGN_PRECISION_MIXED): `variant` picks the threads-per-block / register-cap
+ * variant, `sort_kbits` (0..6) bins tracks by direction octant and a
+ * 2^k-per-axis cell of the world box before the step, for warp coherence
+ * (0 = no binning).  Only performance changes, never a result.  Binning uses
+ * a per-geometry device scratch (12 bytes per track plus the histogram):
+ * binned calls on different streams must not overlap.  No counterpart in the
+ * reference, which launches 256 threads per block (backend/cuda/Backend.h:50-96). */
+int vgn_set_step_config(vgn_geometry *geom, int flags, int32_t variant, int32_t sort_kbits);
+int vgn_get_step_config(const vgn_geometry *geom, int flags, int32_t *variant, int32_t *sort_kbits);
+/* Autotuner: times every (variant, sort_kbits) pair on the given batch (device
+ * pointers; outputs are overwritten), keeps the fastest for this precision
+ * form and returns it with its time per batch. */
+int vgn_autotune_step(vgn_geometry *geom, int64_t n, const double *px, const double *py, const double *pz,
+                      const double *dx, const double *dy, const double *dz, const double *step_limit,
+                      const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream,
+                      int32_t *variant, int32_t *sort_kbits, float *best_ms);
+
 /* Wait for the work of the previous calls on `stream`; returns the first
  * device-side error status recorded by a kernel since the last call. */
 int vgn_synchronize(const vgn_geometry *geom, void *stream);

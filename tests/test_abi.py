@@ -87,3 +87,27 @@ def test_c_header_is_plain_c(tmp_path):
     src.write_text('#include "vgnav.h"\nint main(void) { vgn_state s; (void)s; return 0; }\n')
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
                    check=True)
+
+
+def test_step_config_host_logic(vgnav):
+    """Launch configuration setters/getters and their argument checks (host-only geometry, no kernel)."""
+    from helpers import HostTables
+    from vecgeom_gb300 import workloads as W
+
+    h = HostTables(W.box_grid_geometry(seed=7, n=5).desc)
+    L = N.lib()
+    v, k = C.c_int32(-1), C.c_int32(-1)
+    for mixed in (0, N.VGN_PRECISION_MIXED):
+        assert L.vgn_get_step_config(h.h, mixed, C.byref(v), C.byref(k)) == N.VGN_OK
+        assert (v.value, k.value) == (0, 0)
+    assert L.vgn_set_step_config(h.h, N.VGN_PRECISION_MIXED, 2, 4) == N.VGN_OK
+    L.vgn_get_step_config(h.h, N.VGN_PRECISION_MIXED, C.byref(v), C.byref(k))
+    assert (v.value, k.value) == (2, 4)
+    L.vgn_get_step_config(h.h, 0, C.byref(v), C.byref(k))
+    assert (v.value, k.value) == (0, 0)  # forms are configured independently
+    assert L.vgn_set_step_config(h.h, 0, 99, 0) == N.VGN_ERR_ARG
+    assert L.vgn_set_step_config(h.h, 0, 0, -1) == N.VGN_ERR_ARG
+    assert L.vgn_set_step_config(h.h, 0, 0, 7) == N.VGN_ERR_ARG
+    assert L.vgn_set_step_config(None, 0, 0, 0) == N.VGN_ERR_ARG
+    # the autotuner needs a device geometry
+    assert L.vgn_autotune_step(h.h, 1, *([None] * 11), 0, None, None, None, None) == N.VGN_ERR_ARG

@@ -213,3 +213,51 @@ def test_edge_cases(oracle, vgnav, cuda):
     t.states["nav_ind"] = 1
     geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit, vgnav.NavStatePool(t.states),
              vgnav.NavStatePool(out), np.zeros(t.n))
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_launch_configs_bit_exact(oracle, vgnav, cuda, mixed):
+    """Every launch variant, with and without track binning, gives the oracle's results."""
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid, n=100003, seed_points=71, seed_dirs=72)
+    ref = og.step(t, calcsafety=True)
+    n_variants = 4
+    for variant in range(n_variants):
+        for kbits in (0, 1, 3, 5, 6):
+            geo.set_step_config(variant, kbits, mixed=mixed)
+            assert geo.step_config(mixed=mixed) == (variant, kbits)
+            got = gpu_step(cuda, geo, t, mixed=mixed)
+            assert np.array_equal(got["step"], ref["step"]), (variant, kbits)
+            assert np.array_equal(got["safety"], ref["safety"]), (variant, kbits)
+            assert np.array_equal(got["out"], ref["out"]), (variant, kbits)
+    with pytest.raises(N.VgnError):
+        geo.set_step_config(n_variants, 0, mixed=mixed)
+    with pytest.raises(N.VgnError):
+        geo.set_step_config(0, 7, mixed=mixed)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_autotune_then_step(oracle, vgnav, cuda, mixed):
+    """The autotuner keeps a valid configuration; later steps stay bit-exact."""
+    from vecgeom_gb300.navigator import SOA3D, NavStatePool
+
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid, n=1 << 17, seed_points=73, seed_dirs=74)
+    pts = SOA3D(to_dev(cuda, t.x), to_dev(cuda, t.y), to_dev(cuda, t.z))
+    dirs = SOA3D(to_dev(cuda, t.dx), to_dev(cuda, t.dy), to_dev(cuda, t.dz))
+    inp = NavStatePool(states_to_dev(cuda, t.states))
+    out = NavStatePool.empty_like(inp)
+    steps = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
+    saf = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
+    v, k, ms = geo.autotune_step(pts, dirs, to_dev(cuda, t.step_limit), inp, out, steps, saf, mixed=mixed)
+    assert 0 <= v < 4 and k in (0, 3, 4, 5) and ms > 0
+    assert geo.step_config(mixed=mixed) == (v, k)
+    ref = og.step(t, calcsafety=True)
+    got = gpu_step(cuda, geo, t, mixed=mixed)
+    assert np.array_equal(got["step"], ref["step"])
+    assert np.array_equal(got["safety"], ref["safety"])
+    assert np.array_equal(got["out"], ref["out"])

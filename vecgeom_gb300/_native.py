@@ -39,6 +39,9 @@ EXPORTED = [
     "vgn_compute_safety_batch",
     "vgn_locate_batch",
     "vgn_shape_batch",
+    "vgn_set_step_config",
+    "vgn_get_step_config",
+    "vgn_autotune_step",
     "vgn_synchronize",
     "vgn_last_error",
     "vgn_version",
@@ -94,6 +97,10 @@ def lib() -> C.CDLL:
         L.vgn_compute_safety_batch.argtypes = [vp, i64, p, p, p, p, p, C.c_int, vp]
         L.vgn_locate_batch.argtypes = [vp, i64, p, p, p, p, C.c_int, vp]
         L.vgn_shape_batch.argtypes = [vp, i32, i32, i64, p, p, p, p, p, p, p, p, C.c_int, vp]
+        L.vgn_set_step_config.argtypes = [vp, C.c_int, i32, i32]
+        L.vgn_get_step_config.argtypes = [vp, C.c_int, C.POINTER(i32), C.POINTER(i32)]
+        L.vgn_autotune_step.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, p, p, C.c_int, vp,
+                                        C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)]
         L.vgn_synchronize.argtypes = [vp, vp]
         L.vgn_last_error.restype = C.c_char_p
         L.vgn_version.restype = C.c_char_p

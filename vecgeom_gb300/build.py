@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # (source, extra nvcc flags)
 UNITS = [
     ("kernels_nav.cu", ["-fmad=false"]),
+    ("kernels_sort.cu", []),
     ("host_geometry.cpp", []),
     ("host_shapes.cpp", []),
     ("vgnav_api.cpp", []),

@@ -32,16 +32,18 @@ __device__ __forceinline__ void store_state(vgn_state *s, int64_t i, const State
   w[2]        = st.on_boundary & 0xffu;
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(256) step_kernel(GeomView g, int64_t n, const double *__restrict__ px,
+template <bool MIXED, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) step_kernel(GeomView g, int64_t n, const double *__restrict__ px,
                                                    const double *__restrict__ py, const double *__restrict__ pz,
                                                    const double *__restrict__ dx, const double *__restrict__ dy,
                                                    const double *__restrict__ dz, const double *__restrict__ slimit,
                                                    const vgn_state *__restrict__ in, vgn_state *__restrict__ out,
-                                                   double *__restrict__ step, double *__restrict__ safety, int reloc)
+                                                   double *__restrict__ step, double *__restrict__ safety, int reloc,
+                                                   const uint32_t *__restrict__ perm)
 {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const State s = load_state(in, i);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm ? (int64_t)__ldg(perm + t) : t;  // binned visit order, results stay at index i
+    const State s   = load_state(in, i);
     State o       = s;
     double sf = 0., st;
     if (!ni_valid(g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(g, s.last_exited))) {
@@ -127,16 +129,42 @@ static inline unsigned grid_for(int64_t n, int block, int max_blocks)
   return (unsigned)b;
 }
 
-cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s)
+// Launch-shape variants of the step kernel (threads per block, minimum
+// resident blocks per SM -> register cap); the autotuner picks one per geometry.
+struct StepVariant {
+  int block, minb;
+};
+static constexpr StepVariant kStepVariants[] = {{256, 2}, {256, 3}, {128, 6}, {256, 4}};
+static constexpr int kNumStepVariants        = sizeof(kStepVariants) / sizeof(kStepVariants[0]);
+
+int step_variant_count() { return kNumStepVariants; }
+
+template <bool MIXED, int BLOCK, int MINB>
+static void launch_step_v(const GeomView &g, const StepArgs &a, cudaStream_t s)
 {
-  const int block     = 256;
-  const unsigned grid = grid_for(a.n, block, a.max_blocks);
+  // grid-stride over tracks; enough blocks to fill every SM several times over
+  const unsigned grid = grid_for(a.n, BLOCK, a.max_blocks * (256 / BLOCK));
+  dev::step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit,
+                                                              a.in, a.out, a.step, a.safety, a.reloc, a.perm);
+}
+
+template <bool MIXED>
+static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cudaStream_t s)
+{
+  switch (variant) {
+  case 1: launch_step_v<MIXED, 256, 3>(g, a, s); break;
+  case 2: launch_step_v<MIXED, 128, 6>(g, a, s); break;
+  case 3: launch_step_v<MIXED, 256, 4>(g, a, s); break;
+  default: launch_step_v<MIXED, 256, 2>(g, a, s); break;
+  }
+}
+
+cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s)
+{
   if (mixed)
-    dev::step_kernel<true><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit, a.in, a.out,
-                                                  a.step, a.safety, a.reloc);
+    launch_step_m<true>(g, a, variant, s);
   else
-    dev::step_kernel<false><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit, a.in,
-                                                   a.out, a.step, a.safety, a.reloc);
+    launch_step_m<false>(g, a, variant, s);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,103 @@
+// kernels_sort.cu -- track binning for warp coherence.
+//
+// A one-thread-per-track BVH traversal wastes most of every warp when the 32
+// tracks of a warp start at unrelated positions and go in unrelated
+// directions.  Before a step, tracks are counting-sorted by
+//     key = direction octant (3 bits) | Morton order of a 2^k-per-axis cell
+//           of the world bounding box (3k bits)
+// and the step kernel visits them through the resulting permutation.  Each
+// track's result is written back at its own index, so the order only changes
+// which tracks share a warp, never any result.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "launch.h"
+
+namespace vgn {
+namespace dev {
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v)  // 10 bits -> every third bit
+{
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void __launch_bounds__(256) bin_keys_kernel(int64_t n, const double *__restrict__ px,
+                                                       const double *__restrict__ py, const double *__restrict__ pz,
+                                                       const double *__restrict__ dx, const double *__restrict__ dy,
+                                                       const double *__restrict__ dz, BinParams b,
+                                                       uint32_t *__restrict__ keys, uint32_t *__restrict__ hist)
+{
+  const uint32_t cmax = (1u << b.kbits) - 1u;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float fx = ((float)px[i] - b.lo[0]) * b.scale[0];
+    const float fy = ((float)py[i] - b.lo[1]) * b.scale[1];
+    const float fz = ((float)pz[i] - b.lo[2]) * b.scale[2];
+    const uint32_t cx = (uint32_t)fminf(fmaxf(fx, 0.f), (float)cmax);
+    const uint32_t cy = (uint32_t)fminf(fmaxf(fy, 0.f), (float)cmax);
+    const uint32_t cz = (uint32_t)fminf(fmaxf(fz, 0.f), (float)cmax);
+    const uint32_t oct = (dx[i] > 0.0 ? 4u : 0u) | (dy[i] > 0.0 ? 2u : 0u) | (dz[i] > 0.0 ? 1u : 0u);
+    const uint32_t key = (oct << (3 * b.kbits)) | (spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz);
+    keys[i]            = key;
+    atomicAdd(hist + key, 1u);
+  }
+}
+
+// exclusive scan of the histogram in place (one block)
+__global__ void __launch_bounds__(1024) scan_kernel(uint32_t *hist, uint32_t nbins)
+{
+  __shared__ uint32_t part[1024];
+  const uint32_t t     = threadIdx.x;
+  const uint32_t chunk = (nbins + 1023u) / 1024u;
+  const uint32_t beg = t * chunk, end = min(beg + chunk, nbins);
+  uint32_t s = 0;
+  for (uint32_t k = beg; k < end; ++k) s += hist[k];
+  part[t] = s;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024u; off <<= 1) {  // inclusive Hillis-Steele scan of the partial sums
+    const uint32_t v = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - s;
+  for (uint32_t k = beg; k < end; ++k) {
+    const uint32_t h = hist[k];
+    hist[k]          = run;
+    run += h;
+  }
+}
+
+__global__ void __launch_bounds__(256) scatter_kernel(int64_t n, const uint32_t *__restrict__ keys,
+                                                      uint32_t *__restrict__ cursor, uint32_t *__restrict__ perm)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    perm[atomicAdd(cursor + keys[i], 1u)] = (uint32_t)i;
+}
+
+}  // namespace dev
+
+size_t bin_scratch_words(int64_t n, int kbits) { return 2 * (size_t)n + ((size_t)8 << (3 * kbits)); }
+
+cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, const double *pz, const double *dx,
+                              const double *dy, const double *dz, const BinParams &b, uint32_t *scratch,
+                              uint32_t *perm, int max_blocks, cudaStream_t s)
+{
+  const uint32_t nbins = 8u << (3 * b.kbits);
+  uint32_t *keys = scratch, *hist = scratch + n;
+  cudaError_t e  = cudaMemsetAsync(hist, 0, nbins * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > max_blocks) blocks = max_blocks;
+  if (blocks < 1) blocks = 1;
+  dev::bin_keys_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, px, py, pz, dx, dy, dz, b, keys, hist);
+  dev::scan_kernel<<<1, 1024, 0, s>>>(hist, nbins);
+  dev::scatter_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, keys, hist, perm);
+  return cudaGetLastError();
+}
+
+}  // namespace vgn

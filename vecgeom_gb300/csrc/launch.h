@@ -18,10 +18,23 @@ struct StepArgs {
   double *step, *safety;
   int reloc;
   int max_blocks;
+  const uint32_t *perm;  // optional visit order (track binning), nullptr = identity
 };
 
+// track binning (kernels_sort.cu)
+struct BinParams {
+  float lo[3];     // world bounding box corner
+  float scale[3];  // cells per mm along each axis
+  int kbits;       // 2^kbits cells per axis, 1..6
+};
+size_t bin_scratch_words(int64_t n, int kbits);  // keys + histogram (perm not included)
+cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, const double *pz, const double *dx,
+                              const double *dy, const double *dz, const BinParams &b, uint32_t *scratch,
+                              uint32_t *perm, int max_blocks, cudaStream_t s);
+
 // navigation kernels (kernels_nav.cu); mixed = FP32-interval box decisions
-cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s);
+cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s);
+int step_variant_count();
 cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
                           const vgn_state *in, double *safety, bool mixed, int max_blocks, cudaStream_t s);
 cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,

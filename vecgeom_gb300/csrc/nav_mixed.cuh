@@ -369,6 +369,10 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
     if (nchild >= 0) {
       const int off = __ldg(&inodes[id].offset);
       for (int i = 0; i < nchild; ++i) {
+        // cheapest test first: the primitive's box safety against the running minimum
+        const FI sbox = isafety(isafe_p[off + i], r);
+        const int pre = fi_lt(sbox, s.cur);
+        if (pre == kNo) continue;
         const int vol   = __ldg(&iprims[off + i].pv);
         const IXForm &x = g.ixf[vol];
         const bool box  = __ldg(&x.shape) == kBox;
@@ -378,8 +382,7 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
           if (d.lo >= s.cur.hi) continue;  // SafetyToIn >= running minimum: no update either way
         }
         const PrimRec &pr = prims[off + i];
-        if (!saferun_less(g, r, s, isafety(isafe_p[off + i], r), [&] { return box_safety(pr.mn, pr.mx, r.lp); }))
-          continue;
+        if (pre == kMaybe && !saferun_less(g, r, s, sbox, [&] { return box_safety(pr.mn, pr.mx, r.lp); })) continue;
         if (box) {
           if (s.n == kMaxSafeCand) saferun_resolve(g, r, s);
           s.pv[s.n] = vol;

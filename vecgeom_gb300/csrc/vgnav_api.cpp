@@ -29,6 +29,15 @@ struct vgn_geometry {
   std::mutex ws_mutex;
   void *d_ws      = nullptr;
   size_t ws_bytes = 0;
+  // step launch configuration per precision form (0 = FP64, 1 = mixed):
+  // kernel launch-shape variant and track-binning granularity (0 = no binning)
+  int step_variant[2] = {0, 0};
+  int sort_kbits[2]   = {0, 0};
+  vgn::BinParams bin{};
+  // track-binning scratch (keys, histogram, permutation), grown on demand
+  std::mutex sort_mutex;
+  uint32_t *d_sort  = nullptr;
+  size_t sort_words = 0;
 };
 
 namespace {
@@ -134,6 +143,40 @@ void *workspace(vgn_geometry *g, size_t bytes)
 
 int max_blocks(const vgn_geometry *g) { return g->num_sms > 0 ? g->num_sms * 32 : 4096; }
 
+// Enqueue one step batch with the geometry's launch configuration: optional
+// track binning (counting sort into a visit permutation), then the step kernel.
+int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s)
+{
+  const int m     = mixed ? 1 : 0;
+  const int kbits = g->sort_kbits[m];
+  a.perm          = nullptr;
+  if (kbits > 0 && a.n <= (int64_t)UINT32_MAX) {  // the visit permutation holds 32-bit track indices
+    std::lock_guard<std::mutex> lock(g->sort_mutex);
+    const size_t need = vgn::bin_scratch_words(a.n, kbits) + (size_t)a.n;
+    if (need > g->sort_words) {
+      if (g->d_sort) cudaFree(g->d_sort);
+      g->d_sort     = nullptr;
+      g->sort_words = 0;
+      if (cudaMalloc(&g->d_sort, need * sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        g->d_sort = nullptr;
+        return fail(VGN_ERR_NOMEM, "track-binning scratch allocation failed");
+      }
+      g->sort_words = need;
+    }
+    vgn::BinParams b = g->bin;
+    b.kbits          = kbits;
+    for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
+    uint32_t *perm   = g->d_sort + vgn::bin_scratch_words(a.n, kbits);
+    cudaError_t e    = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, g->d_sort, perm,
+                                              max_blocks(g), s);
+    if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+    a.perm = perm;
+  }
+  cudaError_t e = vgn::launch_step(g->view, a, mixed, g->step_variant[m], s);
+  return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
+}
+
 // bump allocator over the staging workspace (256-byte aligned sub-buffers)
 struct Carve {
   char *base;
@@ -215,6 +258,16 @@ int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry 
   v.n_lv         = (int32_t)h.lv.size();
   v.world_pv     = h.world_pv;
   v.max_depth    = h.max_depth;
+  {  // world bounding box for track binning
+    const vgn::HostLV &wl = h.lv[h.pv[h.world_pv].lv];
+    vgn::Vec3 mn, mx;
+    vgn::shape_extent(wl.shape, &h.shape[wl.shape_row], mn, mx);
+    const double lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+    for (int k = 0; k < 3; ++k) {
+      g->bin.lo[k]    = (float)lo[k];
+      g->bin.scale[k] = hi[k] > lo[k] ? (float)(1.0 / (hi[k] - lo[k])) : 0.f;
+    }
+  }
   e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
     vgn_geometry_free(g);
@@ -232,6 +285,7 @@ int vgn_geometry_free(vgn_geometry *g)
     for (void *p : g->allocations) cudaFree(p);
     if (g->d_status) cudaFree(g->d_status);
     if (g->d_ws) cudaFree(g->d_ws);
+    if (g->d_sort) cudaFree(g->d_sort);
   }
   delete g;
   return VGN_OK;
@@ -302,8 +356,7 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
   if (kind == 1) {
     a.px = px; a.py = py; a.pz = pz; a.dx = dx; a.dy = dy; a.dz = dz; a.slimit = step_limit;
     a.in = in; a.out = out; a.step = step; a.safety = safety;
-    cudaError_t e = vgn::launch_step(g->view, a, mixed, s);
-    return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
+    return enqueue_step(g, a, mixed, s);
   }
   // host buffers: stage through the device workspace
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -323,8 +376,8 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   a.px = b[0]; a.py = b[1]; a.pz = b[2]; a.dx = b[3]; a.dy = b[4]; a.dz = b[5]; a.slimit = b[6];
   a.in = din; a.out = dout; a.step = dstep; a.safety = safety ? dsaf : nullptr;
-  e = vgn::launch_step(g->view, a, mixed, s);
-  if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+  const int rc = enqueue_step(g, a, mixed, s);
+  if (rc != VGN_OK) return rc;
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(step, dstep, nd, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && safety) e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, s);
@@ -456,6 +509,80 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   if (e != cudaSuccess) return cuda_fail(e, "shape kernel launch");
   e = cudaMemcpyAsync(out, dout, nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
+int vgn_set_step_config(vgn_geometry *g, int flags, int32_t variant, int32_t sort_kbits)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (variant < 0 || variant >= vgn::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
+  if (sort_kbits < 0 || sort_kbits > 6) return fail(VGN_ERR_ARG, "track-binning granularity must be 0..6");
+  const int m        = (flags & VGN_PRECISION_MIXED) ? 1 : 0;
+  g->step_variant[m] = variant;
+  g->sort_kbits[m]   = sort_kbits;
+  return VGN_OK;
+}
+
+int vgn_get_step_config(const vgn_geometry *g, int flags, int32_t *variant, int32_t *sort_kbits)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  const int m = (flags & VGN_PRECISION_MIXED) ? 1 : 0;
+  if (variant) *variant = g->step_variant[m];
+  if (sort_kbits) *sort_kbits = g->sort_kbits[m];
+  return VGN_OK;
+}
+
+int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double *py, const double *pz,
+                      const double *dx, const double *dy, const double *dz, const double *step_limit,
+                      const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream,
+                      int32_t *variant, int32_t *sort_kbits, float *best_ms)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n <= 0) return fail(VGN_ERR_ARG, "autotuning needs a non-empty batch");
+  DeviceGuard guard(g->device);
+  if (classify({px, py, pz, dx, dy, dz, step_limit, in, out, step, safety}) != 1)
+    return fail(VGN_ERR_ARG, "autotuning needs device pointers");
+  const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
+  const int m      = mixed ? 1 : 0;
+  cudaStream_t s   = static_cast<cudaStream_t>(stream);
+  vgn::StepArgs a{};
+  a.n = n; a.px = px; a.py = py; a.pz = pz; a.dx = dx; a.dy = dy; a.dz = dz; a.slimit = step_limit;
+  a.in = in; a.out = out; a.step = step; a.safety = safety;
+  a.reloc      = (flags & VGN_NO_RELOCATE) ? 0 : 1;
+  a.max_blocks = max_blocks(g);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  static const int kSort[] = {0, 3, 4, 5};
+  float best = 3.4e38f;
+  int bv = 0, bk = 0, rc = VGN_OK;
+  for (int v = 0; v < vgn::step_variant_count() && rc == VGN_OK; ++v) {
+    for (int k : kSort) {
+      g->step_variant[m] = v;
+      g->sort_kbits[m]   = k;
+      if ((rc = enqueue_step(g, a, mixed, s)) != VGN_OK) break;  // warm-up
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 2 && rc == VGN_OK; ++r) rc = enqueue_step(g, a, mixed, s);
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = cuda_fail(cudaGetLastError(), "autotune timing");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms *= 0.5f;
+      if (ms < best) best = ms, bv = v, bk = k;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g->step_variant[m] = bv;
+  g->sort_kbits[m]   = bk;
+  if (rc != VGN_OK) return rc;
+  if (variant) *variant = bv;
+  if (sort_kbits) *sort_kbits = bk;
+  if (best_ms) *best_ms = best;
   return check_status(g, s);
 }
 

@@ -173,6 +173,28 @@ class Geometry:
         N.check(N.lib().vgn_shape_batch(self.handle, lv, op, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z), dx,
                                         dy, dz, None, _ptr(out), 0, _stream_ptr(stream)))
 
+    # ---- step-kernel launch configuration ---------------------------------
+    def set_step_config(self, variant: int, sort_kbits: int, mixed: bool = False):
+        N.check(N.lib().vgn_set_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, variant, sort_kbits))
+
+    def step_config(self, mixed: bool = False) -> tuple[int, int]:
+        v, k = C.c_int32(), C.c_int32()
+        N.check(N.lib().vgn_get_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, C.byref(v),
+                                            C.byref(k)))
+        return v.value, k.value
+
+    def autotune_step(self, pts: SOA3D, dirs: SOA3D, step_limit, in_states: NavStatePool, out_states: NavStatePool,
+                      steps, safeties=None, mixed: bool = False, relocate: bool = True, stream=None):
+        """Time every launch configuration on this (device-resident) batch, keep the fastest.
+        Returns (variant, sort_kbits, ms per batch)."""
+        flags = (N.VGN_PRECISION_MIXED if mixed else 0) | (0 if relocate else N.VGN_NO_RELOCATE)
+        v, k, ms = C.c_int32(), C.c_int32(), C.c_float()
+        N.check(N.lib().vgn_autotune_step(self.handle, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z),
+                                          _ptr(dirs.x), _ptr(dirs.y), _ptr(dirs.z), _ptr(step_limit),
+                                          _ptr(in_states.data), _ptr(out_states.data), _ptr(steps), _ptr(safeties),
+                                          flags, _stream_ptr(stream), C.byref(v), C.byref(k), C.byref(ms)))
+        return v.value, k.value, ms.value
+
     def synchronize(self, stream=None):
         N.check(N.lib().vgn_synchronize(self.handle, _stream_ptr(stream)))
 
