@@ -166,6 +166,31 @@ int vgn_autotune_step(vgn_geometry *geom, int64_t n, const double *px, const dou
                       const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream,
                       int32_t *variant, int32_t *sort_kbits, float *best_ms);
 
+/* Allocation-free binned step.  Same operation and results as
+ * vgn_compute_step_batch with track binning at `sort_kbits` (1..5), but the
+ * binning scratch (sort keys, histogram, visit permutation) lives in one fixed
+ * device buffer that the library declares statically, so the call allocates
+ * no device or host memory.  It is for callers that cannot allocate inside a
+ * navigation call: a transport loop that runs under a fixed device-memory
+ * budget, or one that must not take the device-wide synchronisation that
+ * cudaMalloc/cudaFree imply while other streams are busy.
+ *  - all arrays must be device pointers (host buffers would need staging memory);
+ *  - n <= VGN_STATIC_SCRATCH_MAX_TRACKS, else VGN_ERR_ARG;
+ *  - the first call on a device looks the buffer's address up once for that
+ *    device (with the geometry's device current); make that first call before
+ *    any stream capture begins;
+ *  - there is ONE buffer per device: calls that overlap on that device (other
+ *    streams, other threads, other geometries) race on it and must be ordered
+ *    by the caller.
+ * Uses the step launch variant set for the precision form (vgn_set_step_config).
+ * No counterpart in the reference. */
+#define VGN_STATIC_SCRATCH_MAX_TRACKS 1048576 /* 2^20 tracks per call */
+#define VGN_STATIC_SCRATCH_MAX_KBITS 5        /* largest sort_kbits accepted */
+int vgn_compute_step_batch_static(const vgn_geometry *geom, int64_t n, const double *px, const double *py,
+                                  const double *pz, const double *dx, const double *dy, const double *dz,
+                                  const double *step_limit, const vgn_state *in, vgn_state *out, double *step,
+                                  double *safety, int flags, int32_t sort_kbits, void *stream);
+
 /* Wait for the work of the previous calls on `stream`; returns the first
  * device-side error status recorded by a kernel since the last call. */
 int vgn_synchronize(const vgn_geometry *geom, void *stream);

@@ -23,6 +23,8 @@ VGN_ERR_STATE = 7
 VGN_PRECISION_FP64 = 0x0
 VGN_PRECISION_MIXED = 0x1
 VGN_NO_RELOCATE = 0x10
+VGN_STATIC_SCRATCH_MAX_TRACKS = 1048576
+VGN_STATIC_SCRATCH_MAX_KBITS = 5
 
 OP_DISTANCE_TO_IN, OP_DISTANCE_TO_OUT, OP_SAFETY_TO_IN, OP_SAFETY_TO_OUT, OP_CONTAINS, OP_INSIDE = range(6)
 
@@ -42,6 +44,7 @@ EXPORTED = [
     "vgn_set_step_config",
     "vgn_get_step_config",
     "vgn_autotune_step",
+    "vgn_compute_step_batch_static",
     "vgn_synchronize",
     "vgn_last_error",
     "vgn_version",
@@ -101,6 +104,7 @@ def lib() -> C.CDLL:
         L.vgn_get_step_config.argtypes = [vp, C.c_int, C.POINTER(i32), C.POINTER(i32)]
         L.vgn_autotune_step.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, p, p, C.c_int, vp,
                                         C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)]
+        L.vgn_compute_step_batch_static.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, p, p, C.c_int, i32, vp]
         L.vgn_synchronize.argtypes = [vp, vp]
         L.vgn_last_error.restype = C.c_char_p
         L.vgn_version.restype = C.c_char_p

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "launch.h"
 
@@ -82,6 +83,36 @@ __global__ void __launch_bounds__(256) scatter_kernel(int64_t n, const uint32_t 
 }  // namespace dev
 
 size_t bin_scratch_words(int64_t n, int kbits) { return 2 * (size_t)n + ((size_t)8 << (3 * kbits)); }
+
+// ---- fixed device scratch of vgn_compute_step_batch_static ----------------
+// keys [n] | histogram [8 * 2^(3k)] | visit permutation [n], at the largest n and k
+// the entry point accepts: 2 * 2^20 + 2^18 words = 9 MiB per device.
+static constexpr size_t kStaticScratchWords =
+    2 * (size_t)VGN_STATIC_SCRATCH_MAX_TRACKS + ((size_t)8 << (3 * VGN_STATIC_SCRATCH_MAX_KBITS));
+static __device__ __align__(256) uint32_t g_static_scratch[kStaticScratchWords];
+
+size_t static_scratch_words() { return kStaticScratchWords; }
+
+// Address of the current device's copy of the buffer, looked up once per device.
+cudaError_t static_scratch(uint32_t **ptr)
+{
+  constexpr int kMaxDevices = 64;
+  static std::mutex lock;
+  static uint32_t *addr[kMaxDevices] = {};
+  int dev       = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> guard(lock);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    e       = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return e;
+    addr[dev] = static_cast<uint32_t *>(p);
+  }
+  *ptr = addr[dev];
+  return cudaSuccess;
+}
 
 cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, const double *pz, const double *dx,
                               const double *dy, const double *dz, const BinParams &b, uint32_t *scratch,

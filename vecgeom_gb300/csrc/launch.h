@@ -32,6 +32,10 @@ cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, con
                               const double *dy, const double *dz, const BinParams &b, uint32_t *scratch,
                               uint32_t *perm, int max_blocks, cudaStream_t s);
 
+// fixed device scratch of the allocation-free binned step (kernels_sort.cu)
+size_t static_scratch_words();
+cudaError_t static_scratch(uint32_t **ptr);  // current device's buffer
+
 // navigation kernels (kernels_nav.cu); mixed = FP32-interval box decisions
 cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s);
 int step_variant_count();

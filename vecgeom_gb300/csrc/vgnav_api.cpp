@@ -586,6 +586,49 @@ int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double
   return check_status(g, s);
 }
 
+// Binned step whose binning scratch is the library's static device buffer
+// (kernels_sort.cu): no cudaMalloc, no cudaFree, no staging workspace.
+int vgn_compute_step_batch_static(const vgn_geometry *g, int64_t n, const double *px, const double *py,
+                                  const double *pz, const double *dx, const double *dy, const double *dz,
+                                  const double *step_limit, const vgn_state *in, vgn_state *out, double *step,
+                                  double *safety, int flags, int32_t sort_kbits, void *stream)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
+  if (n > VGN_STATIC_SCRATCH_MAX_TRACKS)
+    return fail(VGN_ERR_ARG, "batch of " + std::to_string(n) + " tracks exceeds the static binning scratch (at most " +
+                                 std::to_string(VGN_STATIC_SCRATCH_MAX_TRACKS) + " tracks per call)");
+  if (sort_kbits < 1 || sort_kbits > VGN_STATIC_SCRATCH_MAX_KBITS)
+    return fail(VGN_ERR_ARG, "sort_kbits must be 1.." + std::to_string(VGN_STATIC_SCRATCH_MAX_KBITS));
+  if (n == 0) return VGN_OK;
+  if (!px || !py || !pz || !dx || !dy || !dz || !step_limit || !in || !out || !step)
+    return fail(VGN_ERR_ARG, "null array argument");
+  DeviceGuard guard(g->device);
+  if (classify({px, py, pz, dx, dy, dz, step_limit, in, out, step, safety}) != 1)
+    return fail(VGN_ERR_ARG, "device pointers required: this entry point stages no host buffers");
+  uint32_t *scratch = nullptr;
+  cudaError_t e     = vgn::static_scratch(&scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static binning scratch)");
+  const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
+  cudaStream_t s   = static_cast<cudaStream_t>(stream);
+  vgn::BinParams b = g->bin;
+  b.kbits          = sort_kbits;
+  for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << sort_kbits);
+  // keys [n] | histogram [8 * 2^(3k)], zeroed by launch_bin_tracks | permutation [n]
+  uint32_t *perm = scratch + (size_t)n + ((size_t)8 << (3 * sort_kbits));
+  e = vgn::launch_bin_tracks(n, px, py, pz, dx, dy, dz, b, scratch, perm, max_blocks(g), s);
+  if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+  vgn::StepArgs a{};
+  a.n = n; a.px = px; a.py = py; a.pz = pz; a.dx = dx; a.dy = dy; a.dz = dz; a.slimit = step_limit;
+  a.in = in; a.out = out; a.step = step; a.safety = safety;
+  a.reloc      = (flags & VGN_NO_RELOCATE) ? 0 : 1;
+  a.max_blocks = max_blocks(g);
+  a.perm       = perm;
+  e = vgn::launch_step(g->view, a, mixed, g->step_variant[mixed ? 1 : 0], s);
+  return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
+}
+
 int vgn_synchronize(const vgn_geometry *g, void *stream)
 {
   if (!g) return fail(VGN_ERR_ARG, "null geometry");
