@@ -259,6 +259,8 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_BOX: return 3;
   case OR_TUBE: return 5;
   case OR_CONE: return 7;
+  case OR_TRD: return 5;
+  case OR_TRAP: return 11;
   default: (void)p; (void)avail; return -1;
   }
 }

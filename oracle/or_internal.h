@@ -102,6 +102,17 @@ typedef struct { /* ConeStruct.h:23-77 cached members, full phi */
   double originalRmax1, originalRmax2;
 } or_cone;
 
+typedef struct { /* TrdStruct.h:19-39 (UniversalTrd: VECGEOM_NO_SPECIALIZATION is the default build) */
+  double dx1, dx2, dy1, dy2, dz;
+  double x2minusx1, y2minusy1, halfx1plusx2, halfy1plusy2, calfx, calfy, secxz, secyz, tolx, toly, fx, fy;
+} or_trd;
+
+typedef struct { /* TrapezoidStruct.h:41-59 with the PlaneShell<4> side planes (VECGEOM_PLANESHELL=ON) */
+  double dz, theta, phi, dy1, dx1, dx2, tanAlpha1, dy2, dx3, dx4, tanAlpha2;
+  double tthetaCphi, tthetaSphi;
+  double a[4], b[4], c[4], d[4];
+} or_trap;
+
 typedef struct {
   int type;
   int param_off;
@@ -112,6 +123,8 @@ typedef struct {
     or_box box;
     or_tube tube;
     or_cone cone;
+    or_trd trd;
+    or_trap trap;
   } s;
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;

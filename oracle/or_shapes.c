@@ -715,6 +715,459 @@ static void cone_extent(const or_cone *c, v3 *mn, v3 *mx)
 }
 
 /* ================================================================== */
+/* Trd (UniversalTrd): kernel/TrdImplementation.h                     */
+/* ================================================================== */
+
+/* TrdStruct(x1, x2, y1, y2, z) + CalculateCached (TrdStruct.h:65-70, 103-119).
+ * fToleranceY is computed from the x half-lengths, as in the reference. */
+static int trd_init(or_trd *t, const double *a, char *err, int errlen)
+{
+  if (!(a[0] >= 0 && a[1] >= 0 && a[2] >= 0 && a[3] >= 0 && a[4] > 0)) {
+    set_err(err, errlen, "Trd: half-lengths must be >= 0 and dz > 0");
+    return -1;
+  }
+  t->dx1 = a[0];
+  t->dx2 = a[1];
+  t->dy1 = a[2];
+  t->dy2 = a[3];
+  t->dz  = a[4];
+  t->x2minusx1    = t->dx2 - t->dx1;
+  t->y2minusy1    = t->dy2 - t->dy1;
+  t->halfx1plusx2 = 0.5 * (t->dx1 + t->dx2);
+  t->halfy1plusy2 = 0.5 * (t->dy1 + t->dy2);
+  t->fx           = 0.5 * (t->dx1 - t->dx2) / t->dz;
+  t->fy           = 0.5 * (t->dy1 - t->dy2) / t->dz;
+  t->secxz        = sqrt(1 + t->fx * t->fx);
+  t->secyz        = sqrt(1 + t->fy * t->fy);
+  t->calfx        = 1. / sqrt(1.0 + t->fx * t->fx);
+  t->calfy        = 1. / sqrt(1.0 + t->fy * t->fy);
+  t->tolx         = kTolerance * sqrt(t->x2minusx1 * t->x2minusx1 + 4 * t->dz * t->dz);
+  t->toly         = kTolerance * sqrt(t->x2minusx1 * t->x2minusx1 + 4 * t->dz * t->dz);
+  return 0;
+}
+
+/* TrdTypes::checkVaryingY for UniversalTrd (TrdTypes.h:66-75) */
+static inline int trd_varying_y(const or_trd *t) { return t->dy1 != t->dy2; }
+
+/* TrdUtilities::FaceTrajectoryIntersection (TrdImplementation.h:80-138); *dist is
+ * only written when the direction faces the plane (the reference's early return). */
+static int trd_face(const or_trd *t, v3 pos, v3 dir, int forY, int mirrored, int toInside, double *dist)
+{
+  double alongV, posV, dirV, posK, dirK, fV, fK, halfKplus, v1, ndotv;
+  if (forY) {
+    alongV = t->y2minusy1; v1 = t->dy1; posV = pos.y; posK = pos.x; dirV = dir.y; dirK = dir.x;
+    fK = t->fx; fV = t->fy; halfKplus = t->halfx1plusx2;
+  } else {
+    alongV = t->x2minusx1; v1 = t->dx1; posV = pos.x; posK = pos.y; dirV = dir.x; dirK = dir.y;
+    fK = t->fy; fV = t->fx; halfKplus = t->halfy1plusy2;
+  }
+  if (mirrored) {
+    posV *= -1.;
+    dirV *= -1.;
+  }
+  ndotv  = dirV + fV * dir.z;
+  int ok = toInside ? ndotv < 0. : ndotv > 0.;
+  if (!ok) return 0;
+  double alongZ = 2.0 * t->dz;
+  *dist = (alongZ * (posV - v1) - alongV * (pos.z + t->dz)) / (dir.z * alongV - dirV * alongZ + kTiny);
+  ok    = ok && *dist > (0. - kHalfTolerance);
+  if (ok) {
+    double hitz = pos.z + *dist * dir.z;
+    ok          = ok && fabs(hitz) <= t->dz;
+    double hitk = posK + *dist * dirK;
+    double dK   = halfKplus - fK * hitz;
+    ok          = ok && fabs(hitk) <= dK;
+    if (ok && fabs(*dist) < kHalfTolerance) *dist = 0.0;
+  }
+  return ok;
+}
+
+/* TrdUtilities::Safety (TrdImplementation.h:140-168) */
+static double trd_safety(const or_trd *t, v3 p, int inside)
+{
+  double safz = t->dz - fabs(p.z);
+  double dist = safz;
+  double distx = t->halfx1plusx2 - t->fx * p.z;
+  int okx      = distx >= 0;
+  double safx  = (distx - fabs(p.x)) * t->calfx;
+  if (okx && safx < dist) dist = safx;
+  if (trd_varying_y(t)) {
+    double disty = t->halfy1plusy2 - t->fy * p.z;
+    int oky      = disty >= 0;
+    double safy  = (disty - fabs(p.y)) * t->calfy;
+    if (oky && safy < dist) dist = safy;
+  } else {
+    double safy = t->dy1 - fabs(p.y);
+    if (safy < dist) dist = safy;
+  }
+  if (!inside) dist = -dist;
+  return dist;
+}
+
+/* TrdUtilities::UnplacedInside (TrdImplementation.h:170-214); UniversalTrd takes
+ * the general cross-product test for y (HasVaryingY is kUnknown). */
+static void trd_unplaced_inside(const or_trd *t, v3 p, int surfaceT, int *cin, int *cout)
+{
+  double pzPlusDz = p.z + t->dz;
+  *cout = fabs(p.z) > (surfaceT ? t->dz + kHalfTolerance : t->dz);
+  if (surfaceT) *cin = fabs(p.z) < t->dz - kHalfTolerance;
+  /* PointLineOrientation: cross = vx * py - vy * px */
+  double cross = t->x2minusx1 * pzPlusDz - (2.0 * t->dz) * (fabs(p.x) - t->dx1);
+  if (surfaceT) {
+    *cout = *cout || cross < -t->tolx;
+    *cin  = *cin && cross > t->tolx;
+  } else {
+    *cout = *cout || cross < 0;
+  }
+  cross = t->y2minusy1 * pzPlusDz - (2.0 * t->dz) * (fabs(p.y) - t->dy1);
+  if (surfaceT) {
+    *cout = *cout || cross < -t->toly;
+    *cin  = *cin && cross > t->toly;
+  } else {
+    *cout = *cout || cross < 0;
+  }
+}
+
+static int trd_contains(const or_trd *t, v3 p) /* TrdImplementation.h:263-272 */
+{
+  int cin = 0, cout = 0;
+  trd_unplaced_inside(t, p, 0, &cin, &cout);
+  return !cout;
+}
+
+static int trd_inside(const or_trd *t, v3 p) /* TrdImplementation.h:274-298 */
+{
+  int cin = 0, cout = 0, r = kSurfaceE;
+  trd_unplaced_inside(t, p, 1, &cin, &cout);
+  if (cin) r = kInsideE;
+  if (cout) r = kOutsideE;
+  return r;
+}
+
+static inline double trd_clamp(double d) { return fabs(d) < kHalfTolerance ? 0.0 : d; }
+
+/* TrdImplementation::DistanceToIn (TrdImplementation.h:300-394) */
+static double trd_dist_in(const or_trd *t, v3 p, v3 d)
+{
+  double distance = kInfLength;
+  int inz         = fabs(p.z) < t->dz - kHalfTolerance;
+  double distx    = t->halfx1plusx2 - t->fx * p.z;
+  int inx         = (distx - fabs(p.x)) * t->calfx > 0. + kHalfTolerance;
+  double disty;
+  int iny;
+  const int vary = trd_varying_y(t);
+  if (vary) {
+    disty = t->halfy1plusy2 - t->fy * p.z;
+    iny   = (disty - fabs(p.y)) * t->calfy > 0. + kHalfTolerance;
+  } else {
+    disty = fabs(p.y) - t->dy1;
+    iny   = disty < 0. - kHalfTolerance;
+  }
+  int inside = inx && iny && inz;
+  if (inside) distance = -1.;
+  int done = inside;
+  int okz  = p.z * d.z < 0.;
+  okz      = okz && !inz;
+  if (okz) {
+    double distz = (fabs(p.z) - t->dz) / fabs(d.z);
+    double hitx  = fabs(p.x + distz * d.x);
+    double hity  = fabs(p.y + distz * d.y);
+    int okzt     = p.z > (t->dz - kHalfTolerance) && hitx <= t->dx2 && hity <= t->dy2;
+    int okzb     = p.z < (-t->dz + kHalfTolerance) && hitx <= t->dx1 && hity <= t->dy1;
+    okz          = okz && (okzt || okzb);
+    if (okz) distance = distz;
+  }
+  done = done || okz;
+  if (done) return trd_clamp(distance);
+
+  int okx = 0;
+  if (!inx) {
+    okx = trd_face(t, p, d, 0, 0, 1, &distx);
+    if (okx) distance = distx;
+    okx = trd_face(t, p, d, 0, 1, 1, &distx);
+    if (okx) distance = distx;
+  }
+  done = done || okx;
+  if (done) return trd_clamp(distance);
+
+  if (vary) {
+    if (!iny) {
+      int oky = trd_face(t, p, d, 1, 0, 1, &disty);
+      if (oky) distance = disty;
+      oky = trd_face(t, p, d, 1, 1, 1, &disty);
+      if (oky) distance = disty;
+    }
+  } else {
+    if (!iny) {
+      disty /= fabs(d.y);
+      double zhit = p.z + disty * d.z;
+      double xhit = p.x + disty * d.x;
+      double dx   = t->halfx1plusx2 - t->fx * zhit;
+      int oky     = p.y * d.y < 0 && disty > -kHalfTolerance && fabs(xhit) < dx && fabs(zhit) < t->dz;
+      if (oky) distance = disty;
+    }
+  }
+  return trd_clamp(distance);
+}
+
+/* TrdImplementation::DistanceToOut (TrdImplementation.h:396-499); the scalar
+ * backend allows the early returns. */
+static double trd_dist_out(const or_trd *t, v3 p, v3 d)
+{
+  double distance = 0.0;
+  double invdir   = 1. / fabs(d.z + kTiny);
+  double safz     = t->dz - fabs(p.z);
+  int out         = safz < 0. - kHalfTolerance;
+  double distx    = t->halfx1plusx2 - t->fx * p.z;
+  out             = out || (distx - fabs(p.x)) * t->calfx < 0. - kHalfTolerance;
+  double disty;
+  const int vary = trd_varying_y(t);
+  if (vary) {
+    disty = t->halfy1plusy2 - t->fy * p.z;
+    out   = out || (disty - fabs(p.y)) * t->calfy < 0. - kHalfTolerance;
+  } else {
+    disty = t->dy1 - fabs(p.y);
+    out   = out || disty < 0. - kHalfTolerance;
+  }
+  if (out) return -1.;
+  if (d.z > 0.) {
+    double distz = (t->dz - p.z) * invdir;
+    double hitx  = fabs(p.x + distz * d.x);
+    double hity  = fabs(p.y + distz * d.y);
+    if (hitx <= t->dx2 && hity <= t->dy2) return trd_clamp(distz);
+  }
+  if (d.z < 0.) {
+    double distz = (p.z + t->dz) * invdir;
+    double hitx  = fabs(p.x + distz * d.x);
+    double hity  = fabs(p.y + distz * d.y);
+    if (hitx <= t->dx1 && hity <= t->dy1) return trd_clamp(distz);
+  }
+  if (trd_face(t, p, d, 0, 0, 0, &distx)) return trd_clamp(distx);
+  if (trd_face(t, p, d, 0, 1, 0, &distx)) return trd_clamp(distx);
+  if (vary) {
+    if (trd_face(t, p, d, 1, 0, 0, &disty)) return trd_clamp(disty);
+    if (trd_face(t, p, d, 1, 1, 0, &disty)) distance = disty;
+  } else {
+    double plane = t->dy1;
+    if (d.y < 0.) plane = -t->dy1;
+    disty       = (plane - p.y) / d.y;
+    double zhit = p.z + disty * d.z;
+    double xhit = p.x + disty * d.x;
+    double dx   = t->halfx1plusx2 - t->fx * zhit;
+    int oky     = fabs(xhit) < dx && fabs(zhit) < t->dz;
+    if (oky) distance = disty;
+  }
+  return trd_clamp(distance);
+}
+
+/* UnplacedTrd::Extent (UnplacedTrd.h:218-222) */
+static void trd_extent(const or_trd *t, v3 *mn, v3 *mx)
+{
+  double mxx = t->dx1 > t->dx2 ? t->dx1 : t->dx2;
+  double mxy = t->dy1 > t->dy2 ? t->dy1 : t->dy2;
+  *mn        = v3_make(-mxx, -mxy, -t->dz);
+  *mx        = v3_make(mxx, mxy, t->dz);
+}
+
+/* ================================================================== */
+/* Trapezoid: kernel/TrapezoidImplementation.h with base/PlaneShell.h */
+/* ================================================================== */
+
+static inline v3 v3_cross(v3 a, v3 b) /* Vector3D::Cross (Vector3D.h:230-234) */
+{
+  return v3_make(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+static inline double v3_dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+/* UnplacedTrapezoid::MakeAPlane (source/UnplacedTrapezoid.cpp:568-619): the normal is
+ * (p3 - p1) x (p4 - p2), normalised by multiplying with 1/Length(); d = -n.centroid. */
+static void trap_make_plane(or_trap *t, v3 p1, v3 p2, v3 p3, v3 p4, int i)
+{
+  v3 n     = v3_cross(v3_sub(p3, p1), v3_sub(p4, p2));
+  double r = 1. / sqrt(v3_dot3(n, n));
+  n        = v3_make(n.x * r, n.y * r, n.z * r);
+  v3 sum   = v3_add(v3_add(v3_add(p1, p2), p3), p4);
+  v3 centr = v3_make(0.25 * sum.x, 0.25 * sum.y, 0.25 * sum.z);
+  t->a[i]  = n.x;
+  t->b[i]  = n.y;
+  t->c[i]  = n.z;
+  t->d[i]  = -v3_dot3(n, centr);
+}
+
+/* UnplacedTrapezoid(dz, theta, phi, dy1, dx1, dx2, Alpha1, dy2, dx3, dx4, Alpha2)
+ * (UnplacedTrapezoid.h:56-64): tangents of the alphas, TrapezoidStruct::CalculateCached
+ * (TrapezoidStruct.h:90-95), FromParametersToCorners + MakePlanes
+ * (source/UnplacedTrapezoid.cpp:447-466, 630-675). */
+static int trap_init(or_trap *t, const double *a, char *err, int errlen)
+{
+  if (!(a[0] > 0 && a[3] > 0 && a[7] > 0 && a[4] >= 0 && a[5] >= 0 && a[8] >= 0 && a[9] >= 0 &&
+        fabs(a[1]) < 0.5 * kPi)) {
+    set_err(err, errlen, "Trapezoid: needs dz, dy1, dy2 > 0, dx >= 0 and |theta| < pi/2");
+    return -1;
+  }
+  t->dz = a[0]; t->theta = a[1]; t->phi = a[2]; t->dy1 = a[3]; t->dx1 = a[4]; t->dx2 = a[5];
+  t->tanAlpha1 = tan(a[6]);
+  t->dy2 = a[7]; t->dx3 = a[8]; t->dx4 = a[9];
+  t->tanAlpha2  = tan(a[10]);
+  t->tthetaCphi = tan(t->theta) * cos(t->phi);
+  t->tthetaSphi = tan(t->theta) * sin(t->phi);
+  double dxdyDy1 = t->tanAlpha1 * t->dy1;
+  double dxdyDy2 = t->tanAlpha2 * t->dy2;
+  double dxdzDz  = t->tthetaCphi * t->dz;
+  double dydzDz  = t->tthetaSphi * t->dz;
+  v3 pt[8];
+  pt[0] = v3_make(-dxdzDz - dxdyDy1 - t->dx1, -dydzDz - t->dy1, -t->dz);
+  pt[1] = v3_make(-dxdzDz - dxdyDy1 + t->dx1, -dydzDz - t->dy1, -t->dz);
+  pt[2] = v3_make(-dxdzDz + dxdyDy1 - t->dx2, -dydzDz + t->dy1, -t->dz);
+  pt[3] = v3_make(-dxdzDz + dxdyDy1 + t->dx2, -dydzDz + t->dy1, -t->dz);
+  pt[4] = v3_make(+dxdzDz - dxdyDy2 - t->dx3, +dydzDz - t->dy2, +t->dz);
+  pt[5] = v3_make(+dxdzDz - dxdyDy2 + t->dx3, +dydzDz - t->dy2, +t->dz);
+  pt[6] = v3_make(+dxdzDz + dxdyDy2 - t->dx4, +dydzDz + t->dy2, +t->dz);
+  pt[7] = v3_make(+dxdzDz + dxdyDy2 + t->dx4, +dydzDz + t->dy2, +t->dz);
+  trap_make_plane(t, pt[0], pt[1], pt[5], pt[4], 0); /* ~ -Y */
+  trap_make_plane(t, pt[2], pt[6], pt[7], pt[3], 1); /* ~ +Y */
+  trap_make_plane(t, pt[0], pt[4], pt[6], pt[2], 2); /* ~ -X */
+  trap_make_plane(t, pt[1], pt[3], pt[7], pt[5], 3); /* ~ +X */
+  return 0;
+}
+
+static inline double trap_pdist(const or_trap *t, int i, v3 p)
+{
+  return t->a[i] * p.x + t->b[i] * p.y + t->c[i] * p.z + t->d[i];
+}
+
+static inline double trap_proj(const or_trap *t, int i, v3 d) { return t->a[i] * d.x + t->b[i] * d.y + t->c[i] * d.z; }
+
+/* GenericKernelForContainsAndInside (TrapezoidImplementation.h:124-162, PlaneShell.h:130-151) */
+static void trap_generic_ci(const or_trap *t, v3 p, int forInside, int *cin, int *cout)
+{
+  *cout = fabs(p.z) > (forInside ? t->dz + kHalfTolerance : t->dz);
+  if (forInside) *cin = fabs(p.z) < t->dz - kHalfTolerance;
+  for (int i = 0; i < 4; ++i) {
+    double dist = trap_pdist(t, i, p);
+    *cout       = *cout || dist > (forInside ? 0. + kHalfTolerance : 0.);
+    if (forInside) *cin = *cin && dist < 0. - kHalfTolerance;
+  }
+}
+
+static int trap_contains(const or_trap *t, v3 p)
+{
+  int cin = 0, cout = 0;
+  trap_generic_ci(t, p, 0, &cin, &cout);
+  return !cout;
+}
+
+static int trap_inside(const or_trap *t, v3 p) /* TrapezoidImplementation.h:107-122 */
+{
+  int cin = 0, cout = 0, r = kSurfaceE;
+  trap_generic_ci(t, p, 1, &cin, &cout);
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+/* DistanceToIn (TrapezoidImplementation.h:177-216) with PlaneShell::DistanceToIn
+ * (PlaneShell.h:161-213); the scalar backend takes every early return. */
+static double trap_dist_in(const or_trap *t, v3 p, v3 d)
+{
+  double signZdir = or_sign(d.z);
+  double max      = signZdir * t->dz - p.z;
+  if (signZdir * max < 0.0 + kHalfTolerance) return kInfLength;
+  double invdir = 1.0 / NonZero(d.z);
+  double smax   = max * invdir;
+  double smin   = -(signZdir * t->dz + p.z) * invdir;
+  double pdist[4], proj[4], vdist[4];
+  for (int i = 0; i < 4; ++i) {
+    pdist[i] = trap_pdist(t, i, p);
+    proj[i]  = trap_proj(t, i, d);
+    vdist[i] = -pdist[i] / NonZero(proj[i]);
+  }
+  for (int i = 0; i < 4; ++i) {
+    if (pdist[i] > 0. + kHalfTolerance && proj[i] >= 0.) return kInfLength;
+    if (pdist[i] > 0. - kHalfTolerance && proj[i] > 0.) return kInfLength;
+  }
+  for (int i = 0; i < 4; ++i) {
+    int posPoint     = pdist[i] > 0. - kHalfTolerance;
+    int posDir       = proj[i] > 0;
+    int fromInside   = !posPoint && posDir;
+    int fromOutside  = posPoint && !posDir;
+    if (fromInside && vdist[i] < smin) return kInfLength;
+    if (fromOutside && vdist[i] > smax) return kInfLength;
+    if (fromOutside && vdist[i] > smin) smin = vdist[i];
+    if (fromInside && vdist[i] < smax) smax = vdist[i];
+  }
+  return smin <= smax ? smin : kInfLength;
+}
+
+/* DistanceToOut (TrapezoidImplementation.h:270-299) with PlaneShell::DistanceToOut
+ * (PlaneShell.h:219-257) */
+static double trap_dist_out(const or_trap *t, v3 p, v3 d)
+{
+  if (fabs(p.z) > t->dz + kHalfTolerance) return -1.0;
+  double distance = kInfLength;
+  double distz    = (or_sign(d.z) * t->dz - p.z) / NonZero(d.z);
+  if (d.z != 0.) distance = distz;
+  double distOut = kInfLength;
+  for (int i = 0; i < 4; ++i) {
+    double pdist = trap_pdist(t, i, p);
+    double proj  = trap_proj(t, i, d);
+    double vdist = -pdist / NonZero(proj);
+    if (pdist > kHalfTolerance) distOut = -1.;
+    if (proj > 0. && vdist < distOut) distOut = vdist;
+  }
+  if (distOut < distance) distance = distOut;
+  return distance;
+}
+
+/* SafetyToIn / SafetyToOut (TrapezoidImplementation.h:341-401, PlaneShell.h:260-305) */
+static double trap_safe_in(const or_trap *t, v3 p)
+{
+  double safety = fabs(p.z) - t->dz;
+  for (int i = 0; i < 4; ++i) {
+    double dist = trap_pdist(t, i, p);
+    if (dist > safety) safety = dist;
+  }
+  return safety;
+}
+
+static double trap_safe_out(const or_trap *t, v3 p)
+{
+  double safety = t->dz - fabs(p.z);
+  for (int i = 0; i < 4; ++i) {
+    double dist = -trap_pdist(t, i, p);
+    if (dist < safety) safety = dist;
+  }
+  return safety;
+}
+
+/* UnplacedTrapezoid::Extent via fromPlanesToCorners (source/UnplacedTrapezoid.cpp:297-337, 467-494) */
+static void trap_extent(const or_trap *t, v3 *mn, v3 *mx)
+{
+  const double dz = t->dz;
+  const double *A = t->a, *B = t->b, *C = t->c, *D = t->d;
+  double py[8], px[8];
+  py[0] = py[1] = -(D[0] - dz * C[0]) / B[0];
+  py[2] = py[3] = -(D[1] - dz * C[1]) / B[1];
+  py[4] = py[5] = -(D[0] + dz * C[0]) / B[0];
+  py[6] = py[7] = -(D[1] + dz * C[1]) / B[1];
+  px[0] = ((B[2] / B[0]) * (D[0] - dz * C[0]) - (D[2] - dz * C[2])) / A[2];
+  px[1] = ((B[3] / B[0]) * (D[0] - dz * C[0]) - (D[3] - dz * C[3])) / A[3];
+  px[2] = ((B[2] / B[1]) * (D[1] - dz * C[1]) - (D[2] - dz * C[2])) / A[2];
+  px[3] = ((B[3] / B[1]) * (D[1] - dz * C[1]) - (D[3] - dz * C[3])) / A[3];
+  px[4] = ((B[2] / B[0]) * (D[0] + dz * C[0]) - (D[2] + dz * C[2])) / A[2];
+  px[5] = ((B[3] / B[0]) * (D[0] + dz * C[0]) - (D[3] + dz * C[3])) / A[3];
+  px[6] = ((B[2] / B[1]) * (D[1] + dz * C[1]) - (D[2] + dz * C[2])) / A[2];
+  px[7] = ((B[3] / B[1]) * (D[1] + dz * C[1]) - (D[3] + dz * C[3])) / A[3];
+  mx->x = or_max(or_max(or_max(px[0], px[1]), or_max(px[2], px[3])), or_max(or_max(px[4], px[5]), or_max(px[6], px[7])));
+  mn->x = or_min(or_min(or_min(px[0], px[1]), or_min(px[2], px[3])), or_min(or_min(px[4], px[5]), or_min(px[6], px[7])));
+  mx->y = or_max(or_max(or_max(py[0], py[1]), or_max(py[2], py[3])), or_max(or_max(py[4], py[5]), or_max(py[6], py[7])));
+  mn->y = or_min(or_min(or_min(py[0], py[1]), or_min(py[2], py[3])), or_min(or_min(py[4], py[5]), or_min(py[6], py[7])));
+  mn->z = -dz;
+  mx->z = dz;
+}
+
+/* ================================================================== */
 /* dispatch                                                           */
 /* ================================================================== */
 
@@ -729,6 +1182,8 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
     return 0;
   case OR_TUBE: return tube_init(&lv->s.tube, p, err, errlen);
   case OR_CONE: return cone_init(&lv->s.cone, p, err, errlen);
+  case OR_TRD: return trd_init(&lv->s.trd, p, err, errlen);
+  case OR_TRAP: return trap_init(&lv->s.trap, p, err, errlen);
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -742,6 +1197,8 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
     return;
   case OR_TUBE: tube_extent(&lv->s.tube, mn, mx); return;
   case OR_CONE: cone_extent(&lv->s.cone, mn, mx); return;
+  case OR_TRD: trd_extent(&lv->s.trd, mn, mx); return;
+  case OR_TRAP: trap_extent(&lv->s.trap, mn, mx); return;
   }
 }
 
@@ -756,6 +1213,8 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_BOX: return box_dist_in(&lv->s.box, p, d);
   case OR_TUBE: return tube_dist_in(&lv->s.tube, p, d);
   case OR_CONE: return cone_dist_in(&lv->s.cone, p, d);
+  case OR_TRD: return trd_dist_in(&lv->s.trd, p, d);
+  case OR_TRAP: return trap_dist_in(&lv->s.trap, p, d);
   }
   return kInfLength;
 }
@@ -768,6 +1227,8 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_BOX: return box_dist_out(&lv->s.box, p, d);
   case OR_TUBE: return tube_dist_out(&lv->s.tube, p, d);
   case OR_CONE: return cone_dist_out(&lv->s.cone, p, d);
+  case OR_TRD: return trd_dist_out(&lv->s.trd, p, d);
+  case OR_TRAP: return trap_dist_out(&lv->s.trap, p, d);
   }
   return -1.;
 }
@@ -779,6 +1240,8 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_BOX: return box_safe_in(&lv->s.box, p);
   case OR_TUBE: return tube_safe_in(&lv->s.tube, p);
   case OR_CONE: return cone_safe_in(&lv->s.cone, p);
+  case OR_TRD: return trd_safety(&lv->s.trd, p, 0);
+  case OR_TRAP: return trap_safe_in(&lv->s.trap, p);
   }
   return kInfLength;
 }
@@ -790,6 +1253,8 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_BOX: return box_safe_out(&lv->s.box, p);
   case OR_TUBE: return tube_safe_out(&lv->s.tube, p);
   case OR_CONE: return cone_safe_out(&lv->s.cone, p);
+  case OR_TRD: return trd_safety(&lv->s.trd, p, 1);
+  case OR_TRAP: return trap_safe_out(&lv->s.trap, p);
   }
   return 0.;
 }
@@ -801,6 +1266,8 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_BOX: return box_contains(&lv->s.box, p);
   case OR_TUBE: return tube_contains(&lv->s.tube, p);
   case OR_CONE: return cone_contains(&lv->s.cone, p);
+  case OR_TRD: return trd_contains(&lv->s.trd, p);
+  case OR_TRAP: return trap_contains(&lv->s.trap, p);
   }
   return 0;
 }
@@ -812,6 +1279,8 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_BOX: return box_inside(&lv->s.box, p);
   case OR_TUBE: return tube_inside(&lv->s.tube, p);
   case OR_CONE: return cone_inside(&lv->s.cone, p);
+  case OR_TRD: return trd_inside(&lv->s.trd, p);
+  case OR_TRAP: return trap_inside(&lv->s.trap, p);
   }
   return kOutsideE;
 }

@@ -341,7 +341,213 @@ CONE_CASES = [
     _case(f"{C}:1075", CONE, CT1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
 ]
 
-ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES
+TRD = 3
+TD = "test/unit_tests/TestTrd.cpp"
+TRD1 = (20.0, 20.0, 30.0, 30.0, 40.0)  # TestTrd.cpp:51 trd1 (x1, x2, y1, y2, z)
+TRD2 = (10.0, 30.0, 20.0, 40.0, 40.0)  # TestTrd.cpp:52 trd2
+TRD3 = (0.14999999999999999, 0.14999999999999999, 24.707000000000001, 24.707000000000001,
+        22.699999999999999)  # TestTrd.cpp:53 "BABAR Trd"
+COSA, SINA = 4 / math.sqrt(17.0), 1 / math.sqrt(17.0)  # TestTrd.cpp:209
+TRD_CASES = [
+    _case(f"{TD}:69", TRD, TRD1, "inside", pzero, None, 1, "eq"),
+    _case(f"{TD}:70", TRD, TRD1, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{TD}:71", TRD, TRD1, "inside", (20.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TD}:72", TRD, TRD1, "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TD}:73", TRD, TRD1, "inside", (0.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:77", TRD, TRD1, "inside", (20.0, 30.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:81", TRD, TRD1, "inside", (-20.0, 30.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:85", TRD, TRD1, "inside", (20.0, -30.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:89", TRD, TRD1, "inside", (20.0, 30.0, -40.0), None, 2, "eq"),
+    _case(f"{TD}:93", TRD, TRD1, "inside", (20.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TD}:97", TRD, TRD1, "inside", (0.0, 30.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:101", TRD, TRD1, "inside", (20.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:105", TRD, TRD1, "inside", (-20.0, -30.0, -40.0), None, 2, "eq"),
+    _case(f"{TD}:107", TRD, TRD2, "inside", pzero, None, 1, "eq"),
+    _case(f"{TD}:108", TRD, TRD2, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{TD}:109", TRD, TRD2, "inside", (20.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TD}:110", TRD, TRD2, "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TD}:111", TRD, TRD2, "inside", (0.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{TD}:231", TRD, TRD1, "safe_out", pzero, None, 20.0),
+    _case(f"{TD}:233", TRD, TRD1, "safe_out", vx, None, 19.0),
+    _case(f"{TD}:235", TRD, TRD1, "safe_out", vy, None, 20.0),
+    _case(f"{TD}:237", TRD, TRD1, "safe_out", vz, None, 20.0),
+    _case(f"{TD}:240", TRD, TRD2, "safe_out", pzero, None, 20 * COSA),
+    _case(f"{TD}:242", TRD, TRD2, "safe_out", vx, None, 19 * COSA),
+    _case(f"{TD}:244", TRD, TRD2, "safe_out", vy, None, 20 * COSA),
+    _case(f"{TD}:246", TRD, TRD2, "safe_out", vz, None, 20 * COSA + SINA),
+    _case(f"{TD}:251", TRD, TRD1, "dist_out", pzero, vx, 20.0),
+    _case(f"{TD}:253", TRD, TRD1, "dist_out", pzero, vmx, 20.0),
+    _case(f"{TD}:255", TRD, TRD1, "dist_out", pzero, vy, 30.0),
+    _case(f"{TD}:257", TRD, TRD1, "dist_out", pzero, vmy, 30.0),
+    _case(f"{TD}:259", TRD, TRD1, "dist_out", pzero, vz, 40.0),
+    _case(f"{TD}:261", TRD, TRD1, "dist_out", pzero, vmz, 40.0),
+    _case(f"{TD}:263", TRD, TRD1, "dist_out", pzero, vxy, math.sqrt(800.0)),
+    _case(f"{TD}:266", TRD, TRD1, "dist_out", (20.0, 0.0, 0.0), vx, 0.0),
+    _case(f"{TD}:268", TRD, TRD1, "dist_out", (-20.0, 0.0, 0.0), vmx, 0.0),
+    _case(f"{TD}:270", TRD, TRD1, "dist_out", (0.0, 30.0, 0.0), vy, 0.0),
+    _case(f"{TD}:272", TRD, TRD1, "dist_out", (0.0, -30.0, 0.0), vmy, 0.0),
+    _case(f"{TD}:274", TRD, TRD1, "dist_out", (0.0, 0.0, 40.0), vz, 0.0),
+    _case(f"{TD}:276", TRD, TRD1, "dist_out", (0.0, 0.0, -40.0), vmz, 0.0),
+    _case(f"{TD}:280", TRD, TRD2, "dist_out", pzero, vx, 20.0),
+    _case(f"{TD}:284", TRD, TRD2, "dist_out", pzero, vmx, 20.0),
+    _case(f"{TD}:288", TRD, TRD2, "dist_out", pzero, vy, 30.0),
+    _case(f"{TD}:292", TRD, TRD2, "dist_out", pzero, vmy, 30.0),
+    _case(f"{TD}:296", TRD, TRD2, "dist_out", pzero, vz, 40.0),
+    _case(f"{TD}:300", TRD, TRD2, "dist_out", pzero, vmz, 40.0),
+    _case(f"{TD}:304", TRD, TRD2, "dist_out", pzero, vxy, math.sqrt(800.0)),
+    _case(f"{TD}:308", TRD, TRD2, "dist_out", (20.0, 0.0, 0.0), vx, 0.0),
+    _case(f"{TD}:312", TRD, TRD2, "dist_out", (-20.0, 0.0, 0.0), vmx, 0.0),
+    _case(f"{TD}:316", TRD, TRD2, "dist_out", (0.0, 30.0, 0.0), vy, 0.0),
+    _case(f"{TD}:320", TRD, TRD2, "dist_out", (0.0, -30.0, 0.0), vmy, 0.0),
+    _case(f"{TD}:324", TRD, TRD2, "dist_out", (0.0, 0.0, 40.0), vz, 0.0),
+    _case(f"{TD}:328", TRD, TRD2, "dist_out", (0.0, 0.0, -40.0), vmz, 0.0),
+    _case(f"{TD}:333", TRD, TRD1, "safe_in", (100.0, 0.0, 0.0), None, 80.0),
+    _case(f"{TD}:335", TRD, TRD1, "safe_in", (-100.0, 0.0, 0.0), None, 80.0),
+    _case(f"{TD}:337", TRD, TRD1, "safe_in", (0.0, 100.0, 0.0), None, 70.0),
+    _case(f"{TD}:339", TRD, TRD1, "safe_in", (0.0, -100.0, 0.0), None, 70.0),
+    _case(f"{TD}:341", TRD, TRD1, "safe_in", (0.0, 0.0, 100.0), None, 60.0),
+    _case(f"{TD}:343", TRD, TRD1, "safe_in", (0.0, 0.0, -100.0), None, 60.0),
+    _case(f"{TD}:346", TRD, TRD2, "safe_in", (100.0, 0.0, 0.0), None, 80 * COSA),
+    _case(f"{TD}:348", TRD, TRD2, "safe_in", (-100.0, 0.0, 0.0), None, 80 * COSA),
+    _case(f"{TD}:350", TRD, TRD2, "safe_in", (0.0, 100.0, 0.0), None, 70 * COSA),
+    _case(f"{TD}:352", TRD, TRD2, "safe_in", (0.0, -100.0, 0.0), None, 70 * COSA),
+    _case(f"{TD}:354", TRD, TRD2, "safe_in", (0.0, 0.0, 100.0), None, 60.0),
+    _case(f"{TD}:356", TRD, TRD2, "safe_in", (0.0, 0.0, -100.0), None, 60.0),
+    _case(f"{TD}:361", TRD, TRD1, "dist_in", (100.0, 0.0, 0.0), vmx, 80.0),
+    _case(f"{TD}:363", TRD, TRD1, "dist_in", (-100.0, 0.0, 0.0), vx, 80.0),
+    _case(f"{TD}:365", TRD, TRD1, "dist_in", (0.0, 100.0, 0.0), vmy, 70.0),
+    _case(f"{TD}:367", TRD, TRD1, "dist_in", (0.0, -100.0, 0.0), vy, 70.0),
+    _case(f"{TD}:369", TRD, TRD1, "dist_in", (0.0, 0.0, 100.0), vmz, 60.0),
+    _case(f"{TD}:371", TRD, TRD1, "dist_in", (0.0, 0.0, -100.0), vz, 60.0),
+    _case(f"{TD}:373", TRD, TRD1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{TD}:375", TRD, TRD1, "dist_in", (-100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{TD}:378", TRD, TRD2, "dist_in", (100.0, 0.0, 0.0), vmx, 80.0),
+    _case(f"{TD}:380", TRD, TRD2, "dist_in", (-100.0, 0.0, 0.0), vx, 80.0),
+    _case(f"{TD}:382", TRD, TRD2, "dist_in", (0.0, 100.0, 0.0), vmy, 70.0),
+    _case(f"{TD}:384", TRD, TRD2, "dist_in", (0.0, -100.0, 0.0), vy, 70.0),
+    _case(f"{TD}:386", TRD, TRD2, "dist_in", (0.0, 0.0, 100.0), vmz, 60.0),
+    _case(f"{TD}:388", TRD, TRD2, "dist_in", (0.0, 0.0, -100.0), vz, 60.0),
+    _case(f"{TD}:390", TRD, TRD2, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{TD}:392", TRD, TRD2, "dist_in", (-100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{TD}:394-398", TRD, TRD3, "dist_in", (0.15000000000000185, -22.048743592955137, 2.4268539333219472),
+          _unit((-0.76165597579890043, 0.64364445891356026, -0.074515708658524193)), 0.0),
+]
+
+TRAP = 4
+TP = "test/unit_tests/TestTrap.cpp"
+# UnplacedTrapezoid(dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2), angles in radians
+TRAP1 = (40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0)  # TestTrap.cpp:67 box-like
+# TestTrap.cpp:63-71 builds trap2 from its eight corners; these parameters give the same corners
+TRAP2 = (40.0, 0.0, 0.0, 20.0, 10.0, 10.0, 0.0, 40.0, 30.0, 30.0, 0.0)
+TRAP3 = (50.0, 0.0, 0.0, 50.0, 50.0, 50.0, KPI / 4, 50.0, 50.0, 50.0, KPI / 4)    # TestTrap.cpp:73
+TRAP4 = (50.0, 0.0, 0.0, 50.0, 50.0, 50.0, -KPI / 4, 50.0, 50.0, 50.0, -KPI / 4)  # TestTrap.cpp:74
+TRAP353 = (0.5, 0.0, 0.0, 3.0, 14.237500000000001, 12.592500000000001, 0.274166666666666, 3.0,
+           14.237500000000001, 12.592500000000001, 0.274166666666666)  # TestTrap.cpp:735-739 (VECGEOM-353)
+S2T = math.sqrt(2.0)
+vymz = (0.0, S2, -S2)
+_TV = 0.11  # TestTrap.cpp:484
+
+
+def _plus(p, s, v):
+    return (p[0] + s * v[0], p[1] + s * v[1], p[2] + s * v[2])
+
+
+TRAP_CASES = [
+    _case(f"{TP}:134", TRAP, TRAP1, "inside", pzero, None, 1, "eq"),
+    _case(f"{TP}:135", TRAP, TRAP1, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{TP}:136", TRAP, TRAP1, "inside", (20.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TP}:137", TRAP, TRAP1, "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TP}:138", TRAP, TRAP1, "inside", (0.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{TP}:140", TRAP, TRAP2, "inside", pzero, None, 1, "eq"),
+    _case(f"{TP}:141", TRAP, TRAP2, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{TP}:142", TRAP, TRAP2, "inside", (20.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TP}:143", TRAP, TRAP2, "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TP}:144", TRAP, TRAP2, "inside", (0.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{TP}:294", TRAP, TRAP1, "safe_out", pzero, None, 20.0),
+    _case(f"{TP}:296", TRAP, TRAP1, "safe_out", vx, None, 19.0),
+    _case(f"{TP}:298", TRAP, TRAP1, "safe_out", vy, None, 20.0),
+    _case(f"{TP}:300", TRAP, TRAP1, "safe_out", vz, None, 20.0),
+    _case(f"{TP}:303", TRAP, TRAP2, "safe_out", pzero, None, 20 * COSA),
+    _case(f"{TP}:305", TRAP, TRAP2, "safe_out", vx, None, 19 * COSA),
+    _case(f"{TP}:307", TRAP, TRAP2, "safe_out", vy, None, 20 * COSA),
+    _case(f"{TP}:309", TRAP, TRAP2, "safe_out", vz, None, 20 * COSA + SINA),
+]
+for _ln, _p, _d, _e in [(314, pzero, vx, 20.0), (318, pzero, vmx, 20.0), (322, pzero, vy, 30.0), (326, pzero, vmy, 30.0),
+                        (330, pzero, vz, 40.0), (334, pzero, vmz, 40.0), (338, pzero, vxy, math.sqrt(800.0)),
+                        (342, (20.0, 0.0, 0.0), vx, 0.0), (346, (-20.0, 0.0, 0.0), vmx, 0.0),
+                        (350, (0.0, 30.0, 0.0), vy, 0.0), (354, (0.0, -30.0, 0.0), vmy, 0.0),
+                        (358, (0.0, 0.0, 40.0), vz, 0.0), (362, (0.0, 0.0, -40.0), vmz, 0.0),
+                        (366, (20.0, 0.0, 0.0), vmx, 40.0), (371, (-20.0, 0.0, 0.0), vx, 40.0),
+                        (375, (0.0, 30.0, 0.0), vmy, 60.0), (379, (0.0, -30.0, 0.0), vy, 60.0),
+                        (383, (0.0, 0.0, 40.0), vmz, 80.0), (387, (0.0, 0.0, -40.0), vz, 80.0)]:
+    TRAP_CASES.append(_case(f"{TP}:{_ln}", TRAP, TRAP1, "dist_out", _p, _d, _e))
+for _ln, _p, _d, _e in [(391, pzero, vx, 20.0), (395, pzero, vmx, 20.0), (399, pzero, vy, 30.0), (403, pzero, vmy, 30.0),
+                        (407, pzero, vz, 40.0), (411, pzero, vmz, 40.0), (415, pzero, vxy, math.sqrt(800.0)),
+                        (419, (20.0, 0.0, 0.0), vx, 0.0), (423, (-20.0, 0.0, 0.0), vmx, 0.0),
+                        (427, (0.0, 30.0, 0.0), vy, 0.0), (431, (0.0, -30.0, 0.0), vmy, 0.0),
+                        (435, (0.0, 0.0, 40.0), vz, 0.0), (439, (0.0, 0.0, -40.0), vmz, 0.0)]:
+    TRAP_CASES.append(_case(f"{TP}:{_ln}", TRAP, TRAP2, "dist_out", _p, _d, _e))
+for _ln, _p, _e in [(445, (100.0, 100.0, 100.0), 80.0), (449, (100.0, 0.0, 0.0), 80.0), (452, (-100.0, 0.0, 0.0), 80.0),
+                    (455, (0.0, 100.0, 0.0), 70.0), (458, (0.0, -100.0, 0.0), 70.0), (461, (0.0, 0.0, 100.0), 60.0),
+                    (464, (0.0, 0.0, -100.0), 60.0)]:
+    TRAP_CASES.append(_case(f"{TP}:{_ln}", TRAP, TRAP1, "safe_in", _p, None, _e))
+for _ln, _p, _e in [(467, (100.0, 0.0, 0.0), 80 * COSA), (469, (-100.0, 0.0, 0.0), 80 * COSA),
+                    (471, (0.0, 100.0, 0.0), 70 * COSA), (473, (0.0, -100.0, 0.0), 70 * COSA),
+                    (475, (0.0, 0.0, 100.0), 60.0), (477, (0.0, 0.0, -100.0), 60.0)]:
+    TRAP_CASES.append(_case(f"{TP}:{_ln}", TRAP, TRAP2, "safe_in", _p, None, _e))
+# tolerance band around the faces (TestTrap.cpp:483-556): SafetyToIn / SafetyToOut at 0.11 mm off a face
+for _ln, _p, _op, _e, _cmp in [
+        (486, _plus((20.0, 0.0, 0.0), _TV, vx), "safe_in", _TV, "approx"),
+        (488, _plus((20.0, 0.0, 0.0), _TV, vx), "safe_out", 0.0, "le0"),
+        (493, _plus((20.0, 0.0, 0.0), -_TV, vx), "safe_in", 0.0, "le0"),
+        (496, _plus((20.0, 0.0, 0.0), -_TV, vx), "safe_out", _TV, "approx"),
+        (502, _plus((-20.0, 0.0, 0.0), _TV, vx), "safe_out", 0.0, "ge0"),
+        (506, _plus((-20.0, 0.0, 0.0), -_TV, vx), "safe_in", _TV, "approx"),
+        (508, _plus((-20.0, 0.0, 0.0), -_TV, vx), "safe_out", 0.0, "le0"),
+        (512, _plus((0.0, 30.0, 0.0), _TV, vy), "safe_in", _TV, "approx"),
+        (514, _plus((0.0, 30.0, 0.0), _TV, vy), "safe_out", 0.0, "le0"),
+        (519, _plus((0.0, 30.0, 0.0), -_TV, vy), "safe_out", _TV, "approx"),
+        (524, _plus((0.0, -30.0, 0.0), _TV, vy), "safe_out", _TV, "approx"),
+        (528, _plus((0.0, -30.0, 0.0), -_TV, vy), "safe_in", _TV, "approx"),
+        (530, _plus((0.0, -30.0, 0.0), -_TV, vy), "safe_out", 0.0, "le0"),
+        (534, _plus((0.0, 0.0, 40.0), _TV, vz), "safe_in", _TV, "approx"),
+        (536, _plus((0.0, 0.0, 40.0), _TV, vz), "safe_out", 0.0, "le0"),
+        (540, _plus((0.0, 0.0, 40.0), -_TV, vz), "safe_in", 0.0, "le0"),
+        (542, _plus((0.0, 0.0, 40.0), -_TV, vz), "safe_out", _TV, "approx"),
+        (546, _plus((0.0, 0.0, -40.0), _TV, vz), "safe_in", 0.0, "le0"),
+        (549, _plus((0.0, 0.0, -40.0), _TV, vz), "safe_out", _TV, "approx"),
+        (553, _plus((0.0, 0.0, -40.0), -_TV, vz), "safe_in", _TV, "approx"),
+        (555, _plus((0.0, 0.0, -40.0), -_TV, vz), "safe_out", 0.0, "le0")]:
+    TRAP_CASES.append(_case(f"{TP}:{_ln}", TRAP, TRAP1, _op, _p, None, _e, _cmp))
+for _sh, _ln0 in ((TRAP1, 560), (TRAP2, 577)):
+    for _k, (_p, _d, _e) in enumerate([((100.0, 0.0, 0.0), vmx, 80.0), ((-100.0, 0.0, 0.0), vx, 80.0),
+                                       ((0.0, 100.0, 0.0), vmy, 70.0), ((0.0, -100.0, 0.0), vy, 70.0),
+                                       ((0.0, 0.0, 100.0), vmz, 60.0), ((0.0, 0.0, -100.0), vz, 60.0),
+                                       ((100.0, 0.0, 0.0), vxy, INF), ((-100.0, 0.0, 0.0), vxy, INF)]):
+        TRAP_CASES.append(_case(f"{TP}:{_ln0 + 2 * _k + (1 if _sh is TRAP2 and _k > 0 else 0)}", TRAP, _sh, "dist_in",
+                                _p, _d, _e, "inf" if _e == INF else "approx"))
+TRAP_CASES += [
+    _case(f"{TP}:595", TRAP, TRAP3, "dist_in", (50.0, -50.0, 0.0), vy, 50.0),
+    _case(f"{TP}:598", TRAP, TRAP3, "dist_in", (50.0, -50.0, 0.0), vmy, INF, "inf"),
+    _case(f"{TP}:601", TRAP, TRAP4, "dist_in", (50.0, 50.0, 0.0), vy, INF, "inf"),
+    _case(f"{TP}:604", TRAP, TRAP4, "dist_in", (50.0, 50.0, 0.0), vmy, 50.0),
+    _case(f"{TP}:607", TRAP, TRAP1, "dist_in", (0.0, 60.0, 0.0), vxmy, INF, "inf"),
+    _case(f"{TP}:611", TRAP, TRAP1, "dist_in", (0.0, 50.0, 0.0), vxmy, math.sqrt(800.0)),
+    _case(f"{TP}:614", TRAP, TRAP1, "dist_in", (0.0, 40.0, 0.0), vxmy, 10.0 * S2T),
+    _case(f"{TP}:617", TRAP, TRAP1, "dist_in", (0.0, 40.0, 50.0), vxmy, INF, "inf"),
+    _case(f"{TP}:622", TRAP, TRAP1, "dist_in", (40.0, 60.0, 0.0), vmx, INF, "inf"),
+    _case(f"{TP}:625", TRAP, TRAP1, "dist_in", (40.0, 60.0, 0.0), vmy, INF, "inf"),
+    _case(f"{TP}:628", TRAP, TRAP1, "dist_in", (40.0, 60.0, 50.0), vmz, INF, "inf"),
+    _case(f"{TP}:631", TRAP, TRAP1, "dist_in", (0.0, 0.0, 50.0), vymz, 10.0 * S2T),
+    _case(f"{TP}:634", TRAP, TRAP1, "dist_in", (0.0, 0.0, 80.0), vymz, INF, "inf"),
+    _case(f"{TP}:637", TRAP, TRAP1, "dist_in", (0.0, 0.0, 70.0), vymz, 30.0 * S2T),
+    _case(f"{TP}:745", TRAP, TRAP353, "contains", (-16.483749999999997, -6.4512999999999989, 0.00000099999999999999995),
+          None, 0.0, "eq"),
+    _case(f"{TP}:746-748", TRAP, TRAP353, "dist_in",
+          (-16.483749999999997, -6.4512999999999989, 0.00000099999999999999995), vx, INF, "inf"),
+]
+
+ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:
@@ -363,6 +569,8 @@ def check(case, value) -> bool:
         return value <= 0.0
     if c == "lt0":
         return value < 0.0
+    if c == "ge0":
+        return value >= 0.0
     if c == "inf":
         return value >= INF
     if c == "eq":

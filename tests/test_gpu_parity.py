@@ -4,6 +4,8 @@ Bar: bit-exact (np.array_equal on the float64 values, identical 12-byte
 states) for steps, safeties, next volumes, located states and shape queries,
 both through device pointers (torch CUDA tensors) and through host pointers
 (the library's own staging path)."""
+import zlib
+
 import numpy as np
 import pytest
 
@@ -261,3 +263,80 @@ def test_autotune_then_step(oracle, vgnav, cuda, mixed):
     assert np.array_equal(got["step"], ref["step"])
     assert np.array_equal(got["safety"], ref["safety"])
     assert np.array_equal(got["out"], ref["out"])
+
+
+SHAPE_SETS = [
+    ("tube-solid", W.TUBE, (0.0, 30.0, 40.0, 0.0, W.K_TWO_PI)),
+    ("cone-hollow", W.CONE, (10.0, 50.0, 20.0, 40.0, 60.0, 0.0, W.K_TWO_PI)),
+    ("cone-solid-apex", W.CONE, (0.0, 30.0, 0.0, 0.0, 25.0, 0.0, W.K_TWO_PI)),
+    ("cone-inverted", W.CONE, (5.0, 10.0, 20.0, 45.0, 30.0, 0.0, W.K_TWO_PI)),
+    ("trd-varying", W.TRD, (10.0, 30.0, 20.0, 40.0, 40.0)),
+    ("trd-const-y", W.TRD, (20.0, 25.0, 30.0, 30.0, 40.0)),
+    ("trd-boxlike", W.TRD, (20.0, 20.0, 30.0, 30.0, 40.0)),
+    ("trd-wedge", W.TRD, (0.0, 30.0, 10.0, 40.0, 25.0)),
+    ("trap-skewed", W.TRAPEZOID, (60.0, 0.35, 0.087, 40.0, 30.0, 40.0, 0.17, 16.0, 10.0, 14.0, 0.17)),
+    ("trap-twisted-alpha", W.TRAPEZOID, (30.0, 0.1, 2.0, 20.0, 10.0, 25.0, -0.3, 35.0, 30.0, 12.0, 0.25)),
+    ("trap-boxlike", W.TRAPEZOID, (40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0)),
+]
+
+
+@pytest.mark.parametrize("name,shape,params", SHAPE_SETS, ids=[s[0] for s in SHAPE_SETS])
+def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda):
+    """Every query at points inside, outside and on the surface equals the oracle bit for bit."""
+    desc = single_shape(shape, params)
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    rng = np.random.Generator(np.random.PCG64(zlib.crc32(name.encode())))
+    n = 100000
+    reach = 1.3 * float(np.abs(W.trapezoid_corners(params)).max()) if shape == W.TRAPEZOID else 1.3 * max(params[:5])
+    x, y, z = (rng.uniform(-reach, reach, n) for _ in range(3))
+    dx, dy, dz = W.isotropic(rng, n)
+    # surface points: from inside points, move to the exit point along a random ray
+    inside = og.shape(0, OPS["contains"], x, y, z) == 1.0
+    dout = og.shape(0, OPS["dist_out"], x, y, z, dx, dy, dz)
+    sx, sy, sz = (a[inside] + dout[inside] * b[inside] for a, b in ((x, dx), (y, dy), (z, dz)))
+    m = sx.shape[0]
+    ex, ey, ez = W.isotropic(rng, m)
+    X, Y, Z = (np.concatenate([a, b]) for a, b in ((x, sx), (y, sy), (z, sz)))
+    DX, DY, DZ = (np.concatenate([a, b]) for a, b in ((dx, ex), (dy, ey), (dz, ez)))
+    assert m > 1000
+    for op in range(6):
+        got = np.zeros_like(X)
+        geo.shape(0, op, vgnav.SOA3D(X, Y, Z), vgnav.SOA3D(DX, DY, DZ), got)
+        ref = og.shape(0, op, X, Y, Z, DX, DY, DZ)
+        assert np.array_equal(got, ref), (op, int(np.sum(got != ref)))
+    # the surface band really is exercised
+    ins = og.shape(0, OPS["inside"], sx, sy, sz)
+    assert np.mean(ins == 2.0) > 0.5
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed):
+    """8192 daughters of every implemented shape type, full rotations: locate, one step with
+    safety, then every step of a track subset to the world exit, all equal to the oracle."""
+    desc = W.mixed_shape_geometry()
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    t = W.mixed_shape_tracks(1 << 16)
+    st = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st), mixed=mixed)
+    assert np.array_equal(st, og.locate(t.x, t.y, t.z))
+    t.states = st
+    assert np.mean(st["nav_ind"] != 1) > 0.005  # some tracks start inside daughters
+    ref = og.step(t)
+    got = gpu_step(cuda, geo, t, mixed=mixed)
+    assert np.array_equal(got["step"], ref["step"])
+    assert np.array_equal(got["safety"], ref["safety"])
+    assert np.array_equal(got["out"], ref["out"])
+    w = t.head(4096)
+    for it in range(200):
+        ref = og.step(w)
+        got = gpu_step(cuda, geo, w, mixed=mixed)
+        assert np.array_equal(got["step"], ref["step"]), it
+        assert np.array_equal(got["safety"], ref["safety"]), it
+        assert np.array_equal(got["out"], ref["out"]), it
+        w = advance(w, ref["step"], ref["out"])
+        w = keep(w, w.states["nav_ind"] != 0)
+        if w.n == 0:
+            break
+    assert w.n == 0

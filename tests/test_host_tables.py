@@ -2,6 +2,8 @@
 navigation index table and every BVH array must be identical word for word,
 since NavStateIndex values are offsets into the table and leaf order decides
 ties.  No GPU needed (geometry closed with VGN_HOST_ONLY)."""
+import math
+
 import numpy as np
 import pytest
 
@@ -15,6 +17,7 @@ def geometries():
         "nested_3_levels": W.nested_geometry(),
         "single_tube": W.tube_geometry(),
         "box_grid_small": W.box_grid_geometry(seed=7, n=5).desc,
+        "mixed_shapes_8192": W.mixed_shape_geometry(),
     }
 
 
@@ -41,6 +44,31 @@ def test_bvh_depth_rule(oracle):
     assert np.all(b["nchild"][b["nchild"] >= 0] <= 8) or np.any(b["nchild"] > 8)
     internal = np.nonzero(b["nchild"] < 0)[0]
     assert len(internal) > 0 and internal.max() < 4095 // 2
+
+
+@pytest.mark.parametrize("params,lo,hi", [
+    # TestTrap.cpp:755-760 (VECGEOM-393): Trapezoid(60, 20deg, 5deg, 40, 30, 40, 10deg, 16, 10, 14, 10deg)
+    ((60.0, math.radians(20), math.radians(5), 40.0, 30.0, 40.0, math.radians(10), 16.0, 10.0, 14.0, math.radians(10)),
+     (-58.80819229, -41.90332577, -60.0), (38.57634475, 38.09667423, 60.0)),
+    # TestTrap.cpp:646-653: trap1 (box-like) and trap2 (its corners as parameters)
+    ((40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0), (-20.0, -30.0, -40.0), (20.0, 30.0, 40.0)),
+    ((40.0, 0.0, 0.0, 20.0, 10.0, 10.0, 0.0, 40.0, 30.0, 30.0, 0.0), (-30.0, -40.0, -40.0), (30.0, 40.0, 40.0)),
+])
+def test_trapezoid_extent(oracle, vgnav, params, lo, hi):
+    """UnplacedTrapezoid::Extent, seen through the daughter's bounding box (extent +- 1e-3 mm)
+    in both the oracle's and the product's BVH of a world holding the trapezoid unrotated."""
+    from golden.known_answers import approx_equal
+
+    b = W.GeometryBuilder()
+    world = b.logical(W.BOX, (500.0, 500.0, 500.0))
+    b.place(b.logical(W.TRAPEZOID, params), world, W.transform_euler(0.0, 0.0, 0.0))
+    b.place_world(world)
+    desc = b.build()
+    for bvh in (oracle.OracleGeometry(desc).bvh(0), HostTables(desc).bvh(0)):
+        box = bvh["prims"][0]
+        got_lo, got_hi = box[:3] + 1e-3, box[3:] - 1e-3
+        assert all(approx_equal(g, e) for g, e in zip(got_lo, lo)), got_lo
+        assert all(approx_equal(g, e) for g, e in zip(got_hi, hi)), got_hi
 
 
 def test_invalid_descriptions_rejected(vgnav):

@@ -41,6 +41,19 @@ def test_nested_walk(oracle):
     walk_compare(og, t)
 
 
+def test_mixed_shapes_walk(oracle):
+    """Every implemented shape type as a daughter, full rotations, tracks starting inside and outside."""
+    desc = W.mixed_shape_geometry()
+    og = oracle.OracleGeometry(desc)
+    t = W.mixed_shape_tracks(8192, 24, 25)
+    t.states = og.locate(t.x, t.y, t.z)
+    table = og.navindex()
+    top_pv = table[np.unique(t.states["nav_ind"]).astype(np.int64) + 1]  # NavStateIndex word 1: placed volume
+    shapes_hit = set(np.asarray(desc.lv_shape)[np.asarray(desc.pv_logical)[top_pv]].tolist())
+    assert shapes_hit == set(W.IMPLEMENTED_SHAPES)
+    walk_compare(og, t)
+
+
 def test_locate_matches_generator(oracle):
     grid = W.box_grid_geometry()
     og = oracle.OracleGeometry(grid.desc)

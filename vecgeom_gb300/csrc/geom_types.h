@@ -135,6 +135,13 @@ enum { ConeRmin1 = 0, ConeRmax1, ConeRmin2, ConeRmax2, ConeDz, ConeOrigRmax1, Co
        ConeSqRmax1, ConeSqRmax2, ConeTolIz, ConeInnerApex, ConeTanInnerApex, ConeOuterApex, ConeTanOuterApex,
        ConeSecRMin, ConeSecRMax, ConeInvSecRMin, ConeInvSecRMax, ConeTanRMin, ConeTanRMax, ConeZNormInner,
        ConeZNormOuter, ConeArgRmax1, ConeArgRmax2, kConeSize };
+// Trd (UniversalTrd): TrdStruct members and cached values; padded to 16 doubles
+enum { TrdDx1 = 0, TrdDx2, TrdDy1, TrdDy2, TrdDz, TrdX2minusX1, TrdY2minusY1, TrdHalfX1plusX2, TrdHalfY1plusY2,
+       TrdCalfX, TrdCalfY, TrdTolX, TrdTolY, TrdFx, TrdFy, TrdPad, kTrdSize };
+// Trapezoid: half-length in z and the four side planes (PlaneShell<4>: A, B, C, D
+// each of 4), then the TrapezoidStruct parameters and cached values
+enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, TrapTheta = 17, TrapPhi, TrapDy1, TrapDx1, TrapDx2,
+       TrapTanAlpha1, TrapDy2, TrapDx3, TrapDx4, TrapTanAlpha2, TrapTthetaCphi, TrapTthetaSphi, kTrapSize = 32 };
 }  // namespace row
 
 // Plain-pointer view of the device tables, passed to kernels by value.

@@ -27,6 +27,8 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
   case kBox: return 3;
   case kTube: return 5;
   case kCone: return 7;
+  case kTrd: return 5;
+  case kTrapezoid: return 11;
   default: return -1;
   }
 }
@@ -151,6 +153,89 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.insert(shape.end(), r, r + row::kConeSize);
     return VGN_OK;
   }
+  case kTrd: {
+    // TrdStruct(x1, x2, y1, y2, z) + CalculateCached (TrdStruct.h:65-70, 103-119); the y
+    // tolerance is computed from the x half-lengths, as the reference does
+    if (!(p[0] >= 0 && p[1] >= 0 && p[2] >= 0 && p[3] >= 0 && p[4] > 0)) {
+      err = "Trd half-lengths must be >= 0 and dz > 0";
+      return VGN_ERR_ARG;
+    }
+    double r[row::kTrdSize] = {};
+    const double dx1 = p[0], dx2 = p[1], dy1 = p[2], dy2 = p[3], dz = p[4];
+    const double fx = 0.5 * (dx1 - dx2) / dz, fy = 0.5 * (dy1 - dy2) / dz;
+    const double x21         = dx2 - dx1;
+    r[row::TrdDx1]          = dx1;
+    r[row::TrdDx2]          = dx2;
+    r[row::TrdDy1]          = dy1;
+    r[row::TrdDy2]          = dy2;
+    r[row::TrdDz]           = dz;
+    r[row::TrdX2minusX1]    = x21;
+    r[row::TrdY2minusY1]    = dy2 - dy1;
+    r[row::TrdHalfX1plusX2] = 0.5 * (dx1 + dx2);
+    r[row::TrdHalfY1plusY2] = 0.5 * (dy1 + dy2);
+    r[row::TrdFx]           = fx;
+    r[row::TrdFy]           = fy;
+    r[row::TrdCalfX]        = 1. / std::sqrt(1.0 + fx * fx);
+    r[row::TrdCalfY]        = 1. / std::sqrt(1.0 + fy * fy);
+    r[row::TrdTolX]         = kTolerance * std::sqrt(x21 * x21 + 4 * dz * dz);
+    r[row::TrdTolY]         = kTolerance * std::sqrt(x21 * x21 + 4 * dz * dz);
+    shape.insert(shape.end(), r, r + row::kTrdSize);
+    return VGN_OK;
+  }
+  case kTrapezoid: {
+    // UnplacedTrapezoid(dz, theta, phi, dy1, dx1, dx2, Alpha1, dy2, dx3, dx4, Alpha2)
+    // (UnplacedTrapezoid.h:56-64): tan of the alphas, CalculateCached (TrapezoidStruct.h:90-95),
+    // corners from the parameters and one plane per side face
+    // (source/UnplacedTrapezoid.cpp:447-466, 568-675)
+    if (!(p[0] > 0 && p[3] > 0 && p[7] > 0 && p[4] >= 0 && p[5] >= 0 && p[8] >= 0 && p[9] >= 0 &&
+          std::fabs(p[1]) < 0.5 * kPi)) {
+      err = "Trapezoid needs dz, dy1, dy2 > 0, dx >= 0 and |theta| < pi/2";
+      return VGN_ERR_ARG;
+    }
+    double r[row::kTrapSize] = {};
+    const double dz = p[0], theta = p[1], phi = p[2], dy1 = p[3], dx1 = p[4], dx2 = p[5], dy2 = p[7], dx3 = p[8],
+                 dx4 = p[9];
+    const double tanA1 = std::tan(p[6]), tanA2 = std::tan(p[10]);
+    const double tcp = std::tan(theta) * std::cos(phi), tsp = std::tan(theta) * std::sin(phi);
+    const double dxdyDy1 = tanA1 * dy1, dxdyDy2 = tanA2 * dy2, dxdzDz = tcp * dz, dydzDz = tsp * dz;
+    const Vec3 pt[8] = {{-dxdzDz - dxdyDy1 - dx1, -dydzDz - dy1, -dz}, {-dxdzDz - dxdyDy1 + dx1, -dydzDz - dy1, -dz},
+                        {-dxdzDz + dxdyDy1 - dx2, -dydzDz + dy1, -dz}, {-dxdzDz + dxdyDy1 + dx2, -dydzDz + dy1, -dz},
+                        {+dxdzDz - dxdyDy2 - dx3, +dydzDz - dy2, +dz}, {+dxdzDz - dxdyDy2 + dx3, +dydzDz - dy2, +dz},
+                        {+dxdzDz + dxdyDy2 - dx4, +dydzDz + dy2, +dz}, {+dxdzDz + dxdyDy2 + dx4, +dydzDz + dy2, +dz}};
+    // plane through p1..p4 (clockwise seen from inside): n = (p3 - p1) x (p4 - p2) normalised
+    // by multiplying with 1/|n|, d = -n . centroid
+    auto plane = [&](int i, const Vec3 &p1, const Vec3 &p2, const Vec3 &p3, const Vec3 &p4) {
+      const Vec3 a{p3.x - p1.x, p3.y - p1.y, p3.z - p1.z}, b{p4.x - p2.x, p4.y - p2.y, p4.z - p2.z};
+      Vec3 n{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+      const double inv = 1. / std::sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+      n                = {n.x * inv, n.y * inv, n.z * inv};
+      const Vec3 s{((p1.x + p2.x) + p3.x) + p4.x, ((p1.y + p2.y) + p3.y) + p4.y, ((p1.z + p2.z) + p3.z) + p4.z};
+      const Vec3 c{0.25 * s.x, 0.25 * s.y, 0.25 * s.z};
+      r[row::TrapA + i] = n.x;
+      r[row::TrapB + i] = n.y;
+      r[row::TrapC + i] = n.z;
+      r[row::TrapD + i] = -(n.x * c.x + n.y * c.y + n.z * c.z);
+    };
+    plane(0, pt[0], pt[1], pt[5], pt[4]);  // ~ -Y
+    plane(1, pt[2], pt[6], pt[7], pt[3]);  // ~ +Y
+    plane(2, pt[0], pt[4], pt[6], pt[2]);  // ~ -X
+    plane(3, pt[1], pt[3], pt[7], pt[5]);  // ~ +X
+    r[row::TrapDz]         = dz;
+    r[row::TrapTheta]      = theta;
+    r[row::TrapPhi]        = phi;
+    r[row::TrapDy1]        = dy1;
+    r[row::TrapDx1]        = dx1;
+    r[row::TrapDx2]        = dx2;
+    r[row::TrapTanAlpha1]  = tanA1;
+    r[row::TrapDy2]        = dy2;
+    r[row::TrapDx3]        = dx3;
+    r[row::TrapDx4]        = dx4;
+    r[row::TrapTanAlpha2]  = tanA2;
+    r[row::TrapTthetaCphi] = tcp;
+    r[row::TrapTthetaSphi] = tsp;
+    shape.insert(shape.end(), r, r + row::kTrapSize);
+    return VGN_OK;
+  }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
   }
 }
@@ -170,6 +255,36 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     const double m = r[row::ConeArgRmax1] > r[row::ConeArgRmax2] ? r[row::ConeArgRmax1] : r[row::ConeArgRmax2];
     mn = {-m, -m, -r[row::ConeDz]};
     mx = {m, m, r[row::ConeDz]};
+    return;
+  }
+  case kTrd: {  // UnplacedTrd::Extent (UnplacedTrd.h:218-222)
+    const double mxx = r[row::TrdDx1] > r[row::TrdDx2] ? r[row::TrdDx1] : r[row::TrdDx2];
+    const double mxy = r[row::TrdDy1] > r[row::TrdDy2] ? r[row::TrdDy1] : r[row::TrdDy2];
+    mn = {-mxx, -mxy, -r[row::TrdDz]};
+    mx = {mxx, mxy, r[row::TrdDz]};
+    return;
+  }
+  case kTrapezoid: {  // UnplacedTrapezoid::Extent through fromPlanesToCorners (source/UnplacedTrapezoid.cpp:297-337, 467-494)
+    const double dz = r[row::TrapDz];
+    const double *A = r + row::TrapA, *B = r + row::TrapB, *C = r + row::TrapC, *D = r + row::TrapD;
+    double y[8], x[8];
+    y[0] = y[1] = -(D[0] - dz * C[0]) / B[0];
+    y[2] = y[3] = -(D[1] - dz * C[1]) / B[1];
+    y[4] = y[5] = -(D[0] + dz * C[0]) / B[0];
+    y[6] = y[7] = -(D[1] + dz * C[1]) / B[1];
+    x[0] = ((B[2] / B[0]) * (D[0] - dz * C[0]) - (D[2] - dz * C[2])) / A[2];
+    x[1] = ((B[3] / B[0]) * (D[0] - dz * C[0]) - (D[3] - dz * C[3])) / A[3];
+    x[2] = ((B[2] / B[1]) * (D[1] - dz * C[1]) - (D[2] - dz * C[2])) / A[2];
+    x[3] = ((B[3] / B[1]) * (D[1] - dz * C[1]) - (D[3] - dz * C[3])) / A[3];
+    x[4] = ((B[2] / B[0]) * (D[0] + dz * C[0]) - (D[2] + dz * C[2])) / A[2];
+    x[5] = ((B[3] / B[0]) * (D[0] + dz * C[0]) - (D[3] + dz * C[3])) / A[3];
+    x[6] = ((B[2] / B[1]) * (D[1] + dz * C[1]) - (D[2] + dz * C[2])) / A[2];
+    x[7] = ((B[3] / B[1]) * (D[1] + dz * C[1]) - (D[3] + dz * C[3])) / A[3];
+    auto mx2 = [](double a, double b) { return a > b ? a : b; };
+    auto mn2 = [](double a, double b) { return a < b ? a : b; };
+    auto tree = [](const double *v, auto f) { return f(f(f(v[0], v[1]), f(v[2], v[3])), f(f(v[4], v[5]), f(v[6], v[7]))); };
+    mn = {tree(x, mn2), tree(y, mn2), -dz};
+    mx = {tree(x, mx2), tree(y, mx2), dz};
     return;
   }
   default: mn = mx = {0, 0, 0};

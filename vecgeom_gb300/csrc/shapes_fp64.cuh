@@ -567,6 +567,323 @@ __device__ __forceinline__ int cone_inside(const double *c, D3 p)
   return r;
 }
 
+// ---------------------------------------------------------------- Trd
+// UniversalTrd (volumes/kernel/TrdImplementation.h); the default build sets
+// VECGEOM_NO_SPECIALIZATION, so every Trd takes the runtime dy1 != dy2 test.
+namespace td = row;
+constexpr double kTiny = 1e-30;  // base/Math.h:51
+
+__device__ __forceinline__ bool trd_varying_y(const double *t) { return t[td::TrdDy1] != t[td::TrdDy2]; }
+
+// TrdUtilities::FaceTrajectoryIntersection (TrdImplementation.h:80-138); dist is
+// written only once the direction faces the plane.
+template <bool FOR_Y, bool MIRRORED, bool TO_INSIDE>
+__device__ __forceinline__ bool trd_face(const double *t, D3 pos, D3 dir, double &dist)
+{
+  double alongV, posV, dirV, posK, dirK, fV, fK, halfKplus, v1;
+  if (FOR_Y) {
+    alongV = t[td::TrdY2minusY1]; v1 = t[td::TrdDy1]; posV = pos.y; posK = pos.x; dirV = dir.y; dirK = dir.x;
+    fK = t[td::TrdFx]; fV = t[td::TrdFy]; halfKplus = t[td::TrdHalfX1plusX2];
+  } else {
+    alongV = t[td::TrdX2minusX1]; v1 = t[td::TrdDx1]; posV = pos.x; posK = pos.y; dirV = dir.x; dirK = dir.y;
+    fK = t[td::TrdFy]; fV = t[td::TrdFx]; halfKplus = t[td::TrdHalfY1plusY2];
+  }
+  if (MIRRORED) {
+    posV *= -1.;
+    dirV *= -1.;
+  }
+  const double ndotv = dirV + fV * dir.z;
+  bool ok            = TO_INSIDE ? ndotv < 0. : ndotv > 0.;
+  if (!ok) return false;
+  const double fdz    = t[td::TrdDz];
+  const double alongZ = 2.0 * fdz;
+  dist = (alongZ * (posV - v1) - alongV * (pos.z + fdz)) / (dir.z * alongV - dirV * alongZ + kTiny);
+  ok   = dist > (0. - kHalfTolerance);
+  if (ok) {
+    const double hitz = pos.z + dist * dir.z;
+    ok                = fabs(hitz) <= fdz;
+    const double hitk = posK + dist * dirK;
+    const double dK   = halfKplus - fK * hitz;
+    ok                = ok && fabs(hitk) <= dK;
+    if (ok && fabs(dist) < kHalfTolerance) dist = 0.0;
+  }
+  return ok;
+}
+
+// TrdUtilities::Safety (TrdImplementation.h:140-168)
+__device__ __forceinline__ double trd_safety(const double *t, D3 p, bool inside)
+{
+  double dist        = t[td::TrdDz] - fabs(p.z);
+  const double distx = t[td::TrdHalfX1plusX2] - t[td::TrdFx] * p.z;
+  const double safx  = (distx - fabs(p.x)) * t[td::TrdCalfX];
+  if (distx >= 0 && safx < dist) dist = safx;
+  if (trd_varying_y(t)) {
+    const double disty = t[td::TrdHalfY1plusY2] - t[td::TrdFy] * p.z;
+    const double safy  = (disty - fabs(p.y)) * t[td::TrdCalfY];
+    if (disty >= 0 && safy < dist) dist = safy;
+  } else {
+    const double safy = t[td::TrdDy1] - fabs(p.y);
+    if (safy < dist) dist = safy;
+  }
+  return inside ? dist : -dist;
+}
+__device__ __forceinline__ double trd_safe_in(const double *t, D3 p) { return trd_safety(t, p, false); }
+__device__ __forceinline__ double trd_safe_out(const double *t, D3 p) { return trd_safety(t, p, true); }
+
+// TrdUtilities::UnplacedInside (TrdImplementation.h:170-214), general y test
+template <bool SURFACE>
+__device__ __forceinline__ void trd_unplaced_inside(const double *t, D3 p, bool &cin, bool &cout)
+{
+  const double fdz      = t[td::TrdDz];
+  const double pzPlusDz = p.z + fdz;
+  cout                  = fabs(p.z) > (SURFACE ? fdz + kHalfTolerance : fdz);
+  if (SURFACE) cin = fabs(p.z) < fdz - kHalfTolerance;
+  double cross = t[td::TrdX2minusX1] * pzPlusDz - (2.0 * fdz) * (fabs(p.x) - t[td::TrdDx1]);
+  if (SURFACE) {
+    cout = cout || cross < -t[td::TrdTolX];
+    cin  = cin && cross > t[td::TrdTolX];
+  } else {
+    cout = cout || cross < 0;
+  }
+  cross = t[td::TrdY2minusY1] * pzPlusDz - (2.0 * fdz) * (fabs(p.y) - t[td::TrdDy1]);
+  if (SURFACE) {
+    cout = cout || cross < -t[td::TrdTolY];
+    cin  = cin && cross > t[td::TrdTolY];
+  } else {
+    cout = cout || cross < 0;
+  }
+}
+
+__device__ __forceinline__ bool trd_contains(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  trd_unplaced_inside<false>(t, p, cin, cout);
+  return !cout;
+}
+
+__device__ __forceinline__ int trd_inside(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  trd_unplaced_inside<true>(t, p, cin, cout);
+  int r = kSurfaceE;
+  if (cin) r = kInsideE;
+  if (cout) r = kOutsideE;
+  return r;
+}
+
+__device__ __forceinline__ double trd_clamp(double d) { return fabs(d) < kHalfTolerance ? 0.0 : d; }
+
+// DistanceToIn (TrdImplementation.h:300-394)
+__device__ __forceinline__ double trd_dist_in(const double *t, D3 p, D3 d)
+{
+  const double fdz = t[td::TrdDz];
+  double distance  = kInfLength;
+  const bool inz   = fabs(p.z) < fdz - kHalfTolerance;
+  double distx     = t[td::TrdHalfX1plusX2] - t[td::TrdFx] * p.z;
+  const bool inx   = (distx - fabs(p.x)) * t[td::TrdCalfX] > 0. + kHalfTolerance;
+  const bool vary  = trd_varying_y(t);
+  double disty;
+  bool iny;
+  if (vary) {
+    disty = t[td::TrdHalfY1plusY2] - t[td::TrdFy] * p.z;
+    iny   = (disty - fabs(p.y)) * t[td::TrdCalfY] > 0. + kHalfTolerance;
+  } else {
+    disty = fabs(p.y) - t[td::TrdDy1];
+    iny   = disty < 0. - kHalfTolerance;
+  }
+  if (inx && iny && inz) return -1.;  // |-1| >= kHalfTolerance: no clamp
+  if (p.z * d.z < 0. && !inz) {
+    const double distz = (fabs(p.z) - fdz) / fabs(d.z);
+    const double hitx  = fabs(p.x + distz * d.x);
+    const double hity  = fabs(p.y + distz * d.y);
+    const bool okzt    = p.z > (fdz - kHalfTolerance) && hitx <= t[td::TrdDx2] && hity <= t[td::TrdDy2];
+    const bool okzb    = p.z < (-fdz + kHalfTolerance) && hitx <= t[td::TrdDx1] && hity <= t[td::TrdDy1];
+    if (okzt || okzb) return trd_clamp(distz);
+  }
+  if (!inx) {
+    if (trd_face<false, false, true>(t, p, d, distx)) distance = distx;
+    if (trd_face<false, true, true>(t, p, d, distx)) return trd_clamp(distx);
+  }
+  if (vary) {
+    if (!iny) {
+      if (trd_face<true, false, true>(t, p, d, disty)) distance = disty;
+      if (trd_face<true, true, true>(t, p, d, disty)) distance = disty;
+    }
+  } else if (!iny) {
+    disty /= fabs(d.y);
+    const double zhit = p.z + disty * d.z;
+    const double xhit = p.x + disty * d.x;
+    const double dx   = t[td::TrdHalfX1plusX2] - t[td::TrdFx] * zhit;
+    if (p.y * d.y < 0 && disty > -kHalfTolerance && fabs(xhit) < dx && fabs(zhit) < fdz) distance = disty;
+  }
+  return trd_clamp(distance);
+}
+
+// DistanceToOut (TrdImplementation.h:396-499), scalar early returns
+__device__ __forceinline__ double trd_dist_out(const double *t, D3 p, D3 d)
+{
+  const double fdz    = t[td::TrdDz];
+  const double invdir = 1. / fabs(d.z + kTiny);
+  bool out            = (fdz - fabs(p.z)) < 0. - kHalfTolerance;
+  double distx        = t[td::TrdHalfX1plusX2] - t[td::TrdFx] * p.z;
+  out                 = out || (distx - fabs(p.x)) * t[td::TrdCalfX] < 0. - kHalfTolerance;
+  const bool vary     = trd_varying_y(t);
+  double disty;
+  if (vary) {
+    disty = t[td::TrdHalfY1plusY2] - t[td::TrdFy] * p.z;
+    out   = out || (disty - fabs(p.y)) * t[td::TrdCalfY] < 0. - kHalfTolerance;
+  } else {
+    disty = t[td::TrdDy1] - fabs(p.y);
+    out   = out || disty < 0. - kHalfTolerance;
+  }
+  if (out) return -1.;
+  if (d.z > 0.) {
+    const double distz = (fdz - p.z) * invdir;
+    if (fabs(p.x + distz * d.x) <= t[td::TrdDx2] && fabs(p.y + distz * d.y) <= t[td::TrdDy2]) return trd_clamp(distz);
+  }
+  if (d.z < 0.) {
+    const double distz = (p.z + fdz) * invdir;
+    if (fabs(p.x + distz * d.x) <= t[td::TrdDx1] && fabs(p.y + distz * d.y) <= t[td::TrdDy1]) return trd_clamp(distz);
+  }
+  if (trd_face<false, false, false>(t, p, d, distx)) return trd_clamp(distx);
+  if (trd_face<false, true, false>(t, p, d, distx)) return trd_clamp(distx);
+  double distance = 0.0;
+  if (vary) {
+    if (trd_face<true, false, false>(t, p, d, disty)) return trd_clamp(disty);
+    if (trd_face<true, true, false>(t, p, d, disty)) distance = disty;
+  } else {
+    const double plane = d.y < 0. ? -t[td::TrdDy1] : t[td::TrdDy1];
+    disty              = (plane - p.y) / d.y;
+    const double zhit  = p.z + disty * d.z;
+    const double xhit  = p.x + disty * d.x;
+    const double dx    = t[td::TrdHalfX1plusX2] - t[td::TrdFx] * zhit;
+    if (fabs(xhit) < dx && fabs(zhit) < fdz) distance = disty;
+  }
+  return trd_clamp(distance);
+}
+
+// ---------------------------------------------------------------- Trapezoid
+// volumes/kernel/TrapezoidImplementation.h over the four side planes of
+// base/PlaneShell.h (the default VECGEOM_PLANESHELL=ON build).
+__device__ __forceinline__ double trap_pdist(const double *t, int i, D3 p)
+{
+  return t[row::TrapA + i] * p.x + t[row::TrapB + i] * p.y + t[row::TrapC + i] * p.z + t[row::TrapD + i];
+}
+__device__ __forceinline__ double trap_proj(const double *t, int i, D3 d)
+{
+  return t[row::TrapA + i] * d.x + t[row::TrapB + i] * d.y + t[row::TrapC + i] * d.z;
+}
+
+// GenericKernelForContainsAndInside (TrapezoidImplementation.h:124-162, PlaneShell.h:130-151)
+template <bool FOR_INSIDE>
+__device__ __forceinline__ void trap_generic_ci(const double *t, D3 p, bool &cin, bool &cout)
+{
+  const double dz = t[row::TrapDz];
+  cout            = fabs(p.z) > (FOR_INSIDE ? dz + kHalfTolerance : dz);
+  if (FOR_INSIDE) cin = fabs(p.z) < dz - kHalfTolerance;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double dist = trap_pdist(t, i, p);
+    cout              = cout || dist > (FOR_INSIDE ? 0. + kHalfTolerance : 0.);
+    if (FOR_INSIDE) cin = cin && dist < 0. - kHalfTolerance;
+  }
+}
+
+__device__ __forceinline__ bool trap_contains(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  trap_generic_ci<false>(t, p, cin, cout);
+  return !cout;
+}
+
+__device__ __forceinline__ int trap_inside(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  trap_generic_ci<true>(t, p, cin, cout);
+  int r = kSurfaceE;
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+// DistanceToIn (TrapezoidImplementation.h:177-216, PlaneShell.h:161-213), scalar early returns
+__device__ __forceinline__ double trap_dist_in(const double *t, D3 p, D3 d)
+{
+  const double dz       = t[row::TrapDz];
+  const double signZdir = sgn(d.z);
+  const double max      = signZdir * dz - p.z;
+  if (signZdir * max < 0.0 + kHalfTolerance) return kInfLength;
+  const double invdir = 1.0 / nonzero(d.z);
+  double smax         = max * invdir;
+  double smin         = -(signZdir * dz + p.z) * invdir;
+  double pdist[4], proj[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    pdist[i] = trap_pdist(t, i, p);
+    proj[i]  = trap_proj(t, i, d);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (pdist[i] > 0. + kHalfTolerance && proj[i] >= 0.) return kInfLength;
+    if (pdist[i] > 0. - kHalfTolerance && proj[i] > 0.) return kInfLength;
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double vdist     = -pdist[i] / nonzero(proj[i]);
+    const bool posPoint    = pdist[i] > 0. - kHalfTolerance;
+    const bool posDir      = proj[i] > 0;
+    const bool fromInside  = !posPoint && posDir;
+    const bool fromOutside = posPoint && !posDir;
+    if (fromInside && vdist < smin) return kInfLength;
+    if (fromOutside && vdist > smax) return kInfLength;
+    if (fromOutside && vdist > smin) smin = vdist;
+    if (fromInside && vdist < smax) smax = vdist;
+  }
+  return smin <= smax ? smin : kInfLength;
+}
+
+// DistanceToOut (TrapezoidImplementation.h:270-299, PlaneShell.h:219-257)
+__device__ __forceinline__ double trap_dist_out(const double *t, D3 p, D3 d)
+{
+  const double dz = t[row::TrapDz];
+  if (fabs(p.z) > dz + kHalfTolerance) return -1.0;
+  double distance = kInfLength;
+  if (d.z != 0.) distance = (sgn(d.z) * dz - p.z) / nonzero(d.z);
+  double distOut = kInfLength;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double pdist = trap_pdist(t, i, p);
+    const double proj  = trap_proj(t, i, d);
+    const double vdist = -pdist / nonzero(proj);
+    if (pdist > kHalfTolerance) distOut = -1.;
+    if (proj > 0. && vdist < distOut) distOut = vdist;
+  }
+  return distOut < distance ? distOut : distance;
+}
+
+// SafetyToIn / SafetyToOut (TrapezoidImplementation.h:341-401, PlaneShell.h:260-305)
+__device__ __forceinline__ double trap_safe_in(const double *t, D3 p)
+{
+  double safety = fabs(p.z) - t[row::TrapDz];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double dist = trap_pdist(t, i, p);
+    if (dist > safety) safety = dist;
+  }
+  return safety;
+}
+
+__device__ __forceinline__ double trap_safe_out(const double *t, D3 p)
+{
+  double safety = t[row::TrapDz] - fabs(p.z);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double dist = -trap_pdist(t, i, p);
+    if (dist < safety) safety = dist;
+  }
+  return safety;
+}
+
 // ---------------------------------------------------------------- dispatch
 __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
@@ -574,6 +891,8 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   case kBox: return box_dist_in(r, p, d);
   case kTube: return tube_dist_in(r, p, d);
   case kCone: return cone_dist_in(r, p, d);
+  case kTrd: return trd_dist_in(r, p, d);
+  case kTrapezoid: return trap_dist_in(r, p, d);
   }
   return kInfLength;
 }
@@ -584,6 +903,8 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   case kBox: return box_dist_out(r, p, d);
   case kTube: return tube_dist_out(r, p, d);
   case kCone: return cone_dist_out(r, p, d);
+  case kTrd: return trd_dist_out(r, p, d);
+  case kTrapezoid: return trap_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -594,6 +915,8 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   case kBox: return box_safe_in(r, p);
   case kTube: return tube_safe_in(r, p);
   case kCone: return cone_safe_in(r, p);
+  case kTrd: return trd_safe_in(r, p);
+  case kTrapezoid: return trap_safe_in(r, p);
   }
   return kInfLength;
 }
@@ -604,6 +927,8 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   case kBox: return box_safe_out(r, p);
   case kTube: return tube_safe_out(r, p);
   case kCone: return cone_safe_out(r, p);
+  case kTrd: return trd_safe_out(r, p);
+  case kTrapezoid: return trap_safe_out(r, p);
   }
   return 0.;
 }
@@ -614,6 +939,8 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   case kBox: return box_contains(r, p);
   case kTube: return tube_contains(r, p);
   case kCone: return cone_contains(r, p);
+  case kTrd: return trd_contains(r, p);
+  case kTrapezoid: return trap_contains(r, p);
   }
   return false;
 }
@@ -624,6 +951,8 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   case kBox: return box_inside(r, p);
   case kTube: return tube_inside(r, p);
   case kCone: return cone_inside(r, p);
+  case kTrd: return trd_inside(r, p);
+  case kTrapezoid: return trap_inside(r, p);
   }
   return kOutsideE;
 }

@@ -305,3 +305,99 @@ def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_l
     dx, dy, dz = isotropic(np.random.Generator(np.random.PCG64(seed_dirs)), n)
     return TrackBatch(p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), dx, dy, dz, np.full(n, step_limit),
                       np.zeros(n, dtype=STATE_DTYPE))
+
+
+# ---------------------------------------------------------------- mixed shapes
+# Shape types the library implements, in enum order.
+IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID)
+MIXED_WORLD = 2000.0
+MIXED_GRID = (16, 16, 32)  # 8192 cells of 250 x 250 x 125 mm
+MIXED_JITTER = 5.0
+
+
+def _mixed_shape_params(rng: np.random.Generator, shape: int):
+    """Parameters with every length drawn from U[5, 60] mm (Tube radii from U[5, 40] mm),
+    and the half-extent of the shape's bounding box."""
+    u = lambda lo=5.0, hi=60.0: float(rng.uniform(lo, hi))
+    if shape == BOX:
+        p = (u(), u(), u())
+        return p, np.array(p)
+    if shape == TUBE:
+        a, b = sorted((u(5.0, 40.0), u(5.0, 40.0)))
+        rmin, rmax = (a, b) if b - a > 1.0 else (0.0, b)
+        p = (rmin, rmax, u(), 0.0, K_TWO_PI)
+        return p, np.array([rmax, rmax, p[2]])
+    if shape == CONE:
+        rmax1, rmax2, dz = u(), u(), u()
+        solid = rng.uniform() < 0.5
+        rmin1 = 0.0 if solid else float(rng.uniform(0.0, 0.8)) * rmax1
+        rmin2 = 0.0 if solid else float(rng.uniform(0.0, 0.8)) * rmax2
+        r = max(rmax1, rmax2)
+        return (rmin1, rmax1, rmin2, rmax2, dz, 0.0, K_TWO_PI), np.array([r, r, dz])
+    if shape == TRD:
+        x1, x2, y1, dz = u(), u(), u(), u()
+        y2 = y1 if rng.uniform() < 0.25 else u()  # a quarter keep y constant (the reference's Trd1 case)
+        return (x1, x2, y1, y2, dz), np.array([max(x1, x2), max(y1, y2), dz])
+    if shape == TRAPEZOID:
+        dz, dy1, dx1, dx2, dy2, dx3, dx4 = (u() for _ in range(7))
+        theta = math.radians(rng.uniform(0.0, 20.0))
+        phi = rng.uniform(0.0, K_TWO_PI)
+        a1, a2 = (math.radians(rng.uniform(-15.0, 15.0)) for _ in range(2))
+        p = (dz, theta, phi, dy1, dx1, dx2, a1, dy2, dx3, dx4, a2)
+        return p, trapezoid_corners(p).__abs__().max(axis=0)
+    raise ValueError(f"shape {shape} not implemented")
+
+
+_LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
+                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9)}
+
+
+def trapezoid_corners(p) -> np.ndarray:
+    """The eight corners of Trapezoid(dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2)."""
+    dz, theta, phi, dy1, dx1, dx2, a1, dy2, dx3, dx4, a2 = p
+    tcp, tsp = math.tan(theta) * math.cos(phi), math.tan(theta) * math.sin(phi)
+    t1, t2 = math.tan(a1) * dy1, math.tan(a2) * dy2
+    cx, cy = tcp * dz, tsp * dz
+    return np.array([[-cx - t1 - dx1, -cy - dy1, -dz], [-cx - t1 + dx1, -cy - dy1, -dz],
+                     [-cx + t1 - dx2, -cy + dy1, -dz], [-cx + t1 + dx2, -cy + dy1, -dz],
+                     [cx - t2 - dx3, cy - dy2, dz], [cx - t2 + dx3, cy - dy2, dz],
+                     [cx + t2 - dx4, cy + dy2, dz], [cx + t2 + dx4, cy + dy2, dz]])
+
+
+def mixed_shape_geometry(seed: int = 21, grid=MIXED_GRID, world: float = MIXED_WORLD,
+                         shapes=IMPLEMENTED_SHAPES) -> GeometryDescription:
+    """World box of half-length `world` holding one daughter per cell of a
+    jittered grid (16 x 16 x 32 = 8192 cells of 250 x 250 x 125 mm by default);
+    shape types uniform over `shapes`, lengths from U[5, 60] mm, each daughter
+    rotated by a uniform random rotation (Euler angles phi, psi ~ U[0, 360),
+    cos(theta) ~ U[-1, 1]).  A daughter whose bounding sphere (plus the jitter)
+    would leave its cell is scaled down to fit, so daughters never overlap."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nx, ny, nz = grid
+    pitch = np.array([2 * world / nx, 2 * world / ny, 2 * world / nz])
+    limit = 0.5 * pitch.min() - MIXED_JITTER - 0.5
+    b = GeometryBuilder()
+    world_lv = b.logical(BOX, (world, world, world))
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                shape = shapes[int(rng.integers(len(shapes)))]
+                params, ext = _mixed_shape_params(rng, shape)
+                radius = float(np.sqrt(np.sum(ext * ext)))
+                if radius > limit:
+                    params = list(params)
+                    for q in _LENGTH_INDICES[shape]:
+                        params[q] *= limit / radius
+                lv = b.logical(shape, params)
+                c = -world + pitch * (np.array([i, j, k]) + 0.5) + rng.uniform(-MIXED_JITTER, MIXED_JITTER, 3)
+                phi, psi = rng.uniform(0.0, 360.0, 2)
+                theta = math.degrees(math.acos(rng.uniform(-1.0, 1.0)))
+                b.place(lv, world_lv, transform_euler(c[0], c[1], c[2], phi, theta, psi))
+    b.place_world(world_lv)
+    return b.build()
+
+
+def mixed_shape_tracks(n: int, seed_points: int = 22, seed_dirs: int = 23, world: float = MIXED_WORLD,
+                       step_limit: float = 1000.0) -> TrackBatch:
+    """Points uniform in the world box (to be located before stepping), isotropic directions."""
+    return uniform_tracks(n, world * (1.0 - 1e-9), seed_points, seed_dirs, step_limit)
