@@ -261,6 +261,7 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_CONE: return 7;
   case OR_TRD: return 5;
   case OR_TRAP: return 11;
+  case OR_SPHERE: return 6;
   default: (void)p; (void)avail; return -1;
   }
 }

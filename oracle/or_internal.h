@@ -32,6 +32,7 @@
 #define kTwoPi (2. * kPi)
 #define kHalfPi (0.5 * kPi)
 #define kAngTolerance 1e-9
+#define kSqrtTolerance 3.1622777e-5 /* base/Math.h:29 */
 
 typedef struct { double x, y, z; } v3;
 
@@ -113,6 +114,14 @@ typedef struct { /* TrapezoidStruct.h:41-59 with the PlaneShell<4> side planes (
   double a[4], b[4], c[4], d[4];
 } or_trap;
 
+typedef struct { /* SphereStruct.h:21-51, full phi and full theta */
+  double rmin, rmax;
+  /* evolution::Wedge built from the constructor's raw (dphi, sphi) (source/Wedge_Evolution.cpp:17-99) */
+  double a1x, a1y, a2x, a2y, n1x, n1y, n2x, n2y, wdphi;
+  /* ThetaCone built from the raw (stheta, dtheta) (ThetaCone_Evolution.h:62-82) */
+  double tsTheta, teTheta, tanSTheta, tanETheta;
+} or_sphere;
+
 typedef struct {
   int type;
   int param_off;
@@ -125,6 +134,7 @@ typedef struct {
     or_cone cone;
     or_trd trd;
     or_trap trap;
+    or_sphere sph;
   } s;
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;

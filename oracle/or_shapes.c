@@ -1168,6 +1168,267 @@ static void trap_extent(const or_trap *t, v3 *mn, v3 *mx)
 }
 
 /* ================================================================== */
+/* Sphere (full phi, full theta): kernel/SphereImplementation.h,      */
+/* SphereUtilities.h, Wedge_Evolution.h, ThetaCone_Evolution.h        */
+/* ================================================================== */
+
+/* SphereStruct(rmin, rmax, sphi, dphi, stheta, dtheta) (SphereStruct.h:285-304); only the
+ * full sphere (dphi >= 2pi - kAngTolerance/2, stheta = 0, stheta + dtheta >= pi) is
+ * accepted.  The wedge and theta cone keep the raw constructor angles. */
+static int sphere_init(or_sphere *t, const double *a, char *err, int errlen)
+{
+  const double rmin = a[0], rmax = a[1], sphi = a[2], dphi = a[3], stheta = a[4], dtheta = a[5];
+  if (!(rmin >= 0 && rmax > rmin)) {
+    set_err(err, errlen, "Sphere: needs 0 <= rmin < rmax");
+    return -1;
+  }
+  if (!(dphi >= 2 * kPi - kAngTolerance * 0.5) || stheta != 0. || !(dtheta + stheta >= kPi)) {
+    set_err(err, errlen, "Sphere: phi and theta sections are not supported");
+    return -2;
+  }
+  t->rmin  = rmin;
+  t->rmax  = rmax;
+  t->a1x   = cos(sphi);
+  t->a1y   = sin(sphi);
+  t->a2x   = cos(sphi + dphi);
+  t->a2y   = sin(sphi + dphi);
+  t->n1x   = -sin(sphi);
+  t->n1y   = cos(sphi);
+  t->n2x   = sin(sphi + dphi);
+  t->n2y   = -cos(sphi + dphi);
+  t->wdphi = dphi;
+  t->tsTheta = stheta;
+  t->teTheta = stheta + dtheta;
+  double ts = t->tsTheta, te = t->teTheta;
+  if (t->tsTheta > kPi / 2) ts = kPi - t->tsTheta;
+  if (t->teTheta > kPi / 2) te = kPi - t->teTheta;
+  t->tanSTheta = tan(ts);
+  t->tanETheta = tan(te);
+  return 0;
+}
+
+#define kThetaHalfPi (0.5 * kPi) /* ThetaCone_Evolution.h:13 */
+#define kThetaTol 1e-9           /* ThetaCone::kAngTolerance = kTolerance */
+
+/* Wedge::IsOnSurfaceGeneric (Wedge_Evolution.h:341-354) */
+static inline int wedge_on_surface(double ax, double ay, double nx, double ny, v3 p)
+{
+  if (!(ax * p.x + ay * p.y >= 0.)) return 0;
+  return fabs(nx * p.x + ny * p.y) < kTolerance;
+}
+
+/* Wedge::GenericKernelForContainsAndInside (Wedge_Evolution.h:306-339) */
+static void wedge_ci(const or_sphere *t, v3 p, int forInside, int *cin, int *cout)
+{
+  double startCheck = (-p.x * t->a1y + p.y * t->a1x);
+  double endCheck   = (-t->a2x * p.y + t->a2y * p.x);
+  *cout             = startCheck < 0.;
+  if (t->wdphi < kPi)
+    *cout = *cout || endCheck < 0.;
+  else
+    *cout = *cout && endCheck < 0.;
+  if (forInside) {
+    int onSurface = wedge_on_surface(t->a1x, t->a1y, t->n1x, t->n1y, p) ||
+                    wedge_on_surface(t->a2x, t->a2y, t->n2x, t->n2y, p);
+    *cout = *cout && !onSurface;
+    *cin  = !onSurface && !*cout;
+  }
+}
+
+static inline int wedge_contains(const or_sphere *t, v3 p)
+{
+  int cin = 0, cout = 0;
+  wedge_ci(t, p, 0, &cin, &cout);
+  return !cout;
+}
+
+/* ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730) for stheta = 0, etheta >= pi */
+static int theta_completely_inside(const or_sphere *t, v3 p)
+{
+  const double sT = t->tsTheta, eT = t->teTheta;
+  double rho         = sqrt(v3_dot(p, p) - (p.z * p.z));
+  double cone1Radius = fabs(p.z * t->tanSTheta);
+  double cone2Radius = fabs(p.z * t->tanETheta);
+  int onZ  = p.z != 0. && p.x == 0. && p.y == 0.;
+  int onXY = p.z == 0. && (p.x != 0. || p.y != 0.);
+  int ci   = onZ && ((sT == 0. && eT == kPi) || (p.z > 0. && sT == 0.) || (p.z < 0. && eT == kPi));
+  ci = ci || (!ci && (onXY && (sT < kThetaHalfPi && eT > kThetaHalfPi && (kThetaHalfPi - sT) > kThetaTol &&
+                               (eT - kThetaHalfPi) > kTolerance)));
+  /* fSTheta < pi/2 + tol/2 and fETheta > pi/2 + tol/2 with fSTheta < fETheta */
+  double tolAngMin = cone1Radius + 2 * kThetaTol * 10.;
+  double tolAngMax = cone2Radius + 2 * kThetaTol * 10.;
+  ci = ci || (!ci && ((rho >= tolAngMin && p.z > 0.) || (rho >= tolAngMax && p.z < 0.)));
+  return ci;
+}
+
+/* ThetaCone::IsCompletelyOutside (ThetaCone_Evolution.h:733-805) for stheta = 0, etheta >= pi */
+static int theta_completely_outside(const or_sphere *t, v3 p)
+{
+  const double sT = t->tsTheta, eT = t->teTheta;
+  double diff        = p.x * p.x + p.y * p.y;
+  double rho         = sqrt(diff);
+  double cone1Radius = fabs(p.z * t->tanSTheta);
+  double cone2Radius = fabs(p.z * t->tanETheta);
+  int onZ  = p.z != 0. && p.x == 0. && p.y == 0.;
+  int co   = onZ && ((sT != 0. && eT != kPi) || (p.z > 0. && sT != 0.) || (p.z < 0. && eT != kPi));
+  /* the on-xy-plane term needs both angles on one side of pi/2: never for a full theta range */
+  double tolAngMin2 = cone1Radius - 2 * kThetaTol * 10.;
+  double tolAngMax2 = cone2Radius - 2 * kThetaTol * 10.;
+  co = co || (!co && ((rho < tolAngMin2 && p.z > 0.) || (rho < tolAngMax2 && p.z < 0.)));
+  return co;
+}
+
+/* SphereUtilities::IsCompletelyInside / IsCompletelyOutside (SphereUtilities.h:110-141) */
+static int sphere_completely_inside(const or_sphere *t, v3 p)
+{
+  double rad = sqrt(v3_dot(p, p));
+  int inRad  = (rad < (t->rmax - kTolerance)) && (rad > (t->rmin + kTolerance));
+  int cin = 0, cout = 0;
+  wedge_ci(t, p, 1, &cin, &cout);
+  int inTheta = theta_completely_inside(t, p);
+  return inRad && cin && inTheta;
+}
+
+static int sphere_completely_outside(const or_sphere *t, v3 p)
+{
+  double rad = sqrt(v3_dot(p, p));
+  int outRad = (rad > (t->rmax + kTolerance)) || (rad < (t->rmin - kTolerance));
+  int cin = 0, cout = 0;
+  wedge_ci(t, p, 1, &cin, &cout);
+  int outTheta = theta_completely_outside(t, p);
+  return outRad || cout || outTheta;
+}
+
+
+/* SphereUtilities::IsPointOnSurfaceAndMovingOut (SphereUtilities.h:143-195); the phi and
+ * theta faces do not take part for a full sphere */
+static int sphere_on_surface_moving(const or_sphere *t, v3 p, v3 d, int movingOut)
+{
+  double mag2 = v3_dot(p, p);
+  int onOuter = mag2 <= plus_tol_sq(t->rmax, kTolerance) && mag2 >= minus_tol_sq(t->rmax, kTolerance);
+  double dp   = v3_dot(d, p);
+  int outer   = onOuter && (movingOut ? dp > kSqrtTolerance : dp < -kSqrtTolerance);
+  int inner   = 0;
+  if (t->rmin != 0.) {
+    int onInner = mag2 <= plus_tol_sq(t->rmin, kTolerance) && mag2 >= minus_tol_sq(t->rmin, kTolerance);
+    double dmp  = d.x * -p.x + d.y * -p.y + d.z * -p.z;
+    inner       = onInner && (movingOut ? dmp > kSqrtTolerance : dmp < -kSqrtTolerance);
+  }
+  return (outer || inner) && wedge_contains(t, p) && !theta_completely_outside(t, p);
+}
+
+/* SphereImplementation::GenericKernelForContainsAndInside (SphereImplementation.h:89-136) */
+static void sphere_ci(const or_sphere *t, v3 p, int *cin, int *cout)
+{
+  double rad2 = v3_dot(p, p);
+  if (t->rmin != 0.) {
+    *cin  = rad2 <= minus_tol_sq(t->rmax, kTolerance) && rad2 >= plus_tol_sq(t->rmin, kTolerance);
+    *cout = rad2 >= plus_tol_sq(t->rmax, kTolerance) || rad2 <= minus_tol_sq(t->rmin, kTolerance);
+  } else {
+    *cin  = rad2 <= minus_tol_sq(t->rmax, kTolerance);
+    *cout = rad2 >= plus_tol_sq(t->rmax, kTolerance);
+  }
+}
+
+static int sphere_contains(const or_sphere *t, v3 p)
+{
+  int cin = 0, cout = 0;
+  sphere_ci(t, p, &cin, &cout);
+  return !cout;
+}
+
+static int sphere_inside(const or_sphere *t, v3 p) /* SphereImplementation.h:74-87 */
+{
+  int cin = 0, cout = 0, r = kSurfaceE;
+  sphere_ci(t, p, &cin, &cout);
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+/* DistanceToIn (SphereImplementation.h:138-256), full sphere */
+static double sphere_dist_in(const or_sphere *t, v3 p, v3 d)
+{
+  double rad2    = v3_dot(p, p);
+  double pDotV3d = v3_dot(p, d);
+  double c       = rad2 - t->rmax * t->rmax;
+  if (sphere_completely_inside(t, p)) return -1.0;
+  if (sphere_on_surface_moving(t, p, d, 0)) return 0.0;
+  double d2 = (pDotV3d * pDotV3d - c);
+  if (d2 < 0. || ((c > 0.) && (pDotV3d > 0.))) return kInfLength;
+  double sd1 = kInfLength, sd2 = kInfLength;
+  if (d2 >= 0.) sd1 = (-pDotV3d - sqrt(fabs(d2)));
+  double outerDist = kInfLength, innerDist = kInfLength;
+  if (sd1 >= 0.) outerDist = sd1;
+  if (t->rmin != 0.) {
+    c  = rad2 - t->rmin * t->rmin;
+    d2 = pDotV3d * pDotV3d - c;
+    if (d2 >= 0.) sd2 = (-pDotV3d + sqrt(fabs(d2)));
+    if (sd2 >= 0.) innerDist = sd2;
+  }
+  double distance = or_min(outerDist, innerDist);
+  return or_min(kInfLength, distance);
+}
+
+/* DistanceToOut (SphereImplementation.h:258-341), full sphere */
+static double sphere_dist_out(const or_sphere *t, v3 p, v3 d)
+{
+  double pDotV3d = v3_dot(p, d);
+  double rad2    = v3_dot(p, p);
+  double c       = rad2 - t->rmax * t->rmax;
+  if (sphere_completely_outside(t, p)) return -1.0;
+  if (sphere_on_surface_moving(t, p, d, 1)) return 0.0;
+  double sd1 = kInfLength, sd2 = kInfLength;
+  double d2  = (pDotV3d * pDotV3d - c);
+  if (d2 >= 0.) sd1 = (-pDotV3d + sqrt(fabs(d2)));
+  if (t->rmin != 0.) {
+    c  = rad2 - t->rmin * t->rmin;
+    d2 = (pDotV3d * pDotV3d - c);
+    if ((d2 >= 0.) && (pDotV3d < 0.)) sd2 = (-pDotV3d - sqrt(fabs(d2)));
+  }
+  double snxt = or_min(sd1, sd2);
+  return or_min(kInfLength, snxt);
+}
+
+/* SafetyToIn / SafetyToOut (SphereImplementation.h:388-479), full sphere */
+static double sphere_safe_in(const or_sphere *t, v3 p)
+{
+  double rad = sqrt(v3_dot(p, p));
+  int cin = 0, cout = 0;
+  sphere_ci(t, p, &cin, &cout);
+  if (cin) return -1.0;
+  if (!cin && !cout) return 0.0;
+  if (t->rmin != 0.) {
+    double safeRMin = t->rmin - rad;
+    double safeRMax = rad - t->rmax;
+    return safeRMin > safeRMax ? safeRMin : safeRMax;
+  }
+  return rad - t->rmax;
+}
+
+static double sphere_safe_out(const or_sphere *t, v3 p)
+{
+  double rad = sqrt(v3_dot(p, p));
+  int cin = 0, cout = 0;
+  sphere_ci(t, p, &cin, &cout);
+  if (cout) return -1.0;
+  if (!cin && !cout) return 0.0;
+  if (t->rmin != 0.) {
+    double safeRMin = (rad - t->rmin);
+    double safeRMax = (t->rmax - rad);
+    return safeRMin < safeRMax ? safeRMin : safeRMax;
+  }
+  return t->rmax - rad;
+}
+
+/* UnplacedSphere::Extent, full sphere (source/UnplacedSphere.cpp:76-83) */
+static void sphere_extent(const or_sphere *t, v3 *mn, v3 *mx)
+{
+  *mn = v3_make(-t->rmax, -t->rmax, -t->rmax);
+  *mx = v3_make(t->rmax, t->rmax, t->rmax);
+}
+
+/* ================================================================== */
 /* dispatch                                                           */
 /* ================================================================== */
 
@@ -1184,6 +1445,7 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
   case OR_CONE: return cone_init(&lv->s.cone, p, err, errlen);
   case OR_TRD: return trd_init(&lv->s.trd, p, err, errlen);
   case OR_TRAP: return trap_init(&lv->s.trap, p, err, errlen);
+  case OR_SPHERE: return sphere_init(&lv->s.sph, p, err, errlen);
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -1199,6 +1461,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
   case OR_CONE: cone_extent(&lv->s.cone, mn, mx); return;
   case OR_TRD: trd_extent(&lv->s.trd, mn, mx); return;
   case OR_TRAP: trap_extent(&lv->s.trap, mn, mx); return;
+  case OR_SPHERE: sphere_extent(&lv->s.sph, mn, mx); return;
   }
 }
 
@@ -1215,6 +1478,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_CONE: return cone_dist_in(&lv->s.cone, p, d);
   case OR_TRD: return trd_dist_in(&lv->s.trd, p, d);
   case OR_TRAP: return trap_dist_in(&lv->s.trap, p, d);
+  case OR_SPHERE: return sphere_dist_in(&lv->s.sph, p, d);
   }
   return kInfLength;
 }
@@ -1229,6 +1493,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_CONE: return cone_dist_out(&lv->s.cone, p, d);
   case OR_TRD: return trd_dist_out(&lv->s.trd, p, d);
   case OR_TRAP: return trap_dist_out(&lv->s.trap, p, d);
+  case OR_SPHERE: return sphere_dist_out(&lv->s.sph, p, d);
   }
   return -1.;
 }
@@ -1242,6 +1507,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_CONE: return cone_safe_in(&lv->s.cone, p);
   case OR_TRD: return trd_safety(&lv->s.trd, p, 0);
   case OR_TRAP: return trap_safe_in(&lv->s.trap, p);
+  case OR_SPHERE: return sphere_safe_in(&lv->s.sph, p);
   }
   return kInfLength;
 }
@@ -1255,6 +1521,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_CONE: return cone_safe_out(&lv->s.cone, p);
   case OR_TRD: return trd_safety(&lv->s.trd, p, 1);
   case OR_TRAP: return trap_safe_out(&lv->s.trap, p);
+  case OR_SPHERE: return sphere_safe_out(&lv->s.sph, p);
   }
   return 0.;
 }
@@ -1268,6 +1535,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_CONE: return cone_contains(&lv->s.cone, p);
   case OR_TRD: return trd_contains(&lv->s.trd, p);
   case OR_TRAP: return trap_contains(&lv->s.trap, p);
+  case OR_SPHERE: return sphere_contains(&lv->s.sph, p);
   }
   return 0;
 }
@@ -1281,6 +1549,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_CONE: return cone_inside(&lv->s.cone, p);
   case OR_TRD: return trd_inside(&lv->s.trd, p);
   case OR_TRAP: return trap_inside(&lv->s.trap, p);
+  case OR_SPHERE: return sphere_inside(&lv->s.sph, p);
   }
   return kOutsideE;
 }

@@ -547,7 +547,80 @@ TRAP_CASES += [
           (-16.483749999999997, -6.4512999999999989, 0.00000099999999999999995), vx, INF, "inf"),
 ]
 
-ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES
+SPHERE = 5
+SP = "test/unit_tests/TestSphere.cpp"
+PI_T = 3.14159265358979323846  # TestSphere.cpp:12
+# UnplacedSphere(rmin, rmax, sphi, dphi, stheta, dtheta)
+SPH_B4 = (6.0, 8.0, 0.0, 2 * PI_T, 0.0, PI_T)    # TestSphere.cpp:34, 90
+SPH_S1 = (0.0, 50.0, 0.0, 2 * PI_T, 0.0, PI_T)   # TestSphere.cpp:416
+SPH_S2 = (45.0, 50.0, 0.0, 2 * PI_T, 0.0, PI_T)  # TestSphere.cpp:429
+_R2 = math.sqrt(2.0)
+_ponrmin1, _ponrmax1 = (45.0, 0.0, 0.0), (50.0, 0.0, 0.0)  # TestSphere.cpp:389-391
+_ponrmin2, _ponrmax2 = (45 / _R2, 45 / _R2, 0.0), (50 / _R2, 50 / _R2, 0.0)
+SPHERE_CASES = [
+    _case(f"{SP}:95", SPHERE, SPH_B4, "inside", (0.337317535387103, 6.265557026812151, 3.103064940359008), None, 1, "eq"),
+    _case(f"{SP}:100", SPHERE, SPH_B4, "inside", (0.162722224118177, -8.624868144449298, -2.566158796458579), None, 3,
+          "eq"),
+    _case(f"{SP}:105", SPHERE, SPH_B4, "inside", (-2.393620784732096, -4.753290873255242, 5.973006396542139), None, 2,
+          "eq"),
+    _case(f"{SP}:111", SPHERE, SPH_B4, "inside", (-4.231374871926247, -4.183095200116632, -0.772775025466741), None,
+          2, "eq"),
+    _case(f"{SP}:126", SPHERE, SPH_B4, "safe_in", (100.0, 0.0, 0.0), None, 92.0),
+    _case(f"{SP}:130", SPHERE, SPH_B4, "safe_out", pzero, None, 0.0, "le0"),
+    _case(f"{SP}:133", SPHERE, SPH_B4, "safe_out", (0.162722224118177, -8.624868144449298, -2.566158796458579), None,
+          0.0, "le0"),
+    _case(f"{SP}:137", SPHERE, SPH_B4, "safe_out", (9.0, 0.0, 0.0), None, 0.0, "le0"),
+    _case(f"{SP}:141", SPHERE, SPH_B4, "safe_out", (0.0, 9.0, 0.0), None, 0.0, "le0"),
+    _case(f"{SP}:145", SPHERE, SPH_B4, "safe_out", (0.0, 0.0, 9.0), None, 0.0, "le0"),
+    _case(f"{SP}:149", SPHERE, SPH_B4, "safe_out", (6.5, 0.0, 0.0), None, 0.5),
+    _case(f"{SP}:153", SPHERE, SPH_B4, "safe_out", (0.0, 6.5, 0.0), None, 0.5),
+    _case(f"{SP}:157", SPHERE, SPH_B4, "safe_out", (0.0, 0.0, 6.5), None, 0.5),
+    _case(f"{SP}:161", SPHERE, SPH_B4, "safe_out", (7.5, 0.0, 0.0), None, 0.5),
+    _case(f"{SP}:165", SPHERE, SPH_B4, "safe_out", (0.0, 7.5, 0.0), None, 0.5),
+    _case(f"{SP}:169", SPHERE, SPH_B4, "safe_out", (0.0, 0.0, 7.5), None, 0.5),
+    _case(f"{SP}:173", SPHERE, SPH_B4, "safe_in", (7.5, 0.0, 0.0), None, 0.0, "le0"),
+    _case(f"{SP}:176", SPHERE, SPH_B4, "safe_in", (0.0, 7.5, 0.0), None, 0.0, "le0"),
+    _case(f"{SP}:179", SPHERE, SPH_B4, "safe_in", (0.0, 0.0, 7.5), None, 0.0, "le0"),
+    _case(f"{SP}:185", SPHERE, SPH_B4, "safe_in", (3.796560684305335, -6.207283535497058, 2.519078815824183), None,
+          0.0, "le0"),
+    _case(f"{SP}:553", SPHERE, SPH_S1, "inside", pzero, None, 1, "eq"),
+    _case(f"{SP}:554", SPHERE, SPH_S2, "inside", pzero, None, 3, "eq"),
+    _case(f"{SP}:555", SPHERE, SPH_S2, "inside", _ponrmin2, None, 2, "eq"),
+    _case(f"{SP}:556", SPHERE, SPH_S2, "inside", _ponrmax2, None, 2, "eq"),
+    _case(f"{SP}:602", SPHERE, SPH_S1, "safe_out", pzero, None, 50.0),
+    _case(f"{SP}:604", SPHERE, SPH_S1, "safe_out", _ponrmax1, None, 0.0),
+    _case(f"{SP}:606", SPHERE, SPH_S1, "safe_out", (30.0, 0.0, 0.0), None, 20.0),
+    _case(f"{SP}:609", SPHERE, SPH_S2, "safe_out", pzero, None, 0.0, "le0"),
+    _case(f"{SP}:612", SPHERE, SPH_S2, "safe_out", _ponrmax1, None, 0.0),
+    _case(f"{SP}:614", SPHERE, SPH_S2, "safe_out", _ponrmin1, None, 0.0),
+    _case(f"{SP}:648", SPHERE, SPH_S1, "dist_out", (0.0, 0.0, 30.0), vz, 20.0),
+    _case(f"{SP}:652", SPHERE, SPH_S1, "dist_out", _ponrmax1, vx, 0.0),
+    _case(f"{SP}:656", SPHERE, SPH_S2, "dist_out", _ponrmin1, vx, 5.0),
+    _case(f"{SP}:661", SPHERE, SPH_S2, "dist_out", _ponrmax2, vx, 0.0),
+    _case(f"{SP}:665", SPHERE, SPH_S1, "dist_out", pzero, vx, 50.0),
+    _case(f"{SP}:668", SPHERE, SPH_S1, "dist_out", pzero, vmx, 50.0),
+    _case(f"{SP}:671", SPHERE, SPH_S1, "dist_out", pzero, vy, 50.0),
+    _case(f"{SP}:674", SPHERE, SPH_S1, "dist_out", pzero, vmy, 50.0),
+    _case(f"{SP}:677", SPHERE, SPH_S1, "dist_out", pzero, vz, 50.0),
+    _case(f"{SP}:680", SPHERE, SPH_S1, "dist_out", pzero, vmz, 50.0),
+    _case(f"{SP}:683", SPHERE, SPH_S1, "dist_out", pzero, vxy, 50.0),
+    _case(f"{SP}:715", SPHERE, SPH_S2, "dist_out", (100.0, 0.0, 0.0), vx, 0.0, "le0"),
+    _case(f"{SP}:718", SPHERE, SPH_S2, "dist_out", (100.0, 0.0, 0.0), vmx, 0.0, "le0"),
+    _case(f"{SP}:722", SPHERE, SPH_S2, "dist_out", (0.0, 100.0, 0.0), vy, 0.0, "le0"),
+    _case(f"{SP}:725", SPHERE, SPH_S2, "dist_out", (0.0, 100.0, 0.0), vmy, 0.0, "le0"),
+    _case(f"{SP}:826", SPHERE, SPH_S2, "safe_in", pzero, None, 45.0),
+    _case(f"{SP}:828", SPHERE, SPH_S1, "safe_in", _ponrmax1, None, 0.0),
+    _case(f"{SP}:841", SPHERE, SPH_S1, "dist_in", (0.0, 100.0, 0.0), vy, INF, "inf"),
+    _case(f"{SP}:844", SPHERE, SPH_S1, "dist_in", (0.0, 100.0, 0.0), vmy, 50.0),
+    _case(f"{SP}:847", SPHERE, SPH_S2, "dist_in", pzero, vy, 45.0),
+    _case(f"{SP}:850", SPHERE, SPH_S2, "dist_in", pzero, vmy, 45.0),
+    _case(f"{SP}:852", SPHERE, SPH_S2, "dist_in", _ponrmin1, vx, 0.0, "eq"),
+    _case(f"{SP}:855", SPHERE, SPH_S2, "dist_in", _ponrmin1, vmx, 90.0),
+    _case(f"{SP}:859", SPHERE, SPH_S2, "dist_in", _ponrmin2, vx, 0.0, "eq"),
+    _case(f"{SP}:861", SPHERE, SPH_S2, "dist_in", _ponrmin2, vmx, 90 / _R2),
+]
+
+ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:

@@ -277,6 +277,9 @@ SHAPE_SETS = [
     ("trap-skewed", W.TRAPEZOID, (60.0, 0.35, 0.087, 40.0, 30.0, 40.0, 0.17, 16.0, 10.0, 14.0, 0.17)),
     ("trap-twisted-alpha", W.TRAPEZOID, (30.0, 0.1, 2.0, 20.0, 10.0, 25.0, -0.3, 35.0, 30.0, 12.0, 0.25)),
     ("trap-boxlike", W.TRAPEZOID, (40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0)),
+    ("sphere-solid", W.SPHERE, (0.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
+    ("sphere-shell", W.SPHERE, (45.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
+    ("sphere-shell-rotated-wedge", W.SPHERE, (6.0, 8.0, 1.0, W.K_TWO_PI, 0.0, W.K_PI)),
 ]
 
 
@@ -290,6 +293,12 @@ def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda)
     n = 100000
     reach = 1.3 * float(np.abs(W.trapezoid_corners(params)).max()) if shape == W.TRAPEZOID else 1.3 * max(params[:5])
     x, y, z = (rng.uniform(-reach, reach, n) for _ in range(3))
+    # points on the coordinate planes and axes and at the origin (exact zeros take their own branches)
+    y[:4000] = 0.0
+    x[4000:8000] = 0.0
+    x[8000:9000] = y[8000:9000] = 0.0
+    x[9000:9500] = z[9000:9500] = 0.0
+    x[9500], y[9500], z[9500] = 0.0, 0.0, 0.0
     dx, dy, dz = W.isotropic(rng, n)
     # surface points: from inside points, move to the exit point along a random ray
     inside = og.shape(0, OPS["contains"], x, y, z) == 1.0

@@ -80,6 +80,13 @@ def test_invalid_descriptions_rejected(vgnav):
     with pytest.raises(N.VgnError) as e:
         HostTables(b.build())
     assert e.value.code == N.VGN_ERR_UNSUPPORTED
+    for shape, params in ((W.SPHERE, (0.0, 10.0, 0.0, 1.0, 0.0, W.K_PI)),   # phi section
+                          (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0))):  # theta section
+        b = W.GeometryBuilder()
+        b.place_world(b.logical(shape, params))
+        with pytest.raises(N.VgnError) as e:
+            HostTables(b.build())
+        assert e.value.code == N.VGN_ERR_UNSUPPORTED
     b = W.GeometryBuilder()
     lv = b.logical(99, (1.0,))
     b.place_world(lv)

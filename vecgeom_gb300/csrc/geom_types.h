@@ -142,6 +142,10 @@ enum { TrdDx1 = 0, TrdDx2, TrdDy1, TrdDy2, TrdDz, TrdX2minusX1, TrdY2minusY1, Tr
 // each of 4), then the TrapezoidStruct parameters and cached values
 enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, TrapTheta = 17, TrapPhi, TrapDy1, TrapDx1, TrapDx2,
        TrapTanAlpha1, TrapDy2, TrapDx3, TrapDx4, TrapTanAlpha2, TrapTthetaCphi, TrapTthetaSphi, kTrapSize = 32 };
+// Sphere (full phi and theta): radii, the phi wedge's along/normal vectors and raw
+// delta-phi, the theta cone's raw start/end angles and tangents
+enum { SphRmin = 0, SphRmax, SphA1x, SphA1y, SphA2x, SphA2y, SphN1x, SphN1y, SphN2x, SphN2y, SphWedgeDPhi,
+       SphSTheta, SphETheta, SphTanSTheta, SphTanETheta, SphPad, kSphereSize };
 }  // namespace row
 
 // Plain-pointer view of the device tables, passed to kernels by value.

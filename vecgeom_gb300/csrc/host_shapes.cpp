@@ -29,6 +29,7 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
   case kCone: return 7;
   case kTrd: return 5;
   case kTrapezoid: return 11;
+  case kSphere: return 6;
   default: return -1;
   }
 }
@@ -236,6 +237,39 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.insert(shape.end(), r, r + row::kTrapSize);
     return VGN_OK;
   }
+  case kSphere: {
+    // SphereStruct(rmin, rmax, sphi, dphi, stheta, dtheta) (SphereStruct.h:285-304), full
+    // sphere only; its Wedge (source/Wedge_Evolution.cpp:17-99) and ThetaCone
+    // (ThetaCone_Evolution.h:62-82) are built from the raw constructor angles
+    const double rmin = p[0], rmax = p[1], sphi = p[2], dphi = p[3], stheta = p[4], dtheta = p[5];
+    if (!(rmin >= 0 && rmax > rmin)) {
+      err = "Sphere needs 0 <= rmin < rmax";
+      return VGN_ERR_ARG;
+    }
+    if (!(dphi >= kTwoPi - kAngTolerance * 0.5) || stheta != 0. || !(dtheta + stheta >= kPi)) {
+      err = "Sphere phi and theta sections are not supported";
+      return VGN_ERR_UNSUPPORTED;
+    }
+    double r[row::kSphereSize] = {};
+    r[row::SphRmin]      = rmin;
+    r[row::SphRmax]      = rmax;
+    r[row::SphA1x]       = std::cos(sphi);
+    r[row::SphA1y]       = std::sin(sphi);
+    r[row::SphA2x]       = std::cos(sphi + dphi);
+    r[row::SphA2y]       = std::sin(sphi + dphi);
+    r[row::SphN1x]       = -std::sin(sphi);
+    r[row::SphN1y]       = std::cos(sphi);
+    r[row::SphN2x]       = std::sin(sphi + dphi);
+    r[row::SphN2y]       = -std::cos(sphi + dphi);
+    r[row::SphWedgeDPhi] = dphi;
+    const double sT = stheta, eT = stheta + dtheta;
+    r[row::SphSTheta]    = sT;
+    r[row::SphETheta]    = eT;
+    r[row::SphTanSTheta] = std::tan(sT > kPi / 2 ? kPi - sT : sT);
+    r[row::SphTanETheta] = std::tan(eT > kPi / 2 ? kPi - eT : eT);
+    shape.insert(shape.end(), r, r + row::kSphereSize);
+    return VGN_OK;
+  }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
   }
 }
@@ -285,6 +319,12 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     auto tree = [](const double *v, auto f) { return f(f(f(v[0], v[1]), f(v[2], v[3])), f(f(v[4], v[5]), f(v[6], v[7]))); };
     mn = {tree(x, mn2), tree(y, mn2), -dz};
     mx = {tree(x, mx2), tree(y, mx2), dz};
+    return;
+  }
+  case kSphere: {  // UnplacedSphere::Extent, full sphere (source/UnplacedSphere.cpp:76-83)
+    const double rmax = r[row::SphRmax];
+    mn = {-rmax, -rmax, -rmax};
+    mx = {rmax, rmax, rmax};
     return;
   }
   default: mn = mx = {0, 0, 0};

@@ -884,6 +884,222 @@ __device__ __forceinline__ double trap_safe_out(const double *t, D3 p)
   return safety;
 }
 
+// ---------------------------------------------------------------- Sphere (full)
+// volumes/kernel/SphereImplementation.h with SphereUtilities.h.  Even a full sphere
+// consults its phi wedge (Wedge_Evolution.h) and theta cone (ThetaCone_Evolution.h)
+// in the completely-inside/outside and on-surface tests; both are reproduced here
+// for the full ranges (stheta = 0, etheta >= pi).
+namespace sp = row;
+constexpr double kSqrtTolerance = 3.1622777e-5;  // base/Math.h:29
+constexpr double kThetaHalfPi   = 0.5 * 3.14159265358979323846;
+constexpr double kPiD           = 3.14159265358979323846;
+
+__device__ __forceinline__ double sph_plus_tol_sq(double x) { return x * (x + 2.0 * kTolerance); }
+__device__ __forceinline__ double sph_minus_tol_sq(double x) { return fabs(x * (x - 2.0 * kTolerance)); }
+__device__ __forceinline__ double mag2(D3 p) { return p.x * p.x + p.y * p.y + p.z * p.z; }
+
+// Wedge::IsOnSurfaceGeneric (Wedge_Evolution.h:341-354)
+__device__ __forceinline__ bool wedge_on_surface(double ax, double ay, double nx, double ny, D3 p)
+{
+  if (!(ax * p.x + ay * p.y >= 0.)) return false;
+  return fabs(nx * p.x + ny * p.y) < kTolerance;
+}
+
+// Wedge::GenericKernelForContainsAndInside (Wedge_Evolution.h:306-339)
+template <bool FOR_INSIDE>
+__device__ __forceinline__ void wedge_ci(const double *t, D3 p, bool &cin, bool &cout)
+{
+  const double startCheck = (-p.x * t[sp::SphA1y] + p.y * t[sp::SphA1x]);
+  const double endCheck   = (-t[sp::SphA2x] * p.y + t[sp::SphA2y] * p.x);
+  cout                    = startCheck < 0.;
+  if (t[sp::SphWedgeDPhi] < kPiD)
+    cout = cout || endCheck < 0.;
+  else
+    cout = cout && endCheck < 0.;
+  if (FOR_INSIDE) {
+    const bool onSurface = wedge_on_surface(t[sp::SphA1x], t[sp::SphA1y], t[sp::SphN1x], t[sp::SphN1y], p) ||
+                           wedge_on_surface(t[sp::SphA2x], t[sp::SphA2y], t[sp::SphN2x], t[sp::SphN2y], p);
+    cout = cout && !onSurface;
+    cin  = !onSurface && !cout;
+  }
+}
+
+// ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730), stheta = 0 and etheta >= pi
+__device__ __forceinline__ bool theta_completely_inside(const double *t, D3 p)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double rho         = sqrt(mag2(p) - (p.z * p.z));
+  const double cone1Radius = fabs(p.z * t[sp::SphTanSTheta]);
+  const double cone2Radius = fabs(p.z * t[sp::SphTanETheta]);
+  const bool onZ           = p.z != 0. && p.x == 0. && p.y == 0.;
+  const bool onXY          = p.z == 0. && (p.x != 0. || p.y != 0.);
+  bool ci = onZ && ((sT == 0. && eT == kPiD) || (p.z > 0. && sT == 0.) || (p.z < 0. && eT == kPiD));
+  ci      = ci || (!ci && (onXY && (sT < kThetaHalfPi && eT > kThetaHalfPi && (kThetaHalfPi - sT) > kTolerance &&
+                                   (eT - kThetaHalfPi) > kTolerance)));
+  const double tolAngMin = cone1Radius + 2 * kTolerance * 10.;
+  const double tolAngMax = cone2Radius + 2 * kTolerance * 10.;
+  return ci || (!ci && ((rho >= tolAngMin && p.z > 0.) || (rho >= tolAngMax && p.z < 0.)));
+}
+
+// ThetaCone::IsCompletelyOutside (ThetaCone_Evolution.h:733-805), stheta = 0 and etheta >= pi
+__device__ __forceinline__ bool theta_completely_outside(const double *t, D3 p)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double rho         = sqrt(p.x * p.x + p.y * p.y);
+  const double cone1Radius = fabs(p.z * t[sp::SphTanSTheta]);
+  const double cone2Radius = fabs(p.z * t[sp::SphTanETheta]);
+  const bool onZ           = p.z != 0. && p.x == 0. && p.y == 0.;
+  const bool co = onZ && ((sT != 0. && eT != kPiD) || (p.z > 0. && sT != 0.) || (p.z < 0. && eT != kPiD));
+  const double tolAngMin2 = cone1Radius - 2 * kTolerance * 10.;
+  const double tolAngMax2 = cone2Radius - 2 * kTolerance * 10.;
+  return co || (!co && ((rho < tolAngMin2 && p.z > 0.) || (rho < tolAngMax2 && p.z < 0.)));
+}
+
+// SphereUtilities::IsCompletelyInside / IsCompletelyOutside (SphereUtilities.h:110-141)
+__device__ __forceinline__ bool sphere_completely_inside(const double *t, D3 p)
+{
+  const double rad   = sqrt(mag2(p));
+  const bool inRad   = (rad < (t[sp::SphRmax] - kTolerance)) && (rad > (t[sp::SphRmin] + kTolerance));
+  bool cin = false, cout = false;
+  wedge_ci<true>(t, p, cin, cout);
+  return inRad && cin && theta_completely_inside(t, p);
+}
+
+__device__ __forceinline__ bool sphere_completely_outside(const double *t, D3 p)
+{
+  const double rad  = sqrt(mag2(p));
+  const bool outRad = (rad > (t[sp::SphRmax] + kTolerance)) || (rad < (t[sp::SphRmin] - kTolerance));
+  bool cin = false, cout = false;
+  wedge_ci<true>(t, p, cin, cout);
+  return outRad || cout || theta_completely_outside(t, p);
+}
+
+// SphereUtilities::IsPointOnSurfaceAndMovingOut (SphereUtilities.h:143-195), radial faces only
+template <bool MOVING_OUT>
+__device__ __forceinline__ bool sphere_on_surface_moving(const double *t, D3 p, D3 d)
+{
+  const double m2   = mag2(p);
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  const double dp   = d.x * p.x + d.y * p.y + d.z * p.z;
+  const bool outer  = (m2 <= sph_plus_tol_sq(rmax) && m2 >= sph_minus_tol_sq(rmax)) &&
+                     (MOVING_OUT ? dp > kSqrtTolerance : dp < -kSqrtTolerance);
+  bool inner = false;
+  if (rmin != 0.) {
+    const double dmp = d.x * -p.x + d.y * -p.y + d.z * -p.z;
+    inner            = (m2 <= sph_plus_tol_sq(rmin) && m2 >= sph_minus_tol_sq(rmin)) &&
+            (MOVING_OUT ? dmp > kSqrtTolerance : dmp < -kSqrtTolerance);
+  }
+  if (!(outer || inner)) return false;
+  bool cin = false, cout = false;
+  wedge_ci<false>(t, p, cin, cout);
+  return !cout && !theta_completely_outside(t, p);
+}
+
+// SphereImplementation::GenericKernelForContainsAndInside (SphereImplementation.h:89-136)
+__device__ __forceinline__ void sphere_ci(const double *t, D3 p, bool &cin, bool &cout)
+{
+  const double rad2 = mag2(p);
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  if (rmin != 0.) {
+    cin  = rad2 <= sph_minus_tol_sq(rmax) && rad2 >= sph_plus_tol_sq(rmin);
+    cout = rad2 >= sph_plus_tol_sq(rmax) || rad2 <= sph_minus_tol_sq(rmin);
+  } else {
+    cin  = rad2 <= sph_minus_tol_sq(rmax);
+    cout = rad2 >= sph_plus_tol_sq(rmax);
+  }
+}
+
+__device__ __forceinline__ bool sphere_contains(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  sphere_ci(t, p, cin, cout);
+  return !cout;
+}
+
+__device__ __forceinline__ int sphere_inside(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  sphere_ci(t, p, cin, cout);
+  int r = kSurfaceE;
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+// DistanceToIn (SphereImplementation.h:138-256), full sphere
+__device__ __forceinline__ double sphere_dist_in(const double *t, D3 p, D3 d)
+{
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  const double rad2    = mag2(p);
+  const double pDotV3d = p.x * d.x + p.y * d.y + p.z * d.z;
+  double c             = rad2 - rmax * rmax;
+  if (sphere_completely_inside(t, p)) return -1.0;
+  if (sphere_on_surface_moving<false>(t, p, d)) return 0.0;
+  double d2 = (pDotV3d * pDotV3d - c);
+  if (d2 < 0. || ((c > 0.) && (pDotV3d > 0.))) return kInfLength;
+  double outerDist = kInfLength, innerDist = kInfLength;
+  const double sd1 = d2 >= 0. ? (-pDotV3d - sqrt(fabs(d2))) : kInfLength;
+  if (sd1 >= 0.) outerDist = sd1;
+  if (rmin != 0.) {
+    c                = rad2 - rmin * rmin;
+    d2               = pDotV3d * pDotV3d - c;
+    const double sd2 = d2 >= 0. ? (-pDotV3d + sqrt(fabs(d2))) : kInfLength;
+    if (sd2 >= 0.) innerDist = sd2;
+  }
+  return vmin(kInfLength, vmin(outerDist, innerDist));
+}
+
+// DistanceToOut (SphereImplementation.h:258-341), full sphere
+__device__ __forceinline__ double sphere_dist_out(const double *t, D3 p, D3 d)
+{
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  const double pDotV3d = p.x * d.x + p.y * d.y + p.z * d.z;
+  const double rad2    = mag2(p);
+  double c             = rad2 - rmax * rmax;
+  if (sphere_completely_outside(t, p)) return -1.0;
+  if (sphere_on_surface_moving<true>(t, p, d)) return 0.0;
+  double d2        = (pDotV3d * pDotV3d - c);
+  const double sd1 = d2 >= 0. ? (-pDotV3d + sqrt(fabs(d2))) : kInfLength;
+  double sd2       = kInfLength;
+  if (rmin != 0.) {
+    c  = rad2 - rmin * rmin;
+    d2 = (pDotV3d * pDotV3d - c);
+    if ((d2 >= 0.) && (pDotV3d < 0.)) sd2 = (-pDotV3d - sqrt(fabs(d2)));
+  }
+  return vmin(kInfLength, vmin(sd1, sd2));
+}
+
+// SafetyToIn / SafetyToOut (SphereImplementation.h:388-479), full sphere
+__device__ __forceinline__ double sphere_safe_in(const double *t, D3 p)
+{
+  const double rad = sqrt(mag2(p));
+  bool cin = false, cout = false;
+  sphere_ci(t, p, cin, cout);
+  if (cin) return -1.0;
+  if (!cout) return 0.0;
+  if (t[sp::SphRmin] != 0.) {
+    const double safeRMin = t[sp::SphRmin] - rad;
+    const double safeRMax = rad - t[sp::SphRmax];
+    return safeRMin > safeRMax ? safeRMin : safeRMax;
+  }
+  return rad - t[sp::SphRmax];
+}
+
+__device__ __forceinline__ double sphere_safe_out(const double *t, D3 p)
+{
+  const double rad = sqrt(mag2(p));
+  bool cin = false, cout = false;
+  sphere_ci(t, p, cin, cout);
+  if (cout) return -1.0;
+  if (!cin) return 0.0;
+  if (t[sp::SphRmin] != 0.) {
+    const double safeRMin = (rad - t[sp::SphRmin]);
+    const double safeRMax = (t[sp::SphRmax] - rad);
+    return safeRMin < safeRMax ? safeRMin : safeRMax;
+  }
+  return t[sp::SphRmax] - rad;
+}
+
 // ---------------------------------------------------------------- dispatch
 __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
@@ -893,6 +1109,7 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   case kCone: return cone_dist_in(r, p, d);
   case kTrd: return trd_dist_in(r, p, d);
   case kTrapezoid: return trap_dist_in(r, p, d);
+  case kSphere: return sphere_dist_in(r, p, d);
   }
   return kInfLength;
 }
@@ -905,6 +1122,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   case kCone: return cone_dist_out(r, p, d);
   case kTrd: return trd_dist_out(r, p, d);
   case kTrapezoid: return trap_dist_out(r, p, d);
+  case kSphere: return sphere_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -917,6 +1135,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   case kCone: return cone_safe_in(r, p);
   case kTrd: return trd_safe_in(r, p);
   case kTrapezoid: return trap_safe_in(r, p);
+  case kSphere: return sphere_safe_in(r, p);
   }
   return kInfLength;
 }
@@ -929,6 +1148,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   case kCone: return cone_safe_out(r, p);
   case kTrd: return trd_safe_out(r, p);
   case kTrapezoid: return trap_safe_out(r, p);
+  case kSphere: return sphere_safe_out(r, p);
   }
   return 0.;
 }
@@ -941,6 +1161,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   case kCone: return cone_contains(r, p);
   case kTrd: return trd_contains(r, p);
   case kTrapezoid: return trap_contains(r, p);
+  case kSphere: return sphere_contains(r, p);
   }
   return false;
 }
@@ -953,6 +1174,7 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   case kCone: return cone_inside(r, p);
   case kTrd: return trd_inside(r, p);
   case kTrapezoid: return trap_inside(r, p);
+  case kSphere: return sphere_inside(r, p);
   }
   return kOutsideE;
 }

@@ -309,7 +309,7 @@ def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_l
 
 # ---------------------------------------------------------------- mixed shapes
 # Shape types the library implements, in enum order.
-IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID)
+IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE)
 MIXED_WORLD = 2000.0
 MIXED_GRID = (16, 16, 32)  # 8192 cells of 250 x 250 x 125 mm
 MIXED_JITTER = 5.0
@@ -345,11 +345,15 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int):
         a1, a2 = (math.radians(rng.uniform(-15.0, 15.0)) for _ in range(2))
         p = (dz, theta, phi, dy1, dx1, dx2, a1, dy2, dx3, dx4, a2)
         return p, trapezoid_corners(p).__abs__().max(axis=0)
+    if shape == SPHERE:
+        rmax = u()
+        rmin = 0.0 if rng.uniform() < 0.5 else float(rng.uniform(0.1, 0.9)) * rmax
+        return (rmin, rmax, 0.0, K_TWO_PI, 0.0, K_PI), np.array([rmax, rmax, rmax])
     raise ValueError(f"shape {shape} not implemented")
 
 
 _LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
-                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9)}
+                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1)}
 
 
 def trapezoid_corners(p) -> np.ndarray:
