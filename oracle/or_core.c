@@ -262,6 +262,13 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_TRD: return 5;
   case OR_TRAP: return 11;
   case OR_SPHERE: return 6;
+  case OR_POLYCONE: { /* sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] */
+    int nz;
+    if (avail < 3 || !(p[2] >= 2 && p[2] <= 4096)) return -1;
+    nz = (int)p[2];
+    if ((double)nz != p[2]) return -1;
+    return 3 + 3 * nz;
+  }
   default: (void)p; (void)avail; return -1;
   }
 }
@@ -377,6 +384,11 @@ void or_geom_free(or_geom *g)
       free(g->lv[i].nchild);
       free(g->lv[i].nodes);
       free(g->lv[i].aabbs);
+      if (g->lv[i].type == OR_POLYCONE) {
+        free(g->lv[i].s.pcon.zs);
+        free(g->lv[i].s.pcon.shift);
+        free(g->lv[i].s.pcon.sec);
+      }
     }
   }
   free(g->lv);

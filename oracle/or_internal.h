@@ -122,6 +122,13 @@ typedef struct { /* SphereStruct.h:21-51, full phi and full theta */
   double tsTheta, teTheta, tanSTheta, tanETheta;
 } or_sphere;
 
+typedef struct { /* PolyconeStruct.h:24-37: z planes and one full-phi ConeStruct per section */
+  int nsec;
+  double *zs;    /* [nsec + 1] fZs */
+  double *shift; /* [nsec] PolyconeSection::fShift */
+  or_cone *sec;  /* [nsec] PolyconeSection::fSolid */
+} or_polycone;
+
 typedef struct {
   int type;
   int param_off;
@@ -135,6 +142,7 @@ typedef struct {
     or_trd trd;
     or_trap trap;
     or_sphere sph;
+    or_polycone pcon;
   } s;
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;

@@ -1429,6 +1429,328 @@ static void sphere_extent(const or_sphere *t, v3 *mn, v3 *mx)
 }
 
 /* ================================================================== */
+/* Polycone (full phi): kernel/PolyconeImplementation.h over the      */
+/* ConeStruct sections of PolyconeStruct                               */
+/* ================================================================== */
+
+/* UnplacedPolycone(phistart, deltaphi, Nz, z, rmin, rmax) -> PolyconeStruct::Init
+ * (UnplacedPolycone.h:78-88, PolyconeStruct.h:144-291): planes reversed when z runs
+ * downwards, one section per z step larger than kTolerance, each section a ConeStruct
+ * built with the raw phi arguments, shift = centre of the section in z.  The reference
+ * only prints a message for rmin > rmax or a z direction change; both are rejected here. */
+static int polycone_init(or_polycone *t, const double *a, char *err, int errlen)
+{
+  const double sphi = a[0], dphi = a[1];
+  const int nz      = (int)a[2];
+  const double *z0 = a + 3, *rin0 = a + 3 + nz, *rout0 = a + 3 + 2 * nz;
+  double *z = (double *)malloc(sizeof(double) * (size_t)nz * 3), *rin = z + nz, *rout = z + 2 * nz;
+  int i, rev = z0[0] > z0[nz - 1];
+  if (!z) return -1;
+  for (i = 0; i < nz; ++i) {
+    z[i]    = rev ? z0[nz - 1 - i] : z0[i];
+    rin[i]  = rev ? rin0[nz - 1 - i] : rin0[i];
+    rout[i] = rev ? rout0[nz - 1 - i] : rout0[i];
+  }
+  if (!(dphi >= kTwoPi - 0.5 * kAngTolerance)) {
+    free(z);
+    set_err(err, errlen, "Polycone: phi sections are not supported");
+    return -2;
+  }
+  for (i = 0; i < nz; ++i) {
+    if (!(rin[i] >= 0 && rout[i] >= rin[i]) || (i > 0 && !(z[i] >= z[i - 1]))) {
+      free(z);
+      set_err(err, errlen, "Polycone: needs 0 <= rmin <= rmax and monotonic z planes");
+      return -1;
+    }
+  }
+  t->zs    = (double *)malloc(sizeof(double) * (size_t)nz);
+  t->shift = (double *)malloc(sizeof(double) * (size_t)nz);
+  t->sec   = (or_cone *)calloc((size_t)nz, sizeof(or_cone));
+  t->nsec  = 0;
+  if (!t->zs || !t->shift || !t->sec) {
+    free(z);
+    return -1;
+  }
+  double prevZ = z[0], prevRmax = 0, prevRmin = 0;
+  int dirZ = 1, nzs = 0;
+  if (z[1] < z[0]) dirZ = -1;
+  for (i = 0; i < nz; ++i) {
+    double rMin = rin[i], rMax = rout[i], zz = z[i];
+    if (i > 0) {
+      if (((zz > prevZ + kTolerance) && (dirZ > 0)) || ((zz < prevZ - kTolerance) && (dirZ < 0))) {
+        double dz       = (zz - prevZ) / 2;
+        double cpar[7]  = {prevRmin, prevRmax, rMin, rMax, dz, sphi, dphi};
+        if (cone_init(&t->sec[t->nsec], cpar, err, errlen)) {
+          free(z);
+          return -1;
+        }
+        t->zs[nzs++]        = zz;
+        t->shift[t->nsec++] = t->zs[nzs - 2] + 0.5 * (t->zs[nzs - 1] - t->zs[nzs - 2]);
+      }
+    } else {
+      t->zs[nzs++] = zz;
+    }
+    prevZ    = zz;
+    prevRmin = rMin;
+    prevRmax = rMax;
+  }
+  free(z);
+  if (t->nsec == 0) {
+    set_err(err, errlen, "Polycone: no section longer than kTolerance");
+    return -1;
+  }
+  return 0;
+}
+
+/* PolyconeStruct::GetSectionIndex (PolyconeStruct.h:302-311) */
+static int polycone_section_index(const or_polycone *t, double zpos)
+{
+  if (zpos < t->zs[0]) return -1;
+  for (int i = 0; i < t->nsec; ++i)
+    if (zpos >= t->zs[i] && zpos <= t->zs[i + 1]) return i;
+  return -2;
+}
+
+static inline v3 pcon_local(const or_polycone *t, int i, v3 p) { return v3_make(p.x, p.y, p.z - t->shift[i]); }
+
+/* GenericKernelForASection (PolyconeImplementation.h:69-97) */
+static void polycone_section_ci(const or_polycone *t, int isect, v3 p, int forInside, int *cin, int *cout)
+{
+  if (isect < 0) {
+    *cin  = 0;
+    *cout = 1;
+    return;
+  }
+  cone_generic_ci(&t->sec[isect], pcon_local(t, isect, p), forInside, cin, cout);
+}
+
+/* GenericKernelForContainsAndInside (PolyconeImplementation.h:127-187); cin/cout keep
+ * the caller's initial values where the reference leaves them untouched */
+static void polycone_ci(const or_polycone *t, v3 p, int forInside, int *cin, int *cout)
+{
+  int indexLow  = polycone_section_index(t, p.z - kTolerance);
+  int indexHigh = polycone_section_index(t, p.z + kTolerance);
+  if (indexLow < 0 && indexHigh < 0) {
+    *cout = 1;
+    return;
+  }
+  if (indexLow < 0 && indexHigh == 0) {
+    polycone_section_ci(t, 0, p, forInside, cin, cout);
+    return;
+  }
+  if (indexHigh < 0 && indexLow == (t->nsec - 1)) {
+    polycone_section_ci(t, t->nsec - 1, p, forInside, cin, cout);
+    return;
+  }
+  if (indexLow >= 0 && indexHigh >= 0) {
+    if (indexLow == indexHigh) {
+      polycone_section_ci(t, indexLow, p, forInside, cin, cout);
+      return;
+    }
+    int secInLow = 0, secOutLow = 0, secInHigh = 0, secOutHigh = 0;
+    polycone_section_ci(t, indexLow, p, forInside, &secInLow, &secOutLow);
+    polycone_section_ci(t, indexHigh, p, forInside, &secInHigh, &secOutHigh);
+    int surfLow  = !secInLow && !secOutLow;
+    int surfHigh = !secInHigh && !secOutHigh;
+    if (surfLow && surfHigh) {
+      *cin = 1;
+      return;
+    }
+    if (secOutLow && secOutHigh) {
+      *cout = 1;
+      return;
+    }
+  }
+}
+
+static int polycone_contains(const or_polycone *t, v3 p) /* PolyconeImplementation.h:99-108 */
+{
+  int cin = 0, cout = 0;
+  polycone_ci(t, p, 0, &cin, &cout);
+  return !cout;
+}
+
+static int polycone_inside(const or_polycone *t, v3 p) /* PolyconeImplementation.h:112-125 */
+{
+  int cin = 0, cout = 0, r = kSurfaceE;
+  polycone_ci(t, p, 1, &cin, &cout);
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+/* DistanceToIn (PolyconeImplementation.h:189-237): sections visited from the point's own
+ * along the direction's z sign until one is hit */
+static double polycone_dist_in(const or_polycone *t, v3 p, v3 v)
+{
+  double distance = kInfLength;
+  int increment   = (v.z > 0) ? 1 : -1;
+  if (fabs(v.z) < kTolerance) increment = 0;
+  int index = polycone_section_index(t, p.z);
+  if (index == -1) index = 0;
+  if (index == -2) index = t->nsec - 1;
+  do {
+    distance = cone_dist_in(&t->sec[index], pcon_local(t, index, p), v);
+    if (distance < kInfLength || !increment) break;
+    index += increment;
+  } while (index >= 0 && index < t->nsec);
+  return distance;
+}
+
+/* DistanceToOut (PolyconeImplementation.h:239-379) */
+static double polycone_dist_out(const or_polycone *t, v3 point, v3 dir)
+{
+  double distance = kInfLength;
+  v3 pn           = point;
+  if (t->nsec == 1) return cone_dist_out(&t->sec[0], pcon_local(t, 0, point), dir);
+  int indexLow  = polycone_section_index(t, point.z - kTolerance);
+  int indexHigh = polycone_section_index(t, point.z + kTolerance);
+  int index     = 0;
+  if (indexLow < 0 && indexHigh < 0) {
+    return -1;
+  } else if (indexLow < 0 && indexHigh >= 0) {
+    index = indexHigh;
+    if (cone_inside(&t->sec[index], pcon_local(t, index, point)) == kOutsideE) return -1;
+  } else if (indexLow != indexHigh && (indexLow >= 0)) {
+    if (cone_inside(&t->sec[indexLow], pcon_local(t, indexLow, point)) == kOutsideE)
+      index = indexHigh;
+    else
+      index = indexLow;
+  } else {
+    index = indexLow;
+    if (index < 0) index = polycone_section_index(t, point.z);
+  }
+  if (index < 0) {
+    return 0.;
+  } else {
+    if (cone_inside(&t->sec[index], pcon_local(t, index, point)) == kOutsideE) return -1;
+  }
+  double totalDistance = 0., dist;
+  int increment        = (dir.z > 0) ? 1 : -1;
+  if (fabs(dir.z) < kTolerance) increment = 0;
+  int istep = 0;
+  do {
+    if ((totalDistance != 0) || (istep < 2)) {
+      pn = v3_make(point.x + totalDistance * dir.x, point.y + totalDistance * dir.y, point.z + totalDistance * dir.z);
+      pn.z -= t->shift[index];
+      if (cone_inside(&t->sec[index], pn) == kOutsideE) break;
+    } else
+      pn.z -= t->shift[index];
+    istep++;
+    dist = cone_dist_out(&t->sec[index], pn, dir);
+    if (dist == -1) return distance;
+    if (fabs(dist) < 0.5 * kTolerance) {
+      int index1 = index;
+      if ((index > 0) && (index < t->nsec - 1)) {
+        index1 += increment;
+      } else {
+        if ((index == 0) && (increment > 0)) index1 += increment;
+        if ((index == t->nsec - 1) && (increment < 0)) index1 += increment;
+      }
+      double td = totalDistance + dist;
+      v3 pte    = v3_make(point.x + td * dir.x, point.y + td * dir.y, point.z + td * dir.z);
+      pte.z -= t->shift[index1];
+      if (cone_inside(&t->sec[index1], pte) == 3 || (increment == 0)) break;
+    }
+    totalDistance += dist;
+    index += increment;
+  } while (increment != 0 && index >= 0 && index < t->nsec);
+  return totalDistance;
+}
+
+/* SafetyToIn (PolyconeImplementation.h:381-450) */
+static double polycone_safe_in(const or_polycone *t, v3 p)
+{
+  int index = polycone_section_index(t, p.z);
+  int needZ = 0;
+  double safety, minSafety;
+  if (index < 0) {
+    needZ = 1;
+    if (index == -1) index = 0;
+    if (index == -2) index = t->nsec - 1;
+  }
+  safety = cone_safe_in(&t->sec[index], pcon_local(t, index, p));
+  if (needZ) return safety;
+  if (safety < kTolerance) return safety;
+  minSafety    = safety;
+  double zbase = t->zs[index + 1];
+  for (int i = index + 1; i < t->nsec; ++i) {
+    double dz = t->zs[i] - zbase;
+    if (dz >= minSafety) break;
+    safety = cone_safe_in(&t->sec[i], pcon_local(t, i, p));
+    if (safety < minSafety) minSafety = safety;
+  }
+  if (index > 0) {
+    zbase = t->zs[index - 1];
+    for (int i = index - 1; i >= 0; --i) {
+      double dz = zbase - t->zs[i];
+      if (dz >= minSafety) break;
+      safety = cone_safe_in(&t->sec[i], pcon_local(t, i, p));
+      if (safety < minSafety) minSafety = safety;
+    }
+  }
+  return minSafety;
+}
+
+/* SafetyToOut (PolyconeImplementation.h:452-517); the neighbouring sections are probed
+ * with the cone's SafetyToIn, as the reference does */
+static double polycone_safe_out(const or_polycone *t, v3 p)
+{
+  int cin = 0, cout = 0;
+  polycone_ci(t, p, 1, &cin, &cout);
+  if (cout) return -1;
+  int index = polycone_section_index(t, p.z);
+  if (index < 0) return -1;
+  double safety    = cone_safe_out(&t->sec[index], pcon_local(t, index, p));
+  double minSafety = safety;
+  if (minSafety == kInfLength) return 0.;
+  if (minSafety < kTolerance) return 0.;
+  double zbase = t->zs[index + 1];
+  for (int i = index + 1; i < t->nsec; ++i) {
+    double dz = t->zs[i] - zbase;
+    if (dz >= minSafety) break;
+    safety = cone_safe_in(&t->sec[i], pcon_local(t, i, p));
+    if (safety < minSafety) minSafety = safety;
+  }
+  if (index > 0) {
+    zbase = t->zs[index - 1];
+    for (int i = index - 1; i >= 0; --i) {
+      double dz = zbase - t->zs[i];
+      if (dz >= minSafety) break;
+      safety = cone_safe_in(&t->sec[i], pcon_local(t, i, p));
+      if (safety < minSafety) minSafety = safety;
+    }
+  }
+  return minSafety;
+}
+
+/* UnplacedPolycone::Extent, full phi (source/UnplacedPolycone.cpp:865-900): z from the
+ * end planes, x/y from a cone (minR, maxR, minR, maxR) over the sections' constructor radii */
+static void polycone_extent(const or_polycone *t, v3 *mn, v3 *mx)
+{
+  double maxR = 0, minR = kInfLength;
+  for (int i = 0; i < t->nsec; i++) {
+    const or_cone *c = &t->sec[i];
+    maxR             = or_max(maxR, or_max(c->o_rmax1, c->o_rmax2));
+    minR             = or_min(minR, or_min(c->o_rmin1, c->o_rmin2));
+  }
+  double minz, maxz;
+  if (t->zs[0] > t->zs[t->nsec]) {
+    maxz = t->zs[0];
+    minz = t->zs[t->nsec];
+  } else {
+    minz = t->zs[0];
+    maxz = t->zs[t->nsec];
+  }
+  or_cone tmp;
+  double cpar[7] = {minR, maxR, minR, maxR, 1, 0., kTwoPi};
+  cone_init(&tmp, cpar, NULL, 0);
+  cone_extent(&tmp, mn, mx);
+  mn->z = minz;
+  mx->z = maxz;
+}
+
+/* ================================================================== */
 /* dispatch                                                           */
 /* ================================================================== */
 
@@ -1446,6 +1768,7 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
   case OR_TRD: return trd_init(&lv->s.trd, p, err, errlen);
   case OR_TRAP: return trap_init(&lv->s.trap, p, err, errlen);
   case OR_SPHERE: return sphere_init(&lv->s.sph, p, err, errlen);
+  case OR_POLYCONE: return polycone_init(&lv->s.pcon, p, err, errlen);
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -1462,6 +1785,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
   case OR_TRD: trd_extent(&lv->s.trd, mn, mx); return;
   case OR_TRAP: trap_extent(&lv->s.trap, mn, mx); return;
   case OR_SPHERE: sphere_extent(&lv->s.sph, mn, mx); return;
+  case OR_POLYCONE: polycone_extent(&lv->s.pcon, mn, mx); return;
   }
 }
 
@@ -1479,6 +1803,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_TRD: return trd_dist_in(&lv->s.trd, p, d);
   case OR_TRAP: return trap_dist_in(&lv->s.trap, p, d);
   case OR_SPHERE: return sphere_dist_in(&lv->s.sph, p, d);
+  case OR_POLYCONE: return polycone_dist_in(&lv->s.pcon, p, d);
   }
   return kInfLength;
 }
@@ -1494,6 +1819,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_TRD: return trd_dist_out(&lv->s.trd, p, d);
   case OR_TRAP: return trap_dist_out(&lv->s.trap, p, d);
   case OR_SPHERE: return sphere_dist_out(&lv->s.sph, p, d);
+  case OR_POLYCONE: return polycone_dist_out(&lv->s.pcon, p, d);
   }
   return -1.;
 }
@@ -1508,6 +1834,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRD: return trd_safety(&lv->s.trd, p, 0);
   case OR_TRAP: return trap_safe_in(&lv->s.trap, p);
   case OR_SPHERE: return sphere_safe_in(&lv->s.sph, p);
+  case OR_POLYCONE: return polycone_safe_in(&lv->s.pcon, p);
   }
   return kInfLength;
 }
@@ -1522,6 +1849,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRD: return trd_safety(&lv->s.trd, p, 1);
   case OR_TRAP: return trap_safe_out(&lv->s.trap, p);
   case OR_SPHERE: return sphere_safe_out(&lv->s.sph, p);
+  case OR_POLYCONE: return polycone_safe_out(&lv->s.pcon, p);
   }
   return 0.;
 }
@@ -1536,6 +1864,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRD: return trd_contains(&lv->s.trd, p);
   case OR_TRAP: return trap_contains(&lv->s.trap, p);
   case OR_SPHERE: return sphere_contains(&lv->s.sph, p);
+  case OR_POLYCONE: return polycone_contains(&lv->s.pcon, p);
   }
   return 0;
 }
@@ -1550,6 +1879,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRD: return trd_inside(&lv->s.trd, p);
   case OR_TRAP: return trap_inside(&lv->s.trap, p);
   case OR_SPHERE: return sphere_inside(&lv->s.sph, p);
+  case OR_POLYCONE: return polycone_inside(&lv->s.pcon, p);
   }
   return kOutsideE;
 }

@@ -620,7 +620,88 @@ SPHERE_CASES = [
     _case(f"{SP}:861", SPHERE, SPH_S2, "dist_in", _ponrmin2, vmx, 90 / _R2),
 ]
 
-ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES
+POLYCONE = 6
+PC = "test/unit_tests/TestPolycone.cpp"
+KPI_V = 3.14159265358979323846  # vecgeom::kPi
+
+
+def _pcon(sphi, dphi, z, rmin, rmax):
+    """Polycone parameters: sphi, dphi, nz, z[nz], rmin[nz], rmax[nz]."""
+    return (sphi, dphi, float(len(z))) + tuple(z) + tuple(rmin) + tuple(rmax)
+
+
+# TestPolycone.cpp:42-60 poly1 (4 planes)
+PCON1 = _pcon(0.0, 360.0 * KPI_V / 180.0, (-1.0, -0.5, 0.5, 2.0), (0.1, 0.0, 0.0, 0.4), (1.0, 2.0, 2.0, 1.5))
+# TestPolycone.cpp:32-35 "SimpleTube+Cone"
+PCON_SIMPLE = _pcon(0.0, 360.0 * KPI_V / 180.0, (-10.0, 0.0, 10.0), (0.0, 0.0, 0.0), (70.0, 70.0, 80.0))
+# TestPolycone.cpp:538-542 pcon175 (equal-z planes)
+PCON175 = _pcon(0.0, 360.0 * KPI_V / 180.0, (71.0, 121.5, 121.5, 122.5, 122.5, 282.0),
+                (53.0, 53.0, 53.0, 53.0, 114.0, 114.0), (54.0, 54.0, 115.0, 115.0, 115.0, 115.0))
+POLYCONE_CASES = [
+    _case(f"{PC}:88", POLYCONE, PCON1, "contains", (0.0, 0.0, 0.0), None, 1.0, "eq"),
+    _case(f"{PC}:89", POLYCONE, PCON1, "contains", (0.0, 0.0, -2.0), None, 0.0, "eq"),
+    _case(f"{PC}:90", POLYCONE, PCON1, "contains", (0.0, 0.0, -0.8), None, 0.0, "eq"),
+    _case(f"{PC}:91", POLYCONE, PCON1, "contains", (0.0, 0.0, -1.8), None, 0.0, "eq"),
+    _case(f"{PC}:92", POLYCONE, PCON1, "contains", (0.0, 0.0, 10.0), None, 0.0, "eq"),
+    _case(f"{PC}:93", POLYCONE, PCON1, "contains", (0.0, 0.0, 1.8), None, 0.0, "eq"),
+    _case(f"{PC}:96", POLYCONE, PCON1, "dist_in", (0.0, 0.0, -3.0), vz, 2.5, "eq"),
+    _case(f"{PC}:97", POLYCONE, PCON1, "dist_in", (0.0, 0.0, -2.0), vmz, INF, "eq"),
+    _case(f"{PC}:98", POLYCONE, PCON1, "dist_in", (0.0, 0.0, 3.0), vmz, 2.5, "eq"),
+    _case(f"{PC}:99", POLYCONE, PCON1, "dist_in", (0.0, 0.0, 3.0), vz, INF, "eq"),
+    _case(f"{PC}:100", POLYCONE, PCON1, "dist_in", (3.0, 0.0, 0.0), vmx, 1.0, "eq"),
+    _case(f"{PC}:101", POLYCONE, PCON1, "dist_in", (0.0, 0.0, 1.9999999), vx, 0.4, "near"),
+    _case(f"{PC}:105", POLYCONE, PCON1, "safe_in", (0.0, 0.0, -3.0), None, 2.0, "eq"),
+    _case(f"{PC}:106", POLYCONE, PCON1, "safe_in", (0.5, 0.0, -1.0), None, 0.0, "eq"),
+    _case(f"{PC}:107", POLYCONE, PCON1, "safe_in", (0.0, 0.0, 3.0), None, 1.0, "eq"),
+    _case(f"{PC}:108", POLYCONE, PCON1, "safe_in", (2.0, 0.0, 0.1), None, 0.0, "eq"),
+    _case(f"{PC}:111", POLYCONE, PCON1, "safe_out", (0.0, 0.0, 0.0), None, 0.5, "eq"),
+    _case(f"{PC}:112", POLYCONE, PCON1, "safe_out", (0.0, 0.0, 0.5), None, 0.0, "eq"),
+    _case(f"{PC}:113", POLYCONE, PCON1, "safe_out", (1.9, 0.0, 0.0), None, 0.1, "near"),
+    _case(f"{PC}:114", POLYCONE, PCON1, "safe_out", (0.2, 0.0, -1.0), None, 0.0, "eq"),
+    _case(f"{PC}:115", POLYCONE, PCON1, "safe_out", (1.4, 0.0, 2.0), None, 0.0, "eq"),
+    _case(f"{PC}:118", POLYCONE, PCON1, "dist_out", (0.0, 0.0, 0.0), vz, 0.5, "eq"),
+    _case(f"{PC}:119", POLYCONE, PCON1, "dist_out", (0.0, 0.0, 0.0), vmz, 0.5, "eq"),
+    _case(f"{PC}:120", POLYCONE, PCON1, "dist_out", (2.0, 0.0, 0.0), vx, 0.0, "eq"),
+    _case(f"{PC}:121", POLYCONE, PCON1, "dist_out", (2.0, 0.0, 0.0), vmx, 4.0, "eq"),
+    _case(f"{PC}:123", POLYCONE, PCON1, "dist_out", (1.0, 0.0, 2.0), vz, 0.0, "eq"),
+    _case(f"{PC}:124", POLYCONE, PCON1, "dist_out", (0.5, 0.0, -1.0), vmz, 0.0, "eq"),
+    _case(f"{PC}:125", POLYCONE, PCON1, "dist_out", (0.5, 0.0, -1.0), vz, 3.0, "eq"),
+    _case(f"{PC}:157", POLYCONE, PCON_SIMPLE, "inside", (0.0, 0.0, 0.0), None, 1, "eq"),
+    _case(f"{PC}:158", POLYCONE, PCON_SIMPLE, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{PC}:159", POLYCONE, PCON_SIMPLE, "inside", (100.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{PC}:160", POLYCONE, PCON_SIMPLE, "inside", (0.0, 100.0, 0.0), None, 3, "eq"),
+    _case(f"{PC}:161", POLYCONE, PCON_SIMPLE, "inside", (70.0, 0.0, -5.0), None, 2, "eq"),
+    _case(f"{PC}:162", POLYCONE, PCON_SIMPLE, "inside", (0.0, 70.0, -5.0), None, 2, "eq"),
+    _case(f"{PC}:163", POLYCONE, PCON_SIMPLE, "inside", (70.0, 0.0, 10.0), None, 2, "eq"),
+    _case(f"{PC}:165", POLYCONE, PCON_SIMPLE, "inside", (-70.0, 0.0, -5.0), None, 2, "eq"),
+    _case(f"{PC}:166", POLYCONE, PCON_SIMPLE, "inside", (0.0, -70.0, -5.0), None, 2, "eq"),
+    _case(f"{PC}:167", POLYCONE, PCON_SIMPLE, "inside", (0.0, 0.0, -10.0), None, 2, "eq"),
+    _case(f"{PC}:168", POLYCONE, PCON_SIMPLE, "inside", (0.0, 25.0, 0.0), None, 1, "eq"),
+    _case(f"{PC}:169", POLYCONE, PCON_SIMPLE, "inside", (4.0, 25.0, 0.0), None, 1, "eq"),
+    _case(f"{PC}:235", POLYCONE, PCON_SIMPLE, "safe_out", (5.0, 5.0, -5.0), None, 5.0),
+    _case(f"{PC}:237", POLYCONE, PCON_SIMPLE, "safe_out", (5.0, 5.0, 7.0), None, 3.0),
+    _case(f"{PC}:239", POLYCONE, PCON_SIMPLE, "safe_out", (69.0, 0.0, -5.0), None, 1.0),
+    _case(f"{PC}:241", POLYCONE, PCON_SIMPLE, "safe_out", (-3.0, -3.0, 8.0), None, 2.0),
+    _case(f"{PC}:246", POLYCONE, PCON_SIMPLE, "dist_out", pzero, vx, 70.0),
+    _case(f"{PC}:251", POLYCONE, PCON_SIMPLE, "dist_out", pzero, vmx, 70.0),
+    _case(f"{PC}:256", POLYCONE, PCON_SIMPLE, "dist_out", pzero, vy, 70.0),
+    _case(f"{PC}:261", POLYCONE, PCON_SIMPLE, "dist_out", pzero, vmy, 70.0),
+    _case(f"{PC}:266", POLYCONE, PCON_SIMPLE, "dist_out", pzero, vz, 10.0),
+    _case(f"{PC}:275", POLYCONE, PCON_SIMPLE, "dist_out", (-70.0, 0.0, -1.0), vmx, 0.0),
+    _case(f"{PC}:277", POLYCONE, PCON_SIMPLE, "dist_out", (0.0, 70.0, -10.0), vy, 0.0),
+    _case(f"{PC}:281", POLYCONE, PCON_SIMPLE, "dist_out", (0.0, -70.0, -1.0), vmy, 0.0),
+    _case(f"{PC}:307", POLYCONE, PCON_SIMPLE, "dist_in", (100.0, 0.0, -1.0), vmx, 30.0),
+    _case(f"{PC}:309", POLYCONE, PCON_SIMPLE, "dist_in", (-100.0, 0.0, -1.0), vx, 30.0),
+    _case(f"{PC}:311", POLYCONE, PCON_SIMPLE, "dist_in", (0.0, 100.0, -5.0), vmy, 30.0),
+    _case(f"{PC}:313", POLYCONE, PCON_SIMPLE, "dist_in", (0.0, -100.0, -5.0), vy, 30.0),
+    _case(f"{PC}:315", POLYCONE, PCON_SIMPLE, "dist_in", (0.0, 0.0, 100.0), vmz, 90.0),
+    _case(f"{PC}:317", POLYCONE, PCON_SIMPLE, "dist_in", (0.0, 0.0, -100.0), vz, 90.0),
+    _case(f"{PC}:319", POLYCONE, PCON_SIMPLE, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
+    _case(f"{PC}:322", POLYCONE, PCON_SIMPLE, "dist_in", (-100.0, 0.0, 0.0), vmxy, INF, "inf"),
+    _case(f"{PC}:546", POLYCONE, PCON175, "inside", (-18.1079855387881, -54.3917837284389, 121.5), None, 2, "eq"),
+]
+
+ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES + POLYCONE_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:
@@ -648,6 +729,8 @@ def check(case, value) -> bool:
         return value >= INF
     if c == "eq":
         return value == case["expect"]
+    if c == "near":  # |value - expect| < 1000 kTolerance (TestPolycone.cpp:101-102, 113)
+        return abs(value - case["expect"]) < 1000.0 * 1e-9
     if c == "range":
         return case["expect"] - 1e-4 <= value <= case["expect"] + 1e-4
     raise ValueError(c)

@@ -46,22 +46,32 @@ def test_bvh_depth_rule(oracle):
     assert len(internal) > 0 and internal.max() < 4095 // 2
 
 
-@pytest.mark.parametrize("params,lo,hi", [
+@pytest.mark.parametrize("shape,params,lo,hi", [
     # TestTrap.cpp:755-760 (VECGEOM-393): Trapezoid(60, 20deg, 5deg, 40, 30, 40, 10deg, 16, 10, 14, 10deg)
-    ((60.0, math.radians(20), math.radians(5), 40.0, 30.0, 40.0, math.radians(10), 16.0, 10.0, 14.0, math.radians(10)),
+    (W.TRAPEZOID, (60.0, math.radians(20), math.radians(5), 40.0, 30.0, 40.0, math.radians(10), 16.0, 10.0, 14.0, math.radians(10)),
      (-58.80819229, -41.90332577, -60.0), (38.57634475, 38.09667423, 60.0)),
     # TestTrap.cpp:646-653: trap1 (box-like) and trap2 (its corners as parameters)
-    ((40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0), (-20.0, -30.0, -40.0), (20.0, 30.0, 40.0)),
-    ((40.0, 0.0, 0.0, 20.0, 10.0, 10.0, 0.0, 40.0, 30.0, 30.0, 0.0), (-30.0, -40.0, -40.0), (30.0, 40.0, 40.0)),
+    (W.TRAPEZOID, (40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0), (-20.0, -30.0, -40.0),
+     (20.0, 30.0, 40.0)),
+    (W.TRAPEZOID, (40.0, 0.0, 0.0, 20.0, 10.0, 10.0, 0.0, 40.0, 30.0, 30.0, 0.0), (-30.0, -40.0, -40.0),
+     (30.0, 40.0, 40.0)),
+    # TestTrd.cpp:405-416
+    (W.TRD, (20.0, 20.0, 30.0, 30.0, 40.0), (-20.0, -30.0, -40.0), (20.0, 30.0, 40.0)),
+    (W.TRD, (10.0, 30.0, 20.0, 40.0, 40.0), (-30.0, -40.0, -40.0), (30.0, 40.0, 40.0)),
+    # TestSphere.cpp:63-68 (b1: rmax 3)
+    (W.SPHERE, (0.0, 3.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI), (-3.0, -3.0, -3.0), (3.0, 3.0, 3.0)),
+    # TestPolycone.cpp:329-333 ("SimpleTube+Cone")
+    (W.POLYCONE, (0.0, 360.0 * W.K_PI / 180.0, 3.0, -10.0, 0.0, 10.0, 0.0, 0.0, 0.0, 70.0, 70.0, 80.0),
+     (-80.0, -80.0, -10.0), (80.0, 80.0, 10.0)),
 ])
-def test_trapezoid_extent(oracle, vgnav, params, lo, hi):
-    """UnplacedTrapezoid::Extent, seen through the daughter's bounding box (extent +- 1e-3 mm)
-    in both the oracle's and the product's BVH of a world holding the trapezoid unrotated."""
+def test_shape_extent(oracle, vgnav, shape, params, lo, hi):
+    """The shapes' Extent, seen through the daughter's bounding box (extent +- 1e-3 mm) in
+    both the oracle's and the product's BVH of a world holding the shape unrotated."""
     from golden.known_answers import approx_equal
 
     b = W.GeometryBuilder()
     world = b.logical(W.BOX, (500.0, 500.0, 500.0))
-    b.place(b.logical(W.TRAPEZOID, params), world, W.transform_euler(0.0, 0.0, 0.0))
+    b.place(b.logical(shape, params), world, W.transform_euler(0.0, 0.0, 0.0))
     b.place_world(world)
     desc = b.build()
     for bvh in (oracle.OracleGeometry(desc).bvh(0), HostTables(desc).bvh(0)):
@@ -81,7 +91,8 @@ def test_invalid_descriptions_rejected(vgnav):
         HostTables(b.build())
     assert e.value.code == N.VGN_ERR_UNSUPPORTED
     for shape, params in ((W.SPHERE, (0.0, 10.0, 0.0, 1.0, 0.0, W.K_PI)),   # phi section
-                          (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0))):  # theta section
+                          (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0)),  # theta section
+                          (W.POLYCONE, (0.0, 1.0, 2.0, -1.0, 1.0, 0.0, 0.0, 5.0, 5.0))):  # phi section
         b = W.GeometryBuilder()
         b.place_world(b.logical(shape, params))
         with pytest.raises(N.VgnError) as e:

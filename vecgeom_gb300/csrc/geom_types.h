@@ -146,6 +146,17 @@ enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, TrapTheta = 17, 
 // delta-phi, the theta cone's raw start/end angles and tangents
 enum { SphRmin = 0, SphRmax, SphA1x, SphA1y, SphA2x, SphA2y, SphN1x, SphN1y, SphN2x, SphN2y, SphWedgeDPhi,
        SphSTheta, SphETheta, SphTanSTheta, SphTanETheta, SphPad, kSphereSize };
+// Polycone (full phi), variable length: [0] section count n, [1, n+1] the n+1 z planes,
+// [n+2, 2n+1] the section z shifts, then n cone rows of kConeSize doubles
+#ifdef __CUDACC__
+#define VGN_HD __host__ __device__
+#else
+#define VGN_HD
+#endif
+constexpr int PconNSec = 0;
+constexpr int PconZs   = 1;
+VGN_HD inline int pcon_shift(int n) { return 2 + n; }
+VGN_HD inline int pcon_cone(int n, int k) { return 2 + 2 * n + k * kConeSize; }
 }  // namespace row
 
 // Plain-pointer view of the device tables, passed to kernels by value.

@@ -21,8 +21,6 @@ static inline double nonzero(double x) { return x + std::copysign(1.0e-30, x); }
 
 int shape_param_count(int32_t type, const double *p, int32_t n_avail)
 {
-  (void)p;
-  (void)n_avail;
   switch (type) {
   case kBox: return 3;
   case kTube: return 5;
@@ -30,6 +28,10 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
   case kTrd: return 5;
   case kTrapezoid: return 11;
   case kSphere: return 6;
+  case kPolycone: {  // sphi, dphi, nz, z[nz], rmin[nz], rmax[nz]
+    if (n_avail < 3 || !(p[2] >= 2 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
+    return 3 + 3 * (int)p[2];
+  }
   default: return -1;
   }
 }
@@ -270,6 +272,58 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.insert(shape.end(), r, r + row::kSphereSize);
     return VGN_OK;
   }
+  case kPolycone: {
+    // UnplacedPolycone(phistart, deltaphi, Nz, z, rmin, rmax) -> PolyconeStruct::Init
+    // (UnplacedPolycone.h:78-88, PolyconeStruct.h:144-291): planes reversed when z runs
+    // downwards; a section (a ConeStruct built with the raw phi arguments) for every z
+    // step larger than kTolerance, shifted to the step's centre.  rmin > rmax and a z
+    // direction change, which the reference only reports, are rejected.
+    const double sphi = p[0], dphi = p[1];
+    const int nz      = (int)p[2];
+    std::vector<double> z(nz), rin(nz), rout(nz);
+    const bool rev = p[3] > p[3 + nz - 1];
+    for (int i = 0; i < nz; ++i) {
+      const int k = rev ? nz - 1 - i : i;
+      z[i]        = p[3 + k];
+      rin[i]      = p[3 + nz + k];
+      rout[i]     = p[3 + 2 * nz + k];
+    }
+    if (!(dphi >= kTwoPi - 0.5 * kAngTolerance)) {
+      err = "Polycone phi sections are not supported";
+      return VGN_ERR_UNSUPPORTED;
+    }
+    for (int i = 0; i < nz; ++i)
+      if (!(rin[i] >= 0 && rout[i] >= rin[i]) || (i > 0 && !(z[i] >= z[i - 1]))) {
+        err = "Polycone needs 0 <= rmin <= rmax and monotonic z planes";
+        return VGN_ERR_ARG;
+      }
+    std::vector<double> zs{z[0]}, shift, cones;
+    double prevZ = z[0], prevRmin = rin[0], prevRmax = rout[0];
+    const int dirZ = z[1] < z[0] ? -1 : 1;
+    for (int i = 1; i < nz; ++i) {
+      if (((z[i] > prevZ + kTolerance) && (dirZ > 0)) || ((z[i] < prevZ - kTolerance) && (dirZ < 0))) {
+        const double cpar[7] = {prevRmin, prevRmax, rin[i], rout[i], (z[i] - prevZ) / 2, sphi, dphi};
+        const int rc         = shape_make_row(kCone, cpar, 7, cones, err);
+        if (rc) return rc;
+        zs.push_back(z[i]);
+        const size_t zi = zs.size() - 1;
+        shift.push_back(zs[zi - 1] + 0.5 * (zs[zi] - zs[zi - 1]));
+      }
+      prevZ    = z[i];
+      prevRmin = rin[i];
+      prevRmax = rout[i];
+    }
+    const int nsec = (int)shift.size();
+    if (nsec == 0) {
+      err = "Polycone has no section longer than kTolerance";
+      return VGN_ERR_ARG;
+    }
+    shape.push_back((double)nsec);
+    shape.insert(shape.end(), zs.begin(), zs.end());
+    shape.insert(shape.end(), shift.begin(), shift.end());
+    shape.insert(shape.end(), cones.begin(), cones.end());
+    return VGN_OK;
+  }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
   }
 }
@@ -325,6 +379,21 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     const double rmax = r[row::SphRmax];
     mn = {-rmax, -rmax, -rmax};
     mx = {rmax, rmax, rmax};
+    return;
+  }
+  case kPolycone: {
+    // UnplacedPolycone::Extent, full phi (source/UnplacedPolycone.cpp:865-900): z from the
+    // end planes; x and y from a full cone of the sections' largest constructor rmax
+    const int n = (int)r[row::PconNSec];
+    double maxR = 0;
+    for (int k = 0; k < n; ++k) {
+      const double *c  = r + row::pcon_cone(n, k);
+      const double m12 = c[row::ConeArgRmax1] > c[row::ConeArgRmax2] ? c[row::ConeArgRmax1] : c[row::ConeArgRmax2];
+      maxR             = maxR > m12 ? maxR : m12;
+    }
+    const double z0 = r[row::PconZs], zn = r[row::PconZs + n];
+    mn = {-maxR, -maxR, z0 > zn ? zn : z0};
+    mx = {maxR, maxR, z0 > zn ? z0 : zn};
     return;
   }
   default: mn = mx = {0, 0, 0};

@@ -1100,6 +1100,216 @@ __device__ __forceinline__ double sphere_safe_out(const double *t, D3 p)
   return t[sp::SphRmax] - rad;
 }
 
+// ---------------------------------------------------------------- Polycone (full phi)
+// volumes/kernel/PolyconeImplementation.h over the sections' cone rows
+__device__ __forceinline__ int pcon_n(const double *t) { return (int)t[row::PconNSec]; }
+__device__ __forceinline__ const double *pcon_sec(const double *t, int n, int k) { return t + row::pcon_cone(n, k); }
+__device__ __forceinline__ D3 pcon_local(const double *t, int n, int k, D3 p)
+{
+  return d3(p.x, p.y, p.z - t[row::pcon_shift(n) + k]);
+}
+
+// PolyconeStruct::GetSectionIndex (PolyconeStruct.h:302-311)
+__device__ __forceinline__ int pcon_section_index(const double *t, int n, double zpos)
+{
+  const double *zs = t + row::PconZs;
+  if (zpos < zs[0]) return -1;
+  for (int i = 0; i < n; ++i)
+    if (zpos >= zs[i] && zpos <= zs[i + 1]) return i;
+  return -2;
+}
+
+// GenericKernelForASection (PolyconeImplementation.h:69-97)
+__device__ __forceinline__ void pcon_section_ci(const double *t, int n, int k, D3 p, bool forInside, bool &cin,
+                                                bool &cout)
+{
+  if (k < 0) {
+    cin  = false;
+    cout = true;
+    return;
+  }
+  cone_generic_ci(pcon_sec(t, n, k), pcon_local(t, n, k, p), forInside, cin, cout);
+}
+
+// GenericKernelForContainsAndInside (PolyconeImplementation.h:127-187); cin/cout keep the
+// caller's initial values where the reference leaves them untouched
+__device__ __forceinline__ void pcon_ci(const double *t, D3 p, bool forInside, bool &cin, bool &cout)
+{
+  const int n   = pcon_n(t);
+  const int lo  = pcon_section_index(t, n, p.z - kTolerance);
+  const int hi  = pcon_section_index(t, n, p.z + kTolerance);
+  if (lo < 0 && hi < 0) {
+    cout = true;
+    return;
+  }
+  if (lo < 0 && hi == 0) {
+    pcon_section_ci(t, n, 0, p, forInside, cin, cout);
+    return;
+  }
+  if (hi < 0 && lo == n - 1) {
+    pcon_section_ci(t, n, n - 1, p, forInside, cin, cout);
+    return;
+  }
+  if (lo >= 0 && hi >= 0) {
+    if (lo == hi) {
+      pcon_section_ci(t, n, lo, p, forInside, cin, cout);
+      return;
+    }
+    bool inLo = false, outLo = false, inHi = false, outHi = false;
+    pcon_section_ci(t, n, lo, p, forInside, inLo, outLo);
+    pcon_section_ci(t, n, hi, p, forInside, inHi, outHi);
+    if ((!inLo && !outLo) && (!inHi && !outHi)) {
+      cin = true;
+      return;
+    }
+    if (outLo && outHi) cout = true;
+  }
+}
+
+__device__ __forceinline__ bool pcon_contains(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  pcon_ci(t, p, false, cin, cout);
+  return !cout;
+}
+
+__device__ __forceinline__ int pcon_inside(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  pcon_ci(t, p, true, cin, cout);
+  int r = kSurfaceE;
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+// DistanceToIn (PolyconeImplementation.h:189-237)
+__device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
+{
+  const int n     = pcon_n(t);
+  double distance = kInfLength;
+  int increment   = (v.z > 0) ? 1 : -1;
+  if (fabs(v.z) < kTolerance) increment = 0;
+  int index = pcon_section_index(t, n, p.z);
+  if (index == -1) index = 0;
+  if (index == -2) index = n - 1;
+  do {
+    distance = cone_dist_in(pcon_sec(t, n, index), pcon_local(t, n, index, p), v);
+    if (distance < kInfLength || !increment) break;
+    index += increment;
+  } while (index >= 0 && index < n);
+  return distance;
+}
+
+// DistanceToOut (PolyconeImplementation.h:239-379)
+__device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 dir)
+{
+  const int n = pcon_n(t);
+  if (n == 1) return cone_dist_out(pcon_sec(t, n, 0), pcon_local(t, n, 0, point), dir);
+  const int lo = pcon_section_index(t, n, point.z - kTolerance);
+  const int hi = pcon_section_index(t, n, point.z + kTolerance);
+  int index    = 0;
+  if (lo < 0 && hi < 0) {
+    return -1;
+  } else if (lo < 0 && hi >= 0) {
+    index = hi;
+    if (cone_inside(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
+  } else if (lo != hi && lo >= 0) {
+    index = cone_inside(pcon_sec(t, n, lo), pcon_local(t, n, lo, point)) == kOutsideE ? hi : lo;
+  } else {
+    index = lo;
+    if (index < 0) index = pcon_section_index(t, n, point.z);
+  }
+  if (index < 0) return 0.;
+  if (cone_inside(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
+  double totalDistance = 0.;
+  int increment        = (dir.z > 0) ? 1 : -1;
+  if (fabs(dir.z) < kTolerance) increment = 0;
+  int istep = 0;
+  D3 pn     = point;
+  do {
+    const double shift = t[row::pcon_shift(n) + index];
+    if ((totalDistance != 0) || (istep < 2)) {
+      pn = d3(point.x + totalDistance * dir.x, point.y + totalDistance * dir.y, point.z + totalDistance * dir.z);
+      pn.z -= shift;
+      if (cone_inside(pcon_sec(t, n, index), pn) == kOutsideE) break;
+    } else {
+      pn.z -= shift;
+    }
+    istep++;
+    const double dist = cone_dist_out(pcon_sec(t, n, index), pn, dir);
+    if (dist == -1) return kInfLength;
+    if (fabs(dist) < 0.5 * kTolerance) {
+      int index1 = index;
+      if ((index > 0) && (index < n - 1)) {
+        index1 += increment;
+      } else {
+        if ((index == 0) && (increment > 0)) index1 += increment;
+        if ((index == n - 1) && (increment < 0)) index1 += increment;
+      }
+      const double td = totalDistance + dist;
+      D3 pte          = d3(point.x + td * dir.x, point.y + td * dir.y, point.z + td * dir.z);
+      pte.z -= t[row::pcon_shift(n) + index1];
+      if (cone_inside(pcon_sec(t, n, index1), pte) == kOutsideE || (increment == 0)) break;
+    }
+    totalDistance += dist;
+    index += increment;
+  } while (increment != 0 && index >= 0 && index < n);
+  return totalDistance;
+}
+
+// neighbour scan shared by SafetyToIn and SafetyToOut (PolyconeImplementation.h:413-446, 487-513)
+__device__ __forceinline__ double pcon_scan_neighbours(const double *t, int n, int index, D3 p, double minSafety)
+{
+  const double *zs = t + row::PconZs;
+  double zbase     = zs[index + 1];
+  for (int i = index + 1; i < n; ++i) {
+    if (zs[i] - zbase >= minSafety) break;
+    const double s = cone_safe_in(pcon_sec(t, n, i), pcon_local(t, n, i, p));
+    if (s < minSafety) minSafety = s;
+  }
+  if (index > 0) {
+    zbase = zs[index - 1];
+    for (int i = index - 1; i >= 0; --i) {
+      if (zbase - zs[i] >= minSafety) break;
+      const double s = cone_safe_in(pcon_sec(t, n, i), pcon_local(t, n, i, p));
+      if (s < minSafety) minSafety = s;
+    }
+  }
+  return minSafety;
+}
+
+// SafetyToIn (PolyconeImplementation.h:381-450)
+__device__ __forceinline__ double pcon_safe_in(const double *t, D3 p)
+{
+  const int n = pcon_n(t);
+  int index   = pcon_section_index(t, n, p.z);
+  bool needZ  = false;
+  if (index < 0) {
+    needZ = true;
+    if (index == -1) index = 0;
+    if (index == -2) index = n - 1;
+  }
+  const double safety = cone_safe_in(pcon_sec(t, n, index), pcon_local(t, n, index, p));
+  if (needZ || safety < kTolerance) return safety;
+  return pcon_scan_neighbours(t, n, index, p, safety);
+}
+
+// SafetyToOut (PolyconeImplementation.h:452-517); neighbours probed with the cone's SafetyToIn
+__device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  pcon_ci(t, p, true, cin, cout);
+  if (cout) return -1;
+  const int n     = pcon_n(t);
+  const int index = pcon_section_index(t, n, p.z);
+  if (index < 0) return -1;
+  const double minSafety = cone_safe_out(pcon_sec(t, n, index), pcon_local(t, n, index, p));
+  if (minSafety == kInfLength) return 0.;
+  if (minSafety < kTolerance) return 0.;
+  return pcon_scan_neighbours(t, n, index, p, minSafety);
+}
+
 // ---------------------------------------------------------------- dispatch
 __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
@@ -1110,6 +1320,7 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   case kTrd: return trd_dist_in(r, p, d);
   case kTrapezoid: return trap_dist_in(r, p, d);
   case kSphere: return sphere_dist_in(r, p, d);
+  case kPolycone: return pcon_dist_in(r, p, d);
   }
   return kInfLength;
 }
@@ -1123,6 +1334,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   case kTrd: return trd_dist_out(r, p, d);
   case kTrapezoid: return trap_dist_out(r, p, d);
   case kSphere: return sphere_dist_out(r, p, d);
+  case kPolycone: return pcon_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -1136,6 +1348,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   case kTrd: return trd_safe_in(r, p);
   case kTrapezoid: return trap_safe_in(r, p);
   case kSphere: return sphere_safe_in(r, p);
+  case kPolycone: return pcon_safe_in(r, p);
   }
   return kInfLength;
 }
@@ -1149,6 +1362,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   case kTrd: return trd_safe_out(r, p);
   case kTrapezoid: return trap_safe_out(r, p);
   case kSphere: return sphere_safe_out(r, p);
+  case kPolycone: return pcon_safe_out(r, p);
   }
   return 0.;
 }
@@ -1162,6 +1376,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   case kTrd: return trd_contains(r, p);
   case kTrapezoid: return trap_contains(r, p);
   case kSphere: return sphere_contains(r, p);
+  case kPolycone: return pcon_contains(r, p);
   }
   return false;
 }
@@ -1175,6 +1390,7 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   case kTrd: return trd_inside(r, p);
   case kTrapezoid: return trap_inside(r, p);
   case kSphere: return sphere_inside(r, p);
+  case kPolycone: return pcon_inside(r, p);
   }
   return kOutsideE;
 }

@@ -309,7 +309,7 @@ def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_l
 
 # ---------------------------------------------------------------- mixed shapes
 # Shape types the library implements, in enum order.
-IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE)
+IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE)
 MIXED_WORLD = 2000.0
 MIXED_GRID = (16, 16, 32)  # 8192 cells of 250 x 250 x 125 mm
 MIXED_JITTER = 5.0
@@ -349,11 +349,32 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int):
         rmax = u()
         rmin = 0.0 if rng.uniform() < 0.5 else float(rng.uniform(0.1, 0.9)) * rmax
         return (rmin, rmax, 0.0, K_TWO_PI, 0.0, K_PI), np.array([rmax, rmax, rmax])
+    if shape == POLYCONE:  # four z planes
+        h = u()
+        z = [-h] + sorted(float(v) for v in rng.uniform(-h, h, 2)) + [h]
+        rmax = [u() for _ in range(4)]
+        solid = rng.uniform() < 0.5
+        rmin = [0.0 if solid else float(rng.uniform(0.0, 0.8)) * r for r in rmax]
+        return (0.0, K_TWO_PI, 4.0, *z, *rmin, *rmax), np.array([max(rmax), max(rmax), h])
     raise ValueError(f"shape {shape} not implemented")
 
 
 _LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
-                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1)}
+                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15))}
+
+
+def shape_bbox(shape: int, params):
+    """(lo, hi) corners of a box holding the shape (for sampling points around it)."""
+    if shape == TRAPEZOID:
+        c = trapezoid_corners(params)
+        return c.min(axis=0), c.max(axis=0)
+    if shape == POLYCONE:
+        nz = int(params[2])
+        z = np.asarray(params[3:3 + nz])
+        r = float(max(params[3 + 2 * nz:3 + 3 * nz]))
+        return np.array([-r, -r, z.min()]), np.array([r, r, z.max()])
+    h = float(params[1]) if shape == SPHERE else float(max(params[:5]))
+    return np.full(3, -h), np.full(3, h)
 
 
 def trapezoid_corners(p) -> np.ndarray:
