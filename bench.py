@@ -1,12 +1,16 @@
 #!/usr/bin/env python
 """Benchmark: batched BVH navigation steps/s on one GB300 (replicas for N>1).
 
-Workload (BASELINE configs[1]): world box of half-length 1 m holding 4096
-rotated boxes (half-lengths U[5,30] mm, jittered 16^3 grid), 2^22 tracks
-uniform in the world outside all boxes, isotropic directions, step limit
-1 m; one step = ComputeStepAndNextVolume (step + propagated/relocated
-NavStateIndex) plus ComputeSafety for every track, in one launch of the
-all-FP64 kernel.  Synthetic data with the stated seeds.
+Headline workload: world box of half-length 1 m holding 4096 rotated boxes
+(half-lengths U[5,30] mm, jittered 16^3 grid), 2^22 tracks uniform in the
+world outside all boxes, isotropic directions, step limit 1 m; one step =
+ComputeStepAndNextVolume (step + propagated/relocated NavStateIndex) plus
+ComputeSafety for every track.  `value` is the mixed-precision form (track
+binning + step kernel, launch configuration from the library's autotuner),
+`plain_fp64` the all-FP64 form; both are bit-identical to the CPU
+restatement.  At N = 1 the line also carries the 8192-mixed-shape workload
+(2^23 tracks) in both forms, the compute roofline against measured FMA
+peaks, and the CPU baseline.  Synthetic data with the stated seeds.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -173,6 +177,208 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def fma_peaks(device: int) -> dict:
+    """Measured FP64 and FP32 FMA throughput of this GPU (TFLOP/s), the compute-roofline
+    denominators: MEASURED_PEAKS.json holds only HBM and bf16 tensor peaks."""
+    import ctypes as C
+
+    from vecgeom_gb300 import build as B
+
+    lib = C.CDLL(str(B.PEAK_LIB))
+    lib.vgp_fma_peak.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_double)]
+    out = {}
+    for name, fp64, iters in (("fp64", 1, 4096), ("fp32", 0, 65536)):
+        best = 0.0
+        for _ in range(3):
+            ms, fl = C.c_float(), C.c_double()
+            if lib.vgp_fma_peak(device, fp64, iters, C.byref(ms), C.byref(fl)) == 0 and ms.value > 0:
+                best = max(best, fl.value / (ms.value * 1e-3) / 1e12)
+        out[name] = best
+    return out
+
+
+def roofline_ops() -> dict:
+    p = ROOT / "vecgeom_gb300" / "roofline_ops.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def time_steps(torch, geo, args_tuple, mixed, steps, warmup, stream):
+    """Per-step CUDA-event times (ms) of `steps` launches after `warmup` untimed ones."""
+    for _ in range(max(warmup, 3)):
+        geo.step(*args_tuple, mixed=mixed, stream=stream)
+    geo.synchronize(stream)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for a, b in evs:
+        a.record(stream)
+        geo.step(*args_tuple, mixed=mixed, stream=stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    geo.synchronize(stream)
+    return [a.elapsed_time(b) for a, b in evs], evs[0][0].elapsed_time(evs[-1][1])
+
+
+def run_mixed_shapes(torch, V, local, steps, warmup, n_tracks, stream) -> dict:
+    """Mixed-shape workload: 8192 daughters (Box, Tube, Cone, Trd, Trapezoid, Sphere, 4-plane
+    Polycone; lengths U[5,60] mm, full rotations) in a 2 m world; tracks uniform in the world,
+    located on the GPU, then stepped in both precision forms.  Reports steps/s of each form
+    and how many results of the mixed form differ from the FP64 form's (which equals the
+    CPU restatement bit for bit)."""
+    from vecgeom_gb300 import workloads as W
+
+    desc = W.mixed_shape_geometry()
+    t = W.mixed_shape_tracks(n_tracks)
+    geo = V.Geometry(desc, device=local)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pts = V.SOA3D(dev(t.x), dev(t.y), dev(t.z))
+    dirs = V.SOA3D(dev(t.dx), dev(t.dy), dev(t.dz))
+    sl = dev(t.step_limit)
+    inp = V.NavStatePool(torch.zeros((t.n, 3), dtype=torch.int32, device="cuda"))
+    geo.locate(pts, inp, mixed=True, stream=stream)
+    geo.synchronize(stream)
+    res = {}
+    outs = {}
+    for mixed in (False, True):
+        out = V.NavStatePool.empty_like(inp)
+        stp = torch.empty(t.n, dtype=torch.float64, device="cuda")
+        saf = torch.empty(t.n, dtype=torch.float64, device="cuda")
+        k = min(t.n, 1 << 21)  # autotune on a 2^21-track prefix
+        sub = lambda a: a[:k]
+        v, kb, _ = geo.autotune_step(V.SOA3D(sub(pts.x), sub(pts.y), sub(pts.z)),
+                                     V.SOA3D(sub(dirs.x), sub(dirs.y), sub(dirs.z)), sub(sl),
+                                     V.NavStatePool(inp.data[:k]), V.NavStatePool(out.data[:k]), sub(stp), sub(saf),
+                                     mixed=mixed, stream=stream)
+        per, total = time_steps(torch, geo, (pts, dirs, sl, inp, out, stp, saf), mixed, steps, warmup, stream)
+        res["mixed" if mixed else "fp64"] = {
+            "value": t.n * steps / (total * 1e-3), "unit": UNIT, "ms_per_step": total / steps,
+            "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
+            "launch": {"variant": v, "sort_kbits": kb}}
+        outs[mixed] = (stp, saf, out.data)
+    (s0, f0, o0), (s1, f1, o1) = outs[False], outs[True]
+    res["mixed_over_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+    res["mixed_vs_fp64"] = {
+        "tracks": t.n,
+        "step_mismatches": int((s0 != s1).sum().item()),
+        "safety_mismatches": int((f0 != f1).sum().item()),
+        "state_mismatches": int((o0 != o1).any(dim=1).sum().item()),
+        "max_abs_step_diff_mm": float((s0 - s1).abs().max().item()),
+    }
+    res["workload"] = (f"mixed shapes: 8192 daughters (7 shape types, lengths U[5,60] mm, full rotations) in a "
+                       f"2 m world, {t.n} tracks located in the world, ComputeStepAndNextVolume + ComputeSafety")
+    return res
+
+
+def run_batched(torch, V, local, steps, warmup, stream) -> dict:
+    """Batched uneven workload: 64 mixed-shape geometries (2^6..2^14 daughters, log-uniform)
+    with track batches log-uniform in [1k, 512k], all stepped (mixed form) in one persistent
+    launch recorded in a CUDA graph and replayed; against the same jobs as one launch per
+    geometry, the reference's way.  Both give identical results (checked)."""
+    from vecgeom_gb300 import workloads as W
+
+    work = W.batched_workload(64, seed=10)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    jobs, total = [], 0
+    for desc, t in work:
+        geo = V.Geometry(desc, device=local)
+        pts = V.SOA3D(dev(t.x), dev(t.y), dev(t.z))
+        dirs = V.SOA3D(dev(t.dx), dev(t.dy), dev(t.dz))
+        inp = V.NavStatePool(torch.zeros((t.n, 3), dtype=torch.int32, device="cuda"))
+        torch.cuda.synchronize()  # the copies above ran on the default stream
+        geo.locate(pts, inp, mixed=True, stream=stream)
+        out = V.NavStatePool.empty_like(inp)
+        jobs.append((geo, pts, dirs, dev(t.step_limit), inp, out, torch.empty(t.n, dtype=torch.float64,
+                                                                              device="cuda"),
+                     torch.empty(t.n, dtype=torch.float64, device="cuda")))
+        total += t.n
+    torch.cuda.synchronize()
+    batch = V.StepBatch(local)
+    batch.set_jobs(jobs, mixed=True)
+    variant, kbits, _ = batch.autotune(stream)
+    # one graph = queue reset + per-job binning + one persistent launch
+    with torch.cuda.stream(stream):
+        batch.step(stream)
+    stream.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        batch.step(torch.cuda.current_stream())
+
+    def timed(fn):
+        for _ in range(max(warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    def replay():
+        with torch.cuda.stream(stream):
+            graph.replay()
+
+    ms_batch = timed(replay)
+    batch.synchronize(stream)
+    ref = [(j[6].clone(), j[7].clone(), j[5].data.clone()) for j in jobs]
+    for j in jobs:  # the reference's way: one launch (sequence) per geometry and batch
+        j[0].set_step_config(variant, kbits, mixed=True)
+
+    def separate():
+        for geo, pts, dirs, sl, inp, out, stp, saf in jobs:
+            geo.step(pts, dirs, sl, inp, out, stp, saf, mixed=True, stream=stream)
+
+    ms_sep = timed(separate)
+    torch.cuda.synchronize()
+    mism = sum(int((r[0] != j[6]).sum().item()) + int((r[1] != j[7]).sum().item()) +
+               int((r[2] != j[5].data).any(dim=1).sum().item()) for r, j in zip(ref, jobs))
+    sizes = sorted(t.n for _, t in work)
+    return {
+        "workload": "64 mixed-shape geometries (2^6..2^14 daughters, log-uniform), batches log-uniform "
+                    f"in [1k, 512k] tracks ({total} tracks), mixed form",
+        "tracks_per_step": total, "batch_sizes_min_median_max": [sizes[0], sizes[len(sizes) // 2], sizes[-1]],
+        "persistent_graph": {"value": total / (ms_batch * 1e-3), "unit": UNIT, "ms_per_step": ms_batch,
+                             "launch": {"variant": variant, "sort_kbits": kbits},
+                             "graph": "queue reset + per-job binning + one persistent launch"},
+        "one_launch_per_geometry": {"value": total / (ms_sep * 1e-3), "unit": UNIT, "ms_per_step": ms_sep},
+        "speedup": ms_sep / ms_batch, "result_mismatches": mism,
+    }
+
+
+def run_serving(torch, V, local, seconds: float) -> dict:
+    """Serving loop against the resident 8192-mixed-shape geometry: requests of log-uniform
+    size in [256, 1M] tracks arrive as a Poisson process; each is copied in, located and
+    stepped to the world exit on the device (states stay on the device), and its step counts
+    copied back.  Peak = a saturating burst of eight 1M-track requests; then offered loads of
+    25/50/90 % of that peak.  Latency = arrival to reply in host memory."""
+    from vecgeom_gb300 import serving as S
+    from vecgeom_gb300 import workloads as W
+
+    streams = 4
+    geo = V.Geometry(W.mixed_shape_geometry(), device=local)
+    free, _ = torch.cuda.mem_get_info()
+    pool_bytes = int(min(free // 4, 16 << 30))
+    ex = S.GpuExecutor(geo, W.MIXED_WORLD, pool_bytes, streams, mixed=True)
+    pool = S.Pool(pool_bytes)
+    burst = lambda seed: [S.Request(arrival=0.0, rid=k, n=1 << 20, seed=seed + k) for k in range(8)]
+    S.serve(burst(100), ex, pool, streams)  # warm-up
+    peak = S.summarize(S.serve(burst(200), ex, pool, streams))
+    steps_per_track = peak["steps"] / peak["tracks"]
+    mean_n = S.mean_batch()
+    out = {"workload": "resident 8192-mixed-shape geometry; Poisson requests, batch sizes log-uniform in "
+                       "[256, 1M] tracks, each track stepped to the world exit (mixed form)",
+           "streams": streams, "pool_bytes": pool_bytes, "admission": "first-fit in a device pool of free HBM",
+           "peak": {"steps_per_s": peak["steps_per_s"], "steps_per_track": steps_per_track}, "loads": {}}
+    for frac in (0.25, 0.5, 0.9):
+        rate = frac * peak["steps_per_s"] / (mean_n * steps_per_track)
+        reqs = S.poisson_requests(rate, seconds, seed=int(frac * 100))
+        summ = S.summarize(S.serve(reqs, ex, pool, streams))
+        summ["offered_requests_per_s"] = rate
+        summ["offered_steps_per_s"] = frac * peak["steps_per_s"]
+        out["loads"][f"{int(frac * 100)}%"] = summ
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import torch
 
@@ -238,8 +444,14 @@ def run_ours(args, ws, rank, local):
         return per, total
 
     # launch configuration (block shape, track binning) picked by the library's autotuner
+    # (or fixed with --fixed-launch VARIANT,KBITS, for profiling runs without the tuning launches)
     launch_cfg = {}
     for mixed in (False, True):
+        if args.fixed_launch:
+            v, k = (int(x) for x in args.fixed_launch.split(","))
+            geo.set_step_config(v, k, mixed=mixed)
+            launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k, "autotune_ms": None}
+            continue
         v, k, ms = geo.autotune_step(pts, dirs, sl, inp, out, steps, saf, mixed=mixed, stream=stream)
         launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k, "autotune_ms": ms}
     geo.synchronize(stream)
@@ -288,9 +500,40 @@ def run_ours(args, ws, rank, local):
             rate, cores, sample = cpu_sample_rate(grid, t, min_seconds=args.cpu_seconds)
             cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         traffic = None
-        tp = ROOT / "profiles" / "traffic_step_fp64.json"
+        tp = ROOT / "profiles" / "step_kernel_traffic.json"
         if tp.exists():
-            traffic = json.loads(tp.read_text()).get("bytes_per_launch_full_size")
+            traffic = json.loads(tp.read_text()).get("mixed_bytes_per_launch_full_size")
+        # compute roofline: algorithmic FP64 operations per step (frozen oracle work counts)
+        # against the measured FMA peaks of this GPU
+        fpk = fma_peaks(local)
+        ops = roofline_ops().get("box_grid", {}).get("fp64_ops_per_step")
+        compute = None
+        if ops and fpk.get("fp64"):
+            plain_tf = ops * plain_value / ws / 1e12
+            mixed_tf = ops * value / ws / 1e12
+            compute = {
+                "bound": "fp64 pipe (plain); fp32/int + fp64 (mixed)", "unit": "TFLOP/s",
+                "fp64_ops_per_step": ops, "ops_source": "vecgeom_gb300/roofline_ops.json (oracle work counters)",
+                "peak_fp64_measured": fpk["fp64"], "peak_fp32_measured": fpk["fp32"],
+                "plain": {"achieved": plain_tf, "frac_of_fp64_peak": plain_tf / fpk["fp64"]},
+                "mixed": {"achieved_fp64_equivalent": mixed_tf, "frac_of_fp64_peak": mixed_tf / fpk["fp64"]},
+            }
+        mixed_shapes = None
+        if ws == 1 and not args.no_mixed_shapes:
+            mixed_shapes = run_mixed_shapes(torch, V, local, args.mixed_shapes_steps, args.warmup,
+                                            args.mixed_shapes_tracks, stream)
+            ms_ops = roofline_ops().get("mixed_shapes", {}).get("fp64_ops_per_step")
+            if ms_ops and fpk.get("fp64"):
+                a = ms_ops * mixed_shapes["fp64"]["value"] / 1e12
+                mixed_shapes["compute_roofline_fp64"] = {"fp64_ops_per_step": ms_ops, "achieved": a,
+                                                         "unit": "TFLOP/s", "frac_of_fp64_peak": a / fpk["fp64"]}
+        batched = None
+        if ws == 1 and not args.no_batched:
+            # a side stream: CUDA graphs cannot be captured on the legacy default stream
+            batched = run_batched(torch, V, local, args.batched_steps, args.warmup, torch.cuda.Stream())
+        serving = None
+        if ws == 1 and not args.no_serving:
+            serving = run_serving(torch, V, local, args.serving_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -316,8 +559,12 @@ def run_ours(args, ws, rank, local):
                          "kernel": "step_kernel<mixed>", "kernel_avg_ms": avg_ms,
                          "timing": "whole step (track binning + step kernel) per CUDA events: "
                                    "a lower bound on the step kernel's own rate"},
+            "compute_roofline": compute,
             "clocks": clock_log[0] if clock_log else None,
             "cpu_baseline": cpu,
+            "mixed_shapes": mixed_shapes,
+            "batched_uneven": batched,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -334,6 +581,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tracks", type=int, default=N_TRACKS, help="tracks per step (smaller only for profiling)")
+    ap.add_argument("--no-mixed-shapes", action="store_true", help="skip the 8192-mixed-shape workload")
+    ap.add_argument("--fixed-launch", default="", help="VARIANT,KBITS instead of autotuning (profiling runs)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-geometry batched workload")
+    ap.add_argument("--batched-steps", type=int, default=10)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serving-seconds", type=float, default=6.0)
+    ap.add_argument("--mixed-shapes-tracks", type=int, default=1 << 23)
+    ap.add_argument("--mixed-shapes-steps", type=int, default=5)
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -166,6 +166,50 @@ int vgn_autotune_step(vgn_geometry *geom, int64_t n, const double *px, const dou
                       const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream,
                       int32_t *variant, int32_t *sort_kbits, float *best_ms);
 
+/* Transport loop on the device: every track is stepped (ComputeStepAndPropagatedState,
+ * VNavigator.h:436-492, no safety) and moved by its step, p += step * d, until it leaves
+ * the world (nav_ind 0) or after max_steps steps -- the caller-side loop of the
+ * reference's transport examples (persistency/gdml/test/TestVGDMLNavigation/
+ * TestVGDMLNavigation.cpp:86-102) with the state kept on the device.  Positions and
+ * states are updated in place; nsteps[i] receives the steps taken (-1: invalid state).
+ * Device pointers only.  No single counterpart call in the reference. */
+int vgn_walk_batch(const vgn_geometry *geom, int64_t n, double *px, double *py, double *pz, const double *dx,
+                   const double *dy, const double *dz, const double *step_limit, vgn_state *state,
+                   int32_t max_steps, int32_t *nsteps, int flags, void *stream);
+
+/* ---- batched uneven workloads: many (geometry, track batch) jobs per launch ------
+ * The reference launches one kernel per batch and geometry (NavigationBenchmarker.cu:43,
+ * VNavigator.h:913-941); a vgn_batch runs up to VGN_BATCH_MAX_JOBS jobs, each with its
+ * own geometry and SOA3D arrays, in ONE persistent launch whose warps take 32-track
+ * chunks from a device work queue, so small and large batches share the GPU evenly.
+ * Results equal vgn_compute_step_batch on each job bit for bit.
+ *   create -> set_jobs (uploads nothing per step; allocates the per-job binning
+ *   scratch) -> step (enqueue only: queue reset, optional per-job binning, one launch;
+ *   no allocation or host synchronisation, so it can be recorded into a CUDA graph)
+ * All job arrays are device pointers on the batch's device; the jobs' geometries must
+ * live on that device.  No counterpart in the reference. */
+#define VGN_BATCH_MAX_JOBS 64
+typedef struct vgn_step_job {
+  const vgn_geometry *geom;
+  int64_t n;
+  const double *px, *py, *pz, *dx, *dy, *dz, *step_limit;
+  const vgn_state *in;
+  vgn_state *out;
+  double *step;
+  double *safety; /* may be NULL: no safety */
+} vgn_step_job;
+typedef struct vgn_batch vgn_batch;
+int vgn_batch_create(int device, vgn_batch **out);
+int vgn_batch_free(vgn_batch *batch);
+/* flags: VGN_PRECISION_MIXED, VGN_NO_RELOCATE; sort_kbits 0..6 as in vgn_set_step_config */
+int vgn_batch_set_jobs(vgn_batch *batch, int n_jobs, const vgn_step_job *jobs, int flags, int32_t variant,
+                       int32_t sort_kbits);
+int vgn_batch_step(vgn_batch *batch, void *stream);
+/* waits for `stream` and returns the first device-side error of any job's geometry */
+int vgn_batch_synchronize(vgn_batch *batch, void *stream);
+/* times every (variant, sort_kbits) pair on the current jobs, keeps the fastest */
+int vgn_batch_autotune(vgn_batch *batch, void *stream, int32_t *variant, int32_t *sort_kbits, float *best_ms);
+
 /* Allocation-free binned step.  Same operation and results as
  * vgn_compute_step_batch with track binning at `sort_kbits` (1..5), but the
  * binning scratch (sort keys, histogram, visit permutation) lives in one fixed

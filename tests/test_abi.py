@@ -27,6 +27,12 @@ def test_version_and_errors(vgnav):
     assert b"sm_103a" in L.vgn_version()
     assert L.vgn_compute_step_batch(None, 1, *([None] * 11), 0, None) == N.VGN_ERR_ARG
     assert b"null geometry" in L.vgn_last_error()
+    # batches: no such device, null handles
+    h = C.c_void_p()
+    assert L.vgn_batch_create(9999, C.byref(h)) == N.VGN_ERR_ARG and not h
+    assert L.vgn_batch_step(None, None) == N.VGN_ERR_ARG
+    assert L.vgn_batch_set_jobs(None, 1, None, 0, 0, 0) == N.VGN_ERR_ARG
+    assert L.vgn_batch_free(None) == N.VGN_OK
 
 
 CPP_PROGRAM = r"""

@@ -225,7 +225,7 @@ def test_launch_configs_bit_exact(oracle, vgnav, cuda, mixed):
     geo = vgnav.Geometry(grid.desc)
     t = W.box_grid_tracks(grid, n=100003, seed_points=71, seed_dirs=72)
     ref = og.step(t, calcsafety=True)
-    n_variants = 4
+    n_variants = 6
     for variant in range(n_variants):
         for kbits in (0, 1, 3, 5, 6):
             geo.set_step_config(variant, kbits, mixed=mixed)
@@ -256,7 +256,7 @@ def test_autotune_then_step(oracle, vgnav, cuda, mixed):
     steps = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
     saf = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
     v, k, ms = geo.autotune_step(pts, dirs, to_dev(cuda, t.step_limit), inp, out, steps, saf, mixed=mixed)
-    assert 0 <= v < 4 and k in (0, 3, 4, 5) and ms > 0
+    assert 0 <= v < 6 and k in (0, 3, 4, 5) and ms > 0
     assert geo.step_config(mixed=mixed) == (v, k)
     ref = og.step(t, calcsafety=True)
     got = gpu_step(cuda, geo, t, mixed=mixed)
@@ -356,3 +356,57 @@ def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed):
         if w.n == 0:
             break
     assert w.n == 0
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("which", ["box_grid", "mixed_shapes"])
+def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed):
+    """vgn_walk_batch (the transport loop on the device) ends every track where the oracle's
+    step-by-step loop ends it: same final point, state and number of steps."""
+    torch = cuda
+    if which == "box_grid":
+        grid = W.box_grid_geometry()
+        desc = grid.desc
+        t = W.box_grid_tracks(grid, n=20000, seed_points=81, seed_dirs=82)
+    else:
+        desc = W.mixed_shape_geometry()
+        t = W.mixed_shape_tracks(20000, 83, 84)
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    if which == "mixed_shapes":
+        t.states = og.locate(t.x, t.y, t.z)
+    # oracle: step until the world is left, recording where each track ends
+    n = t.n
+    ref_x, ref_y, ref_z = t.x.copy(), t.y.copy(), t.z.copy()
+    ref_steps = np.zeros(n, np.int32)
+    ref_state = t.states.copy()
+    idx = np.arange(n)
+    cur = t
+    for it in range(1000):
+        r = og.step(cur, calcsafety=False)
+        cur = advance(cur, r["step"], r["out"])
+        ref_steps[idx] += 1
+        ref_x[idx], ref_y[idx], ref_z[idx] = cur.x, cur.y, cur.z
+        ref_state[idx] = cur.states
+        live = cur.states["nav_ind"] != 0
+        cur, idx = keep(cur, live), idx[live]
+        if cur.n == 0:
+            break
+    assert cur.n == 0
+    pts = vgnav.SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+    dirs = vgnav.SOA3D(to_dev(torch, t.dx), to_dev(torch, t.dy), to_dev(torch, t.dz))
+    st = vgnav.NavStatePool(states_to_dev(torch, t.states))
+    nsteps = torch.zeros(n, dtype=torch.int32, device="cuda")
+    geo.walk(pts, dirs, to_dev(torch, t.step_limit), st, nsteps, mixed=mixed)
+    geo.synchronize()
+    assert np.array_equal(nsteps.cpu().numpy(), ref_steps)
+    assert np.array_equal(pts.x.cpu().numpy(), ref_x)
+    assert np.array_equal(pts.y.cpu().numpy(), ref_y)
+    assert np.array_equal(pts.z.cpu().numpy(), ref_z)
+    assert np.array_equal(st.to_numpy(), ref_state)
+    # a step cap stops tracks early and leaves them inside
+    pts2 = vgnav.SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+    st2 = vgnav.NavStatePool(states_to_dev(torch, t.states))
+    geo.walk(pts2, dirs, to_dev(torch, t.step_limit), st2, nsteps, max_steps=1, mixed=mixed)
+    geo.synchronize()
+    assert np.all(nsteps.cpu().numpy() == np.where(t.states["nav_ind"] != 0, 1, 0))

@@ -6,7 +6,8 @@ distance/safety queries.  This package holds its in-tree build, a ctypes
 binding, a Python mirror of VecGeom's batched navigator interface and the
 seeded synthetic workloads.
 """
-from .navigator import SOA3D, BVHNavigator, Geometry, NavStatePool  # noqa: F401
+from .navigator import SOA3D, BVHNavigator, Geometry, NavStatePool, StepBatch  # noqa: F401
 from .workloads import GeometryBuilder, GeometryDescription  # noqa: F401
 
-__all__ = ["SOA3D", "BVHNavigator", "Geometry", "NavStatePool", "GeometryBuilder", "GeometryDescription"]
+__all__ = ["SOA3D", "BVHNavigator", "Geometry", "NavStatePool", "StepBatch", "GeometryBuilder",
+           "GeometryDescription"]

@@ -45,6 +45,13 @@ EXPORTED = [
     "vgn_get_step_config",
     "vgn_autotune_step",
     "vgn_compute_step_batch_static",
+    "vgn_walk_batch",
+    "vgn_batch_create",
+    "vgn_batch_free",
+    "vgn_batch_set_jobs",
+    "vgn_batch_step",
+    "vgn_batch_synchronize",
+    "vgn_batch_autotune",
     "vgn_synchronize",
     "vgn_last_error",
     "vgn_version",
@@ -71,6 +78,16 @@ class GeometryDesc(C.Structure):
         ("pv_transform", C.c_void_p),
         ("world_placed", C.c_int32),
     ]
+
+
+class StepJob(C.Structure):
+    """vgn_step_job: one (geometry, track batch) job of a vgn_batch."""
+
+    _fields_ = [("geom", C.c_void_p), ("n", C.c_int64)] + [
+        (f, C.c_void_p) for f in ("px", "py", "pz", "dx", "dy", "dz", "step_limit", "in_", "out", "step", "safety")]
+
+
+VGN_BATCH_MAX_JOBS = 64
 
 
 class VgnError(RuntimeError):
@@ -105,6 +122,13 @@ def lib() -> C.CDLL:
         L.vgn_autotune_step.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, p, p, C.c_int, vp,
                                         C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)]
         L.vgn_compute_step_batch_static.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, p, p, C.c_int, i32, vp]
+        L.vgn_walk_batch.argtypes = [vp, i64, p, p, p, p, p, p, p, p, i32, p, C.c_int, vp]
+        L.vgn_batch_create.argtypes = [C.c_int, C.POINTER(vp)]
+        L.vgn_batch_free.argtypes = [vp]
+        L.vgn_batch_set_jobs.argtypes = [vp, C.c_int, C.POINTER(StepJob), C.c_int, i32, i32]
+        L.vgn_batch_step.argtypes = [vp, vp]
+        L.vgn_batch_synchronize.argtypes = [vp, vp]
+        L.vgn_batch_autotune.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)]
         L.vgn_synchronize.argtypes = [vp, vp]
         L.vgn_last_error.restype = C.c_char_p
         L.vgn_version.restype = C.c_char_p

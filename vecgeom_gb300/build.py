@@ -19,6 +19,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libvgnav.so"
+PEAK_LIB = LIBDIR / "libvgpeak.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -47,6 +48,7 @@ def _compile(nvcc: str, src: str, extra: list[str]) -> Path:
     if out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return out
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
+    common += os.environ.get("VGN_NVCC_FLAGS", "").split()  # extra defines for build experiments
     if src.endswith(".cu"):
         cmd = [nvcc, *ARCH, "-lineinfo", "-Xptxas", "-v", *common, *extra, "-c", str(srcp), "-o", str(out)]
     else:
@@ -70,6 +72,14 @@ def build(verbose: bool = False) -> Path:
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    # FMA throughput probe used by bench.py for the compute roofline (not part of libvgnav)
+    peak_src = CSRC / "peak_fp.cu"
+    if not PEAK_LIB.exists() or PEAK_LIB.stat().st_mtime < peak_src.stat().st_mtime:
+        cmd = [nvcc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(peak_src), "-o", str(PEAK_LIB),
+               "-cudart", "static"]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"build failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     if verbose:
         print(f"built {LIB}", file=sys.stderr)
     return LIB

@@ -59,6 +59,86 @@ __global__ void __launch_bounds__(BLOCK, MINB) step_kernel(GeomView g, int64_t n
   }
 }
 
+// Persistent multi-job step: every warp repeatedly takes the next 32-track chunk from the
+// work queue, finds its job (jobs are laid out back to back in chunk space) and steps
+// those tracks in the job's geometry.  The job table is a __grid_constant__ parameter,
+// read through the constant path with a warp-uniform index.
+template <bool MIXED, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) multi_step_kernel(const __grid_constant__ JobTable jt,
+                                                                 uint32_t *__restrict__ queue, int reloc)
+{
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t chunk = 0;
+    if (lane == 0) chunk = atomicAdd(queue, 1u);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk >= jt.chunk_begin[jt.n_jobs]) return;
+    int lo = 0, hi = jt.n_jobs - 1;  // last job whose first chunk is <= chunk
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jt.chunk_begin[mid] <= chunk) lo = mid;
+      else hi = mid - 1;
+    }
+    const JobRec &j = jt.job[lo];
+    const int64_t t = (int64_t)(chunk - jt.chunk_begin[lo]) * 32 + lane;
+    if (t < j.n) {  // the job's last chunk may be partly empty
+      const int64_t i = j.perm ? (int64_t)__ldg(j.perm + t) : t;
+      const State s   = load_state(j.in, i);
+      State o         = s;
+      double sf = 0., st;
+      if (!ni_valid(j.g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(j.g, s.last_exited))) {
+        raise_error(j.g, kErrState);
+        st = 0.;
+      } else {
+        st = nav_step<MIXED>(j.g, d3(j.px[i], j.py[i], j.pz[i]), d3(j.dx[i], j.dy[i], j.dz[i]), j.slimit[i], s,
+                             o, j.safety != nullptr, sf, reloc != 0);
+      }
+      j.step[i] = st;
+      if (j.safety) j.safety[i] = sf;
+      store_state(j.out, i, o);
+    }
+    __syncwarp();
+  }
+}
+
+// Transport loop per track: ComputeStepAndPropagatedState, then p += step * d, until the
+// track leaves the world (state 0) or after max_steps steps; positions and states are
+// updated in place (the loop of TestVGDMLNavigation.cpp:86-102, kept on the device).
+template <bool MIXED>
+__global__ void __launch_bounds__(128, 6) walk_kernel(GeomView g, int64_t n, double *__restrict__ px,
+                                                      double *__restrict__ py, double *__restrict__ pz,
+                                                      const double *__restrict__ dx, const double *__restrict__ dy,
+                                                      const double *__restrict__ dz,
+                                                      const double *__restrict__ slimit, vgn_state *__restrict__ state,
+                                                      int max_steps, int32_t *__restrict__ nsteps)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    State s = load_state(state, i);
+    if (s.nav_ind != 0 && (!ni_valid(g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(g, s.last_exited)))) {
+      raise_error(g, kErrState);
+      nsteps[i] = -1;
+      continue;
+    }
+    D3 p            = d3(px[i], py[i], pz[i]);
+    const D3 d      = d3(dx[i], dy[i], dz[i]);
+    const double sl = slimit[i];
+    int k           = 0;
+    while (s.nav_ind != 0 && k < max_steps) {
+      State o = s;
+      double sf;
+      const double st = nav_step<MIXED>(g, p, d, sl, s, o, false, sf, true);
+      p               = d3(p.x + st * d.x, p.y + st * d.y, p.z + st * d.z);
+      s               = o;
+      ++k;
+    }
+    px[i] = p.x;
+    py[i] = p.y;
+    pz[i] = p.z;
+    store_state(state, i, s);
+    nsteps[i] = k;
+  }
+}
+
 // VSafetyEstimatorHelper::ComputeSafety (VSafetyEstimator.h:98-107)
 template <bool MIXED>
 __global__ void __launch_bounds__(256) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
@@ -134,7 +214,7 @@ static inline unsigned grid_for(int64_t n, int block, int max_blocks)
 struct StepVariant {
   int block, minb;
 };
-static constexpr StepVariant kStepVariants[] = {{256, 2}, {256, 3}, {128, 6}, {256, 4}};
+static constexpr StepVariant kStepVariants[] = {{256, 2}, {256, 3}, {128, 6}, {256, 4}, {128, 5}, {128, 4}};
 static constexpr int kNumStepVariants        = sizeof(kStepVariants) / sizeof(kStepVariants[0]);
 
 int step_variant_count() { return kNumStepVariants; }
@@ -155,6 +235,8 @@ static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cud
   case 1: launch_step_v<MIXED, 256, 3>(g, a, s); break;
   case 2: launch_step_v<MIXED, 128, 6>(g, a, s); break;
   case 3: launch_step_v<MIXED, 256, 4>(g, a, s); break;
+  case 4: launch_step_v<MIXED, 128, 5>(g, a, s); break;
+  case 5: launch_step_v<MIXED, 128, 4>(g, a, s); break;
   default: launch_step_v<MIXED, 256, 2>(g, a, s); break;
   }
 }
@@ -165,6 +247,52 @@ cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int va
     launch_step_m<true>(g, a, variant, s);
   else
     launch_step_m<false>(g, a, variant, s);
+  return cudaGetLastError();
+}
+
+template <bool MIXED, int BLOCK, int MINB>
+static void launch_multi_v(const JobTable &jt, uint32_t *queue, int reloc, int num_sms, cudaStream_t s)
+{
+  // persistent: as many blocks as the variant keeps resident on every SM
+  const unsigned grid = (unsigned)(num_sms * MINB);
+  dev::multi_step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, 0, s>>>(jt, queue, reloc);
+}
+
+template <bool MIXED>
+static void launch_multi_m(const JobTable &jt, uint32_t *queue, int reloc, int num_sms, int variant, cudaStream_t s)
+{
+  switch (variant) {
+  case 1: launch_multi_v<MIXED, 256, 3>(jt, queue, reloc, num_sms, s); break;
+  case 2: launch_multi_v<MIXED, 128, 6>(jt, queue, reloc, num_sms, s); break;
+  case 3: launch_multi_v<MIXED, 256, 4>(jt, queue, reloc, num_sms, s); break;
+  case 4: launch_multi_v<MIXED, 128, 5>(jt, queue, reloc, num_sms, s); break;
+  case 5: launch_multi_v<MIXED, 128, 4>(jt, queue, reloc, num_sms, s); break;
+  default: launch_multi_v<MIXED, 256, 2>(jt, queue, reloc, num_sms, s); break;
+  }
+}
+
+cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, int reloc, int num_sms, int variant,
+                              cudaStream_t s)
+{
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  if (mixed)
+    launch_multi_m<true>(jt, queue, reloc, num_sms, variant, s);
+  else
+    launch_multi_m<false>(jt, queue, reloc, num_sms, variant, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, double *pz, const double *dx,
+                        const double *dy, const double *dz, const double *slimit, vgn_state *state, int max_steps,
+                        int32_t *nsteps, bool mixed, int max_blocks, cudaStream_t s)
+{
+  const int block     = 128;
+  const unsigned grid = grid_for(n, block, max_blocks * 2);
+  if (mixed)
+    dev::walk_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps);
+  else
+    dev::walk_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps);
   return cudaGetLastError();
 }
 

@@ -36,9 +36,33 @@ cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, con
 size_t static_scratch_words();
 cudaError_t static_scratch(uint32_t **ptr);  // current device's buffer
 
+// one job of a multi-job launch: geometry view, SOA3D arrays and visit order
+struct JobRec {
+  GeomView g;
+  const double *px, *py, *pz, *dx, *dy, *dz, *slimit;
+  const vgn_state *in;
+  vgn_state *out;
+  double *step, *safety;
+  const uint32_t *perm;  // nullptr = identity
+  int64_t n;
+};
+// the whole multi-job launch description, passed by value as a kernel parameter
+struct JobTable {
+  JobRec job[VGN_BATCH_MAX_JOBS];
+  uint32_t chunk_begin[VGN_BATCH_MAX_JOBS + 1];  // first 32-track chunk of each job; [n_jobs] = total
+  int32_t n_jobs;
+};
+static_assert(sizeof(JobTable) < 32000, "kernel parameters are limited to 32764 bytes");
+// queue reset + one persistent launch over all jobs
+cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, int reloc, int num_sms, int variant,
+                              cudaStream_t s);
+
 // navigation kernels (kernels_nav.cu); mixed = FP32-interval box decisions
 cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s);
 int step_variant_count();
+cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, double *pz, const double *dx,
+                        const double *dy, const double *dz, const double *slimit, vgn_state *state, int max_steps,
+                        int32_t *nsteps, bool mixed, int max_blocks, cudaStream_t s);
 cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
                           const vgn_state *in, double *safety, bool mixed, int max_blocks, cudaStream_t s);
 cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,

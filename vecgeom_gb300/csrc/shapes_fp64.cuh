@@ -1311,7 +1311,15 @@ __device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
 }
 
 // ---------------------------------------------------------------- dispatch
-__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
+// The dispatchers are inlined by default; VGN_NOINLINE_SHAPES makes them real calls, which
+// keeps the seven shapes' code out of every call site (smaller kernels, less register
+// pressure in the traversal loops).
+#ifdef VGN_NOINLINE_SHAPES
+#define VGN_SHAPE_DISPATCH __device__ __noinline__
+#else
+#define VGN_SHAPE_DISPATCH __device__ __forceinline__
+#endif
+VGN_SHAPE_DISPATCH double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
   switch (type) {
   case kBox: return box_dist_in(r, p, d);
@@ -1325,7 +1333,7 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   return kInfLength;
 }
 
-__device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p, D3 d)
+VGN_SHAPE_DISPATCH double shape_dist_out(int type, const double *r, D3 p, D3 d)
 {
   switch (type) {
   case kBox: return box_dist_out(r, p, d);
@@ -1339,7 +1347,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   return -1.;
 }
 
-__device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
+VGN_SHAPE_DISPATCH double shape_safe_in(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_safe_in(r, p);
@@ -1353,7 +1361,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   return kInfLength;
 }
 
-__device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p)
+VGN_SHAPE_DISPATCH double shape_safe_out(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_safe_out(r, p);
@@ -1367,7 +1375,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   return 0.;
 }
 
-__device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
+VGN_SHAPE_DISPATCH bool shape_contains(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_contains(r, p);
@@ -1381,7 +1389,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   return false;
 }
 
-__device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
+VGN_SHAPE_DISPATCH int shape_inside(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_inside(r, p);

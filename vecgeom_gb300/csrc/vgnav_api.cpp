@@ -586,6 +586,241 @@ int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double
   return check_status(g, s);
 }
 
+int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, double *pz, const double *dx,
+                   const double *dy, const double *dz, const double *step_limit, vgn_state *state,
+                   int32_t max_steps, int32_t *nsteps, int flags, void *stream)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n < 0 || max_steps < 0) return fail(VGN_ERR_ARG, "negative batch size or step count");
+  if (n == 0) return VGN_OK;
+  if (!px || !py || !pz || !dx || !dy || !dz || !step_limit || !state || !nsteps)
+    return fail(VGN_ERR_ARG, "null array argument");
+  DeviceGuard guard(g->device);
+  if (classify({px, py, pz, dx, dy, dz, step_limit, state, nsteps}) != 1)
+    return fail(VGN_ERR_ARG, "device pointers required");
+  cudaError_t e = vgn::launch_walk(g->view, n, px, py, pz, dx, dy, dz, step_limit, state, max_steps, nsteps,
+                                   (flags & VGN_PRECISION_MIXED) != 0, max_blocks(g),
+                                   static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? VGN_OK : cuda_fail(e, "walk kernel launch");
+}
+
+// ---- batched uneven workloads ------------------------------------------------
+struct vgn_batch {
+  int device  = 0;
+  int num_sms = 0;
+  uint32_t *d_queue = nullptr;  // work-queue counter of the persistent launch
+  vgn::JobTable jt{};
+  std::vector<vgn_step_job> jobs;
+  std::vector<vgn::BinParams> bins;
+  std::vector<uint32_t *> d_sort;  // per-job binning scratch: keys | histogram | permutation
+  std::vector<size_t> sort_words;
+  bool mixed  = false;
+  int reloc   = 1;
+  int variant = 0;
+  int kbits   = 0;
+};
+
+namespace {
+
+// (re)build the per-job visit orders for `kbits` (0 = none); allocates only when a job's
+// scratch is too small
+int batch_configure(vgn_batch *b, int kbits)
+{
+  const size_t nj = b->jobs.size();
+  b->d_sort.resize(nj, nullptr);
+  b->sort_words.resize(nj, 0);
+  b->bins.resize(nj);
+  for (size_t k = 0; k < nj; ++k) {
+    vgn::JobRec &r = b->jt.job[k];
+    r.perm         = nullptr;
+    if (kbits == 0 || r.n == 0 || r.n > (int64_t)UINT32_MAX) continue;
+    const size_t need = vgn::bin_scratch_words(r.n, kbits) + (size_t)r.n;
+    if (need > b->sort_words[k]) {
+      if (b->d_sort[k]) cudaFree(b->d_sort[k]);
+      b->d_sort[k]     = nullptr;
+      b->sort_words[k] = 0;
+      if (cudaMalloc(&b->d_sort[k], need * sizeof(uint32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VGN_ERR_NOMEM, "batch binning scratch allocation failed");
+      }
+      b->sort_words[k] = need;
+    }
+    vgn::BinParams bp = b->jobs[k].geom->bin;
+    bp.kbits          = kbits;
+    for (int a = 0; a < 3; ++a) bp.scale[a] = b->jobs[k].geom->bin.scale[a] * (float)(1 << kbits);
+    b->bins[k] = bp;
+    r.perm     = b->d_sort[k] + vgn::bin_scratch_words(r.n, kbits);
+  }
+  b->kbits = kbits;
+  return VGN_OK;
+}
+
+int batch_enqueue(vgn_batch *b, cudaStream_t s)
+{
+  if (b->kbits > 0) {
+    for (int k = 0; k < b->jt.n_jobs; ++k) {
+      const vgn::JobRec &r = b->jt.job[k];
+      if (!r.perm) continue;
+      cudaError_t e = vgn::launch_bin_tracks(r.n, r.px, r.py, r.pz, r.dx, r.dy, r.dz, b->bins[k], b->d_sort[k],
+                                             const_cast<uint32_t *>(r.perm), b->num_sms * 32, s);
+      if (e != cudaSuccess) return cuda_fail(e, "batch track binning launch");
+    }
+  }
+  cudaError_t e = vgn::launch_multi_step(b->jt, b->d_queue, b->mixed, b->reloc, b->num_sms, b->variant, s);
+  return e == cudaSuccess ? VGN_OK : cuda_fail(e, "batch step launch");
+}
+
+}  // namespace
+
+int vgn_batch_create(int device, vgn_batch **out)
+{
+  if (!out) return fail(VGN_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return fail(VGN_ERR_ARG, "no such CUDA device");
+  }
+  vgn_batch *b = new (std::nothrow) vgn_batch();
+  if (!b) return fail(VGN_ERR_NOMEM, "host allocation failed");
+  b->device = device;
+  DeviceGuard guard(device);
+  cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaMalloc(&b->d_queue, 256) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    return fail(VGN_ERR_NOMEM, "batch work-queue allocation failed");
+  }
+  *out = b;
+  return VGN_OK;
+}
+
+int vgn_batch_free(vgn_batch *b)
+{
+  if (!b) return VGN_OK;
+  DeviceGuard guard(b->device);
+  for (uint32_t *p : b->d_sort)
+    if (p) cudaFree(p);
+  if (b->d_queue) cudaFree(b->d_queue);
+  delete b;
+  return VGN_OK;
+}
+
+int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int flags, int32_t variant,
+                       int32_t sort_kbits)
+{
+  if (!b) return fail(VGN_ERR_ARG, "null batch");
+  if (n_jobs < 1 || n_jobs > VGN_BATCH_MAX_JOBS || !jobs)
+    return fail(VGN_ERR_ARG, "a batch holds 1.." + std::to_string(VGN_BATCH_MAX_JOBS) + " jobs");
+  if (variant < 0 || variant >= vgn::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
+  if (sort_kbits < 0 || sort_kbits > 6) return fail(VGN_ERR_ARG, "track-binning granularity must be 0..6");
+  DeviceGuard guard(b->device);
+  uint64_t chunks = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    const vgn_step_job &j = jobs[k];
+    if (!j.geom || j.geom->device != b->device)
+      return fail(VGN_ERR_ARG, "job " + std::to_string(k) + ": geometry missing or on another device");
+    if (j.n < 0) return fail(VGN_ERR_ARG, "job " + std::to_string(k) + ": negative batch size");
+    if (j.n > 0) {
+      if (!j.px || !j.py || !j.pz || !j.dx || !j.dy || !j.dz || !j.step_limit || !j.in || !j.out || !j.step)
+        return fail(VGN_ERR_ARG, "job " + std::to_string(k) + ": null array argument");
+      if (classify({j.px, j.py, j.pz, j.dx, j.dy, j.dz, j.step_limit, j.in, j.out, j.step, j.safety}) != 1)
+        return fail(VGN_ERR_ARG, "job " + std::to_string(k) + ": device pointers required");
+    }
+    chunks += ((uint64_t)j.n + 31) / 32;
+  }
+  if (chunks >= UINT32_MAX) return fail(VGN_ERR_ARG, "too many tracks in one batch");
+  b->jobs.assign(jobs, jobs + n_jobs);
+  b->jt        = vgn::JobTable{};
+  b->jt.n_jobs = n_jobs;
+  uint32_t c   = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    const vgn_step_job &j = jobs[k];
+    vgn::JobRec &r        = b->jt.job[k];
+    r.g = j.geom->view;
+    r.px = j.px; r.py = j.py; r.pz = j.pz; r.dx = j.dx; r.dy = j.dy; r.dz = j.dz; r.slimit = j.step_limit;
+    r.in = j.in; r.out = j.out; r.step = j.step; r.safety = j.safety;
+    r.n                   = j.n;
+    r.perm                = nullptr;
+    b->jt.chunk_begin[k]  = c;
+    c += (uint32_t)(((uint64_t)j.n + 31) / 32);
+  }
+  b->jt.chunk_begin[n_jobs] = c;
+  b->mixed                  = (flags & VGN_PRECISION_MIXED) != 0;
+  b->reloc                  = (flags & VGN_NO_RELOCATE) ? 0 : 1;
+  b->variant                = variant;
+  return batch_configure(b, sort_kbits);
+}
+
+int vgn_batch_step(vgn_batch *b, void *stream)
+{
+  if (!b) return fail(VGN_ERR_ARG, "null batch");
+  if (b->jt.n_jobs == 0) return fail(VGN_ERR_ARG, "batch has no jobs");
+  DeviceGuard guard(b->device);
+  return batch_enqueue(b, static_cast<cudaStream_t>(stream));
+}
+
+int vgn_batch_synchronize(vgn_batch *b, void *stream)
+{
+  if (!b) return fail(VGN_ERR_ARG, "null batch");
+  DeviceGuard guard(b->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc         = VGN_OK;
+  for (const vgn_step_job &j : b->jobs) {
+    const int r = check_status(j.geom, s);
+    if (r != VGN_OK && rc == VGN_OK) rc = r;
+  }
+  if (b->jobs.empty()) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
+  }
+  return rc;
+}
+
+int vgn_batch_autotune(vgn_batch *b, void *stream, int32_t *variant, int32_t *sort_kbits, float *best_ms)
+{
+  if (!b) return fail(VGN_ERR_ARG, "null batch");
+  if (b->jt.n_jobs == 0) return fail(VGN_ERR_ARG, "batch has no jobs");
+  DeviceGuard guard(b->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  static const int kSort[] = {0, 3, 4, 5};
+  float best = 3.4e38f;
+  int bv = 0, bk = 0, rc = VGN_OK;
+  for (int k : kSort) {
+    if ((rc = batch_configure(b, k)) != VGN_OK) break;
+    for (int v = 0; v < vgn::step_variant_count() && rc == VGN_OK; ++v) {
+      b->variant = v;
+      if ((rc = batch_enqueue(b, s)) != VGN_OK) break;  // warm-up
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 2 && rc == VGN_OK; ++r) rc = batch_enqueue(b, s);
+      cudaEventRecord(e1, s);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = cuda_fail(cudaGetLastError(), "batch autotune timing");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms *= 0.5f;
+      if (ms < best) best = ms, bv = v, bk = k;
+    }
+    if (rc != VGN_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->variant = bv;
+  const int rc2 = batch_configure(b, bk);
+  if (rc != VGN_OK) return rc;
+  if (rc2 != VGN_OK) return rc2;
+  if (variant) *variant = bv;
+  if (sort_kbits) *sort_kbits = bk;
+  if (best_ms) *best_ms = best;
+  return vgn_batch_synchronize(b, stream);
+}
+
 // Binned step whose binning scratch is the library's static device buffer
 // (kernels_sort.cu): no cudaMalloc, no cudaFree, no staging workspace.
 int vgn_compute_step_batch_static(const vgn_geometry *g, int64_t n, const double *px, const double *py,

@@ -173,6 +173,15 @@ class Geometry:
         N.check(N.lib().vgn_shape_batch(self.handle, lv, op, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z), dx,
                                         dy, dz, None, _ptr(out), 0, _stream_ptr(stream)))
 
+    def walk(self, pts: SOA3D, dirs: SOA3D, step_limit, states: NavStatePool, nsteps, max_steps: int = 1 << 20,
+             mixed: bool = False, stream=None):
+        """Step every track (p += step * d, state = propagated state) until it leaves the world
+        or after `max_steps` steps, on the device; `pts` and `states` are updated in place and
+        `nsteps` (int32) receives the steps taken."""
+        N.check(N.lib().vgn_walk_batch(self.handle, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z), _ptr(dirs.x),
+                                       _ptr(dirs.y), _ptr(dirs.z), _ptr(step_limit), _ptr(states.data), max_steps,
+                                       _ptr(nsteps), N.VGN_PRECISION_MIXED if mixed else 0, _stream_ptr(stream)))
+
     # ---- step-kernel launch configuration ---------------------------------
     def set_step_config(self, variant: int, sort_kbits: int, mixed: bool = False):
         N.check(N.lib().vgn_set_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, variant, sort_kbits))
@@ -227,3 +236,49 @@ class BVHNavigator:
 
     def LocatePoints(self, globalpoints: SOA3D, out_states: NavStatePool, stream=None):
         self.geometry.locate(globalpoints, out_states, mixed=self.mixed, stream=stream)
+
+
+class StepBatch:
+    """Many (geometry, track batch) jobs stepped in one persistent launch (vgn_batch).
+
+    ``set_jobs`` takes a list of ``(geometry, points, dirs, step_limit, in_states, out_states,
+    steps, safeties_or_None)`` tuples of device arrays; ``step`` enqueues one step of every job
+    on ``stream`` (no allocation, no host synchronisation: it can be recorded into a CUDA
+    graph); ``synchronize`` waits and reports device-side errors of any job's geometry."""
+
+    def __init__(self, device: int = 0):
+        self.handle = C.c_void_p()
+        N.check(N.lib().vgn_batch_create(device, C.byref(self.handle)))
+        self._keep = None
+
+    def close(self):
+        if self.handle:
+            N.lib().vgn_batch_free(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_jobs(self, jobs, mixed: bool = False, relocate: bool = True, variant: int = 0, sort_kbits: int = 0):
+        arr = (N.StepJob * len(jobs))()
+        for k, (geo, pts, dirs, sl, inp, out, steps, saf) in enumerate(jobs):
+            arr[k] = N.StepJob(geo.handle, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z), _ptr(dirs.x),
+                               _ptr(dirs.y), _ptr(dirs.z), _ptr(sl), _ptr(inp.data), _ptr(out.data), _ptr(steps),
+                               _ptr(saf))
+        flags = (N.VGN_PRECISION_MIXED if mixed else 0) | (0 if relocate else N.VGN_NO_RELOCATE)
+        N.check(N.lib().vgn_batch_set_jobs(self.handle, len(jobs), arr, flags, variant, sort_kbits))
+        self._keep = jobs  # the arrays must outlive the batch's use of them
+
+    def step(self, stream=None):
+        N.check(N.lib().vgn_batch_step(self.handle, _stream_ptr(stream)))
+
+    def synchronize(self, stream=None):
+        N.check(N.lib().vgn_batch_synchronize(self.handle, _stream_ptr(stream)))
+
+    def autotune(self, stream=None) -> tuple[int, int, float]:
+        v, k, ms = C.c_int32(), C.c_int32(), C.c_float()
+        N.check(N.lib().vgn_batch_autotune(self.handle, _stream_ptr(stream), C.byref(v), C.byref(k), C.byref(ms)))
+        return v.value, k.value, ms.value

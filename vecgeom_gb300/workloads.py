@@ -426,3 +426,26 @@ def mixed_shape_tracks(n: int, seed_points: int = 22, seed_dirs: int = 23, world
                        step_limit: float = 1000.0) -> TrackBatch:
     """Points uniform in the world box (to be located before stepping), isotropic directions."""
     return uniform_tracks(n, world * (1.0 - 1e-9), seed_points, seed_dirs, step_limit)
+
+
+# ---------------------------------------------------------------- batched uneven workload
+def batched_workload(n_geometries: int = 64, seed: int = 10, daughters=(64, 16384), tracks=(1000, 524288)):
+    """`n_geometries` mixed-shape geometries (geometry g uses seed `seed + g`) with daughter
+    counts 2^k, k uniform over the powers of two in `daughters` (log-uniform), on a jittered
+    grid of 250 mm pitch along its longest axis, and a track batch per geometry of a size
+    log-uniform in `tracks` (points uniform in the world, to be located before stepping).
+    Returns a list of (GeometryDescription, TrackBatch)."""
+    out = []
+    kmin, kmax = int(round(math.log2(daughters[0]))), int(round(math.log2(daughters[1])))
+    for g in range(n_geometries):
+        rng = np.random.Generator(np.random.PCG64(seed + g))
+        k = int(rng.integers(kmin, kmax + 1))
+        a = k // 3
+        b = (k - a) // 2
+        grid = (1 << a, 1 << b, 1 << (k - a - b))
+        world = 125.0 * max(grid)
+        desc = mixed_shape_geometry(seed=seed + g, grid=grid, world=world)
+        n = int(round(math.exp(rng.uniform(math.log(tracks[0]), math.log(tracks[1])))))
+        t = mixed_shape_tracks(n, seed_points=1000 + seed + g, seed_dirs=2000 + seed + g, world=world)
+        out.append((desc, t))
+    return out
