@@ -1311,15 +1311,7 @@ __device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
 }
 
 // ---------------------------------------------------------------- dispatch
-// The dispatchers are inlined by default; VGN_NOINLINE_SHAPES makes them real calls, which
-// keeps the seven shapes' code out of every call site (smaller kernels, less register
-// pressure in the traversal loops).
-#ifdef VGN_NOINLINE_SHAPES
-#define VGN_SHAPE_DISPATCH __device__ __noinline__
-#else
-#define VGN_SHAPE_DISPATCH __device__ __forceinline__
-#endif
-VGN_SHAPE_DISPATCH double shape_dist_in(int type, const double *r, D3 p, D3 d)
+__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
   switch (type) {
   case kBox: return box_dist_in(r, p, d);
@@ -1333,7 +1325,7 @@ VGN_SHAPE_DISPATCH double shape_dist_in(int type, const double *r, D3 p, D3 d)
   return kInfLength;
 }
 
-VGN_SHAPE_DISPATCH double shape_dist_out(int type, const double *r, D3 p, D3 d)
+__device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p, D3 d)
 {
   switch (type) {
   case kBox: return box_dist_out(r, p, d);
@@ -1347,7 +1339,7 @@ VGN_SHAPE_DISPATCH double shape_dist_out(int type, const double *r, D3 p, D3 d)
   return -1.;
 }
 
-VGN_SHAPE_DISPATCH double shape_safe_in(int type, const double *r, D3 p)
+__device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_safe_in(r, p);
@@ -1361,7 +1353,7 @@ VGN_SHAPE_DISPATCH double shape_safe_in(int type, const double *r, D3 p)
   return kInfLength;
 }
 
-VGN_SHAPE_DISPATCH double shape_safe_out(int type, const double *r, D3 p)
+__device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_safe_out(r, p);
@@ -1375,7 +1367,7 @@ VGN_SHAPE_DISPATCH double shape_safe_out(int type, const double *r, D3 p)
   return 0.;
 }
 
-VGN_SHAPE_DISPATCH bool shape_contains(int type, const double *r, D3 p)
+__device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_contains(r, p);
@@ -1389,7 +1381,7 @@ VGN_SHAPE_DISPATCH bool shape_contains(int type, const double *r, D3 p)
   return false;
 }
 
-VGN_SHAPE_DISPATCH int shape_inside(int type, const double *r, D3 p)
+__device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_inside(r, p);
