@@ -118,9 +118,23 @@ struct alignas(128) IXForm {  // placement transform as intervals + box half-len
   float r_lo[9], r_hi[9];
   float h_lo[3], h_hi[3];  // box half-lengths; zero for other shapes
   int32_t shape;
-  int32_t pad[1];
+  int32_t isin;  // first (lo, hi) pair of the shape's GeomView::isin row; -1: no interval SafetyToIn
 };
 static_assert(sizeof(IXForm) == 128, "IXForm must be 128 bytes");
+
+// Rows of GeomView::isin: FP32 (lo, hi) enclosures of the doubles that each shape's
+// SafetyToIn reads or derives from its parameters (derived values computed on the
+// host with the device's FP64 operations), so that the interval SafetyToIn of the
+// mixed kernels runs without FP64 instructions.  Flags are stored as 0/1 pairs.
+namespace irow {
+enum { TubeZ = 0, TubeRmax, TubeRmin, TubeHasRmin, kTubeRow };
+enum { ConeDz = 0, ConeMinusConeTol, ConeTol, ConeHasRmin, ConeOuterConst, ConeOuterR, ConeOuterSlope,
+       ConeOuterOffset, ConeTwoOuterTol, ConeInnerConst, ConeInnerR, ConeInnerSlope, ConeInnerOffset,
+       ConeTwoInnerTol, ConeTanRMax, ConeAvgRmax, ConeInvSecRMax, ConeTanRMin, ConeAvgRmin, ConeInvSecRMin, kConeRow };
+enum { TrdDz = 0, TrdHalfX, TrdFx, TrdCalfX, TrdVaryingY, TrdHalfY, TrdFy, TrdCalfY, TrdDy1, kTrdRow };
+enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, kTrapRow = 17 };
+enum { SphHasRmin = 0, SphRmin, SphRmax, SphMsqMax, SphPsqMax, SphPsqMin, SphMsqMin, kSphereRow };
+}  // namespace irow
 
 // Row layouts (doubles) of GeomView::shape per shape type.
 namespace row {
@@ -175,6 +189,7 @@ struct GeomView {
   const IPrimSlab *iprims;   // indexed like prims
   const ISafe *iprim_safe;
   const IXForm *ixf;         // per placed volume
+  const float *isin;         // interval SafetyToIn rows (irow), (lo, hi) pairs
   const double *shape;
   uint32_t navind_words;
   int32_t n_pv;

@@ -488,6 +488,70 @@ void set_interval(float *lo, float *hi, double v)
   *hi = round_up(v);
 }
 
+// Appends the interval SafetyToIn row (geom_types.h irow) of one shape to `out` and
+// returns its first pair index, or -1 for shapes without one (Box uses IXForm's
+// half-lengths; Polycone is evaluated in FP64).  Each derived value is computed with
+// the same FP64 operations as the device's SafetyToIn (host code is built with
+// -ffp-contract=off), so its enclosure also encloses the device's double.
+static int build_isin_row(int shape, const double *r, std::vector<float> &out)
+{
+  constexpr double kTolerance = 1e-9, kConeTolerance = 1e-7;  // base/Math.h, ConeStruct
+  std::vector<double> v;
+  switch (shape) {
+  case kTube:  // TubeImplementation.h:912-938
+    v = {r[row::TubeZ], r[row::TubeRmax], r[row::TubeRmin], r[row::TubeRmin] > 0 ? 1. : 0.};
+    break;
+  case kCone: {  // ConeImplementation.h:368-432, ConeUtilities.h cone radius / safety to the conical surface
+    v.assign(irow::kConeRow, 0.);
+    v[irow::ConeDz]           = r[row::ConeDz];
+    v[irow::ConeMinusConeTol] = -kConeTolerance;
+    v[irow::ConeTol]          = kTolerance;
+    v[irow::ConeHasRmin]      = (r[row::ConeRmin1] > 0 || r[row::ConeRmin2] > 0) ? 1. : 0.;
+    v[irow::ConeOuterConst]   = r[row::ConeOrigRmax1] == r[row::ConeOrigRmax2] ? 1. : 0.;
+    v[irow::ConeOuterR]       = r[row::ConeOrigRmax1];
+    v[irow::ConeOuterSlope]   = r[row::ConeOuterSlope];
+    v[irow::ConeOuterOffset]  = r[row::ConeOuterOffset];
+    v[irow::ConeTwoOuterTol]  = 2.0 * r[row::ConeOuterTol];
+    v[irow::ConeInnerConst]   = r[row::ConeRmin1] == r[row::ConeRmin2] ? 1. : 0.;
+    v[irow::ConeInnerR]       = r[row::ConeRmin1];
+    v[irow::ConeInnerSlope]   = r[row::ConeInnerSlope];
+    v[irow::ConeInnerOffset]  = r[row::ConeInnerOffset];
+    v[irow::ConeTwoInnerTol]  = 2.0 * r[row::ConeInnerTol];
+    v[irow::ConeTanRMax]      = r[row::ConeTanRMax];
+    v[irow::ConeAvgRmax]      = (r[row::ConeRmax1] + r[row::ConeRmax2]) * 0.5;
+    v[irow::ConeInvSecRMax]   = r[row::ConeInvSecRMax];
+    v[irow::ConeTanRMin]      = r[row::ConeTanRMin];
+    v[irow::ConeAvgRmin]      = (r[row::ConeRmin1] + r[row::ConeRmin2]) * 0.5;
+    v[irow::ConeInvSecRMin]   = r[row::ConeInvSecRMin];
+    break;
+  }
+  case kTrd:  // TrdImplementation.h:140-168
+    v = {r[row::TrdDz],  r[row::TrdHalfX1plusX2], r[row::TrdFx], r[row::TrdCalfX],
+         r[row::TrdDy1] != r[row::TrdDy2] ? 1. : 0., r[row::TrdHalfY1plusY2], r[row::TrdFy], r[row::TrdCalfY],
+         r[row::TrdDy1]};
+    break;
+  case kTrapezoid:  // TrapezoidImplementation.h:341-371 over PlaneShell<4>
+    v.assign(r, r + irow::kTrapRow);
+    break;
+  case kSphere: {  // SphereImplementation.h:388-420, SphereUtilities.h:54-108 (full sphere)
+    const double rmin = r[row::SphRmin], rmax = r[row::SphRmax];
+    v = {rmin != 0. ? 1. : 0., rmin, rmax, std::fabs(rmax * (rmax - 2.0 * kTolerance)),
+         rmax * (rmax + 2.0 * kTolerance), rmin * (rmin + 2.0 * kTolerance),
+         std::fabs(rmin * (rmin - 2.0 * kTolerance))};
+    break;
+  }
+  default: return -1;
+  }
+  const int pos = (int)(out.size() / 2);
+  for (double d : v) {
+    float lo, hi;
+    set_interval(&lo, &hi, d);
+    out.push_back(lo);
+    out.push_back(hi);
+  }
+  return pos;
+}
+
 // Interval (FP32) images of the FP64 tables, for the mixed-precision kernels.
 void build_interval_images(HostGeometry &g)
 {
@@ -527,6 +591,13 @@ void build_interval_images(HostGeometry &g)
     p.prim = g.prims[i].prim;
     safe(g.prims[i].mn, g.prims[i].mx, g.iprim_safe[i]);
   }
+  // interval SafetyToIn rows, one per logical volume of a shape that has one
+  std::vector<int32_t> lv_isin(g.lv.size(), -1);
+  g.isin.clear();
+  for (size_t l = 0; l < g.lv.size(); ++l) {
+    const int pos = build_isin_row(g.lv[l].shape, &g.shape[g.lv[l].shape_row], g.isin);
+    if (pos >= 0) lv_isin[l] = pos;
+  }
   g.ixf.assign(g.pv.size(), IXForm());
   for (size_t i = 0; i < g.pv.size(); ++i) {
     IXForm &x = g.ixf[i];
@@ -535,6 +606,7 @@ void build_interval_images(HostGeometry &g)
     for (int c = 0; c < 9; ++c) set_interval(&x.r_lo[c], &x.r_hi[c], g.pv[i].xf.r[c]);
     const HostLV &lv = g.lv[g.pv[i].lv];
     x.shape          = lv.shape;
+    x.isin           = lv_isin[g.pv[i].lv];
     if (lv.shape == kBox)
       for (int c = 0; c < 3; ++c) set_interval(&x.h_lo[c], &x.h_hi[c], g.shape[lv.shape_row + c]);
   }

@@ -72,6 +72,7 @@ struct HostGeometry {
   std::vector<IPrimSlab> iprims;
   std::vector<ISafe> iprim_safe;
   std::vector<IXForm> ixf;
+  std::vector<float> isin;  // interval SafetyToIn rows (geom_types.h irow), (lo, hi) pairs
 };
 
 // Returns 0 on success, a VGN_ERR_* code otherwise (message in err).

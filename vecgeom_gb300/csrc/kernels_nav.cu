@@ -38,9 +38,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) step_kernel(GeomView g, int64_t n
                                                    const double *__restrict__ dx, const double *__restrict__ dy,
                                                    const double *__restrict__ dz, const double *__restrict__ slimit,
                                                    const vgn_state *__restrict__ in, vgn_state *__restrict__ out,
-                                                   double *__restrict__ step, double *__restrict__ safety, int reloc,
+                                                   double *__restrict__ step, int reloc,
                                                    const uint32_t *__restrict__ perm)
 {
+  // the step only: safeties come from safety_kernel, a separate pass over the same order
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = perm ? (int64_t)__ldg(perm + t) : t;  // binned visit order, results stay at index i
     const State s   = load_state(in, i);
@@ -50,11 +51,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) step_kernel(GeomView g, int64_t n
       raise_error(g, kErrState);
       st = 0.;
     } else {
-      st = nav_step<MIXED>(g, d3(px[i], py[i], pz[i]), d3(dx[i], dy[i], dz[i]), slimit[i], s, o,
-                           safety != nullptr, sf, reloc != 0);
+      st = nav_step<MIXED>(g, d3(px[i], py[i], pz[i]), d3(dx[i], dy[i], dz[i]), slimit[i], s, o, false, sf,
+                           reloc != 0);
     }
     step[i] = st;
-    if (safety) safety[i] = sf;
     store_state(out, i, o);
   }
 }
@@ -89,12 +89,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) multi_step_kernel(const __grid_co
       if (!ni_valid(j.g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(j.g, s.last_exited))) {
         raise_error(j.g, kErrState);
         st = 0.;
-      } else {
+      } else {  // safeties come from multi_safety_kernel, launched before this kernel
         st = nav_step<MIXED>(j.g, d3(j.px[i], j.py[i], j.pz[i]), d3(j.dx[i], j.dy[i], j.dz[i]), j.slimit[i], s,
-                             o, j.safety != nullptr, sf, reloc != 0);
+                             o, false, sf, reloc != 0);
       }
       j.step[i] = st;
-      if (j.safety) j.safety[i] = sf;
       store_state(j.out, i, o);
     }
     __syncwarp();
@@ -139,23 +138,74 @@ __global__ void __launch_bounds__(128, 6) walk_kernel(GeomView g, int64_t n, dou
   }
 }
 
-// VSafetyEstimatorHelper::ComputeSafety (VSafetyEstimator.h:98-107)
+// Safety of one track at its state's volume: VSafetyEstimatorHelper::ComputeSafety
+// (VSafetyEstimator.h:98-107), also the safety part of ComputeStepAndSafetyAndPropagatedState
+// (VNavigator.h:1014-1064), which takes it at the input state before the step.  With
+// `step_checks` the track is rejected like the step kernel rejects it (invalid last-exited
+// state too), so a step followed by this pass writes what one fused step would.
+__device__ __forceinline__ bool safety_state_ok(const GeomView &g, const State &s, bool step_checks)
+{
+  return ni_valid(g, s.nav_ind) && !(step_checks && s.last_exited != 0 && !ni_valid(g, s.last_exited));
+}
+
+template <bool MIXED>
+__device__ __forceinline__ double track_safety(const GeomView &g, const State &s, D3 gp)
+{
+  Xf m;
+  top_matrix(g, s.nav_ind, m);
+  const LVRec lv = load_lv(g, pv_lv(g, ni_top(g, s.nav_ind)));
+  return safety_local<MIXED>(g, lv, xf_point(m.t, m.r, gp), d3(1., 0., 0.));
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(256) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
                                                      const double *__restrict__ py, const double *__restrict__ pz,
-                                                     const vgn_state *__restrict__ in, double *__restrict__ safety)
+                                                     const vgn_state *__restrict__ in, double *__restrict__ safety,
+                                                     const uint32_t *__restrict__ perm, int step_checks)
 {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const State s = load_state(in, i);
-    if (!ni_valid(g, s.nav_ind)) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm ? (int64_t)__ldg(perm + t) : t;
+    const State s   = load_state(in, i);
+    if (!safety_state_ok(g, s, step_checks != 0)) {
       raise_error(g, kErrState);
       safety[i] = 0.;
       continue;
     }
-    Xf m;
-    top_matrix(g, s.nav_ind, m);
-    const LVRec lv = load_lv(g, pv_lv(g, ni_top(g, s.nav_ind)));
-    safety[i]      = safety_local<MIXED>(g, lv, xf_point(m.t, m.r, d3(px[i], py[i], pz[i])), d3(1., 0., 0.));
+    safety[i] = track_safety<MIXED>(g, s, d3(px[i], py[i], pz[i]));
+  }
+}
+
+// Persistent multi-job safety pass over the same job table and chunk space as
+// multi_step_kernel, for the jobs that asked for safeties.
+template <bool MIXED>
+__global__ void __launch_bounds__(256, 4) multi_safety_kernel(const __grid_constant__ JobTable jt,
+                                                              uint32_t *__restrict__ queue)
+{
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    uint32_t chunk = 0;
+    if (lane == 0) chunk = atomicAdd(queue, 1u);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if (chunk >= jt.chunk_begin[jt.n_jobs]) return;
+    int lo = 0, hi = jt.n_jobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jt.chunk_begin[mid] <= chunk) lo = mid;
+      else hi = mid - 1;
+    }
+    const JobRec &j = jt.job[lo];
+    const int64_t t = (int64_t)(chunk - jt.chunk_begin[lo]) * 32 + lane;
+    if (j.safety && t < j.n) {
+      const int64_t i = j.perm ? (int64_t)__ldg(j.perm + t) : t;
+      const State s   = load_state(j.in, i);
+      if (!safety_state_ok(j.g, s, true)) {
+        raise_error(j.g, kErrState);
+        j.safety[i] = 0.;
+      } else {
+        j.safety[i] = track_safety<MIXED>(j.g, s, d3(j.px[i], j.py[i], j.pz[i]));
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -225,7 +275,7 @@ static void launch_step_v(const GeomView &g, const StepArgs &a, cudaStream_t s)
   // grid-stride over tracks; enough blocks to fill every SM several times over
   const unsigned grid = grid_for(a.n, BLOCK, a.max_blocks * (256 / BLOCK));
   dev::step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit,
-                                                              a.in, a.out, a.step, a.safety, a.reloc, a.perm);
+                                                              a.in, a.out, a.step, a.reloc, a.perm);
 }
 
 template <bool MIXED>
@@ -241,8 +291,23 @@ static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cud
   }
 }
 
+// The safety runs as its own pass over the same visit order, before the step (which may
+// overwrite the input states when out == in): fused into the step kernel it shares one
+// register budget and one instruction footprint with the step traversal and the
+// relocation, which measured slower than the two passes together.
+static void launch_safety_pass(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(a.n, block, a.max_blocks);
+  if (mixed)
+    dev::safety_kernel<true><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety, a.perm, 1);
+  else
+    dev::safety_kernel<false><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety, a.perm, 1);
+}
+
 cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s)
 {
+  if (a.safety) launch_safety_pass(g, a, mixed, s);
   if (mixed)
     launch_step_m<true>(g, a, variant, s);
   else
@@ -274,8 +339,17 @@ static void launch_multi_m(const JobTable &jt, uint32_t *queue, int reloc, int n
 cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, int reloc, int num_sms, int variant,
                               cudaStream_t s)
 {
-  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+  cudaError_t e = cudaMemsetAsync(queue, 0, 2 * sizeof(uint32_t), s);  // step and safety queues
   if (e != cudaSuccess) return e;
+  bool any_safety = false;
+  for (int k = 0; k < jt.n_jobs; ++k) any_safety = any_safety || jt.job[k].safety != nullptr;
+  if (any_safety) {  // before the step, which may overwrite the input states
+    const unsigned grid = (unsigned)(num_sms * 4);
+    if (mixed)
+      dev::multi_safety_kernel<true><<<grid, 256, 0, s>>>(jt, queue + 1);
+    else
+      dev::multi_safety_kernel<false><<<grid, 256, 0, s>>>(jt, queue + 1);
+  }
   if (mixed)
     launch_multi_m<true>(jt, queue, reloc, num_sms, variant, s);
   else
@@ -302,9 +376,9 @@ cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const 
   const int block     = 256;
   const unsigned grid = grid_for(n, block, max_blocks);
   if (mixed)
-    dev::safety_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety);
+    dev::safety_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety, nullptr, 0);
   else
-    dev::safety_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety);
+    dev::safety_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety, nullptr, 0);
   return cudaGetLastError();
 }
 

@@ -194,6 +194,189 @@ __device__ __forceinline__ FI ibox_safety_in(const IXForm &x, const FI *p)
   return m;
 }
 
+// ---- interval SafetyToIn of the other shapes --------------------------------
+// Each follows the FP64 operation sequence of the shape's SafetyToIn with outward-
+// rounded FP32 intervals over the precomputed enclosures of GeomView::isin, so every
+// intermediate interval contains the double the FP64 code computes; a branch the
+// intervals cannot decide makes the bound unavailable (false) and the caller falls
+// back to FP64.  No FP64 instruction is issued here.
+__device__ __forceinline__ FI fi_sqr(FI a)  // a * a
+{
+  const float l = fabsf(a.lo), h = fabsf(a.hi);
+  if (a.lo <= 0.f && a.hi >= 0.f) {
+    const float m = fmaxf(l, h);
+    return FI{0.f, __fmul_ru(m, m)};
+  }
+  const float m = fminf(l, h), M = fmaxf(l, h);
+  return FI{__fmul_rd(m, m), __fmul_ru(M, M)};
+}
+__device__ __forceinline__ FI fi_sqrt(FI a) { return FI{__fsqrt_rd(fmaxf(a.lo, 0.f)), __fsqrt_ru(fmaxf(a.hi, 0.f))}; }
+__device__ __forceinline__ FI fi_neg(FI a) { return FI{-a.hi, -a.lo}; }
+__device__ __forceinline__ FI iq(const float *q, int k)
+{
+  const float2 v = __ldg(reinterpret_cast<const float2 *>(q) + k);
+  return FI{v.x, v.y};
+}
+__device__ __forceinline__ bool iflag(const float *q, int k) { return __ldg(q + 2 * k) != 0.f; }
+
+// the daughter-frame point: Transformation3D::Transform, (p - t) then the rotation
+__device__ __forceinline__ void ixf_local(const IXForm &x, const FI *p, FI *l)
+{
+  FI t[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) t[k] = fi_sub(p[k], FI{__ldg(&x.t_lo[k]), __ldg(&x.t_hi[k])});
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    FI v = fi_mul(t[0], FI{__ldg(&x.r_lo[i]), __ldg(&x.r_hi[i])});
+    v    = fi_add(v, fi_mul(t[1], FI{__ldg(&x.r_lo[3 + i]), __ldg(&x.r_hi[3 + i])}));
+    l[i] = fi_add(v, fi_mul(t[2], FI{__ldg(&x.r_lo[6 + i]), __ldg(&x.r_hi[6 + i])}));
+  }
+}
+
+// TubeImplementation SafetyToInOld (TubeImplementation.h:912-938)
+__device__ __forceinline__ bool itube_safe_in(const float *q, const FI *p, FI &out)
+{
+  FI s       = fi_sub(fi_abs(p[2]), iq(q, irow::TubeZ));
+  const FI r = fi_sqrt(fi_add(fi_sqr(p[0]), fi_sqr(p[1])));
+  s          = fi_max(s, fi_sub(r, iq(q, irow::TubeRmax)));
+  if (iflag(q, irow::TubeHasRmin)) s = fi_max(s, fi_sub(iq(q, irow::TubeRmin), r));
+  out = s;
+  return true;
+}
+
+// ConeImplementation SafetyToIn (ConeImplementation.h:368-432)
+__device__ __forceinline__ bool icone_safe_in(const float *q, const FI *p, FI &out)
+{
+  using namespace irow;
+  const bool hasrmin = iflag(q, ConeHasRmin);
+  const FI distz     = fi_sub(fi_abs(p[2]), iq(q, ConeDz));
+  const FI rsq       = fi_add(fi_sqr(p[0]), fi_sqr(p[1]));
+  int inside         = fi_lt(distz, iq(q, ConeMinusConeTol));
+  {  // rsq < |R (R - 2 tol)|, R the outer radius at z (ConeUtilities.h GetRadiusOfConeAtPoint)
+    const FI R = iflag(q, ConeOuterConst) ? iq(q, ConeOuterR)
+                                          : fi_add(fi_mul(iq(q, ConeOuterSlope), p[2]), iq(q, ConeOuterOffset));
+    inside = and3(inside, fi_lt(rsq, fi_abs(fi_mul(R, fi_sub(R, iq(q, ConeTwoOuterTol))))), kYes);
+  }
+  if (hasrmin) {  // rsq > R (R + 2 tol), R the inner radius at z
+    const FI R = iflag(q, ConeInnerConst) ? iq(q, ConeInnerR)
+                                          : fi_add(fi_mul(iq(q, ConeInnerSlope), p[2]), iq(q, ConeInnerOffset));
+    inside = and3(inside, fi_lt(fi_mul(R, fi_add(R, iq(q, ConeTwoInnerTol))), rsq), kYes);
+  }
+  if (inside == kMaybe) return false;
+  if (inside == kYes) {
+    out = FI{-1.f, -1.f};
+    return true;
+  }
+  const FI rho = fi_sqrt(rsq);
+  const FI pRMax = fi_add(fi_mul(iq(q, ConeTanRMax), p[2]), iq(q, ConeAvgRmax));
+  FI s           = fi_neg(fi_mul(fi_sub(pRMax, rho), iq(q, ConeInvSecRMax)));
+  if (hasrmin) {
+    const FI pRMin = fi_add(fi_mul(iq(q, ConeTanRMin), p[2]), iq(q, ConeAvgRmin));
+    s              = fi_max(s, fi_neg(fi_mul(fi_sub(rho, pRMin), iq(q, ConeInvSecRMin))));
+  }
+  s = fi_max(distz, s);
+  // fabs(safety) < kTolerance ? 0 : safety
+  const FI tol = iq(q, ConeTol);
+  if (s.lo > -tol.lo && s.hi < tol.lo) {
+    s = FI{0.f, 0.f};
+  } else if (!(s.lo >= tol.hi || s.hi <= -tol.hi)) {
+    return false;
+  }
+  out = s;
+  return true;
+}
+
+// TrdUtilities::Safety<inside = false> (TrdImplementation.h:140-168)
+__device__ __forceinline__ bool itrd_safe_in(const float *q, const FI *p, FI &out)
+{
+  using namespace irow;
+  FI dist        = fi_sub(iq(q, TrdDz), fi_abs(p[2]));
+  const FI distx = fi_sub(iq(q, TrdHalfX), fi_mul(iq(q, TrdFx), p[2]));
+  const int okx  = fi_ge0(distx);
+  if (okx == kMaybe) return false;
+  if (okx == kYes) dist = fi_min(dist, fi_mul(fi_sub(distx, fi_abs(p[0])), iq(q, TrdCalfX)));
+  if (iflag(q, TrdVaryingY)) {
+    const FI disty = fi_sub(iq(q, TrdHalfY), fi_mul(iq(q, TrdFy), p[2]));
+    const int oky  = fi_ge0(disty);
+    if (oky == kMaybe) return false;
+    if (oky == kYes) dist = fi_min(dist, fi_mul(fi_sub(disty, fi_abs(p[1])), iq(q, TrdCalfY)));
+  } else {
+    dist = fi_min(dist, fi_sub(iq(q, TrdDy1), fi_abs(p[1])));
+  }
+  out = fi_neg(dist);
+  return true;
+}
+
+// TrapezoidImplementation SafetyToIn over the four side planes (TrapezoidImplementation.h:341-371)
+__device__ __forceinline__ bool itrap_safe_in(const float *q, const FI *p, FI &out)
+{
+  using namespace irow;
+  FI s = fi_sub(fi_abs(p[2]), iq(q, TrapDz));
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    FI d = fi_add(fi_mul(iq(q, TrapA + i), p[0]), fi_mul(iq(q, TrapB + i), p[1]));
+    d    = fi_add(fi_add(d, fi_mul(iq(q, TrapC + i), p[2])), iq(q, TrapD + i));
+    s    = fi_max(s, d);
+  }
+  out = s;
+  return true;
+}
+
+// SphereImplementation SafetyToIn, full sphere (SphereImplementation.h:388-420)
+__device__ __forceinline__ bool isphere_safe_in(const float *q, const FI *p, FI &out)
+{
+  using namespace irow;
+  const bool hasrmin = iflag(q, SphHasRmin);
+  const FI rad2      = fi_add(fi_add(fi_sqr(p[0]), fi_sqr(p[1])), fi_sqr(p[2]));
+  int cin, cout;
+  if (hasrmin) {
+    cin         = and3(fi_le(rad2, iq(q, SphMsqMax)), fi_le(iq(q, SphPsqMin), rad2), kYes);
+    const int a = fi_le(iq(q, SphPsqMax), rad2), b = fi_le(rad2, iq(q, SphMsqMin));
+    cout        = (a == kYes || b == kYes) ? kYes : ((a == kNo && b == kNo) ? kNo : kMaybe);
+  } else {
+    cin  = fi_le(rad2, iq(q, SphMsqMax));
+    cout = fi_le(iq(q, SphPsqMax), rad2);
+  }
+  if (cin == kMaybe) return false;
+  if (cin == kYes) {
+    out = FI{-1.f, -1.f};
+    return true;
+  }
+  if (cout == kMaybe) return false;
+  if (cout == kNo) {
+    out = FI{0.f, 0.f};
+    return true;
+  }
+  const FI rad = fi_sqrt(rad2);
+  out = hasrmin ? fi_max(fi_sub(iq(q, SphRmin), rad), fi_sub(rad, iq(q, SphRmax))) : fi_sub(rad, iq(q, SphRmax));
+  return true;
+}
+
+// Interval SafetyToIn of a daughter at the mother-frame interval point p: Box from
+// IXForm's half-lengths, Tube/Cone/Trd/Trapezoid/Sphere from GeomView::isin; false
+// for Polycone or an undecided branch.
+__device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm &x, const FI *p, FI &out)
+{
+  const int type = __ldg(&x.shape);
+  if (type == kBox) {
+    out = ibox_safety_in(x, p);
+    return true;
+  }
+  const int off = __ldg(&x.isin);
+  if (off < 0) return false;
+  FI l[3];
+  ixf_local(x, p, l);
+  const float *q = g.isin + 2 * off;
+  switch (type) {
+  case kTube: return itube_safe_in(q, l, out);
+  case kCone: return icone_safe_in(q, l, out);
+  case kTrd: return itrd_safe_in(q, l, out);
+  case kTrapezoid: return itrap_safe_in(q, l, out);
+  case kSphere: return isphere_safe_in(q, l, out);
+  }
+  return false;
+}
+
 // ------------------------------------------------------------------ step
 constexpr int kMaxStepCand = 16;
 
@@ -298,8 +481,8 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
 constexpr int kMaxSafeCand = 8;
 
 // Running minimum of BVH::ComputeSafety known as: an exact part `known`
-// (mother safety and daughters evaluated in FP64) and pending box daughters
-// whose SafetyToIn is known as an FP32 interval.
+// (mother safety and daughters evaluated in FP64) and pending daughters whose
+// SafetyToIn is known as an FP32 interval (ishape_safety_in).
 struct SafeRun {
   double known;
   FI knownI;
@@ -344,8 +527,9 @@ __device__ __forceinline__ bool saferun_less(const GeomView &g, const MixedRay &
   return exact() < s.known;
 }
 
-// BVH::ComputeSafety (BVH.h:172-209) with exact pruning decisions and
-// deferred FP64 evaluation of box daughters.
+// BVH::ComputeSafety (BVH.h:172-209) with exact pruning decisions and deferred
+// FP64 evaluation of the daughters that have an interval SafetyToIn (all shapes
+// but Polycone, which is evaluated in FP64 at once).
 __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRec &lv, const MixedRay &r,
                                                    double safety)
 {
@@ -375,15 +559,12 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
         if (pre == kNo) continue;
         const int vol   = __ldg(&iprims[off + i].pv);
         const IXForm &x = g.ixf[vol];
-        const bool box  = __ldg(&x.shape) == kBox;
         FI d{0.f, 0.f};
-        if (box) {
-          d = ibox_safety_in(x, r.p);
-          if (d.lo >= s.cur.hi) continue;  // SafetyToIn >= running minimum: no update either way
-        }
+        const bool bound = ishape_safety_in(g, x, r.p, d);
+        if (bound && d.lo >= s.cur.hi) continue;  // SafetyToIn >= running minimum: no update either way
         const PrimRec &pr = prims[off + i];
         if (pre == kMaybe && !saferun_less(g, r, s, sbox, [&] { return box_safety(pr.mn, pr.mx, r.lp); })) continue;
-        if (box) {
+        if (bound) {
           if (s.n == kMaxSafeCand) saferun_resolve(g, r, s);
           s.pv[s.n] = vol;
           s.lo[s.n] = d.lo;

@@ -242,7 +242,7 @@ int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry 
       (rc = upload(g, h.fprims, &v.fprims)) || (rc = upload(g, h.shape, &v.shape)) ||
       (rc = upload(g, h.inodes, &v.inodes)) || (rc = upload(g, h.inode_safe, &v.inode_safe)) ||
       (rc = upload(g, h.iprims, &v.iprims)) || (rc = upload(g, h.iprim_safe, &v.iprim_safe)) ||
-      (rc = upload(g, h.ixf, &v.ixf))) {
+      (rc = upload(g, h.ixf, &v.ixf)) || (rc = upload(g, h.isin, &v.isin))) {
     vgn_geometry_free(g);
     return rc;
   }
