@@ -46,13 +46,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) step_kernel(GeomView g, int64_t n
     const int64_t i = perm ? (int64_t)__ldg(perm + t) : t;  // binned visit order, results stay at index i
     const State s   = load_state(in, i);
     State o       = s;
-    double sf = 0., st;
+    double st;
     if (!ni_valid(g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(g, s.last_exited))) {
       raise_error(g, kErrState);
       st = 0.;
     } else {
-      st = nav_step<MIXED>(g, d3(px[i], py[i], pz[i]), d3(dx[i], dy[i], dz[i]), slimit[i], s, o, false, sf,
-                           reloc != 0);
+      st = nav_step<MIXED>(g, d3(px[i], py[i], pz[i]), d3(dx[i], dy[i], dz[i]), slimit[i], s, o, reloc != 0);
     }
     step[i] = st;
     store_state(out, i, o);
@@ -85,13 +84,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) multi_step_kernel(const __grid_co
       const int64_t i = j.perm ? (int64_t)__ldg(j.perm + t) : t;
       const State s   = load_state(j.in, i);
       State o         = s;
-      double sf = 0., st;
+      double st;
       if (!ni_valid(j.g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(j.g, s.last_exited))) {
         raise_error(j.g, kErrState);
         st = 0.;
       } else {  // safeties come from multi_safety_kernel, launched before this kernel
         st = nav_step<MIXED>(j.g, d3(j.px[i], j.py[i], j.pz[i]), d3(j.dx[i], j.dy[i], j.dz[i]), j.slimit[i], s,
-                             o, false, sf, reloc != 0);
+                             o, reloc != 0);
       }
       j.step[i] = st;
       store_state(j.out, i, o);
@@ -124,8 +123,7 @@ __global__ void __launch_bounds__(128, 6) walk_kernel(GeomView g, int64_t n, dou
     int k           = 0;
     while (s.nav_ind != 0 && k < max_steps) {
       State o = s;
-      double sf;
-      const double st = nav_step<MIXED>(g, p, d, sl, s, o, false, sf, true);
+      const double st = nav_step<MIXED>(g, p, d, sl, s, o, true);
       p               = d3(p.x + st * d.x, p.y + st * d.y, p.z + st * d.z);
       s               = o;
       ++k;
@@ -137,6 +135,11 @@ __global__ void __launch_bounds__(128, 6) walk_kernel(GeomView g, int64_t n, dou
     nsteps[i] = k;
   }
 }
+
+// Safety kernels: 128-thread blocks, each thread's traversal stack and pending daughters in
+// dynamic shared memory (bvh_safety_mixed), 28 KiB per block.
+constexpr int kSafetyBlock         = 128;
+constexpr size_t kSafetySmemBytes = (size_t)kSafetySmemWords * kSafetyBlock * sizeof(uint32_t);
 
 // Safety of one track at its state's volume: VSafetyEstimatorHelper::ComputeSafety
 // (VSafetyEstimator.h:98-107), also the safety part of ComputeStepAndSafetyAndPropagatedState
@@ -158,7 +161,7 @@ __device__ __forceinline__ double track_safety(const GeomView &g, const State &s
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(256) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
+__global__ void __launch_bounds__(kSafetyBlock, 6) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
                                                      const double *__restrict__ py, const double *__restrict__ pz,
                                                      const vgn_state *__restrict__ in, double *__restrict__ safety,
                                                      const uint32_t *__restrict__ perm, int step_checks)
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(256) safety_kernel(GeomView g, int64_t n, cons
 // Persistent multi-job safety pass over the same job table and chunk space as
 // multi_step_kernel, for the jobs that asked for safeties.
 template <bool MIXED>
-__global__ void __launch_bounds__(256, 4) multi_safety_kernel(const __grid_constant__ JobTable jt,
+__global__ void __launch_bounds__(kSafetyBlock, 6) multi_safety_kernel(const __grid_constant__ JobTable jt,
                                                               uint32_t *__restrict__ queue)
 {
   const int lane = threadIdx.x & 31;
@@ -297,12 +300,12 @@ static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cud
 // relocation, which measured slower than the two passes together.
 static void launch_safety_pass(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s)
 {
-  const int block     = 256;
-  const unsigned grid = grid_for(a.n, block, a.max_blocks);
+  const unsigned grid = grid_for(a.n, dev::kSafetyBlock, a.max_blocks * (256 / dev::kSafetyBlock));
   if (mixed)
-    dev::safety_kernel<true><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety, a.perm, 1);
+    dev::safety_kernel<true><<<grid, dev::kSafetyBlock, dev::kSafetySmemBytes, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety,
+                                                                         a.perm, 1);
   else
-    dev::safety_kernel<false><<<grid, block, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety, a.perm, 1);
+    dev::safety_kernel<false><<<grid, dev::kSafetyBlock, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety, a.perm, 1);
 }
 
 cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s)
@@ -344,11 +347,11 @@ cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, i
   bool any_safety = false;
   for (int k = 0; k < jt.n_jobs; ++k) any_safety = any_safety || jt.job[k].safety != nullptr;
   if (any_safety) {  // before the step, which may overwrite the input states
-    const unsigned grid = (unsigned)(num_sms * 4);
+    const unsigned grid = (unsigned)(num_sms * 6);
     if (mixed)
-      dev::multi_safety_kernel<true><<<grid, 256, 0, s>>>(jt, queue + 1);
+      dev::multi_safety_kernel<true><<<grid, dev::kSafetyBlock, dev::kSafetySmemBytes, s>>>(jt, queue + 1);
     else
-      dev::multi_safety_kernel<false><<<grid, 256, 0, s>>>(jt, queue + 1);
+      dev::multi_safety_kernel<false><<<grid, dev::kSafetyBlock, 0, s>>>(jt, queue + 1);
   }
   if (mixed)
     launch_multi_m<true>(jt, queue, reloc, num_sms, variant, s);
@@ -373,12 +376,11 @@ cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, do
 cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
                           const vgn_state *in, double *safety, bool mixed, int max_blocks, cudaStream_t s)
 {
-  const int block     = 256;
-  const unsigned grid = grid_for(n, block, max_blocks);
+  const unsigned grid = grid_for(n, dev::kSafetyBlock, max_blocks * (256 / dev::kSafetyBlock));
   if (mixed)
-    dev::safety_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety, nullptr, 0);
+    dev::safety_kernel<true><<<grid, dev::kSafetyBlock, dev::kSafetySmemBytes, s>>>(g, n, px, py, pz, in, safety, nullptr, 0);
   else
-    dev::safety_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, in, safety, nullptr, 0);
+    dev::safety_kernel<false><<<grid, dev::kSafetyBlock, 0, s>>>(g, n, px, py, pz, in, safety, nullptr, 0);
   return cudaGetLastError();
 }
 

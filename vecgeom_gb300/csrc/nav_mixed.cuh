@@ -377,6 +377,15 @@ __device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm
   return false;
 }
 
+// A per-thread array in shared memory, strided by the block size: element i of thread t at
+// base[i * stride + t], so the threads of a warp touch consecutive banks.
+template <typename T>
+struct SArr {
+  T *p;
+  int stride;
+  __device__ __forceinline__ T &operator[](int i) const { return p[i * stride]; }
+};
+
 // ------------------------------------------------------------------ step
 constexpr int kMaxStepCand = 16;
 
@@ -487,10 +496,15 @@ struct SafeRun {
   double known;
   FI knownI;
   int n;
-  int pv[kMaxSafeCand];
-  float lo[kMaxSafeCand], hi[kMaxSafeCand];
+  SArr<int> pv;  // kMaxSafeCand pending daughters, in shared memory
+  SArr<float> lo, hi;
   FI cur;  // interval of the current running minimum
 };
+
+// Dynamic shared memory of the kernels that run bvh_safety_mixed: per thread the traversal
+// stack and the pending daughters, kSafetySmemWords words strided by the block size.
+constexpr int kSafetySmemWords = kStackSize + 3 * kMaxSafeCand;
+extern __shared__ uint32_t vgn_safety_smem[];
 
 __device__ __forceinline__ void saferun_update(SafeRun &s)
 {
@@ -533,10 +547,15 @@ __device__ __forceinline__ bool saferun_less(const GeomView &g, const MixedRay &
 __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRec &lv, const MixedRay &r,
                                                    double safety)
 {
-  unsigned stack[kStackSize];
+  const int stride = blockDim.x;
+  uint32_t *base   = vgn_safety_smem + threadIdx.x;
+  const SArr<unsigned> stack{base, stride};
   int sp   = 1;
   stack[0] = 0;
   SafeRun s;
+  s.pv     = SArr<int>{reinterpret_cast<int *>(base + kStackSize * stride), stride};
+  s.lo     = SArr<float>{reinterpret_cast<float *>(base + (kStackSize + kMaxSafeCand) * stride), stride};
+  s.hi     = SArr<float>{reinterpret_cast<float *>(base + (kStackSize + 2 * kMaxSafeCand) * stride), stride};
   s.known  = safety;
   s.knownI = fi(safety);
   s.n      = 0;

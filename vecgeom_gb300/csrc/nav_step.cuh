@@ -134,11 +134,13 @@ __device__ __forceinline__ double safety_local(const GeomView &g, const LVRec &l
   return safety;
 }
 
-// ComputeStepAndSafetyAndPropagatedState (VNavigator.h:1014-1064) with
-// PrepareOutState (VNavigator.h:192-235) and MovePointAfterBoundary (168-173).
+// ComputeStepAndPropagatedState (VNavigator.h:436-492) with PrepareOutState
+// (VNavigator.h:192-235) and MovePointAfterBoundary (168-173).  The safety of
+// ComputeStepAndSafetyAndPropagatedState (VNavigator.h:1014-1064) is taken at the
+// input state and does not affect the step: the safety pass (safety_local) computes it.
 template <bool MIXED>
 __device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, double slimit, const State &in,
-                                           State &out, bool calcsafety, double &safety, bool reloc)
+                                           State &out, bool reloc)
 {
   Xf m;
   top_matrix(g, in.nav_ind, m);
@@ -149,22 +151,11 @@ __device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, doub
   double step    = shape_dist_out(lv.shape, g.shape + lv.shape_row, lp, ld);
   if (step < 0.) step = 0.;
   int hit = -1;
-  safety  = 0.;
   if (MIXED) {
     MixedRay r;
     make_ray(r, lp, ld);
-    if (calcsafety) {
-      double s = shape_safe_out(lv.shape, g.shape + lv.shape_row, lp);
-      if (s > 0.0 && lv.nd > 0) s = bvh_safety_mixed(g, lv, r, s);
-      safety = s;
-    }
     if (lv.nd > 0) bvh_check_daughters_mixed(g, lv, r, step, ni_top(g, in.last_exited), hit);
   } else {
-    if (calcsafety) {
-      double s = shape_safe_out(lv.shape, g.shape + lv.shape_row, lp);
-      if (s > 0.0 && lv.nd > 0) s = bvh_safety(g, lv, lp, s);
-      safety = s;
-    }
     if (lv.nd > 0) bvh_check_daughters(g, lv, lp, ld, step, ni_top(g, in.last_exited), hit);
   }
 
