@@ -87,10 +87,17 @@ static inline int aabb_contains(const or_aabb *b, v3 p)
 /* ---- shape parameter structs (cached members as the reference's *Struct) ---- */
 typedef struct { double d[3]; } or_box; /* BoxStruct.h fDimensions */
 
-typedef struct { /* TubeStruct.h:15-41 (no phi wedge: full-phi tubes) */
+typedef struct { /* evolution::Wedge (Wedge_Evolution.h:43-50), source/Wedge_Evolution.cpp:17-99 */
+  double a1x, a1y, a2x, a2y; /* fAlongVector1/2 */
+  double n1x, n1y, n2x, n2y; /* fNormalVector1/2 */
+  double dphi;               /* fDPhi */
+} or_wedge;
+
+typedef struct { /* TubeStruct.h:15-41 */
   double rmin, rmax, z, sphi, dphi;
   double rmin2, rmax2, alongphi1x, alongphi1y, alongphi2x, alongphi2y;
   double tolIrmin2, tolOrmin2, tolIrmax2, tolOrmax2, tolIz, tolOz, tolIrmin, tolOrmin, tolIrmax, tolOrmax, maxval;
+  or_wedge w; /* fPhiWedge, built from the constructor's raw (dphi, sphi) */
 } or_tube;
 
 typedef struct { /* ConeStruct.h:23-77 cached members, full phi */
@@ -116,8 +123,7 @@ typedef struct { /* TrapezoidStruct.h:41-59 with the PlaneShell<4> side planes (
 
 typedef struct { /* SphereStruct.h:21-51, full phi and full theta */
   double rmin, rmax;
-  /* evolution::Wedge built from the constructor's raw (dphi, sphi) (source/Wedge_Evolution.cpp:17-99) */
-  double a1x, a1y, a2x, a2y, n1x, n1y, n2x, n2y, wdphi;
+  or_wedge w; /* evolution::Wedge built from the constructor's raw (dphi, sphi) */
   /* ThetaCone built from the raw (stheta, dtheta) (ThetaCone_Evolution.h:62-82) */
   double tsTheta, teTheta, tanSTheta, tanETheta;
 } or_sphere;

@@ -73,10 +73,72 @@ static double box_safe_out(const or_box *b, v3 p)
 }
 
 /* ================================================================== */
-/* Tube (UniversalTube, full phi): kernel/TubeImplementation.h        */
+/* evolution::Wedge: VecGeom/volumes/Wedge_Evolution.h                */
 /* ================================================================== */
 
-/* TubeStruct constructor + CalculateCached (TubeStruct.h:43-72, 153-175) */
+/* Wedge(angle, zeroangle) (source/Wedge_Evolution.cpp:17-99) */
+static void wedge_init(or_wedge *w, double dphi, double sphi)
+{
+  w->a1x  = cos(sphi);
+  w->a1y  = sin(sphi);
+  w->a2x  = cos(sphi + dphi);
+  w->a2y  = sin(sphi + dphi);
+  w->n1x  = -sin(sphi);
+  w->n1y  = cos(sphi);
+  w->n2x  = sin(sphi + dphi);
+  w->n2y  = -cos(sphi + dphi);
+  w->dphi = dphi;
+}
+
+/* Wedge::IsOnSurfaceGeneric (Wedge_Evolution.h:341-354) */
+static inline int wedge_on_surface(double ax, double ay, double nx, double ny, v3 p)
+{
+  if (!(ax * p.x + ay * p.y >= 0.)) return 0;
+  return fabs(nx * p.x + ny * p.y) < kTolerance;
+}
+
+/* Wedge::GenericKernelForContainsAndInside (Wedge_Evolution.h:306-339) */
+static void wedge_ci(const or_wedge *w, v3 p, int forInside, int *cin, int *cout)
+{
+  double startCheck = (-p.x * w->a1y + p.y * w->a1x);
+  double endCheck   = (-w->a2x * p.y + w->a2y * p.x);
+  *cout             = startCheck < 0.;
+  if (w->dphi < kPi)
+    *cout = *cout || endCheck < 0.;
+  else
+    *cout = *cout && endCheck < 0.;
+  if (forInside) {
+    int onSurface = wedge_on_surface(w->a1x, w->a1y, w->n1x, w->n1y, p) ||
+                    wedge_on_surface(w->a2x, w->a2y, w->n2x, w->n2y, p);
+    *cout = *cout && !onSurface;
+    *cin  = !onSurface && !*cout;
+  }
+}
+
+/* Wedge::Contains (Wedge_Evolution.h:296-303) */
+static inline int wedge_contains(const or_wedge *w, v3 p)
+{
+  int cin = 0, cout = 0;
+  wedge_ci(w, p, 0, &cin, &cout);
+  return !cout;
+}
+
+/* Wedge::SafetyToOut (Wedge_Evolution.h:356-372) */
+static double wedge_safe_out(const or_wedge *w, v3 p)
+{
+  double dist1 = p.x * w->n1x + p.y * w->n1y;
+  double dist2 = p.x * w->n2x + p.y * w->n2y;
+  if (w->dphi < kPi) return or_min(dist1, dist2);
+  return or_max(dist1, dist2);
+}
+
+/* ================================================================== */
+/* Tube (UniversalTube): kernel/TubeImplementation.h                  */
+/* ================================================================== */
+
+/* TubeStruct constructor + CalculateCached (TubeStruct.h:43-72, 153-175): the raw
+ * (sphi, dphi) are kept (the constructor does not call SetAndCheck*PhiAngle); the phi
+ * treatment is on when dphi < 2 pi (TubeTypes.h:91-98, UniversalTube) */
 static int tube_init(or_tube *t, const double *a, char *err, int errlen)
 {
   t->rmin = a[0] < 0.0 ? 0.0 : a[0];
@@ -84,8 +146,8 @@ static int tube_init(or_tube *t, const double *a, char *err, int errlen)
   t->z    = a[2];
   t->sphi = a[3];
   t->dphi = a[4];
-  if (t->dphi < kTwoPi) {
-    set_err(err, errlen, "tube: phi sections are not supported");
+  if (!(t->rmax > t->rmin && t->z > 0 && t->dphi > 0)) {
+    set_err(err, errlen, "tube: needs rmax > rmin, dz > 0 and dphi > 0");
     return -1;
   }
   /* UpdatedZ */
@@ -110,10 +172,24 @@ static int tube_init(or_tube *t, const double *a, char *err, int errlen)
   t->alongphi2x = cos(t->sphi + t->dphi);
   t->alongphi2y = sin(t->sphi + t->dphi);
   t->maxval     = or_max(t->rmax, t->z);
+  wedge_init(&t->w, t->dphi, t->sphi);
   return 0;
 }
 
-/* TubeUtilities::CircleTrajectoryIntersection (TubeImplementation.h:103-160), full phi */
+static inline int tube_has_phi(const or_tube *t) { return t->dphi < kTwoPi; } /* checkPhiTreatment */
+
+/* TubeUtilities::PointInCyclicalSector<..., onSurfaceT = false> (TubeImplementation.h:58-101);
+ * UniversalTube decides "smaller than pi" at run time (dphi <= M_PI) */
+static int tube_in_sector(const or_tube *t, double x, double y, int includeSurface)
+{
+  double startCheck = (-x * t->alongphi1y + y * t->alongphi1x);
+  double endCheck   = (-t->alongphi2x * y + t->alongphi2y * x);
+  double tol        = includeSurface ? -kHalfTolerance : kHalfTolerance;
+  if (t->dphi <= kPi) return (startCheck >= tol) && (endCheck >= tol);
+  return (startCheck >= tol) || (endCheck >= tol);
+}
+
+/* TubeUtilities::CircleTrajectoryIntersection (TubeImplementation.h:103-160) */
 static void tube_circle(double b, double c, const or_tube *t, v3 pos, v3 dir, int largest, int insector, double *dist,
                         int *ok)
 {
@@ -129,15 +205,59 @@ static void tube_circle(double b, double c, const or_tube *t, v3 pos, v3 dir, in
   if (insector) {
     double hitz = pos.z + *dist * dir.z;
     *ok &= (fabs(hitz) <= t->z);
+    if (!*ok) return;
+    if (tube_has_phi(t)) {
+      double hitx = pos.x + *dist * dir.x;
+      double hity = pos.y + *dist * dir.y;
+      *ok &= tube_in_sector(t, hitx, hity, 1);
+    }
   }
 }
 
-/* DistanceToInKernel (TubeImplementation.h:504-681), rmin treatment at run time */
+/* TubeUtilities::PhiPlaneTrajectoryIntersection (TubeImplementation.h:249-301) */
+static void tube_phi_plane(const or_tube *t, double alongX, double alongY, double normalX, double normalY, v3 pos,
+                           v3 dir, int posdir, int insector, double *dist, int *ok)
+{
+  double dirDotNorm = dir.x * normalX + dir.y * normalY;
+  double dirDotXY;
+  *ok      = insector ? (dirDotNorm > 0.) : (dirDotNorm < 0.);
+  dirDotXY = (dir.y * alongX - dir.x * alongY);
+  *dist    = (alongY * pos.x - alongX * pos.y) / NonZero(dirDotXY);
+  *ok &= (*dist * fabs(dirDotNorm)) > -kHalfTolerance;
+  if (insector) {
+    double hitx = pos.x + *dist * dir.x;
+    double hity = pos.y + *dist * dir.y;
+    double hitz = pos.z + *dist * dir.z;
+    double r2   = hitx * hitx + hity * hity;
+    *ok &= fabs(hitz) <= t->tolOz && (r2 >= t->tolOrmin2) && (r2 <= t->tolOrmax2);
+    if (posdir) *ok = *ok && (hitx * alongX + hity * alongY) > 0.;
+  } else if (posdir) {
+    double hitx = pos.x + *dist * dir.x;
+    double hity = pos.y + *dist * dir.y;
+    *ok         = *ok && (hitx * alongX + hity * alongY) >= 0.;
+  }
+}
+
+/* TubeUtilities::PhiPlaneSafety<inside = false> (TubeImplementation.h:210-247), UniversalTube */
+static double tube_phi_safety(const or_tube *t, v3 pos)
+{
+  double safety = t->dphi > kPi ? sqrt(pos.x * pos.x + pos.y * pos.y) : kInfLength;
+  double phi1   = pos.x * t->alongphi1y - pos.y * t->alongphi1x; /* PerpDist2D */
+  double phi2;
+  if (phi1 > -kHalfTolerance && phi1 < safety) safety = phi1;
+  phi2 = pos.x * t->alongphi2y - pos.y * t->alongphi2x;
+  phi2 *= -1;
+  if (phi2 > -kHalfTolerance && phi2 < safety) safety = phi2;
+  return safety;
+}
+
+/* DistanceToInKernel (TubeImplementation.h:504-681), rmin and phi treatment at run time */
 static double tube_dist_in_kernel(const or_tube *t, v3 p, v3 d)
 {
-  int done = 0, inside, okz, onsurf, ok_rmax, ok_rmin;
-  double distance = kInfLength, distz, rsq, rdotn, hitx, hity, r2, invnsq, b, crmax, dist_rmax, dist_rmin;
+  int done = 0, inside, okz, onsurf, ok_rmax, ok_rmin, ok_phi;
+  double distance = kInfLength, distz, rsq, rdotn, hitx, hity, r2, invnsq, b, crmax, dist_rmax, dist_rmin, dist_phi;
   const int hasrmin = t->rmin > 0;
+  const int hasphi  = tube_has_phi(t);
 
   distz = fabs(p.z) - t->z;
   done |= distz > kHalfTolerance && p.z * d.z >= 0;
@@ -150,6 +270,7 @@ static double tube_dist_in_kernel(const or_tube *t, v3 p, v3 d)
   inside   = distz < -kHalfTolerance;
   inside &= rsq < t->tolIrmax2;
   if (hasrmin) inside &= rsq > t->tolIrmin2;
+  if (hasphi && inside) inside &= tube_in_sector(t, p.x, p.y, 0);
   done |= inside;
   if (done) return distance;
 
@@ -161,11 +282,12 @@ static double tube_dist_in_kernel(const or_tube *t, v3 p, v3 d)
   okz  = distz > -kHalfTolerance && (p.z * d.z < 0);
   okz &= (r2 <= t->rmax2);
   if (hasrmin) okz &= (t->rmin2 <= r2);
+  if (hasphi && okz) okz &= tube_in_sector(t, hitx, hity, 1);
   if (!done && okz) distance = distz;
   done |= okz;
 
   {
-    /* IsMovingInsideTubeSurface (TubeImplementation.h:399-435) */
+    /* IsMovingInsideTubeSurface (TubeImplementation.h:317-343) */
     const double rho = p.x * p.x + p.y * p.y;
     onsurf = (rho >= t->tolIrmax2) && (rho <= t->tolOrmax2) && (fabs(p.z) < (t->z + kTolerance)) &&
              (d.x * p.x + d.y * p.y + d.z * 0. <= 0.);
@@ -173,6 +295,7 @@ static double tube_dist_in_kernel(const or_tube *t, v3 p, v3 d)
       onsurf |= (rho >= t->tolOrmin2) && (rho <= t->tolIrmin2) && (fabs(p.z) < (t->z + kTolerance)) &&
                 (d.x * -p.x + d.y * -p.y + d.z * 0. <= 0.);
   }
+  if (hasphi) onsurf = onsurf && tube_in_sector(t, p.x, p.y, 1);
   if (!done && onsurf) distance = 0.;
   done |= onsurf;
   if (done) return distance;
@@ -191,6 +314,15 @@ static double tube_dist_in_kernel(const or_tube *t, v3 p, v3 d)
     tube_circle(b, crmin, t, p, d, 1, 1, &dist_rmin, &ok_rmin);
     ok_rmin &= dist_rmin < distance;
     if (!done && ok_rmin) distance = dist_rmin;
+  }
+
+  if (hasphi) { /* SectorType of UniversalTube is unknown: both planes, positive-direction check */
+    tube_phi_plane(t, t->alongphi1x, t->alongphi1y, t->w.n1x, t->w.n1y, p, d, 1, 1, &dist_phi, &ok_phi);
+    ok_phi &= dist_phi < distance;
+    if (!done && ok_phi) distance = dist_phi;
+    done |= ok_phi;
+    tube_phi_plane(t, t->alongphi2x, t->alongphi2y, t->w.n2x, t->w.n2y, p, d, 1, 1, &dist_phi, &ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
   }
   return distance;
 }
@@ -214,9 +346,10 @@ static double tube_dist_in(const or_tube *t, v3 pt, v3 d)
 /* DistanceToOut (TubeImplementation.h:683-823) */
 static double tube_dist_out(const or_tube *t, v3 p, v3 d)
 {
-  int done = 0, ok_rmin, ok_rmax;
-  double distance = -1., distz, rsq, rdotn, crmax, crmin, invdirz, invnsq, b, dist_rmin, dist_rmax;
+  int done = 0, ok_rmin, ok_rmax, ok_phi;
+  double distance = -1., distz, rsq, rdotn, crmax, crmin, invdirz, invnsq, b, dist_rmin, dist_rmax, dist_phi;
   const int hasrmin = t->rmin > 0;
+  const int hasphi  = tube_has_phi(t);
 
   distz = t->z - fabs(p.z);
   done |= distz < -kHalfTolerance;
@@ -230,6 +363,12 @@ static double tube_dist_out(const or_tube *t, v3 p, v3 d)
   if (hasrmin) {
     crmin -= t->rmin2;
     done |= crmin < -2.0 * kTolerance * t->rmin;
+    if (done) return distance;
+  }
+  if (hasphi) {
+    int cin = 0, cout = 0;
+    wedge_ci(&t->w, p, 1, &cin, &cout);
+    done |= cout;
     if (done) return distance;
   }
   distance = kInfLength;
@@ -248,10 +387,17 @@ static double tube_dist_out(const or_tube *t, v3 p, v3 d)
   crmax *= invnsq;
   tube_circle(b, crmax, t, p, d, 1, 0, &dist_rmax, &ok_rmax);
   if (ok_rmax && dist_rmax < distance) distance = dist_rmax;
+
+  if (hasphi) { /* angle bigger than pi or unknown: positive-direction check on both planes */
+    tube_phi_plane(t, t->alongphi1x, t->alongphi1y, t->w.n1x, t->w.n1y, p, d, 1, 0, &dist_phi, &ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    tube_phi_plane(t, t->alongphi2x, t->alongphi2y, t->w.n2x, t->w.n2y, p, d, 1, 0, &dist_phi, &ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
+  }
   return distance;
 }
 
-/* SafetyToInOld (TubeImplementation.h:912-938) */
+/* SafetyToInOld (TubeImplementation.h:912-938; TUBE_SAFETY_OLD is defined at line 14) */
 static double tube_safe_in(const or_tube *t, v3 p)
 {
   double safety = fabs(p.z) - t->z;
@@ -262,10 +408,17 @@ static double tube_safe_in(const or_tube *t, v3 p)
     double safermin = t->rmin - r;
     if (safermin > safety) safety = safermin;
   }
+  if (tube_has_phi(t)) {
+    int insector = tube_in_sector(t, p.x, p.y, 0);
+    double safephi;
+    if (insector) return safety;
+    safephi = tube_phi_safety(t, p);
+    if (!insector && safephi < kInfLength && safephi > safety) safety = safephi;
+  }
   return safety;
 }
 
-/* SafetyToOutOld (TubeImplementation.h:940-960) */
+/* SafetyToOutOld (TubeImplementation.h:940-966) */
 static double tube_safe_out(const or_tube *t, v3 p)
 {
   double safety = t->z - fabs(p.z);
@@ -275,6 +428,10 @@ static double tube_safe_out(const or_tube *t, v3 p)
   if (t->rmin > 0) {
     double safermin = r - t->rmin;
     if (safermin < safety) safety = safermin;
+  }
+  if (tube_has_phi(t)) {
+    double safephi = wedge_safe_out(&t->w, p);
+    if (safephi < safety) safety = safephi;
   }
   return safety;
 }
@@ -294,6 +451,13 @@ static void tube_generic_ci(const or_tube *t, v3 p, int forinside, int *cin, int
   if (t->rmin > 0) {
     *cout |= r2 <= (forinside ? fabs(t->rmin * (t->rmin - 2.0 * kTolerance)) : t->rmin * t->rmin);
     if (forinside) *cin &= r2 > t->rmin * (t->rmin + 2.0 * kTolerance);
+    if (*cout) return;
+  }
+  if (tube_has_phi(t)) {
+    int cinphi = 0, coutphi = 0;
+    wedge_ci(&t->w, p, forinside, &cinphi, &coutphi);
+    *cout |= coutphi;
+    if (forinside) *cin &= cinphi;
   }
 }
 
@@ -313,11 +477,41 @@ static int tube_inside(const or_tube *t, v3 p)
   return r;
 }
 
-/* UnplacedTube::Extent (source/UnplacedTube.cpp:214-220), full phi */
+/* UnplacedTube::Extent (source/UnplacedTube.cpp:214-266) */
 static void tube_extent(const or_tube *t, v3 *mn, v3 *mx)
 {
+  double Rin, Cx, Dx, Cy, Dy, Ax, Bx, Ay, By, temp;
+  int phi0out, phi90out, phi180out, phi270out;
   *mn = v3_make(-t->rmax, -t->rmax, -t->z);
   *mx = v3_make(t->rmax, t->rmax, t->z);
+  if (t->dphi == kTwoPi) return;
+  Rin       = 0.5 * (t->rmax + t->rmin);
+  phi0out   = !wedge_contains(&t->w, v3_make(Rin, 0, 0));
+  phi90out  = !wedge_contains(&t->w, v3_make(0, Rin, 0));
+  phi180out = !wedge_contains(&t->w, v3_make(-Rin, 0, 0));
+  phi270out = !wedge_contains(&t->w, v3_make(0, -Rin, 0));
+  if (!(phi0out || phi90out || phi180out || phi270out)) return;
+  Cx = t->rmax * cos(t->sphi);
+  Dx = t->rmax * cos(t->sphi + t->dphi);
+  Cy = t->rmax * sin(t->sphi);
+  Dy = t->rmax * sin(t->sphi + t->dphi);
+  if (phi0out) mx->x = or_max(Cx, Dx);
+  if (phi90out) mx->y = or_max(Cy, Dy);
+  if (phi180out) mn->x = or_min(Cx, Dx);
+  if (phi270out) mn->y = or_min(Cy, Dy);
+  if (t->dphi >= kPi) return;
+  Ax = t->rmin * cos(t->sphi);
+  Bx = t->rmin * cos(t->sphi + t->dphi);
+  Ay = t->rmin * sin(t->sphi);
+  By = t->rmin * sin(t->sphi + t->dphi);
+  temp  = or_max(Ax, Bx);
+  mx->x = temp > mx->x ? temp : mx->x;
+  temp  = or_max(Ay, By);
+  mx->y = temp > mx->y ? temp : mx->y;
+  temp  = or_min(Ax, Bx);
+  mn->x = temp < mn->x ? temp : mn->x;
+  temp  = or_min(Ay, By);
+  mn->y = temp < mn->y ? temp : mn->y;
 }
 
 /* ================================================================== */
@@ -1188,15 +1382,7 @@ static int sphere_init(or_sphere *t, const double *a, char *err, int errlen)
   }
   t->rmin  = rmin;
   t->rmax  = rmax;
-  t->a1x   = cos(sphi);
-  t->a1y   = sin(sphi);
-  t->a2x   = cos(sphi + dphi);
-  t->a2y   = sin(sphi + dphi);
-  t->n1x   = -sin(sphi);
-  t->n1y   = cos(sphi);
-  t->n2x   = sin(sphi + dphi);
-  t->n2y   = -cos(sphi + dphi);
-  t->wdphi = dphi;
+  wedge_init(&t->w, dphi, sphi);
   t->tsTheta = stheta;
   t->teTheta = stheta + dtheta;
   double ts = t->tsTheta, te = t->teTheta;
@@ -1209,38 +1395,6 @@ static int sphere_init(or_sphere *t, const double *a, char *err, int errlen)
 
 #define kThetaHalfPi (0.5 * kPi) /* ThetaCone_Evolution.h:13 */
 #define kThetaTol 1e-9           /* ThetaCone::kAngTolerance = kTolerance */
-
-/* Wedge::IsOnSurfaceGeneric (Wedge_Evolution.h:341-354) */
-static inline int wedge_on_surface(double ax, double ay, double nx, double ny, v3 p)
-{
-  if (!(ax * p.x + ay * p.y >= 0.)) return 0;
-  return fabs(nx * p.x + ny * p.y) < kTolerance;
-}
-
-/* Wedge::GenericKernelForContainsAndInside (Wedge_Evolution.h:306-339) */
-static void wedge_ci(const or_sphere *t, v3 p, int forInside, int *cin, int *cout)
-{
-  double startCheck = (-p.x * t->a1y + p.y * t->a1x);
-  double endCheck   = (-t->a2x * p.y + t->a2y * p.x);
-  *cout             = startCheck < 0.;
-  if (t->wdphi < kPi)
-    *cout = *cout || endCheck < 0.;
-  else
-    *cout = *cout && endCheck < 0.;
-  if (forInside) {
-    int onSurface = wedge_on_surface(t->a1x, t->a1y, t->n1x, t->n1y, p) ||
-                    wedge_on_surface(t->a2x, t->a2y, t->n2x, t->n2y, p);
-    *cout = *cout && !onSurface;
-    *cin  = !onSurface && !*cout;
-  }
-}
-
-static inline int wedge_contains(const or_sphere *t, v3 p)
-{
-  int cin = 0, cout = 0;
-  wedge_ci(t, p, 0, &cin, &cout);
-  return !cout;
-}
 
 /* ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730) for stheta = 0, etheta >= pi */
 static int theta_completely_inside(const or_sphere *t, v3 p)
@@ -1284,7 +1438,7 @@ static int sphere_completely_inside(const or_sphere *t, v3 p)
   double rad = sqrt(v3_dot(p, p));
   int inRad  = (rad < (t->rmax - kTolerance)) && (rad > (t->rmin + kTolerance));
   int cin = 0, cout = 0;
-  wedge_ci(t, p, 1, &cin, &cout);
+  wedge_ci(&t->w, p, 1, &cin, &cout);
   int inTheta = theta_completely_inside(t, p);
   return inRad && cin && inTheta;
 }
@@ -1294,7 +1448,7 @@ static int sphere_completely_outside(const or_sphere *t, v3 p)
   double rad = sqrt(v3_dot(p, p));
   int outRad = (rad > (t->rmax + kTolerance)) || (rad < (t->rmin - kTolerance));
   int cin = 0, cout = 0;
-  wedge_ci(t, p, 1, &cin, &cout);
+  wedge_ci(&t->w, p, 1, &cin, &cout);
   int outTheta = theta_completely_outside(t, p);
   return outRad || cout || outTheta;
 }
@@ -1314,7 +1468,7 @@ static int sphere_on_surface_moving(const or_sphere *t, v3 p, v3 d, int movingOu
     double dmp  = d.x * -p.x + d.y * -p.y + d.z * -p.z;
     inner       = onInner && (movingOut ? dmp > kSqrtTolerance : dmp < -kSqrtTolerance);
   }
-  return (outer || inner) && wedge_contains(t, p) && !theta_completely_outside(t, p);
+  return (outer || inner) && wedge_contains(&t->w, p) && !theta_completely_outside(t, p);
 }
 
 /* SphereImplementation::GenericKernelForContainsAndInside (SphereImplementation.h:89-136) */

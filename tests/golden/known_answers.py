@@ -167,27 +167,27 @@ TWO_PI = 2 * KPI
 T1 = (0.0, 50.0, 50.0, 0.0, TWO_PI)      # TestTube.cpp:52
 T2 = (45.0, 50.0, 50.0, 0.0, TWO_PI)     # TestTube.cpp:54
 T2A = (5.0, 50.0, 50.0, 0.0, TWO_PI)     # TestTube.cpp:55
-TUBE8 = (2550.0, 2580.0, 2000.0, 0.0, TWO_PI)   # TestTube.cpp:66
-TUBE9 = (1150.0, 1180.0, 2000.0, 0.0, TWO_PI)   # TestTube.cpp:67
-TUBE10 = (400.0, 405.0, 400.0, 0.0, TWO_PI)     # TestTube.cpp:68
+TUBE8 = (2550.0, 2580.0, 2000.0, 0.0, TWO_PI)   # TestTube.cpp:65
+TUBE9 = (1150.0, 1180.0, 2000.0, 0.0, TWO_PI)   # TestTube.cpp:66
+TUBE10 = (400.0, 405.0, 400.0, 0.0, TWO_PI)     # TestTube.cpp:67
 
 TUBE_CASES = [
     _case(f"{T}:120", TUBE, T1, "dist_out", (44.991, 21.816, 4.677), _unit((0.16636, 0.64765, -0.74356)), 0.0, "lt0"),
-    _case(f"{T}:152", TUBE, T1, "inside", pzero, None, 1, "eq"),
-    _case(f"{T}:153", TUBE, T1, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
-    _case(f"{T}:154", TUBE, T1, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
-    _case(f"{T}:155", TUBE, T1, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
-    _case(f"{T}:156", TUBE, T1, "inside", (0.0, 0.0, 50.0), None, 2, "eq"),
-    _case(f"{T}:164", TUBE, T2, "inside", pzero, None, 3, "eq"),
-    _case(f"{T}:165", TUBE, T2, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
-    _case(f"{T}:166", TUBE, T2, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
-    _case(f"{T}:167", TUBE, T2, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
-    _case(f"{T}:168", TUBE, T2, "inside", (0.0, 0.0, 50.0), None, 3, "eq"),
-    _case(f"{T}:170", TUBE, T2A, "inside", pzero, None, 3, "eq"),
-    _case(f"{T}:171", TUBE, T2A, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
-    _case(f"{T}:172", TUBE, T2A, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
-    _case(f"{T}:173", TUBE, T2A, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
-    _case(f"{T}:174", TUBE, T2A, "inside", (0.0, 0.0, 50.0), None, 3, "eq"),
+    _case(f"{T}:134", TUBE, T1, "inside", pzero, None, 1, "eq"),
+    _case(f"{T}:135", TUBE, T1, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:136", TUBE, T1, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:137", TUBE, T1, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:138", TUBE, T1, "inside", (0.0, 0.0, 50.0), None, 2, "eq"),
+    _case(f"{T}:144", TUBE, T2, "inside", pzero, None, 3, "eq"),
+    _case(f"{T}:145", TUBE, T2, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:146", TUBE, T2, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:147", TUBE, T2, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:148", TUBE, T2, "inside", (0.0, 0.0, 50.0), None, 3, "eq"),
+    _case(f"{T}:149", TUBE, T2A, "inside", pzero, None, 3, "eq"),
+    _case(f"{T}:150", TUBE, T2A, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:151", TUBE, T2A, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:152", TUBE, T2A, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:153", TUBE, T2A, "inside", (0.0, 0.0, 50.0), None, 3, "eq"),
     _case(f"{T}:179", TUBE, T1, "safe_out", pzero, None, 50.0),
     _case(f"{T}:183", TUBE, T1, "dist_out", pzero, vx, 50.0),
     _case(f"{T}:187", TUBE, T1, "dist_out", pzero, vmx, 50.0),
@@ -209,8 +209,8 @@ TUBE_CASES = [
     _case(f"{T}:289", TUBE, T1, "dist_in", (0.0, 0.0, 100.0), vmz, 50.0),
     _case(f"{T}:291", TUBE, T1, "dist_in", (0.0, 0.0, -100.0), vz, 50.0),
     _case(f"{T}:293", TUBE, T1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
-    _case(f"{T}:396", TUBE, T1, "inside", pzero, None, 1, "eq"),
-    _case(f"{T}:397", TUBE, T1, "inside", (100.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{T}:392", TUBE, T1, "inside", pzero, None, 1, "eq"),
+    _case(f"{T}:393", TUBE, T1, "inside", (100.0, 0.0, 0.0), None, 3, "eq"),
     _case(f"{T}:399", TUBE, TUBE10, "inside", (-114.8213313833317, 382.7843220719649, -32.20788536438663), None, 3,
           "eq"),
     _case(f"{T}:414", TUBE, TUBE8, "dist_out", (6.71645645882942, 2579.415860329989, -1.519530725281157),
@@ -218,6 +218,89 @@ TUBE_CASES = [
     _case(f"{T}:418", TUBE, TUBE9, "dist_out", (2.267347771505638, 1170.164934028592, 4.820317321984064),
           (-0.1443054266272111, -0.01508874701037938, 0.9894181489944458), 2016.51817758),
 ]
+
+# phi sections (TestTube.cpp:53-70): (rmin, rmax, dz, sphi, dphi)
+T1A = (0.0, 50.0, 50.0, 0.0, 0.5 * KPI)
+T3 = (0.0, 50.0, 50.0, 0.5 * KPI, 0.5 * KPI)
+T5 = (50.0, 100.0, 50.0, 0.0, 1.5 * KPI)
+TUBE6 = (750.0, 760.0, 350.0, 0.31415926535897931, 5.6548667764616276)
+TUBE7 = (2200.0, 3200.0, 2500.0, -0.68977164349384879, 3.831364227270472)
+CLAD = (90.0, 110.0, 105.0, 0.0, KPI)   # TestTube.cpp:68
+CORE = (95.0, 105.0, 100.0, 0.0, KPI)   # TestTube.cpp:69
+ARC = (1000.0, 1100.0, 10.0, -KPI / 12.0, KPI / 6.0)  # TestTube.cpp:364
+T4SN = (45.0, 50.0, 50.0, KPI / 4.0, KPI / 8.0)      # TestTube.cpp:476
+DEG = KPI / 180.0
+JIRA174 = (57.555599999999998, 205.55599999999998, 348.0, -5.5747247 * DEG, 5.5747247 * DEG)  # TestTube.cpp:81-82
+
+
+def _jira174():
+    """jira174Tube (TestTube.cpp:80-106): a point 5e-15 beyond the phi = 0 plane, entering and leaving."""
+    d = (0.303163, -0.492481, 0.815815)
+    m = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+    d = (d[0] / m, d[1] / m, d[2] / m)  # dir174 /= dir174.Mag()
+    p = (92.4733, 5.32907e-15, 19.943)
+    q = (92.4733, -5.32907e-15, 19.943)
+    md = (-d[0], -d[1], -d[2])
+    return [_case(f"{T}:91", TUBE, JIRA174, "dist_in", p, d, 0.0),
+            _case(f"{T}:93", TUBE, JIRA174, "dist_out", p, d, 19.499),
+            _case(f"{T}:100", TUBE, JIRA174, "dist_in", q, md, INF, "inf"),
+            _case(f"{T}:104", TUBE, JIRA174, "dist_out", q, md, 0.0)]
+
+
+_arc1 = (1050 * math.cos(-KPI / 12.0), 1050 * math.sin(-KPI / 12.0), 0.0)
+TUBE_PHI_CASES = _jira174() + [
+    _case(f"{T}:129", TUBE, T5, "dist_in", (60.0, -60.0, 10.0), _unit((-1.0, 1.0, 0.001)), 134.8528474556),
+    _case(f"{T}:139", TUBE, T1A, "inside", pzero, None, 2, "eq"),
+    _case(f"{T}:140", TUBE, T1A, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{T}:141", TUBE, T1A, "inside", (50.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:142", TUBE, T1A, "inside", (0.0, 50.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:143", TUBE, T1A, "inside", (0.0, 0.0, 50.0), None, 2, "eq"),
+    _case(f"{T}:238", TUBE, T3, "dist_out", (0.0, 10.0, 0.0), vx, 0.0),
+    _case(f"{T}:242", TUBE, T3, "dist_out", (0.5, 10.0, 0.0), vx, 0.0, "lt0"),
+    _case(f"{T}:243", TUBE, T3, "inside", (0.5, 10.0, 0.0), None, 3, "eq"),
+    _case(f"{T}:248", TUBE, T3, "dist_out", (-0.5, 9.0, 0.0), vx, 0.5),
+    _case(f"{T}:252", TUBE, T3, "dist_out", (-5.0, 9.5, 0.0), vx, 5.0),
+    _case(f"{T}:256", TUBE, T3, "dist_out", (-5.0, 9.5, 0.0), vmy, 9.5),
+    _case(f"{T}:260", TUBE, T3, "dist_out", (-5.0, 9.0, 0.0), vxmy, 7.0710678),
+    _case(f"{T}:296", TUBE, T1A, "dist_in", (0.0, 0.0, 100.0), vmz, 50.0),
+    _case(f"{T}:314", TUBE, T3, "dist_in", (49.5, 5.0, 0.0), vmx, 49.5),
+    _case(f"{T}:318", TUBE, T3, "dist_in", (49.5, -0.5, 0.0), vmx, INF, "inf"),
+    _case(f"{T}:322", TUBE, T5, "dist_in", (30.0, -20.0, 0.0), vxy, 28.284271),
+    _case(f"{T}:327", TUBE, T5, "dist_in", (30.0, -70.0, 0.0), vxy, 70.0 * math.sqrt(2.0), "inf_or"),
+    _case(f"{T}:331", TUBE, T5, "dist_in", (30.0, -20.0, 0.0), vmxmy, 42.426407),
+    _case(f"{T}:336", TUBE, T5, "dist_in", (30.0, -70.0, 0.0), vmxmy, 30.0 * math.sqrt(2.0), "inf_or"),
+    _case(f"{T}:340", TUBE, T5, "dist_in", (50.0, -20.0, 0.0), vy, 20.0),
+    _case(f"{T}:345", TUBE, T5, "dist_in", (100.0, -20.0, 0.0), vy, 20.0, "inf_or"),
+    _case(f"{T}:349", TUBE, T5, "dist_in", (30.0, -50.0, 0.0), vmx, 30.0),
+    _case(f"{T}:354", TUBE, T5, "dist_in", (30.0, -100.0, 0.0), vmx, 30.0, "inf_or"),
+    _case(f"{T}:386", TUBE, ARC, "inside", _arc1, None, 2, "eq"),
+    _case(f"{T}:388", TUBE, ARC, "inside", (_arc1[0], _arc1[1] + 0.001 * 1e-9, 0.0), None, 2, "eq"),
+    _case(f"{T}:390", TUBE, ARC, "inside", (_arc1[0], _arc1[1] - 0.001 * 1e-9, 0.0), None, 2, "eq"),
+    _case(f"{T}:396", TUBE, T5, "inside", (60.0, -0.001 * 1e-9, 0.0), None, 2, "eq"),
+    _case(f"{T}:404", TUBE, TUBE6, "dist_out", (-388.20504321896431, -641.71398957741451, 332.85995254027955),
+          (-0.47312863350457468, -0.782046391443315, 0.40565100491504164), 10.940583),
+    _case(f"{T}:410", TUBE, TUBE7, "dist_out", (-2460.0, 1030.0, -2500.0),
+          (-0.086580540180167642, 0.070084247882560638, 0.9937766390194761), 4950.348576972614),
+    _case(f"{T}:422", TUBE, T1A, "dist_out", (0.0, 0.0, 50.0), vx, 50.0),
+    _case(f"{T}:426", TUBE, T1A, "dist_out", (0.0, 5.0, 50.0), vmy, 5.0),
+    # TestTube.cpp:434-473: a point walked along +y through the clad and core half tubes; the
+    # reference asserts the Inside states at the points reached (distances 90, 5, 10, 5)
+    _case(f"{T}:436", TUBE, CLAD, "dist_in", pzero, vy, 90.0),
+    _case(f"{T}:440", TUBE, CORE, "inside", (0.0, 90.0, 0.0), None, 3, "eq"),
+    _case(f"{T}:444", TUBE, CLAD, "inside", (0.0, 90.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:446", TUBE, CORE, "dist_in", (0.0, 90.0, 0.0), vy, 5.0),
+    _case(f"{T}:450", TUBE, CORE, "inside", (0.0, 95.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:453", TUBE, CLAD, "inside", (0.0, 95.0, 0.0), None, 1, "eq"),
+    _case(f"{T}:455", TUBE, CORE, "dist_out", (0.0, 95.0, 0.0), vy, 10.0),
+    _case(f"{T}:459", TUBE, CORE, "inside", (0.0, 105.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:462", TUBE, CLAD, "inside", (0.0, 105.0, 0.0), None, 1, "eq"),
+    _case(f"{T}:465", TUBE, CLAD, "dist_out", (0.0, 105.0, 0.0), vy, 5.0),
+    _case(f"{T}:469", TUBE, CORE, "inside", (0.0, 110.0, 0.0), None, 3, "eq"),
+    _case(f"{T}:472", TUBE, CLAD, "inside", (0.0, 110.0, 0.0), None, 2, "eq"),
+    _case(f"{T}:478", TUBE, T4SN, "inside", (33.315052227388207, 37.284142675357259, 33.366096020078537), None, 2,
+          "eq"),
+]
+TUBE_CASES += TUBE_PHI_CASES
 
 CONE = 2
 C = "test/unit_tests/TestCons.cpp"
@@ -727,6 +810,8 @@ def check(case, value) -> bool:
         return value >= 0.0
     if c == "inf":
         return value >= INF
+    if c == "inf_or":  # ApproxEqual(value, kInfLength) || ApproxEqual(value, expect)
+        return approx_equal(value, INF) or approx_equal(value, case["expect"])
     if c == "eq":
         return value == case["expect"]
     if c == "near":  # |value - expect| < 1000 kTolerance (TestPolycone.cpp:101-102, 113)

@@ -267,6 +267,10 @@ def test_autotune_then_step(oracle, vgnav, cuda, mixed):
 
 SHAPE_SETS = [
     ("tube-solid", W.TUBE, (0.0, 30.0, 40.0, 0.0, W.K_TWO_PI)),
+    ("tube-quarter-sector", W.TUBE, (10.0, 50.0, 40.0, 0.5 * W.K_PI, 0.5 * W.K_PI)),
+    ("tube-large-sector", W.TUBE, (20.0, 60.0, 40.0, 0.3, 1.5 * W.K_PI)),
+    ("tube-half-solid", W.TUBE, (0.0, 50.0, 30.0, 0.0, W.K_PI)),
+    ("tube-thin-sector-negative-start", W.TUBE, KA.JIRA174),
     ("cone-hollow", W.CONE, (10.0, 50.0, 20.0, 40.0, 60.0, 0.0, W.K_TWO_PI)),
     ("cone-solid-apex", W.CONE, (0.0, 30.0, 0.0, 0.0, 25.0, 0.0, W.K_TWO_PI)),
     ("cone-inverted", W.CONE, (5.0, 10.0, 20.0, 45.0, 30.0, 0.0, W.K_TWO_PI)),
@@ -326,11 +330,13 @@ def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda)
     assert np.mean(ins == 2.0) > 0.5
 
 
+@pytest.mark.parametrize("sections", [False, True], ids=["full", "tube-phi-sections"])
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
-def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed):
-    """8192 daughters of every implemented shape type, full rotations: locate, one step with
-    safety, then every step of a track subset to the world exit, all equal to the oracle."""
-    desc = W.mixed_shape_geometry()
+def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
+    """8192 daughters of every implemented shape type, full rotations (with `sections`, most
+    tubes are phi sections): locate, one step with safety, then every step of a track subset
+    to the world exit, all equal to the oracle."""
+    desc = W.mixed_shape_geometry(sections=sections)
     og = oracle.OracleGeometry(desc)
     geo = vgnav.Geometry(desc)
     t = W.mixed_shape_tracks(1 << 16)

@@ -18,6 +18,7 @@ def geometries():
         "single_tube": W.tube_geometry(),
         "box_grid_small": W.box_grid_geometry(seed=7, n=5).desc,
         "mixed_shapes_8192": W.mixed_shape_geometry(),
+        "mixed_shapes_tube_sections": W.mixed_shape_geometry(seed=31, grid=(8, 8, 8), sections=True),
     }
 
 
@@ -58,6 +59,11 @@ def test_bvh_depth_rule(oracle):
     # TestTrd.cpp:405-416
     (W.TRD, (20.0, 20.0, 30.0, 30.0, 40.0), (-20.0, -30.0, -40.0), (20.0, 30.0, 40.0)),
     (W.TRD, (10.0, 30.0, 20.0, 40.0, 40.0), (-30.0, -40.0, -40.0), (30.0, 40.0, 40.0)),
+    # UnplacedTube::Extent of phi sections (source/UnplacedTube.cpp:214-266): the box shrinks on
+    # the sides whose axis direction the sector does not contain (TestTube.cpp t3, clad, t5)
+    (W.TUBE, (0.0, 50.0, 50.0, 0.5 * W.K_PI, 0.5 * W.K_PI), (-50.0, 0.0, -50.0), (0.0, 50.0, 50.0)),
+    (W.TUBE, (90.0, 110.0, 105.0, 0.0, W.K_PI), (-110.0, 0.0, -105.0), (110.0, 110.0, 105.0)),
+    (W.TUBE, (50.0, 100.0, 50.0, 0.0, 1.5 * W.K_PI), (-100.0, -100.0, -50.0), (100.0, 100.0, 50.0)),
     # TestSphere.cpp:63-68 (b1: rmax 3)
     (W.SPHERE, (0.0, 3.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI), (-3.0, -3.0, -3.0), (3.0, 3.0, 3.0)),
     # TestPolycone.cpp:329-333 ("SimpleTube+Cone")
@@ -84,12 +90,12 @@ def test_shape_extent(oracle, vgnav, shape, params, lo, hi):
 def test_invalid_descriptions_rejected(vgnav):
     from vecgeom_gb300 import _native as N
 
-    b = W.GeometryBuilder()
-    lv = b.logical(W.TUBE, (10.0, 50.0, 100.0, 0.0, 1.0))  # phi section: not supported
-    b.place_world(lv)
-    with pytest.raises(N.VgnError) as e:
-        HostTables(b.build())
-    assert e.value.code == N.VGN_ERR_UNSUPPORTED
+    for params in ((10.0, 50.0, 100.0, 0.0, 0.0), (50.0, 10.0, 100.0, 0.0, 1.0)):  # dphi <= 0, rmin > rmax
+        b = W.GeometryBuilder()
+        b.place_world(b.logical(W.TUBE, params))
+        with pytest.raises(N.VgnError) as e:
+            HostTables(b.build())
+        assert e.value.code == N.VGN_ERR_ARG
     for shape, params in ((W.SPHERE, (0.0, 10.0, 0.0, 1.0, 0.0, W.K_PI)),   # phi section
                           (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0)),  # theta section
                           (W.POLYCONE, (0.0, 1.0, 2.0, -1.0, 1.0, 0.0, 0.0, 5.0, 5.0))):  # phi section

@@ -140,9 +140,12 @@ enum { SphHasRmin = 0, SphRmin, SphRmax, SphMsqMax, SphPsqMax, SphPsqMin, SphMsq
 namespace row {
 // Box: BoxStruct::fDimensions
 constexpr int kBoxSize = 4;
-// Tube (full phi): TubeStruct cached members
+// Tube: TubeStruct cached members, then its phi wedge as a Wedge block (the along vectors
+// are both TubeStruct::fAlongPhi* and the wedge's; the block's last entry is fDphi)
 enum { TubeRmin = 0, TubeRmax, TubeZ, TubeRmin2, TubeRmax2, TubeTolIrmin2, TubeTolOrmin2, TubeTolIrmax2,
-       TubeTolOrmax2, TubeMaxVal, kTubeSize };
+       TubeTolOrmax2, TubeMaxVal, TubeSphi, TubeTolOz, TubeWedge, TubeDphi = TubeWedge + 8, kTubeSize };
+// Wedge block (evolution::Wedge): along vectors, normal vectors, fDPhi
+enum { WedgeA1x = 0, WedgeA1y, WedgeA2x, WedgeA2y, WedgeN1x, WedgeN1y, WedgeN2x, WedgeN2y, WedgeDPhi, kWedgeSize };
 // Cone (full phi): ConeStruct cached members
 enum { ConeRmin1 = 0, ConeRmax1, ConeRmin2, ConeRmax2, ConeDz, ConeOrigRmax1, ConeOrigRmax2, ConeInnerSlope,
        ConeOuterSlope, ConeInnerOffset, ConeOuterOffset, ConeInnerTol, ConeOuterTol, ConeSqRmin1, ConeSqRmin2,

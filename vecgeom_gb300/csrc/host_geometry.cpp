@@ -498,7 +498,8 @@ static int build_isin_row(int shape, const double *r, std::vector<float> &out)
   constexpr double kTolerance = 1e-9, kConeTolerance = 1e-7;  // base/Math.h, ConeStruct
   std::vector<double> v;
   switch (shape) {
-  case kTube:  // TubeImplementation.h:912-938
+  case kTube:  // TubeImplementation.h:912-938; a phi section is evaluated in FP64
+    if (r[row::TubeDphi] < 2. * 3.14159265358979323846) return -1;
     v = {r[row::TubeZ], r[row::TubeRmax], r[row::TubeRmin], r[row::TubeRmin] > 0 ? 1. : 0.};
     break;
   case kCone: {  // ConeImplementation.h:368-432, ConeUtilities.h cone radius / safety to the conical surface

@@ -19,6 +19,35 @@ static constexpr double kAngTolerance  = 1e-9;
 
 static inline double nonzero(double x) { return x + std::copysign(1.0e-30, x); }  // Global.h:174-178
 
+// evolution::Wedge(angle = dphi, zeroangle = sphi) (source/Wedge_Evolution.cpp:17-99) into a
+// row::Wedge* block
+static void wedge_fill(double *w, double dphi, double sphi)
+{
+  w[row::WedgeA1x]  = std::cos(sphi);
+  w[row::WedgeA1y]  = std::sin(sphi);
+  w[row::WedgeA2x]  = std::cos(sphi + dphi);
+  w[row::WedgeA2y]  = std::sin(sphi + dphi);
+  w[row::WedgeN1x]  = -std::sin(sphi);
+  w[row::WedgeN1y]  = std::cos(sphi);
+  w[row::WedgeN2x]  = std::sin(sphi + dphi);
+  w[row::WedgeN2y]  = -std::cos(sphi + dphi);
+  w[row::WedgeDPhi] = dphi;
+}
+
+// Wedge::Contains: !completelyoutside of GenericKernelForContainsAndInside<false>
+// (Wedge_Evolution.h:296-339) at a point of the z = 0 plane
+static bool wedge_contains(const double *w, double x, double y)
+{
+  const double startCheck = (-x * w[row::WedgeA1y] + y * w[row::WedgeA1x]);
+  const double endCheck   = (-w[row::WedgeA2x] * y + w[row::WedgeA2y] * x);
+  bool out                = startCheck < 0.;
+  if (w[row::WedgeDPhi] < kPi)
+    out = out || endCheck < 0.;
+  else
+    out = out && endCheck < 0.;
+  return !out;
+}
+
 int shape_param_count(int32_t type, const double *p, int32_t n_avail)
 {
   switch (type) {
@@ -53,17 +82,17 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     return VGN_OK;
   }
   case kTube: {
-    // TubeStruct(rmin, rmax, z, sphi, dphi) + CalculateCached (TubeStruct.h:43-72, 153-175)
-    const double rmin = p[0] < 0.0 ? 0.0 : p[0], rmax = p[1], z = p[2], dphi = p[4];
-    if (dphi < kTwoPi) {
-      err = "tube phi sections are not supported";
-      return VGN_ERR_UNSUPPORTED;
-    }
-    if (!(rmax > rmin && z > 0)) {
-      err = "tube needs rmax > rmin and dz > 0";
+    // TubeStruct(rmin, rmax, z, sphi, dphi) + CalculateCached (TubeStruct.h:43-72, 153-175);
+    // the constructor keeps the raw (sphi, dphi) and builds its Wedge from them
+    const double rmin = p[0] < 0.0 ? 0.0 : p[0], rmax = p[1], z = p[2], sphi = p[3], dphi = p[4];
+    if (!(rmax > rmin && z > 0 && dphi > 0)) {
+      err = "tube needs rmax > rmin, dz > 0 and dphi > 0";
       return VGN_ERR_ARG;
     }
     double row[row::kTubeSize];
+    row[row::TubeSphi] = sphi;
+    row[row::TubeTolOz] = z + kHalfTolerance;
+    wedge_fill(row + row::TubeWedge, dphi, sphi);  // also fAlongPhi1/2 and fDphi
     row[row::TubeRmin] = rmin;
     row[row::TubeRmax] = rmax;
     row[row::TubeZ]    = z;
@@ -255,15 +284,7 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     double r[row::kSphereSize] = {};
     r[row::SphRmin]      = rmin;
     r[row::SphRmax]      = rmax;
-    r[row::SphA1x]       = std::cos(sphi);
-    r[row::SphA1y]       = std::sin(sphi);
-    r[row::SphA2x]       = std::cos(sphi + dphi);
-    r[row::SphA2y]       = std::sin(sphi + dphi);
-    r[row::SphN1x]       = -std::sin(sphi);
-    r[row::SphN1y]       = std::cos(sphi);
-    r[row::SphN2x]       = std::sin(sphi + dphi);
-    r[row::SphN2y]       = -std::cos(sphi + dphi);
-    r[row::SphWedgeDPhi] = dphi;
+    wedge_fill(r + row::SphA1x, dphi, sphi);  // SphA1x..SphWedgeDPhi is a Wedge block
     const double sT = stheta, eT = stheta + dtheta;
     r[row::SphSTheta]    = sT;
     r[row::SphETheta]    = eT;
@@ -335,10 +356,40 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mn = {-r[0], -r[1], -r[2]};
     mx = {r[0], r[1], r[2]};
     return;
-  case kTube:  // UnplacedTube::Extent, full phi (source/UnplacedTube.cpp:214-220)
-    mn = {-r[row::TubeRmax], -r[row::TubeRmax], -r[row::TubeZ]};
-    mx = {r[row::TubeRmax], r[row::TubeRmax], r[row::TubeZ]};
+  case kTube: {  // UnplacedTube::Extent (source/UnplacedTube.cpp:214-266)
+    const double rmax = r[row::TubeRmax], rmin = r[row::TubeRmin], sphi = r[row::TubeSphi], dphi = r[row::TubeDphi];
+    const double *w = r + row::TubeWedge;
+    mn = {-rmax, -rmax, -r[row::TubeZ]};
+    mx = {rmax, rmax, r[row::TubeZ]};
+    if (dphi == kTwoPi) return;
+    const double Rin     = 0.5 * (rmax + rmin);
+    const bool phi0out   = !wedge_contains(w, Rin, 0);
+    const bool phi90out  = !wedge_contains(w, 0, Rin);
+    const bool phi180out = !wedge_contains(w, -Rin, 0);
+    const bool phi270out = !wedge_contains(w, 0, -Rin);
+    if (!(phi0out || phi90out || phi180out || phi270out)) return;
+    auto vmax = [](double a, double b) { return a > b ? a : b; };
+    auto vmin = [](double a, double b) { return a < b ? a : b; };
+    const double Cx = rmax * std::cos(sphi), Dx = rmax * std::cos(sphi + dphi);
+    const double Cy = rmax * std::sin(sphi), Dy = rmax * std::sin(sphi + dphi);
+    if (phi0out) mx.x = vmax(Cx, Dx);
+    if (phi90out) mx.y = vmax(Cy, Dy);
+    if (phi180out) mn.x = vmin(Cx, Dx);
+    if (phi270out) mn.y = vmin(Cy, Dy);
+    if (dphi >= kPi) return;
+    const double Ax = rmin * std::cos(sphi), Bx = rmin * std::cos(sphi + dphi);
+    const double Ay = rmin * std::sin(sphi), By = rmin * std::sin(sphi + dphi);
+    double temp;
+    temp = vmax(Ax, Bx);
+    mx.x = temp > mx.x ? temp : mx.x;
+    temp = vmax(Ay, By);
+    mx.y = temp > mx.y ? temp : mx.y;
+    temp = vmin(Ax, Bx);
+    mn.x = temp < mn.x ? temp : mn.x;
+    temp = vmin(Ay, By);
+    mn.y = temp < mn.y ? temp : mn.y;
     return;
+  }
   case kCone: {  // UnplacedCone::Extent, full phi (source/UnplacedCone.cpp:149-165)
     const double m = r[row::ConeArgRmax1] > r[row::ConeArgRmax2] ? r[row::ConeArgRmax1] : r[row::ConeArgRmax2];
     mn = {-m, -m, -r[row::ConeDz]};

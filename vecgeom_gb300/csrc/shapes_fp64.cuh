@@ -83,13 +83,68 @@ __device__ __forceinline__ double box_safe_out(const double *h, D3 p)
   return min3(h[0] - fabs(p.x), h[1] - fabs(p.y), h[2] - fabs(p.z));
 }
 
-// ---------------------------------------------------------------- Tube (full phi)
-// kernel/TubeImplementation.h; row layout vgn::row::Tube*
+// ---------------------------------------------------------------- Wedge
+// evolution::Wedge (Wedge_Evolution.h) over a row::Wedge* block of doubles
+constexpr double kPiD = 3.14159265358979323846;
+
+// Wedge::IsOnSurfaceGeneric (Wedge_Evolution.h:341-354)
+__device__ __forceinline__ bool wedge_on_surface(double ax, double ay, double nx, double ny, D3 p)
+{
+  if (!(ax * p.x + ay * p.y >= 0.)) return false;
+  return fabs(nx * p.x + ny * p.y) < kTolerance;
+}
+
+// Wedge::GenericKernelForContainsAndInside (Wedge_Evolution.h:306-339)
+template <bool FOR_INSIDE>
+__device__ __forceinline__ void wedge_ci(const double *w, D3 p, bool &cin, bool &cout)
+{
+  const double startCheck = (-p.x * w[row::WedgeA1y] + p.y * w[row::WedgeA1x]);
+  const double endCheck   = (-w[row::WedgeA2x] * p.y + w[row::WedgeA2y] * p.x);
+  cout                    = startCheck < 0.;
+  if (w[row::WedgeDPhi] < kPiD)
+    cout = cout || endCheck < 0.;
+  else
+    cout = cout && endCheck < 0.;
+  if (FOR_INSIDE) {
+    const bool onSurface =
+        wedge_on_surface(w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p) ||
+        wedge_on_surface(w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p);
+    cout = cout && !onSurface;
+    cin  = !onSurface && !cout;
+  }
+}
+
+// Wedge::SafetyToOut (Wedge_Evolution.h:356-372)
+__device__ __forceinline__ double wedge_safe_out(const double *w, D3 p)
+{
+  const double dist1 = p.x * w[row::WedgeN1x] + p.y * w[row::WedgeN1y];
+  const double dist2 = p.x * w[row::WedgeN2x] + p.y * w[row::WedgeN2y];
+  if (w[row::WedgeDPhi] < kPiD) return dist1 < dist2 ? dist1 : dist2;
+  return dist1 > dist2 ? dist1 : dist2;
+}
+
+// ---------------------------------------------------------------- Tube
+// kernel/TubeImplementation.h (UniversalTube: rmin and phi treatment decided at run
+// time, TubeTypes.h:91-139); row layout vgn::row::Tube*, the phi wedge at TubeWedge
 namespace tb = row;
 
-// CircleTrajectoryIntersection (TubeImplementation.h:103-160), no phi
-__device__ __forceinline__ void tube_circle(double b, double c, double fz, D3 pos, D3 dir, bool largest, bool insector,
-                                            double &dist, bool &ok)
+__device__ __forceinline__ bool tube_has_phi(const double *t) { return t[tb::TubeDphi] < 2. * kPiD; }
+
+// TubeUtilities::PointInCyclicalSector<..., onSurfaceT = false> (TubeImplementation.h:58-101);
+// "smaller than pi" is dphi <= M_PI, decided at run time
+__device__ __forceinline__ bool tube_in_sector(const double *t, double x, double y, bool includeSurface)
+{
+  const double *w         = t + tb::TubeWedge;
+  const double startCheck = (-x * w[row::WedgeA1y] + y * w[row::WedgeA1x]);
+  const double endCheck   = (-w[row::WedgeA2x] * y + w[row::WedgeA2y] * x);
+  const double tol        = includeSurface ? -kHalfTolerance : kHalfTolerance;
+  if (t[tb::TubeDphi] <= kPiD) return (startCheck >= tol) && (endCheck >= tol);
+  return (startCheck >= tol) || (endCheck >= tol);
+}
+
+// CircleTrajectoryIntersection (TubeImplementation.h:103-160)
+__device__ __forceinline__ void tube_circle(const double *t, double b, double c, D3 pos, D3 dir, bool largest,
+                                            bool insector, double &dist, bool &ok)
 {
   double delta = b * b - c;
   ok           = delta > 0.;
@@ -102,14 +157,54 @@ __device__ __forceinline__ void tube_circle(double b, double c, double fz, D3 po
   if (!ok) return;
   if (insector) {
     const double hitz = pos.z + dist * dir.z;
-    ok &= (fabs(hitz) <= fz);
+    ok &= (fabs(hitz) <= t[tb::TubeZ]);
+    if (!ok) return;
+    if (tube_has_phi(t)) ok &= tube_in_sector(t, pos.x + dist * dir.x, pos.y + dist * dir.y, true);
   }
+}
+
+// PhiPlaneTrajectoryIntersection (TubeImplementation.h:249-301)
+__device__ __forceinline__ void tube_phi_plane(const double *t, double alongX, double alongY, double normalX,
+                                               double normalY, D3 pos, D3 dir, bool posdir, bool insector,
+                                               double &dist, bool &ok)
+{
+  const double dirDotNorm = dir.x * normalX + dir.y * normalY;
+  ok                      = insector ? (dirDotNorm > 0.) : (dirDotNorm < 0.);
+  const double dirDotXY   = (dir.y * alongX - dir.x * alongY);
+  dist                    = (alongY * pos.x - alongX * pos.y) / nonzero(dirDotXY);
+  ok &= (dist * fabs(dirDotNorm)) > -kHalfTolerance;
+  if (insector) {
+    const double hitx = pos.x + dist * dir.x;
+    const double hity = pos.y + dist * dir.y;
+    const double hitz = pos.z + dist * dir.z;
+    const double r2   = hitx * hitx + hity * hity;
+    ok &= fabs(hitz) <= t[tb::TubeTolOz] && (r2 >= t[tb::TubeTolOrmin2]) && (r2 <= t[tb::TubeTolOrmax2]);
+    if (posdir) ok = ok && (hitx * alongX + hity * alongY) > 0.;
+  } else if (posdir) {
+    const double hitx = pos.x + dist * dir.x;
+    const double hity = pos.y + dist * dir.y;
+    ok                = ok && (hitx * alongX + hity * alongY) >= 0.;
+  }
+}
+
+// PhiPlaneSafety<inside = false> (TubeImplementation.h:210-247), UniversalTube
+__device__ __forceinline__ double tube_phi_safety(const double *t, D3 pos)
+{
+  const double *w = t + tb::TubeWedge;
+  double safety   = t[tb::TubeDphi] > kPiD ? sqrt(pos.x * pos.x + pos.y * pos.y) : kInfLength;
+  const double phi1 = pos.x * w[row::WedgeA1y] - pos.y * w[row::WedgeA1x];  // PerpDist2D
+  if (phi1 > -kHalfTolerance && phi1 < safety) safety = phi1;
+  double phi2 = pos.x * w[row::WedgeA2y] - pos.y * w[row::WedgeA2x];
+  phi2 *= -1;
+  if (phi2 > -kHalfTolerance && phi2 < safety) safety = phi2;
+  return safety;
 }
 
 // DistanceToInKernel (TubeImplementation.h:504-681)
 __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 d)
 {
   const bool hasrmin = t[tb::TubeRmin] > 0;
+  const bool hasphi  = tube_has_phi(t);
   bool done          = false;
   double distance    = kInfLength;
   double distz       = fabs(p.z) - t[tb::TubeZ];
@@ -123,6 +218,7 @@ __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 
   bool inside = distz < -kHalfTolerance;
   inside &= rsq < t[tb::TubeTolIrmax2];
   if (hasrmin) inside &= rsq > t[tb::TubeTolIrmin2];
+  if (hasphi && inside) inside &= tube_in_sector(t, p.x, p.y, false);
   done |= inside;
   if (done) return distance;
 
@@ -134,6 +230,7 @@ __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 
   bool okz          = distz > -kHalfTolerance && (p.z * d.z < 0);
   okz &= (r2 <= t[tb::TubeRmax2]);
   if (hasrmin) okz &= (t[tb::TubeRmin2] <= r2);
+  if (hasphi && okz) okz &= tube_in_sector(t, hitx, hity, true);
   if (!done && okz) distance = distz;
   done |= okz;
 
@@ -143,6 +240,7 @@ __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 
   if (hasrmin)
     onsurf |= (rho >= t[tb::TubeTolOrmin2]) && (rho <= t[tb::TubeTolIrmin2]) &&
               (fabs(p.z) < (t[tb::TubeZ] + kTolerance)) && (d.x * -p.x + d.y * -p.y + d.z * 0. <= 0.);
+  if (hasphi) onsurf = onsurf && tube_in_sector(t, p.x, p.y, true);
   if (!done && onsurf) distance = 0.;
   done |= onsurf;
   if (done) return distance;
@@ -152,7 +250,7 @@ __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 
   const double crmax  = invnsq * (rsq - t[tb::TubeRmax2]);
   double dist_rmax;
   bool ok_rmax;
-  tube_circle(b, crmax, t[tb::TubeZ], p, d, false, true, dist_rmax, ok_rmax);
+  tube_circle(t, b, crmax, p, d, false, true, dist_rmax, ok_rmax);
   ok_rmax &= dist_rmax < distance;
   if (!done && ok_rmax) distance = dist_rmax;
   done |= ok_rmax;
@@ -161,9 +259,22 @@ __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 
     const double crmin = invnsq * (rsq - t[tb::TubeRmin2]);
     double dist_rmin;
     bool ok_rmin;
-    tube_circle(b, crmin, t[tb::TubeZ], p, d, true, true, dist_rmin, ok_rmin);
+    tube_circle(t, b, crmin, p, d, true, true, dist_rmin, ok_rmin);
     ok_rmin &= dist_rmin < distance;
     if (!done && ok_rmin) distance = dist_rmin;
+  }
+  if (hasphi) {  // sector type unknown at compile time: both planes, positive-direction check
+    const double *w = t + tb::TubeWedge;
+    double dist_phi;
+    bool ok_phi;
+    tube_phi_plane(t, w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p, d, true, true,
+                   dist_phi, ok_phi);
+    ok_phi &= dist_phi < distance;
+    if (!done && ok_phi) distance = dist_phi;
+    done |= ok_phi;
+    tube_phi_plane(t, w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p, d, true, true,
+                   dist_phi, ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
   }
   return distance;
 }
@@ -188,6 +299,7 @@ __device__ __forceinline__ double tube_dist_in(const double *t, D3 pt, D3 d)
 __device__ __forceinline__ double tube_dist_out(const double *t, D3 p, D3 d)
 {
   const bool hasrmin = t[tb::TubeRmin] > 0;
+  const bool hasphi  = tube_has_phi(t);
   const double fz    = t[tb::TubeZ];
   double distz       = fz - fabs(p.z);
   if (distz < -kHalfTolerance) return -1.;
@@ -200,6 +312,11 @@ __device__ __forceinline__ double tube_dist_out(const double *t, D3 p, D3 d)
     crmin -= t[tb::TubeRmin2];
     if (crmin < -2.0 * kTolerance * t[tb::TubeRmin]) return -1.;
   }
+  if (hasphi) {
+    bool cin = false, cout = false;
+    wedge_ci<true>(t + tb::TubeWedge, p, cin, cout);
+    if (cout) return -1.;
+  }
   double distance      = kInfLength;
   const double invdirz = 1. / nonzero(d.z);
   distz                = (fz - p.z) * invdirz;
@@ -211,18 +328,29 @@ __device__ __forceinline__ double tube_dist_out(const double *t, D3 p, D3 d)
     double dist_rmin;
     bool ok_rmin;
     crmin *= invnsq;
-    tube_circle(b, crmin, fz, p, d, false, false, dist_rmin, ok_rmin);
+    tube_circle(t, b, crmin, p, d, false, false, dist_rmin, ok_rmin);
     if (ok_rmin && dist_rmin < distance) distance = dist_rmin;
   }
   double dist_rmax;
   bool ok_rmax;
   crmax *= invnsq;
-  tube_circle(b, crmax, fz, p, d, true, false, dist_rmax, ok_rmax);
+  tube_circle(t, b, crmax, p, d, true, false, dist_rmax, ok_rmax);
   if (ok_rmax && dist_rmax < distance) distance = dist_rmax;
+  if (hasphi) {  // angle bigger than pi or unknown: positive-direction check on both planes
+    const double *w = t + tb::TubeWedge;
+    double dist_phi;
+    bool ok_phi;
+    tube_phi_plane(t, w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p, d, true, false,
+                   dist_phi, ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
+    tube_phi_plane(t, w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p, d, true, false,
+                   dist_phi, ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
+  }
   return distance;
 }
 
-// SafetyToInOld (TubeImplementation.h:912-938)
+// SafetyToInOld (TubeImplementation.h:912-938; TUBE_SAFETY_OLD is defined at line 14)
 __device__ __forceinline__ double tube_safe_in(const double *t, D3 p)
 {
   double safety         = fabs(p.z) - t[tb::TubeZ];
@@ -233,10 +361,16 @@ __device__ __forceinline__ double tube_safe_in(const double *t, D3 p)
     const double safermin = t[tb::TubeRmin] - r;
     if (safermin > safety) safety = safermin;
   }
+  if (tube_has_phi(t)) {
+    const bool insector = tube_in_sector(t, p.x, p.y, false);
+    if (insector) return safety;
+    const double safephi = tube_phi_safety(t, p);
+    if (!insector && safephi < kInfLength && safephi > safety) safety = safephi;
+  }
   return safety;
 }
 
-// SafetyToOutOld (TubeImplementation.h:940-960)
+// SafetyToOutOld (TubeImplementation.h:940-966)
 __device__ __forceinline__ double tube_safe_out(const double *t, D3 p)
 {
   double safety         = t[tb::TubeZ] - fabs(p.z);
@@ -246,6 +380,10 @@ __device__ __forceinline__ double tube_safe_out(const double *t, D3 p)
   if (t[tb::TubeRmin] > 0) {
     const double safermin = r - t[tb::TubeRmin];
     if (safermin < safety) safety = safermin;
+  }
+  if (tube_has_phi(t)) {
+    const double safephi = wedge_safe_out(t + tb::TubeWedge, p);
+    if (safephi < safety) safety = safephi;
   }
   return safety;
 }
@@ -265,6 +403,16 @@ __device__ __forceinline__ void tube_generic_ci(const double *t, D3 p, bool fori
   if (rmin > 0) {
     cout |= r2 <= (forinside ? fabs(rmin * (rmin - 2.0 * kTolerance)) : rmin * rmin);
     if (forinside) cin &= r2 > rmin * (rmin + 2.0 * kTolerance);
+    if (cout) return;
+  }
+  if (tube_has_phi(t)) {
+    bool cinphi = false, coutphi = false;
+    if (forinside)
+      wedge_ci<true>(t + tb::TubeWedge, p, cinphi, coutphi);
+    else
+      wedge_ci<false>(t + tb::TubeWedge, p, cinphi, coutphi);
+    cout |= coutphi;
+    if (forinside) cin &= cinphi;
   }
 }
 
@@ -892,37 +1040,11 @@ __device__ __forceinline__ double trap_safe_out(const double *t, D3 p)
 namespace sp = row;
 constexpr double kSqrtTolerance = 3.1622777e-5;  // base/Math.h:29
 constexpr double kThetaHalfPi   = 0.5 * 3.14159265358979323846;
-constexpr double kPiD           = 3.14159265358979323846;
 
 __device__ __forceinline__ double sph_plus_tol_sq(double x) { return x * (x + 2.0 * kTolerance); }
 __device__ __forceinline__ double sph_minus_tol_sq(double x) { return fabs(x * (x - 2.0 * kTolerance)); }
 __device__ __forceinline__ double mag2(D3 p) { return p.x * p.x + p.y * p.y + p.z * p.z; }
 
-// Wedge::IsOnSurfaceGeneric (Wedge_Evolution.h:341-354)
-__device__ __forceinline__ bool wedge_on_surface(double ax, double ay, double nx, double ny, D3 p)
-{
-  if (!(ax * p.x + ay * p.y >= 0.)) return false;
-  return fabs(nx * p.x + ny * p.y) < kTolerance;
-}
-
-// Wedge::GenericKernelForContainsAndInside (Wedge_Evolution.h:306-339)
-template <bool FOR_INSIDE>
-__device__ __forceinline__ void wedge_ci(const double *t, D3 p, bool &cin, bool &cout)
-{
-  const double startCheck = (-p.x * t[sp::SphA1y] + p.y * t[sp::SphA1x]);
-  const double endCheck   = (-t[sp::SphA2x] * p.y + t[sp::SphA2y] * p.x);
-  cout                    = startCheck < 0.;
-  if (t[sp::SphWedgeDPhi] < kPiD)
-    cout = cout || endCheck < 0.;
-  else
-    cout = cout && endCheck < 0.;
-  if (FOR_INSIDE) {
-    const bool onSurface = wedge_on_surface(t[sp::SphA1x], t[sp::SphA1y], t[sp::SphN1x], t[sp::SphN1y], p) ||
-                           wedge_on_surface(t[sp::SphA2x], t[sp::SphA2y], t[sp::SphN2x], t[sp::SphN2y], p);
-    cout = cout && !onSurface;
-    cin  = !onSurface && !cout;
-  }
-}
 
 // ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730), stheta = 0 and etheta >= pi
 __device__ __forceinline__ bool theta_completely_inside(const double *t, D3 p)
@@ -961,7 +1083,7 @@ __device__ __forceinline__ bool sphere_completely_inside(const double *t, D3 p)
   const double rad   = sqrt(mag2(p));
   const bool inRad   = (rad < (t[sp::SphRmax] - kTolerance)) && (rad > (t[sp::SphRmin] + kTolerance));
   bool cin = false, cout = false;
-  wedge_ci<true>(t, p, cin, cout);
+  wedge_ci<true>(t + sp::SphA1x, p, cin, cout);
   return inRad && cin && theta_completely_inside(t, p);
 }
 
@@ -970,7 +1092,7 @@ __device__ __forceinline__ bool sphere_completely_outside(const double *t, D3 p)
   const double rad  = sqrt(mag2(p));
   const bool outRad = (rad > (t[sp::SphRmax] + kTolerance)) || (rad < (t[sp::SphRmin] - kTolerance));
   bool cin = false, cout = false;
-  wedge_ci<true>(t, p, cin, cout);
+  wedge_ci<true>(t + sp::SphA1x, p, cin, cout);
   return outRad || cout || theta_completely_outside(t, p);
 }
 
@@ -991,7 +1113,7 @@ __device__ __forceinline__ bool sphere_on_surface_moving(const double *t, D3 p, 
   }
   if (!(outer || inner)) return false;
   bool cin = false, cout = false;
-  wedge_ci<false>(t, p, cin, cout);
+  wedge_ci<false>(t + sp::SphA1x, p, cin, cout);
   return !cout && !theta_completely_outside(t, p);
 }
 

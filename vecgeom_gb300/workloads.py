@@ -315,9 +315,10 @@ MIXED_GRID = (16, 16, 32)  # 8192 cells of 250 x 250 x 125 mm
 MIXED_JITTER = 5.0
 
 
-def _mixed_shape_params(rng: np.random.Generator, shape: int):
+def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = False):
     """Parameters with every length drawn from U[5, 60] mm (Tube radii from U[5, 40] mm),
-    and the half-extent of the shape's bounding box."""
+    and the half-extent of the shape's full (unsectioned) bounding box.  With `sections`,
+    three quarters of the tubes are phi sections (start U[0, 2 pi), width U[0.2, 2 pi - 0.2])."""
     u = lambda lo=5.0, hi=60.0: float(rng.uniform(lo, hi))
     if shape == BOX:
         p = (u(), u(), u())
@@ -325,7 +326,11 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int):
     if shape == TUBE:
         a, b = sorted((u(5.0, 40.0), u(5.0, 40.0)))
         rmin, rmax = (a, b) if b - a > 1.0 else (0.0, b)
-        p = (rmin, rmax, u(), 0.0, K_TWO_PI)
+        sphi, dphi = 0.0, K_TWO_PI
+        dz = u()
+        if sections and rng.uniform() < 0.75:
+            sphi, dphi = float(rng.uniform(0.0, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+        p = (rmin, rmax, dz, sphi, dphi)
         return p, np.array([rmax, rmax, p[2]])
     if shape == CONE:
         rmax1, rmax2, dz = u(), u(), u()
@@ -390,13 +395,14 @@ def trapezoid_corners(p) -> np.ndarray:
 
 
 def mixed_shape_geometry(seed: int = 21, grid=MIXED_GRID, world: float = MIXED_WORLD,
-                         shapes=IMPLEMENTED_SHAPES) -> GeometryDescription:
+                         shapes=IMPLEMENTED_SHAPES, sections: bool = False) -> GeometryDescription:
     """World box of half-length `world` holding one daughter per cell of a
     jittered grid (16 x 16 x 32 = 8192 cells of 250 x 250 x 125 mm by default);
     shape types uniform over `shapes`, lengths from U[5, 60] mm, each daughter
     rotated by a uniform random rotation (Euler angles phi, psi ~ U[0, 360),
     cos(theta) ~ U[-1, 1]).  A daughter whose bounding sphere (plus the jitter)
-    would leave its cell is scaled down to fit, so daughters never overlap."""
+    would leave its cell is scaled down to fit, so daughters never overlap.  `sections`
+    makes most tubes phi sections (see _mixed_shape_params)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     nx, ny, nz = grid
     pitch = np.array([2 * world / nx, 2 * world / ny, 2 * world / nz])
@@ -407,7 +413,7 @@ def mixed_shape_geometry(seed: int = 21, grid=MIXED_GRID, world: float = MIXED_W
         for j in range(ny):
             for k in range(nz):
                 shape = shapes[int(rng.integers(len(shapes)))]
-                params, ext = _mixed_shape_params(rng, shape)
+                params, ext = _mixed_shape_params(rng, shape, sections)
                 radius = float(np.sqrt(np.sum(ext * ext)))
                 if radius > limit:
                     params = list(params)
