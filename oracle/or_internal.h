@@ -100,7 +100,7 @@ typedef struct { /* TubeStruct.h:15-41 */
   or_wedge w; /* fPhiWedge, built from the constructor's raw (dphi, sphi) */
 } or_tube;
 
-typedef struct { /* ConeStruct.h:23-77 cached members, full phi */
+typedef struct { /* ConeStruct.h:23-77 cached members */
   double rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi;
   double o_rmin1, o_rmin2, o_rmax1, o_rmax2; /* _frmin1.. (constructor arguments) */
   double innerSlope, outerSlope, innerOffset, outerOffset, innerTolerance, outerTolerance;
@@ -108,6 +108,8 @@ typedef struct { /* ConeStruct.h:23-77 cached members, full phi */
   double innerConeApex, tanInnerApexAngle, outerConeApex, tanOuterApexAngle;
   double secRMin, secRMax, invSecRMin, invSecRMax, tanRMin, tanRMax, zNormInner, zNormOuter;
   double originalRmax1, originalRmax2;
+  double alongphi1x, alongphi1y, alongphi2x, alongphi2y; /* from the checked (sphi, dphi) */
+  or_wedge w; /* fPhiWedge: vectors from the raw constructor angles, fDPhi the checked one */
 } or_cone;
 
 typedef struct { /* TrdStruct.h:19-39 (UniversalTrd: VECGEOM_NO_SPECIALIZATION is the default build) */

@@ -123,6 +123,15 @@ static inline int wedge_contains(const or_wedge *w, v3 p)
   return !cout;
 }
 
+/* Wedge::SafetyToIn (Wedge_Evolution.h:374-391) */
+static double wedge_safe_in(const or_wedge *w, v3 p)
+{
+  double dist1 = p.x * w->n1x + p.y * w->n1y;
+  double dist2 = p.x * w->n2x + p.y * w->n2y;
+  if (w->dphi < kPi) return or_max(-1 * dist1, -1 * dist2);
+  return or_min(-1 * dist1, -1 * dist2);
+}
+
 /* Wedge::SafetyToOut (Wedge_Evolution.h:356-372) */
 static double wedge_safe_out(const or_wedge *w, v3 p)
 {
@@ -521,7 +530,7 @@ static void tube_extent(const or_tube *t, v3 *mn, v3 *mx)
 /* ConeStruct constructor + CalculateCached (ConeStruct.h:79-157, 414-426) */
 static int cone_init(or_cone *c, const double *a, char *err, int errlen)
 {
-  double dphi = a[6];
+  double dphi = a[6], sphi = a[5];
   c->rmin1 = a[0] < 0.0 ? 0.0 : a[0];
   c->rmax1 = a[1];
   c->rmin2 = a[2] < 0.0 ? 0.0 : a[2];
@@ -532,13 +541,29 @@ static int cone_init(or_cone *c, const double *a, char *err, int errlen)
   c->o_rmax1 = a[1];
   c->o_rmin2 = a[2];
   c->o_rmax2 = a[3];
+  if (!(dphi > 0)) {
+    set_err(err, errlen, "cone: needs dphi > 0");
+    return -1;
+  }
+  /* fPhiWedge(_dphi, _sphi), then SetAndCheckDPhiAngle(_dphi) and SetAndCheckSPhiAngle(_sphi)
+   * (ConeStruct.h:321-360, 413-425): the wedge keeps the raw angles' vectors and takes the
+   * checked delta; the along vectors use the checked angles */
+  wedge_init(&c->w, dphi, sphi);
+  c->dphi = dphi;
   if (dphi >= kTwoPi - 0.5 * kAngTolerance) {
     c->dphi = kTwoPi;
     c->sphi = 0;
-  } else {
-    set_err(err, errlen, "cone: phi sections are not supported");
-    return -1;
   }
+  c->w.dphi = c->dphi;
+  if (sphi < 0)
+    c->sphi = kTwoPi - fmod(fabs(sphi), kTwoPi);
+  else
+    c->sphi = fmod(sphi, kTwoPi);
+  if (c->sphi + c->dphi > kTwoPi) c->sphi -= kTwoPi;
+  c->alongphi1x = cos(c->sphi);
+  c->alongphi1y = sin(c->sphi);
+  c->alongphi2x = cos(c->sphi + c->dphi);
+  c->alongphi2y = sin(c->sphi + c->dphi);
   c->originalRmax1 = c->rmax1;
   c->originalRmax2 = c->rmax2;
   if (c->rmin1 == c->rmax1) c->rmax1 += kConeTolerance;
@@ -599,6 +624,48 @@ static inline double cone_radius(const or_cone *c, double z, int inner)
   return c->originalRmax1 == c->originalRmax2 ? c->originalRmax1 : c->outerSlope * z + c->outerOffset;
 }
 
+static inline int cone_has_phi(const or_cone *c) { return c->dphi < kTwoPi; } /* ConeTypes.h:101-107 */
+
+/* ConeUtilities::PointInCyclicalSector<..., onSurfaceT = false> (ConeUtilities.h:64-114),
+ * UniversalCone: "smaller than pi" is dphi <= M_PI */
+static int cone_in_sector(const or_cone *c, double x, double y, int includeSurface)
+{
+  double startCheck = (-x * c->alongphi1y) + (y * c->alongphi1x);
+  double endCheck   = (-c->alongphi2x * y) + (c->alongphi2y * x);
+  double tol        = includeSurface ? -kConeTolerance : kConeTolerance;
+  if (c->dphi <= kPi) return (startCheck >= tol) && (endCheck >= tol);
+  return (startCheck >= tol) || (endCheck >= tol);
+}
+
+/* ConeUtilities::PhiPlaneTrajectoryIntersection (ConeUtilities.h:155-204) */
+static void cone_phi_plane(const or_cone *c, double alongX, double alongY, double normalX, double normalY, v3 pos,
+                           v3 dir, int posdir, int insector, double *dist, int *ok)
+{
+  double dirDotXY;
+  *dist = kInfLength;
+  if (insector)
+    *ok = ((dir.x * normalX) + (dir.y * normalY) > 0.);
+  else
+    *ok = ((dir.x * normalX) + (dir.y * normalY) < 0.);
+  dirDotXY = (dir.y * alongX) - (dir.x * alongY);
+  if (dirDotXY != 0) *dist = ((alongY * pos.x) - (alongX * pos.y)) / NonZero(dirDotXY);
+  *ok &= *dist > -kConeTolerance;
+  if (insector) {
+    double hitx = pos.x + *dist * dir.x;
+    double hity = pos.y + *dist * dir.y;
+    double hitz = pos.z + *dist * dir.z;
+    double r2   = (hitx * hitx) + (hity * hity);
+    double innerRadIrTol = cone_radius(c, hitz, 1) + kTolerance;
+    double outerRadIrTol = cone_radius(c, hitz, 0) - kTolerance;
+    *ok &= fabs(hitz) <= c->tolIz && (r2 >= innerRadIrTol * innerRadIrTol) && (r2 <= outerRadIrTol * outerRadIrTol);
+    if (posdir) *ok = *ok && ((hitx * alongX) + (hity * alongY)) > 0.;
+  } else if (posdir) {
+    double hitx = pos.x + *dist * dir.x;
+    double hity = pos.y + *dist * dir.y;
+    *ok         = *ok && ((hitx * alongX) + (hity * alongY)) >= 0.;
+  }
+}
+
 /* ConeUtilities::GetNormal (ConeUtilities.h:206-238) */
 static inline v3 cone_normal(const or_cone *c, v3 p, int inner)
 {
@@ -633,10 +700,11 @@ static int cone_conical(const or_cone *c, v3 p, v3 d, int fordistin, int inner, 
   n         = cone_normal(c, p, inner);
   if (onsurf && fabs(v3_dot(d, n)) == 0.) return 0;
   if (onsurf) {
-    if (fordistin) {
-      if (v3_dot(d, n) <= 0.) { *distance = 0.; return 1; }
-    } else {
-      if (v3_dot(d, n) >= 0.) { *distance = 0.; return 1; }
+    int moving = fordistin ? (v3_dot(d, n) <= 0.) : (v3_dot(d, n) >= 0.);
+    if (cone_has_phi(c)) moving = cone_in_sector(c, p.x, p.y, 1) && moving;
+    if (moving) {
+      *distance = 0.;
+      return 1;
     }
   }
   pDotV2D = p.x * d.x + p.y * d.y;
@@ -714,6 +782,14 @@ static int cone_conical(const or_cone *c, v3 p, v3 d, int fordistin, int inner, 
     }
     if (*distance < 0.) return 0;
   }
+  if (cone_has_phi(c)) {
+    double hitx = 0, hity = 0;
+    if (*distance < kInfLength) {
+      hitx = p.x + *distance * d.x;
+      hity = p.y + *distance * d.y;
+    }
+    ok &= (cone_in_sector(c, hitx, hity, 1) && (*distance < kInfLength));
+  }
   return ok;
 }
 
@@ -723,6 +799,7 @@ static double cone_dist_in(const or_cone *c, v3 p, v3 d)
   int done = 0, inside, okz, top, bot, ok;
   double distance = kInfLength, distz, outerRad, rsq, hitx, hity, r2, dr;
   const int hasrmin = cone_has_rmin(c);
+  const int hasphi  = cone_has_phi(c);
   distz = fabs(p.z) - c->dz;
   done |= (distz > kConeTolerance && (p.z * d.z) >= 0.) || (fabs(distz) < kConeTolerance && (p.z * d.z) > 0.);
   if (done) return distance;
@@ -734,6 +811,7 @@ static double cone_dist_in(const or_cone *c, v3 p, v3 d)
   inside   = distz < -kConeTolerance;
   inside &= rsq < minus_tol_sq(outerRad, c->outerTolerance);
   if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, 1), c->innerTolerance);
+  if (hasphi) inside &= cone_in_sector(c, p.x, p.y, 0);
   done |= inside;
   if (done) return distance;
   distance = kInfLength;
@@ -749,6 +827,7 @@ static double cone_dist_in(const or_cone *c, v3 p, v3 d)
     bot &= (r2 >= c->sqRmin1 - kTolerance);
     okz &= (top || bot);
   }
+  if (hasphi) okz &= cone_in_sector(c, hitx, hity, 1);
   if (!done && okz) distance = distz;
   done |= okz;
   if (done) return distance;
@@ -761,6 +840,16 @@ static double cone_dist_in(const or_cone *c, v3 p, v3 d)
     ok = cone_conical(c, p, d, 1, 1, &dr);
     ok &= dr < distance;
     if (!done && ok) distance = dr;
+  }
+  if (hasphi) { /* SectorType of UniversalCone is unknown: both planes, positive-direction check */
+    double dist_phi;
+    int ok_phi;
+    cone_phi_plane(c, c->alongphi1x, c->alongphi1y, c->w.n1x, c->w.n1y, p, d, 1, 1, &dist_phi, &ok_phi);
+    ok_phi &= dist_phi < distance;
+    if (!done && ok_phi) distance = dist_phi;
+    done |= ok_phi;
+    cone_phi_plane(c, c->alongphi2x, c->alongphi2y, c->w.n2x, c->w.n2y, p, d, 1, 1, &dist_phi, &ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
   }
   return distance;
 }
@@ -803,6 +892,25 @@ static double cone_dist_out(const or_cone *c, v3 p, v3 d)
     ok = cone_conical(c, p, d, 0, 1, &dr);
     if (!done && ok && dr < distance) distance = dr;
   }
+  if (cone_has_phi(c)) {
+    /* the outside test's phi part (ConeImplementation.h:293-297) only runs where the point is
+     * already outside, so it never changes the result of the scalar kernel */
+    double dist_phi;
+    int ok_phi;
+    const int onStart = wedge_on_surface(c->w.a1x, c->w.a1y, c->w.n1x, c->w.n1y, p); /* IsOnStartPhi */
+    const int onEnd   = wedge_on_surface(c->w.a2x, c->w.a2y, c->w.n2x, c->w.n2y, p); /* IsOnEndPhi */
+    const int cond    = (onStart && (d.x * -c->w.n1x + d.y * -c->w.n1y + d.z * -0.) > 0.) ||
+                     (onEnd && (d.x * -c->w.n2x + d.y * -c->w.n2y + d.z * -0.) > 0.);
+    if (!done && cond) distance = 0.;
+    done |= cond;
+    if (done) return distance;
+    cone_phi_plane(c, c->alongphi1x, c->alongphi1y, c->w.n1x, c->w.n1y, p, d, 1, 0, &dist_phi, &ok_phi);
+    ok_phi &= dist_phi < distance;
+    if (!done && ok_phi) distance = dist_phi;
+    done |= ok_phi;
+    cone_phi_plane(c, c->alongphi2x, c->alongphi2y, c->w.n2x, c->w.n2y, p, d, 1, 0, &dist_phi, &ok_phi);
+    if (ok_phi && dist_phi < distance) distance = dist_phi;
+  }
   if (distance < 0. && fabs(distance) < kTolerance) distance = 0.;
   return distance;
 }
@@ -834,11 +942,13 @@ static double cone_safe_in(const or_cone *c, v3 p)
   rsq      = v3_perp2(p);
   inside &= rsq < minus_tol_sq(outerRad, c->outerTolerance);
   if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, 1), c->innerTolerance);
+  if (cone_has_phi(c) && inside) inside &= cone_in_sector(c, p.x, p.y, 0);
   if (inside) return safety;
   safeZ = fabs(p.z) - c->dz;
   so    = -cone_safe_surface(c, p, 0);
   if (hasrmin) si = -cone_safe_surface(c, p, 1);
   safety = or_max(safeZ, or_max(so, si));
+  if (cone_has_phi(c)) safety = or_max(wedge_safe_in(&c->w, p), safety);
   if (fabs(safety) < kTolerance) safety = 0.;
   return safety;
 }
@@ -861,6 +971,7 @@ static double cone_safe_out(const or_cone *c, v3 p)
   so    = cone_safe_surface(c, p, 0);
   if (hasrmin) si = cone_safe_surface(c, p, 1);
   safety = or_min(safeZ, or_min(so, si));
+  if (cone_has_phi(c)) safety = or_min(wedge_safe_out(&c->w, p), safety);
   if (fabs(safety) < kTolerance) safety = 0.;
   return safety;
 }
@@ -881,6 +992,13 @@ static void cone_generic_ci(const or_cone *c, v3 p, int forinside, int *cin, int
     double rmin = c->innerSlope * p.z + c->innerOffset;
     *cout |= r2 <= (forinside ? minus_tol_sq(rmin, c->innerTolerance) : rmin * rmin);
     if (forinside) *cin &= r2 > plus_tol_sq(rmin, c->innerTolerance);
+    if (*cout) return;
+  }
+  if (cone_has_phi(c)) {
+    int cinphi = 0, coutphi = 0;
+    wedge_ci(&c->w, p, forinside, &cinphi, &coutphi);
+    *cout |= coutphi;
+    if (forinside) *cin &= cinphi;
   }
 }
 
@@ -900,12 +1018,43 @@ static int cone_inside(const or_cone *c, v3 p)
   return r;
 }
 
-/* UnplacedCone::Extent, full phi (source/UnplacedCone.cpp:149-165) */
+/* UnplacedCone::Extent (source/UnplacedCone.cpp:146-206, the phi-aware definition compiled in) */
 static void cone_extent(const or_cone *c, v3 *mn, v3 *mx)
 {
-  double m = c->o_rmax1 > c->o_rmax2 ? c->o_rmax1 : c->o_rmax2;
-  *mn      = v3_make(-m, -m, -c->dz);
-  *mx      = v3_make(m, m, c->dz);
+  double max = c->o_rmax1 > c->o_rmax2 ? c->o_rmax1 : c->o_rmax2;
+  double min = c->o_rmin1 > c->o_rmin2 ? c->o_rmin2 : c->o_rmin1;
+  double Rin, Cx, Dx, Cy, Dy, Ax, Bx, Ay, By, temp;
+  int phi0out, phi90out, phi180out, phi270out;
+  *mn = v3_make(-max, -max, -c->dz);
+  *mx = v3_make(max, max, c->dz);
+  if (c->dphi == kTwoPi) return;
+  Rin       = 0.5 * (max + min);
+  phi0out   = !wedge_contains(&c->w, v3_make(Rin, 0, 0));
+  phi90out  = !wedge_contains(&c->w, v3_make(0, Rin, 0));
+  phi180out = !wedge_contains(&c->w, v3_make(-Rin, 0, 0));
+  phi270out = !wedge_contains(&c->w, v3_make(0, -Rin, 0));
+  if (!(phi0out || phi90out || phi180out || phi270out)) return;
+  Cx = max * cos(c->sphi);
+  Dx = max * cos(c->sphi + c->dphi);
+  Cy = max * sin(c->sphi);
+  Dy = max * sin(c->sphi + c->dphi);
+  if (phi0out) mx->x = or_max(Cx, Dx);
+  if (phi90out) mx->y = or_max(Cy, Dy);
+  if (phi180out) mn->x = or_min(Cx, Dx);
+  if (phi270out) mn->y = or_min(Cy, Dy);
+  if (c->dphi >= kPi) return;
+  Ax = min * cos(c->sphi);
+  Bx = min * cos(c->sphi + c->dphi);
+  Ay = min * sin(c->sphi);
+  By = min * sin(c->sphi + c->dphi);
+  temp  = or_max(Ax, Bx);
+  mx->x = temp > mx->x ? temp : mx->x;
+  temp  = or_max(Ay, By);
+  mx->y = temp > mx->y ? temp : mx->y;
+  temp  = or_min(Ax, Bx);
+  mn->x = temp < mn->x ? temp : mn->x;
+  temp  = or_min(Ay, By);
+  mn->y = temp < mn->y ? temp : mn->y;
 }
 
 /* ================================================================== */

@@ -424,6 +424,121 @@ CONE_CASES = [
     _case(f"{C}:1075", CONE, CT1, "dist_in", (100.0, 0.0, 0.0), vxy, INF, "inf"),
 ]
 
+# phi sections (TestCons.cpp:88-91, 102-103): (rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi)
+C3 = (50.0, 100.0, 50.0, 100.0, 50.0, -KPI / 6, KPI / 3)
+C4 = (50.0, 100.0, 50.0, 200.0, 50.0, -KPI / 6, KPI / 3)
+C5 = (25.0, 50.0, 75.0, 150.0, 50.0, 0.0, 1.5 * KPI)
+CTEST10 = (20.0, 60.0, 80.0, 140.0, 100.0, 10 * KPI / 180.0, 300 * KPI / 180.0)
+ponphi2 = (60 * math.cos(KPI / 6), 60 * math.sin(KPI / 6), 0.0)
+pydx = (60.0, 150.0, 0.0)
+pct10 = (60.0, 0.0, 0.0)
+pct10mx = (-50.0, 0.0, 0.0)
+pct10phi1 = (60 * math.cos(10.0 * KPI / 180.0), 60 * math.sin(10 * KPI / 180.0), 0.0)
+pct10phi2 = (60 * math.cos(50.0 * KPI / 180.0), -60 * math.sin(50 * KPI / 180.0), 0.0)
+pct10phi1r = (90.0 * math.cos(10.0 * KPI / 180.0), 90.0 * math.sin(10 * KPI / 180.0), 0.0)
+pct10phi2r = (90.0 * math.cos(50.0 * KPI / 180.0), -90.0 * math.sin(50 * KPI / 180.0), 0.0)
+pct10e1 = (-691.0 - 500.0, 174.0, 404.0)
+pct10e2 = (400.0 - 500.0, 20.9, 5.89)
+pct10e3 = (456.0 - 500.0, 13.0, -14.7)
+pct10e4 = (537.0 - 500.0, 1.67, -44.1)
+pct10e5 = (537.0, 1.67, -44.1)
+pct10e6 = (1e+03, -63.5, -213.0)
+pt10s1 = (6.454731216775542, -90.42080754048007, 100.0)
+pt10s2 = (22.65282328600368, -69.34877585931267, 76.51600623610082)
+pt10s3 = (51.28206938732319, -32.10510677306267, 35.00932544708616)
+vt10d = (0.4567090876640433, 0.5941309830320264, -0.6621368319663807)
+
+
+def _dir(a, b):
+    """TestCons.cpp:118-122: (b - a) divided by its length, component by component."""
+    a1, a2, a3 = b[0] - a[0], b[1] - a[1], b[2] - a[2]
+    am = math.sqrt(a1 * a1 + a2 * a2 + a3 * a3)
+    return (a1 / am, a2 / am, a3 / am)
+
+
+d1 = _dir(pct10e1, pct10e2)
+alex1P = (49.840299921054168, -59.39735648688918, -20.893051766050633)
+alex1V = (0.6068108874999103, 0.35615926907657169, 0.71058505603651234)
+alex2P = (127.0075852717127, -514.1050841937065, 69.47104834263656)
+alex2V = (0.1277616879490939, 0.4093610465777845, 0.9033828007202369)
+CONE_PHI_CASES = [
+    _case(f"{C}:183", CONE, CTEST10, "inside", pct10e1, None, 3, "eq"),
+    _case(f"{C}:187", CONE, CTEST10, "inside", pct10e2, None, 1, "eq"),
+    _case(f"{C}:191", CONE, CTEST10, "inside", pct10e3, None, 1, "eq"),
+    _case(f"{C}:195", CONE, CTEST10, "inside", pct10e4, None, 3, "eq"),
+    _case(f"{C}:199", CONE, CTEST10, "inside", pct10e5, None, 3, "eq"),
+    _case(f"{C}:203", CONE, CTEST10, "inside", pct10e6, None, 3, "eq"),
+    _case(f"{C}:207", CONE, CTEST10, "inside", pct10mx, None, 2, "eq"),
+    _case(f"{C}:211", CONE, CTEST10, "inside", pt10s1, None, 2, "eq"),
+    _case(f"{C}:215", CONE, CTEST10, "inside", pt10s2, None, 2, "eq"),
+    _case(f"{C}:219", CONE, CTEST10, "inside", pt10s3, None, 3, "eq"),
+    _case(f"{C}:233", CONE, C3, "inside", pplx, None, 3, "eq"),
+    _case(f"{C}:235", CONE, C4, "inside", pplx, None, 1, "eq"),
+    _case(f"{C}:245", CONE, C3, "inside", ponphi1, None, 2, "eq"),
+    _case(f"{C}:247", CONE, C3, "inside", ponphi2, None, 2, "eq"),
+    _case(f"{C}:250", CONE, C5, "inside", (70.0, 1.0, 0.0), None, 1, "eq"),
+    _case(f"{C}:253", CONE, C5, "inside", (50.0, -50.0, 0.0), None, 3, "eq"),
+    _case(f"{C}:256", CONE, C5, "inside", (70.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{C}:260", CONE, C5, "inside", (100.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{C}:263", CONE, C3, "inside", (100.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{C}:267", CONE, C5, "inside", (100.0, 0.0, 50.0), None, 2, "eq"),
+    _case(f"{C}:270", CONE, C3, "inside", (100.0, 0.0, 50.0), None, 2, "eq"),
+    _case(f"{C}:369", CONE, C4, "safe_out", ponphi1, None, 0.0, "range"),
+    _case(f"{C}:396", CONE, C5, "safe_out", (0.0, -70.0, 0.0), None, 0.0, "range"),
+    _case(f"{C}:402", CONE, C4, "dist_out", pplx, vx, 30.0, "range"),
+    _case(f"{C}:412", CONE, C4, "dist_out", pplx, vmx, 70.0, "range"),
+    _case(f"{C}:422", CONE, C3, "dist_out", ponphi1, vmy, 0.0, "range"),
+    _case(f"{C}:426", CONE, C3, "dist_out", ponphi1, vy, 2 * 60 * math.sin(KPI / 6), "range"),
+    _case(f"{C}:432", CONE, C3, "dist_out", ponphi2, vy, 0.0, "range"),
+    _case(f"{C}:437", CONE, C3, "dist_out", ponphi2, vmy, 2 * 60 * math.sin(KPI / 6), "range"),
+    _case(f"{C}:638", CONE, C4, "safe_in", pply, None, 120 * math.sin(KPI / 3), "range"),
+    _case(f"{C}:642", CONE, C4, "safe_in", (0.0, -120.0, 0.0), None, 120 * math.sin(KPI / 3), "range"),
+    _case(f"{C}:650", CONE, C5, "safe_in", pplx, None, 20.0 / math.sqrt(2.0), "range"),
+    _case(f"{C}:667", CONE, C3, "dist_in", pplz, vmz, INF, "range"),
+    _case(f"{C}:671", CONE, C4, "dist_in", pplz, vmz, INF, "range"),
+    _case(f"{C}:675", CONE, C5, "dist_in", pplz, vmz, INF, "range"),
+    _case(f"{C}:718", CONE, C3, "dist_in", pmiz, vz, INF, "range"),
+    _case(f"{C}:722", CONE, C4, "dist_in", pmiz, vz, INF, "range"),
+    _case(f"{C}:726", CONE, C5, "dist_in", pmiz, vz, INF, "range"),
+    _case(f"{C}:762", CONE, C4, "dist_in", pply, vmy, INF, "range"),
+    _case(f"{C}:769", CONE, C3, "dist_in", pydx, vmy, 150 - 60 * math.tan(KPI / 6), "range"),
+    _case(f"{C}:780", CONE, C4, "dist_in", (500.0, 0.0, 0.0), vmx, 350.0, "range"),
+    _case(f"{C}:784", CONE, C4, "dist_in", pzero, vx, 50.0, "range"),
+    _case(f"{C}:835", CONE, CTEST10, "dist_in", pct10, vx, INF, "range"),
+    _case(f"{C}:839", CONE, CTEST10, "dist_in", pct10, vmx, 110.0, "range"),
+    _case(f"{C}:843", CONE, CTEST10, "dist_in", pct10, vy, 10.57961, "range"),
+    _case(f"{C}:847", CONE, CTEST10, "dist_in", pct10, vmy, 71.5052, "range"),
+    _case(f"{C}:851", CONE, CTEST10, "dist_in", pct10, vz, INF, "range"),
+    _case(f"{C}:855", CONE, CTEST10, "dist_in", pct10phi1, vx, INF, "range"),
+    _case(f"{C}:859", CONE, CTEST10, "dist_in", pct10phi1, vmx, 0.0, "range"),
+    _case(f"{C}:863", CONE, CTEST10, "dist_in", pct10phi1, vy, 0.0, "range"),
+    _case(f"{C}:867", CONE, CTEST10, "dist_in", pct10phi1, vmy, 80.83778, "range"),
+    _case(f"{C}:871", CONE, CTEST10, "dist_in", pct10phi1, vz, INF, "range"),
+    _case(f"{C}:875", CONE, CTEST10, "dist_in", pct10phi1, vmz, INF, "range"),
+    _case(f"{C}:879", CONE, CTEST10, "dist_in", pct10phi2, vx, INF, "range"),
+    _case(f"{C}:883", CONE, CTEST10, "dist_in", pct10phi2, vmx, 0.0, "range"),
+    _case(f"{C}:887", CONE, CTEST10, "dist_in", pct10phi2, vy, 77.78352, "range"),
+    _case(f"{C}:891", CONE, CTEST10, "dist_in", pct10phi2, vmy, 0.0, "range"),
+    _case(f"{C}:895", CONE, CTEST10, "dist_in", pct10phi2, vz, INF, "range"),
+    _case(f"{C}:899", CONE, CTEST10, "dist_in", pct10phi2, vmz, INF, "range"),
+    _case(f"{C}:903", CONE, CTEST10, "dist_in", pct10mx, vx, INF, "range"),
+    _case(f"{C}:907", CONE, CTEST10, "dist_in", pct10mx, vmx, 0.0, "range"),
+    _case(f"{C}:911", CONE, CTEST10, "dist_in", pct10mx, vy, INF, "range"),
+    _case(f"{C}:915", CONE, CTEST10, "dist_in", pct10mx, vmy, INF, "range"),
+    _case(f"{C}:919", CONE, CTEST10, "dist_in", pct10mx, vz, INF, "range"),
+    _case(f"{C}:923", CONE, CTEST10, "dist_in", pct10mx, vmz, 0.0, "range"),
+    _case(f"{C}:927", CONE, CTEST10, "dist_in", pct10e1, d1, 1171.1712, "range"),
+    _case(f"{C}:931", CONE, CTEST10, "dist_in", pct10e4, d1, INF, "range"),
+    _case(f"{C}:935", CONE, CTEST10, "dist_in", pt10s2, vt10d, 142.8017, "range"),
+    _case(f"{C}:946", CONE, CTEST10, "dist_in", pct10phi1r, vmy, INF, "range"),
+    _case(f"{C}:950", CONE, CTEST10, "dist_in", pct10phi2r, vx, INF, "range"),
+    _case(f"{C}:961", CONE, CTEST10, "dist_in", alex1P, alex1V, INF, "range"),
+    _case(f"{C}:965", CONE, CTEST10, "dist_out", alex1P, alex1V, 0.0, "range"),
+    _case(f"{C}:973", CONE, CTEST10, "inside", alex2P, None, 3, "eq"),
+    _case(f"{C}:977", CONE, CTEST10, "dist_in", alex2P, alex2V, INF, "range"),
+]
+CONE_CASES += CONE_PHI_CASES
+
 TRD = 3
 TD = "test/unit_tests/TestTrd.cpp"
 TRD1 = (20.0, 20.0, 30.0, 30.0, 40.0)  # TestTrd.cpp:51 trd1 (x1, x2, y1, y2, z)

@@ -274,6 +274,10 @@ SHAPE_SETS = [
     ("cone-hollow", W.CONE, (10.0, 50.0, 20.0, 40.0, 60.0, 0.0, W.K_TWO_PI)),
     ("cone-solid-apex", W.CONE, (0.0, 30.0, 0.0, 0.0, 25.0, 0.0, W.K_TWO_PI)),
     ("cone-inverted", W.CONE, (5.0, 10.0, 20.0, 45.0, 30.0, 0.0, W.K_TWO_PI)),
+    ("cone-sector-60deg-negative-start", W.CONE, KA.C4),
+    ("cone-sector-270deg", W.CONE, KA.C5),
+    ("cone-sector-300deg", W.CONE, KA.CTEST10),
+    ("cone-solid-half", W.CONE, (0.0, 40.0, 0.0, 20.0, 30.0, 1.0, W.K_PI)),
     ("trd-varying", W.TRD, (10.0, 30.0, 20.0, 40.0, 40.0)),
     ("trd-const-y", W.TRD, (20.0, 25.0, 30.0, 30.0, 40.0)),
     ("trd-boxlike", W.TRD, (20.0, 20.0, 30.0, 30.0, 40.0)),

@@ -64,6 +64,10 @@ def test_bvh_depth_rule(oracle):
     (W.TUBE, (0.0, 50.0, 50.0, 0.5 * W.K_PI, 0.5 * W.K_PI), (-50.0, 0.0, -50.0), (0.0, 50.0, 50.0)),
     (W.TUBE, (90.0, 110.0, 105.0, 0.0, W.K_PI), (-110.0, 0.0, -105.0), (110.0, 110.0, 105.0)),
     (W.TUBE, (50.0, 100.0, 50.0, 0.0, 1.5 * W.K_PI), (-100.0, -100.0, -50.0), (100.0, 100.0, 50.0)),
+    # UnplacedCone::Extent of phi sections (source/UnplacedCone.cpp:146-206): TestCons.cpp c5
+    # (three quarters) and a quarter-section cone
+    (W.CONE, (25.0, 50.0, 75.0, 150.0, 50.0, 0.0, 1.5 * W.K_PI), (-150.0, -150.0, -50.0), (150.0, 150.0, 50.0)),
+    (W.CONE, (10.0, 30.0, 20.0, 60.0, 40.0, 0.5 * W.K_PI, 0.5 * W.K_PI), (-60.0, 0.0, -40.0), (0.0, 60.0, 40.0)),
     # TestSphere.cpp:63-68 (b1: rmax 3)
     (W.SPHERE, (0.0, 3.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI), (-3.0, -3.0, -3.0), (3.0, 3.0, 3.0)),
     # TestPolycone.cpp:329-333 ("SimpleTube+Cone")

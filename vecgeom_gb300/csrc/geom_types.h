@@ -151,7 +151,9 @@ enum { ConeRmin1 = 0, ConeRmax1, ConeRmin2, ConeRmax2, ConeDz, ConeOrigRmax1, Co
        ConeOuterSlope, ConeInnerOffset, ConeOuterOffset, ConeInnerTol, ConeOuterTol, ConeSqRmin1, ConeSqRmin2,
        ConeSqRmax1, ConeSqRmax2, ConeTolIz, ConeInnerApex, ConeTanInnerApex, ConeOuterApex, ConeTanOuterApex,
        ConeSecRMin, ConeSecRMax, ConeInvSecRMin, ConeInvSecRMax, ConeTanRMin, ConeTanRMax, ConeZNormInner,
-       ConeZNormOuter, ConeArgRmax1, ConeArgRmax2, kConeSize };
+       ConeZNormOuter, ConeArgRmax1, ConeArgRmax2, ConeArgRmin1, ConeArgRmin2,
+       // checked fSPhi, fDPhi and fAlongPhi1/2 (ConeStruct::SetAndCheck*PhiAngle), then fPhiWedge
+       ConeSPhi, ConeDPhi, ConeAP1x, ConeAP1y, ConeAP2x, ConeAP2y, ConeWedge, kConeSize = ConeWedge + 9 };
 // Trd (UniversalTrd): TrdStruct members and cached values; padded to 16 doubles
 enum { TrdDx1 = 0, TrdDx2, TrdDy1, TrdDy2, TrdDz, TrdX2minusX1, TrdY2minusY1, TrdHalfX1plusX2, TrdHalfY1plusY2,
        TrdCalfX, TrdCalfY, TrdTolX, TrdTolY, TrdFx, TrdFy, TrdPad, kTrdSize };

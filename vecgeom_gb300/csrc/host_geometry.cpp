@@ -503,6 +503,7 @@ static int build_isin_row(int shape, const double *r, std::vector<float> &out)
     v = {r[row::TubeZ], r[row::TubeRmax], r[row::TubeRmin], r[row::TubeRmin] > 0 ? 1. : 0.};
     break;
   case kCone: {  // ConeImplementation.h:368-432, ConeUtilities.h cone radius / safety to the conical surface
+    if (r[row::ConeDPhi] < 2. * 3.14159265358979323846) return -1;  // a phi section is evaluated in FP64
     v.assign(irow::kConeRow, 0.);
     v[irow::ConeDz]           = r[row::ConeDz];
     v[irow::ConeMinusConeTol] = -kConeTolerance;

@@ -110,19 +110,38 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
   }
   case kCone: {
     // ConeStruct(rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi) + CalculateCached (ConeStruct.h:79-157, 414-426)
-    if (p[6] < kTwoPi - 0.5 * kAngTolerance) {
-      err = "cone phi sections are not supported";
-      return VGN_ERR_UNSUPPORTED;
-    }
     double rmin1 = p[0] < 0.0 ? 0.0 : p[0], rmax1 = p[1], rmin2 = p[2] < 0.0 ? 0.0 : p[2], rmax2 = p[3];
-    const double dz = p[4];
-    if (!(dz > 0 && rmax1 >= rmin1 && rmax2 >= rmin2 && (rmax1 > 0 || rmax2 > 0))) {
-      err = "cone needs dz > 0 and rmax >= rmin at both ends";
+    const double dz = p[4], sphi = p[5], dphi = p[6];
+    if (!(dz > 0 && rmax1 >= rmin1 && rmax2 >= rmin2 && (rmax1 > 0 || rmax2 > 0) && dphi > 0)) {
+      err = "cone needs dz > 0, rmax >= rmin at both ends and dphi > 0";
       return VGN_ERR_ARG;
     }
     double r[row::kConeSize];
     r[row::ConeArgRmax1]  = p[1];
     r[row::ConeArgRmax2]  = p[3];
+    r[row::ConeArgRmin1]  = p[0];
+    r[row::ConeArgRmin2]  = p[2];
+    // fPhiWedge(_dphi, _sphi), then SetAndCheckDPhiAngle(_dphi) and SetAndCheckSPhiAngle(_sphi)
+    // (ConeStruct.h:321-360, 413-425): the wedge keeps the raw angles' vectors and takes the
+    // checked delta; the along vectors use the checked angles
+    wedge_fill(r + row::ConeWedge, dphi, sphi);
+    double cdphi = dphi, csphi = sphi;
+    if (dphi >= kTwoPi - 0.5 * kAngTolerance) {
+      cdphi = kTwoPi;
+      csphi = 0;
+    }
+    r[row::ConeWedge + row::WedgeDPhi] = cdphi;
+    if (sphi < 0)
+      csphi = kTwoPi - std::fmod(std::fabs(sphi), kTwoPi);
+    else
+      csphi = std::fmod(sphi, kTwoPi);
+    if (csphi + cdphi > kTwoPi) csphi -= kTwoPi;
+    r[row::ConeSPhi] = csphi;
+    r[row::ConeDPhi] = cdphi;
+    r[row::ConeAP1x] = std::cos(csphi);
+    r[row::ConeAP1y] = std::sin(csphi);
+    r[row::ConeAP2x] = std::cos(csphi + cdphi);
+    r[row::ConeAP2y] = std::sin(csphi + cdphi);
     r[row::ConeOrigRmax1] = rmax1;
     r[row::ConeOrigRmax2] = rmax2;
     if (rmin1 == rmax1) rmax1 += kConeTolerance;
@@ -390,10 +409,40 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mn.y = temp < mn.y ? temp : mn.y;
     return;
   }
-  case kCone: {  // UnplacedCone::Extent, full phi (source/UnplacedCone.cpp:149-165)
-    const double m = r[row::ConeArgRmax1] > r[row::ConeArgRmax2] ? r[row::ConeArgRmax1] : r[row::ConeArgRmax2];
-    mn = {-m, -m, -r[row::ConeDz]};
-    mx = {m, m, r[row::ConeDz]};
+  case kCone: {  // UnplacedCone::Extent (source/UnplacedCone.cpp:146-206, the phi-aware definition)
+    const double max = r[row::ConeArgRmax1] > r[row::ConeArgRmax2] ? r[row::ConeArgRmax1] : r[row::ConeArgRmax2];
+    const double min = r[row::ConeArgRmin1] > r[row::ConeArgRmin2] ? r[row::ConeArgRmin2] : r[row::ConeArgRmin1];
+    const double sphi = r[row::ConeSPhi], dphi = r[row::ConeDPhi];
+    const double *w = r + row::ConeWedge;
+    mn = {-max, -max, -r[row::ConeDz]};
+    mx = {max, max, r[row::ConeDz]};
+    if (dphi == kTwoPi) return;
+    const double Rin     = 0.5 * (max + min);
+    const bool phi0out   = !wedge_contains(w, Rin, 0);
+    const bool phi90out  = !wedge_contains(w, 0, Rin);
+    const bool phi180out = !wedge_contains(w, -Rin, 0);
+    const bool phi270out = !wedge_contains(w, 0, -Rin);
+    if (!(phi0out || phi90out || phi180out || phi270out)) return;
+    auto vmax = [](double a, double b) { return a > b ? a : b; };
+    auto vmin = [](double a, double b) { return a < b ? a : b; };
+    const double Cx = max * std::cos(sphi), Dx = max * std::cos(sphi + dphi);
+    const double Cy = max * std::sin(sphi), Dy = max * std::sin(sphi + dphi);
+    if (phi0out) mx.x = vmax(Cx, Dx);
+    if (phi90out) mx.y = vmax(Cy, Dy);
+    if (phi180out) mn.x = vmin(Cx, Dx);
+    if (phi270out) mn.y = vmin(Cy, Dy);
+    if (dphi >= kPi) return;
+    const double Ax = min * std::cos(sphi), Bx = min * std::cos(sphi + dphi);
+    const double Ay = min * std::sin(sphi), By = min * std::sin(sphi + dphi);
+    double temp;
+    temp = vmax(Ax, Bx);
+    mx.x = temp > mx.x ? temp : mx.x;
+    temp = vmax(Ay, By);
+    mx.y = temp > mx.y ? temp : mx.y;
+    temp = vmin(Ax, Bx);
+    mn.x = temp < mn.x ? temp : mn.x;
+    temp = vmin(Ay, By);
+    mn.y = temp < mn.y ? temp : mn.y;
     return;
   }
   case kTrd: {  // UnplacedTrd::Extent (UnplacedTrd.h:218-222)

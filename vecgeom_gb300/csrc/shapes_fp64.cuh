@@ -114,6 +114,16 @@ __device__ __forceinline__ void wedge_ci(const double *w, D3 p, bool &cin, bool 
   }
 }
 
+// Wedge::SafetyToIn (Wedge_Evolution.h:374-391)
+__device__ __forceinline__ double wedge_safe_in(const double *w, D3 p)
+{
+  const double dist1 = p.x * w[row::WedgeN1x] + p.y * w[row::WedgeN1y];
+  const double dist2 = p.x * w[row::WedgeN2x] + p.y * w[row::WedgeN2y];
+  const double m1 = -1 * dist1, m2 = -1 * dist2;
+  if (w[row::WedgeDPhi] < kPiD) return m1 > m2 ? m1 : m2;
+  return m1 < m2 ? m1 : m2;
+}
+
 // Wedge::SafetyToOut (Wedge_Evolution.h:356-372)
 __device__ __forceinline__ double wedge_safe_out(const double *w, D3 p)
 {
@@ -185,6 +195,25 @@ __device__ __forceinline__ void tube_phi_plane(const double *t, double alongX, d
     const double hity = pos.y + dist * dir.y;
     ok                = ok && (hitx * alongX + hity * alongY) >= 0.;
   }
+}
+
+// The two phi-plane candidates that end DistanceToIn (`in`, TubeImplementation.h:656-679) and
+// DistanceToOut (790-821) of a tube section.  The sector type of UniversalTube is unknown at
+// compile time, so both planes are checked, with the positive-direction test.  In both kernels
+// the first plane's candidate is taken when it is below the distance so far, then the second's
+// when it is below that; out of line, since only phi sections take it.
+__device__ __noinline__ double tube_phi_planes(const double *t, D3 p, D3 d, double distance, bool in)
+{
+  const double *w = t + tb::TubeWedge;
+  double dist_phi;
+  bool ok_phi;
+  tube_phi_plane(t, w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p, d, true, in,
+                 dist_phi, ok_phi);
+  if (ok_phi && dist_phi < distance) distance = dist_phi;
+  tube_phi_plane(t, w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p, d, true, in,
+                 dist_phi, ok_phi);
+  if (ok_phi && dist_phi < distance) distance = dist_phi;
+  return distance;
 }
 
 // PhiPlaneSafety<inside = false> (TubeImplementation.h:210-247), UniversalTube
@@ -263,19 +292,7 @@ __device__ __forceinline__ double tube_dist_in_kernel(const double *t, D3 p, D3 
     ok_rmin &= dist_rmin < distance;
     if (!done && ok_rmin) distance = dist_rmin;
   }
-  if (hasphi) {  // sector type unknown at compile time: both planes, positive-direction check
-    const double *w = t + tb::TubeWedge;
-    double dist_phi;
-    bool ok_phi;
-    tube_phi_plane(t, w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p, d, true, true,
-                   dist_phi, ok_phi);
-    ok_phi &= dist_phi < distance;
-    if (!done && ok_phi) distance = dist_phi;
-    done |= ok_phi;
-    tube_phi_plane(t, w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p, d, true, true,
-                   dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
-  }
+  if (hasphi) distance = tube_phi_planes(t, p, d, distance, true);
   return distance;
 }
 
@@ -336,17 +353,7 @@ __device__ __forceinline__ double tube_dist_out(const double *t, D3 p, D3 d)
   crmax *= invnsq;
   tube_circle(t, b, crmax, p, d, true, false, dist_rmax, ok_rmax);
   if (ok_rmax && dist_rmax < distance) distance = dist_rmax;
-  if (hasphi) {  // angle bigger than pi or unknown: positive-direction check on both planes
-    const double *w = t + tb::TubeWedge;
-    double dist_phi;
-    bool ok_phi;
-    tube_phi_plane(t, w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p, d, true, false,
-                   dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
-    tube_phi_plane(t, w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p, d, true, false,
-                   dist_phi, ok_phi);
-    if (ok_phi && dist_phi < distance) distance = dist_phi;
-  }
+  if (hasphi) distance = tube_phi_planes(t, p, d, distance, false);
   return distance;
 }
 
@@ -433,8 +440,9 @@ __device__ __forceinline__ int tube_inside(const double *t, D3 p)
   return r;
 }
 
-// ---------------------------------------------------------------- Cone (full phi)
-// kernel/ConeImplementation.h:117-516, ConeUtilities.h:116-813; row layout vgn::row::Cone*
+// ---------------------------------------------------------------- Cone
+// kernel/ConeImplementation.h:117-516, ConeUtilities.h:64-813 (the scalar ConeHelpers<double>
+// specialisation); UniversalCone: rmin and phi treatment at run time; row layout vgn::row::Cone*
 constexpr double kConeTolerance = 1e-7;
 
 // MakePlus/MinusTolerantSquare<true> (kernel/GenericKernels.h:65-82)
@@ -451,6 +459,68 @@ __device__ __forceinline__ double cone_radius(const double *c, double z, bool in
                                                     : c[row::ConeInnerSlope] * z + c[row::ConeInnerOffset];
   return c[row::ConeOrigRmax1] == c[row::ConeOrigRmax2] ? c[row::ConeOrigRmax1]
                                                           : c[row::ConeOuterSlope] * z + c[row::ConeOuterOffset];
+}
+
+__device__ __forceinline__ bool cone_has_phi(const double *c) { return c[row::ConeDPhi] < 2. * kPiD; }
+
+// PointInCyclicalSector<..., onSurfaceT = false> (ConeUtilities.h:64-114); "smaller than pi"
+// is dphi <= M_PI, decided at run time
+__device__ __forceinline__ bool cone_in_sector(const double *c, double x, double y, bool includeSurface)
+{
+  const double startCheck = (-x * c[row::ConeAP1y]) + (y * c[row::ConeAP1x]);
+  const double endCheck   = (-c[row::ConeAP2x] * y) + (c[row::ConeAP2y] * x);
+  const double tol        = includeSurface ? -kConeTolerance : kConeTolerance;
+  if (c[row::ConeDPhi] <= kPiD) return (startCheck >= tol) && (endCheck >= tol);
+  return (startCheck >= tol) || (endCheck >= tol);
+}
+
+// PhiPlaneTrajectoryIntersection (ConeUtilities.h:155-204)
+__device__ __forceinline__ void cone_phi_plane(const double *c, double alongX, double alongY, double normalX,
+                                               double normalY, D3 pos, D3 dir, bool posdir, bool insector,
+                                               double &dist, bool &ok)
+{
+  dist = kInfLength;
+  if (insector)
+    ok = ((dir.x * normalX) + (dir.y * normalY) > 0.);
+  else
+    ok = ((dir.x * normalX) + (dir.y * normalY) < 0.);
+  const double dirDotXY = (dir.y * alongX) - (dir.x * alongY);
+  if (dirDotXY != 0) dist = ((alongY * pos.x) - (alongX * pos.y)) / nonzero(dirDotXY);
+  ok &= dist > -kConeTolerance;
+  if (insector) {
+    const double hitx          = pos.x + dist * dir.x;
+    const double hity          = pos.y + dist * dir.y;
+    const double hitz          = pos.z + dist * dir.z;
+    const double r2            = (hitx * hitx) + (hity * hity);
+    const double innerRadIrTol = cone_radius(c, hitz, true) + kTolerance;
+    const double outerRadIrTol = cone_radius(c, hitz, false) - kTolerance;
+    ok &= fabs(hitz) <= c[row::ConeTolIz] && (r2 >= innerRadIrTol * innerRadIrTol) &&
+          (r2 <= outerRadIrTol * outerRadIrTol);
+    if (posdir) ok = ok && ((hitx * alongX) + (hity * alongY)) > 0.;
+  } else if (posdir) {
+    const double hitx = pos.x + dist * dir.x;
+    const double hity = pos.y + dist * dir.y;
+    ok                = ok && ((hitx * alongX) + (hity * alongY)) >= 0.;
+  }
+}
+
+// The two phi-plane candidates that end DistanceToIn (`in`, ConeImplementation.h:233-254) and
+// DistanceToOut (336-364) of a cone section: the sector type of UniversalCone is unknown at
+// compile time, so both planes are checked, with the positive-direction test; the first
+// plane's candidate is taken when below the distance so far, then the second's when below
+// that.  Out of line, since only phi sections take it.
+__device__ __noinline__ double cone_phi_planes(const double *c, D3 p, D3 d, double distance, bool in)
+{
+  const double *w = c + row::ConeWedge;
+  double dist_phi;
+  bool ok_phi;
+  cone_phi_plane(c, c[row::ConeAP1x], c[row::ConeAP1y], w[row::WedgeN1x], w[row::WedgeN1y], p, d, true, in,
+                 dist_phi, ok_phi);
+  if (ok_phi && dist_phi < distance) distance = dist_phi;
+  cone_phi_plane(c, c[row::ConeAP2x], c[row::ConeAP2y], w[row::WedgeN2x], w[row::WedgeN2y], p, d, true, in,
+                 dist_phi, ok_phi);
+  if (ok_phi && dist_phi < distance) distance = dist_phi;
+  return distance;
 }
 
 // GetNormal (ConeUtilities.h:206-238)
@@ -479,6 +549,7 @@ __device__ __forceinline__ bool cone_on_surface(const double *c, D3 p, bool inne
 }
 
 // ConeHelpers<double>::DetectIntersectionAndCalculateDistanceToConicalSurface (ConeUtilities.h:591-762)
+template <bool PHI = true>
 __device__ __forceinline__ bool cone_conical(const double *c, D3 p, D3 d, bool fordistin, bool inner, double &distance)
 {
   distance          = kInfLength;
@@ -487,7 +558,9 @@ __device__ __forceinline__ bool cone_conical(const double *c, D3 p, D3 d, bool f
   const double dn   = dot3(d, n);
   if (onsurf && fabs(dn) == 0.) return false;
   if (onsurf) {
-    if (fordistin ? (dn <= 0.) : (dn >= 0.)) {
+    bool moving = fordistin ? (dn <= 0.) : (dn >= 0.);
+    if ((PHI && cone_has_phi(c))) moving = cone_in_sector(c, p.x, p.y, true) && moving;
+    if (moving) {
       distance = 0.;
       return true;
     }
@@ -551,13 +624,23 @@ __device__ __forceinline__ bool cone_conical(const double *c, D3 p, D3 d, bool f
     }
     if (distance < 0.) return false;
   }
+  if ((PHI && cone_has_phi(c))) {
+    double hitx = 0, hity = 0;
+    if (distance < kInfLength) {
+      hitx = p.x + distance * d.x;
+      hity = p.y + distance * d.y;
+    }
+    ok &= (cone_in_sector(c, hitx, hity, true) && (distance < kInfLength));
+  }
   return ok;
 }
 
 // DistanceToIn (ConeImplementation.h:117-255)
+template <bool PHI = true>
 __device__ __forceinline__ double cone_dist_in(const double *c, D3 p, D3 d)
 {
   const bool hasrmin = cone_has_rmin(c);
+  const bool hasphi  = (PHI && cone_has_phi(c));
   const double dz    = c[row::ConeDz];
   double distance    = kInfLength;
   double distz       = fabs(p.z) - dz;
@@ -570,6 +653,7 @@ __device__ __forceinline__ double cone_dist_in(const double *c, D3 p, D3 d)
   bool inside = distz < -kConeTolerance;
   inside &= rsq < minus_tol_sq(outerRad, c[row::ConeOuterTol]);
   if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, true), c[row::ConeInnerTol]);
+  if (hasphi) inside &= cone_in_sector(c, p.x, p.y, false);
   if (inside) return -1.0;
   distance = kInfLength;
   distz /= nonzero(fabs(d.z));
@@ -584,20 +668,23 @@ __device__ __forceinline__ double cone_dist_in(const double *c, D3 p, D3 d)
     bot &= (r2 >= c[row::ConeSqRmin1] - kTolerance);
     okz &= (top || bot);
   }
+  if (hasphi) okz &= cone_in_sector(c, hitx, hity, true);
   if (okz) return distz;
   double dr;
-  bool ok = cone_conical(c, p, d, true, false, dr);
+  bool ok = cone_conical<PHI>(c, p, d, true, false, dr);
   ok &= dr < distance;
   if (ok) return dr;
   if (hasrmin) {
-    ok = cone_conical(c, p, d, true, true, dr);
+    ok = cone_conical<PHI>(c, p, d, true, true, dr);
     ok &= dr < distance;
     if (ok) distance = dr;
   }
+  if (hasphi) distance = cone_phi_planes(c, p, d, distance, true);
   return distance;
 }
 
 // DistanceToOut (ConeImplementation.h:257-366)
+template <bool PHI = true>
 __device__ __forceinline__ double cone_dist_out(const double *c, D3 p, D3 d)
 {
   const bool hasrmin = cone_has_rmin(c);
@@ -619,11 +706,22 @@ __device__ __forceinline__ double cone_dist_out(const double *c, D3 p, D3 d)
   if (up) distance = (dz - p.z) * dirZInv;
   if (down) distance = (-dz - p.z) * dirZInv;
   double dr;
-  bool ok = cone_conical(c, p, d, false, false, dr);
+  bool ok = cone_conical<PHI>(c, p, d, false, false, dr);
   if (ok && dr < distance) distance = dr;
   if (hasrmin) {
-    ok = cone_conical(c, p, d, false, true, dr);
+    ok = cone_conical<PHI>(c, p, d, false, true, dr);
     if (ok && dr < distance) distance = dr;
+  }
+  if ((PHI && cone_has_phi(c))) {
+    // the outside test's phi part (ConeImplementation.h:293-297) only runs where the point is
+    // already outside, so it never changes the result of the scalar kernel
+    const double *w    = c + row::ConeWedge;
+    const bool onStart = wedge_on_surface(w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x], w[row::WedgeN1y], p);
+    const bool onEnd   = wedge_on_surface(w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x], w[row::WedgeN2y], p);
+    if ((onStart && (d.x * -w[row::WedgeN1x] + d.y * -w[row::WedgeN1y] + d.z * -0.) > 0.) ||
+        (onEnd && (d.x * -w[row::WedgeN2x] + d.y * -w[row::WedgeN2y] + d.z * -0.) > 0.))
+      return 0.;
+    distance = cone_phi_planes(c, p, d, distance, false);
   }
   if (distance < 0. && fabs(distance) < kTolerance) distance = 0.;
   return distance;
@@ -642,6 +740,7 @@ __device__ __forceinline__ double cone_safe_surface(const double *c, D3 p, bool 
 }
 
 // SafetyToIn (ConeImplementation.h:368-432)
+template <bool PHI = true>
 __device__ __forceinline__ double cone_safe_in(const double *c, D3 p)
 {
   const bool hasrmin = cone_has_rmin(c);
@@ -650,16 +749,19 @@ __device__ __forceinline__ double cone_safe_in(const double *c, D3 p)
   bool inside        = distz < -kConeTolerance;
   inside &= rsq < minus_tol_sq(cone_radius(c, p.z, false), c[row::ConeOuterTol]);
   if (hasrmin) inside &= rsq > plus_tol_sq(cone_radius(c, p.z, true), c[row::ConeInnerTol]);
+  if ((PHI && cone_has_phi(c)) && inside) inside &= cone_in_sector(c, p.x, p.y, false);
   if (inside) return -1.0;
   const double safeZ = fabs(p.z) - c[row::ConeDz];
   const double so    = -cone_safe_surface(c, p, false);
   const double si    = hasrmin ? -cone_safe_surface(c, p, true) : -kInfLength;
   double safety      = vmax(safeZ, vmax(so, si));
+  if ((PHI && cone_has_phi(c))) safety = vmax(wedge_safe_in(c + row::ConeWedge, p), safety);
   if (fabs(safety) < kTolerance) safety = 0.;
   return safety;
 }
 
 // SafetyToOut (ConeImplementation.h:434-499)
+template <bool PHI = true>
 __device__ __forceinline__ double cone_safe_out(const double *c, D3 p)
 {
   const bool hasrmin = cone_has_rmin(c);
@@ -673,11 +775,13 @@ __device__ __forceinline__ double cone_safe_out(const double *c, D3 p)
   const double so    = cone_safe_surface(c, p, false);
   const double si    = hasrmin ? cone_safe_surface(c, p, true) : kInfLength;
   double safety      = vmin(safeZ, vmin(so, si));
+  if ((PHI && cone_has_phi(c))) safety = vmin(wedge_safe_out(c + row::ConeWedge, p), safety);
   if (fabs(safety) < kTolerance) safety = 0.;
   return safety;
 }
 
 // ConeHelpers<double>::GenericKernelForContainsAndInside (ConeUtilities.h:764-813)
+template <bool PHI = true>
 __device__ __forceinline__ void cone_generic_ci(const double *c, D3 p, bool forinside, bool &cin, bool &cout)
 {
   const double dz = c[row::ConeDz], absz = fabs(p.z);
@@ -695,20 +799,32 @@ __device__ __forceinline__ void cone_generic_ci(const double *c, D3 p, bool fori
     const double rmin = c[row::ConeInnerSlope] * p.z + c[row::ConeInnerOffset];
     cout |= r2 <= (forinside ? minus_tol_sq(rmin, c[row::ConeInnerTol]) : rmin * rmin);
     if (forinside) cin &= r2 > plus_tol_sq(rmin, c[row::ConeInnerTol]);
+    if (cout) return;
+  }
+  if ((PHI && cone_has_phi(c))) {
+    bool cinphi = false, coutphi = false;
+    if (forinside)
+      wedge_ci<true>(c + row::ConeWedge, p, cinphi, coutphi);
+    else
+      wedge_ci<false>(c + row::ConeWedge, p, cinphi, coutphi);
+    cout |= coutphi;
+    if (forinside) cin &= cinphi;
   }
 }
 
+template <bool PHI = true>
 __device__ __forceinline__ bool cone_contains(const double *c, D3 p)
 {
   bool cin = false, cout = false;
-  cone_generic_ci(c, p, false, cin, cout);
+  cone_generic_ci<PHI>(c, p, false, cin, cout);
   return !cout;
 }
 
+template <bool PHI = true>
 __device__ __forceinline__ int cone_inside(const double *c, D3 p)
 {
   bool cin = false, cout = false;
-  cone_generic_ci(c, p, true, cin, cout);
+  cone_generic_ci<PHI>(c, p, true, cin, cout);
   int r = kSurfaceE;
   if (cout) r = kOutsideE;
   if (cin) r = kInsideE;
@@ -1250,7 +1366,7 @@ __device__ __forceinline__ void pcon_section_ci(const double *t, int n, int k, D
     cout = true;
     return;
   }
-  cone_generic_ci(pcon_sec(t, n, k), pcon_local(t, n, k, p), forInside, cin, cout);
+  cone_generic_ci<false>(pcon_sec(t, n, k), pcon_local(t, n, k, p), forInside, cin, cout);
 }
 
 // GenericKernelForContainsAndInside (PolyconeImplementation.h:127-187); cin/cout keep the
@@ -1316,7 +1432,7 @@ __device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
   if (index == -1) index = 0;
   if (index == -2) index = n - 1;
   do {
-    distance = cone_dist_in(pcon_sec(t, n, index), pcon_local(t, n, index, p), v);
+    distance = cone_dist_in<false>(pcon_sec(t, n, index), pcon_local(t, n, index, p), v);
     if (distance < kInfLength || !increment) break;
     index += increment;
   } while (index >= 0 && index < n);
@@ -1327,7 +1443,7 @@ __device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
 __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 dir)
 {
   const int n = pcon_n(t);
-  if (n == 1) return cone_dist_out(pcon_sec(t, n, 0), pcon_local(t, n, 0, point), dir);
+  if (n == 1) return cone_dist_out<false>(pcon_sec(t, n, 0), pcon_local(t, n, 0, point), dir);
   const int lo = pcon_section_index(t, n, point.z - kTolerance);
   const int hi = pcon_section_index(t, n, point.z + kTolerance);
   int index    = 0;
@@ -1335,15 +1451,15 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
     return -1;
   } else if (lo < 0 && hi >= 0) {
     index = hi;
-    if (cone_inside(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
+    if (cone_inside<false>(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
   } else if (lo != hi && lo >= 0) {
-    index = cone_inside(pcon_sec(t, n, lo), pcon_local(t, n, lo, point)) == kOutsideE ? hi : lo;
+    index = cone_inside<false>(pcon_sec(t, n, lo), pcon_local(t, n, lo, point)) == kOutsideE ? hi : lo;
   } else {
     index = lo;
     if (index < 0) index = pcon_section_index(t, n, point.z);
   }
   if (index < 0) return 0.;
-  if (cone_inside(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
+  if (cone_inside<false>(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
   double totalDistance = 0.;
   int increment        = (dir.z > 0) ? 1 : -1;
   if (fabs(dir.z) < kTolerance) increment = 0;
@@ -1354,12 +1470,12 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
     if ((totalDistance != 0) || (istep < 2)) {
       pn = d3(point.x + totalDistance * dir.x, point.y + totalDistance * dir.y, point.z + totalDistance * dir.z);
       pn.z -= shift;
-      if (cone_inside(pcon_sec(t, n, index), pn) == kOutsideE) break;
+      if (cone_inside<false>(pcon_sec(t, n, index), pn) == kOutsideE) break;
     } else {
       pn.z -= shift;
     }
     istep++;
-    const double dist = cone_dist_out(pcon_sec(t, n, index), pn, dir);
+    const double dist = cone_dist_out<false>(pcon_sec(t, n, index), pn, dir);
     if (dist == -1) return kInfLength;
     if (fabs(dist) < 0.5 * kTolerance) {
       int index1 = index;
@@ -1372,7 +1488,7 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
       const double td = totalDistance + dist;
       D3 pte          = d3(point.x + td * dir.x, point.y + td * dir.y, point.z + td * dir.z);
       pte.z -= t[row::pcon_shift(n) + index1];
-      if (cone_inside(pcon_sec(t, n, index1), pte) == kOutsideE || (increment == 0)) break;
+      if (cone_inside<false>(pcon_sec(t, n, index1), pte) == kOutsideE || (increment == 0)) break;
     }
     totalDistance += dist;
     index += increment;
@@ -1387,14 +1503,14 @@ __device__ __forceinline__ double pcon_scan_neighbours(const double *t, int n, i
   double zbase     = zs[index + 1];
   for (int i = index + 1; i < n; ++i) {
     if (zs[i] - zbase >= minSafety) break;
-    const double s = cone_safe_in(pcon_sec(t, n, i), pcon_local(t, n, i, p));
+    const double s = cone_safe_in<false>(pcon_sec(t, n, i), pcon_local(t, n, i, p));
     if (s < minSafety) minSafety = s;
   }
   if (index > 0) {
     zbase = zs[index - 1];
     for (int i = index - 1; i >= 0; --i) {
       if (zbase - zs[i] >= minSafety) break;
-      const double s = cone_safe_in(pcon_sec(t, n, i), pcon_local(t, n, i, p));
+      const double s = cone_safe_in<false>(pcon_sec(t, n, i), pcon_local(t, n, i, p));
       if (s < minSafety) minSafety = s;
     }
   }
@@ -1412,7 +1528,7 @@ __device__ __forceinline__ double pcon_safe_in(const double *t, D3 p)
     if (index == -1) index = 0;
     if (index == -2) index = n - 1;
   }
-  const double safety = cone_safe_in(pcon_sec(t, n, index), pcon_local(t, n, index, p));
+  const double safety = cone_safe_in<false>(pcon_sec(t, n, index), pcon_local(t, n, index, p));
   if (needZ || safety < kTolerance) return safety;
   return pcon_scan_neighbours(t, n, index, p, safety);
 }
@@ -1426,7 +1542,7 @@ __device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
   const int n     = pcon_n(t);
   const int index = pcon_section_index(t, n, p.z);
   if (index < 0) return -1;
-  const double minSafety = cone_safe_out(pcon_sec(t, n, index), pcon_local(t, n, index, p));
+  const double minSafety = cone_safe_out<false>(pcon_sec(t, n, index), pcon_local(t, n, index, p));
   if (minSafety == kInfLength) return 0.;
   if (minSafety < kTolerance) return 0.;
   return pcon_scan_neighbours(t, n, index, p, minSafety);

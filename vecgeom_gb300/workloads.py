@@ -318,7 +318,8 @@ MIXED_JITTER = 5.0
 def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = False):
     """Parameters with every length drawn from U[5, 60] mm (Tube radii from U[5, 40] mm),
     and the half-extent of the shape's full (unsectioned) bounding box.  With `sections`,
-    three quarters of the tubes are phi sections (start U[0, 2 pi), width U[0.2, 2 pi - 0.2])."""
+    three quarters of the tubes and cones are phi sections (width U[0.2, 2 pi - 0.2], start
+    U[0, 2 pi) for tubes and U[-pi, 2 pi) for cones, whose start angle the reference folds)."""
     u = lambda lo=5.0, hi=60.0: float(rng.uniform(lo, hi))
     if shape == BOX:
         p = (u(), u(), u())
@@ -338,7 +339,10 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
         rmin1 = 0.0 if solid else float(rng.uniform(0.0, 0.8)) * rmax1
         rmin2 = 0.0 if solid else float(rng.uniform(0.0, 0.8)) * rmax2
         r = max(rmax1, rmax2)
-        return (rmin1, rmax1, rmin2, rmax2, dz, 0.0, K_TWO_PI), np.array([r, r, dz])
+        sphi, dphi = 0.0, K_TWO_PI
+        if sections and rng.uniform() < 0.75:
+            sphi, dphi = float(rng.uniform(-K_PI, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+        return (rmin1, rmax1, rmin2, rmax2, dz, sphi, dphi), np.array([r, r, dz])
     if shape == TRD:
         x1, x2, y1, dz = u(), u(), u(), u()
         y2 = y1 if rng.uniform() < 0.25 else u()  # a quarter keep y constant (the reference's Trd1 case)
@@ -402,7 +406,7 @@ def mixed_shape_geometry(seed: int = 21, grid=MIXED_GRID, world: float = MIXED_W
     rotated by a uniform random rotation (Euler angles phi, psi ~ U[0, 360),
     cos(theta) ~ U[-1, 1]).  A daughter whose bounding sphere (plus the jitter)
     would leave its cell is scaled down to fit, so daughters never overlap.  `sections`
-    makes most tubes phi sections (see _mixed_shape_params)."""
+    makes most tubes and cones phi sections (see _mixed_shape_params)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     nx, ny, nz = grid
     pitch = np.array([2 * world / nx, 2 * world / ny, 2 * world / nz])
