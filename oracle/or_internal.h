@@ -130,8 +130,9 @@ typedef struct { /* SphereStruct.h:21-51, full phi and full theta */
   double tsTheta, teTheta, tanSTheta, tanETheta;
 } or_sphere;
 
-typedef struct { /* PolyconeStruct.h:24-37: z planes and one full-phi ConeStruct per section */
+typedef struct { /* PolyconeStruct.h:24-37: z planes and one ConeStruct per section */
   int nsec;
+  double startPhi, deltaPhi; /* fStartPhi, fDeltaPhi after PolyconeStruct::Init */
   double *zs;    /* [nsec + 1] fZs */
   double *shift; /* [nsec] PolyconeSection::fShift */
   or_cone *sec;  /* [nsec] PolyconeSection::fSolid */

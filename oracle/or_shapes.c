@@ -1754,10 +1754,15 @@ static int polycone_init(or_polycone *t, const double *a, char *err, int errlen)
     rin[i]  = rev ? rin0[nz - 1 - i] : rin0[i];
     rout[i] = rev ? rout0[nz - 1 - i] : rout0[i];
   }
-  if (!(dphi >= kTwoPi - 0.5 * kAngTolerance)) {
-    free(z);
-    set_err(err, errlen, "Polycone: phi sections are not supported");
-    return -2;
+  /* SetAndCheckDPhiAngle, SetAndCheckSPhiAngle and the override that follows them
+   * (PolyconeStruct.h:152-184, 355-390): the sections' cones take the raw angles */
+  t->deltaPhi = dphi >= kTwoPi - 0.5 * kAngTolerance ? kTwoPi : dphi;
+  t->startPhi = 0;
+  if (dphi <= 0. || dphi > kTwoPi - kTolerance) {
+    t->deltaPhi = kTwoPi;
+  } else {
+    t->startPhi = sphi;
+    while (t->startPhi < 0) t->startPhi += kTwoPi;
   }
   for (i = 0; i < nz; ++i) {
     if (!(rin[i] >= 0 && rout[i] >= rin[i]) || (i > 0 && !(z[i] >= z[i - 1]))) {
@@ -2027,8 +2032,9 @@ static double polycone_safe_out(const or_polycone *t, v3 p)
   return minSafety;
 }
 
-/* UnplacedPolycone::Extent, full phi (source/UnplacedPolycone.cpp:865-900): z from the
- * end planes, x/y from a cone (minR, maxR, minR, maxR) over the sections' constructor radii */
+/* UnplacedPolycone::Extent (source/UnplacedPolycone.cpp:865-902): z from the end planes,
+ * x/y from Cone(minR, maxR, minR, maxR, 1, fStartPhi, fDeltaPhi) over the sections'
+ * constructor radii */
 static void polycone_extent(const or_polycone *t, v3 *mn, v3 *mx)
 {
   double maxR = 0, minR = kInfLength;
@@ -2046,7 +2052,7 @@ static void polycone_extent(const or_polycone *t, v3 *mn, v3 *mx)
     maxz = t->zs[t->nsec];
   }
   or_cone tmp;
-  double cpar[7] = {minR, maxR, minR, maxR, 1, 0., kTwoPi};
+  double cpar[7] = {minR, maxR, minR, maxR, 1, t->startPhi, t->deltaPhi};
   cone_init(&tmp, cpar, NULL, 0);
   cone_extent(&tmp, mn, mx);
   mn->z = minz;

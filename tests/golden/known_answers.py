@@ -830,6 +830,9 @@ def _pcon(sphi, dphi, z, rmin, rmax):
 
 # TestPolycone.cpp:42-60 poly1 (4 planes)
 PCON1 = _pcon(0.0, 360.0 * KPI_V / 180.0, (-1.0, -0.5, 0.5, 2.0), (0.1, 0.0, 0.0, 0.4), (1.0, 2.0, 2.0, 1.5))
+# TestPolycone.cpp:24-30 MyPCone: a 10-degree phi section from -10 degrees, 8 planes
+MYPCONE = _pcon(-10.0 * KPI_V / 180.0, 10.0 * KPI_V / 180.0, (-20.0, -10.0, -10.0, 0.0, 10.0, 20.0, 30.0, 40.0),
+                (30.0, 30.0, 0.0, 0.0, 0.0, 0.0, 40.0, 40.0), (70.0, 70.0, 70.0, 40.0, 40.0, 80.0, 80.0, 60.0))
 # TestPolycone.cpp:32-35 "SimpleTube+Cone"
 PCON_SIMPLE = _pcon(0.0, 360.0 * KPI_V / 180.0, (-10.0, 0.0, 10.0), (0.0, 0.0, 0.0), (70.0, 70.0, 80.0))
 # TestPolycone.cpp:538-542 pcon175 (equal-z planes)

@@ -289,6 +289,9 @@ SHAPE_SETS = [
     ("sphere-shell", W.SPHERE, (45.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
     ("sphere-shell-rotated-wedge", W.SPHERE, (6.0, 8.0, 1.0, W.K_TWO_PI, 0.0, W.K_PI)),
     ("polycone-4plane", W.POLYCONE, KA.PCON1),
+    ("polycone-phi-section-mypcone", W.POLYCONE, KA.MYPCONE),
+    ("polycone-4plane-half-sector", W.POLYCONE, KA._pcon(-1.0, W.K_PI, (-1.0, -0.5, 0.5, 2.0), (0.1, 0.0, 0.0, 0.4),
+                                                         (1.0, 2.0, 2.0, 1.5))),
     ("polycone-simple", W.POLYCONE, KA.PCON_SIMPLE),
     ("polycone-steps", W.POLYCONE, KA.PCON175),
     ("polycone-cms-trak", W.POLYCONE, KA._pcon(0.0, W.K_TWO_PI, (-2935., -1899., -1899., -1899., 1899., 1899., 1899.,

@@ -100,9 +100,13 @@ def test_invalid_descriptions_rejected(vgnav):
         with pytest.raises(N.VgnError) as e:
             HostTables(b.build())
         assert e.value.code == N.VGN_ERR_ARG
+    b = W.GeometryBuilder()  # a polycone section cone with dphi <= 0
+    b.place_world(b.logical(W.POLYCONE, (0.0, 0.0, 2.0, -1.0, 1.0, 0.0, 0.0, 5.0, 5.0)))
+    with pytest.raises(N.VgnError) as e:
+        HostTables(b.build())
+    assert e.value.code == N.VGN_ERR_ARG
     for shape, params in ((W.SPHERE, (0.0, 10.0, 0.0, 1.0, 0.0, W.K_PI)),   # phi section
-                          (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0)),  # theta section
-                          (W.POLYCONE, (0.0, 1.0, 2.0, -1.0, 1.0, 0.0, 0.0, 5.0, 5.0))):  # phi section
+                          (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0))):  # theta section
         b = W.GeometryBuilder()
         b.place_world(b.logical(shape, params))
         with pytest.raises(N.VgnError) as e:

@@ -165,8 +165,9 @@ enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, TrapTheta = 17, 
 // delta-phi, the theta cone's raw start/end angles and tangents
 enum { SphRmin = 0, SphRmax, SphA1x, SphA1y, SphA2x, SphA2y, SphN1x, SphN1y, SphN2x, SphN2y, SphWedgeDPhi,
        SphSTheta, SphETheta, SphTanSTheta, SphTanETheta, SphPad, kSphereSize };
-// Polycone (full phi), variable length: [0] section count n, [1, n+1] the n+1 z planes,
-// [n+2, 2n+1] the section z shifts, then n cone rows of kConeSize doubles
+// Polycone, variable length: [0] section count n, [1, n+1] the n+1 z planes, [n+2, 2n+1]
+// the section z shifts, then n cone rows of kConeSize doubles, then the raw phi start and
+// total angle
 #ifdef __CUDACC__
 #define VGN_HD __host__ __device__
 #else
@@ -176,6 +177,7 @@ constexpr int PconNSec = 0;
 constexpr int PconZs   = 1;
 VGN_HD inline int pcon_shift(int n) { return 2 + n; }
 VGN_HD inline int pcon_cone(int n, int k) { return 2 + 2 * n + k * kConeSize; }
+VGN_HD inline int pcon_phi(int n) { return pcon_cone(n, n); }  // the raw (phiStart, phiTotal)
 }  // namespace row
 
 // Plain-pointer view of the device tables, passed to kernels by value.

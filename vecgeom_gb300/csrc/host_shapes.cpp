@@ -328,10 +328,6 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
       rin[i]      = p[3 + nz + k];
       rout[i]     = p[3 + 2 * nz + k];
     }
-    if (!(dphi >= kTwoPi - 0.5 * kAngTolerance)) {
-      err = "Polycone phi sections are not supported";
-      return VGN_ERR_UNSUPPORTED;
-    }
     for (int i = 0; i < nz; ++i)
       if (!(rin[i] >= 0 && rout[i] >= rin[i]) || (i > 0 && !(z[i] >= z[i - 1]))) {
         err = "Polycone needs 0 <= rmin <= rmax and monotonic z planes";
@@ -362,6 +358,8 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.insert(shape.end(), zs.begin(), zs.end());
     shape.insert(shape.end(), shift.begin(), shift.end());
     shape.insert(shape.end(), cones.begin(), cones.end());
+    shape.push_back(sphi);  // raw phi arguments, for the Extent (row::pcon_phi)
+    shape.push_back(dphi);
     return VGN_OK;
   }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
@@ -482,18 +480,36 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     return;
   }
   case kPolycone: {
-    // UnplacedPolycone::Extent, full phi (source/UnplacedPolycone.cpp:865-900): z from the
-    // end planes; x and y from a full cone of the sections' largest constructor rmax
+    // UnplacedPolycone::Extent (source/UnplacedPolycone.cpp:865-902): z from the end planes;
+    // x and y from the Extent of Cone(minR, maxR, minR, maxR, 1, fStartPhi, fDeltaPhi), the
+    // sections' smallest constructor rmin and largest rmax and the polycone's phi range
+    // (PolyconeStruct::Init, PolyconeStruct.h:152-184)
     const int n = (int)r[row::PconNSec];
-    double maxR = 0;
+    auto vmax   = [](double a, double b) { return a > b ? a : b; };
+    auto vmin   = [](double a, double b) { return a < b ? a : b; };
+    double maxR = 0, minR = 1.7976931348623157e308;  // kInfLength
     for (int k = 0; k < n; ++k) {
-      const double *c  = r + row::pcon_cone(n, k);
-      const double m12 = c[row::ConeArgRmax1] > c[row::ConeArgRmax2] ? c[row::ConeArgRmax1] : c[row::ConeArgRmax2];
-      maxR             = maxR > m12 ? maxR : m12;
+      const double *c = r + row::pcon_cone(n, k);
+      maxR            = vmax(maxR, vmax(c[row::ConeArgRmax1], c[row::ConeArgRmax2]));
+      minR            = vmin(minR, vmin(c[row::ConeArgRmin1], c[row::ConeArgRmin2]));
     }
+    const double phiStart = r[row::pcon_phi(n)], phiTotal = r[row::pcon_phi(n) + 1];
+    double dphi = phiTotal >= kTwoPi - 0.5 * kAngTolerance ? kTwoPi : phiTotal;  // SetAndCheckDPhiAngle
+    double sphi = 0;
+    if (phiTotal <= 0. || phiTotal > kTwoPi - kTolerance) {
+      dphi = kTwoPi;
+    } else {
+      sphi = phiStart;
+      while (sphi < 0) sphi += kTwoPi;
+    }
+    std::vector<double> cone;
+    std::string unused;
+    const double cpar[7] = {minR, maxR, minR, maxR, 1, sphi, dphi};
+    shape_make_row(kCone, cpar, 7, cone, unused);
+    shape_extent(kCone, cone.data(), mn, mx);
     const double z0 = r[row::PconZs], zn = r[row::PconZs + n];
-    mn = {-maxR, -maxR, z0 > zn ? zn : z0};
-    mx = {maxR, maxR, z0 > zn ? z0 : zn};
+    mn.z = z0 > zn ? zn : z0;
+    mx.z = z0 > zn ? z0 : zn;
     return;
   }
   default: mn = mx = {0, 0, 0};

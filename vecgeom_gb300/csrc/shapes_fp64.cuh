@@ -1338,8 +1338,12 @@ __device__ __forceinline__ double sphere_safe_out(const double *t, D3 p)
   return t[sp::SphRmax] - rad;
 }
 
-// ---------------------------------------------------------------- Polycone (full phi)
-// volumes/kernel/PolyconeImplementation.h over the sections' cone rows
+// ---------------------------------------------------------------- Polycone
+// volumes/kernel/PolyconeImplementation.h over the sections' cone rows.  The kernels have
+// no phi logic of their own: a phi section reaches them through its section cones (built
+// with the polycone's raw phi arguments, PolyconeStruct.h:256).  They are instantiated
+// with phi-free cones (PHI = false) for full polycones and with phi cones for sections;
+// both are inline (a call would change the register allocation of the callers' loops).
 __device__ __forceinline__ int pcon_n(const double *t) { return (int)t[row::PconNSec]; }
 __device__ __forceinline__ const double *pcon_sec(const double *t, int n, int k) { return t + row::pcon_cone(n, k); }
 __device__ __forceinline__ D3 pcon_local(const double *t, int n, int k, D3 p)
@@ -1358,7 +1362,8 @@ __device__ __forceinline__ int pcon_section_index(const double *t, int n, double
 }
 
 // GenericKernelForASection (PolyconeImplementation.h:69-97)
-__device__ __forceinline__ void pcon_section_ci(const double *t, int n, int k, D3 p, bool forInside, bool &cin,
+template <bool PHI>
+__device__ __forceinline__ void pcon_section_ci_t(const double *t, int n, int k, D3 p, bool forInside, bool &cin,
                                                 bool &cout)
 {
   if (k < 0) {
@@ -1366,12 +1371,13 @@ __device__ __forceinline__ void pcon_section_ci(const double *t, int n, int k, D
     cout = true;
     return;
   }
-  cone_generic_ci<false>(pcon_sec(t, n, k), pcon_local(t, n, k, p), forInside, cin, cout);
+  cone_generic_ci<PHI>(pcon_sec(t, n, k), pcon_local(t, n, k, p), forInside, cin, cout);
 }
 
 // GenericKernelForContainsAndInside (PolyconeImplementation.h:127-187); cin/cout keep the
 // caller's initial values where the reference leaves them untouched
-__device__ __forceinline__ void pcon_ci(const double *t, D3 p, bool forInside, bool &cin, bool &cout)
+template <bool PHI>
+__device__ __forceinline__ void pcon_ci_t(const double *t, D3 p, bool forInside, bool &cin, bool &cout)
 {
   const int n   = pcon_n(t);
   const int lo  = pcon_section_index(t, n, p.z - kTolerance);
@@ -1381,21 +1387,21 @@ __device__ __forceinline__ void pcon_ci(const double *t, D3 p, bool forInside, b
     return;
   }
   if (lo < 0 && hi == 0) {
-    pcon_section_ci(t, n, 0, p, forInside, cin, cout);
+    pcon_section_ci_t<PHI>(t, n, 0, p, forInside, cin, cout);
     return;
   }
   if (hi < 0 && lo == n - 1) {
-    pcon_section_ci(t, n, n - 1, p, forInside, cin, cout);
+    pcon_section_ci_t<PHI>(t, n, n - 1, p, forInside, cin, cout);
     return;
   }
   if (lo >= 0 && hi >= 0) {
     if (lo == hi) {
-      pcon_section_ci(t, n, lo, p, forInside, cin, cout);
+      pcon_section_ci_t<PHI>(t, n, lo, p, forInside, cin, cout);
       return;
     }
     bool inLo = false, outLo = false, inHi = false, outHi = false;
-    pcon_section_ci(t, n, lo, p, forInside, inLo, outLo);
-    pcon_section_ci(t, n, hi, p, forInside, inHi, outHi);
+    pcon_section_ci_t<PHI>(t, n, lo, p, forInside, inLo, outLo);
+    pcon_section_ci_t<PHI>(t, n, hi, p, forInside, inHi, outHi);
     if ((!inLo && !outLo) && (!inHi && !outHi)) {
       cin = true;
       return;
@@ -1404,17 +1410,19 @@ __device__ __forceinline__ void pcon_ci(const double *t, D3 p, bool forInside, b
   }
 }
 
-__device__ __forceinline__ bool pcon_contains(const double *t, D3 p)
+template <bool PHI>
+__device__ __forceinline__ bool pcon_contains_t(const double *t, D3 p)
 {
   bool cin = false, cout = false;
-  pcon_ci(t, p, false, cin, cout);
+  pcon_ci_t<PHI>(t, p, false, cin, cout);
   return !cout;
 }
 
-__device__ __forceinline__ int pcon_inside(const double *t, D3 p)
+template <bool PHI>
+__device__ __forceinline__ int pcon_inside_t(const double *t, D3 p)
 {
   bool cin = false, cout = false;
-  pcon_ci(t, p, true, cin, cout);
+  pcon_ci_t<PHI>(t, p, true, cin, cout);
   int r = kSurfaceE;
   if (cout) r = kOutsideE;
   if (cin) r = kInsideE;
@@ -1422,7 +1430,8 @@ __device__ __forceinline__ int pcon_inside(const double *t, D3 p)
 }
 
 // DistanceToIn (PolyconeImplementation.h:189-237)
-__device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
+template <bool PHI>
+__device__ __forceinline__ double pcon_dist_in_t(const double *t, D3 p, D3 v)
 {
   const int n     = pcon_n(t);
   double distance = kInfLength;
@@ -1432,7 +1441,7 @@ __device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
   if (index == -1) index = 0;
   if (index == -2) index = n - 1;
   do {
-    distance = cone_dist_in<false>(pcon_sec(t, n, index), pcon_local(t, n, index, p), v);
+    distance = cone_dist_in<PHI>(pcon_sec(t, n, index), pcon_local(t, n, index, p), v);
     if (distance < kInfLength || !increment) break;
     index += increment;
   } while (index >= 0 && index < n);
@@ -1440,10 +1449,11 @@ __device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
 }
 
 // DistanceToOut (PolyconeImplementation.h:239-379)
-__device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 dir)
+template <bool PHI>
+__device__ __forceinline__ double pcon_dist_out_t(const double *t, D3 point, D3 dir)
 {
   const int n = pcon_n(t);
-  if (n == 1) return cone_dist_out<false>(pcon_sec(t, n, 0), pcon_local(t, n, 0, point), dir);
+  if (n == 1) return cone_dist_out<PHI>(pcon_sec(t, n, 0), pcon_local(t, n, 0, point), dir);
   const int lo = pcon_section_index(t, n, point.z - kTolerance);
   const int hi = pcon_section_index(t, n, point.z + kTolerance);
   int index    = 0;
@@ -1451,15 +1461,15 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
     return -1;
   } else if (lo < 0 && hi >= 0) {
     index = hi;
-    if (cone_inside<false>(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
+    if (cone_inside<PHI>(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
   } else if (lo != hi && lo >= 0) {
-    index = cone_inside<false>(pcon_sec(t, n, lo), pcon_local(t, n, lo, point)) == kOutsideE ? hi : lo;
+    index = cone_inside<PHI>(pcon_sec(t, n, lo), pcon_local(t, n, lo, point)) == kOutsideE ? hi : lo;
   } else {
     index = lo;
     if (index < 0) index = pcon_section_index(t, n, point.z);
   }
   if (index < 0) return 0.;
-  if (cone_inside<false>(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
+  if (cone_inside<PHI>(pcon_sec(t, n, index), pcon_local(t, n, index, point)) == kOutsideE) return -1;
   double totalDistance = 0.;
   int increment        = (dir.z > 0) ? 1 : -1;
   if (fabs(dir.z) < kTolerance) increment = 0;
@@ -1470,12 +1480,12 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
     if ((totalDistance != 0) || (istep < 2)) {
       pn = d3(point.x + totalDistance * dir.x, point.y + totalDistance * dir.y, point.z + totalDistance * dir.z);
       pn.z -= shift;
-      if (cone_inside<false>(pcon_sec(t, n, index), pn) == kOutsideE) break;
+      if (cone_inside<PHI>(pcon_sec(t, n, index), pn) == kOutsideE) break;
     } else {
       pn.z -= shift;
     }
     istep++;
-    const double dist = cone_dist_out<false>(pcon_sec(t, n, index), pn, dir);
+    const double dist = cone_dist_out<PHI>(pcon_sec(t, n, index), pn, dir);
     if (dist == -1) return kInfLength;
     if (fabs(dist) < 0.5 * kTolerance) {
       int index1 = index;
@@ -1488,7 +1498,7 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
       const double td = totalDistance + dist;
       D3 pte          = d3(point.x + td * dir.x, point.y + td * dir.y, point.z + td * dir.z);
       pte.z -= t[row::pcon_shift(n) + index1];
-      if (cone_inside<false>(pcon_sec(t, n, index1), pte) == kOutsideE || (increment == 0)) break;
+      if (cone_inside<PHI>(pcon_sec(t, n, index1), pte) == kOutsideE || (increment == 0)) break;
     }
     totalDistance += dist;
     index += increment;
@@ -1497,20 +1507,21 @@ __device__ __forceinline__ double pcon_dist_out(const double *t, D3 point, D3 di
 }
 
 // neighbour scan shared by SafetyToIn and SafetyToOut (PolyconeImplementation.h:413-446, 487-513)
-__device__ __forceinline__ double pcon_scan_neighbours(const double *t, int n, int index, D3 p, double minSafety)
+template <bool PHI>
+__device__ __forceinline__ double pcon_scan_neighbours_t(const double *t, int n, int index, D3 p, double minSafety)
 {
   const double *zs = t + row::PconZs;
   double zbase     = zs[index + 1];
   for (int i = index + 1; i < n; ++i) {
     if (zs[i] - zbase >= minSafety) break;
-    const double s = cone_safe_in<false>(pcon_sec(t, n, i), pcon_local(t, n, i, p));
+    const double s = cone_safe_in<PHI>(pcon_sec(t, n, i), pcon_local(t, n, i, p));
     if (s < minSafety) minSafety = s;
   }
   if (index > 0) {
     zbase = zs[index - 1];
     for (int i = index - 1; i >= 0; --i) {
       if (zbase - zs[i] >= minSafety) break;
-      const double s = cone_safe_in<false>(pcon_sec(t, n, i), pcon_local(t, n, i, p));
+      const double s = cone_safe_in<PHI>(pcon_sec(t, n, i), pcon_local(t, n, i, p));
       if (s < minSafety) minSafety = s;
     }
   }
@@ -1518,7 +1529,8 @@ __device__ __forceinline__ double pcon_scan_neighbours(const double *t, int n, i
 }
 
 // SafetyToIn (PolyconeImplementation.h:381-450)
-__device__ __forceinline__ double pcon_safe_in(const double *t, D3 p)
+template <bool PHI>
+__device__ __forceinline__ double pcon_safe_in_t(const double *t, D3 p)
 {
   const int n = pcon_n(t);
   int index   = pcon_section_index(t, n, p.z);
@@ -1528,24 +1540,52 @@ __device__ __forceinline__ double pcon_safe_in(const double *t, D3 p)
     if (index == -1) index = 0;
     if (index == -2) index = n - 1;
   }
-  const double safety = cone_safe_in<false>(pcon_sec(t, n, index), pcon_local(t, n, index, p));
+  const double safety = cone_safe_in<PHI>(pcon_sec(t, n, index), pcon_local(t, n, index, p));
   if (needZ || safety < kTolerance) return safety;
-  return pcon_scan_neighbours(t, n, index, p, safety);
+  return pcon_scan_neighbours_t<PHI>(t, n, index, p, safety);
 }
 
 // SafetyToOut (PolyconeImplementation.h:452-517); neighbours probed with the cone's SafetyToIn
-__device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
+template <bool PHI>
+__device__ __forceinline__ double pcon_safe_out_t(const double *t, D3 p)
 {
   bool cin = false, cout = false;
-  pcon_ci(t, p, true, cin, cout);
+  pcon_ci_t<PHI>(t, p, true, cin, cout);
   if (cout) return -1;
   const int n     = pcon_n(t);
   const int index = pcon_section_index(t, n, p.z);
   if (index < 0) return -1;
-  const double minSafety = cone_safe_out<false>(pcon_sec(t, n, index), pcon_local(t, n, index, p));
+  const double minSafety = cone_safe_out<PHI>(pcon_sec(t, n, index), pcon_local(t, n, index, p));
   if (minSafety == kInfLength) return 0.;
   if (minSafety < kTolerance) return 0.;
-  return pcon_scan_neighbours(t, n, index, p, minSafety);
+  return pcon_scan_neighbours_t<PHI>(t, n, index, p, minSafety);
+}
+
+__device__ __forceinline__ bool pcon_has_phi(const double *t) { return cone_has_phi(pcon_sec(t, pcon_n(t), 0)); }
+
+__device__ __forceinline__ bool pcon_contains(const double *t, D3 p)
+{
+  return pcon_has_phi(t) ? pcon_contains_t<true>(t, p) : pcon_contains_t<false>(t, p);
+}
+__device__ __forceinline__ int pcon_inside(const double *t, D3 p)
+{
+  return pcon_has_phi(t) ? pcon_inside_t<true>(t, p) : pcon_inside_t<false>(t, p);
+}
+__device__ __forceinline__ double pcon_dist_in(const double *t, D3 p, D3 v)
+{
+  return pcon_has_phi(t) ? pcon_dist_in_t<true>(t, p, v) : pcon_dist_in_t<false>(t, p, v);
+}
+__device__ __forceinline__ double pcon_dist_out(const double *t, D3 p, D3 v)
+{
+  return pcon_has_phi(t) ? pcon_dist_out_t<true>(t, p, v) : pcon_dist_out_t<false>(t, p, v);
+}
+__device__ __forceinline__ double pcon_safe_in(const double *t, D3 p)
+{
+  return pcon_has_phi(t) ? pcon_safe_in_t<true>(t, p) : pcon_safe_in_t<false>(t, p);
+}
+__device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
+{
+  return pcon_has_phi(t) ? pcon_safe_out_t<true>(t, p) : pcon_safe_out_t<false>(t, p);
 }
 
 // ---------------------------------------------------------------- dispatch

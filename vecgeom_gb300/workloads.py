@@ -318,8 +318,9 @@ MIXED_JITTER = 5.0
 def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = False):
     """Parameters with every length drawn from U[5, 60] mm (Tube radii from U[5, 40] mm),
     and the half-extent of the shape's full (unsectioned) bounding box.  With `sections`,
-    three quarters of the tubes and cones are phi sections (width U[0.2, 2 pi - 0.2], start
-    U[0, 2 pi) for tubes and U[-pi, 2 pi) for cones, whose start angle the reference folds)."""
+    three quarters of the tubes, cones and polycones are phi sections (width U[0.2, 2 pi - 0.2],
+    start U[0, 2 pi) for tubes and U[-pi, 2 pi) for cones and polycones, whose start angle the
+    reference folds)."""
     u = lambda lo=5.0, hi=60.0: float(rng.uniform(lo, hi))
     if shape == BOX:
         p = (u(), u(), u())
@@ -364,7 +365,10 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
         rmax = [u() for _ in range(4)]
         solid = rng.uniform() < 0.5
         rmin = [0.0 if solid else float(rng.uniform(0.0, 0.8)) * r for r in rmax]
-        return (0.0, K_TWO_PI, 4.0, *z, *rmin, *rmax), np.array([max(rmax), max(rmax), h])
+        sphi, dphi = 0.0, K_TWO_PI
+        if sections and rng.uniform() < 0.75:
+            sphi, dphi = float(rng.uniform(-K_PI, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+        return (sphi, dphi, 4.0, *z, *rmin, *rmax), np.array([max(rmax), max(rmax), h])
     raise ValueError(f"shape {shape} not implemented")
 
 
@@ -406,7 +410,7 @@ def mixed_shape_geometry(seed: int = 21, grid=MIXED_GRID, world: float = MIXED_W
     rotated by a uniform random rotation (Euler angles phi, psi ~ U[0, 360),
     cos(theta) ~ U[-1, 1]).  A daughter whose bounding sphere (plus the jitter)
     would leave its cell is scaled down to fit, so daughters never overlap.  `sections`
-    makes most tubes and cones phi sections (see _mixed_shape_params)."""
+    makes most tubes, cones and polycones phi sections (see _mixed_shape_params)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     nx, ny, nz = grid
     pitch = np.array([2 * world / nx, 2 * world / ny, 2 * world / nz])
