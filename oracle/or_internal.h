@@ -123,11 +123,19 @@ typedef struct { /* TrapezoidStruct.h:41-59 with the PlaneShell<4> side planes (
   double a[4], b[4], c[4], d[4];
 } or_trap;
 
-typedef struct { /* SphereStruct.h:21-51, full phi and full theta */
+typedef struct { /* ThetaCone (ThetaCone_Evolution.h:45-83) */
+  double sT, dT, eT;             /* fSTheta, fDTheta, fETheta */
+  double tanS, tanE, tanS2, tanE2; /* tanSTheta, tanETheta and their squares */
+  double tanBis, slope1, slope2; /* tanBisector, slope1, slope2 */
+} or_theta;
+
+typedef struct { /* SphereStruct.h:21-51 */
   double rmin, rmax;
-  or_wedge w; /* evolution::Wedge built from the constructor's raw (dphi, sphi) */
-  /* ThetaCone built from the raw (stheta, dtheta) (ThetaCone_Evolution.h:62-82) */
-  double tsTheta, teTheta, tanSTheta, tanETheta;
+  double sPhi, dPhi;             /* checked fSPhi, fDPhi (CheckPhiAngles) */
+  double sTheta, dTheta, eTheta; /* fSTheta, checked fDTheta (CheckThetaAngles), eTheta */
+  int fullPhi, fullTheta, full;  /* fFullPhiSphere, fFullThetaSphere, fFullSphere */
+  or_wedge w;  /* evolution::Wedge built from the constructor's raw (dphi, sphi) */
+  or_theta tc; /* ThetaCone built from the constructor's raw (stheta, dtheta) */
 } or_sphere;
 
 typedef struct { /* PolyconeStruct.h:24-37: z planes and one ConeStruct per section */

@@ -1511,84 +1511,437 @@ static void trap_extent(const or_trap *t, v3 *mn, v3 *mx)
 }
 
 /* ================================================================== */
-/* Sphere (full phi, full theta): kernel/SphereImplementation.h,      */
-/* SphereUtilities.h, Wedge_Evolution.h, ThetaCone_Evolution.h        */
+/* Sphere: kernel/SphereImplementation.h, SphereUtilities.h,          */
+/* Wedge_Evolution.h, ThetaCone_Evolution.h                           */
 /* ================================================================== */
 
-/* SphereStruct(rmin, rmax, sphi, dphi, stheta, dtheta) (SphereStruct.h:285-304); only the
- * full sphere (dphi >= 2pi - kAngTolerance/2, stheta = 0, stheta + dtheta >= pi) is
- * accepted.  The wedge and theta cone keep the raw constructor angles. */
-static int sphere_init(or_sphere *t, const double *a, char *err, int errlen)
+/* ---- evolution::Wedge pieces only the sphere uses ---- */
+
+/* Wedge::IsPointOnSurfaceAndMovingOut<start, movingOut> (Wedge_Evolution.h:233-246): on the
+ * face and moving along / against its inward normal */
+static int wedge_moving(const or_wedge *w, int start, int movingOut, v3 p, v3 d)
 {
-  const double rmin = a[0], rmax = a[1], sphi = a[2], dphi = a[3], stheta = a[4], dtheta = a[5];
-  if (!(rmin >= 0 && rmax > rmin)) {
-    set_err(err, errlen, "Sphere: needs 0 <= rmin < rmax");
-    return -1;
-  }
-  if (!(dphi >= 2 * kPi - kAngTolerance * 0.5) || stheta != 0. || !(dtheta + stheta >= kPi)) {
-    set_err(err, errlen, "Sphere: phi and theta sections are not supported");
-    return -2;
-  }
-  t->rmin  = rmin;
-  t->rmax  = rmax;
-  wedge_init(&t->w, dphi, sphi);
-  t->tsTheta = stheta;
-  t->teTheta = stheta + dtheta;
-  double ts = t->tsTheta, te = t->teTheta;
-  if (t->tsTheta > kPi / 2) ts = kPi - t->tsTheta;
-  if (t->teTheta > kPi / 2) te = kPi - t->teTheta;
-  t->tanSTheta = tan(ts);
-  t->tanETheta = tan(te);
-  return 0;
+  double ax = start ? w->a1x : w->a2x, ay = start ? w->a1y : w->a2y;
+  double nx = start ? w->n1x : w->n2x, ny = start ? w->n1y : w->n2y;
+  if (!wedge_on_surface(ax, ay, nx, ny, p)) return 0;
+  double dn = d.x * -nx + d.y * -ny; /* dir.Dot(-normal); the normal has z = 0 */
+  return movingOut ? dn > 0.005 * kHalfTolerance : dn < 0.005 * kHalfTolerance;
 }
 
-#define kThetaHalfPi (0.5 * kPi) /* ThetaCone_Evolution.h:13 */
-#define kThetaTol 1e-9           /* ThetaCone::kAngTolerance = kTolerance */
-
-/* ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730) for stheta = 0, etheta >= pi */
-static int theta_completely_inside(const or_sphere *t, v3 p)
+/* Wedge::DistanceToIn / DistanceToOut (Wedge_Evolution.h:393-446): distances to the two
+ * half-planes, kInfLength unless the ray approaches the plane from the chosen side */
+static void wedge_dist(const or_wedge *w, v3 p, v3 d, int toIn, double *dist1, double *dist2)
 {
-  const double sT = t->tsTheta, eT = t->teTheta;
+  double comp1 = d.x * w->n1x + d.y * w->n1y;
+  double comp2 = d.x * w->n2x + d.y * w->n2y;
+  *dist1 = kInfLength;
+  *dist2 = kInfLength;
+  if (toIn ? comp1 > 0. : comp1 < 0.) {
+    double tmp = -(p.x * w->n1x + p.y * w->n1y) / comp1;
+    if (tmp > 0.) *dist1 = tmp;
+  }
+  if (toIn ? comp2 > 0. : comp2 < 0.) {
+    double tmp = -(p.x * w->n2x + p.y * w->n2y) / comp2;
+    if (tmp > 0.) *dist2 = tmp;
+  }
+}
+
+/* ---- ThetaCone (ThetaCone_Evolution.h) ---- */
+#define kThHalfTol (0.5 * kTolerance) /* halfAngTolerance; kAngTolerance = kTolerance */
+#define kThTolAng (2 * kTolerance * 10.)
+
+/* ThetaCone(sTheta, dTheta) (ThetaCone_Evolution.h:62-82) */
+static void theta_init(or_theta *c, double sT, double dT)
+{
+  c->sT = sT;
+  c->dT = dT;
+  c->eT = c->sT + c->dT;
+  double ts = c->sT, te = c->eT;
+  if (c->sT > kPi / 2) ts = kPi - c->sT;
+  if (c->eT > kPi / 2) te = kPi - c->eT;
+  c->tanS   = tan(ts);
+  c->tanS2  = c->tanS * c->tanS;
+  c->tanE   = tan(te);
+  c->tanE2  = c->tanE * c->tanE;
+  c->tanBis = tan(ts + (c->dT / 2));
+  if (c->sT > kPi / 2 && c->eT > kPi / 2) c->tanBis = tan(ts - (c->dT / 2));
+  c->slope1 = tan(kPi / 2 - c->sT);
+  c->slope2 = tan(kPi / 2 - c->eT);
+}
+
+/* ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730) */
+static int theta_completely_inside(const or_theta *c, v3 p)
+{
+  const double sT = c->sT, eT = c->eT;
   double rho         = sqrt(v3_dot(p, p) - (p.z * p.z));
-  double cone1Radius = fabs(p.z * t->tanSTheta);
-  double cone2Radius = fabs(p.z * t->tanETheta);
+  double cone1Radius = fabs(p.z * c->tanS);
+  double cone2Radius = fabs(p.z * c->tanE);
   int onZ  = p.z != 0. && p.x == 0. && p.y == 0.;
   int onXY = p.z == 0. && (p.x != 0. || p.y != 0.);
   int ci   = onZ && ((sT == 0. && eT == kPi) || (p.z > 0. && sT == 0.) || (p.z < 0. && eT == kPi));
-  ci = ci || (!ci && (onXY && (sT < kThetaHalfPi && eT > kThetaHalfPi && (kThetaHalfPi - sT) > kThetaTol &&
-                               (eT - kThetaHalfPi) > kTolerance)));
-  /* fSTheta < pi/2 + tol/2 and fETheta > pi/2 + tol/2 with fSTheta < fETheta */
-  double tolAngMin = cone1Radius + 2 * kThetaTol * 10.;
-  double tolAngMax = cone2Radius + 2 * kThetaTol * 10.;
-  ci = ci || (!ci && ((rho >= tolAngMin && p.z > 0.) || (rho >= tolAngMax && p.z < 0.)));
+  ci = ci || (!ci && (onXY && (sT < kHalfPi && eT > kHalfPi && (kHalfPi - sT) > kTolerance &&
+                               (eT - kHalfPi) > kTolerance)));
+  if (sT < kHalfPi + kThHalfTol) {
+    if (eT < kHalfPi + kThHalfTol && sT < eT) {
+      double tolAngMin = cone1Radius + kThTolAng;
+      double tolAngMax = cone2Radius - kThTolAng;
+      ci = ci || (!ci && (((rho <= tolAngMax) && (rho >= tolAngMin) && (p.z > 0.) && (sT != 0.)) ||
+                          ((rho <= tolAngMax) && (sT == 0.) && (p.z > 0.))));
+    }
+    if (eT > kHalfPi + kThHalfTol && sT < eT) {
+      double tolAngMin = cone1Radius + kThTolAng;
+      double tolAngMax = cone2Radius + kThTolAng;
+      ci = ci || (!ci && (((rho >= tolAngMin) && (p.z > 0.)) || ((rho >= tolAngMax) && (p.z < 0.))));
+    }
+    if (eT >= kHalfPi - kThHalfTol && eT <= kHalfPi + kThHalfTol) ci = ci && !(fabs(p.z) < kThHalfTol);
+  }
+  if (eT > kHalfPi + kThHalfTol) {
+    if (sT >= kHalfPi - kThHalfTol && sT <= kHalfPi + kThHalfTol) ci = ci && !(fabs(p.z) < kThHalfTol);
+    if (sT > kHalfPi + kThHalfTol && sT < eT) {
+      double tolAngMin = cone1Radius - kThTolAng;
+      double tolAngMax = cone2Radius + kThTolAng;
+      ci = ci || (!ci && (((rho <= tolAngMin) && (rho >= tolAngMax) && (p.z < 0.) && (eT != kPi)) ||
+                          ((rho <= tolAngMin) && (p.z < 0.) && (eT == kPi))));
+    }
+  }
   return ci;
 }
 
-/* ThetaCone::IsCompletelyOutside (ThetaCone_Evolution.h:733-805) for stheta = 0, etheta >= pi */
-static int theta_completely_outside(const or_sphere *t, v3 p)
+/* ThetaCone::IsCompletelyOutside (ThetaCone_Evolution.h:733-805) */
+static int theta_completely_outside(const or_theta *c, v3 p)
 {
-  const double sT = t->tsTheta, eT = t->teTheta;
+  const double sT = c->sT, eT = c->eT;
   double diff        = p.x * p.x + p.y * p.y;
   double rho         = sqrt(diff);
-  double cone1Radius = fabs(p.z * t->tanSTheta);
-  double cone2Radius = fabs(p.z * t->tanETheta);
+  double cone1Radius = fabs(p.z * c->tanS);
+  double cone2Radius = fabs(p.z * c->tanE);
   int onZ  = p.z != 0. && p.x == 0. && p.y == 0.;
+  int onXY = p.z == 0. && (p.x != 0. || p.y != 0.);
   int co   = onZ && ((sT != 0. && eT != kPi) || (p.z > 0. && sT != 0.) || (p.z < 0. && eT != kPi));
-  /* the on-xy-plane term needs both angles on one side of pi/2: never for a full theta range */
-  double tolAngMin2 = cone1Radius - 2 * kThetaTol * 10.;
-  double tolAngMax2 = cone2Radius - 2 * kThetaTol * 10.;
-  co = co || (!co && ((rho < tolAngMin2 && p.z > 0.) || (rho < tolAngMax2 && p.z < 0.)));
+  co = co || (!co && (onXY && (((sT < kHalfPi) && (eT < kHalfPi) && ((kHalfPi - sT) > kTolerance) &&
+                                ((kHalfPi - eT) > kTolerance)) ||
+                               ((sT > kHalfPi && eT > kHalfPi) && ((sT - kHalfPi) > kTolerance) &&
+                                ((eT - kHalfPi) > kTolerance)))));
+  if (sT < kHalfPi + kThHalfTol) {
+    if (eT < kHalfPi + kThHalfTol && sT < eT) {
+      double tolAngMin2 = cone1Radius - kThTolAng;
+      double tolAngMax2 = cone2Radius + kThTolAng;
+      co = co || (!co && ((rho < tolAngMin2) || (rho > tolAngMax2) || (p.z < 0.)));
+    }
+    if (eT > kHalfPi + kThHalfTol && sT < eT) {
+      double tolAngMin2 = cone1Radius - kThTolAng;
+      double tolAngMax2 = cone2Radius - kThTolAng;
+      co = co || (!co && (((rho < tolAngMin2) && (p.z > 0.)) || ((rho < tolAngMax2) && (p.z < 0.))));
+    }
+    if (eT >= kHalfPi - kThHalfTol && eT <= kHalfPi + kThHalfTol) co = co && !(fabs(p.z) < kThHalfTol);
+  }
+  if (eT > kHalfPi + kThHalfTol) {
+    if (sT >= kHalfPi - kThHalfTol && sT <= kHalfPi + kThHalfTol) co = co && !(fabs(p.z) < kThHalfTol);
+    if (sT > kHalfPi + kThHalfTol && sT < eT) {
+      double tolAngMin2 = cone1Radius + kThTolAng;
+      double tolAngMax2 = cone2Radius - kThTolAng;
+      co = co || (!co && ((rho < tolAngMax2) || (rho > tolAngMin2) || (p.z > 0.)));
+    }
+  }
   return co;
 }
 
-/* SphereUtilities::IsCompletelyInside / IsCompletelyOutside (SphereUtilities.h:110-141) */
+/* ThetaCone::Contains (ThetaCone_Evolution.h:231-240) */
+static inline int theta_contains(const or_theta *c, v3 p) { return !theta_completely_outside(c, p); }
+
+/* ThetaCone::IsPointOnSurfaceAndMovingOut<start, movingOut> (ThetaCone_Evolution.h:164-229):
+ * on the cone face (IsOnSurfaceGeneric) and moving along / against GetNormal<start> */
+static int theta_moving(const or_theta *c, int start, int movingOut, v3 p, v3 d)
+{
+  double rhs  = fabs((start ? c->tanS : c->tanE) * p.z);
+  double rho2 = p.x * p.x + p.y * p.y;
+  if (!(rho2 >= minus_tol_sq(rhs, kTolerance) && rho2 <= plus_tol_sq(rhs, kTolerance))) return 0;
+  v3 n = v3_make(p.x, p.y, -(start ? c->tanS2 : c->tanE2) * p.z);
+  if (start ? c->sT <= kHalfPi : !(c->eT <= kHalfPi)) n = v3_make(-n.x, -n.y, -n.z);
+  double dn = v3_dot(d, n);
+  return movingOut ? dn > 0. : dn < 0.;
+}
+
+/* ThetaCone::DistanceToLine (ThetaCone_Evolution.h:358-365) */
+static inline double theta_dist_line(double slope, double x, double y)
+{
+  double dist = (y - slope * x) / sqrt(1. + slope * slope);
+  return fabs(dist);
+}
+
+/* ThetaCone::SafetyToIn (ThetaCone_Evolution.h:276-316) */
+static double theta_safe_in(const or_theta *c, v3 p)
+{
+  const double sT = c->sT, eT = c->eT;
+  double pointRad  = sqrt(p.x * p.x + p.y * p.y);
+  double sfTh1     = theta_dist_line(c->slope1, pointRad, p.z);
+  double sfTh2     = theta_dist_line(c->slope2, pointRad, p.z);
+  double safeTheta = or_min(sfTh1, sfTh2);
+  if (theta_contains(c, p)) return 0.;
+  if (sT < kPi / 2 + kThHalfTol) {
+    if (eT < kPi / 2 + kThHalfTol && sT < eT && p.z < 0.) safeTheta = sfTh2;
+    if (eT > kPi / 2 + kThHalfTol && sT < eT) {
+      if (p.z > 0.) safeTheta = sfTh1;
+      if (p.z < 0.) safeTheta = sfTh2;
+    }
+  }
+  if (eT > kPi / 2 + kThHalfTol && sT > kPi / 2 + kThHalfTol && sT < eT && p.z > 0.) safeTheta = sfTh1;
+  return safeTheta;
+}
+
+/* ThetaCone::SafetyToOut (ThetaCone_Evolution.h:318-356) */
+static double theta_safe_out(const or_theta *c, v3 p)
+{
+  const double sT = c->sT, eT = c->eT;
+  double pointRad    = sqrt(p.x * p.x + p.y * p.y);
+  double bisectorRad = fabs(p.z * c->tanBis);
+  int cond           = 0;
+  double sfTh1       = theta_dist_line(c->slope1, pointRad, p.z);
+  double sfTh2       = theta_dist_line(c->slope2, pointRad, p.z);
+  if (sT < kPi / 2 + kThHalfTol) {
+    if (eT < kPi / 2 + kThHalfTol && sT < eT) cond = (pointRad < bisectorRad) && (sT != 0.);
+    if (eT > kPi / 2 + kThHalfTol && sT < eT) cond = sfTh1 < sfTh2;
+  }
+  if (eT > kPi / 2 + kThHalfTol && sT > kPi / 2 + kThHalfTol && sT < eT)
+    cond = !((pointRad < bisectorRad) && (eT != kPi));
+  return cond ? sfTh1 : sfTh2;
+}
+
+/* The root clean-up ThetaCone::DistanceToIn applies to each cone root: a root within
+ * 3 kTolerance of zero becomes 0 and sets `done`; a negative root becomes kInfLength unless
+ * `done` is already set (ThetaCone_Evolution.h:387-395) */
+static inline double theta_in_root(double root, int *done)
+{
+  *done = *done || (fabs(root) < 3. * kTolerance);
+  if (fabs(root) < 3. * kTolerance) root = 0.;
+  if (!*done && root < 0.) root = kInfLength;
+  return root;
+}
+
+/* ThetaCone::DistanceToIn (ThetaCone_Evolution.h:367-496); dist1/dist2 and int1/int2 come
+ * in as kInfLength and false and are only overwritten by the branches that apply */
+static void theta_dist_in(const or_theta *c, v3 p, v3 d, double *dist1, double *dist2, int *int1, int *int2)
+{
+  const double sT = c->sT, eT = c->eT;
+  int done          = 0;
+  double firstRoot  = kInfLength, secondRoot = kInfLength;
+  double pDotV2d    = p.x * d.x + p.y * d.y;
+  double rho2       = p.x * p.x + p.y * p.y;
+  double dirRho2    = d.x * d.x + d.y * d.y;
+  double b          = pDotV2d - p.z * d.z * c->tanS2;
+  double a          = dirRho2 - d.z * d.z * c->tanS2;
+  double cc         = rho2 - p.z * p.z * c->tanS2;
+  double d2         = b * b - a * cc;
+  double aInv       = 1. / NonZero(a);
+  if (d2 > 0.) firstRoot = (-b + sqrt(fabs(d2))) * aInv;
+  firstRoot = theta_in_root(firstRoot, &done);
+
+  double b2    = pDotV2d - p.z * d.z * c->tanE2;
+  double a2    = dirRho2 - d.z * d.z * c->tanE2;
+  double c2    = rho2 - p.z * p.z * c->tanE2;
+  double d22   = b2 * b2 - a2 * c2;
+  double a2Inv = 1. / NonZero(a2);
+  if (d22 > 0.) secondRoot = (-b2 - sqrt(fabs(d22))) * a2Inv;
+  if (!done && fabs(secondRoot) < 3. * kTolerance) secondRoot = 0.;
+  done = done || (fabs(secondRoot) < 3. * kTolerance);
+  if (!done && secondRoot < 0.) secondRoot = kInfLength;
+
+  if (sT < kHalfPi + kThHalfTol) {
+    if (eT < kHalfPi + kThHalfTol && sT < eT) {
+      *dist1 = firstRoot;
+      *dist2 = secondRoot;
+      double z1 = (p.z + *dist1 * d.z), z2 = (p.z + *dist2 * d.z);
+      *int1 = ((d2 > 0.) && (z1 > 0.));
+      *int2 = ((d22 > 0.) && (z2 > 0.));
+    }
+    if (eT >= kHalfPi - kThHalfTol && eT <= kHalfPi + kThHalfTol) {
+      if (d.z > 0.) *dist2 = -p.z / d.z;
+      double z2 = (p.z + *dist2 * d.z);
+      *int2 = ((*dist2 != kInfLength) && (fabs(z2) < kThHalfTol));
+    }
+    if (eT > kHalfPi + kThHalfTol && sT < eT) {
+      *dist1 = firstRoot;
+      if (d22 > 0.) secondRoot = (-b2 + sqrt(fabs(d22))) * a2Inv;
+      done       = 0;
+      secondRoot = theta_in_root(secondRoot, &done);
+      *dist2     = secondRoot;
+      double z1 = (p.z + *dist1 * d.z), z2 = (p.z + *dist2 * d.z);
+      *int1 = ((d2 > 0) && (*dist1 != kInfLength) && (z1 > 0.));
+      *int2 = ((d22 > 0) && (*dist2 != kInfLength) && (z2 < 0.));
+    }
+  }
+  if (sT >= kHalfPi - kThHalfTol && eT > kHalfPi + kThHalfTol && sT < eT) {
+    if (d2 > 0.) firstRoot = (-b - sqrt(fabs(d2))) * aInv;
+    done      = 0;
+    firstRoot = theta_in_root(firstRoot, &done);
+    *dist1    = firstRoot;
+    if (d22 > 0.) secondRoot = (-b2 + sqrt(fabs(d22))) * a2Inv;
+    done       = 0;
+    secondRoot = theta_in_root(secondRoot, &done);
+    *dist2     = secondRoot;
+    double z1 = (p.z + *dist1 * d.z), z2 = (p.z + *dist2 * d.z);
+    *int1 = ((d2 > 0) && (*dist1 != kInfLength) && (z1 < 0.));
+    *int2 = ((d22 > 0) && (*dist2 != kInfLength) && (z2 < 0.));
+  }
+  if (sT >= kHalfPi - kThHalfTol && sT <= kHalfPi + kThHalfTol) {
+    if (d.z < 0.) *dist1 = -p.z / d.z;
+    double z1 = (p.z + *dist1 * d.z);
+    *int1 = ((*dist1 != kInfLength) && (fabs(z1) < kThHalfTol));
+  }
+}
+
+/* ThetaCone::DistanceToOut (ThetaCone_Evolution.h:498-652), same conventions */
+static void theta_dist_out(const or_theta *c, v3 p, v3 d, double *dist1, double *dist2, int *int1, int *int2)
+{
+  const double sT = c->sT, eT = c->eT;
+  double inf       = kInfLength;
+  double firstRoot = kInfLength, secondRoot = kInfLength;
+  double pDotV2d   = p.x * d.x + p.y * d.y;
+  double rho2      = p.x * p.x + p.y * p.y;
+  double b         = pDotV2d - p.z * d.z * c->tanS2;
+  double a         = d.x * d.x + d.y * d.y - d.z * d.z * c->tanS2;
+  double cc        = rho2 - p.z * p.z * c->tanS2;
+  double d2        = b * b - a * cc;
+  if (d2 < 0. && fabs(d2) < kHalfTolerance) d2 = 0.;
+  if ((d2 >= 0.) && b >= 0. && a != 0.) firstRoot = ((-b - sqrt(fabs(d2))) / NonZero(a));
+  if ((d2 >= 0.) && b < 0.) firstRoot = ((cc) / NonZero(-b + sqrt(fabs(d2))));
+  if (firstRoot < 0.) firstRoot = kInfLength;
+
+  double b2  = p.x * d.x + p.y * d.y - p.z * d.z * c->tanE2;
+  double a2  = d.x * d.x + d.y * d.y - d.z * d.z * c->tanE2;
+  double c2  = p.x * p.x + p.y * p.y - p.z * p.z * c->tanE2;
+  double d22 = (b2 * b2) - (a2 * c2);
+  if (d22 < 0. && fabs(d22) < kHalfTolerance) d22 = 0.;
+  if ((d22 >= 0.) && b2 >= 0.) secondRoot = ((c2) / NonZero(-b2 - sqrt(fabs(d22))));
+  if ((d22 >= 0.) && b2 < 0. && a2 != 0.) secondRoot = ((-b2 + sqrt(fabs(d22))) / NonZero(a2));
+  if (secondRoot < 0. && fabs(secondRoot) > kTolerance) secondRoot = kInfLength;
+  if (fabs(secondRoot) < kTolerance) secondRoot = 0.;
+
+  if (sT < kPi / 2 + kThHalfTol) {
+    if (eT < kPi / 2 + kThHalfTol && sT < eT) {
+      *dist1 = firstRoot;
+      *dist2 = secondRoot;
+      double z1 = (p.z + *dist1 * d.z), z2 = (p.z + *dist2 * d.z);
+      *int1 = ((d2 > 0) && (*dist1 != kInfLength) && ((z1) > -kHalfTolerance));
+      *int2 = ((d22 > 0) && (*dist2 != kInfLength) && ((z2) > -kHalfTolerance));
+      double dirRho2 = d.x * d.x + d.y * d.y;
+      double zs = kInfLength, ze = kInfLength;
+      if (sT != 0.) zs = dirRho2 / c->tanS;
+      if (eT != 0.) ze = dirRho2 / c->tanE;
+      int cond = (p.x == 0. && p.y == 0. && p.z == 0. && d.z < zs && d.z < ze);
+      if (cond) *dist1 = 0.;
+      if (cond) *dist2 = 0.;
+      *int1 = *int1 || cond;
+      *int2 = *int2 || cond;
+    }
+    if (eT >= kPi / 2 - kThHalfTol && eT <= kPi / 2 + kThHalfTol) {
+      *dist1 = firstRoot;
+      *dist2 = inf;
+      if (d.z < 0.) *dist2 = -1. * p.z / d.z;
+      double z2 = (p.z + *dist2 * d.z), z1 = (p.z + *dist1 * d.z);
+      *int2 = ((*dist2 != kInfLength) && (fabs(z2) < kHalfTolerance) && !(d.z == 0.));
+      *int1 = ((d2 >= 0) && (*dist1 != kInfLength) && (fabs(z1) < kHalfTolerance) && !(d.z == 0.));
+    }
+    if (eT > kPi / 2 + kThHalfTol && sT < eT) {
+      *dist1 = firstRoot;
+      if ((d22 >= 0.) && b2 > 0. && a2 != 0.) secondRoot = ((-b2 - sqrt(fabs(d22))) / NonZero(a2));
+      if ((d22 >= 0.) && b2 <= 0.) secondRoot = ((c2) / NonZero(-b2 + sqrt(fabs(d22))));
+      if (secondRoot < 0.) secondRoot = kInfLength;
+      *dist2 = secondRoot;
+      double z1 = (p.z + *dist1 * d.z), z2 = (p.z + *dist2 * d.z);
+      *int1 = ((d2 >= 0) && (*dist1 != kInfLength) && ((z1) > -kHalfTolerance));
+      *int2 = ((d22 >= 0) && (*dist2 != kInfLength) && ((z2) < kHalfTolerance));
+    }
+  }
+  if (eT > kPi / 2 + kThHalfTol && sT < eT) {
+    secondRoot = kInfLength;
+    if ((d22 >= 0.) && b2 > 0. && a2 != 0.) secondRoot = ((-b2 - sqrt(fabs(d22))) / NonZero(a2));
+    if ((d22 >= 0.) && b2 <= 0.) secondRoot = ((c2) / NonZero(-b2 + sqrt(fabs(d22))));
+    *dist2 = secondRoot;
+    if (sT > kPi / 2 + kThHalfTol) {
+      if ((d2 >= 0.) && b > 0.) firstRoot = ((cc) / NonZero(-b - sqrt(fabs(d2))));
+      if ((d2 >= 0.) && b <= 0. && a != 0.) firstRoot = ((-b + sqrt(fabs(d2))) / NonZero(a));
+      if (firstRoot < 0.) firstRoot = kInfLength;
+      *dist1    = firstRoot;
+      double z1 = (p.z + *dist1 * d.z);
+      *int1     = ((d2 > 0) && (*dist1 != kInfLength) && ((z1) < kHalfTolerance));
+      double z2 = (p.z + *dist2 * d.z);
+      *int2     = ((d22 > 0) && (*dist2 != kInfLength) && ((z2) < kHalfTolerance));
+      double dirRho2 = d.x * d.x + d.y * d.y;
+      double zs = -kInfLength, ze = -kInfLength;
+      if (c->tanS != 0.) zs = -dirRho2 / c->tanS;
+      if (c->tanE != 0.) ze = -dirRho2 / c->tanE;
+      int cond = (p.x == 0. && p.y == 0. && p.z == 0. && d.z > zs && d.z > ze);
+      if (cond) *dist1 = 0.;
+      if (cond) *dist2 = 0.;
+      *int1 = *int1 || cond;
+      *int2 = *int2 || cond;
+    }
+  }
+  if (sT >= kPi / 2 - kThHalfTol && sT <= kPi / 2 + kThHalfTol) {
+    *dist2 = secondRoot;
+    *dist1 = kInfLength;
+    if (d.z > 0.) *dist1 = -1. * p.z / NonZero(d.z);
+    double z1 = (p.z + *dist1 * d.z);
+    double z2 = (p.z + *dist2 * d.z);
+    *int1 = ((*dist1 != kInfLength) && (fabs(z1) < kHalfTolerance) && (d.z != 0.));
+    *int2 = ((d22 >= 0) && (*dist2 != kInfLength) && (fabs(z2) < kHalfTolerance) && (d.z != 0.));
+  }
+}
+
+/* ---- the sphere ---- */
+
+/* SphereStruct(rmin, rmax, sphi, dphi, stheta, dtheta) (SphereStruct.h:285-304):
+ * CheckPhiAngles and CheckThetaAngles set the checked angles and the full-range flags;
+ * the Wedge and the ThetaCone keep the raw constructor angles.  Arguments for which the
+ * reference only reports an error (dphi <= 0, stheta outside [0, pi], dtheta <= 0) are
+ * rejected. */
+static int sphere_init(or_sphere *t, const double *a, char *err, int errlen)
+{
+  const double rmin = a[0], rmax = a[1], sphi = a[2], dphi = a[3], stheta = a[4], dtheta = a[5];
+  if (!(rmin >= 0 && rmax > rmin) || !(dphi > 0) || !(stheta >= 0 && stheta <= kPi) || !(dtheta > 0)) {
+    set_err(err, errlen, "Sphere: needs 0 <= rmin < rmax, dphi > 0, 0 <= stheta <= pi and dtheta > 0");
+    return -1;
+  }
+  t->rmin = rmin;
+  t->rmax = rmax;
+  /* CheckDPhiAngle / CheckSPhiAngle (SphereStruct.h:129-176) */
+  if (dphi >= 2 * kPi - kAngTolerance * 0.5) {
+    t->dPhi    = 2 * kPi;
+    t->sPhi    = 0;
+    t->fullPhi = 1;
+  } else {
+    t->fullPhi = 0;
+    t->dPhi    = dphi;
+    if (sphi < 0)
+      t->sPhi = 2 * kPi - fmod(fabs(sphi), 2 * kPi);
+    else
+      t->sPhi = fmod(sphi, 2 * kPi);
+    if (t->sPhi + t->dPhi > 2 * kPi) t->sPhi -= 2 * kPi;
+  }
+  /* CheckThetaAngles (SphereStruct.h:87-126) */
+  t->sTheta = stheta;
+  if (dtheta + stheta >= kPi)
+    t->dTheta = kPi - stheta;
+  else
+    t->dTheta = dtheta;
+  t->fullTheta = !(t->dTheta - t->sTheta < kPi);
+  t->full      = t->fullPhi && t->fullTheta;
+  t->eTheta    = t->sTheta + t->dTheta;
+  wedge_init(&t->w, dphi, sphi);
+  theta_init(&t->tc, stheta, dtheta);
+  return 0;
+}
+
+/* SphereUtilities::IsCompletelyInside / IsCompletelyOutside (SphereUtilities.h:110-141):
+ * the wedge and the theta cone take part whatever the ranges */
 static int sphere_completely_inside(const or_sphere *t, v3 p)
 {
   double rad = sqrt(v3_dot(p, p));
   int inRad  = (rad < (t->rmax - kTolerance)) && (rad > (t->rmin + kTolerance));
   int cin = 0, cout = 0;
   wedge_ci(&t->w, p, 1, &cin, &cout);
-  int inTheta = theta_completely_inside(t, p);
+  int inTheta = theta_completely_inside(&t->tc, p);
   return inRad && cin && inTheta;
 }
 
@@ -1598,13 +1951,11 @@ static int sphere_completely_outside(const or_sphere *t, v3 p)
   int outRad = (rad > (t->rmax + kTolerance)) || (rad < (t->rmin - kTolerance));
   int cin = 0, cout = 0;
   wedge_ci(&t->w, p, 1, &cin, &cout);
-  int outTheta = theta_completely_outside(t, p);
+  int outTheta = theta_completely_outside(&t->tc, p);
   return outRad || cout || outTheta;
 }
 
-
-/* SphereUtilities::IsPointOnSurfaceAndMovingOut (SphereUtilities.h:143-195); the phi and
- * theta faces do not take part for a full sphere */
+/* SphereUtilities::IsPointOnSurfaceAndMovingOut (SphereUtilities.h:143-195) */
 static int sphere_on_surface_moving(const or_sphere *t, v3 p, v3 d, int movingOut)
 {
   double mag2 = v3_dot(p, p);
@@ -1617,11 +1968,18 @@ static int sphere_on_surface_moving(const or_sphere *t, v3 p, v3 d, int movingOu
     double dmp  = d.x * -p.x + d.y * -p.y + d.z * -p.z;
     inner       = onInner && (movingOut ? dmp > kSqrtTolerance : dmp < -kSqrtTolerance);
   }
-  return (outer || inner) && wedge_contains(&t->w, p) && !theta_completely_outside(t, p);
+  int phiFace = 0, thetaFace = 0;
+  if (t->dPhi < (kTwoPi - kHalfTolerance))
+    phiFace = wedge_moving(&t->w, 1, movingOut, p, d) || wedge_moving(&t->w, 0, movingOut, p, d);
+  if (t->dTheta < (kPi - kHalfTolerance))
+    thetaFace = theta_moving(&t->tc, 1, movingOut, p, d) || theta_moving(&t->tc, 0, movingOut, p, d);
+  int inShell = (mag2 >= t->rmin * t->rmin) && (mag2 <= t->rmax * t->rmax);
+  return ((outer || inner) && wedge_contains(&t->w, p) && theta_contains(&t->tc, p)) ||
+         (phiFace && inShell && theta_contains(&t->tc, p)) || (thetaFace && inShell && wedge_contains(&t->w, p));
 }
 
-/* SphereImplementation::GenericKernelForContainsAndInside (SphereImplementation.h:89-136) */
-static void sphere_ci(const or_sphere *t, v3 p, int *cin, int *cout)
+/* SphereImplementation::GenericKernelForContainsAndInside<ForInside> (SphereImplementation.h:89-136) */
+static void sphere_ci(const or_sphere *t, v3 p, int forInside, int *cin, int *cout)
 {
   double rad2 = v3_dot(p, p);
   if (t->rmin != 0.) {
@@ -1631,25 +1989,61 @@ static void sphere_ci(const or_sphere *t, v3 p, int *cin, int *cout)
     *cin  = rad2 <= minus_tol_sq(t->rmax, kTolerance);
     *cout = rad2 >= plus_tol_sq(t->rmax, kTolerance);
   }
+  if (!t->fullPhi) {
+    int ci = 0, co = 0;
+    wedge_ci(&t->w, p, forInside, &ci, &co);
+    *cout = *cout || co;
+    if (forInside) *cin = *cin && ci;
+  }
+  if (!t->fullTheta) {
+    int ci = forInside ? theta_completely_inside(&t->tc, p) : 0;
+    int co = theta_completely_outside(&t->tc, p);
+    *cout  = *cout || co;
+    if (forInside) *cin = *cin && ci;
+  }
 }
 
-static int sphere_contains(const or_sphere *t, v3 p)
+static int sphere_contains(const or_sphere *t, v3 p) /* SphereImplementation.h:62-70 */
 {
   int cin = 0, cout = 0;
-  sphere_ci(t, p, &cin, &cout);
+  sphere_ci(t, p, 0, &cin, &cout);
   return !cout;
 }
 
 static int sphere_inside(const or_sphere *t, v3 p) /* SphereImplementation.h:74-87 */
 {
   int cin = 0, cout = 0, r = kSurfaceE;
-  sphere_ci(t, p, &cin, &cout);
+  sphere_ci(t, p, 1, &cin, &cout);
   if (cout) r = kOutsideE;
   if (cin) r = kInsideE;
   return r;
 }
 
-/* DistanceToIn (SphereImplementation.h:138-256), full sphere */
+/* SphereImplementation::GetMinDistFromPhi<DistToIn> (SphereImplementation.h:343-386): the
+ * nearer, else the farther, phi-plane crossing that lies on its half-plane, strictly inside
+ * the radial shell and within the theta range */
+static void sphere_min_dist_phi(const or_sphere *t, v3 p, v3 d, int toIn, double *distance)
+{
+  double distPhi1 = kInfLength, distPhi2 = kInfLength;
+  wedge_dist(&t->w, p, d, toIn, &distPhi1, &distPhi2);
+  const or_wedge *w = &t->w;
+  double dist = or_min(distPhi1, distPhi2);
+  v3 tmp      = v3_add(p, v3_scale(dist, d));
+  double rad2 = v3_dot(tmp, tmp);
+  int onFace  = ((dist == distPhi1) && wedge_on_surface(w->a1x, w->a1y, w->n1x, w->n1y, tmp)) ||
+               ((dist == distPhi2) && wedge_on_surface(w->a2x, w->a2y, w->n2x, w->n2y, tmp));
+  int cond1 = onFace && (rad2 > t->rmin * t->rmin) && (rad2 < t->rmax * t->rmax) && theta_contains(&t->tc, tmp);
+  if (cond1) *distance = or_min(dist, *distance);
+  dist   = or_max(distPhi1, distPhi2);
+  tmp    = v3_add(p, v3_scale(dist, d));
+  rad2   = v3_dot(tmp, tmp);
+  onFace = ((dist == distPhi1) && wedge_on_surface(w->a1x, w->a1y, w->n1x, w->n1y, tmp)) ||
+           ((dist == distPhi2) && wedge_on_surface(w->a2x, w->a2y, w->n2x, w->n2y, tmp));
+  int cond2 = onFace && (rad2 > t->rmin * t->rmin) && (rad2 < t->rmax * t->rmax) && theta_contains(&t->tc, tmp);
+  if (!cond1 && cond2) *distance = or_min(dist, *distance);
+}
+
+/* DistanceToIn (SphereImplementation.h:138-256) */
 static double sphere_dist_in(const or_sphere *t, v3 p, v3 d)
 {
   double rad2    = v3_dot(p, p);
@@ -1662,18 +2056,55 @@ static double sphere_dist_in(const or_sphere *t, v3 p, v3 d)
   double sd1 = kInfLength, sd2 = kInfLength;
   if (d2 >= 0.) sd1 = (-pDotV3d - sqrt(fabs(d2)));
   double outerDist = kInfLength, innerDist = kInfLength;
-  if (sd1 >= 0.) outerDist = sd1;
+  if (t->full) {
+    if (sd1 >= 0.) outerDist = sd1;
+  } else {
+    v3 tmp = v3_add(p, v3_scale(sd1, d));
+    if (wedge_contains(&t->w, tmp) && theta_contains(&t->tc, tmp) && (sd1 >= 0.)) outerDist = sd1;
+  }
   if (t->rmin != 0.) {
     c  = rad2 - t->rmin * t->rmin;
     d2 = pDotV3d * pDotV3d - c;
     if (d2 >= 0.) sd2 = (-pDotV3d + sqrt(fabs(d2)));
-    if (sd2 >= 0.) innerDist = sd2;
+    if (t->full) {
+      if (sd2 >= 0.) innerDist = sd2;
+    } else {
+      v3 tmp = v3_add(p, v3_scale(sd2, d));
+      if ((sd2 >= 0.) && wedge_contains(&t->w, tmp) && theta_contains(&t->tc, tmp)) innerDist = sd2;
+    }
   }
   double distance = or_min(outerDist, innerDist);
-  return or_min(kInfLength, distance);
+  if (!t->fullPhi) sphere_min_dist_phi(t, p, d, 1, &distance);
+  double distThetaMin = kInfLength;
+  if (!t->fullTheta) {
+    int int1 = 0, int2 = 0;
+    double dt1 = kInfLength, dt2 = kInfLength;
+    theta_dist_in(&t->tc, p, d, &dt1, &dt2, &int1, &int2);
+    v3 c1 = v3_add(p, v3_scale(dt1, d)), c2 = v3_add(p, v3_scale(dt2, d));
+    double r1 = v3_dot(c1, c1), r2 = v3_dot(c2, c2);
+    int valid1 = (r1 >= t->rmin * t->rmin && r1 <= t->rmax * t->rmax) && int1;
+    int valid2 = (r2 >= t->rmin * t->rmin && r2 <= t->rmax * t->rmax) && int2;
+    if (!t->fullPhi) {
+      valid1 = valid1 && wedge_contains(&t->w, c1);
+      valid2 = valid2 && wedge_contains(&t->w, c2);
+    }
+    if (valid2 && !valid1) distThetaMin = dt2;
+    if (valid1 && !valid2) distThetaMin = dt1;
+    if (valid1 && valid2) distThetaMin = or_min(dt1, dt2);
+  }
+  distance = or_min(distThetaMin, distance);
+  /* a ray aimed at the centre of a theta section enters at the apex */
+  v3 toC        = v3_make(0. - p.x, 0. - p.y, 0. - p.z);
+  double m2     = v3_dot(toC, toC);
+  double newDist = sqrt(m2);
+  double un     = sqrt(m2 + DBL_MIN);
+  if ((t->sTheta > kHalfTolerance || t->eTheta < (kPi - kHalfTolerance)) && (fabs(toC.x / un - d.x) < kHalfTolerance) &&
+      (fabs(toC.y / un - d.y) < kHalfTolerance) && (fabs(toC.z / un - d.z) < kHalfTolerance))
+    distance = or_min(distance, newDist);
+  return distance;
 }
 
-/* DistanceToOut (SphereImplementation.h:258-341), full sphere */
+/* DistanceToOut (SphereImplementation.h:258-341) */
 static double sphere_dist_out(const or_sphere *t, v3 p, v3 d)
 {
   double pDotV3d = v3_dot(p, d);
@@ -1689,46 +2120,131 @@ static double sphere_dist_out(const or_sphere *t, v3 p, v3 d)
     d2 = (pDotV3d * pDotV3d - c);
     if ((d2 >= 0.) && (pDotV3d < 0.)) sd2 = (-pDotV3d - sqrt(fabs(d2)));
   }
-  double snxt = or_min(sd1, sd2);
-  return or_min(kInfLength, snxt);
+  double snxt  = or_min(sd1, sd2);
+  int condSemi = ((t->sTheta == 0. && t->eTheta == kPi / 2.) && d.z >= 0.) ||
+                 ((t->sTheta == kPi / 2. && t->eTheta == kPi) && d.z <= 0.);
+  if (condSemi) return snxt;
+  double distThetaMin = kInfLength;
+  if (!t->fullTheta) {
+    int int1 = 0, int2 = 0;
+    double dt1 = kInfLength, dt2 = kInfLength;
+    theta_dist_out(&t->tc, p, d, &dt1, &dt2, &int1, &int2);
+    if (int2 && !int1) distThetaMin = dt2;
+    if (!int2 && int1) distThetaMin = dt1;
+    if (int2 && int1) distThetaMin = or_min(dt1, dt2);
+  }
+  double distance = or_min(distThetaMin, snxt);
+  if (!t->fullPhi) {
+    if (t->dPhi <= kPi) {
+      double dp1, dp2;
+      wedge_dist(&t->w, p, d, 0, &dp1, &dp2);
+      distance = or_min(or_min(dp1, dp2), distance);
+    } else {
+      sphere_min_dist_phi(t, p, d, 0, &distance);
+    }
+  }
+  return distance;
 }
 
-/* SafetyToIn / SafetyToOut (SphereImplementation.h:388-479), full sphere */
+/* SafetyToIn / SafetyToOut (SphereImplementation.h:388-479) */
 static double sphere_safe_in(const or_sphere *t, v3 p)
 {
   double rad = sqrt(v3_dot(p, p));
   int cin = 0, cout = 0;
-  sphere_ci(t, p, &cin, &cout);
+  sphere_ci(t, p, 1, &cin, &cout);
   if (cin) return -1.0;
   if (!cin && !cout) return 0.0;
+  double safety;
   if (t->rmin != 0.) {
     double safeRMin = t->rmin - rad;
     double safeRMax = rad - t->rmax;
-    return safeRMin > safeRMax ? safeRMin : safeRMax;
+    safety          = safeRMin > safeRMax ? safeRMin : safeRMax;
+  } else {
+    safety = rad - t->rmax;
   }
-  return rad - t->rmax;
+  if (!t->fullPhi) safety = or_max(wedge_safe_in(&t->w, p), safety);
+  if (!t->fullTheta) safety = or_max(theta_safe_in(&t->tc, p), safety);
+  return safety;
 }
 
 static double sphere_safe_out(const or_sphere *t, v3 p)
 {
   double rad = sqrt(v3_dot(p, p));
   int cin = 0, cout = 0;
-  sphere_ci(t, p, &cin, &cout);
+  sphere_ci(t, p, 1, &cin, &cout);
   if (cout) return -1.0;
   if (!cin && !cout) return 0.0;
+  double safety;
   if (t->rmin != 0.) {
     double safeRMin = (rad - t->rmin);
     double safeRMax = (t->rmax - rad);
-    return safeRMin < safeRMax ? safeRMin : safeRMax;
+    safety          = safeRMin < safeRMax ? safeRMin : safeRMax;
+  } else {
+    safety = t->rmax - rad;
   }
-  return t->rmax - rad;
+  if (!t->fullPhi) safety = or_min(wedge_safe_out(&t->w, p), safety);
+  if (!t->fullTheta) safety = or_min(theta_safe_out(&t->tc, p), safety);
+  return safety;
 }
 
-/* UnplacedSphere::Extent, full sphere (source/UnplacedSphere.cpp:76-83) */
+/* UnplacedSphere::Extent with the phi and theta cuts (source/UnplacedSphere.cpp:74-158) */
 static void sphere_extent(const or_sphere *t, v3 *mn, v3 *mx)
 {
-  *mn = v3_make(-t->rmax, -t->rmax, -t->rmax);
-  *mx = v3_make(t->rmax, t->rmax, t->rmax);
+  const double rmax = t->rmax, rmin = t->rmin;
+  *mn = v3_make(-rmax, -rmax, -rmax);
+  *mx = v3_make(rmax, rmax, rmax);
+  double eTheta = t->sTheta + t->dTheta;
+  if (t->full) return;
+  double st1 = 0., st2 = 0.;
+  if (!t->fullTheta) {
+    mx->z = ((t->sTheta <= kPi / 2.) ? rmax : rmin) * cos(t->sTheta);
+    mn->z = ((eTheta <= kPi / 2.) ? rmin : rmax) * cos(eTheta);
+    st1   = sin(t->sTheta);
+    st2   = sin(t->eTheta);
+    if (t->sTheta <= kPi / 2.) {
+      if ((eTheta) < kPi / 2.) {
+        mx->x = rmax * st2;
+        mn->x = -rmax * st2;
+        mx->y = rmax * st2;
+        mn->y = -rmax * st2;
+      }
+    } else {
+      mx->x = rmax * st1;
+      mn->x = -rmax * st1;
+      mx->y = rmax * st1;
+      mn->y = -rmax * st1;
+    }
+  }
+  if (!t->fullPhi) {
+    double Rmax = rmax;
+    if (t->sTheta > kPi / 2.) Rmax *= st1;
+    if (eTheta < kPi / 2.) Rmax *= st2;
+    double Rmin = rmin * or_min(st1, st2);
+    double Rin  = 0.5 * (Rmax + Rmin);
+    int phi0out   = !wedge_contains(&t->w, v3_make(Rin, 0, 0));
+    int phi90out  = !wedge_contains(&t->w, v3_make(0, Rin, 0));
+    int phi180out = !wedge_contains(&t->w, v3_make(-Rin, 0, 0));
+    int phi270out = !wedge_contains(&t->w, v3_make(0, -Rin, 0));
+    if (!(phi0out || phi90out || phi180out || phi270out)) return;
+    double Cx = Rmax * cos(t->sPhi), Dx = Rmax * cos(t->sPhi + t->dPhi);
+    double Cy = Rmax * sin(t->sPhi), Dy = Rmax * sin(t->sPhi + t->dPhi);
+    if (phi0out) mx->x = or_max(Cx, Dx);
+    if (phi90out) mx->y = or_max(Cy, Dy);
+    if (phi180out) mn->x = or_min(Cx, Dx);
+    if (phi270out) mn->y = or_min(Cy, Dy);
+    if (t->dPhi >= kPi) return;
+    double Ax = Rmin * cos(t->sPhi), Bx = Rmin * cos(t->sPhi + t->dPhi);
+    double Ay = Rmin * sin(t->sPhi), By = Rmin * sin(t->sPhi + t->dPhi);
+    double temp;
+    temp  = or_max(Ax, Bx);
+    mx->x = temp > mx->x ? temp : mx->x;
+    temp  = or_max(Ay, By);
+    mx->y = temp > mx->y ? temp : mx->y;
+    temp  = or_min(Ax, Bx);
+    mn->x = temp < mn->x ? temp : mn->x;
+    temp  = or_min(Ay, By);
+    mn->y = temp < mn->y ? temp : mn->y;
+  }
 }
 
 /* ================================================================== */

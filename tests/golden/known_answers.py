@@ -818,6 +818,206 @@ SPHERE_CASES = [
     _case(f"{SP}:861", SPHERE, SPH_S2, "dist_in", _ponrmin2, vmx, 90 / _R2),
 ]
 
+# Sphere phi and theta sections (TestSphere.cpp); `deg` is the test's macro `PI / 180.`,
+# so `a * deg` evaluates as (a * PI) / 180.
+def _deg(a):
+    return a * PI_T / 180.
+
+
+SPH_B5 = (6.0, 8.0, 0.0, (2 * PI_T) / 2, 0.0, PI_T)                    # TestSphere.cpp:210
+SPH_B6 = (6.0, 8.0, PI_T / 6, PI_T / 3, 0.0, PI_T)                     # TestSphere.cpp:238
+SPH_B8 = (6.0, 8.0, PI_T / 6, PI_T / 6, 0.0, PI_T)                     # TestSphere.cpp:257
+SPH_B7 = (6.0, 8.0, PI_T / 6, PI_T / 6, 0.0, PI_T / 6)                 # TestSphere.cpp:313
+SPH_B9 = (6.0, 8.0, PI_T / 6, PI_T / 6, PI_T / 6, PI_T / 6)            # TestSphere.cpp:341
+SPH_SN11 = (0.0, 50.0, 0.0, 2 * PI_T, 0.0, 0.5 * PI_T)                 # TestSphere.cpp:421
+SPH_SN12 = (0.0, 50.0, 0.0, 2 * PI_T, 0.0, 0.25 * PI_T)                # TestSphere.cpp:422
+SPH_SN13 = (0.0, 50.0, 0.0, 2 * PI_T, 0.75 * PI_T, 0.25 * PI_T)        # TestSphere.cpp:423
+SPH_SN14 = (0.0, 50.0, 0.0, 2 * PI_T, 0.25 * PI_T, 0.75 * PI_T)        # TestSphere.cpp:424
+SPH_SN17 = (0.0, 50.0, 0.0, 2 * PI_T, _deg(91.), _deg(89.))            # TestSphere.cpp:427
+SPH_SN22 = (0.0, 50.0, 0.5 * PI_T, 0.5 * PI_T, 0.0, PI_T)              # TestSphere.cpp:431
+SPH_S3 = (45.0, 50.0, 0.0, 2 * PI_T, PI_T / 4, 0.5 * PI_T)             # TestSphere.cpp:433
+SPH_S32 = (45.0, 50.0, 0.0, 2 * PI_T, 0.0, PI_T / 4)                   # TestSphere.cpp:434
+SPH_S33 = (45.0, 50.0, 0.0, 2 * PI_T, PI_T * 3 / 4, PI_T / 4)          # TestSphere.cpp:435
+SPH_S4 = (45.0, 50.0, -PI_T / 4, 0.5 * PI_T, 0.0, 2 * PI_T)            # TestSphere.cpp:437
+SPH_S41 = (5.0, 50.0, -PI_T, 3. * PI_T / 2., 0.0, 2 * PI_T)            # TestSphere.cpp:439
+SPH_S42 = (5.0, 50.0, -PI_T / 2, 3. * PI_T / 2., 0.0, 2 * PI_T)        # TestSphere.cpp:440
+SPH_S5 = (45.0, 50.0, -PI_T / 4, 0.5 * PI_T, PI_T / 4, 0.5 * PI_T)     # TestSphere.cpp:441
+SPH_S9 = (0.0, 410.0, _deg(0), _deg(360), _deg(90), _deg(90))          # TestSphere.cpp:450
+SPH_B658 = (209.6, 211.2658, _deg(0.0), _deg(360), _deg(0.0), _deg(90))  # TestSphere.cpp:488
+SPH_S13 = (5.0, 50.0, 0.0, 2 * PI_T, PI_T / 6., 0.5 * PI_T)            # TestSphere.cpp:501
+SPH_S14 = (5.0, 50.0, 0.0, 2 * PI_T, PI_T / 3., 0.5 * PI_T)            # TestSphere.cpp:502
+_MIN_THETA = _deg(18.0)                                                # TestSphere.cpp:508
+SPH_B830 = (21.45 * 10, 85.0 * 10, 0.0, math.pi * 2, _MIN_THETA, math.pi - 2 * _MIN_THETA)  # TestSphere.cpp:510
+SPH_SNTEST = (0.0, 50.0, 0.0, 2 * PI_T, 0.0, 0.75 * PI_T)              # TestSphere.cpp:963
+SPH_SNTESTB = (0.0, 50.0, 0.0, 2 * PI_T, 0.50 * PI_T, 0.50 * PI_T)     # TestSphere.cpp:1004
+SPH_NORMAL = (80.0, 100.0, 0.0, 2 * PI_T, 0.0, 2.268928027592628)      # TestSphere.cpp:1098
+B830_P = (81.61117212, -27.77179755, 196.4143423)                      # TestSphere.cpp:512-513
+B830_V = (0.1644697995, 0.18507236, 0.9688642354)
+
+_pbig = [(100.0, 0.0, 0.0), (0.0, 100.0, 0.0), (0.0, 0.0, 100.0), (-100.0, 0.0, 0.0), (0.0, -100.0, 0.0),
+         (0.0, 0.0, -100.0)]                                           # TestSphere.cpp:39-41
+_px, _py, _pz = (30.0, 0.0, 0.0), (0.0, 30.0, 0.0), (0.0, 0.0, 30.0)   # TestSphere.cpp:389-390
+_pmx, _pmy, _pmz = (-30.0, 0.0, 0.0), (0.0, -30.0, 0.0), (0.0, 0.0, -30.0)
+_ponphi1, _ponphi2 = (48 / _R2, -48 / _R2, 0.0), (48 / _R2, 48 / _R2, 0.0)  # TestSphere.cpp:394-395
+_pInPhi, _pOverPhi = (48 * 0.866, -24.0, 0.0), (-48 / _R2, 48 / _R2, 0.0)
+_pontheta1 = (0.0, 48 * math.sin(PI_T / 4), 48 * math.cos(PI_T / 4))      # TestSphere.cpp:396-397
+_pontheta2 = (0.0, 48 * math.sin(PI_T / 4), -48 * math.cos(PI_T / 4))
+_ptestphi1, _ptestphi2 = (-100.0, -45 / _R2, 0.0), (-100.0, 45 / _R2, 0.0)  # TestSphere.cpp:399
+_ptesttheta1 = (0.0, 48 / _R2, 100.0)                                   # TestSphere.cpp:401
+_vmxz = (-S2, 0.0, S2)
+_south, _north = (0.0, 0.0, -50.0), (0.0, 0.0, 50.0)                    # TestSphere.cpp:1062, 1071
+
+SPHERE_SECTION_CASES = [
+    _case(f"{SP}:215", SPHERE, SPH_B5, "inside", (-6.354024677915919, 2.724956501738179, -1.095893451057325), None, 1,
+          "eq"),
+    _case(f"{SP}:221", SPHERE, SPH_B5, "inside", (-2.523183636323228, -3.188902592924771, -5.697757856405303), None, 3,
+          "eq"),
+    _case(f"{SP}:229", SPHERE, SPH_B5, "inside", (-6.975035234148935, 0.000000000583791, -0.590663594934467), None, 2,
+          "eq"),
+    _case(f"{SP}:242", SPHERE, SPH_B6, "inside", (5.343263338886987, 3.536603816131425, -2.818150162612158), None, 1,
+          "eq"),
+    _case(f"{SP}:247", SPHERE, SPH_B6, "inside", (6.043467293054153, 0.461937628581358, 3.501873313683026), None, 3,
+          "eq"),
+    _case(f"{SP}:250", SPHERE, SPH_B6, "inside", (0.139868946641446, 0.080753374000628, 6.998136578429498), None, 2,
+          "eq"),
+    _case(f"{SP}:255", SPHERE, SPH_B6, "inside", (4.589551141500899, 2.649778586424563, 4.573258549707597), None, 2,
+          "eq"),
+    _case(f"{SP}:261", SPHERE, SPH_B8, "safe_in", (0.0, 5.0, 0.0), None, 2.5),
+] + [_case(f"{SP}:{ln}", SPHERE, SPH_B8, "safe_in", p, None, 92.0) for ln, p in zip((264, 266, 268, 270, 272, 274), _pbig)
+] + [_case(f"{SP}:{ln}", SPHERE, SPH_B8, "safe_out", p, None, 0.0, "le0")
+     for ln, p in zip((277, 280, 283, 286, 289, 292), _pbig)
+] + [
+    _case(f"{SP}:299", SPHERE, SPH_B8, "safe_out", (0.041433182037376, 3.902131470711286, -6.637895244481554), None,
+          0.0, "le0"),
+    _case(f"{SP}:302", SPHERE, SPH_B8, "safe_in", (0.041433182037376, 3.902131470711286, -6.637895244481554), None,
+          1.91518354715165),
+    _case(f"{SP}:319", SPHERE, SPH_B7, "inside", (2.051950506806283, 1.301790637821730, 6.564666042754737), None, 1,
+          "eq"),
+    _case(f"{SP}:325", SPHERE, SPH_B7, "inside", (3.038887886090341, 3.240358815458723, 5.409735221140894), None, 3,
+          "eq"),
+    _case(f"{SP}:332", SPHERE, SPH_B7, "inside", (2.421058285775014, 2.527543625149363, 6.062177826478448), None, 2,
+          "eq"),
+    _case(f"{SP}:339", SPHERE, SPH_B7, "inside", (2.983684745081379, 1.829651698111631, 6.062177826950138), None, 2,
+          "eq"),
+] + [_case(f"{SP}:{ln}", SPHERE, SPH_B9, "safe_in", p, None, 92.0) for ln, p in zip((343, 345, 347, 349, 351, 353), _pbig)
+] + [_case(f"{SP}:{ln}", SPHERE, SPH_B9, "safe_out", p, None, 0.0, "le0")
+     for ln, p in zip((357, 360, 363, 366, 369, 372), _pbig)
+] + [
+    _case(f"{SP}:376", SPHERE, SPH_B7, "safe_in", (2.051950506806283, 1.301790637821730, 6.564666042754737), None,
+          0.0, "le0"),
+    _case(f"{SP}:379", SPHERE, SPH_B7, "safe_in", (3.038887886090341, 3.240358815458723, 5.409735221140894), None,
+          1.142348737370068),
+    _case(f"{SP}:550", SPHERE, SPH_B658, "inside", (-35.69953348982516, 198.3183279249958, 56.30959457033987), None, 3,
+          "eq"),
+    _case(f"{SP}:557", SPHERE, SPH_S3, "inside", _pontheta1, None, 2, "eq"),
+    _case(f"{SP}:558", SPHERE, SPH_S3, "inside", _pontheta2, None, 2, "eq"),
+    _case(f"{SP}:559", SPHERE, SPH_S4, "inside", _ponphi1, None, 2, "eq"),
+    _case(f"{SP}:561", SPHERE, SPH_S4, "inside", _pOverPhi, None, 3, "eq"),
+    _case(f"{SP}:562", SPHERE, SPH_S4, "inside", _pInPhi, None, 1, "eq"),
+    _case(f"{SP}:563", SPHERE, SPH_S5, "inside", (0.0, 0.0, 100.0), None, 3, "eq"),
+    _case(f"{SP}:565", SPHERE, SPH_S41, "inside", _pmx, None, 2, "eq"),
+    _case(f"{SP}:566", SPHERE, SPH_S42, "inside", _pmx, None, 2, "eq"),
+    _case(f"{SP}:567", SPHERE, SPH_SN11, "inside", pzero, None, 2, "eq"),
+    _case(f"{SP}:568", SPHERE, SPH_SN12, "inside", pzero, None, 2, "eq"),
+    _case(f"{SP}:573", SPHERE, SPH_SN13, "inside", pzero, None, 2, "eq"),
+    _case(f"{SP}:574", SPHERE, SPH_SN13, "inside", _pmz, None, 1, "eq"),
+    _case(f"{SP}:575", SPHERE, SPH_SN12, "inside", _pz, None, 1, "eq"),
+    _case(f"{SP}:576", SPHERE, SPH_SN12, "inside", _px, None, 3, "eq"),
+    _case(f"{SP}:577", SPHERE, SPH_SN11, "inside", _px, None, 2, "eq"),
+    _case(f"{SP}:618", SPHERE, SPH_SN11, "safe_out", pzero, None, 0.0),
+    _case(f"{SP}:621", SPHERE, SPH_SN11, "safe_out", _px, None, 0.0),
+    _case(f"{SP}:623", SPHERE, SPH_SN12, "safe_out", pzero, None, 0.0),
+    _case(f"{SP}:626", SPHERE, SPH_SN12, "safe_out", _pz, None, 20.0),
+    _case(f"{SP}:628", SPHERE, SPH_SN13, "safe_out", _pmz, None, 20.0),
+    _case(f"{SP}:630", SPHERE, SPH_S3, "safe_out", pzero, None, 0.0, "le0"),
+    _case(f"{SP}:635", SPHERE, SPH_S9, "safe_out", pzero, None, 0.0),
+    _case(f"{SP}:638", SPHERE, SPH_S9, "safe_out", _px, None, 0.0),
+    _case(f"{SP}:641", SPHERE, SPH_S41, "safe_out", pzero, None, 0.0, "le0"),
+    _case(f"{SP}:644", SPHERE, SPH_S41, "safe_out", _ponrmax1, None, 0.0),
+    _case(f"{SP}:731", SPHERE, SPH_SN22, "dist_out", (0.0, 49.0, 0.0), vmy, 49.0),
+    _case(f"{SP}:734", SPHERE, SPH_SN22, "dist_out", (-45.0, 0.0, 0.0), vx, 45.0),
+    _case(f"{SP}:740", SPHERE, SPH_S13, "dist_out", (20.0, 0.0, 0.0), vz, 34.641016151377549),
+    _case(f"{SP}:744", SPHERE, SPH_S13, "dist_out", (20.0, 0.0, 0.0), vmz, 11.547005383792508),
+    _case(f"{SP}:748", SPHERE, SPH_S14, "dist_out", (20.0, 0.0, 0.0), vz, 11.547005383792508),
+    _case(f"{SP}:752", SPHERE, SPH_S14, "dist_out", (20.0, 0.0, 0.0), vmz, 34.641016151377549),
+    _case(f"{SP}:762", SPHERE, SPH_SN11, "dist_out", (0.0, 0.0, 20.0), vmz, 20.0),
+    _case(f"{SP}:766", SPHERE, SPH_SN11, "dist_out", pzero, vmz, 0.0),
+    _case(f"{SP}:770", SPHERE, SPH_SN11, "dist_out", pzero, vz, 50.0),
+    _case(f"{SP}:774", SPHERE, SPH_SN11, "dist_out", (10.0, 0.0, 0.0), vmz, 0.0),
+    _case(f"{SP}:778", SPHERE, SPH_SN12, "dist_out", (0.0, 0.0, 20.0), vxmz, 20.0 / math.sqrt(2.0)),
+    _case(f"{SP}:782", SPHERE, SPH_SN12, "dist_out", pzero, vmz, 0.0),
+    _case(f"{SP}:786", SPHERE, SPH_SN12, "dist_out", (10.0, 0.0, 10.0), vz, 38.989794855663561179),
+    _case(f"{SP}:790", SPHERE, SPH_SN12, "dist_out", (10.0, 0.0, 10.0), vmz, 0.0),
+    _case(f"{SP}:794", SPHERE, SPH_SN14, "dist_out", (10.0, 0.0, 10.0), vz, 0.0),
+    _case(f"{SP}:798", SPHERE, SPH_SN14, "dist_out", (10.0, 0.0, 5.0), vz, 5.0),
+    _case(f"{SP}:802", SPHERE, SPH_SN14, "dist_out", (10.0, 0.0, 5.0), _vmxz, 3.5355339059327381968),
+    _case(f"{SP}:806", SPHERE, SPH_SN14, "dist_out", (10.0, 0.0, 10.0), _vmxz, 0.0),
+    _case(f"{SP}:810", SPHERE, SPH_SN12, "dist_out", pzero, vx, 0.0),
+    _case(f"{SP}:819", SPHERE, SPH_SN17, "inside", (16.20075504802145, -22.42917454903122, -41.6469406430184), None,
+          2, "eq"),
+    _case(f"{SP}:822", SPHERE, SPH_SN17, "dist_out", (16.20075504802145, -22.42917454903122, -41.6469406430184),
+          (-0.280469198715188, 0.4463870649961534, 0.8497503261406731), 48.95871780757848768),
+    _case(f"{SP}:837", SPHERE, SPH_SN17, "dist_in", (-10.276604989981144911, -4.7072500741022338389, 1.0),
+          (-0.28873162920537848164, 0.51647890054938394577, -0.80615357816219324061), 1.4874615083453075481),
+    _case(f"{SP}:866", SPHERE, SPH_S3, "dist_in", _ptesttheta1, vmz, 100 - 48 / _R2),
+    _case(f"{SP}:870", SPHERE, SPH_S3, "dist_in", _pontheta1, vz, INF),
+    _case(f"{SP}:872", SPHERE, SPH_S3, "dist_in", _pontheta1, vmz, 0.0, "eq"),
+    _case(f"{SP}:875", SPHERE, SPH_S3, "dist_in", _pontheta2, vz, 0.0, "eq"),
+    _case(f"{SP}:878", SPHERE, SPH_S3, "dist_in", _pontheta2, vmz, INF),
+    _case(f"{SP}:881", SPHERE, SPH_S32, "dist_in", _pontheta1, vz, 0.0, "eq"),
+    _case(f"{SP}:885", SPHERE, SPH_S32, "dist_in", _pontheta1, vmz, INF),
+    _case(f"{SP}:889", SPHERE, SPH_S33, "dist_in", _pontheta2, vz, INF),
+    _case(f"{SP}:892", SPHERE, SPH_S33, "dist_in", _pontheta2, vmz, 0.0, "eq"),
+    _case(f"{SP}:896", SPHERE, SPH_S4, "dist_in", (0.0, 100.0, 0.0), vmy, INF),
+    _case(f"{SP}:899", SPHERE, SPH_S4, "dist_in", (0.0, 0.0, 100.0), vmz, 50.0),
+    _case(f"{SP}:902", SPHERE, SPH_S4, "dist_in", pzero, vy, INF),
+    _case(f"{SP}:905", SPHERE, SPH_S4, "dist_in", pzero, vx, 45.0),
+    _case(f"{SP}:908", SPHERE, SPH_S4, "dist_in", _ptestphi1, vx, 100 + 45 / _R2),
+    _case(f"{SP}:911", SPHERE, SPH_S4, "dist_in", _ponphi1, vmxmy, INF),
+    _case(f"{SP}:915", SPHERE, SPH_S4, "dist_in", _ponphi1, vxy, 0.0),
+    _case(f"{SP}:918", SPHERE, SPH_S4, "dist_in", _ptestphi2, vx, 100 + 45 / _R2),
+    _case(f"{SP}:921", SPHERE, SPH_S4, "dist_in", _ponphi2, vmxy, INF),
+    _case(f"{SP}:925", SPHERE, SPH_S4, "dist_in", _ponphi2, vxmy, 0.0),
+    _case(f"{SP}:928", SPHERE, SPH_S3, "dist_in", pzero, vx, 45.0),
+    _case(f"{SP}:930", SPHERE, SPH_S3, "dist_in", _ptesttheta1, vmz, 100 - 48 / _R2),
+    _case(f"{SP}:936", SPHERE, SPH_B658, "dist_in", pzero, vz, 209.59999999999999432),
+    _case(f"{SP}:940", SPHERE, SPH_S13, "dist_in", (20.0, 0.0, -70.0), vz, 58.452994616207498),
+    _case(f"{SP}:944", SPHERE, SPH_S13, "dist_in", (20.0, 0.0, 70.0), vmz, 35.358983848622451),
+    _case(f"{SP}:948", SPHERE, SPH_S14, "dist_in", (20.0, 0.0, -70.0), vz, 35.358983848622451),
+    _case(f"{SP}:952", SPHERE, SPH_S14, "dist_in", (20.0, 0.0, 70.0), vmz, 58.452994616207498),
+] + [_case(f"{SP}:{ln}", SPHERE, SPH_SNTESTB, "dist_out", p, d, e) for ln, p, d, e in (
+    (1006, pzero, vmz, 50.0), (1009, pzero, vz, 0.0), (1012, _px, vz, 0.0), (1015, _px, vmz, 40.0),
+    (1018, _py, vz, 0.0), (1021, _py, vmz, 40.0), (1024, _pmz, vz, 30.0), (1027, _pmz, vmz, 20.0),
+    (1030, (30.0, 0.0, -30.0), vz, 30.0), (1033, (30.0, 0.0, -30.0), vmz, 10.0), (1036, _px, vx, 20.0),
+    (1039, _px, vmx, 80.0), (1042, _pmx, vx, 80.0), (1045, _pmx, vmx, 20.0), (1048, _pmy, vy, 80.0),
+    (1051, _pmy, vmy, 20.0), (1054, _pmy, vx, 40.0), (1057, _pmy, vmx, 40.0))
+] + [
+    _case(f"{SP}:1060", SPHERE, SPH_SNTESTB, "dist_in", pzero, vmz, 0.0),
+    _case(f"{SP}:1064", SPHERE, SPH_SNTESTB, "dist_in", _south, vz, 0.0),
+    _case(f"{SP}:1066", SPHERE, SPH_SNTESTB, "inside", _south, None, 2, "eq"),
+    _case(f"{SP}:1067", SPHERE, SPH_SNTESTB, "inside", pzero, None, 2, "eq"),
+    _case(f"{SP}:1068", SPHERE, SPH_SNTESTB, "inside", _px, None, 2, "eq"),
+    _case(f"{SP}:1069", SPHERE, SPH_SNTESTB, "inside", _pmy, None, 2, "eq"),
+    _case(f"{SP}:1073", SPHERE, SPH_SNTESTB, "dist_in", _north, vmz, 50.0),
+    _case(f"{SP}:1075", SPHERE, SPH_SNTESTB, "inside", _north, None, 3, "eq"),
+    _case(f"{SP}:1078", SPHERE, SPH_SNTEST, "dist_in", _south, vz, 50.0),
+    _case(f"{SP}:1079", SPHERE, SPH_SNTEST, "inside", _south, None, 3, "eq"),
+    _case(f"{SP}:1082", SPHERE, SPH_SNTEST, "dist_in", _north, vmz, 0.0),
+    _case(f"{SP}:1084", SPHERE, SPH_SNTEST, "inside", _north, None, 2, "eq"),
+    _case(f"{SP}:1088", SPHERE, SPH_SNTEST, "inside", _px, None, 1, "eq"),
+    _case(f"{SP}:1089", SPHERE, SPH_SNTEST, "inside", _py, None, 1, "eq"),
+    _case(f"{SP}:1092", SPHERE, SPH_SNTEST, "inside", _pz, None, 1, "eq"),
+    _case(f"{SP}:1093", SPHERE, SPH_SNTEST, "inside", _pmz, None, 3, "eq"),
+    _case(f"{SP}:1094", SPHERE, SPH_SNTESTB, "inside", _pz, None, 3, "eq"),
+    _case(f"{SP}:1095", SPHERE, SPH_SNTESTB, "inside", _pmz, None, 1, "eq"),
+    _case(f"{SP}:1100", SPHERE, SPH_NORMAL, "inside", (-57.1682, -73.6533, -32.3008), None, 1, "eq"),
+    _case(f"{SP}:1107", SPHERE, SPH_NORMAL, "inside", (-58.16821296689909, -74.65330731271325, -32.30081589545529),
+          None, 2, "eq"),
+    _case(f"{SP}:1114", SPHERE, SPH_NORMAL, "inside", (46.76611644842609, -40.66413203238494, -52.00144394546794),
+          None, 2, "eq"),
+]
+SPHERE_CASES += SPHERE_SECTION_CASES
+
 POLYCONE = 6
 PC = "test/unit_tests/TestPolycone.cpp"
 KPI_V = 3.14159265358979323846  # vecgeom::kPi

@@ -63,6 +63,19 @@ def test_kernel_known_answer(vgnav, cuda, case):
     assert KA.check(case, float(out[0])), (case["ref"], float(out[0]))
 
 
+def test_kernel_sphere_b830(vgnav, cuda):
+    """TestSphere.cpp:754-757 (b830): DistanceToOut of a theta-sectioned shell lands on its surface."""
+    geo = vgnav.Geometry(single_shape(KA.SPHERE, KA.SPH_B830))
+    p, v = KA.B830_P, KA.B830_V
+    dist = np.zeros(1)
+    geo.shape(0, OPS["dist_out"], vgnav.SOA3D(*[np.array([c]) for c in p]), vgnav.SOA3D(*[np.array([c]) for c in v]),
+              dist)
+    q = [np.array([p[i] + float(dist[0]) * v[i]]) for i in range(3)]
+    out = np.zeros(1)
+    geo.shape(0, OPS["inside"], vgnav.SOA3D(*q), vgnav.SOA3D(*[np.zeros(1)] * 3), out)
+    assert int(out[0]) == 2
+
+
 def test_tube_points_bit_exact(oracle, vgnav, cuda):
     """Tube(10,50,100) with 2^20 points inside: DistanceToOut and SafetyToOut, plus the other queries."""
     torch = cuda
@@ -288,6 +301,19 @@ SHAPE_SETS = [
     ("sphere-solid", W.SPHERE, (0.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
     ("sphere-shell", W.SPHERE, (45.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
     ("sphere-shell-rotated-wedge", W.SPHERE, (6.0, 8.0, 1.0, W.K_TWO_PI, 0.0, W.K_PI)),
+    ("sphere-phi-quarter-shell", W.SPHERE, KA.SPH_S4),
+    ("sphere-phi-270-solid", W.SPHERE, (0.0, 50.0, -0.5 * W.K_PI, 1.5 * W.K_PI, 0.0, W.K_PI)),
+    ("sphere-phi-half-solid", W.SPHERE, KA.SPH_SN22),
+    ("sphere-theta-band-shell", W.SPHERE, KA.SPH_S3),
+    ("sphere-theta-band-thick", W.SPHERE, KA.SPH_S13),
+    ("sphere-theta-north-cap", W.SPHERE, KA.SPH_SN12),
+    ("sphere-theta-south-cap", W.SPHERE, KA.SPH_SN13),
+    ("sphere-upper-hemisphere", W.SPHERE, KA.SPH_SN11),
+    ("sphere-lower-hemisphere", W.SPHERE, KA.SPH_SNTESTB),
+    ("sphere-theta-past-equator", W.SPHERE, KA.SPH_SN14),
+    ("sphere-theta-91-180deg", W.SPHERE, KA.SPH_SN17),
+    ("sphere-patch-phi-theta", W.SPHERE, KA.SPH_S5),
+    ("sphere-patch-b9", W.SPHERE, KA.SPH_B9),
     ("polycone-4plane", W.POLYCONE, KA.PCON1),
     ("polycone-phi-section-mypcone", W.POLYCONE, KA.MYPCONE),
     ("polycone-4plane-half-sector", W.POLYCONE, KA._pcon(-1.0, W.K_PI, (-1.0, -0.5, 0.5, 2.0), (0.1, 0.0, 0.0, 0.4),
@@ -300,6 +326,10 @@ SHAPE_SETS = [
 ]
 
 
+# sampling boxes of sections much smaller than their full shape's box
+SAMPLE_BOXES = {"sphere-patch-b9": ((0.0, 0.0, 2.0), (7.0, 7.0, 8.0))}
+
+
 @pytest.mark.parametrize("name,shape,params", SHAPE_SETS, ids=[s[0] for s in SHAPE_SETS])
 def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda):
     """Every query at points inside, outside and on the surface equals the oracle bit for bit."""
@@ -308,7 +338,8 @@ def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda)
     geo = vgnav.Geometry(desc)
     rng = np.random.Generator(np.random.PCG64(zlib.crc32(name.encode())))
     n = 100000
-    lo, hi = W.shape_bbox(shape, params)
+    lo, hi = SAMPLE_BOXES.get(name, W.shape_bbox(shape, params))
+    lo, hi = np.asarray(lo, dtype=np.float64), np.asarray(hi, dtype=np.float64)
     mid, half = 0.5 * (lo + hi), 0.65 * (hi - lo)  # the bounding box enlarged by 30 %
     x, y, z = (rng.uniform(mid[k] - half[k], mid[k] + half[k], n) for k in range(3))
     # points on the coordinate planes and axes and at the origin (exact zeros take their own branches)

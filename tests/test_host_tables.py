@@ -70,6 +70,11 @@ def test_bvh_depth_rule(oracle):
     (W.CONE, (10.0, 30.0, 20.0, 60.0, 40.0, 0.5 * W.K_PI, 0.5 * W.K_PI), (-60.0, 0.0, -40.0), (0.0, 60.0, 40.0)),
     # TestSphere.cpp:63-68 (b1: rmax 3)
     (W.SPHERE, (0.0, 3.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI), (-3.0, -3.0, -3.0), (3.0, 3.0, 3.0)),
+    # UnplacedSphere::Extent with cuts (source/UnplacedSphere.cpp:74-158): TestSphere.cpp:69-74
+    # (b2: a 30-120 degree phi section) and a theta cap of 45 degrees
+    (W.SPHERE, (0.0, 3.0, W.K_PI / 6, W.K_PI / 2, 0.0, W.K_PI), (-1.5, 0.0, -3.0), (2.59808, 3.0, 3.0)),
+    (W.SPHERE, (0.0, 50.0, 0.0, W.K_TWO_PI, 0.0, 0.25 * W.K_PI), (-50.0 * math.sin(0.25 * W.K_PI),) * 2 + (0.0,),
+     (50.0 * math.sin(0.25 * W.K_PI),) * 2 + (50.0,)),
     # TestPolycone.cpp:329-333 ("SimpleTube+Cone")
     (W.POLYCONE, (0.0, 360.0 * W.K_PI / 180.0, 3.0, -10.0, 0.0, 10.0, 0.0, 0.0, 0.0, 70.0, 70.0, 80.0),
      (-80.0, -80.0, -10.0), (80.0, 80.0, 10.0)),
@@ -105,13 +110,14 @@ def test_invalid_descriptions_rejected(vgnav):
     with pytest.raises(N.VgnError) as e:
         HostTables(b.build())
     assert e.value.code == N.VGN_ERR_ARG
-    for shape, params in ((W.SPHERE, (0.0, 10.0, 0.0, 1.0, 0.0, W.K_PI)),   # phi section
-                          (W.SPHERE, (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 1.0))):  # theta section
+    for params in ((0.0, 10.0, 0.0, 0.0, 0.0, W.K_PI),           # sphere dphi <= 0
+                   (0.0, 10.0, 0.0, W.K_TWO_PI, -0.1, W.K_PI),   # stheta < 0
+                   (0.0, 10.0, 0.0, W.K_TWO_PI, 0.3, 0.0)):      # dtheta <= 0
         b = W.GeometryBuilder()
-        b.place_world(b.logical(shape, params))
+        b.place_world(b.logical(W.SPHERE, params))
         with pytest.raises(N.VgnError) as e:
             HostTables(b.build())
-        assert e.value.code == N.VGN_ERR_UNSUPPORTED
+        assert e.value.code == N.VGN_ERR_ARG
     b = W.GeometryBuilder()
     lv = b.logical(99, (1.0,))
     b.place_world(lv)

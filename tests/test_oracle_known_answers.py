@@ -23,3 +23,12 @@ def test_oracle_known_answer(oracle, case):
     d = [np.array([v]) for v in (case["d"] or (0.0, 0.0, 0.0))]
     val = float(g.shape(0, OPS[case["op"]], *p, *d)[0])
     assert KA.check(case, val), f"{case['ref']}: {case['op']} -> {val!r}, expected {case['cmp']} {case['expect']!r}"
+
+
+def test_oracle_sphere_b830(oracle):
+    """TestSphere.cpp:754-757 (b830): DistanceToOut of a theta-sectioned shell lands on its surface."""
+    g = oracle.OracleGeometry(single_shape(KA.SPHERE, KA.SPH_B830))
+    p, v = KA.B830_P, KA.B830_V
+    dist = float(g.shape(0, OPS["dist_out"], *[np.array([c]) for c in p], *[np.array([c]) for c in v])[0])
+    q = [np.array([p[i] + dist * v[i]]) for i in range(3)]
+    assert int(g.shape(0, OPS["inside"], *q, *[np.zeros(1)] * 3)[0]) == 2

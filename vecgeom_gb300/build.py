@@ -24,13 +24,15 @@ INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-# (source, extra nvcc flags)
+# (source, object name, extra nvcc flags); the navigation kernels are compiled twice:
+# with the phi/theta section code (namespace `sections`) and without it (`full_ranges`)
 UNITS = [
-    ("kernels_nav.cu", ["-fmad=false"]),
-    ("kernels_sort.cu", []),
-    ("host_geometry.cpp", []),
-    ("host_shapes.cpp", []),
-    ("vgnav_api.cpp", []),
+    ("kernels_nav.cu", "kernels_nav_sections", ["-fmad=false", "-DVGN_SECTIONS=1"]),
+    ("kernels_nav.cu", "kernels_nav_full_ranges", ["-fmad=false", "-DVGN_SECTIONS=0"]),
+    ("kernels_sort.cu", "kernels_sort", []),
+    ("host_geometry.cpp", "host_geometry", []),
+    ("host_shapes.cpp", "host_shapes", []),
+    ("vgnav_api.cpp", "vgnav_api", []),
 ]
 
 
@@ -41,10 +43,11 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libvgnav")
 
 
-def _compile(nvcc: str, src: str, extra: list[str]) -> Path:
-    out = BUILD / (src.replace(".", "_") + ".o")
+def _compile(nvcc: str, src: str, name: str, extra: list[str]) -> Path:
+    out = BUILD / (name + ".o")
     srcp = CSRC / src
-    deps = [srcp] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "vgnav.h"]
+    deps = [srcp] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.inc"))
+    deps += [INCLUDE / "vgnav.h"]
     if out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return out
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(INCLUDE), "-I", str(CSRC)]
@@ -56,7 +59,7 @@ def _compile(nvcc: str, src: str, extra: list[str]) -> Path:
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
-    (BUILD / (src + ".ptxas.txt")).write_text(res.stderr)
+    (BUILD / (name + ".ptxas.txt")).write_text(res.stderr)
     return out
 
 
@@ -66,7 +69,7 @@ def build(verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
-        objs = list(ex.map(lambda u: _compile(nvcc, u[0], u[1]), UNITS))
+        objs = list(ex.map(lambda u: _compile(nvcc, *u), UNITS))
     if not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
         cmd = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-cudart", "static", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)

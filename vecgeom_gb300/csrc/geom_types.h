@@ -161,10 +161,15 @@ enum { TrdDx1 = 0, TrdDx2, TrdDy1, TrdDy2, TrdDz, TrdX2minusX1, TrdY2minusY1, Tr
 // each of 4), then the TrapezoidStruct parameters and cached values
 enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, TrapTheta = 17, TrapPhi, TrapDy1, TrapDx1, TrapDx2,
        TrapTanAlpha1, TrapDy2, TrapDx3, TrapDx4, TrapTanAlpha2, TrapTthetaCphi, TrapTthetaSphi, kTrapSize = 32 };
-// Sphere (full phi and theta): radii, the phi wedge's along/normal vectors and raw
-// delta-phi, the theta cone's raw start/end angles and tangents
+// Sphere: radii, the phi wedge's along/normal vectors and raw delta-phi (a Wedge block),
+// the theta cone's raw start/end angles and tangents, the fFullSphere flag; then the
+// theta cone's squared tangents, bisector tangent and face slopes, the checked fDPhi,
+// fDTheta and eTheta, the fFullPhiSphere / fFullThetaSphere flags (1 or 0) and the
+// checked fSPhi
 enum { SphRmin = 0, SphRmax, SphA1x, SphA1y, SphA2x, SphA2y, SphN1x, SphN1y, SphN2x, SphN2y, SphWedgeDPhi,
-       SphSTheta, SphETheta, SphTanSTheta, SphTanETheta, SphPad, kSphereSize };
+       SphSTheta, SphETheta, SphTanSTheta, SphTanETheta, SphFull, SphTanSTheta2, SphTanETheta2, SphTanBisector,
+       SphSlope1, SphSlope2, SphDPhi, SphDTheta, SphEThetaChk, SphFullPhi, SphFullTheta, SphSPhi, SphPad,
+       kSphereSize };
 // Polycone, variable length: [0] section count n, [1, n+1] the n+1 z planes, [n+2, 2n+1]
 // the section z shifts, then n cone rows of kConeSize doubles, then the raw phi start and
 // total angle

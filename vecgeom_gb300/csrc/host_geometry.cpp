@@ -361,6 +361,7 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
       err = "logical volume " + std::to_string(i) + ": " + err;
       return rc;
     }
+    g.sections = g.sections || shape_row_has_sections(d.lv_shape[i], g.shape.data() + g.lv[i].shape_row);
   }
   for (int i = 0; i < d.n_placed; ++i) {
     const int l = d.pv_logical[i], m = d.pv_mother[i];
@@ -536,6 +537,7 @@ static int build_isin_row(int shape, const double *r, std::vector<float> &out)
     v.assign(r, r + irow::kTrapRow);
     break;
   case kSphere: {  // SphereImplementation.h:388-420, SphereUtilities.h:54-108 (full sphere)
+    if (r[row::SphFull] == 0.) return -1;  // phi or theta sections: FP64 only
     const double rmin = r[row::SphRmin], rmax = r[row::SphRmax];
     v = {rmin != 0. ? 1. : 0., rmin, rmax, std::fabs(rmax * (rmax - 2.0 * kTolerance)),
          rmax * (rmax + 2.0 * kTolerance), rmin * (rmin + 2.0 * kTolerance),

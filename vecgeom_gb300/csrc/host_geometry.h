@@ -73,6 +73,7 @@ struct HostGeometry {
   std::vector<ISafe> iprim_safe;
   std::vector<IXForm> ixf;
   std::vector<float> isin;  // interval SafetyToIn rows (geom_types.h irow), (lo, hi) pairs
+  bool sections = false;    // some shape has a phi or theta section: needs the `sections` kernel set
 };
 
 // Returns 0 on success, a VGN_ERR_* code otherwise (message in err).
@@ -88,5 +89,6 @@ Vec3 xform_inverse_transform(const HostXForm &m, const Vec3 &p);
 int shape_make_row(int32_t type, const double *params, int32_t n_avail, std::vector<double> &shape, std::string &err);
 int shape_param_count(int32_t type, const double *params, int32_t n_avail);
 void shape_extent(int32_t type, const double *row, Vec3 &mn, Vec3 &mx);
+bool shape_row_has_sections(int32_t type, const double *row);  // a phi or theta section
 
 }  // namespace vgn

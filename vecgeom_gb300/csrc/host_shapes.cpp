@@ -288,27 +288,47 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     return VGN_OK;
   }
   case kSphere: {
-    // SphereStruct(rmin, rmax, sphi, dphi, stheta, dtheta) (SphereStruct.h:285-304), full
-    // sphere only; its Wedge (source/Wedge_Evolution.cpp:17-99) and ThetaCone
-    // (ThetaCone_Evolution.h:62-82) are built from the raw constructor angles
+    // SphereStruct(rmin, rmax, sphi, dphi, stheta, dtheta) (SphereStruct.h:285-304):
+    // CheckPhiAngles / CheckThetaAngles (SphereStruct.h:87-185) give the checked angles
+    // and the full-range flags; the Wedge (source/Wedge_Evolution.cpp:17-99) and the
+    // ThetaCone (ThetaCone_Evolution.h:62-82) keep the raw constructor angles.  Arguments
+    // the reference only reports are rejected.
     const double rmin = p[0], rmax = p[1], sphi = p[2], dphi = p[3], stheta = p[4], dtheta = p[5];
-    if (!(rmin >= 0 && rmax > rmin)) {
-      err = "Sphere needs 0 <= rmin < rmax";
+    if (!(rmin >= 0 && rmax > rmin) || !(dphi > 0) || !(stheta >= 0 && stheta <= kPi) || !(dtheta > 0)) {
+      err = "Sphere needs 0 <= rmin < rmax, dphi > 0, 0 <= stheta <= pi and dtheta > 0";
       return VGN_ERR_ARG;
     }
-    if (!(dphi >= kTwoPi - kAngTolerance * 0.5) || stheta != 0. || !(dtheta + stheta >= kPi)) {
-      err = "Sphere phi and theta sections are not supported";
-      return VGN_ERR_UNSUPPORTED;
+    const bool fullPhi     = dphi >= 2 * kPi - kAngTolerance * 0.5;
+    const double dPhiChk   = fullPhi ? 2 * kPi : dphi;
+    const double dThetaChk = dtheta + stheta >= kPi ? kPi - stheta : dtheta;
+    const bool fullTheta   = !(dThetaChk - stheta < kPi);
+    double sPhiChk         = 0;
+    if (!fullPhi) {
+      sPhiChk = sphi < 0 ? 2 * kPi - std::fmod(std::fabs(sphi), 2 * kPi) : std::fmod(sphi, 2 * kPi);
+      if (sPhiChk + dPhiChk > 2 * kPi) sPhiChk -= 2 * kPi;
     }
     double r[row::kSphereSize] = {};
-    r[row::SphRmin]      = rmin;
-    r[row::SphRmax]      = rmax;
+    r[row::SphRmin] = rmin;
+    r[row::SphRmax] = rmax;
     wedge_fill(r + row::SphA1x, dphi, sphi);  // SphA1x..SphWedgeDPhi is a Wedge block
     const double sT = stheta, eT = stheta + dtheta;
-    r[row::SphSTheta]    = sT;
-    r[row::SphETheta]    = eT;
-    r[row::SphTanSTheta] = std::tan(sT > kPi / 2 ? kPi - sT : sT);
-    r[row::SphTanETheta] = std::tan(eT > kPi / 2 ? kPi - eT : eT);
+    const double ts = sT > kPi / 2 ? kPi - sT : sT, te = eT > kPi / 2 ? kPi - eT : eT;
+    r[row::SphSTheta]      = sT;
+    r[row::SphETheta]      = eT;
+    r[row::SphTanSTheta]   = std::tan(ts);
+    r[row::SphTanETheta]   = std::tan(te);
+    r[row::SphTanSTheta2]  = r[row::SphTanSTheta] * r[row::SphTanSTheta];
+    r[row::SphTanETheta2]  = r[row::SphTanETheta] * r[row::SphTanETheta];
+    r[row::SphTanBisector] = (sT > kPi / 2 && eT > kPi / 2) ? std::tan(ts - (dtheta / 2)) : std::tan(ts + (dtheta / 2));
+    r[row::SphSlope1]      = std::tan(kPi / 2 - sT);
+    r[row::SphSlope2]      = std::tan(kPi / 2 - eT);
+    r[row::SphDPhi]        = dPhiChk;
+    r[row::SphDTheta]      = dThetaChk;
+    r[row::SphEThetaChk]   = stheta + dThetaChk;
+    r[row::SphFullPhi]     = fullPhi ? 1. : 0.;
+    r[row::SphFullTheta]   = fullTheta ? 1. : 0.;
+    r[row::SphFull]        = fullPhi && fullTheta ? 1. : 0.;
+    r[row::SphSPhi]        = sPhiChk;
     shape.insert(shape.end(), r, r + row::kSphereSize);
     return VGN_OK;
   }
@@ -363,6 +383,20 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     return VGN_OK;
   }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
+  }
+}
+
+bool shape_row_has_sections(int32_t type, const double *r)
+{
+  switch (type) {
+  case kTube: return r[row::TubeDphi] < 2. * kPi;
+  case kCone: return r[row::ConeDPhi] < 2. * kPi;
+  case kPolycone: {  // the polycone's phi range lives in its section cones
+    const int n = (int)r[row::PconNSec];
+    return r[row::pcon_cone(n, 0) + row::ConeDPhi] < 2. * kPi;
+  }
+  case kSphere: return r[row::SphFull] == 0.;
+  default: return false;
   }
 }
 
@@ -473,10 +507,66 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mx = {tree(x, mx2), tree(y, mx2), dz};
     return;
   }
-  case kSphere: {  // UnplacedSphere::Extent, full sphere (source/UnplacedSphere.cpp:76-83)
-    const double rmax = r[row::SphRmax];
+  case kSphere: {  // UnplacedSphere::Extent with the phi and theta cuts (source/UnplacedSphere.cpp:74-158)
+    auto vmin = [](double a, double b) { return a < b ? a : b; };
+    auto vmax = [](double a, double b) { return a > b ? a : b; };
+    const double rmax = r[row::SphRmax], rmin = r[row::SphRmin];
+    const double sTheta = r[row::SphSTheta], eTheta = r[row::SphEThetaChk];
     mn = {-rmax, -rmax, -rmax};
     mx = {rmax, rmax, rmax};
+    if (r[row::SphFull] != 0.) return;
+    double st1 = 0., st2 = 0.;
+    if (r[row::SphFullTheta] == 0.) {
+      mx.z = ((sTheta <= kPi / 2.) ? rmax : rmin) * std::cos(sTheta);
+      mn.z = ((eTheta <= kPi / 2.) ? rmin : rmax) * std::cos(eTheta);
+      st1  = std::sin(sTheta);
+      st2  = std::sin(eTheta);
+      if (sTheta <= kPi / 2.) {
+        if (eTheta < kPi / 2.) {
+          mx.x = rmax * st2;
+          mn.x = -rmax * st2;
+          mx.y = rmax * st2;
+          mn.y = -rmax * st2;
+        }
+      } else {
+        mx.x = rmax * st1;
+        mn.x = -rmax * st1;
+        mx.y = rmax * st1;
+        mn.y = -rmax * st1;
+      }
+    }
+    if (r[row::SphFullPhi] == 0.) {
+      double Rmax = rmax;
+      if (sTheta > kPi / 2.) Rmax *= st1;
+      if (eTheta < kPi / 2.) Rmax *= st2;
+      const double Rmin = rmin * vmin(st1, st2);
+      const double Rin  = 0.5 * (Rmax + Rmin);
+      const double *w   = r + row::SphA1x;
+      const bool phi0out   = !wedge_contains(w, Rin, 0);
+      const bool phi90out  = !wedge_contains(w, 0, Rin);
+      const bool phi180out = !wedge_contains(w, -Rin, 0);
+      const bool phi270out = !wedge_contains(w, 0, -Rin);
+      if (!(phi0out || phi90out || phi180out || phi270out)) return;
+      const double sphi = r[row::SphSPhi], dphi = r[row::SphDPhi];
+      const double Cx = Rmax * std::cos(sphi), Dx = Rmax * std::cos(sphi + dphi);
+      const double Cy = Rmax * std::sin(sphi), Dy = Rmax * std::sin(sphi + dphi);
+      if (phi0out) mx.x = vmax(Cx, Dx);
+      if (phi90out) mx.y = vmax(Cy, Dy);
+      if (phi180out) mn.x = vmin(Cx, Dx);
+      if (phi270out) mn.y = vmin(Cy, Dy);
+      if (dphi >= kPi) return;
+      const double Ax = Rmin * std::cos(sphi), Bx = Rmin * std::cos(sphi + dphi);
+      const double Ay = Rmin * std::sin(sphi), By = Rmin * std::sin(sphi + dphi);
+      double temp;
+      temp = vmax(Ax, Bx);
+      mx.x = temp > mx.x ? temp : mx.x;
+      temp = vmax(Ay, By);
+      mx.y = temp > mx.y ? temp : mx.y;
+      temp = vmin(Ax, Bx);
+      mn.x = temp < mn.x ? temp : mn.x;
+      temp = vmin(Ay, By);
+      mn.y = temp < mn.y ? temp : mn.y;
+    }
     return;
   }
   case kPolycone: {

@@ -13,6 +13,7 @@
 
 namespace vgn {
 namespace dev {
+inline namespace VGN_KSET {
 
 __device__ __forceinline__ State load_state(const vgn_state *s, int64_t i)
 {
@@ -252,7 +253,10 @@ __global__ void __launch_bounds__(256) shape_kernel_fp64(int type, const double 
   }
 }
 
+}  // namespace VGN_KSET
 }  // namespace dev
+
+namespace VGN_KSET {
 
 static inline unsigned grid_for(int64_t n, int block, int max_blocks)
 {
@@ -425,4 +429,5 @@ cudaError_t launch_shape_fp64(int op, int type, const double *row, int64_t n, co
   return cudaGetLastError();
 }
 
+}  // namespace VGN_KSET
 }  // namespace vgn

@@ -53,22 +53,14 @@ struct JobTable {
   int32_t n_jobs;
 };
 static_assert(sizeof(JobTable) < 32000, "kernel parameters are limited to 32764 bytes");
-// queue reset + one persistent launch over all jobs
-cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, int reloc, int num_sms, int variant,
-                              cudaStream_t s);
-
-// navigation kernels (kernels_nav.cu); mixed = FP32-interval box decisions
-cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s);
-int step_variant_count();
-cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, double *pz, const double *dx,
-                        const double *dy, const double *dz, const double *slimit, vgn_state *state, int max_steps,
-                        int32_t *nsteps, bool mixed, int max_blocks, cudaStream_t s);
-cudaError_t launch_safety(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
-                          const vgn_state *in, double *safety, bool mixed, int max_blocks, cudaStream_t s);
-cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const double *py, const double *pz,
-                          vgn_state *out, bool mixed, int max_blocks, cudaStream_t s);
-cudaError_t launch_shape_fp64(int op, int type, const double *row, int64_t n, const double *px, const double *py,
-                              const double *pz, const double *dx, const double *dy, const double *dz, double *out,
-                              int max_blocks, cudaStream_t s);
+// Navigation kernels (kernels_nav.cu), compiled twice: `sections` handles phi and theta
+// sections, `full_ranges` leaves that code out (geometries whose shapes all span the full
+// angular ranges).  Both sets give identical results on full-range geometries.
+namespace sections {
+#include "launch_set.inc"
+}  // namespace sections
+namespace full_ranges {
+#include "launch_set.inc"
+}  // namespace full_ranges
 
 }  // namespace vgn

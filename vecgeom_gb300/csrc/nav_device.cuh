@@ -13,6 +13,7 @@
 
 namespace vgn {
 namespace dev {
+inline namespace VGN_KSET {
 
 struct State {
   uint32_t nav_ind, last_exited;
@@ -334,5 +335,6 @@ __device__ __forceinline__ LVRec load_lv(const GeomView &g, int lvi)
 
 __device__ __forceinline__ int pv_lv(const GeomView &g, int pv) { return __ldg(&g.pv[pv].lv); }
 
+}  // namespace VGN_KSET
 }  // namespace dev
 }  // namespace vgn

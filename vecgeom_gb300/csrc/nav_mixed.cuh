@@ -34,6 +34,7 @@
 
 namespace vgn {
 namespace dev {
+inline namespace VGN_KSET {
 
 struct FI {
   float lo, hi;
@@ -694,5 +695,6 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
   return false;
 }
 
+}  // namespace VGN_KSET
 }  // namespace dev
 }  // namespace vgn

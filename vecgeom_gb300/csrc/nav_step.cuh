@@ -9,6 +9,7 @@
 
 namespace vgn {
 namespace dev {
+inline namespace VGN_KSET {
 
 template <bool MIXED>
 __device__ __forceinline__ bool level_locate(const GeomView &g, const LVRec &lv, int excl, D3 lp, int &pvol, D3 &dlp)
@@ -179,5 +180,6 @@ __device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, doub
   return step;
 }
 
+}  // namespace VGN_KSET
 }  // namespace dev
 }  // namespace vgn

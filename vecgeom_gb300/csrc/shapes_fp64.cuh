@@ -11,8 +11,22 @@
 
 #include "geom_types.h"
 
+// Two kernel sets are compiled from these sources: VGN_SECTIONS=1 (namespace `sections`)
+// handles phi sections of tubes, cones and polycones and phi/theta sections of spheres;
+// VGN_SECTIONS=0 (namespace `full_ranges`) compiles that code out, for geometries whose
+// shapes all span the full angular ranges.  The host picks the set per geometry.
+#ifndef VGN_SECTIONS
+#define VGN_SECTIONS 1
+#endif
+#if VGN_SECTIONS
+#define VGN_KSET sections
+#else
+#define VGN_KSET full_ranges
+#endif
+
 namespace vgn {
 namespace dev {
+inline namespace VGN_KSET {
 
 constexpr double kTolerance     = 1e-9;
 constexpr double kHalfTolerance = 0.5 * kTolerance;
@@ -138,7 +152,7 @@ __device__ __forceinline__ double wedge_safe_out(const double *w, D3 p)
 // time, TubeTypes.h:91-139); row layout vgn::row::Tube*, the phi wedge at TubeWedge
 namespace tb = row;
 
-__device__ __forceinline__ bool tube_has_phi(const double *t) { return t[tb::TubeDphi] < 2. * kPiD; }
+__device__ __forceinline__ bool tube_has_phi(const double *t) { return VGN_SECTIONS && t[tb::TubeDphi] < 2. * kPiD; }
 
 // TubeUtilities::PointInCyclicalSector<..., onSurfaceT = false> (TubeImplementation.h:58-101);
 // "smaller than pi" is dphi <= M_PI, decided at run time
@@ -461,7 +475,7 @@ __device__ __forceinline__ double cone_radius(const double *c, double z, bool in
                                                           : c[row::ConeOuterSlope] * z + c[row::ConeOuterOffset];
 }
 
-__device__ __forceinline__ bool cone_has_phi(const double *c) { return c[row::ConeDPhi] < 2. * kPiD; }
+__device__ __forceinline__ bool cone_has_phi(const double *c) { return VGN_SECTIONS && c[row::ConeDPhi] < 2. * kPiD; }
 
 // PointInCyclicalSector<..., onSurfaceT = false> (ConeUtilities.h:64-114); "smaller than pi"
 // is dphi <= M_PI, decided at run time
@@ -1148,11 +1162,12 @@ __device__ __forceinline__ double trap_safe_out(const double *t, D3 p)
   return safety;
 }
 
-// ---------------------------------------------------------------- Sphere (full)
+// ---------------------------------------------------------------- Sphere
 // volumes/kernel/SphereImplementation.h with SphereUtilities.h.  Even a full sphere
 // consults its phi wedge (Wedge_Evolution.h) and theta cone (ThetaCone_Evolution.h)
-// in the completely-inside/outside and on-surface tests; both are reproduced here
-// for the full ranges (stheta = 0, etheta >= pi).
+// in the completely-inside/outside and on-surface tests; the full-range path below
+// reproduces them for stheta = 0, etheta >= pi (what a full theta range implies), and a
+// sphere with sections goes to the out-of-line sphere_sect_* functions.
 namespace sp = row;
 constexpr double kSqrtTolerance = 3.1622777e-5;  // base/Math.h:29
 constexpr double kThetaHalfPi   = 0.5 * 3.14159265358979323846;
@@ -1160,6 +1175,626 @@ constexpr double kThetaHalfPi   = 0.5 * 3.14159265358979323846;
 __device__ __forceinline__ double sph_plus_tol_sq(double x) { return x * (x + 2.0 * kTolerance); }
 __device__ __forceinline__ double sph_minus_tol_sq(double x) { return fabs(x * (x - 2.0 * kTolerance)); }
 __device__ __forceinline__ double mag2(D3 p) { return p.x * p.x + p.y * p.y + p.z * p.z; }
+
+// ---------------------------------------------------------------- Sphere sections
+// The general sphere (a phi range below 2 pi or a theta range short of [0, pi]): the
+// full-range tests of SphereImplementation.h and SphereUtilities.h with the phi wedge's
+// half-plane distances (Wedge_Evolution.h) and the theta cone (ThetaCone_Evolution.h).
+// Each operation is one out-of-line function so the traversal kernels carry a call, not
+// the section code, for every sphere.
+constexpr double kThHalfTol = 0.5 * kTolerance;       // ThetaCone::halfAngTolerance
+constexpr double kThTolAng  = 2 * kTolerance * 10.;   // ThetaCone_Evolution.h:677-747
+
+__device__ __forceinline__ bool sph_flag(const double *t, int i) { return t[i] != 0.; }
+
+// Wedge::IsPointOnSurfaceAndMovingOut<START, MOVING_OUT> (Wedge_Evolution.h:233-246)
+template <bool START, bool MOVING_OUT>
+__device__ __forceinline__ bool wedge_moving(const double *w, D3 p, D3 d)
+{
+  const double ax = START ? w[row::WedgeA1x] : w[row::WedgeA2x], ay = START ? w[row::WedgeA1y] : w[row::WedgeA2y];
+  const double nx = START ? w[row::WedgeN1x] : w[row::WedgeN2x], ny = START ? w[row::WedgeN1y] : w[row::WedgeN2y];
+  if (!wedge_on_surface(ax, ay, nx, ny, p)) return false;
+  const double dn = d.x * -nx + d.y * -ny;  // dir.Dot(-normal), the normal has z = 0
+  return MOVING_OUT ? dn > 0.005 * kHalfTolerance : dn < 0.005 * kHalfTolerance;
+}
+
+// Wedge::DistanceToIn / DistanceToOut (Wedge_Evolution.h:393-446)
+template <bool TO_IN>
+__device__ __forceinline__ void wedge_dist(const double *w, D3 p, D3 d, double &dist1, double &dist2)
+{
+  const double comp1 = d.x * w[row::WedgeN1x] + d.y * w[row::WedgeN1y];
+  const double comp2 = d.x * w[row::WedgeN2x] + d.y * w[row::WedgeN2y];
+  dist1 = kInfLength;
+  dist2 = kInfLength;
+  if (TO_IN ? comp1 > 0. : comp1 < 0.) {
+    const double tmp = -(p.x * w[row::WedgeN1x] + p.y * w[row::WedgeN1y]) / comp1;
+    if (tmp > 0.) dist1 = tmp;
+  }
+  if (TO_IN ? comp2 > 0. : comp2 < 0.) {
+    const double tmp = -(p.x * w[row::WedgeN2x] + p.y * w[row::WedgeN2y]) / comp2;
+    if (tmp > 0.) dist2 = tmp;
+  }
+}
+
+__device__ __forceinline__ bool wedge_contains_p(const double *w, D3 p)
+{
+  bool cin = false, cout = false;
+  wedge_ci<false>(w, p, cin, cout);
+  return !cout;
+}
+
+// ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730)
+__device__ __forceinline__ bool thc_completely_inside(const double *t, D3 p)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double rho         = sqrt(mag2(p) - (p.z * p.z));
+  const double cone1Radius = fabs(p.z * t[sp::SphTanSTheta]);
+  const double cone2Radius = fabs(p.z * t[sp::SphTanETheta]);
+  const bool onZ           = p.z != 0. && p.x == 0. && p.y == 0.;
+  const bool onXY          = p.z == 0. && (p.x != 0. || p.y != 0.);
+  bool ci = onZ && ((sT == 0. && eT == kPiD) || (p.z > 0. && sT == 0.) || (p.z < 0. && eT == kPiD));
+  ci      = ci || (!ci && (onXY && (sT < kThetaHalfPi && eT > kThetaHalfPi && (kThetaHalfPi - sT) > kTolerance &&
+                                   (eT - kThetaHalfPi) > kTolerance)));
+  if (sT < kThetaHalfPi + kThHalfTol) {
+    if (eT < kThetaHalfPi + kThHalfTol && sT < eT) {
+      const double tolAngMin = cone1Radius + kThTolAng, tolAngMax = cone2Radius - kThTolAng;
+      ci = ci || (!ci && (((rho <= tolAngMax) && (rho >= tolAngMin) && (p.z > 0.) && (sT != 0.)) ||
+                          ((rho <= tolAngMax) && (sT == 0.) && (p.z > 0.))));
+    }
+    if (eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      const double tolAngMin = cone1Radius + kThTolAng, tolAngMax = cone2Radius + kThTolAng;
+      ci = ci || (!ci && (((rho >= tolAngMin) && (p.z > 0.)) || ((rho >= tolAngMax) && (p.z < 0.))));
+    }
+    if (eT >= kThetaHalfPi - kThHalfTol && eT <= kThetaHalfPi + kThHalfTol) ci = ci && !(fabs(p.z) < kThHalfTol);
+  }
+  if (eT > kThetaHalfPi + kThHalfTol) {
+    if (sT >= kThetaHalfPi - kThHalfTol && sT <= kThetaHalfPi + kThHalfTol) ci = ci && !(fabs(p.z) < kThHalfTol);
+    if (sT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      const double tolAngMin = cone1Radius - kThTolAng, tolAngMax = cone2Radius + kThTolAng;
+      ci = ci || (!ci && (((rho <= tolAngMin) && (rho >= tolAngMax) && (p.z < 0.) && (eT != kPiD)) ||
+                          ((rho <= tolAngMin) && (p.z < 0.) && (eT == kPiD))));
+    }
+  }
+  return ci;
+}
+
+// ThetaCone::IsCompletelyOutside (ThetaCone_Evolution.h:733-805)
+__device__ __forceinline__ bool thc_completely_outside(const double *t, D3 p)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double rho         = sqrt(p.x * p.x + p.y * p.y);
+  const double cone1Radius = fabs(p.z * t[sp::SphTanSTheta]);
+  const double cone2Radius = fabs(p.z * t[sp::SphTanETheta]);
+  const bool onZ           = p.z != 0. && p.x == 0. && p.y == 0.;
+  const bool onXY          = p.z == 0. && (p.x != 0. || p.y != 0.);
+  bool co = onZ && ((sT != 0. && eT != kPiD) || (p.z > 0. && sT != 0.) || (p.z < 0. && eT != kPiD));
+  co      = co || (!co && (onXY && (((sT < kThetaHalfPi) && (eT < kThetaHalfPi) && ((kThetaHalfPi - sT) > kTolerance) &&
+                                     ((kThetaHalfPi - eT) > kTolerance)) ||
+                                    ((sT > kThetaHalfPi && eT > kThetaHalfPi) && ((sT - kThetaHalfPi) > kTolerance) &&
+                                     ((eT - kThetaHalfPi) > kTolerance)))));
+  if (sT < kThetaHalfPi + kThHalfTol) {
+    if (eT < kThetaHalfPi + kThHalfTol && sT < eT) {
+      const double tolAngMin2 = cone1Radius - kThTolAng, tolAngMax2 = cone2Radius + kThTolAng;
+      co = co || (!co && ((rho < tolAngMin2) || (rho > tolAngMax2) || (p.z < 0.)));
+    }
+    if (eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      const double tolAngMin2 = cone1Radius - kThTolAng, tolAngMax2 = cone2Radius - kThTolAng;
+      co = co || (!co && (((rho < tolAngMin2) && (p.z > 0.)) || ((rho < tolAngMax2) && (p.z < 0.))));
+    }
+    if (eT >= kThetaHalfPi - kThHalfTol && eT <= kThetaHalfPi + kThHalfTol) co = co && !(fabs(p.z) < kThHalfTol);
+  }
+  if (eT > kThetaHalfPi + kThHalfTol) {
+    if (sT >= kThetaHalfPi - kThHalfTol && sT <= kThetaHalfPi + kThHalfTol) co = co && !(fabs(p.z) < kThHalfTol);
+    if (sT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      const double tolAngMin2 = cone1Radius + kThTolAng, tolAngMax2 = cone2Radius - kThTolAng;
+      co = co || (!co && ((rho < tolAngMax2) || (rho > tolAngMin2) || (p.z > 0.)));
+    }
+  }
+  return co;
+}
+
+__device__ __forceinline__ bool thc_contains(const double *t, D3 p) { return !thc_completely_outside(t, p); }
+
+// ThetaCone::IsPointOnSurfaceAndMovingOut<START, MOVING_OUT> (ThetaCone_Evolution.h:164-229)
+template <bool START, bool MOVING_OUT>
+__device__ __forceinline__ bool thc_moving(const double *t, D3 p, D3 d)
+{
+  const double rhs  = fabs(t[START ? sp::SphTanSTheta : sp::SphTanETheta] * p.z);
+  const double rho2 = p.x * p.x + p.y * p.y;
+  if (!(rho2 >= sph_minus_tol_sq(rhs) && rho2 <= sph_plus_tol_sq(rhs))) return false;
+  D3 n{p.x, p.y, -t[START ? sp::SphTanSTheta2 : sp::SphTanETheta2] * p.z};
+  if (START ? t[sp::SphSTheta] <= kThetaHalfPi : !(t[sp::SphETheta] <= kThetaHalfPi)) n = D3{-n.x, -n.y, -n.z};
+  const double dn = d.x * n.x + d.y * n.y + d.z * n.z;
+  return MOVING_OUT ? dn > 0. : dn < 0.;
+}
+
+// ThetaCone::DistanceToLine (ThetaCone_Evolution.h:358-365)
+__device__ __forceinline__ double thc_dist_line(double slope, double x, double y)
+{
+  const double dist = (y - slope * x) / sqrt(1. + slope * slope);
+  return fabs(dist);
+}
+
+// ThetaCone::SafetyToIn (ThetaCone_Evolution.h:276-316)
+__device__ __forceinline__ double thc_safe_in(const double *t, D3 p)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double pointRad = sqrt(p.x * p.x + p.y * p.y);
+  const double sfTh1    = thc_dist_line(t[sp::SphSlope1], pointRad, p.z);
+  const double sfTh2    = thc_dist_line(t[sp::SphSlope2], pointRad, p.z);
+  double safeTheta      = vmin(sfTh1, sfTh2);
+  if (thc_contains(t, p)) return 0.;
+  if (sT < kThetaHalfPi + kThHalfTol) {
+    if (eT < kThetaHalfPi + kThHalfTol && sT < eT && p.z < 0.) safeTheta = sfTh2;
+    if (eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      if (p.z > 0.) safeTheta = sfTh1;
+      if (p.z < 0.) safeTheta = sfTh2;
+    }
+  }
+  if (eT > kThetaHalfPi + kThHalfTol && sT > kThetaHalfPi + kThHalfTol && sT < eT && p.z > 0.) safeTheta = sfTh1;
+  return safeTheta;
+}
+
+// ThetaCone::SafetyToOut (ThetaCone_Evolution.h:318-356)
+__device__ __forceinline__ double thc_safe_out(const double *t, D3 p)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double pointRad    = sqrt(p.x * p.x + p.y * p.y);
+  const double bisectorRad = fabs(p.z * t[sp::SphTanBisector]);
+  bool cond                = false;
+  const double sfTh1       = thc_dist_line(t[sp::SphSlope1], pointRad, p.z);
+  const double sfTh2       = thc_dist_line(t[sp::SphSlope2], pointRad, p.z);
+  if (sT < kThetaHalfPi + kThHalfTol) {
+    if (eT < kThetaHalfPi + kThHalfTol && sT < eT) cond = (pointRad < bisectorRad) && (sT != 0.);
+    if (eT > kThetaHalfPi + kThHalfTol && sT < eT) cond = sfTh1 < sfTh2;
+  }
+  if (eT > kThetaHalfPi + kThHalfTol && sT > kThetaHalfPi + kThHalfTol && sT < eT)
+    cond = !((pointRad < bisectorRad) && (eT != kPiD));
+  return cond ? sfTh1 : sfTh2;
+}
+
+// ThetaCone::DistanceToIn's root clean-up (ThetaCone_Evolution.h:387-395)
+__device__ __forceinline__ double thc_in_root(double root, bool &done)
+{
+  done = done || (fabs(root) < 3. * kTolerance);
+  if (fabs(root) < 3. * kTolerance) root = 0.;
+  if (!done && root < 0.) root = kInfLength;
+  return root;
+}
+
+// ThetaCone::DistanceToIn (ThetaCone_Evolution.h:367-496); dist1/dist2 and int1/int2 come
+// in as kInfLength and false
+__device__ __forceinline__ void thc_dist_in(const double *t, D3 p, D3 d, double &dist1, double &dist2, bool &int1,
+                                            bool &int2)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double tanS2 = t[sp::SphTanSTheta2], tanE2 = t[sp::SphTanETheta2];
+  bool done          = false;
+  double firstRoot = kInfLength, secondRoot = kInfLength;
+  const double pDotV2d = p.x * d.x + p.y * d.y;
+  const double rho2    = p.x * p.x + p.y * p.y;
+  const double dirRho2 = d.x * d.x + d.y * d.y;
+  const double b       = pDotV2d - p.z * d.z * tanS2;
+  const double a       = dirRho2 - d.z * d.z * tanS2;
+  const double cc      = rho2 - p.z * p.z * tanS2;
+  const double d2      = b * b - a * cc;
+  const double aInv    = 1. / nonzero(a);
+  if (d2 > 0.) firstRoot = (-b + sqrt(fabs(d2))) * aInv;
+  firstRoot = thc_in_root(firstRoot, done);
+
+  const double b2    = pDotV2d - p.z * d.z * tanE2;
+  const double a2    = dirRho2 - d.z * d.z * tanE2;
+  const double c2    = rho2 - p.z * p.z * tanE2;
+  const double d22   = b2 * b2 - a2 * c2;
+  const double a2Inv = 1. / nonzero(a2);
+  if (d22 > 0.) secondRoot = (-b2 - sqrt(fabs(d22))) * a2Inv;
+  if (!done && fabs(secondRoot) < 3. * kTolerance) secondRoot = 0.;
+  done = done || (fabs(secondRoot) < 3. * kTolerance);
+  if (!done && secondRoot < 0.) secondRoot = kInfLength;
+
+  if (sT < kThetaHalfPi + kThHalfTol) {
+    if (eT < kThetaHalfPi + kThHalfTol && sT < eT) {
+      dist1 = firstRoot;
+      dist2 = secondRoot;
+      const double z1 = (p.z + dist1 * d.z), z2 = (p.z + dist2 * d.z);
+      int1 = ((d2 > 0.) && (z1 > 0.));
+      int2 = ((d22 > 0.) && (z2 > 0.));
+    }
+    if (eT >= kThetaHalfPi - kThHalfTol && eT <= kThetaHalfPi + kThHalfTol) {
+      if (d.z > 0.) dist2 = -p.z / d.z;
+      const double z2 = (p.z + dist2 * d.z);
+      int2 = ((dist2 != kInfLength) && (fabs(z2) < kThHalfTol));
+    }
+    if (eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      dist1 = firstRoot;
+      if (d22 > 0.) secondRoot = (-b2 + sqrt(fabs(d22))) * a2Inv;
+      done       = false;
+      secondRoot = thc_in_root(secondRoot, done);
+      dist2      = secondRoot;
+      const double z1 = (p.z + dist1 * d.z), z2 = (p.z + dist2 * d.z);
+      int1 = ((d2 > 0) && (dist1 != kInfLength) && (z1 > 0.));
+      int2 = ((d22 > 0) && (dist2 != kInfLength) && (z2 < 0.));
+    }
+  }
+  if (sT >= kThetaHalfPi - kThHalfTol && eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+    if (d2 > 0.) firstRoot = (-b - sqrt(fabs(d2))) * aInv;
+    done      = false;
+    firstRoot = thc_in_root(firstRoot, done);
+    dist1     = firstRoot;
+    if (d22 > 0.) secondRoot = (-b2 + sqrt(fabs(d22))) * a2Inv;
+    done       = false;
+    secondRoot = thc_in_root(secondRoot, done);
+    dist2      = secondRoot;
+    const double z1 = (p.z + dist1 * d.z), z2 = (p.z + dist2 * d.z);
+    int1 = ((d2 > 0) && (dist1 != kInfLength) && (z1 < 0.));
+    int2 = ((d22 > 0) && (dist2 != kInfLength) && (z2 < 0.));
+  }
+  if (sT >= kThetaHalfPi - kThHalfTol && sT <= kThetaHalfPi + kThHalfTol) {
+    if (d.z < 0.) dist1 = -p.z / d.z;
+    const double z1 = (p.z + dist1 * d.z);
+    int1 = ((dist1 != kInfLength) && (fabs(z1) < kThHalfTol));
+  }
+}
+
+// ThetaCone::DistanceToOut (ThetaCone_Evolution.h:498-652), same conventions
+__device__ __forceinline__ void thc_dist_out(const double *t, D3 p, D3 d, double &dist1, double &dist2, bool &int1,
+                                             bool &int2)
+{
+  const double sT = t[sp::SphSTheta], eT = t[sp::SphETheta];
+  const double tanS2 = t[sp::SphTanSTheta2], tanE2 = t[sp::SphTanETheta2];
+  double firstRoot = kInfLength, secondRoot = kInfLength;
+  const double pDotV2d = p.x * d.x + p.y * d.y;
+  const double rho2    = p.x * p.x + p.y * p.y;
+  const double b       = pDotV2d - p.z * d.z * tanS2;
+  const double a       = d.x * d.x + d.y * d.y - d.z * d.z * tanS2;
+  const double cc      = rho2 - p.z * p.z * tanS2;
+  double d2            = b * b - a * cc;
+  if (d2 < 0. && fabs(d2) < kHalfTolerance) d2 = 0.;
+  if ((d2 >= 0.) && b >= 0. && a != 0.) firstRoot = ((-b - sqrt(fabs(d2))) / nonzero(a));
+  if ((d2 >= 0.) && b < 0.) firstRoot = ((cc) / nonzero(-b + sqrt(fabs(d2))));
+  if (firstRoot < 0.) firstRoot = kInfLength;
+
+  const double b2 = p.x * d.x + p.y * d.y - p.z * d.z * tanE2;
+  const double a2 = d.x * d.x + d.y * d.y - d.z * d.z * tanE2;
+  const double c2 = p.x * p.x + p.y * p.y - p.z * p.z * tanE2;
+  double d22      = (b2 * b2) - (a2 * c2);
+  if (d22 < 0. && fabs(d22) < kHalfTolerance) d22 = 0.;
+  if ((d22 >= 0.) && b2 >= 0.) secondRoot = ((c2) / nonzero(-b2 - sqrt(fabs(d22))));
+  if ((d22 >= 0.) && b2 < 0. && a2 != 0.) secondRoot = ((-b2 + sqrt(fabs(d22))) / nonzero(a2));
+  if (secondRoot < 0. && fabs(secondRoot) > kTolerance) secondRoot = kInfLength;
+  if (fabs(secondRoot) < kTolerance) secondRoot = 0.;
+
+  if (sT < kThetaHalfPi + kThHalfTol) {
+    if (eT < kThetaHalfPi + kThHalfTol && sT < eT) {
+      dist1 = firstRoot;
+      dist2 = secondRoot;
+      const double z1 = (p.z + dist1 * d.z), z2 = (p.z + dist2 * d.z);
+      int1 = ((d2 > 0) && (dist1 != kInfLength) && ((z1) > -kHalfTolerance));
+      int2 = ((d22 > 0) && (dist2 != kInfLength) && ((z2) > -kHalfTolerance));
+      const double dirRho2 = d.x * d.x + d.y * d.y;
+      double zs = kInfLength, ze = kInfLength;
+      if (sT != 0.) zs = dirRho2 / t[sp::SphTanSTheta];
+      if (eT != 0.) ze = dirRho2 / t[sp::SphTanETheta];
+      const bool cond = (p.x == 0. && p.y == 0. && p.z == 0. && d.z < zs && d.z < ze);
+      if (cond) dist1 = 0.;
+      if (cond) dist2 = 0.;
+      int1 = int1 || cond;
+      int2 = int2 || cond;
+    }
+    if (eT >= kThetaHalfPi - kThHalfTol && eT <= kThetaHalfPi + kThHalfTol) {
+      dist1 = firstRoot;
+      dist2 = kInfLength;
+      if (d.z < 0.) dist2 = -1. * p.z / d.z;
+      const double z2 = (p.z + dist2 * d.z), z1 = (p.z + dist1 * d.z);
+      int2 = ((dist2 != kInfLength) && (fabs(z2) < kHalfTolerance) && !(d.z == 0.));
+      int1 = ((d2 >= 0) && (dist1 != kInfLength) && (fabs(z1) < kHalfTolerance) && !(d.z == 0.));
+    }
+    if (eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+      dist1 = firstRoot;
+      if ((d22 >= 0.) && b2 > 0. && a2 != 0.) secondRoot = ((-b2 - sqrt(fabs(d22))) / nonzero(a2));
+      if ((d22 >= 0.) && b2 <= 0.) secondRoot = ((c2) / nonzero(-b2 + sqrt(fabs(d22))));
+      if (secondRoot < 0.) secondRoot = kInfLength;
+      dist2 = secondRoot;
+      const double z1 = (p.z + dist1 * d.z), z2 = (p.z + dist2 * d.z);
+      int1 = ((d2 >= 0) && (dist1 != kInfLength) && ((z1) > -kHalfTolerance));
+      int2 = ((d22 >= 0) && (dist2 != kInfLength) && ((z2) < kHalfTolerance));
+    }
+  }
+  if (eT > kThetaHalfPi + kThHalfTol && sT < eT) {
+    secondRoot = kInfLength;
+    if ((d22 >= 0.) && b2 > 0. && a2 != 0.) secondRoot = ((-b2 - sqrt(fabs(d22))) / nonzero(a2));
+    if ((d22 >= 0.) && b2 <= 0.) secondRoot = ((c2) / nonzero(-b2 + sqrt(fabs(d22))));
+    dist2 = secondRoot;
+    if (sT > kThetaHalfPi + kThHalfTol) {
+      if ((d2 >= 0.) && b > 0.) firstRoot = ((cc) / nonzero(-b - sqrt(fabs(d2))));
+      if ((d2 >= 0.) && b <= 0. && a != 0.) firstRoot = ((-b + sqrt(fabs(d2))) / nonzero(a));
+      if (firstRoot < 0.) firstRoot = kInfLength;
+      dist1           = firstRoot;
+      const double z1 = (p.z + dist1 * d.z);
+      int1            = ((d2 > 0) && (dist1 != kInfLength) && ((z1) < kHalfTolerance));
+      const double z2 = (p.z + dist2 * d.z);
+      int2            = ((d22 > 0) && (dist2 != kInfLength) && ((z2) < kHalfTolerance));
+      const double dirRho2 = d.x * d.x + d.y * d.y;
+      double zs = -kInfLength, ze = -kInfLength;
+      if (t[sp::SphTanSTheta] != 0.) zs = -dirRho2 / t[sp::SphTanSTheta];
+      if (t[sp::SphTanETheta] != 0.) ze = -dirRho2 / t[sp::SphTanETheta];
+      const bool cond = (p.x == 0. && p.y == 0. && p.z == 0. && d.z > zs && d.z > ze);
+      if (cond) dist1 = 0.;
+      if (cond) dist2 = 0.;
+      int1 = int1 || cond;
+      int2 = int2 || cond;
+    }
+  }
+  if (sT >= kThetaHalfPi - kThHalfTol && sT <= kThetaHalfPi + kThHalfTol) {
+    dist2 = secondRoot;
+    dist1 = kInfLength;
+    if (d.z > 0.) dist1 = -1. * p.z / nonzero(d.z);
+    const double z1 = (p.z + dist1 * d.z);
+    const double z2 = (p.z + dist2 * d.z);
+    int1 = ((dist1 != kInfLength) && (fabs(z1) < kHalfTolerance) && (d.z != 0.));
+    int2 = ((d22 >= 0) && (dist2 != kInfLength) && (fabs(z2) < kHalfTolerance) && (d.z != 0.));
+  }
+}
+
+// SphereUtilities::IsCompletelyInside / IsCompletelyOutside (SphereUtilities.h:110-141)
+__device__ __forceinline__ bool sphs_completely_inside(const double *t, D3 p)
+{
+  const double rad = sqrt(mag2(p));
+  const bool inRad = (rad < (t[sp::SphRmax] - kTolerance)) && (rad > (t[sp::SphRmin] + kTolerance));
+  bool cin = false, cout = false;
+  wedge_ci<true>(t + sp::SphA1x, p, cin, cout);
+  return inRad && cin && thc_completely_inside(t, p);
+}
+
+__device__ __forceinline__ bool sphs_completely_outside(const double *t, D3 p)
+{
+  const double rad  = sqrt(mag2(p));
+  const bool outRad = (rad > (t[sp::SphRmax] + kTolerance)) || (rad < (t[sp::SphRmin] - kTolerance));
+  bool cin = false, cout = false;
+  wedge_ci<true>(t + sp::SphA1x, p, cin, cout);
+  return outRad || cout || thc_completely_outside(t, p);
+}
+
+// SphereUtilities::IsPointOnSurfaceAndMovingOut (SphereUtilities.h:143-195)
+template <bool MOVING_OUT>
+__device__ __forceinline__ bool sphs_on_surface_moving(const double *t, D3 p, D3 d)
+{
+  const double m2   = mag2(p);
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  const double dp   = d.x * p.x + d.y * p.y + d.z * p.z;
+  const bool outer  = (m2 <= sph_plus_tol_sq(rmax) && m2 >= sph_minus_tol_sq(rmax)) &&
+                     (MOVING_OUT ? dp > kSqrtTolerance : dp < -kSqrtTolerance);
+  bool inner = false;
+  if (rmin != 0.) {
+    const double dmp = d.x * -p.x + d.y * -p.y + d.z * -p.z;
+    inner            = (m2 <= sph_plus_tol_sq(rmin) && m2 >= sph_minus_tol_sq(rmin)) &&
+            (MOVING_OUT ? dmp > kSqrtTolerance : dmp < -kSqrtTolerance);
+  }
+  const double *w = t + sp::SphA1x;
+  bool phiFace = false, thetaFace = false;
+  if (t[sp::SphDPhi] < (2. * kPiD - kHalfTolerance))
+    phiFace = wedge_moving<true, MOVING_OUT>(w, p, d) || wedge_moving<false, MOVING_OUT>(w, p, d);
+  if (t[sp::SphDTheta] < (kPiD - kHalfTolerance))
+    thetaFace = thc_moving<true, MOVING_OUT>(t, p, d) || thc_moving<false, MOVING_OUT>(t, p, d);
+  const bool inShell = (m2 >= rmin * rmin) && (m2 <= rmax * rmax);
+  return ((outer || inner) && wedge_contains_p(w, p) && thc_contains(t, p)) ||
+         (phiFace && inShell && thc_contains(t, p)) || (thetaFace && inShell && wedge_contains_p(w, p));
+}
+
+// SphereImplementation::GenericKernelForContainsAndInside<FOR_INSIDE> (SphereImplementation.h:89-136)
+template <bool FOR_INSIDE>
+__device__ __forceinline__ void sphs_ci(const double *t, D3 p, bool &cin, bool &cout)
+{
+  const double rad2 = mag2(p);
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  if (rmin != 0.) {
+    cin  = rad2 <= sph_minus_tol_sq(rmax) && rad2 >= sph_plus_tol_sq(rmin);
+    cout = rad2 >= sph_plus_tol_sq(rmax) || rad2 <= sph_minus_tol_sq(rmin);
+  } else {
+    cin  = rad2 <= sph_minus_tol_sq(rmax);
+    cout = rad2 >= sph_plus_tol_sq(rmax);
+  }
+  if (!sph_flag(t, sp::SphFullPhi)) {
+    bool ci = false, co = false;
+    wedge_ci<FOR_INSIDE>(t + sp::SphA1x, p, ci, co);
+    cout = cout || co;
+    if (FOR_INSIDE) cin = cin && ci;
+  }
+  if (!sph_flag(t, sp::SphFullTheta)) {
+    const bool ci = FOR_INSIDE ? thc_completely_inside(t, p) : false;
+    const bool co = thc_completely_outside(t, p);
+    cout          = cout || co;
+    if (FOR_INSIDE) cin = cin && ci;
+  }
+}
+
+// SphereImplementation::GetMinDistFromPhi<TO_IN> (SphereImplementation.h:343-386)
+template <bool TO_IN>
+__device__ __forceinline__ void sphs_min_dist_phi(const double *t, D3 p, D3 d, double &distance)
+{
+  const double *w = t + sp::SphA1x;
+  const double rmin2 = t[sp::SphRmin] * t[sp::SphRmin], rmax2 = t[sp::SphRmax] * t[sp::SphRmax];
+  double distPhi1, distPhi2;
+  wedge_dist<TO_IN>(w, p, d, distPhi1, distPhi2);
+  double dist = vmin(distPhi1, distPhi2);
+  D3 tmp{p.x + dist * d.x, p.y + dist * d.y, p.z + dist * d.z};
+  double rad2 = mag2(tmp);
+  bool onFace = ((dist == distPhi1) && wedge_on_surface(w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x],
+                                                         w[row::WedgeN1y], tmp)) ||
+                ((dist == distPhi2) && wedge_on_surface(w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x],
+                                                         w[row::WedgeN2y], tmp));
+  const bool cond1 = onFace && (rad2 > rmin2) && (rad2 < rmax2) && thc_contains(t, tmp);
+  if (cond1) distance = vmin(dist, distance);
+  dist   = vmax(distPhi1, distPhi2);
+  tmp    = D3{p.x + dist * d.x, p.y + dist * d.y, p.z + dist * d.z};
+  rad2   = mag2(tmp);
+  onFace = ((dist == distPhi1) && wedge_on_surface(w[row::WedgeA1x], w[row::WedgeA1y], w[row::WedgeN1x],
+                                                    w[row::WedgeN1y], tmp)) ||
+           ((dist == distPhi2) && wedge_on_surface(w[row::WedgeA2x], w[row::WedgeA2y], w[row::WedgeN2x],
+                                                    w[row::WedgeN2y], tmp));
+  const bool cond2 = onFace && (rad2 > rmin2) && (rad2 < rmax2) && thc_contains(t, tmp);
+  if (!cond1 && cond2) distance = vmin(dist, distance);
+}
+
+// DistanceToIn (SphereImplementation.h:138-256) of a sphere with sections
+__device__ __noinline__ double sphere_sect_dist_in(const double *t, D3 p, D3 d)
+{
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  const double *w      = t + sp::SphA1x;
+  const double rad2    = mag2(p);
+  const double pDotV3d = p.x * d.x + p.y * d.y + p.z * d.z;
+  double c             = rad2 - rmax * rmax;
+  if (sphs_completely_inside(t, p)) return -1.0;
+  if (sphs_on_surface_moving<false>(t, p, d)) return 0.0;
+  double d2 = (pDotV3d * pDotV3d - c);
+  if (d2 < 0. || ((c > 0.) && (pDotV3d > 0.))) return kInfLength;
+  double sd1 = kInfLength, sd2 = kInfLength;
+  if (d2 >= 0.) sd1 = (-pDotV3d - sqrt(fabs(d2)));
+  double outerDist = kInfLength, innerDist = kInfLength;
+  {
+    const D3 tmp{p.x + sd1 * d.x, p.y + sd1 * d.y, p.z + sd1 * d.z};
+    if (wedge_contains_p(w, tmp) && thc_contains(t, tmp) && (sd1 >= 0.)) outerDist = sd1;
+  }
+  if (rmin != 0.) {
+    c  = rad2 - rmin * rmin;
+    d2 = pDotV3d * pDotV3d - c;
+    if (d2 >= 0.) sd2 = (-pDotV3d + sqrt(fabs(d2)));
+    const D3 tmp{p.x + sd2 * d.x, p.y + sd2 * d.y, p.z + sd2 * d.z};
+    if ((sd2 >= 0.) && wedge_contains_p(w, tmp) && thc_contains(t, tmp)) innerDist = sd2;
+  }
+  double distance = vmin(outerDist, innerDist);
+  if (!sph_flag(t, sp::SphFullPhi)) sphs_min_dist_phi<true>(t, p, d, distance);
+  double distThetaMin = kInfLength;
+  if (!sph_flag(t, sp::SphFullTheta)) {
+    bool int1 = false, int2 = false;
+    double dt1 = kInfLength, dt2 = kInfLength;
+    thc_dist_in(t, p, d, dt1, dt2, int1, int2);
+    const D3 c1{p.x + dt1 * d.x, p.y + dt1 * d.y, p.z + dt1 * d.z};
+    const D3 c2{p.x + dt2 * d.x, p.y + dt2 * d.y, p.z + dt2 * d.z};
+    const double r1 = mag2(c1), r2 = mag2(c2);
+    bool valid1 = (r1 >= rmin * rmin && r1 <= rmax * rmax) && int1;
+    bool valid2 = (r2 >= rmin * rmin && r2 <= rmax * rmax) && int2;
+    if (!sph_flag(t, sp::SphFullPhi)) {
+      valid1 = valid1 && wedge_contains_p(w, c1);
+      valid2 = valid2 && wedge_contains_p(w, c2);
+    }
+    if (valid2 && !valid1) distThetaMin = dt2;
+    if (valid1 && !valid2) distThetaMin = dt1;
+    if (valid1 && valid2) distThetaMin = vmin(dt1, dt2);
+  }
+  distance = vmin(distThetaMin, distance);
+  // a ray aimed at the centre of a theta section enters at the apex
+  const D3 toC         = {0. - p.x, 0. - p.y, 0. - p.z};
+  const double m2      = mag2(toC);
+  const double newDist = sqrt(m2);
+  const double un      = sqrt(m2 + 2.2250738585072014e-308);  // Vector3D::Unit: / Sqrt(mag2 + kMinimum)
+  if ((t[sp::SphSTheta] > kHalfTolerance || t[sp::SphEThetaChk] < (kPiD - kHalfTolerance)) &&
+      (fabs(toC.x / un - d.x) < kHalfTolerance) && (fabs(toC.y / un - d.y) < kHalfTolerance) &&
+      (fabs(toC.z / un - d.z) < kHalfTolerance))
+    distance = vmin(distance, newDist);
+  return distance;
+}
+
+// DistanceToOut (SphereImplementation.h:258-341) of a sphere with sections
+__device__ __noinline__ double sphere_sect_dist_out(const double *t, D3 p, D3 d)
+{
+  const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
+  const double pDotV3d = p.x * d.x + p.y * d.y + p.z * d.z;
+  const double rad2    = mag2(p);
+  double c             = rad2 - rmax * rmax;
+  if (sphs_completely_outside(t, p)) return -1.0;
+  if (sphs_on_surface_moving<true>(t, p, d)) return 0.0;
+  double d2  = (pDotV3d * pDotV3d - c);
+  double sd1 = kInfLength, sd2 = kInfLength;
+  if (d2 >= 0.) sd1 = (-pDotV3d + sqrt(fabs(d2)));
+  if (rmin != 0.) {
+    c  = rad2 - rmin * rmin;
+    d2 = (pDotV3d * pDotV3d - c);
+    if ((d2 >= 0.) && (pDotV3d < 0.)) sd2 = (-pDotV3d - sqrt(fabs(d2)));
+  }
+  const double snxt = vmin(sd1, sd2);
+  const double sT = t[sp::SphSTheta], eTc = t[sp::SphEThetaChk];
+  const bool condSemi = ((sT == 0. && eTc == kPiD / 2.) && d.z >= 0.) || ((sT == kPiD / 2. && eTc == kPiD) && d.z <= 0.);
+  if (condSemi) return snxt;
+  double distThetaMin = kInfLength;
+  if (!sph_flag(t, sp::SphFullTheta)) {
+    bool int1 = false, int2 = false;
+    double dt1 = kInfLength, dt2 = kInfLength;
+    thc_dist_out(t, p, d, dt1, dt2, int1, int2);
+    if (int2 && !int1) distThetaMin = dt2;
+    if (!int2 && int1) distThetaMin = dt1;
+    if (int2 && int1) distThetaMin = vmin(dt1, dt2);
+  }
+  double distance = vmin(distThetaMin, snxt);
+  if (!sph_flag(t, sp::SphFullPhi)) {
+    if (t[sp::SphDPhi] <= kPiD) {
+      double dp1, dp2;
+      wedge_dist<false>(t + sp::SphA1x, p, d, dp1, dp2);
+      distance = vmin(vmin(dp1, dp2), distance);
+    } else {
+      sphs_min_dist_phi<false>(t, p, d, distance);
+    }
+  }
+  return distance;
+}
+
+// SafetyToIn / SafetyToOut (SphereImplementation.h:388-479) of a sphere with sections
+__device__ __noinline__ double sphere_sect_safe_in(const double *t, D3 p)
+{
+  const double rad = sqrt(mag2(p));
+  bool cin = false, cout = false;
+  sphs_ci<true>(t, p, cin, cout);
+  if (cin) return -1.0;
+  if (!cout) return 0.0;
+  double safety;
+  if (t[sp::SphRmin] != 0.) {
+    const double safeRMin = t[sp::SphRmin] - rad;
+    const double safeRMax = rad - t[sp::SphRmax];
+    safety                = safeRMin > safeRMax ? safeRMin : safeRMax;
+  } else {
+    safety = rad - t[sp::SphRmax];
+  }
+  if (!sph_flag(t, sp::SphFullPhi)) safety = vmax(wedge_safe_in(t + sp::SphA1x, p), safety);
+  if (!sph_flag(t, sp::SphFullTheta)) safety = vmax(thc_safe_in(t, p), safety);
+  return safety;
+}
+
+__device__ __noinline__ double sphere_sect_safe_out(const double *t, D3 p)
+{
+  const double rad = sqrt(mag2(p));
+  bool cin = false, cout = false;
+  sphs_ci<true>(t, p, cin, cout);
+  if (cout) return -1.0;
+  if (!cin) return 0.0;
+  double safety;
+  if (t[sp::SphRmin] != 0.) {
+    const double safeRMin = (rad - t[sp::SphRmin]);
+    const double safeRMax = (t[sp::SphRmax] - rad);
+    safety                = safeRMin < safeRMax ? safeRMin : safeRMax;
+  } else {
+    safety = t[sp::SphRmax] - rad;
+  }
+  if (!sph_flag(t, sp::SphFullPhi)) safety = vmin(wedge_safe_out(t + sp::SphA1x, p), safety);
+  if (!sph_flag(t, sp::SphFullTheta)) safety = vmin(thc_safe_out(t, p), safety);
+  return safety;
+}
+
+// Contains / Inside (SphereImplementation.h:62-87) of a sphere with sections
+__device__ __noinline__ int sphere_sect_inside(const double *t, D3 p, bool for_contains)
+{
+  bool cin = false, cout = false;
+  if (for_contains) {
+    sphs_ci<false>(t, p, cin, cout);
+    return !cout;
+  }
+  sphs_ci<true>(t, p, cin, cout);
+  int r = kSurfaceE;
+  if (cout) r = kOutsideE;
+  if (cin) r = kInsideE;
+  return r;
+}
+
+// ---------------------------------------------------------------- Sphere (full ranges)
 
 
 // ThetaCone::IsCompletelyInside (ThetaCone_Evolution.h:655-730), stheta = 0 and etheta >= pi
@@ -1249,6 +1884,7 @@ __device__ __forceinline__ void sphere_ci(const double *t, D3 p, bool &cin, bool
 
 __device__ __forceinline__ bool sphere_contains(const double *t, D3 p)
 {
+  if (VGN_SECTIONS && !sph_flag(t, sp::SphFull)) return sphere_sect_inside(t, p, true);
   bool cin = false, cout = false;
   sphere_ci(t, p, cin, cout);
   return !cout;
@@ -1256,6 +1892,7 @@ __device__ __forceinline__ bool sphere_contains(const double *t, D3 p)
 
 __device__ __forceinline__ int sphere_inside(const double *t, D3 p)
 {
+  if (VGN_SECTIONS && !sph_flag(t, sp::SphFull)) return sphere_sect_inside(t, p, false);
   bool cin = false, cout = false;
   sphere_ci(t, p, cin, cout);
   int r = kSurfaceE;
@@ -1267,6 +1904,7 @@ __device__ __forceinline__ int sphere_inside(const double *t, D3 p)
 // DistanceToIn (SphereImplementation.h:138-256), full sphere
 __device__ __forceinline__ double sphere_dist_in(const double *t, D3 p, D3 d)
 {
+  if (VGN_SECTIONS && !sph_flag(t, sp::SphFull)) return sphere_sect_dist_in(t, p, d);
   const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
   const double rad2    = mag2(p);
   const double pDotV3d = p.x * d.x + p.y * d.y + p.z * d.z;
@@ -1290,6 +1928,7 @@ __device__ __forceinline__ double sphere_dist_in(const double *t, D3 p, D3 d)
 // DistanceToOut (SphereImplementation.h:258-341), full sphere
 __device__ __forceinline__ double sphere_dist_out(const double *t, D3 p, D3 d)
 {
+  if (VGN_SECTIONS && !sph_flag(t, sp::SphFull)) return sphere_sect_dist_out(t, p, d);
   const double rmax = t[sp::SphRmax], rmin = t[sp::SphRmin];
   const double pDotV3d = p.x * d.x + p.y * d.y + p.z * d.z;
   const double rad2    = mag2(p);
@@ -1310,6 +1949,7 @@ __device__ __forceinline__ double sphere_dist_out(const double *t, D3 p, D3 d)
 // SafetyToIn / SafetyToOut (SphereImplementation.h:388-479), full sphere
 __device__ __forceinline__ double sphere_safe_in(const double *t, D3 p)
 {
+  if (VGN_SECTIONS && !sph_flag(t, sp::SphFull)) return sphere_sect_safe_in(t, p);
   const double rad = sqrt(mag2(p));
   bool cin = false, cout = false;
   sphere_ci(t, p, cin, cout);
@@ -1325,6 +1965,7 @@ __device__ __forceinline__ double sphere_safe_in(const double *t, D3 p)
 
 __device__ __forceinline__ double sphere_safe_out(const double *t, D3 p)
 {
+  if (VGN_SECTIONS && !sph_flag(t, sp::SphFull)) return sphere_sect_safe_out(t, p);
   const double rad = sqrt(mag2(p));
   bool cin = false, cout = false;
   sphere_ci(t, p, cin, cout);
@@ -1673,5 +2314,6 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   return kOutsideE;
 }
 
+}  // namespace VGN_KSET
 }  // namespace dev
 }  // namespace vgn

@@ -40,6 +40,10 @@ struct vgn_geometry {
   size_t sort_words = 0;
 };
 
+// The kernel set a call runs on: `sections` when a shape of the geometry has a phi or
+// theta section, else `full_ranges` (the same kernels compiled without the section code).
+#define VGN_KSET_FN(sect, fn) ((sect) ? vgn::sections::fn : vgn::full_ranges::fn)
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -173,7 +177,7 @@ int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s)
     if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
     a.perm = perm;
   }
-  cudaError_t e = vgn::launch_step(g->view, a, mixed, g->step_variant[m], s);
+  cudaError_t e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[m], s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
 }
 
@@ -408,7 +412,7 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
   const int kind = classify({px, py, pz, in, safety});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = vgn::launch_safety(g->view, n, px, py, pz, in, safety, mixed, max_blocks(g), s);
+    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_safety)(g->view, n, px, py, pz, in, safety, mixed, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "safety kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -424,7 +428,7 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
   if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = vgn::launch_safety(g->view, n, bx, by, bz, din, dsaf, mixed, max_blocks(g), s);
+  e = VGN_KSET_FN(g->host.sections, launch_safety)(g->view, n, bx, by, bz, din, dsaf, mixed, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "safety kernel launch");
   e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
@@ -446,7 +450,7 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   const int kind = classify({px, py, pz, out});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = vgn::launch_locate(g->view, n, px, py, pz, out, mixed, max_blocks(g), s);
+    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_locate)(g->view, n, px, py, pz, out, mixed, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "locate kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -460,7 +464,7 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   if (e == cudaSuccess) e = cudaMemcpyAsync(by, py, nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = vgn::launch_locate(g->view, n, bx, by, bz, dout, mixed, max_blocks(g), s);
+  e = VGN_KSET_FN(g->host.sections, launch_locate)(g->view, n, bx, by, bz, dout, mixed, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "locate kernel launch");
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
@@ -489,7 +493,7 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   const int kind = needdir ? classify({px, py, pz, dx, dy, dz, out}) : classify({px, py, pz, out});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = vgn::launch_shape_fp64(op, type, row, n, px, py, pz, dx, dy, dz, out, max_blocks(g), s);
+    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, px, py, pz, dx, dy, dz, out, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "shape kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -505,7 +509,7 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   cudaError_t e        = cudaSuccess;
   for (int k = 0; k < ncopy && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = vgn::launch_shape_fp64(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5], dout, max_blocks(g), s);
+  e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5], dout, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "shape kernel launch");
   e = cudaMemcpyAsync(out, dout, nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
@@ -515,7 +519,7 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
 int vgn_set_step_config(vgn_geometry *g, int flags, int32_t variant, int32_t sort_kbits)
 {
   if (!g) return fail(VGN_ERR_ARG, "null geometry");
-  if (variant < 0 || variant >= vgn::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
+  if (variant < 0 || variant >= vgn::sections::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
   if (sort_kbits < 0 || sort_kbits > 6) return fail(VGN_ERR_ARG, "track-binning granularity must be 0..6");
   const int m        = (flags & VGN_PRECISION_MIXED) ? 1 : 0;
   g->step_variant[m] = variant;
@@ -557,7 +561,7 @@ int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double
   static const int kSort[] = {0, 3, 4, 5};
   float best = 3.4e38f;
   int bv = 0, bk = 0, rc = VGN_OK;
-  for (int v = 0; v < vgn::step_variant_count() && rc == VGN_OK; ++v) {
+  for (int v = 0; v < vgn::sections::step_variant_count() && rc == VGN_OK; ++v) {
     for (int k : kSort) {
       g->step_variant[m] = v;
       g->sort_kbits[m]   = k;
@@ -599,7 +603,7 @@ int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, dou
   DeviceGuard guard(g->device);
   if (classify({px, py, pz, dx, dy, dz, step_limit, state, nsteps}) != 1)
     return fail(VGN_ERR_ARG, "device pointers required");
-  cudaError_t e = vgn::launch_walk(g->view, n, px, py, pz, dx, dy, dz, step_limit, state, max_steps, nsteps,
+  cudaError_t e = VGN_KSET_FN(g->host.sections, launch_walk)(g->view, n, px, py, pz, dx, dy, dz, step_limit, state, max_steps, nsteps,
                                    (flags & VGN_PRECISION_MIXED) != 0, max_blocks(g),
                                    static_cast<cudaStream_t>(stream));
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "walk kernel launch");
@@ -615,10 +619,11 @@ struct vgn_batch {
   std::vector<vgn::BinParams> bins;
   std::vector<uint32_t *> d_sort;  // per-job binning scratch: keys | histogram | permutation
   std::vector<size_t> sort_words;
-  bool mixed  = false;
-  int reloc   = 1;
-  int variant = 0;
-  int kbits   = 0;
+  bool mixed    = false;
+  bool sections = false;  // some job's geometry needs the `sections` kernel set
+  int reloc     = 1;
+  int variant   = 0;
+  int kbits     = 0;
 };
 
 namespace {
@@ -667,7 +672,7 @@ int batch_enqueue(vgn_batch *b, cudaStream_t s)
       if (e != cudaSuccess) return cuda_fail(e, "batch track binning launch");
     }
   }
-  cudaError_t e = vgn::launch_multi_step(b->jt, b->d_queue, b->mixed, b->reloc, b->num_sms, b->variant, s);
+  cudaError_t e = VGN_KSET_FN(b->sections, launch_multi_step)(b->jt, b->d_queue, b->mixed, b->reloc, b->num_sms, b->variant, s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "batch step launch");
 }
 
@@ -713,7 +718,7 @@ int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int f
   if (!b) return fail(VGN_ERR_ARG, "null batch");
   if (n_jobs < 1 || n_jobs > VGN_BATCH_MAX_JOBS || !jobs)
     return fail(VGN_ERR_ARG, "a batch holds 1.." + std::to_string(VGN_BATCH_MAX_JOBS) + " jobs");
-  if (variant < 0 || variant >= vgn::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
+  if (variant < 0 || variant >= vgn::sections::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
   if (sort_kbits < 0 || sort_kbits > 6) return fail(VGN_ERR_ARG, "track-binning granularity must be 0..6");
   DeviceGuard guard(b->device);
   uint64_t chunks = 0;
@@ -747,6 +752,8 @@ int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int f
     c += (uint32_t)(((uint64_t)j.n + 31) / 32);
   }
   b->jt.chunk_begin[n_jobs] = c;
+  b->sections               = false;
+  for (int k = 0; k < n_jobs; ++k) b->sections = b->sections || jobs[k].geom->host.sections;
   b->mixed                  = (flags & VGN_PRECISION_MIXED) != 0;
   b->reloc                  = (flags & VGN_NO_RELOCATE) ? 0 : 1;
   b->variant                = variant;
@@ -792,7 +799,7 @@ int vgn_batch_autotune(vgn_batch *b, void *stream, int32_t *variant, int32_t *so
   int bv = 0, bk = 0, rc = VGN_OK;
   for (int k : kSort) {
     if ((rc = batch_configure(b, k)) != VGN_OK) break;
-    for (int v = 0; v < vgn::step_variant_count() && rc == VGN_OK; ++v) {
+    for (int v = 0; v < vgn::sections::step_variant_count() && rc == VGN_OK; ++v) {
       b->variant = v;
       if ((rc = batch_enqueue(b, s)) != VGN_OK) break;  // warm-up
       cudaEventRecord(e0, s);
@@ -860,7 +867,7 @@ int vgn_compute_step_batch_static(const vgn_geometry *g, int64_t n, const double
   a.reloc      = (flags & VGN_NO_RELOCATE) ? 0 : 1;
   a.max_blocks = max_blocks(g);
   a.perm       = perm;
-  e = vgn::launch_step(g->view, a, mixed, g->step_variant[mixed ? 1 : 0], s);
+  e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[mixed ? 1 : 0], s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
 }
 

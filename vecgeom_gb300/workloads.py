@@ -320,7 +320,8 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
     and the half-extent of the shape's full (unsectioned) bounding box.  With `sections`,
     three quarters of the tubes, cones and polycones are phi sections (width U[0.2, 2 pi - 0.2],
     start U[0, 2 pi) for tubes and U[-pi, 2 pi) for cones and polycones, whose start angle the
-    reference folds)."""
+    reference folds), and three quarters of the spheres have a phi section, a theta section
+    (hemispheres or bands) or both."""
     u = lambda lo=5.0, hi=60.0: float(rng.uniform(lo, hi))
     if shape == BOX:
         p = (u(), u(), u())
@@ -358,7 +359,21 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
     if shape == SPHERE:
         rmax = u()
         rmin = 0.0 if rng.uniform() < 0.5 else float(rng.uniform(0.1, 0.9)) * rmax
-        return (rmin, rmax, 0.0, K_TWO_PI, 0.0, K_PI), np.array([rmax, rmax, rmax])
+        sphi, dphi, stheta, dtheta = 0.0, K_TWO_PI, 0.0, K_PI
+        if sections and rng.uniform() < 0.75:
+            kind = int(rng.integers(3))  # 0: phi section, 1: theta section, 2: both
+            if kind != 1:
+                sphi, dphi = float(rng.uniform(-K_PI, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+            if kind != 0:
+                c = rng.uniform()
+                if c < 0.2:  # upper hemisphere (the theta cone's XY-plane face)
+                    stheta, dtheta = 0.0, 0.5 * K_PI
+                elif c < 0.4:  # lower hemisphere
+                    stheta, dtheta = 0.5 * K_PI, 0.5 * K_PI
+                else:  # a band; some reach past pi and are clipped
+                    stheta = float(rng.uniform(0.0, K_PI - 0.2))
+                    dtheta = float(rng.uniform(0.2, K_PI - stheta + 0.2))
+        return (rmin, rmax, sphi, dphi, stheta, dtheta), np.array([rmax, rmax, rmax])
     if shape == POLYCONE:  # four z planes
         h = u()
         z = [-h] + sorted(float(v) for v in rng.uniform(-h, h, 2)) + [h]
