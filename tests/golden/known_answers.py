@@ -48,8 +48,8 @@ def _normalize(v):
 
 
 def _case(ref, shape, params, op, p, d, expect, cmp="approx"):
-    return dict(ref=ref, shape=shape, params=tuple(params), op=op, p=tuple(p), d=tuple(d) if d else None,
-                expect=expect, cmp=cmp)
+    return dict(ref=ref, shape=shape, params=tuple(float(v) for v in params), op=op, p=tuple(float(v) for v in p),
+                d=tuple(float(v) for v in d) if d else None, expect=expect, cmp=cmp)
 
 
 B1 = (20.0, 30.0, 40.0)   # TestBox.cpp:46 b1
@@ -1017,6 +1017,138 @@ SPHERE_SECTION_CASES = [
           None, 2, "eq"),
 ]
 SPHERE_CASES += SPHERE_SECTION_CASES
+
+
+# ThetaCone (test/core/ThetaConeTest.cpp) through the sphere that carries it: a solid sphere of
+# radius 1000 mm with full phi and theta range (s, d), so every tested point (|p| <= 30 mm) is
+# radially inside and Inside / Contains are the theta cone's.  The test exercises the older
+# ThetaCone.h; its predicates agree with ThetaCone_Evolution.h, the class SphereStruct holds.
+TC = "test/core/ThetaConeTest.cpp"
+_S3 = math.sqrt(3)
+
+
+def _tc_sphere(s, d):
+    return (0.0, 1000.0, 0.0, 2 * PI_T, s, d)
+
+
+THETA_CONE_CASES = [
+    _case(f"{TC}:50-51", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (0.0, 0.0, 1.0), None, 1, "eq"),
+    _case(f"{TC}:54", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (0.0, 0.0, -1.0), None, 3, "eq"),
+    _case(f"{TC}:56", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (1.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:57", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (-1.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:58", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (0.0, 1.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:59", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (0.0, -1.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:60", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (1.0, 0.0, 1.0), None, 1, "eq"),
+    _case(f"{TC}:61", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (0.0, 1.0, 1.0), None, 1, "eq"),
+    _case(f"{TC}:62", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (0.0, _S3, 1.0), None, 2, "eq"),
+    _case(f"{TC}:63", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (-_S3, 0.0, 1.0), None, 2, "eq"),
+    _case(f"{TC}:64", SPHERE, _tc_sphere(0, PI_T / 3), "inside", (-_S3, 0.0, -1.0), None, 3, "eq"),
+    _case(f"{TC}:67", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (1.0, 0.0, 0.0), None, 0.0, "eq"),
+    _case(f"{TC}:68", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (-1.0, 0.0, 0.0), None, 0.0, "eq"),
+    _case(f"{TC}:69", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (0.0, 1.0, 0.0), None, 0.0, "eq"),
+    _case(f"{TC}:70", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (0.0, -1.0, 0.0), None, 0.0, "eq"),
+    _case(f"{TC}:71", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (1.0, 0.0, 1.0), None, 1.0, "eq"),
+    _case(f"{TC}:72", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (-1.0, 0.0, 1.0), None, 1.0, "eq"),
+    _case(f"{TC}:73", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (0.0, 2.0, 1.0), None, 0.0, "eq"),
+    _case(f"{TC}:74", SPHERE, _tc_sphere(0, PI_T / 3), "contains", (0.0, -1.0, 1.0), None, 1.0, "eq"),
+    _case(f"{TC}:77", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (0.0, 0.0, 1.0), None, 3, "eq"),
+    _case(f"{TC}:78", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (0.0, 0.0, -1.0), None, 1, "eq"),
+    _case(f"{TC}:79", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (1.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:80", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (-1.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:81", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (0.0, 1.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:82", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (0.0, -1.0, 0.0), None, 3, "eq"),
+    _case(f"{TC}:83", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (1.0, 0.0, -1.0), None, 1, "eq"),
+    _case(f"{TC}:84", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (0.0, 1.0, -1.0), None, 1, "eq"),
+    _case(f"{TC}:85", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (0.0, _S3, -1.0), None, 2, "eq"),
+    _case(f"{TC}:86", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (-_S3, 0.0, -1.0), None, 2, "eq"),
+    _case(f"{TC}:87", SPHERE, _tc_sphere(2 * PI_T / 3, PI_T / 3), "inside", (-_S3, 0.0, 1.0), None, 3, "eq"),
+    _case(f"{TC}:90", SPHERE, _tc_sphere(0, 2 * PI_T / 3), "inside", (0.0, 0.0, 1.0), None, 1, "eq"),
+    _case(f"{TC}:91", SPHERE, _tc_sphere(0, 2 * PI_T / 3), "inside", (1.0, 0.0, 0.0), None, 1, "eq"),
+    _case(f"{TC}:92", SPHERE, _tc_sphere(0, 2 * PI_T / 3), "inside", (0.0, 1.0, 0.0), None, 1, "eq"),
+    _case(f"{TC}:93", SPHERE, _tc_sphere(0, 2 * PI_T / 3), "inside", (0.0, 0.0, -1.0), None, 3, "eq"),
+    _case(f"{TC}:96", SPHERE, _tc_sphere(PI_T / 3, 2 * PI_T / 3), "inside", (0.0, 0.0, 1.0), None, 3, "eq"),
+    _case(f"{TC}:97", SPHERE, _tc_sphere(PI_T / 3, 2 * PI_T / 3), "inside", (1.0, 0.0, 0.0), None, 1, "eq"),
+    _case(f"{TC}:98", SPHERE, _tc_sphere(PI_T / 3, 2 * PI_T / 3), "inside", (0.0, 1.0, 0.0), None, 1, "eq"),
+    _case(f"{TC}:99", SPHERE, _tc_sphere(PI_T / 3, 2 * PI_T / 3), "inside", (0.0, 0.0, -1.0), None, 1, "eq"),
+    _case(f"{TC}:102", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, 0.0, 1.0), None, 1, "eq"),
+    _case(f"{TC}:103", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, 0.0, -1.0), None, 3, "eq"),
+    _case(f"{TC}:104", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (1.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:105", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (-1.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:106", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, 1.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:107", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, -1.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:108", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, 0.0, 30.0), None, 1, "eq"),
+    _case(f"{TC}:109", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, 0.0, -30.0), None, 3, "eq"),
+    _case(f"{TC}:110", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (30.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:111", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (-30.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:112", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:113", SPHERE, _tc_sphere(0, 0.50 * PI_T), "inside", (0.0, -30.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:116", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, 0.0, 1.0), None, 3, "eq"),
+    _case(f"{TC}:117", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, 0.0, -1.0), None, 1, "eq"),
+    _case(f"{TC}:118", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (1.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:119", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (-1.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:120", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, 1.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:121", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, -1.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:122", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, 0.0, 30.0), None, 3, "eq"),
+    _case(f"{TC}:123", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, 0.0, -30.0), None, 1, "eq"),
+    _case(f"{TC}:124", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (30.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:125", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (-30.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:126", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, 30.0, 0.0), None, 2, "eq"),
+    _case(f"{TC}:127", SPHERE, _tc_sphere(0.50 * PI_T, 0.50 * PI_T), "inside", (0.0, -30.0, 0.0), None, 2, "eq"),
+]
+SPHERE_CASES += THETA_CONE_CASES
+
+
+# evolution::Wedge (test/core/PhiWedgeTest.cpp, written for the older Wedge.h with the same
+# predicates) through the sphere that carries it: a solid sphere of radius 1000 mm with full
+# theta and phi range (zeroangle, angle), so Inside / Contains at the tested points are the
+# wedge's (the origin is radially inside).  IsOnSurface1/2 (lines 31-32) have no shape-level
+# counterpart and are left out.
+PW = "test/core/PhiWedgeTest.cpp"
+_kTol, _kAngTol = 1e-9, 1e-9  # vecgeom::kTolerance, kAngTolerance (VecGeom/base/Math.h:30)
+_PW_ANGLE = KPI + KPI / 3.    # PhiWedgeTest.cpp:74
+
+
+def _pw_sphere(sphi, dphi):
+    return (0.0, 1000.0, sphi, dphi, 0.0, PI_T)
+
+
+PHI_WEDGE_CASES = [
+    _case(f"{PW}:34-35", SPHERE, _pw_sphere(KPI / 6., 3. * KPI / 2.), "inside", (4.589551141500899, 2.649778586424563, 4.573258549707597), None, 2, "eq"),
+    _case(f"{PW}:38", SPHERE, _pw_sphere(KPI / 6., 3. * KPI / 2.), "contains", (-4.589551141500899, -2.649778586424563, 4.573258549707597), None, 1.0, "eq"),
+    _case(f"{PW}:39-40", SPHERE, _pw_sphere(KPI / 6., 3. * KPI / 2.), "inside", (-4.589551141500899, -2.649778586424563, 4.573258549707597), None, 1, "eq"),
+    _case(f"{PW}:42", SPHERE, _pw_sphere(KPI / 6., 3. * KPI / 2.), "inside", (0., 0., 0.), None, 2, "eq"),
+    _case(f"{PW}:50", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (1., -2. * _kTol, 0.), None, 0.0, "eq"),
+    _case(f"{PW}:51", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (1., 0., 0.), None, 1.0, "eq"),
+    _case(f"{PW}:52", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (1., -1. * _kTol, 0.), None, 0.0, "eq"),
+    _case(f"{PW}:53", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (-1, -1., 0.), None, 0.0, "eq"),
+    _case(f"{PW}:54", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (math.cos(KPI / 3.), math.sin(KPI / 3.), 0.), None, 1.0, "eq"),
+    _case(f"{PW}:55", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (math.cos(KPI / 3. + _kAngTol), math.sin(KPI / 3. + _kAngTol), 0.), None, 0.0, "eq"),
+    _case(f"{PW}:56", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (math.cos(KPI / 6.), math.sin(KPI / 6.), 0.), None, 1.0, "eq"),
+    _case(f"{PW}:57", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (math.cos(KPI / 2.), math.sin(KPI / 2.), 0.), None, 0.0, "eq"),
+    _case(f"{PW}:59", SPHERE, _pw_sphere(0.0, KPI / 3.), "contains", (-1., 0., 0.), None, 0.0, "eq"),
+    _case(f"{PW}:62", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (1., 0., 0.), None, 2, "eq"),
+    _case(f"{PW}:63", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (1., -0.5 * _kTol, 0.), None, 2, "eq"),
+    _case(f"{PW}:64", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (1., 0.5 * _kTol, 0.), None, 2, "eq"),
+    _case(f"{PW}:65", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (math.cos(KPI / 3.), math.sin(KPI / 3.), 0.), None, 2, "eq"),
+    _case(f"{PW}:66-67", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (math.cos(KPI / 3. + _kAngTol), math.sin(KPI / 3. + _kAngTol), 0.), None, 3, "eq"),
+    _case(f"{PW}:68", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (math.cos(KPI / 6.), math.sin(KPI / 6.), 0.), None, 1, "eq"),
+    _case(f"{PW}:69", SPHERE, _pw_sphere(0.0, KPI / 3.), "inside", (math.cos(KPI / 2.), math.sin(KPI / 2.), 0.), None, 3, "eq"),
+    _case(f"{PW}:78", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (1., -2. * _kTol, 0.), None, 0.0, "eq"),
+    _case(f"{PW}:79", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (1., 0., 0.), None, 1.0, "eq"),
+    _case(f"{PW}:80", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (1., -1. * _kTol, 0.), None, 0.0, "eq"),
+    _case(f"{PW}:81", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (math.cos(_PW_ANGLE / 3.), math.sin(_PW_ANGLE / 3.), 0.), None, 1.0, "eq"),
+    _case(f"{PW}:82", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (math.cos(_PW_ANGLE + _kAngTol), math.sin(_PW_ANGLE + _kAngTol), 0.), None, 0.0, "eq"),
+    _case(f"{PW}:83", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (math.cos(_PW_ANGLE / 6.), math.sin(_PW_ANGLE / 6.), 0.), None, 1.0, "eq"),
+    _case(f"{PW}:84", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "contains", (math.cos(_PW_ANGLE + 0.1), math.sin(_PW_ANGLE + 0.1), 0.), None, 0.0, "eq"),
+    _case(f"{PW}:87", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (1., 0., 0.), None, 2, "eq"),
+    _case(f"{PW}:88", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (1., -0.5 * _kTol, 0.), None, 2, "eq"),
+    _case(f"{PW}:89", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (1., 0.5 * _kTol, 0.), None, 2, "eq"),
+    _case(f"{PW}:90", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (math.cos(_PW_ANGLE), math.sin(_PW_ANGLE), 0.), None, 2, "eq"),
+    _case(f"{PW}:91-92", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (math.cos(_PW_ANGLE + _kAngTol), math.sin(_PW_ANGLE + _kAngTol), 0.), None, 3, "eq"),
+    _case(f"{PW}:93", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (math.cos(_PW_ANGLE / 6.), math.sin(_PW_ANGLE / 6.), 0.), None, 1, "eq"),
+    _case(f"{PW}:94", SPHERE, _pw_sphere(0.0, _PW_ANGLE), "inside", (math.cos(_PW_ANGLE + 0.1), math.sin(_PW_ANGLE + 0.1), 0.), None, 3, "eq"),
+]
+SPHERE_CASES += PHI_WEDGE_CASES
 
 POLYCONE = 6
 PC = "test/unit_tests/TestPolycone.cpp"
