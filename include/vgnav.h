@@ -158,6 +158,14 @@ int vgn_shape_batch(const vgn_geometry *geom, int32_t lv, int32_t op, int64_t n,
  * reference, which launches 256 threads per block (backend/cuda/Backend.h:50-96). */
 int vgn_set_step_config(vgn_geometry *geom, int flags, int32_t variant, int32_t sort_kbits);
 int vgn_get_step_config(const vgn_geometry *geom, int flags, int32_t *variant, int32_t *sort_kbits);
+/* Staging of step calls made with host buffers: the batch is split into `chunks`
+ * pieces that alternate between two internal streams, so the host<->device copies of
+ * one piece overlap the kernels of the other (0 = automatic: pieces of at least 2^19
+ * tracks, at most 8; 1 = one piece, copies and kernels in sequence on the caller's
+ * stream).  Only performance changes, never a result.  No counterpart in the
+ * reference, whose batched navigator works on host memory. */
+int vgn_set_staging_chunks(vgn_geometry *geom, int32_t chunks);
+int vgn_get_staging_chunks(const vgn_geometry *geom, int32_t *chunks);
 /* Autotuner: times every (variant, sort_kbits) pair on the given batch (device
  * pointers; outputs are overwritten), keeps the fastest for this precision
  * form and returns it with its time per batch. */

@@ -143,6 +143,28 @@ def test_box_grid_host_pointer_path(oracle, vgnav, cuda, mixed):
     assert np.array_equal(steps2, ref["step"]) and np.array_equal(out2, ref["out"])
 
 
+@pytest.mark.parametrize("chunks", [0, 1, 3, 8])
+def test_box_grid_host_pointer_pipelined(oracle, vgnav, cuda, chunks):
+    """Host-buffer steps split into pieces on the internal streams (uneven last piece, binned
+    and unbinned) equal the oracle."""
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid, n=(1 << 20) + 12345, seed_points=45, seed_dirs=46)
+    ref = og.step(t)
+    geo.set_staging_chunks(chunks)
+    assert geo.staging_chunks() == chunks
+    for kbits in (0, 4):
+        geo.set_step_config(0, kbits, mixed=True)
+        out = np.zeros(t.n, dtype=W.STATE_DTYPE)
+        steps = np.full(t.n, -7.0)
+        saf = np.full(t.n, -7.0)
+        geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit,
+                 vgnav.NavStatePool(t.states), vgnav.NavStatePool(out), steps, saf, mixed=True)
+        assert np.array_equal(steps, ref["step"]) and np.array_equal(saf, ref["safety"])
+        assert np.array_equal(out, ref["out"])
+
+
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["box_grid", "nested"])
 def test_walk_to_world_exit(oracle, vgnav, cuda, which, mixed):

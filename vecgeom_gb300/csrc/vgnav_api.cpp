@@ -38,6 +38,13 @@ struct vgn_geometry {
   std::mutex sort_mutex;
   uint32_t *d_sort  = nullptr;
   size_t sort_words = 0;
+  // pipelined staging of host-buffer steps: pieces alternate between two internal streams,
+  // each with its own half of the staging workspace and of `d_pipe_sort`
+  int staging_chunks      = 0;  // 0 = automatic
+  cudaStream_t pipe[2]    = {nullptr, nullptr};
+  cudaEvent_t pipe_ev[3]  = {nullptr, nullptr, nullptr};  // fork, join of pipe[0], join of pipe[1]
+  uint32_t *d_pipe_sort   = nullptr;
+  size_t pipe_sort_words  = 0;
 };
 
 // The kernel set a call runs on: `sections` when a shape of the geometry has a phi or
@@ -149,12 +156,23 @@ int max_blocks(const vgn_geometry *g) { return g->num_sms > 0 ? g->num_sms * 32 
 
 // Enqueue one step batch with the geometry's launch configuration: optional
 // track binning (counting sort into a visit permutation), then the step kernel.
-int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s)
+// `scratch` (bin_scratch_words(n, kbits) + n words) replaces the geometry's shared
+// binning scratch, for batches staged on the internal streams.
+int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s, uint32_t *scratch = nullptr)
 {
   const int m     = mixed ? 1 : 0;
   const int kbits = g->sort_kbits[m];
   a.perm          = nullptr;
-  if (kbits > 0 && a.n <= (int64_t)UINT32_MAX) {  // the visit permutation holds 32-bit track indices
+  if (kbits > 0 && a.n <= (int64_t)UINT32_MAX && scratch) {
+    vgn::BinParams b = g->bin;
+    b.kbits          = kbits;
+    for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
+    uint32_t *perm = scratch + vgn::bin_scratch_words(a.n, kbits);
+    cudaError_t e  = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, scratch, perm,
+                                            max_blocks(g), s);
+    if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+    a.perm = perm;
+  } else if (kbits > 0 && a.n <= (int64_t)UINT32_MAX) {  // the visit permutation holds 32-bit track indices
     std::lock_guard<std::mutex> lock(g->sort_mutex);
     const size_t need = vgn::bin_scratch_words(a.n, kbits) + (size_t)a.n;
     if (need > g->sort_words) {
@@ -290,6 +308,11 @@ int vgn_geometry_free(vgn_geometry *g)
     if (g->d_status) cudaFree(g->d_status);
     if (g->d_ws) cudaFree(g->d_ws);
     if (g->d_sort) cudaFree(g->d_sort);
+    if (g->d_pipe_sort) cudaFree(g->d_pipe_sort);
+    for (cudaStream_t ps : g->pipe)
+      if (ps) cudaStreamDestroy(ps);
+    for (cudaEvent_t ev : g->pipe_ev)
+      if (ev) cudaEventDestroy(ev);
   }
   delete g;
   return VGN_OK;
@@ -337,6 +360,87 @@ int vgn_geometry_device_bytes(const vgn_geometry *g, size_t *bytes)
   return VGN_OK;
 }
 
+namespace {
+
+// A host-buffer step in `nchunk` pieces: piece i is copied in, binned, stepped and copied out
+// on internal stream i % 2, so the copies of one piece overlap the kernels of the other.
+// Tracks are independent, so the results do not depend on the split.  Called with
+// ws_mutex held; `s` is forked to the two streams and joins them again.
+int staged_step_pipelined(vgn_geometry *g, int64_t n, const double *const src[7], const vgn_state *in,
+                          vgn_state *out, double *step, double *safety, bool mixed, int reloc, int nchunk,
+                          cudaStream_t s)
+{
+  const int64_t cn = (n + nchunk - 1) / nchunk;
+  const size_t nd = (size_t)cn * sizeof(double), ns = (size_t)cn * sizeof(vgn_state);
+  const size_t half = carve_bytes({nd, nd, nd, nd, nd, nd, nd, ns, ns, nd, nd});
+  char *ws          = static_cast<char *>(workspace(g, 2 * half));
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  const int kbits         = g->sort_kbits[mixed ? 1 : 0];
+  const size_t sort_words = kbits > 0 ? vgn::bin_scratch_words(cn, kbits) + (size_t)cn : 0;
+  if (2 * sort_words > g->pipe_sort_words) {
+    if (g->d_pipe_sort) cudaFree(g->d_pipe_sort);
+    g->d_pipe_sort     = nullptr;
+    g->pipe_sort_words = 0;
+    if (cudaMalloc(&g->d_pipe_sort, 2 * sort_words * sizeof(uint32_t)) != cudaSuccess) {
+      cudaGetLastError();
+      g->d_pipe_sort = nullptr;
+      return fail(VGN_ERR_NOMEM, "staging binning scratch allocation failed");
+    }
+    g->pipe_sort_words = 2 * sort_words;
+  }
+  if (!g->pipe[0]) {
+    for (int k = 0; k < 2; ++k)
+      if (cudaStreamCreateWithFlags(&g->pipe[k], cudaStreamNonBlocking) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "staging stream creation");
+    for (int k = 0; k < 3; ++k)
+      if (cudaEventCreateWithFlags(&g->pipe_ev[k], cudaEventDisableTiming) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "staging event creation");
+  }
+  cudaError_t e = cudaEventRecord(g->pipe_ev[0], s);
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(g->pipe[k], g->pipe_ev[0], 0);
+  if (e != cudaSuccess) return cuda_fail(e, "staging fork");
+  int rc = VGN_OK;
+  for (int i = 0; i < nchunk && rc == VGN_OK; ++i) {
+    const int64_t off = (int64_t)i * cn, m = n - off < cn ? n - off : cn;
+    if (m <= 0) break;
+    const int j       = i & 1;
+    cudaStream_t ps   = g->pipe[j];
+    const size_t md = (size_t)m * sizeof(double), ms = (size_t)m * sizeof(vgn_state);
+    Carve c{ws + j * half};
+    double *b[7];
+    for (int k = 0; k < 7; ++k) b[k] = c.take<double>(cn);
+    vgn_state *din = c.take<vgn_state>(cn), *dout = c.take<vgn_state>(cn);
+    double *dstep = c.take<double>(cn), *dsaf = c.take<double>(cn);
+    for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k] + off, md, cudaMemcpyHostToDevice, ps);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(din, in + off, ms, cudaMemcpyHostToDevice, ps);
+    if (e != cudaSuccess) {
+      rc = cuda_fail(e, "host to device copy");
+      break;
+    }
+    vgn::StepArgs a{};
+    a.n = m;
+    a.reloc = reloc;
+    a.max_blocks = max_blocks(g);
+    a.px = b[0]; a.py = b[1]; a.pz = b[2]; a.dx = b[3]; a.dy = b[4]; a.dz = b[5]; a.slimit = b[6];
+    a.in = din; a.out = dout; a.step = dstep; a.safety = safety ? dsaf : nullptr;
+    rc = enqueue_step(g, a, mixed, ps, sort_words ? g->d_pipe_sort + j * sort_words : nullptr);
+    if (rc != VGN_OK) break;
+    e = cudaMemcpyAsync(out + off, dout, ms, cudaMemcpyDeviceToHost, ps);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(step + off, dstep, md, cudaMemcpyDeviceToHost, ps);
+    if (e == cudaSuccess && safety) e = cudaMemcpyAsync(safety + off, dsaf, md, cudaMemcpyDeviceToHost, ps);
+    if (e != cudaSuccess) rc = cuda_fail(e, "device to host copy");
+  }
+  // join both streams back into the caller's stream, also after an error
+  for (int k = 0; k < 2; ++k) {
+    cudaEventRecord(g->pipe_ev[1 + k], g->pipe[k]);
+    cudaStreamWaitEvent(s, g->pipe_ev[1 + k], 0);
+  }
+  if (rc != VGN_OK) return rc;
+  return check_status(g, s);
+}
+
+}  // namespace
+
 int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, const double *py, const double *pz,
                            const double *dx, const double *dy, const double *dz, const double *step_limit,
                            const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream)
@@ -362,8 +466,14 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
     a.in = in; a.out = out; a.step = step; a.safety = safety;
     return enqueue_step(g, a, mixed, s);
   }
-  // host buffers: stage through the device workspace
+  // host buffers: stage through the device workspace, in pipelined pieces for large batches
   std::lock_guard<std::mutex> lock(g->ws_mutex);
+  int nchunk = g->staging_chunks;
+  if (nchunk <= 0) nchunk = (int)(n >> 19 < 8 ? n >> 19 : 8);  // automatic: pieces of >= 2^19 tracks
+  if (nchunk > 1 && n >= nchunk) {
+    const double *src[7] = {px, py, pz, dx, dy, dz, step_limit};
+    return staged_step_pipelined(g, n, src, in, out, step, safety, mixed, a.reloc, nchunk, s);
+  }
   const size_t nd = (size_t)n * sizeof(double), ns = (size_t)n * sizeof(vgn_state);
   const size_t bytes = carve_bytes({nd, nd, nd, nd, nd, nd, nd, ns, ns, nd, nd});
   void *ws = workspace(g, bytes);
@@ -533,6 +643,22 @@ int vgn_get_step_config(const vgn_geometry *g, int flags, int32_t *variant, int3
   const int m = (flags & VGN_PRECISION_MIXED) ? 1 : 0;
   if (variant) *variant = g->step_variant[m];
   if (sort_kbits) *sort_kbits = g->sort_kbits[m];
+  return VGN_OK;
+}
+
+int vgn_set_staging_chunks(vgn_geometry *g, int32_t chunks)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (chunks < 0 || chunks > 64) return fail(VGN_ERR_ARG, "staging pieces must be 0..64");
+  std::lock_guard<std::mutex> lock(g->ws_mutex);
+  g->staging_chunks = chunks;
+  return VGN_OK;
+}
+
+int vgn_get_staging_chunks(const vgn_geometry *g, int32_t *chunks)
+{
+  if (!g || !chunks) return fail(VGN_ERR_ARG, "null argument");
+  *chunks = g->staging_chunks;
   return VGN_OK;
 }
 

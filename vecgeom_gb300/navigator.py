@@ -186,6 +186,15 @@ class Geometry:
     def set_step_config(self, variant: int, sort_kbits: int, mixed: bool = False):
         N.check(N.lib().vgn_set_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, variant, sort_kbits))
 
+    def set_staging_chunks(self, chunks: int):
+        """Pieces a host-buffer step is split into for copy/kernel overlap (0 = automatic)."""
+        N.check(N.lib().vgn_set_staging_chunks(self.handle, chunks))
+
+    def staging_chunks(self) -> int:
+        c = C.c_int32()
+        N.check(N.lib().vgn_get_staging_chunks(self.handle, C.byref(c)))
+        return c.value
+
     def step_config(self, mixed: bool = False) -> tuple[int, int]:
         v, k = C.c_int32(), C.c_int32()
         N.check(N.lib().vgn_get_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, C.byref(v),
