@@ -160,10 +160,11 @@ int vgn_set_step_config(vgn_geometry *geom, int flags, int32_t variant, int32_t 
 int vgn_get_step_config(const vgn_geometry *geom, int flags, int32_t *variant, int32_t *sort_kbits);
 /* Staging of step calls made with host buffers: the batch is split into `chunks`
  * pieces that alternate between two internal streams, so the host<->device copies of
- * one piece overlap the kernels of the other (0 = automatic: pieces of at least 2^19
- * tracks, at most 8; 1 = one piece, copies and kernels in sequence on the caller's
- * stream).  Only performance changes, never a result.  No counterpart in the
- * reference, whose batched navigator works on host memory. */
+ * one piece overlap the kernels of the other (0 = automatic, currently one piece:
+ * copies and kernels in sequence on the caller's stream).  Pieces pay off only where the
+ * copies are slow against the kernels; each piece bins its tracks separately.  Only
+ * performance changes, never a result.  No counterpart in the reference, whose batched
+ * navigator works on host memory. */
 int vgn_set_staging_chunks(vgn_geometry *geom, int32_t chunks);
 int vgn_get_staging_chunks(const vgn_geometry *geom, int32_t *chunks);
 /* Autotuner: times every (variant, sort_kbits) pair on the given batch (device

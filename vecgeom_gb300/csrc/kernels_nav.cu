@@ -139,6 +139,9 @@ __global__ void __launch_bounds__(128, 6) walk_kernel(GeomView g, int64_t n, dou
 
 // Safety kernels: 128-thread blocks, each thread's traversal stack and pending daughters in
 // dynamic shared memory (bvh_safety_mixed), 28 KiB per block.
+#ifndef VGN_SAFETY_MINB
+#define VGN_SAFETY_MINB 6  // resident safety blocks per SM the register cap is set for
+#endif
 constexpr int kSafetyBlock         = 128;
 constexpr size_t kSafetySmemBytes = (size_t)kSafetySmemWords * kSafetyBlock * sizeof(uint32_t);
 
@@ -162,7 +165,7 @@ __device__ __forceinline__ double track_safety(const GeomView &g, const State &s
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(kSafetyBlock, 6) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
+__global__ void __launch_bounds__(kSafetyBlock, VGN_SAFETY_MINB) safety_kernel(GeomView g, int64_t n, const double *__restrict__ px,
                                                      const double *__restrict__ py, const double *__restrict__ pz,
                                                      const vgn_state *__restrict__ in, double *__restrict__ safety,
                                                      const uint32_t *__restrict__ perm, int step_checks)
@@ -182,7 +185,7 @@ __global__ void __launch_bounds__(kSafetyBlock, 6) safety_kernel(GeomView g, int
 // Persistent multi-job safety pass over the same job table and chunk space as
 // multi_step_kernel, for the jobs that asked for safeties.
 template <bool MIXED>
-__global__ void __launch_bounds__(kSafetyBlock, 6) multi_safety_kernel(const __grid_constant__ JobTable jt,
+__global__ void __launch_bounds__(kSafetyBlock, VGN_SAFETY_MINB) multi_safety_kernel(const __grid_constant__ JobTable jt,
                                                               uint32_t *__restrict__ queue)
 {
   const int lane = threadIdx.x & 31;
