@@ -115,6 +115,23 @@ def dist_setup():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, dist=None, device="cpu") -> float:
+    """The largest `x` over all ranks: a replicated job's time is its slowest rank's."""
+    if dist is None:
+        return x
+    import torch
+
+    tt = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(ws: int, tracks_per_rank: int, steps: int, seconds: float) -> float:
+    """Whole-job steps/s of `ws` replicas, each stepping `tracks_per_rank` tracks `steps` times
+    (weak scaling: every rank processes its own full batch)."""
+    return ws * tracks_per_rank * steps / seconds
+
+
 def make_workload(n_tracks: int = N_TRACKS):
     from vecgeom_gb300 import workloads as W
 
@@ -436,11 +453,7 @@ def run_ours(args, ws, rank, local):
             clocks.append(sampler.summary())
         geo.synchronize(stream)
         per = [a.elapsed_time(b) for a, b in evs]
-        total = evs[0][0].elapsed_time(evs[-1][1])
-        if dist is not None:
-            tt = torch.tensor([total], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            total = float(tt.item())
+        total = max_over_ranks(evs[0][0].elapsed_time(evs[-1][1]), dist, "cuda")
         return per, total
 
     # launch configuration (block shape, track binning) picked by the library's autotuner
@@ -461,8 +474,8 @@ def run_ours(args, ws, rank, local):
     plain_per, plain_ms = timed(False)
     clock_log = []
     per, total_ms = timed(True, clock_log)
-    plain_value = ws * t.n * args.steps / (plain_ms * 1e-3)
-    value = ws * t.n * args.steps / (total_ms * 1e-3)
+    plain_value = job_rate(ws, t.n, args.steps, plain_ms * 1e-3)
+    value = job_rate(ws, t.n, args.steps, total_ms * 1e-3)
 
     # ---- end to end through the C ABI with pinned host buffers ----
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -483,12 +496,8 @@ def run_ours(args, ws, rank, local):
     for _ in range(e2e_steps):
         one_host()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    e2e = ws * t.n * e2e_steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    e2e = job_rate(ws, t.n, e2e_steps, e2e_s)
     h2d = t.n * (7 * 8 + 12)
     d2h = t.n * (12 + 8 + 8)
 
