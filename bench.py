@@ -461,15 +461,20 @@ def run_ours(args, ws, rank, local):
     launch_cfg = {}
     for mixed in (False, True):
         if args.fixed_launch:
-            v, k = (int(x) for x in args.fixed_launch.split(","))
+            v, k, *ks = (int(x) for x in args.fixed_launch.split(","))
+            ks = ks[0] if ks else 0
             geo.set_step_config(v, k, mixed=mixed)
-            launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k, "autotune_ms": None}
+            geo.set_safety_binning(ks, mixed=mixed)
+            launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k, "safety_kbits": ks,
+                                                        "autotune_ms": None}
             continue
         v, k, ms = geo.autotune_step(pts, dirs, sl, inp, out, steps, saf, mixed=mixed, stream=stream)
-        launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k, "autotune_ms": ms}
+        launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k,
+                                                    "safety_kbits": geo.safety_binning(mixed=mixed), "autotune_ms": ms}
     geo.synchronize(stream)
-    # safety pass + step kernel, plus 3 binning kernels (keys, scan, scatter) when binning
-    launches_per_step = 2 + (3 if launch_cfg["mixed"]["sort_kbits"] > 0 else 0)
+    # safety pass + step kernel, plus 3 binning kernels (keys, scan, scatter) per binned order
+    mcfg = launch_cfg["mixed"]
+    launches_per_step = 2 + 3 * ((mcfg["sort_kbits"] > 0) + (mcfg["safety_kbits"] > 0))
 
     plain_per, plain_ms = timed(False)
     clock_log = []
@@ -594,7 +599,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tracks", type=int, default=N_TRACKS, help="tracks per step (smaller only for profiling)")
     ap.add_argument("--no-mixed-shapes", action="store_true", help="skip the 8192-mixed-shape workload")
-    ap.add_argument("--fixed-launch", default="", help="VARIANT,KBITS instead of autotuning (profiling runs)")
+    ap.add_argument("--fixed-launch", default="",
+                    help="VARIANT,KBITS[,SAFETY_KBITS] instead of autotuning (profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-geometry batched workload")
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")

@@ -167,9 +167,18 @@ int vgn_get_step_config(const vgn_geometry *geom, int flags, int32_t *variant, i
  * navigator works on host memory. */
 int vgn_set_staging_chunks(vgn_geometry *geom, int32_t chunks);
 int vgn_get_staging_chunks(const vgn_geometry *geom, int32_t *chunks);
+/* The safety pass's own visit order (steps that ask for safeties): tracks binned by
+ * position alone into 2^kbits cells per axis of the world box, 1..6 (the safety does
+ * not depend on the direction, so the octant split of the step's order only scatters
+ * neighbours); 0 = the safety pass follows the step's order.  Only performance
+ * changes, never a result; shares the per-geometry binning scratch. */
+int vgn_set_safety_binning(vgn_geometry *geom, int flags, int32_t kbits);
+int vgn_get_safety_binning(const vgn_geometry *geom, int flags, int32_t *kbits);
 /* Autotuner: times every (variant, sort_kbits) pair on the given batch (device
  * pointers; outputs are overwritten), keeps the fastest for this precision
- * form and returns it with its time per batch. */
+ * form and returns it with its time per batch; when `safety` is given, it then
+ * times the safety pass's binning (0, 4, 5, 6) with that configuration and keeps
+ * the fastest (vgn_get_safety_binning reads it). */
 int vgn_autotune_step(vgn_geometry *geom, int64_t n, const double *px, const double *py, const double *pz,
                       const double *dx, const double *dy, const double *dz, const double *step_limit,
                       const vgn_state *in, vgn_state *out, double *step, double *safety, int flags, void *stream,

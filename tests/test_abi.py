@@ -115,5 +115,17 @@ def test_step_config_host_logic(vgnav):
     assert L.vgn_set_step_config(h.h, 0, 0, -1) == N.VGN_ERR_ARG
     assert L.vgn_set_step_config(h.h, 0, 0, 7) == N.VGN_ERR_ARG
     assert L.vgn_set_step_config(None, 0, 0, 0) == N.VGN_ERR_ARG
+    # the safety pass's own (position-only) binning
+    ks = C.c_int32(-1)
+    assert L.vgn_get_safety_binning(h.h, N.VGN_PRECISION_MIXED, C.byref(ks)) == N.VGN_OK and ks.value == 0
+    assert L.vgn_set_safety_binning(h.h, N.VGN_PRECISION_MIXED, 6) == N.VGN_OK
+    L.vgn_get_safety_binning(h.h, N.VGN_PRECISION_MIXED, C.byref(ks))
+    assert ks.value == 6
+    L.vgn_get_safety_binning(h.h, 0, C.byref(ks))
+    assert ks.value == 0
+    for bad in (-1, 7):
+        assert L.vgn_set_safety_binning(h.h, 0, bad) == N.VGN_ERR_ARG
+    assert L.vgn_set_safety_binning(None, 0, 1) == N.VGN_ERR_ARG
+    assert L.vgn_get_safety_binning(h.h, 0, None) == N.VGN_ERR_ARG
     # the autotuner needs a device geometry
     assert L.vgn_autotune_step(h.h, 1, *([None] * 11), 0, None, None, None, None) == N.VGN_ERR_ARG

@@ -143,6 +143,27 @@ def test_box_grid_host_pointer_path(oracle, vgnav, cuda, mixed):
     assert np.array_equal(steps2, ref["step"]) and np.array_equal(out2, ref["out"])
 
 
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("kbits,safety_kbits", [(0, 6), (5, 6), (5, 3), (3, 1)])
+def test_safety_pass_own_order(oracle, vgnav, cuda, mixed, kbits, safety_kbits):
+    """The safety pass on its own position-only visit order (with and without the step's binned
+    order) gives the oracle's steps, safeties and states, on the box grid and the mixed shapes."""
+    grid = W.box_grid_geometry()
+    cases = [(grid.desc, W.box_grid_tracks(grid, n=1 << 16, seed_points=48, seed_dirs=49)),
+             (W.mixed_shape_geometry(), W.mixed_shape_tracks(1 << 15, seed_points=50, seed_dirs=51))]
+    for desc, t in cases:
+        og = oracle.OracleGeometry(desc)
+        geo = vgnav.Geometry(desc)
+        if desc is not grid.desc:  # mixed-shape tracks start where the oracle locates them
+            t.states = og.locate(t.x, t.y, t.z)
+        geo.set_step_config(0, kbits, mixed=mixed)
+        geo.set_safety_binning(safety_kbits, mixed=mixed)
+        ref = og.step(t, calcsafety=True)
+        got = gpu_step(cuda, geo, t, mixed=mixed)
+        assert np.array_equal(got["step"], ref["step"]) and np.array_equal(got["safety"], ref["safety"])
+        assert np.array_equal(got["out"], ref["out"])
+
+
 @pytest.mark.parametrize("chunks", [0, 1, 3, 8])
 def test_box_grid_host_pointer_pipelined(oracle, vgnav, cuda, chunks):
     """Host-buffer steps split into pieces on the internal streams (uneven last piece, binned

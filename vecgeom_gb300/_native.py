@@ -43,6 +43,8 @@ EXPORTED = [
     "vgn_shape_batch",
     "vgn_set_step_config",
     "vgn_get_step_config",
+    "vgn_set_safety_binning",
+    "vgn_get_safety_binning",
     "vgn_set_staging_chunks",
     "vgn_get_staging_chunks",
     "vgn_autotune_step",
@@ -121,6 +123,8 @@ def lib() -> C.CDLL:
         L.vgn_shape_batch.argtypes = [vp, i32, i32, i64, p, p, p, p, p, p, p, p, C.c_int, vp]
         L.vgn_set_step_config.argtypes = [vp, C.c_int, i32, i32]
         L.vgn_get_step_config.argtypes = [vp, C.c_int, C.POINTER(i32), C.POINTER(i32)]
+        L.vgn_set_safety_binning.argtypes = [vp, C.c_int, i32]
+        L.vgn_get_safety_binning.argtypes = [vp, C.c_int, C.POINTER(i32)]
         L.vgn_set_staging_chunks.argtypes = [vp, i32]
         L.vgn_get_staging_chunks.argtypes = [vp, C.POINTER(i32)]
         L.vgn_autotune_step.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, p, p, C.c_int, vp,

@@ -301,18 +301,20 @@ static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cud
   }
 }
 
-// The safety runs as its own pass over the same visit order, before the step (which may
-// overwrite the input states when out == in): fused into the step kernel it shares one
-// register budget and one instruction footprint with the step traversal and the
-// relocation, which measured slower than the two passes together.
+// The safety runs as its own pass, before the step (which may overwrite the input states when
+// out == in): fused into the step kernel it shares one register budget and one instruction
+// footprint with the step traversal and the relocation, which measured slower than the two
+// passes together.  Its visit order is its own when the caller binned tracks by position
+// alone (the safety does not depend on the direction), else the step's.
 static void launch_safety_pass(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s)
 {
   const unsigned grid = grid_for(a.n, dev::kSafetyBlock, a.max_blocks * (256 / dev::kSafetyBlock));
   if (mixed)
     dev::safety_kernel<true><<<grid, dev::kSafetyBlock, dev::kSafetySmemBytes, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety,
-                                                                         a.perm, 1);
+                                                                         a.perm_safety ? a.perm_safety : a.perm, 1);
   else
-    dev::safety_kernel<false><<<grid, dev::kSafetyBlock, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety, a.perm, 1);
+    dev::safety_kernel<false><<<grid, dev::kSafetyBlock, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.in, a.safety,
+                                                                  a.perm_safety ? a.perm_safety : a.perm, 1);
 }
 
 cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s)

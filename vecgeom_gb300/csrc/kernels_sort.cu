@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256) bin_keys_kernel(int64_t n, const double *
     const uint32_t cy = (uint32_t)fminf(fmaxf(fy, 0.f), (float)cmax);
     const uint32_t cz = (uint32_t)fminf(fmaxf(fz, 0.f), (float)cmax);
     const uint32_t oct = (dx[i] > 0.0 ? 4u : 0u) | (dy[i] > 0.0 ? 2u : 0u) | (dz[i] > 0.0 ? 1u : 0u);
-    const uint32_t key = (oct << (3 * b.kbits)) | (spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz);
+    const uint32_t key = (b.octants ? oct << (3 * b.kbits) : 0u) | (spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz);
     keys[i]            = key;
     atomicAdd(hist + key, 1u);
   }
@@ -118,7 +118,7 @@ cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, con
                               const double *dy, const double *dz, const BinParams &b, uint32_t *scratch,
                               uint32_t *perm, int max_blocks, cudaStream_t s)
 {
-  const uint32_t nbins = 8u << (3 * b.kbits);
+  const uint32_t nbins = (b.octants ? 8u : 1u) << (3 * b.kbits);
   uint32_t *keys = scratch, *hist = scratch + n;
   cudaError_t e  = cudaMemsetAsync(hist, 0, nbins * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;

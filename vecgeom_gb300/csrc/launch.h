@@ -19,6 +19,7 @@ struct StepArgs {
   int reloc;
   int max_blocks;
   const uint32_t *perm;  // optional visit order (track binning), nullptr = identity
+  const uint32_t *perm_safety = nullptr;  // the safety pass's own order, nullptr = `perm`
 };
 
 // track binning (kernels_sort.cu)
@@ -26,6 +27,7 @@ struct BinParams {
   float lo[3];     // world bounding box corner
   float scale[3];  // cells per mm along each axis
   int kbits;       // 2^kbits cells per axis, 1..6
+  int octants = 1; // 1: key = direction octant, then cell (the step's order); 0: cell only
 };
 size_t bin_scratch_words(int64_t n, int kbits);  // keys + histogram (perm not included)
 cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, const double *pz, const double *dx,

@@ -33,6 +33,9 @@ struct vgn_geometry {
   // kernel launch-shape variant and track-binning granularity (0 = no binning)
   int step_variant[2] = {0, 0};
   int sort_kbits[2]   = {0, 0};
+  // the safety pass's own visit order: tracks binned by position alone into 2^k cells per
+  // axis (0 = the step's order)
+  int safety_kbits[2] = {0, 0};
   vgn::BinParams bin{};
   // track-binning scratch (keys, histogram, permutation), grown on demand
   std::mutex sort_mutex;
@@ -172,28 +175,47 @@ int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s, u
                                             max_blocks(g), s);
     if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
     a.perm = perm;
-  } else if (kbits > 0 && a.n <= (int64_t)UINT32_MAX) {  // the visit permutation holds 32-bit track indices
-    std::lock_guard<std::mutex> lock(g->sort_mutex);
-    const size_t need = vgn::bin_scratch_words(a.n, kbits) + (size_t)a.n;
-    if (need > g->sort_words) {
-      if (g->d_sort) cudaFree(g->d_sort);
-      g->d_sort     = nullptr;
-      g->sort_words = 0;
-      if (cudaMalloc(&g->d_sort, need * sizeof(uint32_t)) != cudaSuccess) {
-        cudaGetLastError();
-        g->d_sort = nullptr;
-        return fail(VGN_ERR_NOMEM, "track-binning scratch allocation failed");
+  } else if (a.n <= (int64_t)UINT32_MAX) {  // the visit permutations hold 32-bit track indices
+    const int ks = a.safety ? g->safety_kbits[m] : 0;
+    if (kbits > 0 || ks > 0) {
+      std::lock_guard<std::mutex> lock(g->sort_mutex);
+      // keys and histogram (reused by the two binnings in stream order), then the orders
+      size_t head = kbits > 0 ? vgn::bin_scratch_words(a.n, kbits) : 0;
+      if (ks > 0 && vgn::bin_scratch_words(a.n, ks) > head) head = vgn::bin_scratch_words(a.n, ks);
+      const size_t need = head + (size_t)a.n * ((kbits > 0 ? 1 : 0) + (ks > 0 ? 1 : 0));
+      if (need > g->sort_words) {
+        if (g->d_sort) cudaFree(g->d_sort);
+        g->d_sort     = nullptr;
+        g->sort_words = 0;
+        if (cudaMalloc(&g->d_sort, need * sizeof(uint32_t)) != cudaSuccess) {
+          cudaGetLastError();
+          g->d_sort = nullptr;
+          return fail(VGN_ERR_NOMEM, "track-binning scratch allocation failed");
+        }
+        g->sort_words = need;
       }
-      g->sort_words = need;
+      uint32_t *next = g->d_sort + head;
+      if (kbits > 0) {  // the step's order: direction octant, then position
+        vgn::BinParams b = g->bin;
+        b.kbits          = kbits;
+        for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
+        cudaError_t e = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, g->d_sort, next,
+                                               max_blocks(g), s);
+        if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+        a.perm = next;
+        next += a.n;
+      }
+      if (ks > 0) {  // the safety pass's order: position alone
+        vgn::BinParams b = g->bin;
+        b.kbits          = ks;
+        b.octants        = 0;
+        for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << ks);
+        cudaError_t e = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, g->d_sort, next,
+                                               max_blocks(g), s);
+        if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+        a.perm_safety = next;
+      }
     }
-    vgn::BinParams b = g->bin;
-    b.kbits          = kbits;
-    for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
-    uint32_t *perm   = g->d_sort + vgn::bin_scratch_words(a.n, kbits);
-    cudaError_t e    = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, g->d_sort, perm,
-                                              max_blocks(g), s);
-    if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
-    a.perm = perm;
   }
   cudaError_t e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[m], s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
@@ -648,6 +670,21 @@ int vgn_get_step_config(const vgn_geometry *g, int flags, int32_t *variant, int3
   return VGN_OK;
 }
 
+int vgn_set_safety_binning(vgn_geometry *g, int flags, int32_t kbits)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (kbits < 0 || kbits > 6) return fail(VGN_ERR_ARG, "safety binning granularity must be 0..6");
+  g->safety_kbits[(flags & VGN_PRECISION_MIXED) ? 1 : 0] = kbits;
+  return VGN_OK;
+}
+
+int vgn_get_safety_binning(const vgn_geometry *g, int flags, int32_t *kbits)
+{
+  if (!g || !kbits) return fail(VGN_ERR_ARG, "null argument");
+  *kbits = g->safety_kbits[(flags & VGN_PRECISION_MIXED) ? 1 : 0];
+  return VGN_OK;
+}
+
 int vgn_set_staging_chunks(vgn_geometry *g, int32_t chunks)
 {
   if (!g) return fail(VGN_ERR_ARG, "null geometry");
@@ -686,31 +723,51 @@ int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  // time one configuration: a warm-up call, then the mean of two
+  auto time_cfg = [&](float &ms) -> int {
+    int r = enqueue_step(g, a, mixed, s);
+    if (r != VGN_OK) return r;
+    cudaEventRecord(e0, s);
+    for (int k = 0; k < 2 && r == VGN_OK; ++k) r = enqueue_step(g, a, mixed, s);
+    cudaEventRecord(e1, s);
+    if (r != VGN_OK) return r;
+    if (cudaEventSynchronize(e1) != cudaSuccess) return cuda_fail(cudaGetLastError(), "autotune timing");
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms *= 0.5f;
+    return VGN_OK;
+  };
+  // launch shape and the step's binning, with the safety pass on a 2^6-per-axis position order;
+  // then the safety pass's order with the chosen step configuration
   static const int kSort[] = {0, 3, 4, 5};
+  static const int kSafetySort[] = {0, 4, 5, 6};
   float best = 3.4e38f;
-  int bv = 0, bk = 0, rc = VGN_OK;
+  int bv = 0, bk = 0, bs = 0, rc = VGN_OK;
+  g->safety_kbits[m] = safety ? 6 : 0;
   for (int v = 0; v < vgn::sections::step_variant_count() && rc == VGN_OK; ++v) {
     for (int k : kSort) {
       g->step_variant[m] = v;
       g->sort_kbits[m]   = k;
-      if ((rc = enqueue_step(g, a, mixed, s)) != VGN_OK) break;  // warm-up
-      cudaEventRecord(e0, s);
-      for (int r = 0; r < 2 && rc == VGN_OK; ++r) rc = enqueue_step(g, a, mixed, s);
-      cudaEventRecord(e1, s);
-      if (cudaEventSynchronize(e1) != cudaSuccess) {
-        rc = cuda_fail(cudaGetLastError(), "autotune timing");
-        break;
-      }
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      ms *= 0.5f;
+      float ms           = 0.f;
+      if ((rc = time_cfg(ms)) != VGN_OK) break;
       if (ms < best) best = ms, bv = v, bk = k;
+    }
+  }
+  g->step_variant[m] = bv;
+  g->sort_kbits[m]   = bk;
+  bs                 = g->safety_kbits[m];
+  if (safety) {
+    best = 3.4e38f;
+    for (int k : kSafetySort) {
+      if (rc != VGN_OK) break;
+      g->safety_kbits[m] = k;
+      float ms           = 0.f;
+      if ((rc = time_cfg(ms)) != VGN_OK) break;
+      if (ms < best) best = ms, bs = k;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  g->step_variant[m] = bv;
-  g->sort_kbits[m]   = bk;
+  g->safety_kbits[m] = bs;
   if (rc != VGN_OK) return rc;
   if (variant) *variant = bv;
   if (sort_kbits) *sort_kbits = bk;

@@ -186,6 +186,16 @@ class Geometry:
     def set_step_config(self, variant: int, sort_kbits: int, mixed: bool = False):
         N.check(N.lib().vgn_set_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, variant, sort_kbits))
 
+    def set_safety_binning(self, kbits: int, mixed: bool = False):
+        """The safety pass's own visit order: tracks binned by position alone into 2^kbits cells
+        per axis (0 = the step's order)."""
+        N.check(N.lib().vgn_set_safety_binning(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, kbits))
+
+    def safety_binning(self, mixed: bool = False) -> int:
+        k = C.c_int32()
+        N.check(N.lib().vgn_get_safety_binning(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, C.byref(k)))
+        return k.value
+
     def set_staging_chunks(self, chunks: int):
         """Pieces a host-buffer step is split into for copy/kernel overlap (0 = automatic)."""
         N.check(N.lib().vgn_set_staging_chunks(self.handle, chunks))
