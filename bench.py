@@ -472,9 +472,10 @@ def run_ours(args, ws, rank, local):
         launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k,
                                                     "safety_kbits": geo.safety_binning(mixed=mixed), "autotune_ms": ms}
     geo.synchronize(stream)
-    # safety pass + step kernel, plus 3 binning kernels (keys, scan, scatter) per binned order
+    # safety pass + step kernel, plus 5 binning kernels per binned order (keys, tile sums,
+    # tile-sum scan, tile scan, scatter)
     mcfg = launch_cfg["mixed"]
-    launches_per_step = 2 + 3 * ((mcfg["sort_kbits"] > 0) + (mcfg["safety_kbits"] > 0))
+    launches_per_step = 2 + 5 * ((mcfg["sort_kbits"] > 0) + (mcfg["safety_kbits"] > 0))
 
     plain_per, plain_ms = timed(False)
     clock_log = []

@@ -203,7 +203,8 @@ __global__ void __launch_bounds__(kSafetyBlock, VGN_SAFETY_MINB) multi_safety_ke
     const JobRec &j = jt.job[lo];
     const int64_t t = (int64_t)(chunk - jt.chunk_begin[lo]) * 32 + lane;
     if (j.safety && t < j.n) {
-      const int64_t i = j.perm ? (int64_t)__ldg(j.perm + t) : t;
+      const uint32_t *order = j.perm_safety ? j.perm_safety : j.perm;
+      const int64_t i       = order ? (int64_t)__ldg(order + t) : t;
       const State s   = load_state(j.in, i);
       if (!safety_state_ok(j.g, s, true)) {
         raise_error(j.g, kErrState);

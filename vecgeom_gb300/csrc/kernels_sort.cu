@@ -73,6 +73,71 @@ __global__ void __launch_bounds__(1024) scan_kernel(uint32_t *hist, uint32_t nbi
   }
 }
 
+// Exclusive scan of the histogram in three coalesced passes over 4096-bin tiles: per-tile
+// sums, an in-place scan of the tile sums (scan_kernel, at most 512 of them), then each
+// tile's own scan offset by its prefix.  Thread t of a block owns bins 4t..4t+3 of the tile.
+constexpr uint32_t kScanTile = 4096;
+static_assert((8u << 18) / kScanTile <= 512, "tile sums of the largest histogram fit kScanSumWords");
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total)
+{
+  __shared__ uint32_t warp_sums[32];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {  // inclusive scan within the warp
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= (uint32_t)off) x += y;
+  }
+  if (lane == 31u) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_sums[lane];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= (uint32_t)off) w += y;
+    }
+    warp_sums[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  const uint32_t before = warp ? warp_sums[warp - 1] : 0u;
+  if (total) *total = warp_sums[31];
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(1024) tile_sum_kernel(const uint32_t *__restrict__ hist, uint32_t nbins,
+                                                        uint32_t *__restrict__ sums)
+{
+  const uint32_t b = blockIdx.x * kScanTile + 4u * threadIdx.x;
+  uint32_t s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k)
+    if (b + k < nbins) s += hist[b + k];
+  uint32_t total = 0;
+  block_exclusive_scan(s, &total);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) tile_scan_kernel(uint32_t *__restrict__ hist, uint32_t nbins,
+                                                         const uint32_t *__restrict__ prefix)
+{
+  const uint32_t b = blockIdx.x * kScanTile + 4u * threadIdx.x;
+  uint32_t v[4];
+  uint32_t s = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    v[k] = b + k < nbins ? hist[b + k] : 0u;
+    s += v[k];
+  }
+  uint32_t run = prefix[blockIdx.x] + block_exclusive_scan(s, nullptr);
+#pragma unroll
+  for (uint32_t k = 0; k < 4; ++k) {
+    if (b + k < nbins) hist[b + k] = run;
+    run += v[k];
+  }
+}
+
 __global__ void __launch_bounds__(256) scatter_kernel(int64_t n, const uint32_t *__restrict__ keys,
                                                       uint32_t *__restrict__ cursor, uint32_t *__restrict__ perm)
 {
@@ -82,13 +147,14 @@ __global__ void __launch_bounds__(256) scatter_kernel(int64_t n, const uint32_t 
 
 }  // namespace dev
 
-size_t bin_scratch_words(int64_t n, int kbits) { return 2 * (size_t)n + ((size_t)8 << (3 * kbits)); }
+// keys [n] | histogram [8 * 2^(3k)] | tile sums [512] | spare [n]
+size_t bin_scratch_words(int64_t n, int kbits) { return 2 * (size_t)n + ((size_t)8 << (3 * kbits)) + kScanSumWords; }
 
 // ---- fixed device scratch of vgn_compute_step_batch_static ----------------
-// keys [n] | histogram [8 * 2^(3k)] | visit permutation [n], at the largest n and k
-// the entry point accepts: 2 * 2^20 + 2^18 words = 9 MiB per device.
+// keys [n] | histogram [8 * 2^(3k)] | tile sums [512] | visit permutation [n], at the largest
+// n and k the entry point accepts: 2 * 2^20 + 2^18 + 512 words = 9 MiB per device.
 static constexpr size_t kStaticScratchWords =
-    2 * (size_t)VGN_STATIC_SCRATCH_MAX_TRACKS + ((size_t)8 << (3 * VGN_STATIC_SCRATCH_MAX_KBITS));
+    2 * (size_t)VGN_STATIC_SCRATCH_MAX_TRACKS + ((size_t)8 << (3 * VGN_STATIC_SCRATCH_MAX_KBITS)) + kScanSumWords;
 static __device__ __align__(256) uint32_t g_static_scratch[kStaticScratchWords];
 
 size_t static_scratch_words() { return kStaticScratchWords; }
@@ -126,7 +192,11 @@ cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, con
   if (blocks > max_blocks) blocks = max_blocks;
   if (blocks < 1) blocks = 1;
   dev::bin_keys_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, px, py, pz, dx, dy, dz, b, keys, hist);
-  dev::scan_kernel<<<1, 1024, 0, s>>>(hist, nbins);
+  const uint32_t tiles = (nbins + dev::kScanTile - 1) / dev::kScanTile;  // <= kScanSumWords for kbits <= 6
+  uint32_t *sums       = hist + ((size_t)8 << (3 * b.kbits));
+  dev::tile_sum_kernel<<<tiles, 1024, 0, s>>>(hist, nbins, sums);
+  dev::scan_kernel<<<1, 1024, 0, s>>>(sums, tiles);
+  dev::tile_scan_kernel<<<tiles, 1024, 0, s>>>(hist, nbins, sums);
   dev::scatter_kernel<<<(unsigned)blocks, 256, 0, s>>>(n, keys, hist, perm);
   return cudaGetLastError();
 }

@@ -29,7 +29,8 @@ struct BinParams {
   int kbits;       // 2^kbits cells per axis, 1..6
   int octants = 1; // 1: key = direction octant, then cell (the step's order); 0: cell only
 };
-size_t bin_scratch_words(int64_t n, int kbits);  // keys + histogram (perm not included)
+constexpr size_t kScanSumWords = 512;             // tile sums of the histogram scan (kbits <= 6)
+size_t bin_scratch_words(int64_t n, int kbits);  // keys + histogram + tile sums (perm not included)
 cudaError_t launch_bin_tracks(int64_t n, const double *px, const double *py, const double *pz, const double *dx,
                               const double *dy, const double *dz, const BinParams &b, uint32_t *scratch,
                               uint32_t *perm, int max_blocks, cudaStream_t s);
@@ -46,6 +47,7 @@ struct JobRec {
   vgn_state *out;
   double *step, *safety;
   const uint32_t *perm;  // nullptr = identity
+  const uint32_t *perm_safety;  // the safety pass's own order, nullptr = `perm`
   int64_t n;
 };
 // the whole multi-job launch description, passed by value as a kernel parameter

@@ -806,6 +806,7 @@ struct vgn_batch {
   std::vector<size_t> sort_words;
   bool mixed    = false;
   bool sections = false;  // some job's geometry needs the `sections` kernel set
+  int safety_kbits = 0;   // the safety pass's own position-only order (0 = the step's)
   int reloc     = 1;
   int variant   = 0;
   int kbits     = 0;
@@ -815,17 +816,21 @@ namespace {
 
 // (re)build the per-job visit orders for `kbits` (0 = none); allocates only when a job's
 // scratch is too small
-int batch_configure(vgn_batch *b, int kbits)
+int batch_configure(vgn_batch *b, int kbits, int ks)
 {
   const size_t nj = b->jobs.size();
   b->d_sort.resize(nj, nullptr);
   b->sort_words.resize(nj, 0);
-  b->bins.resize(nj);
+  b->bins.resize(2 * nj);  // per job: the step's order, the safety pass's order
   for (size_t k = 0; k < nj; ++k) {
     vgn::JobRec &r = b->jt.job[k];
     r.perm         = nullptr;
-    if (kbits == 0 || r.n == 0 || r.n > (int64_t)UINT32_MAX) continue;
-    const size_t need = vgn::bin_scratch_words(r.n, kbits) + (size_t)r.n;
+    r.perm_safety  = nullptr;
+    const int kss  = r.safety ? ks : 0;
+    if ((kbits == 0 && kss == 0) || r.n == 0 || r.n > (int64_t)UINT32_MAX) continue;
+    size_t head = kbits > 0 ? vgn::bin_scratch_words(r.n, kbits) : 0;
+    if (kss > 0 && vgn::bin_scratch_words(r.n, kss) > head) head = vgn::bin_scratch_words(r.n, kss);
+    const size_t need = head + (size_t)r.n * ((kbits > 0 ? 1 : 0) + (kss > 0 ? 1 : 0));
     if (need > b->sort_words[k]) {
       if (b->d_sort[k]) cudaFree(b->d_sort[k]);
       b->d_sort[k]     = nullptr;
@@ -836,24 +841,33 @@ int batch_configure(vgn_batch *b, int kbits)
       }
       b->sort_words[k] = need;
     }
-    vgn::BinParams bp = b->jobs[k].geom->bin;
-    bp.kbits          = kbits;
-    for (int a = 0; a < 3; ++a) bp.scale[a] = b->jobs[k].geom->bin.scale[a] * (float)(1 << kbits);
-    b->bins[k] = bp;
-    r.perm     = b->d_sort[k] + vgn::bin_scratch_words(r.n, kbits);
+    uint32_t *next = b->d_sort[k] + head;
+    for (int o = 0; o < 2; ++o) {
+      const int kb = o == 0 ? kbits : kss;
+      if (kb == 0) continue;
+      vgn::BinParams bp = b->jobs[k].geom->bin;
+      bp.kbits          = kb;
+      bp.octants        = o == 0 ? 1 : 0;
+      for (int a = 0; a < 3; ++a) bp.scale[a] = b->jobs[k].geom->bin.scale[a] * (float)(1 << kb);
+      b->bins[2 * k + o] = bp;
+      (o == 0 ? r.perm : r.perm_safety) = next;
+      next += r.n;
+    }
   }
-  b->kbits = kbits;
+  b->kbits        = kbits;
+  b->safety_kbits = ks;
   return VGN_OK;
 }
 
 int batch_enqueue(vgn_batch *b, cudaStream_t s)
 {
-  if (b->kbits > 0) {
-    for (int k = 0; k < b->jt.n_jobs; ++k) {
-      const vgn::JobRec &r = b->jt.job[k];
-      if (!r.perm) continue;
-      cudaError_t e = vgn::launch_bin_tracks(r.n, r.px, r.py, r.pz, r.dx, r.dy, r.dz, b->bins[k], b->d_sort[k],
-                                             const_cast<uint32_t *>(r.perm), b->num_sms * 32, s);
+  for (int k = 0; k < b->jt.n_jobs; ++k) {
+    const vgn::JobRec &r = b->jt.job[k];
+    const uint32_t *orders[2] = {r.perm, r.perm_safety};
+    for (int o = 0; o < 2; ++o) {
+      if (!orders[o]) continue;
+      cudaError_t e = vgn::launch_bin_tracks(r.n, r.px, r.py, r.pz, r.dx, r.dy, r.dz, b->bins[2 * k + o],
+                                             b->d_sort[k], const_cast<uint32_t *>(orders[o]), b->num_sms * 32, s);
       if (e != cudaSuccess) return cuda_fail(e, "batch track binning launch");
     }
   }
@@ -933,6 +947,7 @@ int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int f
     r.in = j.in; r.out = j.out; r.step = j.step; r.safety = j.safety;
     r.n                   = j.n;
     r.perm                = nullptr;
+    r.perm_safety         = nullptr;
     b->jt.chunk_begin[k]  = c;
     c += (uint32_t)(((uint64_t)j.n + 31) / 32);
   }
@@ -942,7 +957,7 @@ int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int f
   b->mixed                  = (flags & VGN_PRECISION_MIXED) != 0;
   b->reloc                  = (flags & VGN_NO_RELOCATE) ? 0 : 1;
   b->variant                = variant;
-  return batch_configure(b, sort_kbits);
+  return batch_configure(b, sort_kbits, b->safety_kbits);
 }
 
 int vgn_batch_step(vgn_batch *b, void *stream)
@@ -979,11 +994,16 @@ int vgn_batch_autotune(vgn_batch *b, void *stream, int32_t *variant, int32_t *so
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  // launch shape and the step's binning with the safety pass on a 2^6-per-axis position order,
+  // then the safety pass's order with that configuration
   static const int kSort[] = {0, 3, 4, 5};
+  static const int kSafetySort[] = {0, 4, 5, 6};
+  bool any_safety = false;
+  for (int k = 0; k < b->jt.n_jobs; ++k) any_safety = any_safety || b->jt.job[k].safety;
   float best = 3.4e38f;
-  int bv = 0, bk = 0, rc = VGN_OK;
+  int bv = 0, bk = 0, bs = any_safety ? 6 : 0, rc = VGN_OK;
   for (int k : kSort) {
-    if ((rc = batch_configure(b, k)) != VGN_OK) break;
+    if ((rc = batch_configure(b, k, bs)) != VGN_OK) break;
     for (int v = 0; v < vgn::sections::step_variant_count() && rc == VGN_OK; ++v) {
       b->variant = v;
       if ((rc = batch_enqueue(b, s)) != VGN_OK) break;  // warm-up
@@ -1001,10 +1021,32 @@ int vgn_batch_autotune(vgn_batch *b, void *stream, int32_t *variant, int32_t *so
     }
     if (rc != VGN_OK) break;
   }
+  b->variant = bv;
+  if (any_safety && rc == VGN_OK) {
+    float best_s = 3.4e38f;
+    int bss      = bs;
+    for (int ks : kSafetySort) {
+      if ((rc = batch_configure(b, bk, ks)) != VGN_OK) break;
+      if ((rc = batch_enqueue(b, s)) != VGN_OK) break;  // warm-up
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 2 && rc == VGN_OK; ++r) rc = batch_enqueue(b, s);
+      cudaEventRecord(e1, s);
+      if (rc != VGN_OK) break;
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = cuda_fail(cudaGetLastError(), "batch autotune timing");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms *= 0.5f;
+      if (ms < best_s) best_s = ms, bss = ks;
+    }
+    bs   = bss;
+    best = best_s;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  b->variant = bv;
-  const int rc2 = batch_configure(b, bk);
+  const int rc2 = batch_configure(b, bk, bs);
   if (rc != VGN_OK) return rc;
   if (rc2 != VGN_OK) return rc2;
   if (variant) *variant = bv;
@@ -1042,8 +1084,8 @@ int vgn_compute_step_batch_static(const vgn_geometry *g, int64_t n, const double
   vgn::BinParams b = g->bin;
   b.kbits          = sort_kbits;
   for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << sort_kbits);
-  // keys [n] | histogram [8 * 2^(3k)], zeroed by launch_bin_tracks | permutation [n]
-  uint32_t *perm = scratch + (size_t)n + ((size_t)8 << (3 * sort_kbits));
+  // keys [n] | histogram [8 * 2^(3k)], zeroed by launch_bin_tracks | tile sums | permutation [n]
+  uint32_t *perm = scratch + (size_t)n + ((size_t)8 << (3 * sort_kbits)) + vgn::kScanSumWords;
   e = vgn::launch_bin_tracks(n, px, py, pz, dx, dy, dz, b, scratch, perm, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
   vgn::StepArgs a{};
