@@ -362,7 +362,7 @@ def run_batched(torch, V, local, steps, warmup, stream) -> dict:
     }
 
 
-def run_serving(torch, V, local, seconds: float) -> dict:
+def run_serving(torch, V, local, seconds: float, launch=None) -> dict:
     """Serving loop against the resident 8192-mixed-shape geometry: requests of log-uniform
     size in [256, 1M] tracks arrive as a Poisson process; each is copied in, located and
     stepped to the world exit on the device (states stay on the device), and its step counts
@@ -373,6 +373,8 @@ def run_serving(torch, V, local, seconds: float) -> dict:
 
     streams = 4
     geo = V.Geometry(W.mixed_shape_geometry(), device=local)
+    if launch:  # the mixed-shape workload's tuned configuration: the walks visit tracks in its binned order
+        geo.set_step_config(launch["variant"], launch["sort_kbits"], mixed=True)
     free, _ = torch.cuda.mem_get_info()
     pool_bytes = int(min(free // 4, 16 << 30))
     ex = S.GpuExecutor(geo, W.MIXED_WORLD, pool_bytes, streams, mixed=True)
@@ -549,7 +551,8 @@ def run_ours(args, ws, rank, local):
             batched = run_batched(torch, V, local, args.batched_steps, args.warmup, torch.cuda.Stream())
         serving = None
         if ws == 1 and not args.no_serving:
-            serving = run_serving(torch, V, local, args.serving_seconds)
+            serving = run_serving(torch, V, local, args.serving_seconds,
+                                  mixed_shapes["mixed"]["launch"] if mixed_shapes else None)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,

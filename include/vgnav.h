@@ -190,6 +190,8 @@ int vgn_autotune_step(vgn_geometry *geom, int64_t n, const double *px, const dou
  * reference's transport examples (persistency/gdml/test/TestVGDMLNavigation/
  * TestVGDMLNavigation.cpp:86-102) with the state kept on the device.  Positions and
  * states are updated in place; nsteps[i] receives the steps taken (-1: invalid state).
+ * Tracks are visited in the binned order of the geometry's step configuration for this
+ * precision form (vgn_set_step_config / vgn_autotune_step), with stream-ordered scratch.
  * Device pointers only.  No single counterpart call in the reference. */
 int vgn_walk_batch(const vgn_geometry *geom, int64_t n, double *px, double *py, double *pz, const double *dx,
                    const double *dy, const double *dz, const double *step_limit, vgn_state *state,

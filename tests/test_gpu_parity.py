@@ -445,11 +445,13 @@ def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
     assert w.n == 0
 
 
+@pytest.mark.parametrize("kbits", [0, 4], ids=["unbinned", "binned"])
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["box_grid", "mixed_shapes"])
-def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed):
+def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed, kbits):
     """vgn_walk_batch (the transport loop on the device) ends every track where the oracle's
-    step-by-step loop ends it: same final point, state and number of steps."""
+    step-by-step loop ends it: same final point, state and number of steps; also with the
+    tracks visited in the binned order of the geometry's step configuration."""
     torch = cuda
     if which == "box_grid":
         grid = W.box_grid_geometry()
@@ -460,6 +462,7 @@ def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed):
         t = W.mixed_shape_tracks(20000, 83, 84)
     og = oracle.OracleGeometry(desc)
     geo = vgnav.Geometry(desc)
+    geo.set_step_config(0, kbits, mixed=mixed)
     if which == "mixed_shapes":
         t.states = og.locate(t.x, t.y, t.z)
     # oracle: step until the world is left, recording where each track ends

@@ -109,10 +109,12 @@ __global__ void __launch_bounds__(128, 6) walk_kernel(GeomView g, int64_t n, dou
                                                       const double *__restrict__ dx, const double *__restrict__ dy,
                                                       const double *__restrict__ dz,
                                                       const double *__restrict__ slimit, vgn_state *__restrict__ state,
-                                                      int max_steps, int32_t *__restrict__ nsteps)
+                                                      int max_steps, int32_t *__restrict__ nsteps,
+                                                      const uint32_t *__restrict__ perm)
 {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    State s = load_state(state, i);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm ? (int64_t)__ldg(perm + t) : t;  // binned visit order, results stay at index i
+    State s         = load_state(state, i);
     if (s.nav_ind != 0 && (!ni_valid(g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(g, s.last_exited)))) {
       raise_error(g, kErrState);
       nsteps[i] = -1;
@@ -372,14 +374,16 @@ cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, i
 
 cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, double *pz, const double *dx,
                         const double *dy, const double *dz, const double *slimit, vgn_state *state, int max_steps,
-                        int32_t *nsteps, bool mixed, int max_blocks, cudaStream_t s)
+                        int32_t *nsteps, const uint32_t *perm, bool mixed, int max_blocks, cudaStream_t s)
 {
   const int block     = 128;
   const unsigned grid = grid_for(n, block, max_blocks * 2);
   if (mixed)
-    dev::walk_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps);
+    dev::walk_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps,
+                                                  perm);
   else
-    dev::walk_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps);
+    dev::walk_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps,
+                                                   perm);
   return cudaGetLastError();
 }
 

@@ -788,9 +788,32 @@ int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, dou
   DeviceGuard guard(g->device);
   if (classify({px, py, pz, dx, dy, dz, step_limit, state, nsteps}) != 1)
     return fail(VGN_ERR_ARG, "device pointers required");
-  cudaError_t e = VGN_KSET_FN(g->host.sections, launch_walk)(g->view, n, px, py, pz, dx, dy, dz, step_limit, state, max_steps, nsteps,
-                                   (flags & VGN_PRECISION_MIXED) != 0, max_blocks(g),
-                                   static_cast<cudaStream_t>(stream));
+  const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
+  cudaStream_t s   = static_cast<cudaStream_t>(stream);
+  // tracks binned like the step's (direction octant, then cell) when the geometry bins its
+  // steps; the scratch is stream-ordered (cudaMallocAsync), so walks on several streams of
+  // one geometry do not share it
+  const int kbits  = g->sort_kbits[mixed ? 1 : 0];
+  uint32_t *sort   = nullptr, *perm = nullptr;
+  if (kbits > 0 && n <= (int64_t)UINT32_MAX) {
+    const size_t words = vgn::bin_scratch_words(n, kbits) + (size_t)n;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&sort), words * sizeof(uint32_t), s) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(VGN_ERR_NOMEM, "walk binning scratch allocation failed");
+    }
+    vgn::BinParams b = g->bin;
+    b.kbits          = kbits;
+    for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
+    perm          = sort + vgn::bin_scratch_words(n, kbits);
+    cudaError_t e = vgn::launch_bin_tracks(n, px, py, pz, dx, dy, dz, b, sort, perm, max_blocks(g), s);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(sort, s);
+      return cuda_fail(e, "walk binning launch");
+    }
+  }
+  cudaError_t e = VGN_KSET_FN(g->host.sections, launch_walk)(g->view, n, px, py, pz, dx, dy, dz, step_limit, state,
+                                                             max_steps, nsteps, perm, mixed, max_blocks(g), s);
+  if (sort) cudaFreeAsync(sort, s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "walk kernel launch");
 }
 
