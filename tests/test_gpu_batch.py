@@ -123,7 +123,7 @@ def test_batch_autotune_and_argument_checks(oracle, vgnav, cuda):
     batch = vgnav.StepBatch(0)
     batch.set_jobs([j.spec() for j in jobs], mixed=True)
     v, k, ms = batch.autotune()
-    assert 0 <= v < 6 and k in (0, 3, 4, 5) and ms > 0
+    assert 0 <= v < 6 and k in (0, 3, 4, 5, 6) and ms > 0
     for j in jobs:
         j.steps.fill_(-7.0)
     batch.step()

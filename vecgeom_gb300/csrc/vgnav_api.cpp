@@ -738,7 +738,7 @@ int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double
   };
   // launch shape and the step's binning, with the safety pass on a 2^6-per-axis position order;
   // then the safety pass's order with the chosen step configuration
-  static const int kSort[] = {0, 3, 4, 5};
+  static const int kSort[] = {0, 3, 4, 5, 6};
   static const int kSafetySort[] = {0, 4, 5, 6};
   float best = 3.4e38f;
   int bv = 0, bk = 0, bs = 0, rc = VGN_OK;
@@ -1019,7 +1019,7 @@ int vgn_batch_autotune(vgn_batch *b, void *stream, int32_t *variant, int32_t *so
     return cuda_fail(cudaGetLastError(), "cudaEventCreate");
   // launch shape and the step's binning with the safety pass on a 2^6-per-axis position order,
   // then the safety pass's order with that configuration
-  static const int kSort[] = {0, 3, 4, 5};
+  static const int kSort[] = {0, 3, 4, 5, 6};
   static const int kSafetySort[] = {0, 4, 5, 6};
   bool any_safety = false;
   for (int k = 0; k < b->jt.n_jobs; ++k) any_safety = any_safety || b->jt.job[k].safety;
