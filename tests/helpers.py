@@ -63,3 +63,26 @@ def advance(t: W.TrackBatch, step: np.ndarray, out_states: np.ndarray) -> W.Trac
 
 def keep(t: W.TrackBatch, mask: np.ndarray) -> W.TrackBatch:
     return W.TrackBatch(*(a[mask] for a in (t.x, t.y, t.z, t.dx, t.dy, t.dz, t.step_limit, t.states)))
+
+
+def navindex_pad_words(table: np.ndarray, n_words: int) -> np.ndarray:
+    """Mask of the words of a navigation table that NavIndexTable's builder reserves but never
+    writes (source/NavIndexTable.cpp:9-99, allocation NavIndexTable.h:92-101): the filler word
+    after a node's daughter list when the daughter count is even, and the alignment word before
+    a cached matrix.  The reference leaves them uninitialised; the builders here write zeros.
+    `n_words` is the reference's table size (GetTableSize() / 4)."""
+    pad = np.zeros(n_words, dtype=bool)
+    i = 1
+    while i < n_words:
+        w = int(table[i + 2])
+        hasm, nd = (w >> 8) & 0xFF, w >> 16
+        if (nd + 1) & 1:
+            pad[i + 3 + nd] = True
+        cur = i + 3 + nd + ((nd + 1) & 1)
+        if hasm:
+            if cur % 2:
+                pad[cur] = True
+                cur += 1
+            cur += 24
+        i = cur
+    return pad

@@ -4,20 +4,16 @@ Bar: bit-exact (np.array_equal on the float64 values, identical 12-byte
 states) for steps, safeties, next volumes, located states and shape queries,
 both through device pointers (torch CUDA tensors) and through host pointers
 (the library's own staging path)."""
-import zlib
-
 import numpy as np
 import pytest
 
 from golden import known_answers as KA
 from helpers import advance, keep
+from shape_sets import OPS, SHAPE_SETS, shape_points, single_shape
 from vecgeom_gb300 import workloads as W
 from vecgeom_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
-
-OPS = {"dist_in": 0, "dist_out": 1, "safe_in": 2, "safe_out": 3, "contains": 4, "inside": 5}
-
 
 def to_dev(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
@@ -44,13 +40,6 @@ def gpu_step(torch, geo, t, safety=True, relocate=True, mixed=False):
     geo.step(pts, dirs, sl, inp, out, steps, saf, relocate=relocate, mixed=mixed)
     geo.synchronize()
     return dict(step=steps.cpu().numpy(), out=out.to_numpy(), safety=None if saf is None else saf.cpu().numpy())
-
-
-def single_shape(shape, params):
-    b = W.GeometryBuilder()
-    lv = b.logical(shape, params)
-    b.place_world(lv)
-    return b.build()
 
 
 @pytest.mark.parametrize("case", KA.ALL_CASES, ids=lambda c: f"{c['ref'].split('/')[-1]}-{c['op']}")
@@ -321,85 +310,15 @@ def test_autotune_then_step(oracle, vgnav, cuda, mixed):
     assert np.array_equal(got["out"], ref["out"])
 
 
-SHAPE_SETS = [
-    ("tube-solid", W.TUBE, (0.0, 30.0, 40.0, 0.0, W.K_TWO_PI)),
-    ("tube-quarter-sector", W.TUBE, (10.0, 50.0, 40.0, 0.5 * W.K_PI, 0.5 * W.K_PI)),
-    ("tube-large-sector", W.TUBE, (20.0, 60.0, 40.0, 0.3, 1.5 * W.K_PI)),
-    ("tube-half-solid", W.TUBE, (0.0, 50.0, 30.0, 0.0, W.K_PI)),
-    ("tube-thin-sector-negative-start", W.TUBE, KA.JIRA174),
-    ("cone-hollow", W.CONE, (10.0, 50.0, 20.0, 40.0, 60.0, 0.0, W.K_TWO_PI)),
-    ("cone-solid-apex", W.CONE, (0.0, 30.0, 0.0, 0.0, 25.0, 0.0, W.K_TWO_PI)),
-    ("cone-inverted", W.CONE, (5.0, 10.0, 20.0, 45.0, 30.0, 0.0, W.K_TWO_PI)),
-    ("cone-sector-60deg-negative-start", W.CONE, KA.C4),
-    ("cone-sector-270deg", W.CONE, KA.C5),
-    ("cone-sector-300deg", W.CONE, KA.CTEST10),
-    ("cone-solid-half", W.CONE, (0.0, 40.0, 0.0, 20.0, 30.0, 1.0, W.K_PI)),
-    ("trd-varying", W.TRD, (10.0, 30.0, 20.0, 40.0, 40.0)),
-    ("trd-const-y", W.TRD, (20.0, 25.0, 30.0, 30.0, 40.0)),
-    ("trd-boxlike", W.TRD, (20.0, 20.0, 30.0, 30.0, 40.0)),
-    ("trd-wedge", W.TRD, (0.0, 30.0, 10.0, 40.0, 25.0)),
-    ("trap-skewed", W.TRAPEZOID, (60.0, 0.35, 0.087, 40.0, 30.0, 40.0, 0.17, 16.0, 10.0, 14.0, 0.17)),
-    ("trap-twisted-alpha", W.TRAPEZOID, (30.0, 0.1, 2.0, 20.0, 10.0, 25.0, -0.3, 35.0, 30.0, 12.0, 0.25)),
-    ("trap-boxlike", W.TRAPEZOID, (40.0, 0.0, 0.0, 30.0, 20.0, 20.0, 0.0, 30.0, 20.0, 20.0, 0.0)),
-    ("sphere-solid", W.SPHERE, (0.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
-    ("sphere-shell", W.SPHERE, (45.0, 50.0, 0.0, W.K_TWO_PI, 0.0, W.K_PI)),
-    ("sphere-shell-rotated-wedge", W.SPHERE, (6.0, 8.0, 1.0, W.K_TWO_PI, 0.0, W.K_PI)),
-    ("sphere-phi-quarter-shell", W.SPHERE, KA.SPH_S4),
-    ("sphere-phi-270-solid", W.SPHERE, (0.0, 50.0, -0.5 * W.K_PI, 1.5 * W.K_PI, 0.0, W.K_PI)),
-    ("sphere-phi-half-solid", W.SPHERE, KA.SPH_SN22),
-    ("sphere-theta-band-shell", W.SPHERE, KA.SPH_S3),
-    ("sphere-theta-band-thick", W.SPHERE, KA.SPH_S13),
-    ("sphere-theta-north-cap", W.SPHERE, KA.SPH_SN12),
-    ("sphere-theta-south-cap", W.SPHERE, KA.SPH_SN13),
-    ("sphere-upper-hemisphere", W.SPHERE, KA.SPH_SN11),
-    ("sphere-lower-hemisphere", W.SPHERE, KA.SPH_SNTESTB),
-    ("sphere-theta-past-equator", W.SPHERE, KA.SPH_SN14),
-    ("sphere-theta-91-180deg", W.SPHERE, KA.SPH_SN17),
-    ("sphere-patch-phi-theta", W.SPHERE, KA.SPH_S5),
-    ("sphere-patch-b9", W.SPHERE, KA.SPH_B9),
-    ("polycone-4plane", W.POLYCONE, KA.PCON1),
-    ("polycone-phi-section-mypcone", W.POLYCONE, KA.MYPCONE),
-    ("polycone-4plane-half-sector", W.POLYCONE, KA._pcon(-1.0, W.K_PI, (-1.0, -0.5, 0.5, 2.0), (0.1, 0.0, 0.0, 0.4),
-                                                         (1.0, 2.0, 2.0, 1.5))),
-    ("polycone-simple", W.POLYCONE, KA.PCON_SIMPLE),
-    ("polycone-steps", W.POLYCONE, KA.PCON175),
-    ("polycone-cms-trak", W.POLYCONE, KA._pcon(0.0, W.K_TWO_PI, (-2935., -1899., -1899., -1899., 1899., 1899., 1899.,
-                                                                 2935.), (74., 34., 31., 31., 31., 31., 34., 74.),
-                                               (1233.,) * 8)),
-]
-
-
-# sampling boxes of sections much smaller than their full shape's box
-SAMPLE_BOXES = {"sphere-patch-b9": ((0.0, 0.0, 2.0), (7.0, 7.0, 8.0))}
-
-
 @pytest.mark.parametrize("name,shape,params", SHAPE_SETS, ids=[s[0] for s in SHAPE_SETS])
 def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda):
     """Every query at points inside, outside and on the surface equals the oracle bit for bit."""
     desc = single_shape(shape, params)
     og = oracle.OracleGeometry(desc)
     geo = vgnav.Geometry(desc)
-    rng = np.random.Generator(np.random.PCG64(zlib.crc32(name.encode())))
-    n = 100000
-    lo, hi = SAMPLE_BOXES.get(name, W.shape_bbox(shape, params))
-    lo, hi = np.asarray(lo, dtype=np.float64), np.asarray(hi, dtype=np.float64)
-    mid, half = 0.5 * (lo + hi), 0.65 * (hi - lo)  # the bounding box enlarged by 30 %
-    x, y, z = (rng.uniform(mid[k] - half[k], mid[k] + half[k], n) for k in range(3))
-    # points on the coordinate planes and axes and at the origin (exact zeros take their own branches)
-    y[:4000] = 0.0
-    x[4000:8000] = 0.0
-    x[8000:9000] = y[8000:9000] = 0.0
-    x[9000:9500] = z[9000:9500] = 0.0
-    x[9500], y[9500], z[9500] = 0.0, 0.0, 0.0
-    dx, dy, dz = W.isotropic(rng, n)
-    # surface points: from inside points, move to the exit point along a random ray
-    inside = og.shape(0, OPS["contains"], x, y, z) == 1.0
-    dout = og.shape(0, OPS["dist_out"], x, y, z, dx, dy, dz)
-    sx, sy, sz = (a[inside] + dout[inside] * b[inside] for a, b in ((x, dx), (y, dy), (z, dz)))
-    m = sx.shape[0]
-    ex, ey, ez = W.isotropic(rng, m)
-    X, Y, Z = (np.concatenate([a, b]) for a, b in ((x, sx), (y, sy), (z, sz)))
-    DX, DY, DZ = (np.concatenate([a, b]) for a, b in ((dx, ex), (dy, ey), (dz, ez)))
+    X, Y, Z, DX, DY, DZ, m = shape_points(name, shape, params, 100000,
+                                          lambda x, y, z: og.shape(0, OPS["contains"], x, y, z),
+                                          lambda *a: og.shape(0, OPS["dist_out"], *a))
     assert m > 300  # thin-walled shapes (polycone-steps) hold few of the sampled points
     for op in range(6):
         got = np.zeros_like(X)
@@ -407,6 +326,7 @@ def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda)
         ref = og.shape(0, op, X, Y, Z, DX, DY, DZ)
         assert np.array_equal(got, ref), (op, int(np.sum(got != ref)))
     # the surface band really is exercised
+    sx, sy, sz = X[-m:], Y[-m:], Z[-m:]
     ins = og.shape(0, OPS["inside"], sx, sy, sz)
     assert np.mean(ins == 2.0) > 0.5
 
