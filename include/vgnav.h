@@ -124,7 +124,8 @@ int vgn_compute_step_batch(const vgn_geometry *geom, int64_t n, const double *px
                            const vgn_state *in, vgn_state *out, double *step, double *safety, int flags,
                            void *stream);
 
-/* Alias with the name the spec API uses for the same operation. */
+/* The same operation under the name of its result, the next volume
+ * ("ComputeStepAndNextVolume"): out->nav_ind is the volume the track enters. */
 int vgn_step_and_next_volume(const vgn_geometry *geom, int64_t n, const double *px, const double *py,
                              const double *pz, const double *dx, const double *dy, const double *dz,
                              const double *step_limit, const vgn_state *in, vgn_state *out, double *step,
@@ -152,10 +153,12 @@ int vgn_shape_batch(const vgn_geometry *geom, int32_t lv, int32_t op, int64_t n,
  * VGN_PRECISION_MIXED): `variant` picks the threads-per-block / register-cap
  * variant, `sort_kbits` (0..6) bins tracks by direction octant and a
  * 2^k-per-axis cell of the world box before the step, for warp coherence
- * (0 = no binning).  Only performance changes, never a result.  Binning uses
- * a per-geometry device scratch (12 bytes per track plus the histogram):
- * binned calls on different streams must not overlap.  No counterpart in the
- * reference, which launches 256 threads per block (backend/cuda/Backend.h:50-96). */
+ * (0 = no binning).  Only performance changes, never a result.  Binning takes
+ * its scratch (about 12 bytes per track plus the histogram) from a stream-ordered
+ * memory pool the library keeps per device, so calls on different streams or
+ * threads may overlap, on one geometry too; the pool keeps its blocks for reuse
+ * until the process exits.  No counterpart in the reference, which launches 256
+ * threads per block (backend/cuda/Backend.h:50-96). */
 int vgn_set_step_config(vgn_geometry *geom, int flags, int32_t variant, int32_t sort_kbits);
 int vgn_get_step_config(const vgn_geometry *geom, int flags, int32_t *variant, int32_t *sort_kbits);
 /* Staging of step calls made with host buffers: the batch is split into `chunks`
@@ -171,7 +174,7 @@ int vgn_get_staging_chunks(const vgn_geometry *geom, int32_t *chunks);
  * position alone into 2^kbits cells per axis of the world box, 1..6 (the safety does
  * not depend on the direction, so the octant split of the step's order only scatters
  * neighbours); 0 = the safety pass follows the step's order.  Only performance
- * changes, never a result; shares the per-geometry binning scratch. */
+ * changes, never a result; its scratch comes with the step's (one pool allocation per call). */
 int vgn_set_safety_binning(vgn_geometry *geom, int flags, int32_t kbits);
 int vgn_get_safety_binning(const vgn_geometry *geom, int flags, int32_t *kbits);
 /* Autotuner: times every (variant, sort_kbits) pair on the given batch (device
@@ -254,6 +257,17 @@ int vgn_compute_step_batch_static(const vgn_geometry *geom, int64_t n, const dou
                                   const double *pz, const double *dx, const double *dy, const double *dz,
                                   const double *step_limit, const vgn_state *in, vgn_state *out, double *step,
                                   double *safety, int flags, int32_t sort_kbits, void *stream);
+
+/* Bounds of the device loops, for exercising their error paths: BVH traversal stack
+ * entries (2..32; the reference's BVH_MAX_DEPTH, BVH.h:33, is 32) and relocation levels
+ * (1..30).  A traversal that needs more stack, or a relocation that descends more levels,
+ * stops and records VGN_ERR_STACK / VGN_ERR_RELOCATE, which the call (host buffers) or
+ * vgn_synchronize (device buffers) returns; no fault, the context stays usable.  Lower
+ * bounds than the defaults change results, so they are for tests only; the defaults
+ * (32, 30) never bind on a geometry the library accepts.  Applies to later calls on the
+ * geometry (a vgn_batch keeps the bounds its jobs were set with).  No counterpart in the
+ * reference, whose loops are unbounded or assert. */
+int vgn_set_device_limits(vgn_geometry *geom, int32_t stack_entries, int32_t levels);
 
 /* Wait for the work of the previous calls on `stream`; returns the first
  * device-side error status recorded by a kernel since the last call. */

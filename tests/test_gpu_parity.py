@@ -420,3 +420,88 @@ def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed, 
     geo.walk(pts2, dirs, to_dev(torch, t.step_limit), st2, nsteps, max_steps=1, mixed=mixed)
     geo.synchronize()
     assert np.all(nsteps.cpu().numpy() == np.where(t.states["nav_ind"] != 0, 1, 0))
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_binned_calls_on_two_streams(oracle, vgnav, cuda, mixed):
+    """Binned steps with safeties on two streams of one geometry, enqueued back to back so
+    that they overlap on the device: each equals the oracle (their binning scratch is their own)."""
+    torch = cuda
+    grid = W.box_grid_geometry()
+    og = oracle.OracleGeometry(grid.desc)
+    geo = vgnav.Geometry(grid.desc)
+    geo.set_step_config(5, 5, mixed=mixed)
+    geo.set_safety_binning(4, mixed=mixed)
+    batches = [W.box_grid_tracks(grid, n=n, seed_points=sp, seed_dirs=sp + 1)
+               for n, sp in ((300001, 91), (200003, 93))]
+    refs = [og.step(t, calcsafety=True) for t in batches]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    bufs = []
+    for t, s in zip(batches, streams):
+        with torch.cuda.stream(s):
+            pts = vgnav.SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+            dirs = vgnav.SOA3D(to_dev(torch, t.dx), to_dev(torch, t.dy), to_dev(torch, t.dz))
+            inp = vgnav.NavStatePool(states_to_dev(torch, t.states))
+            bufs.append((pts, dirs, to_dev(torch, t.step_limit), inp, vgnav.NavStatePool.empty_like(inp),
+                         torch.empty(t.n, dtype=torch.float64, device="cuda"),
+                         torch.empty(t.n, dtype=torch.float64, device="cuda")))
+    torch.cuda.synchronize()
+    for rep in range(3):
+        for b, s in zip(bufs, streams):
+            geo.step(*b, mixed=mixed, stream=s)
+        torch.cuda.synchronize()
+        for b, ref in zip(bufs, refs):
+            assert np.array_equal(b[5].cpu().numpy(), ref["step"]), rep
+            assert np.array_equal(b[6].cpu().numpy(), ref["safety"]), rep
+            assert np.array_equal(b[4].to_numpy(), ref["out"]), rep
+    geo.synchronize()
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_device_limits_report_errors(oracle, vgnav, cuda, mixed):
+    """A traversal stack or a relocation depth that runs out stops the kernel's loop and
+    comes back as VGN_ERR_STACK / VGN_ERR_RELOCATE (host-buffer calls and vgn_synchronize);
+    the context stays usable and later calls are bit-exact again."""
+    torch = cuda
+    desc = W.nested_geometry()
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    t = W.uniform_tracks(4096, 480.0, 55, 56)
+    ref_loc = og.locate(t.x, t.y, t.z)
+    t.states = ref_loc
+    # relocation levels: locating points three levels down needs more than one
+    geo.set_device_limits(32, 1)
+    st = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    with pytest.raises(N.VgnError) as e:
+        geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st), mixed=mixed)
+    assert e.value.code == N.VGN_ERR_RELOCATE
+    # traversal stack: the 27-mother world BVH needs more than two entries
+    geo.set_device_limits(2, 30)
+    out = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    with pytest.raises(N.VgnError) as e:
+        geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit,
+                 vgnav.NavStatePool(t.states), vgnav.NavStatePool(out), np.zeros(t.n), np.zeros(t.n), mixed=mixed)
+    assert e.value.code == N.VGN_ERR_STACK
+    # device-pointer calls: the status comes back from synchronize
+    pts = vgnav.SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+    dirs = vgnav.SOA3D(to_dev(torch, t.dx), to_dev(torch, t.dy), to_dev(torch, t.dz))
+    inp = vgnav.NavStatePool(states_to_dev(torch, t.states))
+    outp = vgnav.NavStatePool.empty_like(inp)
+    steps = torch.empty(t.n, dtype=torch.float64, device="cuda")
+    geo.step(pts, dirs, to_dev(torch, t.step_limit), inp, outp, steps, mixed=mixed)
+    with pytest.raises(N.VgnError) as e:
+        geo.synchronize()
+    assert e.value.code == N.VGN_ERR_STACK
+    with pytest.raises(N.VgnError):
+        geo.set_device_limits(1, 30)
+    with pytest.raises(N.VgnError):
+        geo.set_device_limits(33, 30)
+    # defaults back: everything bit-exact, status clean
+    geo.set_device_limits()
+    st = np.zeros(t.n, dtype=W.STATE_DTYPE)
+    geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st), mixed=mixed)
+    assert np.array_equal(st, ref_loc)
+    got = gpu_step(torch, geo, t, mixed=mixed)
+    ref = og.step(t)
+    assert np.array_equal(got["step"], ref["step"]) and np.array_equal(got["safety"], ref["safety"])
+    assert np.array_equal(got["out"], ref["out"])

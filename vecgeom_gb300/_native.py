@@ -56,6 +56,7 @@ EXPORTED = [
     "vgn_batch_step",
     "vgn_batch_synchronize",
     "vgn_batch_autotune",
+    "vgn_set_device_limits",
     "vgn_synchronize",
     "vgn_last_error",
     "vgn_version",
@@ -137,6 +138,7 @@ def lib() -> C.CDLL:
         L.vgn_batch_step.argtypes = [vp, vp]
         L.vgn_batch_synchronize.argtypes = [vp, vp]
         L.vgn_batch_autotune.argtypes = [vp, vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)]
+        L.vgn_set_device_limits.argtypes = [vp, i32, i32]
         L.vgn_synchronize.argtypes = [vp, vp]
         L.vgn_last_error.restype = C.c_char_p
         L.vgn_version.restype = C.c_char_p

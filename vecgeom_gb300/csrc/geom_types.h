@@ -209,6 +209,10 @@ struct GeomView {
   int32_t world_pv;
   int32_t max_depth;
   uint32_t *status;  // device error word (DevError bits)
+  // bounds of the device loops: traversal stack entries (<= kStackSize) and relocation
+  // levels (<= kMaxLevels); lowered only to exercise the error paths (vgn_set_device_limits)
+  int32_t stack_limit;
+  int32_t level_limit;
 };
 
 }  // namespace vgn

@@ -7,6 +7,10 @@
 // form uses explicitly rounded intrinsics, which are never contracted.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "../../include/vgnav.h"
 #include "launch.h"
 #include "nav_step.cuh"
@@ -264,6 +268,32 @@ __global__ void __launch_bounds__(256) shape_kernel_fp64(int type, const double 
 
 namespace VGN_KSET {
 
+// dynamic shared memory of the step-path kernels (traversal stacks and candidate queues)
+static constexpr size_t step_smem_bytes(int block) { return (size_t)dev::kStepSmemWords * block * sizeof(uint32_t); }
+static constexpr size_t locate_smem_bytes(int block)
+{
+  return VGN_SMEM_STACK ? (size_t)kStackSize * block * sizeof(uint32_t) : 0;
+}
+
+// Opt a kernel in to more than 48 KiB of dynamic shared memory, once per (kernel, device).
+template <typename Kernel>
+static cudaError_t allow_smem(Kernel kernel, size_t bytes)
+{
+  static std::mutex m;
+  static std::vector<std::pair<const void *, int>> done;
+  if (bytes <= 48u * 1024u) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const auto key = std::make_pair(reinterpret_cast<const void *>(kernel), dev);
+  std::lock_guard<std::mutex> lock(m);
+  for (const auto &k : done)
+    if (k == key) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done.push_back(key);
+  return e;
+}
+
 static inline unsigned grid_for(int64_t n, int block, int max_blocks)
 {
   int64_t b = (n + block - 1) / block;
@@ -287,8 +317,9 @@ static void launch_step_v(const GeomView &g, const StepArgs &a, cudaStream_t s)
 {
   // grid-stride over tracks; enough blocks to fill every SM several times over
   const unsigned grid = grid_for(a.n, BLOCK, a.max_blocks * (256 / BLOCK));
-  dev::step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, 0, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit,
-                                                              a.in, a.out, a.step, a.reloc, a.perm);
+  if (allow_smem(dev::step_kernel<MIXED, BLOCK, MINB>, step_smem_bytes(BLOCK)) != cudaSuccess) return;
+  dev::step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, step_smem_bytes(BLOCK), s>>>(
+      g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit, a.in, a.out, a.step, a.reloc, a.perm);
 }
 
 template <bool MIXED>
@@ -335,7 +366,8 @@ static void launch_multi_v(const JobTable &jt, uint32_t *queue, int reloc, int n
 {
   // persistent: as many blocks as the variant keeps resident on every SM
   const unsigned grid = (unsigned)(num_sms * MINB);
-  dev::multi_step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, 0, s>>>(jt, queue, reloc);
+  if (allow_smem(dev::multi_step_kernel<MIXED, BLOCK, MINB>, step_smem_bytes(BLOCK)) != cudaSuccess) return;
+  dev::multi_step_kernel<MIXED, BLOCK, MINB><<<grid, BLOCK, step_smem_bytes(BLOCK), s>>>(jt, queue, reloc);
 }
 
 template <bool MIXED>
@@ -378,12 +410,13 @@ cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, do
 {
   const int block     = 128;
   const unsigned grid = grid_for(n, block, max_blocks * 2);
+  const size_t smem   = step_smem_bytes(block);
   if (mixed)
-    dev::walk_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps,
-                                                  perm);
+    dev::walk_kernel<true><<<grid, block, smem, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps,
+                                                     perm);
   else
-    dev::walk_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps,
-                                                   perm);
+    dev::walk_kernel<false><<<grid, block, smem, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps,
+                                                      nsteps, perm);
   return cudaGetLastError();
 }
 
@@ -404,9 +437,9 @@ cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const 
   const int block     = 256;
   const unsigned grid = grid_for(n, block, max_blocks);
   if (mixed)
-    dev::locate_kernel<true><<<grid, block, 0, s>>>(g, n, px, py, pz, out);
+    dev::locate_kernel<true><<<grid, block, locate_smem_bytes(block), s>>>(g, n, px, py, pz, out);
   else
-    dev::locate_kernel<false><<<grid, block, 0, s>>>(g, n, px, py, pz, out);
+    dev::locate_kernel<false><<<grid, block, locate_smem_bytes(block), s>>>(g, n, px, py, pz, out);
   return cudaGetLastError();
 }
 

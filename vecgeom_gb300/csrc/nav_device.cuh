@@ -197,11 +197,40 @@ __device__ __forceinline__ bool box_contains_pt(const double *mn, const double *
          p.z >= __ldg(mn + 2) && p.z <= __ldg(mx + 2);
 }
 
+// A per-thread array in shared memory, strided by the block size: element i of thread t at
+// base[i * stride + t], so the threads of a warp touch consecutive banks.
+template <typename T>
+struct SArr {
+  T *p;
+  int stride;
+  __device__ __forceinline__ T &operator[](int i) const { return p[i * stride]; }
+};
+
+// Traversal scratch of the kernels on the step path (step, multi-job step, walk, locate):
+// the BVH stack of the step's traversal, of the relocation's level locate and of point
+// location (used one after the other, never nested), then the mixed traversal's candidate
+// queue (pv, box-entry lower bound).  It lives in dynamic shared memory, kStepSmemWords words
+// per thread strided by the block size, instead of a local-memory stack frame: the frame's
+// spills went through L1 to DRAM.  VGN_SMEM_STACK=0 keeps the stacks in local memory.
+#ifndef VGN_SMEM_STACK
+#define VGN_SMEM_STACK 1
+#endif
+constexpr int kMaxStepCand   = 16;
+constexpr int kStepSmemWords = VGN_SMEM_STACK ? kStackSize + 2 * kMaxStepCand : 0;
+extern __shared__ uint32_t vgn_step_smem[];
+
+#if VGN_SMEM_STACK
+#define VGN_TRAVERSAL_STACK(name) \
+  const SArr<unsigned> name { vgn_step_smem + threadIdx.x, (int)blockDim.x }
+#else
+#define VGN_TRAVERSAL_STACK(name) unsigned name[kStackSize]
+#endif
+
 // BVH::CheckDaughterIntersections (BVH.h:96-146), FP64
 __device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVRec &lv, D3 lp, D3 ld, double &step,
                                                     int last, int &hit)
 {
-  unsigned stack[kStackSize];
+  VGN_TRAVERSAL_STACK(stack);
   int sp        = 1;
   stack[0]      = 0;
   const D3 inv  = d3(1.0 / nonzero(ld.x), 1.0 / nonzero(ld.y), 1.0 / nonzero(ld.z));
@@ -229,7 +258,7 @@ __device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVR
       slab(nodes[R].mn, nodes[R].mx, lp, inv, tminR, tmaxR);
       const bool trL = tminL <= tmaxL && tmaxL >= 0.0 && tminL < step;
       const bool trR = tminR <= tmaxR && tmaxR >= 0.0 && tminR < step;
-      if (sp + 2 > kStackSize) {
+      if (sp + 2 > g.stack_limit) {
         raise_error(g, kErrStack);
         return false;
       }
@@ -270,7 +299,7 @@ __device__ __forceinline__ double bvh_safety(const GeomView &g, const LVRec &lv,
       const double sL = box_safety(nodes[L].mn, nodes[L].mx, lp);
       const double sR = box_safety(nodes[R].mn, nodes[R].mx, lp);
       const bool trL = sL < safety, trR = sR < safety;
-      if (sp + 2 > kStackSize) {
+      if (sp + 2 > g.stack_limit) {
         raise_error(g, kErrStack);
         return safety;
       }
@@ -290,7 +319,7 @@ __device__ __forceinline__ double bvh_safety(const GeomView &g, const LVRec &lv,
 __device__ __forceinline__ bool bvh_level_locate(const GeomView &g, const LVRec &lv, int excl, D3 lp, int &pvol,
                                                  D3 &dlp)
 {
-  unsigned stack[kStackSize];
+  VGN_TRAVERSAL_STACK(stack);
   int sp   = 1;
   stack[0] = 0;
   const NodeRec *nodes = g.nodes + lv.nodes_off;
@@ -312,7 +341,7 @@ __device__ __forceinline__ bool bvh_level_locate(const GeomView &g, const LVRec 
       }
     } else {
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
-      if (sp + 2 > kStackSize) {
+      if (sp + 2 > g.stack_limit) {
         raise_error(g, kErrStack);
         return false;
       }

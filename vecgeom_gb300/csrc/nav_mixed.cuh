@@ -378,22 +378,17 @@ __device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm
   return false;
 }
 
-// A per-thread array in shared memory, strided by the block size: element i of thread t at
-// base[i * stride + t], so the threads of a warp touch consecutive banks.
-template <typename T>
-struct SArr {
-  T *p;
-  int stride;
-  __device__ __forceinline__ T &operator[](int i) const { return p[i * stride]; }
-};
-
 // ------------------------------------------------------------------ step
-constexpr int kMaxStepCand = 16;
-
+// candidate queue of one track, in visit order (a ring of kMaxStepCand entries)
 struct StepCands {
   int n, head;
+#if VGN_SMEM_STACK
+  SArr<int> pv;
+  SArr<float> tmin_lo;
+#else
   int pv[kMaxStepCand];
   float tmin_lo[kMaxStepCand];
+#endif
 };
 
 // Acceptance of one candidate, as in BVH.h:113-118; a candidate whose box is
@@ -415,7 +410,7 @@ __device__ __forceinline__ void eval_step_candidate(const GeomView &g, const Mix
 __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, const LVRec &lv, MixedRay &r,
                                                           double &step, int last, int &hit)
 {
-  unsigned stack[kStackSize];
+  VGN_TRAVERSAL_STACK(stack);
   int sp   = 1;
   stack[0] = 0;
   FI stepI = fi(step);
@@ -423,6 +418,11 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
   // the step the FP64 traversal would hold at the same point.
   StepCands c;
   c.n = c.head = 0;
+#if VGN_SMEM_STACK
+  c.pv      = SArr<int>{reinterpret_cast<int *>(vgn_step_smem + kStackSize * blockDim.x + threadIdx.x), (int)blockDim.x};
+  c.tmin_lo = SArr<float>{reinterpret_cast<float *>(vgn_step_smem + (kStackSize + kMaxStepCand) * blockDim.x + threadIdx.x),
+                          (int)blockDim.x};
+#endif
   const INodeSlab *inodes = g.inodes + lv.nodes_off;
   const IPrimSlab *iprims = g.iprims + lv.prims_off;
   const NodeRec *nodes    = g.nodes + lv.nodes_off;
@@ -465,7 +465,7 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
           rfirst = cc < a ? kYes : kNo;
         }
       }
-      if (sp + 2 > kStackSize) {
+      if (sp + 2 > g.stack_limit) {
         raise_error(g, kErrStack);
         ok = false;
         break;
@@ -612,7 +612,7 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
         rfirst = o == kMaybe ? box_safety(nodes[R].mn, nodes[R].mx, r.lp) < box_safety(nodes[L].mn, nodes[L].mx, r.lp)
                              : o == kYes;
       }
-      if (sp + 2 > kStackSize) {
+      if (sp + 2 > g.stack_limit) {
         raise_error(g, kErrStack);
         break;
       }
@@ -650,7 +650,7 @@ __device__ __forceinline__ int icontains(const float *mn_lo, const float *mn_hi,
 __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const LVRec &lv, int excl, D3 lp,
                                                        int &pvol, D3 &dlp)
 {
-  unsigned stack[kStackSize];
+  VGN_TRAVERSAL_STACK(stack);
   int sp   = 1;
   stack[0] = 0;
   const FI p[3] = {fi(lp.x), fi(lp.y), fi(lp.z)};
@@ -680,7 +680,7 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
       }
     } else {
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
-      if (sp + 2 > kStackSize) {
+      if (sp + 2 > g.stack_limit) {
         raise_error(g, kErrStack);
         return false;
       }

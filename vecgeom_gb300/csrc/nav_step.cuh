@@ -30,7 +30,7 @@ __device__ __forceinline__ int locate_global_point(const GeomView &g, int vol, D
     bool godeeper = true;
     int guard     = 0;
     while (lv.nd > 0 && godeeper) {
-      if (++guard > kMaxLevels) {
+      if (++guard > g.level_limit) {
         raise_error(g, kErrRelocate);
         break;
       }
@@ -60,7 +60,7 @@ __device__ __forceinline__ void locate_global_point_excl(const GeomView &g, int 
   bool godeeper = true;
   int guard     = 0;
   while (lv.nd > 0 && godeeper) {
-    if (++guard > kMaxLevels) {
+    if (++guard > g.level_limit) {
       raise_error(g, kErrRelocate);
       break;
     }
@@ -84,7 +84,7 @@ __device__ __forceinline__ void relocate_force_different(const GeomView &g, D3 l
   D3 tmp    = lp;
   int guard = 0;
   while (cm >= 0) {
-    if (++guard > kMaxLevels + 1) {
+    if (++guard > g.level_limit + 1) {
       raise_error(g, kErrRelocate);
       return;
     }

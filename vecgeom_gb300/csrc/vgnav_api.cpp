@@ -37,10 +37,6 @@ struct vgn_geometry {
   // axis (0 = the step's order)
   int safety_kbits[2] = {0, 0};
   vgn::BinParams bin{};
-  // track-binning scratch (keys, histogram, permutation), grown on demand
-  std::mutex sort_mutex;
-  uint32_t *d_sort  = nullptr;
-  size_t sort_words = 0;
   // pipelined staging of host-buffer steps: pieces alternate between two internal streams,
   // each with its own half of the staging workspace and of `d_pipe_sort`
   int staging_chunks      = 0;  // 0 = automatic
@@ -157,6 +153,37 @@ void *workspace(vgn_geometry *g, size_t bytes)
 
 int max_blocks(const vgn_geometry *g) { return g->num_sms > 0 ? g->num_sms * 32 : 4096; }
 
+// Per-call device scratch (track binning) comes from a stream-ordered memory pool that the
+// library creates once per device: an allocation belongs to the stream of the call that made
+// it and is released in that stream's order, so calls on different streams (or threads) never
+// share scratch.  The pool keeps released blocks (release threshold = no limit), so steady
+// calls of one size allocate nothing new; the blocks stay with the process until it exits.
+cudaError_t pool_alloc(int device, size_t bytes, cudaStream_t s, void **p)
+{
+  static std::mutex m;
+  static std::vector<cudaMemPool_t> pools;
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(m);
+    if ((int)pools.size() <= device) pools.resize((size_t)device + 1, nullptr);
+    if (!pools[(size_t)device]) {
+      cudaMemPoolProps props{};
+      props.allocType     = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id   = device;
+      cudaError_t e       = cudaMemPoolCreate(&pools[(size_t)device], &props);
+      if (e != cudaSuccess) {
+        pools[(size_t)device] = nullptr;
+        return e;
+      }
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pools[(size_t)device], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool = pools[(size_t)device];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
 // Enqueue one step batch with the geometry's launch configuration: optional
 // track binning (counting sort into a visit permutation), then the step kernel.
 // `scratch` (bin_scratch_words(n, kbits) + n words) replaces the geometry's shared
@@ -178,43 +205,37 @@ int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s, u
   } else if (a.n <= (int64_t)UINT32_MAX) {  // the visit permutations hold 32-bit track indices
     const int ks = a.safety ? g->safety_kbits[m] : 0;
     if (kbits > 0 || ks > 0) {
-      std::lock_guard<std::mutex> lock(g->sort_mutex);
-      // keys and histogram (reused by the two binnings in stream order), then the orders
+      // keys and histogram (reused by the two binnings in stream order), then the orders;
+      // stream-ordered scratch of this call alone, so calls on other streams never share it
       size_t head = kbits > 0 ? vgn::bin_scratch_words(a.n, kbits) : 0;
       if (ks > 0 && vgn::bin_scratch_words(a.n, ks) > head) head = vgn::bin_scratch_words(a.n, ks);
       const size_t need = head + (size_t)a.n * ((kbits > 0 ? 1 : 0) + (ks > 0 ? 1 : 0));
-      if (need > g->sort_words) {
-        if (g->d_sort) cudaFree(g->d_sort);
-        g->d_sort     = nullptr;
-        g->sort_words = 0;
-        if (cudaMalloc(&g->d_sort, need * sizeof(uint32_t)) != cudaSuccess) {
-          cudaGetLastError();
-          g->d_sort = nullptr;
-          return fail(VGN_ERR_NOMEM, "track-binning scratch allocation failed");
-        }
-        g->sort_words = need;
+      uint32_t *buf = nullptr;
+      if (pool_alloc(g->device, need * sizeof(uint32_t), s, reinterpret_cast<void **>(&buf)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VGN_ERR_NOMEM, "track-binning scratch allocation failed");
       }
-      uint32_t *next = g->d_sort + head;
+      uint32_t *next = buf + head;
+      cudaError_t e  = cudaSuccess;
       if (kbits > 0) {  // the step's order: direction octant, then position
         vgn::BinParams b = g->bin;
         b.kbits          = kbits;
         for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
-        cudaError_t e = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, g->d_sort, next,
-                                               max_blocks(g), s);
-        if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+        e      = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, buf, next, max_blocks(g), s);
         a.perm = next;
         next += a.n;
       }
-      if (ks > 0) {  // the safety pass's order: position alone
+      if (e == cudaSuccess && ks > 0) {  // the safety pass's order: position alone
         vgn::BinParams b = g->bin;
         b.kbits          = ks;
         b.octants        = 0;
         for (int k = 0; k < 3; ++k) b.scale[k] = g->bin.scale[k] * (float)(1 << ks);
-        cudaError_t e = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, g->d_sort, next,
-                                               max_blocks(g), s);
-        if (e != cudaSuccess) return cuda_fail(e, "track binning launch");
+        e             = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, buf, next, max_blocks(g), s);
         a.perm_safety = next;
       }
+      if (e == cudaSuccess) e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[m], s);
+      cudaFreeAsync(buf, s);
+      return e == cudaSuccess ? VGN_OK : cuda_fail(e, "binned step launch");
     }
   }
   cudaError_t e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[m], s);
@@ -302,6 +323,8 @@ int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry 
   v.n_lv         = (int32_t)h.lv.size();
   v.world_pv     = h.world_pv;
   v.max_depth    = h.max_depth;
+  v.stack_limit  = vgn::kStackSize;
+  v.level_limit  = vgn::kMaxLevels;
   {  // world bounding box for track binning
     const vgn::HostLV &wl = h.lv[h.pv[h.world_pv].lv];
     vgn::Vec3 mn, mx;
@@ -329,7 +352,6 @@ int vgn_geometry_free(vgn_geometry *g)
     for (void *p : g->allocations) cudaFree(p);
     if (g->d_status) cudaFree(g->d_status);
     if (g->d_ws) cudaFree(g->d_ws);
-    if (g->d_sort) cudaFree(g->d_sort);
     if (g->d_pipe_sort) cudaFree(g->d_pipe_sort);
     for (cudaStream_t ps : g->pipe)
       if (ps) cudaStreamDestroy(ps);
@@ -791,13 +813,13 @@ int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, dou
   const bool mixed = (flags & VGN_PRECISION_MIXED) != 0;
   cudaStream_t s   = static_cast<cudaStream_t>(stream);
   // tracks binned like the step's (direction octant, then cell) when the geometry bins its
-  // steps; the scratch is stream-ordered (cudaMallocAsync), so walks on several streams of
-  // one geometry do not share it
+  // steps; the scratch is stream-ordered (pool_alloc), so walks on several streams of one
+  // geometry do not share it
   const int kbits  = g->sort_kbits[mixed ? 1 : 0];
   uint32_t *sort   = nullptr, *perm = nullptr;
   if (kbits > 0 && n <= (int64_t)UINT32_MAX) {
     const size_t words = vgn::bin_scratch_words(n, kbits) + (size_t)n;
-    if (cudaMallocAsync(reinterpret_cast<void **>(&sort), words * sizeof(uint32_t), s) != cudaSuccess) {
+    if (pool_alloc(g->device, words * sizeof(uint32_t), s, reinterpret_cast<void **>(&sort)) != cudaSuccess) {
       cudaGetLastError();
       return fail(VGN_ERR_NOMEM, "walk binning scratch allocation failed");
     }
@@ -1119,6 +1141,16 @@ int vgn_compute_step_batch_static(const vgn_geometry *g, int64_t n, const double
   a.perm       = perm;
   e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[mixed ? 1 : 0], s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
+}
+
+int vgn_set_device_limits(vgn_geometry *g, int32_t stack_entries, int32_t levels)
+{
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (stack_entries < 2 || stack_entries > vgn::kStackSize || levels < 1 || levels > vgn::kMaxLevels)
+    return fail(VGN_ERR_ARG, "device limits out of range (stack 2..32, levels 1..30)");
+  g->view.stack_limit = stack_entries;
+  g->view.level_limit = levels;
+  return VGN_OK;
 }
 
 int vgn_synchronize(const vgn_geometry *g, void *stream)

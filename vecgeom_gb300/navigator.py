@@ -226,6 +226,10 @@ class Geometry:
     def synchronize(self, stream=None):
         N.check(N.lib().vgn_synchronize(self.handle, _stream_ptr(stream)))
 
+    def set_device_limits(self, stack_entries: int = 32, levels: int = 30):
+        """Bounds of the device loops (defaults 32, 30); lower ones exercise the error paths."""
+        N.check(N.lib().vgn_set_device_limits(self.handle, stack_entries, levels))
+
 
 class BVHNavigator:
     """Batched navigator with VecGeom's method names (VNavigator.h:878-975)."""
