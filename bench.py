@@ -15,8 +15,11 @@ peaks, and the CPU baseline.  Synthetic data with the stated seeds.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line (rank 0).  --impl reference times the CPU
-implementation of the same path (the oracle restatement: the reference
-itself cannot be built here) on all host cores.
+implementation of the same path on all host cores: the oracle, a C
+restatement of the reference's scalar BVHNavigator path that the tests pin
+bit for bit to the reference's own sources (compiled where the reference tree
+is present; this machine runs the restatement).  The line also carries the
+single-Tube shape-kernel workload (2^20 points) and a single-core CPU rate.
 """
 from __future__ import annotations
 
@@ -140,14 +143,14 @@ def make_workload(n_tracks: int = N_TRACKS):
     return grid, t
 
 
-def cpu_sample_rate(grid, t, min_seconds: float, threads: int = 0):
+def cpu_sample_rate(grid, t, min_seconds: float, threads: int = 0, n: int = 1 << 20):
     """Oracle (CPU restatement of the reference) steps/s on host cores, over repeated passes
-    of a 2^20-track sample until `min_seconds` of work is done."""
+    of an `n`-track sample until `min_seconds` of work is done."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import pyoracle
 
     og = pyoracle.OracleGeometry(grid.desc)
-    sample = t.head(1 << 20)
+    sample = t.head(n)
     og.step(sample.head(1 << 14), calcsafety=True, nthreads=threads)  # warm caches
     done, passes, t0 = 0, 0, pyoracle.now()
     while True:
@@ -158,7 +161,7 @@ def cpu_sample_rate(grid, t, min_seconds: float, threads: int = 0):
         if el >= min_seconds:
             break
     cores = threads if threads > 0 else pyoracle.ncores()
-    return done / el, cores, f"{passes} passes x 2^20 tracks of the same workload ({el:.1f} s)"
+    return done / el, cores, f"{passes} passes x {n} tracks of the same workload ({el:.1f} s, {cores} threads)"
 
 
 def run_reference(args, ws, rank):
@@ -180,6 +183,7 @@ def run_reference(args, ws, rank):
     total = sum(times)
     value = sample.n * args.steps / total
     cores = pyoracle.ncores()
+    r1, _, s1 = cpu_sample_rate(grid, t, min_seconds=2.0, threads=1, n=1 << 18)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
@@ -187,7 +191,9 @@ def run_reference(args, ws, rank):
         "config": {"workload": WORKLOAD, "tracks_per_step": sample.n, "daughters": 4096},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"2^20 tracks of the 2^22-track workload per step, {args.steps} steps; "
-                                   "CPU restatement of VecGeom's BVHNavigator (reference not buildable here)"},
+                                   "CPU restatement of VecGeom's BVHNavigator, bit-exact with it (the "
+                                   "reference's own sources are not on this machine)",
+                         "single_core": {"value": r1, "unit": UNIT, "cores": 1, "sample": s1}},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -235,7 +241,7 @@ def time_steps(torch, geo, args_tuple, mixed, steps, warmup, stream):
     return [a.elapsed_time(b) for a, b in evs], evs[0][0].elapsed_time(evs[-1][1])
 
 
-def run_mixed_shapes(torch, V, local, steps, warmup, n_tracks, stream) -> dict:
+def run_mixed_shapes(torch, V, local, steps, warmup, n_tracks, stream, fixed=None) -> dict:
     """Mixed-shape workload: 8192 daughters (Box, Tube, Cone, Trd, Trapezoid, Sphere, 4-plane
     Polycone; lengths U[5,60] mm, full rotations) in a 2 m world; tracks uniform in the world,
     located on the GPU, then stepped in both precision forms.  Reports steps/s of each form
@@ -259,12 +265,17 @@ def run_mixed_shapes(torch, V, local, steps, warmup, n_tracks, stream) -> dict:
         out = V.NavStatePool.empty_like(inp)
         stp = torch.empty(t.n, dtype=torch.float64, device="cuda")
         saf = torch.empty(t.n, dtype=torch.float64, device="cuda")
-        k = min(t.n, 1 << 21)  # autotune on a 2^21-track prefix
-        sub = lambda a: a[:k]
-        v, kb, _ = geo.autotune_step(V.SOA3D(sub(pts.x), sub(pts.y), sub(pts.z)),
-                                     V.SOA3D(sub(dirs.x), sub(dirs.y), sub(dirs.z)), sub(sl),
-                                     V.NavStatePool(inp.data[:k]), V.NavStatePool(out.data[:k]), sub(stp), sub(saf),
-                                     mixed=mixed, stream=stream)
+        if fixed:  # profiling runs: a given launch configuration, no tuning launches
+            v, kb, ks = fixed
+            geo.set_step_config(v, kb, mixed=mixed)
+            geo.set_safety_binning(ks, mixed=mixed)
+        else:
+            k = min(t.n, 1 << 21)  # autotune on a 2^21-track prefix
+            sub = lambda a: a[:k]
+            v, kb, _ = geo.autotune_step(V.SOA3D(sub(pts.x), sub(pts.y), sub(pts.z)),
+                                         V.SOA3D(sub(dirs.x), sub(dirs.y), sub(dirs.z)), sub(sl),
+                                         V.NavStatePool(inp.data[:k]), V.NavStatePool(out.data[:k]), sub(stp),
+                                         sub(saf), mixed=mixed, stream=stream)
         per, total = time_steps(torch, geo, (pts, dirs, sl, inp, out, stp, saf), mixed, steps, warmup, stream)
         res["mixed" if mixed else "fp64"] = {
             "value": t.n * steps / (total * 1e-3), "unit": UNIT, "ms_per_step": total / steps,
@@ -282,6 +293,69 @@ def run_mixed_shapes(torch, V, local, steps, warmup, n_tracks, stream) -> dict:
     }
     res["workload"] = (f"mixed shapes: 8192 daughters (7 shape types, lengths U[5,60] mm, full rotations) in a "
                        f"2 m world, {t.n} tracks located in the world, ComputeStepAndNextVolume + ComputeSafety")
+    return res
+
+
+def run_tube_shape(torch, V, local, steps, warmup, stream, fp64_peak=None, cpu=True) -> dict:
+    """Single-shape workload: UnplacedTube(rmin 10, rmax 50, dz 100 mm, full phi), 2^20 points
+    uniform inside, isotropic directions; per point DistanceToOut and SafetyToOut with the FP64
+    shape kernels (the reference's scalar kernels restated, bit-exact).  Inputs (48 MB) fit in
+    L2, so L2 is flushed (a 512 MB write) before every timed iteration, outside its events."""
+    from vecgeom_gb300 import workloads as W
+
+    tp = W.tube_points()
+    geo = V.Geometry(W.tube_geometry(), device=local)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pts = V.SOA3D(dev(tp.x), dev(tp.y), dev(tp.z))
+    dirs = V.SOA3D(dev(tp.dx), dev(tp.dy), dev(tp.dz))
+    dout = torch.empty(tp.n, dtype=torch.float64, device="cuda")
+    sout = torch.empty(tp.n, dtype=torch.float64, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def one():
+        geo.shape(0, 1, pts, dirs, dout, stream=stream)  # VGN_OP_DISTANCE_TO_OUT
+        geo.shape(0, 3, pts, None, sout, stream=stream)  # VGN_OP_SAFETY_TO_OUT
+
+    for _ in range(max(warmup, 3)):
+        one()
+    torch.cuda.synchronize()
+    per = []
+    for _ in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        one()
+        b.record(stream)
+        torch.cuda.synchronize()
+        per.append(a.elapsed_time(b))
+    ms = statistics.mean(per)
+    value = tp.n / (ms * 1e-3)
+    ops = roofline_ops().get("kernel_weights", [[0] * 6, [0, 45, 0, 15, 0, 0]])[1]
+    ops_per_point = ops[1] + ops[3]
+    # algorithmic bytes: DistanceToOut reads p, d (48 B) and writes 8 B; SafetyToOut reads p
+    # (24 B) and writes 8 B
+    bytes_per_point = 48 + 8 + 24 + 8
+    res = {"workload": "Tube(rmin 10, rmax 50, dz 100 mm, full phi), 2^20 points inside, isotropic directions; "
+                       "DistanceToOut + SafetyToOut per point (FP64 shape kernels, bit-exact)",
+           "value": value, "unit": "points/s", "ms_per_batch": ms, "p50_ms": float(np.percentile(per, 50)),
+           "p99_ms": float(np.percentile(per, 99)), "l2": "flushed (512 MB write) before every timed batch",
+           "hbm": {"algorithmic_bytes_per_point": bytes_per_point,
+                   "achieved_gbs": bytes_per_point * value / 1e9},
+           "fp64": {"ops_per_point": ops_per_point, "achieved_tflops": ops_per_point * value / 1e12}}
+    if fp64_peak:
+        res["fp64"]["peak_tflops_measured"] = fp64_peak
+        res["fp64"]["frac_of_peak"] = ops_per_point * value / 1e12 / fp64_peak
+    if cpu:  # the oracle's scalar shape kernels on one host core, same points
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+
+        og = pyoracle.OracleGeometry(W.tube_geometry())
+        t0 = pyoracle.now()
+        og.shape(0, 1, tp.x, tp.y, tp.z, tp.dx, tp.dy, tp.dz)
+        og.shape(0, 3, tp.x, tp.y, tp.z)
+        el = pyoracle.now() - t0
+        res["cpu_port_single_core"] = {"value": tp.n / el, "unit": "points/s", "cores": 1, "kind": "port"}
     return res
 
 
@@ -366,32 +440,37 @@ def run_serving(torch, V, local, seconds: float, launch=None) -> dict:
     """Serving loop against the resident 8192-mixed-shape geometry: requests of log-uniform
     size in [256, 1M] tracks arrive as a Poisson process; each is copied in, located and
     stepped to the world exit on the device (states stay on the device), and its step counts
-    copied back.  Peak = a saturating burst of eight 1M-track requests; then offered loads of
-    25/50/90 % of that peak.  Latency = arrival to reply in host memory."""
+    and final states copied back.  Requests of up to 16k tracks run on high-priority streams
+    and are admitted first; larger ones are cut into 256k-track slices on normal streams;
+    admission by live device-memory headroom.  Peak = a saturating burst of eight 1M-track
+    requests; then offered loads of 25/50/90 % of that peak.  Latency = arrival to reply in
+    host memory, overall and per request-size bucket."""
     from vecgeom_gb300 import serving as S
     from vecgeom_gb300 import workloads as W
 
-    streams = 4
+    small_streams, large_streams, small_max, slice_tracks = 8, 4, 16384, 262144
     geo = V.Geometry(W.mixed_shape_geometry(), device=local)
     if launch:  # the mixed-shape workload's tuned configuration: the walks visit tracks in its binned order
         geo.set_step_config(launch["variant"], launch["sort_kbits"], mixed=True)
-    free, _ = torch.cuda.mem_get_info()
-    pool_bytes = int(min(free // 4, 16 << 30))
-    ex = S.GpuExecutor(geo, W.MIXED_WORLD, pool_bytes, streams, mixed=True)
-    pool = S.Pool(pool_bytes)
+    ex = S.GpuExecutor(geo, W.MIXED_WORLD, small_streams, large_streams, mixed=True)
+    serve = lambda reqs: S.serve(reqs, ex, small_streams, large_streams, small_max=small_max,
+                                 slice_tracks=slice_tracks)
     burst = lambda seed: [S.Request(arrival=0.0, rid=k, n=1 << 20, seed=seed + k) for k in range(8)]
-    S.serve(burst(100), ex, pool, streams)  # warm-up
-    peak = S.summarize(S.serve(burst(200), ex, pool, streams))
+    serve(burst(100))  # warm-up
+    peak = S.summarize(serve(burst(200)))
     steps_per_track = peak["steps"] / peak["tracks"]
     mean_n = S.mean_batch()
     out = {"workload": "resident 8192-mixed-shape geometry; Poisson requests, batch sizes log-uniform in "
                        "[256, 1M] tracks, each track stepped to the world exit (mixed form)",
-           "streams": streams, "pool_bytes": pool_bytes, "admission": "first-fit in a device pool of free HBM",
+           "streams": {"high_priority": small_streams, "normal": large_streams},
+           "small_max_tracks": small_max, "slice_tracks": slice_tracks,
+           "admission": "small requests first; pieces admitted while live device-memory headroom allows "
+                        "(free HBM + allocator cache - 2 GiB reserve)",
            "peak": {"steps_per_s": peak["steps_per_s"], "steps_per_track": steps_per_track}, "loads": {}}
     for frac in (0.25, 0.5, 0.9):
         rate = frac * peak["steps_per_s"] / (mean_n * steps_per_track)
         reqs = S.poisson_requests(rate, seconds, seed=int(frac * 100))
-        summ = S.summarize(S.serve(reqs, ex, pool, streams))
+        summ = S.summarize(serve(reqs))
         summ["offered_requests_per_s"] = rate
         summ["offered_steps_per_s"] = frac * peak["steps_per_s"]
         out["loads"][f"{int(frac * 100)}%"] = summ
@@ -411,6 +490,13 @@ def run_ours(args, ws, rank, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    if args.mixed_shapes_only:  # profiling runs: the 8192-mixed-shape leg alone, fixed launch configuration
+        fixed = tuple(int(x) for x in (args.fixed_launch or "4,6,6").split(","))
+        res = run_mixed_shapes(torch, V, local, args.mixed_shapes_steps, args.warmup, args.mixed_shapes_tracks,
+                               torch.cuda.current_stream(), fixed=(fixed + (0, 0))[:3])
+        print(json.dumps({"mixed_shapes": res}), flush=True)
+        return 0
 
     grid, t = make_workload(args.tracks)
     geo = V.Geometry(grid.desc, device=local)
@@ -516,7 +602,12 @@ def run_ours(args, ws, rank, local):
         cpu = None
         if ws == 1 and not args.no_cpu_baseline:
             rate, cores, sample = cpu_sample_rate(grid, t, min_seconds=args.cpu_seconds)
-            cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+            r1, _, s1 = cpu_sample_rate(grid, t, min_seconds=2.0, threads=1, n=1 << 18)
+            cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                   "single_core": {"value": r1, "unit": UNIT, "cores": 1, "sample": s1},
+                   "note": "the oracle: the reference's scalar BVHNavigator path restated in C, bit-exact with "
+                           "it; the reference's own sources need its build host (see the design notes for "
+                           "its rate next to the port's there)"}
         traffic = None
         tp = ROOT / "profiles" / "step_kernel_traffic.json"
         if tp.exists():
@@ -545,6 +636,10 @@ def run_ours(args, ws, rank, local):
                 a = ms_ops * mixed_shapes["fp64"]["value"] / 1e12
                 mixed_shapes["compute_roofline_fp64"] = {"fp64_ops_per_step": ms_ops, "achieved": a,
                                                          "unit": "TFLOP/s", "frac_of_fp64_peak": a / fpk["fp64"]}
+        tube_shape = None
+        if ws == 1 and not args.no_tube_shape:
+            tube_shape = run_tube_shape(torch, V, local, 10, args.warmup, stream, fpk.get("fp64"),
+                                        cpu=not args.no_cpu_baseline)
         batched = None
         if ws == 1 and not args.no_batched:
             # a side stream: CUDA graphs cannot be captured on the legacy default stream
@@ -584,6 +679,7 @@ def run_ours(args, ws, rank, local):
             "clocks": clock_log[0] if clock_log else None,
             "cpu_baseline": cpu,
             "mixed_shapes": mixed_shapes,
+            "tube_shape_kernel": tube_shape,
             "batched_uneven": batched,
             "serving": serving,
         }
@@ -606,11 +702,14 @@ def main():
     ap.add_argument("--fixed-launch", default="",
                     help="VARIANT,KBITS[,SAFETY_KBITS] instead of autotuning (profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-geometry batched workload")
+    ap.add_argument("--no-tube-shape", action="store_true", help="skip the single-Tube shape-kernel workload")
     ap.add_argument("--batched-steps", type=int, default=10)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
     ap.add_argument("--serving-seconds", type=float, default=6.0)
     ap.add_argument("--mixed-shapes-tracks", type=int, default=1 << 23)
     ap.add_argument("--mixed-shapes-steps", type=int, default=5)
+    ap.add_argument("--mixed-shapes-only", action="store_true",
+                    help="profiling runs: only the mixed-shape leg, launch from --fixed-launch (default 4,6,6)")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -42,7 +42,8 @@ enum vgn_shape_type {
   VGN_TRD       = 3, /* params: x1, x2, y1, y2, z                 (UnplacedTrd.h)       */
   VGN_TRAPEZOID = 4, /* params: dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2 (UnplacedTrapezoid.h) */
   VGN_SPHERE    = 5, /* params: rmin, rmax, sphi, dphi, stheta, dtheta (UnplacedSphere.h) */
-  VGN_POLYCONE  = 6  /* params: sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] (UnplacedPolycone.h:79) */
+  VGN_POLYCONE  = 6, /* params: sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] (UnplacedPolycone.h:79) */
+  VGN_ORB       = 7  /* params: r                                 (UnplacedOrb.h)       */
 };
 
 /* ---- shape operations for vgn_shape_batch ------------------------------- */
@@ -98,6 +99,14 @@ typedef struct vgn_geometry vgn_geometry;
  * source/CudaManager.cpp:101-222, source/BVHManager.cpp:33-45). */
 #define VGN_HOST_ONLY (-1) /* `device` value: close on the host only (tables can be inspected, no kernels) */
 int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry **out);
+/* The same with a transformation cache depth, GeoManager::SetTransformationCacheDepth before
+ * closing (VecGeom/management/GeoManager.h:121, used at source/GeoManager.cpp:220-221):
+ * navigation-table nodes deeper than `cache_depth` levels store no global matrix, and a
+ * state's matrix is accumulated from the placements up to its nearest cached ancestor
+ * (NavStateIndex::TopMatrixImpl, NavStateIndex.h:232-265).  0 caches every level, as
+ * vgn_geometry_create does; the table then equals the reference's for the same depth. */
+int vgn_geometry_create_with_cache_depth(const vgn_geometry_desc *desc, int device, int32_t cache_depth,
+                                         vgn_geometry **out);
 int vgn_geometry_free(vgn_geometry *geom);
 
 /* Host copy of the navigation index table (NavIndexTable::GetTable,
@@ -194,7 +203,8 @@ int vgn_autotune_step(vgn_geometry *geom, int64_t n, const double *px, const dou
  * TestVGDMLNavigation.cpp:86-102) with the state kept on the device.  Positions and
  * states are updated in place; nsteps[i] receives the steps taken (-1: invalid state).
  * Tracks are visited in the binned order of the geometry's step configuration for this
- * precision form (vgn_set_step_config / vgn_autotune_step), with stream-ordered scratch.
+ * precision form (vgn_set_step_config / vgn_autotune_step), with stream-ordered scratch;
+ * batches of fewer than 32768 tracks are walked unbinned.
  * Device pointers only.  No single counterpart call in the reference. */
 int vgn_walk_batch(const vgn_geometry *geom, int64_t n, double *px, double *py, double *pz, const double *dx,
                    const double *dy, const double *dz, const double *step_limit, vgn_state *state,

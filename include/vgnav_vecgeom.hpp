@@ -57,6 +57,7 @@
 #include "VecGeom/volumes/PlacedVolume.h"
 #include "VecGeom/volumes/UnplacedBox.h"
 #include "VecGeom/volumes/UnplacedCone.h"
+#include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
 #include "VecGeom/volumes/UnplacedTrapezoid.h"
@@ -132,6 +133,10 @@ inline int shape_row(vecgeom::VUnplacedVolume const *u, std::vector<double> &p)
     p = {s->GetInnerRadius(),     s->GetOuterRadius(),     s->GetStartPhiAngle(),
          s->GetDeltaPhiAngle(),   s->GetStartThetaAngle(), s->GetDeltaThetaAngle()};
     return VGN_SPHERE;
+  }
+  if (auto o = dynamic_cast<UnplacedOrb const *>(u)) {
+    p = {o->GetRadius()};
+    return VGN_ORB;
   }
   if (auto c = dynamic_cast<UnplacedPolycone const *>(u)) {
     auto const *h = c->GetOriginalParameters();  // the constructor's planes (PolyconeStruct.h:279-285)

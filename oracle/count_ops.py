@@ -44,6 +44,7 @@ KERNEL_WEIGHTS = [
     [60, 50, 32, 32, 30, 32],     # TrapezoidImplementation.h:177-401
     [55, 50, 10, 10, 8, 8],       # SphereImplementation.h:138-479
     [270, 240, 75, 75, 36, 42],   # PolyconeImplementation.h:189-517 (three cone sections)
+    [20, 20, 8, 8, 6, 8],         # OrbImplementation.h:102-220
 ]
 
 

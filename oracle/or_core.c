@@ -198,7 +198,12 @@ static uint32_t nav_apply(const or_geom *g, nav_visitor *v, int level, uint32_t 
   size_t before       = v->count ? v->table_bytes / 4 : v->current;
   uint32_t dindices   = 3 + nd + ((nd + 1) & 1);
   int pad             = ((before + dindices) * 4) % 8 != 0;
-  size_t cur_size     = (dindices + (size_t)pad) * 4 + 12 * 8; /* all levels cached (GeoManager.cpp:220-221) */
+  /* depth limit: the level count when unset or larger (GeoManager.cpp:220-221); deeper
+     levels cache no matrix (NavIndexTable.cpp:18), the counting pass sizes the pad anyway */
+  int levels          = g->max_depth + 1;
+  int limit           = (g->cache_depth == 0 || g->cache_depth > levels) ? levels : g->cache_depth;
+  int cache           = !(limit > 0 && level > limit);
+  size_t cur_size     = (dindices + (size_t)pad) * 4 + (cache ? 12 * 8 : 0);
   unsigned char *bytes;
   or_xf mat;
   int i;
@@ -217,6 +222,7 @@ static uint32_t nav_apply(const or_geom *g, nav_visitor *v, int level, uint32_t 
   memcpy(bytes + 2, &nd, 2);
   for (i = 0; i < nd; ++i) v->tab[v->current + 3 + i] = 0;
   v->current += dindices;
+  if (!cache) return new_mother;
 
   /* NavStatePath::TopMatrix (NavStatePath.h:616-628): identity times levels 1..level */
   xf_identity(&mat);
@@ -262,6 +268,7 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_TRD: return 5;
   case OR_TRAP: return 11;
   case OR_SPHERE: return 6;
+  case OR_ORB: return 1;
   case OR_POLYCONE: { /* sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] */
     int nz;
     if (avail < 3 || !(p[2] >= 2 && p[2] <= 4096)) return -1;
@@ -277,6 +284,14 @@ or_geom *or_geom_create(int n_lv, const int *lv_shape, const int *lv_param_off, 
                         int n_pv, const int *pv_lv, const int *pv_mother, const double *pv_trans, int world_pv,
                         char *err, int errlen)
 {
+  return or_geom_create_ex(n_lv, lv_shape, lv_param_off, params, n_params, n_pv, pv_lv, pv_mother, pv_trans,
+                           world_pv, 0, err, errlen);
+}
+
+or_geom *or_geom_create_ex(int n_lv, const int *lv_shape, const int *lv_param_off, const double *params,
+                           int n_params, int n_pv, const int *pv_lv, const int *pv_mother, const double *pv_trans,
+                           int world_pv, int cache_depth, char *err, int errlen)
+{
   or_geom *g;
   int i, *count;
   nav_visitor nv;
@@ -289,6 +304,7 @@ or_geom *or_geom_create(int n_lv, const int *lv_shape, const int *lv_param_off, 
   g->n_lv  = n_lv;
   g->n_pv  = n_pv;
   g->world_pv = world_pv;
+  g->cache_depth = cache_depth < 0 ? 0 : cache_depth;
   g->lv    = (or_lv *)calloc((size_t)n_lv, sizeof(or_lv));
   g->pv    = (or_pv *)calloc((size_t)n_pv, sizeof(or_pv));
   for (i = 0; i < n_lv; ++i) {

@@ -146,6 +146,8 @@ typedef struct { /* PolyconeStruct.h:24-37: z planes and one ConeStruct per sect
   or_cone *sec;  /* [nsec] PolyconeSection::fSolid */
 } or_polycone;
 
+typedef struct { double r; } or_orb; /* OrbStruct.h:19 fR */
+
 typedef struct {
   int type;
   int param_off;
@@ -160,6 +162,7 @@ typedef struct {
     or_trap trap;
     or_sphere sph;
     or_polycone pcon;
+    or_orb orb;
   } s;
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;
@@ -181,6 +184,7 @@ struct or_geom {
   uint32_t *navind;
   size_t navind_words;
   int max_depth;
+  int cache_depth; /* GeoManager::SetTransformationCacheDepth; 0 = every level cached */
 };
 
 /* shapes (or_shapes.c) */

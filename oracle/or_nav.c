@@ -7,8 +7,9 @@
  * BVHNavigator<false> + BVHSafetyEstimator + BVHLevelLocator; leaf volumes
  * carry NewSimpleNavigator (no daughters to test, so its step equals the BVH
  * navigator's) -- the set-up of test/globalbenchmarks/XRayBenchmarkFromROOTFile.cpp:206-238.
- * The navigation index table caches every level's global matrix
- * (GeoManager.cpp:220-221), as a CUDA build of the reference does.
+ * The navigation index table caches every level's global matrix unless a
+ * transformation cache depth is given (GeoManager.cpp:218-221); top_matrix then
+ * accumulates the uncached levels' placements (NavStateIndex.h:232-265).
  */
 #define _GNU_SOURCE
 #include <pthread.h>

@@ -2578,6 +2578,85 @@ static void polycone_extent(const or_polycone *t, v3 *mn, v3 *mx)
 /* ================================================================== */
 /* dispatch                                                           */
 /* ================================================================== */
+/* Orb (OrbImplementation.h:60-225, OrbStruct.h:19-25, source/UnplacedOrb.cpp:58-63)    */
+
+/* GenericKernelForContainsAndInside (OrbImplementation.h:88-100) */
+static int orb_contains(const or_orb *o, v3 p)
+{
+  double rad2 = v3_mag2(p);
+  double tolR = o->r + kTolerance;
+  return !(rad2 >= tolR * tolR);
+}
+
+static int orb_inside(const or_orb *o, v3 p) /* OrbImplementation.h:72-85 */
+{
+  double rad2 = v3_mag2(p);
+  double tolR = o->r - kTolerance;
+  int cin     = rad2 <= tolR * tolR;
+  int cout;
+  tolR = o->r + kTolerance;
+  cout = rad2 >= tolR * tolR;
+  return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+}
+
+/* DetectIntersectionAndCalculateDistance (OrbImplementation.h:197-220) */
+static int orb_intersect(const or_orb *o, v3 p, v3 d, int toIn, double *dist)
+{
+  double rad2    = v3_mag2(p);
+  double pDotV3D = v3_dot(p, d);
+  double c       = rad2 - o->r * o->r;
+  double d2      = pDotV3D * pDotV3D - c;
+  if (toIn) {
+    if (d2 >= 0. && pDotV3D <= 0.) {
+      *dist = -pDotV3D - sqrt(fabs(d2));
+      return 1;
+    }
+    return 0;
+  }
+  if (d2 >= 0.) {
+    *dist = -pDotV3D + sqrt(fabs(d2));
+    return 1;
+  }
+  return 0;
+}
+
+static double orb_dist_in(const or_orb *o, v3 p, v3 d) /* OrbImplementation.h:102-124 */
+{
+  double rad = sqrt(v3_mag2(p)), pDotV3D, dist = kInfLength;
+  if (rad < o->r - kTolerance) return -1.;
+  pDotV3D = v3_dot(p, d);
+  if (rad >= o->r - kTolerance && rad <= o->r + kTolerance && pDotV3D < 0.) return 0.;
+  return orb_intersect(o, p, d, 1, &dist) ? dist : kInfLength;
+}
+
+static double orb_dist_out(const or_orb *o, v3 p, v3 d) /* OrbImplementation.h:126-150 */
+{
+  double rad = sqrt(v3_mag2(p)), pDotV3D, dist = kInfLength;
+  if (rad > o->r + kTolerance) return -1.;
+  pDotV3D = v3_dot(p, d);
+  if (rad >= o->r - kTolerance && rad <= o->r + kTolerance && pDotV3D > 0.) return 0.;
+  return orb_intersect(o, p, d, 0, &dist) ? dist : kInfLength;
+}
+
+static double orb_safe_in(const or_orb *o, v3 p) /* OrbImplementation.h:152-165 */
+{
+  double rad    = sqrt(v3_mag2(p));
+  double safety = rad - o->r;
+  if (rad < o->r - kTolerance) return -1.;
+  if (rad > o->r - kTolerance && rad < o->r + kTolerance) safety = 0.;
+  return safety;
+}
+
+static double orb_safe_out(const or_orb *o, v3 p) /* OrbImplementation.h:167-181 */
+{
+  double rad    = sqrt(v3_mag2(p));
+  double safety = o->r - rad;
+  if (rad > o->r + kTolerance) return -1.;
+  if (rad > o->r - kTolerance && rad < o->r + kTolerance) safety = 0.;
+  return safety;
+}
+
+/* ================================================================== */
 
 int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
 {
@@ -2594,6 +2673,9 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
   case OR_TRAP: return trap_init(&lv->s.trap, p, err, errlen);
   case OR_SPHERE: return sphere_init(&lv->s.sph, p, err, errlen);
   case OR_POLYCONE: return polycone_init(&lv->s.pcon, p, err, errlen);
+  case OR_ORB:
+    lv->s.orb.r = p[0];
+    return 0;
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -2611,6 +2693,10 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
   case OR_TRAP: trap_extent(&lv->s.trap, mn, mx); return;
   case OR_SPHERE: sphere_extent(&lv->s.sph, mn, mx); return;
   case OR_POLYCONE: polycone_extent(&lv->s.pcon, mn, mx); return;
+  case OR_ORB:
+    *mn = v3_make(-lv->s.orb.r, -lv->s.orb.r, -lv->s.orb.r);
+    *mx = v3_make(lv->s.orb.r, lv->s.orb.r, lv->s.orb.r);
+    return;
   }
 }
 
@@ -2629,6 +2715,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_TRAP: return trap_dist_in(&lv->s.trap, p, d);
   case OR_SPHERE: return sphere_dist_in(&lv->s.sph, p, d);
   case OR_POLYCONE: return polycone_dist_in(&lv->s.pcon, p, d);
+  case OR_ORB: return orb_dist_in(&lv->s.orb, p, d);
   }
   return kInfLength;
 }
@@ -2645,6 +2732,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_TRAP: return trap_dist_out(&lv->s.trap, p, d);
   case OR_SPHERE: return sphere_dist_out(&lv->s.sph, p, d);
   case OR_POLYCONE: return polycone_dist_out(&lv->s.pcon, p, d);
+  case OR_ORB: return orb_dist_out(&lv->s.orb, p, d);
   }
   return -1.;
 }
@@ -2660,6 +2748,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRAP: return trap_safe_in(&lv->s.trap, p);
   case OR_SPHERE: return sphere_safe_in(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_safe_in(&lv->s.pcon, p);
+  case OR_ORB: return orb_safe_in(&lv->s.orb, p);
   }
   return kInfLength;
 }
@@ -2675,6 +2764,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRAP: return trap_safe_out(&lv->s.trap, p);
   case OR_SPHERE: return sphere_safe_out(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_safe_out(&lv->s.pcon, p);
+  case OR_ORB: return orb_safe_out(&lv->s.orb, p);
   }
   return 0.;
 }
@@ -2690,6 +2780,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRAP: return trap_contains(&lv->s.trap, p);
   case OR_SPHERE: return sphere_contains(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_contains(&lv->s.pcon, p);
+  case OR_ORB: return orb_contains(&lv->s.orb, p);
   }
   return 0;
 }
@@ -2705,6 +2796,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_TRAP: return trap_inside(&lv->s.trap, p);
   case OR_SPHERE: return sphere_inside(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_inside(&lv->s.pcon, p);
+  case OR_ORB: return orb_inside(&lv->s.orb, p);
   }
   return kOutsideE;
 }

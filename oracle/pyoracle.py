@@ -23,12 +23,12 @@ OP_DIST_IN, OP_DIST_OUT, OP_SAFE_IN, OP_SAFE_OUT, OP_CONTAINS, OP_INSIDE = range
 class Counters(C.Structure):
     _fields_ = [("node_slab", C.c_uint64), ("prim_slab", C.c_uint64), ("node_safety", C.c_uint64),
                 ("prim_safety", C.c_uint64), ("prim_contains", C.c_uint64), ("transforms", C.c_uint64),
-                ("kernel", (C.c_uint64 * 6) * 7)]
+                ("kernel", (C.c_uint64 * 6) * 8)]
 
     def as_dict(self) -> dict:
         d = {k: int(getattr(self, k)) for k in ("node_slab", "prim_slab", "node_safety", "prim_safety",
                                                 "prim_contains", "transforms")}
-        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(7)]
+        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(8)]
         return d
 
 
@@ -50,6 +50,8 @@ def lib() -> C.CDLL:
         p, i, l = C.c_void_p, C.c_int, C.c_long
         L.or_geom_create.restype = p
         L.or_geom_create.argtypes = [i, p, p, p, i, i, p, p, p, i, C.c_char_p, i]
+        L.or_geom_create_ex.restype = p
+        L.or_geom_create_ex.argtypes = [i, p, p, p, i, i, p, p, p, i, i, C.c_char_p, i]
         L.or_geom_free.argtypes = [p]
         L.or_geom_navindex.restype = C.POINTER(C.c_uint32)
         L.or_geom_navindex.argtypes = [p, C.POINTER(C.c_size_t)]
@@ -71,7 +73,7 @@ def _p(a):
 
 
 class OracleGeometry:
-    def __init__(self, desc):
+    def __init__(self, desc, cache_depth: int = 0):
         L = lib()
         self._keep = [np.ascontiguousarray(desc.lv_shape, np.int32),
                       np.ascontiguousarray(desc.lv_param_offset, np.int32),
@@ -81,8 +83,8 @@ class OracleGeometry:
                       np.ascontiguousarray(desc.pv_transform, np.float64).reshape(-1)]
         k = self._keep
         err = C.create_string_buffer(256)
-        h = L.or_geom_create(desc.n_logical, _p(k[0]), _p(k[1]), _p(k[2]), k[2].shape[0], desc.n_placed, _p(k[3]),
-                             _p(k[4]), _p(k[5]), desc.world_placed, err, 256)
+        h = L.or_geom_create_ex(desc.n_logical, _p(k[0]), _p(k[1]), _p(k[2]), k[2].shape[0], desc.n_placed,
+                                _p(k[3]), _p(k[4]), _p(k[5]), desc.world_placed, int(cache_depth), err, 256)
         if not h:
             raise ValueError("oracle geometry: " + err.value.decode())
         self.h = h

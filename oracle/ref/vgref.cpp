@@ -40,6 +40,7 @@
 #include "VecGeom/volumes/PlacedVolume.h"
 #include "VecGeom/volumes/UnplacedBox.h"
 #include "VecGeom/volumes/UnplacedCone.h"
+#include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
 #include "VecGeom/volumes/UnplacedTrapezoid.h"
@@ -95,6 +96,8 @@ VUnplacedVolume *make_shape(int type, const double *p)
     const int nz = (int)p[2];
     return GeoManager::MakeInstance<UnplacedPolycone>(p[0], p[1], nz, p + 3, p + 3 + nz, p + 3 + 2 * nz);
   }
+  case 7:
+    return GeoManager::MakeInstance<UnplacedOrb>(p[0]);
   default:
     return nullptr;
   }

@@ -22,7 +22,8 @@ extern "C" {
 #endif
 
 /* shape type ids (same numbering as the product's vgn_shape_type) */
-enum { OR_BOX = 0, OR_TUBE = 1, OR_CONE = 2, OR_TRD = 3, OR_TRAP = 4, OR_SPHERE = 5, OR_POLYCONE = 6, OR_NSHAPES = 7 };
+enum { OR_BOX = 0, OR_TUBE = 1, OR_CONE = 2, OR_TRD = 3, OR_TRAP = 4, OR_SPHERE = 5, OR_POLYCONE = 6, OR_ORB = 7,
+       OR_NSHAPES = 8 };
 
 /* shape operations for or_shape_batch */
 enum { OR_OP_DIST_IN = 0, OR_OP_DIST_OUT = 1, OR_OP_SAFE_IN = 2, OR_OP_SAFE_OUT = 3, OR_OP_CONTAINS = 4, OR_OP_INSIDE = 5 };
@@ -59,6 +60,11 @@ typedef struct or_geom or_geom;
 or_geom *or_geom_create(int n_lv, const int *lv_shape, const int *lv_param_off, const double *params, int n_params,
                         int n_pv, const int *pv_lv, const int *pv_mother, const double *pv_trans, int world_pv,
                         char *err, int errlen);
+/* the same with GeoManager::SetTransformationCacheDepth(cache_depth) before closing
+ * (GeoManager.h:121): table nodes deeper than cache_depth levels store no matrix */
+or_geom *or_geom_create_ex(int n_lv, const int *lv_shape, const int *lv_param_off, const double *params,
+                           int n_params, int n_pv, const int *pv_lv, const int *pv_mother, const double *pv_trans,
+                           int world_pv, int cache_depth, char *err, int errlen);
 void or_geom_free(or_geom *g);
 
 /* exported tables for cross-checks against the product's host builder */

@@ -1234,7 +1234,67 @@ POLYCONE_CASES = [
     _case(f"{PC}:546", POLYCONE, PCON175, "inside", (-18.1079855387881, -54.3917837284389, 121.5), None, 2, "eq"),
 ]
 
-ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES + POLYCONE_CASES
+ORB = 7
+OB = "test/unit_tests/TestOrb.cpp"
+_FR = 9.0                      # TestOrb.cpp:32 fR
+ORB1, ORB2 = (_FR,), (6.0,)    # TestOrb.cpp:52-53 b1, b2
+ORB3, ORB6 = (3.0,), (50.0,)   # TestOrb.cpp:339, 369 b3, b6
+_PBIG = {"x": (100.0, 0.0, 0.0), "y": (0.0, 100.0, 0.0), "z": (0.0, 0.0, 100.0),
+         "mx": (-100.0, 0.0, 0.0), "my": (0.0, -100.0, 0.0), "mz": (0.0, 0.0, -100.0)}
+_PON = {"x": (_FR, 0.0, 0.0), "mx": (-_FR, 0.0, 0.0), "y": (0.0, _FR, 0.0), "my": (0.0, -_FR, 0.0),
+        "z": (0.0, 0.0, _FR), "mz": (0.0, 0.0, -_FR)}
+_V = {"x": vx, "mx": vmx, "y": vy, "my": vmy, "z": vz, "mz": vmz}
+_PO = (-8.363470934547895, 2.754420966126675, -2.665617952433236)      # TestOrb.cpp:276
+_POT = (8.884242447222299, 0.134875592787852, -1.432495973274375)      # TestOrb.cpp:298
+_PI = (-3.618498437781364, 2.401810108299175, -6.718465394675017)      # TestOrb.cpp:314
+ORB_CASES = [
+    # DistanceToOut from the centre and from the surface points on the axes (TestOrb.cpp:111-181)
+    *[_case(f"{OB}:{111 + 4 * k}", ORB, ORB1, "dist_out", pzero, _V[a], _FR)
+      for k, a in enumerate(("x", "mx", "y", "my", "z", "mz"))],
+    *[_case(f"{OB}:{135 + 8 * k + 4 * j}", ORB, ORB1, "dist_out", _PON[a], _V[b], 0.0 if a == b else 2 * _FR)
+      for k, a in enumerate(("x", "mx", "y", "my", "z", "mz"))
+      for j, b in enumerate((a.replace("m", ""), "m" + a.replace("m", "")))],
+    _case(f"{OB}:184", ORB, ORB1, "inside", pzero, None, 1, "eq"),
+    *[_case(f"{OB}:{185 + k}", ORB, ORB1, "inside", _PBIG[a], None, 3, "eq") for k, a in enumerate("xyz")],
+    *[_case(f"{OB}:{189 + k}", ORB, ORB1, "inside", _PON[a], None, 2, "eq") for k, a in enumerate("xyz")],
+    _case(f"{OB}:193", ORB, ORB2, "inside", pzero, None, 1, "eq"),
+    *[_case(f"{OB}:{194 + k}", ORB, ORB2, "inside", _PON[a], None, 3, "eq") for k, a in enumerate("xyz")],
+    _case(f"{OB}:197", ORB, ORB2, "inside", (6.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{OB}:198", ORB, ORB2, "inside", (0.0, 6.0, 0.0), None, 2, "eq"),
+    _case(f"{OB}:199", ORB, ORB2, "inside", (0.0, 0.0, 6.0), None, 2, "eq"),
+    _case(f"{OB}:202", ORB, ORB1, "safe_out", pzero, None, _FR),
+    _case(f"{OB}:204", ORB, ORB1, "safe_out", vx, None, _FR - 1),
+    _case(f"{OB}:206", ORB, ORB1, "safe_out", vy, None, _FR - 1),
+    _case(f"{OB}:208", ORB, ORB1, "safe_out", vz, None, _FR - 1),
+    *[_case(f"{OB}:{212 + 2 * k}", ORB, ORB1, "safe_in", _PBIG[a], None, 100 - _FR)
+      for k, a in enumerate(("x", "mx", "y", "my", "z", "mz"))],
+    *[_case(f"{OB}:{226 + 2 * k}", ORB, ORB1, "dist_in", _PBIG[a], _V[("m" + a).replace("mm", "")], 100 - _FR)
+      for k, a in enumerate(("x", "mx", "y", "my", "z", "mz"))],
+    _case(f"{OB}:239", ORB, ORB1, "dist_in", _PBIG["x"], vxy, INF, "inf"),
+    _case(f"{OB}:243", ORB, ORB1, "dist_in", _PBIG["mx"], vxy, INF, "inf"),
+    _case(f"{OB}:248", ORB, ORB2, "dist_in", (9.0, 0.0, 12.0), vxmz, INF, "inf"),
+    _case(f"{OB}:253", ORB, ORB2, "dist_in", (12.0, 9.0, 0.0), vmxy, INF, "inf"),
+    _case(f"{OB}:257", ORB, ORB2, "dist_in", (12.0, 9.0, 0.0), vmx, INF, "inf"),
+    _case(f"{OB}:262", ORB, ORB2, "dist_in", (8.0, 0.0, 0.0), vmx, 2.0),
+    _case(f"{OB}:266", ORB, ORB2, "dist_in", (7.0, 5.0, 0.0), vmx, 3.6833752),
+    _case(f"{OB}:269", ORB, ORB1, "dist_in", (-25.0, -35.0, 0.0), vx, INF, "inf"),
+    _case(f"{OB}:273", ORB, ORB1, "dist_in", (-25.0, -35.0, 0.0), vy, INF, "inf"),
+    _case(f"{OB}:278", ORB, ORB1, "dist_in", _PO, tuple(c / 9.2 for c in _PO), INF, "inf"),
+    _case(f"{OB}:282", ORB, ORB1, "dist_out", _PO, tuple(c / 9.2 for c in _PO), 0.0, "le0"),
+    _case(f"{OB}:288", ORB, ORB1, "dist_in", _PO, tuple(-c / 9.2 for c in _PO), 0.2),
+    _case(f"{OB}:301", ORB, ORB1, "dist_in", _POT, tuple(c / 9 for c in _POT), INF, "inf"),
+    _case(f"{OB}:308", ORB, ORB1, "dist_in", _POT, tuple(-c / 9 for c in _POT), 0.0),
+    _case(f"{OB}:317", ORB, ORB1, "dist_in", _PI, tuple(c / 8 for c in _PI), 0.0, "lt0"),
+    _case(f"{OB}:323", ORB, ORB1, "dist_out", _PI, tuple(c / 8 for c in _PI), 1.0),
+    _case(f"{OB}:330", ORB, ORB1, "dist_in", _PI, tuple(-c / 8 for c in _PI), 0.0, "lt0"),
+    _case(f"{OB}:335", ORB, ORB1, "dist_out", _PI, tuple(-c / 8 for c in _PI), 17.0),
+    _case(f"{OB}:342", ORB, ORB3, "dist_in", (-1.704652541027918744, 0.92532982039202238411, -2.2886512267834184797),
+          (0.55992127966252225324, -0.73207465430510332283, 0.38801399601708530529), 0.0),
+    _case(f"{OB}:384", ORB, ORB6, "dist_in", (-46.418969559619192466, -17.038092391528927294, 7.4150301880992222081),
+          (0.84546676256780450842, -0.33558962646945966757, -0.41541010579811871173), 0.0),
+]
+
+ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES + POLYCONE_CASES + ORB_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:

@@ -13,7 +13,11 @@ writes inputs and outputs to tests/golden/ref_fixtures.npz:
                 rotations, 250 mm pitch as in the 8192-daughter workload): 4096 located
                 tracks, one step with safety, and 1024 of them walked to the world exit
   mixed_sections  the same with phi- and theta-sectioned shapes: 2048 tracks, one step
+  mixed_all     the same kind of geometry with every implemented shape type (Orb too):
+                2048 located tracks, one step, 512 of them walked to the world exit
   nested        the three-level geometry: 2048 located tracks, one step, a walk
+  deep_cache1   the five-level geometry with global matrices cached down to level 1 only
+                (transformation cache depth 1): 2048 located tracks, one step, a walk
   shapes        every parameter set of tests/shape_sets.py: up to 192 points (random,
                 coordinate planes and axes, surface), all six queries
 
@@ -68,6 +72,11 @@ def put_desc(out: dict, key: str, desc) -> None:
 def get_desc(fx, key: str):
     return W.GeometryDescription(*(np.asarray(fx[f"{key}/desc/{k}"]) for k in DESC_KEYS),
                                  int(fx[f"{key}/desc/world_placed"]))
+
+
+def get_cache_depth(fx, key: str) -> int:
+    k = f"{key}/desc/cache_depth"
+    return int(fx[k]) if k in fx else 0
 
 
 def put_tracks(out: dict, key: str, t) -> None:
@@ -163,6 +172,16 @@ def generate() -> dict:
         if not sections:
             _walk(out, key, rg, t.head(1024))
 
+    # every implemented shape type
+    desc = W.mixed_shape_geometry(seed=31, grid=MIXED_GRID, world=MIXED_WORLD, shapes=W.ALL_SHAPES)
+    rg = pyref.RefGeometry(desc)
+    t = W.mixed_shape_tracks(2048, seed_points=32, seed_dirs=33, world=MIXED_WORLD)
+    t.states = rg.locate(t.x, t.y, t.z)
+    put_desc(out, "mixed_all", desc)
+    put_tracks(out, "mixed_all", t)
+    _steps(out, "mixed_all", rg, t)
+    _walk(out, "mixed_all", rg, t.head(512))
+
     # three-level nested geometry
     desc = W.nested_geometry()
     rg = pyref.RefGeometry(desc)
@@ -172,6 +191,17 @@ def generate() -> dict:
     put_tracks(out, "nested", t)
     _steps(out, "nested", rg, t)
     _walk(out, "nested", rg, t)
+
+    # five levels, transformation cache depth 1
+    desc = W.deep_geometry()
+    rg = pyref.RefGeometry(desc, cache_depth=1)
+    t = W.uniform_tracks(2048, 590.0, 57, 58)
+    t.states = rg.locate(t.x, t.y, t.z)
+    put_desc(out, "deep_cache1", desc)
+    out["deep_cache1/desc/cache_depth"] = np.array(1)
+    put_tracks(out, "deep_cache1", t)
+    _steps(out, "deep_cache1", rg, t)
+    _walk(out, "deep_cache1", rg, t)
 
     # every shape parameter set
     for i, (name, shape, params) in enumerate(SHAPE_SETS):

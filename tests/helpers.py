@@ -14,7 +14,7 @@ ROOT = Path(__file__).resolve().parents[1]
 class HostTables:
     """libvgnav geometry closed on the host only (VGN_HOST_ONLY): tables, no kernels."""
 
-    def __init__(self, desc):
+    def __init__(self, desc, cache_depth: int = 0):
         L = N.lib()
         self._keep = [np.ascontiguousarray(desc.lv_shape, np.int32), np.ascontiguousarray(desc.lv_param_offset, np.int32),
                       np.ascontiguousarray(desc.params, np.float64), np.ascontiguousarray(desc.pv_logical, np.int32),
@@ -24,7 +24,7 @@ class HostTables:
         d = N.GeometryDesc(desc.n_logical, k[0].ctypes.data, k[1].ctypes.data, k[2].ctypes.data, k[2].shape[0],
                            desc.n_placed, k[3].ctypes.data, k[4].ctypes.data, k[5].ctypes.data, desc.world_placed)
         self.h = C.c_void_p()
-        N.check(L.vgn_geometry_create(C.byref(d), -1, C.byref(self.h)))
+        N.check(L.vgn_geometry_create_with_cache_depth(C.byref(d), -1, int(cache_depth), C.byref(self.h)))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -68,21 +68,21 @@ def keep(t: W.TrackBatch, mask: np.ndarray) -> W.TrackBatch:
 def navindex_pad_words(table: np.ndarray, n_words: int) -> np.ndarray:
     """Mask of the words of a navigation table that NavIndexTable's builder reserves but never
     writes (source/NavIndexTable.cpp:9-99, allocation NavIndexTable.h:92-101): the filler word
-    after a node's daughter list when the daughter count is even, and the alignment word before
-    a cached matrix.  The reference leaves them uninitialised; the builders here write zeros.
+    after a node's daughter list when the daughter count is even, the alignment word before a
+    cached matrix, and, with a transformation cache depth, the tail that the counting pass
+    sizes for pad words of uncached nodes.  The reference leaves them uninitialised; the
+    builders here write zeros.  Found by walking the node tree from the world's record.
     `n_words` is the reference's table size (GetTableSize() / 4)."""
-    pad = np.zeros(n_words, dtype=bool)
-    i = 1
-    while i < n_words:
+    written = np.zeros(n_words, dtype=bool)
+    todo = [1]
+    while todo:
+        i = todo.pop()
         w = int(table[i + 2])
         hasm, nd = (w >> 8) & 0xFF, w >> 16
-        if (nd + 1) & 1:
-            pad[i + 3 + nd] = True
+        written[i:i + 3 + nd] = True
         cur = i + 3 + nd + ((nd + 1) & 1)
         if hasm:
-            if cur % 2:
-                pad[cur] = True
-                cur += 1
-            cur += 24
-        i = cur
-    return pad
+            cur += cur % 2
+            written[cur:cur + 24] = True
+        todo.extend(int(table[i + 3 + k]) for k in range(nd))
+    return ~written

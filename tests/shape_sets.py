@@ -59,6 +59,9 @@ SHAPE_SETS = [
     ("polycone-cms-trak", W.POLYCONE, KA._pcon(0.0, W.K_TWO_PI, (-2935., -1899., -1899., -1899., 1899., 1899., 1899.,
                                                                  2935.), (74., 34., 31., 31., 31., 31., 34., 74.),
                                                (1233.,) * 8)),
+    ("orb-testorb-b1", W.ORB, KA.ORB1),
+    ("orb-large", W.ORB, (50.0,)),
+    ("orb-small", W.ORB, (3.0,)),
 ]
 
 

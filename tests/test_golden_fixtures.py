@@ -12,8 +12,8 @@ from golden import make_ref_fixtures as F
 from shape_sets import SHAPE_SETS
 from vecgeom_gb300 import workloads as W
 
-NAV_KEYS = ["box_grid", "mixed", "mixed_sections", "nested"]
-WALK_KEYS = ["mixed", "nested"]
+NAV_KEYS = ["box_grid", "mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1"]
+WALK_KEYS = ["mixed", "mixed_all", "nested", "deep_cache1"]
 
 
 @pytest.fixture(scope="module")
@@ -39,7 +39,7 @@ def test_fixture_covers_every_shape_set(fx):
 
 @pytest.mark.parametrize("key", NAV_KEYS)
 def test_oracle_steps_equal_reference(oracle, fx, key):
-    og = oracle.OracleGeometry(F.get_desc(fx, key))
+    og = oracle.OracleGeometry(F.get_desc(fx, key), cache_depth=F.get_cache_depth(fx, key))
     t = F.get_tracks(fx, key)
     r = og.step(t, calcsafety=True)
     expect_step(fx, key, r["step"], r["safety"], r["out"])
@@ -53,7 +53,7 @@ def test_oracle_steps_equal_reference(oracle, fx, key):
 
 @pytest.mark.parametrize("key", WALK_KEYS)
 def test_oracle_walk_equals_reference(oracle, fx, key):
-    og = oracle.OracleGeometry(F.get_desc(fx, key))
+    og = oracle.OracleGeometry(F.get_desc(fx, key), cache_depth=F.get_cache_depth(fx, key))
     t = F.get_tracks(fx, key)
     n = fx[f"{key}/walk/nsteps"].shape[0]
     x, y, z, st, ns = F.walk(lambda c: og.step(c, calcsafety=False), t.head(n))
@@ -89,7 +89,7 @@ def _states_dev(torch, st):
 @pytest.mark.parametrize("key", NAV_KEYS)
 def test_gpu_steps_equal_reference(vgnav, cuda, fx, key, mixed):
     torch = cuda
-    geo = vgnav.Geometry(F.get_desc(fx, key))
+    geo = vgnav.Geometry(F.get_desc(fx, key), cache_depth=F.get_cache_depth(fx, key))
     t = F.get_tracks(fx, key)
     pts = vgnav.SOA3D(_dev(torch, t.x), _dev(torch, t.y), _dev(torch, t.z))
     dirs = vgnav.SOA3D(_dev(torch, t.dx), _dev(torch, t.dy), _dev(torch, t.dz))
@@ -120,7 +120,7 @@ def test_gpu_walk_equals_reference(vgnav, cuda, fx, key, mixed):
     """vgn_walk_batch (the transport loop on the device) ends each track where the reference's
     loop ends it."""
     torch = cuda
-    geo = vgnav.Geometry(F.get_desc(fx, key))
+    geo = vgnav.Geometry(F.get_desc(fx, key), cache_depth=F.get_cache_depth(fx, key))
     n = fx[f"{key}/walk/nsteps"].shape[0]
     t = F.get_tracks(fx, key).head(n)
     pts = vgnav.SOA3D(_dev(torch, t.x), _dev(torch, t.y), _dev(torch, t.z))

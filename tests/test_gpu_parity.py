@@ -176,19 +176,25 @@ def test_box_grid_host_pointer_pipelined(oracle, vgnav, cuda, chunks):
 
 
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
-@pytest.mark.parametrize("which", ["box_grid", "nested"])
+@pytest.mark.parametrize("which", ["box_grid", "nested", "deep_cache1", "deep_cache2", "deep_cache0"])
 def test_walk_to_world_exit(oracle, vgnav, cuda, which, mixed):
-    """Every step of every track, stepped until it leaves the world, equals the oracle."""
+    """Every step of every track, stepped until it leaves the world, equals the oracle; on the
+    five-level geometry also with global matrices cached only down to level 1 or 2."""
+    cache_depth = 0
     if which == "box_grid":
         grid = W.box_grid_geometry()
         desc = grid.desc
         t = W.box_grid_tracks(grid, n=8192, seed_points=51, seed_dirs=52)
-    else:
+    elif which == "nested":
         desc = W.nested_geometry()
         t = W.uniform_tracks(8192, 480.0, 53, 54)
-    og = oracle.OracleGeometry(desc)
-    geo = vgnav.Geometry(desc)
-    if which == "nested":
+    else:
+        desc = W.deep_geometry()
+        cache_depth = int(which[-1])
+        t = W.uniform_tracks(8192, 590.0, 59, 60)
+    og = oracle.OracleGeometry(desc, cache_depth=cache_depth)
+    geo = vgnav.Geometry(desc, cache_depth=cache_depth)
+    if which != "box_grid":
         st = np.zeros(t.n, dtype=W.STATE_DTYPE)
         geo.locate(vgnav.SOA3D(t.x, t.y, t.z), vgnav.NavStatePool(st), mixed=mixed)
         assert np.array_equal(st, og.locate(t.x, t.y, t.z))
@@ -331,13 +337,17 @@ def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda)
     assert np.mean(ins == 2.0) > 0.5
 
 
-@pytest.mark.parametrize("sections", [False, True], ids=["full", "tube-phi-sections"])
+@pytest.mark.parametrize("sections", ["full", "sections", "all-shapes"])
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
-    """8192 daughters of every implemented shape type, full rotations (with `sections`, most
-    tubes are phi sections): locate, one step with safety, then every step of a track subset
-    to the world exit, all equal to the oracle."""
-    desc = W.mixed_shape_geometry(sections=sections)
+    """8192 daughters of the benchmark's seven shape types, full rotations (with "sections",
+    most tubes, cones and polycones are phi sections and spheres phi/theta sections; with
+    "all-shapes", every implemented type, Orb too): locate, one step with safety, then every
+    step of a track subset to the world exit, all equal to the oracle."""
+    if sections == "all-shapes":
+        desc = W.mixed_shape_geometry(seed=26, shapes=W.ALL_SHAPES)
+    else:
+        desc = W.mixed_shape_geometry(sections=sections == "sections")
     og = oracle.OracleGeometry(desc)
     geo = vgnav.Geometry(desc)
     t = W.mixed_shape_tracks(1 << 16)

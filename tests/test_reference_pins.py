@@ -26,15 +26,25 @@ def same_states(a, b):
 
 def geometries():
     grid = W.box_grid_geometry(seed=3)
+    deep = W.deep_geometry()
     return {
         "box_grid": (grid.desc, W.box_grid_tracks(grid, n=1 << 16, seed_points=4, seed_dirs=5)),
         "mixed": (W.mixed_shape_geometry(), W.mixed_shape_tracks(1 << 16)),
         "mixed_sections": (W.mixed_shape_geometry(sections=True), W.mixed_shape_tracks(1 << 15, 24, 25)),
+        "mixed_all": (W.mixed_shape_geometry(seed=26, shapes=W.ALL_SHAPES), W.mixed_shape_tracks(1 << 15, 27, 28)),
         "nested": (W.nested_geometry(), W.uniform_tracks(1 << 15, 480.0, 31, 32)),
+        # five levels, global matrices cached down to level 1 / 3 only (the deeper levels'
+        # matrices are accumulated from the placements, NavStateIndex.h:232-265)
+        "deep_cache1": (deep, W.uniform_tracks(1 << 15, 590.0, 33, 34)),
+        "deep_cache3": (deep, W.uniform_tracks(1 << 15, 590.0, 35, 36)),
     }
 
 
-GEOS = ["box_grid", "mixed", "mixed_sections", "nested"]
+GEOS = ["box_grid", "mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "deep_cache3"]
+
+
+def cache_depth(which):
+    return int(which[-1]) if which.startswith("deep_cache") else 0
 
 
 @pytest.fixture(scope="module")
@@ -47,15 +57,17 @@ def test_tables_equal_reference(oracle, vgnav, cases, which):
     """Navigation index table and every BVH: the product's host builder and the oracle's equal
     the reference's word for word."""
     desc, _ = cases[which]
-    rg = pyref.RefGeometry(desc)
+    cd = cache_depth(which)
+    rg = pyref.RefGeometry(desc, cache_depth=cd)
     ref = rg.navindex()
     pad = navindex_pad_words(ref, ref.shape[0])
-    for name, table in (("oracle", oracle.OracleGeometry(desc).navindex()), ("product", HostTables(desc).navindex())):
+    for name, table in (("oracle", oracle.OracleGeometry(desc, cache_depth=cd).navindex()),
+                        ("product", HostTables(desc, cache_depth=cd).navindex())):
         # the builders here allocate one spare word past the reference's table size, as it does
         assert table.shape[0] == ref.shape[0] + 1, name
         assert np.array_equal(table[:-1][~pad], ref[~pad]), name
         assert not np.any(table[:-1][pad]), name
-    og, ht = oracle.OracleGeometry(desc), HostTables(desc)
+    og, ht = oracle.OracleGeometry(desc, cache_depth=cd), HostTables(desc, cache_depth=cd)
     n_bvh = 0
     for lv in range(desc.n_logical):
         try:
@@ -75,8 +87,8 @@ def test_navigation_equals_reference(oracle, cases, which):
     """Point location, one step with safety (ComputeStepAndSafetyAndPropagatedState), one
     step without relocation (ComputeStep) and ComputeSafety: oracle == reference."""
     desc, t = cases[which]
-    rg = pyref.RefGeometry(desc)
-    og = oracle.OracleGeometry(desc)
+    rg = pyref.RefGeometry(desc, cache_depth=cache_depth(which))
+    og = oracle.OracleGeometry(desc, cache_depth=cache_depth(which))
     loc = rg.locate(t.x, t.y, t.z)
     assert same_states(og.locate(t.x, t.y, t.z), loc)
     if which != "box_grid":
@@ -107,12 +119,12 @@ def test_vector_interface_equals_scalar(oracle, cases):
     assert np.array_equal(o["step"], v["step"]) and same_states(o["out"], v["out"])
 
 
-@pytest.mark.parametrize("which", ["mixed", "mixed_sections", "nested"])
+@pytest.mark.parametrize("which", ["mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "deep_cache3"])
 def test_walk_equals_reference(oracle, cases, which):
     """Every step of a track subset, stepped until it leaves the world: oracle == reference."""
     desc, t = cases[which]
-    rg = pyref.RefGeometry(desc)
-    og = oracle.OracleGeometry(desc)
+    rg = pyref.RefGeometry(desc, cache_depth=cache_depth(which))
+    og = oracle.OracleGeometry(desc, cache_depth=cache_depth(which))
     w = t.head(4096)
     w.states = rg.locate(w.x, w.y, w.z)
     for it in range(400):

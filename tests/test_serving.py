@@ -1,6 +1,6 @@
-"""Serving-loop scheduler on the CPU: Poisson arrivals, admission by the device-memory pool,
-FIFO order, one request per stream, latency accounting.  A fake executor stands in for the
-GPU (each request takes a fixed time per track)."""
+"""Serving-loop scheduler on the CPU: Poisson arrivals, two priority classes, slicing of large
+requests, admission by live memory headroom, latency accounting per size bucket.  A fake
+executor stands in for the GPU (each piece takes a fixed time per track)."""
 import time
 
 import numpy as np
@@ -9,35 +9,29 @@ from vecgeom_gb300 import serving as S
 
 
 class FakeExecutor:
-    def __init__(self, seconds_per_track: float):
+    def __init__(self, seconds_per_track: float, headroom: int = 1 << 40):
         self.spt = seconds_per_track
+        self.room = headroom
+        self.in_use = 0
         self.started = []
 
-    def start(self, req, block, stream):
-        self.started.append((req.rid, block, stream, time.perf_counter()))
-        return (time.perf_counter() + req.n * self.spt, req.n)
+    def bytes(self, n):
+        return S.BYTES_PER_TRACK * n
+
+    def headroom(self):
+        return self.room - self.in_use
+
+    def start(self, piece, cls, stream):
+        self.in_use += self.bytes(piece.n)
+        self.started.append((piece.req.rid, piece.lo, piece.n, cls, stream, time.perf_counter()))
+        return [time.perf_counter() + piece.n * self.spt, piece]
 
     def done(self, h):
         return time.perf_counter() >= h[0]
 
     def finish(self, h):
-        return 3 * h[1]  # three steps per track
-
-
-def test_pool_first_fit_and_merge():
-    p = S.Pool(4096)
-    a = p.alloc(1000)
-    b = p.alloc(1000)
-    c = p.alloc(1000)
-    assert a == (0, 1024) and b == (1024, 1024) and c == (2048, 1024)
-    assert p.alloc(2000) is None
-    p.release(b)
-    assert p.alloc(1100) is None  # 1024 free in the middle, 1024 at the end
-    p.release(a)
-    assert p.alloc(2000) == (0, 2048)  # merged with the hole
-    p.release((0, 2048))
-    p.release(c)
-    assert p.free == [(0, 4096)] and p.in_use() == 0
+        self.in_use -= self.bytes(h[1].n)
+        return 3 * h[1].n  # three steps per track
 
 
 def test_poisson_arrivals_and_sizes():
@@ -50,29 +44,69 @@ def test_poisson_arrivals_and_sizes():
     assert abs(np.log(sizes).mean() - 0.5 * (np.log(256) + np.log(1 << 20))) < 0.4  # log-uniform
 
 
-def test_serve_admits_by_memory_in_fifo_order():
+def test_large_requests_are_sliced_and_complete_once():
+    reqs = [S.Request(arrival=0.0, rid=0, n=200000, seed=1), S.Request(arrival=0.0, rid=1, n=70000, seed=2)]
+    ex = FakeExecutor(1e-8)
+    done = S.serve(reqs, ex, small_streams=2, large_streams=2, slice_tracks=65536)
+    assert sorted(r.rid for r in done) == [0, 1]
+    pieces = sorted((rid, lo, n) for rid, lo, n, cls, s, t in ex.started)
+    assert pieces == [(0, 0, 65536), (0, 65536, 65536), (0, 131072, 65536), (0, 196608, 200000 - 196608),
+                      (1, 0, 65536), (1, 65536, 70000 - 65536)]
+    assert all(cls == S.LARGE for *_, cls, s, t in ex.started)
+    for r in done:
+        assert r.steps == 3 * r.n
+    assert ex.in_use == 0
+
+
+def test_small_requests_overtake_waiting_large_ones():
+    # one large stream busy with a long slice; small requests arriving later start at once on
+    # their own streams, and a second large request waits for the large stream
+    reqs = [S.Request(arrival=0.0, rid=0, n=60000, seed=1), S.Request(arrival=0.0, rid=1, n=60000, seed=2)]
+    reqs += [S.Request(arrival=0.002 + 0.001 * k, rid=2 + k, n=1000, seed=3 + k) for k in range(5)]
+    ex = FakeExecutor(1e-6)  # a 60000-track slice takes 60 ms, a small request 1 ms
+    done = S.serve(reqs, ex, small_streams=2, large_streams=1, small_max=16384)
+    by = {r.rid: r for r in done}
+    for k in range(2, 7):
+        assert by[k].done_at - by[k].arrival < 0.03  # not queued behind the 60 ms slices
+        assert by[k].done_at < by[1].done_at
+    assert by[1].done_at > by[0].done_at + 0.05  # the second large request ran after the first
+    order = [rid for rid, *_ in ex.started]
+    assert order.index(1) > order.index(2)  # a small one started before the waiting large one
+
+
+def test_admission_by_memory_headroom():
+    # room for about 6000 tracks at a time: the third request waits for memory
     reqs = [S.Request(arrival=0.001 * k, rid=k, n=n, seed=k) for k, n in enumerate([1000, 5000, 200, 4000, 300])]
-    # the pool holds about 6000 tracks: the third request waits behind the second's memory
-    pool = S.Pool(6000 * S.BYTES_PER_TRACK)
-    ex = FakeExecutor(2e-6)
-    done = S.serve(reqs, ex, pool, streams=4)
+    ex = FakeExecutor(2e-6, headroom=6000 * S.BYTES_PER_TRACK)
+    seen = []
+    orig_start = ex.start
+
+    def start(piece, cls, s):
+        h = orig_start(piece, cls, s)
+        seen.append(ex.in_use)
+        return h
+
+    ex.start = start
+    done = S.serve(reqs, ex, small_streams=4, large_streams=1)
     assert sorted(r.rid for r in done) == [0, 1, 2, 3, 4]
-    assert [s[0] for s in ex.started] == [0, 1, 2, 3, 4]  # admissions in arrival order
-    assert pool.in_use() == 0
+    assert max(seen) <= 6000 * S.BYTES_PER_TRACK
+    assert ex.in_use == 0
     for r in done:
         assert r.done_at >= r.arrival + r.n * 2e-6 * 0.9
         assert r.steps == 3 * r.n
-    summ = S.summarize(done)
-    assert summ["requests"] == 5 and summ["steps"] == 3 * sum(r.n for r in reqs)
-    assert summ["p99_ms"] >= summ["p50_ms"] > 0
 
 
-def test_serve_respects_stream_count():
-    reqs = [S.Request(arrival=0.0, rid=k, n=1000, seed=k) for k in range(6)]
-    ex = FakeExecutor(5e-6)
-    t0 = time.perf_counter()
-    done = S.serve(reqs, ex, S.Pool(1 << 30), streams=2)
-    el = time.perf_counter() - t0
-    assert len(done) == 6
-    assert el >= 3 * 1000 * 5e-6 * 0.9  # six equal requests, two at a time
-    assert len({s[2] for s in ex.started}) == 2
+def test_summary_buckets():
+    done = []
+    for k, n in enumerate([100, 3000, 5000, 60000, 70000, 900000]):
+        r = S.Request(arrival=0.0, rid=k, n=n, seed=k)
+        r.done_at = 0.001 * (k + 1)
+        r.steps = 2 * n
+        done.append(r)
+    s = S.summarize(done)
+    assert s["requests"] == 6 and s["steps"] == 2 * sum(r.n for r in done)
+    assert s["by_size"]["<=4k"]["requests"] == 2
+    assert s["by_size"]["<=64k"]["requests"] == 2
+    assert s["by_size"]["<=1M"]["requests"] == 2
+    assert s["by_size"]["<=4k"]["p99_ms"] <= s["by_size"]["<=1M"]["p50_ms"]
+    assert s["p99_ms"] >= s["p50_ms"] > 0

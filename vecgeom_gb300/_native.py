@@ -31,6 +31,7 @@ OP_DISTANCE_TO_IN, OP_DISTANCE_TO_OUT, OP_SAFETY_TO_IN, OP_SAFETY_TO_OUT, OP_CON
 # symbols declared in include/vgnav.h
 EXPORTED = [
     "vgn_geometry_create",
+    "vgn_geometry_create_with_cache_depth",
     "vgn_geometry_free",
     "vgn_geometry_navindex",
     "vgn_geometry_bvh_info",
@@ -112,6 +113,7 @@ def lib() -> C.CDLL:
         L = C.CDLL(str(LIB_PATH))
         p, i32, i64, vp = C.c_void_p, C.c_int32, C.c_int64, C.c_void_p
         L.vgn_geometry_create.argtypes = [C.POINTER(GeometryDesc), C.c_int, C.POINTER(vp)]
+        L.vgn_geometry_create_with_cache_depth.argtypes = [C.POINTER(GeometryDesc), C.c_int, i32, C.POINTER(vp)]
         L.vgn_geometry_free.argtypes = [vp]
         L.vgn_geometry_navindex.argtypes = [vp, C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_size_t)]
         L.vgn_geometry_bvh_info.argtypes = [vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]

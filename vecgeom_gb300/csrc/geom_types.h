@@ -22,7 +22,13 @@ namespace vgn {
 constexpr int kStackSize = 32;  // BVH::BVH_MAX_DEPTH (BVH.h:33)
 constexpr int kMaxLevels = 30;  // bound on geometry depth (relocation loops)
 
-enum ShapeType : int32_t { kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kNumShapes = 7 };
+enum ShapeType : int32_t {
+  kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kOrb = 7, kNumShapes = 8
+};
+
+// flags of a placement transformation (Transformation3D::SetProperties,
+// source/Transformation3D.cpp:117-126); none set = identity
+enum XfFlags : int32_t { kXfTrans = 1, kXfRot = 2 };
 
 // device error bits (OR-ed into the status word)
 enum DevError : uint32_t { kErrStack = 1u, kErrRelocate = 2u, kErrState = 4u };
@@ -38,7 +44,8 @@ struct alignas(128) PVRec {
   int32_t child_id;   // position in the mother's daughter list
   int32_t shape;      // shape type of lv (cached)
   int32_t shape_row;  // offset of lv's shape row in GeomView::shape (cached)
-  int32_t pad[4];
+  int32_t xf_flags;   // kXfTrans | kXfRot: Transformation3D::HasTranslation / HasRotation of xf
+  int32_t pad[3];
 };
 static_assert(sizeof(PVRec) == 128, "PVRec must be 128 bytes");
 
@@ -140,6 +147,8 @@ enum { SphHasRmin = 0, SphRmin, SphRmax, SphMsqMax, SphPsqMax, SphPsqMin, SphMsq
 namespace row {
 // Box: BoxStruct::fDimensions
 constexpr int kBoxSize = 4;
+// Orb: OrbStruct::fR
+constexpr int kOrbSize = 1;
 // Tube: TubeStruct cached members, then its phi wedge as a Wedge block (the along vectors
 // are both TubeStruct::fAlongPhi* and the wedge's; the block's last entry is fDphi)
 enum { TubeRmin = 0, TubeRmax, TubeZ, TubeRmin2, TubeRmax2, TubeTolIrmin2, TubeTolOrmin2, TubeTolIrmax2,

@@ -242,8 +242,14 @@ private:
     const size_t before     = counting_ ? bytes_ / 4 : current_;
     const uint32_t dindices = 3 + nd + ((nd + 1) & 1);
     const bool pad          = ((before + dindices) * 4) % 8 != 0;
+    // GeoManager::CloseGeometry: the cache depth limit is the geometry's level count when
+    // unset or larger (GeoManager.cpp:220-221); deeper nodes cache no matrix
+    // (NavIndexTable.cpp:18).  The counting pass sizes the pad word even without a matrix.
+    const int levels = g_.max_depth + 1;
+    const int limit  = (g_.cache_depth == 0 || g_.cache_depth > levels) ? levels : g_.cache_depth;
+    const bool cache = !(limit > 0 && level > limit);
     if (counting_) {
-      bytes_ += (dindices + (pad ? 1 : 0)) * 4 + 12 * 8;
+      bytes_ += (dindices + (pad ? 1 : 0)) * 4 + (cache ? 12 * 8 : 0);
       return 0;
     }
     uint32_t *tab      = g_.navind.data();
@@ -257,6 +263,7 @@ private:
     std::memcpy(bytes + 2, &nd, 2);
     for (int i = 0; i < nd; ++i) tab[current_ + 3 + i] = 0;
     current_ += dindices;
+    if (!cache) return new_mother;
     // global matrix of this level: identity times placements of levels 1..level
     HostXForm mat;
     xform_identity(mat);
@@ -328,8 +335,13 @@ inline float round_up(double v)
 
 void build_interval_images(HostGeometry &g);
 
-int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string &err)
+int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string &err, int32_t cache_depth)
 {
+  if (cache_depth < 0) {
+    err = "negative transformation cache depth";
+    return VGN_ERR_ARG;
+  }
+  g.cache_depth = cache_depth;
   if (d.n_logical <= 0 || d.n_placed <= 0 || !d.lv_shape || !d.lv_param_offset || !d.params || !d.pv_logical ||
       !d.pv_mother || !d.pv_transform) {
     err = "geometry description has empty or null arrays";
@@ -417,6 +429,7 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
     for (int k = 0; k < 9; ++k) r.xf.r[k] = g.pv[i].xf.r[k];
     r.lv        = g.pv[i].lv;
     r.child_id  = g.pv[i].child_id;
+    r.xf_flags  = (g.pv[i].xf.has_trans ? kXfTrans : 0) | (g.pv[i].xf.has_rot ? kXfRot : 0);
     r.shape     = g.lv[r.lv].shape;
     r.shape_row = g.lv[r.lv].shape_row;
   }

@@ -57,7 +57,8 @@ struct HostGeometry {
   std::vector<uint32_t> navind;   // navigation index table
   std::vector<uint32_t> node_start; // bitset over navind words: 1 where a state's record starts
   int32_t world_pv = 0;
-  int32_t max_depth = 0;
+  int32_t max_depth = 0;    // deepest level below the world (the world is level 0)
+  int32_t cache_depth = 0;  // GeoManager::SetTransformationCacheDepth: 0 = every level's matrix cached
 
   // flattened device images
   std::vector<PVRec> pv_rec;
@@ -76,8 +77,10 @@ struct HostGeometry {
   bool sections = false;    // some shape has a phi or theta section: needs the `sections` kernel set
 };
 
-// Returns 0 on success, a VGN_ERR_* code otherwise (message in err).
-int build_host_geometry(const vgn_geometry_desc &desc, HostGeometry &g, std::string &err);
+// Returns 0 on success, a VGN_ERR_* code otherwise (message in err).  `cache_depth` as
+// GeoManager::SetTransformationCacheDepth (GeoManager.h:121): navigation-table nodes deeper
+// than it carry no cached global matrix (0: all levels cached).
+int build_host_geometry(const vgn_geometry_desc &desc, HostGeometry &g, std::string &err, int32_t cache_depth = 0);
 
 // transformation helpers (Transformation3D semantics)
 HostXForm xform_from12(const double *a);

@@ -57,6 +57,7 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
   case kTrd: return 5;
   case kTrapezoid: return 11;
   case kSphere: return 6;
+  case kOrb: return 1;
   case kPolycone: {  // sphi, dphi, nz, z[nz], rmin[nz], rmax[nz]
     if (n_avail < 3 || !(p[2] >= 2 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
     return 3 + 3 * (int)p[2];
@@ -382,6 +383,15 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.push_back(dphi);
     return VGN_OK;
   }
+  case kOrb: {
+    // OrbStruct fR (OrbStruct.h:19-25)
+    if (!(p[0] > 0)) {
+      err = "orb radius must be positive";
+      return VGN_ERR_ARG;
+    }
+    shape.push_back(p[0]);
+    return VGN_OK;
+  }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
   }
 }
@@ -602,6 +612,10 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mx.z = z0 > zn ? z0 : zn;
     return;
   }
+  case kOrb:  // UnplacedOrb::Extent (source/UnplacedOrb.cpp:58-63)
+    mn = {-r[0], -r[0], -r[0]};
+    mx = {r[0], r[0], r[0]};
+    return;
   default: mn = mx = {0, 0, 0};
   }
 }

@@ -41,31 +41,94 @@ struct Xf {
   double r[9];
 };
 
-// TopMatrixImpl with a cached global matrix at every level (NavStateIndex.h:232-265):
-// identity if the matrix flags are clear, else the stored translation/rotation.
-__device__ __forceinline__ void top_matrix(const GeomView &g, uint32_t ni, Xf &m)
+// Transformation3D::MultiplyFromRight (Transformation3D.h:878-946) on a transform with its
+// identity / translation / rotation flags (flags: kXfTrans | kXfRot, none = identity)
+__device__ __forceinline__ void xf_mul_right(Xf &m, int &mflags, const double *rt, const double *rr, int rflags)
+{
+  if (rflags == 0) return;
+  if (rflags & kXfTrans) {
+    mflags |= kXfTrans;
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+      m.t[row] += m.r[3 * row + 0] * rt[0];
+      m.t[row] += m.r[3 * row + 1] * rt[1];
+      m.t[row] += m.r[3 * row + 2] * rt[2];
+    }
+  }
+  if (rflags & kXfRot) {
+    mflags |= kXfRot;
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+      double *r      = m.r + 3 * row;
+      const double x = r[0], y = r[1], z = r[2];
+      r[0] = x * rr[0];
+      r[1] = x * rr[1];
+      r[2] = x * rr[2];
+      r[0] += y * rr[3];
+      r[1] += y * rr[4];
+      r[2] += y * rr[5];
+      r[0] += z * rr[6];
+      r[1] += z * rr[7];
+      r[2] += z * rr[8];
+    }
+  }
+}
+
+__device__ __forceinline__ void xf_set_identity(Xf &m)
 {
   m.t[0] = m.t[1] = m.t[2] = 0.;
   m.r[0] = 1.; m.r[1] = 0.; m.r[2] = 0.;
   m.r[3] = 0.; m.r[4] = 1.; m.r[5] = 0.;
   m.r[6] = 0.; m.r[7] = 0.; m.r[8] = 1.;
+}
+
+// TopMatrixImpl (NavStateIndex.h:232-265): the global-to-local matrix of a state.  Levels
+// without a cached matrix (deeper than the table's cache depth) contribute their placement
+// transforms, t.MultiplyFromRight(trans), walking up to the first cached ancestor, whose
+// matrix is applied last; with every level cached the first node's matrix is the result.
+__device__ __forceinline__ void top_matrix(const GeomView &g, uint32_t ni, Xf &m)
+{
+  xf_set_identity(m);
+  int mflags = 0;
   if (ni == 0) return;
-  const uint32_t w      = ni_word(g, ni + 2);
-  const uint32_t hasm   = (w >> 8) & 0xffu;
-  const uint32_t nd     = w >> 16;
+  uint32_t w    = ni_word(g, ni + 2);
+  uint32_t hasm = (w >> 8) & 0xffu;
+  while (!(hasm & 0x04u)) {  // no cached matrix at this level
+    const int pv = ni_top(g, ni);
+    Xf t;
+    const double *x = &g.pv[pv].xf.t[0];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) t.t[i] = __ldg(x + i);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) t.r[i] = __ldg(x + 3 + i);
+    int tflags = __ldg(&g.pv[pv].xf_flags);
+    xf_mul_right(t, tflags, m.t, m.r, mflags);
+    m      = t;
+    mflags = tflags;
+    ni     = ni_pop(g, ni);
+    if (ni == 0) return;
+    w    = ni_word(g, ni + 2);
+    hasm = (w >> 8) & 0xffu;
+  }
   if ((hasm & 0x03u) == 0) return;
-  uint32_t idx = ni + 3 + nd + ((nd + 1) & 1);
+  const uint32_t nd = w >> 16;
+  uint32_t idx      = ni + 3 + nd + ((nd + 1) & 1);
   if ((idx * 4) % 8 != 0) idx += 1;
   const double *a = reinterpret_cast<const double *>(g.navind + idx);
+  Xf t;
+  xf_set_identity(t);
+  int tflags = ((hasm & 0x02u) ? kXfTrans : 0) | ((hasm & 0x01u) ? kXfRot : 0);  // Transformation3D::Set
   if (hasm & 0x02u) {
-    m.t[0] = __ldg(a + 0);
-    m.t[1] = __ldg(a + 1);
-    m.t[2] = __ldg(a + 2);
+    t.t[0] = __ldg(a + 0);
+    t.t[1] = __ldg(a + 1);
+    t.t[2] = __ldg(a + 2);
   }
   if (hasm & 0x01u) {
 #pragma unroll
-    for (int i = 0; i < 9; ++i) m.r[i] = __ldg(a + 3 + i);
+    for (int i = 0; i < 9; ++i) t.r[i] = __ldg(a + 3 + i);
   }
+  xf_mul_right(t, tflags, m.t, m.r, mflags);
+  m = t;
 }
 
 // Transform<kGeneric,kGeneric> (Transformation3D.h:663-673, 729-735, 746-770)

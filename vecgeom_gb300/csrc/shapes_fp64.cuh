@@ -2229,6 +2229,86 @@ __device__ __forceinline__ double pcon_safe_out(const double *t, D3 p)
   return pcon_has_phi(t) ? pcon_safe_out_t<true>(t, p) : pcon_safe_out_t<false>(t, p);
 }
 
+// ---------------------------------------------------------------- Orb
+// kernel/OrbImplementation.h:60-225; row = fR (OrbStruct.h:19)
+__device__ __forceinline__ double orb_mag2(D3 p) { return p.x * p.x + p.y * p.y + p.z * p.z; }
+
+__device__ __forceinline__ bool orb_contains(const double *o, D3 p)  // GenericKernelForContainsAndInside
+{
+  const double rad2 = orb_mag2(p);
+  const double tolR = o[0] + kTolerance;
+  return !(rad2 >= tolR * tolR);
+}
+
+__device__ __forceinline__ int orb_inside(const double *o, D3 p)
+{
+  const double rad2 = orb_mag2(p);
+  double tolR       = o[0] - kTolerance;
+  const bool cin    = rad2 <= tolR * tolR;
+  tolR              = o[0] + kTolerance;
+  const bool cout   = rad2 >= tolR * tolR;
+  return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+}
+
+// DetectIntersectionAndCalculateDistance (OrbImplementation.h:197-220)
+__device__ __forceinline__ bool orb_intersect(const double *o, D3 p, D3 d, bool toIn, double &dist)
+{
+  const double rad2    = orb_mag2(p);
+  const double pDotV3D = p.x * d.x + p.y * d.y + p.z * d.z;
+  const double c       = rad2 - o[0] * o[0];
+  const double d2      = pDotV3D * pDotV3D - c;
+  if (toIn) {
+    if (d2 >= 0. && pDotV3D <= 0.) {
+      dist = -pDotV3D - sqrt(fabs(d2));
+      return true;
+    }
+    return false;
+  }
+  if (d2 >= 0.) {
+    dist = -pDotV3D + sqrt(fabs(d2));
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ double orb_dist_in(const double *o, D3 p, D3 d)
+{
+  const double rad = sqrt(orb_mag2(p));
+  if (rad < o[0] - kTolerance) return -1.;
+  const double pDotV3D = p.x * d.x + p.y * d.y + p.z * d.z;
+  if (rad >= o[0] - kTolerance && rad <= o[0] + kTolerance && pDotV3D < 0.) return 0.;
+  double dist = kInfLength;
+  return orb_intersect(o, p, d, true, dist) ? dist : kInfLength;
+}
+
+__device__ __forceinline__ double orb_dist_out(const double *o, D3 p, D3 d)
+{
+  const double rad = sqrt(orb_mag2(p));
+  if (rad > o[0] + kTolerance) return -1.;
+  const double pDotV3D = p.x * d.x + p.y * d.y + p.z * d.z;
+  if (rad >= o[0] - kTolerance && rad <= o[0] + kTolerance && pDotV3D > 0.) return 0.;
+  double dist = kInfLength;
+  return orb_intersect(o, p, d, false, dist) ? dist : kInfLength;
+}
+
+__device__ __forceinline__ double orb_safe_in(const double *o, D3 p)
+{
+  const double rad = sqrt(orb_mag2(p));
+  double safety    = rad - o[0];
+  if (rad < o[0] - kTolerance) return -1.;
+  if (rad > o[0] - kTolerance && rad < o[0] + kTolerance) safety = 0.;
+  return safety;
+}
+
+__device__ __forceinline__ double orb_safe_out(const double *o, D3 p)
+{
+  const double rad = sqrt(orb_mag2(p));
+  double safety    = o[0] - rad;
+  if (rad > o[0] + kTolerance) return -1.;
+  if (rad > o[0] - kTolerance && rad < o[0] + kTolerance) safety = 0.;
+  return safety;
+}
+
 // ---------------------------------------------------------------- dispatch
 __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
 {
@@ -2240,6 +2320,7 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   case kTrapezoid: return trap_dist_in(r, p, d);
   case kSphere: return sphere_dist_in(r, p, d);
   case kPolycone: return pcon_dist_in(r, p, d);
+  case kOrb: return orb_dist_in(r, p, d);
   }
   return kInfLength;
 }
@@ -2254,6 +2335,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   case kTrapezoid: return trap_dist_out(r, p, d);
   case kSphere: return sphere_dist_out(r, p, d);
   case kPolycone: return pcon_dist_out(r, p, d);
+  case kOrb: return orb_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -2268,6 +2350,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   case kTrapezoid: return trap_safe_in(r, p);
   case kSphere: return sphere_safe_in(r, p);
   case kPolycone: return pcon_safe_in(r, p);
+  case kOrb: return orb_safe_in(r, p);
   }
   return kInfLength;
 }
@@ -2282,6 +2365,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   case kTrapezoid: return trap_safe_out(r, p);
   case kSphere: return sphere_safe_out(r, p);
   case kPolycone: return pcon_safe_out(r, p);
+  case kOrb: return orb_safe_out(r, p);
   }
   return 0.;
 }
@@ -2296,6 +2380,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   case kTrapezoid: return trap_contains(r, p);
   case kSphere: return sphere_contains(r, p);
   case kPolycone: return pcon_contains(r, p);
+  case kOrb: return orb_contains(r, p);
   }
   return false;
 }
@@ -2310,6 +2395,7 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   case kTrapezoid: return trap_inside(r, p);
   case kSphere: return sphere_inside(r, p);
   case kPolycone: return pcon_inside(r, p);
+  case kOrb: return orb_inside(r, p);
   }
   return kOutsideE;
 }

@@ -272,12 +272,18 @@ const char *vgn_version(void) { return "vgnav-gb300 0.1 (sm_103a)"; }
 
 int vgn_geometry_create(const vgn_geometry_desc *desc, int device, vgn_geometry **out)
 {
+  return vgn_geometry_create_with_cache_depth(desc, device, 0, out);
+}
+
+int vgn_geometry_create_with_cache_depth(const vgn_geometry_desc *desc, int device, int32_t cache_depth,
+                                         vgn_geometry **out)
+{
   if (!desc || !out) return fail(VGN_ERR_ARG, "null argument");
   *out = nullptr;
   vgn_geometry *g = new (std::nothrow) vgn_geometry();
   if (!g) return fail(VGN_ERR_NOMEM, "host allocation failed");
   std::string err;
-  int rc = vgn::build_host_geometry(*desc, g->host, err);
+  int rc = vgn::build_host_geometry(*desc, g->host, err, cache_depth);
   if (rc) {
     delete g;
     return fail(rc, err);
@@ -817,7 +823,10 @@ int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, dou
   // geometry do not share it
   const int kbits  = g->sort_kbits[mixed ? 1 : 0];
   uint32_t *sort   = nullptr, *perm = nullptr;
-  if (kbits > 0 && n <= (int64_t)UINT32_MAX) {
+  // small batches walk unbinned: the histogram scan over up to 2^21 bins would cost more
+  // than the warp coherence it buys
+  constexpr int64_t kWalkBinMin = 32768;
+  if (kbits > 0 && n >= kWalkBinMin && n <= (int64_t)UINT32_MAX) {
     const size_t words = vgn::bin_scratch_words(n, kbits) + (size_t)n;
     if (pool_alloc(g->device, words * sizeof(uint32_t), s, reinterpret_cast<void **>(&sort)) != cudaSuccess) {
       cudaGetLastError();

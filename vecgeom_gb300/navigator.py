@@ -95,7 +95,9 @@ class NavStatePool:
 class Geometry:
     """A closed geometry resident on one GPU (vgn_geometry)."""
 
-    def __init__(self, desc: GeometryDescription, device: int = 0):
+    def __init__(self, desc: GeometryDescription, device: int = 0, cache_depth: int = 0):
+        """Close `desc` and make it resident on `device`; `cache_depth` > 0 caches global
+        matrices only down to that many levels (GeoManager::SetTransformationCacheDepth)."""
         L = N.lib()
         self._keep = [np.ascontiguousarray(desc.lv_shape, dtype=np.int32),
                       np.ascontiguousarray(desc.lv_param_offset, dtype=np.int32),
@@ -107,7 +109,7 @@ class Geometry:
         d = N.GeometryDesc(desc.n_logical, k[0].ctypes.data, k[1].ctypes.data, k[2].ctypes.data, k[2].shape[0],
                            desc.n_placed, k[3].ctypes.data, k[4].ctypes.data, k[5].ctypes.data, desc.world_placed)
         h = C.c_void_p()
-        N.check(L.vgn_geometry_create(C.byref(d), int(device), C.byref(h)))
+        N.check(L.vgn_geometry_create_with_cache_depth(C.byref(d), int(device), int(cache_depth), C.byref(h)))
         self.handle = h
         self.desc = desc
         self.device = device

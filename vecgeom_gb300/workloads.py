@@ -22,8 +22,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE = range(7)
-SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone"]
+BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB = range(8)
+SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb"]
 
 K_PI = 3.14159265358979323846
 K_TWO_PI = 2.0 * K_PI
@@ -298,6 +298,42 @@ def nested_geometry(seed: int = 11) -> GeometryDescription:
     return b.build()
 
 
+def deep_geometry(seed: int = 12) -> GeometryDescription:
+    """Five-level geometry for transformation-cache tests: a world box (half 600 mm) holding
+    8 sector boxes (half 250 mm, 2x2x2 grid), each holding 4 module boxes (half 75 mm), each
+    holding 2 cells alternating Box and Tube, each cell holding one crystal box -- levels 0
+    (world) to 4 (crystal).  Every placement is rotated by small Euler angles (within 10
+    degrees), so each level's global matrix is a full rotation while no volume overlaps its
+    neighbours or leaves its mother."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = GeometryBuilder()
+    world = b.logical(BOX, (600.0, 600.0, 600.0))
+    rot = lambda: (rng.uniform(-10, 10), rng.uniform(0, 10), rng.uniform(-10, 10))
+    sectors = []
+    for i in range(8):
+        sector = b.logical(BOX, (250.0, 250.0, 250.0))
+        for m in range(4):
+            module = b.logical(BOX, (75.0, 75.0, 75.0))
+            for c in range(2):
+                if c == 0:
+                    cell = b.logical(BOX, tuple(rng.uniform(22.0, 28.0, 3)))
+                else:
+                    cell = b.logical(TUBE, (float(rng.uniform(2.0, 6.0)), float(rng.uniform(22.0, 28.0)),
+                                            float(rng.uniform(22.0, 28.0)), 0.0, K_TWO_PI))
+                crystal = b.logical(BOX, tuple(rng.uniform(9.0, 12.0, 3)))
+                b.place(crystal, cell, transform_euler(*(rng.uniform(-2, 2, 3)), *rot()))
+                b.place(cell, module, transform_euler(-38.0 + 76.0 * c, *(rng.uniform(-2, 2, 2)), *rot()))
+            mx, my = -100.0 + 200.0 * (m % 2), -100.0 + 200.0 * (m // 2)
+            b.place(module, sector, transform_euler(mx, my, float(rng.uniform(-50, 50)), *rot()))
+        sectors.append(sector)
+    for i, sector in enumerate(sectors):
+        c = np.array([-300.0 + 600.0 * ((i >> 2) & 1), -300.0 + 600.0 * ((i >> 1) & 1), -300.0 + 600.0 * (i & 1)])
+        c = c + rng.uniform(-5, 5, 3)
+        b.place(sector, world, transform_euler(c[0], c[1], c[2], rng.uniform(-8, 8), rng.uniform(0, 5), 0.0))
+    b.place_world(world)
+    return b.build()
+
+
 def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_limit: float = 1e4) -> TrackBatch:
     """Points uniform in a cube of half-length `half`, isotropic directions, unlocated states."""
     rng = np.random.Generator(np.random.PCG64(seed_points))
@@ -308,8 +344,10 @@ def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_l
 
 
 # ---------------------------------------------------------------- mixed shapes
-# Shape types the library implements, in enum order.
+# The shape types of the 8192-daughter mixed-shape benchmark geometry (its definition: seven
+# types), and every shape type the library implements (for parity geometries).
 IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE)
+ALL_SHAPES = IMPLEMENTED_SHAPES + (ORB,)
 MIXED_WORLD = 2000.0
 MIXED_GRID = (16, 16, 32)  # 8192 cells of 250 x 250 x 125 mm
 MIXED_JITTER = 5.0
@@ -384,11 +422,14 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
         if sections and rng.uniform() < 0.75:
             sphi, dphi = float(rng.uniform(-K_PI, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
         return (sphi, dphi, 4.0, *z, *rmin, *rmax), np.array([max(rmax), max(rmax), h])
+    if shape == ORB:
+        r = u()
+        return (r,), np.array([r, r, r])
     raise ValueError(f"shape {shape} not implemented")
 
 
 _LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
-                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15))}
+                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15)), ORB: (0,)}
 
 
 def shape_bbox(shape: int, params):
