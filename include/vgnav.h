@@ -43,7 +43,9 @@ enum vgn_shape_type {
   VGN_TRAPEZOID = 4, /* params: dz, theta, phi, dy1, dx1, dx2, alpha1, dy2, dx3, dx4, alpha2 (UnplacedTrapezoid.h) */
   VGN_SPHERE    = 5, /* params: rmin, rmax, sphi, dphi, stheta, dtheta (UnplacedSphere.h) */
   VGN_POLYCONE  = 6, /* params: sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] (UnplacedPolycone.h:79) */
-  VGN_ORB       = 7  /* params: r                                 (UnplacedOrb.h)       */
+  VGN_ORB       = 7, /* params: r                                 (UnplacedOrb.h)       */
+  VGN_CUTTUBE   = 8  /* params: rmin, rmax, dz, sphi, dphi, bottom normal bx, by, bz, top normal
+                        tx, ty, tz                                (UnplacedCutTube.h:54-57) */
 };
 
 /* ---- shape operations for vgn_shape_batch ------------------------------- */

@@ -57,6 +57,7 @@
 #include "VecGeom/volumes/PlacedVolume.h"
 #include "VecGeom/volumes/UnplacedBox.h"
 #include "VecGeom/volumes/UnplacedCone.h"
+#include "VecGeom/volumes/UnplacedCutTube.h"
 #include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
@@ -133,6 +134,11 @@ inline int shape_row(vecgeom::VUnplacedVolume const *u, std::vector<double> &p)
     p = {s->GetInnerRadius(),     s->GetOuterRadius(),     s->GetStartPhiAngle(),
          s->GetDeltaPhiAngle(),   s->GetStartThetaAngle(), s->GetDeltaThetaAngle()};
     return VGN_SPHERE;
+  }
+  if (auto c = dynamic_cast<UnplacedCutTube const *>(u)) {  // the cut planes' unit normals
+    const auto b = c->BottomNormal(), t = c->TopNormal();
+    p = {c->rmin(), c->rmax(), c->z(), c->sphi(), c->dphi(), b.x(), b.y(), b.z(), t.x(), t.y(), t.z()};
+    return VGN_CUTTUBE;
   }
   if (auto o = dynamic_cast<UnplacedOrb const *>(u)) {
     p = {o->GetRadius()};

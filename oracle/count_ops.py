@@ -45,6 +45,7 @@ KERNEL_WEIGHTS = [
     [55, 50, 10, 10, 8, 8],       # SphereImplementation.h:138-479
     [270, 240, 75, 75, 36, 42],   # PolyconeImplementation.h:189-517 (three cone sections)
     [20, 20, 8, 8, 6, 8],         # OrbImplementation.h:102-220
+    [110, 60, 25, 25, 20, 24],    # CutTubeImplementation.h:158-290 (tube + two cut planes)
 ]
 
 

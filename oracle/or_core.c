@@ -269,6 +269,7 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_TRAP: return 11;
   case OR_SPHERE: return 6;
   case OR_ORB: return 1;
+  case OR_CUTTUBE: return 11;
   case OR_POLYCONE: { /* sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] */
     int nz;
     if (avail < 3 || !(p[2] >= 2 && p[2] <= 4096)) return -1;

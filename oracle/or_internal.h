@@ -148,6 +148,17 @@ typedef struct { /* PolyconeStruct.h:24-37: z planes and one ConeStruct per sect
 
 typedef struct { double r; } or_orb; /* OrbStruct.h:19 fR */
 
+typedef struct { /* Plane (VecGeom/volumes/Plane.h:22-95): unit normal and signed distance */
+  double n[3], d;
+} or_plane;
+
+typedef struct { /* CutTubeStruct.h:21-46 */
+  double dz;            /* fDz */
+  or_tube tube;         /* fTubeStruct: the tube with an infinite half-length */
+  or_plane cut[2];      /* fCutPlanes: bottom, top */
+  double cosphi1, sinphi1, cosphi2, sinphi2, maxval;
+} or_cuttube;
+
 typedef struct {
   int type;
   int param_off;
@@ -163,6 +174,7 @@ typedef struct {
     or_sphere sph;
     or_polycone pcon;
     or_orb orb;
+    or_cuttube ctube;
   } s;
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;

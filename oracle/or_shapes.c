@@ -2657,6 +2657,252 @@ static double orb_safe_out(const or_orb *o, v3 p) /* OrbImplementation.h:167-181
 }
 
 /* ================================================================== */
+/* CutTube (CutTubeImplementation.h:101-290, CutTubeStruct.h:21-46, CutPlanes.h:95-170,
+ * Plane.h:44-191, source/UnplacedCutTube.cpp:128-172)                                  */
+
+/* Plane::Set(normal, origin) (Plane.h:44-51) with Vector3D::FixZeroes (Vector3D.h:298-305) */
+static void plane_set(or_plane *pl, v3 normal, v3 origin)
+{
+  v3 f = normal;
+  double inv;
+  if (fabs(f.x) < kTolerance) f.x = 0.0;
+  if (fabs(f.y) < kTolerance) f.y = 0.0;
+  if (fabs(f.z) < kTolerance) f.z = 0.0;
+  inv      = 1. / sqrt(v3_mag2(f));
+  pl->n[0] = inv * f.x;
+  pl->n[1] = inv * f.y;
+  pl->n[2] = inv * f.z;
+  pl->d    = inv * -v3_dot(f, origin);
+}
+
+static inline double plane_dist(const or_plane *pl, v3 p) /* DistPlane (Plane.h:102-107) */
+{
+  return p.x * pl->n[0] + p.y * pl->n[1] + p.z * pl->n[2] + pl->d;
+}
+
+static inline double plane_ndd(const or_plane *pl, v3 d) { return NonZero(d.x * pl->n[0] + d.y * pl->n[1] + d.z * pl->n[2]); }
+
+static double plane_dist_in(const or_plane *pl, v3 p, v3 d) /* Plane.h:131-147 */
+{
+  double ndd = plane_ndd(pl, d), saf = plane_dist(pl, p);
+  if (ndd < 0. && saf > -kTolerance) return -saf / ndd;
+  return -kInfLength;
+}
+
+static double plane_dist_out(const or_plane *pl, v3 p, v3 d) /* Plane.h:152-171 */
+{
+  double ndd = plane_ndd(pl, d), saf = plane_dist(pl, p), distance = kInfLength;
+  int valid = ndd > 0. && saf < kTolerance;
+  if (saf > kTolerance) distance = -kInfLength;
+  if (valid) distance = -saf / ndd;
+  return distance;
+}
+
+static int cutplanes_contains(const or_cuttube *c, v3 p) /* CutPlanes.h:101-105 */
+{
+  return plane_dist(&c->cut[0], p) < 0. && plane_dist(&c->cut[1], p) < 0.;
+}
+
+static int cutplanes_inside(const or_cuttube *c, v3 p) /* CutPlanes.h:107-119 */
+{
+  double d0 = plane_dist(&c->cut[0], p), d1 = plane_dist(&c->cut[1], p);
+  int inside = (d0 < 0.0 && d1 < 0.0) ? kInsideE : kOutsideE;
+  if (fabs(d0) < kTolerance || fabs(d1) < kTolerance) inside = kSurfaceE;
+  return inside;
+}
+
+static double cutplanes_dist_in(const or_cuttube *c, v3 p, v3 d) /* CutPlanes.h:121-136 */
+{
+  double d0 = plane_dist_in(&c->cut[0], p, d), d1;
+  if (d.x * c->cut[0].n[0] + d.y * c->cut[0].n[1] + d.z * c->cut[0].n[2] > 0.) d0 = -kInfLength;
+  d1 = plane_dist_in(&c->cut[1], p, d);
+  if (d.x * c->cut[1].n[0] + d.y * c->cut[1].n[1] + d.z * c->cut[1].n[2] > 0.) d1 = -kInfLength;
+  return or_max(d0, d1);
+}
+
+static double cutplanes_dist_out(const or_cuttube *c, v3 p, v3 d) /* CutPlanes.h:138-146 */
+{
+  return or_min(plane_dist_out(&c->cut[0], p, d), plane_dist_out(&c->cut[1], p, d));
+}
+
+static double cutplanes_safe_in(const or_cuttube *c, v3 p) /* CutPlanes.h:148-156 */
+{
+  return or_max(plane_dist(&c->cut[0], p), plane_dist(&c->cut[1], p));
+}
+
+static double cutplanes_safe_out(const or_cuttube *c, v3 p) /* CutPlanes.h:158-166 */
+{
+  return or_min(-plane_dist(&c->cut[0], p), -plane_dist(&c->cut[1], p));
+}
+
+/* Vector3D::Unit (Vector3D.h:284-290) */
+static v3 v3_unit(v3 a)
+{
+  double m = sqrt(v3_mag2(a) + 2.2250738585072014e-308); /* + kMinimum */
+  return v3_make(a.x / m, a.y / m, a.z / m);
+}
+
+/* UnplacedCutTube(rmin, rmax, z, sphi, dphi, bx, by, bz, tx, ty, tz) -> CutTubeStruct
+ * (UnplacedCutTube.h:54-70, CutTubeStruct.h:34-46) */
+static int cuttube_init(or_cuttube *c, const double *a, char *err, int errlen)
+{
+  double tp[5];
+  v3 bn = v3_make(a[5], a[6], a[7]), tn = v3_make(a[8], a[9], a[10]);
+  if (bn.z >= 0 || tn.z <= 0) {
+    set_err(err, errlen, "cut tube: illegal normal direction for cut planes");
+    return -1;
+  }
+  tp[0] = a[0];
+  tp[1] = a[1];
+  tp[2] = kInfLength; /* the tube of a cut tube has an infinite half-length */
+  tp[3] = a[3];
+  tp[4] = a[4];
+  if (tube_init(&c->tube, tp, err, errlen)) return -1;
+  c->dz = a[2];
+  plane_set(&c->cut[0], v3_unit(bn), v3_make(0., 0., -a[2]));
+  plane_set(&c->cut[1], v3_unit(tn), v3_make(0., 0., a[2]));
+  c->cosphi1 = cos(a[3]);
+  c->sinphi1 = sin(a[3]);
+  c->cosphi2 = cos(a[3] + a[4]);
+  c->sinphi2 = sin(a[3] + a[4]);
+  c->maxval  = or_max(a[1], a[2]);
+  return 0;
+}
+
+static int cuttube_contains(const or_cuttube *c, v3 p) /* CutTubeImplementation.h:101-113 */
+{
+  if (!cutplanes_contains(c, p)) return 0; /* EarlyReturnAllowed */
+  return tube_contains(&c->tube, p);
+}
+
+static int cuttube_inside(const or_cuttube *c, v3 p) /* CutTubeImplementation.h:115-130 */
+{
+  int incp = cutplanes_inside(c, p), inside;
+  if (incp == kOutsideE) return kOutsideE; /* MaskFull(inside_cutplanes == kOutside) */
+  inside = tube_inside(&c->tube, p);
+  if (incp == kOutsideE || (incp == kSurfaceE && inside != kOutsideE)) inside = incp;
+  return inside;
+}
+
+/* DistanceToInKernel (CutTubeImplementation.h:158-245) */
+static double cuttube_dist_in_kernel(const or_cuttube *c, v3 p, v3 d, double stepmax)
+{
+  double distance = kInfLength, dplanes, safplanes, dexit, dtube;
+  int incp, instart, hitplanes, done, inside;
+  v3 prop;
+  incp    = cutplanes_inside(c, p);
+  instart = tube_inside(&c->tube, p);
+  if (incp == kOutsideE || (incp == kSurfaceE && instart != kOutsideE)) instart = incp;
+  if (instart == kInsideE) distance = -1.;
+  dplanes   = cutplanes_dist_in(c, p, d);
+  safplanes = cutplanes_safe_in(c, p);
+  hitplanes = fabs(dplanes) < stepmax && safplanes > -kTolerance;
+  if (incp != kInsideE && !hitplanes) return distance;
+  prop = p;
+  if (!hitplanes) dplanes = 0.;
+  if (hitplanes) {
+    prop = v3_add(prop, v3_scale(dplanes, d));
+    incp = cutplanes_inside(c, prop);
+  }
+  done = incp == kOutsideE;
+  done |= instart == kInsideE;
+  if (done) return distance;
+  instart = tube_inside(&c->tube, prop);
+  inside  = hitplanes && instart != kOutsideE;
+  if (inside && !done) distance = dplanes;
+  done |= inside;
+  if (done) {
+    if (fabs(distance) < kTolerance) distance = 0.;
+    return distance;
+  }
+  dexit = cutplanes_dist_out(c, prop, d);
+  dtube = tube_dist_in_kernel(&c->tube, prop, d);
+  if (dtube < 0.) dtube = 0.;
+  if (dexit < dtube) dtube = kInfLength;
+  if (!done && (dtube + dplanes) < stepmax) distance = dtube + dplanes;
+  return distance;
+}
+
+/* DistanceToIn with the far-point pre-move (CutTubeImplementation.h:132-156) */
+static double cuttube_dist_in(const or_cuttube *c, v3 pt, v3 d, double stepmax)
+{
+  v3 p          = pt;
+  double ptDist = sqrt(v3_mag2(p)), distToMove = 0., distance;
+  const double order = 100.;
+  if (ptDist > order * c->maxval) {
+    distToMove = ptDist - order * c->maxval;
+    p          = v3_add(p, v3_scale(distToMove, d));
+  }
+  distance = cuttube_dist_in_kernel(c, p, d, stepmax);
+  distance += distToMove;
+  return distance;
+}
+
+static double cuttube_dist_out(const or_cuttube *c, v3 p, v3 d) /* CutTubeImplementation.h:247-259 */
+{
+  double distance = cutplanes_dist_out(c, p, d);
+  double dtube    = tube_dist_out(&c->tube, p, d);
+  if (dtube < distance) distance = dtube;
+  return distance;
+}
+
+static double cuttube_safe_in(const or_cuttube *c, v3 p) /* CutTubeImplementation.h:261-269 */
+{
+  double safety = cutplanes_safe_in(c, p), saftube = tube_safe_in(&c->tube, p);
+  if (saftube > safety) safety = saftube;
+  return safety;
+}
+
+static double cuttube_safe_out(const or_cuttube *c, v3 p) /* CutTubeImplementation.h:271-279 */
+{
+  double safety = cutplanes_safe_out(c, p), saftube = tube_safe_out(&c->tube, p);
+  if (saftube < safety) safety = saftube;
+  return safety;
+}
+
+/* ZlimitTop / ZlimitBottom (UnplacedCutTube.h:135-147) */
+static double cuttube_zlimit(const or_cuttube *c, int top, double rval, double phival)
+{
+  const double *n = c->cut[top].n;
+  return (top ? c->dz : -c->dz) - (rval / n[2]) * (n[0] * cos(phival) + n[1] * sin(phival));
+}
+
+static void cuttube_extent(const or_cuttube *c, v3 *mn, v3 *mx) /* source/UnplacedCutTube.cpp:128-172 */
+{
+  const or_tube *t = &c->tube;
+  const double *bn = c->cut[0].n, *tn = c->cut[1].n;
+  double dztop    = t->rmax * sqrt(1. - tn[2] * tn[2]) / tn[2];
+  double dzbottom = -t->rmax * sqrt(1. - bn[2] * bn[2]) / bn[2];
+  *mn = v3_make(-t->rmax, -t->rmax, -c->dz - dzbottom);
+  *mx = v3_make(t->rmax, t->rmax, c->dz + dztop);
+  if (t->dphi == kTwoPi) return;
+  if (!wedge_contains(&t->w, v3_make(-tn[0], -tn[1], 0.))) {
+    mx->z = or_max(cuttube_zlimit(c, 1, t->rmax, t->sphi), cuttube_zlimit(c, 1, t->rmax, t->sphi + t->dphi));
+    mx->z = or_max(mx->z, or_max(cuttube_zlimit(c, 1, t->rmin, t->sphi), cuttube_zlimit(c, 1, t->rmin, t->sphi + t->dphi)));
+  }
+  if (!wedge_contains(&t->w, v3_make(-bn[0], -bn[1], 0.))) {
+    mn->z = or_min(cuttube_zlimit(c, 0, t->rmax, t->sphi), cuttube_zlimit(c, 0, t->rmax, t->sphi + t->dphi));
+    mn->z = or_min(mn->z, or_min(cuttube_zlimit(c, 0, t->rmin, t->sphi), cuttube_zlimit(c, 0, t->rmin, t->sphi + t->dphi)));
+  }
+  if (!wedge_contains(&t->w, v3_make(1., 0., 0.))) {
+    mx->x = or_max(t->rmax * c->cosphi1, t->rmax * c->cosphi2);
+    mx->x = or_max(mx->x, or_max(t->rmin * c->cosphi1, t->rmin * c->cosphi2));
+  }
+  if (!wedge_contains(&t->w, v3_make(-1., 0., 0.))) {
+    mn->x = or_min(t->rmax * c->cosphi1, t->rmax * c->cosphi2);
+    mn->x = or_min(mn->x, or_min(t->rmin * c->cosphi1, t->rmin * c->cosphi2));
+  }
+  if (!wedge_contains(&t->w, v3_make(0., 1., 0.))) {
+    mx->y = or_max(t->rmax * c->sinphi1, t->rmax * c->sinphi2);
+    mx->y = or_max(mx->y, or_max(t->rmin * c->sinphi1, t->rmin * c->sinphi2));
+  }
+  if (!wedge_contains(&t->w, v3_make(0., -1., 0.))) {
+    mn->y = or_min(t->rmax * c->sinphi1, t->rmax * c->sinphi2);
+    mn->y = or_min(mn->y, or_min(t->rmin * c->sinphi1, t->rmin * c->sinphi2));
+  }
+}
+
+/* ================================================================== */
 
 int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
 {
@@ -2676,6 +2922,7 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
   case OR_ORB:
     lv->s.orb.r = p[0];
     return 0;
+  case OR_CUTTUBE: return cuttube_init(&lv->s.ctube, p, err, errlen);
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -2697,6 +2944,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
     *mn = v3_make(-lv->s.orb.r, -lv->s.orb.r, -lv->s.orb.r);
     *mx = v3_make(lv->s.orb.r, lv->s.orb.r, lv->s.orb.r);
     return;
+  case OR_CUTTUBE: cuttube_extent(&lv->s.ctube, mn, mx); return;
   }
 }
 
@@ -2716,6 +2964,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_SPHERE: return sphere_dist_in(&lv->s.sph, p, d);
   case OR_POLYCONE: return polycone_dist_in(&lv->s.pcon, p, d);
   case OR_ORB: return orb_dist_in(&lv->s.orb, p, d);
+  case OR_CUTTUBE: return cuttube_dist_in(&lv->s.ctube, p, d, stepmax);
   }
   return kInfLength;
 }
@@ -2733,6 +2982,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_SPHERE: return sphere_dist_out(&lv->s.sph, p, d);
   case OR_POLYCONE: return polycone_dist_out(&lv->s.pcon, p, d);
   case OR_ORB: return orb_dist_out(&lv->s.orb, p, d);
+  case OR_CUTTUBE: return cuttube_dist_out(&lv->s.ctube, p, d);
   }
   return -1.;
 }
@@ -2749,6 +2999,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_SPHERE: return sphere_safe_in(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_safe_in(&lv->s.pcon, p);
   case OR_ORB: return orb_safe_in(&lv->s.orb, p);
+  case OR_CUTTUBE: return cuttube_safe_in(&lv->s.ctube, p);
   }
   return kInfLength;
 }
@@ -2765,6 +3016,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_SPHERE: return sphere_safe_out(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_safe_out(&lv->s.pcon, p);
   case OR_ORB: return orb_safe_out(&lv->s.orb, p);
+  case OR_CUTTUBE: return cuttube_safe_out(&lv->s.ctube, p);
   }
   return 0.;
 }
@@ -2781,6 +3033,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_SPHERE: return sphere_contains(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_contains(&lv->s.pcon, p);
   case OR_ORB: return orb_contains(&lv->s.orb, p);
+  case OR_CUTTUBE: return cuttube_contains(&lv->s.ctube, p);
   }
   return 0;
 }
@@ -2797,6 +3050,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_SPHERE: return sphere_inside(&lv->s.sph, p);
   case OR_POLYCONE: return polycone_inside(&lv->s.pcon, p);
   case OR_ORB: return orb_inside(&lv->s.orb, p);
+  case OR_CUTTUBE: return cuttube_inside(&lv->s.ctube, p);
   }
   return kOutsideE;
 }

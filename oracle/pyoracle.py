@@ -23,12 +23,12 @@ OP_DIST_IN, OP_DIST_OUT, OP_SAFE_IN, OP_SAFE_OUT, OP_CONTAINS, OP_INSIDE = range
 class Counters(C.Structure):
     _fields_ = [("node_slab", C.c_uint64), ("prim_slab", C.c_uint64), ("node_safety", C.c_uint64),
                 ("prim_safety", C.c_uint64), ("prim_contains", C.c_uint64), ("transforms", C.c_uint64),
-                ("kernel", (C.c_uint64 * 6) * 8)]
+                ("kernel", (C.c_uint64 * 6) * 9)]
 
     def as_dict(self) -> dict:
         d = {k: int(getattr(self, k)) for k in ("node_slab", "prim_slab", "node_safety", "prim_safety",
                                                 "prim_contains", "transforms")}
-        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(8)]
+        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(9)]
         return d
 
 
@@ -112,10 +112,11 @@ class OracleGeometry:
         L.or_geom_bvh_arrays(self.h, lv, _p(prim), _p(off), _p(nch), _p(nodes), _p(prims))
         return dict(depth=d.value, prim_id=prim, offset=off, nchild=nch, nodes=nodes, prims=prims)
 
-    def shape(self, lv, op, x, y, z, dx=None, dy=None, dz=None):
+    def shape(self, lv, op, x, y, z, dx=None, dy=None, dz=None, stepmax=None):
         n = x.shape[0]
         out = np.zeros(n)
-        rc = lib().or_shape_batch(self.h, lv, op, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), None, _p(out))
+        sm = None if stepmax is None else np.ascontiguousarray(stepmax, np.float64)
+        rc = lib().or_shape_batch(self.h, lv, op, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(sm), _p(out))
         if rc:
             raise ValueError("bad shape query")
         return out

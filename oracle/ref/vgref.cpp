@@ -40,6 +40,7 @@
 #include "VecGeom/volumes/PlacedVolume.h"
 #include "VecGeom/volumes/UnplacedBox.h"
 #include "VecGeom/volumes/UnplacedCone.h"
+#include "VecGeom/volumes/UnplacedCutTube.h"
 #include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
@@ -98,6 +99,9 @@ VUnplacedVolume *make_shape(int type, const double *p)
   }
   case 7:
     return GeoManager::MakeInstance<UnplacedOrb>(p[0]);
+  case 8:
+    return GeoManager::MakeInstance<UnplacedCutTube>(p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9],
+                                                     p[10]);
   default:
     return nullptr;
   }

@@ -23,7 +23,7 @@ extern "C" {
 
 /* shape type ids (same numbering as the product's vgn_shape_type) */
 enum { OR_BOX = 0, OR_TUBE = 1, OR_CONE = 2, OR_TRD = 3, OR_TRAP = 4, OR_SPHERE = 5, OR_POLYCONE = 6, OR_ORB = 7,
-       OR_NSHAPES = 8 };
+       OR_CUTTUBE = 8, OR_NSHAPES = 9 };
 
 /* shape operations for or_shape_batch */
 enum { OR_OP_DIST_IN = 0, OR_OP_DIST_OUT = 1, OR_OP_SAFE_IN = 2, OR_OP_SAFE_OUT = 3, OR_OP_CONTAINS = 4, OR_OP_INSIDE = 5 };

@@ -62,6 +62,16 @@ SHAPE_SETS = [
     ("orb-testorb-b1", W.ORB, KA.ORB1),
     ("orb-large", W.ORB, (50.0,)),
     ("orb-small", W.ORB, (3.0,)),
+    # the reference's cut-tube shape tester set-ups (test/shape_tester/shape_testCutTube.cpp:23-48)
+    ("cuttube-solid", W.CUTTUBE, W.cuttube_params(0., 5., 10., 0., 2 * KA.KPI, 3 * KA.KPI / 4, KA.KPI / 3, KA.KPI / 4,
+                                                   2 * KA.KPI / 3)),
+    ("cuttube-hollow", W.CUTTUBE, W.cuttube_params(3., 5., 10., 0., 2 * KA.KPI, 3 * KA.KPI / 4, KA.KPI / 3,
+                                                    KA.KPI / 4, 2 * KA.KPI / 3)),
+    ("cuttube-sector", W.CUTTUBE, W.cuttube_params(0., 5., 10., 0., 2 * KA.KPI / 3, 3 * KA.KPI / 4, KA.KPI / 3,
+                                                    KA.KPI / 4, 2 * KA.KPI / 3)),
+    ("cuttube-hollow-sector", W.CUTTUBE, W.cuttube_params(3., 5., 10., 0., 2 * KA.KPI / 3, 3 * KA.KPI / 4,
+                                                           KA.KPI / 3, KA.KPI / 4, 2 * KA.KPI / 3)),
+    ("cuttube-large-tilted", W.CUTTUBE, W.cuttube_params(10., 40., 30., 0.5, 4.5, 2.6, 0.4, 0.45, 2.0)),
 ]
 
 

@@ -53,6 +53,7 @@ GEOMETRIES = {
     "box_grid": lambda: W.box_grid_geometry(seed=3).desc,
     "mixed": lambda: W.mixed_shape_geometry(),
     "mixed_sections": lambda: W.mixed_shape_geometry(sections=True),
+    "mixed_all_shapes": lambda: W.mixed_shape_geometry(seed=26, shapes=W.ALL_SHAPES),
     "nested": lambda: W.nested_geometry(),
 }
 

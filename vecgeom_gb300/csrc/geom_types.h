@@ -23,7 +23,8 @@ constexpr int kStackSize = 32;  // BVH::BVH_MAX_DEPTH (BVH.h:33)
 constexpr int kMaxLevels = 30;  // bound on geometry depth (relocation loops)
 
 enum ShapeType : int32_t {
-  kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kOrb = 7, kNumShapes = 8
+  kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kOrb = 7, kCutTube = 8,
+  kNumShapes = 9
 };
 
 // flags of a placement transformation (Transformation3D::SetProperties,
@@ -153,6 +154,10 @@ constexpr int kOrbSize = 1;
 // are both TubeStruct::fAlongPhi* and the wedge's; the block's last entry is fDphi)
 enum { TubeRmin = 0, TubeRmax, TubeZ, TubeRmin2, TubeRmax2, TubeTolIrmin2, TubeTolOrmin2, TubeTolIrmax2,
        TubeTolOrmax2, TubeMaxVal, TubeSphi, TubeTolOz, TubeWedge, TubeDphi = TubeWedge + 8, kTubeSize };
+// CutTube: CutTubeStruct (CutTubeStruct.h:21-46): its tube's row (infinite half-length), then
+// fDz, the bottom and top cut planes (unit normal, distance), cos/sin of phi and phi+dphi, fMaxVal
+enum { CutTubeDz = kTubeSize, CutTubeN0, CutTubeD0 = CutTubeN0 + 3, CutTubeN1, CutTubeD1 = CutTubeN1 + 3,
+       CutTubeCos1, CutTubeSin1, CutTubeCos2, CutTubeSin2, CutTubeMaxVal, kCutTubeSize };
 // Wedge block (evolution::Wedge): along vectors, normal vectors, fDPhi
 enum { WedgeA1x = 0, WedgeA1y, WedgeA2x, WedgeA2y, WedgeN1x, WedgeN1y, WedgeN2x, WedgeN2y, WedgeDPhi, kWedgeSize };
 // Cone (full phi): ConeStruct cached members

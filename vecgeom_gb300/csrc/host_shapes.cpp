@@ -3,6 +3,7 @@
 // A row holds the shape's defining parameters plus the cached members the
 // reference precomputes in its *Struct constructors, computed with the same
 // expressions so the device kernels see the same doubles.
+#include <algorithm>
 #include <cmath>
 
 #include "../../include/vgnav.h"
@@ -58,6 +59,7 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
   case kTrapezoid: return 11;
   case kSphere: return 6;
   case kOrb: return 1;
+  case kCutTube: return 11;
   case kPolycone: {  // sphi, dphi, nz, z[nz], rmin[nz], rmax[nz]
     if (n_avail < 3 || !(p[2] >= 2 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
     return 3 + 3 * (int)p[2];
@@ -383,6 +385,46 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.push_back(dphi);
     return VGN_OK;
   }
+  case kCutTube: {
+    // UnplacedCutTube(rmin, rmax, z, sphi, dphi, bx, by, bz, tx, ty, tz) -> CutTubeStruct
+    // (UnplacedCutTube.h:54-70, CutTubeStruct.h:34-46): a tube of infinite half-length, the two
+    // cut planes through (0, 0, -+z) with the normals made unit (Vector3D::Unit), then
+    // Plane::Set (Plane.h:44-51: FixZeroes, 1 / Mag)
+    if (!(p[7] < 0 && p[10] > 0)) {
+      err = "cut tube needs a bottom normal with z < 0 and a top normal with z > 0";
+      return VGN_ERR_ARG;
+    }
+    if (!(p[2] > 0)) {
+      err = "cut tube needs dz > 0";
+      return VGN_ERR_ARG;
+    }
+    const double tp[5] = {p[0], p[1], 1.7976931348623157e308, p[3], p[4]};  // kInfLength
+    std::vector<double> tube;
+    const int rc = shape_make_row(kTube, tp, 5, tube, err);
+    if (rc) return rc;
+    double r[row::kCutTubeSize];
+    std::copy(tube.begin(), tube.end(), r);
+    r[row::CutTubeDz] = p[2];
+    for (int k = 0; k < 2; ++k) {
+      const double *n0 = p + 5 + 3 * k;
+      const double m   = std::sqrt((n0[0] * n0[0] + n0[1] * n0[1] + n0[2] * n0[2]) + 2.2250738585072014e-308);
+      double f[3]      = {n0[0] / m, n0[1] / m, n0[2] / m};  // Vector3D::Unit (Vector3D.h:284-290)
+      for (int i = 0; i < 3; ++i)
+        if (std::fabs(f[i]) < kTolerance) f[i] = 0.0;
+      const double inv = 1. / std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+      const double oz  = k == 0 ? -p[2] : p[2];
+      double *n        = r + (k == 0 ? row::CutTubeN0 : row::CutTubeN1);
+      for (int i = 0; i < 3; ++i) n[i] = inv * f[i];
+      r[k == 0 ? row::CutTubeD0 : row::CutTubeD1] = inv * -(f[0] * 0. + f[1] * 0. + f[2] * oz);
+    }
+    r[row::CutTubeCos1]   = std::cos(p[3]);
+    r[row::CutTubeSin1]   = std::sin(p[3]);
+    r[row::CutTubeCos2]   = std::cos(p[3] + p[4]);
+    r[row::CutTubeSin2]   = std::sin(p[3] + p[4]);
+    r[row::CutTubeMaxVal] = p[1] > p[2] ? p[1] : p[2];
+    shape.insert(shape.end(), r, r + row::kCutTubeSize);
+    return VGN_OK;
+  }
   case kOrb: {
     // OrbStruct fR (OrbStruct.h:19-25)
     if (!(p[0] > 0)) {
@@ -399,7 +441,8 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
 bool shape_row_has_sections(int32_t type, const double *r)
 {
   switch (type) {
-  case kTube: return r[row::TubeDphi] < 2. * kPi;
+  case kTube:
+  case kCutTube: return r[row::TubeDphi] < 2. * kPi;  // a cut tube's row starts with its tube's
   case kCone: return r[row::ConeDPhi] < 2. * kPi;
   case kPolycone: {  // the polycone's phi range lives in its section cones
     const int n = (int)r[row::PconNSec];
@@ -610,6 +653,47 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     const double z0 = r[row::PconZs], zn = r[row::PconZs + n];
     mn.z = z0 > zn ? zn : z0;
     mx.z = z0 > zn ? z0 : zn;
+    return;
+  }
+  case kCutTube: {  // UnplacedCutTube::Extent (source/UnplacedCutTube.cpp:128-172)
+    const double rmax = r[row::TubeRmax], rmin = r[row::TubeRmin], sphi = r[row::TubeSphi], dphi = r[row::TubeDphi];
+    const double *w = r + row::TubeWedge, *bn = r + row::CutTubeN0, *tn = r + row::CutTubeN1, z = r[row::CutTubeDz];
+    auto vmax = [](double a, double b) { return a > b ? a : b; };
+    auto vmin = [](double a, double b) { return a < b ? a : b; };
+    auto zlim = [&](bool top, double rv, double ph) {  // ZlimitTop / ZlimitBottom (UnplacedCutTube.h:135-147)
+      const double *n = top ? tn : bn;
+      return (top ? z : -z) - (rv / n[2]) * (n[0] * std::cos(ph) + n[1] * std::sin(ph));
+    };
+    const double dztop    = rmax * std::sqrt(1. - tn[2] * tn[2]) / tn[2];
+    const double dzbottom = -rmax * std::sqrt(1. - bn[2] * bn[2]) / bn[2];
+    mn = {-rmax, -rmax, -z - dzbottom};
+    mx = {rmax, rmax, z + dztop};
+    if (dphi == kTwoPi) return;
+    const double c1 = r[row::CutTubeCos1], s1 = r[row::CutTubeSin1], c2 = r[row::CutTubeCos2], s2 = r[row::CutTubeSin2];
+    if (!wedge_contains(w, -tn[0], -tn[1])) {
+      mx.z = vmax(zlim(true, rmax, sphi), zlim(true, rmax, sphi + dphi));
+      mx.z = vmax(mx.z, vmax(zlim(true, rmin, sphi), zlim(true, rmin, sphi + dphi)));
+    }
+    if (!wedge_contains(w, -bn[0], -bn[1])) {
+      mn.z = vmin(zlim(false, rmax, sphi), zlim(false, rmax, sphi + dphi));
+      mn.z = vmin(mn.z, vmin(zlim(false, rmin, sphi), zlim(false, rmin, sphi + dphi)));
+    }
+    if (!wedge_contains(w, 1., 0.)) {
+      mx.x = vmax(rmax * c1, rmax * c2);
+      mx.x = vmax(mx.x, vmax(rmin * c1, rmin * c2));
+    }
+    if (!wedge_contains(w, -1., 0.)) {
+      mn.x = vmin(rmax * c1, rmax * c2);
+      mn.x = vmin(mn.x, vmin(rmin * c1, rmin * c2));
+    }
+    if (!wedge_contains(w, 0., 1.)) {
+      mx.y = vmax(rmax * s1, rmax * s2);
+      mx.y = vmax(mx.y, vmax(rmin * s1, rmin * s2));
+    }
+    if (!wedge_contains(w, 0., -1.)) {
+      mn.y = vmin(rmax * s1, rmax * s2);
+      mn.y = vmin(mn.y, vmin(rmin * s1, rmin * s2));
+    }
     return;
   }
   case kOrb:  // UnplacedOrb::Extent (source/UnplacedOrb.cpp:58-63)

@@ -242,13 +242,13 @@ __global__ void __launch_bounds__(256) shape_kernel_fp64(int type, const double 
                                                          const double *__restrict__ px, const double *__restrict__ py,
                                                          const double *__restrict__ pz, const double *__restrict__ dx,
                                                          const double *__restrict__ dy, const double *__restrict__ dz,
-                                                         double *__restrict__ out)
+                                                         const double *__restrict__ step_max, double *__restrict__ out)
 {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const D3 p = d3(px[i], py[i], pz[i]);
     double r;
     if (OP == VGN_OP_DISTANCE_TO_IN)
-      r = shape_dist_in(type, row, p, d3(dx[i], dy[i], dz[i]));
+      r = shape_dist_in(type, row, p, d3(dx[i], dy[i], dz[i]), step_max ? step_max[i] : kInfLength);
     else if (OP == VGN_OP_DISTANCE_TO_OUT)
       r = shape_dist_out(type, row, p, d3(dx[i], dy[i], dz[i]));
     else if (OP == VGN_OP_SAFETY_TO_IN)
@@ -444,29 +444,29 @@ cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const 
 }
 
 cudaError_t launch_shape_fp64(int op, int type, const double *row, int64_t n, const double *px, const double *py,
-                              const double *pz, const double *dx, const double *dy, const double *dz, double *out,
-                              int max_blocks, cudaStream_t s)
+                              const double *pz, const double *dx, const double *dy, const double *dz,
+                              const double *step_max, double *out, int max_blocks, cudaStream_t s)
 {
   const int block     = 256;
   const unsigned grid = grid_for(n, block, max_blocks);
   switch (op) {
   case VGN_OP_DISTANCE_TO_IN:
-    dev::shape_kernel_fp64<VGN_OP_DISTANCE_TO_IN><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    dev::shape_kernel_fp64<VGN_OP_DISTANCE_TO_IN><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, step_max, out);
     break;
   case VGN_OP_DISTANCE_TO_OUT:
-    dev::shape_kernel_fp64<VGN_OP_DISTANCE_TO_OUT><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    dev::shape_kernel_fp64<VGN_OP_DISTANCE_TO_OUT><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, step_max, out);
     break;
   case VGN_OP_SAFETY_TO_IN:
-    dev::shape_kernel_fp64<VGN_OP_SAFETY_TO_IN><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    dev::shape_kernel_fp64<VGN_OP_SAFETY_TO_IN><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, step_max, out);
     break;
   case VGN_OP_SAFETY_TO_OUT:
-    dev::shape_kernel_fp64<VGN_OP_SAFETY_TO_OUT><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    dev::shape_kernel_fp64<VGN_OP_SAFETY_TO_OUT><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, step_max, out);
     break;
   case VGN_OP_CONTAINS:
-    dev::shape_kernel_fp64<VGN_OP_CONTAINS><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    dev::shape_kernel_fp64<VGN_OP_CONTAINS><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, step_max, out);
     break;
   default:
-    dev::shape_kernel_fp64<VGN_OP_INSIDE><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, out);
+    dev::shape_kernel_fp64<VGN_OP_INSIDE><<<grid, block, 0, s>>>(type, row, n, px, py, pz, dx, dy, dz, step_max, out);
     break;
   }
   return cudaGetLastError();

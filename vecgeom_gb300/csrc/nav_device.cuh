@@ -195,13 +195,13 @@ __device__ __forceinline__ const double *pv_row(const GeomView &g, int pv, int &
 }
 
 // placed DistanceToIn / SafetyToIn / Contains (SpecializedPlacedVolImplHelper.h:118-175)
-__device__ __forceinline__ double pv_dist_in(const GeomView &g, int pv, D3 p, D3 d)
+__device__ __forceinline__ double pv_dist_in(const GeomView &g, int pv, D3 p, D3 d, double stepmax)
 {
   PvXf x;
   load_pv_xf(g, pv, x);
   int type;
   const double *row = pv_row(g, pv, type);
-  return shape_dist_in(type, row, xf_point(x.t, x.r, p), xf_dir(x.r, d));
+  return shape_dist_in(type, row, xf_point(x.t, x.r, p), xf_dir(x.r, d), stepmax);
 }
 
 __device__ __forceinline__ double pv_safe_in(const GeomView &g, int pv, D3 p)
@@ -310,7 +310,7 @@ __device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVR
         slab(q.mn, q.mx, lp, inv, tmin, tmax);
         if (tmin <= tmax && tmax >= 0.0 && tmin < step) {
           const int vol     = __ldg(&q.pv);
-          const double dist = pv_dist_in(g, vol, lp, ld);
+          const double dist = pv_dist_in(g, vol, lp, ld, step);
           if (dist < step && !(dist <= 0.0 && vol == last)) step = dist, hit = vol;
         }
       }

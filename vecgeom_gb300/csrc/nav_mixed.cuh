@@ -397,7 +397,7 @@ __device__ __forceinline__ void eval_step_candidate(const GeomView &g, const Mix
                                                     double &step, FI &stepI, int last, int &hit)
 {
   if (tmin_lo >= stepI.hi) return;
-  const double dist = pv_dist_in(g, pv, r.lp, r.ld);
+  const double dist = pv_dist_in(g, pv, r.lp, r.ld, step);
   if (dist < step && !(dist <= 0.0 && pv == last)) {
     step  = dist;
     hit   = pv;

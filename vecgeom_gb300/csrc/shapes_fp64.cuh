@@ -2309,8 +2309,146 @@ __device__ __forceinline__ double orb_safe_out(const double *o, D3 p)
   return safety;
 }
 
+// ---------------------------------------------------------------- CutTube
+// kernel/CutTubeImplementation.h:101-279 over CutPlanes (CutPlanes.h:101-166) and Plane
+// (Plane.h:102-191); row: the tube's row (infinite half-length), then row::CutTube*
+__device__ __forceinline__ double ct_plane(const double *r, int k, D3 p)  // Plane::DistPlane
+{
+  const double *n = r + (k ? row::CutTubeN1 : row::CutTubeN0);
+  return p.x * n[0] + p.y * n[1] + p.z * n[2] + r[k ? row::CutTubeD1 : row::CutTubeD0];
+}
+__device__ __forceinline__ double ct_ndir(const double *r, int k, D3 d)
+{
+  const double *n = r + (k ? row::CutTubeN1 : row::CutTubeN0);
+  return d.x * n[0] + d.y * n[1] + d.z * n[2];
+}
+__device__ __forceinline__ double ct_plane_dist_in(const double *r, int k, D3 p, D3 d)  // Plane::DistanceToIn
+{
+  const double ndd = nonzero(ct_ndir(r, k, d)), saf = ct_plane(r, k, p);
+  return (ndd < 0. && saf > -kTolerance) ? -saf / ndd : -kInfLength;
+}
+__device__ __forceinline__ double ct_plane_dist_out(const double *r, int k, D3 p, D3 d)  // Plane::DistanceToOut
+{
+  const double ndd = nonzero(ct_ndir(r, k, d)), saf = ct_plane(r, k, p);
+  double distance  = kInfLength;
+  if (saf > kTolerance) distance = -kInfLength;
+  if (ndd > 0. && saf < kTolerance) distance = -saf / ndd;
+  return distance;
+}
+__device__ __forceinline__ int ct_planes_inside(const double *r, D3 p)
+{
+  const double d0 = ct_plane(r, 0, p), d1 = ct_plane(r, 1, p);
+  int inside      = (d0 < 0.0 && d1 < 0.0) ? kInsideE : kOutsideE;
+  if (fabs(d0) < kTolerance || fabs(d1) < kTolerance) inside = kSurfaceE;
+  return inside;
+}
+__device__ __forceinline__ double ct_planes_dist_in(const double *r, D3 p, D3 d)
+{
+  double d0 = ct_plane_dist_in(r, 0, p, d);
+  if (ct_ndir(r, 0, d) > 0.) d0 = -kInfLength;
+  double d1 = ct_plane_dist_in(r, 1, p, d);
+  if (ct_ndir(r, 1, d) > 0.) d1 = -kInfLength;
+  return vmax(d0, d1);
+}
+__device__ __forceinline__ double ct_planes_dist_out(const double *r, D3 p, D3 d)
+{
+  return vmin(ct_plane_dist_out(r, 0, p, d), ct_plane_dist_out(r, 1, p, d));
+}
+
+__device__ __forceinline__ bool cuttube_contains(const double *r, D3 p)
+{
+  if (!(ct_plane(r, 0, p) < 0. && ct_plane(r, 1, p) < 0.)) return false;
+  return tube_contains(r, p);
+}
+
+__device__ __forceinline__ int cuttube_inside(const double *r, D3 p)
+{
+  const int incp = ct_planes_inside(r, p);
+  if (incp == kOutsideE) return kOutsideE;
+  int inside = tube_inside(r, p);
+  if (incp == kOutsideE || (incp == kSurfaceE && inside != kOutsideE)) inside = incp;
+  return inside;
+}
+
+__device__ __forceinline__ double cuttube_dist_in_kernel(const double *r, D3 p, D3 d, double stepmax)
+{
+  double distance = kInfLength;
+  int incp        = ct_planes_inside(r, p);
+  int instart     = tube_inside(r, p);
+  if (incp == kOutsideE || (incp == kSurfaceE && instart != kOutsideE)) instart = incp;
+  if (instart == kInsideE) distance = -1.;
+  double dplanes         = ct_planes_dist_in(r, p, d);
+  const double safplanes = vmax(ct_plane(r, 0, p), ct_plane(r, 1, p));
+  const bool hitplanes   = fabs(dplanes) < stepmax && safplanes > -kTolerance;
+  if (incp != kInsideE && !hitplanes) return distance;
+  D3 prop = p;
+  if (!hitplanes) dplanes = 0.;
+  if (hitplanes) {
+    prop = d3(prop.x + dplanes * d.x, prop.y + dplanes * d.y, prop.z + dplanes * d.z);
+    incp = ct_planes_inside(r, prop);
+  }
+  bool done = incp == kOutsideE;
+  done |= instart == kInsideE;
+  if (done) return distance;
+  instart           = tube_inside(r, prop);
+  const bool inside = hitplanes && instart != kOutsideE;
+  if (inside && !done) distance = dplanes;
+  done |= inside;
+  if (done) {
+    if (fabs(distance) < kTolerance) distance = 0.;
+    return distance;
+  }
+  const double dexit = ct_planes_dist_out(r, prop, d);
+  double dtube       = tube_dist_in_kernel(r, prop, d);
+  if (dtube < 0.) dtube = 0.;
+  if (dexit < dtube) dtube = kInfLength;
+  if (!done && (dtube + dplanes) < stepmax) distance = dtube + dplanes;
+  return distance;
+}
+
+__device__ __forceinline__ double cuttube_dist_in(const double *r, D3 pt, D3 d, double stepmax)
+{
+  D3 p                = pt;
+  const double ptDist = sqrt(p.x * p.x + p.y * p.y + p.z * p.z);
+  double distToMove   = 0.;
+  const double order  = 100.;
+  if (ptDist > order * r[row::CutTubeMaxVal]) {
+    distToMove = ptDist - order * r[row::CutTubeMaxVal];
+    p          = d3(p.x + distToMove * d.x, p.y + distToMove * d.y, p.z + distToMove * d.z);
+  }
+  double distance = cuttube_dist_in_kernel(r, p, d, stepmax);
+  distance += distToMove;
+  return distance;
+}
+
+__device__ __forceinline__ double cuttube_dist_out(const double *r, D3 p, D3 d)
+{
+  double distance    = ct_planes_dist_out(r, p, d);
+  const double dtube = tube_dist_out(r, p, d);
+  if (dtube < distance) distance = dtube;
+  return distance;
+}
+
+__device__ __forceinline__ double cuttube_safe_in(const double *r, D3 p)
+{
+  double safety        = vmax(ct_plane(r, 0, p), ct_plane(r, 1, p));
+  const double saftube = tube_safe_in(r, p);
+  if (saftube > safety) safety = saftube;
+  return safety;
+}
+
+__device__ __forceinline__ double cuttube_safe_out(const double *r, D3 p)
+{
+  double safety        = vmin(-ct_plane(r, 0, p), -ct_plane(r, 1, p));
+  const double saftube = tube_safe_out(r, p);
+  if (saftube < safety) safety = saftube;
+  return safety;
+}
+
 // ---------------------------------------------------------------- dispatch
-__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d)
+// `stepmax` is the step the caller still accepts (the BVH passes its running step,
+// BVH.h:115); only the cut tube's DistanceToIn reads it
+__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d, double stepmax = kInfLength)
 {
   switch (type) {
   case kBox: return box_dist_in(r, p, d);
@@ -2321,6 +2459,7 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   case kSphere: return sphere_dist_in(r, p, d);
   case kPolycone: return pcon_dist_in(r, p, d);
   case kOrb: return orb_dist_in(r, p, d);
+  case kCutTube: return cuttube_dist_in(r, p, d, stepmax);
   }
   return kInfLength;
 }
@@ -2336,6 +2475,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   case kSphere: return sphere_dist_out(r, p, d);
   case kPolycone: return pcon_dist_out(r, p, d);
   case kOrb: return orb_dist_out(r, p, d);
+  case kCutTube: return cuttube_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -2351,6 +2491,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   case kSphere: return sphere_safe_in(r, p);
   case kPolycone: return pcon_safe_in(r, p);
   case kOrb: return orb_safe_in(r, p);
+  case kCutTube: return cuttube_safe_in(r, p);
   }
   return kInfLength;
 }
@@ -2366,6 +2507,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   case kSphere: return sphere_safe_out(r, p);
   case kPolycone: return pcon_safe_out(r, p);
   case kOrb: return orb_safe_out(r, p);
+  case kCutTube: return cuttube_safe_out(r, p);
   }
   return 0.;
 }
@@ -2381,6 +2523,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   case kSphere: return sphere_contains(r, p);
   case kPolycone: return pcon_contains(r, p);
   case kOrb: return orb_contains(r, p);
+  case kCutTube: return cuttube_contains(r, p);
   }
   return false;
 }
@@ -2396,6 +2539,7 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   case kSphere: return sphere_inside(r, p);
   case kPolycone: return pcon_inside(r, p);
   case kOrb: return orb_inside(r, p);
+  case kCutTube: return cuttube_inside(r, p);
   }
   return kOutsideE;
 }

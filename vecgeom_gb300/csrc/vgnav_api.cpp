@@ -637,7 +637,6 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
                     const double *pz, const double *dx, const double *dy, const double *dz, const double *step_max,
                     double *out, int flags, void *stream)
 {
-  (void)step_max;
   vgn_geometry *g = const_cast<vgn_geometry *>(gc);
   if (!g) return fail(VGN_ERR_ARG, "null geometry");
   if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
@@ -652,26 +651,30 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int type   = g->host.lv[lv].shape;
   const double *row = g->view.shape + g->host.lv[lv].shape_row;
-  const int kind = needdir ? classify({px, py, pz, dx, dy, dz, out}) : classify({px, py, pz, out});
+  const double *smax = needdir ? step_max : nullptr;  // only the distance ops read it
+  const int kind     = needdir ? classify({px, py, pz, dx, dy, dz, smax, out}) : classify({px, py, pz, out});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, px, py, pz, dx, dy, dz, out, max_blocks(g), s);
+    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, px, py, pz, dx, dy, dz, smax,
+                                                                     out, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "shape kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
   const size_t nd = (size_t)n * sizeof(double);
-  void *ws = workspace(g, carve_bytes({nd, nd, nd, nd, nd, nd, nd}));
+  void *ws = workspace(g, carve_bytes({nd, nd, nd, nd, nd, nd, nd, nd}));
   if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
   Carve c{static_cast<char *>(ws)};
-  double *b[6];
-  for (int k = 0; k < 6; ++k) b[k] = c.take<double>(n);
+  double *b[7];
+  for (int k = 0; k < 7; ++k) b[k] = c.take<double>(n);
   double *dout = c.take<double>(n);
-  const double *src[6] = {px, py, pz, dx, dy, dz};
+  const double *src[7] = {px, py, pz, dx, dy, dz, smax};
   const int ncopy      = needdir ? 6 : 3;
   cudaError_t e        = cudaSuccess;
   for (int k = 0; k < ncopy && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && smax) e = cudaMemcpyAsync(b[6], smax, nd, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5], dout, max_blocks(g), s);
+  e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5],
+                                                       smax ? b[6] : nullptr, dout, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "shape kernel launch");
   e = cudaMemcpyAsync(out, dout, nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");

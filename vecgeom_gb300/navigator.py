@@ -168,12 +168,12 @@ class Geometry:
                                          _ptr(out_states.data), N.VGN_PRECISION_MIXED if mixed else 0,
                                          _stream_ptr(stream)))
 
-    def shape(self, lv: int, op: int, pts: SOA3D, dirs: SOA3D | None, out, stream=None):
+    def shape(self, lv: int, op: int, pts: SOA3D, dirs: SOA3D | None, out, stream=None, step_max=None):
         dx = dy = dz = None
         if dirs is not None:
             dx, dy, dz = _ptr(dirs.x), _ptr(dirs.y), _ptr(dirs.z)
         N.check(N.lib().vgn_shape_batch(self.handle, lv, op, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z), dx,
-                                        dy, dz, None, _ptr(out), 0, _stream_ptr(stream)))
+                                        dy, dz, _ptr(step_max), _ptr(out), 0, _stream_ptr(stream)))
 
     def walk(self, pts: SOA3D, dirs: SOA3D, step_limit, states: NavStatePool, nsteps, max_steps: int = 1 << 20,
              mixed: bool = False, stream=None):

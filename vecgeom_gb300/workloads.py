@@ -22,8 +22,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB = range(8)
-SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb"]
+BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE = range(9)
+SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb", "cuttube"]
 
 K_PI = 3.14159265358979323846
 K_TWO_PI = 2.0 * K_PI
@@ -347,7 +347,15 @@ def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_l
 # The shape types of the 8192-daughter mixed-shape benchmark geometry (its definition: seven
 # types), and every shape type the library implements (for parity geometries).
 IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE)
-ALL_SHAPES = IMPLEMENTED_SHAPES + (ORB,)
+ALL_SHAPES = IMPLEMENTED_SHAPES + (ORB, CUTTUBE)
+
+
+def cuttube_params(rmin, rmax, dz, sphi, dphi, thb, phib, tht, phit):
+    """UnplacedCutTube parameters with the cut-plane normals given by polar and azimuthal
+    angles, as the reference's cut-tube benchmark builds them (test/benchmark/CutTubeBenchmark.cpp:13-14)."""
+    nb = (math.sin(thb) * math.cos(phib), math.sin(thb) * math.sin(phib), math.cos(thb))
+    nt = (math.sin(tht) * math.cos(phit), math.sin(tht) * math.sin(phit), math.cos(tht))
+    return (float(rmin), float(rmax), float(dz), float(sphi), float(dphi), *nb, *nt)
 MIXED_WORLD = 2000.0
 MIXED_GRID = (16, 16, 32)  # 8192 cells of 250 x 250 x 125 mm
 MIXED_JITTER = 5.0
@@ -425,11 +433,22 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
     if shape == ORB:
         r = u()
         return (r,), np.array([r, r, r])
+    if shape == CUTTUBE:  # a tube cut by two planes tilted by up to 0.6 rad
+        a, b = sorted((u(5.0, 40.0), u(5.0, 40.0)))
+        rmin, rmax = (a, b) if b - a > 1.0 else (0.0, b)
+        dz = u()
+        sphi, dphi = 0.0, K_TWO_PI
+        if sections and rng.uniform() < 0.75:
+            sphi, dphi = float(rng.uniform(0.0, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+        thb, tht = K_PI - float(rng.uniform(0.0, 0.6)), float(rng.uniform(0.0, 0.6))
+        phib, phit = (float(v) for v in rng.uniform(0.0, K_TWO_PI, 2))
+        return cuttube_params(rmin, rmax, dz, sphi, dphi, thb, phib, tht, phit), np.array([rmax, rmax, dz + 0.7 * rmax])
     raise ValueError(f"shape {shape} not implemented")
 
 
 _LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
-                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15)), ORB: (0,)}
+                   TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15)), ORB: (0,),
+                   CUTTUBE: (0, 1, 2)}
 
 
 def shape_bbox(shape: int, params):
@@ -442,6 +461,9 @@ def shape_bbox(shape: int, params):
         z = np.asarray(params[3:3 + nz])
         r = float(max(params[3 + 2 * nz:3 + 3 * nz]))
         return np.array([-r, -r, z.min()]), np.array([r, r, z.max()])
+    if shape == CUTTUBE:  # the cut planes tilt the end faces
+        h = float(params[1]) + float(params[2])
+        return np.full(3, -h), np.full(3, h)
     h = float(params[1]) if shape == SPHERE else float(max(params[:5]))
     return np.full(3, -h), np.full(3, h)
 
