@@ -267,6 +267,8 @@ def run_mixed_shapes(torch, V, local, steps, warmup, n_tracks, stream, fixed=Non
         saf = torch.empty(t.n, dtype=torch.float64, device="cuda")
         if fixed:  # profiling runs: a given launch configuration, no tuning launches
             v, kb, ks = fixed
+            if v >= V.Geometry.step_variant_count(mixed):  # a block-grouped variant: mixed form only
+                v = 5
             geo.set_step_config(v, kb, mixed=mixed)
             geo.set_safety_binning(ks, mixed=mixed)
         else:
@@ -448,7 +450,10 @@ def run_serving(torch, V, local, seconds: float, launch=None) -> dict:
     from vecgeom_gb300 import serving as S
     from vecgeom_gb300 import workloads as W
 
-    small_streams, large_streams, small_max, slice_tracks = 8, 4, 16384, 262144
+    # two normal-priority streams: more concurrent slices raise the peak (4: 156 M steps/s against
+    # 130 M) but keep the multiprocessors saturated, so small requests wait longer for them (p99 of
+    # <=4k-track requests at 50 % load 21 ms against 9 ms)
+    small_streams, large_streams, small_max, slice_tracks = 8, 2, 16384, 262144
     geo = V.Geometry(W.mixed_shape_geometry(), device=local)
     if launch:  # the mixed-shape workload's tuned configuration: the walks visit tracks in its binned order
         geo.set_step_config(launch["variant"], launch["sort_kbits"], mixed=True)
@@ -551,6 +556,8 @@ def run_ours(args, ws, rank, local):
         if args.fixed_launch:
             v, k, *ks = (int(x) for x in args.fixed_launch.split(","))
             ks = ks[0] if ks else 0
+            if v >= V.Geometry.step_variant_count(mixed):  # a block-grouped variant: mixed form only
+                v = 5
             geo.set_step_config(v, k, mixed=mixed)
             geo.set_safety_binning(ks, mixed=mixed)
             launch_cfg["mixed" if mixed else "fp64"] = {"variant": v, "sort_kbits": k, "safety_kbits": ks,

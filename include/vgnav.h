@@ -160,6 +160,18 @@ int vgn_shape_batch(const vgn_geometry *geom, int32_t lv, int32_t op, int64_t n,
                     const double *pz, const double *dx, const double *dy, const double *dz, const double *step_max,
                     double *out, int flags, void *stream);
 
+/* BVH::ApproachNextDaughter per track (VecGeom/base/BVH.h:158, source/BVH.cpp:395-449): over
+ * the BVH of logical volume lv[i], with the point and direction in that volume's frame, step[i]
+ * (in/out) is lowered to the entry distance into the bounding box of the nearest daughter the
+ * ray meets before it (the daughter's VUnplacedVolume::ApproachSolid, UnplacedVolume.h:274-281,
+ * in its own frame), skipping last_pv[i] at distance <= 0 (the last exited placed volume, -1 for
+ * none; NULL: -1 for every track).  FP64, bit-exact with the reference.  Host buffers: a volume
+ * out of range or without daughters, or a last_pv out of range, is VGN_ERR_ARG; device buffers:
+ * such a track keeps its step and the call (or vgn_synchronize) returns VGN_ERR_STATE. */
+int vgn_approach_next_daughter_batch(const vgn_geometry *geom, int64_t n, const int32_t *lv, const double *px,
+                                     const double *py, const double *pz, const double *dx, const double *dy,
+                                     const double *dz, const int32_t *last_pv, double *step, void *stream);
+
 /* Launch configuration of the step kernel for one precision form (flags &
  * VGN_PRECISION_MIXED): `variant` picks the threads-per-block / register-cap
  * variant, `sort_kbits` (0..6) bins tracks by direction octant and a
@@ -172,6 +184,11 @@ int vgn_shape_batch(const vgn_geometry *geom, int32_t lv, int32_t op, int64_t n,
  * threads per block (backend/cuda/Backend.h:50-96). */
 int vgn_set_step_config(vgn_geometry *geom, int flags, int32_t variant, int32_t sort_kbits);
 int vgn_get_step_config(const vgn_geometry *geom, int flags, int32_t *variant, int32_t *sort_kbits);
+/* Number of launch variants of the step for the precision form: 0..5 for both forms; the
+ * mixed form adds 6..8, which compute the candidates' FP64 DistanceToIn grouped by shape type
+ * across the whole thread block (every warp runs 32 candidates of one shape type at a time).
+ * vgn_batch_set_jobs takes variants 0..5.  No counterpart in the reference. */
+int vgn_get_step_variant_count(int flags, int32_t *count);
 /* Staging of step calls made with host buffers: the batch is split into `chunks`
  * pieces that alternate between two internal streams, so the host<->device copies of
  * one piece overlap the kernels of the other (0 = automatic, currently one piece:
@@ -255,12 +272,15 @@ int vgn_batch_autotune(vgn_batch *batch, void *stream, int32_t *variant, int32_t
  * cudaMalloc/cudaFree imply while other streams are busy.
  *  - all arrays must be device pointers (host buffers would need staging memory);
  *  - n <= VGN_STATIC_SCRATCH_MAX_TRACKS, else VGN_ERR_ARG;
- *  - the first call on a device looks the buffer's address up once for that
- *    device (with the geometry's device current); make that first call before
- *    any stream capture begins;
+ *  - the buffer's address is looked up on every call, in the current context
+ *    (with the geometry's device current); the first call on a device may load
+ *    the library's device code, so make it before any stream capture begins;
  *  - there is ONE buffer per device: calls that overlap on that device (other
  *    streams, other threads, other geometries) race on it and must be ordered
- *    by the caller.
+ *    by the caller;
+ *  - the buffer holds one visit permutation, the step's: the safety pass runs
+ *    in that order too, not in the order of vgn_set_safety_binning (same
+ *    results; vgn_compute_step_batch may be faster on the safety).
  * Uses the step launch variant set for the precision form (vgn_set_step_config).
  * No counterpart in the reference. */
 #define VGN_STATIC_SCRATCH_MAX_TRACKS 1048576 /* 2^20 tracks per call */

@@ -322,6 +322,7 @@ or_geom *or_geom_create_ex(int n_lv, const int *lv_shape, const int *lv_param_of
       or_geom_free(g);
       return NULL;
     }
+    shape_extent(&g->lv[i], &g->lv[i].bbox_min, &g->lv[i].bbox_max); /* ComputeBBox at construction */
   }
   count = (int *)calloc((size_t)n_lv, sizeof(int));
   for (i = 0; i < n_pv; ++i) {

@@ -176,6 +176,7 @@ typedef struct {
     or_orb orb;
     or_cuttube ctube;
   } s;
+  v3 bbox_min, bbox_max; /* VUnplacedVolume::fBBox: the shape's Extent (UnplacedVolume.h:45, 76-80) */
   /* BVH (BVH.h:364-370), present when nd > 0 */
   int bvh_depth, bvh_nodes;
   int *prim_id, *offset, *nchild;

@@ -142,6 +142,80 @@ static void bvh_check_daughters(const or_geom *g, const or_lv *lv, v3 lp, v3 ld,
   } while (ptr > stack);
 }
 
+/* VUnplacedVolume::ApproachSolid (UnplacedVolume.h:274-281): the ray's entry into the shape's
+ * bounding box (its Extent, cached at construction), BoxImplementation::IntersectCachedKernel2
+ * (BoxImplementation.h:326-368) with t0 = 0, t1 = kInfLength */
+static double approach_solid(v3 mn, v3 mx, v3 p, v3 inv)
+{
+  const v3 c[2] = {mn, mx};
+  const int sx = inv.x < 0, sy = inv.y < 0, sz = inv.z < 0;
+  double tmin, tmax, tymin, tymax, tzmin, tzmax;
+  int done;
+  tmin  = (c[sx].x - p.x) * inv.x;
+  tymax = (c[1 - sy].y - p.y) * inv.y;
+  done  = tmin > tymax;
+  if (done) return kInfLength;
+  tmax  = (c[1 - sx].x - p.x) * inv.x;
+  tymin = (c[sy].y - p.y) * inv.y;
+  done |= tymin > tmax;
+  if (done) return kInfLength;
+  tmin  = tmin > tymin ? tmin : tymin; /* Max(tmin, tymin) */
+  tmax  = tmax < tymax ? tmax : tymax; /* Min(tmax, tymax) */
+  tzmin = (c[sz].z - p.z) * inv.z;
+  tzmax = (c[1 - sz].z - p.z) * inv.z;
+  done |= (tmin > tzmax) || (tzmin > tmax);
+  if (done) return kInfLength;
+  tmin = tmin > tzmin ? tmin : tzmin;
+  tmax = tmax < tzmax ? tmax : tzmax;
+  done |= !((tmin <= kInfLength + kTolerance) && (tmax > 0. - kTolerance));
+  return done ? kInfLength : tmin;
+}
+
+/* BVH::ApproachNextDaughter (BVH.cpp:395-449): the traversal of CheckDaughterIntersections with
+ * each daughter's ApproachSolid in its own frame in place of its DistanceToIn */
+static void bvh_approach(const or_geom *g, const or_lv *lv, v3 lp, v3 ld, double *step, int last)
+{
+  unsigned stack[STACK_DEPTH], *ptr = &stack[1];
+  v3 invdir = v3_make(1.0 / NonZero(ld.x), 1.0 / NonZero(ld.y), 1.0 / NonZero(ld.z));
+  stack[0]  = 0;
+  do {
+    const unsigned id = *--ptr;
+    if (lv->nchild[id] >= 0) {
+      int i;
+      for (i = 0; i < lv->nchild[id]; ++i) {
+        const int prim = lv->prim_id[lv->offset[id] + i];
+        double tmin, tmax;
+        aabb_intersect_invdir(&lv->aabbs[prim], lp, invdir, &tmin, &tmax);
+        if (tmin <= tmax && tmax >= 0.0 && tmin < *step) {
+          const int vol      = lv->daughters[prim];
+          const or_pv *pv    = &g->pv[vol];
+          const v3 p         = xf_transform(&pv->xf, lp);
+          const v3 d         = xf_transform_dir(&pv->xf, ld);
+          const v3 inv       = v3_make(1.0 / NonZero(d.x), 1.0 / NonZero(d.y), 1.0 / NonZero(d.z));
+          const or_lv *dlv   = &g->lv[pv->lv];
+          const double dist  = approach_solid(dlv->bbox_min, dlv->bbox_max, p, inv);
+          if (dist < *step && !(dist <= 0.0 && vol == last)) *step = dist;
+        }
+      }
+    } else {
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      double tminL = kInfLength, tmaxL = -kInfLength, tminR = kInfLength, tmaxR = -kInfLength;
+      int trL, trR;
+      aabb_intersect_invdir(&lv->nodes[L], lp, invdir, &tminL, &tmaxL);
+      aabb_intersect_invdir(&lv->nodes[R], lp, invdir, &tminR, &tmaxR);
+      trL = tminL <= tmaxL && tmaxL >= 0.0 && tminL < *step;
+      trR = tminR <= tmaxR && tmaxR >= 0.0 && tminR < *step;
+      if (tminR < tminL) {
+        if (trR) *ptr++ = R;
+        if (trL) *ptr++ = L;
+      } else {
+        if (trL) *ptr++ = L;
+        if (trR) *ptr++ = R;
+      }
+    }
+  } while (ptr > stack);
+}
+
 /* NewSimpleNavigator::CheckDaughterIntersections (NewSimpleNavigator.h:30-70) */
 static void simple_check_daughters(const or_geom *g, const or_lv *lv, v3 lp, v3 ld, double *step, int last, int *hit)
 {
@@ -518,6 +592,20 @@ void or_locate_batch(const or_geom *g, long n, const double *px, const double *p
   memset(&j, 0, sizeof(j));
   j.g = g; j.px = px; j.py = py; j.pz = pz; j.out = out; j.mode = 3;
   run_jobs(&j, n, nthreads, NULL);
+}
+
+/* BVH::ApproachNextDaughter per track over logical volume lv[i]'s BVH (local point and
+ * direction, step in/out, last[i] the last exited placed volume or -1); 1 if a volume has no BVH */
+int or_approach_batch(const or_geom *g, long n, const int *lv, const double *px, const double *py,
+                      const double *pz, const double *dx, const double *dy, const double *dz, const int *last,
+                      double *step)
+{
+  long i;
+  for (i = 0; i < n; ++i)
+    if (lv[i] < 0 || lv[i] >= g->n_lv || g->lv[lv[i]].nd == 0) return 1;
+  for (i = 0; i < n; ++i)
+    bvh_approach(g, &g->lv[lv[i]], v3_make(px[i], py[i], pz[i]), v3_make(dx[i], dy[i], dz[i]), &step[i], last[i]);
+  return 0;
 }
 
 /* unplaced shape queries */

@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
         L.or_nav_step_norel_batch.argtypes = [p, l, p, p, p, p, p, p, p, p, p, p, i]
         L.or_safety_batch.argtypes = [p, l, p, p, p, p, p, i]
         L.or_locate_batch.argtypes = [p, l, p, p, p, p, i]
+        L.or_approach_batch.argtypes = [p, l, p, p, p, p, p, p, p, p, p]
         L.or_now.restype = C.c_double
         L.or_ncores.restype = C.c_int
         _lib = L
@@ -119,6 +120,19 @@ class OracleGeometry:
         rc = lib().or_shape_batch(self.h, lv, op, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(sm), _p(out))
         if rc:
             raise ValueError("bad shape query")
+        return out
+
+    def approach(self, lv, x, y, z, dx, dy, dz, last, step):
+        """BVH::ApproachNextDaughter per track over logical volume lv[i]'s BVH (local point and
+        direction; last[i] the last exited placed volume or -1): the approached steps (a copy of
+        `step`, the starting values, updated)."""
+        n = x.shape[0]
+        lv = np.ascontiguousarray(lv, np.int32)
+        last = np.ascontiguousarray(last, np.int32)
+        out = np.array(step, np.float64)
+        a = [np.ascontiguousarray(v, np.float64) for v in (x, y, z, dx, dy, dz)]
+        if lib().or_approach_batch(self.h, n, _p(lv), *(_p(v) for v in a), _p(last), _p(out)):
+            raise ValueError("a logical volume without daughters")
         return out
 
     def step(self, t, calcsafety=True, simple=False, nthreads=0, counters=False, relocate=True):

@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
         L.vgref_step_vector.argtypes = [l, p, p, p, p, p, p, p, p, p, p, p, p, i]
         L.vgref_safety_batch.argtypes = [l, p, p, p, p, p, i]
         L.vgref_locate_batch.argtypes = [l, p, p, p, p, i]
+        L.vgref_approach_batch.argtypes = [l, p, p, p, p, p, p, p, p, p, i]
         L.vgref_ncores.restype = i
         _lib = L
     return _lib
@@ -166,6 +167,18 @@ class RefGeometry:
         x, y, z = _c(x), _c(y), _c(z)
         out = np.zeros(x.shape[0])
         lib().vgref_safety_batch(x.shape[0], _p(x), _p(y), _p(z), _p(np.ascontiguousarray(states)), _p(out), nthreads)
+        return out
+
+    def approach(self, lv, x, y, z, dx, dy, dz, last, step, nthreads=0):
+        """BVH::ApproachNextDaughter per track over logical volume lv[i]'s BVH: the approached
+        steps (a copy of `step`, the starting values, updated)."""
+        self._check()
+        lv = np.ascontiguousarray(lv, np.int32)
+        last = np.ascontiguousarray(last, np.int32)
+        out = np.array(step, np.float64)
+        a = [_c(v) for v in (x, y, z, dx, dy, dz)]
+        if lib().vgref_approach_batch(lv.shape[0], _p(lv), *(_p(v) for v in a), _p(last), _p(out), nthreads):
+            raise ValueError("a logical volume without a BVH")
         return out
 
     def locate(self, x, y, z, nthreads=0):

@@ -391,6 +391,26 @@ void vgref_locate_batch(long n, const double *px, const double *py, const double
   });
 }
 
+// BVH::ApproachNextDaughter (BVH.cpp:395-449) of logical volume lv[i]'s BVH for each track:
+// local point and direction in that volume, step in/out, last[i] the id of the last exited
+// placed volume or -1.  Returns 1 if a volume has no BVH.
+int vgref_approach_batch(long n, const int *lv, const double *px, const double *py, const double *pz,
+                         const double *dx, const double *dy, const double *dz, const int *last, double *step,
+                         int nthreads)
+{
+  if (!g_ready) return 1;
+  for (long i = 0; i < n; ++i)
+    if (lv[i] < 0 || lv[i] >= (int)g_lv.size() || !BVHManager::GetBVH(lv[i])) return 1;
+  parallel_for(n, nthreads, [&](long lo, long hi) {
+    for (long i = lo; i < hi; ++i) {
+      VPlacedVolume const *lastpv = last[i] >= 0 ? GeoManager::Instance().FindPlacedVolume(last[i]) : nullptr;
+      BVHManager::GetBVH(lv[i])->ApproachNextDaughter(Vector3D<Precision>(px[i], py[i], pz[i]),
+                                                      Vector3D<Precision>(dx[i], dy[i], dz[i]), step[i], lastpv);
+    }
+  });
+  return 0;
+}
+
 int vgref_ncores(void)
 {
   return (int)std::max(1u, std::thread::hardware_concurrency());

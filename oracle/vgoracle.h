@@ -99,6 +99,13 @@ void or_safety_batch(const or_geom *g, long n, const double *px, const double *p
 void or_locate_batch(const or_geom *g, long n, const double *px, const double *py, const double *pz, or_state *out,
                      int nthreads);
 
+/* BVH::ApproachNextDaughter (BVH.cpp:395-449) per track over logical volume lv[i]'s BVH: local
+ * point and direction in that volume, step in/out, last[i] the last exited placed volume or -1.
+ * Returns 1 (nothing computed) if a volume has no daughters. */
+int or_approach_batch(const or_geom *g, long n, const int *lv, const double *px, const double *py,
+                      const double *pz, const double *dx, const double *dy, const double *dz, const int *last,
+                      double *step);
+
 /* wall-clock helper for the CPU baseline */
 double or_now(void);
 int or_ncores(void);

@@ -18,6 +18,8 @@ writes inputs and outputs to tests/golden/ref_fixtures.npz:
   nested        the three-level geometry: 2048 located tracks, one step, a walk
   deep_cache1   the five-level geometry with global matrices cached down to level 1 only
                 (transformation cache depth 1): 2048 located tracks, one step, a walk
+  approach/<key>  BVH::ApproachNextDaughter on the mixed_all, nested and deep_cache1
+                geometries: 4096 tracks over their BVHs (tests/helpers.py approach_inputs)
   shapes        every parameter set of tests/shape_sets.py: up to 192 points (random,
                 coordinate planes and axes, surface), all six queries
 
@@ -45,6 +47,7 @@ from vecgeom_gb300 import workloads as W  # noqa: E402
 FIXTURE = HERE / "ref_fixtures.npz"
 DESC_KEYS = ("lv_shape", "lv_param_offset", "params", "pv_logical", "pv_mother", "pv_transform")
 TRACK_KEYS = ("x", "y", "z", "dx", "dy", "dz", "step_limit")
+APPROACH_KEYS = ("lv", "x", "y", "z", "dx", "dy", "dz", "last", "step")
 MIXED_GRID = (8, 8, 8)
 MIXED_WORLD = 1000.0  # 250 mm pitch, as in the 8192-daughter workload
 SHAPE_POINTS = 128
@@ -83,6 +86,11 @@ def put_tracks(out: dict, key: str, t) -> None:
     for k in TRACK_KEYS:
         out[f"{key}/in/{k}"] = np.asarray(getattr(t, k))
     out[f"{key}/in/states"] = states_to_words(t.states)
+
+
+def get_approach(fx, key: str):
+    """Inputs of the approach fixture `key`: lv, x, y, z, dx, dy, dz, last, step."""
+    return tuple(np.asarray(fx[f"approach/{key}/in/{k}"]) for k in APPROACH_KEYS)
 
 
 def get_tracks(fx, key: str):
@@ -202,6 +210,16 @@ def generate() -> dict:
     put_tracks(out, "deep_cache1", t)
     _steps(out, "deep_cache1", rg, t)
     _walk(out, "deep_cache1", rg, t)
+
+    # BVH::ApproachNextDaughter
+    from helpers import approach_inputs
+    for key, half in (("mixed_all", 1000.0), ("nested", 480.0), ("deep_cache1", 590.0)):
+        desc = get_desc(out, key)
+        rg = pyref.RefGeometry(desc, cache_depth=get_cache_depth(out, key))
+        a = approach_inputs(desc, 4096, 71, half)
+        for k, v in zip(APPROACH_KEYS, a):
+            out[f"approach/{key}/in/{k}"] = np.asarray(v)
+        out[f"approach/{key}/out/step"] = rg.approach(*a)
 
     # every shape parameter set
     for i, (name, shape, params) in enumerate(SHAPE_SETS):

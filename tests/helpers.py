@@ -86,3 +86,21 @@ def navindex_pad_words(table: np.ndarray, n_words: int) -> np.ndarray:
             written[cur:cur + 24] = True
         todo.extend(int(table[i + 3 + k]) for k in range(nd))
     return ~written
+
+
+def approach_inputs(desc, n: int, seed: int, half: float):
+    """Inputs of BVH::ApproachNextDaughter for `n` tracks: a logical volume with daughters per
+    track, points uniform in a cube of half-width `half` and isotropic directions in that
+    volume's frame, a last exited placed volume for 30 % of the tracks (-1 for the others) and
+    starting steps, half of them infinite and half uniform in [0, 2 half)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lvs = np.array([l for l in range(desc.n_logical) if np.any(desc.pv_mother == l)], np.int32)
+    lv = rng.choice(lvs, n).astype(np.int32)
+    x, y, z = rng.uniform(-half, half, (3, n))
+    cz = rng.uniform(-1.0, 1.0, n)
+    phi = rng.uniform(0.0, 2.0 * np.pi, n)
+    sz = np.sqrt(1.0 - cz * cz)
+    dx, dy, dz = sz * np.cos(phi), sz * np.sin(phi), cz
+    last = np.where(rng.uniform(size=n) < 0.3, rng.integers(0, len(desc.pv_logical), n), -1).astype(np.int32)
+    step = np.where(rng.uniform(size=n) < 0.5, np.finfo(np.float64).max, rng.uniform(0.0, 2.0 * half, n))  # kInfLength
+    return lv, x, y, z, dx, dy, dz, last, step

@@ -112,6 +112,15 @@ def test_step_config_host_logic(vgnav):
     L.vgn_get_step_config(h.h, 0, C.byref(v), C.byref(k))
     assert (v.value, k.value) == (0, 0)  # forms are configured independently
     assert L.vgn_set_step_config(h.h, 0, 99, 0) == N.VGN_ERR_ARG
+    # the block-grouped variants exist for the mixed form only
+    nv = C.c_int32()
+    assert L.vgn_get_step_variant_count(0, C.byref(nv)) == N.VGN_OK and nv.value == 6
+    assert L.vgn_get_step_variant_count(N.VGN_PRECISION_MIXED, C.byref(nv)) == N.VGN_OK and nv.value == 9
+    assert L.vgn_set_step_config(h.h, N.VGN_PRECISION_MIXED, 8, 5) == N.VGN_OK
+    assert L.vgn_set_step_config(h.h, N.VGN_PRECISION_MIXED, 9, 5) == N.VGN_ERR_ARG
+    assert L.vgn_set_step_config(h.h, 0, 6, 5) == N.VGN_ERR_ARG
+    assert L.vgn_set_step_config(h.h, N.VGN_PRECISION_MIXED, 2, 4) == N.VGN_OK
+    assert L.vgn_get_step_variant_count(0, None) == N.VGN_ERR_ARG
     assert L.vgn_set_step_config(h.h, 0, 0, -1) == N.VGN_ERR_ARG
     assert L.vgn_set_step_config(h.h, 0, 0, 7) == N.VGN_ERR_ARG
     assert L.vgn_set_step_config(None, 0, 0, 0) == N.VGN_ERR_ARG

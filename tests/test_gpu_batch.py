@@ -51,8 +51,8 @@ class Job:
         return self.steps.cpu().numpy(), self.saf.cpu().numpy(), self.out.to_numpy()
 
 
-def _setup(oracle, vgnav, torch, n_geo=6):
-    work = W.batched_workload(n_geo, seed=40, daughters=(64, 512), tracks=(1000, 20000))
+def _setup(oracle, vgnav, torch, n_geo=6, daughters=(64, 512), tracks=(1000, 20000)):
+    work = W.batched_workload(n_geo, seed=40, daughters=daughters, tracks=tracks)
     ogs, jobs, tracks = [], [], []
     for desc, t in work:
         og = oracle.OracleGeometry(desc)
@@ -60,6 +60,7 @@ def _setup(oracle, vgnav, torch, n_geo=6):
         ogs.append(og)
         tracks.append(t)
         jobs.append(Job(torch, vgnav, vgnav.Geometry(desc), t))
+        jobs[-1].n_placed = len(desc.pv_logical)
     return ogs, jobs, tracks
 
 
@@ -77,6 +78,23 @@ def test_batch_matches_oracle(oracle, vgnav, cuda, mixed):
     ogs, jobs, tracks = _setup(oracle, vgnav, cuda)
     batch = vgnav.StepBatch(0)
     for variant, kbits in ((0, 0), (2, 5), (3, 3)):
+        for j in jobs:
+            j.steps.fill_(-7.0)
+        batch.set_jobs([j.spec() for j in jobs], mixed=mixed, variant=variant, sort_kbits=kbits)
+        batch.step()
+        batch.synchronize()
+        _check(ogs, jobs, tracks)
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_batch_full_daughter_range(oracle, vgnav, cuda, mixed):
+    """The batched workload's whole daughter range: nine geometries of 2^6 to 2^14 daughters
+    (both ends present) in one persistent launch, batches of 1k-50k tracks, equal to the oracle."""
+    ogs, jobs, tracks = _setup(oracle, vgnav, cuda, n_geo=9, daughters=(64, 16384), tracks=(1000, 50000))
+    nd = sorted(j.n_placed - 1 for j in jobs)  # every placement but the world's is a world daughter
+    assert nd[0] == 64 and nd[-1] == 16384
+    batch = vgnav.StepBatch(0)
+    for variant, kbits in ((0, 5), (2, 4)):
         for j in jobs:
             j.steps.fill_(-7.0)
         batch.set_jobs([j.spec() for j in jobs], mixed=mixed, variant=variant, sort_kbits=kbits)

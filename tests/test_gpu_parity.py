@@ -276,7 +276,8 @@ def test_launch_configs_bit_exact(oracle, vgnav, cuda, mixed):
     geo = vgnav.Geometry(grid.desc)
     t = W.box_grid_tracks(grid, n=100003, seed_points=71, seed_dirs=72)
     ref = og.step(t, calcsafety=True)
-    n_variants = 6
+    n_variants = vgnav.Geometry.step_variant_count(mixed)
+    assert n_variants == (9 if mixed else 6)
     for variant in range(n_variants):
         for kbits in (0, 1, 3, 5, 6):
             geo.set_step_config(variant, kbits, mixed=mixed)
@@ -307,7 +308,7 @@ def test_autotune_then_step(oracle, vgnav, cuda, mixed):
     steps = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
     saf = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
     v, k, ms = geo.autotune_step(pts, dirs, to_dev(cuda, t.step_limit), inp, out, steps, saf, mixed=mixed)
-    assert 0 <= v < 6 and k in (0, 3, 4, 5, 6) and ms > 0
+    assert 0 <= v < vgnav.Geometry.step_variant_count(mixed) and k in (0, 3, 4, 5, 6) and ms > 0
     assert geo.step_config(mixed=mixed) == (v, k)
     ref = og.step(t, calcsafety=True)
     got = gpu_step(cuda, geo, t, mixed=mixed)
@@ -375,24 +376,57 @@ def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
     assert w.n == 0
 
 
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+def test_mixed_shapes_at_benchmark_size(oracle, vgnav, cuda, mixed):
+    """The 8192-daughter mixed-shape benchmark geometry with 2^21 tracks located in the world
+    (a quarter of the benchmark's batch): one step with safety in the autotuned launch
+    configuration, equal to the oracle bit for bit."""
+    desc = W.mixed_shape_geometry()
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    t = W.mixed_shape_tracks(1 << 21)
+    t.states = og.locate(t.x, t.y, t.z, nthreads=0)
+    ref = og.step(t, calcsafety=True, nthreads=0)
+    dev = lambda a: to_dev(cuda, a)
+    pts = vgnav.SOA3D(dev(t.x), dev(t.y), dev(t.z))
+    dirs = vgnav.SOA3D(dev(t.dx), dev(t.dy), dev(t.dz))
+    inp = vgnav.NavStatePool(states_to_dev(cuda, t.states))
+    out = vgnav.NavStatePool.empty_like(inp)
+    steps = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
+    saf = cuda.empty(t.n, dtype=cuda.float64, device="cuda")
+    sl = dev(t.step_limit)
+    geo.autotune_step(pts, dirs, sl, inp, out, steps, saf, mixed=mixed)
+    geo.step(pts, dirs, sl, inp, out, steps, saf, mixed=mixed)
+    geo.synchronize()
+    assert np.array_equal(steps.cpu().numpy(), ref["step"])
+    assert np.array_equal(saf.cpu().numpy(), ref["safety"])
+    assert np.array_equal(out.to_numpy(), ref["out"])
+
+
+@pytest.mark.parametrize("variant", [0, 6, 8], ids=["v0", "grouped128", "grouped256"])
 @pytest.mark.parametrize("kbits", [0, 4], ids=["unbinned", "binned"])
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["box_grid", "mixed_shapes"])
-def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed, kbits):
+def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed, kbits, variant):
     """vgn_walk_batch (the transport loop on the device) ends every track where the oracle's
     step-by-step loop ends it: same final point, state and number of steps; also with the
-    tracks visited in the binned order of the geometry's step configuration."""
+    tracks visited in the binned order of the geometry's step configuration (40000 tracks:
+    batches of 32768 and more are binned), and in the mixed form's block-grouped persistent
+    walk (launch variants 6-8)."""
+    if variant and not mixed:
+        pytest.skip("block-grouped variants exist for the mixed form only")
     torch = cuda
+    n = 40000 if kbits else 20000
     if which == "box_grid":
         grid = W.box_grid_geometry()
         desc = grid.desc
-        t = W.box_grid_tracks(grid, n=20000, seed_points=81, seed_dirs=82)
+        t = W.box_grid_tracks(grid, n=n, seed_points=81, seed_dirs=82)
     else:
         desc = W.mixed_shape_geometry()
-        t = W.mixed_shape_tracks(20000, 83, 84)
+        t = W.mixed_shape_tracks(n, 83, 84)
     og = oracle.OracleGeometry(desc)
     geo = vgnav.Geometry(desc)
-    geo.set_step_config(0, kbits, mixed=mixed)
+    geo.set_step_config(variant, kbits, mixed=mixed)
     if which == "mixed_shapes":
         t.states = og.locate(t.x, t.y, t.z)
     # oracle: step until the world is left, recording where each track ends
@@ -430,6 +464,20 @@ def test_walk_kernel_matches_stepwise_oracle(oracle, vgnav, cuda, which, mixed, 
     geo.walk(pts2, dirs, to_dev(torch, t.step_limit), st2, nsteps, max_steps=1, mixed=mixed)
     geo.synchronize()
     assert np.all(nsteps.cpu().numpy() == np.where(t.states["nav_ind"] != 0, 1, 0))
+    # states that start no table record are refused (nsteps -1, VGN_ERR_STATE); the others walk
+    bad = t.states.copy()
+    bad["nav_ind"][[5, 17]] = (2, 0xFFFFFFFE)
+    pts3 = vgnav.SOA3D(to_dev(torch, t.x), to_dev(torch, t.y), to_dev(torch, t.z))
+    st3 = vgnav.NavStatePool(states_to_dev(torch, bad))
+    geo.walk(pts3, dirs, to_dev(torch, t.step_limit), st3, nsteps, mixed=mixed)
+    with pytest.raises(N.VgnError) as e:
+        geo.synchronize()
+    assert e.value.code == N.VGN_ERR_STATE
+    got = nsteps.cpu().numpy()
+    ok = np.ones(n, bool)
+    ok[[5, 17]] = False
+    assert np.all(got[~ok] == -1) and np.array_equal(got[ok], ref_steps[ok])
+    assert np.array_equal(pts3.x.cpu().numpy()[ok], ref_x[ok])
 
 
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import pyref
-from helpers import HostTables, advance, keep, navindex_pad_words
+from helpers import HostTables, advance, approach_inputs, keep, navindex_pad_words
 from shape_sets import OPS, SHAPE_SETS, shape_points, single_shape
 from vecgeom_gb300 import workloads as W
 
@@ -137,6 +137,21 @@ def test_walk_equals_reference(oracle, cases, which):
         if w.n == 0:
             break
     assert w.n == 0
+
+
+@pytest.mark.parametrize("which", GEOS)
+def test_approach_equals_reference(oracle, cases, which):
+    """BVH::ApproachNextDaughter over every BVH of the geometry (2^15 tracks, local points in a
+    cube around the volume, some with a last exited volume): oracle == reference."""
+    desc, _ = cases[which]
+    cd = cache_depth(which)
+    rg = pyref.RefGeometry(desc, cache_depth=cd)
+    og = oracle.OracleGeometry(desc, cache_depth=cd)
+    half = 1000.0 if which in ("box_grid", "mixed", "mixed_sections", "mixed_all") else 600.0
+    a = approach_inputs(desc, 1 << 15, 61, half)
+    r = rg.approach(*a)
+    assert np.array_equal(og.approach(*a), r)
+    assert np.mean(r != a[-1]) > 0.002  # some steps were lowered
 
 
 @pytest.mark.parametrize("name,shape,params", SHAPE_SETS, ids=[s[0] for s in SHAPE_SETS])

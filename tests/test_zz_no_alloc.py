@@ -75,13 +75,39 @@ def test_static_scratch_step_matches_existing_entry_point(vgnav, cuda, mixed):
         assert np.array_equal(got[2], ref[2])  # propagated states
 
     # repeated calls take no device memory
-    torch.cuda.synchronize()
-    free_before = torch.cuda.mem_get_info()[0]
-    for k in (1, 4, 5):
-        assert L.vgn_compute_step_batch_static(geo.handle, *g0.args(), flags, k, None) == N.VGN_OK
-    geo.synchronize()
-    assert torch.cuda.mem_get_info()[0] >= free_before
+    _assert_no_device_allocation(torch, lambda: [
+        L.vgn_compute_step_batch_static(geo.handle, *g0.args(), flags, k, None) for k in (1, 4, 5)], geo)
     assert np.array_equal(g0.results()[0], ref0[0])
+
+
+def _assert_no_device_allocation(torch, calls, geo):
+    """Run `calls` (returning status codes): all succeed, torch's allocator is untouched and the
+    driver's free memory does not drop by more than 1 MiB (a binning scratch of the dynamic
+    entry point is several MiB at these sizes)."""
+    torch.cuda.synchronize()
+    alloc_before, free_before = torch.cuda.memory_allocated(), torch.cuda.mem_get_info()[0]
+    assert all(rc == N.VGN_OK for rc in calls())
+    geo.synchronize()
+    assert torch.cuda.memory_allocated() == alloc_before
+    assert torch.cuda.mem_get_info()[0] >= free_before - (1 << 20)
+
+
+def test_static_scratch_at_capacity(vgnav, cuda):
+    """n = VGN_STATIC_SCRATCH_MAX_TRACKS at the largest binning granularity: the layout where the
+    visit permutation ends at the buffer's last word.  Bit for bit the existing entry point's
+    results, with no device allocation."""
+    torch = cuda
+    L = N.lib()
+    flags = N.VGN_PRECISION_MIXED
+    grid = W.box_grid_geometry()
+    geo = vgnav.Geometry(grid.desc)
+    t = W.box_grid_tracks(grid, n=N.VGN_STATIC_SCRATCH_MAX_TRACKS, seed_points=95, seed_dirs=96)
+    ref = _existing(geo, DevBatch(torch, t), flags)
+    b = DevBatch(torch, t)
+    _assert_no_device_allocation(torch, lambda: [L.vgn_compute_step_batch_static(
+        geo.handle, *b.args(), flags, N.VGN_STATIC_SCRATCH_MAX_KBITS, None)], geo)
+    for a, r in zip(b.results(), ref):
+        assert np.array_equal(a, r)
 
 
 def test_static_scratch_step_rejects_what_it_cannot_hold(vgnav, cuda):

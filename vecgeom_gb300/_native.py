@@ -42,8 +42,10 @@ EXPORTED = [
     "vgn_compute_safety_batch",
     "vgn_locate_batch",
     "vgn_shape_batch",
+    "vgn_approach_next_daughter_batch",
     "vgn_set_step_config",
     "vgn_get_step_config",
+    "vgn_get_step_variant_count",
     "vgn_set_safety_binning",
     "vgn_get_safety_binning",
     "vgn_set_staging_chunks",
@@ -124,8 +126,10 @@ def lib() -> C.CDLL:
         L.vgn_compute_safety_batch.argtypes = [vp, i64, p, p, p, p, p, C.c_int, vp]
         L.vgn_locate_batch.argtypes = [vp, i64, p, p, p, p, C.c_int, vp]
         L.vgn_shape_batch.argtypes = [vp, i32, i32, i64, p, p, p, p, p, p, p, p, C.c_int, vp]
+        L.vgn_approach_next_daughter_batch.argtypes = [vp, i64, p, p, p, p, p, p, p, p, p, vp]
         L.vgn_set_step_config.argtypes = [vp, C.c_int, i32, i32]
         L.vgn_get_step_config.argtypes = [vp, C.c_int, C.POINTER(i32), C.POINTER(i32)]
+        L.vgn_get_step_variant_count.argtypes = [C.c_int, C.POINTER(i32)]
         L.vgn_set_safety_binning.argtypes = [vp, C.c_int, i32]
         L.vgn_get_safety_binning.argtypes = [vp, C.c_int, C.POINTER(i32)]
         L.vgn_set_staging_chunks.argtypes = [vp, i32]

@@ -17,6 +17,12 @@
 
 #include <cstdint>
 
+#ifdef __CUDACC__
+#define VGN_HD __host__ __device__
+#else
+#define VGN_HD
+#endif
+
 namespace vgn {
 
 constexpr int kStackSize = 32;  // BVH::BVH_MAX_DEPTH (BVH.h:33)
@@ -58,7 +64,8 @@ struct alignas(32) LVRec {
   int32_t nodes_off;     // first BVH node (into nodes / fnodes)
   int32_t n_nodes;       // (2 << depth) - 1, 0 if no daughters
   int32_t prims_off;     // first leaf primitive (into prims / fprims)
-  int32_t depth;
+  uint16_t depth;        // BVH depth
+  uint16_t dtypes;       // bit t set: some daughter is of ShapeType t
 };
 static_assert(sizeof(LVRec) == 32, "LVRec must be 32 bytes");
 
@@ -117,7 +124,8 @@ struct alignas(64) IPrimSlab {  // leaf primitive box in BVH leaf order
   float mn_lo[3], mn_hi[3], mx_lo[3], mx_hi[3];
   int32_t pv;
   int32_t prim;
-  int32_t pad[2];
+  int32_t shape;  // the placed volume's ShapeType (groups the FP64 shape evaluations by type)
+  int32_t pad;
 };
 static_assert(sizeof(IPrimSlab) == 64, "IPrimSlab must be 64 bytes");
 
@@ -142,6 +150,12 @@ enum { ConeDz = 0, ConeMinusConeTol, ConeTol, ConeHasRmin, ConeOuterConst, ConeO
 enum { TrdDz = 0, TrdHalfX, TrdFx, TrdCalfX, TrdVaryingY, TrdHalfY, TrdFy, TrdCalfY, TrdDy1, kTrdRow };
 enum { TrapDz = 0, TrapA = 1, TrapB = 5, TrapC = 9, TrapD = 13, kTrapRow = 17 };
 enum { SphHasRmin = 0, SphRmin, SphRmax, SphMsqMax, SphPsqMax, SphPsqMin, SphMsqMin, kSphereRow };
+enum { OrbR = 0, OrbRMinusTol, OrbRPlusTol, kOrbRow };
+// Polycone (full phi): number of sections n, kTolerance, the n + 1 z planes, the n section
+// shifts, then one Cone row per section
+enum { PconN = 0, PconTol, PconZs };
+VGN_HD inline int pcon_ishift(int n) { return PconZs + n + 1; }
+VGN_HD inline int pcon_icone(int n, int k) { return PconZs + 2 * n + 1 + k * kConeRow; }
 }  // namespace irow
 
 // Row layouts (doubles) of GeomView::shape per shape type.
@@ -187,11 +201,6 @@ enum { SphRmin = 0, SphRmax, SphA1x, SphA1y, SphA2x, SphA2y, SphN1x, SphN1y, Sph
 // Polycone, variable length: [0] section count n, [1, n+1] the n+1 z planes, [n+2, 2n+1]
 // the section z shifts, then n cone rows of kConeSize doubles, then the raw phi start and
 // total angle
-#ifdef __CUDACC__
-#define VGN_HD __host__ __device__
-#else
-#define VGN_HD
-#endif
 constexpr int PconNSec = 0;
 constexpr int PconZs   = 1;
 VGN_HD inline int pcon_shift(int n) { return 2 + n; }
@@ -217,6 +226,7 @@ struct GeomView {
   const IXForm *ixf;         // per placed volume
   const float *isin;         // interval SafetyToIn rows (irow), (lo, hi) pairs
   const double *shape;
+  const double *lv_bbox;     // per logical volume: its shape's Extent, min then max corner (6 doubles)
   uint32_t navind_words;
   int32_t n_pv;
   int32_t n_lv;

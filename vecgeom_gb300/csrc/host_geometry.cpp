@@ -433,6 +433,14 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
     r.shape     = g.lv[r.lv].shape;
     r.shape_row = g.lv[r.lv].shape_row;
   }
+  // every shape's bounding box, as VUnplacedVolume::ComputeBBox caches it at construction
+  g.lv_bbox.assign(6 * g.lv.size(), 0.);
+  for (size_t l = 0; l < g.lv.size(); ++l) {
+    Vec3 lower, upper;
+    shape_extent(g.lv[l].shape, &g.shape[g.lv[l].shape_row], lower, upper);
+    const double b[6] = {lower.x, lower.y, lower.z, upper.x, upper.y, upper.z};
+    std::copy(b, b + 6, g.lv_bbox.begin() + 6 * l);
+  }
   g.lv_rec.assign(g.lv.size(), LVRec());
   g.daughters.clear();
   g.nodes.clear();
@@ -452,7 +460,8 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
     r.nodes_off = (int32_t)g.nodes.size();
     r.n_nodes   = (int32_t)lv.bvh.nodes.size();
     r.prims_off = (int32_t)g.prims.size();
-    r.depth     = lv.bvh.depth;
+    r.depth     = (uint16_t)lv.bvh.depth;
+    for (int d : lv.daughters) r.dtypes |= (uint16_t)(1u << g.lv[g.pv[d].lv].shape);
     for (size_t k = 0; k < lv.bvh.nodes.size(); ++k) {
       NodeRec n;
       FNodeRec f;
@@ -504,7 +513,7 @@ void set_interval(float *lo, float *hi, double v)
 
 // Appends the interval SafetyToIn row (geom_types.h irow) of one shape to `out` and
 // returns its first pair index, or -1 for shapes without one (Box uses IXForm's
-// half-lengths; Polycone is evaluated in FP64).  Each derived value is computed with
+// half-lengths; phi or theta sections and the CutTube are evaluated in FP64).  Each derived value is computed with
 // the same FP64 operations as the device's SafetyToIn (host code is built with
 // -ffp-contract=off), so its enclosure also encloses the device's double.
 static int build_isin_row(int shape, const double *r, std::vector<float> &out)
@@ -557,6 +566,27 @@ static int build_isin_row(int shape, const double *r, std::vector<float> &out)
          std::fabs(rmin * (rmin - 2.0 * kTolerance))};
     break;
   }
+  case kOrb:  // OrbImplementation.h SafetyToIn: |p| - R, with the tolerance shell around R
+    v = {r[0], r[0] - kTolerance, r[0] + kTolerance};
+    break;
+  case kPolycone: {  // PolyconeImplementation.h:381-450 over the sections' (full) cone rows
+    const int n = (int)r[row::PconNSec];
+    std::vector<float> cones;
+    for (int k = 0; k < n; ++k)
+      if (build_isin_row(kCone, r + row::pcon_cone(n, k), cones) < 0) return -1;  // phi section
+    v = {(double)n, kTolerance};
+    for (int k = 0; k <= n; ++k) v.push_back(r[row::PconZs + k]);
+    for (int k = 0; k < n; ++k) v.push_back(r[row::pcon_shift(n) + k]);
+    const int pos = (int)(out.size() / 2);
+    for (double d : v) {
+      float lo, hi;
+      set_interval(&lo, &hi, d);
+      out.push_back(lo);
+      out.push_back(hi);
+    }
+    out.insert(out.end(), cones.begin(), cones.end());
+    return pos;
+  }
   default: return -1;
   }
   const int pos = (int)(out.size() / 2);
@@ -606,6 +636,7 @@ void build_interval_images(HostGeometry &g)
     slab(g.prims[i].mn, g.prims[i].mx, p.mn_lo, p.mn_hi, p.mx_lo, p.mx_hi);
     p.pv   = g.prims[i].pv;
     p.prim = g.prims[i].prim;
+    p.shape = g.lv[g.pv[p.pv].lv].shape;
     safe(g.prims[i].mn, g.prims[i].mx, g.iprim_safe[i]);
   }
   // interval SafetyToIn rows, one per logical volume of a shape that has one

@@ -74,6 +74,7 @@ struct HostGeometry {
   std::vector<ISafe> iprim_safe;
   std::vector<IXForm> ixf;
   std::vector<float> isin;  // interval SafetyToIn rows (geom_types.h irow), (lo, hi) pairs
+  std::vector<double> lv_bbox;  // per logical volume: shape Extent, min then max corner (VUnplacedVolume::fBBox)
   bool sections = false;    // some shape has a phi or theta section: needs the `sections` kernel set
 };
 

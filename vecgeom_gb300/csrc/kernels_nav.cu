@@ -7,6 +7,7 @@
 // form uses explicitly rounded intrinsics, which are never contracted.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -62,6 +63,250 @@ __global__ void __launch_bounds__(BLOCK, MINB) step_kernel(GeomView g, int64_t n
     store_state(out, i, o);
   }
 }
+
+// Step kernel of the mixed form with the FP64 DistanceToIn of the BVH candidates grouped by
+// shape type across the whole block.  Per round of BLOCK tracks:
+//   1. each thread: step start, FP32 traversal into its candidate queue, its local point and
+//      direction into shared memory, and for every candidate that may be computed ahead
+//      (step_pending) a place in its shape type's part of the block's item list;
+//   2. the list is laid out type after type, each part padded to a multiple of 32 entries;
+//   3. every warp takes 32 consecutive entries at a time -- candidates of one shape type,
+//      from any thread of the block -- and computes their DistanceToIn into the owners' slots;
+//   4. each thread: the reference's acceptance rule over its queue in visit order
+//      (step_replay), then PrepareOutState and relocation.
+// Every value is computed by the same FP64 code as in the other kernels, and a candidate's
+// DistanceToIn does not depend on when or by which thread it is computed, so the results
+// are those of step_kernel.  Shared memory after the per-thread words: local points and
+// directions (6 doubles per thread), per-type counters and offsets, the item list (16-bit
+// entries: owner thread << 4 | queue slot; 0xffff pads).
+#if VGN_SMEM_STACK
+constexpr int kGroupPad        = 32;
+constexpr uint16_t kGroupEmpty = 0xffffu;
+static_assert(kMaxStepCand <= 16, "queue slot in 4 bits of an item entry");
+template <int BLOCK>
+struct GroupLayout {
+  static_assert(BLOCK <= 1024 && BLOCK % 32 == 0, "owner thread in 12 bits; whole warps");
+  static constexpr int kListCap       = BLOCK * kMaxStepCand + kNumShapes * kGroupPad;
+  static constexpr size_t kThreadBytes = (size_t)kStepSmemWords * BLOCK * sizeof(uint32_t);
+  static constexpr size_t kRayBytes    = (size_t)6 * BLOCK * sizeof(double);
+  static constexpr size_t kCountBytes  = 64 * sizeof(uint32_t);  // counters [16], offsets [17], chunk counter at 48
+  static constexpr size_t kBytes       = kThreadBytes + kRayBytes + kCountBytes + (size_t)kListCap * sizeof(uint16_t);
+};
+
+// One navigation step (nav_step<true> semantics) of every live thread of the block, with the
+// candidates' DistanceToIn grouped by shape type across the block.  Called by every thread of
+// the block (it holds barriers); `live` threads step from (gp, gd, s) and receive the step in
+// `st` and the propagated state in `o`.
+template <int BLOCK>
+__device__ __forceinline__ void grouped_step(const GeomView &g, bool live, D3 gp, D3 gd, double slimit,
+                                             const State &s, State &o, bool reloc, double &st)
+{
+  using L       = GroupLayout<BLOCK>;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double *ray   = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(vgn_step_smem) + L::kThreadBytes);
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(ray + 6 * BLOCK);
+  uint32_t *off = cnt + 16;  // off[t]: first entry of type t; off[kNumShapes]: list length
+  uint16_t *list = reinterpret_cast<uint16_t *>(cnt + 64);
+  const int *cand_pv = reinterpret_cast<const int *>(vgn_step_smem + kStackSize * BLOCK);
+  const SlotWords own{vgn_step_smem + tid, BLOCK};
+  // 1. step start and traversal (the counters were cleared by the previous round or at entry)
+  D3 lp = d3(0., 0., 0.), ld = d3(0., 0., 0.);
+  LVRec lv{};
+  int hit = -1, last = 0;
+  MixedRay r;
+  StepCands c;
+  c.n = 0;
+  FI stepI{0.f, 0.f};
+  unsigned done = 0;
+  st = 0.;
+  if (live) {
+    step_begin(g, gp, gd, s, lp, ld, lv, st);
+    make_ray(r, lp, ld);
+    stepI = fi(st);
+    last  = ni_top(g, s.last_exited);
+    if (lv.nd > 0) {
+      bvh_collect_step_mixed(g, lv, r, st, stepI, last, hit, c);
+      unsigned present;
+      done = step_pending(c, stepI, present);
+      ray[tid]             = lp.x;
+      ray[BLOCK + tid]     = lp.y;
+      ray[2 * BLOCK + tid] = lp.z;
+      ray[3 * BLOCK + tid] = ld.x;
+      ray[4 * BLOCK + tid] = ld.y;
+      ray[5 * BLOCK + tid] = ld.z;
+      for (unsigned rest = done; rest; rest &= rest - 1) {
+        const int q  = __ffs(rest) - 1;
+        own.word(q) = atomicAdd(&cnt[c.type(q)], 1u);  // place within its type
+      }
+    }
+  }
+  __syncthreads();
+  // 2. list layout: exclusive scan of the padded per-type counts, pads marked empty
+  if (warp == 0) {
+    const uint32_t v      = lane < kNumShapes ? cnt[lane] : 0u;
+    const uint32_t padded = (v + kGroupPad - 1) & ~(uint32_t)(kGroupPad - 1);
+    uint32_t incl         = padded;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += y;
+    }
+    const uint32_t excl = incl - padded;
+    if (lane <= kNumShapes) off[lane] = excl;
+    for (int u = 0; u < kNumShapes; ++u) {
+      const uint32_t cu = __shfl_sync(0xffffffffu, v, u);
+      const uint32_t ou = __shfl_sync(0xffffffffu, excl, u);
+      const uint32_t pu = __shfl_sync(0xffffffffu, padded, u);
+      if (cu + (uint32_t)lane < pu) list[ou + cu + lane] = kGroupEmpty;
+    }
+  }
+  __syncthreads();
+  for (unsigned rest = done; rest; rest &= rest - 1) {
+    const int q = __ffs(rest) - 1;
+    list[off[c.type(q)] + own.word(q)] = (uint16_t)((tid << 4) | q);
+  }
+  __syncthreads();
+  // 3. 32 entries of one shape type per warp and turn
+  const uint32_t total = off[kNumShapes];
+  for (uint32_t j = (uint32_t)warp * 32u; j < total; j += BLOCK) {
+    const uint16_t e = list[j + lane];
+    if (e != kGroupEmpty) {
+      const int ow = e >> 4, q = e & 15;
+      const D3 olp = d3(ray[ow], ray[BLOCK + ow], ray[2 * BLOCK + ow]);
+      const D3 old = d3(ray[3 * BLOCK + ow], ray[4 * BLOCK + ow], ray[5 * BLOCK + ow]);
+      SlotWords{vgn_step_smem + ow, BLOCK}.put(q, pv_dist_in(g, cand_pv[q * BLOCK + ow], olp, old, kInfLength));
+    }
+  }
+  if (tid < 16) cnt[tid] = 0;  // for the next round; no thread reads the counters until then
+  __syncthreads();
+  // 4. acceptance in visit order, out state, relocation
+  if (live) {
+    if (lv.nd > 0) step_replay(g, r, c, done, own, st, stepI, last, hit);
+    st = step_finish<true>(g, lp, ld, slimit, s, o, reloc, st, hit);
+  }
+}
+
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) step_kernel_grouped(GeomView g, int64_t n, const double *__restrict__ px,
+                                                           const double *__restrict__ py, const double *__restrict__ pz,
+                                                           const double *__restrict__ dx, const double *__restrict__ dy,
+                                                           const double *__restrict__ dz, const double *__restrict__ slimit,
+                                                           const vgn_state *__restrict__ in, vgn_state *__restrict__ out,
+                                                           double *__restrict__ step, int reloc,
+                                                           const uint32_t *__restrict__ perm)
+{
+  uint32_t *cnt = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(vgn_step_smem) +
+                                               GroupLayout<BLOCK>::kThreadBytes + GroupLayout<BLOCK>::kRayBytes);
+  if (threadIdx.x < 16) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t base = (int64_t)blockIdx.x * BLOCK; base < n; base += (int64_t)gridDim.x * BLOCK) {
+    const int64_t t = base + threadIdx.x;
+    int64_t i       = 0;
+    State s{}, o{};
+    bool ok = false;
+    D3 gp = d3(0., 0., 0.), gd = d3(0., 0., 0.);
+    double sl = 0.;
+    if (t < n) {
+      i  = perm ? (int64_t)__ldg(perm + t) : t;
+      s  = load_state(in, i);
+      o  = s;
+      ok = ni_valid(g, s.nav_ind) && !(s.last_exited != 0 && !ni_valid(g, s.last_exited));
+      if (!ok) raise_error(g, kErrState);
+      if (ok) {
+        gp = d3(px[i], py[i], pz[i]);
+        gd = d3(dx[i], dy[i], dz[i]);
+        sl = slimit[i];
+      }
+    }
+    double st;
+    grouped_step<BLOCK>(g, ok, gp, gd, sl, s, o, reloc != 0, st);
+    if (t < n) {
+      step[i] = ok ? st : 0.;
+      store_state(out, i, o);
+    }
+  }
+}
+
+// Transport loop (walk_kernel semantics) with block-grouped steps.  Each block walks its own
+// chunk of kWalkChunk * BLOCK consecutive tracks (of the visit order): a thread whose track has
+// left the world (or used max_steps) takes the chunk's next track from a shared-memory counter,
+// so the block's threads stay busy until the chunk is done, and every round is one
+// grouped_step over the block's live tracks.  A block lives as long as its chunk, so work of
+// higher-priority streams finds free multiprocessors within about that time.
+constexpr int kWalkChunk = 4;
+
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) walk_kernel_grouped(GeomView g, int64_t n, double *__restrict__ px,
+                                                           double *__restrict__ py, double *__restrict__ pz,
+                                                           const double *__restrict__ dx, const double *__restrict__ dy,
+                                                           const double *__restrict__ dz,
+                                                           const double *__restrict__ slimit,
+                                                           vgn_state *__restrict__ state, int max_steps,
+                                                           int32_t *__restrict__ nsteps,
+                                                           const uint32_t *__restrict__ perm)
+{
+  uint32_t *cnt  = reinterpret_cast<uint32_t *>(reinterpret_cast<unsigned char *>(vgn_step_smem) +
+                                                GroupLayout<BLOCK>::kThreadBytes + GroupLayout<BLOCK>::kRayBytes);
+  uint32_t *next = cnt + 48;  // the chunk's track counter (after the counters and offsets)
+  for (int64_t base = (int64_t)blockIdx.x * kWalkChunk * BLOCK; base < n;
+       base += (int64_t)gridDim.x * kWalkChunk * BLOCK) {
+    const int64_t chunk_n = n - base < (int64_t)kWalkChunk * BLOCK ? n - base : (int64_t)kWalkChunk * BLOCK;
+    if (threadIdx.x < 16) cnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *next = 0;
+    __syncthreads();
+    int64_t i = -1;  // the thread's track, -1: none
+    bool more = true;  // the chunk may still hold tracks
+    D3 p = d3(0., 0., 0.), d = d3(0., 0., 0.);
+    double sl = 0.;
+    State s{};
+    int k = 0;
+    for (;;) {
+      while (i < 0 && more) {  // take the chunk's next track that needs a step
+        const uint32_t c = atomicAdd(next, 1u);
+        if ((int64_t)c >= chunk_n) {
+          more = false;
+          break;
+        }
+        const int64_t t = base + c;
+        i = perm ? (int64_t)__ldg(perm + t) : t;
+        s = load_state(state, i);
+        if (s.nav_ind != 0 && (!ni_valid(g, s.nav_ind) || (s.last_exited != 0 && !ni_valid(g, s.last_exited)))) {
+          raise_error(g, kErrState);
+          nsteps[i] = -1;
+          i         = -1;
+          continue;
+        }
+        if (s.nav_ind == 0 || max_steps <= 0) {  // nothing to do: outside the world already
+          nsteps[i] = 0;
+          i         = -1;
+          continue;
+        }
+        p  = d3(px[i], py[i], pz[i]);
+        d  = d3(dx[i], dy[i], dz[i]);
+        sl = slimit[i];
+        k  = 0;
+      }
+      const bool live = i >= 0;
+      if (!__syncthreads_or(live)) break;
+      State o = s;
+      double st;
+      grouped_step<BLOCK>(g, live, p, d, sl, s, o, true, st);
+      if (live) {
+        p = d3(p.x + st * d.x, p.y + st * d.y, p.z + st * d.z);
+        s = o;
+        ++k;
+        if (s.nav_ind == 0 || k >= max_steps) {
+          px[i] = p.x;
+          py[i] = p.y;
+          pz[i] = p.z;
+          store_state(state, i, s);
+          nsteps[i] = k;
+          i         = -1;
+        }
+      }
+    }
+  }
+}
+#endif  // VGN_SMEM_STACK
 
 // Persistent multi-job step: every warp repeatedly takes the next 32-track chunk from the
 // work queue, finds its job (jobs are laid out back to back in chunk space) and steps
@@ -236,6 +481,33 @@ __global__ void __launch_bounds__(256) locate_kernel(GeomView g, int64_t n, cons
   }
 }
 
+// BVH::ApproachNextDaughter (BVH.cpp:395-449) per track over the BVH of logical volume lvs[i];
+// a volume id out of range or without daughters, or a last-exited id out of range, is recorded
+// as an invalid input (kErrState) and leaves the track's step as it was
+__global__ void __launch_bounds__(256) approach_kernel(GeomView g, int64_t n, const int32_t *__restrict__ lvs,
+                                                       const double *__restrict__ px, const double *__restrict__ py,
+                                                       const double *__restrict__ pz, const double *__restrict__ dx,
+                                                       const double *__restrict__ dy, const double *__restrict__ dz,
+                                                       const int32_t *__restrict__ last, double *__restrict__ step)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int l      = __ldg(lvs + i);
+    const int lastpv = last ? __ldg(last + i) : -1;
+    if (l < 0 || l >= g.n_lv || lastpv < -1 || lastpv >= g.n_pv) {
+      raise_error(g, kErrState);
+      continue;
+    }
+    const LVRec lv = load_lv(g, l);
+    if (lv.nd == 0) {
+      raise_error(g, kErrState);
+      continue;
+    }
+    double st = step[i];
+    bvh_approach(g, lv, d3(px[i], py[i], pz[i]), d3(dx[i], dy[i], dz[i]), st, lastpv);
+    step[i] = st;
+  }
+}
+
 // unplaced shape queries on one logical volume
 template <int OP>
 __global__ void __launch_bounds__(256) shape_kernel_fp64(int type, const double *__restrict__ row, int64_t n,
@@ -310,7 +582,6 @@ struct StepVariant {
 static constexpr StepVariant kStepVariants[] = {{256, 2}, {256, 3}, {128, 6}, {256, 4}, {128, 5}, {128, 4}};
 static constexpr int kNumStepVariants        = sizeof(kStepVariants) / sizeof(kStepVariants[0]);
 
-int step_variant_count() { return kNumStepVariants; }
 
 template <bool MIXED, int BLOCK, int MINB>
 static void launch_step_v(const GeomView &g, const StepArgs &a, cudaStream_t s)
@@ -322,9 +593,40 @@ static void launch_step_v(const GeomView &g, const StepArgs &a, cudaStream_t s)
       g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, a.slimit, a.in, a.out, a.step, a.reloc, a.perm);
 }
 
+// Variants of the mixed form with block-wide grouping (step_kernel_grouped), after the
+// kStepVariants: shared memory decides the resident blocks (128 threads: 43 KiB per block,
+// 256 threads: 85 KiB).
+static constexpr StepVariant kGroupedVariants[] = {{128, 5}, {128, 4}, {256, 2}};
+static constexpr int kNumGroupedVariants        = sizeof(kGroupedVariants) / sizeof(kGroupedVariants[0]);
+
+int step_variant_count(bool mixed) { return kNumStepVariants + (mixed ? kNumGroupedVariants : 0); }
+int multi_variant_count() { return kNumStepVariants; }
+
+template <int BLOCK, int MINB>
+static void launch_step_grouped(const GeomView &g, const StepArgs &a, cudaStream_t s)
+{
+#if !VGN_SMEM_STACK  // the grouping keeps its queues in shared memory: plain mixed step instead
+  launch_step_v<true, BLOCK, MINB>(g, a, s);
+#else
+  const size_t smem   = dev::GroupLayout<BLOCK>::kBytes;
+  const unsigned grid = grid_for(a.n, BLOCK, a.max_blocks * (256 / BLOCK));
+  if (allow_smem(dev::step_kernel_grouped<BLOCK, MINB>, smem) != cudaSuccess) return;
+  dev::step_kernel_grouped<BLOCK, MINB><<<grid, BLOCK, smem, s>>>(g, a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz,
+                                                                  a.slimit, a.in, a.out, a.step, a.reloc, a.perm);
+#endif
+}
+
 template <bool MIXED>
 static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cudaStream_t s)
 {
+  if (MIXED) {
+    switch (variant) {
+    case 6: launch_step_grouped<128, 5>(g, a, s); return;
+    case 7: launch_step_grouped<128, 4>(g, a, s); return;
+    case 8: launch_step_grouped<256, 2>(g, a, s); return;
+    default: break;
+    }
+  }
   switch (variant) {
   case 1: launch_step_v<MIXED, 256, 3>(g, a, s); break;
   case 2: launch_step_v<MIXED, 128, 6>(g, a, s); break;
@@ -404,10 +706,38 @@ cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, i
   return cudaGetLastError();
 }
 
+template <int BLOCK, int MINB>
+static cudaError_t launch_walk_grouped(const GeomView &g, int64_t n, double *px, double *py, double *pz,
+                                       const double *dx, const double *dy, const double *dz, const double *slimit,
+                                       vgn_state *state, int max_steps, int32_t *nsteps, const uint32_t *perm,
+                                       int max_blocks, cudaStream_t s)
+{
+#if VGN_SMEM_STACK
+  const unsigned grid = grid_for(n, dev::kWalkChunk * BLOCK, max_blocks);
+  const size_t smem   = dev::GroupLayout<BLOCK>::kBytes;
+  cudaError_t e       = allow_smem(dev::walk_kernel_grouped<BLOCK, MINB>, smem);
+  if (e != cudaSuccess) return e;
+  dev::walk_kernel_grouped<BLOCK, MINB><<<grid, BLOCK, smem, s>>>(g, n, px, py, pz, dx, dy, dz, slimit, state,
+                                                                 max_steps, nsteps, perm);
+  return cudaGetLastError();
+#else
+  return cudaErrorNotSupported;
+#endif
+}
+
 cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, double *pz, const double *dx,
                         const double *dy, const double *dz, const double *slimit, vgn_state *state, int max_steps,
-                        int32_t *nsteps, const uint32_t *perm, bool mixed, int max_blocks, cudaStream_t s)
+                        int32_t *nsteps, const uint32_t *perm, bool mixed, int variant, int max_blocks,
+                        cudaStream_t s)
 {
+  if (mixed && VGN_SMEM_STACK) {
+    switch (variant) {
+    case 6: return launch_walk_grouped<128, 5>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps, perm, max_blocks, s);
+    case 7: return launch_walk_grouped<128, 4>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps, perm, max_blocks, s);
+    case 8: return launch_walk_grouped<256, 2>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps, perm, max_blocks, s);
+    default: break;
+    }
+  }
   const int block     = 128;
   const unsigned grid = grid_for(n, block, max_blocks * 2);
   const size_t smem   = step_smem_bytes(block);
@@ -440,6 +770,16 @@ cudaError_t launch_locate(const GeomView &g, int64_t n, const double *px, const 
     dev::locate_kernel<true><<<grid, block, locate_smem_bytes(block), s>>>(g, n, px, py, pz, out);
   else
     dev::locate_kernel<false><<<grid, block, locate_smem_bytes(block), s>>>(g, n, px, py, pz, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_approach(const GeomView &g, int64_t n, const int32_t *lv, const double *px, const double *py,
+                            const double *pz, const double *dx, const double *dy, const double *dz,
+                            const int32_t *last, double *step, int max_blocks, cudaStream_t s)
+{
+  const int block     = 256;
+  const unsigned grid = grid_for(n, block, max_blocks);
+  dev::approach_kernel<<<grid, block, locate_smem_bytes(block), s>>>(g, n, lv, px, py, pz, dx, dy, dz, last, step);
   return cudaGetLastError();
 }
 

@@ -11,7 +11,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "launch.h"
 
@@ -159,24 +158,15 @@ static __device__ __align__(256) uint32_t g_static_scratch[kStaticScratchWords];
 
 size_t static_scratch_words() { return kStaticScratchWords; }
 
-// Address of the current device's copy of the buffer, looked up once per device.
+// Address of the buffer in the current context, looked up on every call (no allocation): an
+// address kept from an earlier call would go stale after cudaDeviceReset or in another
+// context on the same device.
 cudaError_t static_scratch(uint32_t **ptr)
 {
-  constexpr int kMaxDevices = 64;
-  static std::mutex lock;
-  static uint32_t *addr[kMaxDevices] = {};
-  int dev       = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p             = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> guard(lock);
-  if (!addr[dev]) {
-    void *p = nullptr;
-    e       = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess) return e;
-    addr[dev] = static_cast<uint32_t *>(p);
-  }
-  *ptr = addr[dev];
+  *ptr = static_cast<uint32_t *>(p);
   return cudaSuccess;
 }
 

@@ -280,6 +280,9 @@ struct SArr {
 #endif
 constexpr int kMaxStepCand   = 16;
 constexpr int kStepSmemWords = VGN_SMEM_STACK ? kStackSize + 2 * kMaxStepCand : 0;
+// the step's FP64 phase keeps one double per queue slot in the (then free) traversal stack
+// and one 4-bit shape type per slot in a 64-bit word
+static_assert(2 * kMaxStepCand <= kStackSize && kMaxStepCand <= 16 && kNumShapes <= 16, "step queue layout");
 extern __shared__ uint32_t vgn_step_smem[];
 
 #if VGN_SMEM_STACK
@@ -312,6 +315,85 @@ __device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVR
           const int vol     = __ldg(&q.pv);
           const double dist = pv_dist_in(g, vol, lp, ld, step);
           if (dist < step && !(dist <= 0.0 && vol == last)) step = dist, hit = vol;
+        }
+      }
+    } else {
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      double tminL, tmaxL, tminR, tmaxR;
+      slab(nodes[L].mn, nodes[L].mx, lp, inv, tminL, tmaxL);
+      slab(nodes[R].mn, nodes[R].mx, lp, inv, tminR, tmaxR);
+      const bool trL = tminL <= tmaxL && tmaxL >= 0.0 && tminL < step;
+      const bool trR = tminR <= tmaxR && tmaxR >= 0.0 && tminR < step;
+      if (sp + 2 > g.stack_limit) {
+        raise_error(g, kErrStack);
+        return false;
+      }
+      if (tminR < tminL) {
+        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = L;
+      } else {
+        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = R;
+      }
+    }
+  } while (sp > 0);
+  return true;
+}
+
+// VUnplacedVolume::ApproachSolid (UnplacedVolume.h:274-281): the ray's entry into the shape's
+// bounding box `bb` (min then max corner: its Extent, cached at construction) by
+// BoxImplementation::IntersectCachedKernel2 (BoxImplementation.h:326-368), t0 = 0, t1 = kInfLength
+__device__ __forceinline__ double approach_solid(const double *bb, D3 p, D3 inv)
+{
+  const int sx = inv.x < 0, sy = inv.y < 0, sz = inv.z < 0;
+  double tmin        = (__ldg(bb + 3 * sx) - p.x) * inv.x;
+  const double tymax = (__ldg(bb + 3 * (1 - sy) + 1) - p.y) * inv.y;
+  bool done          = tmin > tymax;
+  if (done) return kInfLength;
+  double tmax        = (__ldg(bb + 3 * (1 - sx)) - p.x) * inv.x;
+  const double tymin = (__ldg(bb + 3 * sy + 1) - p.y) * inv.y;
+  done |= tymin > tmax;
+  if (done) return kInfLength;
+  tmin               = vmax(tmin, tymin);
+  tmax               = vmin(tmax, tymax);
+  const double tzmin = (__ldg(bb + 3 * sz + 2) - p.z) * inv.z;
+  const double tzmax = (__ldg(bb + 3 * (1 - sz) + 2) - p.z) * inv.z;
+  done |= (tmin > tzmax) || (tzmin > tmax);
+  if (done) return kInfLength;
+  tmin = vmax(tmin, tzmin);
+  tmax = vmin(tmax, tzmax);
+  done |= !((tmin <= kInfLength + kTolerance) && (tmax > 0. - kTolerance));
+  return done ? kInfLength : tmin;
+}
+
+// BVH::ApproachNextDaughter (BVH.cpp:395-449): the traversal of CheckDaughterIntersections with
+// each candidate daughter's ApproachSolid, in the daughter's frame, in place of its DistanceToIn
+__device__ __forceinline__ bool bvh_approach(const GeomView &g, const LVRec &lv, D3 lp, D3 ld, double &step, int last)
+{
+  VGN_TRAVERSAL_STACK(stack);
+  int sp        = 1;
+  stack[0]      = 0;
+  const D3 inv  = d3(1.0 / nonzero(ld.x), 1.0 / nonzero(ld.y), 1.0 / nonzero(ld.z));
+  const NodeRec *nodes = g.nodes + lv.nodes_off;
+  const PrimRec *prims = g.prims + lv.prims_off;
+  do {
+    const unsigned id = stack[--sp];
+    const int nchild  = __ldg(&nodes[id].nchild);
+    if (nchild >= 0) {
+      const int off = __ldg(&nodes[id].offset);
+      for (int i = 0; i < nchild; ++i) {
+        const PrimRec &q = prims[off + i];
+        double tmin, tmax;
+        slab(q.mn, q.mx, lp, inv, tmin, tmax);
+        if (tmin <= tmax && tmax >= 0.0 && tmin < step) {
+          const int vol = __ldg(&q.pv);
+          PvXf x;
+          load_pv_xf(g, vol, x);
+          const D3 p        = xf_point(x.t, x.r, lp);
+          const D3 d        = xf_dir(x.r, ld);
+          const D3 dinv     = d3(1.0 / nonzero(d.x), 1.0 / nonzero(d.y), 1.0 / nonzero(d.z));
+          const double dist = approach_solid(g.lv_bbox + 6 * __ldg(&g.pv[vol].lv), p, dinv);
+          if (dist < step && !(dist <= 0.0 && vol == last)) step = dist;
         }
       }
     } else {
@@ -421,7 +503,8 @@ __device__ __forceinline__ LVRec load_lv(const GeomView &g, int lvi)
   const int4 *src = reinterpret_cast<const int4 *>(g.lv + lvi);
   int4 a = __ldg(src), b = __ldg(src + 1);
   r.shape = a.x; r.shape_row = a.y; r.nd = a.z; r.daughters_off = a.w;
-  r.nodes_off = b.x; r.n_nodes = b.y; r.prims_off = b.z; r.depth = b.w;
+  r.nodes_off = b.x; r.n_nodes = b.y; r.prims_off = b.z;
+  r.depth = (uint16_t)((unsigned)b.w & 0xffffu); r.dtypes = (uint16_t)((unsigned)b.w >> 16);
   return r;
 }
 

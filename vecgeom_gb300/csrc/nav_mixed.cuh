@@ -86,6 +86,9 @@ __device__ __forceinline__ FI fi_mul_signed(FI a, FI b, bool bneg)
   if (!bneg) return FI{__fmul_rd(a.lo, a.lo >= 0.f ? b.lo : b.hi), __fmul_ru(a.hi, a.hi >= 0.f ? b.hi : b.lo)};
   return FI{__fmul_rd(a.hi, a.hi >= 0.f ? b.lo : b.hi), __fmul_ru(a.lo, a.lo >= 0.f ? b.hi : b.lo)};
 }
+// product with a rotation entry's interval: the outward-rounded image of one double, so both
+// ends have the double's sign (or are 0) and the interval never contains 0 in its interior
+__device__ __forceinline__ FI fi_mul_rot(FI a, FI r) { return fi_mul_signed(a, r, r.hi <= 0.f); }
 __device__ __forceinline__ FI fi_abs(FI a)
 {
   if (a.lo >= 0.f) return a;
@@ -186,9 +189,9 @@ __device__ __forceinline__ FI ibox_safety_in(const IXForm &x, const FI *p)
   FI m;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    FI l = fi_mul(t[0], FI{__ldg(&x.r_lo[i]), __ldg(&x.r_hi[i])});
-    l    = fi_add(l, fi_mul(t[1], FI{__ldg(&x.r_lo[3 + i]), __ldg(&x.r_hi[3 + i])}));
-    l    = fi_add(l, fi_mul(t[2], FI{__ldg(&x.r_lo[6 + i]), __ldg(&x.r_hi[6 + i])}));
+    FI l = fi_mul_rot(t[0], FI{__ldg(&x.r_lo[i]), __ldg(&x.r_hi[i])});
+    l    = fi_add(l, fi_mul_rot(t[1], FI{__ldg(&x.r_lo[3 + i]), __ldg(&x.r_hi[3 + i])}));
+    l    = fi_add(l, fi_mul_rot(t[2], FI{__ldg(&x.r_lo[6 + i]), __ldg(&x.r_hi[6 + i])}));
     const FI v = fi_sub(fi_abs(l), FI{__ldg(&x.h_lo[i]), __ldg(&x.h_hi[i])});
     m          = i == 0 ? v : fi_max(m, v);
   }
@@ -228,9 +231,9 @@ __device__ __forceinline__ void ixf_local(const IXForm &x, const FI *p, FI *l)
   for (int k = 0; k < 3; ++k) t[k] = fi_sub(p[k], FI{__ldg(&x.t_lo[k]), __ldg(&x.t_hi[k])});
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    FI v = fi_mul(t[0], FI{__ldg(&x.r_lo[i]), __ldg(&x.r_hi[i])});
-    v    = fi_add(v, fi_mul(t[1], FI{__ldg(&x.r_lo[3 + i]), __ldg(&x.r_hi[3 + i])}));
-    l[i] = fi_add(v, fi_mul(t[2], FI{__ldg(&x.r_lo[6 + i]), __ldg(&x.r_hi[6 + i])}));
+    FI v = fi_mul_rot(t[0], FI{__ldg(&x.r_lo[i]), __ldg(&x.r_hi[i])});
+    v    = fi_add(v, fi_mul_rot(t[1], FI{__ldg(&x.r_lo[3 + i]), __ldg(&x.r_hi[3 + i])}));
+    l[i] = fi_add(v, fi_mul_rot(t[2], FI{__ldg(&x.r_lo[6 + i]), __ldg(&x.r_hi[6 + i])}));
   }
 }
 
@@ -255,12 +258,12 @@ __device__ __forceinline__ bool icone_safe_in(const float *q, const FI *p, FI &o
   int inside         = fi_lt(distz, iq(q, ConeMinusConeTol));
   {  // rsq < |R (R - 2 tol)|, R the outer radius at z (ConeUtilities.h GetRadiusOfConeAtPoint)
     const FI R = iflag(q, ConeOuterConst) ? iq(q, ConeOuterR)
-                                          : fi_add(fi_mul(iq(q, ConeOuterSlope), p[2]), iq(q, ConeOuterOffset));
+                                          : fi_add(fi_mul_rot(p[2], iq(q, ConeOuterSlope)), iq(q, ConeOuterOffset));
     inside = and3(inside, fi_lt(rsq, fi_abs(fi_mul(R, fi_sub(R, iq(q, ConeTwoOuterTol))))), kYes);
   }
   if (hasrmin) {  // rsq > R (R + 2 tol), R the inner radius at z
     const FI R = iflag(q, ConeInnerConst) ? iq(q, ConeInnerR)
-                                          : fi_add(fi_mul(iq(q, ConeInnerSlope), p[2]), iq(q, ConeInnerOffset));
+                                          : fi_add(fi_mul_rot(p[2], iq(q, ConeInnerSlope)), iq(q, ConeInnerOffset));
     inside = and3(inside, fi_lt(fi_mul(R, fi_add(R, iq(q, ConeTwoInnerTol))), rsq), kYes);
   }
   if (inside == kMaybe) return false;
@@ -269,11 +272,11 @@ __device__ __forceinline__ bool icone_safe_in(const float *q, const FI *p, FI &o
     return true;
   }
   const FI rho = fi_sqrt(rsq);
-  const FI pRMax = fi_add(fi_mul(iq(q, ConeTanRMax), p[2]), iq(q, ConeAvgRmax));
-  FI s           = fi_neg(fi_mul(fi_sub(pRMax, rho), iq(q, ConeInvSecRMax)));
+  const FI pRMax = fi_add(fi_mul_rot(p[2], iq(q, ConeTanRMax)), iq(q, ConeAvgRmax));
+  FI s           = fi_neg(fi_mul_rot(fi_sub(pRMax, rho), iq(q, ConeInvSecRMax)));
   if (hasrmin) {
-    const FI pRMin = fi_add(fi_mul(iq(q, ConeTanRMin), p[2]), iq(q, ConeAvgRmin));
-    s              = fi_max(s, fi_neg(fi_mul(fi_sub(rho, pRMin), iq(q, ConeInvSecRMin))));
+    const FI pRMin = fi_add(fi_mul_rot(p[2], iq(q, ConeTanRMin)), iq(q, ConeAvgRmin));
+    s              = fi_max(s, fi_neg(fi_mul_rot(fi_sub(rho, pRMin), iq(q, ConeInvSecRMin))));
   }
   s = fi_max(distz, s);
   // fabs(safety) < kTolerance ? 0 : safety
@@ -292,15 +295,15 @@ __device__ __forceinline__ bool itrd_safe_in(const float *q, const FI *p, FI &ou
 {
   using namespace irow;
   FI dist        = fi_sub(iq(q, TrdDz), fi_abs(p[2]));
-  const FI distx = fi_sub(iq(q, TrdHalfX), fi_mul(iq(q, TrdFx), p[2]));
+  const FI distx = fi_sub(iq(q, TrdHalfX), fi_mul_rot(p[2], iq(q, TrdFx)));
   const int okx  = fi_ge0(distx);
   if (okx == kMaybe) return false;
-  if (okx == kYes) dist = fi_min(dist, fi_mul(fi_sub(distx, fi_abs(p[0])), iq(q, TrdCalfX)));
+  if (okx == kYes) dist = fi_min(dist, fi_mul_rot(fi_sub(distx, fi_abs(p[0])), iq(q, TrdCalfX)));
   if (iflag(q, TrdVaryingY)) {
-    const FI disty = fi_sub(iq(q, TrdHalfY), fi_mul(iq(q, TrdFy), p[2]));
+    const FI disty = fi_sub(iq(q, TrdHalfY), fi_mul_rot(p[2], iq(q, TrdFy)));
     const int oky  = fi_ge0(disty);
     if (oky == kMaybe) return false;
-    if (oky == kYes) dist = fi_min(dist, fi_mul(fi_sub(disty, fi_abs(p[1])), iq(q, TrdCalfY)));
+    if (oky == kYes) dist = fi_min(dist, fi_mul_rot(fi_sub(disty, fi_abs(p[1])), iq(q, TrdCalfY)));
   } else {
     dist = fi_min(dist, fi_sub(iq(q, TrdDy1), fi_abs(p[1])));
   }
@@ -315,8 +318,8 @@ __device__ __forceinline__ bool itrap_safe_in(const float *q, const FI *p, FI &o
   FI s = fi_sub(fi_abs(p[2]), iq(q, TrapDz));
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
-    FI d = fi_add(fi_mul(iq(q, TrapA + i), p[0]), fi_mul(iq(q, TrapB + i), p[1]));
-    d    = fi_add(fi_add(d, fi_mul(iq(q, TrapC + i), p[2])), iq(q, TrapD + i));
+    FI d = fi_add(fi_mul_rot(p[0], iq(q, TrapA + i)), fi_mul_rot(p[1], iq(q, TrapB + i)));
+    d    = fi_add(fi_add(d, fi_mul_rot(p[2], iq(q, TrapC + i))), iq(q, TrapD + i));
     s    = fi_max(s, d);
   }
   out = s;
@@ -353,9 +356,90 @@ __device__ __forceinline__ bool isphere_safe_in(const float *q, const FI *p, FI 
   return true;
 }
 
+// OrbImplementation SafetyToIn (OrbImplementation.h:167-177)
+__device__ __forceinline__ bool iorb_safe_in(const float *q, const FI *p, FI &out)
+{
+  using namespace irow;
+  const FI rad = fi_sqrt(fi_add(fi_add(fi_sqr(p[0]), fi_sqr(p[1])), fi_sqr(p[2])));
+  const int in = fi_lt(rad, iq(q, OrbRMinusTol));
+  if (in == kMaybe) return false;
+  if (in == kYes) {
+    out = FI{-1.f, -1.f};
+    return true;
+  }
+  const int shell = and3(fi_lt(iq(q, OrbRMinusTol), rad), fi_lt(rad, iq(q, OrbRPlusTol)), kYes);
+  if (shell == kMaybe) return false;
+  out = shell == kYes ? FI{0.f, 0.f} : fi_sub(rad, iq(q, OrbR));
+  return true;
+}
+
+// a >= b as a tri-state
+__device__ __forceinline__ int fi_ge(FI a, FI b) { return a.lo >= b.hi ? kYes : (a.hi < b.lo ? kNo : kMaybe); }
+
+// PolyconeImplementation SafetyToIn (PolyconeImplementation.h:381-450), full phi: the section
+// of the point (PolyconeStruct::GetSectionIndex, PolyconeStruct.h:302-311, decided exactly or
+// not at all), its cone's SafetyToIn, and the scan of the neighbouring sections while their
+// z distance stays below the running minimum.
+__device__ __forceinline__ bool ipcon_safe_in(const float *q, const FI *p, FI &out)
+{
+  using namespace irow;
+  const int n = (int)__ldg(q + 2 * PconN);
+  int index   = -2;
+  const int below = fi_lt(p[2], iq(q, PconZs));
+  if (below == kMaybe) return false;
+  if (below == kYes) {
+    index = -1;
+  } else {
+    for (int i = 0; i < n; ++i) {
+      const int in = and3(fi_le(iq(q, PconZs + i), p[2]), fi_le(p[2], iq(q, PconZs + i + 1)), kYes);
+      if (in == kMaybe) return false;
+      if (in == kYes) {
+        index = i;
+        break;
+      }
+    }
+  }
+  const bool needZ = index < 0;
+  if (index == -1) index = 0;
+  if (index == -2) index = n - 1;
+  FI l[3] = {p[0], p[1], fi_sub(p[2], iq(q, pcon_ishift(n) + index))};
+  FI s;
+  if (!icone_safe_in(q + 2 * pcon_icone(n, index), l, s)) return false;
+  if (!needZ) {
+    const int small = fi_lt(s, iq(q, PconTol));
+    if (small == kMaybe) return false;
+    if (small == kNo) {
+      FI zbase = iq(q, PconZs + index + 1);
+      for (int i = index + 1; i < n; ++i) {
+        const int stop = fi_ge(fi_sub(iq(q, PconZs + i), zbase), s);
+        if (stop == kMaybe) return false;
+        if (stop == kYes) break;
+        l[2] = fi_sub(p[2], iq(q, pcon_ishift(n) + i));
+        FI si;
+        if (!icone_safe_in(q + 2 * pcon_icone(n, i), l, si)) return false;
+        s = fi_min(s, si);
+      }
+      if (index > 0) {
+        zbase = iq(q, PconZs + index - 1);
+        for (int i = index - 1; i >= 0; --i) {
+          const int stop = fi_ge(fi_sub(zbase, iq(q, PconZs + i)), s);
+          if (stop == kMaybe) return false;
+          if (stop == kYes) break;
+          l[2] = fi_sub(p[2], iq(q, pcon_ishift(n) + i));
+          FI si;
+          if (!icone_safe_in(q + 2 * pcon_icone(n, i), l, si)) return false;
+          s = fi_min(s, si);
+        }
+      }
+    }
+  }
+  out = s;
+  return true;
+}
+
 // Interval SafetyToIn of a daughter at the mother-frame interval point p: Box from
-// IXForm's half-lengths, Tube/Cone/Trd/Trapezoid/Sphere from GeomView::isin; false
-// for Polycone or an undecided branch.
+// IXForm's half-lengths, Tube/Cone/Trd/Trapezoid/Sphere/Orb/Polycone from GeomView::isin;
+// false for an undecided branch or a shape without a row (sections, CutTube).
 __device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm &x, const FI *p, FI &out)
 {
   const int type = __ldg(&x.shape);
@@ -374,6 +458,8 @@ __device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm
   case kTrd: return itrd_safe_in(q, l, out);
   case kTrapezoid: return itrap_safe_in(q, l, out);
   case kSphere: return isphere_safe_in(q, l, out);
+  case kOrb: return iorb_safe_in(q, l, out);
+  case kPolycone: return ipcon_safe_in(q, l, out);
   }
   return false;
 }
@@ -382,6 +468,7 @@ __device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm
 // candidate queue of one track, in visit order (a ring of kMaxStepCand entries)
 struct StepCands {
   int n, head;
+  uint64_t types;  // shape type of each slot, 4 bits per slot
 #if VGN_SMEM_STACK
   SArr<int> pv;
   SArr<float> tmin_lo;
@@ -389,6 +476,25 @@ struct StepCands {
   int pv[kMaxStepCand];
   float tmin_lo[kMaxStepCand];
 #endif
+  __device__ __forceinline__ int type(int slot) const { return (int)((types >> (4 * slot)) & 0xfull); }
+  __device__ __forceinline__ int slot(int k) const { return (head + k) % kMaxStepCand; }
+};
+
+// Two 32-bit words per queue slot holding a double: the FP64 DistanceToIn of the slot's
+// candidate, computed ahead of the acceptance loop (in the traversal stack, which is free by then).
+struct SlotWords {
+  unsigned *w;
+  int stride;
+  __device__ __forceinline__ unsigned &word(int s) const { return w[2 * s * stride]; }
+  __device__ __forceinline__ void put(int s, double d) const
+  {
+    w[2 * s * stride]       = (unsigned)__double2loint(d);
+    w[(2 * s + 1) * stride] = (unsigned)__double2hiint(d);
+  }
+  __device__ __forceinline__ double get(int s) const
+  {
+    return __hiloint2double((int)w[(2 * s + 1) * stride], (int)w[2 * s * stride]);
+  }
 };
 
 // Acceptance of one candidate, as in BVH.h:113-118; a candidate whose box is
@@ -405,19 +511,19 @@ __device__ __forceinline__ void eval_step_candidate(const GeomView &g, const Mix
   }
 }
 
-// BVH::CheckDaughterIntersections (BVH.h:96-146): FP32 traversal collecting
-// candidates in visit order, then FP64 evaluation in that order.
-__device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, const LVRec &lv, MixedRay &r,
-                                                          double &step, int last, int &hit)
+// BVH::CheckDaughterIntersections (BVH.h:96-146), traversal part: FP32 traversal collecting
+// the leaf candidates in visit order into `c` (a candidate is evaluated at once only when
+// the queue is full, the oldest first, which keeps the order).
+__device__ __forceinline__ bool bvh_collect_step_mixed(const GeomView &g, const LVRec &lv, MixedRay &r,
+                                                       double &step, FI &stepI, int last, int &hit, StepCands &c)
 {
   VGN_TRAVERSAL_STACK(stack);
   int sp   = 1;
   stack[0] = 0;
-  FI stepI = fi(step);
   // Culling uses the step after the candidates evaluated so far: never below
   // the step the FP64 traversal would hold at the same point.
-  StepCands c;
   c.n = c.head = 0;
+  c.types      = 0;
 #if VGN_SMEM_STACK
   c.pv      = SArr<int>{reinterpret_cast<int *>(vgn_step_smem + kStackSize * blockDim.x + threadIdx.x), (int)blockDim.x};
   c.tmin_lo = SArr<float>{reinterpret_cast<float *>(vgn_step_smem + (kStackSize + kMaxStepCand) * blockDim.x + threadIdx.x),
@@ -445,6 +551,7 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
         const int slot   = (c.head + c.n) % kMaxStepCand;
         c.pv[slot]       = __ldg(&q.pv);
         c.tmin_lo[slot]  = tmin.lo;
+        c.types = (c.types & ~(0xfull << (4 * slot))) | ((uint64_t)__ldg(&q.shape) << (4 * slot));
         ++c.n;
       }
     } else {
@@ -479,11 +586,88 @@ __device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, con
       }
     }
   } while (sp > 0);
-  // FP64 phase: the lanes of a warp evaluate their candidates together
+  return ok;
+}
+
+// Slots whose DistanceToIn may be computed ahead of the acceptance loop: every candidate
+// but the cut tubes (their DistanceToIn takes the running step) whose box entry lies below
+// the current step.  The step only decreases, so the acceptance loop reaches no other slot
+// but cut tubes.  `present` receives the shape types of those slots.
+__device__ __forceinline__ unsigned step_pending(const StepCands &c, FI stepI, unsigned &present)
+{
+  unsigned done = 0;
+  present       = 0;
   for (int k = 0; k < c.n; ++k) {
-    const int slot = (c.head + k) % kMaxStepCand;
-    eval_step_candidate(g, r, c.pv[slot], c.tmin_lo[slot], step, stepI, last, hit);
+    const int slot = c.slot(k);
+    const int t    = c.type(slot);
+    if (c.tmin_lo[slot] >= stepI.hi || t == kCutTube) continue;
+    done |= 1u << slot;
+    present |= 1u << t;
   }
+  return done;
+}
+
+// The reference's acceptance rule over the queue in visit order, with the distances of the
+// `done` slots read from `sw`; cut tubes are evaluated here with the running step.
+__device__ __forceinline__ void step_replay(const GeomView &g, const MixedRay &r, const StepCands &c, unsigned done,
+                                            SlotWords sw, double &step, FI &stepI, int last, int &hit)
+{
+  for (int k = 0; k < c.n; ++k) {
+    const int slot = c.slot(k);
+    if (c.tmin_lo[slot] >= stepI.hi) continue;
+    const int pv      = c.pv[slot];
+    const double dist = ((done >> slot) & 1u) ? sw.get(slot) : pv_dist_in(g, pv, r.lp, r.ld, step);
+    if (dist < step && !(dist <= 0.0 && pv == last)) {
+      step  = dist;
+      hit   = pv;
+      stepI = fi(step);
+    }
+  }
+}
+
+// BVH::CheckDaughterIntersections (BVH.h:96-146): FP32 traversal collecting candidates in
+// visit order, then FP64 evaluation in that order.
+__device__ __forceinline__ bool bvh_check_daughters_mixed(const GeomView &g, const LVRec &lv, MixedRay &r,
+                                                          double &step, int last, int &hit)
+{
+  FI stepI = fi(step);
+  StepCands c;
+  const bool ok = bvh_collect_step_mixed(g, lv, r, step, stepI, last, hit, c);
+  // FP64 phase.  Daughters of one shape type: the candidates in visit order with the
+  // reference's acceptance rule, the lanes of a warp running the same shape code.
+  if ((lv.dtypes & (lv.dtypes - 1)) == 0) {
+    for (int k = 0; k < c.n; ++k) {
+      const int slot = c.slot(k);
+      eval_step_candidate(g, r, c.pv[slot], c.tmin_lo[slot], step, stepI, last, hit);
+    }
+    return ok;
+  }
+  // Several types.  A candidate's DistanceToIn does not depend on when it is computed (the
+  // cut tube's excepted), so the values are computed first, grouped by shape type -- the
+  // lanes of a warp run one shape's code at a time, each on its own candidates of that
+  // type, instead of every lane its own shape -- and the acceptance rule then runs over them.
+#if VGN_SMEM_STACK
+  const SlotWords sw{vgn_step_smem + threadIdx.x, (int)blockDim.x};
+#else
+  unsigned words[2 * kMaxStepCand];
+  const SlotWords sw{words, 1};
+#endif
+  unsigned present;
+  const unsigned done = step_pending(c, stepI, present);
+  for (int t = 0; t < kNumShapes; ++t) {
+    if (!((present >> t) & 1u)) continue;
+    unsigned m = 0;
+    for (unsigned rest = done; rest; rest &= rest - 1) {
+      const int s = __ffs(rest) - 1;
+      if (c.type(s) == t) m |= 1u << s;
+    }
+    while (m) {
+      const int s = __ffs(m) - 1;
+      m &= m - 1;
+      sw.put(s, pv_dist_in(g, c.pv[s], r.lp, r.ld, kInfLength));
+    }
+  }
+  step_replay(g, r, c, done, sw, step, stepI, last, hit);
   return ok;
 }
 

@@ -135,31 +135,27 @@ __device__ __forceinline__ double safety_local(const GeomView &g, const LVRec &l
   return safety;
 }
 
-// ComputeStepAndPropagatedState (VNavigator.h:436-492) with PrepareOutState
-// (VNavigator.h:192-235) and MovePointAfterBoundary (168-173).  The safety of
-// ComputeStepAndSafetyAndPropagatedState (VNavigator.h:1014-1064) is taken at the
-// input state and does not affect the step: the safety pass (safety_local) computes it.
-template <bool MIXED>
-__device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, double slimit, const State &in,
-                                           State &out, bool reloc)
+// Start of a step: the input state's global matrix, the local point and direction, the
+// volume and the mother's DistanceToOut (VNavigator.h:444-458; BVHNavigator.h:53-61).
+__device__ __forceinline__ void step_begin(const GeomView &g, D3 gp, D3 gd, const State &in, D3 &lp, D3 &ld,
+                                           LVRec &lv, double &step)
 {
   Xf m;
   top_matrix(g, in.nav_ind, m);
-  const D3 lp    = xf_point(m.t, m.r, gp);
-  const D3 ld    = xf_dir(m.r, gd);
-  const int pv   = ni_top(g, in.nav_ind);
-  const LVRec lv = load_lv(g, pv_lv(g, pv));
-  double step    = shape_dist_out(lv.shape, g.shape + lv.shape_row, lp, ld);
+  lp            = xf_point(m.t, m.r, gp);
+  ld            = xf_dir(m.r, gd);
+  const int pv  = ni_top(g, in.nav_ind);
+  lv            = load_lv(g, pv_lv(g, pv));
+  step          = shape_dist_out(lv.shape, g.shape + lv.shape_row, lp, ld);
   if (step < 0.) step = 0.;
-  int hit = -1;
-  if (MIXED) {
-    MixedRay r;
-    make_ray(r, lp, ld);
-    if (lv.nd > 0) bvh_check_daughters_mixed(g, lv, r, step, ni_top(g, in.last_exited), hit);
-  } else {
-    if (lv.nd > 0) bvh_check_daughters(g, lv, lp, ld, step, ni_top(g, in.last_exited), hit);
-  }
+}
 
+// End of a step, given the daughters' verdict (step, hit): PrepareOutState
+// (VNavigator.h:192-235) and MovePointAfterBoundary (168-173) with relocation.
+template <bool MIXED>
+__device__ __forceinline__ double step_finish(const GeomView &g, D3 lp, D3 ld, double slimit, const State &in,
+                                              State &out, bool reloc, double step, int hit)
+{
   out = in;
   if (step == kInfLength && slimit > 0.) {
     out.on_boundary = 1;
@@ -178,6 +174,29 @@ __device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, doub
   const double s = step + 1E-6;
   relocate<MIXED>(g, d3(lp.x + s * ld.x, lp.y + s * ld.y, lp.z + s * ld.z), in, out);
   return step;
+}
+
+// ComputeStepAndPropagatedState (VNavigator.h:436-492) with PrepareOutState
+// (VNavigator.h:192-235) and MovePointAfterBoundary (168-173).  The safety of
+// ComputeStepAndSafetyAndPropagatedState (VNavigator.h:1014-1064) is taken at the
+// input state and does not affect the step: the safety pass (safety_local) computes it.
+template <bool MIXED>
+__device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, double slimit, const State &in,
+                                           State &out, bool reloc)
+{
+  D3 lp, ld;
+  LVRec lv;
+  double step;
+  step_begin(g, gp, gd, in, lp, ld, lv, step);
+  int hit = -1;
+  if (MIXED) {
+    MixedRay r;
+    make_ray(r, lp, ld);
+    if (lv.nd > 0) bvh_check_daughters_mixed(g, lv, r, step, ni_top(g, in.last_exited), hit);
+  } else {
+    if (lv.nd > 0) bvh_check_daughters(g, lv, lp, ld, step, ni_top(g, in.last_exited), hit);
+  }
+  return step_finish<MIXED>(g, lp, ld, slimit, in, out, reloc, step, hit);
 }
 
 }  // namespace VGN_KSET

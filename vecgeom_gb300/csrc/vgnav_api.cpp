@@ -313,7 +313,7 @@ int vgn_geometry_create_with_cache_depth(const vgn_geometry_desc *desc, int devi
       (rc = upload(g, h.fprims, &v.fprims)) || (rc = upload(g, h.shape, &v.shape)) ||
       (rc = upload(g, h.inodes, &v.inodes)) || (rc = upload(g, h.inode_safe, &v.inode_safe)) ||
       (rc = upload(g, h.iprims, &v.iprims)) || (rc = upload(g, h.iprim_safe, &v.iprim_safe)) ||
-      (rc = upload(g, h.ixf, &v.ixf)) || (rc = upload(g, h.isin, &v.isin))) {
+      (rc = upload(g, h.ixf, &v.ixf)) || (rc = upload(g, h.isin, &v.isin)) || (rc = upload(g, h.lv_bbox, &v.lv_bbox))) {
     vgn_geometry_free(g);
     return rc;
   }
@@ -633,6 +633,55 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   return check_status(g, s);
 }
 
+int vgn_approach_next_daughter_batch(const vgn_geometry *gc, int64_t n, const int32_t *lv, const double *px,
+                                     const double *py, const double *pz, const double *dx, const double *dy,
+                                     const double *dz, const int32_t *last_pv, double *step, void *stream)
+{
+  vgn_geometry *g = const_cast<vgn_geometry *>(gc);
+  if (!g) return fail(VGN_ERR_ARG, "null geometry");
+  if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
+  if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
+  if (n == 0) return VGN_OK;
+  if (!lv || !px || !py || !pz || !dx || !dy || !dz || !step) return fail(VGN_ERR_ARG, "null array argument");
+  DeviceGuard guard(g->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int kind = last_pv ? classify({lv, px, py, pz, dx, dy, dz, last_pv, step})
+                           : classify({lv, px, py, pz, dx, dy, dz, step});
+  if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
+  if (kind == 1) {
+    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_approach)(g->view, n, lv, px, py, pz, dx, dy, dz, last_pv,
+                                                                   step, max_blocks(g), s);
+    return e == cudaSuccess ? VGN_OK : cuda_fail(e, "approach kernel launch");
+  }
+  // host buffers: the volume ids are checked here, before anything is copied
+  const int32_t n_lv = (int32_t)g->host.lv.size(), n_pv = (int32_t)g->host.pv.size();
+  for (int64_t i = 0; i < n; ++i) {
+    if (lv[i] < 0 || lv[i] >= n_lv || g->host.lv[lv[i]].daughters.empty())
+      return fail(VGN_ERR_ARG, "logical volume out of range or without daughters");
+    if (last_pv && (last_pv[i] < -1 || last_pv[i] >= n_pv)) return fail(VGN_ERR_ARG, "last placed volume out of range");
+  }
+  std::lock_guard<std::mutex> lock(g->ws_mutex);
+  const size_t nd = (size_t)n * sizeof(double), ni = (size_t)n * sizeof(int32_t);
+  void *ws = workspace(g, carve_bytes({nd, nd, nd, nd, nd, nd, nd, ni, ni}));
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  Carve c{static_cast<char *>(ws)};
+  double *b[7];
+  for (auto &p : b) p = c.take<double>(n);
+  int32_t *dlv = c.take<int32_t>(n), *dlast = c.take<int32_t>(n);
+  const double *src[7] = {px, py, pz, dx, dy, dz, step};
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 7 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dlv, lv, ni, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && last_pv) e = cudaMemcpyAsync(dlast, last_pv, ni, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  e = VGN_KSET_FN(g->host.sections, launch_approach)(g->view, n, dlv, b[0], b[1], b[2], b[3], b[4], b[5],
+                                                     last_pv ? dlast : nullptr, b[6], max_blocks(g), s);
+  if (e != cudaSuccess) return cuda_fail(e, "approach kernel launch");
+  e = cudaMemcpyAsync(step, b[6], nd, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
 int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, const double *px, const double *py,
                     const double *pz, const double *dx, const double *dy, const double *dz, const double *step_max,
                     double *out, int flags, void *stream)
@@ -684,11 +733,19 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
 int vgn_set_step_config(vgn_geometry *g, int flags, int32_t variant, int32_t sort_kbits)
 {
   if (!g) return fail(VGN_ERR_ARG, "null geometry");
-  if (variant < 0 || variant >= vgn::sections::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
+  const int m = (flags & VGN_PRECISION_MIXED) ? 1 : 0;
+  if (variant < 0 || variant >= vgn::sections::step_variant_count(m != 0))
+    return fail(VGN_ERR_ARG, "unknown launch variant");
   if (sort_kbits < 0 || sort_kbits > 6) return fail(VGN_ERR_ARG, "track-binning granularity must be 0..6");
-  const int m        = (flags & VGN_PRECISION_MIXED) ? 1 : 0;
   g->step_variant[m] = variant;
   g->sort_kbits[m]   = sort_kbits;
+  return VGN_OK;
+}
+
+int vgn_get_step_variant_count(int flags, int32_t *count)
+{
+  if (!count) return fail(VGN_ERR_ARG, "null argument");
+  *count = vgn::sections::step_variant_count((flags & VGN_PRECISION_MIXED) != 0);
   return VGN_OK;
 }
 
@@ -774,7 +831,7 @@ int vgn_autotune_step(vgn_geometry *g, int64_t n, const double *px, const double
   float best = 3.4e38f;
   int bv = 0, bk = 0, bs = 0, rc = VGN_OK;
   g->safety_kbits[m] = safety ? 6 : 0;
-  for (int v = 0; v < vgn::sections::step_variant_count() && rc == VGN_OK; ++v) {
+  for (int v = 0; v < vgn::sections::step_variant_count(m != 0) && rc == VGN_OK; ++v) {
     for (int k : kSort) {
       g->step_variant[m] = v;
       g->sort_kbits[m]   = k;
@@ -845,8 +902,11 @@ int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, dou
       return cuda_fail(e, "walk binning launch");
     }
   }
+  // the mixed form's block-grouped launch variants walk chunks of tracks per block with
+  // block-grouped steps (walk_kernel_grouped)
+  const int variant = g->step_variant[mixed ? 1 : 0];
   cudaError_t e = VGN_KSET_FN(g->host.sections, launch_walk)(g->view, n, px, py, pz, dx, dy, dz, step_limit, state,
-                                                             max_steps, nsteps, perm, mixed, max_blocks(g), s);
+                                                             max_steps, nsteps, perm, mixed, variant, max_blocks(g), s);
   if (sort) cudaFreeAsync(sort, s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "walk kernel launch");
 }
@@ -974,7 +1034,7 @@ int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int f
   if (!b) return fail(VGN_ERR_ARG, "null batch");
   if (n_jobs < 1 || n_jobs > VGN_BATCH_MAX_JOBS || !jobs)
     return fail(VGN_ERR_ARG, "a batch holds 1.." + std::to_string(VGN_BATCH_MAX_JOBS) + " jobs");
-  if (variant < 0 || variant >= vgn::sections::step_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
+  if (variant < 0 || variant >= vgn::sections::multi_variant_count()) return fail(VGN_ERR_ARG, "unknown launch variant");
   if (sort_kbits < 0 || sort_kbits > 6) return fail(VGN_ERR_ARG, "track-binning granularity must be 0..6");
   DeviceGuard guard(b->device);
   uint64_t chunks = 0;
@@ -1061,7 +1121,7 @@ int vgn_batch_autotune(vgn_batch *b, void *stream, int32_t *variant, int32_t *so
   int bv = 0, bk = 0, bs = any_safety ? 6 : 0, rc = VGN_OK;
   for (int k : kSort) {
     if ((rc = batch_configure(b, k, bs)) != VGN_OK) break;
-    for (int v = 0; v < vgn::sections::step_variant_count() && rc == VGN_OK; ++v) {
+    for (int v = 0; v < vgn::sections::multi_variant_count() && rc == VGN_OK; ++v) {
       b->variant = v;
       if ((rc = batch_enqueue(b, s)) != VGN_OK) break;  // warm-up
       cudaEventRecord(e0, s);

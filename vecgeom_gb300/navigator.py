@@ -175,6 +175,15 @@ class Geometry:
         N.check(N.lib().vgn_shape_batch(self.handle, lv, op, pts.size(), _ptr(pts.x), _ptr(pts.y), _ptr(pts.z), dx,
                                         dy, dz, _ptr(step_max), _ptr(out), 0, _stream_ptr(stream)))
 
+    def approach_next_daughter(self, lv, pts: SOA3D, dirs: SOA3D, step, last=None, stream=None):
+        """BVH::ApproachNextDaughter per track: over the BVH of logical volume lv[i] (int32), with
+        local points and directions, `step` (float64, in/out) is lowered to the entry distance
+        into the bounding box of the nearest daughter met before it; `last` (int32 placed-volume
+        ids, -1 for none) is the last exited volume."""
+        N.check(N.lib().vgn_approach_next_daughter_batch(self.handle, pts.size(), _ptr(lv), _ptr(pts.x), _ptr(pts.y),
+                                                         _ptr(pts.z), _ptr(dirs.x), _ptr(dirs.y), _ptr(dirs.z),
+                                                         _ptr(last), _ptr(step), _stream_ptr(stream)))
+
     def walk(self, pts: SOA3D, dirs: SOA3D, step_limit, states: NavStatePool, nsteps, max_steps: int = 1 << 20,
              mixed: bool = False, stream=None):
         """Step every track (p += step * d, state = propagated state) until it leaves the world
@@ -185,6 +194,14 @@ class Geometry:
                                        _ptr(nsteps), N.VGN_PRECISION_MIXED if mixed else 0, _stream_ptr(stream)))
 
     # ---- step-kernel launch configuration ---------------------------------
+    @staticmethod
+    def step_variant_count(mixed: bool = False) -> int:
+        """Launch variants of the step for the precision form (the mixed form's last three group
+        the candidates' FP64 shape evaluations by shape type across the thread block)."""
+        c = C.c_int32()
+        N.check(N.lib().vgn_get_step_variant_count(N.VGN_PRECISION_MIXED if mixed else 0, C.byref(c)))
+        return c.value
+
     def set_step_config(self, variant: int, sort_kbits: int, mixed: bool = False):
         N.check(N.lib().vgn_set_step_config(self.handle, N.VGN_PRECISION_MIXED if mixed else 0, variant, sort_kbits))
 
