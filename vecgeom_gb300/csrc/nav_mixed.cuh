@@ -464,6 +464,42 @@ __device__ __forceinline__ bool ishape_safety_in(const GeomView &g, const IXForm
   return false;
 }
 
+// ------------------------------------------------------------------ traversal stack entries
+// Entries of the mixed traversals' stacks: an internal node is its id; a leaf is its primitive
+// range (bit 31, the primitive count in bits 26-29, the first primitive in bits 0-25) when that
+// fits, else its id with bits 31 and 30 set (the range is then loaded when it is popped).  A
+// child's range is read with the record its box test loads anyway, so visiting an internal node
+// costs one dependent load (its children's boxes) instead of two, and a small leaf none.
+static_assert(offsetof(INodeSlab, offset) == offsetof(INodeSlab, nchild) + 4 && offsetof(INodeSlab, nchild) % 8 == 0,
+              "a node's (nchild, offset) pair is one 8-byte load");
+__device__ __forceinline__ int2 inode_range(const INodeSlab *inodes, unsigned id)
+{
+  return __ldg(reinterpret_cast<const int2 *>(&inodes[id].nchild));
+}
+__device__ __forceinline__ unsigned stack_entry(unsigned id, int2 range)
+{
+  if (range.x < 0) return id;
+  if (range.x < 16 && (unsigned)range.y < (1u << 26)) return 0x80000000u | ((unsigned)range.x << 26) | (unsigned)range.y;
+  return 0xC0000000u | id;
+}
+// the node of entry e: its id (internal nodes) and its primitive range (nchild < 0: internal)
+__device__ __forceinline__ unsigned open_entry(const INodeSlab *inodes, unsigned e, int &nchild, int &off)
+{
+  nchild = -1;
+  off    = 0;
+  if (!(e & 0x80000000u)) return e;
+  if (!(e & 0x40000000u)) {
+    nchild = (int)((e >> 26) & 15u);
+    off    = (int)(e & 0x3ffffffu);
+    return 0u;
+  }
+  const unsigned id = e & 0x3fffffffu;
+  const int2 range  = inode_range(inodes, id);
+  nchild            = range.x;
+  off               = range.y;
+  return id;
+}
+
 // ------------------------------------------------------------------ step
 // candidate queue of one track, in visit order (a ring of kMaxStepCand entries)
 struct StepCands {
@@ -532,12 +568,12 @@ __device__ __forceinline__ bool bvh_collect_step_mixed(const GeomView &g, const 
   const INodeSlab *inodes = g.inodes + lv.nodes_off;
   const IPrimSlab *iprims = g.iprims + lv.prims_off;
   const NodeRec *nodes    = g.nodes + lv.nodes_off;
+  stack[0]                = stack_entry(0u, inode_range(inodes, 0u));
   bool ok = true;
   do {
-    const unsigned id = stack[--sp];
-    const int nchild  = __ldg(&inodes[id].nchild);
+    int nchild, off;
+    const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
     if (nchild >= 0) {
-      const int off = __ldg(&inodes[id].offset);
       for (int i = 0; i < nchild; ++i) {
         const IPrimSlab &q = iprims[off + i];
         FI tmin, tmax;
@@ -556,6 +592,7 @@ __device__ __forceinline__ bool bvh_collect_step_mixed(const GeomView &g, const 
       }
     } else {
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      const unsigned eL = stack_entry(L, inode_range(inodes, L)), eR = stack_entry(R, inode_range(inodes, R));
       FI tminL, tmaxL, tminR, tmaxR;
       islab(inodes[L].mn_lo, inodes[L].mn_hi, inodes[L].mx_lo, inodes[L].mx_hi, r, tminL, tmaxL);
       islab(inodes[R].mn_lo, inodes[R].mn_hi, inodes[R].mx_lo, inodes[R].mx_hi, r, tminR, tmaxR);
@@ -578,11 +615,11 @@ __device__ __forceinline__ bool bvh_collect_step_mixed(const GeomView &g, const 
         break;
       }
       if (rfirst == kYes) {
-        if (trR) stack[sp++] = R;
-        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = eR;
+        if (trL) stack[sp++] = eL;
       } else {
-        if (trL) stack[sp++] = L;
-        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = eL;
+        if (trR) stack[sp++] = eR;
       }
     }
   } while (sp > 0);
@@ -735,8 +772,7 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
   const int stride = blockDim.x;
   uint32_t *base   = vgn_safety_smem + threadIdx.x;
   const SArr<unsigned> stack{base, stride};
-  int sp   = 1;
-  stack[0] = 0;
+  int sp = 1;
   SafeRun s;
   s.pv     = SArr<int>{reinterpret_cast<int *>(base + kStackSize * stride), stride};
   s.lo     = SArr<float>{reinterpret_cast<float *>(base + (kStackSize + kMaxSafeCand) * stride), stride};
@@ -751,11 +787,11 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
   const IPrimSlab *iprims = g.iprims + lv.prims_off;
   const NodeRec *nodes    = g.nodes + lv.nodes_off;
   const PrimRec *prims    = g.prims + lv.prims_off;
+  stack[0]                = stack_entry(0u, inode_range(inodes, 0u));
   do {
-    const unsigned id = stack[--sp];
-    const int nchild  = __ldg(&inodes[id].nchild);
+    int nchild, off;
+    const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
     if (nchild >= 0) {
-      const int off = __ldg(&inodes[id].offset);
       for (int i = 0; i < nchild; ++i) {
         // cheapest test first: the primitive's box safety against the running minimum
         const FI sbox = isafety(isafe_p[off + i], r);
@@ -786,6 +822,7 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
       }
     } else {
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      const unsigned eL = stack_entry(L, inode_range(inodes, L)), eR = stack_entry(R, inode_range(inodes, R));
       const FI sL = isafety(isafe_n[L], r);
       const FI sR = isafety(isafe_n[R], r);
       const bool trL = saferun_less(g, r, s, sL, [&] { return box_safety(nodes[L].mn, nodes[L].mx, r.lp); });
@@ -801,11 +838,11 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
         break;
       }
       if (rfirst) {
-        if (trR) stack[sp++] = R;
-        if (trL) stack[sp++] = L;
+        if (trR) stack[sp++] = eR;
+        if (trL) stack[sp++] = eL;
       } else {
-        if (trL) stack[sp++] = L;
-        if (trR) stack[sp++] = R;
+        if (trL) stack[sp++] = eL;
+        if (trR) stack[sp++] = eR;
       }
     }
   } while (sp > 0);
@@ -835,18 +872,17 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
                                                        int &pvol, D3 &dlp)
 {
   VGN_TRAVERSAL_STACK(stack);
-  int sp   = 1;
-  stack[0] = 0;
+  int sp = 1;
   const FI p[3] = {fi(lp.x), fi(lp.y), fi(lp.z)};
   const INodeSlab *inodes = g.inodes + lv.nodes_off;
   const IPrimSlab *iprims = g.iprims + lv.prims_off;
   const NodeRec *nodes    = g.nodes + lv.nodes_off;
   const PrimRec *prims    = g.prims + lv.prims_off;
+  stack[0]                = stack_entry(0u, inode_range(inodes, 0u));
   do {
-    const unsigned id = stack[--sp];
-    const int nchild  = __ldg(&inodes[id].nchild);
+    int nchild, off;
+    const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
     if (nchild >= 0) {
-      const int off = __ldg(&inodes[id].offset);
       for (int i = 0; i < nchild; ++i) {
         const IPrimSlab &q = iprims[off + i];
         int dec = icontains(q.mn_lo, q.mn_hi, q.mx_lo, q.mx_hi, p);
@@ -870,10 +906,10 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
       }
       int cL = icontains(inodes[L].mn_lo, inodes[L].mn_hi, inodes[L].mx_lo, inodes[L].mx_hi, p);
       if (cL == kMaybe) cL = box_contains_pt(nodes[L].mn, nodes[L].mx, lp) ? kYes : kNo;
-      if (cL == kYes) stack[sp++] = L;
+      if (cL == kYes) stack[sp++] = stack_entry(L, inode_range(inodes, L));
       int cR = icontains(inodes[R].mn_lo, inodes[R].mn_hi, inodes[R].mx_lo, inodes[R].mx_hi, p);
       if (cR == kMaybe) cR = box_contains_pt(nodes[R].mn, nodes[R].mx, lp) ? kYes : kNo;
-      if (cR == kYes) stack[sp++] = R;
+      if (cR == kYes) stack[sp++] = stack_entry(R, inode_range(inodes, R));
     }
   } while (sp > 0);
   return false;
