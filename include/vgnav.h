@@ -44,9 +44,26 @@ enum vgn_shape_type {
   VGN_SPHERE    = 5, /* params: rmin, rmax, sphi, dphi, stheta, dtheta (UnplacedSphere.h) */
   VGN_POLYCONE  = 6, /* params: sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] (UnplacedPolycone.h:79) */
   VGN_ORB       = 7, /* params: r                                 (UnplacedOrb.h)       */
-  VGN_CUTTUBE   = 8  /* params: rmin, rmax, dz, sphi, dphi, bottom normal bx, by, bz, top normal
+  VGN_CUTTUBE   = 8, /* params: rmin, rmax, dz, sphi, dphi, bottom normal bx, by, bz, top normal
                         tx, ty, tz                                (UnplacedCutTube.h:54-57) */
+  VGN_BOOLEAN   = 9  /* params: op (VGN_BOOL_UNION / _INTERSECTION / _SUBTRACTION), left operand,
+                        right operand: ids of placed volumes whose mother is VGN_BOOLEAN_OPERAND
+                        (UnplacedBooleanVolume.h:59, BooleanStruct.h:23-25)        */
 };
+
+/* Boolean solids (VGN_BOOLEAN).  The operands are placements of other logical volumes
+ * relative to the boolean's frame, listed in vgn_geometry_desc like any placement but with
+ * pv_mother = VGN_BOOLEAN_OPERAND: they belong to no mother and take no part in navigation
+ * other than through their boolean.  Rules:
+ *  - each operand placement (anywhere in the placed-volume list, so VecGeom's own ids can be
+ *    kept) is used by exactly one boolean;
+ *  - an operand's logical volume has a smaller index than its boolean, has no daughters, and
+ *    is a primitive shape or a boolean of primitive shapes (two levels at most).
+ * A geometry holding booleans may hold no phi or theta section (VGN_ERR_UNSUPPORTED).
+ * vgn_shape_batch with VGN_OP_INSIDE on a union is VGN_ERR_UNSUPPORTED (its surface case takes
+ * the operands' normals, which the library does not compute); every navigation call works. */
+#define VGN_BOOLEAN_OPERAND (-2)
+enum vgn_boolean_op { VGN_BOOL_UNION = 0, VGN_BOOL_INTERSECTION = 1, VGN_BOOL_SUBTRACTION = 2 };
 
 /* ---- shape operations for vgn_shape_batch ------------------------------- */
 enum vgn_shape_op {

@@ -32,6 +32,9 @@
 // Arrays may be host memory (the usual SOA3D and NavStatePool; the library stages them)
 // or device memory.  Errors throw vgnav::Error with the library's status and message.
 //
+// Boolean solids export as their operation and the ids of their placed operands, which
+// keep VecGeom's ids and get the mother VGN_BOOLEAN_OPERAND.
+//
 // Shape parameters are exported as the shapes hold them.  They reproduce the shape exactly
 // when the shape keeps its constructor's values: full-range shapes, and phi sections whose
 // start angle lies in [0, 2 pi) and whose end does not pass 2 pi.  Trapezoids keep
@@ -55,6 +58,7 @@
 #include "VecGeom/navigation/VNavigator.h"
 #include "VecGeom/volumes/LogicalVolume.h"
 #include "VecGeom/volumes/PlacedVolume.h"
+#include "VecGeom/volumes/UnplacedBooleanVolume.h"
 #include "VecGeom/volumes/UnplacedBox.h"
 #include "VecGeom/volumes/UnplacedCone.h"
 #include "VecGeom/volumes/UnplacedCutTube.h"
@@ -144,6 +148,17 @@ inline int shape_row(vecgeom::VUnplacedVolume const *u, std::vector<double> &p)
     p = {o->GetRadius()};
     return VGN_ORB;
   }
+  // booleans: the operation and the ids of the two placed operands (BooleanStruct.h:23-25)
+  BooleanStruct const *bs = nullptr;
+  if (auto b = dynamic_cast<UnplacedBooleanVolume<kUnion> const *>(u)) bs = &b->GetStruct();
+  if (auto b = dynamic_cast<UnplacedBooleanVolume<kIntersection> const *>(u)) bs = &b->GetStruct();
+  if (auto b = dynamic_cast<UnplacedBooleanVolume<kSubtraction> const *>(u)) bs = &b->GetStruct();
+  if (bs) {
+    const int op = bs->fOp == kUnion ? VGN_BOOL_UNION : bs->fOp == kIntersection ? VGN_BOOL_INTERSECTION
+                                                                                  : VGN_BOOL_SUBTRACTION;
+    p = {(double)op, (double)bs->fLeftVolume->id(), (double)bs->fRightVolume->id()};
+    return VGN_BOOLEAN;
+  }
   if (auto c = dynamic_cast<UnplacedPolycone const *>(u)) {
     auto const *h = c->GetOriginalParameters();  // the constructor's planes (PolyconeStruct.h:279-285)
     if (!h) return -1;
@@ -197,8 +212,14 @@ inline ExportedGeometry ExportGeometry()
     for (int k = 0; k < 3; ++k) e.pv_transform[12 * i + k] = t->Translation(k);
     for (int k = 0; k < 9; ++k) e.pv_transform[12 * i + 3 + k] = t->Rotation(k);
   }
-  for (unsigned i = 0; i < n_lv; ++i)
+  for (unsigned i = 0; i < n_lv; ++i) {
     for (VPlacedVolume const *d : lvs.at(i)->GetDaughters()) e.pv_mother[d->id()] = (int32_t)i;
+    if (e.lv_shape[i] == VGN_BOOLEAN) {  // the operands belong to no mother
+      const double *p = &e.params[(size_t)e.lv_param_offset[i]];
+      for (int k = 1; k <= 2; ++k)
+        if (p[k] >= 0 && p[k] < n_pv) e.pv_mother[(size_t)p[k]] = VGN_BOOLEAN_OPERAND;
+    }
+  }
   e.world_placed = (int32_t)gm.GetWorld()->id();
   return e;
 }

@@ -46,6 +46,8 @@ KERNEL_WEIGHTS = [
     [270, 240, 75, 75, 36, 42],   # PolyconeImplementation.h:189-517 (three cone sections)
     [20, 20, 8, 8, 6, 8],         # OrbImplementation.h:102-220
     [110, 60, 25, 25, 20, 24],    # CutTubeImplementation.h:158-290 (tube + two cut planes)
+    [12, 12, 6, 6, 4, 4],         # Boolean*Implementation.h: the combination and the operands' transforms
+                                  # (the operands' own kernels are counted under their shapes)
 ]
 
 

@@ -270,6 +270,7 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_SPHERE: return 6;
   case OR_ORB: return 1;
   case OR_CUTTUBE: return 11;
+  case OR_BOOLEAN: return 3; /* op, left operand placement, right operand placement */
   case OR_POLYCONE: { /* sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] */
     int nz;
     if (avail < 3 || !(p[2] >= 2 && p[2] <= 4096)) return -1;
@@ -279,6 +280,65 @@ static int shape_nparams(int type, const double *p, int avail)
   }
   default: (void)p; (void)avail; return -1;
   }
+}
+
+/* Boolean solids: each operand placement (pv_mother OR_BOOLEAN_OPERAND, anywhere in the
+ * placement list) is used by exactly one boolean (UnplacedBooleanVolume.h:59 holds its own
+ * placed operands); an operand's logical volume precedes its boolean, has no daughters and is
+ * a primitive or a boolean of primitives.  Links each boolean to its operands and computes its
+ * extent. */
+static int link_booleans(or_geom *g, const int *pv_mother, char *err, int errlen)
+{
+  int i, used = 0, n_operands = 0, rc = 0;
+  char *taken = (char *)calloc((size_t)g->n_pv + 1, 1);
+  if (!taken) {
+    set_err(err, errlen, "out of host memory");
+    return -1;
+  }
+  for (i = 0; i < g->n_pv; ++i)
+    if (pv_mother[i] == OR_BOOLEAN_OPERAND) ++n_operands;
+  for (i = 0; i < g->n_lv; ++i) {
+    or_boolean *b = &g->lv[i].s.boo;
+    int k;
+    if (g->lv[i].type != OR_BOOLEAN) continue;
+    for (k = 0; k < 2; ++k) {
+      const int pv = k == 0 ? b->left_pv : b->right_pv;
+      const or_lv *o;
+      if (pv < 0 || pv >= g->n_pv || pv_mother[pv] != OR_BOOLEAN_OPERAND || taken[pv]++) {
+        set_err(err, errlen, "a boolean operand must be a placement with the operand mother, used once");
+        rc = -1;
+        goto done;
+      }
+      ++used;
+      if (g->pv[pv].lv >= i) {
+        set_err(err, errlen, "a boolean operand's logical volume must precede the boolean");
+        rc = -1;
+        goto done;
+      }
+      o = &g->lv[g->pv[pv].lv];
+      if (o->nd != 0 || (o->type == OR_BOOLEAN && (o->s.boo.left->type == OR_BOOLEAN ||
+                                                   o->s.boo.right->type == OR_BOOLEAN))) {
+        set_err(err, errlen, "a boolean operand must have no daughters and be at most a boolean of primitives");
+        rc = -1;
+        goto done;
+      }
+      if (k == 0) {
+        b->left = o;
+        b->lxf  = g->pv[pv].xf;
+      } else {
+        b->right = o;
+        b->rxf   = g->pv[pv].xf;
+      }
+    }
+    shape_extent(&g->lv[i], &g->lv[i].bbox_min, &g->lv[i].bbox_max);
+  }
+  if (used != n_operands) {
+    set_err(err, errlen, "a boolean operand placement is not used by exactly one boolean");
+    rc = -1;
+  }
+done:
+  free(taken);
+  return rc;
 }
 
 or_geom *or_geom_create(int n_lv, const int *lv_shape, const int *lv_param_off, const double *params, int n_params,
@@ -322,11 +382,12 @@ or_geom *or_geom_create_ex(int n_lv, const int *lv_shape, const int *lv_param_of
       or_geom_free(g);
       return NULL;
     }
-    shape_extent(&g->lv[i], &g->lv[i].bbox_min, &g->lv[i].bbox_max); /* ComputeBBox at construction */
+    if (lv_shape[i] != OR_BOOLEAN) /* ComputeBBox at construction; booleans once linked */
+      shape_extent(&g->lv[i], &g->lv[i].bbox_min, &g->lv[i].bbox_max);
   }
   count = (int *)calloc((size_t)n_lv, sizeof(int));
   for (i = 0; i < n_pv; ++i) {
-    if (pv_lv[i] < 0 || pv_lv[i] >= n_lv || pv_mother[i] < -1 || pv_mother[i] >= n_lv) {
+    if (pv_lv[i] < 0 || pv_lv[i] >= n_lv || pv_mother[i] < OR_BOOLEAN_OPERAND || pv_mother[i] >= n_lv) {
       set_err(err, errlen, "placed volume refers to an unknown logical volume");
       free(count);
       or_geom_free(g);
@@ -339,6 +400,11 @@ or_geom *or_geom_create_ex(int n_lv, const int *lv_shape, const int *lv_param_of
   }
   if (pv_mother[world_pv] != -1) {
     set_err(err, errlen, "world placement must have no mother");
+    free(count);
+    or_geom_free(g);
+    return NULL;
+  }
+  if (link_booleans(g, pv_mother, err, errlen)) {
     free(count);
     or_geom_free(g);
     return NULL;

@@ -159,7 +159,15 @@ typedef struct { /* CutTubeStruct.h:21-46 */
   double cosphi1, sinphi1, cosphi2, sinphi2, maxval;
 } or_cuttube;
 
-typedef struct {
+struct or_lv_s;
+typedef struct { /* BooleanStruct (BooleanStruct.h:23-25): the operation and the two placed operands */
+  int op;                             /* 0 union, 1 intersection, 2 subtraction (BooleanStruct.h:9) */
+  int left_pv, right_pv;              /* the operand placements (pv_mother OR_BOOLEAN_OPERAND) */
+  const struct or_lv_s *left, *right; /* their logical volumes */
+  or_xf lxf, rxf;                     /* their placements' transformations */
+} or_boolean;
+
+typedef struct or_lv_s {
   int type;
   int param_off;
   int nd;           /* number of daughters */
@@ -175,6 +183,7 @@ typedef struct {
     or_polycone pcon;
     or_orb orb;
     or_cuttube ctube;
+    or_boolean boo;
   } s;
   v3 bbox_min, bbox_max; /* VUnplacedVolume::fBBox: the shape's Extent (UnplacedVolume.h:45, 76-80) */
   /* BVH (BVH.h:364-370), present when nd > 0 */

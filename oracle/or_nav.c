@@ -608,6 +608,16 @@ int or_approach_batch(const or_geom *g, long n, const int *lv, const double *px,
   return 0;
 }
 
+/* the shape's extent (VUnplacedVolume::Extent): min then max corner */
+int or_shape_extent(const or_geom *g, int lvi, double *out6)
+{
+  v3 mn, mx;
+  if (lvi < 0 || lvi >= g->n_lv) return -1;
+  shape_extent(&g->lv[lvi], &mn, &mx);
+  out6[0] = mn.x, out6[1] = mn.y, out6[2] = mn.z, out6[3] = mx.x, out6[4] = mx.y, out6[5] = mx.z;
+  return 0;
+}
+
 /* unplaced shape queries */
 int or_shape_batch(const or_geom *g, int lvi, int op, long n, const double *px, const double *py, const double *pz,
                    const double *dx, const double *dy, const double *dz, const double *stepmax, double *out)

@@ -2904,6 +2904,350 @@ static void cuttube_extent(const or_cuttube *c, v3 *mn, v3 *mx) /* source/Unplac
 
 /* ================================================================== */
 
+/* ---------------------------------------------------------------- */
+/* Boolean solids over placed operands: BooleanImplementation.h (subtraction),
+ * BooleanUnionImplementation.h, BooleanIntersectionImplementation.h.  A placed operand's
+ * Contains, Inside, DistanceToIn, PlacedDistanceToOut and SafetyToIn take the boolean-frame
+ * point into the operand's frame (SpecializedPlacedVolImplHelper.h:99-172); its DistanceToOut
+ * and SafetyToOut do not (PlacedVolImplHelper.h:76-100).  The reference's loops are unbounded;
+ * these stop after OR_BOOL_MAX_ITER rounds (never reached on a valid solid). */
+#define OR_BOOL_MAX_ITER 1000000
+enum { OR_INSIDE = 1, OR_SURFACE = 2, OR_OUTSIDE = 3 };
+
+static int bo_contains(const or_lv *o, const or_xf *x, v3 p, or_counters *c)
+{
+  return shape_contains(o, xf_transform(x, p), c);
+}
+static int bo_inside(const or_lv *o, const or_xf *x, v3 p, or_counters *c)
+{
+  return shape_inside(o, xf_transform(x, p), c);
+}
+static double bo_dist_in(const or_lv *o, const or_xf *x, v3 p, v3 d, double stepmax, or_counters *c)
+{
+  return shape_dist_in(o, xf_transform(x, p), xf_transform_dir(x, d), stepmax, c);
+}
+static double bo_placed_dist_out(const or_lv *o, const or_xf *x, v3 p, v3 d, double stepmax, or_counters *c)
+{
+  return shape_dist_out(o, xf_transform(x, p), xf_transform_dir(x, d), stepmax, c);
+}
+static double bo_safe_in(const or_lv *o, const or_xf *x, v3 p, or_counters *c)
+{
+  return shape_safe_in(o, xf_transform(x, p), c);
+}
+static v3 v3_axpy(v3 p, double a, v3 d) { return v3_make(p.x + a * d.x, p.y + a * d.y, p.z + a * d.z); }
+
+static int boolean_contains(const or_boolean *b, v3 p, or_counters *c)
+{
+  switch (b->op) {
+  case 0: /* BooleanUnionImplementation.h Contains */
+    if (bo_contains(b->left, &b->lxf, p, c)) return 1;
+    return bo_contains(b->right, &b->rxf, p, c);
+  case 1: /* BooleanIntersectionImplementation.h Contains */
+  {
+    const int a = bo_contains(b->left, &b->lxf, p, c);
+    const int r = bo_contains(b->right, &b->rxf, p, c);
+    return a && r;
+  }
+  default: /* BooleanImplementation.h Contains (subtraction) */
+    if (!bo_contains(b->left, &b->lxf, p, c)) return 0;
+    return !bo_contains(b->right, &b->rxf, p, c);
+  }
+}
+
+/* -1: a union point on both operands' surfaces, whose answer takes their normals (unsupported) */
+static int boolean_inside(const or_boolean *b, v3 p, or_counters *c)
+{
+  const int a = bo_inside(b->left, &b->lxf, p, c);
+  int r;
+  switch (b->op) {
+  case 0:
+    if (a == OR_INSIDE) return OR_INSIDE;
+    r = bo_inside(b->right, &b->rxf, p, c);
+    if (r == OR_INSIDE) return OR_INSIDE;
+    if (a == OR_SURFACE && r == OR_SURFACE) return -1;
+    if (r == OR_SURFACE || a == OR_SURFACE) return OR_SURFACE;
+    return OR_OUTSIDE;
+  case 1:
+    if (a == OR_OUTSIDE) return OR_OUTSIDE;
+    r = bo_inside(b->right, &b->rxf, p, c);
+    if (a == OR_INSIDE && r == OR_INSIDE) return OR_INSIDE;
+    if ((a == OR_INSIDE && r == OR_SURFACE) || (r == OR_INSIDE && a == OR_SURFACE) ||
+        (a == OR_SURFACE && r == OR_SURFACE))
+      return OR_SURFACE;
+    return OR_OUTSIDE;
+  default:
+    if (a == OR_OUTSIDE) return OR_OUTSIDE;
+    r = bo_inside(b->right, &b->rxf, p, c);
+    if (a == OR_INSIDE && r == OR_OUTSIDE) return OR_INSIDE;
+    if ((a == OR_INSIDE && r == OR_SURFACE) || (r == OR_OUTSIDE && a == OR_SURFACE)) return OR_SURFACE;
+    return OR_OUTSIDE;
+  }
+}
+
+static double boolean_dist_in(const or_boolean *b, v3 p, v3 d, double stepmax, or_counters *c)
+{
+  const or_lv *L = b->left, *R = b->right;
+  const or_xf *lx = &b->lxf, *rx = &b->rxf;
+  long it;
+  if (b->op == 0) { /* union */
+    const double d1 = bo_dist_in(L, lx, p, d, stepmax, c);
+    const double d2 = bo_dist_in(R, rx, p, d, stepmax, c);
+    return d1 < d2 ? d1 : d2; /* Min */
+  }
+  if (b->op == 1) { /* intersection */
+    v3 hit      = p;
+    int inleft  = bo_contains(L, lx, hit, c);
+    int inright = bo_contains(R, rx, hit, c);
+    double d1 = 0., d2 = 0., snext = 0.;
+    if (inleft && inright) {
+      d1 = bo_placed_dist_out(L, lx, hit, d, stepmax, c);
+      d2 = bo_placed_dist_out(R, rx, hit, d, stepmax, c);
+      if (d1 < 2 * kTolerance) inleft = 0;
+      if (d2 < 2 * kTolerance) inright = 0;
+      if (inleft && inright) return 0.0;
+    }
+    for (it = 0; it < OR_BOOL_MAX_ITER; ++it) {
+      d1 = d2 = 0;
+      if (!inleft) {
+        d1 = bo_dist_in(L, lx, hit, d, kInfLength, c);
+        d1 = d1 > kTolerance ? d1 : kTolerance; /* Max */
+        if (d1 > 1E20) return kInfLength;
+      }
+      if (!inright) {
+        d2 = bo_dist_in(R, rx, hit, d, kInfLength, c);
+        d2 = d2 > kTolerance ? d2 : kTolerance;
+        if (d2 > 1E20) return kInfLength;
+      }
+      if (d1 > d2) {
+        snext += d1;
+        inleft  = 1;
+        hit     = v3_axpy(hit, d1, d);
+        inright = bo_contains(R, rx, v3_axpy(hit, kTolerance, d), c);
+        if (inright) return snext;
+      } else {
+        snext += d2;
+        inright = 1;
+        hit     = v3_axpy(hit, d2, d);
+        inleft  = bo_contains(L, lx, v3_axpy(hit, kTolerance, d), c);
+        if (inleft) return snext;
+      }
+    }
+    return kInfLength;
+  }
+  { /* subtraction */
+    double d1, d2, snxt = 0.;
+    v3 hit              = p;
+    int insideRight     = bo_contains(R, rx, p, c);
+    const double epsil  = kPushTolerance;
+    for (it = 0; it < OR_BOOL_MAX_ITER; ++it) {
+      if (insideRight) {
+        d1 = bo_placed_dist_out(R, rx, hit, d, stepmax, c);
+        snxt += (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : 0.;
+        hit = v3_axpy(hit, (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : 0., d);
+        if (bo_contains(L, lx, hit, c)) {
+          const double check = bo_placed_dist_out(L, lx, hit, d, kInfLength, c);
+          if (check > epsil) return snxt;
+        }
+      }
+      d2 = bo_dist_in(L, lx, hit, d, stepmax, c);
+      d2 = d2 > 0. ? d2 : 0.; /* Max(d2, 0) */
+      if (d2 == kInfLength) return kInfLength;
+      d1 = bo_dist_in(R, rx, hit, d, stepmax, c);
+      if (d2 < d1 - kTolerance) {
+        snxt += d2 + epsil;
+        return snxt;
+      }
+      snxt += (d1 >= 0. && d1 < kInfLength) ? d1 + epsil : 0.;
+      hit         = v3_axpy(hit, (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : epsil, d);
+      insideRight = 1;
+    }
+    return kInfLength;
+  }
+}
+
+/* BooleanUnionImplementation.h DistanceToOut: the loop over connecting operands */
+static double union_dist_out_walk(const or_lv *A, const or_xf *ax, const or_lv *B, const or_xf *bx, v3 p, v3 d,
+                                  or_counters *c)
+{
+  double dist = 0.;
+  const double pushdist = kPushTolerance;
+  v3 nextp = p;
+  int connecting;
+  long it = 0;
+  do {
+    double disTmp;
+    connecting = 0;
+    disTmp     = bo_placed_dist_out(A, ax, nextp, d, kInfLength, c);
+    dist += (disTmp >= 0. && disTmp < kInfLength) ? disTmp : 0;
+    dist += pushdist;
+    nextp = v3_axpy(p, dist, d);
+    if (bo_inside(B, bx, nextp, c) != OR_OUTSIDE) {
+      disTmp = bo_placed_dist_out(B, bx, nextp, d, kInfLength, c);
+      dist += (disTmp >= 0. && disTmp < kInfLength) ? disTmp : 0;
+      dist += pushdist;
+      nextp      = v3_axpy(p, dist, d);
+      connecting = 1;
+    }
+  } while (connecting && bo_inside(A, ax, nextp, c) != OR_OUTSIDE && ++it < OR_BOOL_MAX_ITER);
+  return dist;
+}
+
+static double boolean_dist_out(const or_boolean *b, v3 p, v3 d, double stepmax, or_counters *c)
+{
+  const or_lv *L = b->left, *R = b->right;
+  const or_xf *lx = &b->lxf, *rx = &b->rxf;
+  if (b->op == 0) {
+    const int posA = bo_inside(L, lx, p, c);
+    const double dist = posA != OR_OUTSIDE ? union_dist_out_walk(L, lx, R, rx, p, d, c)
+                                           : union_dist_out_walk(R, rx, L, lx, p, d, c);
+    double distance = dist - kPushTolerance;
+    if (distance < kTolerance && posA == OR_OUTSIDE && bo_inside(R, rx, p, c) == OR_OUTSIDE) distance = -kTolerance;
+    return distance;
+  }
+  if (b->op == 1) {
+    const double a = shape_dist_out(L, p, d, kInfLength, c); /* the left operand unplaced */
+    const double r = bo_placed_dist_out(R, rx, p, d, kInfLength, c);
+    return a < r ? a : r;
+  }
+  {
+    const double distancel = bo_placed_dist_out(L, lx, p, d, stepmax, c);
+    const double dinright  = bo_dist_in(R, rx, p, d, stepmax, c);
+    return distancel < dinright ? distancel : dinright;
+  }
+}
+
+static double boolean_safe_in(const or_boolean *b, v3 p, or_counters *c)
+{
+  const or_lv *L = b->left, *R = b->right;
+  const or_xf *lx = &b->lxf, *rx = &b->rxf;
+  if (b->op == 0) {
+    const double a = bo_safe_in(L, lx, p, c), r = bo_safe_in(R, rx, p, c);
+    return a < r ? a : r;
+  }
+  if (b->op == 1) {
+    const int insideA = bo_contains(L, lx, p, c);
+    const int insideB = bo_contains(R, rx, p, c);
+    if (!insideA && insideB) return bo_safe_in(L, lx, p, c);
+    if (!insideB && insideA) return bo_safe_in(R, rx, p, c);
+    {
+      const double a = bo_safe_in(L, lx, p, c), r = bo_safe_in(R, rx, p, c);
+      return a < r ? a : r;
+    }
+  }
+  if (bo_contains(L, lx, p, c) && bo_contains(R, rx, p, c)) return shape_safe_out(R, xf_transform(rx, p), c);
+  return bo_safe_in(L, lx, p, c);
+}
+
+static double boolean_safe_out(const or_boolean *b, v3 p, or_counters *c)
+{
+  const or_lv *L = b->left, *R = b->right;
+  const or_xf *lx = &b->lxf, *rx = &b->rxf;
+  if (b->op == 0) {
+    const int insideA = bo_inside(L, lx, p, c);
+    const int insideB = bo_inside(R, rx, p, c);
+    if (insideA == OR_OUTSIDE && insideB == OR_OUTSIDE) return -kTolerance;
+    if (insideA != OR_OUTSIDE && insideB != OR_OUTSIDE) {
+      const double a = shape_safe_out(L, p, c), r = shape_safe_out(R, xf_transform(rx, p), c);
+      return a > r ? a : r; /* Max */
+    }
+    if (insideA == OR_SURFACE || insideB == OR_SURFACE) return -kTolerance;
+    if (insideA == OR_OUTSIDE) return shape_safe_out(R, xf_transform(rx, p), c);
+    return shape_safe_out(L, p, c);
+  }
+  if (b->op == 1) {
+    const double a = shape_safe_out(L, p, c), r = shape_safe_out(R, xf_transform(rx, p), c);
+    double safety = a < r ? a : r;
+    if (safety < 0.) safety = 0.;
+    return safety;
+  }
+  {
+    const double a = shape_safe_out(L, p, c), r = bo_safe_in(R, rx, p, c);
+    return a < r ? a : r;
+  }
+}
+
+/* VPlacedVolume::Extent (source/PlacedVolume.cpp:139-175): the shape's extent taken into its
+ * mother's frame (the eight corners when the placement rotates, else the two extremes) */
+static void placed_extent(const or_lv *o, const or_xf *x, v3 *mn, v3 *mx)
+{
+  v3 pmin, pmax;
+  shape_extent(o, &pmin, &pmax);
+  if (x->has_rot) {
+    v3 b[8];
+    int i;
+    b[0] = xf_inverse_transform(x, v3_make(pmin.x, pmin.y, pmin.z));
+    b[1] = xf_inverse_transform(x, v3_make(pmax.x, pmin.y, pmin.z));
+    b[2] = xf_inverse_transform(x, v3_make(pmin.x, pmax.y, pmin.z));
+    b[3] = xf_inverse_transform(x, v3_make(pmax.x, pmax.y, pmin.z));
+    b[4] = xf_inverse_transform(x, v3_make(pmin.x, pmin.y, pmax.z));
+    b[5] = xf_inverse_transform(x, v3_make(pmax.x, pmin.y, pmax.z));
+    b[6] = xf_inverse_transform(x, v3_make(pmin.x, pmax.y, pmax.z));
+    b[7] = xf_inverse_transform(x, v3_make(pmax.x, pmax.y, pmax.z));
+    *mn = b[0];
+    *mx = b[0];
+    for (i = 1; i < 8; ++i) {
+      *mn = v3_make(or_min(mn->x, b[i].x), or_min(mn->y, b[i].y), or_min(mn->z, b[i].z));
+      *mx = v3_make(or_max(mx->x, b[i].x), or_max(mx->y, b[i].y), or_max(mx->z, b[i].z));
+    }
+  } else {
+    *mn = xf_inverse_transform(x, pmin);
+    *mx = xf_inverse_transform(x, pmax);
+  }
+}
+
+/* TransformedExtent (source/UnplacedBooleanVolume.cpp:403-442): the box of the operand's
+ * placed extent, whose corners it takes through the placement once more (the placed extent is
+ * already in the boolean's frame, so a translated or rotated operand's box comes out larger
+ * than the operand; the reference's extents, and so its bounding boxes, are these) */
+static void transformed_extent(const or_lv *o, const or_xf *x, v3 *mn, v3 *mx)
+{
+  v3 lower, upper, delta;
+  double minx = kInfLength, miny = kInfLength, minz = kInfLength;
+  double maxx = -kInfLength, maxy = -kInfLength, maxz = -kInfLength;
+  int i, j, k;
+  placed_extent(o, x, &lower, &upper);
+  delta = v3_sub(upper, lower);
+  for (i = 0; i <= 1; ++i)
+    for (j = 0; j <= 1; ++j)
+      for (k = 0; k <= 1; ++k) {
+        v3 corner, tc;
+        corner.x = lower.x + i * delta.x;
+        corner.y = lower.y + j * delta.y;
+        corner.z = lower.z + k * delta.z;
+        tc       = xf_inverse_transform(x, corner);
+        minx     = tc.x < minx ? tc.x : minx; /* std::min(minx, v) */
+        miny     = tc.y < miny ? tc.y : miny;
+        minz     = tc.z < minz ? tc.z : minz;
+        maxx     = maxx < tc.x ? tc.x : maxx; /* std::max(maxx, v) */
+        maxy     = maxy < tc.y ? tc.y : maxy;
+        maxz     = maxz < tc.z ? tc.z : maxz;
+      }
+  *mn = v3_make(minx, miny, minz);
+  *mx = v3_make(maxx, maxy, maxz);
+}
+
+/* UnplacedBooleanVolume<op>::Extent (source/UnplacedBooleanVolume.cpp:444-490) */
+static void boolean_extent(const or_boolean *b, v3 *mn, v3 *mx)
+{
+  v3 minL, maxL, minR, maxR;
+  transformed_extent(b->left, &b->lxf, &minL, &maxL);
+  transformed_extent(b->right, &b->rxf, &minR, &maxR);
+  if (b->op == 2) {
+    *mn = minL;
+    *mx = maxL;
+  } else if (b->op == 0) {
+    *mn = v3_make(minL.x < minR.x ? minL.x : minR.x, minL.y < minR.y ? minL.y : minR.y,
+                  minL.z < minR.z ? minL.z : minR.z);
+    *mx = v3_make(maxL.x > maxR.x ? maxL.x : maxR.x, maxL.y > maxR.y ? maxL.y : maxR.y,
+                  maxL.z > maxR.z ? maxL.z : maxR.z);
+  } else {
+    *mn = v3_make(minL.x > minR.x ? minL.x : minR.x, minL.y > minR.y ? minL.y : minR.y,
+                  minL.z > minR.z ? minL.z : minR.z);
+    *mx = v3_make(maxL.x < maxR.x ? maxL.x : maxR.x, maxL.y < maxR.y ? maxL.y : maxR.y,
+                  maxL.z < maxR.z ? maxL.z : maxR.z);
+  }
+}
+
 int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
 {
   (void)n_avail;
@@ -2923,6 +3267,16 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
     lv->s.orb.r = p[0];
     return 0;
   case OR_CUTTUBE: return cuttube_init(&lv->s.ctube, p, err, errlen);
+  case OR_BOOLEAN: /* operands are linked once the placements are known (or_core.c) */
+    if (!(p[0] == 0. || p[0] == 1. || p[0] == 2.) || !(p[1] >= 0. && p[1] <= 2147483647. && p[1] == floor(p[1])) ||
+        !(p[2] >= 0. && p[2] <= 2147483647. && p[2] == floor(p[2]))) {
+      set_err(err, errlen, "boolean: bad operation or operand ids");
+      return -1;
+    }
+    lv->s.boo.op       = (int)p[0];
+    lv->s.boo.left_pv  = (int)p[1];
+    lv->s.boo.right_pv = (int)p[2];
+    return 0;
   default: set_err(err, errlen, "unsupported shape type"); return -1;
   }
 }
@@ -2945,6 +3299,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
     *mx = v3_make(lv->s.orb.r, lv->s.orb.r, lv->s.orb.r);
     return;
   case OR_CUTTUBE: cuttube_extent(&lv->s.ctube, mn, mx); return;
+  case OR_BOOLEAN: boolean_extent(&lv->s.boo, mn, mx); return;
   }
 }
 
@@ -2965,6 +3320,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_POLYCONE: return polycone_dist_in(&lv->s.pcon, p, d);
   case OR_ORB: return orb_dist_in(&lv->s.orb, p, d);
   case OR_CUTTUBE: return cuttube_dist_in(&lv->s.ctube, p, d, stepmax);
+  case OR_BOOLEAN: return boolean_dist_in(&lv->s.boo, p, d, stepmax, c);
   }
   return kInfLength;
 }
@@ -2983,6 +3339,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_POLYCONE: return polycone_dist_out(&lv->s.pcon, p, d);
   case OR_ORB: return orb_dist_out(&lv->s.orb, p, d);
   case OR_CUTTUBE: return cuttube_dist_out(&lv->s.ctube, p, d);
+  case OR_BOOLEAN: return boolean_dist_out(&lv->s.boo, p, d, stepmax, c);
   }
   return -1.;
 }
@@ -3000,6 +3357,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_POLYCONE: return polycone_safe_in(&lv->s.pcon, p);
   case OR_ORB: return orb_safe_in(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_safe_in(&lv->s.ctube, p);
+  case OR_BOOLEAN: return boolean_safe_in(&lv->s.boo, p, c);
   }
   return kInfLength;
 }
@@ -3017,6 +3375,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_POLYCONE: return polycone_safe_out(&lv->s.pcon, p);
   case OR_ORB: return orb_safe_out(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_safe_out(&lv->s.ctube, p);
+  case OR_BOOLEAN: return boolean_safe_out(&lv->s.boo, p, c);
   }
   return 0.;
 }
@@ -3034,6 +3393,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_POLYCONE: return polycone_contains(&lv->s.pcon, p);
   case OR_ORB: return orb_contains(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_contains(&lv->s.ctube, p);
+  case OR_BOOLEAN: return boolean_contains(&lv->s.boo, p, c);
   }
   return 0;
 }
@@ -3051,6 +3411,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_POLYCONE: return polycone_inside(&lv->s.pcon, p);
   case OR_ORB: return orb_inside(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_inside(&lv->s.ctube, p);
+  case OR_BOOLEAN: return boolean_inside(&lv->s.boo, p, c);
   }
   return kOutsideE;
 }

@@ -23,12 +23,12 @@ OP_DIST_IN, OP_DIST_OUT, OP_SAFE_IN, OP_SAFE_OUT, OP_CONTAINS, OP_INSIDE = range
 class Counters(C.Structure):
     _fields_ = [("node_slab", C.c_uint64), ("prim_slab", C.c_uint64), ("node_safety", C.c_uint64),
                 ("prim_safety", C.c_uint64), ("prim_contains", C.c_uint64), ("transforms", C.c_uint64),
-                ("kernel", (C.c_uint64 * 6) * 9)]
+                ("kernel", (C.c_uint64 * 6) * 10)]  # per shape type (OR_NSHAPES) and query
 
     def as_dict(self) -> dict:
         d = {k: int(getattr(self, k)) for k in ("node_slab", "prim_slab", "node_safety", "prim_safety",
                                                 "prim_contains", "transforms")}
-        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(9)]
+        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(10)]
         return d
 
 
@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
         L.or_safety_batch.argtypes = [p, l, p, p, p, p, p, i]
         L.or_locate_batch.argtypes = [p, l, p, p, p, p, i]
         L.or_approach_batch.argtypes = [p, l, p, p, p, p, p, p, p, p, p]
+        L.or_shape_extent.argtypes = [p, i, p]
         L.or_now.restype = C.c_double
         L.or_ncores.restype = C.c_int
         _lib = L
@@ -120,6 +121,13 @@ class OracleGeometry:
         rc = lib().or_shape_batch(self.h, lv, op, n, _p(x), _p(y), _p(z), _p(dx), _p(dy), _p(dz), _p(sm), _p(out))
         if rc:
             raise ValueError("bad shape query")
+        return out
+
+    def extent(self, lv: int) -> np.ndarray:
+        """The shape's Extent (VUnplacedVolume::Extent): min then max corner."""
+        out = np.zeros(6)
+        if lib().or_shape_extent(self.h, lv, _p(out)):
+            raise ValueError("bad logical volume")
         return out
 
     def approach(self, lv, x, y, z, dx, dy, dz, last, step):

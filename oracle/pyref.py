@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
         L.vgref_safety_batch.argtypes = [l, p, p, p, p, p, i]
         L.vgref_locate_batch.argtypes = [l, p, p, p, p, i]
         L.vgref_approach_batch.argtypes = [l, p, p, p, p, p, p, p, p, p, i]
+        L.vgref_extent.argtypes = [i, p]
         L.vgref_ncores.restype = i
         _lib = L
     return _lib
@@ -167,6 +168,14 @@ class RefGeometry:
         x, y, z = _c(x), _c(y), _c(z)
         out = np.zeros(x.shape[0])
         lib().vgref_safety_batch(x.shape[0], _p(x), _p(y), _p(z), _p(np.ascontiguousarray(states)), _p(out), nthreads)
+        return out
+
+    def extent(self, lv: int) -> np.ndarray:
+        """The shape's Extent (VUnplacedVolume::Extent): min then max corner."""
+        self._check()
+        out = np.zeros(6)
+        if lib().vgref_extent(lv, _p(out)):
+            raise ValueError("bad logical volume")
         return out
 
     def approach(self, lv, x, y, z, dx, dy, dz, last, step, nthreads=0):

@@ -38,6 +38,7 @@
 #include "VecGeom/navigation/NavigationState.h"
 #include "VecGeom/volumes/LogicalVolume.h"
 #include "VecGeom/volumes/PlacedVolume.h"
+#include "VecGeom/volumes/BooleanVolume.h"
 #include "VecGeom/volumes/UnplacedBox.h"
 #include "VecGeom/volumes/UnplacedCone.h"
 #include "VecGeom/volumes/UnplacedCutTube.h"
@@ -168,7 +169,34 @@ int vgref_geom_create(int n_lv, const int *lv_shape, const int *lv_param_off, co
       set_err(err, errlen, "shape parameters out of range");
       return 1;
     }
-    VUnplacedVolume *u = make_shape(lv_shape[i], params + lv_param_off[i]);
+    VUnplacedVolume *u = nullptr;
+    if (lv_shape[i] == 9) {  // boolean: place its operands now, as a boolean's creator does
+      const double *p = params + lv_param_off[i];
+      VPlacedVolume const *operand[2] = {nullptr, nullptr};
+      for (int k = 0; k < 2; ++k) {
+        const int pv = (int)p[1 + k];
+        if (pv < 0 || pv >= n_pv || pv_mother[pv] != -2 || pv_lv[pv] < 0 || pv_lv[pv] >= i) {
+          set_err(err, errlen, "bad boolean operand");
+          return 1;
+        }
+        const double *t = pv_trans + 12 * (size_t)pv;
+        auto *xf = new Transformation3D(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], t[9], t[10], t[11]);
+        const std::string name = "op" + std::to_string(pv);
+        operand[k]             = g_lv[(size_t)pv_lv[pv]]->Place(name.c_str(), xf);
+        if (operand[k]->id() != (unsigned)pv) {  // ids count up in creation order
+          set_err(err, errlen, "this driver creates operands with their boolean: their ids must follow that order");
+          return 1;
+        }
+      }
+      switch ((int)p[0]) {
+      case 0: u = new UnplacedBooleanVolume<kUnion>(kUnion, operand[0], operand[1]); break;
+      case 1: u = new UnplacedBooleanVolume<kIntersection>(kIntersection, operand[0], operand[1]); break;
+      case 2: u = new UnplacedBooleanVolume<kSubtraction>(kSubtraction, operand[0], operand[1]); break;
+      default: break;
+      }
+    } else {
+      u = make_shape(lv_shape[i], params + lv_param_off[i]);
+    }
     if (!u) {
       set_err(err, errlen, "unsupported shape type");
       return 1;
@@ -179,10 +207,11 @@ int vgref_geom_create(int n_lv, const int *lv_shape, const int *lv_param_off, co
   VPlacedVolume *world = nullptr;
   // placements in id order: VPlacedVolume ids count up in creation order (source/PlacedVolume.cpp:32)
   for (int i = 0; i < n_pv; ++i) {
-    if (pv_lv[i] < 0 || pv_lv[i] >= n_lv || pv_mother[i] < -1 || pv_mother[i] >= n_lv) {
+    if (pv_lv[i] < 0 || pv_lv[i] >= n_lv || pv_mother[i] < -2 || pv_mother[i] >= n_lv) {
       set_err(err, errlen, "placement refers to an unknown logical volume");
       return 1;
     }
+    if (pv_mother[i] == -2) continue;  // a boolean operand, placed with its boolean
     const double *t = pv_trans + 12 * (size_t)i;
     auto *xf = new Transformation3D(t[0], t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8], t[9], t[10], t[11]);
     if (pv_mother[i] < 0) {
@@ -408,6 +437,16 @@ int vgref_approach_batch(long n, const int *lv, const double *px, const double *
                                                       Vector3D<Precision>(dx[i], dy[i], dz[i]), step[i], lastpv);
     }
   });
+  return 0;
+}
+
+// VUnplacedVolume::Extent of logical volume lv's shape: min then max corner
+int vgref_extent(int lv, double *out6)
+{
+  if (!g_ready || lv < 0 || lv >= (int)g_lv.size()) return 1;
+  Vector3D<Precision> mn, mx;
+  g_lv[(size_t)lv]->GetUnplacedVolume()->Extent(mn, mx);
+  for (int k = 0; k < 3; ++k) out6[k] = mn[k], out6[3 + k] = mx[k];
   return 0;
 }
 

@@ -23,7 +23,9 @@ extern "C" {
 
 /* shape type ids (same numbering as the product's vgn_shape_type) */
 enum { OR_BOX = 0, OR_TUBE = 1, OR_CONE = 2, OR_TRD = 3, OR_TRAP = 4, OR_SPHERE = 5, OR_POLYCONE = 6, OR_ORB = 7,
-       OR_CUTTUBE = 8, OR_NSHAPES = 9 };
+       OR_CUTTUBE = 8, OR_BOOLEAN = 9, OR_NSHAPES = 10 };
+/* pv_mother of a boolean solid's operand placement (outside the hierarchy) */
+#define OR_BOOLEAN_OPERAND (-2)
 
 /* shape operations for or_shape_batch */
 enum { OR_OP_DIST_IN = 0, OR_OP_DIST_OUT = 1, OR_OP_SAFE_IN = 2, OR_OP_SAFE_OUT = 3, OR_OP_CONTAINS = 4, OR_OP_INSIDE = 5 };
@@ -105,6 +107,9 @@ void or_locate_batch(const or_geom *g, long n, const double *px, const double *p
 int or_approach_batch(const or_geom *g, long n, const int *lv, const double *px, const double *py,
                       const double *pz, const double *dx, const double *dy, const double *dz, const int *last,
                       double *step);
+
+/* VUnplacedVolume::Extent of logical volume lv's shape: min then max corner */
+int or_shape_extent(const or_geom *g, int lv, double *out6);
 
 /* wall-clock helper for the CPU baseline */
 double or_now(void);

@@ -18,8 +18,13 @@ writes inputs and outputs to tests/golden/ref_fixtures.npz:
   nested        the three-level geometry: 2048 located tracks, one step, a walk
   deep_cache1   the five-level geometry with global matrices cached down to level 1 only
                 (transformation cache depth 1): 2048 located tracks, one step, a walk
-  approach/<key>  BVH::ApproachNextDaughter on the mixed_all, nested and deep_cache1
-                geometries: 4096 tracks over their BVHs (tests/helpers.py approach_inputs)
+  booleans      64 boolean solids (subtraction, union, intersection, a box minus a union
+                of two tubes) in a box world: 2048 located tracks, one step, a walk
+  bool_shapes/<k>  those four boolean kinds alone: 1024 points in 1.3 times their extent,
+                the six shape queries (Inside only for the two kinds without a union)
+  approach/<key>  BVH::ApproachNextDaughter on the mixed_all, nested, deep_cache1 and
+                booleans geometries: 4096 tracks over their BVHs (tests/helpers.py
+                approach_inputs)
   shapes        every parameter set of tests/shape_sets.py: up to 192 points (random,
                 coordinate planes and axes, surface), all six queries
 
@@ -211,9 +216,40 @@ def generate() -> dict:
     _steps(out, "deep_cache1", rg, t)
     _walk(out, "deep_cache1", rg, t)
 
+    # 64 boolean solids of four kinds
+    desc = W.boolean_geometry()
+    rg = pyref.RefGeometry(desc)
+    t = W.uniform_tracks(2048, 490.0, 63, 64)
+    t.states = rg.locate(t.x, t.y, t.z)
+    put_desc(out, "booleans", desc)
+    put_tracks(out, "booleans", t)
+    _steps(out, "booleans", rg, t)
+    _walk(out, "booleans", rg, t)
+
+    # the boolean kinds' six shape queries (INSIDE only without a union: the reference's
+    # union Inside is not restated)
+    for kind in range(4):
+        b = W.GeometryBuilder()
+        lv = W.boolean_solid(b, kind)
+        b.place_world(lv)
+        desc = b.build()
+        rg = pyref.RefGeometry(desc)
+        key = f"bool_shapes/{kind}"
+        ext = rg.extent(lv)
+        mid, half = 0.5 * (ext[:3] + ext[3:]), 0.65 * (ext[3:] - ext[:3])
+        rng = np.random.Generator(np.random.PCG64(80 + kind))
+        X, Y, Z = (rng.uniform(mid[k] - half[k], mid[k] + half[k], 1024) for k in range(3))
+        DX, DY, DZ = W.isotropic(rng, 1024)
+        put_desc(out, key, desc)
+        out[f"{key}/lv"] = np.array(lv)
+        for k, a in zip(TRACK_KEYS[:6], (X, Y, Z, DX, DY, DZ)):
+            out[f"{key}/in/{k}"] = a
+        for op in range(5 if kind in (1, 3) else 6):
+            out[f"{key}/out/op{op}"] = rg.shape(lv, op, X, Y, Z, DX, DY, DZ)
+
     # BVH::ApproachNextDaughter
     from helpers import approach_inputs
-    for key, half in (("mixed_all", 1000.0), ("nested", 480.0), ("deep_cache1", 590.0)):
+    for key, half in (("mixed_all", 1000.0), ("nested", 480.0), ("deep_cache1", 590.0), ("booleans", 490.0)):
         desc = get_desc(out, key)
         rg = pyref.RefGeometry(desc, cache_depth=get_cache_depth(out, key))
         a = approach_inputs(desc, 4096, 71, half)

@@ -12,8 +12,8 @@ from golden import make_ref_fixtures as F
 from shape_sets import SHAPE_SETS
 from vecgeom_gb300 import workloads as W
 
-NAV_KEYS = ["box_grid", "mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1"]
-WALK_KEYS = ["mixed", "mixed_all", "nested", "deep_cache1"]
+NAV_KEYS = ["box_grid", "mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "booleans"]
+WALK_KEYS = ["mixed", "mixed_all", "nested", "deep_cache1", "booleans"]
 
 
 @pytest.fixture(scope="module")
@@ -62,7 +62,7 @@ def test_oracle_walk_equals_reference(oracle, fx, key):
     assert np.array_equal(words(st), fx[f"{key}/walk/states"])
 
 
-APPROACH_FX = ["mixed_all", "nested", "deep_cache1"]
+APPROACH_FX = ["mixed_all", "nested", "deep_cache1", "booleans"]
 
 
 @pytest.mark.parametrize("key", APPROACH_FX)

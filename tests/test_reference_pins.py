@@ -37,10 +37,12 @@ def geometries():
         # matrices are accumulated from the placements, NavStateIndex.h:232-265)
         "deep_cache1": (deep, W.uniform_tracks(1 << 15, 590.0, 33, 34)),
         "deep_cache3": (deep, W.uniform_tracks(1 << 15, 590.0, 35, 36)),
+        # boolean solids: subtraction, union, intersection and a nested subtraction of a union
+        "booleans": (W.boolean_geometry(), W.uniform_tracks(1 << 15, 490.0, 37, 38)),
     }
 
 
-GEOS = ["box_grid", "mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "deep_cache3"]
+GEOS = ["box_grid", "mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "deep_cache3", "booleans"]
 
 
 def cache_depth(which):
@@ -119,7 +121,8 @@ def test_vector_interface_equals_scalar(oracle, cases):
     assert np.array_equal(o["step"], v["step"]) and same_states(o["out"], v["out"])
 
 
-@pytest.mark.parametrize("which", ["mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "deep_cache3"])
+@pytest.mark.parametrize("which", ["mixed", "mixed_sections", "mixed_all", "nested", "deep_cache1", "deep_cache3",
+                                   "booleans"])
 def test_walk_equals_reference(oracle, cases, which):
     """Every step of a track subset, stepped until it leaves the world: oracle == reference."""
     desc, t = cases[which]
@@ -148,6 +151,8 @@ def test_approach_equals_reference(oracle, cases, which):
     rg = pyref.RefGeometry(desc, cache_depth=cd)
     og = oracle.OracleGeometry(desc, cache_depth=cd)
     half = 1000.0 if which in ("box_grid", "mixed", "mixed_sections", "mixed_all") else 600.0
+    if which == "booleans":
+        half = 500.0
     a = approach_inputs(desc, 1 << 15, 61, half)
     r = rg.approach(*a)
     assert np.array_equal(og.approach(*a), r)

@@ -55,6 +55,7 @@ GEOMETRIES = {
     "mixed_sections": lambda: W.mixed_shape_geometry(sections=True),
     "mixed_all_shapes": lambda: W.mixed_shape_geometry(seed=26, shapes=W.ALL_SHAPES),
     "nested": lambda: W.nested_geometry(),
+    "booleans": lambda: W.boolean_geometry(),
 }
 
 

@@ -24,11 +24,14 @@ INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-# (source, object name, extra nvcc flags); the navigation kernels are compiled twice:
-# with the phi/theta section code (namespace `sections`) and without it (`full_ranges`)
+# (source, object name, extra nvcc flags); the navigation kernels are compiled three times:
+# with the phi/theta section code (namespace `sections`), without it (`full_ranges`) and with
+# the boolean-solid code but not the section code (`booleans`, one launch shape per kernel
+# family: with the section code as well this unit compiled for seven minutes)
 UNITS = [
     ("kernels_nav.cu", "kernels_nav_sections", ["-fmad=false", "-DVGN_SECTIONS=1"]),
     ("kernels_nav.cu", "kernels_nav_full_ranges", ["-fmad=false", "-DVGN_SECTIONS=0"]),
+    ("kernels_nav.cu", "kernels_nav_booleans", ["-fmad=false", "-DVGN_SECTIONS=0", "-DVGN_BOOLEANS=1"]),
     ("kernels_sort.cu", "kernels_sort", []),
     ("host_geometry.cpp", "host_geometry", []),
     ("host_shapes.cpp", "host_shapes", []),

@@ -30,7 +30,7 @@ constexpr int kMaxLevels = 30;  // bound on geometry depth (relocation loops)
 
 enum ShapeType : int32_t {
   kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kOrb = 7, kCutTube = 8,
-  kNumShapes = 9
+  kBoolean = 9, kNumShapes = 10
 };
 
 // flags of a placement transformation (Transformation3D::SetProperties,
@@ -168,6 +168,12 @@ constexpr int kOrbSize = 1;
 // are both TubeStruct::fAlongPhi* and the wedge's; the block's last entry is fDphi)
 enum { TubeRmin = 0, TubeRmax, TubeZ, TubeRmin2, TubeRmax2, TubeTolIrmin2, TubeTolOrmin2, TubeTolIrmax2,
        TubeTolOrmax2, TubeMaxVal, TubeSphi, TubeTolOz, TubeWedge, TubeDphi = TubeWedge + 8, kTubeSize };
+// Boolean: BooleanStruct (BooleanStruct.h:23-25) with its placed operands resolved: the
+// operation (0 union, 1 intersection, 2 subtraction), each operand's shape type and the offset
+// of its shape row relative to this row, then each operand placement's transformation
+// (tx, ty, tz, r0..r8), left then right
+enum { BoolOp = 0, BoolLeftType, BoolLeftRow, BoolRightType, BoolRightRow, BoolLeftXf, BoolRightXf = BoolLeftXf + 12,
+       kBoolSize = BoolRightXf + 12 };
 // CutTube: CutTubeStruct (CutTubeStruct.h:21-46): its tube's row (infinite half-length), then
 // fDz, the bottom and top cut planes (unit normal, distance), cos/sin of phi and phi+dphi, fMaxVal
 enum { CutTubeDz = kTubeSize, CutTubeN0, CutTubeD0 = CutTubeN0 + 3, CutTubeN1, CutTubeD1 = CutTubeN1 + 3,

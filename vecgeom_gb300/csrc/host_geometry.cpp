@@ -335,6 +335,60 @@ inline float round_up(double v)
 
 void build_interval_images(HostGeometry &g);
 
+// Boolean solids (vgn_shape_type VGN_BOOLEAN): each operand placement (pv_mother
+// VGN_BOOLEAN_OPERAND, anywhere in the placement list) is used by exactly one boolean
+// (UnplacedBooleanVolume.h:59 holds its own placed operands); an operand's logical volume
+// precedes its boolean, has no daughters and is a primitive or a boolean of primitives.  Fills each boolean's row with its operands' shape types, row
+// offsets (relative to the boolean's row) and placement transforms.
+static int link_booleans(HostGeometry &g, const vgn_geometry_desc &d, std::string &err)
+{
+  int used = 0, n_operands = 0;
+  std::vector<char> taken(d.n_placed, 0);
+  for (int i = 0; i < d.n_placed; ++i)
+    if (d.pv_mother[i] == VGN_BOOLEAN_OPERAND) ++n_operands;
+  for (size_t l = 0; l < g.lv.size(); ++l) {
+    if (g.lv[l].shape != kBoolean) continue;
+    g.booleans = true;
+    double *b  = &g.shape[g.lv[l].shape_row];
+    for (int k = 0; k < 2; ++k) {
+      const int rowi = k == 0 ? row::BoolLeftRow : row::BoolRightRow;
+      const int pv   = (int)b[rowi];
+      if (pv >= d.n_placed || d.pv_mother[pv] != VGN_BOOLEAN_OPERAND || taken[pv]++) {
+        err = "a boolean operand must be a placement whose mother is VGN_BOOLEAN_OPERAND, used once";
+        return VGN_ERR_ARG;
+      }
+      ++used;
+      const int olv = d.pv_logical[pv];
+      if (olv >= (int)l) {
+        err = "a boolean operand's logical volume must precede the boolean";
+        return VGN_ERR_ARG;
+      }
+      const HostLV &o = g.lv[olv];
+      if (!o.daughters.empty()) {
+        err = "a boolean operand must have no daughters";
+        return VGN_ERR_ARG;
+      }
+      if (o.shape == kBoolean) {
+        const double *ob = &g.shape[o.shape_row];
+        if (ob[row::BoolLeftType] == kBoolean || ob[row::BoolRightType] == kBoolean) {
+          err = "booleans nest two levels at most";
+          return VGN_ERR_UNSUPPORTED;
+        }
+      }
+      b[k == 0 ? row::BoolLeftType : row::BoolRightType] = o.shape;
+      b[rowi]                                           = (double)(o.shape_row - g.lv[l].shape_row);
+      std::copy(d.pv_transform + 12 * (size_t)pv, d.pv_transform + 12 * (size_t)pv + 12,
+                b + (k == 0 ? row::BoolLeftXf : row::BoolRightXf));
+    }
+    g.sections = g.sections || shape_row_has_sections(kBoolean, b);
+  }
+  if (used != n_operands) {
+    err = "a boolean operand placement is not used by exactly one boolean";
+    return VGN_ERR_ARG;
+  }
+  return VGN_OK;
+}
+
 int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string &err, int32_t cache_depth)
 {
   if (cache_depth < 0) {
@@ -377,7 +431,7 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
   }
   for (int i = 0; i < d.n_placed; ++i) {
     const int l = d.pv_logical[i], m = d.pv_mother[i];
-    if (l < 0 || l >= d.n_logical || m < -1 || m >= d.n_logical || (m == -1 && i != d.world_placed)) {
+    if (l < 0 || l >= d.n_logical || m < VGN_BOOLEAN_OPERAND || m >= d.n_logical || (m == -1 && i != d.world_placed)) {
       err = "placed volume " + std::to_string(i) + " refers to an invalid logical volume";
       return VGN_ERR_ARG;
     }
@@ -388,6 +442,11 @@ int build_host_geometry(const vgn_geometry_desc &d, HostGeometry &g, std::string
       g.pv[i].child_id = (int32_t)g.lv[m].daughters.size();
       g.lv[m].daughters.push_back(i);
     }
+  }
+  if (int rc = link_booleans(g, d, err)) return rc;
+  if (g.booleans && g.sections) {
+    err = "boolean solids in a geometry with phi or theta sections are not supported";
+    return VGN_ERR_UNSUPPORTED;
   }
   for (const HostLV &lv : g.lv)
     if (lv.daughters.size() >= 65535) {

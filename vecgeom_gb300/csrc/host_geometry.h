@@ -76,6 +76,9 @@ struct HostGeometry {
   std::vector<float> isin;  // interval SafetyToIn rows (geom_types.h irow), (lo, hi) pairs
   std::vector<double> lv_bbox;  // per logical volume: shape Extent, min then max corner (VUnplacedVolume::fBBox)
   bool sections = false;    // some shape has a phi or theta section: needs the `sections` kernel set
+  bool booleans = false;    // some shape is a boolean solid: needs the `booleans` kernel set
+  // the kernel set for this geometry: 0 full_ranges, 1 sections, 2 booleans (full ranges and booleans)
+  int kset() const { return booleans ? 2 : (sections ? 1 : 0); }
 };
 
 // Returns 0 on success, a VGN_ERR_* code otherwise (message in err).  `cache_depth` as

@@ -60,6 +60,7 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
   case kSphere: return 6;
   case kOrb: return 1;
   case kCutTube: return 11;
+  case kBoolean: return 3;  // operation, left and right operand placements
   case kPolycone: {  // sphi, dphi, nz, z[nz], rmin[nz], rmax[nz]
     if (n_avail < 3 || !(p[2] >= 2 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
     return 3 + 3 * (int)p[2];
@@ -434,6 +435,20 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.push_back(p[0]);
     return VGN_OK;
   }
+  case kBoolean: {  // operands resolved by link_booleans (host_geometry.cpp) once placements are read
+    auto is_id = [](double v) { return v >= 0. && v <= 2147483647. && v == std::floor(v); };
+    if (!(p[0] == 0. || p[0] == 1. || p[0] == 2.) || !is_id(p[1]) || !is_id(p[2])) {
+      err = "boolean: the operation must be 0, 1 or 2 and the operands placement ids";
+      return VGN_ERR_ARG;
+    }
+    std::vector<double> b(row::kBoolSize, 0.);
+    b[row::BoolOp]       = p[0];
+    b[row::BoolLeftRow]  = p[1];  // operand placement ids until linked
+    b[row::BoolRightRow] = p[2];
+    b[row::BoolLeftType] = b[row::BoolRightType] = -1.;
+    shape.insert(shape.end(), b.begin(), b.end());
+    return VGN_OK;
+  }
   default: err = "unsupported shape type " + std::to_string(type); return VGN_ERR_UNSUPPORTED;
   }
 }
@@ -449,7 +464,85 @@ bool shape_row_has_sections(int32_t type, const double *r)
     return r[row::pcon_cone(n, 0) + row::ConeDPhi] < 2. * kPi;
   }
   case kSphere: return r[row::SphFull] == 0.;
+  case kBoolean:  // the operands' (once linked)
+    return (r[row::BoolLeftType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolLeftType], r + (int64_t)r[row::BoolLeftRow])) ||
+           (r[row::BoolRightType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolRightType], r + (int64_t)r[row::BoolRightRow]));
   default: return false;
+  }
+}
+
+static inline double vmin(double a, double b) { return a < b ? a : b; }  // vecCore::math::Min
+static inline double vmax(double a, double b) { return a > b ? a : b; }  // vecCore::math::Max
+
+// VPlacedVolume::Extent (source/PlacedVolume.cpp:139-175) of a boolean's operand: its shape's
+// extent taken into the boolean's frame (the eight corners when the placement rotates, else
+// the two extremes)
+static void operand_placed_extent(const double *b, int k, Vec3 &mn, Vec3 &mx)
+{
+  const int32_t type  = (int32_t)b[k == 0 ? row::BoolLeftType : row::BoolRightType];
+  const double *orow  = b + (int64_t)b[k == 0 ? row::BoolLeftRow : row::BoolRightRow];
+  const HostXForm x   = xform_from12(b + (k == 0 ? row::BoolLeftXf : row::BoolRightXf));
+  Vec3 pmin, pmax;
+  shape_extent(type, orow, pmin, pmax);
+  if (x.has_rot) {
+    const Vec3 c[8] = {{pmin.x, pmin.y, pmin.z}, {pmax.x, pmin.y, pmin.z}, {pmin.x, pmax.y, pmin.z},
+                       {pmax.x, pmax.y, pmin.z}, {pmin.x, pmin.y, pmax.z}, {pmax.x, pmin.y, pmax.z},
+                       {pmin.x, pmax.y, pmax.z}, {pmax.x, pmax.y, pmax.z}};
+    mn = mx = xform_inverse_transform(x, c[0]);
+    for (int i = 1; i < 8; ++i) {
+      const Vec3 t = xform_inverse_transform(x, c[i]);
+      mn           = {vmin(mn.x, t.x), vmin(mn.y, t.y), vmin(mn.z, t.z)};
+      mx           = {vmax(mx.x, t.x), vmax(mx.y, t.y), vmax(mx.z, t.z)};
+    }
+  } else {
+    mn = xform_inverse_transform(x, pmin);
+    mx = xform_inverse_transform(x, pmax);
+  }
+}
+
+// TransformedExtent (source/UnplacedBooleanVolume.cpp:403-442): the box of the operand's placed
+// extent, whose corners it takes through the placement once more (the placed extent is already
+// in the boolean's frame, so a moved operand's box comes out larger than the operand: the
+// reference's extents, and so its bounding boxes, are these)
+static void operand_transformed_extent(const double *b, int k, Vec3 &mn, Vec3 &mx)
+{
+  const HostXForm x = xform_from12(b + (k == 0 ? row::BoolLeftXf : row::BoolRightXf));
+  Vec3 lower, upper;
+  operand_placed_extent(b, k, lower, upper);
+  const Vec3 delta{upper.x - lower.x, upper.y - lower.y, upper.z - lower.z};
+  double minx = 1.7976931348623157e308, miny = minx, minz = minx;
+  double maxx = -minx, maxy = -minx, maxz = -minx;
+  for (int i = 0; i <= 1; ++i)
+    for (int j = 0; j <= 1; ++j)
+      for (int l = 0; l <= 1; ++l) {
+        const Vec3 t = xform_inverse_transform(x, {lower.x + i * delta.x, lower.y + j * delta.y, lower.z + l * delta.z});
+        minx = std::min(minx, t.x);
+        miny = std::min(miny, t.y);
+        minz = std::min(minz, t.z);
+        maxx = std::max(maxx, t.x);
+        maxy = std::max(maxy, t.y);
+        maxz = std::max(maxz, t.z);
+      }
+  mn = {minx, miny, minz};
+  mx = {maxx, maxy, maxz};
+}
+
+// UnplacedBooleanVolume<op>::Extent (source/UnplacedBooleanVolume.cpp:444-490)
+static void boolean_extent(const double *b, Vec3 &mn, Vec3 &mx)
+{
+  Vec3 minL, maxL, minR, maxR;
+  operand_transformed_extent(b, 0, minL, maxL);
+  operand_transformed_extent(b, 1, minR, maxR);
+  const int op = (int)b[row::BoolOp];
+  if (op == 2) {
+    mn = minL;
+    mx = maxL;
+  } else if (op == 0) {
+    mn = {vmin(minL.x, minR.x), vmin(minL.y, minR.y), vmin(minL.z, minR.z)};
+    mx = {vmax(maxL.x, maxR.x), vmax(maxL.y, maxR.y), vmax(maxL.z, maxR.z)};
+  } else {
+    mn = {vmax(minL.x, minR.x), vmax(minL.y, minR.y), vmax(minL.z, minR.z)};
+    mx = {vmin(maxL.x, maxR.x), vmin(maxL.y, maxR.y), vmin(maxL.z, maxR.z)};
   }
 }
 
@@ -700,6 +793,7 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mn = {-r[0], -r[0], -r[0]};
     mx = {r[0], r[0], r[0]};
     return;
+  case kBoolean: boolean_extent(r, mn, mx); return;
   default: mn = mx = {0, 0, 0};
   }
 }

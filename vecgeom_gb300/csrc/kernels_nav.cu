@@ -120,7 +120,7 @@ __device__ __forceinline__ void grouped_step(const GeomView &g, bool live, D3 gp
   unsigned done = 0;
   st = 0.;
   if (live) {
-    step_begin(g, gp, gd, s, lp, ld, lv, st);
+    step_begin(g, gp, gd, slimit, s, lp, ld, lv, st);
     make_ray(r, lp, ld);
     stepI = fi(st);
     last  = ni_top(g, s.last_exited);
@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(256) shape_kernel_fp64(int type, const double 
     if (OP == VGN_OP_DISTANCE_TO_IN)
       r = shape_dist_in(type, row, p, d3(dx[i], dy[i], dz[i]), step_max ? step_max[i] : kInfLength);
     else if (OP == VGN_OP_DISTANCE_TO_OUT)
-      r = shape_dist_out(type, row, p, d3(dx[i], dy[i], dz[i]));
+      r = shape_dist_out(type, row, p, d3(dx[i], dy[i], dz[i]), step_max ? step_max[i] : kInfLength);
     else if (OP == VGN_OP_SAFETY_TO_IN)
       r = shape_safe_in(type, row, p);
     else if (OP == VGN_OP_SAFETY_TO_OUT)
@@ -574,6 +574,11 @@ static inline unsigned grid_for(int64_t n, int block, int max_blocks)
   return (unsigned)b;
 }
 
+// The `sections` and `booleans` kernel sets instantiate one launch shape per kernel family
+// (every variant number maps to it; results do not depend on the launch shape): with every
+// shape, their units compiled for six and seven minutes.
+#define VGN_ONE_LAUNCH_SHAPE (VGN_SECTIONS || VGN_BOOLEANS)
+
 // Launch-shape variants of the step kernel (threads per block, minimum
 // resident blocks per SM -> register cap); the autotuner picks one per geometry.
 struct StepVariant {
@@ -619,6 +624,12 @@ static void launch_step_grouped(const GeomView &g, const StepArgs &a, cudaStream
 template <bool MIXED>
 static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cudaStream_t s)
 {
+#if VGN_ONE_LAUNCH_SHAPE  // one launch shape per kernel family keeps this set's build short
+  if (MIXED && variant >= kNumStepVariants)
+    launch_step_grouped<128, 4>(g, a, s);
+  else
+    launch_step_v<MIXED, 128, 4>(g, a, s);
+#else
   if (MIXED) {
     switch (variant) {
     case 6: launch_step_grouped<128, 5>(g, a, s); return;
@@ -635,6 +646,7 @@ static void launch_step_m(const GeomView &g, const StepArgs &a, int variant, cud
   case 5: launch_step_v<MIXED, 128, 4>(g, a, s); break;
   default: launch_step_v<MIXED, 256, 2>(g, a, s); break;
   }
+#endif
 }
 
 // The safety runs as its own pass, before the step (which may overwrite the input states when
@@ -675,6 +687,10 @@ static void launch_multi_v(const JobTable &jt, uint32_t *queue, int reloc, int n
 template <bool MIXED>
 static void launch_multi_m(const JobTable &jt, uint32_t *queue, int reloc, int num_sms, int variant, cudaStream_t s)
 {
+#if VGN_ONE_LAUNCH_SHAPE
+  (void)variant;
+  launch_multi_v<MIXED, 128, 4>(jt, queue, reloc, num_sms, s);
+#else
   switch (variant) {
   case 1: launch_multi_v<MIXED, 256, 3>(jt, queue, reloc, num_sms, s); break;
   case 2: launch_multi_v<MIXED, 128, 6>(jt, queue, reloc, num_sms, s); break;
@@ -683,6 +699,7 @@ static void launch_multi_m(const JobTable &jt, uint32_t *queue, int reloc, int n
   case 5: launch_multi_v<MIXED, 128, 4>(jt, queue, reloc, num_sms, s); break;
   default: launch_multi_v<MIXED, 256, 2>(jt, queue, reloc, num_sms, s); break;
   }
+#endif
 }
 
 cudaError_t launch_multi_step(const JobTable &jt, uint32_t *queue, bool mixed, int reloc, int num_sms, int variant,
@@ -730,6 +747,10 @@ cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, do
                         int32_t *nsteps, const uint32_t *perm, bool mixed, int variant, int max_blocks,
                         cudaStream_t s)
 {
+#if VGN_ONE_LAUNCH_SHAPE
+  if (mixed && VGN_SMEM_STACK && variant >= kNumStepVariants)
+    return launch_walk_grouped<128, 4>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps, perm, max_blocks, s);
+#else
   if (mixed && VGN_SMEM_STACK) {
     switch (variant) {
     case 6: return launch_walk_grouped<128, 5>(g, n, px, py, pz, dx, dy, dz, slimit, state, max_steps, nsteps, perm, max_blocks, s);
@@ -738,6 +759,7 @@ cudaError_t launch_walk(const GeomView &g, int64_t n, double *px, double *py, do
     default: break;
     }
   }
+#endif
   const int block     = 128;
   const unsigned grid = grid_for(n, block, max_blocks * 2);
   const size_t smem   = step_smem_bytes(block);

@@ -57,12 +57,17 @@ struct JobTable {
   int32_t n_jobs;
 };
 static_assert(sizeof(JobTable) < 32000, "kernel parameters are limited to 32764 bytes");
-// Navigation kernels (kernels_nav.cu), compiled twice: `sections` handles phi and theta
+// Navigation kernels (kernels_nav.cu), compiled three times: `sections` handles phi and theta
 // sections, `full_ranges` leaves that code out (geometries whose shapes all span the full
-// angular ranges).  Both sets give identical results on full-range geometries.
+// angular ranges), `booleans` adds the boolean solids to `full_ranges` (a geometry may not
+// hold both booleans and sections).  The sets give identical results on the geometries they
+// all handle.
 namespace sections {
 #include "launch_set.inc"
 }  // namespace sections
+namespace booleans {
+#include "launch_set.inc"
+}  // namespace booleans
 namespace full_ranges {
 #include "launch_set.inc"
 }  // namespace full_ranges

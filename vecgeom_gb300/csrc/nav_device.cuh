@@ -131,32 +131,7 @@ __device__ __forceinline__ void top_matrix(const GeomView &g, uint32_t ni, Xf &m
   m = t;
 }
 
-// Transform<kGeneric,kGeneric> (Transformation3D.h:663-673, 729-735, 746-770)
-__device__ __forceinline__ D3 xf_point(const double *t, const double *r, D3 p)
-{
-  const double t0 = p.x - t[0], t1 = p.y - t[1], t2 = p.z - t[2];
-  double l0 = t0 * r[0], l1 = t0 * r[1], l2 = t0 * r[2];
-  l0 += t1 * r[3];
-  l1 += t1 * r[4];
-  l2 += t1 * r[5];
-  l0 += t2 * r[6];
-  l1 += t2 * r[7];
-  l2 += t2 * r[8];
-  return d3(l0, l1, l2);
-}
-
-// TransformDirection<kGeneric>
-__device__ __forceinline__ D3 xf_dir(const double *r, D3 d)
-{
-  double l0 = d.x * r[0], l1 = d.x * r[1], l2 = d.x * r[2];
-  l0 += d.y * r[3];
-  l1 += d.y * r[4];
-  l2 += d.y * r[5];
-  l0 += d.z * r[6];
-  l1 += d.z * r[7];
-  l2 += d.z * r[8];
-  return d3(l0, l1, l2);
-}
+// Transform<kGeneric,kGeneric>: xf_point and xf_dir (shapes_fp64.cuh)
 
 // InverseTransform (Transformation3D.h:793-827)
 __device__ __forceinline__ D3 xf_inverse(const double *t, const double *r, D3 l)

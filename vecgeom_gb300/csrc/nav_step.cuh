@@ -136,9 +136,10 @@ __device__ __forceinline__ double safety_local(const GeomView &g, const LVRec &l
 }
 
 // Start of a step: the input state's global matrix, the local point and direction, the
-// volume and the mother's DistanceToOut (VNavigator.h:444-458; BVHNavigator.h:53-61).
-__device__ __forceinline__ void step_begin(const GeomView &g, D3 gp, D3 gd, const State &in, D3 &lp, D3 &ld,
-                                           LVRec &lv, double &step)
+// volume and the mother's DistanceToOut, given the step limit (VNavigator.h:241-249, 444-458;
+// BVHNavigator.h:53-61; a boolean mother hands it to its operands).
+__device__ __forceinline__ void step_begin(const GeomView &g, D3 gp, D3 gd, double slimit, const State &in, D3 &lp,
+                                           D3 &ld, LVRec &lv, double &step)
 {
   Xf m;
   top_matrix(g, in.nav_ind, m);
@@ -146,7 +147,7 @@ __device__ __forceinline__ void step_begin(const GeomView &g, D3 gp, D3 gd, cons
   ld            = xf_dir(m.r, gd);
   const int pv  = ni_top(g, in.nav_ind);
   lv            = load_lv(g, pv_lv(g, pv));
-  step          = shape_dist_out(lv.shape, g.shape + lv.shape_row, lp, ld);
+  step          = shape_dist_out(lv.shape, g.shape + lv.shape_row, lp, ld, slimit);
   if (step < 0.) step = 0.;
 }
 
@@ -187,7 +188,7 @@ __device__ __forceinline__ double nav_step(const GeomView &g, D3 gp, D3 gd, doub
   D3 lp, ld;
   LVRec lv;
   double step;
-  step_begin(g, gp, gd, in, lp, ld, lv, step);
+  step_begin(g, gp, gd, slimit, in, lp, ld, lv, step);
   int hit = -1;
   if (MIXED) {
     MixedRay r;

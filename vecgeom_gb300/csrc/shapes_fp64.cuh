@@ -18,7 +18,12 @@
 #ifndef VGN_SECTIONS
 #define VGN_SECTIONS 1
 #endif
-#if VGN_SECTIONS
+#ifndef VGN_BOOLEANS
+#define VGN_BOOLEANS 0  // the kernel set carries the boolean solids' code (built without the sections')
+#endif
+#if VGN_BOOLEANS
+#define VGN_KSET booleans
+#elif VGN_SECTIONS
 #define VGN_KSET sections
 #else
 #define VGN_KSET full_ranges
@@ -30,6 +35,7 @@ inline namespace VGN_KSET {
 
 constexpr double kTolerance     = 1e-9;
 constexpr double kHalfTolerance = 0.5 * kTolerance;
+constexpr double kPushTolerance = 1e-6;  // Math.h:28
 constexpr double kInfLength     = DBL_MAX;
 constexpr double kEpsilon       = DBL_EPSILON;
 
@@ -40,6 +46,34 @@ struct D3 {
 };
 
 __device__ __forceinline__ D3 d3(double x, double y, double z) { return D3{x, y, z}; }
+
+// Transform<kGeneric,kGeneric> (Transformation3D.h:663-673, 729-735, 746-770): a point and a
+// direction into the frame of a placement (translation t, row-major rotation r)
+__device__ __forceinline__ D3 xf_point(const double *t, const double *r, D3 p)
+{
+  const double t0 = p.x - t[0], t1 = p.y - t[1], t2 = p.z - t[2];
+  double l0 = t0 * r[0], l1 = t0 * r[1], l2 = t0 * r[2];
+  l0 += t1 * r[3];
+  l1 += t1 * r[4];
+  l2 += t1 * r[5];
+  l0 += t2 * r[6];
+  l1 += t2 * r[7];
+  l2 += t2 * r[8];
+  return d3(l0, l1, l2);
+}
+
+// TransformDirection<kGeneric>
+__device__ __forceinline__ D3 xf_dir(const double *r, D3 d)
+{
+  double l0 = d.x * r[0], l1 = d.x * r[1], l2 = d.x * r[2];
+  l0 += d.y * r[3];
+  l1 += d.y * r[4];
+  l2 += d.y * r[5];
+  l0 += d.z * r[6];
+  l1 += d.z * r[7];
+  l2 += d.z * r[8];
+  return d3(l0, l1, l2);
+}
 __device__ __forceinline__ double vmin(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double vmax(double a, double b) { return a > b ? a : b; }
 __device__ __forceinline__ double min3(double a, double b, double c) { return vmin(vmin(a, b), c); }
@@ -2445,10 +2479,10 @@ __device__ __forceinline__ double cuttube_safe_out(const double *r, D3 p)
   return safety;
 }
 
-// ---------------------------------------------------------------- dispatch
-// `stepmax` is the step the caller still accepts (the BVH passes its running step,
-// BVH.h:115); only the cut tube's DistanceToIn reads it
-__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d, double stepmax = kInfLength)
+// ---------------------------------------------------------------- dispatch (primitive shapes)
+// `stepmax` is the step the caller still accepts; of the primitives only the cut tube's DistanceToIn
+// reads it (booleans hand it to their operands)
+__device__ __forceinline__ double prim_dist_in(int type, const double *r, D3 p, D3 d, double stepmax)
 {
   switch (type) {
   case kBox: return box_dist_in(r, p, d);
@@ -2464,7 +2498,7 @@ __device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p,
   return kInfLength;
 }
 
-__device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p, D3 d)
+__device__ __forceinline__ double prim_dist_out(int type, const double *r, D3 p, D3 d)
 {
   switch (type) {
   case kBox: return box_dist_out(r, p, d);
@@ -2480,7 +2514,7 @@ __device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p
   return -1.;
 }
 
-__device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
+__device__ __forceinline__ double prim_safe_in(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_safe_in(r, p);
@@ -2496,7 +2530,7 @@ __device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
   return kInfLength;
 }
 
-__device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p)
+__device__ __forceinline__ double prim_safe_out(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_safe_out(r, p);
@@ -2512,7 +2546,7 @@ __device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p
   return 0.;
 }
 
-__device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
+__device__ __forceinline__ bool prim_contains(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_contains(r, p);
@@ -2528,7 +2562,7 @@ __device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
   return false;
 }
 
-__device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
+__device__ __forceinline__ int prim_inside(int type, const double *r, D3 p)
 {
   switch (type) {
   case kBox: return box_inside(r, p);
@@ -2543,6 +2577,381 @@ __device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
   }
   return kOutsideE;
 }
+
+#if VGN_BOOLEANS
+// ---------------------------------------------------------------- Boolean solids
+// BooleanImplementation.h (subtraction), BooleanUnionImplementation.h and
+// BooleanIntersectionImplementation.h over placed operands.  A placed operand's Contains,
+// Inside, DistanceToIn, PlacedDistanceToOut and SafetyToIn take the boolean-frame point into the
+// operand's frame (SpecializedPlacedVolImplHelper.h:99-172); its DistanceToOut and SafetyToOut
+// do not (PlacedVolImplHelper.h:76-100).  Operands are primitives or (DEPTH 2) booleans of
+// primitives.  The reference's loops are unbounded; these stop after kBoolMaxIter rounds
+// (never reached on a valid solid).  Out of line: a boolean's code holds the operands' shape
+// dispatch several times over and is needed only where booleans are placed.
+constexpr long kBoolMaxIter = 1000000;
+
+struct BoolOperand {
+  int type;
+  const double *row, *t, *r;  // shape row, placement translation and rotation
+};
+__device__ __forceinline__ BoolOperand bool_operand(const double *b, int k)
+{
+  const int ti = k == 0 ? row::BoolLeftType : row::BoolRightType;
+  const int ri = k == 0 ? row::BoolLeftRow : row::BoolRightRow;
+  const double *x = b + (k == 0 ? row::BoolLeftXf : row::BoolRightXf);
+  return BoolOperand{(int)b[ti], b + (long)b[ri], x, x + 3};
+}
+__device__ __forceinline__ D3 axpy(D3 p, double a, D3 d) { return d3(p.x + a * d.x, p.y + a * d.y, p.z + a * d.z); }
+
+template <int DEPTH> __device__ __noinline__ bool bool_contains(const double *b, D3 p);
+template <int DEPTH> __device__ __noinline__ int bool_inside(const double *b, D3 p);
+template <int DEPTH> __device__ __noinline__ double bool_dist_in(const double *b, D3 p, D3 d, double stepmax);
+template <int DEPTH> __device__ __noinline__ double bool_dist_out(const double *b, D3 p, D3 d, double stepmax);
+template <int DEPTH> __device__ __noinline__ double bool_safe_in(const double *b, D3 p);
+template <int DEPTH> __device__ __noinline__ double bool_safe_out(const double *b, D3 p);
+
+// the primitive dispatch for the booleans' operands, once each, out of line
+__device__ __noinline__ bool prim_contains_ool(int type, const double *r, D3 p) { return prim_contains(type, r, p); }
+__device__ __noinline__ int prim_inside_ool(int type, const double *r, D3 p) { return prim_inside(type, r, p); }
+__device__ __noinline__ double prim_dist_in_ool(int type, const double *r, D3 p, D3 d, double stepmax)
+{
+  return prim_dist_in(type, r, p, d, stepmax);
+}
+__device__ __noinline__ double prim_dist_out_ool(int type, const double *r, D3 p, D3 d)
+{
+  return prim_dist_out(type, r, p, d);
+}
+__device__ __noinline__ double prim_safe_in_ool(int type, const double *r, D3 p) { return prim_safe_in(type, r, p); }
+__device__ __noinline__ double prim_safe_out_ool(int type, const double *r, D3 p) { return prim_safe_out(type, r, p); }
+
+// an operand's unplaced queries: a primitive, or at DEPTH 2 a boolean of primitives
+template <int DEPTH>
+__device__ __forceinline__ bool op_contains(int type, const double *r, D3 p)
+{
+  if constexpr (DEPTH > 1) {
+    if (type == kBoolean) return bool_contains<DEPTH - 1>(r, p);
+  }
+  return prim_contains_ool(type, r, p);
+}
+template <int DEPTH>
+__device__ __forceinline__ int op_inside(int type, const double *r, D3 p)
+{
+  if constexpr (DEPTH > 1) {
+    if (type == kBoolean) return bool_inside<DEPTH - 1>(r, p);
+  }
+  return prim_inside_ool(type, r, p);
+}
+template <int DEPTH>
+__device__ __forceinline__ double op_dist_in(int type, const double *r, D3 p, D3 d, double stepmax)
+{
+  if constexpr (DEPTH > 1) {
+    if (type == kBoolean) return bool_dist_in<DEPTH - 1>(r, p, d, stepmax);
+  }
+  return prim_dist_in_ool(type, r, p, d, stepmax);
+}
+template <int DEPTH>
+__device__ __forceinline__ double op_dist_out(int type, const double *r, D3 p, D3 d, double stepmax)
+{
+  if constexpr (DEPTH > 1) {
+    if (type == kBoolean) return bool_dist_out<DEPTH - 1>(r, p, d, stepmax);
+  }
+  return prim_dist_out_ool(type, r, p, d);
+}
+template <int DEPTH>
+__device__ __forceinline__ double op_safe_in(int type, const double *r, D3 p)
+{
+  if constexpr (DEPTH > 1) {
+    if (type == kBoolean) return bool_safe_in<DEPTH - 1>(r, p);
+  }
+  return prim_safe_in_ool(type, r, p);
+}
+template <int DEPTH>
+__device__ __forceinline__ double op_safe_out(int type, const double *r, D3 p)
+{
+  if constexpr (DEPTH > 1) {
+    if (type == kBoolean) return bool_safe_out<DEPTH - 1>(r, p);
+  }
+  return prim_safe_out_ool(type, r, p);
+}
+// placed forms
+template <int DEPTH>
+__device__ __forceinline__ bool pl_contains(const BoolOperand &o, D3 p)
+{
+  return op_contains<DEPTH>(o.type, o.row, xf_point(o.t, o.r, p));
+}
+template <int DEPTH>
+__device__ __forceinline__ int pl_inside(const BoolOperand &o, D3 p)
+{
+  return op_inside<DEPTH>(o.type, o.row, xf_point(o.t, o.r, p));
+}
+template <int DEPTH>
+__device__ __forceinline__ double pl_dist_in(const BoolOperand &o, D3 p, D3 d, double stepmax)
+{
+  return op_dist_in<DEPTH>(o.type, o.row, xf_point(o.t, o.r, p), xf_dir(o.r, d), stepmax);
+}
+template <int DEPTH>
+__device__ __forceinline__ double pl_dist_out(const BoolOperand &o, D3 p, D3 d, double stepmax)
+{
+  return op_dist_out<DEPTH>(o.type, o.row, xf_point(o.t, o.r, p), xf_dir(o.r, d), stepmax);
+}
+template <int DEPTH>
+__device__ __forceinline__ double pl_safe_in(const BoolOperand &o, D3 p)
+{
+  return op_safe_in<DEPTH>(o.type, o.row, xf_point(o.t, o.r, p));
+}
+
+template <int DEPTH>
+__device__ __noinline__ bool bool_contains(const double *b, D3 p)
+{
+  const BoolOperand L = bool_operand(b, 0), R = bool_operand(b, 1);
+  switch ((int)b[row::BoolOp]) {
+  case 0:  // BooleanUnionImplementation.h Contains
+    if (pl_contains<DEPTH>(L, p)) return true;
+    return pl_contains<DEPTH>(R, p);
+  case 1: {  // BooleanIntersectionImplementation.h Contains
+    const bool a = pl_contains<DEPTH>(L, p);
+    const bool r = pl_contains<DEPTH>(R, p);
+    return a && r;
+  }
+  default:  // BooleanImplementation.h Contains
+    if (!pl_contains<DEPTH>(L, p)) return false;
+    return !pl_contains<DEPTH>(R, p);
+  }
+}
+
+// kSurfaceE on both operands of a union takes their normals: answered -1 (not supported)
+template <int DEPTH>
+__device__ __noinline__ int bool_inside(const double *b, D3 p)
+{
+  const BoolOperand L = bool_operand(b, 0), R = bool_operand(b, 1);
+  const int a = pl_inside<DEPTH>(L, p);
+  int r;
+  switch ((int)b[row::BoolOp]) {
+  case 0:
+    if (a == kInsideE) return kInsideE;
+    r = pl_inside<DEPTH>(R, p);
+    if (r == kInsideE) return kInsideE;
+    if (a == kSurfaceE && r == kSurfaceE) return -1;
+    if (r == kSurfaceE || a == kSurfaceE) return kSurfaceE;
+    return kOutsideE;
+  case 1:
+    if (a == kOutsideE) return kOutsideE;
+    r = pl_inside<DEPTH>(R, p);
+    if (a == kInsideE && r == kInsideE) return kInsideE;
+    if ((a == kInsideE && r == kSurfaceE) || (r == kInsideE && a == kSurfaceE) || (a == kSurfaceE && r == kSurfaceE))
+      return kSurfaceE;
+    return kOutsideE;
+  default:
+    if (a == kOutsideE) return kOutsideE;
+    r = pl_inside<DEPTH>(R, p);
+    if (a == kInsideE && r == kOutsideE) return kInsideE;
+    if ((a == kInsideE && r == kSurfaceE) || (r == kOutsideE && a == kSurfaceE)) return kSurfaceE;
+    return kOutsideE;
+  }
+}
+
+template <int DEPTH>
+__device__ __noinline__ double bool_dist_in(const double *b, D3 p, D3 d, double stepmax)
+{
+  const BoolOperand L = bool_operand(b, 0), R = bool_operand(b, 1);
+  const int op = (int)b[row::BoolOp];
+  if (op == 0) {
+    const double d1 = pl_dist_in<DEPTH>(L, p, d, stepmax);
+    const double d2 = pl_dist_in<DEPTH>(R, p, d, stepmax);
+    return vmin(d1, d2);
+  }
+  if (op == 1) {
+    D3 hit       = p;
+    bool inleft  = pl_contains<DEPTH>(L, hit);
+    bool inright = pl_contains<DEPTH>(R, hit);
+    double d1 = 0., d2 = 0., snext = 0.;
+    if (inleft && inright) {
+      d1 = pl_dist_out<DEPTH>(L, hit, d, stepmax);
+      d2 = pl_dist_out<DEPTH>(R, hit, d, stepmax);
+      if (d1 < 2 * kTolerance) inleft = false;
+      if (d2 < 2 * kTolerance) inright = false;
+      if (inleft && inright) return 0.0;
+    }
+    for (long it = 0; it < kBoolMaxIter; ++it) {
+      d1 = d2 = 0;
+      if (!inleft) {
+        d1 = vmax(pl_dist_in<DEPTH>(L, hit, d, kInfLength), kTolerance);
+        if (d1 > 1E20) return kInfLength;
+      }
+      if (!inright) {
+        d2 = vmax(pl_dist_in<DEPTH>(R, hit, d, kInfLength), kTolerance);
+        if (d2 > 1E20) return kInfLength;
+      }
+      if (d1 > d2) {
+        snext += d1;
+        inleft  = true;
+        hit     = axpy(hit, d1, d);
+        inright = pl_contains<DEPTH>(R, axpy(hit, kTolerance, d));
+        if (inright) return snext;
+      } else {
+        snext += d2;
+        inright = true;
+        hit     = axpy(hit, d2, d);
+        inleft  = pl_contains<DEPTH>(L, axpy(hit, kTolerance, d));
+        if (inleft) return snext;
+      }
+    }
+    return kInfLength;
+  }
+  double d1, d2, snxt = 0.;
+  D3 hit             = p;
+  bool insideRight   = pl_contains<DEPTH>(R, p);
+  const double epsil = kPushTolerance;
+  for (long it = 0; it < kBoolMaxIter; ++it) {
+    if (insideRight) {
+      d1 = pl_dist_out<DEPTH>(R, hit, d, stepmax);
+      snxt += (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : 0.;
+      hit = axpy(hit, (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : 0., d);
+      if (pl_contains<DEPTH>(L, hit)) {
+        const double check = pl_dist_out<DEPTH>(L, hit, d, kInfLength);
+        if (check > epsil) return snxt;
+      }
+    }
+    d2 = vmax(pl_dist_in<DEPTH>(L, hit, d, stepmax), 0.);
+    if (d2 == kInfLength) return kInfLength;
+    d1 = pl_dist_in<DEPTH>(R, hit, d, stepmax);
+    if (d2 < d1 - kTolerance) {
+      snxt += d2 + epsil;
+      return snxt;
+    }
+    snxt += (d1 >= 0. && d1 < kInfLength) ? d1 + epsil : 0.;
+    hit         = axpy(hit, (d1 >= 0. && d1 < kInfLength) ? (d1 + epsil) : epsil, d);
+    insideRight = true;
+  }
+  return kInfLength;
+}
+
+// BooleanUnionImplementation.h DistanceToOut: the walk over connecting operands
+template <int DEPTH>
+__device__ __forceinline__ double union_out_walk(const BoolOperand &A, const BoolOperand &B, D3 p, D3 d)
+{
+  double dist           = 0.;
+  const double pushdist = kPushTolerance;
+  D3 nextp              = p;
+  bool connecting;
+  long it = 0;
+  do {
+    connecting    = false;
+    double disTmp = pl_dist_out<DEPTH>(A, nextp, d, kInfLength);
+    dist += (disTmp >= 0. && disTmp < kInfLength) ? disTmp : 0;
+    dist += pushdist;
+    nextp = axpy(p, dist, d);
+    if (pl_inside<DEPTH>(B, nextp) != kOutsideE) {
+      disTmp = pl_dist_out<DEPTH>(B, nextp, d, kInfLength);
+      dist += (disTmp >= 0. && disTmp < kInfLength) ? disTmp : 0;
+      dist += pushdist;
+      nextp      = axpy(p, dist, d);
+      connecting = true;
+    }
+  } while (connecting && pl_inside<DEPTH>(A, nextp) != kOutsideE && ++it < kBoolMaxIter);
+  return dist;
+}
+
+template <int DEPTH>
+__device__ __noinline__ double bool_dist_out(const double *b, D3 p, D3 d, double stepmax)
+{
+  const BoolOperand L = bool_operand(b, 0), R = bool_operand(b, 1);
+  const int op = (int)b[row::BoolOp];
+  if (op == 0) {
+    const int posA    = pl_inside<DEPTH>(L, p);
+    const double dist = posA != kOutsideE ? union_out_walk<DEPTH>(L, R, p, d) : union_out_walk<DEPTH>(R, L, p, d);
+    double distance   = dist - kPushTolerance;
+    if (distance < kTolerance && posA == kOutsideE && pl_inside<DEPTH>(R, p) == kOutsideE) distance = -kTolerance;
+    return distance;
+  }
+  if (op == 1) {
+    const double a = op_dist_out<DEPTH>(L.type, L.row, p, d, kInfLength);  // the left operand unplaced
+    const double r = pl_dist_out<DEPTH>(R, p, d, kInfLength);
+    return vmin(a, r);
+  }
+  const double distancel = pl_dist_out<DEPTH>(L, p, d, stepmax);
+  const double dinright  = pl_dist_in<DEPTH>(R, p, d, stepmax);
+  return vmin(distancel, dinright);
+}
+
+template <int DEPTH>
+__device__ __noinline__ double bool_safe_in(const double *b, D3 p)
+{
+  const BoolOperand L = bool_operand(b, 0), R = bool_operand(b, 1);
+  const int op = (int)b[row::BoolOp];
+  if (op == 0) return vmin(pl_safe_in<DEPTH>(L, p), pl_safe_in<DEPTH>(R, p));
+  if (op == 1) {
+    const bool insideA = pl_contains<DEPTH>(L, p);
+    const bool insideB = pl_contains<DEPTH>(R, p);
+    if (!insideA && insideB) return pl_safe_in<DEPTH>(L, p);
+    if (!insideB && insideA) return pl_safe_in<DEPTH>(R, p);
+    return vmin(pl_safe_in<DEPTH>(L, p), pl_safe_in<DEPTH>(R, p));
+  }
+  if (pl_contains<DEPTH>(L, p) && pl_contains<DEPTH>(R, p)) return op_safe_out<DEPTH>(R.type, R.row, xf_point(R.t, R.r, p));
+  return pl_safe_in<DEPTH>(L, p);
+}
+
+template <int DEPTH>
+__device__ __noinline__ double bool_safe_out(const double *b, D3 p)
+{
+  const BoolOperand L = bool_operand(b, 0), R = bool_operand(b, 1);
+  const int op = (int)b[row::BoolOp];
+  if (op == 0) {
+    const int insideA = pl_inside<DEPTH>(L, p);
+    const int insideB = pl_inside<DEPTH>(R, p);
+    if (insideA == kOutsideE && insideB == kOutsideE) return -kTolerance;
+    if (insideA != kOutsideE && insideB != kOutsideE)
+      return vmax(op_safe_out<DEPTH>(L.type, L.row, p), op_safe_out<DEPTH>(R.type, R.row, xf_point(R.t, R.r, p)));
+    if (insideA == kSurfaceE || insideB == kSurfaceE) return -kTolerance;
+    if (insideA == kOutsideE) return op_safe_out<DEPTH>(R.type, R.row, xf_point(R.t, R.r, p));
+    return op_safe_out<DEPTH>(L.type, L.row, p);
+  }
+  if (op == 1) {
+    double safety = vmin(op_safe_out<DEPTH>(L.type, L.row, p), op_safe_out<DEPTH>(R.type, R.row, xf_point(R.t, R.r, p)));
+    if (safety < 0.) safety = 0.;
+    return safety;
+  }
+  return vmin(op_safe_out<DEPTH>(L.type, L.row, p), pl_safe_in<DEPTH>(R, p));
+}
+
+#endif  // VGN_BOOLEANS
+
+// ---------------------------------------------------------------- dispatch (all shape types)
+// `stepmax` is the step the caller still accepts (the BVH passes its running step, BVH.h:115;
+// the navigator its step limit to the mother's DistanceToOut, VNavigator.h:246): the cut tube's
+// DistanceToIn and the booleans use it.  Kernel sets without the boolean code dispatch the
+// primitives only (the host runs geometries with booleans on the `booleans` set).
+#if VGN_BOOLEANS
+#define VGN_BOOL_OR(call, prim) (type == kBoolean ? call : prim)
+#else
+#define VGN_BOOL_OR(call, prim) (prim)
+#endif
+__device__ __forceinline__ double shape_dist_in(int type, const double *r, D3 p, D3 d, double stepmax = kInfLength)
+{
+  return VGN_BOOL_OR((bool_dist_in<2>(r, p, d, stepmax)), (prim_dist_in(type, r, p, d, stepmax)));
+}
+__device__ __forceinline__ double shape_dist_out(int type, const double *r, D3 p, D3 d, double stepmax = kInfLength)
+{
+  (void)stepmax;
+  return VGN_BOOL_OR((bool_dist_out<2>(r, p, d, stepmax)), (prim_dist_out(type, r, p, d)));
+}
+__device__ __forceinline__ double shape_safe_in(int type, const double *r, D3 p)
+{
+  return VGN_BOOL_OR((bool_safe_in<2>(r, p)), (prim_safe_in(type, r, p)));
+}
+__device__ __forceinline__ double shape_safe_out(int type, const double *r, D3 p)
+{
+  return VGN_BOOL_OR((bool_safe_out<2>(r, p)), (prim_safe_out(type, r, p)));
+}
+__device__ __forceinline__ bool shape_contains(int type, const double *r, D3 p)
+{
+  return VGN_BOOL_OR((bool_contains<2>(r, p)), (prim_contains(type, r, p)));
+}
+__device__ __forceinline__ int shape_inside(int type, const double *r, D3 p)
+{
+  return VGN_BOOL_OR((bool_inside<2>(r, p)), (prim_inside(type, r, p)));
+}
+#undef VGN_BOOL_OR
 
 }  // namespace VGN_KSET
 }  // namespace dev

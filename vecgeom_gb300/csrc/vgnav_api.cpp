@@ -46,9 +46,10 @@ struct vgn_geometry {
   size_t pipe_sort_words  = 0;
 };
 
-// The kernel set a call runs on: `sections` when a shape of the geometry has a phi or
-// theta section, else `full_ranges` (the same kernels compiled without the section code).
-#define VGN_KSET_FN(sect, fn) ((sect) ? vgn::sections::fn : vgn::full_ranges::fn)
+// The kernel set a call runs on (HostGeometry::kset): `booleans` when the geometry holds a
+// boolean solid, else `sections` when a shape has a phi or theta section, else `full_ranges`
+// (the same kernels compiled without the section and boolean code).
+#define VGN_KSET_FN(kset, fn) ((kset) == 2 ? vgn::booleans::fn : (kset) == 1 ? vgn::sections::fn : vgn::full_ranges::fn)
 
 namespace {
 
@@ -233,12 +234,12 @@ int enqueue_step(vgn_geometry *g, vgn::StepArgs a, bool mixed, cudaStream_t s, u
         e             = vgn::launch_bin_tracks(a.n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, b, buf, next, max_blocks(g), s);
         a.perm_safety = next;
       }
-      if (e == cudaSuccess) e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[m], s);
+      if (e == cudaSuccess) e = VGN_KSET_FN(g->host.kset(), launch_step)(g->view, a, mixed, g->step_variant[m], s);
       cudaFreeAsync(buf, s);
       return e == cudaSuccess ? VGN_OK : cuda_fail(e, "binned step launch");
     }
   }
-  cudaError_t e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[m], s);
+  cudaError_t e = VGN_KSET_FN(g->host.kset(), launch_step)(g->view, a, mixed, g->step_variant[m], s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
 }
 
@@ -574,7 +575,7 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
   const int kind = classify({px, py, pz, in, safety});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_safety)(g->view, n, px, py, pz, in, safety, mixed, max_blocks(g), s);
+    cudaError_t e = VGN_KSET_FN(g->host.kset(), launch_safety)(g->view, n, px, py, pz, in, safety, mixed, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "safety kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -590,7 +591,7 @@ int vgn_compute_safety_batch(const vgn_geometry *gc, int64_t n, const double *px
   if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = VGN_KSET_FN(g->host.sections, launch_safety)(g->view, n, bx, by, bz, din, dsaf, mixed, max_blocks(g), s);
+  e = VGN_KSET_FN(g->host.kset(), launch_safety)(g->view, n, bx, by, bz, din, dsaf, mixed, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "safety kernel launch");
   e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
@@ -612,7 +613,7 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   const int kind = classify({px, py, pz, out});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_locate)(g->view, n, px, py, pz, out, mixed, max_blocks(g), s);
+    cudaError_t e = VGN_KSET_FN(g->host.kset(), launch_locate)(g->view, n, px, py, pz, out, mixed, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "locate kernel launch");
   }
   std::lock_guard<std::mutex> lock(g->ws_mutex);
@@ -626,7 +627,7 @@ int vgn_locate_batch(const vgn_geometry *gc, int64_t n, const double *px, const 
   if (e == cudaSuccess) e = cudaMemcpyAsync(by, py, nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bz, pz, nd, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = VGN_KSET_FN(g->host.sections, launch_locate)(g->view, n, bx, by, bz, dout, mixed, max_blocks(g), s);
+  e = VGN_KSET_FN(g->host.kset(), launch_locate)(g->view, n, bx, by, bz, dout, mixed, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "locate kernel launch");
   e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
@@ -649,7 +650,7 @@ int vgn_approach_next_daughter_batch(const vgn_geometry *gc, int64_t n, const in
                            : classify({lv, px, py, pz, dx, dy, dz, step});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_approach)(g->view, n, lv, px, py, pz, dx, dy, dz, last_pv,
+    cudaError_t e = VGN_KSET_FN(g->host.kset(), launch_approach)(g->view, n, lv, px, py, pz, dx, dy, dz, last_pv,
                                                                    step, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "approach kernel launch");
   }
@@ -674,12 +675,22 @@ int vgn_approach_next_daughter_batch(const vgn_geometry *gc, int64_t n, const in
   if (e == cudaSuccess) e = cudaMemcpyAsync(dlv, lv, ni, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && last_pv) e = cudaMemcpyAsync(dlast, last_pv, ni, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = VGN_KSET_FN(g->host.sections, launch_approach)(g->view, n, dlv, b[0], b[1], b[2], b[3], b[4], b[5],
+  e = VGN_KSET_FN(g->host.kset(), launch_approach)(g->view, n, dlv, b[0], b[1], b[2], b[3], b[4], b[5],
                                                      last_pv ? dlast : nullptr, b[6], max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "approach kernel launch");
   e = cudaMemcpyAsync(step, b[6], nd, cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
   return check_status(g, s);
+}
+
+// a boolean (or an operand of it) is a union
+static bool boolean_has_union(const vgn::HostGeometry &h, int32_t row_off, int32_t type)
+{
+  if (type != vgn::kBoolean) return false;
+  const double *b = &h.shape[row_off];
+  if (b[vgn::row::BoolOp] == 0.) return true;
+  return boolean_has_union(h, row_off + (int32_t)b[vgn::row::BoolLeftRow], (int32_t)b[vgn::row::BoolLeftType]) ||
+         boolean_has_union(h, row_off + (int32_t)b[vgn::row::BoolRightRow], (int32_t)b[vgn::row::BoolRightType]);
 }
 
 int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, const double *px, const double *py,
@@ -691,6 +702,8 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   if (g->device == VGN_HOST_ONLY) return fail(VGN_ERR_ARG, "geometry was closed on the host only");
   if (lv < 0 || lv >= (int32_t)g->host.lv.size()) return fail(VGN_ERR_ARG, "bad logical volume");
   if (op < VGN_OP_DISTANCE_TO_IN || op > VGN_OP_INSIDE) return fail(VGN_ERR_ARG, "bad shape operation");
+  if (op == VGN_OP_INSIDE && boolean_has_union(g->host, g->host.lv[lv].shape_row, g->host.lv[lv].shape))
+    return fail(VGN_ERR_UNSUPPORTED, "Inside of a boolean union takes its operands' normals, which are not computed");
   if (n < 0) return fail(VGN_ERR_ARG, "negative batch size");
   if (n == 0) return VGN_OK;
   const bool needdir = op <= VGN_OP_DISTANCE_TO_OUT;
@@ -704,7 +717,7 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   const int kind     = needdir ? classify({px, py, pz, dx, dy, dz, smax, out}) : classify({px, py, pz, out});
   if (kind < 0) return fail(VGN_ERR_ARG, "mix of host and device pointers");
   if (kind == 1) {
-    cudaError_t e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, px, py, pz, dx, dy, dz, smax,
+    cudaError_t e = VGN_KSET_FN(g->host.kset(), launch_shape_fp64)(op, type, row, n, px, py, pz, dx, dy, dz, smax,
                                                                      out, max_blocks(g), s);
     return e == cudaSuccess ? VGN_OK : cuda_fail(e, "shape kernel launch");
   }
@@ -722,7 +735,7 @@ int vgn_shape_batch(const vgn_geometry *gc, int32_t lv, int32_t op, int64_t n, c
   for (int k = 0; k < ncopy && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess && smax) e = cudaMemcpyAsync(b[6], smax, nd, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  e = VGN_KSET_FN(g->host.sections, launch_shape_fp64)(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5],
+  e = VGN_KSET_FN(g->host.kset(), launch_shape_fp64)(op, type, row, n, b[0], b[1], b[2], b[3], b[4], b[5],
                                                        smax ? b[6] : nullptr, dout, max_blocks(g), s);
   if (e != cudaSuccess) return cuda_fail(e, "shape kernel launch");
   e = cudaMemcpyAsync(out, dout, nd, cudaMemcpyDeviceToHost, s);
@@ -905,7 +918,7 @@ int vgn_walk_batch(const vgn_geometry *g, int64_t n, double *px, double *py, dou
   // the mixed form's block-grouped launch variants walk chunks of tracks per block with
   // block-grouped steps (walk_kernel_grouped)
   const int variant = g->step_variant[mixed ? 1 : 0];
-  cudaError_t e = VGN_KSET_FN(g->host.sections, launch_walk)(g->view, n, px, py, pz, dx, dy, dz, step_limit, state,
+  cudaError_t e = VGN_KSET_FN(g->host.kset(), launch_walk)(g->view, n, px, py, pz, dx, dy, dz, step_limit, state,
                                                              max_steps, nsteps, perm, mixed, variant, max_blocks(g), s);
   if (sort) cudaFreeAsync(sort, s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "walk kernel launch");
@@ -922,7 +935,7 @@ struct vgn_batch {
   std::vector<uint32_t *> d_sort;  // per-job binning scratch: keys | histogram | permutation
   std::vector<size_t> sort_words;
   bool mixed    = false;
-  bool sections = false;  // some job's geometry needs the `sections` kernel set
+  int kset = 0;  // the kernel set every job's geometry can run on (0 full_ranges, 1 sections, 2 booleans)
   int safety_kbits = 0;   // the safety pass's own position-only order (0 = the step's)
   int reloc     = 1;
   int variant   = 0;
@@ -988,7 +1001,7 @@ int batch_enqueue(vgn_batch *b, cudaStream_t s)
       if (e != cudaSuccess) return cuda_fail(e, "batch track binning launch");
     }
   }
-  cudaError_t e = VGN_KSET_FN(b->sections, launch_multi_step)(b->jt, b->d_queue, b->mixed, b->reloc, b->num_sms, b->variant, s);
+  cudaError_t e = VGN_KSET_FN(b->kset, launch_multi_step)(b->jt, b->d_queue, b->mixed, b->reloc, b->num_sms, b->variant, s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "batch step launch");
 }
 
@@ -1069,8 +1082,8 @@ int vgn_batch_set_jobs(vgn_batch *b, int n_jobs, const vgn_step_job *jobs, int f
     c += (uint32_t)(((uint64_t)j.n + 31) / 32);
   }
   b->jt.chunk_begin[n_jobs] = c;
-  b->sections               = false;
-  for (int k = 0; k < n_jobs; ++k) b->sections = b->sections || jobs[k].geom->host.sections;
+  b->kset                   = 0;
+  for (int k = 0; k < n_jobs; ++k) b->kset = std::max(b->kset, jobs[k].geom->host.kset());
   b->mixed                  = (flags & VGN_PRECISION_MIXED) != 0;
   b->reloc                  = (flags & VGN_NO_RELOCATE) ? 0 : 1;
   b->variant                = variant;
@@ -1211,7 +1224,7 @@ int vgn_compute_step_batch_static(const vgn_geometry *g, int64_t n, const double
   a.reloc      = (flags & VGN_NO_RELOCATE) ? 0 : 1;
   a.max_blocks = max_blocks(g);
   a.perm       = perm;
-  e = VGN_KSET_FN(g->host.sections, launch_step)(g->view, a, mixed, g->step_variant[mixed ? 1 : 0], s);
+  e = VGN_KSET_FN(g->host.kset(), launch_step)(g->view, a, mixed, g->step_variant[mixed ? 1 : 0], s);
   return e == cudaSuccess ? VGN_OK : cuda_fail(e, "step kernel launch");
 }
 

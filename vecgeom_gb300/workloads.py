@@ -22,8 +22,10 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE = range(9)
-SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb", "cuttube"]
+BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE, BOOLEAN = range(10)
+SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb", "cuttube", "boolean"]
+UNION, INTERSECTION, SUBTRACTION = 0, 1, 2  # boolean operations (BooleanStruct.h:9)
+BOOLEAN_OPERAND = -2  # pv_mother of a boolean's operand placement
 
 K_PI = 3.14159265358979323846
 K_TWO_PI = 2.0 * K_PI
@@ -96,12 +98,22 @@ class GeometryBuilder:
         self._pv_mother: list[int] = []
         self._pv_tr: list[list[float]] = []
         self._world = -1
+        self._booleans: list[tuple] = []  # (lv, left lv, left transform, right lv, right transform)
 
     def logical(self, shape: int, params) -> int:
         self._shapes.append(int(shape))
         self._offsets.append(len(self._params))
         self._params.extend(float(p) for p in params)
         return len(self._shapes) - 1
+
+    def boolean(self, op: int, left: int, right: int, left_transform=None, right_transform=None) -> int:
+        """A boolean solid (UNION, INTERSECTION or SUBTRACTION) of logical volumes `left` and
+        `right` placed in its frame with the given transforms (identity by default); returns its
+        logical volume.  The operand placements are laid out by build()."""
+        lv = self.logical(BOOLEAN, [op, -1, -1])
+        self._booleans.append((lv, int(left), list(left_transform if left_transform is not None else IDENTITY),
+                               int(right), list(right_transform if right_transform is not None else IDENTITY)))
+        return lv
 
     def place(self, lv: int, mother: int, transform=None) -> int:
         self._pv_lv.append(int(lv))
@@ -114,16 +126,33 @@ class GeometryBuilder:
         return self._world
 
     def build(self) -> GeometryDescription:
+        """The description; boolean operand placements come first, in the order of their
+        booleans' logical volumes, left before right.  The library takes operands anywhere in the
+        list; this order is the one in which VecGeom creates them when each boolean is built, so
+        the placement ids equal VecGeom's."""
         if self._world < 0:
             raise ValueError("no world placement")
+        params = list(self._params)
+        pv_lv, pv_mother, pv_tr = [], [], []
+        for lv, left, ltr, right, rtr in sorted(self._booleans):
+            off = self._offsets[lv]
+            for k, (olv, otr) in enumerate(((left, ltr), (right, rtr))):
+                params[off + 1 + k] = float(len(pv_lv))
+                pv_lv.append(olv)
+                pv_mother.append(BOOLEAN_OPERAND)
+                pv_tr.append(otr)
+        shift = len(pv_lv)
+        pv_lv += self._pv_lv
+        pv_mother += self._pv_mother
+        pv_tr += self._pv_tr
         return GeometryDescription(
             lv_shape=np.asarray(self._shapes, dtype=np.int32),
             lv_param_offset=np.asarray(self._offsets, dtype=np.int32),
-            params=np.asarray(self._params, dtype=np.float64),
-            pv_logical=np.asarray(self._pv_lv, dtype=np.int32),
-            pv_mother=np.asarray(self._pv_mother, dtype=np.int32),
-            pv_transform=np.asarray(self._pv_tr, dtype=np.float64).reshape(-1, 12),
-            world_placed=self._world,
+            params=np.asarray(params, dtype=np.float64),
+            pv_logical=np.asarray(pv_lv, dtype=np.int32),
+            pv_mother=np.asarray(pv_mother, dtype=np.int32),
+            pv_transform=np.asarray(pv_tr, dtype=np.float64).reshape(-1, 12),
+            world_placed=self._world + shift,
         )
 
 
@@ -260,6 +289,50 @@ def box_grid_tracks(grid: BoxGrid, n: int = 1 << 22, seed_points: int = 4, seed_
     dx, dy, dz = isotropic(np.random.Generator(np.random.PCG64(seed_dirs)), n)
     return TrackBatch(p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), dx, dy, dz,
                       np.full(n, step_limit), world_states(n))
+
+
+# ---------------------------------------------------------------- boolean solids
+def boolean_solid(b: "GeometryBuilder", kind: int, scale: float = 1.0) -> int:
+    """One boolean solid of four kinds built in `b` (its logical volume is returned):
+      0  box minus a tube through it (subtraction, the tube turned 90 degrees about x);
+      1  a tube united with a box across it (union);
+      2  a box intersected with an orb that cuts its corners (intersection);
+      3  a box with two tube holes, the holes a union of two tubes subtracted from the box (the
+         nested combination of the reference's TestBooleans.cpp:22-45)."""
+    L = 40.0 * scale
+    if kind == 0:
+        box = b.logical(BOX, (L, 0.75 * L, 0.5 * L))
+        tube = b.logical(TUBE, (0.0, 0.25 * L, 0.8 * L, 0.0, K_TWO_PI))
+        return b.boolean(SUBTRACTION, box, tube, None, transform_euler(0.1 * L, 0.0, 0.0, 0.0, 90.0, 0.0))
+    if kind == 1:
+        tube = b.logical(TUBE, (0.0, 0.3 * L, 0.5 * L, 0.0, K_TWO_PI))
+        box = b.logical(BOX, (0.6 * L, 0.2 * L, 0.2 * L))
+        return b.boolean(UNION, tube, box, None, transform_euler(0.3 * L, 0.0, 0.1 * L, 30.0, 0.0, 0.0))
+    if kind == 2:
+        box = b.logical(BOX, (0.75 * L, 0.75 * L, 0.75 * L))
+        orb = b.logical(ORB, (0.95 * L,))
+        return b.boolean(INTERSECTION, box, orb, None, transform_euler(0.05 * L, -0.05 * L, 0.0))
+    box = b.logical(BOX, (L, L, L))
+    tube = b.logical(TUBE, (0.0, 0.9 * L / 4.0, L, 0.0, K_TWO_PI))
+    holes = b.boolean(UNION, tube, tube, transform_euler(-L / 4, -L / 4, 0.0), transform_euler(L / 4, L / 4, 0.0))
+    return b.boolean(SUBTRACTION, box, holes, None, transform_euler(-L / 2, -L / 2, 0.0))
+
+
+def boolean_geometry(seed: int = 41, grid=(4, 4, 4), world: float = 500.0, pitch: float = 250.0) -> GeometryDescription:
+    """A world box (half `world` mm) holding boolean solids of the four kinds of
+    boolean_solid, cycling through them, on a jittered grid of `pitch` mm, scales U[0.8, 1.5],
+    full random rotations."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = GeometryBuilder()
+    wlv = b.logical(BOX, (world, world, world))
+    nx, ny, nz = grid
+    cells = [(i, j, k) for i in range(nx) for j in range(ny) for k in range(nz)]
+    lvs = [boolean_solid(b, n % 4, rng.uniform(0.8, 1.5)) for n in range(len(cells))]
+    for lv, (i, j, k) in zip(lvs, cells):
+        c = (np.array([i - (nx - 1) / 2, j - (ny - 1) / 2, k - (nz - 1) / 2]) * pitch + rng.uniform(-10, 10, 3))
+        b.place(lv, wlv, transform_euler(c[0], c[1], c[2], rng.uniform(0, 360), rng.uniform(0, 180), rng.uniform(0, 360)))
+    b.place_world(wlv)
+    return b.build()
 
 
 # ---------------------------------------------------------------- nested (multi-level)
