@@ -46,9 +46,14 @@ enum vgn_shape_type {
   VGN_ORB       = 7, /* params: r                                 (UnplacedOrb.h)       */
   VGN_CUTTUBE   = 8, /* params: rmin, rmax, dz, sphi, dphi, bottom normal bx, by, bz, top normal
                         tx, ty, tz                                (UnplacedCutTube.h:54-57) */
-  VGN_BOOLEAN   = 9  /* params: op (VGN_BOOL_UNION / _INTERSECTION / _SUBTRACTION), left operand,
+  VGN_BOOLEAN   = 9, /* params: op (VGN_BOOL_UNION / _INTERSECTION / _SUBTRACTION), left operand,
                         right operand: ids of placed volumes whose mother is VGN_BOOLEAN_OPERAND
                         (UnplacedBooleanVolume.h:59, BooleanStruct.h:23-25)        */
+  VGN_POLYHEDRON = 10 /* params: sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz]; radii are to
+                        the sides' middles (UnplacedPolyhedron.h:97-108).  Refused where the
+                        reference reads past its arrays: a zero-length first or last segment,
+                        three equal z planes in a row, a zero-length segment with equal radii,
+                        a face with fewer than three distinct corners, dphi / sides >= pi */
 };
 
 /* Boolean solids (VGN_BOOLEAN).  The operands are placements of other logical volumes

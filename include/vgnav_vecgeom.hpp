@@ -64,6 +64,7 @@
 #include "VecGeom/volumes/UnplacedCutTube.h"
 #include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
+#include "VecGeom/volumes/UnplacedPolyhedron.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
 #include "VecGeom/volumes/UnplacedTrapezoid.h"
 #include "VecGeom/volumes/UnplacedTrd.h"
@@ -158,6 +159,14 @@ inline int shape_row(vecgeom::VUnplacedVolume const *u, std::vector<double> &p)
                                                                                   : VGN_BOOL_SUBTRACTION;
     p = {(double)op, (double)bs->fLeftVolume->id(), (double)bs->fRightVolume->id()};
     return VGN_BOOLEAN;
+  }
+  if (auto h = dynamic_cast<UnplacedPolyhedron const *>(u)) {  // the planes the struct keeps
+    const int nz = (int)h->GetZPlanes().size();
+    p            = {h->GetPhiStart(), h->GetPhiDelta(), (double)h->GetSideCount(), (double)nz};
+    for (int i = 0; i < nz; ++i) p.push_back(h->GetZPlanes()[i]);
+    for (int i = 0; i < nz; ++i) p.push_back(h->GetRMin()[i]);
+    for (int i = 0; i < nz; ++i) p.push_back(h->GetRMax()[i]);
+    return VGN_POLYHEDRON;
   }
   if (auto c = dynamic_cast<UnplacedPolycone const *>(u)) {
     auto const *h = c->GetOriginalParameters();  // the constructor's planes (PolyconeStruct.h:279-285)

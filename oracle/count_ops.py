@@ -34,7 +34,8 @@ WEIGHTS = {
     "prim_contains": 6,   # AABB::Contains (AABB.h:205-210)
     "transforms": 33,     # Transformation3D point + direction (Transformation3D.h:663-673, 729-770)
 }
-# per shape (Box, Tube, Cone, Trd, Trapezoid, Sphere, Polycone) and operation
+# per shape (Box, Tube, Cone, Trd, Trapezoid, Sphere, Polycone, Orb, CutTube, Boolean, Polyhedron)
+# and operation
 # (DistanceToIn, DistanceToOut, SafetyToIn, SafetyToOut, Contains, Inside)
 KERNEL_WEIGHTS = [
     [30, 24, 9, 9, 6, 8],         # BoxImplementation.h:73-167
@@ -48,6 +49,8 @@ KERNEL_WEIGHTS = [
     [110, 60, 25, 25, 20, 24],    # CutTubeImplementation.h:158-290 (tube + two cut planes)
     [12, 12, 6, 6, 4, 4],         # Boolean*Implementation.h: the combination and the operands' transforms
                                   # (the operands' own kernels are counted under their shapes)
+    [400, 300, 200, 200, 60, 70], # PolyhedronImplementation.h:598-800 (bounding tube, z segments of eight
+                                  # quadrilateral faces, end caps)
 ]
 
 

@@ -278,6 +278,13 @@ static int shape_nparams(int type, const double *p, int avail)
     if ((double)nz != p[2]) return -1;
     return 3 + 3 * nz;
   }
+  case OR_POLYHEDRON: { /* sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz] */
+    int nz;
+    if (avail < 4 || !(p[3] >= 2 && p[3] <= 4096) || !(p[2] >= 1 && p[2] <= 4096)) return -1;
+    nz = (int)p[3];
+    if ((double)nz != p[3] || (double)(int)p[2] != p[2]) return -1;
+    return 4 + 3 * nz;
+  }
   default: (void)p; (void)avail; return -1;
   }
 }
@@ -468,6 +475,7 @@ void or_geom_free(or_geom *g)
       free(g->lv[i].nchild);
       free(g->lv[i].nodes);
       free(g->lv[i].aabbs);
+      if (g->lv[i].type == OR_POLYHEDRON) polyhedron_free(&g->lv[i].s.phd);
       if (g->lv[i].type == OR_POLYCONE) {
         free(g->lv[i].s.pcon.zs);
         free(g->lv[i].s.pcon.shift);

@@ -159,6 +159,29 @@ typedef struct { /* CutTubeStruct.h:21-46 */
   double cosphi1, sinphi1, cosphi2, sinphi2, maxval;
 } or_cuttube;
 
+typedef struct { /* one face of Quadrilaterals (Quadrilaterals.h:25-36) */
+  double n[3], d;         /* fPlanes: unit normal and distance */
+  double sn[4][3], sd[4]; /* fSideVectors[j]: the side planes */
+  double c[4][3];         /* fCorners[j] */
+} or_quad;
+
+typedef struct { int n; or_quad *q; } or_quads;
+
+typedef struct { or_quads outer, phi, inner; } or_zseg; /* ZSegment (PolyhedronStruct.h:36-46) */
+
+typedef struct { /* PolyhedronStruct.h:52-80 */
+  int sides, nz;                       /* fSideCount, fZPlanes.size() */
+  int hasInner, hasPhi, hasLargePhi;   /* fHasInnerRadii, fHasPhiCutout, fHasLargePhiCutout */
+  double phiStart, phiDelta;           /* fPhiStart (normalised), fPhiDelta (at most 2 pi) */
+  or_wedge w;                          /* fPhiWedge(fPhiDelta, fPhiStart) */
+  or_zseg *seg;                        /* [nz - 1] fZSegments */
+  double *z, *rmin, *rmax;             /* [nz] fZPlanes, fRMin, fRMax */
+  int *samez;                          /* [nz] fSameZ */
+  v3 *phisec;                          /* [sides + 1] fPhiSections */
+  or_tube btube;                       /* fBoundingTube */
+  double btubeOffset;                  /* fBoundingTubeOffset */
+} or_polyhedron;
+
 struct or_lv_s;
 typedef struct { /* BooleanStruct (BooleanStruct.h:23-25): the operation and the two placed operands */
   int op;                             /* 0 union, 1 intersection, 2 subtraction (BooleanStruct.h:9) */
@@ -184,6 +207,7 @@ typedef struct or_lv_s {
     or_orb orb;
     or_cuttube ctube;
     or_boolean boo;
+    or_polyhedron phd;
   } s;
   v3 bbox_min, bbox_max; /* VUnplacedVolume::fBBox: the shape's Extent (UnplacedVolume.h:45, 76-80) */
   /* BVH (BVH.h:364-370), present when nd > 0 */
@@ -217,6 +241,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
 double shape_safe_in(const or_lv *lv, v3 p, or_counters *c);
 double shape_safe_out(const or_lv *lv, v3 p, or_counters *c);
 int shape_contains(const or_lv *lv, v3 p, or_counters *c);
+void polyhedron_free(or_polyhedron *t);
 int shape_inside(const or_lv *lv, v3 p, or_counters *c); /* EInside: kInside=1, kSurface=2, kOutside=3 */
 
 /* BVH build (or_bvh.c) */

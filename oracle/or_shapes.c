@@ -2904,6 +2904,802 @@ static void cuttube_extent(const or_cuttube *c, v3 *mn, v3 *mx) /* source/Unplac
 
 /* ================================================================== */
 
+/* ================================================================== */
+/* Polyhedron: PolyhedronStruct.h, Quadrilaterals.h/.cpp, Planes.h/.cpp,
+ * kernel/PolyhedronImplementation.h.  The specialisation the reference builds for a
+ * placement (UnplacedPolyhedron.cpp:75-103: inner radii and phi cut-out kinds chosen from
+ * the shape) behaves as the generic one with the shape's own flags, which is what is
+ * restated here.                                                     */
+/* ================================================================== */
+
+/* NormalizeAngle<kScalar> (GenericKernels.h:140-146) */
+static double phd_normalize_angle(double a) { return a + kTwoPi * (double)((a < 0) - (int)(a / kTwoPi)); }
+
+/* Vector3D::FixZeroes (Vector3D.h:298-305) */
+static v3 v3_fix_zeroes(v3 a)
+{
+  if (fabs(a.x) < kTolerance) a.x = 0.0;
+  if (fabs(a.y) < kTolerance) a.y = 0.0;
+  if (fabs(a.z) < kTolerance) a.z = 0.0;
+  return a;
+}
+
+/* Vector3D::Normalized (Vector3D.h:202): v * (1 / Length()) */
+static v3 v3_normalized(v3 a)
+{
+  const double inv = 1. / sqrt(v3_mag2(a));
+  return v3_make(a.x * inv, a.y * inv, a.z * inv);
+}
+
+/* operator== of Vector3D<Precision> (Vector3D.h:387-390): componentwise within kTolerance */
+static int v3_tol_eq(v3 a, v3 b)
+{
+  return fabs(a.x - b.x) < kTolerance && fabs(a.y - b.y) < kTolerance && fabs(a.z - b.z) < kTolerance;
+}
+
+static inline v3 quad_corner(const or_quad *q, int j) { return v3_make(q->c[j][0], q->c[j][1], q->c[j][2]); }
+static inline v3 quad_normal(const or_quad *q) { return v3_make(q->n[0], q->n[1], q->n[2]); }
+static inline v3 quad_side(const or_quad *q, int j) { return v3_make(q->sn[j][0], q->sn[j][1], q->sn[j][2]); }
+
+/* Planes::Set(index, normal, origin) (source/Planes.cpp:30-37) of one side plane */
+static void quad_set_side(or_quad *q, int j, v3 normal, v3 origin)
+{
+  const v3 fixed   = v3_fix_zeroes(normal);
+  const double inv = 1. / sqrt(v3_mag2(fixed));
+  q->sn[j][0] = inv * fixed.x;
+  q->sn[j][1] = inv * fixed.y;
+  q->sn[j][2] = inv * fixed.z;
+  q->sd[j]    = inv * -v3_dot(fixed, origin);
+}
+
+/* Quadrilaterals::Set (source/Quadrilaterals.cpp:33-104); -1 when fewer than three corners are
+ * distinct (the reference then reads an unset corner) */
+static int quad_set(or_quad *q, v3 c0, v3 c1, v3 c2, v3 c3)
+{
+  const v3 in[4] = {c0, c1, c2, c3};
+  v3 ch[4];
+  int assigned = 1, tested = 1, j;
+  double a, b, c, d, inv;
+  v3 normal;
+  for (j = 0; j < 4; ++j) {
+    q->c[j][0] = in[j].x;
+    q->c[j][1] = in[j].y;
+    q->c[j][2] = in[j].z;
+  }
+  ch[0] = in[0];
+  while (tested < 4) {
+    int chosen = 1;
+    for (j = 0; j < assigned; ++j)
+      if (v3_tol_eq(ch[j], in[tested])) {
+        chosen = 0;
+        break;
+      }
+    if (chosen) ch[assigned++] = in[tested];
+    ++tested;
+  }
+  if (assigned < 3) return -1;
+  a = ch[0].y * (ch[1].z - ch[2].z) + ch[1].y * (ch[2].z - ch[0].z) + ch[2].y * (ch[0].z - ch[1].z);
+  b = ch[0].z * (ch[1].x - ch[2].x) + ch[1].z * (ch[2].x - ch[0].x) + ch[2].z * (ch[0].x - ch[1].x);
+  c = ch[0].x * (ch[1].y - ch[2].y) + ch[1].x * (ch[2].y - ch[0].y) + ch[2].x * (ch[0].y - ch[1].y);
+  d = -ch[0].x * (ch[1].y * ch[2].z - ch[2].y * ch[1].z) - ch[1].x * (ch[2].y * ch[0].z - ch[0].y * ch[2].z) -
+      ch[2].x * (ch[0].y * ch[1].z - ch[1].y * ch[0].z);
+  normal = v3_make(a, b, c);
+  inv    = 1. / sqrt(v3_mag2(normal));
+  normal = v3_make(normal.x * inv, normal.y * inv, normal.z * inv);
+  d *= inv;
+  normal  = v3_fix_zeroes(normal);
+  q->n[0] = normal.x;
+  q->n[1] = normal.y;
+  q->n[2] = normal.z;
+  q->d    = d;
+  for (j = 0; j < 4; ++j) {
+    const v3 s0 = in[j], s1 = in[(j + 1) % 4];
+    if (!v3_tol_eq(s1, s0)) {
+      quad_set_side(q, j, v3_normalized(v3_cross(normal, v3_sub(s1, s0))), s0);
+    } else {
+      q->sn[j][0] = q->sn[j][1] = q->sn[j][2] = 0.;
+      q->sd[j]                                = 0.;
+    }
+  }
+  return 0;
+}
+
+/* Quadrilaterals::FlipSign -> Planes::FlipSign (source/Planes.cpp:45-49) */
+static void quad_flip(or_quad *q)
+{
+  q->n[0] = -q->n[0];
+  q->n[1] = -q->n[1];
+  q->n[2] = -q->n[2];
+  q->d    = -q->d;
+}
+
+/* Quadrilaterals::RayHitsQuadrilateral (Quadrilaterals.h:139-150) */
+static int quad_ray_hits(const or_quad *q, v3 x)
+{
+  int j;
+  for (j = 0; j < 4; ++j)
+    if (!(v3_dot(x, quad_side(q, j)) + q->sd[j] >= -kTolerance)) return 0;
+  return 1;
+}
+
+/* Quadrilaterals::DistanceToIn<double, behindPlanesT> (Quadrilaterals.h:361-396) */
+static double quads_dist_in(const or_quads *qs, int behind, v3 p, v3 d)
+{
+  double best = kInfLength;
+  int i;
+  for (i = 0; i < qs->n; ++i) {
+    const or_quad *q = &qs->q[i];
+    const v3 n       = quad_normal(q);
+    double dist      = v3_dot(p, n) + q->d;
+    double proj;
+    v3 x;
+    if (!((behind ? -dist : dist) > -kTolerance)) continue;
+    proj = v3_dot(d, n);
+    if (!((behind ? proj : -proj) > 0)) continue;
+    dist /= -(proj + copysign(1E-20, proj));
+    x = v3_add(p, v3_scale(dist, d));
+    if (quad_ray_hits(q, x)) best = dist;
+    if (best < kInfLength) break;
+  }
+  return 0. > best ? 0. : best;
+}
+
+/* Quadrilaterals::DistanceToOut(point, direction, zMin, zMax) (Quadrilaterals.h:466-516) */
+static double quads_dist_out(const or_quads *qs, v3 p, v3 d, double zMin, double zMax)
+{
+  double best = kInfLength;
+  int i;
+  for (i = 0; i < qs->n; ++i) {
+    const or_quad *q = &qs->q[i];
+    const v3 n       = quad_normal(q);
+    double dt        = v3_dot(p, n) + q->d, proj;
+    int valid;
+    if (!(dt < kTolerance)) continue;
+    proj = v3_dot(d, n);
+    if (!(proj > 0)) continue;
+    dt /= -proj;
+    if (!(dt < best)) continue;
+    if (zMin == zMax) {
+      valid = quad_ray_hits(q, v3_add(p, v3_scale(dt, d)));
+    } else {
+      const double zp = p.z + dt * d.z;
+      valid           = (zp >= zMin - kTolerance) && (zp < zMax + kTolerance);
+    }
+    if (!valid) continue;
+    best = dt;
+  }
+  if (best > -kTolerance) best = best > 0. ? best : 0.;
+  return best;
+}
+
+/* DistanceToLineSegmentSquared1 (GenericKernels.h:188-215) */
+static double phd_segment_dist2(v3 c0, v3 c1, v3 p)
+{
+  double result = kInfLength, dot0, dot1;
+  const v3 line = v3_sub(c1, c0);
+  dot0          = v3_dot(v3_sub(p, c0), line);
+  if (dot0 <= 0) return v3_mag2(v3_sub(p, c0));
+  dot1 = v3_mag2(line);
+  if (dot1 <= dot0) result = v3_mag2(v3_sub(p, c1));
+  if (result < kInfLength) return result;
+  return v3_mag2(v3_sub(v3_add(c0, v3_scale(dot0 / dot1, line)), p));
+}
+
+/* Quadrilaterals::ScalarDistanceSquared (Quadrilaterals.h:535-572) */
+static double quad_dist2(const or_quad *q, v3 p)
+{
+  const v3 n      = quad_normal(q);
+  double distance = v3_dot(p, n) + q->d, dsq = kInfLength;
+  const v3 x      = v3_sub(p, v3_scale(distance, n));
+  int within[4], j;
+  for (j = 0; j < 4; ++j)
+    within[j] = x.x * q->sn[j][0] + x.y * q->sn[j][1] + x.z * q->sn[j][2] + q->sd[j] >= 0;
+  if (within[0] && within[1] && within[2] && within[3]) return distance * distance;
+  for (j = 0; j < 4; ++j) {
+    if (!within[j]) {
+      distance = phd_segment_dist2(quad_corner(q, j), quad_corner(q, (j + 1) % 4), p);
+      if (distance < dsq) dsq = distance;
+    }
+  }
+  return dsq;
+}
+
+/* Planes::Contains (Planes.h:192-205) */
+static int quads_contains(const or_quads *qs, v3 p)
+{
+  int i, r = 1;
+  for (i = 0; i < qs->n; ++i) r &= v3_dot(p, quad_normal(&qs->q[i])) + qs->q[i].d < 0;
+  return r;
+}
+
+/* Planes::Inside of one plane (Planes.h:268-281) */
+static int quad_inside(const or_quad *q, v3 p)
+{
+  const double dist = q->n[0] * p.x + q->n[1] * p.y + q->n[2] * p.z + q->d;
+  if (dist > kHalfTolerance) return kOutsideE;
+  if (dist > -kHalfTolerance) return kSurfaceE;
+  return kInsideE;
+}
+
+/* Planes::Inside over all planes (Planes.h:246-266) */
+static int quads_inside(const or_quads *qs, v3 p)
+{
+  int i, r = kInsideE;
+  for (i = 0; i < qs->n; ++i) {
+    const double dist = qs->q[i].n[0] * p.x + qs->q[i].n[1] * p.y + qs->q[i].n[2] * p.z + qs->q[i].d;
+    if (dist > kHalfTolerance) r = kOutsideE;
+    if (r == kInsideE && dist > -kHalfTolerance) r = kSurfaceE;
+    if (r == kOutsideE) break;
+  }
+  return r;
+}
+
+static int phd_alloc_quads(or_quads *qs, int n)
+{
+  qs->n = n;
+  qs->q = n > 0 ? (or_quad *)calloc((size_t)n, sizeof(or_quad)) : NULL;
+  return n > 0 && !qs->q ? -1 : 0;
+}
+
+void polyhedron_free(or_polyhedron *t)
+{
+  int i;
+  if (t->seg)
+    for (i = 0; i < t->nz - 1; ++i) {
+      free(t->seg[i].outer.q);
+      free(t->seg[i].phi.q);
+      free(t->seg[i].inner.q);
+    }
+  free(t->seg);
+  free(t->z);
+  free(t->rmin);
+  free(t->rmax);
+  free(t->samez);
+  free(t->phisec);
+  t->seg = NULL;
+  t->z = t->rmin = t->rmax = NULL;
+  t->samez  = NULL;
+  t->phisec = NULL;
+}
+
+/* PolyhedronStruct(phiStart, phiDelta, sideCount, zPlaneCount, zPlanes, rMin, rMax) and
+ * Initialize (PolyhedronStruct.h:96-110, 264-420); params: sphi, dphi, sides, nz, z[nz],
+ * rmin[nz], rmax[nz].  Refused where the reference would read past its arrays: zero-length
+ * first or last segment, three equal z planes in a row, a zero-length segment whose faces
+ * are all empty, a face with fewer than three distinct corners. */
+static int polyhedron_init(or_polyhedron *t, const double *a, char *err, int errlen)
+{
+  const double phiStart0 = a[0], phiDelta0 = a[1];
+  const int S = (int)a[2], nz = (int)a[3];
+  const double *zp = a + 4, *rmn = a + 4 + nz, *rmx = a + 4 + 2 * nz;
+  double phiStart, phiDelta, sidePhi, cosHalf, inner = kInfLength, outer = -kInfLength, tp[5];
+  int i, iPlane, iSide;
+  memset(t, 0, sizeof(*t));
+  if (!(phiDelta0 > 0) || S < 1 || nz < 2 || !((phiDelta0 > kTwoPi ? kTwoPi : phiDelta0) / S < kPi)) {
+    set_err(err, errlen, "polyhedron: needs dphi > 0, nz >= 2 and sides with dphi / sides < pi");
+    return -1;
+  }
+  for (i = 0; i < nz; ++i) {
+    if (!(rmn[i] >= 0 && rmx[i] >= rmn[i]) || (i > 0 && !(zp[i] >= zp[i - 1]))) {
+      set_err(err, errlen, "polyhedron: needs 0 <= rmin <= rmax and non-decreasing z planes");
+      return -1;
+    }
+    if (i + 2 < nz && zp[i] == zp[i + 1] && zp[i + 1] == zp[i + 2]) {
+      set_err(err, errlen, "polyhedron: three equal z planes in a row");
+      return -1;
+    }
+  }
+  if (zp[0] == zp[1] || zp[nz - 2] == zp[nz - 1]) {
+    set_err(err, errlen, "polyhedron: zero-length first or last segment");
+    return -1;
+  }
+  t->sides       = S;
+  t->nz          = nz;
+  t->hasPhi      = phiDelta0 < kTwoPi;
+  t->hasLargePhi = phiDelta0 < kPi;
+  t->phiStart    = phd_normalize_angle(phiStart0);
+  t->phiDelta    = phiDelta0 > kTwoPi ? kTwoPi : phiDelta0;
+  wedge_init(&t->w, t->phiDelta, t->phiStart);
+  t->seg    = (or_zseg *)calloc((size_t)(nz - 1), sizeof(or_zseg));
+  t->z      = (double *)malloc(sizeof(double) * (size_t)nz);
+  t->rmin   = (double *)malloc(sizeof(double) * (size_t)nz);
+  t->rmax   = (double *)malloc(sizeof(double) * (size_t)nz);
+  t->samez  = (int *)calloc((size_t)nz, sizeof(int));
+  t->phisec = (v3 *)malloc(sizeof(v3) * (size_t)(S + 1));
+  if (!t->seg || !t->z || !t->rmin || !t->rmax || !t->samez || !t->phisec) goto nomem;
+  for (i = 0; i < nz; ++i) {
+    t->z[i]    = zp[i];
+    t->rmin[i] = rmn[i];
+    t->rmax[i] = rmx[i];
+    if (i > 0 && i < nz - 1 && zp[i] == zp[i + 1]) t->samez[i] = 1;
+  }
+  for (i = 0; i < nz - 1; ++i) {
+    const int hasInnerRadius = rmn[i] > 0 || rmn[i + 1] > 0;
+    int mult                 = (zp[i] == zp[i + 1] && rmx[i] == rmx[i + 1]) ? 0 : 1;
+    if (phd_alloc_quads(&t->seg[i].outer, S * mult)) goto nomem;
+    if (t->hasPhi && phd_alloc_quads(&t->seg[i].phi, zp[i] == zp[i + 1] ? 0 : 2)) goto nomem;
+    mult = (zp[i] == zp[i + 1] && rmn[i] == rmn[i + 1]) ? 0 : 1;
+    if (hasInnerRadius && mult > 0) {
+      if (phd_alloc_quads(&t->seg[i].inner, S)) goto nomem;
+      t->hasInner = 1;
+    }
+    if (zp[i] == zp[i + 1] && t->seg[i].outer.n == 0 && t->seg[i].inner.n == 0) {
+      set_err(err, errlen, "polyhedron: a zero-length segment needs different radii on its two planes");
+      polyhedron_free(t);
+      return -1;
+    }
+  }
+  phiStart = phd_normalize_angle(phiStart0);
+  phiDelta = phiDelta0 > kTwoPi ? kTwoPi : phiDelta0;
+  sidePhi  = phiDelta / S;
+#define PHD_PHI(side) phd_normalize_angle(phiStart + ((!t->hasPhi && (side) == S) ? 0 : (side)) * sidePhi)
+  for (i = 0; i <= S; ++i) {
+    const double phi = PHD_PHI(i);
+    const v3 corner  = v3_fix_zeroes(v3_normalized(v3_make(1. * cos(phi), 1. * sin(phi), 0)));
+    t->phisec[i]     = v3_cross(v3_normalized(corner), v3_make(0, 0, -1));
+  }
+  cosHalf = cos(0.5 * sidePhi);
+  for (i = 0; i < nz; ++i) {
+    if (rmn[i] < inner) inner = rmn[i];
+    if (rmx[i] > outer) outer = rmx[i];
+  }
+  outer /= cosHalf;
+  tp[0] = inner - kHalfTolerance;
+  tp[1] = outer + kHalfTolerance;
+  tp[2] = 0.5 * (zp[nz - 1] - zp[0]) + kTolerance;
+  tp[3] = !t->hasPhi ? 0 : phiStart - 100 * kTolerance;
+  tp[4] = !t->hasPhi ? kTwoPi : phiDelta + 2 * (100 * kTolerance);
+  if (tube_init(&t->btube, tp, err, errlen)) {
+    polyhedron_free(t);
+    return -1;
+  }
+  t->btubeOffset = 0.5 * (zp[0] + zp[nz - 1]);
+#define PHD_VTX(r, i, j) \
+  v3_fix_zeroes(v3_make((r)[i] / cosHalf * cos(PHD_PHI(j)), (r)[i] / cosHalf * sin(PHD_PHI(j)), zp[i]))
+  for (iPlane = 0; iPlane < nz - 1; ++iPlane) {
+    or_zseg *sg = &t->seg[iPlane];
+    for (iSide = 0; iSide < sg->outer.n; ++iSide) {
+      const v3 c0 = PHD_VTX(rmx, iPlane, iSide);
+      or_quad *q  = &sg->outer.q[iSide];
+      if (quad_set(q, c0, PHD_VTX(rmx, iPlane, iSide + 1), PHD_VTX(rmx, iPlane + 1, iSide + 1),
+                   PHD_VTX(rmx, iPlane + 1, iSide)))
+        goto degenerate;
+      if (q->n[0] * c0.x + q->n[1] * c0.y < 0) quad_flip(q);
+    }
+    for (iSide = 0; iSide < sg->inner.n; ++iSide) {
+      const v3 c0 = PHD_VTX(rmn, iPlane, iSide);
+      or_quad *q  = &sg->inner.q[iSide];
+      if (quad_set(q, c0, PHD_VTX(rmn, iPlane, iSide + 1), PHD_VTX(rmn, iPlane + 1, iSide + 1),
+                   PHD_VTX(rmn, iPlane + 1, iSide)))
+        goto degenerate;
+      if (q->n[0] * c0.x + q->n[1] * c0.y < 0) quad_flip(q);
+    }
+    if (t->hasPhi && sg->phi.n == 2) {
+      if (quad_set(&sg->phi.q[0], PHD_VTX(rmn, iPlane, 0), PHD_VTX(rmn, iPlane + 1, 0), PHD_VTX(rmx, iPlane + 1, 0),
+                   PHD_VTX(rmx, iPlane, 0)))
+        goto degenerate;
+      if (v3_dot(quad_normal(&sg->phi.q[0]), t->phisec[0]) > 0) quad_flip(&sg->phi.q[0]);
+      if (quad_set(&sg->phi.q[1], PHD_VTX(rmx, iPlane, S), PHD_VTX(rmx, iPlane + 1, S), PHD_VTX(rmn, iPlane + 1, S),
+                   PHD_VTX(rmn, iPlane, S)))
+        goto degenerate;
+      if (v3_dot(quad_normal(&sg->phi.q[1]), t->phisec[S]) < 0) quad_flip(&sg->phi.q[1]);
+    }
+  }
+#undef PHD_VTX
+#undef PHD_PHI
+  return 0;
+degenerate:
+  set_err(err, errlen, "polyhedron: a face has fewer than three distinct corners");
+  polyhedron_free(t);
+  return -1;
+nomem:
+  set_err(err, errlen, "polyhedron: out of host memory");
+  polyhedron_free(t);
+  return -1;
+}
+
+/* FindZSegmentKernel<double> (PolyhedronImplementation.h:232-244) */
+static int phd_find_z(const or_polyhedron *t, double pz)
+{
+  int index = -1, b = 0;
+  while (b < t->nz - 1 && pz - kTolerance > t->z[b]) {
+    ++index;
+    ++b;
+  }
+  if (pz + kTolerance > t->z[b]) return index + 1;
+  return index;
+}
+
+/* FindPhiSegment (PolyhedronImplementation.h:256-276) */
+static int phd_find_phi(const or_polyhedron *t, v3 p)
+{
+  int index = -1, i;
+  double first = p.x * t->phisec[0].x + p.y * t->phisec[0].y + p.z * t->phisec[0].z, second;
+  for (i = 1; i < t->sides + 1; ++i) {
+    second = p.x * t->phisec[i].x + p.y * t->phisec[i].y + p.z * t->phisec[i].z;
+    if (first > -kTolerance && second < kTolerance) index = i - 1;
+    if (index >= 0) break;
+    first = second;
+  }
+  return index;
+}
+
+static inline int phd_clamp_z(const or_polyhedron *t, int z)
+{
+  const int zmax = t->nz - 1;
+  return z < 0 ? 0 : (z >= zmax ? zmax - 1 : z);
+}
+
+/* DistanceToInZSegment (PolyhedronImplementation.h:278-318) */
+static double phd_dist_in_seg(const or_polyhedron *t, int si, v3 p, v3 d)
+{
+  const or_zseg *sg = &t->seg[si];
+  double distance   = quads_dist_in(&sg->outer, 0, p, d);
+  if (distance < kInfLength) return distance;
+  if (t->hasPhi) distance = quads_dist_in(&sg->phi, 0, p, d);
+  if (distance < kInfLength) return distance;
+  if (sg->inner.n > 0) distance = quads_dist_in(&sg->inner, 1, p, d);
+  return distance;
+}
+
+/* DistanceToOutZSegment (PolyhedronImplementation.h:320-362) */
+static double phd_dist_out_seg(const or_polyhedron *t, int si, double zMin, double zMax, v3 p, v3 d)
+{
+  const or_zseg *sg = &t->seg[si];
+  int done          = 0;
+  double distance   = kInfLength;
+  if (sg->inner.n > 0) {
+    distance = quads_dist_in(&sg->inner, 0, p, d);
+    done     = distance < kInfLength;
+    if (done) return distance;
+  }
+  if (t->hasPhi) {
+    const double distphi = quads_dist_in(&sg->phi, 1, p, d);
+    if (!done && distance > -kTolerance) distance = distphi;
+    done = distance > -kTolerance && distance < kInfLength;
+    if (done) return distance;
+  }
+  {
+    const double distout = quads_dist_out(&sg->outer, p, d, zMin, zMax);
+    if (!done) distance = distout;
+  }
+  return distance;
+}
+
+/* InPhiCutoutWedge (PolyhedronImplementation.h:541-555) */
+static int phd_in_cutout(const or_zseg *sg, int large, v3 p)
+{
+  const int s0 = v3_dot(p, quad_normal(&sg->phi.q[0])) + sg->phi.q[0].d >= 0;
+  const int s1 = v3_dot(p, quad_normal(&sg->phi.q[1])) + sg->phi.q[1].d >= 0;
+  return large ? (s0 || s1) : (s0 && s1);
+}
+
+/* ScalarSafetyToZSegmentSquared (PolyhedronImplementation.h:364-466); `phiIndex` may be moved
+ * to the first or last side, as in the reference */
+static double phd_safety_seg2(const or_polyhedron *t, int si, int *phiIndex, v3 p, int pt_inside)
+{
+  const or_zseg *sg = &t->seg[si];
+  const int in_cutout = *phiIndex < 0;
+  double s2           = kInfLength, so, sin_;
+  if (t->hasPhi && sg->phi.n == 2) {
+    if (pt_inside || in_cutout) {
+      double saf;
+      s2  = quad_dist2(&sg->phi.q[0], p);
+      saf = quad_dist2(&sg->phi.q[1], p);
+      if (saf < s2) s2 = saf;
+      if (in_cutout) {
+        if (t->hasLargePhi && sg->inner.n > 0) {
+          sin_ = quad_dist2(&sg->inner.q[0], p);
+          if (sin_ < s2) {
+            *phiIndex = 0;
+            s2        = sin_;
+          }
+          if (sg->inner.n > 1) {
+            sin_ = quad_dist2(&sg->inner.q[sg->inner.n - 1], p);
+            if (sin_ < s2) {
+              *phiIndex = sg->inner.n - 1;
+              s2        = sin_;
+            }
+          }
+        }
+        return s2;
+      }
+    }
+  }
+  if (in_cutout && si > 0 && si < t->nz - 2 && t->z[si] == t->z[si + 1]) {
+    if (sg->outer.n > 0) {
+      so = quad_dist2(&sg->outer.q[0], p);
+      if (so < s2) {
+        *phiIndex = 0;
+        s2        = so;
+      }
+      if (sg->outer.n > 1) {
+        so = quad_dist2(&sg->outer.q[sg->outer.n - 1], p);
+        if (so < s2) {
+          *phiIndex = sg->outer.n - 1;
+          s2        = so;
+        }
+      }
+    }
+    if (sg->inner.n > 0) {
+      sin_ = quad_dist2(&sg->inner.q[0], p);
+      if (sin_ < s2) {
+        *phiIndex = 0;
+        s2        = sin_;
+      }
+      if (sg->inner.n > 1) {
+        sin_ = quad_dist2(&sg->inner.q[sg->inner.n - 1], p);
+        if (sin_ < s2) {
+          *phiIndex = sg->inner.n - 1;
+          s2        = sin_;
+        }
+      }
+    }
+    return s2;
+  }
+  so   = sg->outer.n > 0 ? quad_dist2(&sg->outer.q[*phiIndex], p) : kInfLength;
+  sin_ = sg->inner.n > 0 ? quad_dist2(&sg->inner.q[*phiIndex], p) : kInfLength;
+  if (sin_ < s2) s2 = sin_;
+  if (so < s2) s2 = so;
+  return s2;
+}
+
+/* ScalarDistanceToEndcaps<pointInsideT> (PolyhedronImplementation.h:468-511) */
+static void phd_dist_endcaps(const or_polyhedron *t, int inside, v3 p, v3 d, double *distance)
+{
+  const int nseg = t->nz - 1;
+  const int last = inside ? !(d.z < 0) : (d.z < 0);
+  const or_zseg *sg = &t->seg[last ? nseg - 1 : 0];
+  const double zPlane = t->z[last ? nseg : 0];
+  const double dt     = (zPlane - p.z) / NonZero(d.z);
+  v3 x;
+  if (dt < -kTolerance || dt >= *distance) return;
+  x = v3_add(p, v3_scale(dt, d));
+  if (!quads_contains(&sg->outer, x)) return;
+  if (sg->inner.n > 0 && quads_contains(&sg->inner, x)) return;
+  if (t->hasPhi && phd_in_cutout(sg, t->hasLargePhi, x)) return;
+  *distance = dt;
+}
+
+/* ScalarSafetyToEndcapsSquared (PolyhedronImplementation.h:513-539) */
+static void phd_safety_endcaps2(const or_polyhedron *t, v3 p, double *dist2)
+{
+  const int nseg      = t->nz - 1;
+  const double first  = t->z[0] - p.z;
+  const double lastd  = t->z[nseg] - p.z;
+  const int isFirst   = fabs(first) < fabs(lastd);
+  const or_zseg *sg   = &t->seg[isFirst ? 0 : nseg - 1];
+  const double dt     = isFirst ? first : lastd;
+  const double dt2    = dt * dt;
+  v3 x;
+  if (dt2 >= *dist2) return;
+  x = v3_make(p.x, p.y, p.z + dt);
+  if (!quads_contains(&sg->outer, x)) return;
+  if (sg->inner.n > 0 && quads_contains(&sg->inner, x)) return;
+  if (t->hasPhi && phd_in_cutout(sg, t->hasLargePhi, x)) return;
+  *dist2 = dt2;
+}
+
+/* ScalarInsideSegBorder (PolyhedronImplementation.h:628-664) */
+static int phd_inside_border(const or_polyhedron *t, v3 p, int zi)
+{
+  const or_zseg *sg = &t->seg[zi];
+  const int phiIndex = phd_find_phi(t, p);
+  const or_quad *q;
+  double r;
+  int in1, in2;
+  if (phiIndex < 0) return kOutsideE;
+  q   = sg->outer.n ? &sg->outer.q[phiIndex] : &sg->inner.q[phiIndex];
+  r   = fabs(v3_dot(p, quad_side(q, 0)));
+  in1 = (r > t->rmin[zi] - kTolerance) && (r < t->rmax[zi] + kTolerance);
+  in2 = (r > t->rmin[zi + 1] - kTolerance) && (r < t->rmax[zi + 1] + kTolerance);
+  if (in1 && in2) {
+    if ((r < t->rmin[zi] + kTolerance) || (r > t->rmax[zi] - kTolerance) || (r < t->rmin[zi + 1] + kTolerance) ||
+        (r > t->rmax[zi + 1] - kTolerance))
+      return kSurfaceE;
+    if (t->hasPhi) {
+      int cin = 0, cout = 0;
+      wedge_ci(&t->w, p, 1, &cin, &cout);
+      return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+    }
+    return kInsideE;
+  }
+  if (!in1 && !in2) return kOutsideE;
+  return kSurfaceE;
+}
+
+static inline int phd_wedge_inside(const or_wedge *w, v3 p) /* Wedge::Inside (Wedge_Evolution.h:262-272) */
+{
+  int cin = 0, cout = 0;
+  wedge_ci(w, p, 1, &cin, &cout);
+  return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+}
+
+/* ScalarInsideSegPhi (PolyhedronImplementation.h:666-701) */
+static int phd_inside_seg_phi(const or_polyhedron *t, v3 p, int zi, int phiIndex)
+{
+  const or_zseg *sg = &t->seg[zi];
+  double dz;
+  int r;
+  if (phiIndex < 0) return kOutsideE;
+  dz = fabs(p.z - t->btubeOffset) - 0.5 * (t->z[t->nz - 1] - t->z[0]);
+  if (dz > kHalfTolerance) return kOutsideE;
+  if (t->samez[zi]) return phd_inside_border(t, p, zi);
+  r = quad_inside(&sg->outer.q[phiIndex], p);
+  if (r != kInsideE) return r;
+  if (sg->inner.n > 0) {
+    r = quad_inside(&sg->inner.q[phiIndex], p);
+    if (r == kInsideE) return kOutsideE;
+    if (r == kSurfaceE) return kSurfaceE;
+  }
+  if (t->hasPhi) {
+    r = phd_wedge_inside(&t->w, p);
+    if (r != kInsideE) return r;
+  }
+  if (fabs(dz) < kHalfTolerance) return kSurfaceE;
+  return kInsideE;
+}
+
+/* ScalarContainsKernel (PolyhedronImplementation.h:557-592) */
+static int polyhedron_contains(const or_polyhedron *t, v3 p)
+{
+  int zi;
+  const or_zseg *sg;
+  if (!tube_contains(&t->btube, v3_make(p.x, p.y, p.z - t->btubeOffset))) return 0;
+  zi = phd_find_z(t, p.z);
+  if (!(zi >= 0 && zi < t->nz - 1)) return 0;
+  sg = &t->seg[zi];
+  if (t->samez[zi]) {
+    const int phiIndex = phd_find_phi(t, p);
+    const or_quad *q;
+    double r;
+    if (phiIndex < 0) return 0;
+    q = sg->outer.n ? &sg->outer.q[phiIndex] : &sg->inner.q[phiIndex];
+    r = fabs(v3_dot(p, quad_side(q, 0)));
+    return ((r >= t->rmin[zi]) && (r <= t->rmax[zi])) | ((r >= t->rmin[zi + 1]) && (r <= t->rmax[zi + 1]));
+  }
+  if (!quads_contains(&sg->outer, p)) return 0;
+  if (sg->inner.n > 0 && quads_contains(&sg->inner, p)) return 0;
+  if (t->hasPhi && !quads_contains(&sg->phi, p)) return 0;
+  return 1;
+}
+
+/* ScalarInsideKernel (PolyhedronImplementation.h:594-626) */
+static int polyhedron_inside(const or_polyhedron *t, v3 p)
+{
+  int zi, r;
+  const or_zseg *sg;
+  double dz;
+  if (!tube_contains(&t->btube, v3_make(p.x, p.y, p.z - t->btubeOffset))) return kOutsideE;
+  zi = phd_find_z(t, p.z);
+  if (zi > t->nz - 2) zi = t->nz - 2;
+  if (zi < 0) zi = 0;
+  sg = &t->seg[zi];
+  if (t->samez[zi]) return phd_inside_border(t, p, zi);
+  r = quads_inside(&sg->outer, p);
+  if (r != kInsideE) return r;
+  if (sg->inner.n > 0) {
+    r = quads_inside(&sg->inner, p);
+    if (r == kInsideE) return kOutsideE;
+    if (r == kSurfaceE) return kSurfaceE;
+  }
+  if (t->hasPhi) {
+    r = quads_inside(&sg->phi, p);
+    if (r != kInsideE) return r;
+  }
+  dz = fabs(fabs(p.z - t->btubeOffset) - 0.5 * (t->z[t->nz - 1] - t->z[0]));
+  if (dz < kTolerance) return kSurfaceE;
+  return kInsideE;
+}
+
+/* ScalarDistanceToInKernel (PolyhedronImplementation.h:703-751) */
+static double polyhedron_dist_in(const or_polyhedron *t, v3 p, v3 d)
+{
+  const int nseg = t->nz - 1;
+  double tubeDistance = 0., distance = kInfLength;
+  int zi;
+  const v3 bp = v3_make(p.x, p.y, p.z - t->btubeOffset);
+  if ((p.z < t->z[0] + kTolerance) && d.z <= 0) return kInfLength;
+  if ((p.z > t->z[nseg] - kTolerance) && d.z >= 0) return kInfLength;
+  if (polyhedron_inside(t, p) == kInsideE) return -1.;
+  if (!tube_contains(&t->btube, bp)) {
+    tubeDistance = tube_dist_in(&t->btube, bp, d);
+    if (tubeDistance == kInfLength) return kInfLength;
+  }
+  zi = phd_clamp_z(t, phd_find_z(t, p.z));
+  if (d.z >= 0) {
+    for (; zi < nseg; ++zi) {
+      distance = phd_dist_in_seg(t, zi, p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+    }
+  } else {
+    for (; zi >= 0; --zi) {
+      distance = phd_dist_in_seg(t, zi, p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+    }
+  }
+  phd_dist_endcaps(t, 0, p, d, &distance);
+  return (distance >= tubeDistance - 1E-6) ? distance : kInfLength;
+}
+
+/* ScalarDistanceToOutKernel (PolyhedronImplementation.h:868-914) */
+static double polyhedron_dist_out(const or_polyhedron *t, v3 p, v3 d)
+{
+  const int nseg = t->nz - 1;
+  double distance = kInfLength;
+  int zi;
+  if ((p.z < t->z[0] - kTolerance) || (p.z > t->z[nseg] + kTolerance)) return -1.;
+  if (polyhedron_inside(t, p) == kOutsideE) return -1.;
+  zi = phd_clamp_z(t, phd_find_z(t, p.z));
+  if (d.z >= 0) {
+    for (; zi < nseg; ++zi) {
+      distance = phd_dist_out_seg(t, zi, t->z[zi], t->z[zi + 1], p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+      if (t->z[zi] - p.z > distance) break;
+    }
+  } else {
+    for (; zi >= 0; --zi) {
+      distance = phd_dist_out_seg(t, zi, t->z[zi], t->z[zi + 1], p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+      if (p.z - t->z[zi] > distance) break;
+    }
+  }
+  phd_dist_endcaps(t, 1, p, d, &distance);
+  if (distance >= kInfLength) distance = 0.;
+  return distance;
+}
+
+/* ScalarSafetyKernel (PolyhedronImplementation.h:753-800) */
+static double polyhedron_safety(const or_polyhedron *t, v3 p, int pt_inside)
+{
+  const int nseg = t->nz - 1;
+  double safety  = kInfLength, dz, s;
+  int z, inside;
+  const int zi = phd_clamp_z(t, phd_find_z(t, p.z));
+  int phiIndex = phd_find_phi(t, p);
+  inside       = phd_inside_seg_phi(t, p, zi, phiIndex);
+  if (inside == kSurfaceE) return 0.;
+  if ((inside == kInsideE) ^ (pt_inside != 0)) return -1.;
+  for (z = zi; z < nseg;) {
+    s      = phd_safety_seg2(t, z, &phiIndex, p, pt_inside);
+    safety = safety < s ? safety : s;
+    ++z;
+    dz = t->z[z] - p.z;
+    if (dz * dz > safety) break;
+  }
+  for (z = zi - 1; z >= 0; --z) {
+    s      = phd_safety_seg2(t, z, &phiIndex, p, pt_inside);
+    safety = safety < s ? safety : s;
+    dz     = p.z - t->z[z];
+    if (dz * dz > safety) break;
+  }
+  phd_safety_endcaps2(t, p, &safety);
+  return sqrt(safety);
+}
+
+/* UnplacedPolyhedron::Extent (source/UnplacedPolyhedron.cpp:273-303) */
+static void polyhedron_extent(const or_polyhedron *t, v3 *mn, v3 *mx)
+{
+  const double sidePhi = t->phiDelta / t->sides, conv = 1. / cos(0.5 * sidePhi);
+  double a[3] = {kInfLength, kInfLength, kInfLength}, b[3] = {-kInfLength, -kInfLength, -kInfLength};
+  int iphi, iz, k, w;
+  for (iphi = 0; iphi <= t->sides; ++iphi) {
+    const double phi = t->phiStart + iphi * sidePhi;
+    const double cx = conv * cos(phi), cy = conv * sin(phi);
+    for (iz = 0; iz < t->nz; ++iz)
+      for (w = 0; w < 2; ++w) {
+        const double r   = w == 0 ? t->rmin[iz] : t->rmax[iz];
+        const double c[3] = {r * cx, r * cy, t->z[iz]};
+        for (k = 0; k < 3; ++k) {
+          a[k] = or_min(a[k], c[k]);
+          b[k] = or_max(b[k], c[k]);
+        }
+      }
+  }
+  *mn = v3_make(a[0], a[1], a[2]);
+  *mx = v3_make(b[0], b[1], b[2]);
+}
+
 /* ---------------------------------------------------------------- */
 /* Boolean solids over placed operands: BooleanImplementation.h (subtraction),
  * BooleanUnionImplementation.h, BooleanIntersectionImplementation.h.  A placed operand's
@@ -3267,6 +4063,7 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
     lv->s.orb.r = p[0];
     return 0;
   case OR_CUTTUBE: return cuttube_init(&lv->s.ctube, p, err, errlen);
+  case OR_POLYHEDRON: return polyhedron_init(&lv->s.phd, p, err, errlen);
   case OR_BOOLEAN: /* operands are linked once the placements are known (or_core.c) */
     if (!(p[0] == 0. || p[0] == 1. || p[0] == 2.) || !(p[1] >= 0. && p[1] <= 2147483647. && p[1] == floor(p[1])) ||
         !(p[2] >= 0. && p[2] <= 2147483647. && p[2] == floor(p[2]))) {
@@ -3300,6 +4097,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
     return;
   case OR_CUTTUBE: cuttube_extent(&lv->s.ctube, mn, mx); return;
   case OR_BOOLEAN: boolean_extent(&lv->s.boo, mn, mx); return;
+  case OR_POLYHEDRON: polyhedron_extent(&lv->s.phd, mn, mx); return;
   }
 }
 
@@ -3321,6 +4119,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_ORB: return orb_dist_in(&lv->s.orb, p, d);
   case OR_CUTTUBE: return cuttube_dist_in(&lv->s.ctube, p, d, stepmax);
   case OR_BOOLEAN: return boolean_dist_in(&lv->s.boo, p, d, stepmax, c);
+  case OR_POLYHEDRON: return polyhedron_dist_in(&lv->s.phd, p, d);
   }
   return kInfLength;
 }
@@ -3340,6 +4139,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_ORB: return orb_dist_out(&lv->s.orb, p, d);
   case OR_CUTTUBE: return cuttube_dist_out(&lv->s.ctube, p, d);
   case OR_BOOLEAN: return boolean_dist_out(&lv->s.boo, p, d, stepmax, c);
+  case OR_POLYHEDRON: return polyhedron_dist_out(&lv->s.phd, p, d);
   }
   return -1.;
 }
@@ -3358,6 +4158,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_ORB: return orb_safe_in(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_safe_in(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_safe_in(&lv->s.boo, p, c);
+  case OR_POLYHEDRON: return polyhedron_safety(&lv->s.phd, p, 0);
   }
   return kInfLength;
 }
@@ -3376,6 +4177,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_ORB: return orb_safe_out(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_safe_out(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_safe_out(&lv->s.boo, p, c);
+  case OR_POLYHEDRON: return polyhedron_safety(&lv->s.phd, p, 1);
   }
   return 0.;
 }
@@ -3394,6 +4196,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_ORB: return orb_contains(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_contains(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_contains(&lv->s.boo, p, c);
+  case OR_POLYHEDRON: return polyhedron_contains(&lv->s.phd, p);
   }
   return 0;
 }
@@ -3412,6 +4215,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_ORB: return orb_inside(&lv->s.orb, p);
   case OR_CUTTUBE: return cuttube_inside(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_inside(&lv->s.boo, p, c);
+  case OR_POLYHEDRON: return polyhedron_inside(&lv->s.phd, p);
   }
   return kOutsideE;
 }

@@ -1294,7 +1294,60 @@ ORB_CASES = [
           (0.84546676256780450842, -0.33558962646945966757, -0.41541010579811871173), 0.0),
 ]
 
+POLYHEDRON = 10
+PH = "test/unit_tests/TestPolyhedra.cpp"
+
+
+def _phd(sphi, dphi, sides, z, rmin, rmax):
+    """Polyhedron parameters: sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz]."""
+    return (sphi, dphi, float(sides), float(len(z))) + tuple(z) + tuple(rmin) + tuple(rmax)
+
+
+# TestPolyhedra.cpp:22-56 MyPGon: a 45-degree phi section of five sides, 8 planes
+MYPGON = _phd(0.0, KPI_V / 4.0, 5, (-30.0, -20.0, -10.0, 0.0, 10.0, 20.0, 30.0, 40.0),
+              (30.0, 30.0, 0.0, 0.0, 0.0, 0.0, 40.0, 40.0), (70.0, 70.0, 70.0, 40.0, 40.0, 80.0, 80.0, 60.0))
+# TestPolyhedra.cpp:94-98 MyPGon2, the hexagonal prism given by (r, z) corners {15, 15, 0, 0},
+# {10, -10, -10, 10}: the (r, z) constructor turns the corner radius into the sides' radius
+# 15 cos(pi / 6) (PolyhedronStruct.h:203-218) and gives these planes
+_HEX_R = 15.0 * math.cos(0.5 * (2.0 * KPI_V / 6.0))
+MYPGON2 = _phd(0.0, 2.0 * KPI_V, 6, (-10.0, 10.0), (0.0, 0.0), (_HEX_R, _HEX_R))
+_HALFDPHI = 0.5 * (KPI_V / 4.0) / 5.0
+POLYHEDRON_CASES = [
+    _case(f"{PH}:173", POLYHEDRON, MYPGON, "inside", (0.0, 0.0, -5.0), None, 2, "eq"),
+    _case(f"{PH}:174", POLYHEDRON, MYPGON, "inside", (50.0, 0.0, 40.0), None, 2, "eq"),
+    _case(f"{PH}:175", POLYHEDRON, MYPGON, "inside", (5.0, 1.0, 20.0), None, 1, "eq"),
+    _case(f"{PH}:176", POLYHEDRON, MYPGON, "inside", (45.0, 5.0, 30.0), None, 1, "eq"),
+    _case(f"{PH}:177", POLYHEDRON, MYPGON, "inside", (0.0, 0.0, 30.0), None, 3, "eq"),
+    _case(f"{PH}:178", POLYHEDRON, MYPGON, "inside", (41.0, 0.0, 10.0), None, 3, "eq"),
+    _case(f"{PH}:179", POLYHEDRON, MYPGON2, "inside", (0.0, 0.0, 0.0), None, 1, "eq"),
+    _case(f"{PH}:180", POLYHEDRON, MYPGON2, "inside", (15.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{PH}:188", POLYHEDRON, MYPGON, "contains", (20.0 + 1e-9, 20.0, 5.0), None, 1.0, "eq"),
+    _case(f"{PH}:189", POLYHEDRON, MYPGON, "inside", (20.0 + 1e-9, 20.0, 5.0), None, 1, "eq"),
+    _case(f"{PH}:197", POLYHEDRON, MYPGON, "contains", (20.0, 20.0, 5.0), None, 0.0, "eq"),
+    _case(f"{PH}:198", POLYHEDRON, MYPGON, "inside", (20.0, 20.0, 5.0), None, 2, "eq"),
+    _case(f"{PH}:206", POLYHEDRON, MYPGON, "contains", (20.0 - 1e-9, 20.0, 5.0), None, 0.0, "eq"),
+    _case(f"{PH}:207", POLYHEDRON, MYPGON, "inside", (20.0 - 1e-9, 20.0, 5.0), None, 3, "eq"),
+    _case(f"{PH}:211", POLYHEDRON, MYPGON, "dist_in", (0.0, 0.0, -5.0), vx, 0.0, "abs_tol"),
+    _case(f"{PH}:212", POLYHEDRON, MYPGON, "dist_in", (0.0, 0.0, -5.0), vmy, 0.0, "abs_tol"),
+    _case(f"{PH}:214", POLYHEDRON, MYPGON, "dist_in", (50.0, 0.0, 40.0), vy, 0.0, "abs_tol_or_huge"),
+    _case(f"{PH}:216", POLYHEDRON, MYPGON, "dist_in", (0.0, 0.0, 30.0), vx, 40.12368793931, "abs_tol"),
+    _case(f"{PH}:217", POLYHEDRON, MYPGON, "dist_in", (41.0, 0.0, 10.0), vmx, 0.87631206069, "abs_tol"),
+    _case(f"{PH}:218", POLYHEDRON, MYPGON, "dist_in", (41.0, 0.0, 10.0), vz, 0.218402670765, "abs_tol"),
+    _case(f"{PH}:222", POLYHEDRON, MYPGON, "dist_out", (0.0, 0.0, -5.0), vmx, 0.0, "abs_tol"),
+    _case(f"{PH}:223", POLYHEDRON, MYPGON, "dist_out", (5.0, 1.0, 20.0), vmy, 1.0, "abs_tol"),
+    _case(f"{PH}:224", POLYHEDRON, MYPGON, "dist_out", (5.0, 1.0, 20.0), vz, 1.27382374146, "abs_tol"),
+    _case(f"{PH}:225", POLYHEDRON, MYPGON, "dist_out", (45.0, 5.0, 30.0), vz, 10.0, "abs_tol"),
+    _case(f"{PH}:226", POLYHEDRON, MYPGON, "dist_out", (45.0, 5.0, 30.0), vx, 34.8538673445, "abs_tol"),
+    _case(f"{PH}:227", POLYHEDRON, MYPGON, "dist_out", (45.0, 5.0, 30.0), vy, 40.0, "abs_tol"),
+    _case(f"{PH}:228", POLYHEDRON, MYPGON2, "dist_out", (0.0, 0.0, 0.0), vx, 0.0, "gt0"),
+    _case(f"{PH}:229", POLYHEDRON, MYPGON2, "dist_out", (0.0, 0.0, 0.0), vy, 0.0, "gt0"),
+    _case(f"{PH}:230", POLYHEDRON, MYPGON2, "dist_out", (0.0, 0.0, 0.0), vz, 0.0, "gt0"),
+]
+# TestPolyhedra.cpp:156-157: the extent of MyPGon (ApproxEqual of vectors)
+MYPGON_EXTENT = ((0.0, 0.0, -30.0), (80.0 / math.cos(_HALFDPHI), 40.0 * math.sqrt(2.0) / math.cos(_HALFDPHI), 40.0))
+
 ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES + POLYCONE_CASES + ORB_CASES
+ALL_CASES += POLYHEDRON_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:
@@ -1326,6 +1379,12 @@ def check(case, value) -> bool:
         return value == case["expect"]
     if c == "near":  # |value - expect| < 1000 kTolerance (TestPolycone.cpp:101-102, 113)
         return abs(value - case["expect"]) < 1000.0 * 1e-9
+    if c == "abs_tol":  # |value - expect| < kTolerance (TestPolyhedra.cpp:215-231)
+        return abs(value - case["expect"]) < 1e-9
+    if c == "abs_tol_or_huge":  # |value| < kTolerance || |value| > 1e10 (TestPolyhedra.cpp:218-219)
+        return abs(value - case["expect"]) < 1e-9 or abs(value) > 1e10
+    if c == "gt0":
+        return value > 0.0
     if c == "range":
         return case["expect"] - 1e-4 <= value <= case["expect"] + 1e-4
     raise ValueError(c)

@@ -1,7 +1,7 @@
 """Shape parameter sets and point sampling shared by the shape parity tests.
 
-The sets cover every implemented shape type: full and sectioned Tubes, Cones and
-Polycones, Trd and Trapezoid variants, Spheres with phi and theta sections (many of
+The sets cover every implemented shape type: full and sectioned Tubes, Cones,
+Polycones and Polyhedra, Trd and Trapezoid variants, Spheres with phi and theta sections (many of
 them the parameter sets of the reference's unit tests, from tests/golden/known_answers).
 """
 import zlib
@@ -72,6 +72,19 @@ SHAPE_SETS = [
     ("cuttube-hollow-sector", W.CUTTUBE, W.cuttube_params(3., 5., 10., 0., 2 * KA.KPI / 3, 3 * KA.KPI / 4,
                                                            KA.KPI / 3, KA.KPI / 4, 2 * KA.KPI / 3)),
     ("cuttube-large-tilted", W.CUTTUBE, W.cuttube_params(10., 40., 30., 0.5, 4.5, 2.6, 0.4, 0.45, 2.0)),
+    ("polyhedron-mypgon", W.POLYHEDRON, KA.MYPGON),
+    ("polyhedron-hex-prism", W.POLYHEDRON, KA.MYPGON2),
+    ("polyhedron-solid-6", W.POLYHEDRON, KA._phd(0.0, W.K_TWO_PI, 6, (-30.0, -10.0, 10.0, 30.0), (0.0,) * 4,
+                                                 (20.0, 30.0, 30.0, 20.0))),
+    ("polyhedron-hollow-8-rotated", W.POLYHEDRON, KA._phd(0.4, W.K_TWO_PI, 8, (-30.0, -10.0, 10.0, 30.0),
+                                                          (5.0, 10.0, 10.0, 5.0), (20.0, 25.0, 25.0, 20.0))),
+    ("polyhedron-sector-5-hollow", W.POLYHEDRON, KA._phd(0.3, 4.0, 5, (-20.0, 0.0, 25.0), (8.0, 4.0, 10.0),
+                                                         (20.0, 30.0, 26.0))),
+    ("polyhedron-large-cutout-3", W.POLYHEDRON, KA._phd(-1.0, 2.0, 3, (-20.0, 20.0), (10.0, 10.0), (30.0, 30.0))),
+    ("polyhedron-step-equal-z", W.POLYHEDRON, KA._phd(0.0, W.K_TWO_PI, 5, (-30.0, 0.0, 0.0, 30.0),
+                                                      (0.0, 0.0, 10.0, 10.0), (20.0, 20.0, 30.0, 30.0))),
+    ("polyhedron-sector-equal-z", W.POLYHEDRON, KA._phd(1.0, 3.0, 4, (-25.0, -5.0, -5.0, 20.0),
+                                                        (5.0, 5.0, 12.0, 12.0), (25.0, 15.0, 30.0, 30.0))),
 ]
 
 

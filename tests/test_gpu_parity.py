@@ -338,15 +338,18 @@ def test_shape_random_points_bit_exact(oracle, vgnav, name, shape, params, cuda)
     assert np.mean(ins == 2.0) > 0.5
 
 
-@pytest.mark.parametrize("sections", ["full", "sections", "all-shapes"])
+@pytest.mark.parametrize("sections", ["full", "sections", "all-shapes", "all-shapes-sections"])
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
     """8192 daughters of the benchmark's seven shape types, full rotations (with "sections",
     most tubes, cones and polycones are phi sections and spheres phi/theta sections; with
-    "all-shapes", every implemented type, Orb too): locate, one step with safety, then every
-    step of a track subset to the world exit, all equal to the oracle."""
+    "all-shapes", every implemented type, Orb, CutTube and Polyhedron too, "all-shapes-sections"
+    the same with sections): locate, one step with safety, then every step of a track subset to
+    the world exit, all equal to the oracle."""
     if sections == "all-shapes":
         desc = W.mixed_shape_geometry(seed=26, shapes=W.ALL_SHAPES)
+    elif sections == "all-shapes-sections":
+        desc = W.mixed_shape_geometry(seed=29, shapes=W.ALL_SHAPES, sections=True)
     else:
         desc = W.mixed_shape_geometry(sections=sections == "sections")
     og = oracle.OracleGeometry(desc)
@@ -363,7 +366,7 @@ def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
     assert np.array_equal(got["safety"], ref["safety"])
     assert np.array_equal(got["out"], ref["out"])
     w = t.head(4096)
-    for it in range(200):
+    for it in range(400):
         ref = og.step(w)
         got = gpu_step(cuda, geo, w, mixed=mixed)
         assert np.array_equal(got["step"], ref["step"]), it
@@ -373,7 +376,9 @@ def test_mixed_shapes_locate_step_walk(oracle, vgnav, cuda, mixed, sections):
         w = keep(w, w.states["nav_ind"] != 0)
         if w.n == 0:
             break
-    assert w.n == 0
+    # with sections, a few tracks follow the reference's ping-pong at polyhedra whose phi
+    # cut-out is wider than pi (DistanceToIn ~1e-14 at a cut face, then DistanceToOut 0)
+    assert w.n == 0 or (sections == "all-shapes-sections" and w.n <= 16)
 
 
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])

@@ -32,3 +32,10 @@ def test_oracle_sphere_b830(oracle):
     dist = float(g.shape(0, OPS["dist_out"], *[np.array([c]) for c in p], *[np.array([c]) for c in v])[0])
     q = [np.array([p[i] + dist * v[i]]) for i in range(3)]
     assert int(g.shape(0, OPS["inside"], *q, *[np.zeros(1)] * 3)[0]) == 2
+
+
+def test_oracle_polyhedron_extent(oracle):
+    """TestPolyhedra.cpp:156-157: the extent of MyPGon, ApproxEqual per component."""
+    e = oracle.OracleGeometry(single_shape(KA.POLYHEDRON, KA.MYPGON)).extent(0)
+    lo, hi = KA.MYPGON_EXTENT
+    assert all(KA.approx_equal(float(a), b) for a, b in zip(e, lo + hi)), e

@@ -30,7 +30,7 @@ constexpr int kMaxLevels = 30;  // bound on geometry depth (relocation loops)
 
 enum ShapeType : int32_t {
   kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kOrb = 7, kCutTube = 8,
-  kBoolean = 9, kNumShapes = 10
+  kBoolean = 9, kPolyhedron = 10, kNumShapes = 11
 };
 
 // flags of a placement transformation (Transformation3D::SetProperties,
@@ -180,6 +180,22 @@ enum { CutTubeDz = kTubeSize, CutTubeN0, CutTubeD0 = CutTubeN0 + 3, CutTubeN1, C
        CutTubeCos1, CutTubeSin1, CutTubeCos2, CutTubeSin2, CutTubeMaxVal, kCutTubeSize };
 // Wedge block (evolution::Wedge): along vectors, normal vectors, fDPhi
 enum { WedgeA1x = 0, WedgeA1y, WedgeA2x, WedgeA2y, WedgeN1x, WedgeN1y, WedgeN2x, WedgeN2y, WedgeDPhi, kWedgeSize };
+// Polyhedron: PolyhedronStruct (PolyhedronStruct.h:52-80): the header (with fPhiStart and
+// fPhiDelta), the bounding tube
+// (a Tube row), the phi wedge fPhiWedge (a Wedge block), the arrays fZPlanes, fRMin, fRMax,
+// fSameZ (nz each), fPhiSections (sides + 1 vectors), then per z segment the face counts
+// (outer, phi, inner) and the offset of its first face from the row's start, and the faces
+// (Quadrilaterals: plane, four side planes, four corners), outer then phi then inner
+enum { PhdSides = 0, PhdNz, PhdHasPhi, PhdLargePhi, PhdTubeOffset, PhdPhiStart, PhdPhiDelta, PhdTube,
+       PhdWedge = PhdTube + kTubeSize,
+       PhdArrays = PhdWedge + kWedgeSize };
+enum { QuadN = 0, QuadD = 3, QuadSide = 4, QuadCorner = 20, kQuadSize = 32 };  // side j: 4 doubles at QuadSide + 4 j
+VGN_HD inline int phd_z(int) { return PhdArrays; }
+VGN_HD inline int phd_rmin(int nz) { return PhdArrays + nz; }
+VGN_HD inline int phd_rmax(int nz) { return PhdArrays + 2 * nz; }
+VGN_HD inline int phd_samez(int nz) { return PhdArrays + 3 * nz; }
+VGN_HD inline int phd_phisec(int nz) { return PhdArrays + 4 * nz; }
+VGN_HD inline int phd_segs(int nz, int sides) { return phd_phisec(nz) + 3 * (sides + 1); }  // 4 per segment
 // Cone (full phi): ConeStruct cached members
 enum { ConeRmin1 = 0, ConeRmax1, ConeRmin2, ConeRmax2, ConeDz, ConeOrigRmax1, ConeOrigRmax2, ConeInnerSlope,
        ConeOuterSlope, ConeInnerOffset, ConeOuterOffset, ConeInnerTol, ConeOuterTol, ConeSqRmin1, ConeSqRmin2,

@@ -4,6 +4,7 @@
 // reference precomputes in its *Struct constructors, computed with the same
 // expressions so the device kernels see the same doubles.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 
 #include "../../include/vgnav.h"
@@ -65,9 +66,226 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
     if (n_avail < 3 || !(p[2] >= 2 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
     return 3 + 3 * (int)p[2];
   }
+  case kPolyhedron: {  // sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz]
+    if (n_avail < 4 || !(p[3] >= 2 && p[3] <= 4096) || (double)(int)p[3] != p[3]) return -1;
+    if (!(p[2] >= 1 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
+    return 4 + 3 * (int)p[3];
+  }
   default: return -1;
   }
 }
+
+// ---------------------------------------------------------------- Polyhedron
+// PolyhedronStruct(phiStart, phiDelta, sideCount, zPlaneCount, zPlanes, rMin, rMax) and
+// Initialize (PolyhedronStruct.h:96-110, 264-420), Quadrilaterals::Set (source/Quadrilaterals.cpp:33-104),
+// Planes::Set / FlipSign (source/Planes.cpp:30-49), in the row layout row::Phd*.
+namespace {
+struct PV3 {
+  double x, y, z;
+};
+inline PV3 pv3(double x, double y, double z) { return PV3{x, y, z}; }
+inline PV3 operator-(PV3 a, PV3 b) { return pv3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline double pdot(PV3 a, PV3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline PV3 pcross(PV3 a, PV3 b) { return pv3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline PV3 pfix(PV3 a)  // Vector3D::FixZeroes (Vector3D.h:298-305)
+{
+  if (std::fabs(a.x) < kTolerance) a.x = 0.0;
+  if (std::fabs(a.y) < kTolerance) a.y = 0.0;
+  if (std::fabs(a.z) < kTolerance) a.z = 0.0;
+  return a;
+}
+inline PV3 pnormalized(PV3 a)  // Vector3D::Normalized (Vector3D.h:202)
+{
+  const double inv = 1. / std::sqrt(pdot(a, a));
+  return pv3(a.x * inv, a.y * inv, a.z * inv);
+}
+inline bool ptol_eq(PV3 a, PV3 b)  // operator== (Vector3D.h:387-390)
+{
+  return std::fabs(a.x - b.x) < kTolerance && std::fabs(a.y - b.y) < kTolerance && std::fabs(a.z - b.z) < kTolerance;
+}
+inline double phd_normalize_angle(double a) { return a + kTwoPi * (double)((a < 0) - (int)(a / kTwoPi)); }
+
+// Quadrilaterals::Set of one face into q[kQuadSize]; false when fewer than three corners differ
+bool quad_set(double *q, const PV3 (&in)[4])
+{
+  PV3 ch[4];
+  int assigned = 1;
+  for (int j = 0; j < 4; ++j) {
+    q[row::QuadCorner + 3 * j]     = in[j].x;
+    q[row::QuadCorner + 3 * j + 1] = in[j].y;
+    q[row::QuadCorner + 3 * j + 2] = in[j].z;
+  }
+  ch[0] = in[0];
+  for (int tested = 1; tested < 4; ++tested) {
+    bool chosen = true;
+    for (int j = 0; j < assigned; ++j)
+      if (ptol_eq(ch[j], in[tested])) {
+        chosen = false;
+        break;
+      }
+    if (chosen) ch[assigned++] = in[tested];
+  }
+  if (assigned < 3) return false;
+  const double a = ch[0].y * (ch[1].z - ch[2].z) + ch[1].y * (ch[2].z - ch[0].z) + ch[2].y * (ch[0].z - ch[1].z);
+  const double b = ch[0].z * (ch[1].x - ch[2].x) + ch[1].z * (ch[2].x - ch[0].x) + ch[2].z * (ch[0].x - ch[1].x);
+  const double c = ch[0].x * (ch[1].y - ch[2].y) + ch[1].x * (ch[2].y - ch[0].y) + ch[2].x * (ch[0].y - ch[1].y);
+  double d = -ch[0].x * (ch[1].y * ch[2].z - ch[2].y * ch[1].z) - ch[1].x * (ch[2].y * ch[0].z - ch[0].y * ch[2].z) -
+             ch[2].x * (ch[0].y * ch[1].z - ch[1].y * ch[0].z);
+  PV3 n            = pv3(a, b, c);
+  const double inv = 1. / std::sqrt(pdot(n, n));
+  n                = pv3(n.x * inv, n.y * inv, n.z * inv);
+  d *= inv;
+  n                  = pfix(n);
+  q[row::QuadN]      = n.x;
+  q[row::QuadN + 1]  = n.y;
+  q[row::QuadN + 2]  = n.z;
+  q[row::QuadD]      = d;
+  for (int j = 0; j < 4; ++j) {
+    double *s     = q + row::QuadSide + 4 * j;
+    const PV3 c0 = in[j], c1 = in[(j + 1) % 4];
+    if (!ptol_eq(c1, c0)) {
+      const PV3 fixed   = pfix(pnormalized(pcross(n, c1 - c0)));
+      const double sinv = 1. / std::sqrt(pdot(fixed, fixed));
+      s[0]              = sinv * fixed.x;
+      s[1]              = sinv * fixed.y;
+      s[2]              = sinv * fixed.z;
+      s[3]              = sinv * -pdot(fixed, c0);
+    } else {
+      s[0] = s[1] = s[2] = s[3] = 0.;
+    }
+  }
+  return true;
+}
+
+void quad_flip(double *q)
+{
+  for (int k = 0; k < 4; ++k) q[k] = -q[k];  // normal and distance (QuadN .. QuadD)
+}
+
+int polyhedron_row(const double *p, std::vector<double> &shape, std::string &err)
+{
+  const double phiStart0 = p[0], phiDelta0 = p[1];
+  const int S = (int)p[2], nz = (int)p[3];
+  const double *zp = p + 4, *rmn = p + 4 + nz, *rmx = p + 4 + 2 * nz;
+  if (!(phiDelta0 > 0) || S < 1 || nz < 2 || !((phiDelta0 > kTwoPi ? kTwoPi : phiDelta0) / S < kPi)) {
+    err = "polyhedron needs dphi > 0, nz >= 2 and sides with dphi / sides < pi";
+    return VGN_ERR_ARG;
+  }
+  for (int i = 0; i < nz; ++i) {
+    if (!(rmn[i] >= 0 && rmx[i] >= rmn[i]) || (i > 0 && !(zp[i] >= zp[i - 1]))) {
+      err = "polyhedron needs 0 <= rmin <= rmax and non-decreasing z planes";
+      return VGN_ERR_ARG;
+    }
+    if (i + 2 < nz && zp[i] == zp[i + 1] && zp[i + 1] == zp[i + 2]) {
+      err = "polyhedron has three equal z planes in a row";
+      return VGN_ERR_ARG;
+    }
+  }
+  if (zp[0] == zp[1] || zp[nz - 2] == zp[nz - 1]) {
+    err = "polyhedron has a zero-length first or last segment";
+    return VGN_ERR_ARG;
+  }
+  const bool hasPhi = phiDelta0 < kTwoPi;
+  const double phiStart = phd_normalize_angle(phiStart0), phiDelta = phiDelta0 > kTwoPi ? kTwoPi : phiDelta0;
+  const double sidePhi = phiDelta / S, cosHalf = std::cos(0.5 * sidePhi);
+  // face counts per segment (Initialize, PolyhedronStruct.h:304-326)
+  std::vector<int> nout(nz - 1), nphi(nz - 1), nin(nz - 1);
+  for (int i = 0; i < nz - 1; ++i) {
+    const bool hasInnerRadius = rmn[i] > 0 || rmn[i + 1] > 0;
+    nout[i]                   = (zp[i] == zp[i + 1] && rmx[i] == rmx[i + 1]) ? 0 : S;
+    nphi[i]                   = hasPhi ? (zp[i] == zp[i + 1] ? 0 : 2) : 0;
+    nin[i]                    = (hasInnerRadius && !(zp[i] == zp[i + 1] && rmn[i] == rmn[i + 1])) ? S : 0;
+    if (zp[i] == zp[i + 1] && nout[i] == 0 && nin[i] == 0) {
+      err = "polyhedron has a zero-length segment with equal radii on its two planes";
+      return VGN_ERR_ARG;
+    }
+  }
+  const int segs  = row::phd_segs(nz, S);
+  int nfaces      = 0;
+  for (int i = 0; i < nz - 1; ++i) nfaces += nout[i] + nphi[i] + nin[i];
+  std::vector<double> r((size_t)(segs + 4 * (nz - 1) + nfaces * row::kQuadSize), 0.);
+  r[row::PhdSides]    = S;
+  r[row::PhdNz]       = nz;
+  r[row::PhdHasPhi]   = hasPhi ? 1. : 0.;
+  r[row::PhdLargePhi] = phiDelta0 < kPi ? 1. : 0.;
+  r[row::PhdPhiStart] = phiStart;
+  r[row::PhdPhiDelta] = phiDelta;
+  wedge_fill(&r[row::PhdWedge], phiDelta, phiStart);  // fPhiWedge(fPhiDelta, fPhiStart)
+  for (int i = 0; i < nz; ++i) {
+    r[row::phd_z(nz) + i]     = zp[i];
+    r[row::phd_rmin(nz) + i]  = rmn[i];
+    r[row::phd_rmax(nz) + i]  = rmx[i];
+    r[row::phd_samez(nz) + i] = (i > 0 && i < nz - 1 && zp[i] == zp[i + 1]) ? 1. : 0.;
+  }
+  auto getPhi = [&](int side) { return phd_normalize_angle(phiStart + ((!hasPhi && side == S) ? 0 : side) * sidePhi); };
+  PV3 phisec[2];
+  for (int i = 0; i <= S; ++i) {
+    const double phi = getPhi(i);
+    const PV3 corner = pfix(pnormalized(pv3(1. * std::cos(phi), 1. * std::sin(phi), 0)));
+    const PV3 s      = pcross(pnormalized(corner), pv3(0, 0, -1));
+    r[row::phd_phisec(nz) + 3 * i]     = s.x;
+    r[row::phd_phisec(nz) + 3 * i + 1] = s.y;
+    r[row::phd_phisec(nz) + 3 * i + 2] = s.z;
+    if (i == 0) phisec[0] = s;
+    if (i == S) phisec[1] = s;
+  }
+  // the bounding tube (PolyhedronStruct.h:341-367)
+  double inner = DBL_MAX, outer = -DBL_MAX;  // kInfLength
+  for (int i = 0; i < nz; ++i) {
+    if (rmn[i] < inner) inner = rmn[i];
+    if (rmx[i] > outer) outer = rmx[i];
+  }
+  outer /= cosHalf;
+  const double tp[5] = {inner - kHalfTolerance, outer + kHalfTolerance, 0.5 * (zp[nz - 1] - zp[0]) + kTolerance,
+                        !hasPhi ? 0 : phiStart - 100 * kTolerance, !hasPhi ? kTwoPi : phiDelta + 2 * (100 * kTolerance)};
+  std::vector<double> tube;
+  if (int rc = shape_make_row(kTube, tp, 5, tube, err)) return rc;
+  std::copy(tube.begin(), tube.end(), r.begin() + row::PhdTube);
+  r[row::PhdTubeOffset] = 0.5 * (zp[0] + zp[nz - 1]);
+  // the faces (PolyhedronStruct.h:369-418)
+  auto vtx = [&](const double *rr, int i, int j) {
+    const double phi = getPhi(j), R = rr[i] / cosHalf;
+    return pfix(pv3(R * std::cos(phi), R * std::sin(phi), zp[i]));
+  };
+  int face = segs + 4 * (nz - 1);
+  for (int ip = 0; ip < nz - 1; ++ip) {
+    double *st = &r[segs + 4 * ip];
+    st[0] = nout[ip];
+    st[1] = nphi[ip];
+    st[2] = nin[ip];
+    st[3] = face;
+    for (int k = 0; k < 2; ++k) {  // outer, then (after the phi faces) inner
+      const double *rr = k == 0 ? rmx : rmn;
+      const int n      = k == 0 ? nout[ip] : nin[ip];
+      double *base     = &r[face + (k == 0 ? 0 : (nout[ip] + nphi[ip]) * row::kQuadSize)];
+      for (int is = 0; is < n; ++is) {
+        double *q           = base + is * row::kQuadSize;
+        const PV3 corner[4] = {vtx(rr, ip, is), vtx(rr, ip, is + 1), vtx(rr, ip + 1, is + 1), vtx(rr, ip + 1, is)};
+        if (!quad_set(q, corner)) {
+          err = "polyhedron has a face with fewer than three distinct corners";
+          return VGN_ERR_ARG;
+        }
+        if (q[0] * corner[0].x + q[1] * corner[0].y < 0) quad_flip(q);  // WrongNormal
+      }
+    }
+    if (nphi[ip] == 2) {
+      double *q0       = &r[face + nout[ip] * row::kQuadSize];
+      double *q1       = q0 + row::kQuadSize;
+      const PV3 c0[4]  = {vtx(rmn, ip, 0), vtx(rmn, ip + 1, 0), vtx(rmx, ip + 1, 0), vtx(rmx, ip, 0)};
+      const PV3 c1[4]  = {vtx(rmx, ip, S), vtx(rmx, ip + 1, S), vtx(rmn, ip + 1, S), vtx(rmn, ip, S)};
+      if (!quad_set(q0, c0) || !quad_set(q1, c1)) {
+        err = "polyhedron has a face with fewer than three distinct corners";
+        return VGN_ERR_ARG;
+      }
+      if (pdot(pv3(q0[0], q0[1], q0[2]), phisec[0]) > 0) quad_flip(q0);
+      if (pdot(pv3(q1[0], q1[1], q1[2]), phisec[1]) < 0) quad_flip(q1);
+    }
+    face += (nout[ip] + nphi[ip] + nin[ip]) * row::kQuadSize;
+  }
+  shape.insert(shape.end(), r.begin(), r.end());
+  return VGN_OK;
+}
+} // namespace
 
 int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<double> &shape, std::string &err)
 {
@@ -386,6 +604,7 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     shape.push_back(dphi);
     return VGN_OK;
   }
+  case kPolyhedron: return polyhedron_row(p, shape, err);
   case kCutTube: {
     // UnplacedCutTube(rmin, rmax, z, sphi, dphi, bx, by, bz, tx, ty, tz) -> CutTubeStruct
     // (UnplacedCutTube.h:54-70, CutTubeStruct.h:34-46): a tube of infinite half-length, the two
@@ -464,6 +683,7 @@ bool shape_row_has_sections(int32_t type, const double *r)
     return r[row::pcon_cone(n, 0) + row::ConeDPhi] < 2. * kPi;
   }
   case kSphere: return r[row::SphFull] == 0.;
+  case kPolyhedron: return r[row::PhdHasPhi] != 0.;
   case kBoolean:  // the operands' (once linked)
     return (r[row::BoolLeftType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolLeftType], r + (int64_t)r[row::BoolLeftRow])) ||
            (r[row::BoolRightType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolRightType], r + (int64_t)r[row::BoolRightRow]));
@@ -794,6 +1014,27 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mx = {r[0], r[0], r[0]};
     return;
   case kBoolean: boolean_extent(r, mn, mx); return;
+  case kPolyhedron: {  // UnplacedPolyhedron::Extent (source/UnplacedPolyhedron.cpp:273-303)
+    const int S = (int)r[row::PhdSides], nz = (int)r[row::PhdNz];
+    const double sidePhi = r[row::PhdPhiDelta] / S, conv = 1. / std::cos(0.5 * sidePhi);
+    double a[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, b[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    for (int iphi = 0; iphi <= S; ++iphi) {
+      const double phi = r[row::PhdPhiStart] + iphi * sidePhi;
+      const double cx = conv * std::cos(phi), cy = conv * std::sin(phi);
+      for (int iz = 0; iz < nz; ++iz)
+        for (int w = 0; w < 2; ++w) {
+          const double rr   = r[(w == 0 ? row::phd_rmin(nz) : row::phd_rmax(nz)) + iz];
+          const double c[3] = {rr * cx, rr * cy, r[row::phd_z(nz) + iz]};
+          for (int k = 0; k < 3; ++k) {
+            a[k] = vmin(a[k], c[k]);
+            b[k] = vmax(b[k], c[k]);
+          }
+        }
+    }
+    mn = {a[0], a[1], a[2]};
+    mx = {b[0], b[1], b[2]};
+    return;
+  }
   default: mn = mx = {0, 0, 0};
   }
 }

@@ -2479,6 +2479,539 @@ __device__ __forceinline__ double cuttube_safe_out(const double *r, D3 p)
   return safety;
 }
 
+// ---------------------------------------------------------------- Polyhedron
+// PolyhedronImplementation.h over a row::Phd* row (Quadrilaterals.h, Planes.h for the faces).
+// The reference's placement specialisation by inner radii and phi cut-out
+// (UnplacedPolyhedron.cpp:75-103) behaves as the generic kernel with the shape's own flags.
+// The six entry points are out of line: they loop over faces and would otherwise be inlined
+// into every kernel that dispatches on the shape type.
+namespace ph = row;
+
+struct PhdSeg {
+  const double *outer, *phi, *inner;
+  int no, np, ni;
+};
+
+__device__ __forceinline__ PhdSeg phd_seg(const double *r, int si)
+{
+  const int nz = (int)r[ph::PhdNz], S = (int)r[ph::PhdSides];
+  const double *st = r + ph::phd_segs(nz, S) + 4 * si;
+  PhdSeg s;
+  s.no    = (int)st[0];
+  s.np    = (int)st[1];
+  s.ni    = (int)st[2];
+  s.outer = r + (int64_t)st[3];
+  s.phi   = s.outer + s.no * ph::kQuadSize;
+  s.inner = s.phi + s.np * ph::kQuadSize;
+  return s;
+}
+
+__device__ __forceinline__ bool phd_has_phi(const double *r) { return VGN_SECTIONS && r[ph::PhdHasPhi] != 0.; }
+__device__ __forceinline__ D3 quad_n(const double *q) { return d3(q[ph::QuadN], q[ph::QuadN + 1], q[ph::QuadN + 2]); }
+__device__ __forceinline__ D3 quad_side(const double *q, int j)
+{
+  return d3(q[ph::QuadSide + 4 * j], q[ph::QuadSide + 4 * j + 1], q[ph::QuadSide + 4 * j + 2]);
+}
+__device__ __forceinline__ D3 quad_corner(const double *q, int j)
+{
+  return d3(q[ph::QuadCorner + 3 * j], q[ph::QuadCorner + 3 * j + 1], q[ph::QuadCorner + 3 * j + 2]);
+}
+
+// Quadrilaterals::RayHitsQuadrilateral (Quadrilaterals.h:139-150)
+__device__ __forceinline__ bool quad_ray_hits(const double *q, D3 x)
+{
+  for (int j = 0; j < 4; ++j)
+    if (!(dot3(x, quad_side(q, j)) + q[ph::QuadSide + 4 * j + 3] >= -kTolerance)) return false;
+  return true;
+}
+
+// Quadrilaterals::DistanceToIn<double, behindPlanesT> (Quadrilaterals.h:361-396)
+template <bool BEHIND>
+__device__ __forceinline__ double quads_dist_in(const double *q, int n, D3 p, D3 d)
+{
+  double best = kInfLength;
+  for (int i = 0; i < n; ++i, q += ph::kQuadSize) {
+    const D3 nn = quad_n(q);
+    double dist = dot3(p, nn) + q[ph::QuadD];
+    if (!((BEHIND ? -dist : dist) > -kTolerance)) continue;
+    const double proj = dot3(d, nn);
+    if (!((BEHIND ? proj : -proj) > 0)) continue;
+    dist /= -(proj + copysign(1E-20, proj));
+    if (quad_ray_hits(q, d3(p.x + dist * d.x, p.y + dist * d.y, p.z + dist * d.z))) best = dist;
+    if (best < kInfLength) break;
+  }
+  return 0. > best ? 0. : best;
+}
+
+// Quadrilaterals::DistanceToOut(point, direction, zMin, zMax) (Quadrilaterals.h:466-516)
+__device__ __forceinline__ double quads_dist_out(const double *q, int n, D3 p, D3 d, double zMin, double zMax)
+{
+  double best = kInfLength;
+  for (int i = 0; i < n; ++i, q += ph::kQuadSize) {
+    const D3 nn = quad_n(q);
+    double dt   = dot3(p, nn) + q[ph::QuadD];
+    if (!(dt < kTolerance)) continue;
+    const double proj = dot3(d, nn);
+    if (!(proj > 0)) continue;
+    dt /= -proj;
+    if (!(dt < best)) continue;
+    bool valid;
+    if (zMin == zMax) {
+      valid = quad_ray_hits(q, d3(p.x + dt * d.x, p.y + dt * d.y, p.z + dt * d.z));
+    } else {
+      const double zp = p.z + dt * d.z;
+      valid           = (zp >= zMin - kTolerance) && (zp < zMax + kTolerance);
+    }
+    if (!valid) continue;
+    best = dt;
+  }
+  if (best > -kTolerance) best = best > 0. ? best : 0.;
+  return best;
+}
+
+__device__ __forceinline__ double mag2_3(D3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+
+// DistanceToLineSegmentSquared1 (GenericKernels.h:188-215)
+__device__ __forceinline__ double phd_segment_dist2(D3 c0, D3 c1, D3 p)
+{
+  double result = kInfLength;
+  const D3 line = d3(c1.x - c0.x, c1.y - c0.y, c1.z - c0.z);
+  const D3 pc0  = d3(p.x - c0.x, p.y - c0.y, p.z - c0.z);
+  const double dot0 = dot3(pc0, line);
+  if (dot0 <= 0) return mag2_3(pc0);
+  const double dot1 = mag2_3(line);
+  if (dot1 <= dot0) result = mag2_3(d3(p.x - c1.x, p.y - c1.y, p.z - c1.z));
+  if (result < kInfLength) return result;
+  const double f = dot0 / dot1;
+  return mag2_3(d3((c0.x + f * line.x) - p.x, (c0.y + f * line.y) - p.y, (c0.z + f * line.z) - p.z));
+}
+
+// Quadrilaterals::ScalarDistanceSquared (Quadrilaterals.h:535-572)
+__device__ __forceinline__ double quad_dist2(const double *q, D3 p)
+{
+  const D3 n      = quad_n(q);
+  double distance = dot3(p, n) + q[ph::QuadD];
+  const D3 x      = d3(p.x - distance * n.x, p.y - distance * n.y, p.z - distance * n.z);
+  bool within[4];
+  for (int j = 0; j < 4; ++j) {
+    const double *s = q + ph::QuadSide + 4 * j;
+    within[j]       = x.x * s[0] + x.y * s[1] + x.z * s[2] + s[3] >= 0;
+  }
+  if (within[0] && within[1] && within[2] && within[3]) return distance * distance;
+  double dsq = kInfLength;
+  for (int j = 0; j < 4; ++j) {
+    if (!within[j]) {
+      distance = phd_segment_dist2(quad_corner(q, j), quad_corner(q, (j + 1) % 4), p);
+      if (distance < dsq) dsq = distance;
+    }
+  }
+  return dsq;
+}
+
+// Planes::Contains (Planes.h:192-205)
+__device__ __forceinline__ bool quads_contains(const double *q, int n, D3 p)
+{
+  bool r = true;
+  for (int i = 0; i < n; ++i, q += ph::kQuadSize) r &= dot3(p, quad_n(q)) + q[ph::QuadD] < 0;
+  return r;
+}
+
+// Planes::Inside of one plane (Planes.h:268-281)
+__device__ __forceinline__ int quad_inside(const double *q, D3 p)
+{
+  const double dist = q[0] * p.x + q[1] * p.y + q[2] * p.z + q[ph::QuadD];
+  if (dist > kHalfTolerance) return kOutsideE;
+  if (dist > -kHalfTolerance) return kSurfaceE;
+  return kInsideE;
+}
+
+// Planes::Inside over all planes (Planes.h:246-266)
+__device__ __forceinline__ int quads_inside(const double *q, int n, D3 p)
+{
+  int r = kInsideE;
+  for (int i = 0; i < n; ++i, q += ph::kQuadSize) {
+    const double dist = q[0] * p.x + q[1] * p.y + q[2] * p.z + q[ph::QuadD];
+    if (dist > kHalfTolerance) r = kOutsideE;
+    if (r == kInsideE && dist > -kHalfTolerance) r = kSurfaceE;
+    if (r == kOutsideE) break;
+  }
+  return r;
+}
+
+// FindZSegmentKernel<double> (PolyhedronImplementation.h:232-244)
+__device__ __forceinline__ int phd_find_z(const double *r, double pz)
+{
+  const int nz    = (int)r[ph::PhdNz];
+  const double *z = r + ph::phd_z(nz);
+  int index = -1, b = 0;
+  while (b < nz - 1 && pz - kTolerance > z[b]) {
+    ++index;
+    ++b;
+  }
+  if (pz + kTolerance > z[b]) return index + 1;
+  return index;
+}
+
+// FindPhiSegment (PolyhedronImplementation.h:256-276)
+__device__ __forceinline__ int phd_find_phi(const double *r, D3 p)
+{
+  const int nz = (int)r[ph::PhdNz], S = (int)r[ph::PhdSides];
+  const double *s = r + ph::phd_phisec(nz);
+  int index       = -1;
+  double first    = p.x * s[0] + p.y * s[1] + p.z * s[2];
+  for (int i = 1; i < S + 1; ++i) {
+    const double second = p.x * s[3 * i] + p.y * s[3 * i + 1] + p.z * s[3 * i + 2];
+    if (first > -kTolerance && second < kTolerance) index = i - 1;
+    if (index >= 0) break;
+    first = second;
+  }
+  return index;
+}
+
+__device__ __forceinline__ int phd_clamp_z(const double *r, int z)
+{
+  const int zmax = (int)r[ph::PhdNz] - 1;
+  return z < 0 ? 0 : (z >= zmax ? zmax - 1 : z);
+}
+
+// DistanceToInZSegment (PolyhedronImplementation.h:278-318)
+__device__ __forceinline__ double phd_dist_in_seg(const double *r, int si, D3 p, D3 d)
+{
+  const PhdSeg sg = phd_seg(r, si);
+  double distance = quads_dist_in<false>(sg.outer, sg.no, p, d);
+  if (distance < kInfLength) return distance;
+  if (phd_has_phi(r)) distance = quads_dist_in<false>(sg.phi, sg.np, p, d);
+  if (distance < kInfLength) return distance;
+  if (sg.ni > 0) distance = quads_dist_in<true>(sg.inner, sg.ni, p, d);
+  return distance;
+}
+
+// DistanceToOutZSegment (PolyhedronImplementation.h:320-362)
+__device__ __forceinline__ double phd_dist_out_seg(const double *r, int si, double zMin, double zMax, D3 p, D3 d)
+{
+  const PhdSeg sg = phd_seg(r, si);
+  bool done       = false;
+  double distance = kInfLength;
+  if (sg.ni > 0) {
+    distance = quads_dist_in<false>(sg.inner, sg.ni, p, d);
+    done     = distance < kInfLength;
+    if (done) return distance;
+  }
+  if (phd_has_phi(r)) {
+    const double distphi = quads_dist_in<true>(sg.phi, sg.np, p, d);
+    if (!done && distance > -kTolerance) distance = distphi;
+    done = distance > -kTolerance && distance < kInfLength;
+    if (done) return distance;
+  }
+  const double distout = quads_dist_out(sg.outer, sg.no, p, d, zMin, zMax);
+  if (!done) distance = distout;
+  return distance;
+}
+
+// InPhiCutoutWedge (PolyhedronImplementation.h:541-555)
+__device__ __forceinline__ bool phd_in_cutout(const PhdSeg &sg, bool large, D3 p)
+{
+  const bool s0 = dot3(p, quad_n(sg.phi)) + sg.phi[ph::QuadD] >= 0;
+  const bool s1 = dot3(p, quad_n(sg.phi + ph::kQuadSize)) + sg.phi[ph::kQuadSize + ph::QuadD] >= 0;
+  return large ? (s0 || s1) : (s0 && s1);
+}
+
+// ScalarSafetyToZSegmentSquared (PolyhedronImplementation.h:364-466); `phiIndex` may move to
+// the first or last side, as in the reference
+__device__ __forceinline__ double phd_safety_seg2(const double *r, int si, int &phiIndex, D3 p, bool pt_inside)
+{
+  const PhdSeg sg      = phd_seg(r, si);
+  const int nz         = (int)r[ph::PhdNz];
+  const bool in_cutout = phiIndex < 0;
+  double s2            = kInfLength;
+  if (phd_has_phi(r) && sg.np == 2) {
+    if (pt_inside || in_cutout) {
+      s2               = quad_dist2(sg.phi, p);
+      const double saf = quad_dist2(sg.phi + ph::kQuadSize, p);
+      if (saf < s2) s2 = saf;
+      if (in_cutout) {
+        if (r[ph::PhdLargePhi] != 0. && sg.ni > 0) {
+          double si2 = quad_dist2(sg.inner, p);
+          if (si2 < s2) {
+            phiIndex = 0;
+            s2       = si2;
+          }
+          if (sg.ni > 1) {
+            si2 = quad_dist2(sg.inner + (sg.ni - 1) * ph::kQuadSize, p);
+            if (si2 < s2) {
+              phiIndex = sg.ni - 1;
+              s2       = si2;
+            }
+          }
+        }
+        return s2;
+      }
+    }
+  }
+  if (in_cutout && si > 0 && si < nz - 2 && r[ph::phd_z(nz) + si] == r[ph::phd_z(nz) + si + 1]) {
+    if (sg.no > 0) {
+      double so = quad_dist2(sg.outer, p);
+      if (so < s2) {
+        phiIndex = 0;
+        s2       = so;
+      }
+      if (sg.no > 1) {
+        so = quad_dist2(sg.outer + (sg.no - 1) * ph::kQuadSize, p);
+        if (so < s2) {
+          phiIndex = sg.no - 1;
+          s2       = so;
+        }
+      }
+    }
+    if (sg.ni > 0) {
+      double si2 = quad_dist2(sg.inner, p);
+      if (si2 < s2) {
+        phiIndex = 0;
+        s2       = si2;
+      }
+      if (sg.ni > 1) {
+        si2 = quad_dist2(sg.inner + (sg.ni - 1) * ph::kQuadSize, p);
+        if (si2 < s2) {
+          phiIndex = sg.ni - 1;
+          s2       = si2;
+        }
+      }
+    }
+    return s2;
+  }
+  const double so  = sg.no > 0 ? quad_dist2(sg.outer + phiIndex * ph::kQuadSize, p) : kInfLength;
+  const double si2 = sg.ni > 0 ? quad_dist2(sg.inner + phiIndex * ph::kQuadSize, p) : kInfLength;
+  if (si2 < s2) s2 = si2;
+  if (so < s2) s2 = so;
+  return s2;
+}
+
+// ScalarDistanceToEndcaps<pointInsideT> (PolyhedronImplementation.h:468-511)
+template <bool INSIDE>
+__device__ __forceinline__ void phd_dist_endcaps(const double *r, D3 p, D3 d, double &distance)
+{
+  const int nz = (int)r[ph::PhdNz], nseg = nz - 1;
+  const bool last     = INSIDE ? !(d.z < 0) : (d.z < 0);
+  const PhdSeg sg     = phd_seg(r, last ? nseg - 1 : 0);
+  const double zPlane = r[ph::phd_z(nz) + (last ? nseg : 0)];
+  const double dt     = (zPlane - p.z) / nonzero(d.z);
+  if (dt < -kTolerance || dt >= distance) return;
+  const D3 x = d3(p.x + dt * d.x, p.y + dt * d.y, p.z + dt * d.z);
+  if (!quads_contains(sg.outer, sg.no, x)) return;
+  if (sg.ni > 0 && quads_contains(sg.inner, sg.ni, x)) return;
+  if (phd_has_phi(r) && phd_in_cutout(sg, r[ph::PhdLargePhi] != 0., x)) return;
+  distance = dt;
+}
+
+// ScalarSafetyToEndcapsSquared (PolyhedronImplementation.h:513-539)
+__device__ __forceinline__ void phd_safety_endcaps2(const double *r, D3 p, double &dist2)
+{
+  const int nz = (int)r[ph::PhdNz], nseg = nz - 1;
+  const double first  = r[ph::phd_z(nz)] - p.z;
+  const double lastd  = r[ph::phd_z(nz) + nseg] - p.z;
+  const bool isFirst  = fabs(first) < fabs(lastd);
+  const PhdSeg sg     = phd_seg(r, isFirst ? 0 : nseg - 1);
+  const double dt     = isFirst ? first : lastd;
+  const double dt2    = dt * dt;
+  if (dt2 >= dist2) return;
+  const D3 x = d3(p.x, p.y, p.z + dt);
+  if (!quads_contains(sg.outer, sg.no, x)) return;
+  if (sg.ni > 0 && quads_contains(sg.inner, sg.ni, x)) return;
+  if (phd_has_phi(r) && phd_in_cutout(sg, r[ph::PhdLargePhi] != 0., x)) return;
+  dist2 = dt2;
+}
+
+// Wedge::Inside (Wedge_Evolution.h:262-272)
+__device__ __forceinline__ int phd_wedge_inside(const double *w, D3 p)
+{
+  bool cin = false, cout = false;
+  wedge_ci<true>(w, p, cin, cout);
+  return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+}
+
+// ScalarInsideSegBorder (PolyhedronImplementation.h:628-664)
+__device__ __forceinline__ int phd_inside_border(const double *r, D3 p, int zi)
+{
+  const int nz = (int)r[ph::PhdNz];
+  const PhdSeg sg    = phd_seg(r, zi);
+  const int phiIndex = phd_find_phi(r, p);
+  if (phiIndex < 0) return kOutsideE;
+  const double *q  = (sg.no ? sg.outer : sg.inner) + phiIndex * ph::kQuadSize;
+  const double rr  = fabs(dot3(p, quad_side(q, 0)));
+  const double *rn = r + ph::phd_rmin(nz), *rx = r + ph::phd_rmax(nz);
+  const bool in1   = (rr > rn[zi] - kTolerance) && (rr < rx[zi] + kTolerance);
+  const bool in2   = (rr > rn[zi + 1] - kTolerance) && (rr < rx[zi + 1] + kTolerance);
+  if (in1 && in2) {
+    if ((rr < rn[zi] + kTolerance) || (rr > rx[zi] - kTolerance) || (rr < rn[zi + 1] + kTolerance) ||
+        (rr > rx[zi + 1] - kTolerance))
+      return kSurfaceE;
+    if (phd_has_phi(r)) return phd_wedge_inside(r + ph::PhdWedge, p);
+    return kInsideE;
+  }
+  if (!in1 && !in2) return kOutsideE;
+  return kSurfaceE;
+}
+
+// ScalarInsideSegPhi (PolyhedronImplementation.h:666-701)
+__device__ __forceinline__ int phd_inside_seg_phi(const double *r, D3 p, int zi, int phiIndex)
+{
+  if (phiIndex < 0) return kOutsideE;
+  const int nz    = (int)r[ph::PhdNz];
+  const double dz = fabs(p.z - r[ph::PhdTubeOffset]) - 0.5 * (r[ph::phd_z(nz) + nz - 1] - r[ph::phd_z(nz)]);
+  if (dz > kHalfTolerance) return kOutsideE;
+  if (r[ph::phd_samez(nz) + zi] != 0.) return phd_inside_border(r, p, zi);
+  const PhdSeg sg = phd_seg(r, zi);
+  int res         = quad_inside(sg.outer + phiIndex * ph::kQuadSize, p);
+  if (res != kInsideE) return res;
+  if (sg.ni > 0) {
+    res = quad_inside(sg.inner + phiIndex * ph::kQuadSize, p);
+    if (res == kInsideE) return kOutsideE;
+    if (res == kSurfaceE) return kSurfaceE;
+  }
+  if (phd_has_phi(r)) {
+    res = phd_wedge_inside(r + ph::PhdWedge, p);
+    if (res != kInsideE) return res;
+  }
+  if (fabs(dz) < kHalfTolerance) return kSurfaceE;
+  return kInsideE;
+}
+
+// ScalarContainsKernel (PolyhedronImplementation.h:557-592)
+__device__ __noinline__ bool polyhedron_contains(const double *r, D3 p)
+{
+  if (!tube_contains(r + ph::PhdTube, d3(p.x, p.y, p.z - r[ph::PhdTubeOffset]))) return false;
+  const int nz = (int)r[ph::PhdNz];
+  const int zi = phd_find_z(r, p.z);
+  if (!(zi >= 0 && zi < nz - 1)) return false;
+  const PhdSeg sg = phd_seg(r, zi);
+  if (r[ph::phd_samez(nz) + zi] != 0.) {
+    const int phiIndex = phd_find_phi(r, p);
+    if (phiIndex < 0) return false;
+    const double *q  = (sg.no ? sg.outer : sg.inner) + phiIndex * ph::kQuadSize;
+    const double rr  = fabs(dot3(p, quad_side(q, 0)));
+    const double *rn = r + ph::phd_rmin(nz), *rx = r + ph::phd_rmax(nz);
+    return ((rr >= rn[zi]) && (rr <= rx[zi])) | ((rr >= rn[zi + 1]) && (rr <= rx[zi + 1]));
+  }
+  if (!quads_contains(sg.outer, sg.no, p)) return false;
+  if (sg.ni > 0 && quads_contains(sg.inner, sg.ni, p)) return false;
+  if (phd_has_phi(r) && !quads_contains(sg.phi, sg.np, p)) return false;
+  return true;
+}
+
+// ScalarInsideKernel (PolyhedronImplementation.h:594-626)
+__device__ __forceinline__ int polyhedron_inside_kernel(const double *r, D3 p)
+{
+  if (!tube_contains(r + ph::PhdTube, d3(p.x, p.y, p.z - r[ph::PhdTubeOffset]))) return kOutsideE;
+  const int nz = (int)r[ph::PhdNz];
+  int zi       = phd_find_z(r, p.z);
+  if (zi > nz - 2) zi = nz - 2;
+  if (zi < 0) zi = 0;
+  if (r[ph::phd_samez(nz) + zi] != 0.) return phd_inside_border(r, p, zi);
+  const PhdSeg sg = phd_seg(r, zi);
+  int res         = quads_inside(sg.outer, sg.no, p);
+  if (res != kInsideE) return res;
+  if (sg.ni > 0) {
+    res = quads_inside(sg.inner, sg.ni, p);
+    if (res == kInsideE) return kOutsideE;
+    if (res == kSurfaceE) return kSurfaceE;
+  }
+  if (phd_has_phi(r)) {
+    res = quads_inside(sg.phi, sg.np, p);
+    if (res != kInsideE) return res;
+  }
+  const double dz =
+      fabs(fabs(p.z - r[ph::PhdTubeOffset]) - 0.5 * (r[ph::phd_z(nz) + nz - 1] - r[ph::phd_z(nz)]));
+  if (dz < kTolerance) return kSurfaceE;
+  return kInsideE;
+}
+
+__device__ __noinline__ int polyhedron_inside(const double *r, D3 p) { return polyhedron_inside_kernel(r, p); }
+
+// ScalarDistanceToInKernel (PolyhedronImplementation.h:703-751)
+__device__ __noinline__ double polyhedron_dist_in(const double *r, D3 p, D3 d)
+{
+  const int nz = (int)r[ph::PhdNz], nseg = nz - 1;
+  const double *z = r + ph::phd_z(nz);
+  if ((p.z < z[0] + kTolerance) && d.z <= 0) return kInfLength;
+  if ((p.z > z[nseg] - kTolerance) && d.z >= 0) return kInfLength;
+  if (polyhedron_inside_kernel(r, p) == kInsideE) return -1.;
+  double tubeDistance = 0., distance = kInfLength;
+  const D3 bp = d3(p.x, p.y, p.z - r[ph::PhdTubeOffset]);
+  if (!tube_contains(r + ph::PhdTube, bp)) {
+    tubeDistance = tube_dist_in(r + ph::PhdTube, bp, d);
+    if (tubeDistance == kInfLength) return kInfLength;
+  }
+  int zi = phd_clamp_z(r, phd_find_z(r, p.z));
+  if (d.z >= 0) {
+    for (; zi < nseg; ++zi) {
+      distance = phd_dist_in_seg(r, zi, p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+    }
+  } else {
+    for (; zi >= 0; --zi) {
+      distance = phd_dist_in_seg(r, zi, p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+    }
+  }
+  phd_dist_endcaps<false>(r, p, d, distance);
+  return (distance >= tubeDistance - 1E-6) ? distance : kInfLength;
+}
+
+// ScalarDistanceToOutKernel (PolyhedronImplementation.h:868-914)
+__device__ __noinline__ double polyhedron_dist_out(const double *r, D3 p, D3 d)
+{
+  const int nz = (int)r[ph::PhdNz], nseg = nz - 1;
+  const double *z = r + ph::phd_z(nz);
+  if ((p.z < z[0] - kTolerance) || (p.z > z[nseg] + kTolerance)) return -1.;
+  if (polyhedron_inside_kernel(r, p) == kOutsideE) return -1.;
+  double distance = kInfLength;
+  int zi          = phd_clamp_z(r, phd_find_z(r, p.z));
+  if (d.z >= 0) {
+    for (; zi < nseg; ++zi) {
+      distance = phd_dist_out_seg(r, zi, z[zi], z[zi + 1], p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+      if (z[zi] - p.z > distance) break;
+    }
+  } else {
+    for (; zi >= 0; --zi) {
+      distance = phd_dist_out_seg(r, zi, z[zi], z[zi + 1], p, d);
+      if (distance >= 0 && distance < kInfLength) break;
+      if (p.z - z[zi] > distance) break;
+    }
+  }
+  phd_dist_endcaps<true>(r, p, d, distance);
+  if (distance >= kInfLength) distance = 0.;
+  return distance;
+}
+
+// ScalarSafetyKernel (PolyhedronImplementation.h:753-800)
+__device__ __noinline__ double polyhedron_safety(const double *r, D3 p, bool pt_inside)
+{
+  const int nz = (int)r[ph::PhdNz], nseg = nz - 1;
+  const double *z = r + ph::phd_z(nz);
+  double safety   = kInfLength;
+  const int zi    = phd_clamp_z(r, phd_find_z(r, p.z));
+  int phiIndex    = phd_find_phi(r, p);
+  const int in    = phd_inside_seg_phi(r, p, zi, phiIndex);
+  if (in == kSurfaceE) return 0.;
+  if ((in == kInsideE) ^ pt_inside) return -1.;
+  for (int k = zi; k < nseg;) {
+    const double s = phd_safety_seg2(r, k, phiIndex, p, pt_inside);
+    safety         = safety < s ? safety : s;
+    ++k;
+    const double dz = z[k] - p.z;
+    if (dz * dz > safety) break;
+  }
+  for (int k = zi - 1; k >= 0; --k) {
+    const double s = phd_safety_seg2(r, k, phiIndex, p, pt_inside);
+    safety         = safety < s ? safety : s;
+    const double dz = p.z - z[k];
+    if (dz * dz > safety) break;
+  }
+  phd_safety_endcaps2(r, p, safety);
+  return sqrt(safety);
+}
+
 // ---------------------------------------------------------------- dispatch (primitive shapes)
 // `stepmax` is the step the caller still accepts; of the primitives only the cut tube's DistanceToIn
 // reads it (booleans hand it to their operands)
@@ -2494,6 +3027,7 @@ __device__ __forceinline__ double prim_dist_in(int type, const double *r, D3 p, 
   case kPolycone: return pcon_dist_in(r, p, d);
   case kOrb: return orb_dist_in(r, p, d);
   case kCutTube: return cuttube_dist_in(r, p, d, stepmax);
+  case kPolyhedron: return polyhedron_dist_in(r, p, d);
   }
   return kInfLength;
 }
@@ -2510,6 +3044,7 @@ __device__ __forceinline__ double prim_dist_out(int type, const double *r, D3 p,
   case kPolycone: return pcon_dist_out(r, p, d);
   case kOrb: return orb_dist_out(r, p, d);
   case kCutTube: return cuttube_dist_out(r, p, d);
+  case kPolyhedron: return polyhedron_dist_out(r, p, d);
   }
   return -1.;
 }
@@ -2526,6 +3061,7 @@ __device__ __forceinline__ double prim_safe_in(int type, const double *r, D3 p)
   case kPolycone: return pcon_safe_in(r, p);
   case kOrb: return orb_safe_in(r, p);
   case kCutTube: return cuttube_safe_in(r, p);
+  case kPolyhedron: return polyhedron_safety(r, p, false);
   }
   return kInfLength;
 }
@@ -2542,6 +3078,7 @@ __device__ __forceinline__ double prim_safe_out(int type, const double *r, D3 p)
   case kPolycone: return pcon_safe_out(r, p);
   case kOrb: return orb_safe_out(r, p);
   case kCutTube: return cuttube_safe_out(r, p);
+  case kPolyhedron: return polyhedron_safety(r, p, true);
   }
   return 0.;
 }
@@ -2558,6 +3095,7 @@ __device__ __forceinline__ bool prim_contains(int type, const double *r, D3 p)
   case kPolycone: return pcon_contains(r, p);
   case kOrb: return orb_contains(r, p);
   case kCutTube: return cuttube_contains(r, p);
+  case kPolyhedron: return polyhedron_contains(r, p);
   }
   return false;
 }
@@ -2574,6 +3112,7 @@ __device__ __forceinline__ int prim_inside(int type, const double *r, D3 p)
   case kPolycone: return pcon_inside(r, p);
   case kOrb: return orb_inside(r, p);
   case kCutTube: return cuttube_inside(r, p);
+  case kPolyhedron: return polyhedron_inside(r, p);
   }
   return kOutsideE;
 }

@@ -22,8 +22,9 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE, BOOLEAN = range(10)
-SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb", "cuttube", "boolean"]
+BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE, BOOLEAN, POLYHEDRON = range(11)
+SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb", "cuttube", "boolean",
+               "polyhedron"]
 UNION, INTERSECTION, SUBTRACTION = 0, 1, 2  # boolean operations (BooleanStruct.h:9)
 BOOLEAN_OPERAND = -2  # pv_mother of a boolean's operand placement
 
@@ -420,7 +421,7 @@ def uniform_tracks(n: int, half: float, seed_points: int, seed_dirs: int, step_l
 # The shape types of the 8192-daughter mixed-shape benchmark geometry (its definition: seven
 # types), and every shape type the library implements (for parity geometries).
 IMPLEMENTED_SHAPES = (BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE)
-ALL_SHAPES = IMPLEMENTED_SHAPES + (ORB, CUTTUBE)
+ALL_SHAPES = IMPLEMENTED_SHAPES + (ORB, CUTTUBE, POLYHEDRON)
 
 
 def cuttube_params(rmin, rmax, dz, sphi, dphi, thb, phib, tht, phit):
@@ -516,12 +517,24 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
         thb, tht = K_PI - float(rng.uniform(0.0, 0.6)), float(rng.uniform(0.0, 0.6))
         phib, phit = (float(v) for v in rng.uniform(0.0, K_TWO_PI, 2))
         return cuttube_params(rmin, rmax, dz, sphi, dphi, thb, phib, tht, phit), np.array([rmax, rmax, dz + 0.7 * rmax])
+    if shape == POLYHEDRON:  # four z planes, 3 to 8 sides; radii are to the sides' middles
+        h = u()
+        z = [-h] + sorted(float(v) for v in rng.uniform(-h, h, 2)) + [h]
+        rmax = [u() for _ in range(4)]
+        solid = rng.uniform() < 0.5
+        rmin = [0.0 if solid else float(rng.uniform(0.0, 0.8)) * r for r in rmax]
+        sides = int(rng.integers(3, 9))
+        sphi, dphi = 0.0, K_TWO_PI
+        if sections and rng.uniform() < 0.75:
+            sphi, dphi = float(rng.uniform(-K_PI, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+        rc = max(rmax) / math.cos(0.5 * dphi / sides)
+        return (sphi, dphi, float(sides), 4.0, *z, *rmin, *rmax), np.array([rc, rc, h])
     raise ValueError(f"shape {shape} not implemented")
 
 
 _LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
                    TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15)), ORB: (0,),
-                   CUTTUBE: (0, 1, 2)}
+                   CUTTUBE: (0, 1, 2), POLYHEDRON: tuple(range(4, 16))}
 
 
 def shape_bbox(shape: int, params):
@@ -533,6 +546,11 @@ def shape_bbox(shape: int, params):
         nz = int(params[2])
         z = np.asarray(params[3:3 + nz])
         r = float(max(params[3 + 2 * nz:3 + 3 * nz]))
+        return np.array([-r, -r, z.min()]), np.array([r, r, z.max()])
+    if shape == POLYHEDRON:  # corners lie at rmax / cos(half the side angle)
+        nz, sides = int(params[3]), float(params[2])
+        z = np.asarray(params[4:4 + nz])
+        r = float(max(params[4 + 2 * nz:4 + 3 * nz])) / math.cos(0.5 * min(float(params[1]), K_TWO_PI) / sides)
         return np.array([-r, -r, z.min()]), np.array([r, r, z.max()])
     if shape == CUTTUBE:  # the cut planes tilt the end faces
         h = float(params[1]) + float(params[2])
