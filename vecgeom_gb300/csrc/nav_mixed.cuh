@@ -788,9 +788,41 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
   const NodeRec *nodes    = g.nodes + lv.nodes_off;
   const PrimRec *prims    = g.prims + lv.prims_off;
   stack[0]                = stack_entry(0u, inode_range(inodes, 0u));
+  bool ok                 = true;
   do {
-    int nchild, off;
-    const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
+    // Inner nodes first: every lane descends until it holds a leaf or its stack runs empty,
+    // so that the lanes of a warp reach the leaf code (the costly part) together.  Each lane
+    // visits its nodes in the same order as before; only the interleaving across lanes changes.
+    int nchild = -1, off = 0;
+    while (sp > 0) {
+      const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
+      if (nchild >= 0) break;
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      const unsigned eL = stack_entry(L, inode_range(inodes, L)), eR = stack_entry(R, inode_range(inodes, R));
+      const FI sL = isafety(isafe_n[L], r);
+      const FI sR = isafety(isafe_n[R], r);
+      const bool trL = saferun_less(g, r, s, sL, [&] { return box_safety(nodes[L].mn, nodes[L].mx, r.lp); });
+      const bool trR = saferun_less(g, r, s, sR, [&] { return box_safety(nodes[R].mn, nodes[R].mx, r.lp); });
+      bool rfirst    = false;
+      if (trL && trR) {
+        const int o = fi_lt(sR, sL);
+        rfirst = o == kMaybe ? box_safety(nodes[R].mn, nodes[R].mx, r.lp) < box_safety(nodes[L].mn, nodes[L].mx, r.lp)
+                             : o == kYes;
+      }
+      if (sp + 2 > g.stack_limit) {
+        raise_error(g, kErrStack);
+        ok = false;
+        break;
+      }
+      if (rfirst) {
+        if (trR) stack[sp++] = eR;
+        if (trL) stack[sp++] = eL;
+      } else {
+        if (trL) stack[sp++] = eL;
+        if (trR) stack[sp++] = eR;
+      }
+    }
+    if (!ok) break;
     if (nchild >= 0) {
       for (int i = 0; i < nchild; ++i) {
         // cheapest test first: the primitive's box safety against the running minimum
@@ -819,30 +851,6 @@ __device__ __forceinline__ double bvh_safety_mixed(const GeomView &g, const LVRe
           }
           saferun_update(s);
         }
-      }
-    } else {
-      const unsigned L = 2 * id + 1, R = 2 * id + 2;
-      const unsigned eL = stack_entry(L, inode_range(inodes, L)), eR = stack_entry(R, inode_range(inodes, R));
-      const FI sL = isafety(isafe_n[L], r);
-      const FI sR = isafety(isafe_n[R], r);
-      const bool trL = saferun_less(g, r, s, sL, [&] { return box_safety(nodes[L].mn, nodes[L].mx, r.lp); });
-      const bool trR = saferun_less(g, r, s, sR, [&] { return box_safety(nodes[R].mn, nodes[R].mx, r.lp); });
-      bool rfirst    = false;
-      if (trL && trR) {
-        const int o = fi_lt(sR, sL);
-        rfirst = o == kMaybe ? box_safety(nodes[R].mn, nodes[R].mx, r.lp) < box_safety(nodes[L].mn, nodes[L].mx, r.lp)
-                             : o == kYes;
-      }
-      if (sp + 2 > g.stack_limit) {
-        raise_error(g, kErrStack);
-        break;
-      }
-      if (rfirst) {
-        if (trR) stack[sp++] = eR;
-        if (trL) stack[sp++] = eL;
-      } else {
-        if (trL) stack[sp++] = eL;
-        if (trR) stack[sp++] = eR;
       }
     }
   } while (sp > 0);
