@@ -64,7 +64,8 @@ enum vgn_shape_type {
  *    kept) is used by exactly one boolean;
  *  - an operand's logical volume has a smaller index than its boolean, has no daughters, and
  *    is a primitive shape or a boolean of primitive shapes (two levels at most).
- * A geometry holding booleans may hold no phi or theta section (VGN_ERR_UNSUPPORTED).
+ * A geometry holding booleans may hold no phi or theta section and no polyhedron
+ * (VGN_ERR_UNSUPPORTED).
  * vgn_shape_batch with VGN_OP_INSIDE on a union is VGN_ERR_UNSUPPORTED (its surface case takes
  * the operands' normals, which the library does not compute); every navigation call works. */
 #define VGN_BOOLEAN_OPERAND (-2)

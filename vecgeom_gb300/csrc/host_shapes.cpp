@@ -683,7 +683,7 @@ bool shape_row_has_sections(int32_t type, const double *r)
     return r[row::pcon_cone(n, 0) + row::ConeDPhi] < 2. * kPi;
   }
   case kSphere: return r[row::SphFull] == 0.;
-  case kPolyhedron: return r[row::PhdHasPhi] != 0.;
+  case kPolyhedron: return true;  // its kernels live in the sections set only
   case kBoolean:  // the operands' (once linked)
     return (r[row::BoolLeftType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolLeftType], r + (int64_t)r[row::BoolLeftRow])) ||
            (r[row::BoolRightType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolRightType], r + (int64_t)r[row::BoolRightRow]));

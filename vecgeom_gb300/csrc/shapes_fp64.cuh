@@ -2484,7 +2484,10 @@ __device__ __forceinline__ double cuttube_safe_out(const double *r, D3 p)
 // The reference's placement specialisation by inner radii and phi cut-out
 // (UnplacedPolyhedron.cpp:75-103) behaves as the generic kernel with the shape's own flags.
 // The six entry points are out of line: they loop over faces and would otherwise be inlined
-// into every kernel that dispatches on the shape type.
+// into every kernel that dispatches on the shape type.  Compiled in the sections kernel set
+// only (a geometry holding a polyhedron runs that set): the calls' register saves would
+// otherwise cost the full-range kernels spills.
+#if VGN_SECTIONS
 namespace ph = row;
 
 struct PhdSeg {
@@ -2506,7 +2509,7 @@ __device__ __forceinline__ PhdSeg phd_seg(const double *r, int si)
   return s;
 }
 
-__device__ __forceinline__ bool phd_has_phi(const double *r) { return VGN_SECTIONS && r[ph::PhdHasPhi] != 0.; }
+__device__ __forceinline__ bool phd_has_phi(const double *r) { return r[ph::PhdHasPhi] != 0.; }
 __device__ __forceinline__ D3 quad_n(const double *q) { return d3(q[ph::QuadN], q[ph::QuadN + 1], q[ph::QuadN + 2]); }
 __device__ __forceinline__ D3 quad_side(const double *q, int j)
 {
@@ -3011,6 +3014,7 @@ __device__ __noinline__ double polyhedron_safety(const double *r, D3 p, bool pt_
   phd_safety_endcaps2(r, p, safety);
   return sqrt(safety);
 }
+#endif  // VGN_SECTIONS
 
 // ---------------------------------------------------------------- dispatch (primitive shapes)
 // `stepmax` is the step the caller still accepts; of the primitives only the cut tube's DistanceToIn
@@ -3027,7 +3031,9 @@ __device__ __forceinline__ double prim_dist_in(int type, const double *r, D3 p, 
   case kPolycone: return pcon_dist_in(r, p, d);
   case kOrb: return orb_dist_in(r, p, d);
   case kCutTube: return cuttube_dist_in(r, p, d, stepmax);
+#if VGN_SECTIONS
   case kPolyhedron: return polyhedron_dist_in(r, p, d);
+#endif
   }
   return kInfLength;
 }
@@ -3044,7 +3050,9 @@ __device__ __forceinline__ double prim_dist_out(int type, const double *r, D3 p,
   case kPolycone: return pcon_dist_out(r, p, d);
   case kOrb: return orb_dist_out(r, p, d);
   case kCutTube: return cuttube_dist_out(r, p, d);
+#if VGN_SECTIONS
   case kPolyhedron: return polyhedron_dist_out(r, p, d);
+#endif
   }
   return -1.;
 }
@@ -3061,7 +3069,9 @@ __device__ __forceinline__ double prim_safe_in(int type, const double *r, D3 p)
   case kPolycone: return pcon_safe_in(r, p);
   case kOrb: return orb_safe_in(r, p);
   case kCutTube: return cuttube_safe_in(r, p);
+#if VGN_SECTIONS
   case kPolyhedron: return polyhedron_safety(r, p, false);
+#endif
   }
   return kInfLength;
 }
@@ -3078,7 +3088,9 @@ __device__ __forceinline__ double prim_safe_out(int type, const double *r, D3 p)
   case kPolycone: return pcon_safe_out(r, p);
   case kOrb: return orb_safe_out(r, p);
   case kCutTube: return cuttube_safe_out(r, p);
+#if VGN_SECTIONS
   case kPolyhedron: return polyhedron_safety(r, p, true);
+#endif
   }
   return 0.;
 }
@@ -3095,7 +3107,9 @@ __device__ __forceinline__ bool prim_contains(int type, const double *r, D3 p)
   case kPolycone: return pcon_contains(r, p);
   case kOrb: return orb_contains(r, p);
   case kCutTube: return cuttube_contains(r, p);
+#if VGN_SECTIONS
   case kPolyhedron: return polyhedron_contains(r, p);
+#endif
   }
   return false;
 }
@@ -3112,7 +3126,9 @@ __device__ __forceinline__ int prim_inside(int type, const double *r, D3 p)
   case kPolycone: return pcon_inside(r, p);
   case kOrb: return orb_inside(r, p);
   case kCutTube: return cuttube_inside(r, p);
+#if VGN_SECTIONS
   case kPolyhedron: return polyhedron_inside(r, p);
+#endif
   }
   return kOutsideE;
 }
