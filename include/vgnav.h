@@ -49,11 +49,13 @@ enum vgn_shape_type {
   VGN_BOOLEAN   = 9, /* params: op (VGN_BOOL_UNION / _INTERSECTION / _SUBTRACTION), left operand,
                         right operand: ids of placed volumes whose mother is VGN_BOOLEAN_OPERAND
                         (UnplacedBooleanVolume.h:59, BooleanStruct.h:23-25)        */
-  VGN_POLYHEDRON = 10 /* params: sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz]; radii are to
+  VGN_POLYHEDRON = 10, /* params: sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz]; radii are to
                         the sides' middles (UnplacedPolyhedron.h:97-108).  Refused where the
                         reference reads past its arrays: a zero-length first or last segment,
                         three equal z planes in a row, a zero-length segment with equal radii,
                         a face with fewer than three distinct corners, dphi / sides >= pi */
+  VGN_TORUS2    = 11  /* params: rmin, rmax, rtor, sphi, dphi with 0 <= rmin < rmax < rtor
+                        (UnplacedTorus2.h:64-65)                                     */
 };
 
 /* Boolean solids (VGN_BOOLEAN).  The operands are placements of other logical volumes
@@ -64,7 +66,7 @@ enum vgn_shape_type {
  *    kept) is used by exactly one boolean;
  *  - an operand's logical volume has a smaller index than its boolean, has no daughters, and
  *    is a primitive shape or a boolean of primitive shapes (two levels at most).
- * A geometry holding booleans may hold no phi or theta section and no polyhedron
+ * A geometry holding booleans may hold no phi or theta section, polyhedron or torus
  * (VGN_ERR_UNSUPPORTED).
  * vgn_shape_batch with VGN_OP_INSIDE on a union is VGN_ERR_UNSUPPORTED (its surface case takes
  * the operands' normals, which the library does not compute); every navigation call works. */

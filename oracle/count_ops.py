@@ -34,7 +34,7 @@ WEIGHTS = {
     "prim_contains": 6,   # AABB::Contains (AABB.h:205-210)
     "transforms": 33,     # Transformation3D point + direction (Transformation3D.h:663-673, 729-770)
 }
-# per shape (Box, Tube, Cone, Trd, Trapezoid, Sphere, Polycone, Orb, CutTube, Boolean, Polyhedron)
+# per shape (Box, Tube, Cone, Trd, Trapezoid, Sphere, Polycone, Orb, CutTube, Boolean, Polyhedron, Torus2)
 # and operation
 # (DistanceToIn, DistanceToOut, SafetyToIn, SafetyToOut, Contains, Inside)
 KERNEL_WEIGHTS = [
@@ -51,6 +51,7 @@ KERNEL_WEIGHTS = [
                                   # (the operands' own kernels are counted under their shapes)
     [400, 300, 200, 200, 60, 70], # PolyhedronImplementation.h:598-800 (bounding tube, z segments of eight
                                   # quadrilateral faces, end caps)
+    [600, 500, 12, 12, 10, 12],   # TorusImplementation2.h:158-509 (quartic solver and Newton refinement)
 ]
 
 

@@ -270,6 +270,7 @@ static int shape_nparams(int type, const double *p, int avail)
   case OR_SPHERE: return 6;
   case OR_ORB: return 1;
   case OR_CUTTUBE: return 11;
+  case OR_TORUS: return 5;
   case OR_BOOLEAN: return 3; /* op, left operand placement, right operand placement */
   case OR_POLYCONE: { /* sphi, dphi, nz, z[nz], rmin[nz], rmax[nz] */
     int nz;

@@ -182,6 +182,12 @@ typedef struct { /* PolyhedronStruct.h:52-80 */
   double btubeOffset;                  /* fBoundingTubeOffset */
 } or_polyhedron;
 
+typedef struct { /* TorusStruct2.h:22-32 */
+  double rmin, rmax, rtor, sphi, dphi, rmin2, rmax2, rtor2;
+  or_wedge w;     /* fPhiWedge(dphi, sphi) */
+  or_tube btube;  /* fBoundingTube */
+} or_torus;
+
 struct or_lv_s;
 typedef struct { /* BooleanStruct (BooleanStruct.h:23-25): the operation and the two placed operands */
   int op;                             /* 0 union, 1 intersection, 2 subtraction (BooleanStruct.h:9) */
@@ -208,6 +214,7 @@ typedef struct or_lv_s {
     or_cuttube ctube;
     or_boolean boo;
     or_polyhedron phd;
+    or_torus tor;
   } s;
   v3 bbox_min, bbox_max; /* VUnplacedVolume::fBBox: the shape's Extent (UnplacedVolume.h:45, 76-80) */
   /* BVH (BVH.h:364-370), present when nd > 0 */

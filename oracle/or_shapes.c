@@ -3700,6 +3700,466 @@ static void polyhedron_extent(const or_polyhedron *t, v3 *mn, v3 *mx)
   *mx = v3_make(b[0], b[1], b[2]);
 }
 
+/* ================================================================== */
+/* Torus2: TorusStruct2.h, kernel/TorusImplementation2.h              */
+/* ================================================================== */
+
+/* Elementary functions of the torus' cubic solver, written out so that this restatement and
+ * the GPU kernels evaluate them with the same IEEE operations (+, -, *, /, sqrt): the reference
+ * calls the C library's cbrt, pow, cos and atan2, which round differently from CUDA's.  Each is
+ * within a few units in the last place of the exact value; the oracle therefore equals the
+ * reference build to about 1e-15 relative in the cubic's root, not bit for bit. */
+
+/* cube root of a >= 0: a = m 2^(3q), m in [0.5, 4); Newton's iteration y <- (2 y + m / y^2) / 3
+ * from a linear start, six steps (quadratic convergence from 15 % error) */
+static double tor_cbrt(double a)
+{
+  int e, r, k;
+  double m, y;
+  if (a == 0.0 || !(a < kInfLength)) return a;
+  m = frexp(a, &e);
+  r = e % 3;
+  if (r < 0) r += 3;
+  m = ldexp(m, r);
+  e -= r;
+  y = 0.6 + 0.25 * m;
+  for (k = 0; k < 6; ++k) y = (2.0 * y + m / (y * y)) / 3.0;
+  return ldexp(y, e / 3);
+}
+
+/* a^(1/6) for a >= 0 */
+static double tor_pow16(double a) { return sqrt(tor_cbrt(a)); }
+
+/* atan(z), 0 <= z <= 1: two argument halvings atan(z) = 2 atan(z / (1 + sqrt(1 + z^2))) bring
+ * z below tan(pi / 16), then the Taylor series to z^23 */
+static double tor_atan_unit(double z)
+{
+  double z2, term, s;
+  int k;
+  z    = z / (1.0 + sqrt(1.0 + z * z));
+  z    = z / (1.0 + sqrt(1.0 + z * z));
+  z2   = z * z;
+  term = z;
+  s    = z;
+  for (k = 1; k < 12; ++k) {
+    term *= -z2;
+    s += term / (2 * k + 1);
+  }
+  return 4.0 * s;
+}
+
+/* atan2(y, x) for y > 0 (the cubic solver's u) */
+static double tor_atan2(double y, double x)
+{
+  const double ax = fabs(x);
+  const double a  = (y <= ax) ? tor_atan_unit(y / ax) : 0.5 * kPi - tor_atan_unit(ax / y);
+  return x < 0 ? kPi - a : a;
+}
+
+/* cos(w), |w| <= 1.1: the Taylor series to w^24 */
+static double tor_cos(double w)
+{
+  const double w2 = w * w;
+  double term = 1.0, s = 1.0;
+  int k;
+  for (k = 1; k <= 12; ++k) {
+    term *= -w2 / ((2 * k - 1) * (2 * k));
+    s += term;
+  }
+  return s;
+}
+
+/* SolveCubic (TorusImplementation2.h:17-53) */
+static unsigned tor_solve_cubic(double a, double b, double c, double *x)
+{
+  const double ott = 1. / 3., sq3 = sqrt(3.), inv6sq3 = 1. / (6. * sq3);
+  unsigned ireal = 1;
+  const double p = b - a * a * ott;
+  const double q = c - a * b * ott + 2. * a * a * a * ott * ott * ott;
+  double delta   = 4 * p * p * p + 27. * q * q;
+  double t, u;
+  if (delta >= 0) {
+    delta = sqrt(delta);
+    t     = (-3 * q * sq3 + delta) * inv6sq3;
+    u     = (3 * q * sq3 + delta) * inv6sq3;
+    x[0]  = copysign(1., t) * tor_cbrt(fabs(t)) - copysign(1., u) * tor_cbrt(fabs(u)) - a * ott;
+  } else {
+    delta = sqrt(-delta);
+    t     = -0.5 * q;
+    u     = delta * inv6sq3;
+    x[0]  = 2. * tor_pow16(t * t + u * u) * tor_cos(ott * tor_atan2(u, t));
+    x[0] -= a * ott;
+  }
+  t     = x[0] * x[0] + a * x[0] + b;
+  u     = a + x[0];
+  delta = u * u - 4. * t;
+  if (delta >= 0) {
+    ireal = 3;
+    delta = sqrt(delta);
+    x[1]  = 0.5 * (-u - delta);
+    x[2]  = 0.5 * (-u + delta);
+  }
+  return ireal;
+}
+
+static inline void tor_cmp_swap(double *v, int i, int j) /* CmpAndSwap (TorusImplementation2.h:55-66) */
+{
+  if (v[i] > v[j]) {
+    const double c = v[j];
+    v[j]           = v[i];
+    v[i]           = c;
+  }
+}
+
+static void tor_sort4(double *v) /* Sort4 (TorusImplementation2.h:68-77) */
+{
+  tor_cmp_swap(v, 0, 2);
+  tor_cmp_swap(v, 1, 3);
+  tor_cmp_swap(v, 0, 1);
+  tor_cmp_swap(v, 2, 3);
+  tor_cmp_swap(v, 1, 2);
+}
+
+/* SolveQuartic (TorusImplementation2.h:79-150) */
+static int tor_solve_quartic(double a, double b, double c, double d, double *x)
+{
+  const double e = b - 3. * a * a / 8.;
+  const double f = c + a * a * a / 8. - 0.5 * a * b;
+  const double g = d - 3. * a * a * a * a / 256. + a * a * b / 16. - a * c / 4.;
+  double xx[4] = {kInfLength, kInfLength, kInfLength, kInfLength};
+  double delta, h = 0., j;
+  unsigned ireal = 0, i;
+  if (fabs(f) < 1E-6) {
+    delta = e * e - 4. * g;
+    if (delta < 0.) return 0;
+    delta = sqrt(delta);
+    h     = 0.5 * (-e - delta);
+    if (h >= 0) {
+      h          = sqrt(h);
+      x[ireal++] = -h - 0.25 * a;
+      x[ireal++] = h - 0.25 * a;
+    }
+    h = 0.5 * (-e + delta);
+    if (h >= 0) {
+      h          = sqrt(h);
+      x[ireal++] = -h - 0.25 * a;
+      x[ireal++] = h - 0.25 * a;
+    }
+    tor_sort4(x);
+    return (int)ireal;
+  }
+  if (fabs(g) < 1E-6) {
+    unsigned ncubic;
+    x[ireal++] = -0.25 * a;
+    ncubic     = tor_solve_cubic(0, e, f, xx);
+    for (i = 0; i < ncubic; i++) x[ireal++] = xx[i] - 0.25 * a;
+    tor_sort4(x);
+    return (int)ireal;
+  }
+  ireal = tor_solve_cubic(2. * e, e * e - 4. * g, -f * f, xx);
+  if (ireal == 1) {
+    if (xx[0] <= 0) return 0;
+    h = sqrt(xx[0]);
+  } else {
+    for (i = 0; i < 3; i++) {
+      h = xx[i];
+      if (h >= 0) break;
+    }
+    if (h <= 0) return 0;
+    h = sqrt(h);
+  }
+  j     = 0.5 * (e + h * h - f / h);
+  ireal = 0;
+  delta = h * h - 4. * j;
+  if (delta >= 0) {
+    delta      = sqrt(delta);
+    x[ireal++] = 0.5 * (-h - delta) - 0.25 * a;
+    x[ireal++] = 0.5 * (-h + delta) - 0.25 * a;
+  }
+  delta = h * h - 4. * g / j;
+  if (delta >= 0) {
+    delta      = sqrt(delta);
+    x[ireal++] = 0.5 * (h - delta) - 0.25 * a;
+    x[ireal++] = 0.5 * (h + delta) - 0.25 * a;
+  }
+  tor_sort4(x);
+  return (int)ireal;
+}
+
+/* TorusStruct2(rmin, rmax, rtor, sphi, dphi) (TorusStruct2.h:36-43); the bounding tube
+ * GenericUnplacedTube(rtor - rmax - tol, rtor + rmax + tol, rmax, sphi, dphi) */
+static int torus_init(or_torus *t, const double *a, char *err, int errlen)
+{
+  double tp[5];
+  t->rmin = a[0];
+  t->rmax = a[1];
+  t->rtor = a[2];
+  t->sphi = a[3];
+  t->dphi = a[4];
+  if (!(t->rmin >= 0 && t->rmax > t->rmin && t->rtor > t->rmax + kTolerance && t->dphi > 0)) {
+    set_err(err, errlen, "torus: needs 0 <= rmin < rmax < rtor and dphi > 0");
+    return -1;
+  }
+  t->rmin2 = t->rmin * t->rmin;
+  t->rmax2 = t->rmax * t->rmax;
+  t->rtor2 = t->rtor * t->rtor;
+  wedge_init(&t->w, t->dphi, t->sphi);
+  tp[0] = t->rtor - t->rmax - kTolerance;
+  tp[1] = t->rtor + t->rmax + kTolerance;
+  tp[2] = t->rmax;
+  tp[3] = t->sphi;
+  tp[4] = t->dphi;
+  return tube_init(&t->btube, tp, err, errlen);
+}
+
+static inline int torus_has_phi(const or_torus *t) { return t->dphi < kTwoPi; }
+
+/* GenericKernelForContainsAndInside<ForInside, notForDisk> (TorusImplementation2.h:241-285) */
+static void torus_ci(const or_torus *t, v3 p, int forInside, int notForDisk, int *cin, int *cout)
+{
+  const double tol   = 100. * kTolerance;
+  const double rxy   = sqrt(p.x * p.x + p.y * p.y);
+  const double radsq = (rxy - t->rtor) * (rxy - t->rtor) + p.z * p.z;
+  if (forInside) {
+    *cout = radsq > (tol * t->rmax + t->rmax2);
+    *cin  = radsq < (-tol * t->rmax + t->rmax2);
+  } else {
+    *cout = radsq > t->rmax2;
+  }
+  if (*cout) return;
+  if (forInside) {
+    *cout |= radsq < (-tol * t->rmin + t->rmin2);
+    *cin &= radsq > (tol * t->rmin + t->rmin2);
+  } else {
+    *cout |= radsq < t->rmin2;
+  }
+  if (*cout) return;
+  if (torus_has_phi(t) && notForDisk) {
+    int cinphi = 0, coutphi = 0;
+    wedge_ci(&t->w, p, forInside, &cinphi, &coutphi);
+    *cout |= coutphi;
+    if (forInside) *cin &= cinphi;
+  }
+}
+
+/* Contains (TorusImplementation2.h:391-399): the inside tolerances and no phi test, as the
+ * reference has it */
+static int torus_contains(const or_torus *t, v3 p)
+{
+  int cin = 0, cout = 0;
+  torus_ci(t, p, 1, 0, &cin, &cout);
+  return !cout;
+}
+
+static int torus_inside(const or_torus *t, v3 p) /* InsideKernel (TorusImplementation2.h:227-239) */
+{
+  int cin = 0, cout = 0;
+  torus_ci(t, p, 1, 1, &cin, &cout);
+  return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+}
+
+static int torus_contains_disk(const or_torus *t, v3 p) /* UnplacedContainsDisk (TorusImplementation2.h:219-225) */
+{
+  int cin = 0, cout = 0;
+  torus_ci(t, p, 0, 0, &cin, &cout);
+  return !cout;
+}
+
+/* ToBoundary<ForRmin> (TorusImplementation2.h:287-377) */
+static double torus_to_boundary(const or_torus *t, v3 pt, v3 dir, double radius, int out)
+{
+  const double tol = 100. * kTolerance;
+  const double r0sq   = pt.x * pt.x + pt.y * pt.y + pt.z * pt.z;
+  const double rdotn  = pt.x * dir.x + pt.y * dir.y + pt.z * dir.z;
+  const double rsumsq = t->rtor2 + radius * radius;
+  const double a      = 4. * rdotn;
+  const double b      = 2. * (r0sq + 2. * rdotn * rdotn - rsumsq + 2. * t->rtor2 * dir.z * dir.z);
+  const double c      = 4. * (r0sq * rdotn - rsumsq * rdotn + 2. * t->rtor2 * pt.z * dir.z);
+  const double d = r0sq * r0sq - 2. * r0sq * rsumsq + 4. * t->rtor2 * pt.z * pt.z +
+                   (t->rtor2 - radius * radius) * (t->rtor2 - radius * radius);
+  double x[4] = {kInfLength, kInfLength, kInfLength, kInfLength};
+  int nsol = 0, inner, i;
+  if (fabs(dir.z) < 1E-3 && fabs(pt.z) < 0.1 * radius) {
+    double r0            = t->rtor - sqrt((radius - pt.z) * (radius + pt.z));
+    const double invdxy2 = 1. / (1 - dir.z * dir.z);
+    const double b0      = (pt.x * dir.x + pt.y * dir.y) * invdxy2;
+    double c0            = (pt.x * pt.x + (pt.y - r0) * (pt.y + r0)) * invdxy2;
+    double delta         = b0 * b0 - c0;
+    if (delta > 0) {
+      x[nsol] = -b0 - sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+      x[nsol] = -b0 + sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+    }
+    r0    = t->rtor + sqrt((radius - pt.z) * (radius + pt.z));
+    c0    = (pt.x * pt.x + (pt.y - r0) * (pt.y + r0)) * invdxy2;
+    delta = b0 * b0 - c0;
+    if (delta > 0) {
+      x[nsol] = -b0 - sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+      x[nsol] = -b0 + sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+    }
+    if (nsol) tor_sort4(x);
+  } else {
+    nsol = tor_solve_quartic(a, b, c, d, x);
+  }
+  if (!nsol) return kInfLength;
+  inner = fabs(radius - t->rmin) < kTolerance;
+  for (i = 0; i < nsol; i++) {
+    v3 r0, norm;
+    double ndotd, s, eps, delta, eps0, inv;
+    int ntry;
+    if (x[i] < -10) continue;
+    r0   = v3_add(pt, v3_scale(x[i], dir));
+    norm = r0;
+    r0.z = 0.;
+    inv  = 1. / sqrt(v3_mag2(r0));
+    r0   = v3_make(r0.x * inv, r0.y * inv, r0.z * inv);
+    r0   = v3_make(r0.x * t->rtor, r0.y * t->rtor, r0.z * t->rtor);
+    norm = v3_sub(norm, r0);
+    ndotd = v3_dot(norm, dir);
+    if (inner ^ out) {
+      if (ndotd < 0) continue;
+    } else {
+      if (ndotd > 0) continue;
+    }
+    if (torus_has_phi(t)) {
+      int cin = 0, cout = 0;
+      wedge_ci(&t->w, r0, 1, &cin, &cout); /* Wedge::ContainsWithBoundary */
+      if (cout) continue;
+    }
+    s     = x[i];
+    eps   = kInfLength;
+    delta = s * s * s * s + a * s * s * s + b * s * s + c * s + d;
+    eps0  = -delta / (4. * s * s * s + 3. * a * s * s + 2. * b * s + c);
+    ntry  = 0;
+    while (fabs(eps) > kTolerance) {
+      if (fabs(eps0) > 100) break;
+      s += eps0;
+      if (fabs(s + eps0) < kTolerance) break;
+      delta = s * s * s * s + a * s * s * s + b * s * s + c * s + d;
+      eps   = -delta / (4. * s * s * s + 3. * a * s * s + 2. * b * s + c);
+      if (fabs(eps) >= fabs(eps0)) break;
+      ntry++;
+      if (ntry > 100) break;
+      eps0 = eps;
+    }
+    if (s < -tol) continue;
+    return 0. > s ? 0. : s;
+  }
+  return kInfLength;
+}
+
+/* DistSqrToTorusR (TorusImplementation2.h:149-156) */
+static double torus_dist2_axis(const or_torus *t, v3 p, v3 dir, double dist)
+{
+  const v3 q       = v3_add(p, v3_scale(dist, dir));
+  const double rxy = sqrt(q.x * q.x + q.y * q.y);
+  return (rxy - t->rtor) * (rxy - t->rtor) + q.z * q.z;
+}
+
+/* DistanceToIn (TorusImplementation2.h:415-491), the VECGEOM_NO_SPECIALIZATION branch */
+static double torus_dist_in(const or_torus *t, v3 p, v3 d)
+{
+  double distance = kInfLength, tubeDistance = kInfLength, dd;
+  v3 lp = p;
+  const int inBounds = tube_contains(&t->btube, lp);
+  if (!inBounds)
+    tubeDistance = tube_dist_in(&t->btube, lp, d);
+  else
+    tubeDistance = 0.;
+  if (inBounds) {
+    if (torus_inside(t, p) == kInsideE) return -1.;
+  } else if (tubeDistance == kInfLength) {
+    return kInfLength;
+  }
+  lp = v3_add(lp, v3_scale(tubeDistance, d));
+  if (torus_has_phi(t)) {
+    double d1, d2;
+    wedge_dist(&t->w, lp, d, 1, &d1, &d2);
+    if (d1 != kInfLength) {
+      const double daxis = torus_dist2_axis(t, lp, d, d1);
+      if (daxis >= t->rmin2 && daxis < t->rmax2) {
+        distance = d1;
+        if (fabs(distance) < kTolerance) return distance + tubeDistance;
+      }
+    }
+    if (d2 != kInfLength) {
+      const double daxis = torus_dist2_axis(t, lp, d, d2);
+      if (daxis >= t->rmin2 && daxis < t->rmax2) {
+        distance = d2 < distance ? d2 : distance;
+        if (fabs(distance) < kTolerance) return distance + tubeDistance;
+      }
+    }
+    distance = kInfLength;
+  }
+  dd = torus_to_boundary(t, lp, d, t->rmax, 0);
+  if (t->rmin > 0.) {
+    const double ddrmin = torus_to_boundary(t, lp, d, t->rmin, 0);
+    dd                  = dd < ddrmin ? dd : ddrmin;
+  }
+  distance = distance < dd ? distance : dd;
+  distance += tubeDistance;
+  if (fabs(distance) > kInfLength) distance = kInfLength;
+  return distance;
+}
+
+/* DistanceToOut (TorusImplementation2.h:158-217) */
+static double torus_dist_out(const or_torus *t, v3 p, v3 d)
+{
+  const double rsq = p.x * p.x + p.y * p.y;
+  const double outerExcl = t->rtor + t->rmax + kHalfTolerance, innerExcl = t->rtor - t->rmax - kHalfTolerance;
+  double distance, dout, din = kInfLength;
+  if (fabs(p.z) - t->rmax > kHalfTolerance || rsq > outerExcl * outerExcl || rsq < innerExcl * innerExcl) return -1.;
+  if (torus_inside(t, p) == kOutsideE) return -1.;
+  dout = torus_to_boundary(t, p, d, t->rmax, 1);
+  if (t->rmin > 0) din = torus_to_boundary(t, p, d, t->rmin, 1);
+  distance = dout < din ? dout : din;
+  if (torus_has_phi(t)) {
+    double dp1, dp2;
+    wedge_dist(&t->w, p, d, 0, &dp1, &dp2);
+    if (dp1 < distance) {
+      const v3 ip = v3_add(p, v3_scale(dp1, d));
+      if (torus_contains_disk(t, ip)) {
+        const double diri = ip.x * t->w.a1x + ip.y * t->w.a1y;
+        if (diri >= 0) distance = dp1;
+      }
+    }
+    if (dp2 < distance) {
+      const v3 ip = v3_add(p, v3_scale(dp2, d));
+      if (torus_contains_disk(t, ip)) {
+        const double diri2 = ip.x * t->w.a2x + ip.y * t->w.a2y;
+        if (diri2 >= 0 && dp2 < distance) distance = dp2;
+      }
+    }
+  }
+  if (distance >= kInfLength) distance = -1.;
+  return distance;
+}
+
+/* SafetyToIn (TorusImplementation2.h:493-509) */
+static double torus_safe_in(const or_torus *t, v3 p)
+{
+  const double rxy = sqrt(p.x * p.x + p.y * p.y);
+  const double rad = sqrt((rxy - t->rtor) * (rxy - t->rtor) + p.z * p.z);
+  double safety    = rad - t->rmax;
+  if (t->rmin) safety = or_max(t->rmin - rad, rad - t->rmax);
+  if (torus_has_phi(t) && rxy != 0.) safety = or_max(wedge_safe_in(&t->w, p), safety);
+  return safety;
+}
+
+/* SafetyToOut (TorusImplementation2.h:379-389) */
+static double torus_safe_out(const or_torus *t, v3 p)
+{
+  const double rxy = sqrt(p.x * p.x + p.y * p.y);
+  const double rad = sqrt((rxy - t->rtor) * (rxy - t->rtor) + p.z * p.z);
+  double safety    = t->rmax - rad;
+  if (t->rmin) safety = or_min(rad - t->rmin, t->rmax - rad);
+  if (torus_has_phi(t)) safety = or_min(wedge_safe_out(&t->w, p), safety);
+  return safety;
+}
+
 /* ---------------------------------------------------------------- */
 /* Boolean solids over placed operands: BooleanImplementation.h (subtraction),
  * BooleanUnionImplementation.h, BooleanIntersectionImplementation.h.  A placed operand's
@@ -4064,6 +4524,7 @@ int shape_init(or_lv *lv, const double *p, int n_avail, char *err, int errlen)
     return 0;
   case OR_CUTTUBE: return cuttube_init(&lv->s.ctube, p, err, errlen);
   case OR_POLYHEDRON: return polyhedron_init(&lv->s.phd, p, err, errlen);
+  case OR_TORUS: return torus_init(&lv->s.tor, p, err, errlen);
   case OR_BOOLEAN: /* operands are linked once the placements are known (or_core.c) */
     if (!(p[0] == 0. || p[0] == 1. || p[0] == 2.) || !(p[1] >= 0. && p[1] <= 2147483647. && p[1] == floor(p[1])) ||
         !(p[2] >= 0. && p[2] <= 2147483647. && p[2] == floor(p[2]))) {
@@ -4098,6 +4559,7 @@ void shape_extent(const or_lv *lv, v3 *mn, v3 *mx)
   case OR_CUTTUBE: cuttube_extent(&lv->s.ctube, mn, mx); return;
   case OR_BOOLEAN: boolean_extent(&lv->s.boo, mn, mx); return;
   case OR_POLYHEDRON: polyhedron_extent(&lv->s.phd, mn, mx); return;
+  case OR_TORUS: tube_extent(&lv->s.tor.btube, mn, mx); return; /* UnplacedTorus2.h:210 */
   }
 }
 
@@ -4120,6 +4582,7 @@ double shape_dist_in(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *c
   case OR_CUTTUBE: return cuttube_dist_in(&lv->s.ctube, p, d, stepmax);
   case OR_BOOLEAN: return boolean_dist_in(&lv->s.boo, p, d, stepmax, c);
   case OR_POLYHEDRON: return polyhedron_dist_in(&lv->s.phd, p, d);
+  case OR_TORUS: return torus_dist_in(&lv->s.tor, p, d);
   }
   return kInfLength;
 }
@@ -4140,6 +4603,7 @@ double shape_dist_out(const or_lv *lv, v3 p, v3 d, double stepmax, or_counters *
   case OR_CUTTUBE: return cuttube_dist_out(&lv->s.ctube, p, d);
   case OR_BOOLEAN: return boolean_dist_out(&lv->s.boo, p, d, stepmax, c);
   case OR_POLYHEDRON: return polyhedron_dist_out(&lv->s.phd, p, d);
+  case OR_TORUS: return torus_dist_out(&lv->s.tor, p, d);
   }
   return -1.;
 }
@@ -4159,6 +4623,7 @@ double shape_safe_in(const or_lv *lv, v3 p, or_counters *c)
   case OR_CUTTUBE: return cuttube_safe_in(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_safe_in(&lv->s.boo, p, c);
   case OR_POLYHEDRON: return polyhedron_safety(&lv->s.phd, p, 0);
+  case OR_TORUS: return torus_safe_in(&lv->s.tor, p);
   }
   return kInfLength;
 }
@@ -4178,6 +4643,7 @@ double shape_safe_out(const or_lv *lv, v3 p, or_counters *c)
   case OR_CUTTUBE: return cuttube_safe_out(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_safe_out(&lv->s.boo, p, c);
   case OR_POLYHEDRON: return polyhedron_safety(&lv->s.phd, p, 1);
+  case OR_TORUS: return torus_safe_out(&lv->s.tor, p);
   }
   return 0.;
 }
@@ -4197,6 +4663,7 @@ int shape_contains(const or_lv *lv, v3 p, or_counters *c)
   case OR_CUTTUBE: return cuttube_contains(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_contains(&lv->s.boo, p, c);
   case OR_POLYHEDRON: return polyhedron_contains(&lv->s.phd, p);
+  case OR_TORUS: return torus_contains(&lv->s.tor, p);
   }
   return 0;
 }
@@ -4216,6 +4683,7 @@ int shape_inside(const or_lv *lv, v3 p, or_counters *c)
   case OR_CUTTUBE: return cuttube_inside(&lv->s.ctube, p);
   case OR_BOOLEAN: return boolean_inside(&lv->s.boo, p, c);
   case OR_POLYHEDRON: return polyhedron_inside(&lv->s.phd, p);
+  case OR_TORUS: return torus_inside(&lv->s.tor, p);
   }
   return kOutsideE;
 }

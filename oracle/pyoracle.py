@@ -23,12 +23,12 @@ OP_DIST_IN, OP_DIST_OUT, OP_SAFE_IN, OP_SAFE_OUT, OP_CONTAINS, OP_INSIDE = range
 class Counters(C.Structure):
     _fields_ = [("node_slab", C.c_uint64), ("prim_slab", C.c_uint64), ("node_safety", C.c_uint64),
                 ("prim_safety", C.c_uint64), ("prim_contains", C.c_uint64), ("transforms", C.c_uint64),
-                ("kernel", (C.c_uint64 * 6) * 11)]  # per shape type (OR_NSHAPES) and query
+                ("kernel", (C.c_uint64 * 6) * 12)]  # per shape type (OR_NSHAPES) and query
 
     def as_dict(self) -> dict:
         d = {k: int(getattr(self, k)) for k in ("node_slab", "prim_slab", "node_safety", "prim_safety",
                                                 "prim_contains", "transforms")}
-        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(11)]
+        d["kernel"] = [[int(self.kernel[s][o]) for o in range(6)] for s in range(12)]
         return d
 
 

@@ -45,6 +45,7 @@
 #include "VecGeom/volumes/UnplacedOrb.h"
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedPolyhedron.h"
+#include "VecGeom/volumes/UnplacedTorus2.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
 #include "VecGeom/volumes/UnplacedTrapezoid.h"
 #include "VecGeom/volumes/UnplacedTrd.h"
@@ -104,6 +105,8 @@ VUnplacedVolume *make_shape(int type, const double *p)
   case 8:
     return GeoManager::MakeInstance<UnplacedCutTube>(p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], p[9],
                                                      p[10]);
+  case 11:
+    return GeoManager::MakeInstance<UnplacedTorus2>(p[0], p[1], p[2], p[3], p[4]);
   case 10: {
     const int nz = (int)p[3];
     return GeoManager::MakeInstance<UnplacedPolyhedron>(p[0], p[1], (int)p[2], nz, p + 4, p + 4 + nz, p + 4 + 2 * nz);

@@ -23,7 +23,8 @@ extern "C" {
 
 /* shape type ids (same numbering as the product's vgn_shape_type) */
 enum { OR_BOX = 0, OR_TUBE = 1, OR_CONE = 2, OR_TRD = 3, OR_TRAP = 4, OR_SPHERE = 5, OR_POLYCONE = 6, OR_ORB = 7,
-       OR_CUTTUBE = 8, OR_BOOLEAN = 9, OR_POLYHEDRON = 10, OR_NSHAPES = 11 };
+       OR_CUTTUBE = 8, OR_BOOLEAN = 9, OR_POLYHEDRON = 10, OR_TORUS = 11,
+       OR_NSHAPES = 12 };
 /* pv_mother of a boolean solid's operand placement (outside the hierarchy) */
 #define OR_BOOLEAN_OPERAND (-2)
 

@@ -1346,8 +1346,63 @@ POLYHEDRON_CASES = [
 # TestPolyhedra.cpp:156-157: the extent of MyPGon (ApproxEqual of vectors)
 MYPGON_EXTENT = ((0.0, 0.0, -30.0), (80.0 / math.cos(_HALFDPHI), 40.0 * math.sqrt(2.0) / math.cos(_HALFDPHI), 40.0))
 
+TORUS = 11
+TT = "test/unit_tests/TestTorus2.cpp"
+# TestTorus2.cpp:21-23, 62-65: Rtor = 100, Rmax = 0.9 Rtor, Rmin = 0.1 Rtor
+_RT, _RX, _RN = 100.0, 100.0 * 0.9, 100.0 * 0.1
+T1 = (0.0, _RX, _RT, 0.0, 2.0 * KPI_V)                                        # Solid Torus #1
+T2 = (_RN, _RX, _RT, 0.0, KPI_V / 2.0)                                        # Hole cutted Torus #2
+T3 = (4 * _RN, _RX, _RT, KPI_V / 2.0 - KPI_V / 24, KPI_V / 12)                # Hole cutted Torus #3
+_R2 = 1.0 / math.sqrt(2.0)
+_PONPHI1 = (100 / math.sqrt(2.0), 100 / math.sqrt(2.0), 0.0)
+_PONPHI12 = (190 / math.sqrt(2.0), 190 / math.sqrt(2.0), 0.0)
+_VZT = (0.00001, 0.000001, 1.0)
+_VZT = tuple(c / math.sqrt(sum(x * x for x in _VZT)) for c in _VZT)
+TORUS_CASES = [
+    _case(f"{TT}:107", TORUS, T1, "inside", pzero, None, 3, "eq"),
+    _case(f"{TT}:108", TORUS, T1, "inside", (240.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TT}:109", TORUS, T1, "inside", (190.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TT}:110", TORUS, T2, "inside", (0.0, 110.0, 0.0), None, 2, "eq"),
+    _case(f"{TT}:111", TORUS, T2, "inside", (240.0, 0.0, 0.0), None, 3, "eq"),
+    _case(f"{TT}:112", TORUS, T2, "inside", (0.0, 240.0, 0.0), None, 3, "eq"),
+    _case(f"{TT}:113", TORUS, T2, "inside", _PONPHI1, None, 3, "eq"),
+    _case(f"{TT}:114", TORUS, T2, "inside", (-100 / math.sqrt(2.0), 100 / math.sqrt(2.0), 0.0), None, 3, "eq"),
+    _case(f"{TT}:115", TORUS, T2, "inside", (20.0, 0.0, 0.0), None, 2, "eq"),
+    _case(f"{TT}:116", TORUS, T2, "inside", (0.0, 20.0, 0.0), None, 2, "eq"),
+    _case(f"{TT}:156", TORUS, T1, "safe_out", (0.0, 110.0, 0.0), None, 80.0),
+    _case(f"{TT}:158", TORUS, T1, "safe_out", (190.0, 0.0, 0.0), None, 0.0),
+    _case(f"{TT}:161", TORUS, T2, "safe_out", (20.0, 0.0, 0.0), None, 0.0),
+    _case(f"{TT}:163", TORUS, T2, "safe_out", (0.0, 20.0, 0.0), None, 0.0),
+    _case(f"{TT}:169", TORUS, T1, "dist_out", (190.0, 0.0, 0.0), vx, 0.0),
+    _case(f"{TT}:176", TORUS, T1, "dist_out", (130.0, 0.0, 0.0), vx, 60.0),
+    _case(f"{TT}:180", TORUS, T1, "dist_out", (0.0, 110.0, 0.0), vy, 80.0),
+    _case(f"{TT}:183", TORUS, T1, "dist_out", (0.0, 110.0, 0.0), vmy, 100.0),
+    _case(f"{TT}:189", TORUS, T1, "dist_out", (100.0, 0.0, 0.0), _VZT, 90.0),
+    _case(f"{TT}:195", TORUS, T2, "dist_out", (7.07106781186547524400844362, 7.07106781186547524400844362, 0.0), vmx,
+          0.0),
+    _case(f"{TT}:207", TORUS, T1, "safe_in", (240.0, 0.0, 0.0), None, 50.0),
+    _case(f"{TT}:209", TORUS, T1, "safe_in", (-240.0, 0.0, 0.0), None, 50.0),
+    _case(f"{TT}:211", TORUS, T1, "safe_in", (0.0, 240.0, 0.0), None, 50.0),
+    _case(f"{TT}:213", TORUS, T1, "safe_in", (0.0, -240.0, 0.0), None, 50.0),
+    _case(f"{TT}:226", TORUS, T1, "dist_in", (240.0, 0.0, 0.0), vmx, 50.0),
+    _case(f"{TT}:228", TORUS, T1, "dist_in", (-240.0, 0.0, 0.0), vx, 50.0),
+    _case(f"{TT}:230", TORUS, T1, "dist_in", (0.0, 240.0, 0.0), vmy, 50.0),
+    _case(f"{TT}:232", TORUS, T1, "dist_in", (0.0, -240.0, 0.0), vy, 50.0),
+    _case(f"{TT}:234", TORUS, T1, "dist_in", (0.0, 0.0, 240.0), vmz, INF, "inf"),
+    _case(f"{TT}:236", TORUS, T1, "dist_in", (0.0, 0.0, -240.0), vz, INF, "inf"),
+    _case(f"{TT}:238", TORUS, T1, "dist_in", (240.0, 0.0, 0.0), (_R2, _R2, 0.0), INF, "inf"),
+    _case(f"{TT}:252", TORUS, T2, "dist_in", pzero, vy, 10.0),
+    _case(f"{TT}:256", TORUS, T2, "dist_in", _PONPHI12, vy, INF, "inf"),
+    _case(f"{TT}:258", TORUS, T2, "dist_in", _PONPHI12, vmy, 0.0),
+    _case(f"{TT}:260", TORUS, T2, "dist_in", _PONPHI1, vy, 13.550819613108856743),
+    _case(f"{TT}:263", TORUS, T2, "dist_in", (0.0, 110.0, 0.0), vy, INF, "inf"),
+    _case(f"{TT}:265", TORUS, T2, "dist_in", (0.0, 110.0, 0.0), vmy, INF, "inf"),
+    _case(f"{TT}:268", TORUS, T3, "dist_in", (0.0, 100.0, 0.0), vy, 40.0),
+    _case(f"{TT}:270", TORUS, T3, "dist_in", (0.0, 100.0, 0.0), vmy, 40.0),
+]
+
 ALL_CASES = BOX_CASES + TUBE_CASES + CONE_CASES + TRD_CASES + TRAP_CASES + SPHERE_CASES + POLYCONE_CASES + ORB_CASES
-ALL_CASES += POLYHEDRON_CASES
+ALL_CASES += POLYHEDRON_CASES + TORUS_CASES
 
 
 def approx_equal(x: float, y: float) -> bool:

@@ -22,6 +22,10 @@ writes inputs and outputs to tests/golden/ref_fixtures.npz:
                 of two tubes) in a box world: 2048 located tracks, one step, a walk
   bool_shapes/<k>  those four boolean kinds alone: 1024 points in 1.3 times their extent,
                 the six shape queries (Inside only for the two kinds without a union)
+  torus_shapes/<i>  every Torus2 parameter set of tests/shape_sets.py TORUS_SETS: up to 192
+                points (planes and axes, random, surface), all six queries
+  tori          512 daughters (tori, most of them phi sections, spheres, boxes): 2048 located
+                tracks, one step, a walk
   approach/<key>  BVH::ApproachNextDaughter on the mixed_all, nested, deep_cache1 and
                 booleans geometries: 4096 tracks over their BVHs (tests/helpers.py
                 approach_inputs)
@@ -246,6 +250,32 @@ def generate() -> dict:
             out[f"{key}/in/{k}"] = a
         for op in range(5 if kind in (1, 3) else 6):
             out[f"{key}/out/op{op}"] = rg.shape(lv, op, X, Y, Z, DX, DY, DZ)
+
+    # Torus2: the shape queries of every torus parameter set and navigation among tori
+    from shape_sets import TORUS_SETS
+    for i, (name, shape, params) in enumerate(TORUS_SETS):
+        desc = single_shape(shape, params)
+        rg = pyref.RefGeometry(desc)
+        X, Y, Z, DX, DY, DZ, m = shape_points(name, shape, params, 100000,
+                                              lambda x, y, z: rg.shape(0, OPS["contains"], x, y, z),
+                                              lambda *a: rg.shape(0, OPS["dist_out"], *a))
+        sel = np.concatenate([np.arange(SHAPE_POINTS // 8), np.arange(9500, 9500 + SHAPE_POINTS - SHAPE_POINTS // 8),
+                              X.shape[0] - m + np.arange(min(m, SHAPE_SURFACE))])
+        key = f"torus_shapes/{i}"
+        out[f"{key}/name"] = np.array(name)
+        put_desc(out, key, desc)
+        for k, a in zip(TRACK_KEYS[:6], (X, Y, Z, DX, DY, DZ)):
+            out[f"{key}/in/{k}"] = a[sel]
+        for op in range(6):
+            out[f"{key}/out/op{op}"] = rg.shape(0, op, *(a[sel] for a in (X, Y, Z, DX, DY, DZ)))
+    desc = W.torus_geometry()
+    rg = pyref.RefGeometry(desc)
+    t = W.uniform_tracks(2048, 999.0, 73, 74)
+    t.states = rg.locate(t.x, t.y, t.z)
+    put_desc(out, "tori", desc)
+    put_tracks(out, "tori", t)
+    _steps(out, "tori", rg, t)
+    _walk(out, "tori", rg, t)
 
     # BVH::ApproachNextDaughter
     from helpers import approach_inputs

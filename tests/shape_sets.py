@@ -87,6 +87,16 @@ SHAPE_SETS = [
                                                         (5.0, 5.0, 12.0, 12.0), (25.0, 15.0, 30.0, 30.0))),
 ]
 
+# Torus2 parameter sets (rmin, rmax, rtor, sphi, dphi): their distances equal the reference's to
+# about 1e-13 mm rather than bit for bit, so they are kept apart from SHAPE_SETS
+TORUS_SETS = [
+    ("torus-ring", W.TORUS, (0., 100., 1000., 0., W.K_TWO_PI)),
+    ("torus-clad-half", W.TORUS, (0., 10., 100., 0., W.K_PI)),
+    ("torus-hollow", W.TORUS, (5., 10., 40., 0., W.K_TWO_PI)),
+    ("torus-cms-eecool3", W.TORUS, (0., 6., 1640., 0.09599, 1.4312)),
+    ("torus-hollow-sector", W.TORUS, (3., 8., 30., -1.0, 4.0)),
+    ("torus-testtorus2-t2", W.TORUS, KA.T2),
+]
 
 # sampling boxes of sections much smaller than their full shape's box
 SAMPLE_BOXES = {"sphere-patch-b9": ((0.0, 0.0, 2.0), (7.0, 7.0, 8.0))}

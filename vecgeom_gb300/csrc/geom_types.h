@@ -30,7 +30,7 @@ constexpr int kMaxLevels = 30;  // bound on geometry depth (relocation loops)
 
 enum ShapeType : int32_t {
   kBox = 0, kTube = 1, kCone = 2, kTrd = 3, kTrapezoid = 4, kSphere = 5, kPolycone = 6, kOrb = 7, kCutTube = 8,
-  kBoolean = 9, kPolyhedron = 10, kNumShapes = 11
+  kBoolean = 9, kPolyhedron = 10, kTorus = 11, kNumShapes = 12
 };
 
 // flags of a placement transformation (Transformation3D::SetProperties,
@@ -196,6 +196,10 @@ VGN_HD inline int phd_rmax(int nz) { return PhdArrays + 2 * nz; }
 VGN_HD inline int phd_samez(int nz) { return PhdArrays + 3 * nz; }
 VGN_HD inline int phd_phisec(int nz) { return PhdArrays + 4 * nz; }
 VGN_HD inline int phd_segs(int nz, int sides) { return phd_phisec(nz) + 3 * (sides + 1); }  // 4 per segment
+// Torus2: TorusStruct2 (TorusStruct2.h:22-32): parameters and squares, the phi wedge, the
+// bounding tube (a Tube row)
+enum { TorRmin = 0, TorRmax, TorRtor, TorSphi, TorDphi, TorRmin2, TorRmax2, TorRtor2, TorWedge,
+       TorTube = TorWedge + kWedgeSize, kTorusSize = TorTube + kTubeSize };
 // Cone (full phi): ConeStruct cached members
 enum { ConeRmin1 = 0, ConeRmax1, ConeRmin2, ConeRmax2, ConeDz, ConeOrigRmax1, ConeOrigRmax2, ConeInnerSlope,
        ConeOuterSlope, ConeInnerOffset, ConeOuterOffset, ConeInnerTol, ConeOuterTol, ConeSqRmin1, ConeSqRmin2,

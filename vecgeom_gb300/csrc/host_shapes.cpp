@@ -66,6 +66,7 @@ int shape_param_count(int32_t type, const double *p, int32_t n_avail)
     if (n_avail < 3 || !(p[2] >= 2 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
     return 3 + 3 * (int)p[2];
   }
+  case kTorus: return 5;
   case kPolyhedron: {  // sphi, dphi, sides, nz, z[nz], rmin[nz], rmax[nz]
     if (n_avail < 4 || !(p[3] >= 2 && p[3] <= 4096) || (double)(int)p[3] != p[3]) return -1;
     if (!(p[2] >= 1 && p[2] <= 4096) || (double)(int)p[2] != p[2]) return -1;
@@ -605,6 +606,27 @@ int shape_make_row(int32_t type, const double *p, int32_t n_avail, std::vector<d
     return VGN_OK;
   }
   case kPolyhedron: return polyhedron_row(p, shape, err);
+  case kTorus: {
+    // TorusStruct2(rmin, rmax, rtor, sphi, dphi) (TorusStruct2.h:36-43): the raw angles, the
+    // squares, fPhiWedge(dphi, sphi) and the bounding GenericUnplacedTube(rtor - rmax - tol,
+    // rtor + rmax + tol, rmax, sphi, dphi)
+    if (!(p[0] >= 0 && p[1] > p[0] && p[2] > p[1] + kTolerance && p[4] > 0)) {
+      err = "torus needs 0 <= rmin < rmax < rtor and dphi > 0";
+      return VGN_ERR_ARG;
+    }
+    double r[row::kTorusSize];
+    for (int k = 0; k < 5; ++k) r[row::TorRmin + k] = p[k];
+    r[row::TorRmin2] = p[0] * p[0];
+    r[row::TorRmax2] = p[1] * p[1];
+    r[row::TorRtor2] = p[2] * p[2];
+    wedge_fill(r + row::TorWedge, p[4], p[3]);
+    const double tp[5] = {p[2] - p[1] - kTolerance, p[2] + p[1] + kTolerance, p[1], p[3], p[4]};
+    std::vector<double> tube;
+    if (int rc = shape_make_row(kTube, tp, 5, tube, err)) return rc;
+    std::copy(tube.begin(), tube.end(), r + row::TorTube);
+    shape.insert(shape.end(), r, r + row::kTorusSize);
+    return VGN_OK;
+  }
   case kCutTube: {
     // UnplacedCutTube(rmin, rmax, z, sphi, dphi, bx, by, bz, tx, ty, tz) -> CutTubeStruct
     // (UnplacedCutTube.h:54-70, CutTubeStruct.h:34-46): a tube of infinite half-length, the two
@@ -683,7 +705,8 @@ bool shape_row_has_sections(int32_t type, const double *r)
     return r[row::pcon_cone(n, 0) + row::ConeDPhi] < 2. * kPi;
   }
   case kSphere: return r[row::SphFull] == 0.;
-  case kPolyhedron: return true;  // its kernels live in the sections set only
+  case kPolyhedron:
+  case kTorus: return true;  // their kernels live in the sections set only
   case kBoolean:  // the operands' (once linked)
     return (r[row::BoolLeftType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolLeftType], r + (int64_t)r[row::BoolLeftRow])) ||
            (r[row::BoolRightType] >= 0 && shape_row_has_sections((int32_t)r[row::BoolRightType], r + (int64_t)r[row::BoolRightRow]));
@@ -1014,6 +1037,7 @@ void shape_extent(int32_t type, const double *r, Vec3 &mn, Vec3 &mx)
     mx = {r[0], r[0], r[0]};
     return;
   case kBoolean: boolean_extent(r, mn, mx); return;
+  case kTorus: shape_extent(kTube, r + row::TorTube, mn, mx); return;  // UnplacedTorus2.h:210
   case kPolyhedron: {  // UnplacedPolyhedron::Extent (source/UnplacedPolyhedron.cpp:273-303)
     const int S = (int)r[row::PhdSides], nz = (int)r[row::PhdNz];
     const double sidePhi = r[row::PhdPhiDelta] / S, conv = 1. / std::cos(0.5 * sidePhi);

@@ -3016,6 +3016,428 @@ __device__ __noinline__ double polyhedron_safety(const double *r, D3 p, bool pt_
 }
 #endif  // VGN_SECTIONS
 
+// ---------------------------------------------------------------- Torus2
+// kernel/TorusImplementation2.h over a row::Tor* row.  Compiled in the sections kernel set only
+// (a geometry holding a torus runs that set); the six entry points are out of line, as the
+// polyhedron's are.  The cubic solver's cbrt, pow, cos and atan2 are written out with IEEE
+// operations only (+, -, *, /, sqrt), identically in the oracle, so the two agree bit for bit;
+// the reference calls the C library's, which these match to a few units in the last place.
+#if VGN_SECTIONS
+namespace tr = row;
+
+// cube root of a >= 0: a = m 2^(3q), m in [0.5, 4); Newton's iteration from a linear start
+__device__ __forceinline__ double tor_cbrt(double a)
+{
+  if (a == 0.0 || !(a < kInfLength)) return a;
+  int e;
+  double m = frexp(a, &e);
+  int r    = e % 3;
+  if (r < 0) r += 3;
+  m = ldexp(m, r);
+  e -= r;
+  double y = 0.6 + 0.25 * m;
+  for (int k = 0; k < 6; ++k) y = (2.0 * y + m / (y * y)) / 3.0;
+  return ldexp(y, e / 3);
+}
+
+__device__ __forceinline__ double tor_pow16(double a) { return sqrt(tor_cbrt(a)); }
+
+// atan(z), 0 <= z <= 1: two argument halvings, then the Taylor series to z^23
+__device__ __forceinline__ double tor_atan_unit(double z)
+{
+  z = z / (1.0 + sqrt(1.0 + z * z));
+  z = z / (1.0 + sqrt(1.0 + z * z));
+  const double z2 = z * z;
+  double term = z, s = z;
+  for (int k = 1; k < 12; ++k) {
+    term *= -z2;
+    s += term / (2 * k + 1);
+  }
+  return 4.0 * s;
+}
+
+__device__ __forceinline__ double tor_atan2(double y, double x)  // y > 0
+{
+  const double ax = fabs(x);
+  const double a  = (y <= ax) ? tor_atan_unit(y / ax) : 0.5 * kPiD - tor_atan_unit(ax / y);
+  return x < 0 ? kPiD - a : a;
+}
+
+__device__ __forceinline__ double tor_cos(double w)  // |w| <= 1.1
+{
+  const double w2 = w * w;
+  double term = 1.0, s = 1.0;
+  for (int k = 1; k <= 12; ++k) {
+    term *= -w2 / ((2 * k - 1) * (2 * k));
+    s += term;
+  }
+  return s;
+}
+
+// SolveCubic (TorusImplementation2.h:17-53)
+__device__ __forceinline__ unsigned tor_solve_cubic(double a, double b, double c, double *x)
+{
+  const double ott = 1. / 3., sq3 = sqrt(3.), inv6sq3 = 1. / (6. * sq3);
+  unsigned ireal = 1;
+  const double p = b - a * a * ott;
+  const double q = c - a * b * ott + 2. * a * a * a * ott * ott * ott;
+  double delta   = 4 * p * p * p + 27. * q * q;
+  double t, u;
+  if (delta >= 0) {
+    delta = sqrt(delta);
+    t     = (-3 * q * sq3 + delta) * inv6sq3;
+    u     = (3 * q * sq3 + delta) * inv6sq3;
+    x[0]  = copysign(1., t) * tor_cbrt(fabs(t)) - copysign(1., u) * tor_cbrt(fabs(u)) - a * ott;
+  } else {
+    delta = sqrt(-delta);
+    t     = -0.5 * q;
+    u     = delta * inv6sq3;
+    x[0]  = 2. * tor_pow16(t * t + u * u) * tor_cos(ott * tor_atan2(u, t));
+    x[0] -= a * ott;
+  }
+  t     = x[0] * x[0] + a * x[0] + b;
+  u     = a + x[0];
+  delta = u * u - 4. * t;
+  if (delta >= 0) {
+    ireal = 3;
+    delta = sqrt(delta);
+    x[1]  = 0.5 * (-u - delta);
+    x[2]  = 0.5 * (-u + delta);
+  }
+  return ireal;
+}
+
+__device__ __forceinline__ void tor_cmp_swap(double *v, int i, int j)  // CmpAndSwap
+{
+  if (v[i] > v[j]) {
+    const double c = v[j];
+    v[j]           = v[i];
+    v[i]           = c;
+  }
+}
+
+__device__ __forceinline__ void tor_sort4(double *v)  // Sort4 (TorusImplementation2.h:68-77)
+{
+  tor_cmp_swap(v, 0, 2);
+  tor_cmp_swap(v, 1, 3);
+  tor_cmp_swap(v, 0, 1);
+  tor_cmp_swap(v, 2, 3);
+  tor_cmp_swap(v, 1, 2);
+}
+
+// SolveQuartic (TorusImplementation2.h:79-150)
+__device__ __forceinline__ int tor_solve_quartic(double a, double b, double c, double d, double *x)
+{
+  const double e = b - 3. * a * a / 8.;
+  const double f = c + a * a * a / 8. - 0.5 * a * b;
+  const double g = d - 3. * a * a * a * a / 256. + a * a * b / 16. - a * c / 4.;
+  double xx[4] = {kInfLength, kInfLength, kInfLength, kInfLength};
+  double delta, h = 0.;
+  unsigned ireal = 0;
+  if (fabs(f) < 1E-6) {
+    delta = e * e - 4. * g;
+    if (delta < 0.) return 0;
+    delta = sqrt(delta);
+    h     = 0.5 * (-e - delta);
+    if (h >= 0) {
+      h          = sqrt(h);
+      x[ireal++] = -h - 0.25 * a;
+      x[ireal++] = h - 0.25 * a;
+    }
+    h = 0.5 * (-e + delta);
+    if (h >= 0) {
+      h          = sqrt(h);
+      x[ireal++] = -h - 0.25 * a;
+      x[ireal++] = h - 0.25 * a;
+    }
+    tor_sort4(x);
+    return (int)ireal;
+  }
+  if (fabs(g) < 1E-6) {
+    x[ireal++]            = -0.25 * a;
+    const unsigned ncubic = tor_solve_cubic(0, e, f, xx);
+    for (unsigned i = 0; i < ncubic; i++) x[ireal++] = xx[i] - 0.25 * a;
+    tor_sort4(x);
+    return (int)ireal;
+  }
+  ireal = tor_solve_cubic(2. * e, e * e - 4. * g, -f * f, xx);
+  if (ireal == 1) {
+    if (xx[0] <= 0) return 0;
+    h = sqrt(xx[0]);
+  } else {
+    for (unsigned i = 0; i < 3; i++) {
+      h = xx[i];
+      if (h >= 0) break;
+    }
+    if (h <= 0) return 0;
+    h = sqrt(h);
+  }
+  const double j = 0.5 * (e + h * h - f / h);
+  ireal          = 0;
+  delta          = h * h - 4. * j;
+  if (delta >= 0) {
+    delta      = sqrt(delta);
+    x[ireal++] = 0.5 * (-h - delta) - 0.25 * a;
+    x[ireal++] = 0.5 * (-h + delta) - 0.25 * a;
+  }
+  delta = h * h - 4. * g / j;
+  if (delta >= 0) {
+    delta      = sqrt(delta);
+    x[ireal++] = 0.5 * (h - delta) - 0.25 * a;
+    x[ireal++] = 0.5 * (h + delta) - 0.25 * a;
+  }
+  tor_sort4(x);
+  return (int)ireal;
+}
+
+__device__ __forceinline__ bool torus_has_phi(const double *t) { return t[tr::TorDphi] < 2. * kPiD; }
+
+// GenericKernelForContainsAndInside<ForInside, notForDisk> (TorusImplementation2.h:241-285)
+template <bool FOR_INSIDE, bool NOT_FOR_DISK>
+__device__ __forceinline__ void torus_ci(const double *t, D3 p, bool &cin, bool &cout)
+{
+  const double tol   = 100. * kTolerance;
+  const double rtor  = t[tr::TorRtor];
+  const double rxy   = sqrt(p.x * p.x + p.y * p.y);
+  const double radsq = (rxy - rtor) * (rxy - rtor) + p.z * p.z;
+  if (FOR_INSIDE) {
+    cout = radsq > (tol * t[tr::TorRmax] + t[tr::TorRmax2]);
+    cin  = radsq < (-tol * t[tr::TorRmax] + t[tr::TorRmax2]);
+  } else {
+    cout = radsq > t[tr::TorRmax2];
+  }
+  if (cout) return;
+  if (FOR_INSIDE) {
+    cout |= radsq < (-tol * t[tr::TorRmin] + t[tr::TorRmin2]);
+    cin &= radsq > (tol * t[tr::TorRmin] + t[tr::TorRmin2]);
+  } else {
+    cout |= radsq < t[tr::TorRmin2];
+  }
+  if (cout) return;
+  if (NOT_FOR_DISK && torus_has_phi(t)) {
+    bool cinphi = false, coutphi = false;
+    wedge_ci<FOR_INSIDE>(t + tr::TorWedge, p, cinphi, coutphi);
+    cout |= coutphi;
+    if (FOR_INSIDE) cin &= cinphi;
+  }
+}
+
+__device__ __forceinline__ int torus_inside_kernel(const double *t, D3 p)  // InsideKernel
+{
+  bool cin = false, cout = false;
+  torus_ci<true, true>(t, p, cin, cout);
+  return cout ? kOutsideE : (cin ? kInsideE : kSurfaceE);
+}
+
+__device__ __forceinline__ bool torus_contains_disk(const double *t, D3 p)  // UnplacedContainsDisk
+{
+  bool cin = false, cout = false;
+  torus_ci<false, false>(t, p, cin, cout);
+  return !cout;
+}
+
+// ToBoundary<ForRmin> (TorusImplementation2.h:287-377)
+__device__ __forceinline__ double torus_to_boundary(const double *t, D3 pt, D3 dir, double radius, bool out)
+{
+  const double tol    = 100. * kTolerance;
+  const double rtor = t[tr::TorRtor], rtor2 = t[tr::TorRtor2];
+  const double r0sq   = pt.x * pt.x + pt.y * pt.y + pt.z * pt.z;
+  const double rdotn  = pt.x * dir.x + pt.y * dir.y + pt.z * dir.z;
+  const double rsumsq = rtor2 + radius * radius;
+  const double a      = 4. * rdotn;
+  const double b      = 2. * (r0sq + 2. * rdotn * rdotn - rsumsq + 2. * rtor2 * dir.z * dir.z);
+  const double c      = 4. * (r0sq * rdotn - rsumsq * rdotn + 2. * rtor2 * pt.z * dir.z);
+  const double d      = r0sq * r0sq - 2. * r0sq * rsumsq + 4. * rtor2 * pt.z * pt.z +
+                   (rtor2 - radius * radius) * (rtor2 - radius * radius);
+  double x[4] = {kInfLength, kInfLength, kInfLength, kInfLength};
+  int nsol    = 0;
+  if (fabs(dir.z) < 1E-3 && fabs(pt.z) < 0.1 * radius) {
+    double r0            = rtor - sqrt((radius - pt.z) * (radius + pt.z));
+    const double invdxy2 = 1. / (1 - dir.z * dir.z);
+    const double b0      = (pt.x * dir.x + pt.y * dir.y) * invdxy2;
+    double c0            = (pt.x * pt.x + (pt.y - r0) * (pt.y + r0)) * invdxy2;
+    double delta         = b0 * b0 - c0;
+    if (delta > 0) {
+      x[nsol] = -b0 - sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+      x[nsol] = -b0 + sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+    }
+    r0    = rtor + sqrt((radius - pt.z) * (radius + pt.z));
+    c0    = (pt.x * pt.x + (pt.y - r0) * (pt.y + r0)) * invdxy2;
+    delta = b0 * b0 - c0;
+    if (delta > 0) {
+      x[nsol] = -b0 - sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+      x[nsol] = -b0 + sqrt(delta);
+      if (x[nsol] > -tol) nsol++;
+    }
+    if (nsol) tor_sort4(x);
+  } else {
+    nsol = tor_solve_quartic(a, b, c, d, x);
+  }
+  if (!nsol) return kInfLength;
+  const bool inner = fabs(radius - t[tr::TorRmin]) < kTolerance;
+  for (int i = 0; i < nsol; i++) {
+    if (x[i] < -10) continue;
+    D3 r0         = d3(pt.x + x[i] * dir.x, pt.y + x[i] * dir.y, pt.z + x[i] * dir.z);
+    const D3 norm = r0;
+    r0.z          = 0.;
+    const double inv = 1. / sqrt(r0.x * r0.x + r0.y * r0.y + r0.z * r0.z);
+    r0               = d3(r0.x * inv, r0.y * inv, r0.z * inv);
+    r0               = d3(r0.x * rtor, r0.y * rtor, r0.z * rtor);
+    const double ndotd = (norm.x - r0.x) * dir.x + (norm.y - r0.y) * dir.y + (norm.z - r0.z) * dir.z;
+    if (inner ^ out) {
+      if (ndotd < 0) continue;
+    } else {
+      if (ndotd > 0) continue;
+    }
+    if (torus_has_phi(t)) {
+      bool cin = false, cout = false;
+      wedge_ci<true>(t + tr::TorWedge, r0, cin, cout);  // Wedge::ContainsWithBoundary
+      if (cout) continue;
+    }
+    double s     = x[i];
+    double eps   = kInfLength;
+    double delta = s * s * s * s + a * s * s * s + b * s * s + c * s + d;
+    double eps0  = -delta / (4. * s * s * s + 3. * a * s * s + 2. * b * s + c);
+    int ntry     = 0;
+    while (fabs(eps) > kTolerance) {
+      if (fabs(eps0) > 100) break;
+      s += eps0;
+      if (fabs(s + eps0) < kTolerance) break;
+      delta = s * s * s * s + a * s * s * s + b * s * s + c * s + d;
+      eps   = -delta / (4. * s * s * s + 3. * a * s * s + 2. * b * s + c);
+      if (fabs(eps) >= fabs(eps0)) break;
+      ntry++;
+      if (ntry > 100) break;
+      eps0 = eps;
+    }
+    if (s < -tol) continue;
+    return 0. > s ? 0. : s;
+  }
+  return kInfLength;
+}
+
+// DistSqrToTorusR (TorusImplementation2.h:149-156)
+__device__ __forceinline__ double torus_dist2_axis(const double *t, D3 p, D3 dir, double dist)
+{
+  const D3 q       = d3(p.x + dist * dir.x, p.y + dist * dir.y, p.z + dist * dir.z);
+  const double rxy = sqrt(q.x * q.x + q.y * q.y);
+  return (rxy - t[tr::TorRtor]) * (rxy - t[tr::TorRtor]) + q.z * q.z;
+}
+
+// Contains (TorusImplementation2.h:391-399): inside tolerances and no phi test, as the reference
+__device__ __noinline__ bool torus_contains(const double *t, D3 p)
+{
+  bool cin = false, cout = false;
+  torus_ci<true, false>(t, p, cin, cout);
+  return !cout;
+}
+
+__device__ __noinline__ int torus_inside(const double *t, D3 p) { return torus_inside_kernel(t, p); }
+
+// DistanceToIn (TorusImplementation2.h:415-491), the VECGEOM_NO_SPECIALIZATION branch
+__device__ __noinline__ double torus_dist_in(const double *t, D3 p, D3 d)
+{
+  const double *bt   = t + tr::TorTube;
+  const bool inBounds = tube_contains(bt, p);
+  const double tubeDistance = inBounds ? 0. : tube_dist_in(bt, p, d);
+  if (inBounds) {
+    if (torus_inside_kernel(t, p) == kInsideE) return -1.;
+  } else if (tubeDistance == kInfLength) {
+    return kInfLength;
+  }
+  const D3 lp     = d3(p.x + tubeDistance * d.x, p.y + tubeDistance * d.y, p.z + tubeDistance * d.z);
+  double distance = kInfLength;
+  if (torus_has_phi(t)) {
+    double d1, d2;
+    wedge_dist<true>(t + tr::TorWedge, lp, d, d1, d2);
+    if (d1 != kInfLength) {
+      const double daxis = torus_dist2_axis(t, lp, d, d1);
+      if (daxis >= t[tr::TorRmin2] && daxis < t[tr::TorRmax2]) {
+        distance = d1;
+        if (fabs(distance) < kTolerance) return distance + tubeDistance;
+      }
+    }
+    if (d2 != kInfLength) {
+      const double daxis = torus_dist2_axis(t, lp, d, d2);
+      if (daxis >= t[tr::TorRmin2] && daxis < t[tr::TorRmax2]) {
+        distance = d2 < distance ? d2 : distance;
+        if (fabs(distance) < kTolerance) return distance + tubeDistance;
+      }
+    }
+    distance = kInfLength;
+  }
+  double dd = torus_to_boundary(t, lp, d, t[tr::TorRmax], false);
+  if (t[tr::TorRmin] > 0.) {
+    const double ddrmin = torus_to_boundary(t, lp, d, t[tr::TorRmin], false);
+    dd                  = dd < ddrmin ? dd : ddrmin;
+  }
+  distance = distance < dd ? distance : dd;
+  distance += tubeDistance;
+  if (fabs(distance) > kInfLength) distance = kInfLength;
+  return distance;
+}
+
+// DistanceToOut (TorusImplementation2.h:158-217)
+__device__ __noinline__ double torus_dist_out(const double *t, D3 p, D3 d)
+{
+  const double rtor = t[tr::TorRtor], rmax = t[tr::TorRmax];
+  const double rsq       = p.x * p.x + p.y * p.y;
+  const double outerExcl = rtor + rmax + kHalfTolerance, innerExcl = rtor - rmax - kHalfTolerance;
+  if (fabs(p.z) - rmax > kHalfTolerance || rsq > outerExcl * outerExcl || rsq < innerExcl * innerExcl) return -1.;
+  if (torus_inside_kernel(t, p) == kOutsideE) return -1.;
+  const double dout = torus_to_boundary(t, p, d, rmax, true);
+  double din        = kInfLength;
+  if (t[tr::TorRmin] > 0) din = torus_to_boundary(t, p, d, t[tr::TorRmin], true);
+  double distance = dout < din ? dout : din;
+  if (torus_has_phi(t)) {
+    const double *w = t + tr::TorWedge;
+    double dp1, dp2;
+    wedge_dist<false>(w, p, d, dp1, dp2);
+    if (dp1 < distance) {
+      const D3 ip = d3(p.x + dp1 * d.x, p.y + dp1 * d.y, p.z + dp1 * d.z);
+      if (torus_contains_disk(t, ip)) {
+        const double diri = ip.x * w[row::WedgeA1x] + ip.y * w[row::WedgeA1y];
+        if (diri >= 0) distance = dp1;
+      }
+    }
+    if (dp2 < distance) {
+      const D3 ip = d3(p.x + dp2 * d.x, p.y + dp2 * d.y, p.z + dp2 * d.z);
+      if (torus_contains_disk(t, ip)) {
+        const double diri2 = ip.x * w[row::WedgeA2x] + ip.y * w[row::WedgeA2y];
+        if (diri2 >= 0 && dp2 < distance) distance = dp2;
+      }
+    }
+  }
+  if (distance >= kInfLength) distance = -1.;
+  return distance;
+}
+
+// SafetyToIn (TorusImplementation2.h:493-509)
+__device__ __noinline__ double torus_safe_in(const double *t, D3 p)
+{
+  const double rxy = sqrt(p.x * p.x + p.y * p.y);
+  const double rad = sqrt((rxy - t[tr::TorRtor]) * (rxy - t[tr::TorRtor]) + p.z * p.z);
+  double safety    = rad - t[tr::TorRmax];
+  if (t[tr::TorRmin] != 0.) safety = vmax(t[tr::TorRmin] - rad, rad - t[tr::TorRmax]);
+  if (torus_has_phi(t) && rxy != 0.) safety = vmax(wedge_safe_in(t + tr::TorWedge, p), safety);
+  return safety;
+}
+
+// SafetyToOut (TorusImplementation2.h:379-389)
+__device__ __noinline__ double torus_safe_out(const double *t, D3 p)
+{
+  const double rxy = sqrt(p.x * p.x + p.y * p.y);
+  const double rad = sqrt((rxy - t[tr::TorRtor]) * (rxy - t[tr::TorRtor]) + p.z * p.z);
+  double safety    = t[tr::TorRmax] - rad;
+  if (t[tr::TorRmin] != 0.) safety = vmin(rad - t[tr::TorRmin], t[tr::TorRmax] - rad);
+  if (torus_has_phi(t)) safety = vmin(wedge_safe_out(t + tr::TorWedge, p), safety);
+  return safety;
+}
+#endif  // VGN_SECTIONS
+
 // ---------------------------------------------------------------- dispatch (primitive shapes)
 // `stepmax` is the step the caller still accepts; of the primitives only the cut tube's DistanceToIn
 // reads it (booleans hand it to their operands)
@@ -3033,6 +3455,7 @@ __device__ __forceinline__ double prim_dist_in(int type, const double *r, D3 p, 
   case kCutTube: return cuttube_dist_in(r, p, d, stepmax);
 #if VGN_SECTIONS
   case kPolyhedron: return polyhedron_dist_in(r, p, d);
+  case kTorus: return torus_dist_in(r, p, d);
 #endif
   }
   return kInfLength;
@@ -3052,6 +3475,7 @@ __device__ __forceinline__ double prim_dist_out(int type, const double *r, D3 p,
   case kCutTube: return cuttube_dist_out(r, p, d);
 #if VGN_SECTIONS
   case kPolyhedron: return polyhedron_dist_out(r, p, d);
+  case kTorus: return torus_dist_out(r, p, d);
 #endif
   }
   return -1.;
@@ -3071,6 +3495,7 @@ __device__ __forceinline__ double prim_safe_in(int type, const double *r, D3 p)
   case kCutTube: return cuttube_safe_in(r, p);
 #if VGN_SECTIONS
   case kPolyhedron: return polyhedron_safety(r, p, false);
+  case kTorus: return torus_safe_in(r, p);
 #endif
   }
   return kInfLength;
@@ -3090,6 +3515,7 @@ __device__ __forceinline__ double prim_safe_out(int type, const double *r, D3 p)
   case kCutTube: return cuttube_safe_out(r, p);
 #if VGN_SECTIONS
   case kPolyhedron: return polyhedron_safety(r, p, true);
+  case kTorus: return torus_safe_out(r, p);
 #endif
   }
   return 0.;
@@ -3109,6 +3535,7 @@ __device__ __forceinline__ bool prim_contains(int type, const double *r, D3 p)
   case kCutTube: return cuttube_contains(r, p);
 #if VGN_SECTIONS
   case kPolyhedron: return polyhedron_contains(r, p);
+  case kTorus: return torus_contains(r, p);
 #endif
   }
   return false;
@@ -3128,6 +3555,7 @@ __device__ __forceinline__ int prim_inside(int type, const double *r, D3 p)
   case kCutTube: return cuttube_inside(r, p);
 #if VGN_SECTIONS
   case kPolyhedron: return polyhedron_inside(r, p);
+  case kTorus: return torus_inside(r, p);
 #endif
   }
   return kOutsideE;

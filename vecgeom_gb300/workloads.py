@@ -22,9 +22,9 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE, BOOLEAN, POLYHEDRON = range(11)
+BOX, TUBE, CONE, TRD, TRAPEZOID, SPHERE, POLYCONE, ORB, CUTTUBE, BOOLEAN, POLYHEDRON, TORUS = range(12)
 SHAPE_NAMES = ["box", "tube", "cone", "trd", "trapezoid", "sphere", "polycone", "orb", "cuttube", "boolean",
-               "polyhedron"]
+               "polyhedron", "torus2"]
 UNION, INTERSECTION, SUBTRACTION = 0, 1, 2  # boolean operations (BooleanStruct.h:9)
 BOOLEAN_OPERAND = -2  # pv_mother of a boolean's operand placement
 
@@ -517,6 +517,14 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
         thb, tht = K_PI - float(rng.uniform(0.0, 0.6)), float(rng.uniform(0.0, 0.6))
         phib, phit = (float(v) for v in rng.uniform(0.0, K_TWO_PI, 2))
         return cuttube_params(rmin, rmax, dz, sphi, dphi, thb, phib, tht, phit), np.array([rmax, rmax, dz + 0.7 * rmax])
+    if shape == TORUS:  # swept radius U[20, 40] mm, tube radius up to 15 mm
+        rtor = u(20.0, 40.0)
+        rmax = u(3.0, min(15.0, rtor - 2.0))
+        rmin = 0.0 if rng.uniform() < 0.5 else float(rng.uniform(0.2, 0.8)) * rmax
+        sphi, dphi = 0.0, K_TWO_PI
+        if sections and rng.uniform() < 0.75:
+            sphi, dphi = float(rng.uniform(-K_PI, K_TWO_PI)), float(rng.uniform(0.2, K_TWO_PI - 0.2))
+        return (rmin, rmax, rtor, sphi, dphi), np.array([rtor + rmax, rtor + rmax, rmax])
     if shape == POLYHEDRON:  # four z planes, 3 to 8 sides; radii are to the sides' middles
         h = u()
         z = [-h] + sorted(float(v) for v in rng.uniform(-h, h, 2)) + [h]
@@ -534,7 +542,7 @@ def _mixed_shape_params(rng: np.random.Generator, shape: int, sections: bool = F
 
 _LENGTH_INDICES = {BOX: (0, 1, 2), TUBE: (0, 1, 2), CONE: (0, 1, 2, 3, 4), TRD: (0, 1, 2, 3, 4),
                    TRAPEZOID: (0, 3, 4, 5, 7, 8, 9), SPHERE: (0, 1), POLYCONE: tuple(range(3, 15)), ORB: (0,),
-                   CUTTUBE: (0, 1, 2), POLYHEDRON: tuple(range(4, 16))}
+                   CUTTUBE: (0, 1, 2), POLYHEDRON: tuple(range(4, 16)), TORUS: (0, 1, 2)}
 
 
 def shape_bbox(shape: int, params):
@@ -552,6 +560,9 @@ def shape_bbox(shape: int, params):
         z = np.asarray(params[4:4 + nz])
         r = float(max(params[4 + 2 * nz:4 + 3 * nz])) / math.cos(0.5 * min(float(params[1]), K_TWO_PI) / sides)
         return np.array([-r, -r, z.min()]), np.array([r, r, z.max()])
+    if shape == TORUS:
+        h = float(params[1]) + float(params[2])
+        return np.array([-h, -h, -float(params[1])]), np.array([h, h, float(params[1])])
     if shape == CUTTUBE:  # the cut planes tilt the end faces
         h = float(params[1]) + float(params[2])
         return np.full(3, -h), np.full(3, h)
@@ -603,6 +614,15 @@ def mixed_shape_geometry(seed: int = 21, grid=MIXED_GRID, world: float = MIXED_W
                 b.place(lv, world_lv, transform_euler(c[0], c[1], c[2], phi, theta, psi))
     b.place_world(world_lv)
     return b.build()
+
+
+def torus_geometry(seed: int = 35) -> GeometryDescription:
+    """512 daughters on the mixed-shape grid (250 mm pitch in a 1 m world): tori (most of them
+    with phi sections), spheres and boxes.  Torus queries equal the reference's to about 1e-13 mm
+    rather than bit for bit (the cubic solver's elementary functions), so these shapes live in a
+    geometry of their own."""
+    return mixed_shape_geometry(seed=seed, grid=(8, 8, 8), world=1000.0, shapes=(TORUS, TORUS, SPHERE, BOX),
+                                sections=True)
 
 
 def mixed_shape_tracks(n: int, seed_points: int = 22, seed_dirs: int = 23, world: float = MIXED_WORLD,
