@@ -66,6 +66,7 @@
 #include "VecGeom/volumes/UnplacedPolycone.h"
 #include "VecGeom/volumes/UnplacedPolyhedron.h"
 #include "VecGeom/volumes/UnplacedSphere.h"
+#include "VecGeom/volumes/UnplacedTorus2.h"
 #include "VecGeom/volumes/UnplacedTrapezoid.h"
 #include "VecGeom/volumes/UnplacedTrd.h"
 #include "VecGeom/volumes/UnplacedTube.h"
@@ -159,6 +160,10 @@ inline int shape_row(vecgeom::VUnplacedVolume const *u, std::vector<double> &p)
                                                                                   : VGN_BOOL_SUBTRACTION;
     p = {(double)op, (double)bs->fLeftVolume->id(), (double)bs->fRightVolume->id()};
     return VGN_BOOLEAN;
+  }
+  if (auto t = dynamic_cast<UnplacedTorus2 const *>(u)) {
+    p = {t->rmin(), t->rmax(), t->rtor(), t->sphi(), t->dphi()};
+    return VGN_TORUS2;
   }
   if (auto h = dynamic_cast<UnplacedPolyhedron const *>(u)) {  // the planes the struct keeps
     const int nz = (int)h->GetZPlanes().size();

@@ -56,6 +56,7 @@ GEOMETRIES = {
     "mixed_all_shapes": lambda: W.mixed_shape_geometry(seed=26, shapes=W.ALL_SHAPES),
     "nested": lambda: W.nested_geometry(),
     "booleans": lambda: W.boolean_geometry(),
+    "tori": lambda: W.torus_geometry(),
 }
 
 
@@ -78,9 +79,9 @@ def test_export_and_dispatch(checker, oracle, tmp_path, which):
     assert int(lines["batch_call_status"]) == 1  # VGN_ERR_ARG: the host-only geometry has no kernels
     assert lines["scalar_same"] == "1"
     # shape parameters that do not show in the tables: the exported shapes navigate alike.
-    # Not for the sectioned geometry: its start angles outside [0, 2 pi) and sections whose end
-    # passes 2 pi are folded by the reference's shapes, which keep no copy of the raw angle.
-    if which == "mixed_sections":
+    # Not for the sectioned geometries: their start angles outside [0, 2 pi) and sections whose
+    # end passes 2 pi are folded by the reference's shapes, which keep no copy of the raw angle.
+    if which in ("mixed_sections", "tori"):  # both hold sectioned spheres
         return
     exp = read_desc(tmp_path / "export.bin")
     t = W.uniform_tracks(1 << 14, 0.999 * float(desc.params[desc.lv_param_offset[desc.pv_logical[desc.world_placed]]]),
