@@ -278,21 +278,15 @@ __device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVR
   const NodeRec *nodes = g.nodes + lv.nodes_off;
   const PrimRec *prims = g.prims + lv.prims_off;
   do {
-    const unsigned id = stack[--sp];
-    const int nchild  = __ldg(&nodes[id].nchild);
-    if (nchild >= 0) {
-      const int off = __ldg(&nodes[id].offset);
-      for (int i = 0; i < nchild; ++i) {
-        const PrimRec &q = prims[off + i];
-        double tmin, tmax;
-        slab(q.mn, q.mx, lp, inv, tmin, tmax);
-        if (tmin <= tmax && tmax >= 0.0 && tmin < step) {
-          const int vol     = __ldg(&q.pv);
-          const double dist = pv_dist_in(g, vol, lp, ld, step);
-          if (dist < step && !(dist <= 0.0 && vol == last)) step = dist, hit = vol;
-        }
-      }
-    } else {
+    // Inner nodes first: every lane descends until it holds a leaf or its stack runs empty, so
+    // that the lanes of a warp reach the leaf code together.  Each lane visits its nodes in the
+    // same order as before; only the interleaving across lanes changes.
+    unsigned id = 0;
+    int nchild  = -1;
+    while (sp > 0) {
+      id     = stack[--sp];
+      nchild = __ldg(&nodes[id].nchild);
+      if (nchild >= 0) break;
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
       double tminL, tmaxL, tminR, tmaxR;
       slab(nodes[L].mn, nodes[L].mx, lp, inv, tminL, tmaxL);
@@ -309,6 +303,19 @@ __device__ __forceinline__ bool bvh_check_daughters(const GeomView &g, const LVR
       } else {
         if (trL) stack[sp++] = L;
         if (trR) stack[sp++] = R;
+      }
+    }
+    if (nchild >= 0) {
+      const int off = __ldg(&nodes[id].offset);
+      for (int i = 0; i < nchild; ++i) {
+        const PrimRec &q = prims[off + i];
+        double tmin, tmax;
+        slab(q.mn, q.mx, lp, inv, tmin, tmax);
+        if (tmin <= tmax && tmax >= 0.0 && tmin < step) {
+          const int vol     = __ldg(&q.pv);
+          const double dist = pv_dist_in(g, vol, lp, ld, step);
+          if (dist < step && !(dist <= 0.0 && vol == last)) step = dist, hit = vol;
+        }
       }
     }
   } while (sp > 0);
@@ -403,18 +410,15 @@ __device__ __forceinline__ double bvh_safety(const GeomView &g, const LVRec &lv,
   const NodeRec *nodes = g.nodes + lv.nodes_off;
   const PrimRec *prims = g.prims + lv.prims_off;
   do {
-    const unsigned id = stack[--sp];
-    const int nchild  = __ldg(&nodes[id].nchild);
-    if (nchild >= 0) {
-      const int off = __ldg(&nodes[id].offset);
-      for (int i = 0; i < nchild; ++i) {
-        const PrimRec &q = prims[off + i];
-        if (box_safety(q.mn, q.mx, lp) < safety) {
-          const double dist = pv_safe_in(g, __ldg(&q.pv), lp);
-          if (dist < safety) safety = dist;
-        }
-      }
-    } else {
+    // Inner nodes first: every lane descends until it holds a leaf or its stack runs empty, so
+    // that the lanes of a warp reach the leaf code together.  Each lane visits its nodes in the
+    // same order as before; only the interleaving across lanes changes.
+    unsigned id = 0;
+    int nchild  = -1;
+    while (sp > 0) {
+      id     = stack[--sp];
+      nchild = __ldg(&nodes[id].nchild);
+      if (nchild >= 0) break;
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
       const double sL = box_safety(nodes[L].mn, nodes[L].mx, lp);
       const double sR = box_safety(nodes[R].mn, nodes[R].mx, lp);
@@ -429,6 +433,16 @@ __device__ __forceinline__ double bvh_safety(const GeomView &g, const LVRec &lv,
       } else {
         if (trL) stack[sp++] = L;
         if (trR) stack[sp++] = R;
+      }
+    }
+    if (nchild >= 0) {
+      const int off = __ldg(&nodes[id].offset);
+      for (int i = 0; i < nchild; ++i) {
+        const PrimRec &q = prims[off + i];
+        if (box_safety(q.mn, q.mx, lp) < safety) {
+          const double dist = pv_safe_in(g, __ldg(&q.pv), lp);
+          if (dist < safety) safety = dist;
+        }
       }
     }
   } while (sp > 0);

@@ -571,26 +571,14 @@ __device__ __forceinline__ bool bvh_collect_step_mixed(const GeomView &g, const 
   stack[0]                = stack_entry(0u, inode_range(inodes, 0u));
   bool ok = true;
   do {
-    int nchild, off;
-    const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
-    if (nchild >= 0) {
-      for (int i = 0; i < nchild; ++i) {
-        const IPrimSlab &q = iprims[off + i];
-        FI tmin, tmax;
-        islab(q.mn_lo, q.mn_hi, q.mx_lo, q.mx_hi, r, tmin, tmax);
-        if (slab_decision(tmin, tmax, stepI) == kNo) continue;
-        if (c.n == kMaxStepCand) {  // full: evaluate the oldest now (keeps the order)
-          eval_step_candidate(g, r, c.pv[c.head], c.tmin_lo[c.head], step, stepI, last, hit);
-          c.head = (c.head + 1) % kMaxStepCand;
-          --c.n;
-        }
-        const int slot   = (c.head + c.n) % kMaxStepCand;
-        c.pv[slot]       = __ldg(&q.pv);
-        c.tmin_lo[slot]  = tmin.lo;
-        c.types = (c.types & ~(0xfull << (4 * slot))) | ((uint64_t)__ldg(&q.shape) << (4 * slot));
-        ++c.n;
-      }
-    } else {
+    // Inner nodes first: every lane descends until it holds a leaf or its stack runs empty, so
+    // that the lanes of a warp reach the leaf code together.  Each lane visits its nodes in the
+    // same order as before; only the interleaving across lanes changes.
+    int nchild = -1, off = 0;
+    unsigned id = 0;
+    while (sp > 0) {
+      id = open_entry(inodes, stack[--sp], nchild, off);
+      if (nchild >= 0) break;
       const unsigned L = 2 * id + 1, R = 2 * id + 2;
       const unsigned eL = stack_entry(L, inode_range(inodes, L)), eR = stack_entry(R, inode_range(inodes, R));
       FI tminL, tmaxL, tminR, tmaxR;
@@ -620,6 +608,25 @@ __device__ __forceinline__ bool bvh_collect_step_mixed(const GeomView &g, const 
       } else {
         if (trL) stack[sp++] = eL;
         if (trR) stack[sp++] = eR;
+      }
+    }
+    if (!ok) break;
+    if (nchild >= 0) {
+      for (int i = 0; i < nchild; ++i) {
+        const IPrimSlab &q = iprims[off + i];
+        FI tmin, tmax;
+        islab(q.mn_lo, q.mn_hi, q.mx_lo, q.mx_hi, r, tmin, tmax);
+        if (slab_decision(tmin, tmax, stepI) == kNo) continue;
+        if (c.n == kMaxStepCand) {  // full: evaluate the oldest now (keeps the order)
+          eval_step_candidate(g, r, c.pv[c.head], c.tmin_lo[c.head], step, stepI, last, hit);
+          c.head = (c.head + 1) % kMaxStepCand;
+          --c.n;
+        }
+        const int slot   = (c.head + c.n) % kMaxStepCand;
+        c.pv[slot]       = __ldg(&q.pv);
+        c.tmin_lo[slot]  = tmin.lo;
+        c.types = (c.types & ~(0xfull << (4 * slot))) | ((uint64_t)__ldg(&q.shape) << (4 * slot));
+        ++c.n;
       }
     }
   } while (sp > 0);
