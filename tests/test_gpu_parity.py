@@ -176,6 +176,30 @@ def test_box_grid_host_pointer_pipelined(oracle, vgnav, cuda, chunks):
 
 
 @pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("kbits,safety_kbits", [(0, 0), (5, 6), (4, 0)])
+def test_host_buffers_overlapped_copies(oracle, vgnav, cuda, mixed, kbits, safety_kbits):
+    """Host-buffer steps with safeties of 2^16 tracks and more copy the directions and step
+    limits in while the safety pass runs and the safeties out while the step kernel runs: the
+    mixed-shape geometry's results equal the oracle's for every binning of the two passes."""
+    desc = W.mixed_shape_geometry()
+    og = oracle.OracleGeometry(desc)
+    geo = vgnav.Geometry(desc)
+    t = W.mixed_shape_tracks((1 << 17) + 77, seed_points=52, seed_dirs=53)
+    t.states = og.locate(t.x, t.y, t.z)
+    ref = og.step(t, calcsafety=True)
+    geo.set_step_config(0, kbits, mixed=mixed)
+    geo.set_safety_binning(safety_kbits, mixed=mixed)
+    for _ in range(2):  # the second call reuses the workspace and the side stream
+        out = np.zeros(t.n, dtype=W.STATE_DTYPE)
+        steps = np.full(t.n, -7.0)
+        saf = np.full(t.n, -7.0)
+        geo.step(vgnav.SOA3D(t.x, t.y, t.z), vgnav.SOA3D(t.dx, t.dy, t.dz), t.step_limit,
+                 vgnav.NavStatePool(t.states), vgnav.NavStatePool(out), steps, saf, mixed=mixed)
+        assert np.array_equal(steps, ref["step"]) and np.array_equal(saf, ref["safety"])
+        assert np.array_equal(out, ref["out"])
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("which", ["box_grid", "nested", "deep_cache1", "deep_cache2", "deep_cache0"])
 def test_walk_to_world_exit(oracle, vgnav, cuda, which, mixed):
     """Every step of every track, stepped until it leaves the world, equals the oracle; on the

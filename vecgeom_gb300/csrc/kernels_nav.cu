@@ -665,6 +665,12 @@ static void launch_safety_pass(const GeomView &g, const StepArgs &a, bool mixed,
                                                                   a.perm_safety ? a.perm_safety : a.perm, 1);
 }
 
+cudaError_t launch_safety_only(const GeomView &g, const StepArgs &a, bool mixed, cudaStream_t s)
+{
+  launch_safety_pass(g, a, mixed, s);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_step(const GeomView &g, const StepArgs &a, bool mixed, int variant, cudaStream_t s)
 {
   if (a.safety) launch_safety_pass(g, a, mixed, s);

@@ -40,8 +40,10 @@ __global__ void __launch_bounds__(256) bin_keys_kernel(int64_t n, const double *
     const uint32_t cx = (uint32_t)fminf(fmaxf(fx, 0.f), (float)cmax);
     const uint32_t cy = (uint32_t)fminf(fmaxf(fy, 0.f), (float)cmax);
     const uint32_t cz = (uint32_t)fminf(fmaxf(fz, 0.f), (float)cmax);
-    const uint32_t oct = (dx[i] > 0.0 ? 4u : 0u) | (dy[i] > 0.0 ? 2u : 0u) | (dz[i] > 0.0 ? 1u : 0u);
-    const uint32_t key = (b.octants ? oct << (3 * b.kbits) : 0u) | (spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz);
+    // directions are read only for the octant split (a position-only order never touches them)
+    const uint32_t oct =
+        b.octants ? ((dx[i] > 0.0 ? 4u : 0u) | (dy[i] > 0.0 ? 2u : 0u) | (dz[i] > 0.0 ? 1u : 0u)) : 0u;
+    const uint32_t key = (oct << (3 * b.kbits)) | (spread3(cx) << 2) | (spread3(cy) << 1) | spread3(cz);
     keys[i]            = key;
     atomicAdd(hist + key, 1u);
   }

@@ -413,6 +413,91 @@ int vgn_geometry_device_bytes(const vgn_geometry *g, size_t *bytes)
 
 namespace {
 
+// the two internal streams and three events of the staged paths, created on first use
+int ensure_pipe(vgn_geometry *g)
+{
+  if (g->pipe[0]) return VGN_OK;
+  for (int k = 0; k < 2; ++k)
+    if (cudaStreamCreateWithFlags(&g->pipe[k], cudaStreamNonBlocking) != cudaSuccess)
+      return cuda_fail(cudaGetLastError(), "staging stream creation");
+  for (int k = 0; k < 3; ++k)
+    if (cudaEventCreateWithFlags(&g->pipe_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return cuda_fail(cudaGetLastError(), "staging event creation");
+  return VGN_OK;
+}
+
+// Host buffers, one piece, with safeties: the safety pass needs only the positions and the
+// states, so the directions and step limits are copied on an internal stream while it runs,
+// and the safeties are copied back on that stream while the step kernel runs.  Same kernels,
+// orders and results as the staged call without the overlap.  Called with ws_mutex held.
+int staged_step_overlap(vgn_geometry *g, vgn::StepArgs a, const double *const src[7], const vgn_state *in,
+                        vgn_state *out, double *step, double *safety, bool mixed, cudaStream_t s)
+{
+  const int64_t n = a.n;
+  const size_t nd = (size_t)n * sizeof(double), ns = (size_t)n * sizeof(vgn_state);
+  void *ws        = workspace(g, carve_bytes({nd, nd, nd, nd, nd, nd, nd, ns, ns, nd, nd}));
+  if (!ws) return fail(VGN_ERR_NOMEM, "device staging workspace allocation failed");
+  if (int rc = ensure_pipe(g)) return rc;
+  Carve c{static_cast<char *>(ws)};
+  double *b[7];
+  for (int k = 0; k < 7; ++k) b[k] = c.take<double>(n);
+  vgn_state *din = c.take<vgn_state>(n), *dout = c.take<vgn_state>(n);
+  double *dstep = c.take<double>(n), *dsaf = c.take<double>(n);
+  const int m = mixed ? 1 : 0, kbits = g->sort_kbits[m], ks = g->safety_kbits[m];
+  cudaStream_t ps = g->pipe[0];
+  cudaError_t e   = cudaEventRecord(g->pipe_ev[0], s);  // the side stream follows the caller's prior work
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ps, g->pipe_ev[0], 0);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(din, in, ns, cudaMemcpyHostToDevice, s);
+  for (int k = 3; k < 7 && e == cudaSuccess; ++k) e = cudaMemcpyAsync(b[k], src[k], nd, cudaMemcpyHostToDevice, ps);
+  if (e == cudaSuccess) e = cudaEventRecord(g->pipe_ev[1], ps);  // directions and step limits are in
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  a.px = b[0]; a.py = b[1]; a.pz = b[2]; a.dx = b[3]; a.dy = b[4]; a.dz = b[5]; a.slimit = b[6];
+  a.in = din; a.out = dout; a.step = dstep; a.safety = dsaf; a.perm = nullptr; a.perm_safety = nullptr;
+  // binning scratch: keys and histogram shared by the two binnings in stream order, then the orders
+  size_t head = kbits > 0 ? vgn::bin_scratch_words(n, kbits) : 0;
+  if (ks > 0 && vgn::bin_scratch_words(n, ks) > head) head = vgn::bin_scratch_words(n, ks);
+  const size_t need = head + (size_t)n * ((kbits > 0 ? 1 : 0) + (ks > 0 ? 1 : 0));
+  uint32_t *buf     = nullptr;
+  if (need > 0 && pool_alloc(g->device, need * sizeof(uint32_t), s, reinterpret_cast<void **>(&buf)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(VGN_ERR_NOMEM, "track-binning scratch allocation failed");
+  }
+  uint32_t *next = buf + head;
+  if (ks > 0) {  // the safety pass's order: position alone (the directions are not read)
+    vgn::BinParams bp = g->bin;
+    bp.kbits          = ks;
+    bp.octants        = 0;
+    for (int k = 0; k < 3; ++k) bp.scale[k] = g->bin.scale[k] * (float)(1 << ks);
+    e             = vgn::launch_bin_tracks(n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, bp, buf, next, max_blocks(g), s);
+    a.perm_safety = next;
+    next += n;
+  }
+  if (e == cudaSuccess) e = VGN_KSET_FN(g->host.kset(), launch_safety_only)(g->view, a, mixed, s);
+  if (e == cudaSuccess) e = cudaEventRecord(g->pipe_ev[2], s);  // safeties are final
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g->pipe_ev[1], 0);
+  if (e == cudaSuccess && kbits > 0) {  // the step's order: direction octant, then position
+    vgn::BinParams bp = g->bin;
+    bp.kbits          = kbits;
+    for (int k = 0; k < 3; ++k) bp.scale[k] = g->bin.scale[k] * (float)(1 << kbits);
+    e      = vgn::launch_bin_tracks(n, a.px, a.py, a.pz, a.dx, a.dy, a.dz, bp, buf, next, max_blocks(g), s);
+    a.perm = next;
+  }
+  vgn::StepArgs st = a;
+  st.safety        = nullptr;  // the step kernel alone
+  if (e == cudaSuccess) e = VGN_KSET_FN(g->host.kset(), launch_step)(g->view, st, mixed, g->step_variant[m], s);
+  if (buf) cudaFreeAsync(buf, s);
+  if (e != cudaSuccess) return cuda_fail(e, "overlapped step launch");
+  e = cudaStreamWaitEvent(ps, g->pipe_ev[2], 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(safety, dsaf, nd, cudaMemcpyDeviceToHost, ps);
+  if (e == cudaSuccess) e = cudaEventRecord(g->pipe_ev[1], ps);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, ns, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(step, dstep, nd, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g->pipe_ev[1], 0);  // join the side stream
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  return check_status(g, s);
+}
+
 // A host-buffer step in `nchunk` pieces: piece i is copied in, binned, stepped and copied out
 // on internal stream i % 2, so the copies of one piece overlap the kernels of the other.
 // Tracks are independent, so the results do not depend on the split.  Called with
@@ -439,14 +524,7 @@ int staged_step_pipelined(vgn_geometry *g, int64_t n, const double *const src[7]
     }
     g->pipe_sort_words = 2 * sort_words;
   }
-  if (!g->pipe[0]) {
-    for (int k = 0; k < 2; ++k)
-      if (cudaStreamCreateWithFlags(&g->pipe[k], cudaStreamNonBlocking) != cudaSuccess)
-        return cuda_fail(cudaGetLastError(), "staging stream creation");
-    for (int k = 0; k < 3; ++k)
-      if (cudaEventCreateWithFlags(&g->pipe_ev[k], cudaEventDisableTiming) != cudaSuccess)
-        return cuda_fail(cudaGetLastError(), "staging event creation");
-  }
+  if (int rc = ensure_pipe(g)) return rc;
   cudaError_t e = cudaEventRecord(g->pipe_ev[0], s);
   for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamWaitEvent(g->pipe[k], g->pipe_ev[0], 0);
   if (e != cudaSuccess) return cuda_fail(e, "staging fork");
@@ -526,6 +604,10 @@ int vgn_compute_step_batch(const vgn_geometry *gc, int64_t n, const double *px, 
   if (nchunk > 1 && n >= nchunk) {
     const double *src[7] = {px, py, pz, dx, dy, dz, step_limit};
     return staged_step_pipelined(g, n, src, in, out, step, safety, mixed, a.reloc, nchunk, s);
+  }
+  if (safety && n >= (1 << 16) && n <= (int64_t)UINT32_MAX) {
+    const double *src[7] = {px, py, pz, dx, dy, dz, step_limit};
+    return staged_step_overlap(g, a, src, in, out, step, safety, mixed, s);
   }
   const size_t nd = (size_t)n * sizeof(double), ns = (size_t)n * sizeof(vgn_state);
   const size_t bytes = carve_bytes({nd, nd, nd, nd, nd, nd, nd, ns, ns, nd, nd});
