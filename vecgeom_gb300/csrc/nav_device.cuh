@@ -459,8 +459,21 @@ __device__ __forceinline__ bool bvh_level_locate(const GeomView &g, const LVRec 
   const NodeRec *nodes = g.nodes + lv.nodes_off;
   const PrimRec *prims = g.prims + lv.prims_off;
   do {
-    const unsigned id = stack[--sp];
-    const int nchild  = __ldg(&nodes[id].nchild);
+    // inner nodes first, then the leaf: the lanes of a warp reach the leaf code together
+    unsigned id = 0;
+    int nchild  = -1;
+    while (sp > 0) {
+      id     = stack[--sp];
+      nchild = __ldg(&nodes[id].nchild);
+      if (nchild >= 0) break;
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      if (sp + 2 > g.stack_limit) {
+        raise_error(g, kErrStack);
+        return false;
+      }
+      if (box_contains_pt(nodes[L].mn, nodes[L].mx, lp)) stack[sp++] = L;
+      if (box_contains_pt(nodes[R].mn, nodes[R].mx, lp)) stack[sp++] = R;
+    }
     if (nchild >= 0) {
       const int off = __ldg(&nodes[id].offset);
       for (int i = 0; i < nchild; ++i) {
@@ -473,14 +486,6 @@ __device__ __forceinline__ bool bvh_level_locate(const GeomView &g, const LVRec 
           }
         }
       }
-    } else {
-      const unsigned L = 2 * id + 1, R = 2 * id + 2;
-      if (sp + 2 > g.stack_limit) {
-        raise_error(g, kErrStack);
-        return false;
-      }
-      if (box_contains_pt(nodes[L].mn, nodes[L].mx, lp)) stack[sp++] = L;
-      if (box_contains_pt(nodes[R].mn, nodes[R].mx, lp)) stack[sp++] = R;
     }
   } while (sp > 0);
   return false;

@@ -895,8 +895,23 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
   const PrimRec *prims    = g.prims + lv.prims_off;
   stack[0]                = stack_entry(0u, inode_range(inodes, 0u));
   do {
-    int nchild, off;
-    const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
+    // inner nodes first, then the leaf: the lanes of a warp reach the leaf code together
+    int nchild = -1, off = 0;
+    while (sp > 0) {
+      const unsigned id = open_entry(inodes, stack[--sp], nchild, off);
+      if (nchild >= 0) break;
+      const unsigned L = 2 * id + 1, R = 2 * id + 2;
+      if (sp + 2 > g.stack_limit) {
+        raise_error(g, kErrStack);
+        return false;
+      }
+      int cL = icontains(inodes[L].mn_lo, inodes[L].mn_hi, inodes[L].mx_lo, inodes[L].mx_hi, p);
+      if (cL == kMaybe) cL = box_contains_pt(nodes[L].mn, nodes[L].mx, lp) ? kYes : kNo;
+      if (cL == kYes) stack[sp++] = stack_entry(L, inode_range(inodes, L));
+      int cR = icontains(inodes[R].mn_lo, inodes[R].mn_hi, inodes[R].mx_lo, inodes[R].mx_hi, p);
+      if (cR == kMaybe) cR = box_contains_pt(nodes[R].mn, nodes[R].mx, lp) ? kYes : kNo;
+      if (cR == kYes) stack[sp++] = stack_entry(R, inode_range(inodes, R));
+    }
     if (nchild >= 0) {
       for (int i = 0; i < nchild; ++i) {
         const IPrimSlab &q = iprims[off + i];
@@ -913,18 +928,6 @@ __device__ __forceinline__ bool bvh_level_locate_mixed(const GeomView &g, const 
           return true;
         }
       }
-    } else {
-      const unsigned L = 2 * id + 1, R = 2 * id + 2;
-      if (sp + 2 > g.stack_limit) {
-        raise_error(g, kErrStack);
-        return false;
-      }
-      int cL = icontains(inodes[L].mn_lo, inodes[L].mn_hi, inodes[L].mx_lo, inodes[L].mx_hi, p);
-      if (cL == kMaybe) cL = box_contains_pt(nodes[L].mn, nodes[L].mx, lp) ? kYes : kNo;
-      if (cL == kYes) stack[sp++] = stack_entry(L, inode_range(inodes, L));
-      int cR = icontains(inodes[R].mn_lo, inodes[R].mn_hi, inodes[R].mx_lo, inodes[R].mx_hi, p);
-      if (cR == kMaybe) cR = box_contains_pt(nodes[R].mn, nodes[R].mx, lp) ? kYes : kNo;
-      if (cR == kYes) stack[sp++] = stack_entry(R, inode_range(inodes, R));
     }
   } while (sp > 0);
   return false;
