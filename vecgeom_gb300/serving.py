@@ -13,7 +13,7 @@ work overlaps theirs on the GPU.  Three measures keep small requests fast next t
   * large requests are cut into slices of at most `slice_tracks` tracks, each an independent
     locate + walk on a normal-priority stream, so no request holds the GPU for its whole life
     and slices of different requests interleave;
-  * admission by live device-memory headroom (free HBM reported by the driver plus what the
+  * admission by live device-memory headroom (free HBM reported by cudaMemGetInfo plus what the
     caching allocator holds unused, minus a reserve), not by a pool fixed at start.
 
 Latency is measured from arrival to the moment the whole reply is back in host memory and
